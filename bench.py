@@ -1,0 +1,323 @@
+"""Ray-query benchmark: closest-hit Mrays/s on the 1M-triangle kd-tree.
+
+Workload (one step): closest hit for 4,194,304 rays (origins uniform in the
+scene box, directions uniform on S^2, float32) against a 1,048,576-triangle
+displaced sphere (radius 1, gradient-noise amplitude 0.05, seeded) plus
+50,000 random triangles of edge ~0.01 in the unit cube -- seeded synthetic
+inputs with the shapes of the ray-query microbenchmark configuration.
+
+* value      : rays / kernel time, inputs resident in HBM, L2 flushed (a
+               256 MiB write) before every timed step, CUDA events on the
+               launching stream.
+* e2e        : the same metric through the C ABI host-buffer entry point
+               (skw_intersect_host): pinned host rays in, hits out, copies
+               inside the timed region.
+* roofline   : algorithmic bytes per launch (32 + 16 + 32*N_nodes +
+               36*N_tris per ray, N from the instrumented oracle on a sample
+               of the same rays) / kernel time, against the measured HBM
+               copy bandwidth.
+* cpu_baseline: the reference's own TriangleAccelerator::Intersect (built
+               from its sources) on the host cores over a ray sample.
+
+Multi-GPU: rays are independent, so each rank traces its own 4M-ray batch
+(weak scaling, no data-path collective; a max-reduce of the timings only).
+
+--impl reference runs the reference's CPU path instead (rank 0 only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "closest-hit Mrays/s (1M-triangle kd-tree, 4M uniform rays)"
+UNIT = "Mrays/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--rays", type=int, default=4 * 1024 * 1024)
+    p.add_argument("--subdiv", type=int, default=9)
+    p.add_argument("--nrandom", type=int, default=50_000)
+    p.add_argument("--cpu-sample", type=int, default=1_000_000, help="rays in one CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def config(args, world):
+    return {"workload": f"ray-query: displaced sphere 4*4^{args.subdiv} tris + {args.nrandom} random tris, "
+                        f"{args.rays} uniform rays per GPU, closest hit",
+            "triangles": 4 * 4 ** args.subdiv + args.nrandom, "rays_per_step_per_gpu": args.rays,
+            "l2": "flushed before every timed step (256 MiB write)", "parallelism": f"replicas x{world}"}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi SM clocks and throttle reasons while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.stop = threading.Event()
+        self.t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                for line in out.stdout.strip().splitlines():
+                    self.rows.append([x.strip() for x in line.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def load_traffic(kind: str, rays: int):
+    """DRAM bytes per launch from the committed ncu summary, scaled to `rays`."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text()).get(kind)
+    if not d:
+        return None
+    return d["dram_bytes_per_ray"] * rays
+
+
+def cpu_baseline(meshes, rays, sample, rank):
+    """The reference's own Intersect over `sample` rays on all host cores, plus
+    the instrumented oracle's node / triangle counts on the same rays."""
+    from oracle.api import Oracle, Reference
+    cores = os.cpu_count() or 1
+    sub = rays[:sample]
+    oa = Oracle().accel(meshes)
+    cnt = oa.intersect(sub[:200_000], counters=True)
+    n_nodes, n_tris = float(cnt["nodes"].mean()), float(cnt["tris"].mean())
+    if Reference.available():
+        ra = Reference().accel(meshes)
+        ra.intersect(sub[:10_000])
+        t0 = time.perf_counter()
+        ra.intersect(sub, threads=cores)
+        dt = time.perf_counter() - t0
+        kind = "reference"
+    else:
+        t0 = time.perf_counter()
+        oa.intersect(sub, threads=cores)
+        dt = time.perf_counter() - t0
+        kind = "port"
+    return {"value": sample / dt / 1e6, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"{sample} of the step's rays, TriangleAccelerator::Intersect incl. differential geometry"
+            if kind == "reference" else f"{sample} of the step's rays, oracle restatement"}, (n_nodes, n_tris)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return 0
+    from skwarka_gb300 import scenes
+    from oracle.api import Oracle, Reference
+    meshes = scenes.ray_query_scene(args.subdiv, args.nrandom, seed=3)
+    lo, hi = scenes.scene_bounds(meshes)
+    rays = scenes.uniform_rays(args.cpu_sample, lo, hi, seed=7)
+    cores = os.cpu_count() or 1
+    if Reference.available():
+        acc, kind = Reference().accel(meshes), "reference"
+    else:
+        acc, kind = Oracle().accel(meshes), "port"
+    for _ in range(args.warmup):
+        acc.intersect(rays[:100_000], threads=cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        acc.intersect(rays, threads=cores)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = args.cpu_sample * args.steps / total / 1e6
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {**config(args, world), "rays_per_step_per_gpu": args.cpu_sample,
+                       "note": "each step traces a bounded sample of the workload's rays"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": f"{args.cpu_sample} rays per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from skwarka_gb300 import scenes
+    from skwarka_gb300.accel import Context, Primitive, TriangleAccelerator, TriangleMesh
+
+    meshes = scenes.ray_query_scene(args.subdiv, args.nrandom, seed=3)
+    lo, hi = scenes.scene_bounds(meshes)
+    rays_np = scenes.uniform_rays(args.rays, lo, hi, seed=7 + 1000 * rank)
+    ctx = Context(local)
+    acc = TriangleAccelerator([Primitive(TriangleMesh(v, t)) for v, t in meshes], ctx)
+    rays = torch.from_numpy(rays_np).to(dev)
+    hits = torch.empty((args.rays, 4), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    from skwarka_gb300 import _lib
+    lib = _lib.load()
+
+    def step():
+        _lib.check(lib.skw_intersect(acc.handle, rays.data_ptr(), args.rays, hits.data_ptr(), stream.cuda_stream),
+                   ctx.handle)
+
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    launches0 = ctx.launch_count()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for s, e in evs:
+            flush.fill_(float(len(evs)))
+            s.record(stream)
+            step()
+            e.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    launches = ctx.launch_count() - launches0
+    kern_ms = [s.elapsed_time(e) for s, e in evs]
+    total_ms = torch.tensor([sum(kern_ms)], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(total_ms, op=dist.ReduceOp.MAX)
+    total_s = float(total_ms.item()) / 1e3
+    value = args.rays * args.steps * world / total_s / 1e6
+
+    # End to end through the host-buffer entry point (copies included).
+    hrays = torch.from_numpy(rays_np).pin_memory()
+    hhits = torch.empty((args.rays, 4), dtype=torch.int32).pin_memory()
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        _lib.check(lib.skw_intersect_host(acc.handle, hrays.data_ptr(), args.rays, hhits.data_ptr()), ctx.handle)
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        _lib.check(lib.skw_intersect_host(acc.handle, hrays.data_ptr(), args.rays, hhits.data_ptr()), ctx.handle)
+    e2e_s = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(e2e_s, op=dist.ReduceOp.MAX)
+    e2e = args.rays * e2e_steps * world / float(e2e_s.item()) / 1e6
+
+    # Any-hit throughput (shadow rays, tmax ~ U[0, 2]) for the record.
+    srays = torch.from_numpy(scenes.uniform_rays(args.rays, lo, hi, seed=8 + 1000 * rank, tmax_range=(0, 2))).to(dev)
+    occ = torch.empty(args.rays, dtype=torch.uint8, device=dev)
+    a_ms = []
+    for i in range(args.warmup + 5):
+        flush.fill_(3.0)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        _lib.check(lib.skw_intersect_test(acc.handle, srays.data_ptr(), args.rays, occ.data_ptr(), stream.cuda_stream),
+                   ctx.handle)
+        e.record(stream)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            a_ms.append(s.elapsed_time(e))
+    anyhit = args.rays / (sum(a_ms) / len(a_ms) / 1e3) / 1e6
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return 0
+
+    cpu = None
+    n_nodes, n_tris = None, None
+    if not args.no_cpu_baseline and world == 1:
+        cpu, (n_nodes, n_tris) = cpu_baseline(meshes, rays_np, min(args.cpu_sample, args.rays), rank)
+    peak, peak_kind = peaks()
+    per_launch_s = sum(kern_ms) / len(kern_ms) / 1e3
+    roofline = None
+    if n_nodes is not None:
+        bytes_per_ray = 32 + 16 + 32 * n_nodes + 36 * n_tris
+        achieved = bytes_per_ray * args.rays / per_launch_s / 1e9
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": load_traffic("closest", args.rays),
+                    "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                    else "fallback 6.8 TB/s",
+                    "bytes_per_ray": bytes_per_ray, "nodes_per_ray": n_nodes, "tris_per_ray": n_tris}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sum(kern_ms) / len(kern_ms), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(args, world),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": args.rays * 32,
+                    "d2h_bytes_per_step": args.rays * 16},
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,
+            "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit,
+            "accel": {k: acc.info[k] for k in ("n_nodes", "max_depth", "build_ms", "device_bytes")}}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

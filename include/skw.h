@@ -1,0 +1,168 @@
+/*
+ * skw.h -- C ABI of the GB300 ray-query and light-transport library.
+ *
+ * Plain pointers, sizes and status codes only; no C++ or torch types.  Every
+ * entry point names the reference interface it stands in for (paths are in
+ * the Skwarka source tree).  All functions return SKW_OK (0) on success or a
+ * nonzero skw_status; skw_last_error() gives a one-line message for the last
+ * failure on a context.
+ *
+ * Threading: a context and the handles made from it may be used from one
+ * host thread at a time.  Work is stream-ordered on the caller's CUDA stream
+ * (a cudaStream_t passed as void*, NULL = the legacy default stream).
+ *
+ * Memory: "device" buffers are caller-owned device (or managed) memory on
+ * the context's device; "_host" variants take caller-owned host memory and
+ * do the copies themselves.  Handles own their device memory and free it in
+ * *_destroy.
+ */
+#ifndef SKW_H
+#define SKW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum skw_status {
+  SKW_OK = 0,
+  SKW_ERR_ARG = 1,            /* invalid argument (null pointer, bad size, bad index) */
+  SKW_ERR_CUDA = 2,           /* a CUDA runtime call failed */
+  SKW_ERR_OOM = 3,            /* device or host allocation failed */
+  SKW_ERR_BUDGET = 4,         /* a device loop hit its iteration budget */
+  SKW_ERR_STACK_OVERFLOW = 5, /* traversal stack capacity exceeded */
+  SKW_ERR_UNSUPPORTED = 6,    /* valid input outside what this build implements */
+  SKW_ERR_NO_DEVICE = 7       /* no usable CUDA device */
+} skw_status;
+
+typedef struct skw_ctx skw_ctx;
+typedef struct skw_accel skw_accel;
+typedef struct skw_kdtree skw_kdtree;
+
+/* ------------------------------------------------------------ context -- */
+
+/* Binds a context to a CUDA device (the one the caller's streams use). */
+int skw_ctx_create(int device, skw_ctx **out);
+void skw_ctx_destroy(skw_ctx *ctx);
+/* Message of the last failure on this context ("" if none). */
+const char *skw_last_error(const skw_ctx *ctx);
+/* Library version (major * 10000 + minor * 100 + patch). */
+int skw_version(void);
+
+/* ------------------------------------------------- triangle accelerator -- */
+
+/* A triangle mesh: float xyz per vertex, int32 vertex-index triples.
+ * Mirrors TriangleMesh(vertices, triangles) (Raytracer/Core/TriangleMesh.h:82):
+ * triangles with an out-of-range or repeated vertex index are dropped the
+ * same way (TriangleMesh.cpp:176-182), shifting later mesh triangle indices. */
+typedef struct skw_mesh {
+  const float *vertices;
+  int64_t n_vertices;
+  const int32_t *triangles;
+  int64_t n_triangles;
+} skw_mesh;
+
+/* A primitive: a mesh placed by a row-major 4x4 mesh-to-world matrix (NULL =
+ * identity).  Mirrors Primitive(mesh, transform, ...) (Raytracer/Core/Primitive.h:48). */
+typedef struct skw_primitive {
+  int32_t mesh;
+  const double *mesh_to_world;
+} skw_primitive;
+
+/* Ray: origin, direction (normalised), [tmin, tmax].  32 bytes.  Stands in
+ * for Ray (Math/Ray.h:57-59) with float components widened exactly. */
+typedef struct skw_ray {
+  float ox, oy, oz;
+  float dx, dy, dz;
+  float tmin, tmax;
+} skw_ray;
+
+/* Closest-hit result.  prim = primitive index, tri = triangle index within
+ * that primitive's mesh (the reference's Intersection::mp_primitive and
+ * m_triangle_index), t = ray parameter; prim = tri = -1 and t = +inf on a
+ * miss.  flags: SKW_HIT_* bits.  16 bytes. */
+typedef struct skw_hit {
+  float t;
+  int32_t prim;
+  int32_t tri;
+  uint32_t flags;
+} skw_hit;
+
+/* The hit was decided by the exact double-precision re-test (a grazing hit,
+ * a hit near a triangle edge, or a near-tie in t between two triangles). */
+#define SKW_HIT_FP64_DECIDED 1u
+/* Two candidate triangles had double-precision t within 1e-12 relative. */
+#define SKW_HIT_NEAR_TIE 2u
+
+typedef struct skw_accel_info {
+  int64_t n_triangles;
+  int64_t n_nodes;
+  int64_t n_leaves;
+  int32_t max_depth;   /* deepest node (root = 0) */
+  int32_t stack_need;  /* traversal stack entries that suffice: 2*max_depth+1 */
+  float bounds[6];     /* world bounds: min xyz, max xyz (GetWorldBounds) */
+  double build_ms;     /* host build time */
+  int64_t device_bytes;
+} skw_accel_info;
+
+/* Host-only build of the ternary bbox kd-tree over all primitives (the same
+ * splits, partitions and leaf rule as TriangleAccelerator::TriangleAccelerator,
+ * Raytracer/Core/TriangleAccelerator.cpp:22-147, 505-729), flattened into the
+ * device layout.  Needs no GPU.  threads <= 0 uses all hardware threads.
+ * Meshes shared by several primitives (instancing) are SKW_ERR_UNSUPPORTED.
+ * On failure a message is written to err (if errlen > 0). */
+typedef struct skw_flat_tree skw_flat_tree;
+int skw_flat_tree_build(const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims, int32_t n_prims,
+                        int threads, skw_flat_tree **out, char *err, size_t errlen);
+void skw_flat_tree_destroy(skw_flat_tree *tree);
+/* n_nodes, n_triangles, max_depth (root = 0) of a flat tree. */
+int skw_flat_tree_sizes(const skw_flat_tree *tree, int64_t *n_nodes, int64_t *n_triangles, int32_t *max_depth);
+/* Copies out nodes (8 x 32-bit words each, see skw_accel_export), triangle
+ * slots (9 floats: v0 v1 v2 in world space) and their (primitive, mesh
+ * triangle) ids.  Any pointer may be NULL. */
+int skw_flat_tree_export(const skw_flat_tree *tree, uint32_t *nodes, float *tris, int32_t *tri_prim,
+                         int32_t *tri_index);
+
+/* Uploads a flat tree to the context's device (the tree stays owned by the
+ * caller).  Together with skw_flat_tree_build this is
+ * TriangleAccelerator::TriangleAccelerator. */
+int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_accel **out);
+
+/* skw_flat_tree_build + skw_accel_create_from_flat. */
+int skw_accel_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims,
+                     int32_t n_prims, skw_accel **out);
+void skw_accel_destroy(skw_accel *accel);
+int skw_accel_get_info(const skw_accel *accel, skw_accel_info *info);
+
+/* Copies out the flattened tree for inspection: nodes as 8 x 32-bit words
+ * (min xyz, max xyz as float bits; word 6: first child / first triangle;
+ * word 7: type and child mask / triangle count), and per triangle slot its
+ * (primitive, mesh triangle) ids.  Any pointer may be NULL. */
+int skw_accel_export(const skw_accel *accel, uint32_t *nodes, int32_t *tri_prim, int32_t *tri_index);
+
+/* Closest hit for n rays, device buffers.  Stands in for
+ * TriangleAccelerator::Intersect / Scene::Intersect
+ * (Raytracer/Core/TriangleAccelerator.cpp:295-352, Scene.h:77-85) without the
+ * differential-geometry step. */
+int skw_intersect(skw_accel *accel, const skw_ray *rays, int64_t n, skw_hit *hits, void *stream);
+
+/* Any hit in [tmin, tmax] for n rays, device buffers; occluded[i] = 0 or 1.
+ * Stands in for TriangleAccelerator::IntersectTest / Scene::IntersectTest
+ * (Raytracer/Core/TriangleAccelerator.cpp:354-468, Scene.h:140-148). */
+int skw_intersect_test(skw_accel *accel, const skw_ray *rays, int64_t n, uint8_t *occluded, void *stream);
+
+/* Same as above with host buffers (pinned or pageable): copies rays in,
+ * runs, copies results out, and waits for completion. */
+int skw_intersect_host(skw_accel *accel, const skw_ray *rays, int64_t n, skw_hit *hits);
+int skw_intersect_test_host(skw_accel *accel, const skw_ray *rays, int64_t n, uint8_t *occluded);
+
+/* Kernel launches made by this library since the context was created. */
+int64_t skw_launch_count(const skw_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKW_H */

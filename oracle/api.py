@@ -1,0 +1,278 @@
+"""ctypes access to the oracle (test infrastructure only).
+
+``Oracle`` wraps ``oracle/_build/libskw_oracle.so`` (the CPU restatement in
+``oracle/skw_oracle.cpp``); ``Reference`` wraps ``oracle/_ref/libskw_ref.so``
+(the reference's own sources, built by ``oracle/build_ref.py``) and is None
+where that library is absent.  Only tests, ``__graft_entry__.smoke`` and the
+CPU-baseline leg of ``bench.py`` use this module, as the checker.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_LIB = HERE / "_build" / "libskw_oracle.so"
+REF_LIB = HERE / "_ref" / "libskw_ref.so"
+
+_P = C.c_void_p
+_i64 = C.c_int64
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _declare(lib, table):
+    for name, res, args in table:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+_ORACLE_SIGS = [
+    ("oracle_accel_create", _P, [_P, _P, _P, _i64]),
+    ("oracle_accel_destroy", None, [_P]),
+    ("oracle_accel_num_nodes", _i64, [_P]),
+    ("oracle_accel_export", None, [_P, _P, _P, _P, _P]),
+    ("oracle_intersect", None, [_P, _P, _i64, _P, _P, _P, _P, _P, C.c_int]),
+    ("oracle_intersect_test", None, [_P, _P, _i64, _P, _P, _P, C.c_int]),
+    ("oracle_brute_force", None, [_P, _P, _P, _i64, _P, _i64, _P, _P, _P, C.c_int]),
+    ("oracle_kdtree_create", _P, [_P, _P, _i64, _P, _P]),
+    ("oracle_kdtree_destroy", None, [_P]),
+    ("oracle_knn", None, [_P, _P, _P, _i64, C.c_int32, C.c_double, C.c_double, _P, _P, _P, _P, C.c_int]),
+    ("oracle_compressed_direction_table", None, [_P]),
+]
+
+_REF_SIGS = [
+    ("skw_ref_accel_create", _P, [C.c_int, _P, C.c_int, _P, _P, _P, _P, _P]),
+    ("skw_ref_accel_destroy", None, [_P]),
+    ("skw_ref_intersect", None, [_P, _P, _i64, _P, _P, _P, C.c_int]),
+    ("skw_ref_intersect_test", None, [_P, _P, _i64, _P, C.c_int]),
+    ("skw_ref_accel_num_nodes", _i64, [_P]),
+    ("skw_ref_accel_num_triangles", _i64, [_P]),
+    ("skw_ref_accel_export", None, [_P, _P, _P, _P, _P, _P]),
+    ("skw_ref_kdtree_create", _P, [_P, _P, _P, _i64, _P, _P]),
+    ("skw_ref_kdtree_destroy", None, [_P]),
+    ("skw_ref_knn", None, [_P, _P, _P, _i64, C.c_int32, C.c_double, C.c_double, _P, _P, _P, C.c_int]),
+    ("skw_ref_nearest", None, [_P, _P, _i64, C.c_double, _P, C.c_int]),
+    ("skw_ref_compressed_direction_table", None, [_P]),
+    ("skw_ref_compress_direction", C.c_uint16, [C.c_double, C.c_double, C.c_double]),
+]
+
+
+def world_triangles(meshes):
+    """Flatten [(vertices, triangles)] with identity transforms into the
+    reference's triangle order: (tris float32 (n, 9), prim int32, tri int32)."""
+    tv, pr, ti = [], [], []
+    for p, (v, t) in enumerate(meshes):
+        v = np.asarray(v, np.float32)
+        t = np.asarray(t, np.int64)
+        ok = ((t >= 0) & (t < len(v))).all(1) & (t[:, 0] != t[:, 1]) & (t[:, 0] != t[:, 2]) & (t[:, 1] != t[:, 2])
+        t = t[ok]
+        tv.append(v[t].reshape(-1, 9))
+        pr.append(np.full(len(t), p, np.int32))
+        ti.append(np.arange(len(t), dtype=np.int32))
+    return (np.ascontiguousarray(np.concatenate(tv)), np.concatenate(pr), np.concatenate(ti))
+
+
+class Oracle:
+    def __init__(self):
+        if not ORACLE_LIB.exists():
+            from . import build
+            build.build_oracle()
+        self.lib = _declare(C.CDLL(str(ORACLE_LIB)), _ORACLE_SIGS)
+
+    # -- accelerator --
+    def accel(self, meshes):
+        tris, prim, tidx = world_triangles(meshes)
+        return OracleAccel(self.lib, tris, prim, tidx)
+
+    def brute_force(self, tris, prim, tidx, rays, threads=0):
+        n = rays.shape[0]
+        p, t, th = np.empty(n, np.int32), np.empty(n, np.int32), np.empty(n, np.float64)
+        self.lib.oracle_brute_force(_ptr(tris), _ptr(prim), _ptr(tidx), tris.shape[0], _ptr(rays), n, _ptr(p),
+                                    _ptr(t), _ptr(th), threads)
+        return p, t, th
+
+    # -- photon kd-tree --
+    def kdtree(self, pos, normal_ids=None):
+        return OracleKD(self.lib, pos, normal_ids)
+
+    def direction_table(self):
+        out = np.empty((1 << 16, 3), np.float64)
+        self.lib.oracle_compressed_direction_table(_ptr(out))
+        return out
+
+
+class OracleAccel:
+    def __init__(self, lib, tris, prim, tidx):
+        self.lib = lib
+        self.tris, self.prim, self.tidx = tris, prim, tidx
+        self.h = lib.oracle_accel_create(_ptr(tris), _ptr(prim), _ptr(tidx), tris.shape[0])
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.oracle_accel_destroy(self.h)
+            self.h = None
+
+    def export(self):
+        nn = self.lib.oracle_accel_num_nodes(self.h)
+        bbox = np.empty((nn, 6), np.float32)
+        info = np.empty((nn, 8), np.int32)
+        tp = np.empty(max(self.tris.shape[0], 1), np.int32)
+        ti = np.empty(max(self.tris.shape[0], 1), np.int32)
+        self.lib.oracle_accel_export(self.h, _ptr(bbox), _ptr(info), _ptr(tp), _ptr(ti))
+        return bbox, info, tp[:self.tris.shape[0]], ti[:self.tris.shape[0]]
+
+    def intersect(self, rays, counters=False, threads=0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        p, t, th = np.empty(n, np.int32), np.empty(n, np.int32), np.empty(n, np.float64)
+        nv = np.empty(n, np.int32) if counters else None
+        nt = np.empty(n, np.int32) if counters else None
+        self.lib.oracle_intersect(self.h, _ptr(rays), n, _ptr(p), _ptr(t), _ptr(th), _ptr(nv), _ptr(nt), threads)
+        out = {"prim": p, "tri": t, "t": th}
+        if counters:
+            out.update(nodes=nv, tris=nt)
+        return out
+
+    def intersect_test(self, rays, counters=False, threads=0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        occ = np.empty(n, np.uint8)
+        nv = np.empty(n, np.int32) if counters else None
+        nt = np.empty(n, np.int32) if counters else None
+        self.lib.oracle_intersect_test(self.h, _ptr(rays), n, _ptr(occ), _ptr(nv), _ptr(nt), threads)
+        if counters:
+            return occ, nv, nt
+        return occ
+
+
+class OracleKD:
+    def __init__(self, lib, pos, normal_ids=None):
+        self.lib = lib
+        self.pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        self.nids = None if normal_ids is None else np.ascontiguousarray(normal_ids, np.uint16)
+        n = self.pos.shape[0]
+        self.perm = np.empty(n, np.int32)
+        self.nodes = np.empty((n, 2), np.uint32)
+        self.h = lib.oracle_kdtree_create(_ptr(self.pos), _ptr(self.nids), n, _ptr(self.perm), _ptr(self.nodes))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.oracle_kdtree_destroy(self.h)
+            self.h = None
+
+    def knn(self, q, qn, k, max_dist, cos_threshold=-1.0, counters=False, threads=0):
+        q = np.ascontiguousarray(q, np.float64).reshape(-1, 3)
+        qn = None if qn is None else np.ascontiguousarray(qn, np.float64).reshape(-1, 3)
+        nq = q.shape[0]
+        idx = np.empty((nq, k), np.int32)
+        d2 = np.empty((nq, k), np.float64)
+        cnt = np.empty(nq, np.int32)
+        vis = np.empty(nq, np.int32) if counters else None
+        self.lib.oracle_knn(self.h, _ptr(q), _ptr(qn), nq, k, max_dist, cos_threshold, _ptr(idx), _ptr(d2), _ptr(cnt),
+                            _ptr(vis), threads)
+        out = {"idx": idx, "d2": d2, "count": cnt}
+        if counters:
+            out["visited"] = vis
+        return out
+
+
+class Reference:
+    """The reference's own code (oracle/_ref/libskw_ref.so)."""
+
+    def __init__(self):
+        self.lib = _declare(C.CDLL(str(REF_LIB)), _REF_SIGS)
+
+    @staticmethod
+    def available() -> bool:
+        return REF_LIB.exists()
+
+    def accel(self, meshes):
+        return RefAccel(self.lib, meshes)
+
+    def kdtree(self, pos, normal_ids=None, dir_ids=None):
+        return RefKD(self.lib, pos, normal_ids, dir_ids)
+
+    def direction_table(self):
+        out = np.empty((1 << 16, 3), np.float64)
+        self.lib.skw_ref_compressed_direction_table(_ptr(out))
+        return out
+
+
+class RefAccel:
+    def __init__(self, lib, meshes):
+        self.lib = lib
+        self._v = [np.ascontiguousarray(v, np.float32) for v, _ in meshes]
+        self._t = [np.ascontiguousarray(t, np.int32) for _, t in meshes]
+        nm = len(meshes)
+        vp = (C.c_void_p * nm)(*[v.ctypes.data for v in self._v])
+        tp = (C.c_void_p * nm)(*[t.ctypes.data for t in self._t])
+        nv = np.array([v.shape[0] for v in self._v], np.int64)
+        nt = np.array([t.shape[0] for t in self._t], np.int64)
+        mesh_of = np.arange(nm, dtype=np.int32)
+        self.h = lib.skw_ref_accel_create(nm, _ptr(mesh_of), nm, vp, _ptr(nv), tp, _ptr(nt), None)
+        self.n_tris = lib.skw_ref_accel_num_triangles(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.skw_ref_accel_destroy(self.h)
+            self.h = None
+
+    def export(self):
+        nn = self.lib.skw_ref_accel_num_nodes(self.h)
+        bbox = np.empty((nn, 6), np.float32)
+        info = np.empty((nn, 8), np.int32)
+        tp = np.empty(max(self.n_tris, 1), np.int32)
+        ti = np.empty(max(self.n_tris, 1), np.int32)
+        tr = np.empty((max(self.n_tris, 1), 9), np.float32)
+        self.lib.skw_ref_accel_export(self.h, _ptr(bbox), _ptr(info), _ptr(tp), _ptr(ti), _ptr(tr))
+        return bbox, info, tp[:self.n_tris], ti[:self.n_tris]
+
+    def intersect(self, rays, threads=0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        p, t, th = np.empty(n, np.int32), np.empty(n, np.int32), np.empty(n, np.float64)
+        self.lib.skw_ref_intersect(self.h, _ptr(rays), n, _ptr(p), _ptr(t), _ptr(th), threads)
+        return {"prim": p, "tri": t, "t": th}
+
+    def intersect_test(self, rays, threads=0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        occ = np.empty(n, np.uint8)
+        self.lib.skw_ref_intersect_test(self.h, _ptr(rays), n, _ptr(occ), threads)
+        return occ
+
+
+class RefKD:
+    def __init__(self, lib, pos, normal_ids=None, dir_ids=None):
+        self.lib = lib
+        self.pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        n = self.pos.shape[0]
+        self.nids = None if normal_ids is None else np.ascontiguousarray(normal_ids, np.uint16)
+        self.dids = None if dir_ids is None else np.ascontiguousarray(dir_ids, np.uint16)
+        self.perm = np.empty(n, np.int32)
+        self.nodes = np.empty((n, 2), np.uint32)
+        self.h = lib.skw_ref_kdtree_create(_ptr(self.pos), _ptr(self.nids), _ptr(self.dids), n, _ptr(self.perm),
+                                           _ptr(self.nodes))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.skw_ref_kdtree_destroy(self.h)
+            self.h = None
+
+    def knn(self, q, qn, k, max_dist, cos_threshold=-1.0, threads=0):
+        q = np.ascontiguousarray(q, np.float64).reshape(-1, 3)
+        qn = None if qn is None else np.ascontiguousarray(qn, np.float64).reshape(-1, 3)
+        nq = q.shape[0]
+        idx = np.empty((nq, k), np.int32)
+        d2 = np.empty((nq, k), np.float64)
+        cnt = np.empty(nq, np.int32)
+        self.lib.skw_ref_knn(self.h, _ptr(q), _ptr(qn), nq, k, max_dist, cos_threshold, _ptr(idx), _ptr(d2), _ptr(cnt),
+                             threads)
+        return {"idx": idx, "d2": d2, "count": cnt}

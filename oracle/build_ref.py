@@ -1,0 +1,164 @@
+"""Recipe that compiles the reference renderer's own C++ sources into
+``oracle/_ref/libskw_ref.so`` -- test infrastructure, never product code.
+
+What it does:
+
+1. Staging (only where the reference tree is mounted): copies the
+   ``Source/RayLibs/{Common,Math,Raytracer,Shapes}`` sources into
+   ``oracle/_ref/src`` and applies the mechanical, semantics-preserving
+   rewrites g++ needs (the reference targets MSVC 2013):
+
+   * ``X.swap(std::vector<T>())`` (binds a temporary to a non-const
+     reference, an MSVC extension) becomes ``std::vector<T>().swap(X)``
+     (``Raytracer/Core/TriangleAccelerator.cpp:145-146``,
+     ``Raytracer/LTEIntegrators/PhotonLTEIntegrator/PhotonShootingPipeline.cpp:347,357,367``);
+   * ``Texture()`` in the constructors of the texture class templates becomes
+     ``Texture<T>()`` (``Raytracer/Textures/{Constant,Mix,Scale,Windy,Wrinkled}Texture.h``);
+   * a ``MAth`` -> ``Math`` alias for a case typo
+     (``PhotonInternalTypes.h:23``).
+
+   The staged copy is git-ignored; it exists so that the same build can be
+   repeated on a machine without the reference tree.
+2. Shim headers (``oracle/ref_shims``) stand in for Windows, the MSVC debug
+   CRT, Boost (``mt19937``, ``intrusive_ptr``) and TBB (a real thread pool).
+   The MSVC-style ``<a\\b.h>`` includes are satisfied by files whose names
+   contain a literal backslash, generated into ``oracle/_ref/shims``.
+3. Compiles every translation unit except the three that need FreeImage or
+   do not compile upstream (``ImageEnvironmentalLight.cpp``,
+   ``RGBImageSource.cpp``, ``TranslucentMaterial.cpp``; none is on the
+   ray-query / light-transport path), plus ``oracle/ref_driver.cpp`` (our
+   C-ABI shim over the reference classes), into one shared library.
+
+Usage: ``python oracle/build_ref.py`` (idempotent; rebuilds changed files).
+"""
+from __future__ import annotations
+
+import os
+import re
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+SRC = OUT / "src"
+SHIMS = OUT / "shims"
+OBJ = OUT / "obj"
+LIB = OUT / "libskw_ref.so"
+REFERENCE = Path(os.environ.get("SKW_REFERENCE_ROOT", "/root/reference"))
+SUBDIRS = ("Common", "Math", "Raytracer", "Shapes")
+EXCLUDE = {"ImageEnvironmentalLight.cpp", "RGBImageSource.cpp", "TranslucentMaterial.cpp", "dllmain.cpp"}
+# -ffp-contract=off: no fused multiply-add, so that an aarch64 build rounds
+# exactly like the x86-64 (SSE2) build the reference targets.
+CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-fpermissive", "-w", "-DNDEBUG", "-DNOMINMAX", "-pthread",
+            "-ffp-contract=off"]
+
+
+def _rewrite(path: Path) -> None:
+    text = path.read_text(encoding="latin-1")
+    orig = text
+    # X.swap(std::vector<T>())  ->  std::vector<T>().swap(X)
+    text = re.sub(r"(\w+)\.swap\((std::vector<\w+>)\(\)\)", r"\2().swap(\1)", text)
+    if path.parent.name == "Textures" and path.suffix == ".h":
+        text = re.sub(r"^Texture\(\),", "Texture<T>(),", text, flags=re.M)
+    if text != orig:
+        path.write_text(text, encoding="latin-1")
+
+
+def stage() -> None:
+    """Copy + patch the reference sources (only where the reference exists)."""
+    root = REFERENCE / "Source" / "RayLibs"
+    if not root.is_dir():
+        return
+    stamp = SRC / ".staged"
+    if stamp.exists():
+        return
+    if SRC.exists():
+        shutil.rmtree(SRC)
+    for sub in SUBDIRS:
+        shutil.copytree(root / sub, SRC / sub)
+    for p in SRC.rglob("*"):
+        if p.suffix in (".h", ".cpp") and p.is_file():
+            _rewrite(p)
+    (SRC / "MAth").symlink_to("Math")
+    stamp.write_text("staged\n")
+
+
+def make_shims() -> None:
+    SHIMS.mkdir(parents=True, exist_ok=True)
+    src = HERE / "ref_shims"
+    for p in src.rglob("*"):
+        if p.is_file():
+            dst = SHIMS / p.relative_to(src)
+            dst.parent.mkdir(parents=True, exist_ok=True)
+            shutil.copyfile(p, dst)
+    fwd = {
+        "boost\\random\\mersenne_twister.hpp": '#include "boost/mt19937.hpp"\n',
+        "tbb/atomic.h": '#include "tbb.h"\n',
+        "tbb/pipeline.h": '#include "tbb.h"\n',
+        "tbb/parallel_invoke.h": '#include "tbb.h"\n',
+        "tbb/tick_count.h": '#include "tbb.h"\n',
+        "tbb\\enumerable_thread_specific.h": '#include "tbb/tbb.h"\n',
+        "tbb\\cache_aligned_allocator.h": '#include "tbb/tbb.h"\n',
+        "Common\\Common.h": "#include <Common/Common.h>\n",
+    }
+    for name, body in fwd.items():
+        (SHIMS / name).write_text(body)
+
+
+def _sources() -> list[Path]:
+    out = []
+    for sub in SUBDIRS:
+        for p in sorted((SRC / sub).rglob("*.cpp")):
+            if p.name in EXCLUDE or "UnitTests" in p.parts:
+                continue
+            out.append(p)
+    return out
+
+
+def _compile(src: Path, obj: Path, extra: list[str]) -> None:
+    if obj.exists() and obj.stat().st_mtime >= src.stat().st_mtime:
+        return
+    obj.parent.mkdir(parents=True, exist_ok=True)
+    cmd = ["g++", *CXXFLAGS, "-I", str(SHIMS), "-I", str(SRC), "-include", str(SHIMS / "prelude.h"),
+           *extra, "-c", str(src), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle reference build failed on {src}:\n{r.stderr[-4000:]}")
+
+
+def build(verbose: bool = False) -> Path | None:
+    """Build oracle/_ref/libskw_ref.so; returns its path, or None when no
+    staged reference sources are available on this machine."""
+    stage()
+    if not (SRC / ".staged").exists():
+        return None
+    make_shims()
+    flags_stamp = OBJ / ".flags"
+    if OBJ.exists() and (not flags_stamp.exists() or flags_stamp.read_text() != " ".join(CXXFLAGS)):
+        shutil.rmtree(OBJ)
+    OBJ.mkdir(parents=True, exist_ok=True)
+    flags_stamp.write_text(" ".join(CXXFLAGS))
+    srcs = _sources()
+    jobs = [(s, OBJ / (str(s.relative_to(SRC)).replace("/", "__") + ".o"), []) for s in srcs]
+    jobs.append((HERE / "ref_driver.cpp", OBJ / "ref_driver.o", []))
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        list(ex.map(lambda j: _compile(*j), jobs))
+    objs = [str(j[1]) for j in jobs]
+    newest = max(Path(o).stat().st_mtime for o in objs)
+    if not LIB.exists() or LIB.stat().st_mtime < newest:
+        cmd = ["g++", "-shared", "-pthread", "-o", str(LIB), *objs]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"oracle reference link failed:\n{r.stderr[-4000:]}")
+    if verbose:
+        print(f"built {LIB} from {len(srcs)} reference translation units")
+    return LIB
+
+
+if __name__ == "__main__":
+    p = build(verbose=True)
+    if p is None:
+        print("reference sources not available; nothing built", file=sys.stderr)

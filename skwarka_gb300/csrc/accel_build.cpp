@@ -1,0 +1,380 @@
+// Host construction of the ternary bbox kd-tree, restating the reference
+// TriangleAccelerator build (Raytracer/Core/TriangleAccelerator.cpp):
+//   * world-space float triangles per primitive, in primitive order
+//     (ctor steps 3-4, :104-139; the transform is Transform::operator()
+//     on Point3D_f, Math/Transform.h:219-230);
+//   * per node: float AABB of its triangles (_ConstructBBox, :470-481);
+//     leaf if <= 4 triangles, three middle splits on the path, or depth >= 200
+//     (Node::Node, :630-636);
+//   * split search over min(200, 2n) uniform candidate planes per axis with
+//     bucketed left/middle/right boxes and counts, cost
+//     sum(n_child * area_child / area_node) with a 0.8 bonus for an empty
+//     side, first strict minimum per axis, axis ties to the lower axis
+//     (_DetermineBestSplit, :505-617);
+//   * in-place three-way partition with the same swap sequence
+//     (Node::Node, :644-673), so leaves own contiguous triangle ranges.
+// The arithmetic keeps the reference's float/double mix operation by
+// operation (for example the candidate-plane position is computed in float),
+// so that the same input gives the same tree.  Subtrees are built in parallel
+// on disjoint triangle ranges; this changes no result.
+//
+// The tree is then flattened into DevNode/DevTri arrays: pre-order, each
+// internal node's present children stored contiguously.
+#include "accel_build.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <thread>
+
+namespace skw {
+namespace {
+
+constexpr size_t kMaxTrianglesInLeaf = 4;  // TriangleAccelerator.h:128
+constexpr size_t kMaxSplitTries = 200;     // TriangleAccelerator.h:131
+constexpr size_t kMaxTreeDepth = 200;      // TriangleAccelerator.h:134
+
+constexpr float kInfF = std::numeric_limits<float>::infinity();
+constexpr double kInfD = std::numeric_limits<double>::infinity();
+
+struct BoxF {
+  float lo[3] = {kInfF, kInfF, kInfF};
+  float hi[3] = {-kInfF, -kInfF, -kInfF};
+  void unite(const BoxF &o) {
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = std::min(lo[k], o.lo[k]);
+      hi[k] = std::max(hi[k], o.hi[k]);
+    }
+  }
+  // BBox3D<float>::Area (Math/BBox3D.h:141-147): all in float.
+  float area() const {
+    float x = std::fabs(hi[0] - lo[0]);
+    float y = std::fabs(hi[1] - lo[1]);
+    float z = std::fabs(hi[2] - lo[2]);
+    return 2.0f * (x * y + x * z + y * z);
+  }
+};
+
+struct BoxD {
+  double lo[3] = {kInfD, kInfD, kInfD};
+  double hi[3] = {-kInfD, -kInfD, -kInfD};
+  void unite(const BoxF &o) {
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = std::min(lo[k], (double)o.lo[k]);
+      hi[k] = std::max(hi[k], (double)o.hi[k]);
+    }
+  }
+  void unite(const BoxD &o) {
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = std::min(lo[k], o.lo[k]);
+      hi[k] = std::max(hi[k], o.hi[k]);
+    }
+  }
+  double area() const {
+    double x = std::fabs(hi[0] - lo[0]);
+    double y = std::fabs(hi[1] - lo[1]);
+    double z = std::fabs(hi[2] - lo[2]);
+    return 2.0 * (x * y + x * z + y * z);
+  }
+};
+
+// double -> size_t with the result x86-64 g++ code gives for the reference's
+// (size_t) casts: NaN -> 2^63, +inf and values >= 2^64 -> 0.  NaN arises for a
+// node of zero extent along the tested axis (0 * inf).
+inline size_t cast_size(double v) {
+  if (std::isnan(v)) return (size_t)1 << 63;
+  if (v >= 18446744073709551616.0) return 0;
+  if (v >= 9223372036854775808.0) return (size_t)(v - 9223372036854775808.0) + ((size_t)1 << 63);
+  return (size_t)(int64_t)v;
+}
+
+struct BNode {
+  BoxF box;
+  uint32_t tb = 0, te = 0;  // triangle range
+  uint8_t flags = 0;        // 0 leaf, 1..3 axis + 1
+  std::unique_ptr<BNode> child[3];
+};
+
+struct Builder {
+  std::vector<float> tv;      // 9 floats per triangle (world space)
+  std::vector<int32_t> prim;  // primitive index per triangle
+  std::vector<int32_t> tidx;  // mesh triangle index per triangle
+  std::vector<BoxF> tbox;     // per-triangle AABB
+  std::atomic<int> threads_left{0};
+  std::atomic<int32_t> max_depth{0};
+  std::atomic<int64_t> n_leaves{0};
+
+  void swap_tris(size_t a, size_t b) {
+    for (int k = 0; k < 9; ++k) std::swap(tv[9 * a + k], tv[9 * b + k]);
+    std::swap(prim[a], prim[b]);
+    std::swap(tidx[a], tidx[b]);
+    std::swap(tbox[a], tbox[b]);
+  }
+
+  // _DetermineBestSplit (TriangleAccelerator.cpp:505-617), triangles only.
+  void best_split(const BoxF &nb, size_t tb, size_t te, unsigned mask, int &axis_out, double &pos_out) const {
+    const size_t n = te - tb;
+    double best_pos[3] = {0, 0, 0}, best_cost[3] = {kInfD, kInfD, kInfD};
+    for (int axis = 0; axis < 3; ++axis) {
+      if (mask & (1u << axis)) continue;
+      BoxD L[kMaxSplitTries], M[kMaxSplitTries], R[kMaxSplitTries];
+      size_t Ln[kMaxSplitTries] = {0}, Mn[kMaxSplitTries] = {0}, Rn[kMaxSplitTries] = {0};
+      const size_t tries = std::min(kMaxSplitTries, 2 * n);
+      const float ext = nb.hi[axis] - nb.lo[axis];
+      // size_t / float converts the count to float: float division.
+      const double coef = (double)((float)tries / ext);
+      for (size_t i = 0; i < n; ++i) {
+        const BoxF &b = tbox[tb + i];
+        const float dmax = b.hi[axis] - nb.lo[axis];
+        const float dmin = b.lo[axis] - nb.lo[axis];
+        const size_t lefts_begin = std::min(tries, cast_size((double)dmax * coef + 1.0));
+        const size_t rights_end = std::min(tries, cast_size((double)dmin * coef + 1.0));
+        if (rights_end > 0) {
+          R[rights_end - 1].unite(b);
+          Rn[rights_end - 1] += 1;
+        }
+        if (lefts_begin < tries) {
+          L[lefts_begin].unite(b);
+          Ln[lefts_begin] += 1;
+        }
+        for (size_t j = rights_end; j < lefts_begin; ++j) {
+          M[j].unite(b);
+          Mn[j] += 1;
+        }
+      }
+      for (size_t i = 1; i < tries; ++i) {
+        L[i].unite(L[i - 1]);
+        Ln[i] += Ln[i - 1];
+      }
+      for (int i = (int)tries - 2; i >= 0; --i) {
+        R[i].unite(R[i + 1]);
+        Rn[i] += Rn[i + 1];
+      }
+      const double inv_area = 1.0 / (double)nb.area();
+      for (size_t i = 0; i < tries; ++i) {
+        const double p1 = std::min(1.0, L[i].area() * inv_area);
+        const double p2 = std::min(1.0, M[i].area() * inv_area);
+        const double p3 = std::min(1.0, R[i].area() * inv_area);
+        double cost = (double)Ln[i] * p1 + (double)Mn[i] * p2 + (double)Rn[i] * p3;
+        if (Ln[i] == 0 || Rn[i] == 0) cost *= 0.8;
+        if (cost < best_cost[axis]) {
+          best_cost[axis] = cost;
+          // min + i*(max-min)/tries, evaluated in float.
+          best_pos[axis] = (double)(nb.lo[axis] + ((float)i * ext) / (float)tries);
+        }
+      }
+    }
+    if (best_cost[0] <= best_cost[1] && best_cost[0] <= best_cost[2]) {
+      axis_out = 0;
+    } else if (best_cost[1] <= best_cost[0] && best_cost[1] <= best_cost[2]) {
+      axis_out = 1;
+    } else {
+      axis_out = 2;
+    }
+    pos_out = best_pos[axis_out];
+  }
+
+  // Node::Node (TriangleAccelerator.cpp:621-729), triangles only.
+  std::unique_ptr<BNode> build(size_t tb, size_t te, unsigned mask, size_t depth) {
+    auto node = std::make_unique<BNode>();
+    node->tb = (uint32_t)tb;
+    node->te = (uint32_t)te;
+    for (size_t i = tb; i < te; ++i) node->box.unite(tbox[i]);
+    int32_t d = (int32_t)depth;
+    int32_t cur = max_depth.load();
+    while (d > cur && !max_depth.compare_exchange_weak(cur, d)) {
+    }
+    if (te - tb <= kMaxTrianglesInLeaf || mask == 7u || depth >= kMaxTreeDepth) {
+      node->flags = 0;
+      n_leaves.fetch_add(1);
+      return node;
+    }
+    int axis;
+    double split;
+    best_split(node->box, tb, te, mask, axis, split);
+    node->flags = (uint8_t)(axis + 1);
+
+    size_t mid_begin = tb, right_begin = te, i = tb;
+    while (i < right_begin) {
+      const BoxF &b = tbox[i];
+      if ((double)b.hi[axis] < split) {
+        swap_tris(mid_begin, i);
+        ++mid_begin;
+        ++i;
+      } else if ((double)b.lo[axis] > split) {
+        --right_begin;
+        swap_tris(i, right_begin);
+      } else {
+        ++i;
+      }
+    }
+    struct Range {
+      size_t b, e;
+      unsigned m;
+    } ranges[3] = {{tb, mid_begin, mask}, {mid_begin, right_begin, mask | (1u << axis)}, {right_begin, te, mask}};
+    // Large subtrees run on their own thread while the budget lasts.
+    std::thread workers[3];
+    bool spawned[3] = {false, false, false};
+    for (int c = 0; c < 3; ++c) {
+      if (ranges[c].b >= ranges[c].e) continue;
+      if (ranges[c].e - ranges[c].b > 20000 && threads_left.fetch_sub(1) > 0) {
+        spawned[c] = true;
+        workers[c] = std::thread([this, node_ptr = node.get(), c, r = ranges[c], depth]() {
+          node_ptr->child[c] = build(r.b, r.e, r.m, depth + 1);
+        });
+      } else {
+        node->child[c] = build(ranges[c].b, ranges[c].e, ranges[c].m, depth + 1);
+      }
+    }
+    for (int c = 0; c < 3; ++c)
+      if (spawned[c]) workers[c].join();
+    return node;
+  }
+};
+
+// Transform::operator()(const Point3D<float>&) (Math/Transform.h:219-230).
+inline void transform_point(const double *m, const float *p, float *out) {
+  const float x = p[0], y = p[1], z = p[2];
+  float xp = (float)(m[0] * x + m[1] * y + m[2] * z + m[3]);
+  float yp = (float)(m[4] * x + m[5] * y + m[6] * z + m[7]);
+  float zp = (float)(m[8] * x + m[9] * y + m[10] * z + m[11]);
+  float wp = (float)(m[12] * x + m[13] * y + m[14] * z + m[15]);
+  if (wp == 1.0f) {
+    out[0] = xp;
+    out[1] = yp;
+    out[2] = zp;
+  } else {
+    // Point3D<float>::operator/(double): multiply by the double reciprocal.
+    double inv = 1.0 / (double)wp;
+    out[0] = (float)(xp * inv);
+    out[1] = (float)(yp * inv);
+    out[2] = (float)(zp * inv);
+  }
+}
+
+}  // namespace
+
+std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *prims, int32_t n_prims, int threads,
+                        FlatTree &out) {
+  if (n_prims < 0 || n_meshes < 0) return "negative primitive or mesh count";
+  std::vector<int> uses((size_t)n_meshes, 0);
+  for (int32_t p = 0; p < n_prims; ++p) {
+    if (prims[p].mesh < 0 || prims[p].mesh >= n_meshes) return "primitive references a mesh index out of range";
+    if (++uses[(size_t)prims[p].mesh] > 1)
+      return "a mesh shared by several primitives (instancing) is not supported by this build";
+  }
+  Builder B;
+  // TriangleMesh drops triangles with an out-of-range or repeated vertex
+  // index (TriangleMesh.cpp:176-182); mesh triangle indices count kept ones.
+  for (int32_t p = 0; p < n_prims; ++p) {
+    const MeshIn &m = meshes[prims[p].mesh];
+    if (m.n_triangles > 0 && (!m.triangles || !m.vertices)) return "mesh has triangles but null arrays";
+    int32_t kept = 0;
+    for (int64_t t = 0; t < m.n_triangles; ++t) {
+      const int32_t *ix = m.triangles + 3 * t;
+      bool bad = false;
+      for (int k = 0; k < 3; ++k)
+        if (ix[k] < 0 || (int64_t)ix[k] >= m.n_vertices) bad = true;
+      if (bad || ix[0] == ix[1] || ix[0] == ix[2] || ix[1] == ix[2]) continue;
+      float v[9];
+      for (int k = 0; k < 3; ++k) {
+        const float *src = m.vertices + 3 * (int64_t)ix[k];
+        if (prims[p].mesh_to_world) {
+          transform_point(prims[p].mesh_to_world, src, v + 3 * k);
+        } else {
+          v[3 * k] = src[0];
+          v[3 * k + 1] = src[1];
+          v[3 * k + 2] = src[2];
+        }
+      }
+      BoxF b;
+      for (int k = 0; k < 3; ++k) {
+        for (int c = 0; c < 3; ++c) {
+          b.lo[c] = std::min(b.lo[c], v[3 * k + c]);
+          b.hi[c] = std::max(b.hi[c], v[3 * k + c]);
+        }
+      }
+      B.tv.insert(B.tv.end(), v, v + 9);
+      B.prim.push_back(p);
+      B.tidx.push_back(kept++);
+      B.tbox.push_back(b);
+    }
+  }
+  const size_t n = B.prim.size();
+  if (n > (size_t)INT32_MAX) return "too many triangles";
+  unsigned hw = std::thread::hardware_concurrency();
+  B.threads_left = (threads > 0 ? threads : (int)(hw ? hw : 1)) - 1;
+
+  out.nodes.clear();
+  out.tris.clear();
+  if (n == 0) {
+    // An empty accelerator: a single empty leaf whose box culls every ray.
+    DevNode leaf{};
+    for (int k = 0; k < 3; ++k) {
+      leaf.lo[k] = kInfF;
+      leaf.hi[k] = -kInfF;
+    }
+    leaf.a = 0;
+    leaf.b = 0;
+    out.nodes.push_back(leaf);
+    out.max_depth = 0;
+    out.n_leaves = 1;
+    for (int k = 0; k < 6; ++k) out.bounds[k] = 0.f;
+    return "";
+  }
+  std::unique_ptr<BNode> root = B.build(0, n, 0u, 0);
+
+  // Flatten: pre-order; a node's present children occupy consecutive slots.
+  out.nodes.reserve(n);
+  out.nodes.emplace_back();
+  std::vector<std::pair<const BNode *, uint32_t>> stack{{root.get(), 0u}};
+  while (!stack.empty()) {
+    auto [bn, idx] = stack.back();
+    stack.pop_back();
+    DevNode dn{};
+    for (int k = 0; k < 3; ++k) {
+      dn.lo[k] = bn->box.lo[k];
+      dn.hi[k] = bn->box.hi[k];
+    }
+    if (bn->flags == 0) {
+      dn.a = bn->tb;
+      dn.b = (uint32_t)(bn->te - bn->tb) << 8;
+    } else {
+      uint32_t first = (uint32_t)out.nodes.size(), mask = 0, slot = first;
+      std::pair<const BNode *, uint32_t> kids[3];
+      int nk = 0;
+      for (int c = 0; c < 3; ++c)
+        if (bn->child[c]) {
+          mask |= 1u << c;
+          kids[nk++] = {bn->child[c].get(), slot++};
+          out.nodes.emplace_back();
+        }
+      dn.a = first;
+      dn.b = (uint32_t)bn->flags | (mask << 2);
+      for (int k = nk - 1; k >= 0; --k) stack.push_back(kids[k]);
+    }
+    out.nodes[idx] = dn;
+  }
+  out.tris.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    DevTri &t = out.tris[i];
+    std::memcpy(t.v0, &B.tv[9 * i], 12);
+    std::memcpy(t.v1, &B.tv[9 * i + 3], 12);
+    std::memcpy(t.v2, &B.tv[9 * i + 6], 12);
+    t.prim = B.prim[i];
+    t.tri = B.tidx[i];
+    t.slot = (int32_t)i;
+  }
+  out.max_depth = B.max_depth.load();
+  out.n_leaves = B.n_leaves.load();
+  for (int k = 0; k < 3; ++k) {
+    out.bounds[k] = root->box.lo[k];
+    out.bounds[3 + k] = root->box.hi[k];
+  }
+  return "";
+}
+
+}  // namespace skw

@@ -1,0 +1,67 @@
+// Host-side construction of the ternary bbox kd-tree and its flattening into
+// the device layout used by the traversal kernels.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace skw {
+
+// One node of the device tree: 32 bytes, 32-byte aligned, read as two
+// 16-byte vector loads.
+//   lo/hi : float AABB of the node's triangles (the reference's Node::m_bbox)
+//   a     : internal -> index of the first child (children are contiguous, in
+//           left, middle, right order, absent ones skipped)
+//           leaf     -> index of the first triangle slot
+//   b     : bits 0-1 type (0 = leaf, 1..3 = internal with split axis + 1,
+//           the reference's Node::m_flags & 3)
+//           internal -> bits 2-4 child-present mask (1 left, 2 middle, 4 right)
+//           leaf     -> bits 8-31 triangle count
+struct alignas(32) DevNode {
+  float lo[3];
+  float hi[3];
+  uint32_t a;
+  uint32_t b;
+};
+static_assert(sizeof(DevNode) == 32, "DevNode must be 32 bytes");
+
+// One triangle slot: 48 bytes = 3 x float4 (v0, prim), (v1, tri), (v2, slot)
+// with the integer ids stored in the .w lanes as raw bits.
+struct alignas(16) DevTri {
+  float v0[3];
+  int32_t prim;
+  float v1[3];
+  int32_t tri;
+  float v2[3];
+  int32_t slot;
+};
+static_assert(sizeof(DevTri) == 48, "DevTri must be 48 bytes");
+
+struct MeshIn {
+  const float *vertices;
+  int64_t n_vertices;
+  const int32_t *triangles;
+  int64_t n_triangles;
+};
+
+struct PrimIn {
+  int32_t mesh;
+  const double *mesh_to_world;  // row-major 4x4 or null
+};
+
+struct FlatTree {
+  std::vector<DevNode> nodes;
+  std::vector<DevTri> tris;
+  int32_t max_depth = 0;
+  int64_t n_leaves = 0;
+  float bounds[6] = {0, 0, 0, 0, 0, 0};
+};
+
+// Builds the tree (same split search, partition order and leaf rule as the
+// reference TriangleAccelerator) and flattens it.  `threads` <= 0 uses all
+// hardware threads.  Returns an empty string on success, else an error.
+std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *prims, int32_t n_prims,
+                        int threads, FlatTree &out);
+
+}  // namespace skw

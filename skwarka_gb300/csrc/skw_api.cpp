@@ -1,0 +1,284 @@
+// C ABI (include/skw.h): contexts, accelerator handles and ray queries.
+// Host-side logic only; the kernels live in the .cu translation units.
+#include "../../include/skw.h"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "accel_build.h"
+#include "kernels.h"
+#include "skw_internal.h"
+
+using skw::DevNode;
+using skw::DevTri;
+
+struct skw_accel {
+  skw_ctx *ctx = nullptr;
+  DevNode *d_nodes = nullptr;
+  DevTri *d_tris = nullptr;
+  unsigned *d_status = nullptr;
+  int stack_cap = 0;
+  skw_accel_info info{};
+  std::vector<DevNode> h_nodes;
+  std::vector<DevTri> h_tris;
+};
+
+namespace skw {
+
+int fail(skw_ctx *ctx, int code, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+int cuda_fail(skw_ctx *ctx, cudaError_t e, const char *what) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? SKW_ERR_OOM : SKW_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace skw
+
+using skw::cuda_fail;
+using skw::fail;
+
+extern "C" {
+
+int skw_version(void) { return 100; }
+
+int skw_ctx_create(int device, skw_ctx **out) {
+  if (!out) return SKW_ERR_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return SKW_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= count) return SKW_ERR_ARG;
+  auto *ctx = new (std::nothrow) skw_ctx();
+  if (!ctx) return SKW_ERR_OOM;
+  ctx->device = device;
+  *out = ctx;
+  return SKW_OK;
+}
+
+void skw_ctx_destroy(skw_ctx *ctx) { delete ctx; }
+
+const char *skw_last_error(const skw_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int64_t skw_launch_count(const skw_ctx *ctx) { return ctx ? ctx->launches.load() : 0; }
+
+struct skw_flat_tree {
+  skw::FlatTree ft;
+  double build_ms = 0.0;
+};
+
+int skw_flat_tree_build(const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims, int32_t n_prims,
+                        int threads, skw_flat_tree **out, char *err, size_t errlen) {
+  auto set_err = [&](const std::string &m) {
+    if (err && errlen > 0) {
+      std::strncpy(err, m.c_str(), errlen - 1);
+      err[errlen - 1] = 0;
+    }
+  };
+  if (!out || (n_meshes > 0 && !meshes) || (n_prims > 0 && !prims)) {
+    set_err("null argument");
+    return SKW_ERR_ARG;
+  }
+  *out = nullptr;
+  std::vector<skw::MeshIn> m((size_t)std::max(n_meshes, 0));
+  for (int32_t i = 0; i < n_meshes; ++i)
+    m[(size_t)i] = skw::MeshIn{meshes[i].vertices, meshes[i].n_vertices, meshes[i].triangles, meshes[i].n_triangles};
+  std::vector<skw::PrimIn> p((size_t)std::max(n_prims, 0));
+  for (int32_t i = 0; i < n_prims; ++i) p[(size_t)i] = skw::PrimIn{prims[i].mesh, prims[i].mesh_to_world};
+  auto *t = new (std::nothrow) skw_flat_tree();
+  if (!t) return SKW_ERR_OOM;
+  auto t0 = std::chrono::steady_clock::now();
+  std::string e = skw::build_accel(m.data(), n_meshes, p.data(), n_prims, threads, t->ft);
+  t->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (!e.empty()) {
+    delete t;
+    set_err(e);
+    return e.find("instancing") != std::string::npos ? SKW_ERR_UNSUPPORTED : SKW_ERR_ARG;
+  }
+  *out = t;
+  return SKW_OK;
+}
+
+void skw_flat_tree_destroy(skw_flat_tree *t) { delete t; }
+
+int skw_flat_tree_sizes(const skw_flat_tree *t, int64_t *n_nodes, int64_t *n_triangles, int32_t *max_depth) {
+  if (!t) return SKW_ERR_ARG;
+  if (n_nodes) *n_nodes = (int64_t)t->ft.nodes.size();
+  if (n_triangles) *n_triangles = (int64_t)t->ft.tris.size();
+  if (max_depth) *max_depth = t->ft.max_depth;
+  return SKW_OK;
+}
+
+int skw_flat_tree_export(const skw_flat_tree *t, uint32_t *nodes, float *tris, int32_t *tri_prim, int32_t *tri_index) {
+  if (!t) return SKW_ERR_ARG;
+  if (nodes) std::memcpy(nodes, t->ft.nodes.data(), t->ft.nodes.size() * sizeof(DevNode));
+  for (size_t i = 0; i < t->ft.tris.size(); ++i) {
+    const DevTri &d = t->ft.tris[i];
+    if (tris) {
+      std::memcpy(tris + 9 * i, d.v0, 12);
+      std::memcpy(tris + 9 * i + 3, d.v1, 12);
+      std::memcpy(tris + 9 * i + 6, d.v2, 12);
+    }
+    if (tri_prim) tri_prim[i] = d.prim;
+    if (tri_index) tri_index[i] = d.tri;
+  }
+  return SKW_OK;
+}
+
+int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_accel **out) {
+  if (!ctx || !tree || !out) return fail(ctx, SKW_ERR_ARG, "null argument");
+  *out = nullptr;
+  const skw::FlatTree &ft = tree->ft;
+  auto *a = new (std::nothrow) skw_accel();
+  if (!a) return fail(ctx, SKW_ERR_OOM, "host allocation failed");
+  a->ctx = ctx;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) {
+    delete a;
+    return cuda_fail(ctx, e, "cudaSetDevice");
+  }
+  const size_t nb = ft.nodes.size() * sizeof(DevNode), tb = std::max<size_t>(ft.tris.size(), 1) * sizeof(DevTri);
+  if ((e = cudaMalloc(&a->d_nodes, nb)) != cudaSuccess || (e = cudaMalloc(&a->d_tris, tb)) != cudaSuccess ||
+      (e = cudaMalloc(&a->d_status, sizeof(unsigned))) != cudaSuccess) {
+    skw_accel_destroy(a);
+    return cuda_fail(ctx, e, "cudaMalloc (accelerator)");
+  }
+  if ((e = cudaMemcpy(a->d_nodes, ft.nodes.data(), nb, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (!ft.tris.empty() &&
+       (e = cudaMemcpy(a->d_tris, ft.tris.data(), ft.tris.size() * sizeof(DevTri), cudaMemcpyHostToDevice)) !=
+           cudaSuccess) ||
+      (e = cudaMemset(a->d_status, 0, sizeof(unsigned))) != cudaSuccess) {
+    skw_accel_destroy(a);
+    return cuda_fail(ctx, e, "upload (accelerator)");
+  }
+  a->stack_cap = skw::traversal_stack_capacity(ft.max_depth);
+  skw_accel_info &info = a->info;
+  info.n_triangles = (int64_t)ft.tris.size();
+  info.n_nodes = (int64_t)ft.nodes.size();
+  info.n_leaves = ft.n_leaves;
+  info.max_depth = ft.max_depth;
+  info.stack_need = 2 * ft.max_depth + 1;
+  std::memcpy(info.bounds, ft.bounds, sizeof(info.bounds));
+  info.build_ms = tree->build_ms;
+  info.device_bytes = (int64_t)(nb + tb);
+  a->h_nodes = ft.nodes;
+  a->h_tris = ft.tris;
+  *out = a;
+  return SKW_OK;
+}
+
+int skw_accel_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims,
+                     int32_t n_prims, skw_accel **out) {
+  if (!ctx || !out) return fail(ctx, SKW_ERR_ARG, "null argument");
+  skw_flat_tree *t = nullptr;
+  char err[256] = {0};
+  int rc = skw_flat_tree_build(meshes, n_meshes, prims, n_prims, 0, &t, err, sizeof(err));
+  if (rc != SKW_OK) return fail(ctx, rc, err);
+  rc = skw_accel_create_from_flat(ctx, t, out);
+  skw_flat_tree_destroy(t);
+  return rc;
+}
+
+void skw_accel_destroy(skw_accel *a) {
+  if (!a) return;
+  cudaFree(a->d_nodes);
+  cudaFree(a->d_tris);
+  cudaFree(a->d_status);
+  delete a;
+}
+
+int skw_accel_get_info(const skw_accel *a, skw_accel_info *info) {
+  if (!a || !info) return SKW_ERR_ARG;
+  *info = a->info;
+  return SKW_OK;
+}
+
+int skw_accel_export(const skw_accel *a, uint32_t *nodes, int32_t *tri_prim, int32_t *tri_index) {
+  if (!a) return SKW_ERR_ARG;
+  if (nodes) std::memcpy(nodes, a->h_nodes.data(), a->h_nodes.size() * sizeof(DevNode));
+  for (size_t i = 0; i < a->h_tris.size(); ++i) {
+    if (tri_prim) tri_prim[i] = a->h_tris[i].prim;
+    if (tri_index) tri_index[i] = a->h_tris[i].tri;
+  }
+  return SKW_OK;
+}
+
+static int run_query(skw_accel *a, bool closest, const skw_ray *rays, int64_t n, void *out, void *stream) {
+  if (!a) return SKW_ERR_ARG;
+  if (n < 0 || (n > 0 && (!rays || !out))) return fail(a->ctx, SKW_ERR_ARG, "bad ray buffer");
+  if (n > ((int64_t)1 << 31) * 128) return fail(a->ctx, SKW_ERR_ARG, "too many rays for one launch");
+  if (n == 0) return SKW_OK;
+  cudaError_t e = cudaSetDevice(a->ctx->device);
+  if (e != cudaSuccess) return cuda_fail(a->ctx, e, "cudaSetDevice");
+  e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, out, a->d_status,
+                            (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(a->ctx, e, closest ? "closest-hit launch" : "any-hit launch");
+  a->ctx->launches.fetch_add(1);
+  return SKW_OK;
+}
+
+int skw_intersect(skw_accel *a, const skw_ray *rays, int64_t n, skw_hit *hits, void *stream) {
+  return run_query(a, true, rays, n, hits, stream);
+}
+
+int skw_intersect_test(skw_accel *a, const skw_ray *rays, int64_t n, uint8_t *occluded, void *stream) {
+  return run_query(a, false, rays, n, occluded, stream);
+}
+
+static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64_t n, void *out) {
+  if (!a) return SKW_ERR_ARG;
+  if (n < 0 || (n > 0 && (!rays || !out))) return fail(a->ctx, SKW_ERR_ARG, "bad ray buffer");
+  if (n == 0) return SKW_OK;
+  cudaError_t e = cudaSetDevice(a->ctx->device);
+  if (e != cudaSuccess) return cuda_fail(a->ctx, e, "cudaSetDevice");
+  const size_t out_bytes = (size_t)n * (closest ? sizeof(skw_hit) : 1);
+  void *d_rays = nullptr, *d_out = nullptr;
+  cudaStream_t s = nullptr;
+  int rc = SKW_OK;
+  if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(a->ctx, e, "stream");
+  if ((e = cudaMallocAsync(&d_rays, (size_t)n * sizeof(skw_ray), s)) != cudaSuccess ||
+      (e = cudaMallocAsync(&d_out, out_bytes, s)) != cudaSuccess) {
+    rc = cuda_fail(a->ctx, e, "cudaMallocAsync");
+  } else if ((e = cudaMemcpyAsync(d_rays, rays, (size_t)n * sizeof(skw_ray), cudaMemcpyHostToDevice, s)) !=
+             cudaSuccess) {
+    rc = cuda_fail(a->ctx, e, "copy rays in");
+  } else if ((rc = run_query(a, closest, (const skw_ray *)d_rays, n, d_out, s)) == SKW_OK) {
+    if ((e = cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+      rc = cuda_fail(a->ctx, e, "copy results out");
+  }
+  cudaFreeAsync(d_rays, s);
+  cudaFreeAsync(d_out, s);
+  e = cudaStreamSynchronize(s);
+  if (rc == SKW_OK && e != cudaSuccess) rc = cuda_fail(a->ctx, e, "query execution");
+  cudaStreamDestroy(s);
+  if (rc == SKW_OK) {
+    unsigned st = 0;
+    if ((e = cudaMemcpy(&st, a->d_status, sizeof(st), cudaMemcpyDeviceToHost)) != cudaSuccess)
+      return cuda_fail(a->ctx, e, "status read");
+    if (st & 1u) {
+      cudaMemset(a->d_status, 0, sizeof(unsigned));
+      return fail(a->ctx, SKW_ERR_STACK_OVERFLOW, "traversal stack overflow");
+    }
+  }
+  return rc;
+}
+
+int skw_intersect_host(skw_accel *a, const skw_ray *rays, int64_t n, skw_hit *hits) {
+  return run_query_host(a, true, rays, n, hits);
+}
+
+int skw_intersect_test_host(skw_accel *a, const skw_ray *rays, int64_t n, uint8_t *occluded) {
+  return run_query_host(a, false, rays, n, occluded);
+}
+
+}  // extern "C"

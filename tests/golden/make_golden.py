@@ -1,0 +1,76 @@
+"""Generates tests/golden/*.npz from the reference's own code
+(oracle/_ref/libskw_ref.so, built from the reference sources by
+oracle/build_ref.py).  Run from the repository root:
+
+    python tests/golden/make_golden.py
+
+The fixtures hold inputs and the reference's answers; the tests check the
+oracle and the CUDA path against them without needing the reference."""
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+from oracle import build_ref  # noqa: E402
+from oracle.api import Reference  # noqa: E402
+from skwarka_gb300 import scenes  # noqa: E402
+import scene_fixtures as sf  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def accel_golden():
+    meshes = scenes.ray_query_scene(sphere_subdivisions=4, n_random=300, seed=21)
+    lo, hi = scenes.scene_bounds(meshes)
+    rays = scenes.uniform_rays(3000, lo, hi, seed=22)
+    srays = scenes.uniform_rays(3000, lo, hi, seed=23, tmax_range=(0.0, 2.0))
+    ref = Reference()
+    ra = ref.accel(meshes)
+    h = ra.intersect(rays, threads=1)
+    occ = ra.intersect_test(srays, threads=1)
+    bbox, info, tp, ti = ra.export()
+    arrays = {"rays": rays, "shadow_rays": srays, "hit_prim": h["prim"], "hit_tri": h["tri"], "hit_t": h["t"],
+              "occluded": occ, "node_bbox": bbox, "node_info": info, "tri_prim": tp, "tri_index": ti}
+    for i, (v, t) in enumerate(meshes):
+        arrays[f"mesh{i}_vertices"] = v
+        arrays[f"mesh{i}_triangles"] = t
+    np.savez_compressed(OUT / "accel_small.npz", **arrays)
+
+
+def knn_golden():
+    rng = np.random.default_rng(31)
+    n = 4000
+    pos = rng.uniform(0, 1, size=(n, 3)).astype(np.float32)
+    pos[:100] = pos[100:200]  # duplicated points, as in the reference's KDTree test
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    ref = Reference()
+    nids = np.array([ref.lib.skw_ref_compress_direction(*v) for v in nrm], np.uint16)
+    kd = ref.kdtree(pos, nids)
+    q = rng.uniform(0, 1, size=(500, 3))
+    qn = rng.normal(size=(500, 3))
+    qn /= np.linalg.norm(qn, axis=1, keepdims=True)
+    res_f = kd.knn(q, qn, 20, 0.15, 0.5, threads=1)
+    res_u = kd.knn(q, None, 20, 0.2, -1.0, threads=1)
+    np.savez_compressed(OUT / "knn_small.npz", pos=pos, normal_ids=nids, perm=kd.perm, nodes=kd.nodes, q=q, qn=qn,
+                        filt_idx=res_f["idx"], filt_d2=res_f["d2"], filt_count=res_f["count"],
+                        all_idx=res_u["idx"], all_d2=res_u["d2"], all_count=res_u["count"])
+
+
+def direction_golden():
+    tab = Reference().direction_table()
+    sample = np.arange(0, 1 << 16, 97)
+    np.savez_compressed(OUT / "compressed_direction.npz", ids=sample, vectors=tab[sample])
+
+
+if __name__ == "__main__":
+    if build_ref.build() is None:
+        sys.exit("the reference sources are needed to generate the golden fixtures")
+    accel_golden()
+    knn_golden()
+    direction_golden()
+    print("golden fixtures written to", OUT)
