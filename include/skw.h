@@ -95,6 +95,9 @@ typedef struct skw_hit {
 #define SKW_HIT_FP64_DECIDED 1u
 /* Two candidate triangles had double-precision t within 1e-12 relative. */
 #define SKW_HIT_NEAR_TIE 2u
+/* The hit was decided in float but its t was recomputed exactly (grazing
+ * incidence, where the float t's error bound exceeds 5e-6 relative). */
+#define SKW_HIT_T_REFINED 4u
 
 typedef struct skw_accel_info {
   int64_t n_triangles;

@@ -21,8 +21,9 @@
 //
 // Layout: nodes are 32-byte DevNode records read as two 16-byte loads; each
 // triangle slot is 3 x float4 (v0|prim, v1|tri, v2|slot); rays are 2 x float4.
-// The per-thread stack lives in local memory (L1-resident); its capacity CAP
-// is chosen on the host as >= 2 * tree depth + 1, which bounds its use.
+// The per-thread stack (16-byte entries) lives in local memory (L1-resident);
+// its capacity CAP is chosen on the host as >= 2 * tree depth + 1, which
+// bounds its use (at most two entries are pushed per level).
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -32,8 +33,23 @@ namespace skw {
 namespace {
 
 constexpr float kWiden = 8.0f * 5.9604645e-8f;  // 8 * 2^-24: slab interval widening
-constexpr float kTriErr = 16.0f * 5.9604645e-8f; // 16 * 2^-24: triangle-test error bound scale
+// Forward error bound of the float triangle test: with u = 2^-24, the edge
+// and offset vectors carry <= u relative error, the cross products <= 4u of
+// their magnitude sums, and det, n1, n2, nt <= 8u of the matching
+// magnitude dot products (first order); 10u leaves room for the second-order
+// terms and for the bounds being evaluated in float.
+constexpr float kTriErr = 10.0f * 5.9604645e-8f;
 constexpr double kDblEps = 2.220446049250313e-16;
+
+// Launch shape: threads per block and the minimum resident blocks per SM
+// that bounds the register budget (set by measurement; overridable at
+// build time for sweeps).
+#ifndef SKW_TRAV_BLOCK
+#define SKW_TRAV_BLOCK 128
+#endif
+#ifndef SKW_TRAV_MINB
+#define SKW_TRAV_MINB 4
+#endif
 
 enum : int { kMiss = 0, kHit = 1, kAmbiguous = 2 };
 
@@ -85,9 +101,8 @@ __device__ __forceinline__ int tri_test32(const RayF &r, float3 v0, float3 v1, f
   if ((N1 + N2) - (en1 + en2) > D + edet) return kMiss;
   const float inv = 1.0f / D;
   t = NT * inv;
-  et = (ent + fabsf(t) * edet) * inv * 1.0001f + fabsf(t) * 4.0e-7f + 1e-30f;
+  et = (ent + fabsf(t) * edet) * inv * 1.0001f + fabsf(t) * 2.4e-7f + 1e-30f;
   if (t + et < r.tmin) return kMiss;
-  if (et > 1.0e-6f * fabsf(t)) return kAmbiguous;  // keep reported t within 1e-6 relative
   if (N1 - en1 > 0.0f && N2 - en2 > 0.0f && (N1 + N2) + (en1 + en2) < D - edet && t - et >= r.tmin) return kHit;
   return kAmbiguous;
 }
@@ -142,52 +157,124 @@ __device__ __forceinline__ void load_tri(const float4 *__restrict__ tris, uint32
 }
 
 // Reference slab test (TriangleAccelerator.cpp:176-192) on a widened float
-// interval: returns true when the node must be visited.
+// interval.  Returns true when the node must be visited; `lo` receives the
+// widened entry distance max(tnear_x, tnear_y, tnear_z, tmin), which is all
+// a later re-test against a smaller tmax needs.
 __device__ __forceinline__ bool node_visit(const float4 na, const float4 nb, const RayF &r, float ix, float iy,
-                                           float iz, float tcull) {
+                                           float iz, float tcull, float &lo) {
   float tn0 = (na.x - r.ox) * ix, tf0 = (na.w - r.ox) * ix;
   float tn1 = (na.y - r.oy) * iy, tf1 = (nb.x - r.oy) * iy;
   float tn2 = (na.z - r.oz) * iz, tf2 = (nb.y - r.oz) * iz;
-  if (tn0 > tf0) {
-    const float s = tn0;
-    tn0 = tf0;
-    tf0 = s;
-  }
-  if (tn1 > tf1) {
-    const float s = tn1;
-    tn1 = tf1;
-    tf1 = s;
-  }
-  if (tn2 > tf2) {
-    const float s = tn2;
-    tn2 = tf2;
-    tf2 = s;
-  }
-  tn0 = fmaf(-kWiden, fabsf(tn0), tn0);
-  tn1 = fmaf(-kWiden, fabsf(tn1), tn1);
-  tn2 = fmaf(-kWiden, fabsf(tn2), tn2);
-  tf0 = fmaf(kWiden, fabsf(tf0), tf0);
-  tf1 = fmaf(kWiden, fabsf(tf1), tf1);
-  tf2 = fmaf(kWiden, fabsf(tf2), tf2);
-  // fmaxf/fminf skip NaN operands, like the reference's comparisons that are
-  // false on NaN.
-  const float lo = fmaxf(fmaxf(tn0, tn1), fmaxf(tn2, r.tmin));
-  const float hi = fminf(fminf(tf0, tf1), fminf(tf2, tcull));
+  const float a0 = fminf(tn0, tf0), b0 = fmaxf(tn0, tf0);
+  const float a1 = fminf(tn1, tf1), b1 = fmaxf(tn1, tf1);
+  const float a2 = fminf(tn2, tf2), b2 = fmaxf(tn2, tf2);
+  // NaN (0 * inf) slabs: fminf/fmaxf return the other operand, and the
+  // widened bounds below drop NaN, matching the reference's comparisons,
+  // which are all false on NaN.
+  const float l0 = fmaf(-kWiden, fabsf(a0), a0), h0 = fmaf(kWiden, fabsf(b0), b0);
+  const float l1 = fmaf(-kWiden, fabsf(a1), a1), h1 = fmaf(kWiden, fabsf(b1), b1);
+  const float l2 = fmaf(-kWiden, fabsf(a2), a2), h2 = fmaf(kWiden, fabsf(b2), b2);
+  lo = fmaxf(fmaxf(l0, l1), fmaxf(l2, r.tmin));
+  const float hi = fminf(fminf(h0, h1), fminf(h2, tcull));
   return !(lo > hi);
 }
 
+// Per-thread traversal state shared by the closest-hit and any-hit kernels.
+//
+// Visit order equals the reference's (TriangleAccelerator.cpp:170-211): the
+// reference pushes an internal node's children and pops the near-side one
+// first, testing each node's box when it is popped.  Here an internal node's
+// present children (contiguous, so their loads go out together) are box-tested
+// right away; the first passing one in the reference's pop order becomes the
+// current node and the rest are pushed so that they pop in that order.  A
+// pushed entry keeps its widened entry distance, and popping re-culls it
+// against the tmax of that moment -- the only part of the reference's
+// pop-time box test that can change after the push, since tmax only shrinks.
+struct StackEntry {
+  uint32_t a, b;  // the node's words 6 and 7
+  float lo;       // widened entry distance
+  uint32_t pad;
+};
+
 template <int CAP>
-__global__ void __launch_bounds__(128) k_closest_hit(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
+struct Traversal {
+  uint4 stack[CAP];
+  int sp;
+  uint32_t cur_a, cur_b;  // current node (passed its box test)
+
+  __device__ __forceinline__ bool pop(float tcull) {
+    while (sp > 0) {
+      const uint4 e = stack[--sp];
+      if (__uint_as_float(e.z) > tcull) continue;  // the reference culls it at pop
+      cur_a = e.x;
+      cur_b = e.y;
+      return true;
+    }
+    return false;
+  }
+
+  // Expands internal nodes until the current node is a leaf; false when the
+  // stack runs out.  status bit 0 records an (impossible by construction)
+  // stack overflow.
+  __device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const RayF &r, float ix, float iy,
+                                          float iz, float tcull, unsigned *status) {
+    while ((cur_b & 3u) != 0u) {
+      const uint32_t type = cur_b & 3u, mask = (cur_b >> 2) & 7u;
+      const uint32_t sL = cur_a, sM = cur_a + (mask & 1u), sR = sM + ((mask >> 1) & 1u);
+      const float dax = type == 1u ? r.dx : (type == 2u ? r.dy : r.dz);
+      const bool near_left = !(dax > 0.0f);  // reference pops left first when d[axis] > 0
+      // Children in the reference's pop order.
+      uint32_t slot[3];
+      uint32_t present[3];
+      slot[0] = near_left ? sR : sL;
+      present[0] = near_left ? (mask & 4u) : (mask & 1u);
+      slot[1] = sM;
+      present[1] = mask & 2u;
+      slot[2] = near_left ? sL : sR;
+      present[2] = near_left ? (mask & 1u) : (mask & 4u);
+      bool pass[3];
+      float lo[3];
+      uint32_t wa[3], wb[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        pass[k] = false;
+        if (present[k]) {
+          const float4 ca = __ldg(nodes + 2 * slot[k]);
+          const float4 cb = __ldg(nodes + 2 * slot[k] + 1);
+          pass[k] = node_visit(ca, cb, r, ix, iy, iz, tcull, lo[k]);
+          wa[k] = __float_as_uint(cb.z);
+          wb[k] = __float_as_uint(cb.w);
+        }
+      }
+      // Push the passing children after the first, last-visited first.
+      int first = pass[0] ? 0 : (pass[1] ? 1 : (pass[2] ? 2 : -1));
+      if (sp + 2 > CAP) {
+        atomicOr(status, 1u);
+        return false;
+      }
+#pragma unroll
+      for (int k = 2; k >= 1; --k) {
+        if (pass[k] && k != first) stack[sp++] = make_uint4(wa[k], wb[k], __float_as_uint(lo[k]), 0u);
+      }
+      if (first < 0) {
+        if (!pop(tcull)) return false;
+        continue;
+      }
+      cur_a = first == 0 ? wa[0] : (first == 1 ? wa[1] : wa[2]);
+      cur_b = first == 0 ? wb[0] : (first == 1 ? wb[1] : wb[2]);
+    }
+    return true;
+  }
+};
+
+template <int CAP>
+__global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB) k_closest_hit(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
                                                      const float4 *__restrict__ rays, int64_t n,
                                                      int4 *__restrict__ hits, unsigned *__restrict__ status) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const RayF r = load_ray(rays, i);
   const float ix = 1.0f / r.dx, iy = 1.0f / r.dy, iz = 1.0f / r.dz;
-
-  uint32_t stack[CAP];
-  int sp = 0;
-  stack[sp++] = 0;
 
   int best_slot = -1, best_prim = -1, best_tri = -1;
   float best_t = r.tmax, best_et = 0.0f;  // best_t +- best_et holds the reference's current tmax
@@ -196,33 +283,20 @@ __global__ void __launch_bounds__(128) k_closest_hit(const float4 *__restrict__ 
   float tcull = r.tmax;
   uint32_t flags = 0;
 
-  while (sp > 0) {
-    const uint32_t ni = stack[--sp];
-    const float4 na = __ldg(nodes + 2 * ni);
-    const float4 nb = __ldg(nodes + 2 * ni + 1);
-    if (!node_visit(na, nb, r, ix, iy, iz, tcull)) continue;
-    const uint32_t a = __float_as_uint(nb.z), b = __float_as_uint(nb.w);
-    const uint32_t type = b & 3u;
-    if (type != 0u) {
-      const uint32_t mask = (b >> 2) & 7u;
-      const uint32_t cL = a, cM = a + (mask & 1u), cR = cM + ((mask >> 1) & 1u);
-      const float dax = type == 1u ? r.dx : (type == 2u ? r.dy : r.dz);
-      if (sp + 3 > CAP) {
-        atomicOr(status, 1u);
-        break;
-      }
-      if (dax > 0.0f) {
-        if (mask & 4u) stack[sp++] = cR;
-        if (mask & 2u) stack[sp++] = cM;
-        if (mask & 1u) stack[sp++] = cL;
-      } else {
-        if (mask & 1u) stack[sp++] = cL;
-        if (mask & 2u) stack[sp++] = cM;
-        if (mask & 4u) stack[sp++] = cR;
-      }
-      continue;
-    }
-    const uint32_t cnt = b >> 8;
+  Traversal<CAP> tr;
+  tr.sp = 0;
+  bool alive;
+  {
+    const float4 na = __ldg(nodes), nb = __ldg(nodes + 1);
+    float lo;
+    alive = node_visit(na, nb, r, ix, iy, iz, tcull, lo);
+    tr.cur_a = __float_as_uint(nb.z);
+    tr.cur_b = __float_as_uint(nb.w);
+  }
+  while (alive) {
+    if (!tr.descend(nodes, r, ix, iy, iz, tcull, status)) break;
+    // Current node is a leaf: test its triangles in order.
+    const uint32_t a = tr.cur_a, cnt = tr.cur_b >> 8;
     for (uint32_t k = 0; k < cnt; ++k) {
       const uint32_t slot = a + k;
       float3 v0, v1, v2;
@@ -243,7 +317,6 @@ __global__ void __launch_bounds__(128) k_closest_hit(const float4 *__restrict__ 
           tcull = t + et;
           continue;
         }
-        res = kAmbiguous;  // too close to the current tmax to decide in float
       }
       // Exact re-test against the reference's exact current tmax.
       if (!have64) {
@@ -267,6 +340,21 @@ __global__ void __launch_bounds__(128) k_closest_hit(const float4 *__restrict__ 
         flags |= 1u;
       }
     }
+    alive = tr.pop(tcull);
+  }
+  // A float-decided hit whose t bound exceeds half the 1e-5 reporting
+  // tolerance (grazing incidence) gets its t from the exact test, once,
+  // after the traversal loop where the warp has reconverged.
+  if (best_slot >= 0 && !have64 && best_et > 5.0e-6f * fabsf(best_t)) {
+    float3 b0, b1, b2;
+    int bp, bt;
+    load_tri(tris, (uint32_t)best_slot, b0, b1, b2, bp, bt);
+    double tb;
+    if (tri_test64(r, b0, b1, b2, (double)r.tmin, 1.0e308, tb)) {
+      best_t64 = tb;
+      have64 = true;
+      flags |= 4u;
+    }
   }
   int4 h;
   if (best_slot >= 0) {
@@ -278,44 +366,26 @@ __global__ void __launch_bounds__(128) k_closest_hit(const float4 *__restrict__ 
 }
 
 template <int CAP>
-__global__ void __launch_bounds__(128) k_any_hit(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
+__global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB) k_any_hit(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
                                                  const float4 *__restrict__ rays, int64_t n,
                                                  uint8_t *__restrict__ occluded, unsigned *__restrict__ status) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const RayF r = load_ray(rays, i);
   const float ix = 1.0f / r.dx, iy = 1.0f / r.dy, iz = 1.0f / r.dz;
-  uint32_t stack[CAP];
-  int sp = 0;
-  stack[sp++] = 0;
-  bool hit = false;
-  while (sp > 0 && !hit) {
-    const uint32_t ni = stack[--sp];
-    const float4 na = __ldg(nodes + 2 * ni);
-    const float4 nb = __ldg(nodes + 2 * ni + 1);
-    if (!node_visit(na, nb, r, ix, iy, iz, r.tmax)) continue;
-    const uint32_t a = __float_as_uint(nb.z), b = __float_as_uint(nb.w);
-    const uint32_t type = b & 3u;
-    if (type != 0u) {
-      const uint32_t mask = (b >> 2) & 7u;
-      const uint32_t cL = a, cM = a + (mask & 1u), cR = cM + ((mask >> 1) & 1u);
-      const float dax = type == 1u ? r.dx : (type == 2u ? r.dy : r.dz);
-      if (sp + 3 > CAP) {
-        atomicOr(status, 1u);
-        break;
-      }
-      if (dax > 0.0f) {
-        if (mask & 4u) stack[sp++] = cR;
-        if (mask & 2u) stack[sp++] = cM;
-        if (mask & 1u) stack[sp++] = cL;
-      } else {
-        if (mask & 1u) stack[sp++] = cL;
-        if (mask & 2u) stack[sp++] = cM;
-        if (mask & 4u) stack[sp++] = cR;
-      }
-      continue;
-    }
-    const uint32_t cnt = b >> 8;
+  Traversal<CAP> tr;
+  tr.sp = 0;
+  bool alive, hit = false;
+  {
+    const float4 na = __ldg(nodes), nb = __ldg(nodes + 1);
+    float lo;
+    alive = node_visit(na, nb, r, ix, iy, iz, r.tmax, lo);
+    tr.cur_a = __float_as_uint(nb.z);
+    tr.cur_b = __float_as_uint(nb.w);
+  }
+  while (alive && !hit) {
+    if (!tr.descend(nodes, r, ix, iy, iz, r.tmax, status)) break;
+    const uint32_t a = tr.cur_a, cnt = tr.cur_b >> 8;
     for (uint32_t k = 0; k < cnt; ++k) {
       float3 v0, v1, v2;
       int prim, tri;
@@ -336,6 +406,7 @@ __global__ void __launch_bounds__(128) k_any_hit(const float4 *__restrict__ node
         break;
       }
     }
+    if (!hit) alive = tr.pop(r.tmax);
   }
   occluded[i] = hit ? 1 : 0;
 }
@@ -343,7 +414,7 @@ __global__ void __launch_bounds__(128) k_any_hit(const float4 *__restrict__ node
 template <int CAP>
 cudaError_t launch_pair(bool closest, const void *nodes, const void *tris, const void *rays, int64_t n, void *out,
                         unsigned *status, cudaStream_t stream) {
-  const int block = 128;
+  const int block = SKW_TRAV_BLOCK;
   const int64_t grid = (n + block - 1) / block;
   if (closest) {
     k_closest_hit<CAP><<<(unsigned)grid, block, 0, stream>>>((const float4 *)nodes, (const float4 *)tris,
