@@ -12,7 +12,9 @@ int traversal_stack_capacity(int max_depth);
 
 // closest = true: hits is skw_hit[n] (int4); false: out is uint8_t[n].
 // status: device word; bit 0 is set if a stack ever overflowed.
+// scene_abs: the largest absolute coordinate of any vertex in the tree (it
+// bounds the slab-test rounding error).
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
-                             int64_t n, void *out, unsigned *status, cudaStream_t stream);
+                             int64_t n, float scene_abs, void *out, unsigned *status, cudaStream_t stream);
 
 }  // namespace skw

@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <string>
@@ -24,6 +25,7 @@ struct skw_accel {
   DevTri *d_tris = nullptr;
   unsigned *d_status = nullptr;
   int stack_cap = 0;
+  float scene_abs = 0.0f;  // largest absolute vertex coordinate
   skw_accel_info info{};
   std::vector<DevNode> h_nodes;
   std::vector<DevTri> h_tris;
@@ -162,6 +164,8 @@ int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_acce
     return cuda_fail(ctx, e, "upload (accelerator)");
   }
   a->stack_cap = skw::traversal_stack_capacity(ft.max_depth);
+  for (int k = 0; k < 6; ++k)
+    if (std::isfinite(ft.bounds[k])) a->scene_abs = std::max(a->scene_abs, std::fabs(ft.bounds[k]));
   skw_accel_info &info = a->info;
   info.n_triangles = (int64_t)ft.tris.size();
   info.n_nodes = (int64_t)ft.nodes.size();
@@ -220,7 +224,7 @@ static int run_query(skw_accel *a, bool closest, const skw_ray *rays, int64_t n,
   if (n == 0) return SKW_OK;
   cudaError_t e = cudaSetDevice(a->ctx->device);
   if (e != cudaSuccess) return cuda_fail(a->ctx, e, "cudaSetDevice");
-  e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, out, a->d_status,
+  e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, a->scene_abs, out, a->d_status,
                             (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(a->ctx, e, closest ? "closest-hit launch" : "any-hit launch");
   a->ctx->launches.fetch_add(1);

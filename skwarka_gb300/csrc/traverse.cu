@@ -48,7 +48,7 @@ constexpr double kDblEps = 2.220446049250313e-16;
 #define SKW_TRAV_BLOCK 128
 #endif
 #ifndef SKW_TRAV_MINB
-#define SKW_TRAV_MINB 4
+#define SKW_TRAV_MINB 6
 #endif
 
 enum : int { kMiss = 0, kHit = 1, kAmbiguous = 2 };
@@ -156,272 +156,363 @@ __device__ __forceinline__ void load_tri(const float4 *__restrict__ tris, uint32
   tri = __float_as_int(b.w);
 }
 
-// Reference slab test (TriangleAccelerator.cpp:176-192) on a widened float
-// interval.  Returns true when the node must be visited; `lo` receives the
-// widened entry distance max(tnear_x, tnear_y, tnear_z, tmin), which is all
-// a later re-test against a smaller tmax needs.
-__device__ __forceinline__ bool node_visit(const float4 na, const float4 nb, const RayF &r, float ix, float iy,
-                                           float iz, float tcull, float &lo) {
-  float tn0 = (na.x - r.ox) * ix, tf0 = (na.w - r.ox) * ix;
-  float tn1 = (na.y - r.oy) * iy, tf1 = (nb.x - r.oy) * iy;
-  float tn2 = (na.z - r.oz) * iz, tf2 = (nb.y - r.oz) * iz;
-  const float a0 = fminf(tn0, tf0), b0 = fmaxf(tn0, tf0);
-  const float a1 = fminf(tn1, tf1), b1 = fmaxf(tn1, tf1);
-  const float a2 = fminf(tn2, tf2), b2 = fmaxf(tn2, tf2);
-  // NaN (0 * inf) slabs: fminf/fmaxf return the other operand, and the
-  // widened bounds below drop NaN, matching the reference's comparisons,
-  // which are all false on NaN.
-  const float l0 = fmaf(-kWiden, fabsf(a0), a0), h0 = fmaf(kWiden, fabsf(b0), b0);
-  const float l1 = fmaf(-kWiden, fabsf(a1), a1), h1 = fmaf(kWiden, fabsf(b1), b1);
-  const float l2 = fmaf(-kWiden, fabsf(a2), a2), h2 = fmaf(kWiden, fabsf(b2), b2);
-  lo = fmaxf(fmaxf(l0, l1), fmaxf(l2, r.tmin));
-  const float hi = fminf(fminf(h0, h1), fminf(h2, tcull));
+// Per-ray data for the slab test.  A plane distance is computed as
+// fma(coordinate, 1/d, offset) with the offset -o/d -+ w folded in, where the
+// per-axis widening w = 6u (B + |o|) |1/d| (u = 2^-24, B = largest absolute
+// coordinate in the scene) bounds the float result's distance from the exact
+// value for every node of the scene; the reference's double result is within
+// a far smaller distance of the exact one.  The near plane of each axis is
+// selected by the sign of 1/d, which is the reference's "swap if
+// tNear > tFar" for every non-NaN slab.
+struct SlabRay {
+  float ix, iy, iz;  // 1/d
+  float nx, ny, nz;  // near-plane offsets: -o/d - w
+  float fx, fy, fz;  // far-plane offsets:  -o/d + w
+  bool sx, sy, sz;   // 1/d < 0: the near plane is the box maximum
+};
+
+__device__ __forceinline__ SlabRay make_slab_ray(const RayF &r, float scene_abs) {
+  SlabRay s;
+  s.ix = 1.0f / r.dx;
+  s.iy = 1.0f / r.dy;
+  s.iz = 1.0f / r.dz;
+  const float c = 6.0f * 5.9604645e-8f;
+  const float wx = c * (scene_abs + fabsf(r.ox)) * fabsf(s.ix);
+  const float wy = c * (scene_abs + fabsf(r.oy)) * fabsf(s.iy);
+  const float wz = c * (scene_abs + fabsf(r.oz)) * fabsf(s.iz);
+  const float ox = -r.ox * s.ix, oy = -r.oy * s.iy, oz = -r.oz * s.iz;
+  s.nx = ox - wx;
+  s.ny = oy - wy;
+  s.nz = oz - wz;
+  s.fx = ox + wx;
+  s.fy = oy + wy;
+  s.fz = oz + wz;
+  s.sx = signbit(s.ix);
+  s.sy = signbit(s.iy);
+  s.sz = signbit(s.iz);
+  return s;
+}
+
+// The reference's slab test (TriangleAccelerator.cpp:176-192) on the widened
+// interval: true when the node must be visited.  `lo` receives the widened
+// entry distance max(tnear_x, tnear_y, tnear_z, tmin), all that a later
+// re-test against a smaller tmax needs.  fmaxf/fminf drop NaN operands
+// (0 * inf slabs), as the reference's comparisons are all false on NaN.
+__device__ __forceinline__ bool node_visit(const float4 na, const float4 nb, const SlabRay &s, float tmin,
+                                           float tcull, float &lo) {
+  const float tn0 = fmaf(s.sx ? na.w : na.x, s.ix, s.nx), tf0 = fmaf(s.sx ? na.x : na.w, s.ix, s.fx);
+  const float tn1 = fmaf(s.sy ? nb.x : na.y, s.iy, s.ny), tf1 = fmaf(s.sy ? na.y : nb.x, s.iy, s.fy);
+  const float tn2 = fmaf(s.sz ? nb.y : na.z, s.iz, s.nz), tf2 = fmaf(s.sz ? na.z : nb.y, s.iz, s.fz);
+  lo = fmaxf(fmaxf(tn0, tn1), fmaxf(tn2, tmin));
+  const float hi = fminf(fminf(tf0, tf1), fminf(tf2, tcull));
   return !(lo > hi);
 }
 
-// Per-thread traversal state shared by the closest-hit and any-hit kernels.
+#ifndef SKW_TRAV_SCAP
+#define SKW_TRAV_SCAP 16
+#endif
+#ifndef SKW_TRAV_REFILL
+#define SKW_TRAV_REFILL 8
+#endif
+
+// Traversal stack: the first SCAP entries of each thread live in shared
+// memory as three word arrays indexed [entry][thread] (so lanes never
+// conflict on a bank), deeper entries in local memory.  An entry holds a
+// node's words 6-7 and its widened entry distance.
+template <int CAP>
+struct Stack {
+  static constexpr int SCAP = CAP < SKW_TRAV_SCAP ? CAP : SKW_TRAV_SCAP;
+  uint32_t (*sa)[SKW_TRAV_BLOCK];
+  uint32_t (*sb)[SKW_TRAV_BLOCK];
+  float (*slo)[SKW_TRAV_BLOCK];
+  uint4 ovf[CAP - SCAP > 0 ? CAP - SCAP : 1];
+  int sp;
+
+  __device__ __forceinline__ void push(uint32_t a, uint32_t b, float lo) {
+    if (sp < SCAP) {
+      sa[sp][threadIdx.x] = a;
+      sb[sp][threadIdx.x] = b;
+      slo[sp][threadIdx.x] = lo;
+    } else {
+      ovf[sp - SCAP] = make_uint4(a, b, __float_as_uint(lo), 0u);
+    }
+    ++sp;
+  }
+  // Pops until an entry survives the re-cull against tcull (the reference
+  // culls the others when it pops them).
+  __device__ __forceinline__ bool pop(float tcull, uint32_t &a, uint32_t &b) {
+    while (sp > 0) {
+      --sp;
+      float lo;
+      if (sp < SCAP) {
+        lo = slo[sp][threadIdx.x];
+        a = sa[sp][threadIdx.x];
+        b = sb[sp][threadIdx.x];
+      } else {
+        const uint4 e = ovf[sp - SCAP];
+        a = e.x;
+        b = e.y;
+        lo = __uint_as_float(e.z);
+      }
+      if (!(lo > tcull)) return true;
+    }
+    return false;
+  }
+};
+
+// Expands internal nodes until (cur_a, cur_b) is a leaf; false when the
+// stack runs out.
 //
 // Visit order equals the reference's (TriangleAccelerator.cpp:170-211): the
 // reference pushes an internal node's children and pops the near-side one
 // first, testing each node's box when it is popped.  Here an internal node's
-// present children (contiguous, so their loads go out together) are box-tested
-// right away; the first passing one in the reference's pop order becomes the
-// current node and the rest are pushed so that they pop in that order.  A
-// pushed entry keeps its widened entry distance, and popping re-culls it
-// against the tmax of that moment -- the only part of the reference's
-// pop-time box test that can change after the push, since tmax only shrinks.
-struct StackEntry {
-  uint32_t a, b;  // the node's words 6 and 7
-  float lo;       // widened entry distance
-  uint32_t pad;
-};
-
+// present children (contiguous, so their loads go out together) are
+// box-tested right away; the first passing one in the reference's pop order
+// becomes the current node and the rest are pushed so that they pop in that
+// order.  A pushed entry keeps its widened entry distance and is re-culled on
+// pop against the tmax of that moment -- the only part of the reference's
+// pop-time test that can change after the push, since tmax only shrinks.
 template <int CAP>
-struct Traversal {
-  uint4 stack[CAP];
-  int sp;
-  uint32_t cur_a, cur_b;  // current node (passed its box test)
-
-  __device__ __forceinline__ bool pop(float tcull) {
-    while (sp > 0) {
-      const uint4 e = stack[--sp];
-      if (__uint_as_float(e.z) > tcull) continue;  // the reference culls it at pop
-      cur_a = e.x;
-      cur_b = e.y;
-      return true;
-    }
-    return false;
-  }
-
-  // Expands internal nodes until the current node is a leaf; false when the
-  // stack runs out.  status bit 0 records an (impossible by construction)
-  // stack overflow.
-  __device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const RayF &r, float ix, float iy,
-                                          float iz, float tcull, unsigned *status) {
-    while ((cur_b & 3u) != 0u) {
-      const uint32_t type = cur_b & 3u, mask = (cur_b >> 2) & 7u;
-      const uint32_t sL = cur_a, sM = cur_a + (mask & 1u), sR = sM + ((mask >> 1) & 1u);
-      const float dax = type == 1u ? r.dx : (type == 2u ? r.dy : r.dz);
-      const bool near_left = !(dax > 0.0f);  // reference pops left first when d[axis] > 0
-      // Children in the reference's pop order.
-      uint32_t slot[3];
-      uint32_t present[3];
-      slot[0] = near_left ? sR : sL;
-      present[0] = near_left ? (mask & 4u) : (mask & 1u);
-      slot[1] = sM;
-      present[1] = mask & 2u;
-      slot[2] = near_left ? sL : sR;
-      present[2] = near_left ? (mask & 1u) : (mask & 4u);
-      bool pass[3];
-      float lo[3];
-      uint32_t wa[3], wb[3];
+__device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const RayF &r, const SlabRay &s,
+                                        float tcull, Stack<CAP> &st, uint32_t &cur_a, uint32_t &cur_b,
+                                        unsigned *status) {
+  while ((cur_b & 3u) != 0u) {
+    const uint32_t type = cur_b & 3u, mask = (cur_b >> 2) & 7u;
+    const uint32_t sL = cur_a, sM = cur_a + (mask & 1u), sR = sM + ((mask >> 1) & 1u);
+    const float dax = type == 1u ? r.dx : (type == 2u ? r.dy : r.dz);
+    const bool near_right = !(dax > 0.0f);  // the reference pops left first when d[axis] > 0
+    uint32_t slot[3], present[3];
+    slot[0] = near_right ? sR : sL;
+    present[0] = near_right ? (mask & 4u) : (mask & 1u);
+    slot[1] = sM;
+    present[1] = mask & 2u;
+    slot[2] = near_right ? sL : sR;
+    present[2] = near_right ? (mask & 1u) : (mask & 4u);
+    bool pass[3];
+    float lo[3];
+    uint32_t wa[3], wb[3];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        pass[k] = false;
-        if (present[k]) {
-          const float4 ca = __ldg(nodes + 2 * slot[k]);
-          const float4 cb = __ldg(nodes + 2 * slot[k] + 1);
-          pass[k] = node_visit(ca, cb, r, ix, iy, iz, tcull, lo[k]);
-          wa[k] = __float_as_uint(cb.z);
-          wb[k] = __float_as_uint(cb.w);
-        }
+    for (int k = 0; k < 3; ++k) {
+      pass[k] = false;
+      wa[k] = wb[k] = 0u;
+      lo[k] = 0.0f;
+      if (present[k]) {
+        const float4 ca = __ldg(nodes + 2 * slot[k]);
+        const float4 cb = __ldg(nodes + 2 * slot[k] + 1);
+        pass[k] = node_visit(ca, cb, s, r.tmin, tcull, lo[k]);
+        wa[k] = __float_as_uint(cb.z);
+        wb[k] = __float_as_uint(cb.w);
       }
-      // Push the passing children after the first, last-visited first.
-      int first = pass[0] ? 0 : (pass[1] ? 1 : (pass[2] ? 2 : -1));
-      if (sp + 2 > CAP) {
-        atomicOr(status, 1u);
-        return false;
-      }
-#pragma unroll
-      for (int k = 2; k >= 1; --k) {
-        if (pass[k] && k != first) stack[sp++] = make_uint4(wa[k], wb[k], __float_as_uint(lo[k]), 0u);
-      }
-      if (first < 0) {
-        if (!pop(tcull)) return false;
-        continue;
-      }
-      cur_a = first == 0 ? wa[0] : (first == 1 ? wa[1] : wa[2]);
-      cur_b = first == 0 ? wb[0] : (first == 1 ? wb[1] : wb[2]);
     }
-    return true;
+    const int first = pass[0] ? 0 : (pass[1] ? 1 : (pass[2] ? 2 : -1));
+    if (st.sp + 2 > CAP) {
+      atomicOr(status, 1u);
+      return false;
+    }
+    if (pass[2] && first != 2) st.push(wa[2], wb[2], lo[2]);
+    if (pass[1] && first != 1) st.push(wa[1], wb[1], lo[1]);
+    if (first < 0) {
+      if (!st.pop(tcull, cur_a, cur_b)) return false;
+      continue;
+    }
+    cur_a = first == 0 ? wa[0] : (first == 1 ? wa[1] : wa[2]);
+    cur_b = first == 0 ? wb[0] : (first == 1 ? wb[1] : wb[2]);
   }
-};
+  return true;
+}
 
-template <int CAP>
-__global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB) k_closest_hit(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
-                                                     const float4 *__restrict__ rays, int64_t n,
-                                                     int4 *__restrict__ hits, unsigned *__restrict__ status) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const RayF r = load_ray(rays, i);
-  const float ix = 1.0f / r.dx, iy = 1.0f / r.dy, iz = 1.0f / r.dz;
+// Persistent traversal.  Each warp owns a contiguous chunk of rays; a lane
+// whose ray is finished takes the next ray of the chunk when at least
+// SKW_TRAV_REFILL lanes are idle (or all are), so lanes rarely idle while
+// long rays finish.  No global atomics, no cross-warp waits.
+template <int CAP, bool CLOSEST>
+__global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
+    k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, const float4 *__restrict__ rays,
+            int64_t n, int64_t chunk, float scene_abs, void *__restrict__ out, unsigned *__restrict__ status) {
+  constexpr int SCAP = Stack<CAP>::SCAP;
+  __shared__ uint32_t s_a[SCAP][SKW_TRAV_BLOCK];
+  __shared__ uint32_t s_b[SCAP][SKW_TRAV_BLOCK];
+  __shared__ float s_lo[SCAP][SKW_TRAV_BLOCK];
+  Stack<CAP> st;
+  st.sa = s_a;
+  st.sb = s_b;
+  st.slo = s_lo;
+  st.sp = 0;
 
-  int best_slot = -1, best_prim = -1, best_tri = -1;
-  float best_t = r.tmax, best_et = 0.0f;  // best_t +- best_et holds the reference's current tmax
-  double best_t64 = (double)r.tmax;
-  bool have64 = true;  // best_t64 is the reference's exact current tmax
-  float tcull = r.tmax;
+  const unsigned lane = threadIdx.x & 31u;
+  const int64_t warp = ((int64_t)blockIdx.x * SKW_TRAV_BLOCK + threadIdx.x) >> 5;
+  int64_t next = warp * chunk;
+  const int64_t end = min(next + chunk, n);
+
+  int64_t ray_i = -1;
+  RayF r{};
+  SlabRay s{};
+  uint32_t cur_a = 0, cur_b = 0;
+  // closest-hit state: best_t +- best_et holds the reference's current tmax
+  int best_slot = -1;
+  float best_t = 0.0f, best_et = 0.0f, tcull = 0.0f;
+  double best_t64 = 0.0;
+  bool have64 = true;
   uint32_t flags = 0;
 
-  Traversal<CAP> tr;
-  tr.sp = 0;
-  bool alive;
-  {
-    const float4 na = __ldg(nodes), nb = __ldg(nodes + 1);
-    float lo;
-    alive = node_visit(na, nb, r, ix, iy, iz, tcull, lo);
-    tr.cur_a = __float_as_uint(nb.z);
-    tr.cur_b = __float_as_uint(nb.w);
-  }
-  while (alive) {
-    if (!tr.descend(nodes, r, ix, iy, iz, tcull, status)) break;
-    // Current node is a leaf: test its triangles in order.
-    const uint32_t a = tr.cur_a, cnt = tr.cur_b >> 8;
-    for (uint32_t k = 0; k < cnt; ++k) {
-      const uint32_t slot = a + k;
-      float3 v0, v1, v2;
-      int prim, tri;
-      load_tri(tris, slot, v0, v1, v2, prim, tri);
-      float t, et;
-      int res = tri_test32(r, v0, v1, v2, t, et);
-      if (res == kMiss) continue;
-      if (res == kHit) {
-        if (t - et > best_t + best_et) continue;  // certainly beyond the current tmax
-        if (t + et < best_t - best_et) {          // certainly nearer: accept in float
-          best_slot = (int)slot;
-          best_prim = prim;
-          best_tri = tri;
-          best_t = t;
-          best_et = et;
-          have64 = false;
-          tcull = t + et;
-          continue;
-        }
-      }
-      // Exact re-test against the reference's exact current tmax.
-      if (!have64) {
-        float3 b0, b1, b2;
-        int bp, bt;
-        load_tri(tris, (uint32_t)best_slot, b0, b1, b2, bp, bt);
-        double tb;
-        best_t64 = tri_test64(r, b0, b1, b2, (double)r.tmin, 1.0e308, tb) ? tb : (double)best_t;
+  while (true) {
+    const unsigned idle = __ballot_sync(0xffffffffu, ray_i < 0);
+    if (idle != 0u && next < end && (__popc(idle) >= SKW_TRAV_REFILL || idle == 0xffffffffu)) {
+      const int64_t mine = next + __popc(idle & ((1u << lane) - 1u));
+      next += __popc(idle);
+      if (ray_i < 0 && mine < end) {
+        ray_i = mine;
+        r = load_ray(rays, ray_i);
+        s = make_slab_ray(r, scene_abs);
+        best_slot = -1;
+        best_t = r.tmax;
+        best_et = 0.0f;
+        best_t64 = (double)r.tmax;
         have64 = true;
-      }
-      double t64;
-      if (tri_test64(r, v0, v1, v2, (double)r.tmin, best_t64, t64)) {
-        if (best_slot >= 0 && fabs(t64 - best_t64) <= 1e-12 * fabs(t64)) flags |= 2u;
-        best_slot = (int)slot;
-        best_prim = prim;
-        best_tri = tri;
-        best_t64 = t64;
-        best_t = (float)t64;
-        best_et = fabsf(best_t) * 1.2e-7f;
-        tcull = __double2float_ru(t64);
-        flags |= 1u;
-      }
-    }
-    alive = tr.pop(tcull);
-  }
-  // A float-decided hit whose t bound exceeds half the 1e-5 reporting
-  // tolerance (grazing incidence) gets its t from the exact test, once,
-  // after the traversal loop where the warp has reconverged.
-  if (best_slot >= 0 && !have64 && best_et > 5.0e-6f * fabsf(best_t)) {
-    float3 b0, b1, b2;
-    int bp, bt;
-    load_tri(tris, (uint32_t)best_slot, b0, b1, b2, bp, bt);
-    double tb;
-    if (tri_test64(r, b0, b1, b2, (double)r.tmin, 1.0e308, tb)) {
-      best_t64 = tb;
-      have64 = true;
-      flags |= 4u;
-    }
-  }
-  int4 h;
-  if (best_slot >= 0) {
-    h = make_int4(__float_as_int(have64 ? (float)best_t64 : best_t), best_prim, best_tri, (int)flags);
-  } else {
-    h = make_int4(__float_as_int(__int_as_float(0x7f800000)), -1, -1, (int)flags);
-  }
-  hits[i] = h;
-}
-
-template <int CAP>
-__global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB) k_any_hit(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
-                                                 const float4 *__restrict__ rays, int64_t n,
-                                                 uint8_t *__restrict__ occluded, unsigned *__restrict__ status) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const RayF r = load_ray(rays, i);
-  const float ix = 1.0f / r.dx, iy = 1.0f / r.dy, iz = 1.0f / r.dz;
-  Traversal<CAP> tr;
-  tr.sp = 0;
-  bool alive, hit = false;
-  {
-    const float4 na = __ldg(nodes), nb = __ldg(nodes + 1);
-    float lo;
-    alive = node_visit(na, nb, r, ix, iy, iz, r.tmax, lo);
-    tr.cur_a = __float_as_uint(nb.z);
-    tr.cur_b = __float_as_uint(nb.w);
-  }
-  while (alive && !hit) {
-    if (!tr.descend(nodes, r, ix, iy, iz, r.tmax, status)) break;
-    const uint32_t a = tr.cur_a, cnt = tr.cur_b >> 8;
-    for (uint32_t k = 0; k < cnt; ++k) {
-      float3 v0, v1, v2;
-      int prim, tri;
-      load_tri(tris, a + k, v0, v1, v2, prim, tri);
-      float t, et;
-      int res = tri_test32(r, v0, v1, v2, t, et);
-      if (res == kMiss) continue;
-      if (res == kHit) {
-        if (t + et < r.tmax) {
-          hit = true;
-          break;
+        tcull = r.tmax;
+        flags = 0;
+        st.sp = 0;
+        const float4 na = __ldg(nodes), nb = __ldg(nodes + 1);
+        float lo;
+        cur_a = __float_as_uint(nb.z);
+        cur_b = __float_as_uint(nb.w);
+        if (!node_visit(na, nb, s, r.tmin, tcull, lo)) {  // root culled: a miss
+          if (CLOSEST) {
+            ((int4 *)out)[ray_i] = make_int4(0x7f800000, -1, -1, 0);
+          } else {
+            ((uint8_t *)out)[ray_i] = 0;
+          }
+          ray_i = -1;
         }
-        if (t - et > r.tmax) continue;
-      }
-      double t64;
-      if (tri_test64(r, v0, v1, v2, (double)r.tmin, (double)r.tmax, t64)) {
-        hit = true;
-        break;
       }
     }
-    if (!hit) alive = tr.pop(r.tmax);
+    if (__ballot_sync(0xffffffffu, ray_i >= 0) == 0u) {
+      if (next >= end) break;
+      continue;
+    }
+    if (ray_i < 0) continue;
+
+    bool done = !descend(nodes, r, s, tcull, st, cur_a, cur_b, status);
+    bool hit = false;
+    if (!done) {
+      // cur is a leaf: test its triangles in order.
+      const uint32_t a = cur_a, cnt = cur_b >> 8;
+      for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t slot = a + k;
+        float3 v0, v1, v2;
+        int prim, tri;
+        load_tri(tris, slot, v0, v1, v2, prim, tri);
+        float t, et;
+        int res = tri_test32(r, v0, v1, v2, t, et);
+        if (res == kMiss) continue;
+        if (CLOSEST) {
+          if (res == kHit) {
+            if (t - et > best_t + best_et) continue;  // certainly beyond the current tmax
+            if (t + et < best_t - best_et) {          // certainly nearer: accept in float
+              best_slot = (int)slot;
+              best_t = t;
+              best_et = et;
+              have64 = false;
+              tcull = t + et;
+              continue;
+            }
+          }
+          // Exact re-test against the reference's exact current tmax.
+          if (!have64) {
+            float3 b0, b1, b2;
+            int bp, bt;
+            load_tri(tris, (uint32_t)best_slot, b0, b1, b2, bp, bt);
+            double tb;
+            best_t64 = tri_test64(r, b0, b1, b2, (double)r.tmin, 1.0e308, tb) ? tb : (double)best_t;
+            have64 = true;
+          }
+          double t64;
+          if (tri_test64(r, v0, v1, v2, (double)r.tmin, best_t64, t64)) {
+            if (best_slot >= 0 && fabs(t64 - best_t64) <= 1e-12 * fabs(t64)) flags |= 2u;
+            best_slot = (int)slot;
+            best_t64 = t64;
+            best_t = (float)t64;
+            best_et = fabsf(best_t) * 1.2e-7f;
+            tcull = __double2float_ru(t64);
+            flags |= 1u;
+          }
+        } else {
+          if (res == kHit) {
+            if (t + et < r.tmax) {
+              hit = true;
+              break;
+            }
+            if (t - et > r.tmax) continue;
+          }
+          double t64;
+          if (tri_test64(r, v0, v1, v2, (double)r.tmin, (double)r.tmax, t64)) {
+            hit = true;
+            break;
+          }
+        }
+      }
+      done = hit || !st.pop(CLOSEST ? tcull : r.tmax, cur_a, cur_b);
+    }
+    if (done) {
+      if (CLOSEST) {
+        int4 h = make_int4(0x7f800000, -1, -1, (int)flags);
+        if (best_slot >= 0) {
+          const float4 ta = __ldg(tris + 3 * best_slot), tb = __ldg(tris + 3 * best_slot + 1);
+          // A float-decided hit whose t bound exceeds half the 1e-5
+          // reporting tolerance (grazing incidence) takes t from the
+          // exact test.
+          if (!have64 && best_et > 5.0e-6f * fabsf(best_t)) {
+            const float4 tc = __ldg(tris + 3 * best_slot + 2);
+            double tx;
+            if (tri_test64(r, make_float3(ta.x, ta.y, ta.z), make_float3(tb.x, tb.y, tb.z),
+                           make_float3(tc.x, tc.y, tc.z), (double)r.tmin, 1.0e308, tx)) {
+              best_t64 = tx;
+              have64 = true;
+              flags |= 4u;
+            }
+          }
+          h = make_int4(__float_as_int(have64 ? (float)best_t64 : best_t), __float_as_int(ta.w),
+                        __float_as_int(tb.w), (int)flags);
+        }
+        ((int4 *)out)[ray_i] = h;
+      } else {
+        ((uint8_t *)out)[ray_i] = hit ? 1 : 0;
+      }
+      ray_i = -1;
+    }
   }
-  occluded[i] = hit ? 1 : 0;
 }
 
 template <int CAP>
-cudaError_t launch_pair(bool closest, const void *nodes, const void *tris, const void *rays, int64_t n, void *out,
-                        unsigned *status, cudaStream_t stream) {
-  const int block = SKW_TRAV_BLOCK;
-  const int64_t grid = (n + block - 1) / block;
+cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const void *rays, int64_t n,
+                       float scene_abs, void *out, unsigned *status, cudaStream_t stream) {
+  static int blocks_per_sm[2] = {0, 0}, sms = 0;
+  const int which = closest ? 1 : 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  if (blocks_per_sm[which] == 0) {
+    cudaError_t e = closest ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[1], k_trace<CAP, true>,
+                                                                          SKW_TRAV_BLOCK, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[0], k_trace<CAP, false>,
+                                                                          SKW_TRAV_BLOCK, 0);
+    if (e != cudaSuccess) return e;
+    if (blocks_per_sm[which] < 1) blocks_per_sm[which] = 1;
+  }
+  const int64_t warps_per_block = SKW_TRAV_BLOCK / 32;
+  int64_t blocks = (int64_t)blocks_per_sm[which] * sms;
+  const int64_t needed = (n + 32 * warps_per_block - 1) / (32 * warps_per_block);
+  if (blocks > needed) blocks = needed;
+  const int64_t warps = blocks * warps_per_block;
+  const int64_t chunk = (n + warps - 1) / warps;
   if (closest) {
-    k_closest_hit<CAP><<<(unsigned)grid, block, 0, stream>>>((const float4 *)nodes, (const float4 *)tris,
-                                                            (const float4 *)rays, n, (int4 *)out, status);
+    k_trace<CAP, true><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
+        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, n, chunk, scene_abs, out, status);
   } else {
-    k_any_hit<CAP><<<(unsigned)grid, block, 0, stream>>>((const float4 *)nodes, (const float4 *)tris,
-                                                        (const float4 *)rays, n, (uint8_t *)out, status);
+    k_trace<CAP, false><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
+        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, n, chunk, scene_abs, out, status);
   }
   return cudaGetLastError();
 }
@@ -437,17 +528,17 @@ int traversal_stack_capacity(int max_depth) {
 }
 
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
-                             int64_t n, void *out, unsigned *status, cudaStream_t stream) {
+                             int64_t n, float scene_abs, void *out, unsigned *status, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   switch (stack_cap) {
     case 48:
-      return launch_pair<48>(closest, nodes, tris, rays, n, out, status, stream);
+      return launch_cap<48>(closest, nodes, tris, rays, n, scene_abs, out, status, stream);
     case 96:
-      return launch_pair<96>(closest, nodes, tris, rays, n, out, status, stream);
+      return launch_cap<96>(closest, nodes, tris, rays, n, scene_abs, out, status, stream);
     case 192:
-      return launch_pair<192>(closest, nodes, tris, rays, n, out, status, stream);
+      return launch_cap<192>(closest, nodes, tris, rays, n, scene_abs, out, status, stream);
     default:
-      return launch_pair<416>(closest, nodes, tris, rays, n, out, status, stream);
+      return launch_cap<416>(closest, nodes, tris, rays, n, scene_abs, out, status, stream);
   }
 }
 
