@@ -43,6 +43,22 @@ int cuda_fail(skw_ctx *ctx, cudaError_t e, const char *what) {
               std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+cudaError_t ctx_pool(skw_ctx *ctx, cudaMemPool_t *pool) {
+  if (!ctx->pool) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = ctx->device;
+    cudaError_t e = cudaMemPoolCreate(&ctx->pool, &props);
+    if (e != cudaSuccess) return e;
+    uint64_t keep = UINT64_MAX;
+    e = cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess) return e;
+  }
+  *pool = ctx->pool;
+  return cudaSuccess;
+}
+
 }  // namespace skw
 
 using skw::cuda_fail;
@@ -64,11 +80,16 @@ int skw_ctx_create(int device, skw_ctx **out) {
   auto *ctx = new (std::nothrow) skw_ctx();
   if (!ctx) return SKW_ERR_OOM;
   ctx->device = device;
+  cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
   *out = ctx;
   return SKW_OK;
 }
 
-void skw_ctx_destroy(skw_ctx *ctx) { delete ctx; }
+void skw_ctx_destroy(skw_ctx *ctx) {
+  if (!ctx) return;
+  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+  delete ctx;
+}
 
 const char *skw_last_error(const skw_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
@@ -220,14 +241,32 @@ int skw_accel_export(const skw_accel *a, uint32_t *nodes, int32_t *tri_prim, int
 static int run_query(skw_accel *a, bool closest, const skw_ray *rays, int64_t n, void *out, void *stream) {
   if (!a) return SKW_ERR_ARG;
   if (n < 0 || (n > 0 && (!rays || !out))) return fail(a->ctx, SKW_ERR_ARG, "bad ray buffer");
-  if (n > ((int64_t)1 << 31) * 128) return fail(a->ctx, SKW_ERR_ARG, "too many rays for one launch");
+  if (n > (int64_t)INT32_MAX) return fail(a->ctx, SKW_ERR_ARG, "too many rays for one call (max 2^31-1)");
   if (n == 0) return SKW_OK;
-  cudaError_t e = cudaSetDevice(a->ctx->device);
-  if (e != cudaSuccess) return cuda_fail(a->ctx, e, "cudaSetDevice");
-  e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, a->scene_abs, out, a->d_status,
-                            (cudaStream_t)stream);
-  if (e != cudaSuccess) return cuda_fail(a->ctx, e, closest ? "closest-hit launch" : "any-hit launch");
-  a->ctx->launches.fetch_add(1);
+  skw_ctx *ctx = a->ctx;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  cudaStream_t s = (cudaStream_t)stream;
+  const void *trace_rays = rays;
+  const int32_t *index = nullptr;
+  void *ws = nullptr;
+  int launches = 0;
+  if (n >= SKW_RAY_SORT_MIN && a->info.n_triangles > 0) {
+    cudaMemPool_t pool;
+    if ((e = skw::ctx_pool(ctx, &pool)) != cudaSuccess) return cuda_fail(ctx, e, "workspace pool");
+    if ((e = cudaMallocFromPoolAsync(&ws, skw::ray_sort_workspace_bytes(n), pool, s)) != cudaSuccess)
+      return cuda_fail(ctx, e, "workspace allocation");
+    e = skw::launch_ray_sort(rays, n, a->info.bounds, ws, &trace_rays, &index, ctx->sms, s, &launches);
+    if (e != cudaSuccess) {
+      cudaFreeAsync(ws, s);
+      return cuda_fail(ctx, e, "ray binning launch");
+    }
+  }
+  e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, trace_rays, n, a->scene_abs, index, out,
+                            a->d_status, s);
+  if (ws) cudaFreeAsync(ws, s);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, closest ? "closest-hit launch" : "any-hit launch");
+  ctx->launches.fetch_add(launches + 1);
   return SKW_OK;
 }
 

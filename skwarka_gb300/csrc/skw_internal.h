@@ -9,8 +9,12 @@
 
 struct skw_ctx {
   int device = 0;
+  int sms = 0;
   std::string err;
   std::atomic<int64_t> launches{0};
+  // Stream-ordered pool for per-call workspaces; it keeps freed memory
+  // (release threshold = max) so repeated calls do not remap.
+  cudaMemPool_t pool = nullptr;
 };
 
 namespace skw {
@@ -19,5 +23,7 @@ namespace skw {
 int fail(skw_ctx *ctx, int code, const std::string &msg);
 // Maps a CUDA error to SKW_ERR_OOM / SKW_ERR_CUDA with a message.
 int cuda_fail(skw_ctx *ctx, cudaError_t e, const char *what);
+// Creates the context's workspace pool on first use.
+cudaError_t ctx_pool(skw_ctx *ctx, cudaMemPool_t *pool);
 
 }  // namespace skw

@@ -57,9 +57,11 @@ struct RayF {
   float ox, oy, oz, dx, dy, dz, tmin, tmax;
 };
 
+// Rays and results stream through once: loaded and stored with the
+// evict-first policy so that they do not push the tree out of L2.
 __device__ __forceinline__ RayF load_ray(const float4 *__restrict__ rays, int64_t i) {
-  const float4 a = __ldg(rays + 2 * i);
-  const float4 b = __ldg(rays + 2 * i + 1);
+  const float4 a = __ldcs(rays + 2 * i);
+  const float4 b = __ldcs(rays + 2 * i + 1);
   return RayF{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 }
 
@@ -328,7 +330,8 @@ __device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const 
 template <int CAP, bool CLOSEST>
 __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, const float4 *__restrict__ rays,
-            int64_t n, int64_t chunk, float scene_abs, void *__restrict__ out, unsigned *__restrict__ status) {
+            int64_t n, int64_t chunk, float scene_abs, const int32_t *__restrict__ out_index, void *__restrict__ out,
+            unsigned *__restrict__ status) {
   constexpr int SCAP = Stack<CAP>::SCAP;
   __shared__ uint32_t s_a[SCAP][SKW_TRAV_BLOCK];
   __shared__ uint32_t s_b[SCAP][SKW_TRAV_BLOCK];
@@ -377,10 +380,11 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
         cur_a = __float_as_uint(nb.z);
         cur_b = __float_as_uint(nb.w);
         if (!node_visit(na, nb, s, r.tmin, tcull, lo)) {  // root culled: a miss
+          const int64_t o = out_index ? (int64_t)__ldcs(out_index + ray_i) : ray_i;
           if (CLOSEST) {
-            ((int4 *)out)[ray_i] = make_int4(0x7f800000, -1, -1, 0);
+            __stcs((int4 *)out + o, make_int4(0x7f800000, -1, -1, 0));
           } else {
-            ((uint8_t *)out)[ray_i] = 0;
+            ((uint8_t *)out)[o] = 0;
           }
           ray_i = -1;
         }
@@ -454,6 +458,7 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
       done = hit || !st.pop(CLOSEST ? tcull : r.tmax, cur_a, cur_b);
     }
     if (done) {
+      const int64_t o = out_index ? (int64_t)__ldcs(out_index + ray_i) : ray_i;
       if (CLOSEST) {
         int4 h = make_int4(0x7f800000, -1, -1, (int)flags);
         if (best_slot >= 0) {
@@ -474,9 +479,9 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
           h = make_int4(__float_as_int(have64 ? (float)best_t64 : best_t), __float_as_int(ta.w),
                         __float_as_int(tb.w), (int)flags);
         }
-        ((int4 *)out)[ray_i] = h;
+        __stcs((int4 *)out + o, h);
       } else {
-        ((uint8_t *)out)[ray_i] = hit ? 1 : 0;
+        ((uint8_t *)out)[o] = hit ? 1 : 0;
       }
       ray_i = -1;
     }
@@ -485,7 +490,7 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
 
 template <int CAP>
 cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const void *rays, int64_t n,
-                       float scene_abs, void *out, unsigned *status, cudaStream_t stream) {
+                       float scene_abs, const int32_t *out_index, void *out, unsigned *status, cudaStream_t stream) {
   static int blocks_per_sm[2] = {0, 0}, sms = 0;
   const int which = closest ? 1 : 0;
   if (sms == 0) {
@@ -509,10 +514,10 @@ cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const 
   const int64_t chunk = (n + warps - 1) / warps;
   if (closest) {
     k_trace<CAP, true><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
-        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, n, chunk, scene_abs, out, status);
+        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, n, chunk, scene_abs, out_index, out, status);
   } else {
     k_trace<CAP, false><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
-        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, n, chunk, scene_abs, out, status);
+        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, n, chunk, scene_abs, out_index, out, status);
   }
   return cudaGetLastError();
 }
@@ -528,17 +533,18 @@ int traversal_stack_capacity(int max_depth) {
 }
 
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
-                             int64_t n, float scene_abs, void *out, unsigned *status, cudaStream_t stream) {
+                             int64_t n, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
+                             cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   switch (stack_cap) {
     case 48:
-      return launch_cap<48>(closest, nodes, tris, rays, n, scene_abs, out, status, stream);
+      return launch_cap<48>(closest, nodes, tris, rays, n, scene_abs, out_index, out, status, stream);
     case 96:
-      return launch_cap<96>(closest, nodes, tris, rays, n, scene_abs, out, status, stream);
+      return launch_cap<96>(closest, nodes, tris, rays, n, scene_abs, out_index, out, status, stream);
     case 192:
-      return launch_cap<192>(closest, nodes, tris, rays, n, scene_abs, out, status, stream);
+      return launch_cap<192>(closest, nodes, tris, rays, n, scene_abs, out_index, out, status, stream);
     default:
-      return launch_cap<416>(closest, nodes, tris, rays, n, scene_abs, out, status, stream);
+      return launch_cap<416>(closest, nodes, tris, rays, n, scene_abs, out_index, out, status, stream);
   }
 }
 
