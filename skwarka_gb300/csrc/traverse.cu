@@ -57,11 +57,23 @@ struct RayF {
   float ox, oy, oz, dx, dy, dz, tmin, tmax;
 };
 
-// Rays and results stream through once: loaded and stored with the
-// evict-first policy so that they do not push the tree out of L2.
+// Rays and results stream through once: with SKW_TRAV_STREAMING they are
+// loaded and stored with the evict-first policy so that they do not push the
+// tree out of L2.
+#ifndef SKW_TRAV_STREAMING
+#define SKW_TRAV_STREAMING 1
+#endif
+#if SKW_TRAV_STREAMING
+#define SKW_LD_STREAM(p) __ldcs(p)
+#define SKW_ST_STREAM(p, v) __stcs(p, v)
+#else
+#define SKW_LD_STREAM(p) __ldg(p)
+#define SKW_ST_STREAM(p, v) (*(p) = (v))
+#endif
+
 __device__ __forceinline__ RayF load_ray(const float4 *__restrict__ rays, int64_t i) {
-  const float4 a = __ldcs(rays + 2 * i);
-  const float4 b = __ldcs(rays + 2 * i + 1);
+  const float4 a = SKW_LD_STREAM(rays + 2 * i);
+  const float4 b = SKW_LD_STREAM(rays + 2 * i + 1);
   return RayF{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 }
 
@@ -323,14 +335,43 @@ __device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const 
   return true;
 }
 
-// Persistent traversal.  Each warp owns a contiguous chunk of rays; a lane
-// whose ray is finished takes the next ray of the chunk when at least
-// SKW_TRAV_REFILL lanes are idle (or all are), so lanes rarely idle while
-// long rays finish.  No global atomics, no cross-warp waits.
+// Exact double-precision t of the hit on slot `slot` (its barycentric tests
+// are known to pass).
+__device__ __noinline__ double exact_t(const float4 *__restrict__ tris, const RayF &r, int slot, float fallback) {
+  const float4 a = __ldg(tris + 3 * slot), b = __ldg(tris + 3 * slot + 1), c = __ldg(tris + 3 * slot + 2);
+  double t;
+  return tri_test64(r, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z),
+                    (double)r.tmin, 1.0e308, t)
+             ? t
+             : (double)fallback;
+}
+
+template <bool CLOSEST>
+__device__ __forceinline__ void store_result(void *__restrict__ out, const int32_t *__restrict__ out_index, int ray_i,
+                                             int4 h, bool hit) {
+  const int o = out_index ? SKW_LD_STREAM(out_index + ray_i) : ray_i;
+  if (CLOSEST) {
+    SKW_ST_STREAM((int4 *)out + o, h);
+  } else {
+    ((uint8_t *)out)[o] = hit ? 1 : 0;
+  }
+}
+
+// Persistent traversal.  The rays form groups of 32 consecutive rays; warp w
+// of W owns groups w, w + W, w + 2W, ... (interleaved, so that every warp
+// gets a representative mix even when the rays were binned by coherence).  A
+// lane whose ray is finished takes the next ray of the warp's sequence when
+// at least SKW_TRAV_REFILL lanes are idle (or all are), so lanes rarely idle
+// while long rays finish.  No global atomics, no cross-warp waits.
+//
+// Closest-hit state is kept small: the slot of the current best hit and a
+// float interval [lo_t, hi_t] that contains the reference's current tmax
+// (the best hit's double t).  Where a decision needs that tmax exactly, it is
+// recomputed from the slot with the exact test.
 template <int CAP, bool CLOSEST>
 __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, const float4 *__restrict__ rays,
-            int64_t n, int64_t chunk, float scene_abs, const int32_t *__restrict__ out_index, void *__restrict__ out,
+            int n, float scene_abs, const int32_t *__restrict__ out_index, void *__restrict__ out,
             unsigned *__restrict__ status) {
   constexpr int SCAP = Stack<CAP>::SCAP;
   __shared__ uint32_t s_a[SCAP][SKW_TRAV_BLOCK];
@@ -343,49 +384,40 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
   st.sp = 0;
 
   const unsigned lane = threadIdx.x & 31u;
-  const int64_t warp = ((int64_t)blockIdx.x * SKW_TRAV_BLOCK + threadIdx.x) >> 5;
-  int64_t next = warp * chunk;
-  const int64_t end = min(next + chunk, n);
+  const int warp = (int)((blockIdx.x * (unsigned)SKW_TRAV_BLOCK + threadIdx.x) >> 5);
+  const int n_warps = (int)(gridDim.x * (unsigned)(SKW_TRAV_BLOCK / 32));
+  const int groups = (n + 31) >> 5;
+  int next = 0;  // position in this warp's ray sequence
+  const int end = warp < groups ? ((groups - warp + n_warps - 1) / n_warps) << 5 : 0;
 
-  int64_t ray_i = -1;
+  int ray_i = -1;
   RayF r{};
   SlabRay s{};
   uint32_t cur_a = 0, cur_b = 0;
-  // closest-hit state: best_t +- best_et holds the reference's current tmax
   int best_slot = -1;
-  float best_t = 0.0f, best_et = 0.0f, tcull = 0.0f;
-  double best_t64 = 0.0;
-  bool have64 = true;
-  uint32_t flags = 0;
+  float lo_t = 0.0f, hi_t = 0.0f;  // bracket of the reference's current tmax
+  uint32_t flags = 0;              // SKW_HIT_* bits; bit 3: [lo_t, hi_t] brackets an exact double
 
   while (true) {
     const unsigned idle = __ballot_sync(0xffffffffu, ray_i < 0);
     if (idle != 0u && next < end && (__popc(idle) >= SKW_TRAV_REFILL || idle == 0xffffffffu)) {
-      const int64_t mine = next + __popc(idle & ((1u << lane) - 1u));
+      const int mine = next + __popc(idle & ((1u << lane) - 1u));
       next += __popc(idle);
-      if (ray_i < 0 && mine < end) {
-        ray_i = mine;
+      const int idx = ((warp + (mine >> 5) * n_warps) << 5) + (mine & 31);
+      if (ray_i < 0 && mine < end && idx < n) {
+        ray_i = idx;
         r = load_ray(rays, ray_i);
         s = make_slab_ray(r, scene_abs);
         best_slot = -1;
-        best_t = r.tmax;
-        best_et = 0.0f;
-        best_t64 = (double)r.tmax;
-        have64 = true;
-        tcull = r.tmax;
-        flags = 0;
+        lo_t = hi_t = r.tmax;
+        flags = 8u;
         st.sp = 0;
         const float4 na = __ldg(nodes), nb = __ldg(nodes + 1);
         float lo;
         cur_a = __float_as_uint(nb.z);
         cur_b = __float_as_uint(nb.w);
-        if (!node_visit(na, nb, s, r.tmin, tcull, lo)) {  // root culled: a miss
-          const int64_t o = out_index ? (int64_t)__ldcs(out_index + ray_i) : ray_i;
-          if (CLOSEST) {
-            __stcs((int4 *)out + o, make_int4(0x7f800000, -1, -1, 0));
-          } else {
-            ((uint8_t *)out)[o] = 0;
-          }
+        if (!node_visit(na, nb, s, r.tmin, r.tmax, lo)) {  // root culled: a miss
+          store_result<CLOSEST>(out, out_index, ray_i, make_int4(0x7f800000, -1, -1, 0), false);
           ray_i = -1;
         }
       }
@@ -396,49 +428,40 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     }
     if (ray_i < 0) continue;
 
+    const float tcull = CLOSEST ? hi_t : r.tmax;
     bool done = !descend(nodes, r, s, tcull, st, cur_a, cur_b, status);
     bool hit = false;
     if (!done) {
       // cur is a leaf: test its triangles in order.
       const uint32_t a = cur_a, cnt = cur_b >> 8;
       for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t slot = a + k;
+        const int slot = (int)(a + k);
         float3 v0, v1, v2;
         int prim, tri;
-        load_tri(tris, slot, v0, v1, v2, prim, tri);
+        load_tri(tris, (uint32_t)slot, v0, v1, v2, prim, tri);
         float t, et;
         int res = tri_test32(r, v0, v1, v2, t, et);
         if (res == kMiss) continue;
         if (CLOSEST) {
           if (res == kHit) {
-            if (t - et > best_t + best_et) continue;  // certainly beyond the current tmax
-            if (t + et < best_t - best_et) {          // certainly nearer: accept in float
-              best_slot = (int)slot;
-              best_t = t;
-              best_et = et;
-              have64 = false;
-              tcull = t + et;
+            if (__fsub_rd(t, et) > hi_t) continue;  // certainly beyond the current tmax
+            if (__fadd_ru(t, et) < lo_t) {          // certainly nearer: accept in float
+              best_slot = slot;
+              lo_t = __fsub_rd(t, et);
+              hi_t = __fadd_ru(t, et);
+              flags &= ~8u;
               continue;
             }
           }
           // Exact re-test against the reference's exact current tmax.
-          if (!have64) {
-            float3 b0, b1, b2;
-            int bp, bt;
-            load_tri(tris, (uint32_t)best_slot, b0, b1, b2, bp, bt);
-            double tb;
-            best_t64 = tri_test64(r, b0, b1, b2, (double)r.tmin, 1.0e308, tb) ? tb : (double)best_t;
-            have64 = true;
-          }
+          const double cur_max = best_slot < 0 ? (double)r.tmax : exact_t(tris, r, best_slot, hi_t);
           double t64;
-          if (tri_test64(r, v0, v1, v2, (double)r.tmin, best_t64, t64)) {
-            if (best_slot >= 0 && fabs(t64 - best_t64) <= 1e-12 * fabs(t64)) flags |= 2u;
-            best_slot = (int)slot;
-            best_t64 = t64;
-            best_t = (float)t64;
-            best_et = fabsf(best_t) * 1.2e-7f;
-            tcull = __double2float_ru(t64);
-            flags |= 1u;
+          if (tri_test64(r, v0, v1, v2, (double)r.tmin, cur_max, t64)) {
+            if (best_slot >= 0 && fabs(t64 - cur_max) <= 1e-12 * fabs(t64)) flags |= 2u;
+            best_slot = slot;
+            lo_t = __double2float_rd(t64);
+            hi_t = __double2float_ru(t64);
+            flags |= 1u | 8u;
           }
         } else {
           if (res == kHit) {
@@ -455,34 +478,22 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
           }
         }
       }
-      done = hit || !st.pop(CLOSEST ? tcull : r.tmax, cur_a, cur_b);
+      done = hit || !st.pop(CLOSEST ? hi_t : r.tmax, cur_a, cur_b);
     }
     if (done) {
-      const int64_t o = out_index ? (int64_t)__ldcs(out_index + ray_i) : ray_i;
-      if (CLOSEST) {
-        int4 h = make_int4(0x7f800000, -1, -1, (int)flags);
-        if (best_slot >= 0) {
-          const float4 ta = __ldg(tris + 3 * best_slot), tb = __ldg(tris + 3 * best_slot + 1);
-          // A float-decided hit whose t bound exceeds half the 1e-5
-          // reporting tolerance (grazing incidence) takes t from the
-          // exact test.
-          if (!have64 && best_et > 5.0e-6f * fabsf(best_t)) {
-            const float4 tc = __ldg(tris + 3 * best_slot + 2);
-            double tx;
-            if (tri_test64(r, make_float3(ta.x, ta.y, ta.z), make_float3(tb.x, tb.y, tb.z),
-                           make_float3(tc.x, tc.y, tc.z), (double)r.tmin, 1.0e308, tx)) {
-              best_t64 = tx;
-              have64 = true;
-              flags |= 4u;
-            }
-          }
-          h = make_int4(__float_as_int(have64 ? (float)best_t64 : best_t), __float_as_int(ta.w),
-                        __float_as_int(tb.w), (int)flags);
+      int4 h = make_int4(0x7f800000, -1, -1, (int)(flags & 7u));
+      if (CLOSEST && best_slot >= 0) {
+        const float4 ta = __ldg(tris + 3 * best_slot), tb = __ldg(tris + 3 * best_slot + 1);
+        float tout = 0.5f * lo_t + 0.5f * hi_t;
+        // A float-decided hit whose bracket is wider than the 1e-5 reporting
+        // tolerance (grazing incidence) takes t from the exact test.
+        if (!(flags & 8u) && hi_t - lo_t > 1.0e-5f * fabsf(tout)) {
+          tout = (float)exact_t(tris, r, best_slot, tout);
+          flags |= 4u;
         }
-        __stcs((int4 *)out + o, h);
-      } else {
-        ((uint8_t *)out)[o] = hit ? 1 : 0;
+        h = make_int4(__float_as_int(tout), __float_as_int(ta.w), __float_as_int(tb.w), (int)(flags & 7u));
       }
+      store_result<CLOSEST>(out, out_index, ray_i, h, hit);
       ray_i = -1;
     }
   }
@@ -510,14 +521,12 @@ cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const 
   int64_t blocks = (int64_t)blocks_per_sm[which] * sms;
   const int64_t needed = (n + 32 * warps_per_block - 1) / (32 * warps_per_block);
   if (blocks > needed) blocks = needed;
-  const int64_t warps = blocks * warps_per_block;
-  const int64_t chunk = (n + warps - 1) / warps;
   if (closest) {
     k_trace<CAP, true><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
-        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, n, chunk, scene_abs, out_index, out, status);
+        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, scene_abs, out_index, out, status);
   } else {
     k_trace<CAP, false><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
-        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, n, chunk, scene_abs, out_index, out, status);
+        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, scene_abs, out_index, out, status);
   }
   return cudaGetLastError();
 }
