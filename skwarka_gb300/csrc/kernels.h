@@ -19,16 +19,6 @@ cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, con
                              int64_t n, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
                              cudaStream_t stream);
 
-// Ray binning (raysort.cu): bytes of workspace for n rays, and the launch
-// that fills it.  bounds: scene box (min xyz, max xyz).  On return
-// *sorted_out / *index_out point into the workspace.
-size_t ray_sort_workspace_bytes(int64_t n);
-cudaError_t launch_ray_sort(const void *rays, int64_t n, const float *bounds, void *workspace, const void **sorted_out,
-                            const int32_t **index_out, int sms, cudaStream_t stream, int *launches);
 
-// Rays per query at or above which the binning pre-pass runs.
-#ifndef SKW_RAY_SORT_MIN
-#define SKW_RAY_SORT_MIN 65536
-#endif
 
 }  // namespace skw

@@ -246,27 +246,10 @@ static int run_query(skw_accel *a, bool closest, const skw_ray *rays, int64_t n,
   skw_ctx *ctx = a->ctx;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
-  cudaStream_t s = (cudaStream_t)stream;
-  const void *trace_rays = rays;
-  const int32_t *index = nullptr;
-  void *ws = nullptr;
-  int launches = 0;
-  if (n >= SKW_RAY_SORT_MIN && a->info.n_triangles > 0) {
-    cudaMemPool_t pool;
-    if ((e = skw::ctx_pool(ctx, &pool)) != cudaSuccess) return cuda_fail(ctx, e, "workspace pool");
-    if ((e = cudaMallocFromPoolAsync(&ws, skw::ray_sort_workspace_bytes(n), pool, s)) != cudaSuccess)
-      return cuda_fail(ctx, e, "workspace allocation");
-    e = skw::launch_ray_sort(rays, n, a->info.bounds, ws, &trace_rays, &index, ctx->sms, s, &launches);
-    if (e != cudaSuccess) {
-      cudaFreeAsync(ws, s);
-      return cuda_fail(ctx, e, "ray binning launch");
-    }
-  }
-  e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, trace_rays, n, a->scene_abs, index, out,
-                            a->d_status, s);
-  if (ws) cudaFreeAsync(ws, s);
+  e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, a->scene_abs, nullptr, out,
+                            a->d_status, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, closest ? "closest-hit launch" : "any-hit launch");
-  ctx->launches.fetch_add(launches + 1);
+  ctx->launches.fetch_add(1);
   return SKW_OK;
 }
 
@@ -288,9 +271,11 @@ static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64
   void *d_rays = nullptr, *d_out = nullptr;
   cudaStream_t s = nullptr;
   int rc = SKW_OK;
+  cudaMemPool_t pool;
+  if ((e = skw::ctx_pool(a->ctx, &pool)) != cudaSuccess) return cuda_fail(a->ctx, e, "workspace pool");
   if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(a->ctx, e, "stream");
-  if ((e = cudaMallocAsync(&d_rays, (size_t)n * sizeof(skw_ray), s)) != cudaSuccess ||
-      (e = cudaMallocAsync(&d_out, out_bytes, s)) != cudaSuccess) {
+  if ((e = cudaMallocFromPoolAsync(&d_rays, (size_t)n * sizeof(skw_ray), pool, s)) != cudaSuccess ||
+      (e = cudaMallocFromPoolAsync(&d_out, out_bytes, pool, s)) != cudaSuccess) {
     rc = cuda_fail(a->ctx, e, "cudaMallocAsync");
   } else if ((e = cudaMemcpyAsync(d_rays, rays, (size_t)n * sizeof(skw_ray), cudaMemcpyHostToDevice, s)) !=
              cudaSuccess) {

@@ -48,7 +48,7 @@ constexpr double kDblEps = 2.220446049250313e-16;
 #define SKW_TRAV_BLOCK 128
 #endif
 #ifndef SKW_TRAV_MINB
-#define SKW_TRAV_MINB 6
+#define SKW_TRAV_MINB 7
 #endif
 
 enum : int { kMiss = 0, kHit = 1, kAmbiguous = 2 };
@@ -359,7 +359,7 @@ __device__ __forceinline__ void store_result(void *__restrict__ out, const int32
 
 // Persistent traversal.  The rays form groups of 32 consecutive rays; warp w
 // of W owns groups w, w + W, w + 2W, ... (interleaved, so that every warp
-// gets a representative mix even when the rays were binned by coherence).  A
+// gets a representative mix of cheap and expensive rays).  A
 // lane whose ray is finished takes the next ray of the warp's sequence when
 // at least SKW_TRAV_REFILL lanes are idle (or all are), so lanes rarely idle
 // while long rays finish.  No global atomics, no cross-warp waits.
