@@ -124,7 +124,7 @@ __device__ __forceinline__ int tri_test32(const RayF &r, float3 v0, float3 v1, f
 // The reference's double-precision Moller-Trumbore test, operation by
 // operation (TriangleAccelerator.cpp:240-273).  Intrinsics keep every
 // product and sum separately rounded, as in the x86-64 SSE2 build.
-__device__ __noinline__ bool tri_test64(const RayF &r, float3 v0f, float3 v1f, float3 v2f, double tmin, double tmax,
+__device__ __forceinline__ bool tri_test64(const RayF &r, float3 v0f, float3 v1f, float3 v2f, double tmin, double tmax,
                                         double &t_out) {
   const double ox = r.ox, oy = r.oy, oz = r.oz, dx = r.dx, dy = r.dy, dz = r.dz;
   const double v0x = v0f.x, v0y = v0f.y, v0z = v0f.z;
@@ -337,7 +337,7 @@ __device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const 
 
 // Exact double-precision t of the hit on slot `slot` (its barycentric tests
 // are known to pass).
-__device__ __noinline__ double exact_t(const float4 *__restrict__ tris, const RayF &r, int slot, float fallback) {
+__device__ __forceinline__ double exact_t(const float4 *__restrict__ tris, const RayF &r, int slot, float fallback) {
   const float4 a = __ldg(tris + 3 * slot), b = __ldg(tris + 3 * slot + 1), c = __ldg(tris + 3 * slot + 2);
   double t;
   return tri_test64(r, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z),
