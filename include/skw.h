@@ -164,6 +164,55 @@ int skw_intersect_test_host(skw_accel *accel, const skw_ray *rays, int64_t n, ui
 /* Kernel launches made by this library since the context was created. */
 int64_t skw_launch_count(const skw_ctx *ctx);
 
+/* ---------------------------------------------------- photon kd-tree -- */
+
+/* 16-bit direction codec of the reference's CompressedDirection
+ * (Math/CompressedDirection.h:107-133, CompressedDirection.cpp:21-41):
+ * encode a unit vector, and the decoded unit vector of every id (3 doubles
+ * per id, 65536 ids). */
+uint16_t skw_compress_direction(double x, double y, double z);
+int skw_direction_table(double *out);
+
+/* Host-only build of the photon kd-tree (KDTree<T>::KDTree / _Build,
+ * Raytracer/Core/KDTree.h:396-473): perm[i] = input index of the point at
+ * tree position i; node_words: 2 words per node, the reference's
+ * (split coordinate as float bits, right-child/flags word).  Needs no GPU.
+ * Either output may be NULL. */
+int skw_kdtree_build_host(const float *positions, int64_t n, int threads, int32_t *perm, uint32_t *node_words);
+
+/* Builds the tree on the host and uploads it.  positions: float xyz per
+ * photon; normal_ids: the photons' 16-bit surface-normal ids (NULL = all 0),
+ * used by the filtered lookups.  Lookup results index the TREE order
+ * (skw_kdtree_permutation maps them back to input order), as the
+ * reference's pointers index its permuted point array. */
+int skw_kdtree_create(skw_ctx *ctx, const float *positions, const uint16_t *normal_ids, int64_t n,
+                      skw_kdtree **out);
+void skw_kdtree_destroy(skw_kdtree *tree);
+int skw_kdtree_size(const skw_kdtree *tree, int64_t *n);
+int skw_kdtree_permutation(const skw_kdtree *tree, int32_t *perm);
+
+/* k nearest photons within max_dist for nq queries, device buffers.
+ * Stands in for KDTree::GetNearestPoints (Raytracer/Core/KDTree.h:506-533)
+ * with PhotonFilter (LTEIntegrators/PhotonLTEIntegrator/PhotonInternalTypes.h:
+ * 113-137) when cos_threshold >= 0 (query normals qn required), unfiltered
+ * when cos_threshold < 0 (qn may be NULL).  q, qn: 3 doubles per query.
+ * Per query: out_count = points found (<= k); out_idx / out_d2: k slots in
+ * the reference's heap order, -1 / 0 past out_count.  The index sets and
+ * their order equal the reference's bit for bit.  k <= 128 needs no
+ * workspace; larger k (up to 4096) allocates one from the context's
+ * stream-ordered pool. */
+int skw_knn(skw_kdtree *tree, const double *q, const double *qn, int64_t nq, int32_t k, double max_dist,
+            double cos_threshold, int32_t *out_idx, double *out_d2, int32_t *out_count, void *stream);
+/* Same with host buffers; waits for completion. */
+int skw_knn_host(skw_kdtree *tree, const double *q, const double *qn, int64_t nq, int32_t k, double max_dist,
+                 double cos_threshold, int32_t *out_idx, double *out_d2, int32_t *out_count);
+
+/* Nearest accepted photon per query (-1 if none within max_dist), device
+ * buffers.  Stands in for KDTree::GetNearestPoint (KDTree.h:485-503); the
+ * filter applies as in skw_knn. */
+int skw_nearest(skw_kdtree *tree, const double *q, const double *qn, int64_t nq, double max_dist,
+                double cos_threshold, int32_t *out_idx, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,7 @@ _ORACLE_SIGS = [
     ("oracle_kdtree_destroy", None, [_P]),
     ("oracle_knn", None, [_P, _P, _P, _i64, C.c_int32, C.c_double, C.c_double, _P, _P, _P, _P, C.c_int]),
     ("oracle_compressed_direction_table", None, [_P]),
+    ("oracle_nearest", None, [_P, _P, _P, _i64, C.c_double, C.c_double, _P, C.c_int]),
 ]
 
 _REF_SIGS = [
@@ -182,6 +183,13 @@ class OracleKD:
             out["visited"] = vis
         return out
 
+    def nearest(self, q, qn, max_dist, cos_threshold=-1.0, threads=0):
+        q = np.ascontiguousarray(q, np.float64).reshape(-1, 3)
+        qn = None if qn is None else np.ascontiguousarray(qn, np.float64).reshape(-1, 3)
+        out = np.empty(q.shape[0], np.int32)
+        self.lib.oracle_nearest(self.h, _ptr(q), _ptr(qn), q.shape[0], max_dist, cos_threshold, _ptr(out), threads)
+        return out
+
 
 class Reference:
     """The reference's own code (oracle/_ref/libskw_ref.so)."""
@@ -276,3 +284,9 @@ class RefKD:
         self.lib.skw_ref_knn(self.h, _ptr(q), _ptr(qn), nq, k, max_dist, cos_threshold, _ptr(idx), _ptr(d2), _ptr(cnt),
                              threads)
         return {"idx": idx, "d2": d2, "count": cnt}
+
+    def nearest(self, q, max_dist, threads=0):
+        q = np.ascontiguousarray(q, np.float64).reshape(-1, 3)
+        out = np.empty(q.shape[0], np.int32)
+        self.lib.skw_ref_nearest(self.h, _ptr(q), q.shape[0], max_dist, _ptr(out), threads)
+        return out

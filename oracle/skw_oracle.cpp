@@ -623,6 +623,60 @@ void oracle_knn(void *tp, const double *q, const double *qn, int64_t nq, int32_t
   });
 }
 
+// GetNearestPoint (KDTree.h:485-503) with NearestPointProc (KDTree.h:293-323)
+// and, when cos_threshold >= 0, PhotonFilter.
+struct NearestProc {
+  const Filter *f;
+  int32_t best = -1;
+  void visit(const KDTreeO &t, size_t ni, const double q[3], double &maxd2) {
+    const KPoint &pt = t.pts[ni];
+    double dx = pt.p[0] - q[0], dy = pt.p[1] - q[1], dz = pt.p[2] - q[2];
+    double d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 < maxd2 && f->pass(pt)) {
+      best = (int32_t)ni;
+      maxd2 = d2;
+    }
+    uint32_t w = t.nodes[ni].word;
+    if ((w & 3u) != 3u) {
+      unsigned axis = w & 3u;
+      double split = t.nodes[ni].split;
+      double pd = (q[axis] - split) * (q[axis] - split);
+      size_t right = w >> 3;
+      bool has_left = (w & 4u) != 0;
+      if (q[axis] <= split) {
+        if (has_left) visit(t, ni + 1, q, maxd2);
+        if (pd < maxd2 && right < t.nodes.size()) visit(t, right, q, maxd2);
+      } else {
+        if (right < t.nodes.size()) visit(t, right, q, maxd2);
+        if (pd < maxd2 && has_left) visit(t, ni + 1, q, maxd2);
+      }
+    }
+  }
+};
+
+void oracle_nearest(void *tp, const double *q, const double *qn, int64_t nq, double max_dist, double cos_threshold,
+                    int32_t *out_idx, int threads) {
+  init_dir_table();
+  const KDTreeO &t = *(KDTreeO *)tp;
+  for_ranges(nq, threads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      Filter f;
+      f.on = cos_threshold >= 0;
+      for (int c = 0; c < 3; ++c) {
+        f.q[c] = q[3 * i + c];
+        f.n[c] = qn ? qn[3 * i + c] : 0.0;
+      }
+      f.cos_t = cos_threshold;
+      f.sin_t = f.on ? std::sqrt(1.0 - cos_threshold * cos_threshold) : 0.0;
+      NearestProc proc;
+      proc.f = &f;
+      double maxd2 = max_dist * max_dist;
+      if (!t.nodes.empty()) proc.visit(t, 0, f.q, maxd2);
+      out_idx[i] = proc.best;
+    }
+  });
+}
+
 void oracle_compressed_direction_table(double *out) {
   init_dir_table();
   std::memcpy(out, g_dir_table.data(), g_dir_table.size() * sizeof(double));

@@ -6,5 +6,7 @@ interfaces.  Importing it does not load the library; the first query does,
 and fails loudly if it was not built.
 """
 from .accel import Context, Primitive, TriangleAccelerator, TriangleMesh, default_context, unpack_hits
+from .kdtree import PhotonKDTree, compress_direction, direction_table
 
-__all__ = ["Context", "Primitive", "TriangleAccelerator", "TriangleMesh", "default_context", "unpack_hits"]
+__all__ = ["Context", "Primitive", "TriangleAccelerator", "TriangleMesh", "default_context", "unpack_hits",
+           "PhotonKDTree", "compress_direction", "direction_table"]

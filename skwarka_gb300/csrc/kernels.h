@@ -21,4 +21,21 @@ cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, con
 
 
 
+// Photon kd-tree lookups (knn.cu).  nodes: KdNode[n]; nids: uint16 normal
+// id per node; dirs: 3 doubles per 16-bit direction id; q / qn: 3 doubles
+// per query (qn may be null when cos_t < 0, which disables the filter).
+// Outputs per query: k slots of tree positions and squared distances in the
+// reference's heap order (-1 / 0 when unused) and the found count;
+// out_visited (optional) counts visited nodes.  k > 128 needs a scratch
+// buffer of knn_scratch_bytes(nq, k) bytes.  status bit 1: stack overflow.
+size_t knn_scratch_bytes(int64_t nq, int k);
+cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
+                       const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,
+                       double *out_d2, int32_t *out_count, int32_t *out_visited, void *scratch, unsigned *status,
+                       cudaStream_t stream);
+// Nearest accepted point per query (-1 if none within max_dist).
+cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
+                           const double *qn, int64_t nq, double max_dist, double cos_t, int32_t *out_idx,
+                           unsigned *status, cudaStream_t stream);
+
 }  // namespace skw

@@ -1,0 +1,299 @@
+// Photon kd-tree lookups on sm_103a: filtered k-nearest neighbours
+// (KDTree::GetNearestPoints with PhotonFilter) and the nearest point
+// (KDTree::GetNearestPoint), one query per thread.
+//
+// Restated from Raytracer/Core/KDTree.h:
+//   * _Lookup (:537-576): visit a node's own point, then the child on the
+//     query's side of the split, then the other child if the squared plane
+//     distance is below the current search radius -- tested after the near
+//     subtree is done.  The recursion becomes an explicit stack whose entries
+//     carry the plane distance, re-tested on pop against the radius of that
+//     moment, which is exactly when the reference tests it.
+//   * distances in double from float positions and a double query
+//     (:547-550), compared with strict "<" against the radius;
+//   * NearestPointsProc (:331-387): the filter runs first; the first k
+//     accepted points fill an unordered array that becomes a max-heap
+//     (ordered by squared distance, ties by array position = the reference's
+//     pointer order); afterwards each accepted point replaces the heap top.
+//     The heap routines below are the classic binary-heap algorithms in the
+//     same form as the C++ library's make/pop/push_heap (sift the hole to the
+//     bottom, then sift the value up), so that not only the index sets but
+//     the output order match the reference.
+//   * PhotonFilter (PhotonInternalTypes.h:113-137): the photon's normal (from
+//     the 16-bit direction table) within the cosine threshold of the surface
+//     normal, and the photon near the surface's tangent plane.
+// Double products and sums use round-to-nearest intrinsics so that no fused
+// multiply-add changes a result.
+//
+// Layout: 16-byte nodes (x, y, z, word) read with one vector load; the
+// photon normal ids (uint16) are read only for points inside the radius.
+// For k <= 128 the heap and the stack live in local memory, which the L1
+// caches; larger k use a heap in a caller-provided global scratch buffer of
+// k 16-byte entries per query.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "kernels.h"
+
+namespace skw {
+namespace {
+
+constexpr int kMaxStack = 64;  // > tree depth (ceil(log2(n + 1)) <= 31 for n < 2^31)
+
+struct Cand {
+  double d2;
+  int32_t idx;
+};
+
+__device__ __forceinline__ bool cand_less(const Cand &a, const Cand &b) {
+  return a.d2 == b.d2 ? a.idx < b.idx : a.d2 < b.d2;
+}
+
+// Sift `value` up from `hole` towards `top`.
+__device__ __forceinline__ void heap_push_up(Cand *h, int hole, int top, Cand value) {
+  int parent = (hole - 1) / 2;
+  while (hole > top && cand_less(h[parent], value)) {
+    h[hole] = h[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  h[hole] = value;
+}
+
+// Move the hole at `hole` down to a leaf along larger children, then place
+// `value` by sifting it up.
+__device__ __forceinline__ void heap_adjust(Cand *h, int hole, int len, Cand value) {
+  const int top = hole;
+  int second = hole;
+  while (second < (len - 1) / 2) {
+    second = 2 * (second + 1);
+    if (cand_less(h[second], h[second - 1])) second--;
+    h[hole] = h[second];
+    hole = second;
+  }
+  if ((len & 1) == 0 && second == (len - 2) / 2) {
+    second = 2 * (second + 1);
+    h[hole] = h[second - 1];
+    hole = second - 1;
+  }
+  heap_push_up(h, hole, top, value);
+}
+
+__device__ __forceinline__ void heap_make(Cand *h, int len) {
+  if (len < 2) return;
+  for (int parent = (len - 2) / 2;; --parent) {
+    heap_adjust(h, parent, len, h[parent]);
+    if (parent == 0) return;
+  }
+}
+
+struct Query {
+  double q[3];
+  double n[3];
+  double cos_t, sin_t;
+  bool filter;
+};
+
+// PhotonFilter::operator() (PhotonInternalTypes.h:127-133).
+__device__ __forceinline__ bool photon_filter(const Query &Q, const float4 p, uint16_t nid,
+                                              const double *__restrict__ dirs) {
+  const double nx = __ldg(dirs + 3 * nid), ny = __ldg(dirs + 3 * nid + 1), nz = __ldg(dirs + 3 * nid + 2);
+  const double cosn = __dadd_rn(__dadd_rn(__dmul_rn(nx, Q.n[0]), __dmul_rn(ny, Q.n[1])), __dmul_rn(nz, Q.n[2]));
+  if (!(cosn > Q.cos_t)) return false;
+  const double tx = __dsub_rn((double)p.x, Q.q[0]), ty = __dsub_rn((double)p.y, Q.q[1]),
+               tz = __dsub_rn((double)p.z, Q.q[2]);
+  const double dotn = __dadd_rn(__dadd_rn(__dmul_rn(tx, Q.n[0]), __dmul_rn(ty, Q.n[1])), __dmul_rn(tz, Q.n[2]));
+  const double len = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(tx, tx), __dmul_rn(ty, ty)), __dmul_rn(tz, tz)));
+  return fabs(dotn) < __dmul_rn(Q.sin_t, len);
+}
+
+__device__ __forceinline__ double point_d2(const float4 p, const Query &Q) {
+  const double dx = __dsub_rn((double)p.x, Q.q[0]), dy = __dsub_rn((double)p.y, Q.q[1]),
+               dz = __dsub_rn((double)p.z, Q.q[2]);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// Walks the tree in the reference's order, calling visit(ni, p, d2, maxd2)
+// for every point with d2 < maxd2 (visit may shrink maxd2).  Returns nodes
+// visited (for statistics) or -1 on stack overflow.
+template <class Visit>
+__device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, const Query &Q, double &maxd2,
+                                    Visit &&visit) {
+  if (n <= 0) return 0;
+  uint32_t st_node[kMaxStack];
+  double st_d2[kMaxStack];
+  int sp = 0, visited = 0;
+  int cur = 0;
+  for (;;) {
+    const float4 p = __ldg(nodes + cur);
+    ++visited;
+    const double d2 = point_d2(p, Q);
+    if (d2 < maxd2) visit(cur, p, d2, maxd2);
+    const uint32_t w = __float_as_uint(p.w);
+    int next = -1;
+    if ((w & 3u) != 3u) {
+      const uint32_t axis = w & 3u;
+      const double split = (double)(axis == 0 ? p.x : (axis == 1 ? p.y : p.z));
+      const double qa = Q.q[axis];
+      const double pd = __dsub_rn(qa, split);
+      const double pd2 = __dmul_rn(pd, pd);
+      const uint32_t right = w >> 3;
+      const bool has_left = (w & 4u) != 0u, has_right = right < (uint32_t)n;
+      const int left_i = cur + 1;
+      int near_i, far_i;
+      if (qa <= split) {
+        near_i = has_left ? left_i : -1;
+        far_i = has_right ? (int)right : -1;
+      } else {
+        near_i = has_right ? (int)right : -1;
+        far_i = has_left ? left_i : -1;
+      }
+      if (far_i >= 0) {
+        if (sp >= kMaxStack) return -1;
+        st_node[sp] = (uint32_t)far_i;
+        st_d2[sp] = pd2;
+        ++sp;
+      }
+      next = near_i;
+    }
+    while (next < 0 && sp > 0) {
+      --sp;
+      if (st_d2[sp] < maxd2) next = (int)st_node[sp];
+    }
+    if (next < 0) return visited;
+    cur = next;
+  }
+}
+
+// KMAX > 0: heap of KMAX entries in local memory.  KMAX == 0: the heap of
+// query i is scratch[i * k ...].
+template <int KMAX>
+__global__ void __launch_bounds__(128) k_knn(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
+                                             const double *__restrict__ dirs, int n, const double *__restrict__ q,
+                                             const double *__restrict__ qn, int64_t nq, int k, double max_dist,
+                                             double cos_t, int32_t *__restrict__ out_idx,
+                                             double *__restrict__ out_d2, int32_t *__restrict__ out_count,
+                                             int32_t *__restrict__ out_visited, Cand *__restrict__ scratch,
+                                             unsigned *__restrict__ status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  Query Q;
+  Q.q[0] = q[3 * i];
+  Q.q[1] = q[3 * i + 1];
+  Q.q[2] = q[3 * i + 2];
+  Q.filter = cos_t >= 0.0;
+  if (Q.filter) {
+    Q.n[0] = qn[3 * i];
+    Q.n[1] = qn[3 * i + 1];
+    Q.n[2] = qn[3 * i + 2];
+    Q.cos_t = cos_t;
+    Q.sin_t = __dsqrt_rn(__dsub_rn(1.0, __dmul_rn(cos_t, cos_t)));
+  } else {
+    Q.n[0] = Q.n[1] = Q.n[2] = 0.0;
+    Q.cos_t = Q.sin_t = 0.0;
+  }
+  Cand local_heap[KMAX > 0 ? KMAX : 1];
+  Cand *heap = KMAX > 0 ? local_heap : scratch + i * (int64_t)k;
+  int size = 0;
+  double maxd2 = __dmul_rn(max_dist, max_dist);  // KDTree::Lookup (KDTree.h:475-482)
+  int visited = 0;
+  if (k > 0) {
+    visited = walk(nodes, n, Q, maxd2, [&](int ni, const float4 p, double d2, double &md2) {
+      if (Q.filter && !photon_filter(Q, p, __ldg(nids + ni), dirs)) return;
+      if (size < k) {
+        heap[size++] = Cand{d2, ni};
+        if (size == k) {
+          heap_make(heap, size);
+          md2 = heap[0].d2;
+        }
+      } else {
+        // pop_heap: the top goes to the back; the back's old value is re-placed
+        const Cand back = heap[k - 1];
+        heap[k - 1] = heap[0];
+        heap_adjust(heap, 0, k - 1, back);
+        // replace the (popped) back with the new point and push it
+        heap_push_up(heap, k - 1, 0, Cand{d2, ni});
+        md2 = heap[0].d2;
+      }
+    });
+    if (visited < 0) atomicOr(status, 2u);
+  }
+  out_count[i] = size;
+  for (int j = 0; j < k; ++j) {
+    out_idx[i * k + j] = j < size ? heap[j].idx : -1;
+    out_d2[i * k + j] = j < size ? heap[j].d2 : 0.0;
+  }
+  if (out_visited) out_visited[i] = visited;
+}
+
+// GetNearestPoint (KDTree.h:495-503) with NearestPointProc (:293-323):
+// every accepted point becomes the nearest and shrinks the radius.
+__global__ void __launch_bounds__(128) k_nearest(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
+                                                 const double *__restrict__ dirs, int n,
+                                                 const double *__restrict__ q, const double *__restrict__ qn,
+                                                 int64_t nq, double max_dist, double cos_t,
+                                                 int32_t *__restrict__ out_idx, unsigned *__restrict__ status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  Query Q;
+  Q.q[0] = q[3 * i];
+  Q.q[1] = q[3 * i + 1];
+  Q.q[2] = q[3 * i + 2];
+  Q.filter = cos_t >= 0.0;
+  if (Q.filter) {
+    Q.n[0] = qn[3 * i];
+    Q.n[1] = qn[3 * i + 1];
+    Q.n[2] = qn[3 * i + 2];
+    Q.cos_t = cos_t;
+    Q.sin_t = __dsqrt_rn(__dsub_rn(1.0, __dmul_rn(cos_t, cos_t)));
+  } else {
+    Q.n[0] = Q.n[1] = Q.n[2] = 0.0;
+    Q.cos_t = Q.sin_t = 0.0;
+  }
+  double maxd2 = __dmul_rn(max_dist, max_dist);
+  int best = -1;
+  const int v = walk(nodes, n, Q, maxd2, [&](int ni, const float4 p, double d2, double &md2) {
+    if (Q.filter && !photon_filter(Q, p, __ldg(nids + ni), dirs)) return;
+    best = ni;
+    md2 = d2;
+  });
+  if (v < 0) atomicOr(status, 2u);
+  out_idx[i] = best;
+}
+
+}  // namespace
+
+size_t knn_scratch_bytes(int64_t nq, int k) { return k > 128 ? (size_t)nq * (size_t)k * sizeof(Cand) : 0; }
+
+cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
+                       const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,
+                       double *out_d2, int32_t *out_count, int32_t *out_visited, void *scratch, unsigned *status,
+                       cudaStream_t stream) {
+  if (nq <= 0) return cudaSuccess;
+  const int block = 128;
+  const unsigned grid = (unsigned)((nq + block - 1) / block);
+  if (k <= 32) {
+    k_knn<32><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
+                                           out_idx, out_d2, out_count, out_visited, nullptr, status);
+  } else if (k <= 128) {
+    k_knn<128><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
+                                            out_idx, out_d2, out_count, out_visited, nullptr, status);
+  } else {
+    k_knn<0><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
+                                          out_idx, out_d2, out_count, out_visited, (Cand *)scratch, status);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
+                           const double *qn, int64_t nq, double max_dist, double cos_t, int32_t *out_idx,
+                           unsigned *status, cudaStream_t stream) {
+  if (nq <= 0) return cudaSuccess;
+  const int block = 128;
+  const unsigned grid = (unsigned)((nq + block - 1) / block);
+  k_nearest<<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, max_dist, cos_t, out_idx,
+                                        status);
+  return cudaGetLastError();
+}
+
+}  // namespace skw

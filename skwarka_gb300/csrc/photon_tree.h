@@ -1,0 +1,37 @@
+// Host construction of the photon kd-tree (one point per node, median
+// split on the longest axis) and the 16-bit direction codec table.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace skw {
+
+// One tree node = the node's own photon position and the reference's packed
+// node word (KDTree<T>::Node, Raytracer/Core/KDTree.h:188-246): bits 0-1 split
+// axis or 3 for a leaf, bit 2 has-left-child, bits 3-31 right child index
+// ((1 << 29) - 1 when absent).  The node's split coordinate is its own
+// position on the split axis (KDTree.h:455), so it is not stored twice.
+// The left child, when present, is the next node.  16 bytes, one vector load.
+struct alignas(16) KdNode {
+  float x, y, z;
+  uint32_t word;
+};
+static_assert(sizeof(KdNode) == 16, "KdNode must be 16 bytes");
+
+// Builds the tree over n points (float xyz): nodes in tree order and perm[i]
+// = input index of the point at tree position i.  The order equals the
+// reference's KDTree::_Build (KDTree.h:428-473) for the same standard
+// library, since it makes the same std::nth_element calls.  Subtrees are
+// built on several threads (`threads` <= 0: all hardware threads).
+void build_photon_tree(const float *pos, int64_t n, int threads, std::vector<KdNode> &nodes,
+                       std::vector<int32_t> &perm);
+
+// CompressedDirection table (Math/CompressedDirection.cpp:21-41): unit vector
+// of every 16-bit direction id, as 3 doubles per id.
+const std::vector<double> &direction_table();
+
+// CompressedDirection(Vector3D) encoder (Math/CompressedDirection.h:107-133).
+uint16_t compress_direction(double x, double y, double z);
+
+}  // namespace skw

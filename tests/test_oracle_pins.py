@@ -125,3 +125,12 @@ def test_oracle_knn_equals_reference_fresh(oracle, reference):
         a, b = ko.knn(*args), kr.knn(*args)
         for key in ("idx", "d2", "count"):
             assert np.array_equal(a[key], b[key])
+
+
+def test_oracle_nearest_equals_reference(oracle, reference):
+    rng = np.random.default_rng(78)
+    pos = rng.uniform(0, 1, size=(8000, 3)).astype(np.float32)
+    ko, kr = oracle.kdtree(pos), reference.kdtree(pos)
+    q = rng.uniform(-0.1, 1.1, size=(2000, 3))
+    for r in (0.01, 0.05, np.inf):
+        assert np.array_equal(ko.nearest(q, None, r), kr.nearest(q, r))
