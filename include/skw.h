@@ -203,6 +203,26 @@ int skw_kdtree_permutation(const skw_kdtree *tree, int32_t *perm);
  * stream-ordered pool. */
 int skw_knn(skw_kdtree *tree, const double *q, const double *qn, int64_t nq, int32_t k, double max_dist,
             double cos_threshold, int32_t *out_idx, double *out_d2, int32_t *out_count, void *stream);
+/* skw_knn without any allocation, for callers that cannot allocate device
+ * memory at query time: a renderer that reserves its whole device budget up
+ * front and forbids allocations inside a frame, or a host callback that must
+ * not block or synchronise the device the way cudaMalloc / cudaFree can.
+ * This entry point has no counterpart in the reference (which allocates its
+ * per-thread heaps from a host memory pool).
+ *
+ * The heaps live in one static device array of 1,048,576 entries (16 MiB)
+ * that every GPU loading this library holds until the process exits; a call
+ * needs nq * k <= 1,048,576 and returns SKW_ERR_ARG (with a message) beyond
+ * that.  Results are identical to skw_knn.  The first call on a device looks
+ * the array's device address up (cudaGetSymbolAddress), which can load the
+ * library's device code; make that first call before any stream capture.
+ * All calls share the array, and it keeps the previous call's contents:
+ * every heap slot is written before it is read, so nothing needs clearing,
+ * but calls that overlap on the GPU (different streams or contexts) race on
+ * it and must be serialised by the caller.  Device buffers only. */
+int skw_knn_noalloc(skw_kdtree *tree, const double *q, const double *qn, int64_t nq, int32_t k, double max_dist,
+                    double cos_threshold, int32_t *out_idx, double *out_d2, int32_t *out_count, void *stream);
+
 /* Same with host buffers; waits for completion. */
 int skw_knn_host(skw_kdtree *tree, const double *q, const double *qn, int64_t nq, int32_t k, double max_dist,
                  double cos_threshold, int32_t *out_idx, double *out_d2, int32_t *out_count);

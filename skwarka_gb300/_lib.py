@@ -71,6 +71,7 @@ SIGNATURES = [
     ("skw_kdtree_size", C.c_int, [_P, C.POINTER(C.c_int64)]),
     ("skw_kdtree_permutation", C.c_int, [_P, _P]),
     ("skw_knn", C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, C.c_double, C.c_double, _P, _P, _P, _P]),
+    ("skw_knn_noalloc", C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, C.c_double, C.c_double, _P, _P, _P, _P]),
     ("skw_knn_host", C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, C.c_double, C.c_double, _P, _P, _P]),
     ("skw_nearest", C.c_int, [_P, _P, _P, C.c_int64, C.c_double, C.c_double, _P, _P]),
 ]

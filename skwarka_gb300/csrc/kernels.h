@@ -33,6 +33,14 @@ cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *di
                        const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,
                        double *out_d2, int32_t *out_count, int32_t *out_visited, void *scratch, unsigned *status,
                        cudaStream_t stream);
+// k-NN with its heaps in the library's static device scratch (no
+// allocation): nq * k must be <= knn_noalloc_capacity() entries, else
+// cudaErrorInvalidValue.  Overlapping calls race on that scratch.
+int64_t knn_noalloc_capacity();
+cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
+                               const double *qn, int64_t nq, int k, double max_dist, double cos_t,
+                               int32_t *out_idx, double *out_d2, int32_t *out_count, unsigned *status,
+                               cudaStream_t stream);
 // Nearest accepted point per query (-1 if none within max_dist).
 cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                            const double *qn, int64_t nq, double max_dist, double cos_t, int32_t *out_idx,

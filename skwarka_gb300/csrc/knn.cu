@@ -32,8 +32,18 @@
 // k 16-byte entries per query.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <mutex>
 
 #include "kernels.h"
+
+// Scratch of the allocation-free k-NN entry point (skw_knn_noalloc): heaps
+// of SKW_KNN_NOALLOC_ENTRIES 16-byte entries (16 MiB), allocated with the
+// module on every GPU that loads this library and held until the process
+// exits.  Host code must not pass this symbol to a kernel (in host code it
+// is only a stand-in for the device address); knn_noalloc_scratch() looks
+// the device address up.
+#define SKW_KNN_NOALLOC_ENTRIES (1 << 20)
+static __device__ __align__(256) unsigned char g_knn_noalloc_scratch[(size_t)SKW_KNN_NOALLOC_ENTRIES * 16];
 
 namespace skw {
 namespace {
@@ -282,6 +292,47 @@ cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *di
     k_knn<0><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
                                           out_idx, out_d2, out_count, out_visited, (Cand *)scratch, status);
   }
+  return cudaGetLastError();
+}
+
+int64_t knn_noalloc_capacity() { return SKW_KNN_NOALLOC_ENTRIES; }
+
+// Device address of the static scratch for the current device, looked up
+// once per device (cudaGetSymbolAddress with that device current; the first
+// lookup may load this module on the device).
+static cudaError_t knn_noalloc_scratch(void **out) {
+  static std::mutex mu;
+  static void *addr[64] = {nullptr};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_knn_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return cudaSuccess;
+}
+
+cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
+                               const double *qn, int64_t nq, int k, double max_dist, double cos_t,
+                               int32_t *out_idx, double *out_d2, int32_t *out_count, unsigned *status,
+                               cudaStream_t stream) {
+  if (nq <= 0) return cudaSuccess;
+  if (nq * (int64_t)k > SKW_KNN_NOALLOC_ENTRIES) return cudaErrorInvalidValue;
+  void *scratch = nullptr;
+  cudaError_t e = knn_noalloc_scratch(&scratch);
+  if (e != cudaSuccess) return e;
+  // Every heap slot is written before it is read, so the array needs no
+  // clearing between calls.
+  const int block = 128;
+  const unsigned grid = (unsigned)((nq + block - 1) / block);
+  k_knn<0><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
+                                        out_idx, out_d2, out_count, nullptr, (Cand *)scratch, status);
   return cudaGetLastError();
 }
 

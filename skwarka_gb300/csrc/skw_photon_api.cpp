@@ -152,6 +152,28 @@ int skw_knn(skw_kdtree *t, const double *q, const double *qn, int64_t nq, int32_
   return SKW_OK;
 }
 
+int skw_knn_noalloc(skw_kdtree *t, const double *q, const double *qn, int64_t nq, int32_t k, double max_dist,
+                    double cos_threshold, int32_t *out_idx, double *out_d2, int32_t *out_count, void *stream) {
+  int rc = check_query_args(t, q, qn, nq, k, max_dist, cos_threshold, true);
+  if (rc != SKW_OK) return rc;
+  if (nq > 0 && (!out_count || (k > 0 && (!out_idx || !out_d2))))
+    return fail(t->ctx, SKW_ERR_ARG, "null output buffer");
+  const int64_t cap = skw::knn_noalloc_capacity();
+  if (nq * (int64_t)k > cap)
+    return fail(t->ctx, SKW_ERR_ARG,
+                "skw_knn_noalloc: nq * k = " + std::to_string(nq * (int64_t)k) +
+                    " heap entries exceeds the static scratch capacity of " + std::to_string(cap) +
+                    "; split the queries into smaller batches");
+  if (nq == 0) return SKW_OK;
+  cudaError_t e = cudaSetDevice(t->ctx->device);
+  if (e != cudaSuccess) return cuda_fail(t->ctx, e, "cudaSetDevice");
+  e = skw::launch_knn_noalloc(t->d_nodes, t->d_nids, t->d_dirs, (int)t->n, q, qn, nq, k, max_dist, cos_threshold,
+                              out_idx, out_d2, out_count, t->d_status, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(t->ctx, e, "k-NN (no allocation) launch");
+  t->ctx->launches.fetch_add(1);
+  return SKW_OK;
+}
+
 int skw_knn_host(skw_kdtree *t, const double *q, const double *qn, int64_t nq, int32_t k, double max_dist,
                  double cos_threshold, int32_t *out_idx, double *out_d2, int32_t *out_count) {
   int rc = check_query_args(t, q, qn, nq, k, max_dist, cos_threshold, true);
