@@ -40,6 +40,7 @@ typedef enum skw_status {
 typedef struct skw_ctx skw_ctx;
 typedef struct skw_accel skw_accel;
 typedef struct skw_kdtree skw_kdtree;
+typedef struct skw_scene skw_scene;
 
 /* ------------------------------------------------------------ context -- */
 
@@ -232,6 +233,74 @@ int skw_knn_host(skw_kdtree *tree, const double *q, const double *qn, int64_t nq
  * filter applies as in skw_knn. */
 int skw_nearest(skw_kdtree *tree, const double *q, const double *qn, int64_t nq, double max_dist,
                 double cos_threshold, int32_t *out_idx, void *stream);
+
+/* ------------------------------------------------ direct-lighting render -- */
+
+/* Material kinds (Raytracer/Materials): */
+#define SKW_MATERIAL_MATTE 0   /* MatteMaterial: Lambertian (sigma == 0) or Oren-Nayar */
+#define SKW_MATERIAL_PLASTIC 1 /* PlasticMaterial: Lambertian(kd) + Blinn microfacet(ks, 1/roughness), dielectric 1.5 */
+#define SKW_MATERIAL_METAL 2   /* MetalMaterial: Blinn microfacet with a conductor Fresnel (eta, k) */
+
+typedef struct skw_material {
+  int32_t kind;
+  float kd[3];        /* matte reflectance, plastic diffuse reflectance */
+  float ks[3];        /* plastic glossy reflectance */
+  float roughness;    /* plastic / metal, clamped to [0.001, 1] like the reference */
+  float sigma;        /* matte Oren-Nayar sigma (radians); 0 = Lambertian */
+  float eta[3], k[3]; /* metal refractive index and absorption */
+} skw_material;
+
+/* A primitive of the render scene: mesh + transform as for the accelerator,
+ * plus its material, optional area-light emission and shading normals. */
+typedef struct skw_render_primitive {
+  int32_t mesh;
+  const double *mesh_to_world;   /* row-major 4x4 or NULL (area lights must use NULL) */
+  int32_t material;              /* index into the materials array */
+  const float *vertex_normals;   /* per-vertex shading normals (mesh space) or NULL:
+                                    then the geometric normal shades (use_shading_normals = false) */
+  const float *triangle_albedo;  /* optional per-triangle RGB replacing the material's kd */
+  float emission[3];             /* DiffuseAreaLightSource radiance; all 0 = not a light */
+} skw_render_primitive;
+
+typedef struct skw_point_light {
+  float position[3];
+  float intensity[3];
+} skw_point_light;
+
+/* Builds a render scene: the accelerator (as skw_accel_create) plus the
+ * shading data.  Stands in for Scene(primitives, volume, lights)
+ * (Raytracer/Core/Scene.h:107-113) with DiffuseAreaLightSource and
+ * PointLight lights and no participating medium. */
+int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, const skw_render_primitive *prims,
+                     int32_t n_prims, const skw_material *materials, int32_t n_materials,
+                     const skw_point_light *point_lights, int32_t n_point_lights, skw_scene **out);
+void skw_scene_destroy(skw_scene *scene);
+/* The scene's accelerator (owned by the scene), for ray queries. */
+skw_accel *skw_scene_accel(skw_scene *scene);
+
+/* Pinhole PerspectiveCamera (Raytracer/Cameras/PerspectiveCamera.cpp:36-65):
+ * camera-to-world row-major 4x4, horizontal view angle in radians, film size. */
+typedef struct skw_camera {
+  double camera_to_world[16];
+  double x_view_angle;
+  int32_t width, height;
+} skw_camera;
+
+typedef struct skw_render_params {
+  int32_t spp_x, spp_y;        /* stratified pixel samples (StratifiedSampler) */
+  int32_t light_samples;       /* DirectLightingLTEIntegratorParams::m_direct_light_samples_num */
+  uint64_t seed;               /* counter-based random stream seed */
+} skw_render_params;
+
+/* Renders the direct-lighting estimate of every pixel into film_rgb
+ * (height x width x 3 floats, device buffer, row y = image y), the
+ * SamplerBasedRenderer + DirectLightingLTEIntegrator + ImageFilm/BoxFilter
+ * result (Renderers/SamplerBasedRenderer.cpp:200-239, 419-491,
+ * LTEIntegrators/DirectLightingLTEIntegrator.cpp:33-60,
+ * Core/DirectLightingIntegrator.cpp:54-366).  Sample radiances that are
+ * NaN, negative or infinite count as black, as in the reference. */
+int skw_render_direct(skw_scene *scene, const skw_camera *camera, const skw_render_params *params, float *film_rgb,
+                      void *stream);
 
 #ifdef __cplusplus
 }

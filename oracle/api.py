@@ -62,6 +62,9 @@ _REF_SIGS = [
     ("skw_ref_nearest", None, [_P, _P, _i64, C.c_double, _P, C.c_int]),
     ("skw_ref_compressed_direction_table", None, [_P]),
     ("skw_ref_compress_direction", C.c_uint16, [C.c_double, C.c_double, C.c_double]),
+    ("skw_ref_render_direct", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, C.c_int, _P, C.c_int, _P, _P,
+                                        C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
+    ("skw_ref_luminance_weights", None, [_P]),
 ]
 
 
@@ -211,6 +214,26 @@ class Reference:
         out = np.empty((1 << 16, 3), np.float64)
         self.lib.skw_ref_compressed_direction_table(_ptr(out))
         return out
+
+    def render_direct(self, prims, materials, point_lights, camera, spp_x, spp_y, light_samples=1):
+        """The reference's own direct-lighting render of a scene described with
+        skwarka_gb300.render types: (film (h, w, 3) float32, seconds)."""
+        from skwarka_gb300.render import c_material, c_prims
+        cm, nm, cp, keep = c_prims(prims)
+        verts = (C.c_void_p * nm)(*[cm[i].vertices for i in range(nm)])
+        tris = (C.c_void_p * nm)(*[cm[i].triangles for i in range(nm)])
+        nv = np.array([cm[i].n_vertices for i in range(nm)], np.int64)
+        nt = np.array([cm[i].n_triangles for i in range(nm)], np.int64)
+        mats = (type(c_material(materials[0])) * len(materials))(*[c_material(m) for m in materials])
+        pl = np.array([list(l.position) + list(l.intensity) for l in point_lights], np.float32).reshape(-1, 6)
+        c2w = np.ascontiguousarray(camera.camera_to_world, np.float64).reshape(-1)
+        film = np.zeros((camera.height, camera.width, 3), np.float32)
+        sec = np.zeros(1)
+        self.lib.skw_ref_render_direct(nm, verts, _ptr(nv), tris, _ptr(nt), len(prims), C.addressof(cp), len(materials),
+                                       C.addressof(mats), len(point_lights), _ptr(pl) if len(pl) else None, _ptr(c2w),
+                                       camera.x_view_angle, camera.width, camera.height, spp_x, spp_y, light_samples,
+                                       _ptr(film), _ptr(sec))
+        return film, float(sec[0])
 
 
 class RefAccel:

@@ -38,8 +38,25 @@
 #include <Raytracer/LTEIntegrators/PhotonLTEIntegrator.h>
 #include <Raytracer/LTEIntegrators/PhotonLTEIntegrator/PhotonInternalTypes.h>
 #include <Math/CompressedDirection.h>
+#include <Raytracer/Core/Scene.h>
+#include <Raytracer/Core/LightSources.h>
+#include <Raytracer/Core/Texture.h>
+#include <Raytracer/Core/SpectrumRoutines.h>
+#include <Raytracer/Textures/ConstantTexture.h>
+#include <Raytracer/Materials/MatteMaterial.h>
+#include <Raytracer/Materials/PlasticMaterial.h>
+#include <Raytracer/Materials/MetalMaterial.h>
+#include <Raytracer/LightSources/DiffuseAreaLightSource.h>
+#include <Raytracer/LightSources/PointLight.h>
+#include <Raytracer/Cameras/PerspectiveCamera.h>
+#include <Raytracer/Films/ImageFilm.h>
+#include <Raytracer/FilmFilters/BoxFilter.h>
+#include <Raytracer/Samplers/StratifiedSampler.h>
+#include <Raytracer/LTEIntegrators/DirectLightingLTEIntegrator.h>
+#include <Raytracer/Renderers/SamplerBasedRenderer.h>
 #undef private
 #undef protected
+#include <chrono>
 
 namespace {
 
@@ -315,6 +332,139 @@ void skw_ref_compressed_direction_table(double *out) {
 
 uint16_t skw_ref_compress_direction(double x, double y, double z) {
   return CompressedDirection(Vector3D_d(x, y, z)).GetID();
+}
+
+// ------------------------------------------------------------- rendering --
+
+// Per-triangle constant reflectance, looked up by the hit's triangle index.
+class TriangleAlbedoTexture : public Texture<SpectrumCoef_d> {
+ public:
+  explicit TriangleAlbedoTexture(std::vector<SpectrumCoef_d> v) : m_v(std::move(v)) {}
+  SpectrumCoef_d Evaluate(const DifferentialGeometry &, size_t i_triangle_index) const override {
+    return m_v[i_triangle_index];
+  }
+
+ private:
+  std::vector<SpectrumCoef_d> m_v;
+};
+
+// Same layouts as the product's skw_material / skw_render_primitive.
+struct RefMaterialIn {
+  int32_t kind;
+  float kd[3], ks[3];
+  float roughness, sigma;
+  float eta[3], k[3];
+};
+struct RefPrimIn {
+  int32_t mesh;
+  const double *mesh_to_world;
+  int32_t material;
+  const float *vertex_normals;
+  const float *triangle_albedo;
+  float emission[3];
+};
+
+// Renders the direct-lighting image with the reference's SamplerBasedRenderer,
+// StratifiedSampler, DirectLightingLTEIntegrator, PerspectiveCamera and an
+// ImageFilm with a 0.5-wide BoxFilter.  film_out: height x width x 3.
+int skw_ref_render_direct(int n_meshes, const float *const *verts, const int64_t *n_verts, const int32_t *const *tris,
+                          const int64_t *n_tris, int n_prims, const RefPrimIn *prims, int n_materials,
+                          const RefMaterialIn *materials, int n_point_lights, const float *point_lights,
+                          const double *camera_to_world, double x_view_angle, int width, int height, int spp_x,
+                          int spp_y, int light_samples, float *film_out, double *seconds_out) {
+  std::vector<intrusive_ptr<const Primitive>> prim_list;
+  LightSources lights;
+  for (int p = 0; p < n_prims; ++p) {
+    const RefPrimIn &P = prims[p];
+    const int m = P.mesh;
+    std::vector<Point3D_f> v((size_t)n_verts[m]);
+    for (int64_t i = 0; i < n_verts[m]; ++i)
+      v[(size_t)i] = Point3D_f(verts[m][3 * i], verts[m][3 * i + 1], verts[m][3 * i + 2]);
+    std::vector<MeshTriangle> t((size_t)n_tris[m]);
+    for (int64_t i = 0; i < n_tris[m]; ++i) t[(size_t)i] = MeshTriangle(tris[m][3 * i], tris[m][3 * i + 1], tris[m][3 * i + 2]);
+    intrusive_ptr<TriangleMesh> mesh;
+    if (P.vertex_normals) {
+      std::vector<Vector3D_f> nrm((size_t)n_verts[m]);
+      for (int64_t i = 0; i < n_verts[m]; ++i)
+        nrm[(size_t)i] = Vector3D_f(P.vertex_normals[3 * i], P.vertex_normals[3 * i + 1], P.vertex_normals[3 * i + 2]);
+      mesh.reset(new TriangleMesh(v, t, nrm, std::vector<Vector3D_f>(), true, false));
+    } else {
+      mesh.reset(new TriangleMesh(v, t, false, false));
+    }
+    const RefMaterialIn &M = materials[P.material];
+    intrusive_ptr<const Texture<SpectrumCoef_d>> kd;
+    if (P.triangle_albedo) {
+      std::vector<SpectrumCoef_d> a((size_t)n_tris[m]);
+      for (int64_t i = 0; i < n_tris[m]; ++i)
+        a[(size_t)i] = SpectrumCoef_d(P.triangle_albedo[3 * i], P.triangle_albedo[3 * i + 1], P.triangle_albedo[3 * i + 2]);
+      kd.reset(new TriangleAlbedoTexture(a));
+    } else {
+      kd.reset(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.kd[0], M.kd[1], M.kd[2])));
+    }
+    intrusive_ptr<const Material> mat;
+    if (M.kind == 0) {
+      mat.reset(new MatteMaterial(kd, intrusive_ptr<const Texture<double>>(new ConstantTexture<double>(M.sigma))));
+    } else if (M.kind == 1) {
+      mat.reset(new PlasticMaterial(kd, intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(
+                                            SpectrumCoef_d(M.ks[0], M.ks[1], M.ks[2]))),
+                                    intrusive_ptr<const Texture<double>>(new ConstantTexture<double>(M.roughness))));
+    } else {
+      mat.reset(new MetalMaterial(
+          intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.eta[0], M.eta[1], M.eta[2]))),
+          intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.k[0], M.k[1], M.k[2]))),
+          intrusive_ptr<const Texture<double>>(new ConstantTexture<double>(M.roughness))));
+    }
+    intrusive_ptr<const AreaLightSource> light;
+    if (P.emission[0] > 0 || P.emission[1] > 0 || P.emission[2] > 0) {
+      light.reset(new DiffuseAreaLightSource(Spectrum_d(P.emission[0], P.emission[1], P.emission[2]), mesh));
+      lights.m_area_light_sources.push_back(light);
+    }
+    prim_list.push_back(intrusive_ptr<const Primitive>(
+        new Primitive(mesh, make_transform(P.mesh_to_world), mat, light, NULL)));
+  }
+  for (int i = 0; i < n_point_lights; ++i) {
+    const float *L = point_lights + 6 * i;
+    lights.m_delta_light_sources.push_back(intrusive_ptr<const DeltaLightSource>(
+        new PointLight(Point3D_d(L[0], L[1], L[2]), Spectrum_d(L[3], L[4], L[5]))));
+  }
+  intrusive_ptr<const Scene> scene(new Scene(prim_list, NULL, lights));
+  intrusive_ptr<FilmFilter> filter(new BoxFilter(0.5, 0.5));
+  intrusive_ptr<ImageFilm> film(new ImageFilm((size_t)width, (size_t)height, filter));
+  intrusive_ptr<const Camera> camera(new PerspectiveCamera(make_transform(camera_to_world), film, 0.0, 1.0, x_view_angle));
+  Point2D_i begin, end;
+  film->GetSamplingExtent(begin, end);
+  intrusive_ptr<Sampler> sampler(new StratifiedSampler(begin, end, (size_t)spp_x, (size_t)spp_y));
+  DirectLightingLTEIntegratorParams params;
+  params.m_direct_light_samples_num = (size_t)light_samples;
+  params.m_max_specular_depth = 6;
+  params.m_media_step_size = 0.01;
+  intrusive_ptr<LTEIntegrator> integrator(new DirectLightingLTEIntegrator(scene, params));
+  SamplerBasedRenderer renderer(integrator, sampler);
+  auto t0 = std::chrono::steady_clock::now();
+  renderer.Render(camera, false);
+  if (seconds_out) *seconds_out = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  for (int y = 0; y < height; ++y)
+    for (int x = 0; x < width; ++x) {
+      Spectrum_d c;
+      float *o = film_out + 3 * ((int64_t)y * width + x);
+      if (film->GetPixel(Point2D_i(x, y), c, true)) {
+        o[0] = (float)c[0];
+        o[1] = (float)c[1];
+        o[2] = (float)c[2];
+      } else {
+        o[0] = o[1] = o[2] = 0.0f;
+      }
+    }
+  return 0;
+}
+
+// Row Y of the reference's spectrum-to-XYZ matrix (its luminance weights).
+void skw_ref_luminance_weights(double *out) {
+  for (int k = 0; k < 3; ++k) {
+    double rgb[3] = {0, 0, 0};
+    rgb[k] = 1.0;
+    out[k] = SpectrumRoutines::Luminance(Spectrum_d(rgb[0], rgb[1], rgb[2]));
+  }
 }
 
 }  // extern "C"

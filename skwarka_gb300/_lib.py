@@ -73,6 +73,11 @@ SIGNATURES = [
     ("skw_knn", C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, C.c_double, C.c_double, _P, _P, _P, _P]),
     ("skw_knn_noalloc", C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, C.c_double, C.c_double, _P, _P, _P, _P]),
     ("skw_knn_host", C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, C.c_double, C.c_double, _P, _P, _P]),
+    ("skw_scene_create", C.c_int, [_P, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                   C.c_void_p, C.c_int32, C.POINTER(_P)]),
+    ("skw_scene_destroy", None, [_P]),
+    ("skw_scene_accel", _P, [_P]),
+    ("skw_render_direct", C.c_int, [_P, C.c_void_p, C.c_void_p, _P, _P]),
     ("skw_nearest", C.c_int, [_P, _P, _P, C.c_int64, C.c_double, C.c_double, _P, _P]),
 ]
 

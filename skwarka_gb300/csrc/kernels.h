@@ -15,9 +15,12 @@ int traversal_stack_capacity(int max_depth);
 // scene_abs: the largest absolute coordinate of any vertex in the tree (it
 // bounds the slab-test rounding error).
 // out_index (may be null): result of ray j goes to slot out_index[j].
+// n_dev (may be null): device int holding the number of rays to trace (at
+// most n), for queues filled on the device.  out_index (may be null): the
+// result of ray j goes to slot out_index[j].
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
-                             int64_t n, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
-                             cudaStream_t stream);
+                             int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
+                             unsigned *status, cudaStream_t stream);
 
 
 
@@ -45,5 +48,20 @@ cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const do
 cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                            const double *qn, int64_t nq, double max_dist, double cos_t, int32_t *out_idx,
                            unsigned *status, cudaStream_t stream);
+
+// Direct-lighting render stages (render.cu); see render_scene.h.
+struct SceneDev;
+struct CameraDev;
+cudaError_t launch_camera(const CameraDev &cam, int px_begin, int n_px, int sppx, int sppy, uint64_t seed,
+                          void *rays, cudaStream_t s);
+cudaError_t launch_shade(const SceneDev &S, int n, int64_t gid_base, int slots, int n_light_samples, uint64_t seed,
+                         const void *rays, const void *hits, float *contrib, void *srays, int *starget, float *srgb,
+                         int *scount, void *brays, int *btarget, float *brgb, int *bcount, cudaStream_t s);
+cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
+                           const int *starget, const float *srgb, const int *scount, const void *brays,
+                           const void *bhits, const int *btarget, const float *brgb, const int *bcount,
+                           float *contrib, cudaStream_t s);
+cudaError_t launch_film(const float *contrib, int px_begin, int n_px, int spp, int slots, float *film,
+                        cudaStream_t s);
 
 }  // namespace skw

@@ -1,0 +1,64 @@
+// Device-side description of a render scene, shared by the host layer
+// (skw_render_api.cpp) and the kernels (render.cu).  All pointers are
+// device pointers; arrays are in "mesh order": global triangle
+// g = prim_tri_offset[prim] + mesh triangle index.
+#pragma once
+
+#include <cstdint>
+
+namespace skw {
+
+enum BsdfKind : int32_t { kLambert = 0, kOrenNayar = 1, kPlastic = 2, kMetal = 3 };
+
+// Material constants after the reference's clamps (MatteMaterial.cpp:29-50,
+// PlasticMaterial.cpp:33-53, MetalMaterial.cpp:58-101).
+struct DevMaterial {
+  int32_t kind;
+  float kd[3];
+  float ks[3];
+  float exponent;      // Blinn exponent = 1 / clamp(roughness, 0.001, 1)
+  float on_a, on_b;    // Oren-Nayar A, B
+  float eta[3], k2[3]; // conductor refractive index and squared absorption
+};
+
+struct AreaLight {
+  float radiance[3];
+  float area;          // total area of the light's triangles
+  int32_t prim;
+  int32_t tri_begin;   // range in light_tri / light_cdf
+  int32_t tri_count;
+  int32_t pad;
+};
+
+struct PointLightDev {
+  float position[3];
+  float intensity[3];
+};
+
+struct SceneDev {
+  // geometry in mesh order
+  const float *vpos;          // 3 floats per global vertex (world)
+  const float *vnrm;          // 3 floats per global vertex (world shading normal), or null per prim
+  const int32_t *tri_vidx;    // 3 global vertex ids per global triangle
+  const float *tri_albedo;    // 3 floats per global triangle, NaN in [0] = use the material
+  const int32_t *prim_tri_offset;
+  const int32_t *prim_material;
+  const int32_t *prim_light;      // area light index or -1
+  const int32_t *prim_has_normals;
+  const DevMaterial *materials;
+  const AreaLight *area_lights;
+  int32_t n_area_lights;
+  const int32_t *light_tri;       // global triangle ids of all light triangles
+  const float *light_cdf;         // normalised cumulative area per light range
+  const PointLightDev *point_lights;
+  int32_t n_point_lights;
+  float scene_abs;                // largest absolute vertex coordinate
+};
+
+struct CameraDev {
+  double c2w[16];
+  double x_tan, y_tan;
+  int32_t width, height;
+};
+
+}  // namespace skw

@@ -19,18 +19,6 @@
 using skw::DevNode;
 using skw::DevTri;
 
-struct skw_accel {
-  skw_ctx *ctx = nullptr;
-  DevNode *d_nodes = nullptr;
-  DevTri *d_tris = nullptr;
-  unsigned *d_status = nullptr;
-  int stack_cap = 0;
-  float scene_abs = 0.0f;  // largest absolute vertex coordinate
-  skw_accel_info info{};
-  std::vector<DevNode> h_nodes;
-  std::vector<DevTri> h_tris;
-};
-
 namespace skw {
 
 int fail(skw_ctx *ctx, int code, const std::string &msg) {
@@ -246,7 +234,7 @@ static int run_query(skw_accel *a, bool closest, const skw_ray *rays, int64_t n,
   skw_ctx *ctx = a->ctx;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
-  e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, a->scene_abs, nullptr, out,
+  e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, nullptr, a->scene_abs, nullptr, out,
                             a->d_status, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, closest ? "closest-hit launch" : "any-hit launch");
   ctx->launches.fetch_add(1);

@@ -6,6 +6,10 @@
 #include <atomic>
 #include <cstdint>
 #include <string>
+#include <vector>
+
+#include "../../include/skw.h"
+#include "accel_build.h"
 
 struct skw_ctx {
   int device = 0;
@@ -15,6 +19,19 @@ struct skw_ctx {
   // Stream-ordered pool for per-call workspaces; it keeps freed memory
   // (release threshold = max) so repeated calls do not remap.
   cudaMemPool_t pool = nullptr;
+};
+
+// A device-resident accelerator (skw_accel_create / _from_flat).
+struct skw_accel {
+  skw_ctx *ctx = nullptr;
+  skw::DevNode *d_nodes = nullptr;
+  skw::DevTri *d_tris = nullptr;
+  unsigned *d_status = nullptr;
+  int stack_cap = 0;
+  float scene_abs = 0.0f;  // largest absolute vertex coordinate
+  skw_accel_info info{};
+  std::vector<skw::DevNode> h_nodes;
+  std::vector<skw::DevTri> h_tris;
 };
 
 namespace skw {

@@ -371,8 +371,9 @@ __device__ __forceinline__ void store_result(void *__restrict__ out, const int32
 template <int CAP, bool CLOSEST>
 __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, const float4 *__restrict__ rays,
-            int n, float scene_abs, const int32_t *__restrict__ out_index, void *__restrict__ out,
-            unsigned *__restrict__ status) {
+            int n, const int *__restrict__ n_dev, float scene_abs, const int32_t *__restrict__ out_index,
+            void *__restrict__ out, unsigned *__restrict__ status) {
+  if (n_dev) n = min(n, *n_dev);  // a queue whose length lives on the device
   constexpr int SCAP = Stack<CAP>::SCAP;
   __shared__ uint32_t s_a[SCAP][SKW_TRAV_BLOCK];
   __shared__ uint32_t s_b[SCAP][SKW_TRAV_BLOCK];
@@ -501,7 +502,8 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
 
 template <int CAP>
 cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const void *rays, int64_t n,
-                       float scene_abs, const int32_t *out_index, void *out, unsigned *status, cudaStream_t stream) {
+                       const int *n_dev, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
+                       cudaStream_t stream) {
   static int blocks_per_sm[2] = {0, 0}, sms = 0;
   const int which = closest ? 1 : 0;
   if (sms == 0) {
@@ -523,10 +525,10 @@ cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const 
   if (blocks > needed) blocks = needed;
   if (closest) {
     k_trace<CAP, true><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
-        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, scene_abs, out_index, out, status);
+        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, n_dev, scene_abs, out_index, out, status);
   } else {
     k_trace<CAP, false><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
-        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, scene_abs, out_index, out, status);
+        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, n_dev, scene_abs, out_index, out, status);
   }
   return cudaGetLastError();
 }
@@ -542,18 +544,18 @@ int traversal_stack_capacity(int max_depth) {
 }
 
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
-                             int64_t n, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
-                             cudaStream_t stream) {
+                             int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
+                             unsigned *status, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   switch (stack_cap) {
     case 48:
-      return launch_cap<48>(closest, nodes, tris, rays, n, scene_abs, out_index, out, status, stream);
+      return launch_cap<48>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream);
     case 96:
-      return launch_cap<96>(closest, nodes, tris, rays, n, scene_abs, out_index, out, status, stream);
+      return launch_cap<96>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream);
     case 192:
-      return launch_cap<192>(closest, nodes, tris, rays, n, scene_abs, out_index, out, status, stream);
+      return launch_cap<192>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream);
     default:
-      return launch_cap<416>(closest, nodes, tris, rays, n, scene_abs, out_index, out, status, stream);
+      return launch_cap<416>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream);
   }
 }
 

@@ -1,0 +1,158 @@
+"""Host-side mirror of the reference's direct-lighting render setup.
+
+``RenderPrimitive`` / ``Material`` / ``PointLight`` describe a scene like the
+reference's Primitive + Material + light sources; ``RenderScene`` builds it on
+the GPU (``Scene``, Raytracer/Core/Scene.h:107-113) and ``render_direct``
+renders an image the way ``SamplerBasedRenderer`` with a ``StratifiedSampler``,
+``DirectLightingLTEIntegrator``, pinhole ``PerspectiveCamera`` and a
+box-filtered ``ImageFilm`` does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .accel import Context, TriangleMesh, default_context
+
+MATTE, PLASTIC, METAL = 0, 1, 2
+
+
+@dataclass
+class Material:
+    kind: int = MATTE
+    kd: tuple = (0.5, 0.5, 0.5)
+    ks: tuple = (0.0, 0.0, 0.0)
+    roughness: float = 0.1
+    sigma: float = 0.0
+    eta: tuple = (1.0, 1.0, 1.0)
+    k: tuple = (0.0, 0.0, 0.0)
+
+
+@dataclass
+class RenderPrimitive:
+    mesh: TriangleMesh
+    material: int
+    mesh_to_world: np.ndarray | None = None
+    vertex_normals: np.ndarray | None = None
+    triangle_albedo: np.ndarray | None = None
+    emission: tuple = (0.0, 0.0, 0.0)
+
+
+@dataclass
+class PointLight:
+    position: tuple
+    intensity: tuple
+
+
+@dataclass
+class Camera:
+    camera_to_world: np.ndarray
+    x_view_angle: float
+    width: int
+    height: int
+
+    @staticmethod
+    def look_at(eye, target, up, x_view_angle, width, height) -> "Camera":
+        """Camera x -> image right, camera y -> image down, camera z -> forward."""
+        eye, target, up = (np.asarray(v, np.float64) for v in (eye, target, up))
+        f = target - eye
+        f /= np.linalg.norm(f)
+        r = np.cross(f, up)
+        r /= np.linalg.norm(r)
+        d = np.cross(f, r)
+        m = np.eye(4)
+        m[:3, 0], m[:3, 1], m[:3, 2], m[:3, 3] = r, d, f, eye
+        return Camera(m, float(x_view_angle), int(width), int(height))
+
+
+class skw_material(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("roughness", C.c_float),
+                ("sigma", C.c_float), ("eta", C.c_float * 3), ("k", C.c_float * 3)]
+
+
+class skw_render_primitive(C.Structure):
+    _fields_ = [("mesh", C.c_int32), ("mesh_to_world", C.c_void_p), ("material", C.c_int32),
+                ("vertex_normals", C.c_void_p), ("triangle_albedo", C.c_void_p), ("emission", C.c_float * 3)]
+
+
+class skw_point_light(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("intensity", C.c_float * 3)]
+
+
+class skw_camera(C.Structure):
+    _fields_ = [("camera_to_world", C.c_double * 16), ("x_view_angle", C.c_double), ("width", C.c_int32),
+                ("height", C.c_int32)]
+
+
+class skw_render_params(C.Structure):
+    _fields_ = [("spp_x", C.c_int32), ("spp_y", C.c_int32), ("light_samples", C.c_int32), ("seed", C.c_uint64)]
+
+
+def c_material(m: Material) -> skw_material:
+    return skw_material(m.kind, (C.c_float * 3)(*m.kd), (C.c_float * 3)(*m.ks), m.roughness, m.sigma,
+                        (C.c_float * 3)(*m.eta), (C.c_float * 3)(*m.k))
+
+
+def c_camera(cam: Camera) -> skw_camera:
+    return skw_camera((C.c_double * 16)(*np.asarray(cam.camera_to_world, np.float64).reshape(-1)), cam.x_view_angle,
+                      cam.width, cam.height)
+
+
+def c_prims(prims: list[RenderPrimitive]):
+    """(skw_mesh array, skw_render_primitive array, keep-alive list)."""
+    keep, meshes, mesh_ids = [], [], {}
+    for p in prims:
+        if id(p.mesh) not in mesh_ids:
+            mesh_ids[id(p.mesh)] = len(meshes)
+            meshes.append(p.mesh)
+    cm = (_lib.skw_mesh * max(len(meshes), 1))()
+    for i, m in enumerate(meshes):
+        cm[i] = _lib.skw_mesh(m.vertices.ctypes.data, m.vertices.shape[0], m.triangles.ctypes.data, m.triangles.shape[0])
+    cp = (skw_render_primitive * max(len(prims), 1))()
+    for i, p in enumerate(prims):
+        xf = None if p.mesh_to_world is None else np.ascontiguousarray(p.mesh_to_world, np.float64).reshape(4, 4)
+        vn = None if p.vertex_normals is None else np.ascontiguousarray(p.vertex_normals, np.float32).reshape(-1, 3)
+        ta = None if p.triangle_albedo is None else np.ascontiguousarray(p.triangle_albedo, np.float32).reshape(-1, 3)
+        keep += [xf, vn, ta]
+        cp[i] = skw_render_primitive(mesh_ids[id(p.mesh)], None if xf is None else xf.ctypes.data, p.material,
+                                     None if vn is None else vn.ctypes.data, None if ta is None else ta.ctypes.data,
+                                     (C.c_float * 3)(*p.emission))
+    return cm, len(meshes), cp, keep
+
+
+class RenderScene:
+    def __init__(self, prims: list[RenderPrimitive], materials: list[Material], point_lights=(),
+                 ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        lib = _lib.load()
+        cm, nm, cp, self._keep = c_prims(prims)
+        mats = (skw_material * max(len(materials), 1))(*[c_material(m) for m in materials])
+        pls = (skw_point_light * max(len(point_lights), 1))(
+            *[skw_point_light((C.c_float * 3)(*l.position), (C.c_float * 3)(*l.intensity)) for l in point_lights])
+        h = C.c_void_p()
+        _lib.check(lib.skw_scene_create(self.ctx.handle, cm, nm, cp, len(prims), mats, len(materials), pls,
+                                        len(point_lights), C.byref(h)), self.ctx.handle)
+        self.handle = h
+        self.prims, self.materials, self.point_lights = prims, materials, list(point_lights)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            _lib.load().skw_scene_destroy(h)
+            self.handle = None
+
+    def render_direct(self, camera: Camera, spp_x: int = 2, spp_y: int = 2, light_samples: int = 1, seed: int = 0,
+                      out=None, stream=None):
+        """Renders into a CUDA float32 tensor (height, width, 3) and returns it."""
+        import torch
+        if out is None:
+            out = torch.empty((camera.height, camera.width, 3), dtype=torch.float32, device="cuda")
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        cam = c_camera(camera)
+        par = skw_render_params(spp_x, spp_y, light_samples, seed)
+        _lib.check(_lib.load().skw_render_direct(self.handle, C.byref(cam), C.byref(par), out.data_ptr(), s),
+                   self.ctx.handle)
+        return out

@@ -144,3 +144,62 @@ def scene_bounds(meshes) -> tuple[np.ndarray, np.ndarray]:
     lo = np.min([v.min(0) for v, _ in meshes], axis=0)
     hi = np.max([v.max(0) for v, _ in meshes], axis=0)
     return lo.astype(np.float64), hi.astype(np.float64)
+
+
+# ------------------------------------------------------------ render scenes --
+
+def _box_inward(lo=-1.0, hi=1.0):
+    """Closed axis-aligned box of 12 triangles whose geometric normals
+    ((v1 - v0) x (v2 - v0)) point into the box."""
+    c = np.array([[x, y, z] for x in (lo, hi) for y in (lo, hi) for z in (lo, hi)], np.float32)
+    idx = lambda x, y, z: x * 4 + y * 2 + z  # noqa: E731
+    faces = [  # quad corners; the normal noted is the inward one
+        [idx(0, 0, 0), idx(0, 0, 1), idx(0, 1, 1), idx(0, 1, 0)],  # x = lo, normal +x
+        [idx(1, 0, 0), idx(1, 1, 0), idx(1, 1, 1), idx(1, 0, 1)],  # x = hi, normal -x
+        [idx(0, 0, 0), idx(1, 0, 0), idx(1, 0, 1), idx(0, 0, 1)],  # y = lo, normal +y
+        [idx(0, 1, 0), idx(0, 1, 1), idx(1, 1, 1), idx(1, 1, 0)],  # y = hi, normal -y
+        [idx(0, 0, 0), idx(0, 1, 0), idx(1, 1, 0), idx(1, 0, 0)],  # z = lo, normal +z
+        [idx(0, 0, 1), idx(1, 0, 1), idx(1, 1, 1), idx(0, 1, 1)],  # z = hi, normal -z
+    ]
+    tris = []
+    for a, b, cc, d in faces:  # listed outward-facing; reversed to face inward
+        tris += [[a, cc, b], [a, d, cc]]
+    return c, np.array(tris, np.int32)
+
+
+def _jittered_sphere(subdivisions, center, radius, rng, jitter=0.01):
+    v, t = sphere_mesh(subdivisions)
+    r = radius * (1.0 + rng.uniform(-jitter, jitter, size=(v.shape[0], 1)))
+    return (v * r + np.asarray(center)).astype(np.float32), t, v.astype(np.float32)
+
+
+def direct_lighting_box(seed: int = 1, sphere_subdivisions=(6, 5)):
+    """The plain direct-lighting configuration: a closed box of 12 triangles
+    (matte walls, per-wall albedo uniform in [0.2, 0.8], seed+1), two
+    tessellated spheres (4*4^6 + 4*4^5 = 20,480 triangles, radius jittered by
+    +-1 %, plastic Kd 0.5 Ks 0.3 roughness 0.1, shading normals from the
+    sphere), and a 2-triangle quad area light of radiance 10 under the
+    ceiling.  Returns (prims, materials, camera-at(width, height) factory)."""
+    from .accel import TriangleMesh
+    from .render import Camera, Material, PLASTIC, RenderPrimitive
+    rng = np.random.default_rng(seed)
+    arng = np.random.default_rng(seed + 1)
+    bv, bt = _box_inward()
+    wall = arng.uniform(0.2, 0.8, size=(6, 3)).astype(np.float32)
+    albedo = np.repeat(wall, 2, axis=0)
+    s1v, s1t, s1n = _jittered_sphere(sphere_subdivisions[0], (-0.35, -0.6, 0.25), 0.38, rng)
+    s2v, s2t, s2n = _jittered_sphere(sphere_subdivisions[1], (0.45, -0.68, -0.2), 0.3, rng)
+    lv = np.array([[-0.3, 0.98, -0.3], [0.3, 0.98, -0.3], [0.3, 0.98, 0.3], [-0.3, 0.98, 0.3]], np.float32)
+    lt = np.array([[0, 1, 2], [0, 2, 3]], np.int32)  # normal (v1-v0)x(v2-v0) = -y: emits downwards
+    materials = [Material(kd=(0.5, 0.5, 0.5)),  # walls (per-triangle albedo overrides kd)
+                 Material(kind=PLASTIC, kd=(0.5, 0.5, 0.5), ks=(0.3, 0.3, 0.3), roughness=0.1),
+                 Material(kd=(0.0, 0.0, 0.0))]   # the light's own surface
+    prims = [RenderPrimitive(TriangleMesh(bv, bt), 0, triangle_albedo=albedo),
+             RenderPrimitive(TriangleMesh(s1v, s1t), 1, vertex_normals=s1n),
+             RenderPrimitive(TriangleMesh(s2v, s2t), 1, vertex_normals=s2n),
+             RenderPrimitive(TriangleMesh(lv, lt), 2, emission=(10.0, 10.0, 10.0))]
+
+    def camera(width=256, height=256):
+        return Camera.look_at((0.0, 0.1, -0.95), (0.0, -0.3, 1.0), (0.0, 1.0, 0.0), np.radians(75.0), width, height)
+
+    return prims, materials, camera

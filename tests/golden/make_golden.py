@@ -67,10 +67,28 @@ def direction_golden():
     np.savez_compressed(OUT / "compressed_direction.npz", ids=sample, vectors=tab[sample])
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and len(sys.argv) == 1:
     if build_ref.build() is None:
         sys.exit("the reference sources are needed to generate the golden fixtures")
     accel_golden()
     knn_golden()
     direction_golden()
     print("golden fixtures written to", OUT)
+
+
+def render_golden():
+    """Reference renders of the plain direct-lighting box at 64 x 64: 2x2 spp
+    (the noise level at the configuration's sample count) and 16x16 spp (the
+    comparison image)."""
+    from skwarka_gb300 import scenes
+    prims, mats, cam = scenes.direct_lighting_box()
+    c = cam(64, 64)
+    ref = Reference()
+    lo, _ = ref.render_direct(prims, mats, [], c, 2, 2)
+    hi, _ = ref.render_direct(prims, mats, [], c, 16, 16)
+    np.savez_compressed(OUT / "direct_box_64.npz", ref_2x2=lo, ref_16x16=hi)
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "render":
+    render_golden()
+    print("render golden written")
