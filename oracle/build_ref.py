@@ -33,6 +33,7 @@ Usage: ``python oracle/build_ref.py`` (idempotent; rebuilds changed files).
 """
 from __future__ import annotations
 
+import hashlib
 import os
 import re
 import shutil
@@ -136,11 +137,18 @@ def build(verbose: bool = False) -> Path | None:
     if not (SRC / ".staged").exists():
         return None
     make_shims()
+    # The objects depend on the flags and on every shim header: a change to
+    # either rebuilds everything.
+    digest = hashlib.sha256(" ".join(CXXFLAGS).encode())
+    for p in sorted((HERE / "ref_shims").rglob("*")):
+        if p.is_file():
+            digest.update(str(p.relative_to(HERE)).encode() + p.read_bytes())
+    stamp_text = digest.hexdigest()
     flags_stamp = OBJ / ".flags"
-    if OBJ.exists() and (not flags_stamp.exists() or flags_stamp.read_text() != " ".join(CXXFLAGS)):
+    if OBJ.exists() and (not flags_stamp.exists() or flags_stamp.read_text() != stamp_text):
         shutil.rmtree(OBJ)
     OBJ.mkdir(parents=True, exist_ok=True)
-    flags_stamp.write_text(" ".join(CXXFLAGS))
+    flags_stamp.write_text(stamp_text)
     srcs = _sources()
     jobs = [(s, OBJ / (str(s.relative_to(SRC)).replace("/", "__") + ".o"), []) for s in srcs]
     jobs.append((HERE / "ref_driver.cpp", OBJ / "ref_driver.o", []))

@@ -87,6 +87,11 @@ def render_golden():
     lo, _ = ref.render_direct(prims, mats, [], c, 2, 2)
     hi, _ = ref.render_direct(prims, mats, [], c, 16, 16)
     np.savez_compressed(OUT / "direct_box_64.npz", ref_2x2=lo, ref_16x16=hi)
+    # One plane per BSDF under an area light and under a point light, 16x16 spp.
+    planes = {}
+    for name, (p, m, pl, c) in sf.material_plane_scenes().items():
+        planes[name], _ = ref.render_direct(p, m, pl, c, 16, 16)
+    np.savez_compressed(OUT / "direct_planes.npz", **planes)
 
 
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "render":

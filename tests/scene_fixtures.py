@@ -69,3 +69,112 @@ def canonical_leaf_order(info, tri_prim, tri_index):
         seg = pairs[b:e]
         out[b:e] = seg[np.lexsort((seg[:, 1], seg[:, 0]))]
     return out
+
+
+def material_plane_scenes():
+    """One 10 x 10 plane under a 0.6 x 0.6 area light of radiance 10 at height 1
+    (and, separately, under a point light of intensity 3), for each BSDF the
+    direct-lighting path supports.  Returns {name: (prims, materials,
+    point_lights, camera)}; a 24 x 16 camera looks down at the lit region at
+    about 35 degrees, so glossy lobes reflect the light."""
+    from skwarka_gb300.accel import TriangleMesh
+    from skwarka_gb300.render import METAL, PLASTIC, Camera, Material, PointLight, RenderPrimitive
+    s, a = 5.0, 0.6
+    plane = TriangleMesh(np.array([[-s, -s, 0], [s, -s, 0], [s, s, 0], [-s, s, 0]], np.float32),
+                         np.array([[0, 1, 2], [0, 2, 3]], np.int32))
+    light = TriangleMesh(np.array([[-a / 2, -a / 2, 1], [a / 2, -a / 2, 1], [a / 2, a / 2, 1], [-a / 2, a / 2, 1]],
+                                  np.float32), np.array([[0, 2, 1], [0, 3, 2]], np.int32))  # emits towards -z
+    cam = Camera.look_at((1.2, 0.3, 0.9), (-0.2, 0.0, 0.0), (0, 0, 1), np.radians(50.0), 24, 16)
+    copper = dict(eta=(0.2, 0.9, 1.1), k=(3.9, 2.4, 2.2))
+    mats = {
+        "matte": Material(kd=(0.8, 0.6, 0.4)),
+        "oren_nayar": Material(kd=(0.8, 0.6, 0.4), sigma=20.0),
+        "plastic": Material(kind=PLASTIC, kd=(0.4, 0.3, 0.2), ks=(0.5, 0.5, 0.5), roughness=0.1),
+        "plastic_rough": Material(kind=PLASTIC, kd=(0.4, 0.3, 0.2), ks=(0.5, 0.5, 0.5), roughness=0.6),
+        "metal": Material(kind=METAL, roughness=0.05, **copper),
+        "metal_rough": Material(kind=METAL, roughness=0.5, **copper),
+    }
+    out = {}
+    for name, m in mats.items():
+        out["area_" + name] = ([RenderPrimitive(plane, 0), RenderPrimitive(light, 1, emission=(10.0, 10.0, 10.0))],
+                               [m, Material(kd=(0.0, 0.0, 0.0))], [], cam)
+        out["point_" + name] = ([RenderPrimitive(plane, 0)], [m], [PointLight((0.1, -0.2, 0.8), (3.0, 3.0, 3.0))], cam)
+    return out
+
+
+def _ray_mesh_hit(o, d, v, t):
+    """Closest hit of one ray with a triangle mesh (float64 Moller-Trumbore):
+    (point, unit geometric normal facing the ray origin)."""
+    a, b, c = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
+    e1, e2 = b - a, c - a
+    p = np.cross(d, e2)
+    det = (e1 * p).sum(1)
+    ok = np.abs(det) > 1e-14
+    inv = np.where(ok, 1.0 / np.where(ok, det, 1.0), 0.0)
+    s = o - a
+    u = (s * p).sum(1) * inv
+    q = np.cross(s, e1)
+    w = (q * d).sum(1) * inv
+    tt = (e2 * q).sum(1) * inv
+    hit = ok & (u >= 0) & (w >= 0) & (u + w <= 1) & (tt > 0)
+    i = int(np.argmin(np.where(hit, tt, np.inf)))
+    n = np.cross(e1[i], e2[i])
+    n /= np.linalg.norm(n)
+    if np.dot(n, d) > 0:
+        n = -n
+    return o + tt[i] * d, n
+
+
+def sphere_area_lights_case():
+    """Analogue of the reference's DirectLightingIntegrator area-light test
+    (UnitTests/MainTests/Raytracer/Core/DirectLightingIntegrator.test.h:104-135):
+    unit spheres at the origin (white Lambertian), at (10,0,0) (emitting 10)
+    and at (0,10,0) (emitting 20); the point seen from (5,5,0) towards the
+    origin.  Its radiance is sum_i L_i/pi * integral of cos over the sphere's
+    cone, and for a cone of half-angle beta fully above the horizon that
+    integral is pi sin^2(beta) cos(alpha).  Returns (prims, materials, camera,
+    expected radiance)."""
+    from skwarka_gb300.accel import TriangleMesh
+    from skwarka_gb300.render import Camera, Material, RenderPrimitive
+    v, t = scenes.sphere_mesh(6)
+    a, b, c = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
+    outward = (np.cross(b - a, c - a) * (a + b + c)).sum(1) > 0
+    t = np.where(outward[:, None], t, t[:, [0, 2, 1]]).astype(np.int32)
+    centers, radiance = [(0.0, 0.0, 0.0), (10.0, 0.0, 0.0), (0.0, 10.0, 0.0)], [0.0, 10.0, 20.0]
+    prims = [RenderPrimitive(TriangleMesh((v + np.asarray(cc)).astype(np.float32), t), 0 if i == 0 else 1,
+                             emission=(radiance[i],) * 3) for i, cc in enumerate(centers)]
+    mats = [Material(kd=(1.0, 1.0, 1.0)), Material(kd=(0.0, 0.0, 0.0))]
+    eye = np.array([5.0, 5.0, 0.0])
+    d = -eye / np.linalg.norm(eye)
+    p, n = _ray_mesh_hit(eye, d, v.astype(np.float32).astype(np.float64), t)
+    want = 0.0
+    for cc, le in zip(centers[1:], radiance[1:]):
+        to_c = np.asarray(cc) - p
+        dist = np.linalg.norm(to_c)
+        want += le / np.pi * np.pi * (1.0 / dist) ** 2 * np.dot(n, to_c / dist)
+    cam = Camera.look_at(tuple(eye), (0.0, 0.0, 0.0), (0, 0, 1), 1e-5, 2, 2)
+    return prims, mats, cam, float(want)
+
+
+def square_light_case(a=0.6, h=1.0, p=(0.3, 0.2)):
+    """A white Lambertian plane z=0 under an a x a square light of radiance 10
+    at height h facing down; the point p on the plane is seen by a camera of
+    tiny field of view.  The expected radiance rho/pi * E is the irradiance E
+    integrated numerically over the light (2000^2 midpoint rule).  Returns
+    (prims, materials, camera, expected radiance)."""
+    from skwarka_gb300.accel import TriangleMesh
+    from skwarka_gb300.render import Camera, Material, RenderPrimitive
+    s = 5.0
+    plane = TriangleMesh(np.array([[-s, -s, 0], [s, -s, 0], [s, s, 0], [-s, s, 0]], np.float32),
+                         np.array([[0, 1, 2], [0, 2, 3]], np.int32))
+    light = TriangleMesh(np.array([[-a / 2, -a / 2, h], [a / 2, -a / 2, h], [a / 2, a / 2, h], [-a / 2, a / 2, h]],
+                                  np.float32), np.array([[0, 2, 1], [0, 3, 2]], np.int32))
+    prims = [RenderPrimitive(plane, 0), RenderPrimitive(light, 1, emission=(10.0, 10.0, 10.0))]
+    mats = [Material(kd=(1.0, 1.0, 1.0)), Material(kd=(0.0, 0.0, 0.0))]
+    n = 2000
+    xs = (np.arange(n) + 0.5) / n * a - a / 2
+    x, y = np.meshgrid(xs - p[0], xs - p[1])
+    r2 = x * x + y * y + h * h
+    e = 10.0 * (h * h / (r2 * r2)).sum() * (a / n) ** 2
+    cam = Camera.look_at((p[0], p[1], 0.5), (p[0], p[1], 0.0), (0, 1, 0), 1e-3, 2, 2)
+    return prims, mats, cam, float(e / np.pi)

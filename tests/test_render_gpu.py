@@ -2,12 +2,23 @@
 reference's own DirectLightingIntegrator / SamplerBasedRenderer test cases)
 and statistical image parity with the reference's CPU render.
 
-Image parity: the reference's multithreaded render is not deterministic (its
-random streams depend on thread scheduling), so images are compared by mean
-relative error (MRE) of pixel luminance against the reference's high-sample
-render: at the configuration's 2x2 samples the GPU image's MRE must be within
-15 % (+0.005) of the reference's own MRE at 2x2, and at 16x16 samples the two
-images must agree to MRE <= 0.03."""
+Image parity: the GPU draws its own random numbers (a counter-based
+generator, not the reference's per-chunk Mersenne Twister streams), so images
+are compared statistically against the reference's
+16x16-sample render (tests/golden/direct_box_64.npz):
+
+* noise level: at the configuration's 2x2 samples the GPU image's mean
+  relative error (MRE) of pixel luminance must be within 15 % (+0.005) of the
+  reference's own 2x2 MRE;
+* convergence: at 16x16 samples the GPU MRE must fall to at most 0.3 of the
+  2x2 noise level (independent noise of two 16x16 images gives about 0.2);
+* bias: mean luminance within 1 %, and every 8x8-pixel block's mean luminance
+  within 3 % (relative to the block's mean, or to a quarter of the image mean
+  for blocks in shadow, whose relative noise is large).
+
+Per-BSDF parity (tests/golden/direct_planes.npz): a plane of each material
+under an area light and under a point light; GPU mean luminance at 32x32
+samples within 2 % of the reference's at 16x16."""
 from pathlib import Path
 
 import numpy as np
@@ -66,6 +77,12 @@ def test_point_light_inside_sphere(gpu):
     assert np.allclose(img, want, rtol=0.02), (img.min(), img.max(), want)
 
 
+def _block_means(img, b=8):
+    lum = img @ LUM
+    h, w = lum.shape
+    return lum[: h // b * b, : w // b * b].reshape(h // b, b, w // b, b).mean(axis=(1, 3))
+
+
 def test_box_image_parity_with_reference(gpu):
     g = np.load(GOLD / "direct_box_64.npz")
     prims, mats, cam = scenes.direct_lighting_box()
@@ -75,11 +92,27 @@ def test_box_image_parity_with_reference(gpu):
     gpu_hi = sc.render_direct(c, 16, 16, seed=12).cpu().numpy()
     ref_lo, ref_hi = g["ref_2x2"], g["ref_16x16"]
     e_ref, e_gpu, e_hi = mre(ref_lo, ref_hi), mre(gpu_lo, ref_hi), mre(gpu_hi, ref_hi)
+    m_ref, m_gpu = float((ref_hi @ LUM).mean()), float((gpu_hi @ LUM).mean())
+    rb = _block_means(ref_hi)
+    blocks = np.abs(_block_means(gpu_hi) - rb) / np.maximum(rb, 0.25 * m_ref)
     print(f"[box 64x64] MRE vs reference 16x16: reference 2x2 {e_ref:.4f}, GPU 2x2 {e_gpu:.4f}, GPU 16x16 {e_hi:.4f}; "
-          f"mean luminance ref {ref_hi.mean():.4f} gpu {gpu_hi.mean():.4f}")
-    assert e_gpu <= 1.15 * e_ref + 0.005
-    assert e_hi <= 0.03
+          f"mean luminance ref {m_ref:.5f} gpu {m_gpu:.5f}; worst 8x8 block {blocks.max():.4f}")
     assert np.isfinite(gpu_lo).all() and (gpu_lo >= 0).all()
+    assert e_gpu <= 1.15 * e_ref + 0.005
+    assert e_hi <= 0.3 * e_ref
+    assert abs(m_gpu / m_ref - 1.0) <= 0.01
+    assert blocks.max() <= 0.03
+
+
+@pytest.mark.parametrize("name", sorted(np.load(GOLD / "direct_planes.npz").files))
+def test_bsdf_plane_parity_with_reference(gpu, name):
+    import scene_fixtures as sf
+    prims, mats, lights, cam = sf.material_plane_scenes()[name]
+    ref = np.load(GOLD / "direct_planes.npz")[name]
+    img = RenderScene(prims, mats, lights).render_direct(cam, 32, 32, seed=3).cpu().numpy()
+    m_ref, m_gpu = float((ref @ LUM).mean()), float((img @ LUM).mean())
+    print(f"[{name}] mean luminance ref {m_ref:.5f} gpu {m_gpu:.5f}")
+    assert abs(m_gpu / m_ref - 1.0) <= 0.02
 
 
 def test_render_is_deterministic(gpu):
@@ -89,3 +122,25 @@ def test_render_is_deterministic(gpu):
     a = sc.render_direct(c, 2, 2, seed=5).cpu().numpy()
     b = sc.render_direct(c, 2, 2, seed=5).cpu().numpy()
     assert np.array_equal(a, b)
+
+
+def test_sphere_area_lights_known_answer(gpu):
+    """DirectLightingIntegrator.test.h:104-135 analogue: two spherical area
+    lights (radiance 10 and 20) seen from a Lambertian point; the GPU estimate
+    at 64x64 samples per pixel agrees with the closed form within 2 %."""
+    import scene_fixtures as sf
+    prims, mats, cam, want = sf.sphere_area_lights_case()
+    img = RenderScene(prims, mats).render_direct(cam, 64, 64, seed=7).cpu().numpy()
+    print(f"[sphere lights] gpu {img.mean():.5f} closed form {want:.5f}")
+    assert abs(img.mean() / want - 1.0) <= 0.02
+
+
+def test_square_light_known_answer(gpu):
+    """A point under a square area light: the GPU estimate at 32x32 samples
+    per pixel, one light sample each, agrees with the numerical integral of
+    the irradiance within 1 %."""
+    import scene_fixtures as sf
+    prims, mats, cam, want = sf.square_light_case()
+    img = RenderScene(prims, mats).render_direct(cam, 32, 32, seed=9).cpu().numpy()
+    print(f"[square light] gpu {img.mean():.5f} integral {want:.5f}")
+    assert abs(img.mean() / want - 1.0) <= 0.01
