@@ -56,6 +56,7 @@ def parse():
     p.add_argument("--nrandom", type=int, default=50_000)
     p.add_argument("--cpu-sample", type=int, default=1_000_000, help="rays in one CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-render", action="store_true", help="skip the direct-lighting render measurement")
     return p.parse_args()
 
 
@@ -117,6 +118,14 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+_T0 = time.perf_counter()
+
+
+def log(msg: str) -> None:
+    """Progress on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:7.1f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def load_traffic(kind: str, rays: int):
     """DRAM bytes per launch from the committed ncu summary, scaled to `rays`."""
     p = ROOT / "profiles" / "traffic.json"
@@ -152,6 +161,59 @@ def cpu_baseline(meshes, rays, sample, rank):
     return {"value": sample / dt / 1e6, "unit": UNIT, "cores": cores, "kind": kind,
             "sample": f"{sample} of the step's rays, TriangleAccelerator::Intersect incl. differential geometry"
             if kind == "reference" else f"{sample} of the step's rays, oracle restatement"}, (n_nodes, n_tris)
+
+
+def render_bench(args, dev, ctx, measure_cpu):
+    """Plain direct lighting (256 x 256, 2x2 stratified samples, one light
+    sample per hit, the 12-triangle box + 20,480-triangle spheres + quad
+    light): samples/s of the GPU wavefront renderer on the device and end to
+    end (film copied to pinned host memory), next to the reference's
+    SamplerBasedRenderer on the host cores."""
+    import torch
+    from skwarka_gb300 import scenes
+    from skwarka_gb300.render import RenderScene
+    prims, mats, camf = scenes.direct_lighting_box()
+    cam = camf(256, 256)
+    spp = 4
+    samples = cam.width * cam.height * spp
+    sc = RenderScene(prims, mats, ctx=ctx)
+    film = torch.empty((cam.height, cam.width, 3), dtype=torch.float32, device=dev)
+    hfilm = torch.empty((cam.height, cam.width, 3), dtype=torch.float32).pin_memory()
+    stream = torch.cuda.current_stream(dev)
+    for i in range(max(3, args.warmup)):
+        sc.render_direct(cam, 2, 2, seed=i, out=film)
+    torch.cuda.synchronize()
+    steps = max(5, args.steps)
+    l0 = ctx.launch_count()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for i in range(steps):
+        sc.render_direct(cam, 2, 2, seed=100 + i, out=film)
+    e.record(stream)
+    torch.cuda.synchronize()
+    dev_ms = s.elapsed_time(e) / steps
+    launches = (ctx.launch_count() - l0) / steps
+    t0 = time.perf_counter()
+    for i in range(steps):
+        sc.render_direct(cam, 2, 2, seed=200 + i, out=film)
+        hfilm.copy_(film, non_blocking=True)
+        stream.synchronize()
+    e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+    out = {"workload": "direct lighting, 256x256, 2x2 spp, 1 light sample, box + 20,480-tri spheres + quad light",
+           "unit": "Msamples/s", "value": samples / dev_ms / 1e3, "ms_per_frame": dev_ms,
+           "e2e": {"value": samples / e2e_ms / 1e3, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": hfilm.numel() * 4},
+           "gpu_launches_per_frame": launches}
+    if measure_cpu:
+        from oracle.api import Reference
+        if Reference.available():
+            log("reference render")
+            ref = Reference()
+            ref.render_direct(prims, mats, [], camf(64, 64), 2, 2)
+            _, sec = ref.render_direct(prims, mats, [], cam, 2, 2)
+            out["cpu_baseline"] = {"value": samples / sec / 1e6, "unit": "Msamples/s", "cores": os.cpu_count() or 1,
+                                   "kind": "reference", "sample": "one full 256x256 4-spp frame, SamplerBasedRenderer"}
+    return out
 
 
 def run_reference(args):
@@ -208,6 +270,7 @@ def main():
     from skwarka_gb300 import scenes
     from skwarka_gb300.accel import Context, Primitive, TriangleAccelerator, TriangleMesh
 
+    log("building the ray-query scene")
     meshes = scenes.ray_query_scene(args.subdiv, args.nrandom, seed=3)
     lo, hi = scenes.scene_bounds(meshes)
     rays_np = scenes.uniform_rays(args.rays, lo, hi, seed=7 + 1000 * rank)
@@ -224,6 +287,7 @@ def main():
         _lib.check(lib.skw_intersect(acc.handle, rays.data_ptr(), args.rays, hits.data_ptr(), stream.cuda_stream),
                    ctx.handle)
 
+    log("accelerator built; warm-up")
     for _ in range(args.warmup):
         flush.fill_(1.0)
         step()
@@ -250,6 +314,7 @@ def main():
     total_s = float(total_ms.item()) / 1e3
     value = args.rays * args.steps * world / total_s / 1e6
 
+    log("closest-hit timed; end-to-end")
     # End to end through the host-buffer entry point (copies included).
     hrays = torch.from_numpy(rays_np).pin_memory()
     hhits = torch.empty((args.rays, 4), dtype=torch.int32).pin_memory()
@@ -266,6 +331,7 @@ def main():
         dist.all_reduce(e2e_s, op=dist.ReduceOp.MAX)
     e2e = args.rays * e2e_steps * world / float(e2e_s.item()) / 1e6
 
+    log("any-hit")
     # Any-hit throughput (shadow rays, tmax ~ U[0, 2]) for the record.
     srays = torch.from_numpy(scenes.uniform_rays(args.rays, lo, hi, seed=8 + 1000 * rank, tmax_range=(0, 2))).to(dev)
     occ = torch.empty(args.rays, dtype=torch.uint8, device=dev)
@@ -291,7 +357,12 @@ def main():
     cpu = None
     n_nodes, n_tris = None, None
     if not args.no_cpu_baseline and world == 1:
+        log("CPU baseline (reference Intersect)")
         cpu, (n_nodes, n_tris) = cpu_baseline(meshes, rays_np, min(args.cpu_sample, args.rays), rank)
+    render = None
+    if not args.no_render:
+        log("direct-lighting render")
+        render = render_bench(args, dev, ctx, measure_cpu=not args.no_cpu_baseline and world == 1)
     peak, peak_kind = peaks()
     per_launch_s = sum(kern_ms) / len(kern_ms) / 1e3
     roofline = None
@@ -310,7 +381,7 @@ def main():
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": args.rays * 32,
                     "d2h_bytes_per_step": args.rays * 16},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,
-            "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit,
+            "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit, "render": render,
             "accel": {k: acc.info[k] for k in ("n_nodes", "max_depth", "build_ms", "device_bytes")}}
     print(json.dumps(line), flush=True)
     if world > 1:

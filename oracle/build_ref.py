@@ -53,8 +53,11 @@ SUBDIRS = ("Common", "Math", "Raytracer", "Shapes")
 EXCLUDE = {"ImageEnvironmentalLight.cpp", "RGBImageSource.cpp", "TranslucentMaterial.cpp", "dllmain.cpp"}
 # -ffp-contract=off: no fused multiply-add, so that an aarch64 build rounds
 # exactly like the x86-64 (SSE2) build the reference targets.
+# -fsigned-char: the reference counts down with `char` loop indices
+# (Math/Matrix4x4.h:305, `for (char j=3;j>=0;--j)`), which never ends where
+# plain char is unsigned (aarch64); x86-64 char is signed.
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-fpermissive", "-w", "-DNDEBUG", "-DNOMINMAX", "-pthread",
-            "-ffp-contract=off"]
+            "-ffp-contract=off", "-fsigned-char"]
 
 
 def _rewrite(path: Path) -> None:
