@@ -302,6 +302,51 @@ typedef struct skw_render_params {
 int skw_render_direct(skw_scene *scene, const skw_camera *camera, const skw_render_params *params, float *film_rgb,
                       void *stream);
 
+/* ---- Batched multi-view render (no counterpart in the reference, whose
+ * SamplerBasedRenderer::Render renders one camera per call; the batch is the
+ * same estimator as skw_render_direct for every view). ---------------------
+ *
+ * A batch renders n_views cameras of one scene, each with its own film size,
+ * as one wavefront: the views' pixels are concatenated and processed in
+ * passes of up to samples_per_pass samples, alternating between two
+ * workspaces so that consecutive passes overlap on the GPU.  The whole
+ * sequence of passes is captured once into a CUDA graph and each run is a
+ * single graph launch.  View v renders exactly what skw_render_direct renders
+ * for that camera with seed = view_seeds[v] (params->seed + v when
+ * view_seeds is NULL): images are bit-identical to per-view calls. */
+typedef struct skw_render_batch skw_render_batch;
+
+typedef struct skw_batch_config {
+  int64_t samples_per_pass;    /* wavefront queue capacity (samples in flight per workspace) */
+  int32_t stack_cap;           /* traversal stack entries: 48, 96, 192 or 416, at least the tree's need */
+  int32_t trace_ctas_per_sm;   /* persistent traversal CTAs per SM, 0 = as many as fit */
+  int32_t shade_block;         /* threads per CTA of the shading kernel: 64 or 128 */
+  int32_t overlap;             /* 1 = two workspaces on two graph branches, 0 = one */
+} skw_batch_config;
+
+/* cfg may be NULL (defaults).  The batch owns its device workspace. */
+int skw_render_batch_create(skw_scene *scene, const skw_camera *cameras, int32_t n_views,
+                            const skw_render_params *params, const uint64_t *view_seeds,
+                            const skw_batch_config *cfg, skw_render_batch **out);
+void skw_render_batch_destroy(skw_render_batch *batch);
+/* Floats needed for all views' films, and view v's offset (in floats) into
+ * the packed film buffer: view v occupies height_v x width_v x 3 floats. */
+int64_t skw_render_batch_film_floats(const skw_render_batch *batch);
+int64_t skw_render_batch_film_offset(const skw_render_batch *batch, int32_t view);
+int skw_render_batch_get_config(const skw_render_batch *batch, skw_batch_config *out);
+/* Renders every view into films (device, packed as above), stream-ordered
+ * after the work already queued on stream.  The first run with a given films
+ * pointer captures the graph; later runs replay it. */
+int skw_render_batch_run(skw_render_batch *batch, float *films, void *stream);
+/* Autotuner: times candidate configurations of this batch on the GPU
+ * (coordinate descent over samples_per_pass, trace_ctas_per_sm, stack_cap,
+ * shade_block and overlap; each candidate is a captured graph, one warm-up
+ * and two timed launches, CUDA events), installs the fastest and returns it
+ * with its time per run in milliseconds.  scratch_films: device buffer of
+ * skw_render_batch_film_floats floats that the candidates render into. */
+int skw_render_batch_autotune(skw_render_batch *batch, float *scratch_films, void *stream, skw_batch_config *best,
+                              float *best_ms, int32_t *n_candidates);
+
 #ifdef __cplusplus
 }
 #endif

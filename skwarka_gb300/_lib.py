@@ -78,6 +78,15 @@ SIGNATURES = [
     ("skw_scene_destroy", None, [_P]),
     ("skw_scene_accel", _P, [_P]),
     ("skw_render_direct", C.c_int, [_P, C.c_void_p, C.c_void_p, _P, _P]),
+    ("skw_render_batch_create", C.c_int, [_P, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.POINTER(_P)]),
+    ("skw_render_batch_destroy", None, [_P]),
+    ("skw_render_batch_film_floats", C.c_int64, [_P]),
+    ("skw_render_batch_film_offset", C.c_int64, [_P, C.c_int32]),
+    ("skw_render_batch_get_config", C.c_int, [_P, C.c_void_p]),
+    ("skw_render_batch_run", C.c_int, [_P, _P, _P]),
+    ("skw_render_batch_autotune", C.c_int, [_P, _P, _P, C.c_void_p, C.POINTER(C.c_float),
+                                            C.POINTER(C.c_int32)]),
     ("skw_nearest", C.c_int, [_P, _P, _P, C.c_int64, C.c_double, C.c_double, _P, _P]),
 ]
 

@@ -18,9 +18,15 @@ int traversal_stack_capacity(int max_depth);
 // n_dev (may be null): device int holding the number of rays to trace (at
 // most n), for queues filled on the device.  out_index (may be null): the
 // result of ray j goes to slot out_index[j].
+// ctas_per_sm > 0 caps the persistent grid at that many CTAs per SM (0: as
+// many as fit).  prepare_traversal computes the occupancy of a capacity's
+// kernels ahead of a stream capture.
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
                              int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
-                             unsigned *status, cudaStream_t stream);
+                             unsigned *status, cudaStream_t stream, int ctas_per_sm = 0);
+cudaError_t prepare_traversal(int stack_cap);
+// Resident CTAs per SM of the closest-hit kernel at this capacity.
+int traversal_max_ctas_per_sm(int stack_cap);
 
 
 
@@ -50,18 +56,21 @@ cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double
                            unsigned *status, cudaStream_t stream);
 
 // Direct-lighting render stages (render.cu); see render_scene.h.
+// A pass covers global pixels [px_begin, px_begin + n_px) of the views'
+// concatenated films, every pixel with spp samples.
 struct SceneDev;
-struct CameraDev;
-cudaError_t launch_camera(const CameraDev &cam, int px_begin, int n_px, int sppx, int sppy, uint64_t seed,
+struct ViewDev;
+cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, int n_px, int sppx, int sppy,
                           void *rays, cudaStream_t s);
-cudaError_t launch_shade(const SceneDev &S, int n, int64_t gid_base, int slots, int n_light_samples, uint64_t seed,
-                         const void *rays, const void *hits, float *contrib, void *srays, int *starget, float *srgb,
-                         int *scount, void *brays, int *btarget, float *brgb, int *bcount, cudaStream_t s);
+cudaError_t launch_shade(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin, int spp,
+                         int slots, int n_light_samples, const void *rays, const void *hits, float *contrib,
+                         void *srays, int *starget, float *srgb, int *scount, void *brays, int *btarget, float *brgb,
+                         int *bcount, int block, cudaStream_t s);
 cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                            const int *starget, const float *srgb, const int *scount, const void *brays,
                            const void *bhits, const int *btarget, const float *brgb, const int *bcount,
                            float *contrib, cudaStream_t s);
-cudaError_t launch_film(const float *contrib, int px_begin, int n_px, int spp, int slots, float *film,
+cudaError_t launch_film(const float *contrib, int64_t px_begin, int n_px, int spp, int slots, float *film,
                         cudaStream_t s);
 
 }  // namespace skw

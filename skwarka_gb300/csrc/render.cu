@@ -340,14 +340,29 @@ __device__ __forceinline__ void store_rgb(float *c, int64_t slot, V3 v) {
   c[3 * slot + 2] = v.z;
 }
 
-__global__ void k_camera(CameraDev cam, int px_begin, int n_px, int sppx, int sppy, uint64_t seed,
-                         float4 *__restrict__ rays) {
+// The view holding global pixel P: the last view whose first pixel is <= P.
+__device__ __forceinline__ int find_view(const ViewDev *__restrict__ views, int n_views, int64_t P) {
+  int lo = 0, hi = n_views - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (views[mid].px_begin <= P) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Camera rays for the samples of global pixels [px_begin, px_begin + n_px).
+__global__ void k_camera(const ViewDev *__restrict__ views, int n_views, int64_t px_begin, int n_px, int sppx,
+                         int sppy, float4 *__restrict__ rays) {
   const int spp = sppx * sppy;
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= (int64_t)n_px * spp) return;
-  const int px = px_begin + (int)(s / spp), j = (int)(s % spp);
-  const int x = px % cam.width, y = px / cam.width;
-  const uint64_t gid = (uint64_t)px * spp + j;
+  const int64_t P = px_begin + s / spp;
+  const int j = (int)(s % spp);
+  const int v = find_view(views, n_views, P);
+  const CameraDev &cam = views[v].cam;
+  const int64_t px = P - views[v].px_begin;
+  const int x = (int)(px % cam.width), y = (int)(px / cam.width);
+  const uint64_t gid = (uint64_t)px * spp + j, seed = views[v].seed;
   // stratified, jittered pixel sample (StratifiedSampling2D)
   const double ix = x + ((j % sppx) + (double)rnd(seed, gid, 0)) / sppx;
   const double iy = y + ((j / sppx) + (double)rnd(seed, gid, 1)) / sppy;
@@ -368,11 +383,13 @@ __global__ void k_camera(CameraDev cam, int px_begin, int n_px, int sppx, int sp
 }
 
 struct ShadeArgs {
-  int n;               // samples in this chunk
-  int64_t gid_base;    // global id of the chunk's first sample
+  int n;               // samples in this pass
+  int64_t px_begin;    // global pixel of the pass's first sample
+  int spp;
   int slots;           // contribution slots per sample
   int n_light_samples;
-  uint64_t seed;
+  const ViewDev *views;
+  int n_views;
 };
 
 // Per camera hit: emission, light samples, point lights and BSDF samples
@@ -396,7 +413,13 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
   const bool surface = valid && hit.y >= 0;
   const int nl = A.n_light_samples;
   const int64_t slot0 = (int64_t)i * A.slots;
-  const uint64_t gid = (uint64_t)(A.gid_base + i);
+  uint64_t gid = 0, seed = 0;
+  {
+    const int64_t P = A.px_begin + (valid ? i : 0) / A.spp;
+    const int v = find_view(A.views, A.n_views, P);
+    gid = (uint64_t)((P - A.views[v].px_begin) * A.spp + (valid ? i : 0) % A.spp);
+    seed = A.views[v].seed;
+  }
 
   Hit h{};
   Bsdf b{};
@@ -420,8 +443,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
     V3 val = v3(0, 0, 0), dir = v3(0, 0, 0);
     float tmin = 0.0f, tmax = 0.0f;
     if (surface && S.n_area_lights > 0) {
-      const float uc = rnd(A.seed, gid, 2 + 3 * k), u0 = rnd(A.seed, gid, 3 + 3 * k),
-                  u1 = rnd(A.seed, gid, 4 + 3 * k);
+      const float uc = rnd(seed, gid, 2 + 3 * k), u0 = rnd(seed, gid, 3 + 3 * k),
+                  u1 = rnd(seed, gid, 4 + 3 * k);
       const int nls = S.n_area_lights;
       const int li = min((int)(uc * nls), nls - 1);
       const float lcp = 1.0f / nls;
@@ -500,8 +523,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
     V3 val = v3(0, 0, 0), dir = v3(0, 0, 0);
     float pdf = 0.0f, tmin = 0.0f;
     if (surface && S.n_area_lights > 0) {
-      const float uc = rnd(A.seed, gid, 2 + 3 * nl + 3 * k), u0 = rnd(A.seed, gid, 3 + 3 * nl + 3 * k),
-                  u1 = rnd(A.seed, gid, 4 + 3 * nl + 3 * k);
+      const float uc = rnd(seed, gid, 2 + 3 * nl + 3 * k), u0 = rnd(seed, gid, 3 + 3 * nl + 3 * k),
+                  u1 = rnd(seed, gid, 4 + 3 * nl + 3 * k);
       const V3 f = bsdf_sample(b, wo, uc, u0, u1, dir, pdf);
       if (pdf > 0.0f && !black(f)) {
         val = f * (fabsf(dot(dir, shading_n)) / (pdf * nl));
@@ -570,7 +593,7 @@ __global__ void k_resolve_bsdf(SceneDev S, int n_light_samples, const float4 *__
 // renderer's negative-sample check.
 __constant__ float kLumW[3] = {0.05316285f, 0.58515348f, 0.36168367f};
 
-__global__ void k_film(const float *__restrict__ contrib, int px_begin, int n_px, int spp, int slots,
+__global__ void k_film(const float *__restrict__ contrib, int64_t px_begin, int n_px, int spp, int slots,
                        float *__restrict__ film) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n_px) return;
@@ -601,22 +624,24 @@ __global__ void k_film(const float *__restrict__ contrib, int px_begin, int n_px
 
 }  // namespace
 
-cudaError_t launch_camera(const CameraDev &cam, int px_begin, int n_px, int sppx, int sppy, uint64_t seed,
+cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, int n_px, int sppx, int sppy,
                           void *rays, cudaStream_t s) {
   const int64_t n = (int64_t)n_px * sppx * sppy;
   if (n <= 0) return cudaSuccess;
-  k_camera<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(cam, px_begin, n_px, sppx, sppy, seed, (float4 *)rays);
+  k_camera<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(views, n_views, px_begin, n_px, sppx, sppy, (float4 *)rays);
   return cudaGetLastError();
 }
 
-cudaError_t launch_shade(const SceneDev &S, int n, int64_t gid_base, int slots, int n_light_samples, uint64_t seed,
-                         const void *rays, const void *hits, float *contrib, void *srays, int *starget, float *srgb,
-                         int *scount, void *brays, int *btarget, float *brgb, int *bcount, cudaStream_t s) {
+cudaError_t launch_shade(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin, int spp,
+                         int slots, int n_light_samples, const void *rays, const void *hits, float *contrib,
+                         void *srays, int *starget, float *srgb, int *scount, void *brays, int *btarget, float *brgb,
+                         int *bcount, int block, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  ShadeArgs A{n, gid_base, slots, n_light_samples, seed};
-  k_shade<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, A, (const float4 *)rays, (const int4 *)hits, contrib,
-                                                       (float4 *)srays, starget, srgb, scount, (float4 *)brays,
-                                                       btarget, brgb, bcount);
+  if (block != 64) block = 128;
+  ShadeArgs A{n, px_begin, spp, slots, n_light_samples, views, n_views};
+  k_shade<<<(unsigned)((n + block - 1) / block), (unsigned)block, 0, s>>>(
+      S, A, (const float4 *)rays, (const int4 *)hits, contrib, (float4 *)srays, starget, srgb, scount,
+      (float4 *)brays, btarget, brgb, bcount);
   return cudaGetLastError();
 }
 
@@ -632,7 +657,7 @@ cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples,
   return cudaGetLastError();
 }
 
-cudaError_t launch_film(const float *contrib, int px_begin, int n_px, int spp, int slots, float *film,
+cudaError_t launch_film(const float *contrib, int64_t px_begin, int n_px, int spp, int slots, float *film,
                         cudaStream_t s) {
   if (n_px <= 0) return cudaSuccess;
   k_film<<<(unsigned)((n_px + 127) / 128), 128, 0, s>>>(contrib, px_begin, n_px, spp, slots, film);

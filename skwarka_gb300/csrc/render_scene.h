@@ -61,4 +61,15 @@ struct CameraDev {
   int32_t width, height;
 };
 
+// One view of a render: its camera, the index of its first pixel in the
+// concatenation of all views' films (pixel-major, RGB float), and the seed of
+// its random numbers.  A sample's random numbers depend only on (seed, the
+// sample's index within its own view), so a view renders the same whether
+// it is rendered alone or in a batch.
+struct ViewDev {
+  CameraDev cam;
+  int64_t px_begin;
+  uint64_t seed;
+};
+
 }  // namespace skw

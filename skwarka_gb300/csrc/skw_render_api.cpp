@@ -282,95 +282,474 @@ void skw_scene_destroy(skw_scene *s) {
 
 skw_accel *skw_scene_accel(skw_scene *s) { return s ? s->accel : nullptr; }
 
-int skw_render_direct(skw_scene *s, const skw_camera *cam, const skw_render_params *params, float *film_rgb,
-                      void *stream) {
-  if (!s || !cam || !params || !film_rgb) return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "null argument");
-  skw_ctx *ctx = s->ctx;
-  if (cam->width <= 0 || cam->height <= 0 || params->spp_x <= 0 || params->spp_y <= 0 || params->light_samples < 0 ||
-      params->light_samples > 64 || !(cam->x_view_angle > 0.0) || !(cam->x_view_angle < 3.14159265358979))
-    return fail(ctx, SKW_ERR_ARG, "bad camera or render parameters");
-  cudaError_t e = cudaSetDevice(ctx->device);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
-  skw::CameraDev cd{};
-  std::memcpy(cd.c2w, cam->camera_to_world, sizeof(cd.c2w));
-  cd.x_tan = std::tan(cam->x_view_angle / 2.0);  // PerspectiveCamera.cpp:19-33
-  cd.y_tan = cd.x_tan * (double)cam->height / cam->width;
-  cd.width = cam->width;
-  cd.height = cam->height;
-  const int spp = params->spp_x * params->spp_y;
-  const int nl = params->light_samples;
-  const int npl = s->dev.n_point_lights;
-  const int slots = 1 + 2 * nl + npl;
-  const int64_t n_px_total = (int64_t)cam->width * cam->height;
-  // Pixels per chunk: at most 2^21 samples in flight.
-  const int64_t chunk_px = std::max<int64_t>(1, std::min<int64_t>(n_px_total, ((int64_t)1 << 21) / spp));
-  const int64_t cap_samples = chunk_px * spp;
-  const int64_t cap_shadow = cap_samples * (nl + npl), cap_bsdf = cap_samples * nl;
-  if (cap_shadow > INT32_MAX || cap_samples * slots * 3 > ((int64_t)1 << 40))
-    return fail(ctx, SKW_ERR_ARG, "render too large");
-  auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
-  const size_t b_rays = al(cap_samples * 32), b_hits = al(cap_samples * 16), b_contrib = al(cap_samples * slots * 12),
-               b_srays = al(std::max<int64_t>(cap_shadow, 1) * 32), b_starget = al(std::max<int64_t>(cap_shadow, 1) * 4),
-               b_srgb = al(std::max<int64_t>(cap_shadow, 1) * 12), b_occ = al(std::max<int64_t>(cap_shadow, 1)),
-               b_brays = al(std::max<int64_t>(cap_bsdf, 1) * 32), b_btarget = al(std::max<int64_t>(cap_bsdf, 1) * 4),
-               b_brgb = al(std::max<int64_t>(cap_bsdf, 1) * 16), b_bhits = al(std::max<int64_t>(cap_bsdf, 1) * 16),
-               b_cnt = 256;
-  const size_t total = b_rays + b_hits + b_contrib + b_srays + b_starget + b_srgb + b_occ + b_brays + b_btarget +
-                       b_brgb + b_bhits + b_cnt;
-  cudaStream_t st = (cudaStream_t)stream;
-  cudaMemPool_t pool;
-  if ((e = skw::ctx_pool(ctx, &pool)) != cudaSuccess) return cuda_fail(ctx, e, "workspace pool");
-  char *w = nullptr;
-  if ((e = cudaMallocFromPoolAsync((void **)&w, total, pool, st)) != cudaSuccess)
-    return cuda_fail(ctx, e, "render workspace");
-  char *p = w;
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Render passes.  Both the single-camera render and the batch lay the views'
+// pixels end to end and process them in passes of whole pixels; a pass runs
+// camera -> closest hit -> shade (queues shadow and BSDF rays) -> any hit on
+// the shadow queue -> closest hit on the BSDF queue -> resolve -> film.
+namespace {
+
+struct PassConfig {
+  int64_t samples_per_pass = (int64_t)1 << 21;
+  int stack_cap = 0;         // 0: the accelerator's own
+  int trace_ctas_per_sm = 0;
+  int shade_block = 128;
+  int overlap = 0;
+};
+
+struct Plan {
+  std::vector<skw::ViewDev> views;
+  std::vector<int64_t> film_offset;  // floats
+  int sppx = 1, sppy = 1, spp = 1, nl = 0, npl = 0, slots = 1;
+  int64_t n_px_total = 0, chunk_px = 0, cap_samples = 0, cap_shadow = 0, cap_bsdf = 0;
+  PassConfig cfg;
+};
+
+// Device buffers of one workspace (one pass in flight).
+struct Workspace {
+  void *rays = nullptr, *hits = nullptr, *srays = nullptr, *brays = nullptr, *bhits = nullptr;
+  float *contrib = nullptr, *srgb = nullptr, *brgb = nullptr;
+  int *starget = nullptr, *btarget = nullptr, *counts = nullptr;
+  uint8_t *occ = nullptr;
+};
+
+inline size_t al256(int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); }
+
+size_t workspace_bytes(const Plan &P) {
+  const int64_t cs = P.cap_samples, sh = std::max<int64_t>(P.cap_shadow, 1), bs = std::max<int64_t>(P.cap_bsdf, 1);
+  return al256(cs * 32) + al256(cs * 16) + al256(cs * P.slots * 12) + al256(sh * 32) + al256(sh * 4) +
+         al256(sh * 12) + al256(sh) + al256(bs * 32) + al256(bs * 4) + al256(bs * 16) + al256(bs * 16) + 256;
+}
+
+void workspace_carve(const Plan &P, char *base, Workspace *W) {
+  const int64_t cs = P.cap_samples, sh = std::max<int64_t>(P.cap_shadow, 1), bs = std::max<int64_t>(P.cap_bsdf, 1);
+  char *p = base;
   auto take = [&](size_t b) {
     char *r = p;
     p += b;
     return r;
   };
-  void *rays = take(b_rays), *hits = take(b_hits);
-  float *contrib = (float *)take(b_contrib);
-  void *srays = take(b_srays);
-  int *starget = (int *)take(b_starget);
-  float *srgb = (float *)take(b_srgb);
-  uint8_t *occ = (uint8_t *)take(b_occ);
-  void *brays = take(b_brays);
-  int *btarget = (int *)take(b_btarget);
-  float *brgb = (float *)take(b_brgb);
-  void *bhits = take(b_bhits);
-  int *counts = (int *)take(b_cnt);  // [0] shadow queue length, [1] BSDF queue length
-  skw_accel *a = s->accel;
-  int64_t launches = 0;
-  for (int64_t px0 = 0; px0 < n_px_total && e == cudaSuccess; px0 += chunk_px) {
-    const int n_px = (int)std::min<int64_t>(chunk_px, n_px_total - px0);
-    const int n = n_px * spp;
-    if ((e = cudaMemsetAsync(contrib, 0, (size_t)n * slots * 12, st)) != cudaSuccess) break;
-    if ((e = cudaMemsetAsync(counts, 0, 2 * sizeof(int), st)) != cudaSuccess) break;
-    if ((e = skw::launch_camera(cd, (int)px0, n_px, params->spp_x, params->spp_y, params->seed, rays, st)) != cudaSuccess)
-      break;
-    if ((e = skw::launch_traversal(true, a->stack_cap, a->d_nodes, a->d_tris, rays, n, nullptr, a->scene_abs, nullptr,
-                                   hits, a->d_status, st)) != cudaSuccess)
-      break;
-    if ((e = skw::launch_shade(s->dev, n, px0 * spp, slots, nl, params->seed, rays, hits, contrib, srays, starget, srgb,
-                               counts, brays, btarget, brgb, counts + 1, st)) != cudaSuccess)
-      break;
-    const int64_t csh = (int64_t)n * (nl + npl), cbs = (int64_t)n * nl;
-    if (csh > 0 && (e = skw::launch_traversal(false, a->stack_cap, a->d_nodes, a->d_tris, srays, csh, counts,
-                                              a->scene_abs, nullptr, occ, a->d_status, st)) != cudaSuccess)
-      break;
-    if (cbs > 0 && (e = skw::launch_traversal(true, a->stack_cap, a->d_nodes, a->d_tris, brays, cbs, counts + 1,
-                                              a->scene_abs, nullptr, bhits, a->d_status, st)) != cudaSuccess)
-      break;
-    if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), nl, occ, starget, srgb, counts, brays, bhits,
-                                 btarget, brgb, counts + 1, contrib, st)) != cudaSuccess)
-      break;
-    if ((e = skw::launch_film(contrib, (int)px0, n_px, spp, slots, film_rgb, st)) != cudaSuccess) break;
-    launches += 8;
+  W->rays = take(al256(cs * 32));
+  W->hits = take(al256(cs * 16));
+  W->contrib = (float *)take(al256(cs * P.slots * 12));
+  W->srays = take(al256(sh * 32));
+  W->starget = (int *)take(al256(sh * 4));
+  W->srgb = (float *)take(al256(sh * 12));
+  W->occ = (uint8_t *)take(al256(sh));
+  W->brays = take(al256(bs * 32));
+  W->btarget = (int *)take(al256(bs * 4));
+  W->brgb = (float *)take(al256(bs * 16));
+  W->bhits = take(al256(bs * 16));
+  W->counts = (int *)take(256);  // [0] shadow queue length, [1] BSDF queue length
+}
+
+int valid_cap(int c) { return c == 48 || c == 96 || c == 192 || c == 416; }
+
+// Validates the cameras and parameters and lays out the passes.
+int plan_make(skw_scene *s, const skw_camera *cams, int n_views, const skw_render_params *params,
+              const uint64_t *seeds, const PassConfig &cfg, Plan *P) {
+  skw_ctx *ctx = s->ctx;
+  if (n_views <= 0 || n_views > (1 << 20)) return fail(ctx, SKW_ERR_ARG, "bad number of views");
+  if (params->spp_x <= 0 || params->spp_y <= 0 || params->spp_x > 1024 || params->spp_y > 1024 ||
+      params->light_samples < 0 || params->light_samples > 64)
+    return fail(ctx, SKW_ERR_ARG, "bad render parameters");
+  if (cfg.stack_cap != 0 && (!valid_cap(cfg.stack_cap) || cfg.stack_cap < s->accel->stack_cap))
+    return fail(ctx, SKW_ERR_ARG, "stack_cap must be 48, 96, 192 or 416 and cover the tree's depth");
+  if (cfg.shade_block != 64 && cfg.shade_block != 128) return fail(ctx, SKW_ERR_ARG, "shade_block must be 64 or 128");
+  if (cfg.samples_per_pass < 1 || cfg.trace_ctas_per_sm < 0) return fail(ctx, SKW_ERR_ARG, "bad pass configuration");
+  P->views.assign((size_t)n_views, skw::ViewDev{});
+  P->film_offset.assign((size_t)n_views, 0);
+  int64_t px = 0;
+  for (int v = 0; v < n_views; ++v) {
+    const skw_camera *cam = cams + v;
+    if (cam->width <= 0 || cam->height <= 0 || !(cam->x_view_angle > 0.0) || !(cam->x_view_angle < 3.14159265358979))
+      return fail(ctx, SKW_ERR_ARG, "bad camera");
+    skw::ViewDev &V = P->views[(size_t)v];
+    std::memcpy(V.cam.c2w, cam->camera_to_world, sizeof(V.cam.c2w));
+    V.cam.x_tan = std::tan(cam->x_view_angle / 2.0);  // PerspectiveCamera.cpp:19-33
+    V.cam.y_tan = V.cam.x_tan * (double)cam->height / cam->width;
+    V.cam.width = cam->width;
+    V.cam.height = cam->height;
+    V.px_begin = px;
+    V.seed = seeds ? seeds[v] : params->seed + (uint64_t)v;
+    P->film_offset[(size_t)v] = 3 * px;
+    px += (int64_t)cam->width * cam->height;
   }
+  P->sppx = params->spp_x;
+  P->sppy = params->spp_y;
+  P->spp = P->sppx * P->sppy;
+  P->nl = params->light_samples;
+  P->npl = s->dev.n_point_lights;
+  P->slots = 1 + 2 * P->nl + P->npl;
+  P->n_px_total = px;
+  P->cfg = cfg;
+  if (P->cfg.stack_cap == 0) P->cfg.stack_cap = s->accel->stack_cap;
+  P->chunk_px = std::max<int64_t>(1, std::min<int64_t>(px, cfg.samples_per_pass / P->spp));
+  P->cap_samples = P->chunk_px * P->spp;
+  P->cap_shadow = P->cap_samples * (P->nl + P->npl);
+  P->cap_bsdf = P->cap_samples * P->nl;
+  if (P->cap_shadow > INT32_MAX || P->cap_samples > INT32_MAX || P->cap_samples * P->slots * 3 > ((int64_t)1 << 40))
+    return fail(ctx, SKW_ERR_ARG, "render pass too large");
+  return SKW_OK;
+}
+
+// One pass over global pixels [px0, px0 + n_px).
+cudaError_t record_pass(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
+                        int n_px, float *films, cudaStream_t st) {
+  skw_accel *a = s->accel;
+  const int n = n_px * P.spp, nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(W.contrib, 0, (size_t)n * P.slots * 12, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) return e;
+  if ((e = skw::launch_camera(d_views, nv, px0, n_px, P.sppx, P.sppy, W.rays, st)) != cudaSuccess) return e;
+  if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr, W.hits,
+                                 a->d_status, st, ctas)) != cudaSuccess)
+    return e;
+  if ((e = skw::launch_shade(s->dev, d_views, nv, n, px0, P.spp, P.slots, P.nl, W.rays, W.hits, W.contrib, W.srays,
+                             W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb, W.counts + 1, P.cfg.shade_block,
+                             st)) != cudaSuccess)
+    return e;
+  const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
+  if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts, a->scene_abs,
+                                            nullptr, W.occ, a->d_status, st, ctas)) != cudaSuccess)
+    return e;
+  if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
+                                            a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas)) != cudaSuccess)
+    return e;
+  if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
+                               W.bhits, W.btarget, W.brgb, W.counts + 1, W.contrib, st)) != cudaSuccess)
+    return e;
+  return skw::launch_film(W.contrib, px0, n_px, P.spp, P.slots, films, st);
+}
+
+constexpr int kLaunchesPerPass = 8;
+
+int64_t n_passes(const Plan &P) { return (P.n_px_total + P.chunk_px - 1) / P.chunk_px; }
+
+// All passes.  With two workspaces, passes alternate between them on two
+// streams (st and side), joined back into st at the end.
+cudaError_t record_all(skw_scene *s, const Plan &P, const Workspace *W, int n_ws, const skw::ViewDev *d_views,
+                       float *films, cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+  cudaError_t e = cudaSuccess;
+  if (n_ws > 1) {
+    if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(side, fork, 0)) != cudaSuccess) return e;
+  }
+  int64_t k = 0;
+  for (int64_t px0 = 0; px0 < P.n_px_total; px0 += P.chunk_px, ++k) {
+    const int n_px = (int)std::min<int64_t>(P.chunk_px, P.n_px_total - px0);
+    const int w = n_ws > 1 ? (int)(k & 1) : 0;
+    if ((e = record_pass(s, P, W[w], d_views, px0, n_px, films, w ? side : st)) != cudaSuccess) return e;
+  }
+  if (n_ws > 1) {
+    if ((e = cudaEventRecord(join, side)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, join, 0)) != cudaSuccess) return e;
+  }
+  return e;
+}
+
+}  // namespace
+
+struct skw_render_batch {
+  skw_scene *scene = nullptr;
+  Plan plan;
+  skw_render_params params{};
+  std::vector<uint64_t> seeds;
+  std::vector<skw_camera> cams;
+  char *ws = nullptr;  // workspaces (one or two)
+  size_t ws_bytes = 0;
+  skw::ViewDev *d_views = nullptr;
+  cudaStream_t own = nullptr, side = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr, fork = nullptr, join = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  float *graph_films = nullptr;
+};
+
+namespace {
+
+void batch_release(skw_render_batch *b) {
+  // Launches of the old graph still in flight use the workspace.
+  if (b->own) cudaStreamSynchronize(b->own);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  b->graph_films = nullptr;
+}
+
+// (Re)builds the plan for cfg and makes sure the workspace is large enough.
+int batch_configure(skw_render_batch *b, const PassConfig &cfg) {
+  skw_ctx *ctx = b->scene->ctx;
+  Plan P;
+  int rc = plan_make(b->scene, b->cams.data(), (int)b->cams.size(), &b->params, b->seeds.data(), cfg, &P);
+  if (rc != SKW_OK) return rc;
+  cudaError_t e;
+  if ((e = skw::prepare_traversal(P.cfg.stack_cap)) != cudaSuccess) return cuda_fail(ctx, e, "traversal occupancy");
+  const int n_ws = P.cfg.overlap && n_passes(P) > 1 ? 2 : 1;
+  const size_t need = workspace_bytes(P) * (size_t)n_ws;
+  batch_release(b);
+  if (need > b->ws_bytes) {
+    if (b->ws) cudaFree(b->ws);
+    b->ws = nullptr;
+    b->ws_bytes = 0;
+    if ((e = cudaMalloc((void **)&b->ws, need)) != cudaSuccess) return cuda_fail(ctx, e, "batch workspace");
+    b->ws_bytes = need;
+  }
+  batch_release(b);
+  b->plan = std::move(P);
+  return SKW_OK;
+}
+
+int batch_capture(skw_render_batch *b, float *films) {
+  skw_ctx *ctx = b->scene->ctx;
+  const Plan &P = b->plan;
+  const int n_ws = P.cfg.overlap && n_passes(P) > 1 ? 2 : 1;
+  Workspace W[2];
+  const size_t one = workspace_bytes(P);
+  for (int i = 0; i < n_ws; ++i) workspace_carve(P, b->ws + one * (size_t)i, &W[i]);
+  batch_release(b);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(b->own, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
+  cudaError_t er = record_all(b->scene, P, W, n_ws, b->d_views, films, b->own, b->side, b->fork, b->join);
+  e = cudaStreamEndCapture(b->own, &g);
+  if (er != cudaSuccess || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return cuda_fail(ctx, er != cudaSuccess ? er : e, "graph capture");
+  }
+  e = cudaGraphInstantiate(&b->exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    b->exec = nullptr;
+    return cuda_fail(ctx, e, "graph instantiate");
+  }
+  b->graph_films = films;
+  return SKW_OK;
+}
+
+// Launches the graph on the batch's stream, ordered after `stream` and
+// before whatever is queued on `stream` next.
+int batch_launch(skw_render_batch *b, float *films, cudaStream_t stream) {
+  skw_ctx *ctx = b->scene->ctx;
+  if (!b->exec || b->graph_films != films) {
+    int rc = batch_capture(b, films);
+    if (rc != SKW_OK) return rc;
+  }
+  cudaError_t e;
+  if ((e = cudaEventRecord(b->ev_in, stream)) != cudaSuccess) return cuda_fail(ctx, e, "batch run");
+  if ((e = cudaStreamWaitEvent(b->own, b->ev_in, 0)) != cudaSuccess) return cuda_fail(ctx, e, "batch run");
+  if ((e = cudaGraphLaunch(b->exec, b->own)) != cudaSuccess) return cuda_fail(ctx, e, "graph launch");
+  if ((e = cudaEventRecord(b->ev_out, b->own)) != cudaSuccess) return cuda_fail(ctx, e, "batch run");
+  if ((e = cudaStreamWaitEvent(stream, b->ev_out, 0)) != cudaSuccess) return cuda_fail(ctx, e, "batch run");
+  ctx->launches.fetch_add(n_passes(b->plan) * kLaunchesPerPass);
+  return SKW_OK;
+}
+
+PassConfig to_pass_config(const skw_batch_config *c) {
+  PassConfig p;
+  if (!c) {
+    p.overlap = 1;
+    return p;
+  }
+  p.samples_per_pass = c->samples_per_pass;
+  p.stack_cap = c->stack_cap;
+  p.trace_ctas_per_sm = c->trace_ctas_per_sm;
+  p.shade_block = c->shade_block;
+  p.overlap = c->overlap;
+  return p;
+}
+
+void from_pass_config(const PassConfig &p, skw_batch_config *c) {
+  c->samples_per_pass = p.samples_per_pass;
+  c->stack_cap = p.stack_cap;
+  c->trace_ctas_per_sm = p.trace_ctas_per_sm;
+  c->shade_block = p.shade_block;
+  c->overlap = p.overlap;
+}
+
+}  // namespace
+
+extern "C" {
+
+int skw_render_direct(skw_scene *s, const skw_camera *cam, const skw_render_params *params, float *film_rgb,
+                      void *stream) {
+  if (!s || !cam || !params || !film_rgb) return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "null argument");
+  skw_ctx *ctx = s->ctx;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  Plan P;
+  const uint64_t seed = params->seed;
+  int rc = plan_make(s, cam, 1, params, &seed, PassConfig{}, &P);
+  if (rc != SKW_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemPool_t pool;
+  if ((e = skw::ctx_pool(ctx, &pool)) != cudaSuccess) return cuda_fail(ctx, e, "workspace pool");
+  const size_t wbytes = workspace_bytes(P), vbytes = al256(sizeof(skw::ViewDev));
+  char *w = nullptr;
+  if ((e = cudaMallocFromPoolAsync((void **)&w, wbytes + vbytes, pool, st)) != cudaSuccess)
+    return cuda_fail(ctx, e, "render workspace");
+  Workspace W;
+  workspace_carve(P, w, &W);
+  skw::ViewDev *d_view = (skw::ViewDev *)(w + wbytes);
+  e = cudaMemcpyAsync(d_view, P.views.data(), sizeof(skw::ViewDev), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = record_all(s, P, &W, 1, d_view, film_rgb, st, nullptr, nullptr, nullptr);
   cudaFreeAsync(w, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "direct-lighting render");
-  ctx->launches.fetch_add(launches);
+  ctx->launches.fetch_add(n_passes(P) * kLaunchesPerPass);
+  return SKW_OK;
+}
+
+int skw_render_batch_create(skw_scene *s, const skw_camera *cams, int32_t n_views, const skw_render_params *params,
+                            const uint64_t *view_seeds, const skw_batch_config *cfg, skw_render_batch **out) {
+  if (out) *out = nullptr;
+  if (!s || !cams || !params || !out) return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "null argument");
+  skw_ctx *ctx = s->ctx;
+  if (n_views <= 0) return fail(ctx, SKW_ERR_ARG, "bad number of views");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  skw_render_batch *b = new (std::nothrow) skw_render_batch();
+  if (!b) return fail(ctx, SKW_ERR_OOM, "host allocation");
+  b->scene = s;
+  b->params = *params;
+  b->cams.assign(cams, cams + n_views);
+  b->seeds.resize((size_t)n_views);
+  for (int v = 0; v < n_views; ++v) b->seeds[(size_t)v] = view_seeds ? view_seeds[v] : params->seed + (uint64_t)v;
+  int rc = batch_configure(b, to_pass_config(cfg));
+  if (rc == SKW_OK) {
+    if ((e = cudaMalloc((void **)&b->d_views, sizeof(skw::ViewDev) * (size_t)n_views)) != cudaSuccess ||
+        (e = cudaMemcpy(b->d_views, b->plan.views.data(), sizeof(skw::ViewDev) * (size_t)n_views,
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming)) != cudaSuccess)
+      rc = cuda_fail(ctx, e, "batch resources");
+  }
+  if (rc != SKW_OK) {
+    skw_render_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return SKW_OK;
+}
+
+void skw_render_batch_destroy(skw_render_batch *b) {
+  if (!b) return;
+  if (b->own) cudaStreamSynchronize(b->own);
+  if (b->side) cudaStreamSynchronize(b->side);
+  batch_release(b);
+  if (b->ws) cudaFree(b->ws);
+  if (b->d_views) cudaFree(b->d_views);
+  if (b->own) cudaStreamDestroy(b->own);
+  if (b->side) cudaStreamDestroy(b->side);
+  for (cudaEvent_t ev : {b->ev_in, b->ev_out, b->fork, b->join})
+    if (ev) cudaEventDestroy(ev);
+  delete b;
+}
+
+int64_t skw_render_batch_film_floats(const skw_render_batch *b) { return b ? 3 * b->plan.n_px_total : -1; }
+
+int64_t skw_render_batch_film_offset(const skw_render_batch *b, int32_t v) {
+  if (!b || v < 0 || v >= (int32_t)b->plan.film_offset.size()) return -1;
+  return b->plan.film_offset[(size_t)v];
+}
+
+int skw_render_batch_get_config(const skw_render_batch *b, skw_batch_config *out) {
+  if (!b || !out) return SKW_ERR_ARG;
+  from_pass_config(b->plan.cfg, out);
+  return SKW_OK;
+}
+
+int skw_render_batch_run(skw_render_batch *b, float *films, void *stream) {
+  if (!b || !films) return fail(b ? b->scene->ctx : nullptr, SKW_ERR_ARG, "null argument");
+  cudaError_t e = cudaSetDevice(b->scene->ctx->device);
+  if (e != cudaSuccess) return cuda_fail(b->scene->ctx, e, "cudaSetDevice");
+  return batch_launch(b, films, (cudaStream_t)stream);
+}
+
+int skw_render_batch_autotune(skw_render_batch *b, float *scratch, void *stream, skw_batch_config *best_out,
+                              float *best_ms_out, int32_t *n_candidates) {
+  if (!b || !scratch) return fail(b ? b->scene->ctx : nullptr, SKW_ERR_ARG, "null argument");
+  skw_ctx *ctx = b->scene->ctx;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  if ((e = cudaEventCreate(&t0)) != cudaSuccess || (e = cudaEventCreate(&t1)) != cudaSuccess) {
+    if (t0) cudaEventDestroy(t0);
+    return cuda_fail(ctx, e, "autotune events");
+  }
+  int tried = 0;
+  // Time of one run of cfg (ms), or a negative value if cfg is not usable.
+  auto measure = [&](const PassConfig &cfg) -> float {
+    if (batch_configure(b, cfg) != SKW_OK) return -1.0f;
+    if (batch_launch(b, scratch, st) != SKW_OK) return -1.0f;  // capture + warm-up
+    cudaEventRecord(t0, st);
+    for (int r = 0; r < 2; ++r)
+      if (batch_launch(b, scratch, st) != SKW_OK) return -1.0f;
+    cudaEventRecord(t1, st);
+    if (cudaEventSynchronize(t1) != cudaSuccess) return -1.0f;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    ++tried;
+    return ms / 2.0f;
+  };
+  PassConfig best = b->plan.cfg;
+  float best_ms = measure(best);
+  if (best_ms < 0) {
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    return fail(ctx, SKW_ERR_CUDA, "autotune: the starting configuration does not run");
+  }
+  auto consider = [&](PassConfig c) {
+    const float ms = measure(c);
+    if (ms > 0 && ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  };
+  const int64_t total = b->plan.n_px_total * b->plan.spp;
+  for (int64_t q : {(int64_t)1 << 18, (int64_t)1 << 19, (int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22}) {
+    if (q == best.samples_per_pass || q > 2 * total) continue;
+    PassConfig c = best;
+    c.samples_per_pass = q;
+    consider(c);
+  }
+  {
+    PassConfig c = best;
+    c.overlap = best.overlap ? 0 : 1;
+    consider(c);
+  }
+  const int max_ctas = skw::traversal_max_ctas_per_sm(best.stack_cap);
+  for (int k : {max_ctas / 2, (3 * max_ctas) / 4}) {
+    if (k < 1 || k >= max_ctas) continue;
+    PassConfig c = best;
+    c.trace_ctas_per_sm = k;
+    consider(c);
+  }
+  for (int cap : {48, 96, 192, 416}) {
+    if (cap <= best.stack_cap || cap < b->scene->accel->stack_cap) continue;
+    PassConfig c = best;
+    c.stack_cap = cap;
+    consider(c);
+    break;  // the next larger capacity only
+  }
+  {
+    PassConfig c = best;
+    c.shade_block = best.shade_block == 128 ? 64 : 128;
+    consider(c);
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  int rc = batch_configure(b, best);
+  if (rc != SKW_OK) return rc;
+  if (best_out) from_pass_config(best, best_out);
+  if (best_ms_out) *best_ms_out = best_ms;
+  if (n_candidates) *n_candidates = tried;
   return SKW_OK;
 }
 

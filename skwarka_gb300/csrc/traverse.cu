@@ -501,26 +501,44 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
 }
 
 template <int CAP>
-cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const void *rays, int64_t n,
-                       const int *n_dev, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
-                       cudaStream_t stream) {
-  static int blocks_per_sm[2] = {0, 0}, sms = 0;
-  const int which = closest ? 1 : 0;
+int &cap_occupancy(bool closest) {
+  static int blocks_per_sm[2] = {0, 0};
+  return blocks_per_sm[closest ? 1 : 0];
+}
+
+template <int CAP>
+cudaError_t cap_prepare() {
+  for (int which = 0; which < 2; ++which) {
+    int &occ = cap_occupancy<CAP>(which == 1);
+    if (occ != 0) continue;
+    cudaError_t e = which ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<CAP, true>, SKW_TRAV_BLOCK, 0)
+                          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<CAP, false>, SKW_TRAV_BLOCK, 0);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+  }
+  return cudaSuccess;
+}
+
+int device_sms() {
+  static int sms = 0;
   if (sms == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   }
-  if (blocks_per_sm[which] == 0) {
-    cudaError_t e = closest ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[1], k_trace<CAP, true>,
-                                                                          SKW_TRAV_BLOCK, 0)
-                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[0], k_trace<CAP, false>,
-                                                                          SKW_TRAV_BLOCK, 0);
-    if (e != cudaSuccess) return e;
-    if (blocks_per_sm[which] < 1) blocks_per_sm[which] = 1;
-  }
+  return sms;
+}
+
+template <int CAP>
+cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const void *rays, int64_t n,
+                       const int *n_dev, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
+                       cudaStream_t stream, int ctas_per_sm) {
+  cudaError_t e = cap_prepare<CAP>();
+  if (e != cudaSuccess) return e;
+  int per_sm = cap_occupancy<CAP>(closest);
+  if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
   const int64_t warps_per_block = SKW_TRAV_BLOCK / 32;
-  int64_t blocks = (int64_t)blocks_per_sm[which] * sms;
+  int64_t blocks = (int64_t)per_sm * device_sms();
   const int64_t needed = (n + 32 * warps_per_block - 1) / (32 * warps_per_block);
   if (blocks > needed) blocks = needed;
   if (closest) {
@@ -535,6 +553,26 @@ cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const 
 
 }  // namespace
 
+cudaError_t prepare_traversal(int stack_cap) {
+  device_sms();
+  switch (stack_cap) {
+    case 48: return cap_prepare<48>();
+    case 96: return cap_prepare<96>();
+    case 192: return cap_prepare<192>();
+    default: return cap_prepare<416>();
+  }
+}
+
+int traversal_max_ctas_per_sm(int stack_cap) {
+  if (prepare_traversal(stack_cap) != cudaSuccess) return 1;
+  switch (stack_cap) {
+    case 48: return cap_occupancy<48>(true);
+    case 96: return cap_occupancy<96>(true);
+    case 192: return cap_occupancy<192>(true);
+    default: return cap_occupancy<416>(true);
+  }
+}
+
 int traversal_stack_capacity(int max_depth) {
   const int need = 2 * max_depth + 1;
   if (need <= 48) return 48;
@@ -545,17 +583,17 @@ int traversal_stack_capacity(int max_depth) {
 
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
                              int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
-                             unsigned *status, cudaStream_t stream) {
+                             unsigned *status, cudaStream_t stream, int ctas_per_sm) {
   if (n <= 0) return cudaSuccess;
   switch (stack_cap) {
     case 48:
-      return launch_cap<48>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream);
+      return launch_cap<48>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm);
     case 96:
-      return launch_cap<96>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream);
+      return launch_cap<96>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm);
     case 192:
-      return launch_cap<192>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream);
+      return launch_cap<192>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm);
     default:
-      return launch_cap<416>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream);
+      return launch_cap<416>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm);
   }
 }
 

@@ -123,6 +123,14 @@ def c_prims(prims: list[RenderPrimitive]):
     return cm, len(meshes), cp, keep
 
 
+class skw_batch_config(C.Structure):
+    _fields_ = [("samples_per_pass", C.c_int64), ("stack_cap", C.c_int32), ("trace_ctas_per_sm", C.c_int32),
+                ("shade_block", C.c_int32), ("overlap", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class RenderScene:
     def __init__(self, prims: list[RenderPrimitive], materials: list[Material], point_lights=(),
                  ctx: Context | None = None):
@@ -156,3 +164,70 @@ class RenderScene:
         _lib.check(_lib.load().skw_render_direct(self.handle, C.byref(cam), C.byref(par), out.data_ptr(), s),
                    self.ctx.handle)
         return out
+
+
+class RenderBatch:
+    """Many cameras of one RenderScene rendered as one wavefront (one CUDA
+    graph launch per run).  View v gets seed = seeds[v] (default seed + v)
+    and renders exactly what RenderScene.render_direct renders with that
+    seed."""
+
+    def __init__(self, scene: RenderScene, cameras: list[Camera], spp_x: int = 2, spp_y: int = 2,
+                 light_samples: int = 1, seed: int = 0, seeds=None, config: dict | None = None):
+        import numpy as np
+        lib = _lib.load()
+        self.scene, self.cameras = scene, list(cameras)
+        cams = (skw_camera * len(cameras))(*[c_camera(c) for c in cameras])
+        par = skw_render_params(spp_x, spp_y, light_samples, seed)
+        self._seeds = None if seeds is None else np.ascontiguousarray(seeds, np.uint64)
+        cfg = None
+        if config is not None:
+            cfg = skw_batch_config(**config)
+        h = C.c_void_p()
+        _lib.check(lib.skw_render_batch_create(scene.handle, cams, len(cameras), C.byref(par),
+                                               None if self._seeds is None else self._seeds.ctypes.data,
+                                               None if cfg is None else C.byref(cfg), C.byref(h)), scene.ctx.handle)
+        self.handle = h
+        self.n_floats = int(lib.skw_render_batch_film_floats(h))
+        self.offsets = [int(lib.skw_render_batch_film_offset(h, v)) for v in range(len(cameras))]
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            _lib.load().skw_render_batch_destroy(h)
+            self.handle = None
+
+    def config(self) -> dict:
+        c = skw_batch_config()
+        _lib.check(_lib.load().skw_render_batch_get_config(self.handle, C.byref(c)), self.scene.ctx.handle)
+        return c.as_dict()
+
+    def new_films(self):
+        import torch
+        return torch.empty(self.n_floats, dtype=torch.float32, device="cuda")
+
+    def run(self, films=None, stream=None):
+        """Renders all views into the packed float buffer `films` (CUDA) and
+        returns it; view(films, v) is view v's (h, w, 3) image."""
+        import torch
+        if films is None:
+            films = self.new_films()
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _lib.check(_lib.load().skw_render_batch_run(self.handle, films.data_ptr(), s), self.scene.ctx.handle)
+        return films
+
+    def view(self, films, v: int):
+        c = self.cameras[v]
+        o = self.offsets[v]
+        return films[o:o + c.width * c.height * 3].view(c.height, c.width, 3)
+
+    def autotune(self, stream=None) -> tuple[dict, float, int]:
+        """Times candidate configurations on the GPU and installs the best:
+        (config, ms per run, candidates timed)."""
+        import torch
+        scratch = self.new_films()
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        best, ms, n = skw_batch_config(), C.c_float(), C.c_int32()
+        _lib.check(_lib.load().skw_render_batch_autotune(self.handle, scratch.data_ptr(), s, C.byref(best),
+                                                         C.byref(ms), C.byref(n)), self.scene.ctx.handle)
+        return best.as_dict(), float(ms.value), int(n.value)

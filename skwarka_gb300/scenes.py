@@ -203,3 +203,51 @@ def direct_lighting_box(seed: int = 1, sphere_subdivisions=(6, 5)):
         return Camera.look_at((0.0, 0.1, -0.95), (0.0, -0.3, 1.0), (0.0, 1.0, 0.0), np.radians(75.0), width, height)
 
     return prims, materials, camera
+
+
+def batching_scene(seed: int = 4, levels=(6,) * 12 + (3,) * 20, with_light: bool = True):
+    """The 200k-triangle procedural scene: the 12-triangle box, 32 spheres
+    (12 of 4*4^6 and 20 of 4*4^3 triangles = 201,728 + 12) of radius
+    U[0.05, 0.2] at random positions inside the box, each matte, plastic or
+    metal (seeded), shading normals from the sphere, per-wall matte albedo
+    U[0.2, 0.8], and the box's quad light of radiance 10 under the ceiling.
+    Returns (prims, materials)."""
+    from .accel import TriangleMesh
+    from .render import METAL, PLASTIC, Material, RenderPrimitive
+    rng = np.random.default_rng(seed)
+    bv, bt = _box_inward()
+    wall = rng.uniform(0.2, 0.8, size=(6, 3)).astype(np.float32)
+    materials = [Material(kd=(0.5, 0.5, 0.5)),                                             # 0 walls
+                 Material(kd=(0.0, 0.0, 0.0)),                                             # 1 light surface
+                 Material(kd=(0.7, 0.5, 0.3)),                                             # 2 matte
+                 Material(kind=PLASTIC, kd=(0.3, 0.4, 0.6), ks=(0.4, 0.4, 0.4), roughness=0.15),  # 3 plastic
+                 Material(kind=METAL, eta=(0.2, 0.9, 1.1), k=(3.9, 2.4, 2.2), roughness=0.2)]   # 4 metal
+    prims = [RenderPrimitive(TriangleMesh(bv, bt), 0, triangle_albedo=np.repeat(wall, 2, axis=0))]
+    for lvl in levels:
+        r = float(rng.uniform(0.05, 0.2))
+        c = rng.uniform(-0.75, 0.75, size=3)
+        v, t, n = _jittered_sphere(lvl, c, r, rng)
+        prims.append(RenderPrimitive(TriangleMesh(v, t), int(rng.integers(2, 5)), vertex_normals=n))
+    if with_light:
+        lv = np.array([[-0.3, 0.98, -0.3], [0.3, 0.98, -0.3], [0.3, 0.98, 0.3], [-0.3, 0.98, 0.3]], np.float32)
+        lt = np.array([[0, 1, 2], [0, 2, 3]], np.int32)
+        prims.append(RenderPrimitive(TriangleMesh(lv, lt), 1, emission=(10.0, 10.0, 10.0)))
+    return prims, materials
+
+
+def batching_views(n: int = 64, seed: int = 5, lo: int = 64, hi: int = 1024):
+    """n cameras inside the box looking at random points, with square films
+    whose side is log-uniform in [lo, hi] and a field of view in [40, 90]
+    degrees."""
+    from .render import Camera
+    rng = np.random.default_rng(seed)
+    cams = []
+    for _ in range(n):
+        side = int(round(lo * (hi / lo) ** rng.uniform()))
+        eye = rng.uniform(-0.85, 0.85, size=3)
+        eye[1] = rng.uniform(-0.2, 0.8)
+        target = rng.uniform(-0.9, 0.9, size=3)
+        target[1] = rng.uniform(-1.0, 0.2)
+        fov = np.radians(rng.uniform(40.0, 90.0))
+        cams.append(Camera.look_at(tuple(eye), tuple(target), (0.0, 1.0, 0.0), float(fov), side, side))
+    return cams
