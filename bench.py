@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-render", action="store_true", help="skip the direct-lighting render measurement")
     p.add_argument("--no-batch", action="store_true", help="skip the batched multi-view render measurement")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     return p.parse_args()
 
 
@@ -273,6 +274,47 @@ def batch_bench(args, dev, ctx):
             "kernel_launches_per_run": launches, "graph_launches_per_run": 1}
 
 
+def adjoint_bench(args, dev, ctx):
+    """Direct-lighting adjoint on the 200k-triangle scene at 512x512, 16 spp
+    (4x4), one light sample: forward render time against adjoint time (the
+    adjoint replays the forward's rays and accumulates per-triangle albedo
+    and emission-scale gradients), CUDA events on the launching stream."""
+    import numpy as np
+    import torch
+    from skwarka_gb300 import scenes
+    from skwarka_gb300.adjoint import DirectLighting
+    from skwarka_gb300.render import Camera, RenderScene
+    prims, mats = scenes.batching_scene()
+    sc = RenderScene(prims, mats, ctx=ctx)
+    cam = Camera.look_at((0.0, 0.3, -0.9), (0.0, -0.4, 0.6), (0, 1, 0), np.radians(70), 512, 512)
+    r = DirectLighting(sc, cam, 4, 4, 1, seed=3)
+    rng = np.random.default_rng(6)
+    albedo = torch.tensor(rng.uniform(0.1, 0.9, size=(sc.n_triangles, 3)), dtype=torch.float32, device=dev)
+    target = r.forward_image((albedo + torch.tensor(rng.normal(0, 0.05, size=albedo.shape), dtype=torch.float32,
+                                                    device=dev)).clamp(0, 1), 1.0)
+    img = r.forward_image(albedo, 1.0)
+    d_img = 2.0 * (img - target)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(reps):
+            fn()
+        e.record(stream)
+        torch.cuda.synchronize()
+        return s.elapsed_time(e) / reps
+
+    fwd_ms = timed(lambda: r.forward_image(albedo, 1.0))
+    adj_ms = timed(lambda: r.adjoint(albedo, 1.0, d_img))
+    samples = 512 * 512 * 16
+    return {"workload": "adjoint of direct lighting, 201,742-tri scene, 512x512, 16 spp, per-triangle albedo + "
+                        "emission scale", "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
+            "forward_msamples_s": samples / fwd_ms / 1e3, "adjoint_msamples_s": samples / adj_ms / 1e3}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -424,6 +466,10 @@ def main():
     if not args.no_batch:
         log("batched multi-view render")
         batch = batch_bench(args, dev, ctx)
+    adjoint = None
+    if not args.no_adjoint:
+        log("adjoint")
+        adjoint = adjoint_bench(args, dev, ctx)
     peak, peak_kind = peaks()
     per_launch_s = sum(kern_ms) / len(kern_ms) / 1e3
     roofline = None
@@ -442,7 +488,7 @@ def main():
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": args.rays * 32,
                     "d2h_bytes_per_step": args.rays * 16},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,
-            "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit, "render": render, "batch": batch,
+            "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit, "render": render, "batch": batch, "adjoint": adjoint,
             "accel": {k: acc.info[k] for k in ("n_nodes", "max_depth", "build_ms", "device_bytes")}}
     print(json.dumps(line), flush=True)
     if world > 1:

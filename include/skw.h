@@ -302,6 +302,33 @@ typedef struct skw_render_params {
 int skw_render_direct(skw_scene *scene, const skw_camera *camera, const skw_render_params *params, float *film_rgb,
                       void *stream);
 
+/* ---- Direct-lighting adjoint (no counterpart in the reference, which has no
+ * derivatives).  Parameters: the per-triangle albedo (the kd of matte and
+ * plastic materials; metal has none) and one scale that multiplies every
+ * area light's radiance.  Geometry and visibility are held fixed: the
+ * adjoint replays the forward render's rays from the same seed (nothing is
+ * stored between the two) and accumulates the derivatives of its
+ * contributions.  The renderer's rule that drops NaN / negative / infinite
+ * sample radiances is not differentiated (it drops nothing on finite
+ * inputs). */
+/* Triangles in mesh order over all primitives: the albedo arrays below have
+ * 3 floats per triangle, triangle g = (sum of the earlier primitives'
+ * triangles) + mesh triangle index. */
+int64_t skw_scene_n_triangles(const skw_scene *scene);
+/* Replaces the per-triangle albedo (3 floats per triangle, any memory the
+ * device can read, stream-ordered; NaN in the first channel = the
+ * material's kd).  Values are clamped to [0, 1] when shading. */
+int skw_scene_set_triangle_albedo(skw_scene *scene, const float *albedo, void *stream);
+/* Multiplies every area light's radiance (default 1); takes effect for
+ * renders queued afterwards. */
+int skw_scene_set_emission_scale(skw_scene *scene, float scale);
+/* Given d_film = dL/dI (device, same layout as skw_render_direct's film),
+ * ADDS dL/d(albedo) to g_albedo (device, 3 floats per triangle) and
+ * dL/d(emission scale) to *g_emission (device double), for the render of
+ * (camera, params) -- the same seed gives the same rays as the forward. */
+int skw_render_direct_adjoint(skw_scene *scene, const skw_camera *camera, const skw_render_params *params,
+                              const float *d_film, float *g_albedo, double *g_emission, void *stream);
+
 /* ---- Batched multi-view render (no counterpart in the reference, whose
  * SamplerBasedRenderer::Render renders one camera per call; the batch is the
  * same estimator as skw_render_direct for every view). ---------------------

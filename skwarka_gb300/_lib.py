@@ -78,6 +78,10 @@ SIGNATURES = [
     ("skw_scene_destroy", None, [_P]),
     ("skw_scene_accel", _P, [_P]),
     ("skw_render_direct", C.c_int, [_P, C.c_void_p, C.c_void_p, _P, _P]),
+    ("skw_scene_n_triangles", C.c_int64, [_P]),
+    ("skw_scene_set_triangle_albedo", C.c_int, [_P, _P, _P]),
+    ("skw_scene_set_emission_scale", C.c_int, [_P, C.c_float]),
+    ("skw_render_direct_adjoint", C.c_int, [_P, C.c_void_p, C.c_void_p, _P, _P, _P, _P]),
     ("skw_render_batch_create", C.c_int, [_P, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.POINTER(_P)]),
     ("skw_render_batch_destroy", None, [_P]),

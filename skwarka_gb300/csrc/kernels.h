@@ -72,5 +72,18 @@ cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples,
                            float *contrib, cudaStream_t s);
 cudaError_t launch_film(const float *contrib, int64_t px_begin, int n_px, int spp, int slots, float *film,
                         cudaStream_t s);
+// Adjoint of one pass (render.cu): replays the pass's rays and accumulates
+// dL/d(triangle albedo) (3 floats per global triangle) and dL/d(emission
+// scale) from dfilm = dL/dI (3 floats per global pixel).
+cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin, int spp,
+                                 int n_light_samples, const float *dfilm, float *g_albedo, double *g_emission,
+                                 const void *rays, const void *hits, void *srays, int *stri, float *s_dkd,
+                                 float *s_dem, int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
+                                 int *bcount, cudaStream_t s);
+cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
+                                   const int *stri, const float *s_dkd, const float *s_dem, const int *scount,
+                                   const void *brays, const void *bhits, const int *btri, const float *b_dkd,
+                                   const float *brgb, const int *bcount, float *g_albedo, double *g_emission,
+                                   cudaStream_t s);
 
 }  // namespace skw

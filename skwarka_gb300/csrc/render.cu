@@ -204,6 +204,15 @@ __device__ V3 bsdf_eval(const Bsdf &b, V3 wi_w, V3 wo_w) {
   return f;
 }
 
+// The derivative of bsdf_eval with respect to kd (per channel): the diffuse
+// component evaluated with kd = 1 (zero for metal, whose BSDF has no kd).
+__device__ V3 bsdf_eval_dkd(const Bsdf &b, V3 wi_w, V3 wo_w) {
+  if (b.kind == kMetal || !(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f)) return v3(0, 0, 0);
+  Bsdf u = b;
+  u.kd = v3(1.0f, 1.0f, 1.0f);
+  return diffuse_eval(u, b.local(wi_w), b.local(wo_w));
+}
+
 // BSDF::PDF (Core/BSDF.cpp:42-58): average of the component densities.
 __device__ float bsdf_pdf(const Bsdf &b, V3 wi_w, V3 wo_w) {
   const V3 wi = b.local(wi_w), wo = b.local(wo_w);
@@ -392,10 +401,33 @@ struct ShadeArgs {
   int n_views;
 };
 
+// Adjoint pass (ADJ = true).  The same rays as the forward pass are traced
+// (same random numbers), but instead of radiance each queued ray carries the
+// derivatives of its contribution, already multiplied by dL/dI of its pixel
+// divided by spp:
+//   shadow entry q: s_tri[q] (global triangle of the shading point),
+//     s_dkd[3q..] = dI * d(contribution)/d(kd), s_dem[q] = dI . d(contribution)/d(emission scale);
+//   BSDF entry q: b_tri[q], b_dkd[3q..] = dI * d(f |cos| / (pdf n))/d(kd),
+//     brgb[4q..] = (dI * f |cos| / (pdf n), pdf); the light's radiance and
+//     MIS weight multiply both when the ray is resolved.
+struct AdjointArgs {
+  const float *dfilm;   // dL/dI, 3 floats per global pixel
+  float *g_albedo;      // accumulated dL/d(triangle albedo), 3 floats per global triangle
+  double *g_emission;   // accumulated dL/d(emission scale)
+  float *s_dkd, *s_dem, *b_dkd;
+};
+
+__device__ __forceinline__ void add_emission_grad(double *g, float v) {
+  // warp sum, then one atomic per warp
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v != 0.0f) atomicAdd(g, (double)v);
+}
+
 // Per camera hit: emission, light samples, point lights and BSDF samples
 // (DirectLightingLTEIntegrator::_SurfaceRadiance with
 // DirectLightingIntegrator::ComputeDirectLighting).
-__global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const float4 *__restrict__ rays,
+template <bool ADJ>
+__global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointArgs J, const float4 *__restrict__ rays,
                                                const int4 *__restrict__ hits, float *__restrict__ contrib,
                                                float4 *__restrict__ srays, int *__restrict__ starget,
                                                float *__restrict__ srgb, int *__restrict__ scount,
@@ -414,12 +446,16 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
   const int nl = A.n_light_samples;
   const int64_t slot0 = (int64_t)i * A.slots;
   uint64_t gid = 0, seed = 0;
+  V3 dI = v3(0, 0, 0);  // adjoint: dL/dI of this sample's pixel / spp
   {
     const int64_t P = A.px_begin + (valid ? i : 0) / A.spp;
     const int v = find_view(A.views, A.n_views, P);
     gid = (uint64_t)((P - A.views[v].px_begin) * A.spp + (valid ? i : 0) % A.spp);
     seed = A.views[v].seed;
+    if (ADJ && valid) dI = load3(J.dfilm + 3 * P) * (1.0f / A.spp);
   }
+  const float escale = S.emission_scale;
+  float g_em = 0.0f;  // adjoint: this thread's direct emission-gradient terms
 
   Hit h{};
   Bsdf b{};
@@ -431,7 +467,11 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
     wo = d * -1.0f;
     // Area light emission towards the viewer (DiffuseAreaLightSource::Radiance).
     const int li = S.prim_light[hit.y];
-    if (li >= 0 && dot(wo, h.ng) > 0.0f) store_rgb(contrib, slot0, load3(S.area_lights[li].radiance));
+    if (li >= 0 && dot(wo, h.ng) > 0.0f) {
+      const V3 le = load3(S.area_lights[li].radiance);
+      if (ADJ) g_em += dot(dI, le);
+      else store_rgb(contrib, slot0, le * escale);
+    }
   }
   const V3 shading_n = b.n;
 
@@ -440,7 +480,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
   // same expectation; a single light -- all configurations -- has pdf 1).
   for (int k = 0; k < nl; ++k) {
     bool want = false;
-    V3 val = v3(0, 0, 0), dir = v3(0, 0, 0);
+    V3 val = v3(0, 0, 0), dir = v3(0, 0, 0), dkd = v3(0, 0, 0);
+    float dem = 0.0f;
     float tmin = 0.0f, tmax = 0.0f;
     if (surface && S.n_area_lights > 0) {
       const float uc = rnd(seed, gid, 2 + 3 * k), u0 = rnd(seed, gid, 3 + 3 * k),
@@ -474,7 +515,12 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
           const float bpdf = bsdf_pdf(b, wo, dir);
           const float w = power_heuristic(nl, light_pdf * lcp, nl, bpdf) * fabsf(dot(dir, shading_n)) /
                           (light_pdf * lcp);
-          val = mul(f, load3(L.radiance)) * (w / nl);
+          const V3 le = load3(L.radiance);
+          val = mul(f, le) * (escale * w / nl);
+          if (ADJ) {
+            dkd = mul(dI, mul(bsdf_eval_dkd(b, wo, dir), le)) * (escale * w / nl);
+            dem = dot(dI, mul(f, le)) * (w / nl);
+          }
           tmin = next_min_t(h, dir, S.scene_abs);
           tmax = dist - 1e-4f;  // to avoid hitting the light itself (:237)
           want = tmax > tmin;
@@ -484,16 +530,20 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
     const int q = queue_append(want, scount);
     if (want) {
       store_ray(srays, q, h.p, dir, tmin, tmax);
-      starget[q] = (int)(slot0 + 1 + k);
-      srgb[3 * q] = val.x;
-      srgb[3 * q + 1] = val.y;
-      srgb[3 * q + 2] = val.z;
+      if (ADJ) {
+        starget[q] = h.g;
+        store_rgb(J.s_dkd, q, dkd);
+        J.s_dem[q] = dem;
+      } else {
+        starget[q] = (int)(slot0 + 1 + k);
+        store_rgb(srgb, q, val);
+      }
     }
   }
   // Point lights (delta lights, :91-107).
   for (int k = 0; k < S.n_point_lights; ++k) {
     bool want = false;
-    V3 val = v3(0, 0, 0), dir = v3(0, 0, 0);
+    V3 val = v3(0, 0, 0), dir = v3(0, 0, 0), dkd = v3(0, 0, 0);
     float tmin = 0.0f, tmax = 0.0f;
     if (surface) {
       const PointLightDev P = S.point_lights[k];
@@ -503,6 +553,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
       const V3 f = bsdf_eval(b, dir, wo);
       if (!black(f)) {
         val = mul(f, load3(P.intensity)) * (inv * inv * fabsf(dot(dir, shading_n)));
+        if (ADJ)
+          dkd = mul(dI, mul(bsdf_eval_dkd(b, dir, wo), load3(P.intensity))) * (inv * inv * fabsf(dot(dir, shading_n)));
         tmin = next_min_t(h, dir, S.scene_abs);
         tmax = dist;
         want = tmax > tmin;
@@ -511,16 +563,20 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
     const int q = queue_append(want, scount);
     if (want) {
       store_ray(srays, q, h.p, dir, tmin, tmax);
-      starget[q] = (int)(slot0 + 1 + nl + k);
-      srgb[3 * q] = val.x;
-      srgb[3 * q + 1] = val.y;
-      srgb[3 * q + 2] = val.z;
+      if (ADJ) {
+        starget[q] = h.g;
+        store_rgb(J.s_dkd, q, dkd);
+        J.s_dem[q] = 0.0f;
+      } else {
+        starget[q] = (int)(slot0 + 1 + nl + k);
+        store_rgb(srgb, q, val);
+      }
     }
   }
   // BSDF samples (DirectLightingIntegrator::_SampleBSDF, :264-366).
   for (int k = 0; k < nl; ++k) {
     bool want = false;
-    V3 val = v3(0, 0, 0), dir = v3(0, 0, 0);
+    V3 val = v3(0, 0, 0), dir = v3(0, 0, 0), dkd = v3(0, 0, 0);
     float pdf = 0.0f, tmin = 0.0f;
     if (surface && S.n_area_lights > 0) {
       const float uc = rnd(seed, gid, 2 + 3 * nl + 3 * k), u0 = rnd(seed, gid, 3 + 3 * nl + 3 * k),
@@ -528,6 +584,10 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
       const V3 f = bsdf_sample(b, wo, uc, u0, u1, dir, pdf);
       if (pdf > 0.0f && !black(f)) {
         val = f * (fabsf(dot(dir, shading_n)) / (pdf * nl));
+        if (ADJ) {
+          dkd = mul(dI, bsdf_eval_dkd(b, wo, dir)) * (fabsf(dot(dir, shading_n)) / (pdf * nl));
+          val = mul(dI, val);
+        }
         tmin = next_min_t(h, dir, S.scene_abs);
         want = true;
       }
@@ -535,13 +595,15 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, const fl
     const int q = queue_append(want, bcount);
     if (want) {
       store_ray(brays, q, h.p, dir, tmin, __int_as_float(0x7f800000));
-      btarget[q] = (int)(slot0 + 1 + nl + S.n_point_lights + k);
+      btarget[q] = ADJ ? h.g : (int)(slot0 + 1 + nl + S.n_point_lights + k);
+      if (ADJ) store_rgb(J.b_dkd, q, dkd);
       brgb[4 * q] = val.x;
       brgb[4 * q + 1] = val.y;
       brgb[4 * q + 2] = val.z;
       brgb[4 * q + 3] = pdf;
     }
   }
+  if (ADJ) add_emission_grad(J.g_emission, g_em);
 }
 
 __global__ void k_resolve_shadow(const uint8_t *__restrict__ occ, const int *__restrict__ starget,
@@ -583,9 +645,63 @@ __global__ void k_resolve_bsdf(SceneDev S, int n_light_samples, const float4 *__
   const float bpdf = brgb[4 * i + 3];
   const float w = power_heuristic(n_light_samples, bpdf, n_light_samples, light_pdf * lcp);
   const int64_t t = btarget[i];
-  contrib[3 * t] = brgb[4 * i] * L.radiance[0] * w;
-  contrib[3 * t + 1] = brgb[4 * i + 1] * L.radiance[1] * w;
-  contrib[3 * t + 2] = brgb[4 * i + 2] * L.radiance[2] * w;
+  const float sw = S.emission_scale * w;
+  contrib[3 * t] = brgb[4 * i] * L.radiance[0] * sw;
+  contrib[3 * t + 1] = brgb[4 * i + 1] * L.radiance[1] * sw;
+  contrib[3 * t + 2] = brgb[4 * i + 2] * L.radiance[2] * sw;
+}
+
+// Adjoint of k_resolve_shadow: an unoccluded shadow ray adds its derivative
+// terms to its triangle's albedo gradient and to the emission gradient.
+__global__ void k_resolve_shadow_adj(const uint8_t *__restrict__ occ, const int *__restrict__ stri,
+                                     const int *__restrict__ scount, AdjointArgs J) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float dem = 0.0f;
+  if (i < *scount && !occ[i]) {
+    const int64_t g = stri[i];
+    const float *d = J.s_dkd + 3 * (int64_t)i;
+    if (d[0] != 0.0f) atomicAdd(J.g_albedo + 3 * g, d[0]);
+    if (d[1] != 0.0f) atomicAdd(J.g_albedo + 3 * g + 1, d[1]);
+    if (d[2] != 0.0f) atomicAdd(J.g_albedo + 3 * g + 2, d[2]);
+    dem = J.s_dem[i];
+  }
+  add_emission_grad(J.g_emission, dem);
+}
+
+// Adjoint of k_resolve_bsdf (same light density and MIS weight).
+__global__ void k_resolve_bsdf_adj(SceneDev S, int n_light_samples, const float4 *__restrict__ brays,
+                                   const int4 *__restrict__ bhits, const int *__restrict__ btri,
+                                   const float *__restrict__ brgb, const int *__restrict__ bcount, AdjointArgs J) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float dem = 0.0f;
+  if (i < *bcount) {
+    const int4 hit = bhits[i];
+    const int li = hit.y >= 0 ? S.prim_light[hit.y] : -1;
+    if (li >= 0) {
+      const float4 ra = brays[2 * i], rb = brays[2 * i + 1];
+      const V3 d = v3(ra.w, rb.x, rb.y);
+      const int g = S.prim_tri_offset[hit.y] + hit.z;
+      const int j0 = S.tri_vidx[3 * g], j1 = S.tri_vidx[3 * g + 1], j2 = S.tri_vidx[3 * g + 2];
+      const V3 q0 = load3(S.vpos + 3 * j0), q1 = load3(S.vpos + 3 * j1), q2 = load3(S.vpos + 3 * j2);
+      const V3 ln = normalized(cross(q1 - q0, q2 - q0));
+      if (dot(d * -1.0f, ln) > 0.0f) {
+        const AreaLight L = S.area_lights[li];
+        const float dist = __int_as_float(hit.x) - rb.z;
+        const float cosl = fabsf(dot(d, ln));
+        const float light_pdf = cosl > kEps ? dist * dist / (L.area * cosl) : 0.0f;
+        const float lcp = 1.0f / S.n_area_lights;
+        const float w = power_heuristic(n_light_samples, brgb[4 * i + 3], n_light_samples, light_pdf * lcp);
+        const V3 le = load3(L.radiance);
+        const V3 dk = mul(load3(J.b_dkd + 3 * (int64_t)i), le) * (S.emission_scale * w);
+        const int64_t t = btri[i];
+        if (dk.x != 0.0f) atomicAdd(J.g_albedo + 3 * t, dk.x);
+        if (dk.y != 0.0f) atomicAdd(J.g_albedo + 3 * t + 1, dk.y);
+        if (dk.z != 0.0f) atomicAdd(J.g_albedo + 3 * t + 2, dk.z);
+        dem = dot(v3(brgb[4 * i], brgb[4 * i + 1], brgb[4 * i + 2]), le) * w;
+      }
+    }
+  }
+  add_emission_grad(J.g_emission, dem);
 }
 
 // Luminance weights of the reference's RGB spectrum (row Y of its
@@ -639,9 +755,38 @@ cudaError_t launch_shade(const SceneDev &S, const ViewDev *views, int n_views, i
   if (n <= 0) return cudaSuccess;
   if (block != 64) block = 128;
   ShadeArgs A{n, px_begin, spp, slots, n_light_samples, views, n_views};
-  k_shade<<<(unsigned)((n + block - 1) / block), (unsigned)block, 0, s>>>(
-      S, A, (const float4 *)rays, (const int4 *)hits, contrib, (float4 *)srays, starget, srgb, scount,
+  k_shade<false><<<(unsigned)((n + block - 1) / block), (unsigned)block, 0, s>>>(
+      S, A, AdjointArgs{}, (const float4 *)rays, (const int4 *)hits, contrib, (float4 *)srays, starget, srgb, scount,
       (float4 *)brays, btarget, brgb, bcount);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin, int spp,
+                                 int n_light_samples, const float *dfilm, float *g_albedo, double *g_emission,
+                                 const void *rays, const void *hits, void *srays, int *stri, float *s_dkd,
+                                 float *s_dem, int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
+                                 int *bcount, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  ShadeArgs A{n, px_begin, spp, 0, n_light_samples, views, n_views};
+  AdjointArgs J{dfilm, g_albedo, g_emission, s_dkd, s_dem, b_dkd};
+  k_shade<true><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, A, J, (const float4 *)rays, (const int4 *)hits,
+                                                             nullptr, (float4 *)srays, stri, nullptr, scount,
+                                                             (float4 *)brays, btri, brgb, bcount);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
+                                   const int *stri, const float *s_dkd, const float *s_dem, const int *scount,
+                                   const void *brays, const void *bhits, const int *btri, const float *b_dkd,
+                                   const float *brgb, const int *bcount, float *g_albedo, double *g_emission,
+                                   cudaStream_t s) {
+  if (capacity <= 0) return cudaSuccess;
+  AdjointArgs J{nullptr, g_albedo, g_emission, const_cast<float *>(s_dkd), const_cast<float *>(s_dem),
+                const_cast<float *>(b_dkd)};
+  const unsigned grid = (unsigned)((capacity + 255) / 256);
+  k_resolve_shadow_adj<<<grid, 256, 0, s>>>(occ, stri, scount, J);
+  k_resolve_bsdf_adj<<<grid, 256, 0, s>>>(S, n_light_samples, (const float4 *)brays, (const int4 *)bhits, btri, brgb,
+                                          bcount, J);
   return cudaGetLastError();
 }
 

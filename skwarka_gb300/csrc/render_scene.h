@@ -53,6 +53,7 @@ struct SceneDev {
   const PointLightDev *point_lights;
   int32_t n_point_lights;
   float scene_abs;                // largest absolute vertex coordinate
+  float emission_scale;           // multiplies every area light's radiance
 };
 
 struct CameraDev {

@@ -20,6 +20,7 @@ using skw::fail;
 struct skw_scene {
   skw_ctx *ctx = nullptr;
   skw_accel *accel = nullptr;
+  int64_t n_triangles = 0;  // mesh order, over all primitives
   std::vector<void *> buffers;  // device allocations owned by the scene
   skw::SceneDev dev{};
 };
@@ -132,8 +133,9 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
   std::vector<float> vpos, vnrm, albedo;
   std::vector<int32_t> tri_vidx, prim_tri_offset((size_t)std::max(n_prims, 1)), prim_material((size_t)std::max(n_prims, 1)),
       prim_light((size_t)std::max(n_prims, 1), -1), prim_has_normals((size_t)std::max(n_prims, 1), 0);
-  bool any_albedo = false, any_normals = false;
-  for (int32_t p = 0; p < n_prims; ++p) any_albedo |= prims[p].triangle_albedo != nullptr;
+  // Per-triangle albedo is always present (NaN = the material's kd) so that
+  // skw_scene_set_triangle_albedo can replace it.
+  bool any_albedo = true, any_normals = false;
   for (int32_t p = 0; p < n_prims; ++p) any_normals |= prims[p].vertex_normals != nullptr;
   std::vector<skw::AreaLight> lights;
   std::vector<int32_t> light_tri;
@@ -268,6 +270,8 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
   }
   D.n_area_lights = (int32_t)lights.size();
   D.n_point_lights = n_point_lights;
+  D.emission_scale = 1.0f;
+  s->n_triangles = tri_count;
   D.scene_abs = s->accel->scene_abs;
   *out = s;
   return SKW_OK;
@@ -750,6 +754,88 @@ int skw_render_batch_autotune(skw_render_batch *b, float *scratch, void *stream,
   if (best_out) from_pass_config(best, best_out);
   if (best_ms_out) *best_ms_out = best_ms;
   if (n_candidates) *n_candidates = tried;
+  return SKW_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- adjoint --
+
+extern "C" {
+
+int64_t skw_scene_n_triangles(const skw_scene *s) { return s ? s->n_triangles : -1; }
+
+int skw_scene_set_triangle_albedo(skw_scene *s, const float *albedo, void *stream) {
+  if (!s || !albedo) return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "null argument");
+  cudaError_t e = cudaSetDevice(s->ctx->device);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync((void *)s->dev.tri_albedo, albedo, (size_t)s->n_triangles * 3 * sizeof(float),
+                        cudaMemcpyDefault, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(s->ctx, e, "set triangle albedo");
+  return SKW_OK;
+}
+
+int skw_scene_set_emission_scale(skw_scene *s, float scale) {
+  if (!s || !(scale >= 0.0f) || !std::isfinite(scale)) return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "bad scale");
+  s->dev.emission_scale = scale;
+  return SKW_OK;
+}
+
+int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_render_params *params,
+                              const float *d_film, float *g_albedo, double *g_emission, void *stream) {
+  if (!s || !cam || !params || !d_film || !g_albedo || !g_emission)
+    return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "null argument");
+  skw_ctx *ctx = s->ctx;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  Plan P;
+  const uint64_t seed = params->seed;
+  int rc = plan_make(s, cam, 1, params, &seed, PassConfig{}, &P);
+  if (rc != SKW_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemPool_t pool;
+  if ((e = skw::ctx_pool(ctx, &pool)) != cudaSuccess) return cuda_fail(ctx, e, "workspace pool");
+  const int64_t sh = std::max<int64_t>(P.cap_shadow, 1), bs = std::max<int64_t>(P.cap_bsdf, 1);
+  const size_t wbytes = workspace_bytes(P), vbytes = al256(sizeof(skw::ViewDev)), xbytes = al256(sh * 4) + al256(bs * 12);
+  char *w = nullptr;
+  if ((e = cudaMallocFromPoolAsync((void **)&w, wbytes + vbytes + xbytes, pool, st)) != cudaSuccess)
+    return cuda_fail(ctx, e, "adjoint workspace");
+  Workspace W;
+  workspace_carve(P, w, &W);
+  skw::ViewDev *d_view = (skw::ViewDev *)(w + wbytes);
+  float *s_dem = (float *)(w + wbytes + vbytes), *b_dkd = (float *)(w + wbytes + vbytes + al256(sh * 4));
+  float *s_dkd = W.srgb;  // 3 floats per shadow entry, like the forward pass's radiance
+  skw_accel *a = s->accel;
+  e = cudaMemcpyAsync(d_view, P.views.data(), sizeof(skw::ViewDev), cudaMemcpyHostToDevice, st);
+  int64_t launches = 0;
+  for (int64_t px0 = 0; px0 < P.n_px_total && e == cudaSuccess; px0 += P.chunk_px) {
+    const int n_px = (int)std::min<int64_t>(P.chunk_px, P.n_px_total - px0);
+    const int n = n_px * P.spp, cap = P.cfg.stack_cap;
+    if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) break;
+    if ((e = skw::launch_camera(d_view, 1, px0, n_px, P.sppx, P.sppy, W.rays, st)) != cudaSuccess) break;
+    if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr,
+                                   W.hits, a->d_status, st)) != cudaSuccess)
+      break;
+    if ((e = skw::launch_shade_adjoint(s->dev, d_view, 1, n, px0, P.spp, P.nl, d_film, g_albedo, g_emission, W.rays,
+                                       W.hits, W.srays, W.starget, s_dkd, s_dem, W.counts, W.brays, W.btarget, b_dkd,
+                                       W.brgb, W.counts + 1, st)) != cudaSuccess)
+      break;
+    const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
+    if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts,
+                                              a->scene_abs, nullptr, W.occ, a->d_status, st)) != cudaSuccess)
+      break;
+    if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
+                                              a->scene_abs, nullptr, W.bhits, a->d_status, st)) != cudaSuccess)
+      break;
+    if ((e = skw::launch_resolve_adjoint(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, s_dkd, s_dem,
+                                         W.counts, W.brays, W.bhits, W.btarget, b_dkd, W.brgb, W.counts + 1,
+                                         g_albedo, g_emission, st)) != cudaSuccess)
+      break;
+    launches += 7;
+  }
+  cudaFreeAsync(w, st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "direct-lighting adjoint");
+  ctx->launches.fetch_add(launches);
   return SKW_OK;
 }
 
