@@ -302,6 +302,64 @@ typedef struct skw_render_params {
 int skw_render_direct(skw_scene *scene, const skw_camera *camera, const skw_render_params *params, float *film_rgb,
                       void *stream);
 
+/* ---- Photon maps (PhotonLTEIntegrator, LTEIntegrators/PhotonLTEIntegrator/*).
+ *
+ * A photon (PhotonLTEIntegrator::Photon, PhotonInternalTypes.h:35-59):
+ * position, weight, and the 16-bit CompressedDirection ids of the incident
+ * direction and of the surface's geometric normal.  28 bytes. */
+typedef struct skw_photon {
+  float position[3];
+  float weight[3];
+  uint16_t incident;
+  uint16_t normal;
+} skw_photon;
+
+typedef struct skw_photon_map skw_photon_map;
+
+typedef struct skw_photon_params {
+  int64_t paths;          /* photon paths to shoot (ShootPhotons(i_photons)) */
+  int32_t max_bounces;    /* intersections per path, 1..64 (the reference has no cap) */
+  float rr_probability;   /* 0: Russian roulette with the reference's luminance ratio
+                             (PhotonShootingPipeline.cpp:243-250); > 0: that fixed
+                             continue probability */
+  uint64_t seed;          /* random numbers after the first bounce */
+} skw_photon_params;
+
+typedef struct skw_photon_map_info {
+  int64_t n_caustic, n_direct, n_indirect, n_irradiance;
+  int64_t paths_caustic, paths_direct, paths_indirect;
+  double max_irradiance_lookup_dist;  /* m_max_irradiance_lookup_dist (inf if unbounded) */
+  double scene_area;                  /* sum of the primitives' mesh areas */
+  double shoot_ms, build_ms;          /* host wall time: GPU shooting; trees + irradiance map */
+} skw_photon_map_info;
+
+/* Photon maps from given photon arrays (caustic, direct, indirect; any may
+ * be empty except that an indirect map needs a direct one) and the paths each
+ * map's photons came from: builds the three kd-trees (the reference's median
+ * builder, KDTree.h:428-473, on the host) and the irradiance photon map
+ * (_ConstructIrradiancePhotonMap, PhotonLTEIntegrator.cpp:171-245: every 10th
+ * indirect photon in tree order, k = 100 filtered lookups in each map on the
+ * GPU, its kd-tree, and the 0.1 % percentile lookup radius).  scene_area is
+ * the scene's total mesh area (skw_scene_total_area). */
+int skw_photon_map_create(skw_ctx *ctx, const skw_photon *const *photons, const int64_t *n, const int64_t *paths,
+                          double scene_area, skw_photon_map **out);
+/* Shoots params->paths photon paths through the scene on the GPU
+ * (PhotonLTEIntegrator::ShootPhotons, PhotonLTEIntegrator.cpp:247-288 with
+ * PhotonsShootingFilter, PhotonShootingPipeline.cpp:110-267) and builds the
+ * maps as skw_photon_map_create.  Photons are in path order.  A map over the
+ * reference's 40M-photon limit is an error (SKW_ERR_BUDGET). */
+int skw_photon_shoot(skw_scene *scene, const skw_photon_params *params, skw_photon_map **out);
+void skw_photon_map_destroy(skw_photon_map *map);
+int skw_photon_map_get_info(const skw_photon_map *map, skw_photon_map_info *out);
+/* Copies map `which` (0 caustic, 1 direct, 2 indirect) in its input order. */
+int skw_photon_map_export(const skw_photon_map *map, int32_t which, skw_photon *out);
+/* Irradiance photons in kd-tree order: position, external and internal
+ * irradiance (3 floats each), normal id. */
+int skw_photon_map_export_irradiance(const skw_photon_map *map, float *pos, float *ext, float *intr, uint16_t *nrm);
+/* The scene's total mesh area (TriangleMesh::GetArea summed over the
+ * primitives, PhotonLTEIntegrator.cpp:52-55). */
+double skw_scene_total_area(const skw_scene *scene);
+
 /* ---- Direct-lighting adjoint (no counterpart in the reference, which has no
  * derivatives).  Parameters: the per-triangle albedo (the kd of matte and
  * plastic materials; metal has none) and one scale that multiplies every

@@ -65,6 +65,10 @@ _REF_SIGS = [
     ("skw_ref_render_direct", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, C.c_int, _P, C.c_int, _P, _P,
                                         C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
     ("skw_ref_luminance_weights", None, [_P]),
+    ("skw_ref_render_photon", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, C.c_double,
+                                        C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, C.c_int,
+                                        C.c_double, _P, _P, _P]),
+    ("skw_ref_photon_irradiance", C.c_int, [_P, _P, _P, C.c_double, _P, _P, _P, _P, _P, _P]),
 ]
 
 
@@ -214,6 +218,51 @@ class Reference:
         out = np.empty((1 << 16, 3), np.float64)
         self.lib.skw_ref_compressed_direction_table(_ptr(out))
         return out
+
+    def photon_irradiance(self, maps, paths, scene_area):
+        """The reference's _ConstructIrradiancePhotonMap on the given photon
+        maps (structured arrays of PHOTON_DTYPE: caustic, direct, indirect)
+        with their path counts: (positions, external, internal irradiance,
+        normal ids -- in its kd-tree order -- and the max lookup distance)."""
+        from skwarka_gb300.photon import PHOTON_DTYPE
+        arrs = [np.ascontiguousarray(m, PHOTON_DTYPE) for m in maps]
+        ptrs = (C.c_void_p * 3)(*[a.ctypes.data for a in arrs])
+        n = np.array([len(a) for a in arrs], np.int64)
+        pth = np.array(paths, np.int64)
+        cap = len(arrs[2]) // 10 + 1
+        pos, ext, intr = (np.zeros((cap, 3), np.float32) for _ in range(3))
+        nrm = np.zeros(cap, np.uint16)
+        k, md = np.zeros(1, np.int64), np.zeros(1)
+        self.lib.skw_ref_photon_irradiance(ptrs, _ptr(n), _ptr(pth), float(scene_area), _ptr(k), _ptr(pos), _ptr(ext),
+                                           _ptr(intr), _ptr(nrm), _ptr(md))
+        k = int(k[0])
+        return pos[:k], ext[:k], intr[:k], nrm[:k], float(md[0])
+
+    def render_photon(self, prims, materials, point_lights, camera, spp_x, spp_y, n_paths, light_samples=1,
+                      gather_samples=16, caustic_lookup=50, max_caustic_dist=0.1):
+        """The reference's photon-mapping render (PhotonLTEIntegrator:
+        ShootPhotons(n_paths), then the sampler-based render with final
+        gathering): (film, {"shoot_s", "render_s", "caustic", "direct",
+        "indirect", "irradiance"})."""
+        from skwarka_gb300.render import c_material, c_prims
+        cm, nm, cp, keep = c_prims(prims)
+        verts = (C.c_void_p * nm)(*[cm[i].vertices for i in range(nm)])
+        tris = (C.c_void_p * nm)(*[cm[i].triangles for i in range(nm)])
+        nv = np.array([cm[i].n_vertices for i in range(nm)], np.int64)
+        nt = np.array([cm[i].n_triangles for i in range(nm)], np.int64)
+        mats = (type(c_material(materials[0])) * len(materials))(*[c_material(m) for m in materials])
+        pl = np.array([list(l.position) + list(l.intensity) for l in point_lights], np.float32).reshape(-1, 6)
+        c2w = np.ascontiguousarray(camera.camera_to_world, np.float64).reshape(-1)
+        film = np.zeros((max(camera.height, 1), max(camera.width, 1), 3), np.float32)
+        info = np.zeros(4, np.int64)
+        sec = np.zeros(2)
+        self.lib.skw_ref_render_photon(nm, verts, _ptr(nv), tris, _ptr(nt), len(prims), C.addressof(cp),
+                                       C.addressof(mats), len(point_lights), _ptr(pl) if len(pl) else None, _ptr(c2w),
+                                       camera.x_view_angle, camera.width, camera.height, spp_x, spp_y, light_samples,
+                                       int(n_paths), gather_samples, caustic_lookup, max_caustic_dist, _ptr(film),
+                                       _ptr(info), _ptr(sec))
+        return film, {"shoot_s": float(sec[0]), "render_s": float(sec[1]), "caustic": int(info[0]),
+                      "direct": int(info[1]), "indirect": int(info[2]), "irradiance": int(info[3])}
 
     def render_direct(self, prims, materials, point_lights, camera, spp_x, spp_y, light_samples=1):
         """The reference's own direct-lighting render of a scene described with

@@ -364,14 +364,14 @@ struct RefPrimIn {
   float emission[3];
 };
 
-// Renders the direct-lighting image with the reference's SamplerBasedRenderer,
-// StratifiedSampler, DirectLightingLTEIntegrator, PerspectiveCamera and an
-// ImageFilm with a 0.5-wide BoxFilter.  film_out: height x width x 3.
-int skw_ref_render_direct(int n_meshes, const float *const *verts, const int64_t *n_verts, const int32_t *const *tris,
-                          const int64_t *n_tris, int n_prims, const RefPrimIn *prims, int n_materials,
-                          const RefMaterialIn *materials, int n_point_lights, const float *point_lights,
-                          const double *camera_to_world, double x_view_angle, int width, int height, int spp_x,
-                          int spp_y, int light_samples, float *film_out, double *seconds_out) {
+// The reference Scene for the product's scene description (meshes,
+// primitives with materials / emission / shading normals / per-triangle
+// albedo, point lights).
+static intrusive_ptr<const Scene> make_scene(int n_meshes, const float *const *verts, const int64_t *n_verts,
+                                             const int32_t *const *tris, const int64_t *n_tris, int n_prims,
+                                             const RefPrimIn *prims, const RefMaterialIn *materials,
+                                             int n_point_lights, const float *point_lights) {
+  (void)n_meshes;
   std::vector<intrusive_ptr<const Primitive>> prim_list;
   LightSources lights;
   for (int p = 0; p < n_prims; ++p) {
@@ -427,22 +427,24 @@ int skw_ref_render_direct(int n_meshes, const float *const *verts, const int64_t
     lights.m_delta_light_sources.push_back(intrusive_ptr<const DeltaLightSource>(
         new PointLight(Point3D_d(L[0], L[1], L[2]), Spectrum_d(L[3], L[4], L[5]))));
   }
-  intrusive_ptr<const Scene> scene(new Scene(prim_list, NULL, lights));
+  return intrusive_ptr<const Scene>(new Scene(prim_list, NULL, lights));
+}
+
+// Renders `integrator` with the reference's SamplerBasedRenderer,
+// StratifiedSampler, PerspectiveCamera and an ImageFilm with a 0.5-wide
+// BoxFilter into film_out (height x width x 3).
+static double render_film(intrusive_ptr<LTEIntegrator> integrator, const double *camera_to_world, double x_view_angle,
+                          int width, int height, int spp_x, int spp_y, float *film_out) {
   intrusive_ptr<FilmFilter> filter(new BoxFilter(0.5, 0.5));
   intrusive_ptr<ImageFilm> film(new ImageFilm((size_t)width, (size_t)height, filter));
   intrusive_ptr<const Camera> camera(new PerspectiveCamera(make_transform(camera_to_world), film, 0.0, 1.0, x_view_angle));
   Point2D_i begin, end;
   film->GetSamplingExtent(begin, end);
   intrusive_ptr<Sampler> sampler(new StratifiedSampler(begin, end, (size_t)spp_x, (size_t)spp_y));
-  DirectLightingLTEIntegratorParams params;
-  params.m_direct_light_samples_num = (size_t)light_samples;
-  params.m_max_specular_depth = 6;
-  params.m_media_step_size = 0.01;
-  intrusive_ptr<LTEIntegrator> integrator(new DirectLightingLTEIntegrator(scene, params));
   SamplerBasedRenderer renderer(integrator, sampler);
   auto t0 = std::chrono::steady_clock::now();
   renderer.Render(camera, false);
-  if (seconds_out) *seconds_out = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   for (int y = 0; y < height; ++y)
     for (int x = 0; x < width; ++x) {
       Spectrum_d c;
@@ -455,6 +457,130 @@ int skw_ref_render_direct(int n_meshes, const float *const *verts, const int64_t
         o[0] = o[1] = o[2] = 0.0f;
       }
     }
+  return sec;
+}
+
+// Renders the direct-lighting image (DirectLightingLTEIntegrator).
+int skw_ref_render_direct(int n_meshes, const float *const *verts, const int64_t *n_verts, const int32_t *const *tris,
+                          const int64_t *n_tris, int n_prims, const RefPrimIn *prims, int n_materials,
+                          const RefMaterialIn *materials, int n_point_lights, const float *point_lights,
+                          const double *camera_to_world, double x_view_angle, int width, int height, int spp_x,
+                          int spp_y, int light_samples, float *film_out, double *seconds_out) {
+  (void)n_materials;
+  intrusive_ptr<const Scene> scene =
+      make_scene(n_meshes, verts, n_verts, tris, n_tris, n_prims, prims, materials, n_point_lights, point_lights);
+  DirectLightingLTEIntegratorParams params;
+  params.m_direct_light_samples_num = (size_t)light_samples;
+  params.m_max_specular_depth = 6;
+  params.m_media_step_size = 0.01;
+  intrusive_ptr<LTEIntegrator> integrator(new DirectLightingLTEIntegrator(scene, params));
+  const double sec = render_film(integrator, camera_to_world, x_view_angle, width, height, spp_x, spp_y, film_out);
+  if (seconds_out) *seconds_out = sec;
+  return 0;
+}
+
+// Photon-mapping render (PhotonLTEIntegrator): ShootPhotons(n_paths) then
+// the sampler-based render with final gathering.  info_out: caustic, direct,
+// indirect, irradiance photon counts; seconds_out: shooting (incl. the maps)
+// and rendering.
+int skw_ref_render_photon(int n_meshes, const float *const *verts, const int64_t *n_verts, const int32_t *const *tris,
+                          const int64_t *n_tris, int n_prims, const RefPrimIn *prims, const RefMaterialIn *materials,
+                          int n_point_lights, const float *point_lights, const double *camera_to_world,
+                          double x_view_angle, int width, int height, int spp_x, int spp_y, int light_samples,
+                          int64_t n_paths, int gather_samples, int caustic_lookup, double max_caustic_dist,
+                          float *film_out, int64_t *info_out, double *seconds_out) {
+  intrusive_ptr<const Scene> scene =
+      make_scene(n_meshes, verts, n_verts, tris, n_tris, n_prims, prims, materials, n_point_lights, point_lights);
+  PhotonLTEIntegratorParams params;
+  params.m_direct_light_samples_num = (size_t)light_samples;
+  params.m_caustic_lookup_photons_num = (size_t)caustic_lookup;
+  params.m_max_caustic_lookup_dist = max_caustic_dist;
+  params.m_gather_samples_num = (size_t)gather_samples;
+  params.m_max_specular_depth = 6;
+  params.m_media_step_size = 0.01;
+  intrusive_ptr<PhotonLTEIntegrator> integrator(new PhotonLTEIntegrator(scene, params));
+  auto t0 = std::chrono::steady_clock::now();
+  integrator->ShootPhotons((size_t)n_paths, false);
+  const double shoot = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (info_out) {
+    auto &maps = integrator->mp_photon_maps;
+    info_out[0] = maps->GetCausticMap() ? (int64_t)maps->GetCausticMap()->GetNumberOfPoints() : 0;
+    info_out[1] = maps->GetDirectMap() ? (int64_t)maps->GetDirectMap()->GetNumberOfPoints() : 0;
+    info_out[2] = maps->GetIndirectMap() ? (int64_t)maps->GetIndirectMap()->GetNumberOfPoints() : 0;
+    info_out[3] = integrator->mp_irradiance_map ? (int64_t)integrator->mp_irradiance_map->GetNumberOfPoints() : 0;
+  }
+  double render = 0.0;
+  if (width > 0 && height > 0)
+    render = render_film(integrator, camera_to_world, x_view_angle, width, height, spp_x, spp_y, film_out);
+  if (seconds_out) {
+    seconds_out[0] = shoot;
+    seconds_out[1] = render;
+  }
+  return 0;
+}
+
+// _ConstructIrradiancePhotonMap on given photon maps (28-byte records:
+// position, weight, incident id, normal id), each with its number of paths,
+// and the scene's total area: the irradiance photons in the reference's
+// kd-tree order (position, external and internal irradiance, normal id) and
+// m_max_irradiance_lookup_dist.  n_irr_out: their count (the arrays must
+// hold n_indirect / 10 + 1 entries).
+struct RefPhotonIn {
+  float p[3];
+  float w[3];
+  uint16_t dir, nrm;
+};
+int skw_ref_photon_irradiance(const RefPhotonIn *const *photons, const int64_t *n, const int64_t *paths,
+                              double scene_area, int64_t *n_irr_out, float *pos, float *ext, float *intr,
+                              uint16_t *nrm, double *max_dist_out) {
+  // A one-triangle scene: the integrator needs one, and the area is set below.
+  std::vector<Point3D_f> v = {Point3D_f(0, 0, 0), Point3D_f(1, 0, 0), Point3D_f(0, 1, 0)};
+  std::vector<MeshTriangle> t = {MeshTriangle(0, 1, 2)};
+  intrusive_ptr<TriangleMesh> mesh(new TriangleMesh(v, t, false, false));
+  std::vector<intrusive_ptr<const Primitive>> prim_list = {intrusive_ptr<const Primitive>(
+      new Primitive(mesh, Transform(), intrusive_ptr<const Material>(), intrusive_ptr<const AreaLightSource>(), NULL))};
+  LightSources lights;
+  intrusive_ptr<const Scene> scene(new Scene(prim_list, NULL, lights));
+  PhotonLTEIntegratorParams params;
+  params.m_direct_light_samples_num = 1;
+  params.m_caustic_lookup_photons_num = 50;
+  params.m_max_caustic_lookup_dist = 0.1;
+  params.m_gather_samples_num = 4;
+  params.m_max_specular_depth = 6;
+  params.m_media_step_size = 0.01;
+  PhotonLTEIntegrator integ(scene, params);
+  integ.m_scene_total_area = scene_area;
+  integ.mp_photon_maps.reset(new PhotonLTEIntegrator::PhotonMaps());
+  for (int m = 0; m < 3; ++m) {
+    std::vector<RefPhoton> ph((size_t)n[m]);
+    for (int64_t i = 0; i < n[m]; ++i) {
+      const RefPhotonIn &r = photons[m][i];
+      ph[(size_t)i] = RefPhoton(Point3D_f(r.p[0], r.p[1], r.p[2]), Spectrum_f(r.w[0], r.w[1], r.w[2]),
+                                CompressedDirection::FromID(r.dir), CompressedDirection::FromID(r.nrm));
+    }
+    if (m == 0) integ.mp_photon_maps->AddCausticPhotons(ph, (size_t)paths[m]);
+    if (m == 1) integ.mp_photon_maps->AddDirectPhotons(ph, (size_t)paths[m]);
+    if (m == 2) integ.mp_photon_maps->AddIndirectPhotons(ph, (size_t)paths[m]);
+  }
+  integ.mp_photon_maps->GetCausticMap();
+  integ.mp_photon_maps->GetDirectMap();
+  integ.mp_photon_maps->GetIndirectMap();
+  integ._ConstructIrradiancePhotonMap();
+  int64_t k = 0;
+  if (integ.mp_irradiance_map) {
+    const auto &P = integ.mp_irradiance_map->GetAllPoints();
+    for (const auto &ip : P) {
+      for (int c = 0; c < 3; ++c) {
+        pos[3 * k + c] = ip.m_point[c];
+        ext[3 * k + c] = ip.m_external_irradiance[c];
+        intr[3 * k + c] = ip.m_internal_irradiance[c];
+      }
+      nrm[k] = ip.m_normal.GetID();
+      ++k;
+    }
+  }
+  *n_irr_out = k;
+  *max_dist_out = integ.m_max_irradiance_lookup_dist;
   return 0;
 }
 

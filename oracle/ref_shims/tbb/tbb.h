@@ -93,7 +93,9 @@ class blocked_range {
   size_t grain_;
 };
 
-/* Splits [b, e) into grain-sized pieces handed out dynamically. */
+/* Splits [b, e) into grain-sized pieces handed out dynamically.  Like TBB,
+ * every worker runs its own copy of the body (the reference relies on this:
+ * IrradiancePhotonProcess keeps per-copy scratch, PhotonInternalTypes.h:262-301). */
 template <typename Value, typename Body>
 void parallel_for(const blocked_range<Value> &range, const Body &body) {
   size_t total = range.size();
@@ -103,7 +105,8 @@ void parallel_for(const blocked_range<Value> &range, const Body &body) {
   /* Keep pieces small enough to balance but not smaller than the grain. */
   unsigned workers = shim_num_workers();
   if (pieces <= 1 || workers <= 1) {
-    body(range);
+    const Body local(body);
+    local(range);
     return;
   }
   size_t chunk = grain;
@@ -111,11 +114,12 @@ void parallel_for(const blocked_range<Value> &range, const Body &body) {
   std::atomic<size_t> next(0);
   unsigned n = (unsigned)std::min<size_t>(workers, (total + chunk - 1) / chunk);
   shim_run_workers(n, [&](unsigned) {
+    const Body local(body);
     for (;;) {
       size_t s = next.fetch_add(chunk);
       if (s >= total) break;
       size_t e = std::min(total, s + chunk);
-      body(blocked_range<Value>(range.begin() + (Value)s, range.begin() + (Value)e, grain));
+      local(blocked_range<Value>(range.begin() + (Value)s, range.begin() + (Value)e, grain));
     }
   });
 }

@@ -78,6 +78,13 @@ SIGNATURES = [
     ("skw_scene_destroy", None, [_P]),
     ("skw_scene_accel", _P, [_P]),
     ("skw_render_direct", C.c_int, [_P, C.c_void_p, C.c_void_p, _P, _P]),
+    ("skw_photon_map_create", C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.POINTER(_P)]),
+    ("skw_photon_shoot", C.c_int, [_P, C.c_void_p, C.POINTER(_P)]),
+    ("skw_photon_map_destroy", None, [_P]),
+    ("skw_photon_map_get_info", C.c_int, [_P, C.c_void_p]),
+    ("skw_photon_map_export", C.c_int, [_P, C.c_int32, C.c_void_p]),
+    ("skw_photon_map_export_irradiance", C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("skw_scene_total_area", C.c_double, [_P]),
     ("skw_scene_n_triangles", C.c_int64, [_P]),
     ("skw_scene_set_triangle_albedo", C.c_int, [_P, _P, _P]),
     ("skw_scene_set_emission_scale", C.c_int, [_P, C.c_float]),

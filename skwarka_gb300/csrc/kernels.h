@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <functional>
 
 namespace skw {
 
@@ -85,5 +86,25 @@ cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_
                                    const void *brays, const void *bhits, const int *btri, const float *b_dkd,
                                    const float *brgb, const int *bcount, float *g_albedo, double *g_emission,
                                    cudaStream_t s);
+
+// Photon mapping (photon.cu).  trace(rays, n, n_dev, hits, stream) runs the
+// closest-hit traversal of the scene's accelerator.
+struct PhotonRec;
+struct PhotonShootArgs;
+using TraceFn = std::function<cudaError_t(const void *, int64_t, const int *, void *, cudaStream_t)>;
+// Workspace bytes of one shooting chunk of n_paths paths.
+size_t photon_chunk_bytes(int64_t n_paths, int max_bounces);
+// Shoots paths [path0, path0 + n_paths): writes the chunk's direct photons
+// (at most n_paths) and indirect photons (at most n_paths * (max_bounces - 1))
+// in path order, and their counts to d_totals[0], d_totals[1].
+cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, const TraceFn &trace, int64_t path0,
+                               int n_paths, void *ws, PhotonRec *out_direct, PhotonRec *out_indirect,
+                               int *d_totals, cudaStream_t st);
+// Irradiance estimate of nq points from one map's k-NN output (see
+// k_irradiance_sum); first = this is the first map added.
+cudaError_t launch_irradiance_sum(const void *nodes, const float *weight, const uint16_t *dirid, const double *dirs,
+                                  const double *q, const double *qn, const int32_t *idx, const int32_t *count,
+                                  int64_t nq, int k, double paths, double max_lookup_dist, bool first, float *ext,
+                                  float *intr, cudaStream_t st);
 
 }  // namespace skw

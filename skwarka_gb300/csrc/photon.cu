@@ -1,0 +1,455 @@
+// Photon mapping on sm_103a: photon shooting as a wavefront over paths,
+// deterministic compaction of the deposits, and the irradiance estimate of
+// the irradiance photons.
+//
+// Restates PhotonsShootingFilter::operator()
+// (LTEIntegrators/PhotonLTEIntegrator/PhotonShootingPipeline.cpp:110-267):
+//
+//   k_photon_emit    path i: the light chosen by the power CDF with the
+//                    radical inverse of i+1 in base 11, PointLight::SamplePhoton
+//                    (LightSources/PointLight.cpp:44-55) or
+//                    DiffuseAreaLightSource::SamplePhoton
+//                    (LightSources/DiffuseAreaLightSource.cpp:118-150) with
+//                    radical inverses in bases 2, 3, 5, 7 and 13, in double
+//   k_trace          closest hit of every live path (traverse.cu)
+//   k_photon_bounce  deposit at the hit (the first hit into the direct map,
+//                    later hits into the indirect map; the caustic map needs
+//                    a specular bounce, which no BSDF here has), BSDF sample
+//                    (radical inverses in bases 17, 19, 23 at the first hit,
+//                    the counter-based generator after it), Russian roulette
+//                    with the luminance ratio, next ray
+//   k_scan_* / k_gather_photons  per-path deposits -> maps in path order
+//
+// The deposits of path i land in fixed staging slots (i, bounce), so the maps
+// come out in the order of a single-threaded run of the reference: paths in
+// order, each path's photons in bounce order.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "kernels.h"
+#include "photon_types.h"
+#include "render_device.cuh"
+#include "render_scene.h"
+
+namespace skw {
+namespace {
+
+// SamplingRoutines::RadicalInverse (Math/SamplingRoutines.h:492-507).
+__device__ double radical_inverse(unsigned n, unsigned base) {
+  double ret = 0.0;
+  const double inv_base = 1.0 / base;
+  double inv = inv_base;
+  while (n > 0) {
+    const unsigned d = n % base;
+    ret = __dadd_rn(ret, __dmul_rn((double)d, inv));
+    n /= base;
+    inv = __dmul_rn(inv, inv_base);
+  }
+  return ret;
+}
+
+// CompressedDirection(Vector3D_d) (Math/CompressedDirection.h:91-110).
+__device__ uint16_t compress_dir(double x, double y, double z) {
+  unsigned data = 0;
+  if (x < 0) {
+    data |= 1u << 13;
+    x = -x;
+  }
+  if (y < 0) {
+    data |= 1u << 14;
+    y = -y;
+  }
+  if (z < 0) {
+    data |= 1u << 15;
+    z = -z;
+  }
+  const double scale = 126.999 / (x + y + z);
+  unsigned qx = (unsigned)(uint8_t)(x * scale), qy = (unsigned)(uint8_t)(y * scale);
+  if (qy >= 64) {
+    qx = (127u - qx) & 0xFFu;
+    qy = (127u - qy) & 0xFFu;
+  }
+  data |= (qx << 6) | qy;
+  return (uint16_t)data;
+}
+
+__device__ __forceinline__ float luminance(V3 c) {
+  return 0.05316285f * c.x + 0.58515348f * c.y + 0.36168367f * c.z;
+}
+
+struct Queue {
+  float4 *rays;  // 2 per path
+  float *w;      // 3 per path
+  int *path;     // path index within the chunk
+  int *count;
+};
+
+__device__ __forceinline__ void queue_push(const Queue &Q, int q, V3 o, V3 d, float tmin, V3 w, int path) {
+  Q.rays[2 * q] = make_float4(o.x, o.y, o.z, d.x);
+  Q.rays[2 * q + 1] = make_float4(d.y, d.z, tmin, __int_as_float(0x7f800000));
+  Q.w[3 * q] = w.x;
+  Q.w[3 * q + 1] = w.y;
+  Q.w[3 * q + 2] = w.z;
+  Q.path[q] = path;
+}
+
+__global__ void k_photon_emit(SceneDev S, PhotonShootArgs A, int64_t path0, int n, Queue out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool ok = false;
+  V3 o = v3(0, 0, 0), d = v3(0, 0, 0), w = v3(0, 0, 0);
+  float tmin = 0.0f;
+  if (i < n) {
+    const unsigned pi = (unsigned)(path0 + i) + 1u;
+    const double ps0 = radical_inverse(pi, 2), ps1 = radical_inverse(pi, 3);
+    const double ds0 = radical_inverse(pi, 5), ds1 = radical_inverse(pi, 7);
+    // MathRoutines::BinarySearchCDF (Math/MathRoutines.h:191-218)
+    const double u = radical_inverse(pi, 11);
+    int lo = 0, hi = A.n_lights - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (A.lights[mid].cdf <= u) lo = mid + 1; else hi = mid;
+    }
+    const double light_pdf = lo == 0 ? A.lights[0].cdf : A.lights[lo].cdf - A.lights[lo - 1].cdf;
+    const PhotonLight L = A.lights[lo];
+    double pdf = 0.0, wx = 0, wy = 0, wz = 0, ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0;
+    if (L.kind == 0) {
+      // UniformSphereSampling (SamplingRoutines.h:265-275), pdf 1 / (4 pi)
+      const PointLightDev P = S.point_lights[L.index];
+      const double z = 1.0 - 2.0 * ds0, r = sqrt(fmax(0.0, 1.0 - z * z)), phi = 2.0 * 3.14159265358979323846 * ds1;
+      dx = r * cos(phi);
+      dy = r * sin(phi);
+      dz = z;
+      ox = P.position[0];
+      oy = P.position[1];
+      oz = P.position[2];
+      pdf = 1.0 / (4.0 * 3.14159265358979323846);
+      wx = P.intensity[0];
+      wy = P.intensity[1];
+      wz = P.intensity[2];
+    } else {
+      const AreaLight AL = S.area_lights[L.index];
+      const double ts = radical_inverse(pi, 13);
+      int a = 0, b = AL.tri_count - 1;
+      while (a < b) {
+        const int mid = (a + b) >> 1;
+        if ((double)S.light_cdf[AL.tri_begin + mid] <= ts) a = mid + 1; else b = mid;
+      }
+      const int g = S.light_tri[AL.tri_begin + a];
+      const int j0 = S.tri_vidx[3 * g], j1 = S.tri_vidx[3 * g + 1], j2 = S.tri_vidx[3 * g + 2];
+      const float *q0 = S.vpos + 3 * j0, *q1 = S.vpos + 3 * j1, *q2 = S.vpos + 3 * j2;
+      // triangle normal (TriangleMesh::GetTriangleNormal, float)
+      const V3 fn = normalized(cross(load3(q1) - load3(q0), load3(q2) - load3(q0)));
+      const double nx = fn.x, ny = fn.y, nz = fn.z;
+      const double sq = sqrt(ps0), b1 = 1.0 - sq, b2 = ps1 * sq;
+      ox = b1 * q0[0] + b2 * q1[0] + (1.0 - b1 - b2) * q2[0];
+      oy = b1 * q0[1] + b2 * q1[1] + (1.0 - b1 - b2) * q2[1];
+      oz = b1 * q0[2] + b2 * q1[2] + (1.0 - b1 - b2) * q2[2];
+      // MathRoutines::CoordinateSystem (Math/MathRoutines.h:298-312)
+      double e2x, e2y, e2z;
+      if (fabs(nx) > fabs(ny)) {
+        const double il = 1.0 / sqrt(nx * nx + nz * nz);
+        e2x = -nz * il;
+        e2y = 0.0;
+        e2z = nx * il;
+      } else {
+        const double il = 1.0 / sqrt(ny * ny + nz * nz);
+        e2x = 0.0;
+        e2y = nz * il;
+        e2z = -ny * il;
+      }
+      const double e3x = ny * e2z - nz * e2y, e3y = nz * e2x - nx * e2z, e3z = nx * e2y - ny * e2x;
+      const V3 l = cosine_hemisphere((float)ds0, (float)ds1);
+      dx = l.x * e2x + l.y * e3x + l.z * nx;
+      dy = l.x * e2y + l.y * e3y + l.z * ny;
+      dz = l.x * e2z + l.y * e3z + l.z * nz;
+      const double il = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+      dx *= il;
+      dy *= il;
+      dz *= il;
+      pdf = (double)l.z * 0.31830988618379067154 / AL.area;
+      const double c = dx * nx + dy * ny + dz * nz;
+      wx = AL.radiance[0] * S.emission_scale * c;
+      wy = AL.radiance[1] * S.emission_scale * c;
+      wz = AL.radiance[2] * S.emission_scale * c;
+      tmin = 1e-4f;
+    }
+    if (pdf > 0.0 && (wx > 0.0 || wy > 0.0 || wz > 0.0)) {
+      const double inv = 1.0 / (pdf * light_pdf);
+      w = v3((float)(wx * inv), (float)(wy * inv), (float)(wz * inv));
+      o = v3((float)ox, (float)oy, (float)oz);
+      d = v3((float)dx, (float)dy, (float)dz);
+      ok = true;
+    }
+  }
+  const int q = queue_append(ok, out.count);
+  if (ok) queue_push(out, q, o, d, tmin, w, i);
+}
+
+// One bounce of every live path.  Deposits go to staging slot (path, bounce):
+// the direct map holds bounce 0, the indirect map bounces 1 .. B-1.
+__global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootArgs A, int64_t path0, int bounce,
+                                                       int n_cap, Queue in, const int4 *__restrict__ hits, Queue out,
+                                                       PhotonRec *__restrict__ st_direct,
+                                                       uint8_t *__restrict__ has_direct,
+                                                       PhotonRec *__restrict__ st_indirect,
+                                                       int *__restrict__ n_indirect) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = min(n_cap, *in.count);
+  bool cont = false;
+  V3 o = v3(0, 0, 0), dnew = v3(0, 0, 0), wnew = v3(0, 0, 0);
+  float tmin = 0.0f;
+  int path = 0;
+  if (i < n) {
+    const int4 hit = hits[i];
+    path = in.path[i];
+    if (hit.y >= 0) {
+      const float4 ra = in.rays[2 * i], rb = in.rays[2 * i + 1];
+      const V3 ro = v3(ra.x, ra.y, ra.z), d = v3(ra.w, rb.x, rb.y);
+      const Hit h = make_hit(S, ro, d, __int_as_float(hit.x), hit.y, hit.z);
+      const Bsdf b = make_bsdf(S, h, hit.y);
+      const V3 w = v3(in.w[3 * i], in.w[3 * i + 1], in.w[3 * i + 2]);
+      const V3 inc = d * -1.0f;
+      PhotonRec rec;
+      rec.p[0] = h.p.x;
+      rec.p[1] = h.p.y;
+      rec.p[2] = h.p.z;
+      rec.w[0] = w.x;
+      rec.w[1] = w.y;
+      rec.w[2] = w.z;
+      rec.dir = compress_dir(inc.x, inc.y, inc.z);
+      rec.nrm = compress_dir(h.ng.x, h.ng.y, h.ng.z);
+      if (bounce == 0) {
+        st_direct[path] = rec;
+        has_direct[path] = 1;
+      } else {
+        st_indirect[(int64_t)path * (A.max_bounces - 1) + (bounce - 1)] = rec;
+        n_indirect[path] = bounce;
+      }
+      // BSDF::Sample over all components (none is specular here)
+      float uc, u0, u1;
+      const uint64_t gp = (uint64_t)(path0 + path);
+      if (bounce == 0) {
+        const unsigned pi = (unsigned)gp + 1u;
+        u0 = (float)radical_inverse(pi, 17);
+        u1 = (float)radical_inverse(pi, 19);
+        uc = (float)radical_inverse(pi, 23);
+      } else {
+        u0 = rnd(A.seed, gp, 4 * bounce);
+        u1 = rnd(A.seed, gp, 4 * bounce + 1);
+        uc = rnd(A.seed, gp, 4 * bounce + 2);
+      }
+      V3 ex;
+      float pdf = 0.0f;
+      const V3 f = bsdf_sample(b, inc, uc, u0, u1, ex, pdf);
+      if (pdf > 0.0f && bounce + 1 < A.max_bounces) {
+        wnew = mul(w, f) * (fabsf(dot(ex, b.n)) / pdf);
+        float p = A.rr_probability;
+        if (!(p > 0.0f)) {
+          const float lw = luminance(w);
+          p = lw > 0.0f ? fminf(1.0f, luminance(wnew) / lw) : 0.0f;
+        }
+        const float r = rnd(A.seed, gp, 4 * bounce + 3);
+        if (!(r > p) && p > 0.0f) {
+          wnew = wnew * (1.0f / p);
+          o = h.p;
+          dnew = ex;
+          tmin = next_min_t(h, ex, S.scene_abs);
+          cont = true;
+        }
+      }
+    }
+  }
+  const int q = queue_append(cont, out.count);
+  if (cont) queue_push(out, q, o, dnew, tmin, wnew, path);
+}
+
+// Exclusive scan of per-path counts, 1024 per block, then block offsets.
+constexpr int kScanBlock = 1024;
+
+template <typename T>
+__global__ void k_scan_blocks(const T *__restrict__ cnt, int n, int stride_mul, int *__restrict__ excl,
+                              int *__restrict__ block_sums) {
+  __shared__ int s[kScanBlock];
+  const int i = blockIdx.x * kScanBlock + threadIdx.x;
+  const int v = i < n ? (int)cnt[i] * stride_mul : 0;
+  s[threadIdx.x] = v;
+  __syncthreads();
+  for (int off = 1; off < kScanBlock; off <<= 1) {
+    const int t = threadIdx.x >= off ? s[threadIdx.x - off] : 0;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  if (i < n) excl[i] = s[threadIdx.x] - v;
+  if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = s[threadIdx.x];
+}
+
+// Exclusive scan of the block sums in place (one block, any count); the
+// total goes to *total.
+__global__ void k_scan_sums(int *__restrict__ sums, int nb, int *__restrict__ total) {
+  __shared__ int s[kScanBlock];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += kScanBlock) {
+    const int i = base + threadIdx.x;
+    const int v = i < nb ? sums[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < kScanBlock; off <<= 1) {
+      const int t = threadIdx.x >= off ? s[threadIdx.x - off] : 0;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < nb) sums[i] = carry + s[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == kScanBlock - 1) carry += s[threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+// Copies path i's deposits (count per path from has/cnt) to their place.
+__global__ void k_gather_photons(const PhotonRec *__restrict__ staging, int per_path, const uint8_t *__restrict__ has,
+                                 const int *__restrict__ cnt, int n, const int *__restrict__ excl,
+                                 const int *__restrict__ block_off, PhotonRec *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = has ? (int)has[i] : cnt[i];
+  const int o = excl[i] + block_off[i / kScanBlock];
+  for (int j = 0; j < c; ++j) out[o + j] = staging[(int64_t)i * per_path + j];
+}
+
+// _LookupPhotonIrradiance (PhotonLTEIntegrator.cpp:127-169) for one map:
+// the weights of the found photons (k-NN output, the reference's heap
+// order) summed in double by the side of the query normal they arrive from,
+// over pi * paths * r^2 with the reference's radius rule; the result (float)
+// is added to the running irradiance of the query, so that the maps combine
+// as (caustic + direct) + indirect in float.
+__global__ void k_irradiance_sum(const float4 *__restrict__ nodes, const float *__restrict__ weight,
+                                 const uint16_t *__restrict__ dirid, const double *__restrict__ dirs,
+                                 const double *__restrict__ q, const double *__restrict__ qn,
+                                 const int32_t *__restrict__ idx, const int32_t *__restrict__ count, int nq, int k,
+                                 double paths, double max_lookup_dist, bool first, float *__restrict__ ext,
+                                 float *__restrict__ intr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  const int found = count[i];
+  float e[3] = {0, 0, 0}, in[3] = {0, 0, 0};
+  if (found > 0) {
+    double se[3] = {0, 0, 0}, si[3] = {0, 0, 0}, md2 = 0.0;
+    const double px = q[3 * i], py = q[3 * i + 1], pz = q[3 * i + 2];
+    const double nx = qn[3 * i], ny = qn[3 * i + 1], nz = qn[3 * i + 2];
+    for (int j = 0; j < found; ++j) {
+      const int t = idx[(int64_t)i * k + j];
+      const float4 p = nodes[t];
+      const double dx = __dsub_rn((double)p.x, px), dy = __dsub_rn((double)p.y, py), dz = __dsub_rn((double)p.z, pz);
+      const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+      if (d2 > md2) md2 = d2;
+      const int did = dirid[t];
+      const double c = __dadd_rn(__dadd_rn(__dmul_rn(dirs[3 * did], nx), __dmul_rn(dirs[3 * did + 1], ny)),
+                                 __dmul_rn(dirs[3 * did + 2], nz));
+      double *acc = c > 0.0 ? se : si;
+      acc[0] = __dadd_rn(acc[0], (double)weight[3 * (int64_t)t]);
+      acc[1] = __dadd_rn(acc[1], (double)weight[3 * (int64_t)t + 1]);
+      acc[2] = __dadd_rn(acc[2], (double)weight[3 * (int64_t)t + 2]);
+    }
+    if (found < k || md2 == 0.0)
+      md2 = __dmul_rn(max_lookup_dist, max_lookup_dist);
+    else
+      md2 = __dmul_rn(md2, __ddiv_rn((double)found, __dsub_rn((double)found, 0.5)));
+    const double inv = __ddiv_rn(1.0, __dmul_rn(__dmul_rn(3.14159265358979323846, paths), md2));
+    for (int c = 0; c < 3; ++c) {
+      e[c] = (float)__dmul_rn(se[c], inv);
+      in[c] = (float)__dmul_rn(si[c], inv);
+    }
+  }
+  for (int c = 0; c < 3; ++c) {
+    if (first) {
+      ext[3 * i + c] = e[c];
+      intr[3 * i + c] = in[c];
+    } else {
+      ext[3 * i + c] = __fadd_rn(ext[3 * i + c], e[c]);
+      intr[3 * i + c] = __fadd_rn(intr[3 * i + c], in[c]);
+    }
+  }
+}
+
+}  // namespace
+
+size_t photon_chunk_bytes(int64_t n_paths, int max_bounces) {
+  const int64_t B1 = max_bounces > 1 ? max_bounces - 1 : 1;
+  auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
+  const int64_t nb = (n_paths + kScanBlock - 1) / kScanBlock;
+  return 2 * (al(n_paths * 32) + al(n_paths * 12) + al(n_paths * 4)) + al(n_paths * 16) + 256 +
+         al(n_paths * 28) + al(n_paths) + al(n_paths * B1 * 28) + al(n_paths * 4) + 2 * al(n_paths * 4) +
+         2 * al(nb * 4) + 256;
+}
+
+cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, const TraceFn &trace, int64_t path0,
+                               int n_paths, void *ws, PhotonRec *out_direct, PhotonRec *out_indirect,
+                               int *d_totals, cudaStream_t st) {
+  const int64_t B1 = A.max_bounces > 1 ? A.max_bounces - 1 : 1;
+  auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
+  char *p = (char *)ws;
+  auto take = [&](size_t b) {
+    char *r = p;
+    p += b;
+    return r;
+  };
+  Queue Q[2];
+  for (int k = 0; k < 2; ++k) {
+    Q[k].rays = (float4 *)take(al((int64_t)n_paths * 32));
+    Q[k].w = (float *)take(al((int64_t)n_paths * 12));
+    Q[k].path = (int *)take(al((int64_t)n_paths * 4));
+  }
+  int4 *hits = (int4 *)take(al((int64_t)n_paths * 16));
+  int *counts = (int *)take(256);
+  Q[0].count = counts;
+  Q[1].count = counts + 1;
+  PhotonRec *st_direct = (PhotonRec *)take(al((int64_t)n_paths * 28));
+  uint8_t *has_direct = (uint8_t *)take(al(n_paths));
+  PhotonRec *st_indirect = (PhotonRec *)take(al((int64_t)n_paths * B1 * 28));
+  int *n_indirect = (int *)take(al((int64_t)n_paths * 4));
+  int *excl[2] = {(int *)take(al((int64_t)n_paths * 4)), (int *)take(al((int64_t)n_paths * 4))};
+  const int nb = (n_paths + kScanBlock - 1) / kScanBlock;
+  int *bsum[2] = {(int *)take(al((int64_t)nb * 4)), (int *)take(al((int64_t)nb * 4))};
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(counts, 0, 2 * sizeof(int), st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(has_direct, 0, (size_t)n_paths, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(n_indirect, 0, (size_t)n_paths * 4, st)) != cudaSuccess) return e;
+  const unsigned grid = (unsigned)((n_paths + 127) / 128);
+  k_photon_emit<<<grid, 128, 0, st>>>(S, A, path0, n_paths, Q[0]);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  for (int b = 0; b < A.max_bounces; ++b) {
+    Queue &in = Q[b & 1], &out = Q[(b + 1) & 1];
+    if ((e = trace(in.rays, n_paths, in.count, hits, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(out.count, 0, sizeof(int), st)) != cudaSuccess) return e;
+    k_photon_bounce<<<grid, 128, 0, st>>>(S, A, path0, b, n_paths, in, hits, out, st_direct, has_direct,
+                                          st_indirect, n_indirect);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  // direct: one per path; indirect: n_indirect[path] per path
+  k_scan_blocks<uint8_t><<<nb, kScanBlock, 0, st>>>(has_direct, n_paths, 1, excl[0], bsum[0]);
+  k_scan_sums<<<1, kScanBlock, 0, st>>>(bsum[0], nb, d_totals);
+  k_gather_photons<<<grid, 128, 0, st>>>(st_direct, 1, has_direct, nullptr, n_paths, excl[0], bsum[0], out_direct);
+  k_scan_blocks<int><<<nb, kScanBlock, 0, st>>>(n_indirect, n_paths, 1, excl[1], bsum[1]);
+  k_scan_sums<<<1, kScanBlock, 0, st>>>(bsum[1], nb, d_totals + 1);
+  k_gather_photons<<<grid, 128, 0, st>>>(st_indirect, (int)B1, nullptr, n_indirect, n_paths, excl[1], bsum[1],
+                                         out_indirect);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_irradiance_sum(const void *nodes, const float *weight, const uint16_t *dirid, const double *dirs,
+                                  const double *q, const double *qn, const int32_t *idx, const int32_t *count,
+                                  int64_t nq, int k, double paths, double max_lookup_dist, bool first, float *ext,
+                                  float *intr, cudaStream_t st) {
+  if (nq <= 0) return cudaSuccess;
+  k_irradiance_sum<<<(unsigned)((nq + 127) / 128), 128, 0, st>>>((const float4 *)nodes, weight, dirid, dirs, q, qn,
+                                                                  idx, count, (int)nq, k, paths, max_lookup_dist, first,
+                                                                  ext, intr);
+  return cudaGetLastError();
+}
+
+}  // namespace skw

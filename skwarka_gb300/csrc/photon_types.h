@@ -1,0 +1,38 @@
+// Photon-map data shared by the host layer (skw_photon_map.cpp) and the
+// kernels (photon.cu).
+#pragma once
+
+#include <cstdint>
+
+namespace skw {
+
+// A deposited photon (PhotonLTEIntegrator::Photon,
+// LTEIntegrators/PhotonLTEIntegrator/PhotonInternalTypes.h:35-59): position,
+// weight and the 16-bit CompressedDirection ids of the incident direction and
+// of the surface's geometric normal.  28 bytes, the layout of skw_photon.
+struct PhotonRec {
+  float p[3];
+  float w[3];
+  uint16_t dir, nrm;
+};
+static_assert(sizeof(PhotonRec) == 28, "skw_photon layout");
+
+// Photon emission: one entry per light in the reference's order (delta
+// lights, then area lights), with the normalised cumulative luminance of
+// the lights' power (PhotonLTEIntegrator::_GetLightsPowerCDF,
+// PhotonLTEIntegrator.cpp:80-125).
+struct PhotonLight {
+  double cdf;
+  int32_t kind;   // 0 point light, 1 area light
+  int32_t index;  // into SceneDev::point_lights / area_lights
+};
+
+struct PhotonShootArgs {
+  const PhotonLight *lights;
+  int32_t n_lights;
+  int32_t max_bounces;      // intersections per path
+  float rr_probability;     // > 0: fixed Russian-roulette continue probability; 0: the reference's luminance rule
+  uint64_t seed;
+};
+
+}  // namespace skw

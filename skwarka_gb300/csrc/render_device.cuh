@@ -1,0 +1,328 @@
+// Device helpers shared by the wavefront kernels (render.cu, photon.cu):
+// counter-based random numbers, float vectors, the reference's sampling
+// routines, BSDFs (Lambertian, Oren-Nayar, Blinn microfacet with dielectric
+// or conductor Fresnel), hit differential geometry and queue appends.
+// Each translation unit gets its own internal copy.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "render_scene.h"
+
+namespace skw {
+namespace {
+
+constexpr float kPi = 3.14159265358979f;
+constexpr float kInvPi = 0.318309886183791f;
+constexpr float kEps = 2.220446e-16f;  // the reference's DBL_EPS thresholds, kept as tiny floats
+
+// ---------------------------------------------------------------- random --
+// SplitMix64 finaliser (Steele, Lea, Flood 2014) over (seed, sample, dim).
+__device__ __forceinline__ float rnd(uint64_t seed, uint64_t sample, uint32_t dim) {
+  uint64_t z = seed + 0x9E3779B97F4A7C15ull * (sample * 64ull + dim + 1ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (float)(z >> 40) * (1.0f / 16777216.0f);  // 24 bits: in [0, 1)
+}
+
+// ----------------------------------------------------------------- vectors --
+struct V3 {
+  float x, y, z;
+};
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 mul(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+  return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float len(V3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ V3 normalized(V3 a) {
+  const float l2 = dot(a, a);
+  return l2 > 0.0f ? a * (1.0f / sqrtf(l2)) : a;
+}
+__device__ __forceinline__ V3 load3(const float *p) { return v3(p[0], p[1], p[2]); }
+__device__ __forceinline__ bool black(V3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
+
+// ------------------------------------------------------------ sampling --
+// SamplingRoutines::ConcentricDiskSampling (Math/SamplingRoutines.h:197-241).
+__device__ __forceinline__ void concentric_disk(float u0, float u1, float &dx, float &dy) {
+  const float sx = 2.0f * u0 - 1.0f, sy = 2.0f * u1 - 1.0f;
+  if (sx == 0.0f && sy == 0.0f) {
+    dx = dy = 0.0f;
+    return;
+  }
+  float r, theta;
+  if (sx >= -sy) {
+    if (sx > sy) {
+      r = sx;
+      theta = sy > 0.0f ? sy / r : 8.0f + sy / r;
+    } else {
+      r = sy;
+      theta = 2.0f - sx / r;
+    }
+  } else {
+    if (sx <= sy) {
+      r = -sx;
+      theta = 4.0f - sy / r;
+    } else {
+      r = -sy;
+      theta = 6.0f + sx / r;
+    }
+  }
+  theta *= kPi / 4.0f;
+  dx = r * cosf(theta);
+  dy = r * sinf(theta);
+}
+
+// CosineHemisphereSampling (SamplingRoutines.h:282-291).
+__device__ __forceinline__ V3 cosine_hemisphere(float u0, float u1) {
+  float x, y;
+  concentric_disk(u0, u1, x, y);
+  return v3(x, y, sqrtf(fmaxf(0.0f, 1.0f - x * x - y * y)));
+}
+
+// PowerHeuristic (SamplingRoutines.h:449-455).
+__device__ __forceinline__ float power_heuristic(int n1, float p1, int n2, float p2) {
+  const float f = n1 * p1, g = n2 * p2;
+  return (f * f) / (f * f + g * g);
+}
+
+// ------------------------------------------------------------------- BSDF --
+struct Bsdf {
+  V3 n, e1, e2, ng;  // shading frame and geometric normal
+  int kind;
+  V3 kd, ks;
+  float exponent, on_a, on_b;
+  V3 eta, k2;
+  __device__ __forceinline__ V3 local(V3 w) const { return v3(dot(w, e1), dot(w, e2), dot(w, n)); }
+  __device__ __forceinline__ V3 world(V3 l) const { return e1 * l.x + e2 * l.y + n * l.z; }
+  __device__ __forceinline__ int components() const { return kind == kPlastic ? 2 : 1; }
+};
+
+// FresnelDielectric (Core/Fresnel.h:96-124), inner 1.5, outer 1.0.
+__device__ __forceinline__ float fresnel_dielectric(float c) {
+  c = fminf(1.0f, fmaxf(-1.0f, c));
+  float ni = 1.5f, no = 1.0f;
+  if (c < 0.0f) {
+    ni = 1.0f;
+    no = 1.5f;
+  }
+  const float st = no / ni * sqrtf(fmaxf(0.0f, 1.0f - c * c));
+  if (st >= 1.0f) return 1.0f;
+  const float ct = sqrtf(fmaxf(0.0f, 1.0f - st * st));
+  c = fabsf(c);
+  const float rpar = (ni * c - no * ct) / (ni * c + no * ct);
+  const float rper = (no * c - ni * ct) / (no * c + ni * ct);
+  return (rpar * rpar + rper * rper) * 0.5f;
+}
+
+// FresnelConductor (Core/Fresnel.h:132-145), per channel.
+__device__ __forceinline__ float fresnel_conductor1(float c, float eta, float k2) {
+  c = fabsf(c);
+  const float t1 = eta * eta + k2, t2 = t1 * (c * c);
+  const float rpar = (t2 - (2.0f * c) * eta + 1.0f) / (t2 + (2.0f * c) * eta + 1.0f);
+  const float rper = (t1 - (2.0f * eta * c) + c * c) / (t1 + (2.0f * eta * c) + c * c);
+  return (rpar + rper) * 0.5f;
+}
+
+// Microfacet<Fresnel, Blinn>::Evaluate (BxDFs/Microfacet.h:86-104) for the
+// glossy component of plastic (ks, dielectric) or metal (1, conductor).
+__device__ V3 microfacet_eval(const Bsdf &b, V3 wi, V3 wo) {
+  const float ci = fabsf(wi.z), co = fabsf(wo.z);
+  if (ci < kEps || co < kEps) return v3(0, 0, 0);
+  V3 h = wi + wo;
+  if (fabsf(h.x) < kEps && fabsf(h.y) < kEps && fabsf(h.z) < kEps) return v3(0, 0, 0);
+  h = normalized(h);
+  const float ch = dot(wo, h);
+  const float d = (b.exponent + 2.0f) * (0.5f * kInvPi) * powf(fabsf(h.z), b.exponent);
+  const float tmp = 2.0f * fabsf(h.z) / fabsf(dot(wi, h));
+  const float g = fminf(1.0f, fminf(ci * tmp, co * tmp));
+  const float s = d * g / (4.0f * ci * co);
+  if (b.kind == kPlastic) return b.ks * (fresnel_dielectric(ch) * s);
+  return v3(fresnel_conductor1(ch, b.eta.x, b.k2.x) * s, fresnel_conductor1(ch, b.eta.y, b.k2.y) * s,
+            fresnel_conductor1(ch, b.eta.z, b.k2.z) * s);
+}
+
+// BlinnDistribution::PDF (MicrofacetDistributions/BlinnDistribution.h:104-111)
+// inside Microfacet::PDF (Microfacet.h:125-134).
+__device__ float microfacet_pdf(const Bsdf &b, V3 wi, V3 wo) {
+  if (wi.z * wo.z < 0.0f) return 0.0f;
+  const V3 h = normalized(wi + wo);
+  return ((b.exponent + 1.0f) * powf(fabsf(h.z), b.exponent)) / (2.0f * kPi * 4.0f * fabsf(dot(wi, h)));
+}
+
+// Diffuse component: Lambertian (BxDFs/Lambertian.cpp:18-30) or the
+// reference's Oren-Nayar (BxDFs/OrenNayar.cpp:19-42).
+__device__ __forceinline__ V3 diffuse_eval(const Bsdf &b, V3 wi, V3 wo) {
+  if (b.kind != kOrenNayar) return b.kd * kInvPi;
+  const float dcos = fmaxf(0.0f, wi.x * wo.x + wi.y * wo.y);
+  const float denom = fmaxf(fabsf(wi.z), fabsf(wo.z));
+  return b.kd * (kInvPi * (b.on_a + b.on_b * dcos / denom));
+}
+__device__ __forceinline__ float diffuse_pdf(V3 wi, V3 wo) {  // BxDF::PDF (Core/BxDF.cpp:33-37)
+  return wi.z * wo.z > 0.0f ? fabsf(wo.z) * kInvPi : 0.0f;
+}
+
+// BSDF::Evaluate (Core/BSDF.cpp:22-40): every component is a reflection, so
+// directions on opposite sides of the geometric normal give zero.
+__device__ V3 bsdf_eval(const Bsdf &b, V3 wi_w, V3 wo_w) {
+  if (!(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f)) return v3(0, 0, 0);
+  const V3 wi = b.local(wi_w), wo = b.local(wo_w);
+  if (b.kind == kMetal) return microfacet_eval(b, wi, wo);
+  V3 f = diffuse_eval(b, wi, wo);
+  if (b.kind == kPlastic) f = f + microfacet_eval(b, wi, wo);
+  return f;
+}
+
+// The derivative of bsdf_eval with respect to kd (per channel): the diffuse
+// component evaluated with kd = 1 (zero for metal, whose BSDF has no kd).
+__device__ V3 bsdf_eval_dkd(const Bsdf &b, V3 wi_w, V3 wo_w) {
+  if (b.kind == kMetal || !(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f)) return v3(0, 0, 0);
+  Bsdf u = b;
+  u.kd = v3(1.0f, 1.0f, 1.0f);
+  return diffuse_eval(u, b.local(wi_w), b.local(wo_w));
+}
+
+// BSDF::PDF (Core/BSDF.cpp:42-58): average of the component densities.
+__device__ float bsdf_pdf(const Bsdf &b, V3 wi_w, V3 wo_w) {
+  const V3 wi = b.local(wi_w), wo = b.local(wo_w);
+  if (b.kind == kMetal) return microfacet_pdf(b, wi, wo);
+  if (b.kind == kPlastic) return 0.5f * (diffuse_pdf(wi, wo) + microfacet_pdf(b, wi, wo));
+  return diffuse_pdf(wi, wo);
+}
+
+// BSDF::Sample (Core/BSDF.cpp:110-168) over the non-specular components:
+// pick a component uniformly, sample it, average the densities of all
+// components at the sampled direction, evaluate the whole BSDF.
+__device__ V3 bsdf_sample(const Bsdf &b, V3 wi_w, float uc, float u0, float u1, V3 &wo_w, float &pdf) {
+  const V3 wi = b.local(wi_w);
+  const int nc = b.components();
+  const int comp = min((int)(uc * nc), nc - 1);
+  V3 wo;
+  const bool glossy = b.kind == kMetal || (b.kind == kPlastic && comp == 1);
+  if (glossy) {
+    // BlinnDistribution::Sample (BlinnDistribution.h:86-101)
+    const float ct = powf(u0, 1.0f / (b.exponent + 1.0f));
+    const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+    const float phi = u1 * 2.0f * kPi;
+    V3 h = v3(st * cosf(phi), st * sinf(phi), ct);
+    if (wi.z * h.z < 0.0f) h.z = -h.z;
+    wo = h * (2.0f * dot(wi, h)) - wi;
+    if (wi.z * wo.z < 0.0f) {  // Microfacet::Sample rejects the wrong hemisphere
+      pdf = 0.0f;
+      wo_w = b.world(wo);
+      return v3(0, 0, 0);
+    }
+  } else {
+    // BxDF::Sample (Core/BxDF.cpp:20-31): cosine hemisphere on the incident side
+    wo = cosine_hemisphere(u0, u1);
+    if (wi.z < 0.0f) wo.z = -wo.z;
+  }
+  wo_w = b.world(wo);
+  if (b.kind == kMetal) {
+    pdf = microfacet_pdf(b, wi, wo);
+  } else if (b.kind == kPlastic) {
+    pdf = 0.5f * (diffuse_pdf(wi, wo) + microfacet_pdf(b, wi, wo));
+  } else {
+    pdf = diffuse_pdf(wi, wo);
+  }
+  return bsdf_eval(b, wi_w, wo_w);
+}
+
+// ------------------------------------------------------------------ shading --
+struct Hit {
+  V3 p, ng, ns;
+  V3 v0, cr;  // triangle vertex 0 and (v1 - v0) x (v2 - v0), for the next ray's tmin
+  int g;      // global triangle
+};
+
+// Ray start offset for leaving a surface: past the point where the ray
+// crosses the triangle's plane (CoreUtils::GetNextMinT, CoreUtils.h:139-149),
+// plus a margin for the float hit point.
+__device__ __forceinline__ float next_min_t(const Hit &h, V3 w, float scene_abs) {
+  const float den = dot(w, h.cr);
+  float t = 0.0f;
+  if (den != 0.0f) t = fmaxf(0.0f, dot(h.v0 - h.p, h.cr) / den);
+  return t + 2.0e-6f * (1.0f + scene_abs);
+}
+
+__device__ Bsdf make_bsdf(const SceneDev &S, const Hit &h, int prim) {
+  const DevMaterial m = S.materials[S.prim_material[prim]];
+  Bsdf b;
+  b.ng = h.ng;
+  b.n = h.ns;
+  // Any frame around the shading normal: all the BxDFs here are isotropic.
+  const V3 a = fabsf(b.n.x) > 0.9f ? v3(0, 1, 0) : v3(1, 0, 0);
+  b.e1 = normalized(cross(a, b.n));
+  b.e2 = cross(b.n, b.e1);
+  b.kind = m.kind;
+  b.kd = load3(m.kd);
+  if (S.tri_albedo) {
+    const float *ta = S.tri_albedo + 3 * (int64_t)h.g;
+    if (ta[0] == ta[0]) b.kd = v3(fminf(1.0f, fmaxf(0.0f, ta[0])), fminf(1.0f, fmaxf(0.0f, ta[1])),
+                                  fminf(1.0f, fmaxf(0.0f, ta[2])));
+  }
+  b.ks = load3(m.ks);
+  b.exponent = m.exponent;
+  b.on_a = m.on_a;
+  b.on_b = m.on_b;
+  b.eta = load3(m.eta);
+  b.k2 = load3(m.k2);
+  return b;
+}
+
+__device__ Hit make_hit(const SceneDev &S, V3 o, V3 d, float t, int prim, int tri) {
+  Hit h;
+  h.g = S.prim_tri_offset[prim] + tri;
+  const int i0 = S.tri_vidx[3 * h.g], i1 = S.tri_vidx[3 * h.g + 1], i2 = S.tri_vidx[3 * h.g + 2];
+  const V3 p0 = load3(S.vpos + 3 * i0), p1 = load3(S.vpos + 3 * i1), p2 = load3(S.vpos + 3 * i2);
+  h.p = o + d * t;
+  h.v0 = p0;
+  h.cr = cross(p1 - p0, p2 - p0);
+  h.ng = normalized(h.cr);
+  h.ns = h.ng;
+  if (S.prim_has_normals[prim]) {
+    // barycentrics of the hit point (Moller-Trumbore), then the
+    // interpolated vertex normal (TriangleMesh.cpp:478-484)
+    const V3 e1 = p1 - p0, e2 = p2 - p0, s1 = cross(d, e2);
+    const float inv = 1.0f / dot(s1, e1);
+    const V3 dd = o - p0;
+    const float b1 = dot(dd, s1) * inv;
+    const float b2 = dot(d, cross(dd, e1)) * inv;
+    const float b0 = 1.0f - b1 - b2;
+    const V3 n = load3(S.vnrm + 3 * i0) * b0 + load3(S.vnrm + 3 * i1) * b1 + load3(S.vnrm + 3 * i2) * b2;
+    h.ns = normalized(n);
+  }
+  return h;
+}
+
+// Warp-aggregated append: one atomic per warp for the lanes with `want`.
+__device__ __forceinline__ int queue_append(bool want, int *count) {
+  const unsigned mask = __ballot_sync(__activemask(), want);
+  if (!want) return -1;
+  const int leader = __ffs(mask) - 1;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void store_ray(float4 *rays, int i, V3 o, V3 d, float tmin, float tmax) {
+  rays[2 * i] = make_float4(o.x, o.y, o.z, d.x);
+  rays[2 * i + 1] = make_float4(d.y, d.z, tmin, tmax);
+}
+
+__device__ __forceinline__ void store_rgb(float *c, int64_t slot, V3 v) {
+  c[3 * slot] = v.x;
+  c[3 * slot + 1] = v.y;
+  c[3 * slot + 2] = v.z;
+}
+
+}  // namespace
+}  // namespace skw

@@ -10,6 +10,7 @@
 
 #include "../../include/skw.h"
 #include "accel_build.h"
+#include "render_scene.h"
 
 struct skw_ctx {
   int device = 0;
@@ -32,6 +33,16 @@ struct skw_accel {
   skw_accel_info info{};
   std::vector<skw::DevNode> h_nodes;
   std::vector<skw::DevTri> h_tris;
+};
+
+// A render scene (skw_scene_create): its accelerator plus the shading data.
+struct skw_scene {
+  skw_ctx *ctx = nullptr;
+  skw_accel *accel = nullptr;
+  int64_t n_triangles = 0;  // mesh order, over all primitives
+  double total_area = 0.0;  // sum of the primitives' mesh areas (TriangleMesh::GetArea, mesh space)
+  std::vector<void *> buffers;  // device allocations owned by the scene
+  skw::SceneDev dev{};
 };
 
 namespace skw {

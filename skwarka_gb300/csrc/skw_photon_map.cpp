@@ -1,0 +1,461 @@
+// C ABI (include/skw.h): photon maps -- GPU photon shooting, the three photon
+// kd-trees (built on the host for tree identity with the reference) and the
+// irradiance photon map (PhotonLTEIntegrator::_ConstructIrradiancePhotonMap,
+// LTEIntegrators/PhotonLTEIntegrator/PhotonLTEIntegrator.cpp:171-245).
+#include "../../include/skw.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <new>
+#include <vector>
+
+#include "kernels.h"
+#include "photon_tree.h"
+#include "photon_types.h"
+#include "skw_internal.h"
+
+using skw::cuda_fail;
+using skw::fail;
+using skw::PhotonRec;
+
+namespace {
+
+constexpr double kMaxNormalDeviationCos = 0.87;  // PhotonLTEIntegrator.cpp:26
+constexpr int kLookupIrradiance = 100;            // LOOKUP_PHOTONS_NUM_FOR_IRRADIANCE (PhotonLTEIntegrator.h:218)
+constexpr int64_t kMaxPhotonsInMap = 40000000;    // MAX_PHOTONS_IN_MAP (PhotonLTEIntegrator.h:224)
+constexpr double kInvPi = 0.31830988618379067154;
+
+// One photon kd-tree on the device: KdNode per tree position plus the
+// photon's normal id, incident-direction id and weight in tree order.
+struct Map {
+  int64_t n = 0;
+  int64_t paths = 0;
+  std::vector<PhotonRec> input;  // the photons in the order they were given (path order)
+  std::vector<int32_t> perm;     // tree position -> input index
+  void *d_nodes = nullptr;
+  uint16_t *d_nids = nullptr, *d_dirid = nullptr;
+  float *d_weight = nullptr;
+};
+
+}  // namespace
+
+struct skw_photon_map {
+  skw_ctx *ctx = nullptr;
+  Map maps[3];  // caustic, direct, indirect
+  double scene_area = 0.0;
+  double lookup_dist[3] = {0, 0, 0};  // irradiance-estimate radii per map
+  // irradiance photons, tree order
+  int64_t n_irr = 0;
+  std::vector<float> irr_pos, irr_ext, irr_int;
+  std::vector<uint16_t> irr_nrm;
+  void *d_irr_nodes = nullptr;
+  uint16_t *d_irr_nids = nullptr;
+  float *d_irr_ext = nullptr, *d_irr_int = nullptr;
+  double max_irr_dist = std::numeric_limits<double>::infinity();
+  double *d_dirs = nullptr;
+  unsigned *d_status = nullptr;
+  double shoot_ms = 0.0, build_ms = 0.0;
+};
+
+namespace {
+
+template <class T>
+cudaError_t upload(const std::vector<T> &v, T **out) {
+  *out = nullptr;
+  const size_t b = std::max<size_t>(v.size(), 1) * sizeof(T);
+  cudaError_t e = cudaMalloc((void **)out, b);
+  if (e == cudaSuccess && !v.empty()) e = cudaMemcpy(*out, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return e;
+}
+
+void free_map(Map &m) {
+  cudaFree(m.d_nodes);
+  cudaFree(m.d_nids);
+  cudaFree(m.d_dirid);
+  cudaFree(m.d_weight);
+  m.d_nodes = nullptr;
+  m.d_nids = m.d_dirid = nullptr;
+  m.d_weight = nullptr;
+}
+
+// KDTree<Photon>(photons) (Core/KDTree.h:428-473) on the host, then upload.
+cudaError_t build_map(Map &m) {
+  m.n = (int64_t)m.input.size();
+  std::vector<float> pos((size_t)m.n * 3);
+  for (int64_t i = 0; i < m.n; ++i)
+    for (int k = 0; k < 3; ++k) pos[(size_t)(3 * i + k)] = m.input[(size_t)i].p[k];
+  std::vector<skw::KdNode> nodes;
+  skw::build_photon_tree(pos.data(), m.n, 0, nodes, m.perm);
+  std::vector<uint16_t> nids((size_t)m.n), dirid((size_t)m.n);
+  std::vector<float> w((size_t)m.n * 3);
+  for (int64_t t = 0; t < m.n; ++t) {
+    const PhotonRec &r = m.input[(size_t)m.perm[(size_t)t]];
+    nids[(size_t)t] = r.nrm;
+    dirid[(size_t)t] = r.dir;
+    for (int k = 0; k < 3; ++k) w[(size_t)(3 * t + k)] = r.w[k];
+  }
+  skw::KdNode *dn = nullptr;
+  cudaError_t e = upload(nodes, &dn);
+  m.d_nodes = dn;
+  if (e == cudaSuccess) e = upload(nids, &m.d_nids);
+  if (e == cudaSuccess) e = upload(dirid, &m.d_dirid);
+  if (e == cudaSuccess) e = upload(w, &m.d_weight);
+  return e;
+}
+
+const PhotonRec &tree_photon(const Map &m, int64_t t) { return m.input[(size_t)m.perm[(size_t)t]]; }
+
+// _ConstructIrradiancePhotonMap: every 10th indirect photon (in tree order)
+// becomes an irradiance photon whose irradiance is estimated from the three
+// maps; then the 0.1 % percentile of the distance from every 11th indirect
+// photon to its nearest irradiance photon bounds the irradiance lookups.
+int build_irradiance(skw_photon_map *pm, cudaStream_t st) {
+  skw_ctx *ctx = pm->ctx;
+  const Map &dm = pm->maps[1], &im = pm->maps[2];
+  const std::vector<double> &dirs = skw::direction_table();
+  if (im.n == 0) return SKW_OK;  // no indirect map: nothing to do
+  for (int64_t i = 0; i < im.n; i += 10) {
+    const PhotonRec &r = tree_photon(im, i);
+    pm->irr_pos.insert(pm->irr_pos.end(), r.p, r.p + 3);
+    pm->irr_nrm.push_back(r.nrm);
+  }
+  const int64_t nq = (int64_t)pm->irr_nrm.size();
+  const double da = dm.n == 0 ? 0.0 : pm->scene_area / dm.n;
+  const double ia = im.n == 0 ? 0.0 : pm->scene_area / im.n;
+  pm->lookup_dist[1] = std::sqrt(da * kLookupIrradiance * kInvPi);
+  pm->lookup_dist[2] = std::sqrt(ia * kLookupIrradiance * kInvPi);
+  pm->lookup_dist[0] = std::max(pm->lookup_dist[1], pm->lookup_dist[2]);
+  std::vector<double> q((size_t)nq * 3), qn((size_t)nq * 3);
+  for (int64_t i = 0; i < nq; ++i)
+    for (int k = 0; k < 3; ++k) {
+      q[(size_t)(3 * i + k)] = (double)pm->irr_pos[(size_t)(3 * i + k)];
+      qn[(size_t)(3 * i + k)] = dirs[3 * (size_t)pm->irr_nrm[(size_t)i] + k];
+    }
+  // Lookups in chunks of queries (k-NN output is 12 bytes per neighbour).
+  const int64_t chunk = std::min<int64_t>(nq, (int64_t)1 << 20);
+  double *d_q = nullptr, *d_qn = nullptr;
+  int32_t *d_idx = nullptr, *d_cnt = nullptr;
+  double *d_d2 = nullptr;
+  float *d_ext = nullptr, *d_int = nullptr;
+  cudaError_t e = cudaMalloc(&d_q, (size_t)nq * 24);
+  if (e == cudaSuccess) e = cudaMalloc(&d_qn, (size_t)nq * 24);
+  if (e == cudaSuccess) e = cudaMalloc(&d_idx, (size_t)chunk * kLookupIrradiance * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&d_d2, (size_t)chunk * kLookupIrradiance * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&d_cnt, (size_t)chunk * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&d_ext, (size_t)nq * 12);
+  if (e == cudaSuccess) e = cudaMalloc(&d_int, (size_t)nq * 12);
+  if (e == cudaSuccess) e = cudaMemcpy(d_q, q.data(), (size_t)nq * 24, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_qn, qn.data(), (size_t)nq * 24, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_ext, 0, (size_t)nq * 12, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_int, 0, (size_t)nq * 12, st);
+  bool first = true;
+  for (int mi = 0; mi < 3 && e == cudaSuccess; ++mi) {
+    const Map &m = pm->maps[mi];
+    if (m.n == 0) continue;  // a null map adds nothing
+    for (int64_t q0 = 0; q0 < nq && e == cudaSuccess; q0 += chunk) {
+      const int64_t c = std::min(chunk, nq - q0);
+      e = skw::launch_knn(m.d_nodes, m.d_nids, pm->d_dirs, (int)m.n, d_q + 3 * q0, d_qn + 3 * q0, c,
+                          kLookupIrradiance, pm->lookup_dist[mi], kMaxNormalDeviationCos, d_idx, d_d2, d_cnt, nullptr,
+                          nullptr, pm->d_status, st);
+      if (e == cudaSuccess)
+        e = skw::launch_irradiance_sum(m.d_nodes, m.d_weight, m.d_dirid, pm->d_dirs, d_q + 3 * q0, d_qn + 3 * q0,
+                                       d_idx, d_cnt, c, kLookupIrradiance, (double)m.paths, pm->lookup_dist[mi], first,
+                                       d_ext + 3 * q0, d_int + 3 * q0, st);
+    }
+    first = false;
+  }
+  std::vector<float> ext((size_t)nq * 3), intr((size_t)nq * 3);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ext.data(), d_ext, (size_t)nq * 12, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(intr.data(), d_int, (size_t)nq * 12, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_q);
+  cudaFree(d_qn);
+  cudaFree(d_idx);
+  cudaFree(d_d2);
+  cudaFree(d_cnt);
+  cudaFree(d_ext);
+  cudaFree(d_int);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "irradiance photon estimates");
+  // KDTree<IrradiancePhoton>(irradiance_photons)
+  std::vector<skw::KdNode> nodes;
+  std::vector<int32_t> perm;
+  skw::build_photon_tree(pm->irr_pos.data(), nq, 0, nodes, perm);
+  std::vector<float> pos_t((size_t)nq * 3), ext_t((size_t)nq * 3), int_t((size_t)nq * 3);
+  std::vector<uint16_t> nrm_t((size_t)nq);
+  for (int64_t t = 0; t < nq; ++t) {
+    const int32_t s = perm[(size_t)t];
+    for (int k = 0; k < 3; ++k) {
+      pos_t[(size_t)(3 * t + k)] = pm->irr_pos[(size_t)(3 * s + k)];
+      ext_t[(size_t)(3 * t + k)] = ext[(size_t)(3 * s + k)];
+      int_t[(size_t)(3 * t + k)] = intr[(size_t)(3 * s + k)];
+    }
+    nrm_t[(size_t)t] = pm->irr_nrm[(size_t)s];
+  }
+  pm->irr_pos.swap(pos_t);
+  pm->irr_nrm.swap(nrm_t);
+  pm->irr_ext.swap(ext_t);
+  pm->irr_int.swap(int_t);
+  pm->n_irr = nq;
+  skw::KdNode *dn = nullptr;
+  e = upload(nodes, &dn);
+  pm->d_irr_nodes = dn;
+  if (e == cudaSuccess) e = upload(pm->irr_nrm, &pm->d_irr_nids);
+  if (e == cudaSuccess) e = upload(pm->irr_ext, &pm->d_irr_ext);
+  if (e == cudaSuccess) e = upload(pm->irr_int, &pm->d_irr_int);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "irradiance map upload");
+  // max irradiance lookup distance from every 11th indirect photon
+  const int64_t step = 11, ns = (im.n + step - 1) / step;
+  std::vector<double> sq((size_t)ns * 3), sqn((size_t)ns * 3);
+  for (int64_t i = 0; i < ns; ++i) {
+    const PhotonRec &r = tree_photon(im, i * step);
+    for (int k = 0; k < 3; ++k) {
+      sq[(size_t)(3 * i + k)] = (double)r.p[k];
+      sqn[(size_t)(3 * i + k)] = dirs[3 * (size_t)r.nrm + k];
+    }
+  }
+  std::vector<int32_t> nearest((size_t)ns);
+  double *d_sq = nullptr, *d_sqn = nullptr;
+  int32_t *d_near = nullptr;
+  e = cudaMalloc(&d_sq, (size_t)ns * 24);
+  if (e == cudaSuccess) e = cudaMalloc(&d_sqn, (size_t)ns * 24);
+  if (e == cudaSuccess) e = cudaMalloc(&d_near, (size_t)ns * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(d_sq, sq.data(), (size_t)ns * 24, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_sqn, sqn.data(), (size_t)ns * 24, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = skw::launch_nearest(pm->d_irr_nodes, pm->d_irr_nids, pm->d_dirs, (int)nq, d_sq, d_sqn, ns,
+                            std::numeric_limits<double>::infinity(), kMaxNormalDeviationCos, d_near, pm->d_status, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(nearest.data(), d_near, (size_t)ns * 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_sq);
+  cudaFree(d_sqn);
+  cudaFree(d_near);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "irradiance lookup distance");
+  std::vector<double> d2((size_t)ns, 0.0);
+  for (int64_t i = 0; i < ns; ++i) {
+    const int32_t t = nearest[(size_t)i];
+    if (t < 0) continue;  // no irradiance photon: 0 keeps it out of the percentile
+    double s = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double d = sq[(size_t)(3 * i + k)] - (double)pm->irr_pos[(size_t)(3 * t + k)];
+      s += d * d;
+    }
+    d2[(size_t)i] = s;
+  }
+  const size_t index = d2.size() <= 1 ? 0 : std::max(d2.size() / 1000, (size_t)1);
+  std::nth_element(d2.begin(), d2.begin() + (ptrdiff_t)index, d2.end(), std::greater<double>());
+  pm->max_irr_dist = d2[index] == 0.0 ? std::numeric_limits<double>::infinity() : std::sqrt(d2[index]);
+  return SKW_OK;
+}
+
+int finish_map(skw_photon_map *pm, cudaStream_t st) {
+  const auto t0 = std::chrono::steady_clock::now();
+  cudaError_t e = cudaSetDevice(pm->ctx->device);
+  const std::vector<double> &dirs = skw::direction_table();
+  if (e == cudaSuccess) e = upload(dirs, &pm->d_dirs);
+  if (e == cudaSuccess) e = cudaMalloc(&pm->d_status, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(pm->d_status, 0, sizeof(unsigned));
+  for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = build_map(pm->maps[i]);
+  if (e != cudaSuccess) return cuda_fail(pm->ctx, e, "photon map upload");
+  int rc = build_irradiance(pm, st);
+  pm->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int skw_photon_map_create(skw_ctx *ctx, const skw_photon *const *photons, const int64_t *n, const int64_t *paths,
+                          double scene_area, skw_photon_map **out) {
+  if (!ctx || !photons || !n || !paths || !out) return fail(ctx, SKW_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (!(scene_area >= 0.0)) return fail(ctx, SKW_ERR_ARG, "scene_area must be >= 0");
+  for (int i = 0; i < 3; ++i) {
+    if (n[i] < 0 || n[i] > kMaxPhotonsInMap || (n[i] > 0 && !photons[i]) || paths[i] < 0)
+      return fail(ctx, SKW_ERR_ARG, "bad photon array");
+  }
+  if (n[2] > 0 && n[1] == 0) return fail(ctx, SKW_ERR_ARG, "an indirect map needs a direct map");
+  auto *pm = new (std::nothrow) skw_photon_map();
+  if (!pm) return fail(ctx, SKW_ERR_OOM, "host allocation");
+  pm->ctx = ctx;
+  pm->scene_area = scene_area;
+  for (int i = 0; i < 3; ++i) {
+    const PhotonRec *p = reinterpret_cast<const PhotonRec *>(photons[i]);
+    pm->maps[i].input.assign(p, p + n[i]);
+    pm->maps[i].paths = paths[i];
+  }
+  int rc = finish_map(pm, nullptr);
+  if (rc != SKW_OK) {
+    skw_photon_map_destroy(pm);
+    return rc;
+  }
+  *out = pm;
+  return SKW_OK;
+}
+
+int skw_photon_shoot(skw_scene *s, const skw_photon_params *params, skw_photon_map **out) {
+  if (!s || !params || !out) return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "null argument");
+  skw_ctx *ctx = s->ctx;
+  *out = nullptr;
+  if (params->paths <= 0 || params->paths > ((int64_t)1 << 31) || params->max_bounces < 1 ||
+      params->max_bounces > 64 || !(params->rr_probability >= 0.0f) || params->rr_probability > 1.0f)
+    return fail(ctx, SKW_ERR_ARG, "bad photon parameters");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  const auto t0 = std::chrono::steady_clock::now();
+  // Lights by the luminance of their power (PhotonLTEIntegrator.cpp:80-125):
+  // PointLight::Power = 4 pi I, DiffuseAreaLightSource::Power = pi A L.
+  const skw::SceneDev &S = s->dev;
+  std::vector<skw::PointLightDev> pls((size_t)S.n_point_lights);
+  std::vector<skw::AreaLight> als((size_t)S.n_area_lights);
+  if (!pls.empty()) e = cudaMemcpy(pls.data(), S.point_lights, pls.size() * sizeof(pls[0]), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && !als.empty())
+    e = cudaMemcpy(als.data(), S.area_lights, als.size() * sizeof(als[0]), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "light table");
+  const double lw[3] = {0.05316285, 0.58515348, 0.36168367};
+  std::vector<skw::PhotonLight> lights;
+  std::vector<double> power;
+  for (size_t i = 0; i < pls.size(); ++i) {
+    double p = 0;
+    for (int k = 0; k < 3; ++k) p += lw[k] * 4.0 * M_PI * pls[i].intensity[k];
+    lights.push_back({0.0, 0, (int32_t)i});
+    power.push_back(p);
+  }
+  for (size_t i = 0; i < als.size(); ++i) {
+    double p = 0;
+    for (int k = 0; k < 3; ++k) p += lw[k] * M_PI * als[i].area * als[i].radiance[k] * S.emission_scale;
+    lights.push_back({0.0, 1, (int32_t)i});
+    power.push_back(p);
+  }
+  if (lights.empty()) return fail(ctx, SKW_ERR_ARG, "the scene has no lights");
+  for (size_t i = 1; i < power.size(); ++i) power[i] += power[i - 1];
+  const double total = power.back();
+  for (size_t i = 0; i < power.size(); ++i) lights[i].cdf = total > 2.220446049250313e-16 ? power[i] / total : 0.0;
+  if (!(total > 2.220446049250313e-16)) lights.back().cdf = 1.0;
+  skw::PhotonLight *d_lights = nullptr;
+  if ((e = upload(lights, &d_lights)) != cudaSuccess) return cuda_fail(ctx, e, "light table");
+  skw::PhotonShootArgs A{d_lights, (int32_t)lights.size(), params->max_bounces, params->rr_probability, params->seed};
+  skw_accel *a = s->accel;
+  skw::TraceFn trace = [a](const void *rays, int64_t n, const int *n_dev, void *hits, cudaStream_t st) {
+    return skw::launch_traversal(true, a->stack_cap, a->d_nodes, a->d_tris, rays, n, n_dev, a->scene_abs, nullptr,
+                                 hits, a->d_status, st);
+  };
+  const int64_t chunk = std::min<int64_t>(params->paths, (int64_t)1 << 20);
+  const int64_t B1 = std::max(params->max_bounces - 1, 1);
+  void *ws = nullptr;
+  PhotonRec *d_dir = nullptr, *d_ind = nullptr;
+  int *d_tot = nullptr;
+  cudaStream_t st = nullptr;
+  e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&ws, skw::photon_chunk_bytes(chunk, params->max_bounces));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_dir, (size_t)chunk * sizeof(PhotonRec));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_ind, (size_t)(chunk * B1) * sizeof(PhotonRec));
+  if (e == cudaSuccess) e = cudaMalloc(&d_tot, 2 * sizeof(int));
+  auto *pm = new (std::nothrow) skw_photon_map();
+  if (!pm) e = cudaErrorMemoryAllocation;
+  int64_t launches = 0;
+  for (int64_t p0 = 0; p0 < params->paths && e == cudaSuccess; p0 += chunk) {
+    const int n = (int)std::min(chunk, params->paths - p0);
+    e = skw::photon_shoot_chunk(S, A, trace, p0, n, ws, d_dir, d_ind, d_tot, st);
+    int tot[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(tot, d_tot, sizeof(tot), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) break;
+    Map &dm = pm->maps[1], &im = pm->maps[2];
+    const size_t od = dm.input.size(), oi = im.input.size();
+    dm.input.resize(od + (size_t)tot[0]);
+    im.input.resize(oi + (size_t)tot[1]);
+    if (tot[0] > 0) e = cudaMemcpy(dm.input.data() + od, d_dir, (size_t)tot[0] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && tot[1] > 0)
+      e = cudaMemcpy(im.input.data() + oi, d_ind, (size_t)tot[1] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
+    dm.paths += n;
+    im.paths += n;
+    launches += 1 + 2 * params->max_bounces + 6;
+  }
+  cudaFree(ws);
+  cudaFree(d_dir);
+  cudaFree(d_ind);
+  cudaFree(d_tot);
+  cudaFree(d_lights);
+  if (e != cudaSuccess) {
+    if (st) cudaStreamDestroy(st);
+    skw_photon_map_destroy(pm);
+    return cuda_fail(ctx, e, "photon shooting");
+  }
+  ctx->launches.fetch_add(launches);
+  pm->ctx = ctx;
+  pm->scene_area = s->total_area;
+  pm->shoot_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  for (int i = 0; i < 3; ++i)
+    if ((int64_t)pm->maps[i].input.size() > kMaxPhotonsInMap) {
+      cudaStreamDestroy(st);
+      skw_photon_map_destroy(pm);
+      return fail(ctx, SKW_ERR_BUDGET, "a photon map exceeds 40M photons (the reference's MAX_PHOTONS_IN_MAP)");
+    }
+  if (pm->maps[1].input.empty()) pm->maps[1].paths = 0;
+  if (pm->maps[2].input.empty()) pm->maps[2].paths = 0;
+  int rc = finish_map(pm, st);
+  cudaStreamDestroy(st);
+  if (rc != SKW_OK) {
+    skw_photon_map_destroy(pm);
+    return rc;
+  }
+  *out = pm;
+  return SKW_OK;
+}
+
+void skw_photon_map_destroy(skw_photon_map *pm) {
+  if (!pm) return;
+  for (Map &m : pm->maps) free_map(m);
+  cudaFree(pm->d_irr_nodes);
+  cudaFree(pm->d_irr_nids);
+  cudaFree(pm->d_irr_ext);
+  cudaFree(pm->d_irr_int);
+  cudaFree(pm->d_dirs);
+  cudaFree(pm->d_status);
+  delete pm;
+}
+
+int skw_photon_map_get_info(const skw_photon_map *pm, skw_photon_map_info *out) {
+  if (!pm || !out) return SKW_ERR_ARG;
+  std::memset(out, 0, sizeof(*out));
+  out->n_caustic = pm->maps[0].n;
+  out->n_direct = pm->maps[1].n;
+  out->n_indirect = pm->maps[2].n;
+  out->n_irradiance = pm->n_irr;
+  out->paths_caustic = pm->maps[0].paths;
+  out->paths_direct = pm->maps[1].paths;
+  out->paths_indirect = pm->maps[2].paths;
+  out->max_irradiance_lookup_dist = pm->max_irr_dist;
+  out->scene_area = pm->scene_area;
+  out->shoot_ms = pm->shoot_ms;
+  out->build_ms = pm->build_ms;
+  return SKW_OK;
+}
+
+int skw_photon_map_export(const skw_photon_map *pm, int32_t which, skw_photon *out) {
+  if (!pm || which < 0 || which > 2 || (!out && pm->maps[which].n > 0)) return SKW_ERR_ARG;
+  const Map &m = pm->maps[which];
+  if (m.n > 0) std::memcpy(out, m.input.data(), (size_t)m.n * sizeof(PhotonRec));
+  return SKW_OK;
+}
+
+int skw_photon_map_export_irradiance(const skw_photon_map *pm, float *pos, float *ext, float *intr, uint16_t *nrm) {
+  if (!pm) return SKW_ERR_ARG;
+  const size_t n = (size_t)pm->n_irr;
+  if (n == 0) return SKW_OK;
+  if (!pos || !ext || !intr || !nrm) return SKW_ERR_ARG;
+  std::memcpy(pos, pm->irr_pos.data(), n * 12);
+  std::memcpy(ext, pm->irr_ext.data(), n * 12);
+  std::memcpy(intr, pm->irr_int.data(), n * 12);
+  std::memcpy(nrm, pm->irr_nrm.data(), n * 2);
+  return SKW_OK;
+}
+
+}  // extern "C"

@@ -17,14 +17,6 @@
 using skw::cuda_fail;
 using skw::fail;
 
-struct skw_scene {
-  skw_ctx *ctx = nullptr;
-  skw_accel *accel = nullptr;
-  int64_t n_triangles = 0;  // mesh order, over all primitives
-  std::vector<void *> buffers;  // device allocations owned by the scene
-  skw::SceneDev dev{};
-};
-
 namespace {
 
 template <class T>
@@ -171,6 +163,7 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
     double area_sum = 0.0;
     std::vector<double> areas;
     int32_t kept = 0;
+    float mesh_area = 0.0f;
     for (int64_t t = 0; t < m.n_triangles; ++t) {
       const int32_t *ix = m.triangles + 3 * t;
       bool bad = false;
@@ -198,7 +191,16 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
         light_tri.push_back(tri_count + kept);
       }
       ++kept;
+      // TriangleMesh's area: Triangle3D<float>::GetArea summed in float
+      // (Core/TriangleMesh.cpp:193-205, Math/Triangle3D.h:82-86)
+      {
+        const float *a = m.vertices + 3 * ix[0], *b = m.vertices + 3 * ix[1], *c = m.vertices + 3 * ix[2];
+        const float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+        const float cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        mesh_area += 0.5f * std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+      }
     }
+    s->total_area += (double)mesh_area;
     if (light) {
       L.tri_count = (int32_t)areas.size();
       L.area = (float)area_sum;
@@ -285,6 +287,8 @@ void skw_scene_destroy(skw_scene *s) {
 }
 
 skw_accel *skw_scene_accel(skw_scene *s) { return s ? s->accel : nullptr; }
+
+double skw_scene_total_area(const skw_scene *s) { return s ? s->total_area : -1.0; }
 
 
 }  // extern "C"

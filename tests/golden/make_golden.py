@@ -94,6 +94,18 @@ def render_golden():
     np.savez_compressed(OUT / "direct_planes.npz", **planes)
 
 
+def photon_golden():
+    """The reference's irradiance photon map (_ConstructIrradiancePhotonMap)
+    over the seeded synthetic photon maps of scene_fixtures.synthetic_photon_maps."""
+    maps, paths, area = sf.synthetic_photon_maps()
+    pos, ext, intr, nrm, md = Reference().photon_irradiance(maps, paths, area)
+    np.savez_compressed(OUT / "photon_irradiance.npz", pos=pos, ext=ext, int=intr, nrm=nrm, max_dist=np.float64(md))
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "photon":
+    photon_golden()
+    print("photon golden written")
+
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "render":
     render_golden()
     print("render golden written")

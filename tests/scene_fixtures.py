@@ -178,3 +178,46 @@ def square_light_case(a=0.6, h=1.0, p=(0.3, 0.2)):
     e = 10.0 * (h * h / (r2 * r2)).sum() * (a / n) ** 2
     cam = Camera.look_at((p[0], p[1], 0.5), (p[0], p[1], 0.0), (0, 1, 0), 1e-3, 2, 2)
     return prims, mats, cam, float(e / np.pi)
+
+
+def synthetic_photon_maps(seed=31, sizes=(400, 5000, 8000), paths=(15000, 15000, 15000)):
+    """Photon maps on the inside of the box [-1, 1]^3: every photon on a face
+    (positions uniform on it, the face's inward normal), incident directions
+    mostly from the inside (1 in 8 from behind, to give internal irradiance),
+    weights U[0, 1e-3]^3.  Returns ([caustic, direct, indirect] structured
+    arrays, paths, scene area 24)."""
+    from skwarka_gb300.kdtree import compress_directions
+    from skwarka_gb300.photon import PHOTON_DTYPE
+    rng = np.random.default_rng(seed)
+    maps = []
+    for n in sizes:
+        face = rng.integers(0, 6, size=n)
+        axis, side = face // 2, np.where(face % 2 == 0, -1.0, 1.0)
+        p = rng.uniform(-1.0, 1.0, size=(n, 3))
+        p[np.arange(n), axis] = side
+        nrm = np.zeros((n, 3))
+        nrm[np.arange(n), axis] = -side
+        d = rng.normal(size=(n, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        flip = (d * nrm).sum(1) < 0
+        back = rng.uniform(size=n) < 0.125
+        d[flip ^ back] *= -1.0
+        a = np.zeros(n, PHOTON_DTYPE)
+        a["position"] = p.astype(np.float32)
+        a["weight"] = rng.uniform(0.0, 1e-3, size=(n, 3)).astype(np.float32)
+        a["incident"] = compress_directions(d)
+        a["normal"] = compress_directions(nrm)
+        maps.append(a)
+    return maps, list(paths), 24.0
+
+
+def photon_box_scene(albedo=0.5, intensity=50.0):
+    """A closed box [-1, 1]^3 of matte walls (one albedo) with a point light
+    at (0.1, 0.2, 0.3) of the given intensity: every photon path hits a wall,
+    and with a grey Lambertian albedo the reference's Russian roulette keeps
+    each photon's weight at 4 pi I."""
+    from skwarka_gb300.accel import TriangleMesh
+    from skwarka_gb300.render import Material, PointLight, RenderPrimitive
+    bv, bt = scenes._box_inward()
+    prims = [RenderPrimitive(TriangleMesh(bv, bt), 0)]
+    return prims, [Material(kd=(albedo,) * 3)], [PointLight((0.1, 0.2, 0.3), (intensity,) * 3)]

@@ -1,0 +1,63 @@
+"""GPU photon maps: the irradiance photon map built on the GPU (k = 100
+filtered lookups in the three maps, double sums in the reference's heap
+order) against the reference's (tests/golden/photon_irradiance.npz), bit
+for bit; and GPU photon shooting checked for its invariants."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import scene_fixtures as sf
+from skwarka_gb300.photon import PhotonMap
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden" / "photon_irradiance.npz"
+
+
+def test_irradiance_map_matches_reference(gpu):
+    maps, paths, area = sf.synthetic_photon_maps()
+    pm = PhotonMap.from_arrays(maps, paths, area)
+    info = pm.info()
+    assert (info["n_caustic"], info["n_direct"], info["n_indirect"]) == tuple(len(m) for m in maps)
+    pos, ext, intr, nrm = pm.irradiance_photons()
+    g = np.load(GOLD)
+    assert np.array_equal(pos, g["pos"]) and np.array_equal(nrm, g["nrm"])
+    assert np.array_equal(ext, g["ext"]), np.abs(ext - g["ext"]).max()
+    assert np.array_equal(intr, g["int"]), np.abs(intr - g["int"]).max()
+    assert info["max_irradiance_lookup_dist"] == float(g["max_dist"])
+    for k, m in zip(PhotonMap.MAPS, maps):
+        assert np.array_equal(pm.export(k), m)
+
+
+def test_photon_shooting_invariants(gpu):
+    """Point light in a closed grey box: every path deposits one direct
+    photon, every photon weighs 4 pi I (cosine sampling and the luminance
+    Russian roulette cancel), the direct photons are in path order (the
+    emission directions are radical-inverse sequences of the path index), and
+    the expected indirect photons per path are sum_{k=1}^{B-1} rho^k."""
+    from skwarka_gb300.render import RenderScene
+    rho, inten, paths, B = 0.5, 50.0, 200_000, 12
+    prims, mats, lights = sf.photon_box_scene(rho, inten)
+    sc = RenderScene(prims, mats, lights)
+    pm = PhotonMap.shoot(sc, paths, max_bounces=B, seed=3)
+    info = pm.info()
+    assert info["n_direct"] == paths and info["n_caustic"] == 0
+    assert info["paths_direct"] == paths and info["paths_indirect"] == paths
+    d = pm.export("direct")
+    w = 4 * np.pi * inten
+    assert np.allclose(d["weight"], w, rtol=1e-5)
+    assert np.all(np.abs(d["position"]).max(1) > 0.999)  # on the walls
+    # first photon: direction from radical inverses of path 1 in bases 5 and 7
+    z = 1.0 - 2.0 * 0.2
+    phi = 2 * np.pi * (1.0 / 7.0)
+    v = np.array([np.sqrt(1 - z * z) * np.cos(phi), np.sqrt(1 - z * z) * np.sin(phi), z])
+    o = np.array([0.1, 0.2, 0.3])
+    t = min(((np.sign(v[k]) - o[k]) / v[k]) for k in range(3) if v[k] != 0)
+    assert np.allclose(d["position"][0], o + t * v, atol=1e-5)
+    ind = pm.export("indirect")
+    want = sum(rho ** k for k in range(1, B))
+    got = len(ind) / paths
+    print(f"[photons] indirect per path {got:.4f} expected {want:.4f}; irradiance photons {info['n_irradiance']}")
+    assert abs(got - want) < 0.02
+    assert np.allclose(ind["weight"], w, rtol=1e-4)
+    assert info["n_irradiance"] == (len(ind) + 9) // 10
