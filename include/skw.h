@@ -356,6 +356,22 @@ int skw_photon_map_export(const skw_photon_map *map, int32_t which, skw_photon *
 /* Irradiance photons in kd-tree order: position, external and internal
  * irradiance (3 floats each), normal id. */
 int skw_photon_map_export_irradiance(const skw_photon_map *map, float *pos, float *ext, float *intr, uint16_t *nrm);
+/* Photon-mapping render parameters (PhotonLTEIntegratorParams,
+ * LTEIntegrators/PhotonLTEIntegrator.h:33-70). */
+typedef struct skw_photon_render_params {
+  int32_t gather_samples;   /* final-gather samples per strategy, rounded up to a square as the sampler does */
+} skw_photon_render_params;
+
+/* Renders (camera, params) with PhotonLTEIntegrator::_SurfaceRadiance
+ * (PhotonLTEIntegrator.cpp:320-385): emission + direct lighting (as
+ * skw_render_direct) + final gathering (_FinalGather, :387-577: BSDF- and
+ * photon-guided gather rays, the nearest irradiance photon and
+ * BSDF::TotalScattering at each gather hit).  Maps with caustic photons are
+ * rejected (SKW_ERR_UNSUPPORTED): the caustic lookup is not implemented, and
+ * no BSDF here is specular, so GPU-shot maps never have caustic photons. */
+int skw_render_photon(skw_scene *scene, const skw_photon_map *map, const skw_camera *camera,
+                      const skw_render_params *params, const skw_photon_render_params *photon_params, float *film_rgb,
+                      void *stream);
 /* The scene's total mesh area (TriangleMesh::GetArea summed over the
  * primitives, PhotonLTEIntegrator.cpp:52-55). */
 double skw_scene_total_area(const skw_scene *scene);

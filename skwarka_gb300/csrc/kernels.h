@@ -42,7 +42,7 @@ size_t knn_scratch_bytes(int64_t nq, int k);
 cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                        const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,
                        double *out_d2, int32_t *out_count, int32_t *out_visited, void *scratch, unsigned *status,
-                       cudaStream_t stream);
+                       cudaStream_t stream, const int *nq_dev = nullptr);
 // k-NN with its heaps in the library's static device scratch (no
 // allocation): nq * k must be <= knn_noalloc_capacity() entries, else
 // cudaErrorInvalidValue.  Overlapping calls race on that scratch.
@@ -52,9 +52,11 @@ cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const do
                                int32_t *out_idx, double *out_d2, int32_t *out_count, unsigned *status,
                                cudaStream_t stream);
 // Nearest accepted point per query (-1 if none within max_dist).
+// nq_dev (launch_knn, launch_nearest; may be null): device int holding the
+// number of queries to run (at most nq), for queues filled on the device.
 cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                            const double *qn, int64_t nq, double max_dist, double cos_t, int32_t *out_idx,
-                           unsigned *status, cudaStream_t stream);
+                           unsigned *status, cudaStream_t stream, const int *nq_dev = nullptr);
 
 // Direct-lighting render stages (render.cu); see render_scene.h.
 // A pass covers global pixels [px_begin, px_begin + n_px) of the views'
@@ -106,5 +108,15 @@ cudaError_t launch_irradiance_sum(const void *nodes, const float *weight, const 
                                   const double *q, const double *qn, const int32_t *idx, const int32_t *count,
                                   int64_t nq, int k, double paths, double max_lookup_dist, bool first, float *ext,
                                   float *intr, cudaStream_t st);
+
+// Final gather of a render pass (photon.cu): adds each camera hit's gathered
+// indirect radiance to its slots [base_slot, base_slot + 2 gs) of contrib.
+// gws: gather_bytes(n, gs) bytes of workspace.
+struct GatherMaps;
+size_t gather_bytes(int64_t n, int gs);
+cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev *views, int n_views, int n,
+                          int64_t px_begin, int spp, int slots, int base_slot, int gs, const void *rays,
+                          const void *hits, void *gws, float *contrib, const TraceFn &trace, unsigned *status,
+                          cudaStream_t st);
 
 }  // namespace skw

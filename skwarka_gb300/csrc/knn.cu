@@ -184,8 +184,9 @@ __global__ void __launch_bounds__(128) k_knn(const float4 *__restrict__ nodes, c
                                              double cos_t, int32_t *__restrict__ out_idx,
                                              double *__restrict__ out_d2, int32_t *__restrict__ out_count,
                                              int32_t *__restrict__ out_visited, Cand *__restrict__ scratch,
-                                             unsigned *__restrict__ status) {
+                                             unsigned *__restrict__ status, const int *__restrict__ nq_dev) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (nq_dev && *nq_dev < nq) nq = *nq_dev;
   if (i >= nq) return;
   Query Q;
   Q.q[0] = q[3 * i];
@@ -242,8 +243,10 @@ __global__ void __launch_bounds__(128) k_nearest(const float4 *__restrict__ node
                                                  const double *__restrict__ dirs, int n,
                                                  const double *__restrict__ q, const double *__restrict__ qn,
                                                  int64_t nq, double max_dist, double cos_t,
-                                                 int32_t *__restrict__ out_idx, unsigned *__restrict__ status) {
+                                                 int32_t *__restrict__ out_idx, unsigned *__restrict__ status,
+                                                 const int *__restrict__ nq_dev) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (nq_dev && *nq_dev < nq) nq = *nq_dev;
   if (i >= nq) return;
   Query Q;
   Q.q[0] = q[3 * i];
@@ -278,19 +281,19 @@ size_t knn_scratch_bytes(int64_t nq, int k) { return k > 128 ? (size_t)nq * (siz
 cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                        const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,
                        double *out_d2, int32_t *out_count, int32_t *out_visited, void *scratch, unsigned *status,
-                       cudaStream_t stream) {
+                       cudaStream_t stream, const int *nq_dev) {
   if (nq <= 0) return cudaSuccess;
   const int block = 128;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
   if (k <= 32) {
     k_knn<32><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
-                                           out_idx, out_d2, out_count, out_visited, nullptr, status);
+                                           out_idx, out_d2, out_count, out_visited, nullptr, status, nq_dev);
   } else if (k <= 128) {
     k_knn<128><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
-                                            out_idx, out_d2, out_count, out_visited, nullptr, status);
+                                            out_idx, out_d2, out_count, out_visited, nullptr, status, nq_dev);
   } else {
     k_knn<0><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
-                                          out_idx, out_d2, out_count, out_visited, (Cand *)scratch, status);
+                                          out_idx, out_d2, out_count, out_visited, (Cand *)scratch, status, nq_dev);
   }
   return cudaGetLastError();
 }
@@ -332,18 +335,18 @@ cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const do
   const int block = 128;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
   k_knn<0><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
-                                        out_idx, out_d2, out_count, nullptr, (Cand *)scratch, status);
+                                        out_idx, out_d2, out_count, nullptr, (Cand *)scratch, status, nullptr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                            const double *qn, int64_t nq, double max_dist, double cos_t, int32_t *out_idx,
-                           unsigned *status, cudaStream_t stream) {
+                           unsigned *status, cudaStream_t stream, const int *nq_dev) {
   if (nq <= 0) return cudaSuccess;
   const int block = 128;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
   k_nearest<<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, max_dist, cos_t, out_idx,
-                                        status);
+                                        status, nq_dev);
   return cudaGetLastError();
 }
 

@@ -452,4 +452,345 @@ cudaError_t launch_irradiance_sum(const void *nodes, const float *weight, const 
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ final gather --
+// PhotonLTEIntegrator::_FinalGather (PhotonLTEIntegrator.cpp:387-577) as
+// stages over the camera hits of a render pass:
+//   k_gather_sources  camera hits with a surface -> query points of the
+//                     32-photon lookup in the indirect map
+//   k_gather_rays     gather_samples BSDF-sampled and gather_samples
+//                     photon-guided directions (uniform cone of 10 degrees
+//                     around a found photon's incident direction), each
+//                     weighted with the power heuristic of the two densities
+//   k_trace           closest hit of the gather rays
+//   k_gather_hits     at each gather hit: BSDF::TotalScattering over the
+//                     reflection components (a 5x5 grid of samples) and the
+//                     query of the nearest irradiance photon
+//   k_gather_resolve  TotalScattering * irradiance / pi * weight / gather_samples
+namespace {
+
+constexpr double kCosGather = 0.9848;  // 10 degrees (PhotonLTEIntegrator.cpp:397)
+constexpr int kGatherLookup = 32;      // :446-456
+
+// The gather stages' random numbers: a stream of their own per sample.
+__device__ __forceinline__ float rnd_g(uint64_t seed, uint64_t gid, uint32_t d) {
+  return rnd(seed ^ 0x5851F42D4C957F2Dull, gid * 8ull + (d >> 6), d & 63u);
+}
+
+struct GatherArgs {
+  int n;               // samples in the pass
+  int64_t px_begin;
+  int spp;
+  int slots;
+  int base_slot;       // first gather slot of a sample
+  int gs;              // gather samples (a square, as the sampler rounds it)
+  const ViewDev *views;
+  int n_views;
+};
+
+__global__ void k_gather_sources(SceneDev S, GatherArgs G, const float4 *__restrict__ rays,
+                                 const int4 *__restrict__ hits, int *__restrict__ src, double *__restrict__ q,
+                                 double *__restrict__ qn, int *__restrict__ count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool ok = false;
+  Hit h{};
+  if (i < G.n) {
+    const int4 hit = hits[i];
+    if (hit.y >= 0) {
+      const float4 ra = rays[2 * i], rb = rays[2 * i + 1];
+      h = make_hit(S, v3(ra.x, ra.y, ra.z), v3(ra.w, rb.x, rb.y), __int_as_float(hit.x), hit.y, hit.z);
+      ok = true;
+    }
+  }
+  const int j = queue_append(ok, count);
+  if (ok) {
+    src[j] = i;
+    q[3 * j] = h.p.x;
+    q[3 * j + 1] = h.p.y;
+    q[3 * j + 2] = h.p.z;
+    qn[3 * j] = h.ng.x;
+    qn[3 * j + 1] = h.ng.y;
+    qn[3 * j + 2] = h.ng.z;
+  }
+}
+
+__device__ __forceinline__ float photon_pdf_of(const V3 *pd, int found, V3 w) {
+  // uniform cones around the found photons' directions (:473-481, 515-523)
+  const float cone_pdf = (float)(1.0 / (2.0 * 3.14159265358979323846 * (1.0 - kCosGather)));
+  int c = 0;
+  for (int j = 0; j < found; ++j) c += dot(pd[j], w) > (float)kCosGather ? 1 : 0;
+  return found > 0 ? c * cone_pdf / found : 0.0f;
+}
+
+__global__ void __launch_bounds__(128) k_gather_rays(SceneDev S, GatherArgs G, GatherMaps M,
+                                                     const float4 *__restrict__ rays, const int4 *__restrict__ hits,
+                                                     const int *__restrict__ src, const int *__restrict__ src_count,
+                                                     const int32_t *__restrict__ kidx,
+                                                     const int32_t *__restrict__ kcount, float4 *__restrict__ grays,
+                                                     int *__restrict__ gtarget, float *__restrict__ gweight,
+                                                     int *__restrict__ gcount) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = j < *src_count;
+  Hit h{};
+  Bsdf b{};
+  V3 wo = v3(0, 0, 0);
+  uint64_t gid = 0, seed = 0;
+  int64_t slot0 = 0;
+  int found = 0;
+  V3 pd[kGatherLookup];
+  if (valid) {
+    const int i = src[j];
+    const int4 hit = hits[i];
+    const float4 ra = rays[2 * i], rb = rays[2 * i + 1];
+    const V3 d = v3(ra.w, rb.x, rb.y);
+    h = make_hit(S, v3(ra.x, ra.y, ra.z), d, __int_as_float(hit.x), hit.y, hit.z);
+    b = make_bsdf(S, h, hit.y);
+    wo = d * -1.0f;
+    const int64_t P = G.px_begin + i / G.spp;
+    int lo = 0, hi = G.n_views - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (G.views[mid].px_begin <= P) lo = mid; else hi = mid - 1;
+    }
+    gid = (uint64_t)((P - G.views[lo].px_begin) * G.spp + i % G.spp);
+    seed = G.views[lo].seed;
+    slot0 = (int64_t)i * G.slots + G.base_slot;
+    found = kcount[j];
+    for (int k = 0; k < found; ++k) {
+      const int did = M.ind_dirid[kidx[(int64_t)j * kGatherLookup + k]];
+      pd[k] = v3((float)M.dirs[3 * did], (float)M.dirs[3 * did + 1], (float)M.dirs[3 * did + 2]);
+    }
+  }
+  const V3 ns = b.n;
+  const int gs = G.gs;
+  // BSDF samples (:468-497)
+  for (int k = 0; k < gs; ++k) {
+    bool want = false;
+    V3 ex = v3(0, 0, 0), wt = v3(0, 0, 0);
+    float tmin = 0.0f;
+    if (valid) {
+      const float uc = rnd_g(seed, gid, 3 * k), u0 = rnd_g(seed, gid, 3 * k + 1), u1 = rnd_g(seed, gid, 3 * k + 2);
+      float pdf = 0.0f;
+      const V3 f = bsdf_sample(b, wo, uc, u0, u1, ex, pdf);
+      if (pdf > 0.0f && !black(f)) {
+        const float ppdf = photon_pdf_of(pd, found, ex);
+        const float w = power_heuristic(gs, pdf, gs, ppdf);
+        wt = f * (w * fabsf(dot(ex, ns)) / pdf);
+        tmin = next_min_t(h, ex, S.scene_abs);
+        want = true;
+      }
+    }
+    const int q = queue_append(want, gcount);
+    if (want) {
+      store_ray(grays, q, h.p, ex, tmin, __int_as_float(0x7f800000));
+      gtarget[q] = (int)(slot0 + k);
+      store_rgb(gweight, q, wt);
+    }
+  }
+  // Photon-guided samples (:499-533)
+  for (int k = 0; k < gs; ++k) {
+    bool want = false;
+    V3 ex = v3(0, 0, 0), wt = v3(0, 0, 0);
+    float tmin = 0.0f;
+    if (valid && found > 0) {
+      const float u = rnd_g(seed, gid, 3 * gs + 3 * k), c0 = rnd_g(seed, gid, 3 * gs + 3 * k + 1),
+                  c1 = rnd_g(seed, gid, 3 * gs + 3 * k + 2);
+      const int si = min((int)(u * found), found - 1);
+      const V3 n = pd[si];
+      // MathRoutines::CoordinateSystem (Math/MathRoutines.h:298-312)
+      V3 e2;
+      if (fabsf(n.x) > fabsf(n.y)) {
+        const float il = 1.0f / sqrtf(n.x * n.x + n.z * n.z);
+        e2 = v3(-n.z * il, 0.0f, n.x * il);
+      } else {
+        const float il = 1.0f / sqrtf(n.y * n.y + n.z * n.z);
+        e2 = v3(0.0f, n.z * il, -n.y * il);
+      }
+      const V3 e3 = cross(n, e2);
+      // UniformConeSampling (SamplingRoutines.h:300-310)
+      const float ct = (1.0f - c0) + c0 * (float)kCosGather, st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+      const float phi = c1 * 2.0f * kPi;
+      ex = normalized(e2 * (st * cosf(phi)) + e3 * (st * sinf(phi)) + n * ct);
+      const V3 f = bsdf_eval(b, wo, ex);
+      if (!black(f)) {
+        const float bpdf = bsdf_pdf(b, wo, ex);
+        const float ppdf = photon_pdf_of(pd, found, ex);
+        if (ppdf > 0.0f) {
+          const float w = power_heuristic(gs, ppdf, gs, bpdf);
+          wt = f * (w * fabsf(dot(ex, ns)) / ppdf);
+          tmin = next_min_t(h, ex, S.scene_abs);
+          want = true;
+        }
+      }
+    }
+    const int q = queue_append(want, gcount);
+    if (want) {
+      store_ray(grays, q, h.p, ex, tmin, __int_as_float(0x7f800000));
+      gtarget[q] = (int)(slot0 + gs + k);
+      store_rgb(gweight, q, wt);
+    }
+  }
+}
+
+// BxDF::TotalScattering (Core/BxDF.cpp:43-69) of one non-Lambertian BxDF
+// with the 5x5 grid of BSDF::TotalScattering's caller.  The reference hands
+// the BxDF the WORLD incident direction (BSDF.cpp:213-219 passes i_incident,
+// not its local form), which the BxDF then treats as local; this keeps that.
+__device__ V3 total_scattering_bxdf(const Bsdf &b, bool glossy, V3 wi) {
+  V3 ret = v3(0, 0, 0);
+  for (int y = 0; y < 5; ++y)
+    for (int x = 0; x < 5; ++x) {
+      const float u0 = (x + 0.5f) * 0.2f, u1 = (y + 0.5f) * 0.2f;
+      V3 wo;
+      float pdf;
+      V3 f;
+      if (glossy) {
+        // Microfacet::Sample (BxDFs/Microfacet.h:112-129) with BlinnDistribution::Sample
+        const float ct = powf(u0, 1.0f / (b.exponent + 1.0f));
+        const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+        const float phi = u1 * 2.0f * kPi;
+        V3 hh = v3(st * cosf(phi), st * sinf(phi), ct);
+        if (wi.z * hh.z < 0.0f) hh.z = -hh.z;
+        wo = hh * (2.0f * dot(wi, hh)) - wi;
+        pdf = microfacet_pdf(b, wi, wo);
+        if (wi.z * wo.z < 0.0f) continue;
+        f = microfacet_eval(b, wi, wo);
+      } else {
+        wo = cosine_hemisphere(u0, u1);
+        if (wi.z < 0.0f) wo.z = -wo.z;
+        pdf = diffuse_pdf(wi, wo);
+        f = diffuse_eval(b, wi, wo);
+      }
+      if (pdf > 0.0f) ret = ret + f * (fabsf(wo.z) / pdf);
+    }
+  ret = ret * (1.0f / 25.0f);
+  return v3(fminf(1.0f, fmaxf(0.0f, ret.x)), fminf(1.0f, fmaxf(0.0f, ret.y)), fminf(1.0f, fmaxf(0.0f, ret.z)));
+}
+
+// BSDF::TotalScattering over the reflection components (BSDF.cpp:209-224).
+__device__ V3 total_scattering_reflection(const Bsdf &b, V3 wi) {
+  V3 r = v3(0, 0, 0);
+  if (b.kind == kLambert || b.kind == kPlastic) r = b.kd;  // Lambertian::TotalScattering returns kd
+  if (b.kind == kOrenNayar) r = total_scattering_bxdf(b, false, wi);
+  if (b.kind == kPlastic || b.kind == kMetal) r = r + total_scattering_bxdf(b, true, wi);
+  return v3(fminf(1.0f, fmaxf(0.0f, r.x)), fminf(1.0f, fmaxf(0.0f, r.y)), fminf(1.0f, fmaxf(0.0f, r.z)));
+}
+
+__global__ void k_gather_hits(SceneDev S, const float4 *__restrict__ grays, const int4 *__restrict__ ghits,
+                              const int *__restrict__ gcount, int *__restrict__ hsrc, double *__restrict__ q,
+                              double *__restrict__ qn, float *__restrict__ ts, uint8_t *__restrict__ side,
+                              int *__restrict__ hcount) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool ok = false;
+  Hit h{};
+  V3 t = v3(0, 0, 0);
+  bool outside = false;
+  if (i < *gcount) {
+    const int4 hit = ghits[i];
+    if (hit.y >= 0) {
+      const float4 ra = grays[2 * i], rb = grays[2 * i + 1];
+      const V3 d = v3(ra.w, rb.x, rb.y);
+      h = make_hit(S, v3(ra.x, ra.y, ra.z), d, __int_as_float(hit.x), hit.y, hit.z);
+      const Bsdf b = make_bsdf(S, h, hit.y);
+      const V3 gdir = d * -1.0f;
+      outside = dot(gdir, h.ng) > 0.0f;
+      t = total_scattering_reflection(b, gdir);
+      ok = true;
+    }
+  }
+  const int j = queue_append(ok, hcount);
+  if (ok) {
+    hsrc[j] = i;
+    q[3 * j] = h.p.x;
+    q[3 * j + 1] = h.p.y;
+    q[3 * j + 2] = h.p.z;
+    qn[3 * j] = h.ng.x;
+    qn[3 * j + 1] = h.ng.y;
+    qn[3 * j + 2] = h.ng.z;
+    ts[3 * j] = t.x;
+    ts[3 * j + 1] = t.y;
+    ts[3 * j + 2] = t.z;
+    side[j] = outside ? 1 : 0;
+  }
+}
+
+__global__ void k_gather_resolve(GatherMaps M, int gs, const int *__restrict__ hcount, const int *__restrict__ hsrc,
+                                 const int32_t *__restrict__ nearest, const float *__restrict__ ts,
+                                 const uint8_t *__restrict__ side, const int *__restrict__ gtarget,
+                                 const float *__restrict__ gweight, float *__restrict__ contrib) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= *hcount) return;
+  const int t = nearest[j];
+  if (t < 0) return;
+  // the side the gather ray arrives from selects external or internal irradiance
+  const float *E = (side[j] ? M.irr_ext : M.irr_int) + 3 * (int64_t)t;
+  const int g = hsrc[j];
+  const int64_t slot = gtarget[g];
+  const float s = kInvPi / gs;
+  for (int c = 0; c < 3; ++c) contrib[3 * slot + c] = ts[3 * j + c] * E[c] * gweight[3 * g + c] * s;
+}
+
+}  // namespace
+
+cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev *views, int n_views, int n,
+                          int64_t px_begin, int spp, int slots, int base_slot, int gs, const void *rays,
+                          const void *hits, void *gws, float *contrib, const TraceFn &trace, unsigned *status,
+                          cudaStream_t st) {
+  if (n <= 0 || gs <= 0 || M.n_irr <= 0) return cudaSuccess;
+  auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
+  const int64_t ng = (int64_t)n * 2 * gs;
+  char *p = (char *)gws;
+  auto take = [&](size_t b) {
+    char *r = p;
+    p += b;
+    return r;
+  };
+  int *counts = (int *)take(256);  // [0] sources, [1] gather rays, [2] gather hits
+  int *src = (int *)take(al((int64_t)n * 4));
+  double *q = (double *)take(al((int64_t)n * 24)), *qn = (double *)take(al((int64_t)n * 24));
+  int32_t *kidx = (int32_t *)take(al((int64_t)n * kGatherLookup * 4));
+  double *kd2 = (double *)take(al((int64_t)n * kGatherLookup * 8));
+  int32_t *kcnt = (int32_t *)take(al((int64_t)n * 4));
+  float4 *grays = (float4 *)take(al(ng * 32));
+  int4 *ghits = (int4 *)take(al(ng * 16));
+  int *gtarget = (int *)take(al(ng * 4));
+  float *gweight = (float *)take(al(ng * 12));
+  int *hsrc = (int *)take(al(ng * 4));
+  double *hq = (double *)take(al(ng * 24)), *hqn = (double *)take(al(ng * 24));
+  float *ts = (float *)take(al(ng * 12));
+  uint8_t *side = (uint8_t *)take(al(ng));
+  int32_t *nearest = (int32_t *)take(al(ng * 4));
+  GatherArgs G{n, px_begin, spp, slots, base_slot, gs, views, n_views};
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(counts, 0, 3 * sizeof(int), st)) != cudaSuccess) return e;
+  k_gather_sources<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S, G, (const float4 *)rays, (const int4 *)hits, src, q,
+                                                                 qn, counts);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (M.n_ind > 0 &&
+      (e = launch_knn(M.ind_nodes, M.ind_nids, M.dirs, M.n_ind, q, qn, n, kGatherLookup, M.ind_lookup_dist, 0.87,
+                      kidx, kd2, kcnt, nullptr, nullptr, status, st, counts)) != cudaSuccess)
+    return e;
+  if (M.n_ind == 0 && (e = cudaMemsetAsync(kcnt, 0, (size_t)n * 4, st)) != cudaSuccess) return e;
+  k_gather_rays<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S, G, M, (const float4 *)rays, (const int4 *)hits, src,
+                                                              counts, kidx, kcnt, grays, gtarget, gweight, counts + 1);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = trace(grays, ng, counts + 1, ghits, st)) != cudaSuccess) return e;
+  k_gather_hits<<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(S, grays, ghits, counts + 1, hsrc, hq, hqn, ts, side,
+                                                               counts + 2);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = launch_nearest(M.irr_nodes, M.irr_nids, M.dirs, M.n_irr, hq, hqn, ng, M.max_irr_dist, 0.87, nearest,
+                          status, st, counts + 2)) != cudaSuccess)
+    return e;
+  k_gather_resolve<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(M, gs, counts + 2, hsrc, nearest, ts, side, gtarget,
+                                                                  gweight, contrib);
+  return cudaGetLastError();
+}
+
+size_t gather_bytes(int64_t n, int gs) {
+  auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
+  const int64_t ng = n * 2 * gs;
+  return 256 + al(n * 4) + 2 * al(n * 24) + al(n * kGatherLookup * 4) + al(n * kGatherLookup * 8) + al(n * 4) +
+         al(ng * 32) + al(ng * 16) + al(ng * 4) + al(ng * 12) + al(ng * 4) + 2 * al(ng * 24) + al(ng * 12) + al(ng) +
+         al(ng * 4) + 256;
+}
+
 }  // namespace skw

@@ -36,3 +36,23 @@ struct PhotonShootArgs {
 };
 
 }  // namespace skw
+
+namespace skw {
+
+// What the final-gather stages read: the indirect photon map (tree order) and
+// the irradiance photon map (tree order), plus the direction table.
+struct GatherMaps {
+  const void *ind_nodes;
+  const uint16_t *ind_nids;
+  const uint16_t *ind_dirid;
+  int32_t n_ind;
+  double ind_lookup_dist;  // sqrt(area / n_indirect * 32 / pi)
+  const void *irr_nodes;
+  const uint16_t *irr_nids;
+  const float *irr_ext, *irr_int;
+  int32_t n_irr;
+  double max_irr_dist;
+  const double *dirs;
+};
+
+}  // namespace skw

@@ -17,12 +17,14 @@
 
 #include "kernels.h"
 #include "photon_tree.h"
+#include "photon_map_internal.h"
 #include "photon_types.h"
 #include "skw_internal.h"
 
 using skw::cuda_fail;
 using skw::fail;
 using skw::PhotonRec;
+using Map = skw::PhotonMapData;
 
 namespace {
 
@@ -30,40 +32,6 @@ constexpr double kMaxNormalDeviationCos = 0.87;  // PhotonLTEIntegrator.cpp:26
 constexpr int kLookupIrradiance = 100;            // LOOKUP_PHOTONS_NUM_FOR_IRRADIANCE (PhotonLTEIntegrator.h:218)
 constexpr int64_t kMaxPhotonsInMap = 40000000;    // MAX_PHOTONS_IN_MAP (PhotonLTEIntegrator.h:224)
 constexpr double kInvPi = 0.31830988618379067154;
-
-// One photon kd-tree on the device: KdNode per tree position plus the
-// photon's normal id, incident-direction id and weight in tree order.
-struct Map {
-  int64_t n = 0;
-  int64_t paths = 0;
-  std::vector<PhotonRec> input;  // the photons in the order they were given (path order)
-  std::vector<int32_t> perm;     // tree position -> input index
-  void *d_nodes = nullptr;
-  uint16_t *d_nids = nullptr, *d_dirid = nullptr;
-  float *d_weight = nullptr;
-};
-
-}  // namespace
-
-struct skw_photon_map {
-  skw_ctx *ctx = nullptr;
-  Map maps[3];  // caustic, direct, indirect
-  double scene_area = 0.0;
-  double lookup_dist[3] = {0, 0, 0};  // irradiance-estimate radii per map
-  // irradiance photons, tree order
-  int64_t n_irr = 0;
-  std::vector<float> irr_pos, irr_ext, irr_int;
-  std::vector<uint16_t> irr_nrm;
-  void *d_irr_nodes = nullptr;
-  uint16_t *d_irr_nids = nullptr;
-  float *d_irr_ext = nullptr, *d_irr_int = nullptr;
-  double max_irr_dist = std::numeric_limits<double>::infinity();
-  double *d_dirs = nullptr;
-  unsigned *d_status = nullptr;
-  double shoot_ms = 0.0, build_ms = 0.0;
-};
-
-namespace {
 
 template <class T>
 cudaError_t upload(const std::vector<T> &v, T **out) {

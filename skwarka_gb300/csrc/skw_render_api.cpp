@@ -11,6 +11,8 @@
 #include <vector>
 
 #include "kernels.h"
+#include "photon_map_internal.h"
+#include "photon_types.h"
 #include "render_scene.h"
 #include "skw_internal.h"
 
@@ -306,6 +308,7 @@ struct PassConfig {
   int trace_ctas_per_sm = 0;
   int shade_block = 128;
   int overlap = 0;
+  int extra_slots = 0;       // contribution slots after the direct-lighting ones (final gather)
 };
 
 struct Plan {
@@ -391,7 +394,7 @@ int plan_make(skw_scene *s, const skw_camera *cams, int n_views, const skw_rende
   P->spp = P->sppx * P->sppy;
   P->nl = params->light_samples;
   P->npl = s->dev.n_point_lights;
-  P->slots = 1 + 2 * P->nl + P->npl;
+  P->slots = 1 + 2 * P->nl + P->npl + cfg.extra_slots;
   P->n_px_total = px;
   P->cfg = cfg;
   if (P->cfg.stack_cap == 0) P->cfg.stack_cap = s->accel->stack_cap;
@@ -404,9 +407,10 @@ int plan_make(skw_scene *s, const skw_camera *cams, int n_views, const skw_rende
   return SKW_OK;
 }
 
-// One pass over global pixels [px0, px0 + n_px).
-cudaError_t record_pass(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
-                        int n_px, float *films, cudaStream_t st) {
+// The direct-lighting stages of one pass over global pixels
+// [px0, px0 + n_px): every slot of contrib but the extra ones is filled.
+cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
+                          int n_px, cudaStream_t st) {
   skw_accel *a = s->accel;
   const int n = n_px * P.spp, nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
   cudaError_t e;
@@ -427,9 +431,15 @@ cudaError_t record_pass(skw_scene *s, const Plan &P, const Workspace &W, const s
   if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
                                             a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas)) != cudaSuccess)
     return e;
-  if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
-                               W.bhits, W.btarget, W.brgb, W.counts + 1, W.contrib, st)) != cudaSuccess)
-    return e;
+  return skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
+                             W.bhits, W.btarget, W.brgb, W.counts + 1, W.contrib, st);
+}
+
+// One pass: direct lighting, then the film.
+cudaError_t record_pass(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
+                        int n_px, float *films, cudaStream_t st) {
+  cudaError_t e = record_direct(s, P, W, d_views, px0, n_px, st);
+  if (e != cudaSuccess) return e;
   return skw::launch_film(W.contrib, px0, n_px, P.spp, P.slots, films, st);
 }
 
@@ -839,6 +849,86 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
   }
   cudaFreeAsync(w, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "direct-lighting adjoint");
+  ctx->launches.fetch_add(launches);
+  return SKW_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------ photon-map render --
+
+extern "C" {
+
+int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *cam, const skw_render_params *params,
+                      const skw_photon_render_params *pp, float *film_rgb, void *stream) {
+  if (!s || !pm || !cam || !params || !pp || !film_rgb) return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "null argument");
+  skw_ctx *ctx = s->ctx;
+  if (pp->gather_samples < 0 || pp->gather_samples > 1024) return fail(ctx, SKW_ERR_ARG, "gather_samples out of range");
+  if (pm->maps[0].n > 0)
+    return fail(ctx, SKW_ERR_UNSUPPORTED, "caustic photons: the caustic radiance lookup is not implemented");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  // the sampler rounds sequence lengths up to squares (Sampler.cpp:39-57, StratifiedSampler.cpp:33-37)
+  int gs = 0;
+  if (pp->gather_samples > 0) {
+    const int r = (int)std::ceil(std::sqrt((double)pp->gather_samples));
+    gs = r * r;
+  }
+  const bool gather = gs > 0 && pm->n_irr > 0;
+  PassConfig cfg;
+  cfg.samples_per_pass = (int64_t)1 << 19;
+  cfg.extra_slots = gather ? 2 * gs : 0;
+  Plan P;
+  const uint64_t seed = params->seed;
+  int rc = plan_make(s, cam, 1, params, &seed, cfg, &P);
+  if (rc != SKW_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemPool_t pool;
+  if ((e = skw::ctx_pool(ctx, &pool)) != cudaSuccess) return cuda_fail(ctx, e, "workspace pool");
+  const size_t wbytes = workspace_bytes(P), vbytes = al256(sizeof(skw::ViewDev)),
+               gbytes = gather ? skw::gather_bytes(P.cap_samples, gs) : 0;
+  char *w = nullptr;
+  if ((e = cudaMallocFromPoolAsync((void **)&w, wbytes + vbytes + gbytes, pool, st)) != cudaSuccess)
+    return cuda_fail(ctx, e, "photon render workspace");
+  Workspace W;
+  workspace_carve(P, w, &W);
+  skw::ViewDev *d_view = (skw::ViewDev *)(w + wbytes);
+  void *gws = w + wbytes + vbytes;
+  skw::GatherMaps M{};
+  const skw::PhotonMapData &im = pm->maps[2];
+  M.ind_nodes = im.d_nodes;
+  M.ind_nids = im.d_nids;
+  M.ind_dirid = im.d_dirid;
+  M.n_ind = (int32_t)im.n;
+  // max lookup distance of the 32 indirect photons (PhotonLTEIntegrator.cpp:450-453)
+  M.ind_lookup_dist = im.n > 0 ? std::sqrt(pm->scene_area / (double)im.n * 32 * 0.31830988618379067154) : 0.0;
+  M.irr_nodes = pm->d_irr_nodes;
+  M.irr_nids = pm->d_irr_nids;
+  M.irr_ext = pm->d_irr_ext;
+  M.irr_int = pm->d_irr_int;
+  M.n_irr = (int32_t)pm->n_irr;
+  M.max_irr_dist = pm->max_irr_dist;
+  M.dirs = pm->d_dirs;
+  skw_accel *a = s->accel;
+  skw::TraceFn trace = [a](const void *rays, int64_t n, const int *n_dev, void *hits, cudaStream_t stq) {
+    return skw::launch_traversal(true, a->stack_cap, a->d_nodes, a->d_tris, rays, n, n_dev, a->scene_abs, nullptr,
+                                 hits, a->d_status, stq);
+  };
+  e = cudaMemcpyAsync(d_view, P.views.data(), sizeof(skw::ViewDev), cudaMemcpyHostToDevice, st);
+  int64_t launches = 0;
+  const int base_slot = 1 + 2 * P.nl + P.npl;
+  for (int64_t px0 = 0; px0 < P.n_px_total && e == cudaSuccess; px0 += P.chunk_px) {
+    const int n_px = (int)std::min<int64_t>(P.chunk_px, P.n_px_total - px0);
+    const int n = n_px * P.spp;
+    if ((e = record_direct(s, P, W, d_view, px0, n_px, st)) != cudaSuccess) break;
+    if (gather && (e = skw::launch_gather(s->dev, M, d_view, 1, n, px0, P.spp, P.slots, base_slot, gs, W.rays, W.hits,
+                                          gws, W.contrib, trace, pm->d_status, st)) != cudaSuccess)
+      break;
+    if ((e = skw::launch_film(W.contrib, px0, n_px, P.spp, P.slots, film_rgb, st)) != cudaSuccess) break;
+    launches += kLaunchesPerPass + (gather ? 6 : 0);
+  }
+  cudaFreeAsync(w, st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "photon-map render");
   ctx->launches.fetch_add(launches);
   return SKW_OK;
 }

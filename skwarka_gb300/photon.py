@@ -82,5 +82,26 @@ class PhotonMap:
         return pos, ext, intr, nrm
 
 
+class skw_photon_render_params(C.Structure):
+    _fields_ = [("gather_samples", C.c_int32)]
+
+
+def render_photon(scene, photon_map: PhotonMap, camera, spp_x: int = 2, spp_y: int = 2, light_samples: int = 1,
+                  gather_samples: int = 16, seed: int = 0, out=None, stream=None):
+    """Photon-mapping render (emission + direct lighting + final gather) into
+    a CUDA float32 tensor (h, w, 3)."""
+    import torch
+    from .render import c_camera, skw_render_params
+    if out is None:
+        out = torch.empty((camera.height, camera.width, 3), dtype=torch.float32, device="cuda")
+    s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    cam = c_camera(camera)
+    par = skw_render_params(spp_x, spp_y, light_samples, seed)
+    pp = skw_photon_render_params(gather_samples)
+    _lib.check(_lib.load().skw_render_photon(scene.handle, photon_map.handle, C.byref(cam), C.byref(par), C.byref(pp),
+                                             out.data_ptr(), s), scene.ctx.handle)
+    return out
+
+
 def scene_total_area(scene) -> float:
     return float(_lib.load().skw_scene_total_area(scene.handle))

@@ -100,6 +100,15 @@ def photon_golden():
     maps, paths, area = sf.synthetic_photon_maps()
     pos, ext, intr, nrm, md = Reference().photon_irradiance(maps, paths, area)
     np.savez_compressed(OUT / "photon_irradiance.npz", pos=pos, ext=ext, int=intr, nrm=nrm, max_dist=np.float64(md))
+    # Photon-mapping render of the direct-lighting box: 200,000 photon paths,
+    # 16 gather samples, 64 x 64 at 4x4 spp; and its direct-lighting part.
+    prims, mats, cam = scenes.direct_lighting_box()
+    c = cam(64, 64)
+    ref = Reference()
+    photon, info = ref.render_photon(prims, mats, [], c, 4, 4, 200_000, gather_samples=16)
+    direct, _ = ref.render_direct(prims, mats, [], c, 4, 4)
+    np.savez_compressed(OUT / "photon_box_64.npz", photon=photon, direct=direct,
+                        counts=np.array([info["caustic"], info["direct"], info["indirect"], info["irradiance"]]))
 
 
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "photon":
