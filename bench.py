@@ -59,6 +59,7 @@ def parse():
     p.add_argument("--no-render", action="store_true", help="skip the direct-lighting render measurement")
     p.add_argument("--no-batch", action="store_true", help="skip the batched multi-view render measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
+    p.add_argument("--no-photon", action="store_true", help="skip the photon-mapping measurement")
     return p.parse_args()
 
 
@@ -315,6 +316,105 @@ def adjoint_bench(args, dev, ctx):
             "forward_msamples_s": samples / fwd_ms / 1e3, "adjoint_msamples_s": samples / adj_ms / 1e3}
 
 
+def photon_bench(args, dev, ctx, measure_cpu):
+    """Photon mapping on the 1M-triangle scene (matte 0.6, point light of
+    intensity 50): 2M photon paths of at most 8 bounces with Russian roulette
+    p = 0.7 shot on the GPU (paths/s), the maps' host kd-trees and GPU
+    irradiance map (build time), k = 100 filtered nearest photons within 0.05
+    of the 512x512x16 primary hits in the direct map (queries/s), and the
+    photon-mapping render (16 gather samples) at 512x512 with 4 spp
+    (samples/s).  Next to it: the reference's ShootPhotons(2M) (its own
+    bounce and Russian-roulette rules) and its KDTree lookups on a sample of
+    the same queries, on the host cores."""
+    import torch
+    from skwarka_gb300 import scenes
+    from skwarka_gb300.accel import Primitive, TriangleAccelerator
+    from skwarka_gb300.kdtree import PhotonKDTree, direction_table
+    from skwarka_gb300.photon import PhotonMap, render_photon
+    from skwarka_gb300.render import RenderScene
+    prims, mats, lights, camf = scenes.photon_scene(args.subdiv, args.nrandom)
+    sc = RenderScene(prims, mats, lights, ctx=ctx)
+    paths = 2_000_000
+    PhotonMap.shoot(sc, 100_000, max_bounces=8, rr_probability=0.7, seed=1)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pm = PhotonMap.shoot(sc, paths, max_bounces=8, rr_probability=0.7, seed=2)
+    wall = time.perf_counter() - t0
+    info = pm.info()
+    out = {"workload": "2M photon paths (<= 8 bounces, RR p=0.7) on the 1,098,576-tri scene, matte 0.6, "
+                       "point light I=50; k=100 r=0.05 lookups at 512x512x16 primary hits; render 512x512x4 spp",
+           "paths": paths, "shoot_paths_per_s": paths / (info["shoot_ms"] / 1e3), "shoot_ms": info["shoot_ms"],
+           "maps_build_ms": info["build_ms"], "shoot_and_build_wall_s": wall,
+           "photons": {k: info["n_" + k] for k in ("caustic", "direct", "indirect", "irradiance")}}
+    # k-NN at the primary hits
+    cam = camf(512, 512)
+    rays = torch.from_numpy(scenes.camera_rays(cam, 4, 4, seed=3)).to(dev)
+    acc = TriangleAccelerator([Primitive(p.mesh) for p in prims], ctx)
+    hits = acc.intersect(rays)
+    torch.cuda.synchronize()
+    t = hits[:, 0].view(torch.float32)
+    ok = hits[:, 1] >= 0
+    r, tt = rays[ok], t[ok].double()
+    q = (r[:, :3].double() + tt[:, None] * r[:, 3:6].double()).contiguous()
+    prim, tri = hits[ok, 1].long(), hits[ok, 2].long()
+    nrm = torch.zeros_like(q)
+    for pi, p in enumerate(prims):
+        sel = prim == pi
+        if not bool(sel.any()):
+            continue
+        v = torch.from_numpy(np.asarray(p.mesh.vertices, np.float64)).to(dev)
+        tr = torch.from_numpy(np.asarray(p.mesh.triangles, np.int64)).to(dev)[tri[sel]]
+        n = torch.linalg.cross(v[tr[:, 1]] - v[tr[:, 0]], v[tr[:, 2]] - v[tr[:, 0]])
+        nrm[sel] = n / n.norm(dim=1, keepdim=True)
+    qn = nrm.contiguous()
+    direct = pm.export("direct")
+    kd = PhotonKDTree(direct["position"], direct["normal"], ctx=ctx)
+    kd.get_nearest_points(q[:100_000].contiguous(), qn[:100_000].contiguous(), 100, 0.05, 0.87)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    res = kd.get_nearest_points(q, qn, 100, 0.05, 0.87)
+    e.record()
+    torch.cuda.synchronize()
+    knn_ms = s.elapsed_time(e)
+    nq = q.shape[0]
+    out["knn"] = {"queries": nq, "ms": knn_ms, "queries_per_s": nq / (knn_ms / 1e3),
+                  "mean_found": float(res["count"].float().mean())}
+    # photon-mapping render
+    cam4 = camf(512, 512)
+    render_photon(sc, pm, camf(64, 64), 2, 2, gather_samples=16)
+    torch.cuda.synchronize()
+    s.record()
+    render_photon(sc, pm, cam4, 2, 2, gather_samples=16, seed=4)
+    e.record()
+    torch.cuda.synchronize()
+    rms = s.elapsed_time(e)
+    out["render"] = {"samples": 512 * 512 * 4, "ms": rms, "msamples_per_s": 512 * 512 * 4 / rms / 1e3}
+    if measure_cpu:
+        from oracle.api import Reference
+        if Reference.available():
+            log("reference photon shooting and lookups")
+            ref = Reference()
+            from skwarka_gb300.render import Camera
+            nocam = Camera(np.eye(4), 1.0, 0, 0)
+            _, rinfo = ref.render_photon(prims, mats, lights, nocam, 1, 1, paths, gather_samples=16)
+            ns = 200_000
+            rkd = ref.kdtree(direct["position"], direct["normal"], direct["incident"])
+            qs, qns = q[:ns].cpu().numpy(), qn[:ns].cpu().numpy()
+            t0 = time.perf_counter()
+            rkd.knn(qs, qns, 100, 0.05, 0.87, threads=os.cpu_count() or 1)
+            kdt = time.perf_counter() - t0
+            out["cpu_baseline"] = {
+                "kind": "reference", "cores": os.cpu_count() or 1,
+                "shoot_paths_per_s": paths / rinfo["shoot_s"], "shoot_s_incl_maps": rinfo["shoot_s"],
+                "photons": {k: rinfo[k] for k in ("caustic", "direct", "indirect", "irradiance")},
+                "knn_queries_per_s": ns / kdt,
+                "sample": f"ShootPhotons({paths}) with the reference's own rules (no bounce cap, luminance Russian "
+                          f"roulette), incl. its kd-trees and irradiance map; KDTree::GetNearestPoints on {ns} of "
+                          "the GPU's queries against the same direct photons"}
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -470,6 +570,10 @@ def main():
     if not args.no_adjoint:
         log("adjoint")
         adjoint = adjoint_bench(args, dev, ctx)
+    photon = None
+    if not args.no_photon:
+        log("photon mapping")
+        photon = photon_bench(args, dev, ctx, measure_cpu=not args.no_cpu_baseline and world == 1)
     peak, peak_kind = peaks()
     per_launch_s = sum(kern_ms) / len(kern_ms) / 1e3
     roofline = None
@@ -488,7 +592,7 @@ def main():
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": args.rays * 32,
                     "d2h_bytes_per_step": args.rays * 16},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,
-            "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit, "render": render, "batch": batch, "adjoint": adjoint,
+            "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit, "render": render, "batch": batch, "adjoint": adjoint, "photon": photon,
             "accel": {k: acc.info[k] for k in ("n_nodes", "max_depth", "build_ms", "device_bytes")}}
     print(json.dumps(line), flush=True)
     if world > 1:

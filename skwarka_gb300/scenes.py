@@ -251,3 +251,45 @@ def batching_views(n: int = 64, seed: int = 5, lo: int = 64, hi: int = 1024):
         fov = np.radians(rng.uniform(40.0, 90.0))
         cams.append(Camera.look_at(tuple(eye), tuple(target), (0.0, 1.0, 0.0), float(fov), side, side))
     return cams
+
+
+def photon_scene(sphere_subdivisions: int = 9, n_random: int = 50_000, seed: int = 3, albedo: float = 0.6,
+                 intensity: float = 50.0, light=(1.2, 0.9, 0.7)):
+    """The photon-mapping configuration: the ray-query scene (1M-triangle
+    displaced sphere + 50k random triangles) with matte albedo 0.6 and a
+    point light of intensity 50 outside the sphere.  Returns (prims,
+    materials, point_lights, camera(width, height) factory)."""
+    from .accel import TriangleMesh
+    from .render import Camera, Material, PointLight, RenderPrimitive
+    meshes = ray_query_scene(sphere_subdivisions, n_random, seed)
+    prims = [RenderPrimitive(TriangleMesh(v, t), 0) for v, t in meshes]
+
+    def camera(width=512, height=512):
+        return Camera.look_at((2.2, 1.8, 1.6), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), np.radians(38.0), width, height)
+
+    return prims, [Material(kd=(albedo,) * 3)], [PointLight(tuple(light), (intensity,) * 3)], camera
+
+
+def camera_rays(camera, spp_x: int, spp_y: int, seed: int = 0) -> np.ndarray:
+    """Stratified, jittered pinhole rays of a Camera (PerspectiveCamera
+    convention, as the renderer's): float32 (h * w * spp, 8), pixel-major."""
+    rng = np.random.default_rng(seed)
+    w, h = camera.width, camera.height
+    spp = spp_x * spp_y
+    j = np.arange(spp)
+    px = np.arange(w * h)
+    x, y = (px % w)[:, None], (px // w)[:, None]
+    ix = x + ((j % spp_x)[None, :] + rng.uniform(size=(w * h, spp))) / spp_x
+    iy = y + ((j // spp_x)[None, :] + rng.uniform(size=(w * h, spp))) / spp_y
+    xt = np.tan(camera.x_view_angle / 2.0)
+    yt = xt * h / w
+    cx = (2.0 * xt * (ix - w * 0.5) / w).reshape(-1)
+    cy = (2.0 * yt * (iy - h * 0.5) / h).reshape(-1)
+    m = np.asarray(camera.camera_to_world, np.float64).reshape(4, 4)
+    d = np.stack([cx, cy, np.ones_like(cx)], 1) @ m[:3, :3].T
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = np.zeros((d.shape[0], 8), np.float32)
+    r[:, :3] = m[:3, 3]
+    r[:, 3:6] = d
+    r[:, 7] = np.inf
+    return r
