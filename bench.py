@@ -311,9 +311,20 @@ def adjoint_bench(args, dev, ctx):
     fwd_ms = timed(lambda: r.forward_image(albedo, 1.0))
     adj_ms = timed(lambda: r.adjoint(albedo, 1.0, d_img))
     samples = 512 * 512 * 16
-    return {"workload": "adjoint of direct lighting, 201,742-tri scene, 512x512, 16 spp, per-triangle albedo + "
-                        "emission scale", "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
-            "forward_msamples_s": samples / fwd_ms / 1e3, "adjoint_msamples_s": samples / adj_ms / 1e3}
+    out = {"workload": "adjoint of direct lighting, 201,742-tri scene, 512x512, 16 spp, per-triangle albedo + "
+                       "emission scale", "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
+           "forward_msamples_s": samples / fwd_ms / 1e3, "adjoint_msamples_s": samples / adj_ms / 1e3}
+    # the same with the configuration's homogeneous medium in the box
+    from skwarka_gb300.render import Medium
+    sc.set_medium(Medium(sigma_a=(0.05,) * 3, sigma_s=(0.2,) * 3, g=0.3, step=0.05))
+    img = r.forward_image(albedo, 1.0)
+    d_img = 2.0 * (img - target)
+    fwd_m = timed(lambda: r.forward_image(albedo, 1.0), 3)
+    adj_m = timed(lambda: r.adjoint(albedo, 1.0, d_img), 3)
+    out["with_medium"] = {"medium": "sigma_a 0.05, sigma_s 0.2, HG g 0.3, march step 0.05, box [-1,1]^3",
+                          "forward_ms": fwd_m, "adjoint_ms": adj_m, "adjoint_over_forward": adj_m / fwd_m}
+    sc.set_medium(None)
+    return out
 
 
 def photon_bench(args, dev, ctx, measure_cpu):

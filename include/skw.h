@@ -302,6 +302,23 @@ typedef struct skw_render_params {
 int skw_render_direct(skw_scene *scene, const skw_camera *camera, const skw_render_params *params, float *film_rgb,
                       void *stream);
 
+/* Homogeneous participating medium (HomogeneousVolumeRegion with an
+ * HGPhaseFunction, VolumeRegions/HomogeneousVolumeRegion.cpp:20-73,
+ * PhaseFunctions/HGPhaseFunction.h:53-57) filling an axis-aligned box, and
+ * the ray-march step of DirectLightingLTEIntegratorParams::m_media_step_size.
+ * With a medium, skw_render_direct, the batch and the adjoint march every
+ * camera ray through it (DirectLightingLTEIntegrator.cpp:62-175: emission
+ * and one light sample per step) and attenuate light samples through it. */
+typedef struct skw_medium {
+  float lo[3], hi[3];
+  float sigma_a[3], sigma_s[3];
+  float emission[3];
+  float g;      /* Henyey-Greenstein asymmetry, (-1, 1) */
+  float step;   /* march step (> 0) */
+} skw_medium;
+/* Sets (medium != NULL) or removes (NULL) the scene's medium. */
+int skw_scene_set_medium(skw_scene *scene, const skw_medium *medium);
+
 /* ---- Photon maps (PhotonLTEIntegrator, LTEIntegrators/PhotonLTEIntegrator/*).
  *
  * A photon (PhotonLTEIntegrator::Photon, PhotonInternalTypes.h:35-59):

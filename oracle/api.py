@@ -63,7 +63,7 @@ _REF_SIGS = [
     ("skw_ref_compressed_direction_table", None, [_P]),
     ("skw_ref_compress_direction", C.c_uint16, [C.c_double, C.c_double, C.c_double]),
     ("skw_ref_render_direct", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, C.c_int, _P, C.c_int, _P, _P,
-                                        C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
+                                        C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
     ("skw_ref_luminance_weights", None, [_P]),
     ("skw_ref_render_photon", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, C.c_double,
                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, C.c_int,
@@ -264,9 +264,10 @@ class Reference:
         return film, {"shoot_s": float(sec[0]), "render_s": float(sec[1]), "caustic": int(info[0]),
                       "direct": int(info[1]), "indirect": int(info[2]), "irradiance": int(info[3])}
 
-    def render_direct(self, prims, materials, point_lights, camera, spp_x, spp_y, light_samples=1):
+    def render_direct(self, prims, materials, point_lights, camera, spp_x, spp_y, light_samples=1, medium=None):
         """The reference's own direct-lighting render of a scene described with
-        skwarka_gb300.render types: (film (h, w, 3) float32, seconds)."""
+        skwarka_gb300.render types: (film (h, w, 3) float32, seconds).
+        medium: skwarka_gb300.render.Medium or None."""
         from skwarka_gb300.render import c_material, c_prims
         cm, nm, cp, keep = c_prims(prims)
         verts = (C.c_void_p * nm)(*[cm[i].vertices for i in range(nm)])
@@ -278,10 +279,14 @@ class Reference:
         c2w = np.ascontiguousarray(camera.camera_to_world, np.float64).reshape(-1)
         film = np.zeros((camera.height, camera.width, 3), np.float32)
         sec = np.zeros(1)
+        med = None
+        if medium is not None:
+            med = np.array(list(medium.lo) + list(medium.hi) + list(medium.emission) + list(medium.sigma_a)
+                           + list(medium.sigma_s) + [medium.g, medium.step], np.float64)
         self.lib.skw_ref_render_direct(nm, verts, _ptr(nv), tris, _ptr(nt), len(prims), C.addressof(cp), len(materials),
                                        C.addressof(mats), len(point_lights), _ptr(pl) if len(pl) else None, _ptr(c2w),
                                        camera.x_view_angle, camera.width, camera.height, spp_x, spp_y, light_samples,
-                                       _ptr(film), _ptr(sec))
+                                       _ptr(film), _ptr(sec), None if med is None else _ptr(med))
         return film, float(sec[0])
 
 

@@ -54,6 +54,8 @@
 #include <Raytracer/Samplers/StratifiedSampler.h>
 #include <Raytracer/LTEIntegrators/DirectLightingLTEIntegrator.h>
 #include <Raytracer/Renderers/SamplerBasedRenderer.h>
+#include <Raytracer/VolumeRegions/HomogeneousVolumeRegion.h>
+#include <Raytracer/PhaseFunctions/HGPhaseFunction.h>
 #undef private
 #undef protected
 #include <chrono>
@@ -370,7 +372,8 @@ struct RefPrimIn {
 static intrusive_ptr<const Scene> make_scene(int n_meshes, const float *const *verts, const int64_t *n_verts,
                                              const int32_t *const *tris, const int64_t *n_tris, int n_prims,
                                              const RefPrimIn *prims, const RefMaterialIn *materials,
-                                             int n_point_lights, const float *point_lights) {
+                                             int n_point_lights, const float *point_lights,
+                                             const double *medium = nullptr) {
   (void)n_meshes;
   std::vector<intrusive_ptr<const Primitive>> prim_list;
   LightSources lights;
@@ -427,7 +430,15 @@ static intrusive_ptr<const Scene> make_scene(int n_meshes, const float *const *v
     lights.m_delta_light_sources.push_back(intrusive_ptr<const DeltaLightSource>(
         new PointLight(Point3D_d(L[0], L[1], L[2]), Spectrum_d(L[3], L[4], L[5]))));
   }
-  return intrusive_ptr<const Scene>(new Scene(prim_list, NULL, lights));
+  // medium: bounds lo[3], hi[3], emission[3], absorption[3], scattering[3], HG g
+  intrusive_ptr<const VolumeRegion> volume;
+  if (medium) {
+    BBox3D_d b(Point3D_d(medium[0], medium[1], medium[2]), Point3D_d(medium[3], medium[4], medium[5]));
+    Spectrum_d em(medium[6], medium[7], medium[8]);
+    SpectrumCoef_d ab(medium[9], medium[10], medium[11]), sc(medium[12], medium[13], medium[14]);
+    volume.reset(new HomogeneousVolumeRegion(b, em, ab, sc, intrusive_ptr<const PhaseFunction>(new HGPhaseFunction(medium[15]))));
+  }
+  return intrusive_ptr<const Scene>(new Scene(prim_list, volume, lights));
 }
 
 // Renders `integrator` with the reference's SamplerBasedRenderer,
@@ -460,19 +471,21 @@ static double render_film(intrusive_ptr<LTEIntegrator> integrator, const double 
   return sec;
 }
 
-// Renders the direct-lighting image (DirectLightingLTEIntegrator).
+// Renders the direct-lighting image (DirectLightingLTEIntegrator), with an
+// optional homogeneous medium (17 doubles: bounds lo, hi, emission,
+// absorption, scattering, HG g, march step; NULL = none).
 int skw_ref_render_direct(int n_meshes, const float *const *verts, const int64_t *n_verts, const int32_t *const *tris,
                           const int64_t *n_tris, int n_prims, const RefPrimIn *prims, int n_materials,
                           const RefMaterialIn *materials, int n_point_lights, const float *point_lights,
                           const double *camera_to_world, double x_view_angle, int width, int height, int spp_x,
-                          int spp_y, int light_samples, float *film_out, double *seconds_out) {
+                          int spp_y, int light_samples, float *film_out, double *seconds_out, const double *medium) {
   (void)n_materials;
-  intrusive_ptr<const Scene> scene =
-      make_scene(n_meshes, verts, n_verts, tris, n_tris, n_prims, prims, materials, n_point_lights, point_lights);
+  intrusive_ptr<const Scene> scene = make_scene(n_meshes, verts, n_verts, tris, n_tris, n_prims, prims, materials,
+                                                n_point_lights, point_lights, medium);
   DirectLightingLTEIntegratorParams params;
   params.m_direct_light_samples_num = (size_t)light_samples;
   params.m_max_specular_depth = 6;
-  params.m_media_step_size = 0.01;
+  params.m_media_step_size = medium ? medium[16] : 0.01;  // medium[16]: the march step
   intrusive_ptr<LTEIntegrator> integrator(new DirectLightingLTEIntegrator(scene, params));
   const double sec = render_film(integrator, camera_to_world, x_view_angle, width, height, spp_x, spp_y, film_out);
   if (seconds_out) *seconds_out = sec;

@@ -85,6 +85,7 @@ SIGNATURES = [
     ("skw_photon_map_export", C.c_int, [_P, C.c_int32, C.c_void_p]),
     ("skw_photon_map_export_irradiance", C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("skw_scene_total_area", C.c_double, [_P]),
+    ("skw_scene_set_medium", C.c_int, [_P, C.c_void_p]),
     ("skw_render_photon", C.c_int, [_P, _P, C.c_void_p, C.c_void_p, C.c_void_p, _P, _P]),
     ("skw_scene_n_triangles", C.c_int64, [_P]),
     ("skw_scene_set_triangle_albedo", C.c_int, [_P, _P, _P]),

@@ -73,8 +73,22 @@ cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples,
                            const int *starget, const float *srgb, const int *scount, const void *brays,
                            const void *bhits, const int *btarget, const float *brgb, const int *bcount,
                            float *contrib, cudaStream_t s);
+// tcam (may be null): per-sample transmittance of the camera ray's medium
+// segment; with it, slot media_slot is the medium's radiance and the others
+// are scaled by the transmittance.
 cudaError_t launch_film(const float *contrib, int64_t px_begin, int n_px, int spp, int slots, float *film,
-                        cudaStream_t s);
+                        cudaStream_t s, const float *tcam = nullptr, int media_slot = 0);
+// Homogeneous medium along the camera rays (render.cu, k_media): writes tcam
+// and the medium emission slot, queues one light sample per march step
+// (mrays / mtarget / mval; adjoint: mdem = dI . d(value)/d(emission scale)).
+// status bit 2: a ray needed more than the medium's max_steps.
+cudaError_t launch_media(bool adjoint, const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin,
+                         int spp, int slots, int media_slot, const float *dfilm, const void *rays, const void *hits,
+                         float *contrib, float *tcam, void *mrays, int *mtarget, float *mval, float *mdem,
+                         int *mcount, unsigned *status, cudaStream_t s);
+cudaError_t launch_resolve_media(bool adjoint, int64_t capacity, const uint8_t *occ, const int *mtarget,
+                                 const float *mval, const float *mdem, const int *mcount, int slots, int media_slot,
+                                 float *contrib, double *g_emission, cudaStream_t s);
 // Adjoint of one pass (render.cu): replays the pass's rays and accumulates
 // dL/d(triangle albedo) (3 floats per global triangle) and dL/d(emission
 // scale) from dfilm = dL/dI (3 floats per global pixel).
@@ -82,7 +96,7 @@ cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_
                                  int n_light_samples, const float *dfilm, float *g_albedo, double *g_emission,
                                  const void *rays, const void *hits, void *srays, int *stri, float *s_dkd,
                                  float *s_dem, int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
-                                 int *bcount, cudaStream_t s);
+                                 int *bcount, const float *tcam, cudaStream_t s);
 cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                                    const int *stri, const float *s_dkd, const float *s_dem, const int *scount,
                                    const void *brays, const void *bhits, const int *btri, const float *b_dkd,

@@ -90,6 +90,7 @@ struct ShadeArgs {
   int n_light_samples;
   const ViewDev *views;
   int n_views;
+  const float *tcam;   // per sample: transmittance of the camera ray's medium segment (null: no medium)
 };
 
 // Adjoint pass (ADJ = true).  The same rays as the forward pass are traced
@@ -143,7 +144,10 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
     const int v = find_view(A.views, A.n_views, P);
     gid = (uint64_t)((P - A.views[v].px_begin) * A.spp + (valid ? i : 0) % A.spp);
     seed = A.views[v].seed;
-    if (ADJ && valid) dI = load3(J.dfilm + 3 * P) * (1.0f / A.spp);
+    if (ADJ && valid) {
+      dI = load3(J.dfilm + 3 * P) * (1.0f / A.spp);
+      if (A.tcam) dI = mul(dI, load3(A.tcam + 3 * (int64_t)i));
+    }
   }
   const float escale = S.emission_scale;
   float g_em = 0.0f;  // adjoint: this thread's direct emission-gradient terms
@@ -206,14 +210,14 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
           const float bpdf = bsdf_pdf(b, wo, dir);
           const float w = power_heuristic(nl, light_pdf * lcp, nl, bpdf) * fabsf(dot(dir, shading_n)) /
                           (light_pdf * lcp);
-          const V3 le = load3(L.radiance);
+          tmin = next_min_t(h, dir, S.scene_abs);
+          tmax = dist - 1e-4f;  // to avoid hitting the light itself (:237)
+          const V3 le = mul(load3(L.radiance), medium_tr(S.medium, h.p, dir, tmin, tmax));
           val = mul(f, le) * (escale * w / nl);
           if (ADJ) {
             dkd = mul(dI, mul(bsdf_eval_dkd(b, wo, dir), le)) * (escale * w / nl);
             dem = dot(dI, mul(f, le)) * (w / nl);
           }
-          tmin = next_min_t(h, dir, S.scene_abs);
-          tmax = dist - 1e-4f;  // to avoid hitting the light itself (:237)
           want = tmax > tmin;
         }
       }
@@ -243,11 +247,11 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
       dir = lv * inv;
       const V3 f = bsdf_eval(b, dir, wo);
       if (!black(f)) {
-        val = mul(f, load3(P.intensity)) * (inv * inv * fabsf(dot(dir, shading_n)));
-        if (ADJ)
-          dkd = mul(dI, mul(bsdf_eval_dkd(b, dir, wo), load3(P.intensity))) * (inv * inv * fabsf(dot(dir, shading_n)));
         tmin = next_min_t(h, dir, S.scene_abs);
         tmax = dist;
+        const V3 li = mul(load3(P.intensity), medium_tr(S.medium, h.p, dir, tmin, tmax));
+        val = mul(f, li) * (inv * inv * fabsf(dot(dir, shading_n)));
+        if (ADJ) dkd = mul(dI, mul(bsdf_eval_dkd(b, dir, wo), li)) * (inv * inv * fabsf(dot(dir, shading_n)));
         want = tmax > tmin;
       }
     }
@@ -337,9 +341,10 @@ __global__ void k_resolve_bsdf(SceneDev S, int n_light_samples, const float4 *__
   const float w = power_heuristic(n_light_samples, bpdf, n_light_samples, light_pdf * lcp);
   const int64_t t = btarget[i];
   const float sw = S.emission_scale * w;
-  contrib[3 * t] = brgb[4 * i] * L.radiance[0] * sw;
-  contrib[3 * t + 1] = brgb[4 * i + 1] * L.radiance[1] * sw;
-  contrib[3 * t + 2] = brgb[4 * i + 2] * L.radiance[2] * sw;
+  const V3 tr = medium_tr(S.medium, v3(ra.x, ra.y, ra.z), d, rb.z, __int_as_float(hit.x));
+  contrib[3 * t] = brgb[4 * i] * L.radiance[0] * tr.x * sw;
+  contrib[3 * t + 1] = brgb[4 * i + 1] * L.radiance[1] * tr.y * sw;
+  contrib[3 * t + 2] = brgb[4 * i + 2] * L.radiance[2] * tr.z * sw;
 }
 
 // Adjoint of k_resolve_shadow: an unoccluded shadow ray adds its derivative
@@ -382,7 +387,7 @@ __global__ void k_resolve_bsdf_adj(SceneDev S, int n_light_samples, const float4
         const float light_pdf = cosl > kEps ? dist * dist / (L.area * cosl) : 0.0f;
         const float lcp = 1.0f / S.n_area_lights;
         const float w = power_heuristic(n_light_samples, brgb[4 * i + 3], n_light_samples, light_pdf * lcp);
-        const V3 le = load3(L.radiance);
+        const V3 le = mul(load3(L.radiance), medium_tr(S.medium, v3(ra.x, ra.y, ra.z), d, rb.z, __int_as_float(hit.x)));
         const V3 dk = mul(load3(J.b_dkd + 3 * (int64_t)i), le) * (S.emission_scale * w);
         const int64_t t = btri[i];
         if (dk.x != 0.0f) atomicAdd(J.g_albedo + 3 * t, dk.x);
@@ -395,23 +400,203 @@ __global__ void k_resolve_bsdf_adj(SceneDev S, int n_light_samples, const float4
   add_emission_grad(J.g_emission, dem);
 }
 
+// Single scattering along the camera ray's segment in the medium
+// (DirectLightingLTEIntegrator::_MediaRadianceAndTranmsittance,
+// LTEIntegrators/DirectLightingLTEIntegrator.cpp:62-175): march with step
+// base / luminance(transmittance) from a random offset, add the medium's
+// emission, and at every step one light sample (light chosen uniformly with
+// the radical inverse of the step in base 2, area-light position from bases
+// 3 and 5) whose shadow ray goes to the media queue.  Writes the segment's
+// transmittance (it multiplies the surface radiance, LTEIntegrator.cpp:28-55)
+// and the emission term (the sample's medium slot).
+struct MediaArgs {
+  int n;
+  int64_t px_begin;
+  int spp;
+  int slots;
+  int media_slot;
+  const ViewDev *views;
+  int n_views;
+};
+
+__device__ __forceinline__ double radical_inverse_r(unsigned n, unsigned base) {
+  double ret = 0.0;
+  const double inv_base = 1.0 / base;
+  double inv = inv_base;
+  while (n > 0) {
+    ret += (double)(n % base) * inv;
+    n /= base;
+    inv *= inv_base;
+  }
+  return ret;
+}
+
+template <bool ADJ>
+__global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointArgs J, const float4 *__restrict__ rays,
+                                               const int4 *__restrict__ hits, float *__restrict__ contrib,
+                                               float *__restrict__ tcam, float4 *__restrict__ mrays,
+                                               int *__restrict__ mtarget, float *__restrict__ mval,
+                                               float *__restrict__ mdem, int *__restrict__ mcount,
+                                               unsigned *__restrict__ status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const MediumDev &M = S.medium;
+  const float4 ra = rays[2 * i], rb = rays[2 * i + 1];
+  const V3 o = v3(ra.x, ra.y, ra.z), d = v3(ra.w, rb.x, rb.y);
+  const int4 hit = hits[i];
+  float t0 = 0.0f, t1 = hit.y >= 0 ? __int_as_float(hit.x) : __int_as_float(0x7f800000);
+  V3 T = v3(1.0f, 1.0f, 1.0f);
+  if (!medium_segment(M, o, d, t0, t1) || fabsf(t0 - t1) < kEps) {
+    store_rgb(tcam, i, T);
+    return;
+  }
+  const int64_t P = A.px_begin + i / A.spp;
+  int lo = 0, hi = A.n_views - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (A.views[mid].px_begin <= P) lo = mid; else hi = mid - 1;
+  }
+  const uint64_t gid = (uint64_t)((P - A.views[lo].px_begin) * A.spp + i % A.spp), seed = A.views[lo].seed;
+  V3 dI = v3(0, 0, 0);
+  if (ADJ) dI = load3(J.dfilm + 3 * P) * (1.0f / A.spp);
+  const double offset1 = rnd(seed, gid, 62);
+  const V3 ss = load3(M.sigma_s), st = load3(M.sigma_t), em = load3(M.emission);
+  const bool scatters = !black(ss);
+  const int nlights = S.n_point_lights + S.n_area_lights;
+  const V3 dirv = d * -1.0f;
+  double tb = t0;
+  const double te = t1;
+  V3 point = o + d * t0, rad = v3(0, 0, 0);
+  double step = M.step;
+  int steps = 0;
+  for (unsigned k = 0; tb < te - 2.220446049250313e-16; ++k) {
+    if (steps == M.max_steps) {  // the media queue is sized for max_steps per ray
+      atomicOr(status, 4u);
+      break;
+    }
+    ++steps;
+    step = fmin(step, te - tb);
+    const double s1 = radical_inverse_r(k + 1, 2);
+    const float s2a = (float)radical_inverse_r(k + 1, 3), s2b = (float)radical_inverse_r(k + 1, 5);
+    const V3 prev = point;
+    point = o + d * (float)(tb + offset1 * step);
+    tb += step;
+    const float seg = len(point - prev);
+    T = v3(T.x * expf(-st.x * seg), T.y * expf(-st.y * seg), T.z * expf(-st.z * seg));
+    rad = rad + mul(T, em) * (float)step;
+    if (scatters && nlights > 0) {
+      const int li = min((int)(s1 * nlights), nlights - 1);
+      V3 lv = v3(0, 0, 0), ldir = v3(0, 0, 0);
+      float dist = 0.0f, pdf = 1.0f;
+      bool area = false;
+      if (li < S.n_point_lights) {
+        const PointLightDev PL = S.point_lights[li];
+        const V3 to = load3(PL.position) - point;
+        dist = len(to);
+        ldir = to * (1.0f / dist);
+        lv = load3(PL.intensity) * (1.0f / (dist * dist));
+      } else {
+        const AreaLight L = S.area_lights[li - S.n_point_lights];
+        // the reference draws the triangle choice from the thread's generator
+        const float tri_u = rnd(seed ^ 0xD1B54A32D192ED03ull, gid * 4096ull + (k >> 6), k & 63u);
+        int a = 0, b = L.tri_count - 1;
+        while (a < b) {
+          const int mid = (a + b) >> 1;
+          if (S.light_cdf[L.tri_begin + mid] <= tri_u) a = mid + 1; else b = mid;
+        }
+        const int g = S.light_tri[L.tri_begin + a];
+        const int j0 = S.tri_vidx[3 * g], j1 = S.tri_vidx[3 * g + 1], j2 = S.tri_vidx[3 * g + 2];
+        const V3 q0 = load3(S.vpos + 3 * j0), q1 = load3(S.vpos + 3 * j1), q2 = load3(S.vpos + 3 * j2);
+        const V3 ln = normalized(cross(q1 - q0, q2 - q0));
+        const float sq = sqrtf(s2a), b1 = 1.0f - sq, b2 = s2b * sq;
+        const V3 sp = q0 * b1 + q1 * b2 + q2 * (1.0f - b1 - b2);
+        const V3 to = sp - point;
+        dist = len(to);
+        ldir = to * (1.0f / dist);
+        const float cosl = fabsf(dot(ldir, ln));
+        pdf = cosl > kEps ? dist * dist / (L.area * cosl) : 0.0f;
+        if (dot(ln, ldir) < 0.0f) lv = load3(L.radiance) * S.emission_scale;
+        area = true;
+      }
+      const bool want = !black(lv) && pdf > 0.0f;
+      V3 val = v3(0, 0, 0);
+      if (want) {
+        // HGPhaseFunction::ScatteringPDF(incoming = -light direction, outgoing = -ray direction)
+        const float g = M.g, c = dot(ldir, d);
+        const float ph = (float)(1.0 / (4.0 * 3.14159265358979323846)) * (1.0f - g * g) *
+                         powf(1.0f + g * g - 2.0f * g * c, -1.5f);
+        const V3 tr = medium_tr(M, point, ldir, 0.0f, dist);
+        val = mul(mul(mul(T, ss), lv), tr) * (ph * (float)step * nlights / pdf);
+      }
+      const int q = queue_append(want, mcount);
+      if (want) {
+        store_ray(mrays, q, point, ldir, 0.0f, dist);
+        mtarget[q] = i;
+        if (ADJ) {
+          mdem[q] = area && S.emission_scale > 0.0f ? dot(dI, val) / S.emission_scale : 0.0f;
+        } else {
+          store_rgb(mval, q, val);
+        }
+      }
+    }
+    const float lum = 0.05316285f * T.x + 0.58515348f * T.y + 0.36168367f * T.z;
+    if (lum < kEps) break;
+    step = M.step / lum;
+  }
+  store_rgb(tcam, i, T);
+  if (!ADJ) store_rgb(contrib, (int64_t)i * A.slots + A.media_slot, rad);
+}
+
+// An unoccluded media shadow ray adds its in-scattered radiance to its
+// sample's medium slot (adjoint: its emission-scale derivative).
+template <bool ADJ>
+__global__ void k_resolve_media(const uint8_t *__restrict__ occ, const int *__restrict__ mtarget,
+                                const float *__restrict__ mval, const float *__restrict__ mdem,
+                                const int *__restrict__ mcount, int slots, int media_slot, float *__restrict__ contrib,
+                                double *__restrict__ g_emission) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float dem = 0.0f;
+  if (i < *mcount && !occ[i]) {
+    if (ADJ) {
+      dem = mdem[i];
+    } else {
+      const int64_t t = (int64_t)mtarget[i] * slots + media_slot;
+      atomicAdd(contrib + 3 * t, mval[3 * i]);
+      atomicAdd(contrib + 3 * t + 1, mval[3 * i + 1]);
+      atomicAdd(contrib + 3 * t + 2, mval[3 * i + 2]);
+    }
+  }
+  if (ADJ) {
+    for (int o = 16; o > 0; o >>= 1) dem += __shfl_xor_sync(0xffffffffu, dem, o);
+    if ((threadIdx.x & 31) == 0 && dem != 0.0f) atomicAdd(g_emission, (double)dem);
+  }
+}
+
 // Luminance weights of the reference's RGB spectrum (row Y of its
 // Spectrum-to-XYZ matrix, Core/SpectrumRoutines.cpp:20-64), used by the
 // renderer's negative-sample check.
 __constant__ float kLumW[3] = {0.05316285f, 0.58515348f, 0.36168367f};
 
 __global__ void k_film(const float *__restrict__ contrib, int64_t px_begin, int n_px, int spp, int slots,
-                       float *__restrict__ film) {
+                       const float *__restrict__ tcam, int media_slot, float *__restrict__ film) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n_px) return;
   float r = 0.0f, g = 0.0f, bb = 0.0f;
   for (int j = 0; j < spp; ++j) {
     const int64_t base = ((int64_t)p * spp + j) * slots;
     float sr = 0.0f, sg = 0.0f, sb = 0.0f;
-    for (int k = 0; k < slots; ++k) {
+    const int surface_slots = tcam ? media_slot : slots;
+    for (int k = 0; k < surface_slots; ++k) {
       sr += contrib[3 * (base + k)];
       sg += contrib[3 * (base + k) + 1];
       sb += contrib[3 * (base + k) + 2];
+    }
+    if (tcam) {
+      // LTEIntegrator::Radiance: surface * transmittance + medium radiance
+      const int64_t si = (int64_t)p * spp + j;
+      sr = sr * tcam[3 * si] + contrib[3 * (base + media_slot)];
+      sg = sg * tcam[3 * si + 1] + contrib[3 * (base + media_slot) + 1];
+      sb = sb * tcam[3 * si + 2] + contrib[3 * (base + media_slot) + 2];
     }
     const bool bad = !(sr == sr && sg == sg && sb == sb) ||
                      (kLumW[0] * sr + kLumW[1] * sg + kLumW[2] * sb) < -1e-16f || isinf(sr) || isinf(sg) ||
@@ -445,7 +630,7 @@ cudaError_t launch_shade(const SceneDev &S, const ViewDev *views, int n_views, i
                          int *bcount, int block, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   if (block != 64) block = 128;
-  ShadeArgs A{n, px_begin, spp, slots, n_light_samples, views, n_views};
+  ShadeArgs A{n, px_begin, spp, slots, n_light_samples, views, n_views, nullptr};
   k_shade<false><<<(unsigned)((n + block - 1) / block), (unsigned)block, 0, s>>>(
       S, A, AdjointArgs{}, (const float4 *)rays, (const int4 *)hits, contrib, (float4 *)srays, starget, srgb, scount,
       (float4 *)brays, btarget, brgb, bcount);
@@ -456,9 +641,9 @@ cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_
                                  int n_light_samples, const float *dfilm, float *g_albedo, double *g_emission,
                                  const void *rays, const void *hits, void *srays, int *stri, float *s_dkd,
                                  float *s_dem, int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
-                                 int *bcount, cudaStream_t s) {
+                                 int *bcount, const float *tcam, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  ShadeArgs A{n, px_begin, spp, 0, n_light_samples, views, n_views};
+  ShadeArgs A{n, px_begin, spp, 0, n_light_samples, views, n_views, tcam};
   AdjointArgs J{dfilm, g_albedo, g_emission, s_dkd, s_dem, b_dkd};
   k_shade<true><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, A, J, (const float4 *)rays, (const int4 *)hits,
                                                              nullptr, (float4 *)srays, stri, nullptr, scount,
@@ -494,9 +679,40 @@ cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples,
 }
 
 cudaError_t launch_film(const float *contrib, int64_t px_begin, int n_px, int spp, int slots, float *film,
-                        cudaStream_t s) {
+                        cudaStream_t s, const float *tcam, int media_slot) {
   if (n_px <= 0) return cudaSuccess;
-  k_film<<<(unsigned)((n_px + 127) / 128), 128, 0, s>>>(contrib, px_begin, n_px, spp, slots, film);
+  k_film<<<(unsigned)((n_px + 127) / 128), 128, 0, s>>>(contrib, px_begin, n_px, spp, slots, tcam, media_slot, film);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_media(bool adjoint, const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin,
+                         int spp, int slots, int media_slot, const float *dfilm, const void *rays, const void *hits,
+                         float *contrib, float *tcam, void *mrays, int *mtarget, float *mval, float *mdem,
+                         int *mcount, unsigned *status, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  MediaArgs A{n, px_begin, spp, slots, media_slot, views, n_views};
+  AdjointArgs J{dfilm, nullptr, nullptr, nullptr, nullptr, nullptr};
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  if (adjoint)
+    k_media<true><<<grid, 128, 0, s>>>(S, A, J, (const float4 *)rays, (const int4 *)hits, contrib, tcam,
+                                       (float4 *)mrays, mtarget, mval, mdem, mcount, status);
+  else
+    k_media<false><<<grid, 128, 0, s>>>(S, A, J, (const float4 *)rays, (const int4 *)hits, contrib, tcam,
+                                        (float4 *)mrays, mtarget, mval, mdem, mcount, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_resolve_media(bool adjoint, int64_t capacity, const uint8_t *occ, const int *mtarget,
+                                 const float *mval, const float *mdem, const int *mcount, int slots, int media_slot,
+                                 float *contrib, double *g_emission, cudaStream_t s) {
+  if (capacity <= 0) return cudaSuccess;
+  const unsigned grid = (unsigned)((capacity + 255) / 256);
+  if (adjoint)
+    k_resolve_media<true><<<grid, 256, 0, s>>>(occ, mtarget, mval, mdem, mcount, slots, media_slot, contrib,
+                                               g_emission);
+  else
+    k_resolve_media<false><<<grid, 256, 0, s>>>(occ, mtarget, mval, mdem, mcount, slots, media_slot, contrib,
+                                                g_emission);
   return cudaGetLastError();
 }
 

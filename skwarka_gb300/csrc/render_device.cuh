@@ -326,3 +326,39 @@ __device__ __forceinline__ void store_rgb(float *c, int64_t slot, V3 v) {
 
 }  // namespace
 }  // namespace skw
+
+namespace skw {
+namespace {
+
+// BBox3D::Intersect (Math/BBox3D.h:150-171) of the ray segment [t0, t1] with
+// the medium's box; false if they miss.
+__device__ __forceinline__ bool medium_segment(const MediumDev &M, V3 o, V3 d, float &t0, float &t1) {
+  const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+  for (int i = 0; i < 3; ++i) {
+    const float inv = 1.0f / dd[i];
+    float tn = (M.lo[i] - oo[i]) * inv, tf = (M.hi[i] - oo[i]) * inv;
+    if (tn > tf) {
+      const float x = tn;
+      tn = tf;
+      tf = x;
+    }
+    t0 = tn > t0 ? tn : t0;
+    t1 = tf < t1 ? tf : t1;
+    if (t0 > t1) return false;
+  }
+  return true;
+}
+
+// _MediaTransmittance of a ray segment: exp(-OpticalThickness), the
+// homogeneous region's optical thickness being sigma_t * |box segment|
+// (HomogeneousVolumeRegion.cpp:63-73).
+__device__ __forceinline__ V3 medium_tr(const MediumDev &M, V3 o, V3 d, float tmin, float tmax) {
+  if (!M.on) return v3(1.0f, 1.0f, 1.0f);
+  float t0 = tmin, t1 = tmax;
+  if (!medium_segment(M, o, d, t0, t1)) return v3(1.0f, 1.0f, 1.0f);
+  const float l = fabsf(t1 - t0);
+  return v3(expf(-M.sigma_t[0] * l), expf(-M.sigma_t[1] * l), expf(-M.sigma_t[2] * l));
+}
+
+}  // namespace
+}  // namespace skw

@@ -35,6 +35,18 @@ struct PointLightDev {
   float intensity[3];
 };
 
+// Homogeneous participating medium (HomogeneousVolumeRegion with an
+// HGPhaseFunction, VolumeRegions/HomogeneousVolumeRegion.cpp:20-73,
+// PhaseFunctions/HGPhaseFunction.h:53-57) and the march step.
+struct MediumDev {
+  int32_t on;
+  float lo[3], hi[3];
+  float sigma_s[3], sigma_t[3], emission[3];
+  float g;
+  float step;
+  int32_t max_steps;  // per camera ray (the media queue holds n * max_steps rays)
+};
+
 struct SceneDev {
   // geometry in mesh order
   const float *vpos;          // 3 floats per global vertex (world)
@@ -54,6 +66,7 @@ struct SceneDev {
   int32_t n_point_lights;
   float scene_abs;                // largest absolute vertex coordinate
   float emission_scale;           // multiplies every area light's radiance
+  MediumDev medium;
 };
 
 struct CameraDev {

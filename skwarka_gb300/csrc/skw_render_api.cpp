@@ -309,6 +309,7 @@ struct PassConfig {
   int shade_block = 128;
   int overlap = 0;
   int extra_slots = 0;       // contribution slots after the direct-lighting ones (final gather)
+  bool media = true;         // march the scene's medium (if any) along the camera rays (one more slot, last)
 };
 
 struct Plan {
@@ -316,6 +317,9 @@ struct Plan {
   std::vector<int64_t> film_offset;  // floats
   int sppx = 1, sppy = 1, spp = 1, nl = 0, npl = 0, slots = 1;
   int64_t n_px_total = 0, chunk_px = 0, cap_samples = 0, cap_shadow = 0, cap_bsdf = 0;
+  bool media = false;
+  int media_slot = 0;
+  int64_t cap_media = 0;  // media light-sample queue: cap_samples * max_steps
   PassConfig cfg;
 };
 
@@ -325,14 +329,21 @@ struct Workspace {
   float *contrib = nullptr, *srgb = nullptr, *brgb = nullptr;
   int *starget = nullptr, *btarget = nullptr, *counts = nullptr;
   uint8_t *occ = nullptr;
+  // medium
+  float *tcam = nullptr, *mval = nullptr, *mdem = nullptr;
+  void *mrays = nullptr;
+  int *mtarget = nullptr;
+  uint8_t *mocc = nullptr;
 };
 
 inline size_t al256(int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); }
 
 size_t workspace_bytes(const Plan &P) {
   const int64_t cs = P.cap_samples, sh = std::max<int64_t>(P.cap_shadow, 1), bs = std::max<int64_t>(P.cap_bsdf, 1);
+  const int64_t cm = std::max<int64_t>(P.cap_media, 1);
+  const size_t media = P.media ? al256(cs * 12) + al256(cm * 32) + al256(cm * 4) + 2 * al256(cm * 12) + al256(cm) : 0;
   return al256(cs * 32) + al256(cs * 16) + al256(cs * P.slots * 12) + al256(sh * 32) + al256(sh * 4) +
-         al256(sh * 12) + al256(sh) + al256(bs * 32) + al256(bs * 4) + al256(bs * 16) + al256(bs * 16) + 256;
+         al256(sh * 12) + al256(sh) + al256(bs * 32) + al256(bs * 4) + al256(bs * 16) + al256(bs * 16) + 256 + media;
 }
 
 void workspace_carve(const Plan &P, char *base, Workspace *W) {
@@ -354,7 +365,16 @@ void workspace_carve(const Plan &P, char *base, Workspace *W) {
   W->btarget = (int *)take(al256(bs * 4));
   W->brgb = (float *)take(al256(bs * 16));
   W->bhits = take(al256(bs * 16));
-  W->counts = (int *)take(256);  // [0] shadow queue length, [1] BSDF queue length
+  W->counts = (int *)take(256);  // [0] shadow queue length, [1] BSDF queue length, [2] media queue length
+  if (P.media) {
+    const int64_t cm = std::max<int64_t>(P.cap_media, 1);
+    W->tcam = (float *)take(al256(cs * 12));
+    W->mrays = take(al256(cm * 32));
+    W->mtarget = (int *)take(al256(cm * 4));
+    W->mval = (float *)take(al256(cm * 12));
+    W->mdem = (float *)take(al256(cm * 12));
+    W->mocc = (uint8_t *)take(al256(cm));
+  }
 }
 
 int valid_cap(int c) { return c == 48 || c == 96 || c == 192 || c == 416; }
@@ -394,17 +414,42 @@ int plan_make(skw_scene *s, const skw_camera *cams, int n_views, const skw_rende
   P->spp = P->sppx * P->sppy;
   P->nl = params->light_samples;
   P->npl = s->dev.n_point_lights;
-  P->slots = 1 + 2 * P->nl + P->npl + cfg.extra_slots;
+  P->media = cfg.media && s->dev.medium.on;
+  P->slots = 1 + 2 * P->nl + P->npl + cfg.extra_slots + (P->media ? 1 : 0);
+  P->media_slot = P->slots - 1;
   P->n_px_total = px;
   P->cfg = cfg;
   if (P->cfg.stack_cap == 0) P->cfg.stack_cap = s->accel->stack_cap;
-  P->chunk_px = std::max<int64_t>(1, std::min<int64_t>(px, cfg.samples_per_pass / P->spp));
+  int64_t per_pass = cfg.samples_per_pass;
+  if (P->media)  // the media queue holds max_steps light samples per camera ray: at most 2^25 per pass
+    per_pass = std::min<int64_t>(per_pass, std::max<int64_t>(((int64_t)1 << 25) / s->dev.medium.max_steps, 1));
+  P->chunk_px = std::max<int64_t>(1, std::min<int64_t>(px, per_pass / P->spp));
   P->cap_samples = P->chunk_px * P->spp;
+  P->cap_media = P->media ? P->cap_samples * s->dev.medium.max_steps : 0;
   P->cap_shadow = P->cap_samples * (P->nl + P->npl);
   P->cap_bsdf = P->cap_samples * P->nl;
   if (P->cap_shadow > INT32_MAX || P->cap_samples > INT32_MAX || P->cap_samples * P->slots * 3 > ((int64_t)1 << 40))
     return fail(ctx, SKW_ERR_ARG, "render pass too large");
   return SKW_OK;
+}
+
+// The medium stages of a pass: march + light samples, their any-hit
+// traversal, and their resolve (forward: radiance into the medium slot;
+// adjoint: the emission-scale gradient).
+cudaError_t record_media(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
+                         int n, bool adjoint, const float *dfilm, double *g_emission, cudaStream_t st) {
+  skw_accel *a = s->accel;
+  cudaError_t e = skw::launch_media(adjoint, s->dev, d_views, (int)P.views.size(), n, px0, P.spp, P.slots, P.media_slot,
+                                    dfilm, W.rays, W.hits, W.contrib, W.tcam, W.mrays, W.mtarget, W.mval, W.mdem,
+                                    W.counts + 2, a->d_status, st);
+  const int64_t cm = (int64_t)n * s->dev.medium.max_steps;
+  if (e == cudaSuccess)
+    e = skw::launch_traversal(false, P.cfg.stack_cap, a->d_nodes, a->d_tris, W.mrays, cm, W.counts + 2, a->scene_abs,
+                              nullptr, W.mocc, a->d_status, st, P.cfg.trace_ctas_per_sm);
+  if (e == cudaSuccess)
+    e = skw::launch_resolve_media(adjoint, cm, W.mocc, W.mtarget, W.mval, W.mdem, W.counts + 2, P.slots, P.media_slot,
+                                  W.contrib, g_emission, st);
+  return e;
 }
 
 // The direct-lighting stages of one pass over global pixels
@@ -415,11 +460,12 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
   const int n = n_px * P.spp, nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
   cudaError_t e;
   if ((e = cudaMemsetAsync(W.contrib, 0, (size_t)n * P.slots * 12, st)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(W.counts, 0, 3 * sizeof(int), st)) != cudaSuccess) return e;
   if ((e = skw::launch_camera(d_views, nv, px0, n_px, P.sppx, P.sppy, W.rays, st)) != cudaSuccess) return e;
   if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr, W.hits,
                                  a->d_status, st, ctas)) != cudaSuccess)
     return e;
+  if (P.media && (e = record_media(s, P, W, d_views, px0, n, false, nullptr, nullptr, st)) != cudaSuccess) return e;
   if ((e = skw::launch_shade(s->dev, d_views, nv, n, px0, P.spp, P.slots, P.nl, W.rays, W.hits, W.contrib, W.srays,
                              W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb, W.counts + 1, P.cfg.shade_block,
                              st)) != cudaSuccess)
@@ -440,7 +486,7 @@ cudaError_t record_pass(skw_scene *s, const Plan &P, const Workspace &W, const s
                         int n_px, float *films, cudaStream_t st) {
   cudaError_t e = record_direct(s, P, W, d_views, px0, n_px, st);
   if (e != cudaSuccess) return e;
-  return skw::launch_film(W.contrib, px0, n_px, P.spp, P.slots, films, st);
+  return skw::launch_film(W.contrib, px0, n_px, P.spp, P.slots, films, st, P.media ? W.tcam : nullptr, P.media_slot);
 }
 
 constexpr int kLaunchesPerPass = 8;
@@ -825,14 +871,15 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
   for (int64_t px0 = 0; px0 < P.n_px_total && e == cudaSuccess; px0 += P.chunk_px) {
     const int n_px = (int)std::min<int64_t>(P.chunk_px, P.n_px_total - px0);
     const int n = n_px * P.spp, cap = P.cfg.stack_cap;
-    if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(W.counts, 0, 3 * sizeof(int), st)) != cudaSuccess) break;
     if ((e = skw::launch_camera(d_view, 1, px0, n_px, P.sppx, P.sppy, W.rays, st)) != cudaSuccess) break;
     if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr,
                                    W.hits, a->d_status, st)) != cudaSuccess)
       break;
+    if (P.media && (e = record_media(s, P, W, d_view, px0, n, true, d_film, g_emission, st)) != cudaSuccess) break;
     if ((e = skw::launch_shade_adjoint(s->dev, d_view, 1, n, px0, P.spp, P.nl, d_film, g_albedo, g_emission, W.rays,
                                        W.hits, W.srays, W.starget, s_dkd, s_dem, W.counts, W.brays, W.btarget, b_dkd,
-                                       W.brgb, W.counts + 1, st)) != cudaSuccess)
+                                       W.brgb, W.counts + 1, P.media ? W.tcam : nullptr, st)) != cudaSuccess)
       break;
     const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
     if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts,
@@ -878,6 +925,10 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   PassConfig cfg;
   cfg.samples_per_pass = (int64_t)1 << 19;
   cfg.extra_slots = gather ? 2 * gs : 0;
+  // PhotonLTEIntegrator has no medium march (_MediaRadianceAndTranmsittance
+  // returns transmittance 1, PhotonLTEIntegrator.cpp:638-648); its direct
+  // lighting still attenuates light samples through the medium.
+  cfg.media = false;
   Plan P;
   const uint64_t seed = params->seed;
   int rc = plan_make(s, cam, 1, params, &seed, cfg, &P);
@@ -930,6 +981,42 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   cudaFreeAsync(w, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "photon-map render");
   ctx->launches.fetch_add(launches);
+  return SKW_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int skw_scene_set_medium(skw_scene *s, const skw_medium *m) {
+  if (!s) return SKW_ERR_ARG;
+  skw::MediumDev &M = s->dev.medium;
+  if (!m) {
+    M = skw::MediumDev{};
+    return SKW_OK;
+  }
+  bool ok = m->step > 0.0f && std::isfinite(m->step) && m->g > -1.0f && m->g < 1.0f;
+  for (int k = 0; k < 3; ++k)
+    ok = ok && m->lo[k] <= m->hi[k] && m->sigma_a[k] >= 0.0f && m->sigma_s[k] >= 0.0f && m->emission[k] >= 0.0f &&
+         std::isfinite(m->sigma_a[k] + m->sigma_s[k] + m->emission[k] + m->lo[k] + m->hi[k]);
+  if (!ok) return fail(s->ctx, SKW_ERR_ARG, "bad medium");
+  M.on = 1;
+  double diag2 = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    M.lo[k] = m->lo[k];
+    M.hi[k] = m->hi[k];
+    M.sigma_s[k] = m->sigma_s[k];
+    M.sigma_t[k] = m->sigma_a[k] + m->sigma_s[k];  // HomogeneousVolumeRegion.cpp:26
+    M.emission[k] = m->emission[k];
+    diag2 += (double)(m->hi[k] - m->lo[k]) * (m->hi[k] - m->lo[k]);
+  }
+  M.g = m->g;
+  M.step = m->step;
+  // Every step is at least `step` long (step = step / luminance(T) and
+  // luminance(T) <= 1), so a ray crosses the box in at most diag / step + 1.
+  const double steps = std::ceil(std::sqrt(diag2) / m->step) + 2.0;
+  if (steps > (double)((int64_t)1 << 24)) return fail(s->ctx, SKW_ERR_ARG, "medium step too small for its box");
+  M.max_steps = (int32_t)steps;
   return SKW_OK;
 }
 

@@ -42,6 +42,20 @@ class RenderPrimitive:
 
 
 @dataclass
+class Medium:
+    """Homogeneous participating medium in an axis-aligned box with a
+    Henyey-Greenstein phase function (HomogeneousVolumeRegion, HGPhaseFunction);
+    step is the ray-march step (DirectLightingLTEIntegratorParams::m_media_step_size)."""
+    lo: tuple = (-1.0, -1.0, -1.0)
+    hi: tuple = (1.0, 1.0, 1.0)
+    sigma_a: tuple = (0.05, 0.05, 0.05)
+    sigma_s: tuple = (0.2, 0.2, 0.2)
+    emission: tuple = (0.0, 0.0, 0.0)
+    g: float = 0.3
+    step: float = 0.05
+
+
+@dataclass
 class PointLight:
     position: tuple
     intensity: tuple
@@ -123,6 +137,11 @@ def c_prims(prims: list[RenderPrimitive]):
     return cm, len(meshes), cp, keep
 
 
+class skw_medium(C.Structure):
+    _fields_ = [("lo", C.c_float * 3), ("hi", C.c_float * 3), ("sigma_a", C.c_float * 3), ("sigma_s", C.c_float * 3),
+                ("emission", C.c_float * 3), ("g", C.c_float), ("step", C.c_float)]
+
+
 class skw_batch_config(C.Structure):
     _fields_ = [("samples_per_pass", C.c_int64), ("stack_cap", C.c_int32), ("trace_ctas_per_sm", C.c_int32),
                 ("shade_block", C.c_int32), ("overlap", C.c_int32)]
@@ -133,7 +152,7 @@ class skw_batch_config(C.Structure):
 
 class RenderScene:
     def __init__(self, prims: list[RenderPrimitive], materials: list[Material], point_lights=(),
-                 ctx: Context | None = None):
+                 ctx: Context | None = None, medium: "Medium | None" = None):
         self.ctx = ctx or default_context()
         lib = _lib.load()
         cm, nm, cp, self._keep = c_prims(prims)
@@ -145,6 +164,15 @@ class RenderScene:
                                         len(point_lights), C.byref(h)), self.ctx.handle)
         self.handle = h
         self.prims, self.materials, self.point_lights = prims, materials, list(point_lights)
+        if medium is not None:
+            self.set_medium(medium)
+
+    def set_medium(self, medium: "Medium | None") -> None:
+        m = None
+        if medium is not None:
+            m = skw_medium((C.c_float * 3)(*medium.lo), (C.c_float * 3)(*medium.hi), (C.c_float * 3)(*medium.sigma_a),
+                           (C.c_float * 3)(*medium.sigma_s), (C.c_float * 3)(*medium.emission), medium.g, medium.step)
+        _lib.check(_lib.load().skw_scene_set_medium(self.handle, None if m is None else C.byref(m)), self.ctx.handle)
 
     def __del__(self):
         h = getattr(self, "handle", None)

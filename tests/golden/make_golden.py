@@ -94,6 +94,16 @@ def render_golden():
     np.savez_compressed(OUT / "direct_planes.npz", **planes)
 
 
+def medium_golden():
+    """The reference's direct-lighting renders with a homogeneous medium
+    (scene_fixtures.medium_cases) at 32 x 32, 16x16 spp."""
+    ref = Reference()
+    out = {}
+    for name, (p, m, l, c, med) in sf.medium_cases().items():
+        out[name], _ = ref.render_direct(p, m, l, c, 16, 16, 1, medium=med)
+    np.savez_compressed(OUT / "medium_32.npz", **out)
+
+
 def photon_golden():
     """The reference's irradiance photon map (_ConstructIrradiancePhotonMap)
     over the seeded synthetic photon maps of scene_fixtures.synthetic_photon_maps."""
@@ -110,6 +120,10 @@ def photon_golden():
     np.savez_compressed(OUT / "photon_box_64.npz", photon=photon, direct=direct,
                         counts=np.array([info["caustic"], info["direct"], info["indirect"], info["irradiance"]]))
 
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "medium":
+    medium_golden()
+    print("medium golden written")
 
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "photon":
     photon_golden()

@@ -221,3 +221,22 @@ def photon_box_scene(albedo=0.5, intensity=50.0):
     bv, bt = scenes._box_inward()
     prims = [RenderPrimitive(TriangleMesh(bv, bt), 0)]
     return prims, [Material(kd=(albedo,) * 3)], [PointLight((0.1, 0.2, 0.3), (intensity,) * 3)]
+
+
+def medium_cases():
+    """Homogeneous-medium renders: {name: (prims, materials, point_lights,
+    camera, medium)} -- the grey box with a point light filled with a
+    scattering medium, the same with an emitting non-scattering medium, and
+    the direct-lighting box (area light) with the configuration's medium
+    (sigma_a 0.05, sigma_s 0.2, g 0.3)."""
+    from skwarka_gb300.render import Camera, Medium
+    prims, mats, lights = photon_box_scene(0.5, 5.0)
+    cam = Camera.look_at((0.0, 0.0, -0.9), (0.0, 0.0, 1.0), (0, 1, 0), np.radians(70), 32, 32)
+    out = {"point_scatter": (prims, mats, lights, cam, Medium(sigma_a=(0.1, 0.05, 0.02), sigma_s=(0.4, 0.3, 0.2),
+                                                              g=0.3, step=0.05)),
+           "point_emit": (prims, mats, lights, cam, Medium(sigma_a=(0.2, 0.2, 0.2), sigma_s=(0, 0, 0),
+                                                           emission=(0.3, 0.2, 0.1), step=0.05))}
+    bp, bm, bcam = scenes.direct_lighting_box()
+    out["box_area"] = (bp, bm, [], bcam(32, 32), Medium(sigma_a=(0.05,) * 3, sigma_s=(0.2,) * 3, g=0.3, step=0.05))
+    out["box_absorb"] = (bp, bm, [], bcam(32, 32), Medium(sigma_a=(0.25,) * 3, sigma_s=(0, 0, 0), g=0.3, step=0.05))
+    return out
