@@ -240,6 +240,9 @@ int skw_nearest(skw_kdtree *tree, const double *q, const double *qn, int64_t nq,
 #define SKW_MATERIAL_MATTE 0   /* MatteMaterial: Lambertian (sigma == 0) or Oren-Nayar */
 #define SKW_MATERIAL_PLASTIC 1 /* PlasticMaterial: Lambertian(kd) + Blinn microfacet(ks, 1/roughness), dielectric 1.5 */
 #define SKW_MATERIAL_METAL 2   /* MetalMaterial: Blinn microfacet with a conductor Fresnel (eta, k) */
+#define SKW_MATERIAL_MEASURED 3 /* MERLMeasuredMaterial: a tabulated BRDF (skw_merl) */
+
+typedef struct skw_merl skw_merl;
 
 typedef struct skw_material {
   int32_t kind;
@@ -248,7 +251,27 @@ typedef struct skw_material {
   float roughness;    /* plastic / metal, clamped to [0.001, 1] like the reference */
   float sigma;        /* matte Oren-Nayar sigma (radians); 0 = Lambertian */
   float eta[3], k[3]; /* metal refractive index and absorption */
+  const skw_merl *measured; /* SKW_MATERIAL_MEASURED: the tabulated BRDF (must outlive the scene) */
 } skw_material;
+
+/* A measured BRDF in the MERL binary layout (MERLMeasuredData(std::istream&),
+ * Raytracer/BxDFs/MERLMeasured.cpp:169-217): 3 int32 dimensions (90, 90,
+ * 180), then 3 channels of 1,458,000 doubles, scaled by 1/1500, 1.15/1500 and
+ * 1.66/1500, converted RGB -> XYZ -> spectrum coefficients and stored in half
+ * precision as the reference stores them; the sampling segmentations
+ * (_InitializeSegmentations, :219-251) are built on the host. */
+int skw_merl_create(skw_ctx *ctx, const void *bytes, int64_t n_bytes, skw_merl **out);
+/* (ctx = NULL: host tables only -- the host entry points work, a scene
+ * cannot use it.) */
+void skw_merl_destroy(skw_merl *merl);
+/* The converted half table (3 uint16 per entry) and the segmentations (90 x
+ * 1,173 floats: 24 x 45 column CDFs, 24 row CDFs, 45 + 24 grid lines). */
+int skw_merl_export(const skw_merl *merl, uint16_t *table, float *segmentation);
+/* MERLMeasured::Evaluate / PDF / Sample (local frame, double, host) for n
+ * directions: the reference's arithmetic, for checking. */
+int skw_merl_eval_host(const skw_merl *merl, const double *wi, const double *wo, int64_t n, double *f, double *pdf);
+int skw_merl_sample_host(const skw_merl *merl, const double *wi, const double *u, int64_t n, double *wo, double *f,
+                         double *pdf);
 
 /* A primitive of the render scene: mesh + transform as for the accelerator,
  * plus its material, optional area-light emission and shading normals. */

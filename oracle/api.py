@@ -69,6 +69,11 @@ _REF_SIGS = [
                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, C.c_int,
                                         C.c_double, _P, _P, _P]),
     ("skw_ref_photon_irradiance", C.c_int, [_P, _P, _P, C.c_double, _P, _P, _P, _P, _P, _P]),
+    ("skw_ref_merl_create", _P, [C.c_char_p, _i64]),
+    ("skw_ref_merl_destroy", None, [_P]),
+    ("skw_ref_merl_export", None, [_P, _P, _P]),
+    ("skw_ref_merl_eval", None, [_P, _P, _P, _i64, _P, _P]),
+    ("skw_ref_merl_sample", None, [_P, _P, _P, _i64, _P, _P, _P]),
 ]
 
 
@@ -219,6 +224,17 @@ class Reference:
         self.lib.skw_ref_compressed_direction_table(_ptr(out))
         return out
 
+    def _merl(self, measured):
+        """The reference's MERLMeasuredData for a MeasuredBRDF (cached)."""
+        cache = self.__dict__.setdefault("_merl_cache", {})
+        key = id(measured)
+        if key not in cache:
+            cache[key] = (measured, self.lib.skw_ref_merl_create(measured.data, len(measured.data)))
+        return cache[key][1]
+
+    def merl(self, data: bytes):
+        return RefMerl(self.lib, data)
+
     def photon_irradiance(self, maps, paths, scene_area):
         """The reference's _ConstructIrradiancePhotonMap on the given photon
         maps (structured arrays of PHOTON_DTYPE: caustic, direct, indirect)
@@ -250,7 +266,8 @@ class Reference:
         tris = (C.c_void_p * nm)(*[cm[i].triangles for i in range(nm)])
         nv = np.array([cm[i].n_vertices for i in range(nm)], np.int64)
         nt = np.array([cm[i].n_triangles for i in range(nm)], np.int64)
-        mats = (type(c_material(materials[0])) * len(materials))(*[c_material(m) for m in materials])
+        mats = (type(c_material(materials[0])) * len(materials))(
+            *[c_material(m, self._merl(m.measured) if m.measured is not None else None) for m in materials])
         pl = np.array([list(l.position) + list(l.intensity) for l in point_lights], np.float32).reshape(-1, 6)
         c2w = np.ascontiguousarray(camera.camera_to_world, np.float64).reshape(-1)
         film = np.zeros((max(camera.height, 1), max(camera.width, 1), 3), np.float32)
@@ -274,7 +291,8 @@ class Reference:
         tris = (C.c_void_p * nm)(*[cm[i].triangles for i in range(nm)])
         nv = np.array([cm[i].n_vertices for i in range(nm)], np.int64)
         nt = np.array([cm[i].n_triangles for i in range(nm)], np.int64)
-        mats = (type(c_material(materials[0])) * len(materials))(*[c_material(m) for m in materials])
+        mats = (type(c_material(materials[0])) * len(materials))(
+            *[c_material(m, self._merl(m.measured) if m.measured is not None else None) for m in materials])
         pl = np.array([list(l.position) + list(l.intensity) for l in point_lights], np.float32).reshape(-1, 6)
         c2w = np.ascontiguousarray(camera.camera_to_world, np.float64).reshape(-1)
         film = np.zeros((camera.height, camera.width, 3), np.float32)
@@ -367,3 +385,36 @@ class RefKD:
         out = np.empty(q.shape[0], np.int32)
         self.lib.skw_ref_nearest(self.h, _ptr(q), q.shape[0], max_dist, _ptr(out), threads)
         return out
+
+
+class RefMerl:
+    """The reference's MERLMeasuredData / MERLMeasured on a file image."""
+
+    def __init__(self, lib, data: bytes):
+        self.lib = lib
+        self.h = lib.skw_ref_merl_create(data, len(data))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.skw_ref_merl_destroy(self.h)
+            self.h = None
+
+    def export(self):
+        t = np.empty((90 * 90 * 180, 3), np.uint16)
+        sg = np.zeros((90, 1173), np.float32)
+        self.lib.skw_ref_merl_export(self.h, _ptr(t), _ptr(sg))
+        return t, sg
+
+    def eval(self, wi, wo):
+        wi = np.ascontiguousarray(wi, np.float64).reshape(-1, 3)
+        wo = np.ascontiguousarray(wo, np.float64).reshape(-1, 3)
+        f, pdf = np.empty_like(wi), np.empty(len(wi))
+        self.lib.skw_ref_merl_eval(self.h, _ptr(wi), _ptr(wo), len(wi), _ptr(f), _ptr(pdf))
+        return f, pdf
+
+    def sample(self, wi, u):
+        wi = np.ascontiguousarray(wi, np.float64).reshape(-1, 3)
+        u = np.ascontiguousarray(u, np.float64).reshape(-1, 2)
+        wo, f, pdf = np.empty_like(wi), np.empty_like(wi), np.empty(len(wi))
+        self.lib.skw_ref_merl_sample(self.h, _ptr(wi), _ptr(u), len(wi), _ptr(wo), _ptr(f), _ptr(pdf))
+        return wo, f, pdf

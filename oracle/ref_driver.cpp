@@ -56,9 +56,13 @@
 #include <Raytracer/Renderers/SamplerBasedRenderer.h>
 #include <Raytracer/VolumeRegions/HomogeneousVolumeRegion.h>
 #include <Raytracer/PhaseFunctions/HGPhaseFunction.h>
+#include <Raytracer/BxDFs/MERLMeasured.h>
+#include <Raytracer/Materials/MERLMeasuredMaterial.h>
+#include <Raytracer/Core/Color.h>
 #undef private
 #undef protected
 #include <chrono>
+#include <sstream>
 
 namespace {
 
@@ -356,6 +360,7 @@ struct RefMaterialIn {
   float kd[3], ks[3];
   float roughness, sigma;
   float eta[3], k[3];
+  const void *measured;  // kind 3: a MERLMeasuredData (skw_ref_merl_create)
 };
 struct RefPrimIn {
   int32_t mesh;
@@ -411,6 +416,8 @@ static intrusive_ptr<const Scene> make_scene(int n_meshes, const float *const *v
       mat.reset(new PlasticMaterial(kd, intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(
                                             SpectrumCoef_d(M.ks[0], M.ks[1], M.ks[2]))),
                                     intrusive_ptr<const Texture<double>>(new ConstantTexture<double>(M.roughness))));
+    } else if (M.kind == 3) {
+      mat.reset(new MERLMeasuredMaterial(intrusive_ptr<const MERLMeasuredData>((const MERLMeasuredData *)M.measured)));
     } else {
       mat.reset(new MetalMaterial(
           intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.eta[0], M.eta[1], M.eta[2]))),
@@ -595,6 +602,94 @@ int skw_ref_photon_irradiance(const RefPhotonIn *const *photons, const int64_t *
   *n_irr_out = k;
   *max_dist_out = integ.m_max_irradiance_lookup_dist;
   return 0;
+}
+
+// ------------------------------------------------------------- measured BRDF
+
+// MERLMeasuredData from a file image in the MERL binary format (3 int32
+// dims, then 3 channels of doubles).
+void *skw_ref_merl_create(const char *bytes, int64_t n_bytes) {
+  std::string buf(bytes, (size_t)n_bytes);
+  std::istringstream is(buf, std::ios::binary);
+  auto *d = new MERLMeasuredData(is);
+  d->IncRef();
+  return d;
+}
+
+void skw_ref_merl_destroy(void *d) {
+  if (((MERLMeasuredData *)d)->DecRef() == 0) delete (MERLMeasuredData *)d;
+}
+
+// The converted table (half RGB per entry, the reference's m_brdf_data) and
+// the sampling segmentations: per incident theta bin, the 45 x 24 column
+// CDFs, the 24 row CDFs, the 45 X and 24 Y grid lines (1,173 floats).
+void skw_ref_merl_export(void *dp, uint16_t *table, float *seg) {
+  const MERLMeasuredData *d = (const MERLMeasuredData *)dp;
+  for (size_t i = 0; i < d->m_brdf_data.size(); ++i)
+    for (int c = 0; c < 3; ++c) {
+      const HalfFloat h = d->m_brdf_data[i][c];
+      std::memcpy(&table[3 * i + c], &h, 2);
+    }
+  float *o = seg;
+  for (const auto &sg : d->m_segmentations) {
+    for (size_t i = 0; i < MERLMeasuredData::SEGMENTATION_EXITANT_THETA_RES; ++i)
+      for (size_t j = 0; j < MERLMeasuredData::SEGMENTATION_EXITANT_PHI_RES; ++j) *o++ = sg.m_CDF_cols[i][j];
+    for (float v : sg.m_CDF_rows) *o++ = v;
+    for (float v : sg.m_grid_X) *o++ = v;
+    for (float v : sg.m_grid_Y) *o++ = v;
+  }
+}
+
+// MERLMeasured BxDF (local frame): Evaluate / PDF for n direction pairs
+// (3 doubles each); Sample for n incident directions and 2D samples.
+void skw_ref_merl_eval(void *dp, const double *wi, const double *wo, int64_t n, double *f, double *pdf) {
+  MERLMeasured bx((const MERLMeasuredData *)dp);
+  for (int64_t i = 0; i < n; ++i) {
+    const Vector3D_d a(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]), b(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+    const SpectrumCoef_d v = bx.Evaluate(a, b);
+    for (int c = 0; c < 3; ++c) f[3 * i + c] = v[c];
+    pdf[i] = bx.PDF(a, b);
+  }
+}
+
+void skw_ref_merl_sample(void *dp, const double *wi, const double *u, int64_t n, double *wo, double *f, double *pdf) {
+  MERLMeasured bx((const MERLMeasuredData *)dp);
+  for (int64_t i = 0; i < n; ++i) {
+    const Vector3D_d a(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]);
+    Vector3D_d e;
+    double p = 0.0;
+    const SpectrumCoef_d v = bx.Sample(a, e, Point2D_d(u[2 * i], u[2 * i + 1]), p);
+    for (int c = 0; c < 3; ++c) {
+      wo[3 * i + c] = e[c];
+      f[3 * i + c] = v[c];
+    }
+    pdf[i] = p;
+  }
+}
+
+// The loader's colour conversion: RGB -> XYZ (sRGB primaries, E white) ->
+// spectrum coefficients, for n RGB triples.
+void skw_ref_merl_convert(const double *rgb, int64_t n, double *out) {
+  for (int64_t i = 0; i < n; ++i) {
+    RGBColor_d c(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+    XYZColor_d xyz = global_sRGB_E_ColorSystem.RGB_To_XYZ(c);
+    SpectrumCoef_d s = SpectrumRoutines::XYZToSpectrumCoef(xyz);
+    for (int k = 0; k < 3; ++k) out[3 * i + k] = s[k];
+  }
+}
+
+// The two stages of that conversion separately (stage 0: RGB -> XYZ,
+// stage 1: XYZ -> spectrum coefficients).
+void skw_ref_color_stage(int stage, const double *in, int64_t n, double *out) {
+  for (int64_t i = 0; i < n; ++i) {
+    if (stage == 0) {
+      XYZColor_d x = global_sRGB_E_ColorSystem.RGB_To_XYZ(RGBColor_d(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+      for (int k = 0; k < 3; ++k) out[3 * i + k] = x[k];
+    } else {
+      SpectrumCoef_d s = SpectrumRoutines::XYZToSpectrumCoef(XYZColor_d(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+      for (int k = 0; k < 3; ++k) out[3 * i + k] = s[k];
+    }
+  }
 }
 
 // Row Y of the reference's spectrum-to-XYZ matrix (its luminance weights).

@@ -85,6 +85,11 @@ SIGNATURES = [
     ("skw_photon_map_export", C.c_int, [_P, C.c_int32, C.c_void_p]),
     ("skw_photon_map_export_irradiance", C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("skw_scene_total_area", C.c_double, [_P]),
+    ("skw_merl_create", C.c_int, [_P, C.c_void_p, C.c_int64, C.POINTER(_P)]),
+    ("skw_merl_destroy", None, [_P]),
+    ("skw_merl_export", C.c_int, [_P, _P, _P]),
+    ("skw_merl_eval_host", C.c_int, [_P, _P, _P, C.c_int64, _P, _P]),
+    ("skw_merl_sample_host", C.c_int, [_P, _P, _P, C.c_int64, _P, _P, _P]),
     ("skw_scene_set_medium", C.c_int, [_P, C.c_void_p]),
     ("skw_render_photon", C.c_int, [_P, _P, C.c_void_p, C.c_void_p, C.c_void_p, _P, _P]),
     ("skw_scene_n_triangles", C.c_int64, [_P]),

@@ -666,9 +666,25 @@ __device__ V3 total_scattering_bxdf(const Bsdf &b, bool glossy, V3 wi) {
   return v3(fminf(1.0f, fmaxf(0.0f, ret.x)), fminf(1.0f, fmaxf(0.0f, ret.y)), fminf(1.0f, fmaxf(0.0f, ret.z)));
 }
 
+// BxDF::TotalScattering of the measured BRDF: MERLMeasured::Sample over the
+// same grid, again with the world incident direction taken as local.
+__device__ V3 total_scattering_measured(const Bsdf &b, V3 wi) {
+  V3 ret = v3(0, 0, 0);
+  for (int y = 0; y < 5; ++y)
+    for (int x = 0; x < 5; ++x) {
+      V3 wo;
+      float pdf = 0.0f;
+      const V3 f = merl_sample(b.merl, wi, (x + 0.5f) * 0.2f, (y + 0.5f) * 0.2f, wo, pdf);
+      if (pdf > 0.0f) ret = ret + f * (fabsf(wo.z) / pdf);
+    }
+  ret = ret * (1.0f / 25.0f);
+  return v3(fminf(1.0f, fmaxf(0.0f, ret.x)), fminf(1.0f, fmaxf(0.0f, ret.y)), fminf(1.0f, fmaxf(0.0f, ret.z)));
+}
+
 // BSDF::TotalScattering over the reflection components (BSDF.cpp:209-224).
 __device__ V3 total_scattering_reflection(const Bsdf &b, V3 wi) {
   V3 r = v3(0, 0, 0);
+  if (b.kind == kMeasured) r = total_scattering_measured(b, wi);
   if (b.kind == kLambert || b.kind == kPlastic) r = b.kd;  // Lambertian::TotalScattering returns kd
   if (b.kind == kOrenNayar) r = total_scattering_bxdf(b, false, wi);
   if (b.kind == kPlastic || b.kind == kMetal) r = r + total_scattering_bxdf(b, true, wi);

@@ -5,6 +5,7 @@
 // Each translation unit gets its own internal copy.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -99,6 +100,7 @@ struct Bsdf {
   V3 kd, ks;
   float exponent, on_a, on_b;
   V3 eta, k2;
+  MerlDev merl;
   __device__ __forceinline__ V3 local(V3 w) const { return v3(dot(w, e1), dot(w, e2), dot(w, n)); }
   __device__ __forceinline__ V3 world(V3 l) const { return e1 * l.x + e2 * l.y + n * l.z; }
   __device__ __forceinline__ int components() const { return kind == kPlastic ? 2 : 1; }
@@ -168,12 +170,134 @@ __device__ __forceinline__ float diffuse_pdf(V3 wi, V3 wo) {  // BxDF::PDF (Core
   return wi.z * wo.z > 0.0f ? fabsf(wo.z) * kInvPi : 0.0f;
 }
 
+// ------------------------------------------------------- measured BRDF --
+// MERLMeasuredData::GetBRDF / Sample / PDF (BxDFs/MERLMeasured.cpp:254-369)
+// in float, over the loader's half table and the sampling segmentations.
+__device__ __forceinline__ float sph_theta(V3 v) { return acosf(fminf(1.0f, fmaxf(-1.0f, v.z))); }
+__device__ __forceinline__ float sph_phi(V3 v) {
+  const float p = atan2f(v.y, v.x);
+  return p < 0.0f ? p + 2.0f * kPi : p;
+}
+
+__device__ V3 merl_brdf(const MerlDev &m, V3 wi, V3 wo) {
+  V3 h = wi + wo;
+  if (h.x == 0.0f && h.y == 0.0f && h.z == 0.0f) return v3(0, 0, 0);
+  h = normalized(h);
+  const float sin_t = sqrtf(h.x * h.x + h.y * h.y), cos_t = h.z;
+  float sin_p = 0.0f, cos_p = 1.0f;
+  if (sin_t > 1e-10f) {
+    sin_p = h.y / sin_t;
+    cos_p = h.x / sin_t;
+  }
+  const V3 whx = v3(cos_p * cos_t, sin_p * cos_t, -sin_t), why = v3(-sin_p, cos_p, 0.0f);
+  const V3 diff = v3(dot(wi, whx), dot(wi, why), dot(wi, h));
+  const float th = sph_theta(h), td = sph_theta(diff), pd = sph_phi(diff);
+  const int ipd = (int)(pd * kInvPi * kMerlPhiD) % kMerlPhiD;
+  const int itd = min((int)(td * 2.0f * kInvPi * kMerlThetaD), kMerlThetaD - 1);
+  const float ths = sqrtf(th * 2.0f * kInvPi) * kMerlThetaH;
+  const int ith = min((int)ths, kMerlThetaH - 1);
+  const int idx = ipd + (itd + ith * kMerlThetaD) * kMerlPhiD;
+  const uint16_t *t = m.table;
+  V3 a = v3(__half2float(__ushort_as_half(t[3 * idx])), __half2float(__ushort_as_half(t[3 * idx + 1])),
+            __half2float(__ushort_as_half(t[3 * idx + 2])));
+  if (idx < (kMerlThetaH - 1) * kMerlThetaD * kMerlPhiD) {
+    const float w = ths - (float)(int)ths;
+    const int j = idx + kMerlThetaD * kMerlPhiD;
+    const V3 b = v3(__half2float(__ushort_as_half(t[3 * j])), __half2float(__ushort_as_half(t[3 * j + 1])),
+                    __half2float(__ushort_as_half(t[3 * j + 2])));
+    a = a * (1.0f - w) + b * w;
+  }
+  return a;
+}
+
+__device__ __forceinline__ int merl_incident_bin(V3 wi) {
+  return min((int)(sph_theta(wi) * 2.0f * kInvPi * kSegIncident), kSegIncident - 1);
+}
+
+__device__ float merl_data_pdf(const MerlDev &m, V3 wi, V3 wo) {
+  const float *seg = m.seg + merl_incident_bin(wi) * kSegFloats;
+  const float *cols = seg, *rows = seg + kSegTheta * kSegPhi, *gx = rows + kSegTheta, *gy = gx + kSegPhi;
+  float dp = fabsf(sph_phi(wi) - sph_phi(wo));
+  if (dp > kPi) dp = 2.0f * kPi - dp;
+  const float px = dp * kInvPi, py = sph_theta(wo) * 2.0f * kInvPi;
+  int ci = 0, ri = 0;  // last grid line <= the point (upper_bound - 1)
+  while (ci + 1 < kSegPhi && gx[ci + 1] <= px) ++ci;
+  while (ri + 1 < kSegTheta && gy[ri + 1] <= py) ++ri;
+  const float bx0 = gx[ci], by0 = gy[ri];
+  const float bx1 = ci + 1 < kSegPhi ? gx[ci + 1] : 1.0f, by1 = ri + 1 < kSegTheta ? gy[ri + 1] : 1.0f;
+  const float *cc = cols + ri * kSegPhi;
+  const float row_pdf = ri > 0 ? rows[ri] - rows[ri - 1] : rows[ri];
+  const float col_pdf = ci > 0 ? cc[ci] - cc[ci - 1] : cc[ci];
+  const float d_phi = (bx1 - bx0) * kPi, d_cos = cosf(by0 * (0.5f * kPi)) - cosf(by1 * (0.5f * kPi));
+  return 0.5f * row_pdf * col_pdf / (d_phi * d_cos);
+}
+
+// MERLMeasured::Evaluate / PDF: the incident side's hemisphere folded to +z.
+__device__ __forceinline__ V3 merl_eval(const MerlDev &m, V3 wi, V3 wo) {
+  if (wi.z * wo.z < 0.0f) return v3(0, 0, 0);
+  if (wi.z < 0.0f) {
+    wi.z = -wi.z;
+    wo.z = -wo.z;
+  }
+  return merl_brdf(m, wi, wo);
+}
+__device__ __forceinline__ float merl_pdf(const MerlDev &m, V3 wi, V3 wo) {
+  if (wi.z * wo.z < 0.0f) return 0.0f;
+  if (wi.z < 0.0f) {
+    wi.z = -wi.z;
+    wo.z = -wo.z;
+  }
+  return merl_data_pdf(m, wi, wo);
+}
+
+__device__ __forceinline__ int search_cdf_f(const float *cdf, int n, float u, float &pdf) {
+  int b = 0, e = n - 1;
+  while (b < e) {
+    const int mid = b + (e - b) / 2;
+    if (cdf[mid] <= u) b = mid + 1; else e = mid;
+  }
+  pdf = b == 0 ? cdf[0] : cdf[b] - cdf[b - 1];
+  return b;
+}
+
+__device__ V3 merl_sample(const MerlDev &m, V3 wi, float u0, float u1, V3 &wo, float &pdf) {
+  const bool flip = wi.z < 0.0f;
+  if (flip) wi.z = -wi.z;
+  const float *seg = m.seg + merl_incident_bin(wi) * kSegFloats;
+  const float *cols = seg, *rows = seg + kSegTheta * kSegPhi, *gx = rows + kSegTheta, *gy = gx + kSegPhi;
+  bool opposite = false;
+  if (u0 > 0.5f) {
+    opposite = true;
+    u0 = (u0 - 0.5f) * 2.0f;
+  } else {
+    u0 *= 2.0f;
+  }
+  float rp, cp;
+  const int ri = search_cdf_f(rows, kSegTheta, u1, rp);
+  const float *cc = cols + ri * kSegPhi;
+  const int ci = search_cdf_f(cc, kSegPhi, u0, cp);
+  const float r0 = (u0 - (ci > 0 ? cc[ci - 1] : 0.0f)) / cp, r1 = (u1 - (ri > 0 ? rows[ri - 1] : 0.0f)) / rp;
+  const float bx0 = gx[ci], by0 = gy[ri];
+  const float bx1 = ci + 1 < kSegPhi ? gx[ci + 1] : 1.0f, by1 = ri + 1 < kSegTheta ? gy[ri + 1] : 1.0f;
+  const float c1 = cosf(by0 * (0.5f * kPi)), c2 = cosf(by1 * (0.5f * kPi)), d_cos = c1 - c2;
+  float phi = (bx0 + (bx1 - bx0) * r0) * kPi;
+  if (opposite) phi = 2.0f * kPi - phi;
+  phi += sph_phi(wi);
+  const float ct = c1 - r1 * d_cos, st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+  wo = v3(st * cosf(phi), st * sinf(phi), ct);
+  pdf = 0.5f * rp * cp / ((bx1 - bx0) * kPi * d_cos);
+  const V3 f = merl_brdf(m, wi, wo);
+  if (flip) wo.z = -wo.z;
+  return f;
+}
+
 // BSDF::Evaluate (Core/BSDF.cpp:22-40): every component is a reflection, so
 // directions on opposite sides of the geometric normal give zero.
 __device__ V3 bsdf_eval(const Bsdf &b, V3 wi_w, V3 wo_w) {
   if (!(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f)) return v3(0, 0, 0);
   const V3 wi = b.local(wi_w), wo = b.local(wo_w);
   if (b.kind == kMetal) return microfacet_eval(b, wi, wo);
+  if (b.kind == kMeasured) return merl_eval(b.merl, wi, wo);
   V3 f = diffuse_eval(b, wi, wo);
   if (b.kind == kPlastic) f = f + microfacet_eval(b, wi, wo);
   return f;
@@ -192,6 +316,7 @@ __device__ V3 bsdf_eval_dkd(const Bsdf &b, V3 wi_w, V3 wo_w) {
 __device__ float bsdf_pdf(const Bsdf &b, V3 wi_w, V3 wo_w) {
   const V3 wi = b.local(wi_w), wo = b.local(wo_w);
   if (b.kind == kMetal) return microfacet_pdf(b, wi, wo);
+  if (b.kind == kMeasured) return merl_pdf(b.merl, wi, wo);
   if (b.kind == kPlastic) return 0.5f * (diffuse_pdf(wi, wo) + microfacet_pdf(b, wi, wo));
   return diffuse_pdf(wi, wo);
 }
@@ -201,6 +326,13 @@ __device__ float bsdf_pdf(const Bsdf &b, V3 wi_w, V3 wo_w) {
 // components at the sampled direction, evaluate the whole BSDF.
 __device__ V3 bsdf_sample(const Bsdf &b, V3 wi_w, float uc, float u0, float u1, V3 &wo_w, float &pdf) {
   const V3 wi = b.local(wi_w);
+  if (b.kind == kMeasured) {  // the single MERLMeasured component (BSDF.cpp:110-168)
+    V3 wo;
+    merl_sample(b.merl, wi, u0, u1, wo, pdf);
+    wo_w = b.world(wo);
+    if (!(pdf > 0.0f)) return v3(0, 0, 0);
+    return bsdf_eval(b, wi_w, wo_w);
+  }
   const int nc = b.components();
   const int comp = min((int)(uc * nc), nc - 1);
   V3 wo;
@@ -273,6 +405,7 @@ __device__ Bsdf make_bsdf(const SceneDev &S, const Hit &h, int prim) {
   b.on_b = m.on_b;
   b.eta = load3(m.eta);
   b.k2 = load3(m.k2);
+  b.merl = m.merl;
   return b;
 }
 

@@ -6,9 +6,11 @@
 
 #include <cstdint>
 
+#include "merl.h"
+
 namespace skw {
 
-enum BsdfKind : int32_t { kLambert = 0, kOrenNayar = 1, kPlastic = 2, kMetal = 3 };
+enum BsdfKind : int32_t { kLambert = 0, kOrenNayar = 1, kPlastic = 2, kMetal = 3, kMeasured = 4 };
 
 // Material constants after the reference's clamps (MatteMaterial.cpp:29-50,
 // PlasticMaterial.cpp:33-53, MetalMaterial.cpp:58-101).
@@ -19,6 +21,7 @@ struct DevMaterial {
   float exponent;      // Blinn exponent = 1 / clamp(roughness, 0.001, 1)
   float on_a, on_b;    // Oren-Nayar A, B
   float eta[3], k2[3]; // conductor refractive index and squared absorption
+  MerlDev merl;        // kMeasured: the tabulated BRDF
 };
 
 struct AreaLight {

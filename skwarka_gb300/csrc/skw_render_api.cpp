@@ -19,6 +19,8 @@
 using skw::cuda_fail;
 using skw::fail;
 
+extern "C" skw::MerlDev skw_merl_device_view(const skw_merl *m);
+
 namespace {
 
 template <class T>
@@ -242,6 +244,13 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
       d.kind = skw::kPlastic;
     } else if (m.kind == SKW_MATERIAL_METAL) {
       d.kind = skw::kMetal;
+    } else if (m.kind == SKW_MATERIAL_MEASURED) {
+      if (!m.measured) {
+        skw_scene_destroy(s);
+        return fail(ctx, SKW_ERR_ARG, "a measured material needs its skw_merl");
+      }
+      d.kind = skw::kMeasured;
+      d.merl = skw_merl_device_view(m.measured);
     } else {
       skw_scene_destroy(s);
       return fail(ctx, SKW_ERR_UNSUPPORTED, "unknown material kind");

@@ -17,7 +17,56 @@ import numpy as np
 from . import _lib
 from .accel import Context, TriangleMesh, default_context
 
-MATTE, PLASTIC, METAL = 0, 1, 2
+MATTE, PLASTIC, METAL, MEASURED = 0, 1, 2, 3
+
+
+class MeasuredBRDF:
+    """A tabulated BRDF in the MERL binary layout (skw_merl): the file image
+    is converted and its sampling tables built on the host, then uploaded."""
+
+    def __init__(self, data: bytes, ctx: "Context | None" = None, device: bool = True):
+        """device=False builds the host tables only (no GPU needed; the host
+        entry points work, a scene cannot use it)."""
+        self.data = bytes(data)
+        self.ctx = (ctx or default_context()) if device else None
+        ch = self.ctx.handle if self.ctx is not None else None
+        h = C.c_void_p()
+        _lib.check(_lib.load().skw_merl_create(ch, self.data, len(self.data), C.byref(h)), ch)
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            _lib.load().skw_merl_destroy(h)
+            self.handle = None
+
+    def export(self):
+        """(half table (1458000, 3) uint16, segmentations (90, 1173) float32)."""
+        import numpy as np
+        t = np.empty((90 * 90 * 180, 3), np.uint16)
+        sg = np.zeros((90, 1173), np.float32)
+        _lib.check(_lib.load().skw_merl_export(self.handle, t.ctypes.data, sg.ctypes.data))
+        return t, sg
+
+    def eval_host(self, wi, wo):
+        import numpy as np
+        wi = np.ascontiguousarray(wi, np.float64).reshape(-1, 3)
+        wo = np.ascontiguousarray(wo, np.float64).reshape(-1, 3)
+        f = np.empty_like(wi)
+        pdf = np.empty(len(wi))
+        _lib.check(_lib.load().skw_merl_eval_host(self.handle, wi.ctypes.data, wo.ctypes.data, len(wi), f.ctypes.data,
+                                                  pdf.ctypes.data))
+        return f, pdf
+
+    def sample_host(self, wi, u):
+        import numpy as np
+        wi = np.ascontiguousarray(wi, np.float64).reshape(-1, 3)
+        u = np.ascontiguousarray(u, np.float64).reshape(-1, 2)
+        wo, f = np.empty_like(wi), np.empty_like(wi)
+        pdf = np.empty(len(wi))
+        _lib.check(_lib.load().skw_merl_sample_host(self.handle, wi.ctypes.data, u.ctypes.data, len(wi), wo.ctypes.data,
+                                                    f.ctypes.data, pdf.ctypes.data))
+        return wo, f, pdf
 
 
 @dataclass
@@ -29,6 +78,7 @@ class Material:
     sigma: float = 0.0
     eta: tuple = (1.0, 1.0, 1.0)
     k: tuple = (0.0, 0.0, 0.0)
+    measured: "MeasuredBRDF | None" = None
 
 
 @dataclass
@@ -84,7 +134,7 @@ class Camera:
 
 class skw_material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("roughness", C.c_float),
-                ("sigma", C.c_float), ("eta", C.c_float * 3), ("k", C.c_float * 3)]
+                ("sigma", C.c_float), ("eta", C.c_float * 3), ("k", C.c_float * 3), ("measured", C.c_void_p)]
 
 
 class skw_render_primitive(C.Structure):
@@ -105,9 +155,14 @@ class skw_render_params(C.Structure):
     _fields_ = [("spp_x", C.c_int32), ("spp_y", C.c_int32), ("light_samples", C.c_int32), ("seed", C.c_uint64)]
 
 
-def c_material(m: Material) -> skw_material:
+def c_material(m: Material, measured_handle=None) -> skw_material:
+    """measured_handle overrides the handle of m.measured (the reference
+    driver passes its own)."""
+    h = measured_handle
+    if h is None and m.measured is not None:
+        h = m.measured.handle
     return skw_material(m.kind, (C.c_float * 3)(*m.kd), (C.c_float * 3)(*m.ks), m.roughness, m.sigma,
-                        (C.c_float * 3)(*m.eta), (C.c_float * 3)(*m.k))
+                        (C.c_float * 3)(*m.eta), (C.c_float * 3)(*m.k), h)
 
 
 def c_camera(cam: Camera) -> skw_camera:

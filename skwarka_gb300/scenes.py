@@ -293,3 +293,28 @@ def camera_rays(camera, spp_x: int, spp_y: int, seed: int = 0) -> np.ndarray:
     r[:, 3:6] = d
     r[:, 7] = np.inf
     return r
+
+
+def merl_table(seed: int = 7, kd=(0.35, 0.25, 0.15), ks=(0.5, 0.5, 0.5), exponent: float = 40.0,
+               noise: float = 0.02) -> bytes:
+    """A measured-style BRDF in the MERL binary layout (3 int32 dims, then 3
+    channels of 90 x 90 x 180 doubles, stored divided by the loader's channel
+    scales 1/1500, 1.15/1500, 1.66/1500): a seeded microfacet formula --
+    Lambertian kd plus a normalised Blinn lobe in the half-vector angle with
+    Schlick's Fresnel in the difference angle -- times 1 + N(0, noise), at
+    the centre of every (theta_h, theta_d, phi_d) bin (theta_h bins are
+    quadratic, as in the format)."""
+    rng = np.random.default_rng(seed)
+    ih = (np.arange(90) + 0.5) / 90.0
+    th = ih * ih * (np.pi / 2)
+    td = (np.arange(90) + 0.5) * (np.pi / 2) / 90.0
+    TH, TD = np.meshgrid(th, td, indexing="ij")
+    fres = 0.04 + 0.96 * (1.0 - np.cos(TD)) ** 5
+    lobe = (exponent + 2.0) / (8.0 * np.pi) * np.cos(TH) ** exponent * fres
+    out = []
+    scales = (1.0 / 1500, 1.15 / 1500, 1.66 / 1500)
+    for c in range(3):
+        f = kd[c] / np.pi + ks[c] * lobe
+        f = np.repeat(f[:, :, None], 180, axis=2) * (1.0 + noise * rng.normal(size=(90, 90, 180)))
+        out.append((np.maximum(f, 0.0) / scales[c]).astype("<f8").reshape(-1))
+    return np.array([90, 90, 180], "<i4").tobytes() + b"".join(o.tobytes() for o in out)

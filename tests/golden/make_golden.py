@@ -94,6 +94,18 @@ def render_golden():
     np.savez_compressed(OUT / "direct_planes.npz", **planes)
 
 
+def measured_golden():
+    """The reference's renders of a plane with the synthetic measured BRDF
+    (scenes.merl_table) under an area light and a point light, 16x16 spp."""
+    from skwarka_gb300.render import MeasuredBRDF
+    ref = Reference()
+    m = MeasuredBRDF(scenes.merl_table(), device=False)
+    out = {}
+    for name, (p, mats, l, c) in sf.measured_plane_scenes(m).items():
+        out[name], _ = ref.render_direct(p, mats, l, c, 16, 16)
+    np.savez_compressed(OUT / "measured_planes.npz", **out)
+
+
 def medium_golden():
     """The reference's direct-lighting renders with a homogeneous medium
     (scene_fixtures.medium_cases) at 32 x 32, 16x16 spp."""
@@ -120,6 +132,10 @@ def photon_golden():
     np.savez_compressed(OUT / "photon_box_64.npz", photon=photon, direct=direct,
                         counts=np.array([info["caustic"], info["direct"], info["indirect"], info["irradiance"]]))
 
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "measured":
+    measured_golden()
+    print("measured golden written")
 
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "medium":
     medium_golden()

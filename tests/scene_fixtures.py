@@ -240,3 +240,16 @@ def medium_cases():
     out["box_area"] = (bp, bm, [], bcam(32, 32), Medium(sigma_a=(0.05,) * 3, sigma_s=(0.2,) * 3, g=0.3, step=0.05))
     out["box_absorb"] = (bp, bm, [], bcam(32, 32), Medium(sigma_a=(0.25,) * 3, sigma_s=(0, 0, 0), g=0.3, step=0.05))
     return out
+
+
+def measured_plane_scenes(measured):
+    """The plane scenes of material_plane_scenes with the measured BRDF
+    `measured` (a skwarka_gb300.render.MeasuredBRDF) as the plane's material."""
+    from skwarka_gb300.render import MEASURED, Material
+    base = material_plane_scenes()
+    m = Material(kind=MEASURED, measured=measured)
+    out = {}
+    for light in ("area", "point"):
+        prims, mats, lights, cam = base[light + "_matte"]
+        out[light + "_measured"] = (prims, [m] + mats[1:], lights, cam)
+    return out
