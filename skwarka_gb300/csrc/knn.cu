@@ -50,13 +50,22 @@ namespace {
 
 constexpr int kMaxStack = 64;  // > tree depth (ceil(log2(n + 1)) <= 31 for n < 2^31)
 
+// A heap entry: the squared distance as its IEEE bit pattern (for the
+// non-negative doubles here, unsigned integer order is the double order, so
+// the heap compares on the integer pipe) and the tree position.
 struct Cand {
-  double d2;
+  unsigned long long key;
   int32_t idx;
+  __device__ __forceinline__ double d2() const { return __longlong_as_double((long long)key); }
 };
 
+__device__ __forceinline__ Cand make_cand(double d2, int32_t idx) {
+  return Cand{(unsigned long long)__double_as_longlong(d2), idx};
+}
+
+// (d2, idx) lexicographic, as the reference's NearestPoint comparison.
 __device__ __forceinline__ bool cand_less(const Cand &a, const Cand &b) {
-  return a.d2 == b.d2 ? a.idx < b.idx : a.d2 < b.d2;
+  return a.key == b.key ? a.idx < b.idx : a.key < b.key;
 }
 
 // Sift `value` up from `hole` towards `top`.
@@ -102,11 +111,65 @@ struct Query {
   double n[3];
   double cos_t, sin_t;
   bool filter;
+  float qf[3];  // q rounded to float
+  float eq;     // max |q - qf| over the axes
+  bool qle[3];  // q <= qf on the axis (decides q <= split when split == qf)
+  float nf[3];  // the normal in float (filter pre-test)
 };
 
-// PhotonFilter::operator() (PhotonInternalTypes.h:127-133).
+// Fills the float copy of the query point used by the pre-tests.
+__device__ __forceinline__ void query_float(Query &Q) {
+  float e = 0.0f;
+  for (int k = 0; k < 3; ++k) {
+    Q.qf[k] = (float)Q.q[k];
+    Q.qle[k] = Q.q[k] <= (double)Q.qf[k];
+    e = fmaxf(e, (float)fabs(Q.q[k] - (double)Q.qf[k]));
+    Q.nf[k] = (float)Q.n[k];
+  }
+  Q.eq = e * 1.0001f;
+}
+
+// q[axis] <= split for a float split, exactly, without double arithmetic:
+// qf is the float nearest to q, so qf < split implies q < split and
+// qf > split implies q > split.
+__device__ __forceinline__ bool q_le_split(const Query &Q, uint32_t axis, float split) {
+  const float qf = Q.qf[axis];
+  return qf < split || (qf == split && Q.qle[axis]);
+}
+
+// PhotonFilter::operator() (PhotonInternalTypes.h:127-133), with float
+// pre-tests: the normal's cosine and the in-plane test are decided in float
+// when they clear their thresholds by more than the float error (unit
+// vectors: a few 1e-7), else in double as the reference computes them.
+__device__ __forceinline__ bool photon_filter_exact(const Query &Q, const float4 p, uint16_t nid,
+                                                    const double *__restrict__ dirs);
 __device__ __forceinline__ bool photon_filter(const Query &Q, const float4 p, uint16_t nid,
                                               const double *__restrict__ dirs) {
+  const float nx = (float)__ldg(dirs + 3 * nid), ny = (float)__ldg(dirs + 3 * nid + 1),
+              nz = (float)__ldg(dirs + 3 * nid + 2);
+  const float cf = nx * Q.nf[0] + ny * Q.nf[1] + nz * Q.nf[2];
+  const float ct = (float)Q.cos_t;
+  if (cf < ct - 2e-6f) return false;
+  if (cf > ct + 2e-6f) {
+    // |to . n| < sin_t |to|, compared as squares when both sides clearly differ
+    const float tx = p.x - Q.qf[0], ty = p.y - Q.qf[1], tz = p.z - Q.qf[2];
+    const float dn = tx * Q.nf[0] + ty * Q.nf[1] + tz * Q.nf[2];
+    const float l2 = tx * tx + ty * ty + tz * tz;
+    const float st = (float)Q.sin_t;
+    const float lhs = dn * dn, rhs = st * st * l2;
+    // error: the float query rounding eq on each component plus relative rounding
+    const float a = fabsf(tx) + fabsf(ty) + fabsf(tz);
+    // |d(dn)| <= 3 eq + 5e-7 a and |d(l2)| <= 2 a (eq + 6e-8 a) (a = |tx| + |ty| + |tz|), so
+    // the squares move by at most 2 a |d(dn)| + |d(dn)|^2 and st^2 |d(l2)|
+    const float err = 12.0f * Q.eq * (a + Q.eq) + 4e-6f * a * a + 2e-6f * (lhs + rhs) + 1e-37f;
+    if (lhs + err < rhs) return true;
+    if (lhs - err > rhs) return false;
+  }
+  return photon_filter_exact(Q, p, nid, dirs);
+}
+
+__device__ __forceinline__ bool photon_filter_exact(const Query &Q, const float4 p, uint16_t nid,
+                                                    const double *__restrict__ dirs) {
   const double nx = __ldg(dirs + 3 * nid), ny = __ldg(dirs + 3 * nid + 1), nz = __ldg(dirs + 3 * nid + 2);
   const double cosn = __dadd_rn(__dadd_rn(__dmul_rn(nx, Q.n[0]), __dmul_rn(ny, Q.n[1])), __dmul_rn(nz, Q.n[2]));
   if (!(cosn > Q.cos_t)) return false;
@@ -123,35 +186,65 @@ __device__ __forceinline__ double point_d2(const float4 p, const Query &Q) {
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
+// Float pre-tests.  A point's squared distance and a splitting plane's
+// squared distance are first computed in float with a bound E on their
+// distance from the reference's double values (the float query rounding eq,
+// the rounding of each float difference and square, and the double
+// result's own rounding); only when the float value lies within E of the
+// current radius is the exact double value computed.  u = 2^-24.
+__device__ __forceinline__ void sq_bound(float d, float eq, float &sq, float &err) {
+  const float a = fabsf(d);
+  const float ex = a * 5.9604645e-8f + eq;  // |exact difference - d|
+  sq = d * d;
+  err = (2.0f * a + ex) * ex;
+}
+
 // Walks the tree in the reference's order, calling visit(ni, p, d2, maxd2)
 // for every point with d2 < maxd2 (visit may shrink maxd2).  Returns nodes
-// visited (for statistics) or -1 on stack overflow.
+// visited (for statistics) or -1 on stack overflow.  Stack entries hold the
+// far child, its parent (to recompute the plane distance exactly when the
+// float pre-test cannot decide) and the float plane distance.
 template <class Visit>
 __device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, const Query &Q, double &maxd2,
                                     Visit &&visit) {
   if (n <= 0) return 0;
-  uint32_t st_node[kMaxStack];
-  double st_d2[kMaxStack];
+  uint32_t st_node[kMaxStack], st_parent[kMaxStack];
+  float st_pd[kMaxStack];
   int sp = 0, visited = 0;
   int cur = 0;
+  // maxd2 in float, rounded down (a float below it is below maxd2 too)
+  auto lo_f = [](double m) { return __double2float_rd(m); };
+  auto hi_f = [](double m) { return __double2float_ru(m); };
+  float mlo = lo_f(maxd2), mhi = hi_f(maxd2);
   for (;;) {
     const float4 p = __ldg(nodes + cur);
     ++visited;
-    const double d2 = point_d2(p, Q);
-    if (d2 < maxd2) visit(cur, p, d2, maxd2);
+    {
+      float sx, ex, sy, ey, sz, ez;
+      sq_bound(p.x - Q.qf[0], Q.eq, sx, ex);
+      sq_bound(p.y - Q.qf[1], Q.eq, sy, ey);
+      sq_bound(p.z - Q.qf[2], Q.eq, sz, ez);
+      const float d2f = (sx + sy) + sz;
+      const float E = (ex + ey + ez) * 1.0001f + d2f * 4.0e-7f + 1e-37f;
+      if (!(d2f - E >= mhi)) {  // not certainly outside: decide exactly
+        const double d2 = point_d2(p, Q);
+        if (d2 < maxd2) {
+          visit(cur, p, d2, maxd2);
+          mlo = lo_f(maxd2);
+          mhi = hi_f(maxd2);
+        }
+      }
+    }
     const uint32_t w = __float_as_uint(p.w);
     int next = -1;
     if ((w & 3u) != 3u) {
       const uint32_t axis = w & 3u;
-      const double split = (double)(axis == 0 ? p.x : (axis == 1 ? p.y : p.z));
-      const double qa = Q.q[axis];
-      const double pd = __dsub_rn(qa, split);
-      const double pd2 = __dmul_rn(pd, pd);
+      const float split = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
       const uint32_t right = w >> 3;
       const bool has_left = (w & 4u) != 0u, has_right = right < (uint32_t)n;
       const int left_i = cur + 1;
       int near_i, far_i;
-      if (qa <= split) {
+      if (q_le_split(Q, axis, split)) {
         near_i = has_left ? left_i : -1;
         far_i = has_right ? (int)right : -1;
       } else {
@@ -161,14 +254,31 @@ __device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, con
       if (far_i >= 0) {
         if (sp >= kMaxStack) return -1;
         st_node[sp] = (uint32_t)far_i;
-        st_d2[sp] = pd2;
+        st_parent[sp] = (uint32_t)cur;
+        st_pd[sp] = Q.qf[axis] - split;
         ++sp;
       }
       next = near_i;
     }
     while (next < 0 && sp > 0) {
       --sp;
-      if (st_d2[sp] < maxd2) next = (int)st_node[sp];
+      // the reference's pop test: (qa - split)^2 < maxd2, in double
+      float s2, e2;
+      sq_bound(st_pd[sp], Q.eq, s2, e2);
+      const float E = e2 * 1.0001f + s2 * 4.0e-7f + 1e-37f;
+      bool take;
+      if (s2 + E < mlo) {
+        take = true;
+      } else if (s2 - E >= mhi) {
+        take = false;
+      } else {
+        const float4 pp = __ldg(nodes + st_parent[sp]);
+        const uint32_t ax = __float_as_uint(pp.w) & 3u;
+        const double sp_d = (double)(ax == 0 ? pp.x : (ax == 1 ? pp.y : pp.z));
+        const double pd = __dsub_rn(Q.q[ax], sp_d);
+        take = __dmul_rn(pd, pd) < maxd2;
+      }
+      if (take) next = (int)st_node[sp];
     }
     if (next < 0) return visited;
     cur = next;
@@ -203,6 +313,7 @@ __global__ void __launch_bounds__(128) k_knn(const float4 *__restrict__ nodes, c
     Q.n[0] = Q.n[1] = Q.n[2] = 0.0;
     Q.cos_t = Q.sin_t = 0.0;
   }
+  query_float(Q);
   Cand local_heap[KMAX > 0 ? KMAX : 1];
   Cand *heap = KMAX > 0 ? local_heap : scratch + i * (int64_t)k;
   int size = 0;
@@ -212,10 +323,10 @@ __global__ void __launch_bounds__(128) k_knn(const float4 *__restrict__ nodes, c
     visited = walk(nodes, n, Q, maxd2, [&](int ni, const float4 p, double d2, double &md2) {
       if (Q.filter && !photon_filter(Q, p, __ldg(nids + ni), dirs)) return;
       if (size < k) {
-        heap[size++] = Cand{d2, ni};
+        heap[size++] = make_cand(d2, ni);
         if (size == k) {
           heap_make(heap, size);
-          md2 = heap[0].d2;
+          md2 = heap[0].d2();
         }
       } else {
         // pop_heap: the top goes to the back; the back's old value is re-placed
@@ -223,8 +334,8 @@ __global__ void __launch_bounds__(128) k_knn(const float4 *__restrict__ nodes, c
         heap[k - 1] = heap[0];
         heap_adjust(heap, 0, k - 1, back);
         // replace the (popped) back with the new point and push it
-        heap_push_up(heap, k - 1, 0, Cand{d2, ni});
-        md2 = heap[0].d2;
+        heap_push_up(heap, k - 1, 0, make_cand(d2, ni));
+        md2 = heap[0].d2();
       }
     });
     if (visited < 0) atomicOr(status, 2u);
@@ -232,7 +343,7 @@ __global__ void __launch_bounds__(128) k_knn(const float4 *__restrict__ nodes, c
   out_count[i] = size;
   for (int j = 0; j < k; ++j) {
     out_idx[i * k + j] = j < size ? heap[j].idx : -1;
-    out_d2[i * k + j] = j < size ? heap[j].d2 : 0.0;
+    out_d2[i * k + j] = j < size ? heap[j].d2() : 0.0;
   }
   if (out_visited) out_visited[i] = visited;
 }
@@ -263,6 +374,7 @@ __global__ void __launch_bounds__(128) k_nearest(const float4 *__restrict__ node
     Q.n[0] = Q.n[1] = Q.n[2] = 0.0;
     Q.cos_t = Q.sin_t = 0.0;
   }
+  query_float(Q);
   double maxd2 = __dmul_rn(max_dist, max_dist);
   int best = -1;
   const int v = walk(nodes, n, Q, maxd2, [&](int ni, const float4 p, double d2, double &md2) {

@@ -223,10 +223,14 @@ __device__ __forceinline__ bool node_visit(const float4 na, const float4 nb, con
 }
 
 #ifndef SKW_TRAV_SCAP
-#define SKW_TRAV_SCAP 16
+#define SKW_TRAV_SCAP 8
 #endif
 #ifndef SKW_TRAV_REFILL
-#define SKW_TRAV_REFILL 8
+#define SKW_TRAV_REFILL 16
+#endif
+// Postponed leaves (speculative node steps), see k_trace.
+#ifndef SKW_TRAV_POSTPONE
+#define SKW_TRAV_POSTPONE 1
 #endif
 
 // Traversal stack: the first SCAP entries of each thread live in shared
@@ -255,9 +259,12 @@ struct Stack {
   // Pops until an entry survives the re-cull against tcull (the reference
   // culls the others when it pops them).
   __device__ __forceinline__ bool pop(float tcull, uint32_t &a, uint32_t &b) {
+    float lo;
+    return pop(tcull, a, b, lo);
+  }
+  __device__ __forceinline__ bool pop(float tcull, uint32_t &a, uint32_t &b, float &lo) {
     while (sp > 0) {
       --sp;
-      float lo;
       if (sp < SCAP) {
         lo = slo[sp][threadIdx.x];
         a = sa[sp][threadIdx.x];
@@ -335,6 +342,55 @@ __device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const 
   return true;
 }
 
+// One internal-node step of descend(): box-tests the present children of
+// (cur_a, cur_b), makes the first passing one (in the reference's pop order)
+// current and pushes the others; pops when none passes.  cur_lo tracks the
+// current node's widened entry distance.  False when the stack runs out.
+template <int CAP>
+__device__ __forceinline__ bool step_internal(const float4 *__restrict__ nodes, const RayF &r, const SlabRay &s,
+                                              float tcull, Stack<CAP> &st, uint32_t &cur_a, uint32_t &cur_b,
+                                              float &cur_lo, unsigned *status) {
+  const uint32_t type = cur_b & 3u, mask = (cur_b >> 2) & 7u;
+  const uint32_t sL = cur_a, sM = cur_a + (mask & 1u), sR = sM + ((mask >> 1) & 1u);
+  const float dax = type == 1u ? r.dx : (type == 2u ? r.dy : r.dz);
+  const bool near_right = !(dax > 0.0f);
+  uint32_t slot[3], present[3];
+  slot[0] = near_right ? sR : sL;
+  present[0] = near_right ? (mask & 4u) : (mask & 1u);
+  slot[1] = sM;
+  present[1] = mask & 2u;
+  slot[2] = near_right ? sL : sR;
+  present[2] = near_right ? (mask & 1u) : (mask & 4u);
+  bool pass[3];
+  float lo[3];
+  uint32_t wa[3], wb[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    pass[k] = false;
+    wa[k] = wb[k] = 0u;
+    lo[k] = 0.0f;
+    if (present[k]) {
+      const float4 ca = __ldg(nodes + 2 * slot[k]);
+      const float4 cb = __ldg(nodes + 2 * slot[k] + 1);
+      pass[k] = node_visit(ca, cb, s, r.tmin, tcull, lo[k]);
+      wa[k] = __float_as_uint(cb.z);
+      wb[k] = __float_as_uint(cb.w);
+    }
+  }
+  const int first = pass[0] ? 0 : (pass[1] ? 1 : (pass[2] ? 2 : -1));
+  if (st.sp + 2 > CAP) {
+    atomicOr(status, 1u);
+    return false;
+  }
+  if (pass[2] && first != 2) st.push(wa[2], wb[2], lo[2]);
+  if (pass[1] && first != 1) st.push(wa[1], wb[1], lo[1]);
+  if (first < 0) return st.pop(tcull, cur_a, cur_b, cur_lo);
+  cur_a = first == 0 ? wa[0] : (first == 1 ? wa[1] : wa[2]);
+  cur_b = first == 0 ? wb[0] : (first == 1 ? wb[1] : wb[2]);
+  cur_lo = first == 0 ? lo[0] : (first == 1 ? lo[1] : lo[2]);
+  return true;
+}
+
 // Exact double-precision t of the hit on slot `slot` (its barycentric tests
 // are known to pass).
 __device__ __forceinline__ double exact_t(const float4 *__restrict__ tris, const RayF &r, int slot, float fallback) {
@@ -398,6 +454,11 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
   int best_slot = -1;
   float lo_t = 0.0f, hi_t = 0.0f;  // bracket of the reference's current tmax
   uint32_t flags = 0;              // SKW_HIT_* bits; bit 3: [lo_t, hi_t] brackets an exact double
+#if SKW_TRAV_POSTPONE
+  bool trav = false, has_post = false;  // traversal not finished; a leaf is postponed
+  uint32_t post_a = 0, post_cnt = 0;
+  float cur_lo = 0.0f;
+#endif
 
   while (true) {
     const unsigned idle = __ballot_sync(0xffffffffu, ray_i < 0);
@@ -421,6 +482,11 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
           store_result<CLOSEST>(out, out_index, ray_i, make_int4(0x7f800000, -1, -1, 0), false);
           ray_i = -1;
         }
+#if SKW_TRAV_POSTPONE
+        trav = true;
+        has_post = false;
+        cur_lo = lo;
+#endif
       }
     }
     if (__ballot_sync(0xffffffffu, ray_i >= 0) == 0u) {
@@ -429,6 +495,79 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     }
     if (ray_i < 0) continue;
 
+#if SKW_TRAV_POSTPONE
+    // Node steps continue past a lane's first leaf (postponed) until every
+    // lane of the warp holds one or the lane reaches a second leaf; the
+    // leaves are then tested in the order they were reached, which is the
+    // reference's order.  Nodes stepped through before the postponed leaf
+    // is tested see a larger tmax than the reference's -- a superset of its
+    // visits, whose extra triangles all lie beyond the final tmax.
+    const float tcull = CLOSEST ? hi_t : r.tmax;
+    while (trav) {
+      if ((cur_b & 3u) == 0u) {  // a leaf
+        if (has_post) break;
+        if (!(cur_lo > tcull)) {
+          post_a = cur_a;
+          post_cnt = cur_b >> 8;
+          has_post = true;
+        }
+        trav = st.pop(tcull, cur_a, cur_b, cur_lo);
+      } else {
+        trav = step_internal(nodes, r, s, tcull, st, cur_a, cur_b, cur_lo, status);
+      }
+      if (__all_sync(__activemask(), has_post)) break;
+    }
+    bool hit = false;
+    if (has_post) {
+      has_post = false;
+      const uint32_t a = post_a, cnt = post_cnt;
+      for (uint32_t k = 0; k < cnt; ++k) {
+        const int slot = (int)(a + k);
+        float3 v0, v1, v2;
+        int prim, tri;
+        load_tri(tris, (uint32_t)slot, v0, v1, v2, prim, tri);
+        float t, et;
+        int res = tri_test32(r, v0, v1, v2, t, et);
+        if (res == kMiss) continue;
+        if (CLOSEST) {
+          if (res == kHit) {
+            if (__fsub_rd(t, et) > hi_t) continue;  // certainly beyond the current tmax
+            if (__fadd_ru(t, et) < lo_t) {          // certainly nearer: accept in float
+              best_slot = slot;
+              lo_t = __fsub_rd(t, et);
+              hi_t = __fadd_ru(t, et);
+              flags &= ~8u;
+              continue;
+            }
+          }
+          // Exact re-test against the reference's exact current tmax.
+          const double cur_max = best_slot < 0 ? (double)r.tmax : exact_t(tris, r, best_slot, hi_t);
+          double t64;
+          if (tri_test64(r, v0, v1, v2, (double)r.tmin, cur_max, t64)) {
+            if (best_slot >= 0 && fabs(t64 - cur_max) <= 1e-12 * fabs(t64)) flags |= 2u;
+            best_slot = slot;
+            lo_t = __double2float_rd(t64);
+            hi_t = __double2float_ru(t64);
+            flags |= 1u | 8u;
+          }
+        } else {
+          if (res == kHit) {
+            if (t + et < r.tmax) {
+              hit = true;
+              break;
+            }
+            if (t - et > r.tmax) continue;
+          }
+          double t64;
+          if (tri_test64(r, v0, v1, v2, (double)r.tmin, (double)r.tmax, t64)) {
+            hit = true;
+            break;
+          }
+        }
+      }
+    }
+    bool done = hit || (!trav && !has_post);
+#else
     const float tcull = CLOSEST ? hi_t : r.tmax;
     bool done = !descend(nodes, r, s, tcull, st, cur_a, cur_b, status);
     bool hit = false;
@@ -481,6 +620,7 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
       }
       done = hit || !st.pop(CLOSEST ? hi_t : r.tmax, cur_a, cur_b);
     }
+#endif
     if (done) {
       int4 h = make_int4(0x7f800000, -1, -1, (int)(flags & 7u));
       if (CLOSEST && best_slot >= 0) {
