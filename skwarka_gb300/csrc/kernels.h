@@ -68,11 +68,13 @@ cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, i
 cudaError_t launch_shade(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin, int spp,
                          int slots, int n_light_samples, const void *rays, const void *hits, float *contrib,
                          void *srays, int *starget, float *srgb, int *scount, void *brays, int *btarget, float *brgb,
-                         int *bcount, int block, cudaStream_t s);
+                         int *bcount, float *bnrm, int block, cudaStream_t s);
+// bnrm: per BSDF-queue entry, the shading normal turned to the viewer (the
+// light-choice density of the light a BSDF ray hits depends on it).
 cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                            const int *starget, const float *srgb, const int *scount, const void *brays,
                            const void *bhits, const int *btarget, const float *brgb, const int *bcount,
-                           float *contrib, cudaStream_t s);
+                           const float *bnrm, float *contrib, cudaStream_t s);
 // tcam (may be null): per-sample transmittance of the camera ray's medium
 // segment; with it, slot media_slot is the medium's radiance and the others
 // are scaled by the transmittance.
@@ -96,12 +98,12 @@ cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_
                                  int n_light_samples, const float *dfilm, float *g_albedo, double *g_emission,
                                  const void *rays, const void *hits, void *srays, int *stri, float *s_dkd,
                                  float *s_dem, int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
-                                 int *bcount, const float *tcam, cudaStream_t s);
+                                 int *bcount, float *bnrm, const float *tcam, cudaStream_t s);
 cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                                    const int *stri, const float *s_dkd, const float *s_dem, const int *scount,
                                    const void *brays, const void *bhits, const int *btri, const float *b_dkd,
-                                   const float *brgb, const int *bcount, float *g_albedo, double *g_emission,
-                                   cudaStream_t s);
+                                   const float *brgb, const int *bcount, const float *bnrm, float *g_albedo,
+                                   double *g_emission, cudaStream_t s);
 
 // Photon mapping (photon.cu).  trace(rays, n, n_dev, hits, stream) runs the
 // closest-hit traversal of the scene's accelerator.

@@ -124,7 +124,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
                                                float4 *__restrict__ srays, int *__restrict__ starget,
                                                float *__restrict__ srgb, int *__restrict__ scount,
                                                float4 *__restrict__ brays, int *__restrict__ btarget,
-                                               float *__restrict__ brgb, int *__restrict__ bcount) {
+                                               float *__restrict__ brgb, int *__restrict__ bcount,
+                                               float *__restrict__ bnrm) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < A.n;
   int4 hit = make_int4(0x7f800000, -1, -1, 0);
@@ -169,10 +170,9 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
     }
   }
   const V3 shading_n = b.n;
+  const V3 n_view = dot(wo, b.n) >= 0.0f ? b.n : b.n * -1.0f;
 
-  // Light samples (DirectLightingIntegrator::_SampleLights, :158-262).  The
-  // light is chosen uniformly among the area lights (any density gives the
-  // same expectation; a single light -- all configurations -- has pdf 1).
+  // Light samples (DirectLightingIntegrator::_SampleLights, :158-262).
   for (int k = 0; k < nl; ++k) {
     bool want = false;
     V3 val = v3(0, 0, 0), dir = v3(0, 0, 0), dkd = v3(0, 0, 0);
@@ -181,10 +181,11 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
     if (surface && S.n_area_lights > 0) {
       const float uc = rnd(seed, gid, 2 + 3 * k), u0 = rnd(seed, gid, 3 + 3 * k),
                   u1 = rnd(seed, gid, 4 + 3 * k);
-      const int nls = S.n_area_lights;
-      const int li = min((int)(uc * nls), nls - 1);
-      const float lcp = 1.0f / nls;
-      const float tri_u = uc * nls - li;  // the remaining fraction selects the triangle
+      // the light by IrradianceLightsSamplingStrategy at this point, with
+      // the shading normal turned to the viewer (reflection-only BSDFs,
+      // DirectLightingIntegrator.cpp:107-111)
+      float lcp, tri_u;
+      const int li = choose_light(S, uc, h.p, n_view, lcp, tri_u);
       const AreaLight L = S.area_lights[li];
       // BinarySearchCDF over the light's area CDF (MathRoutines.h:191-218)
       int lo = 0, hi = L.tri_count - 1;
@@ -292,6 +293,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
       store_ray(brays, q, h.p, dir, tmin, __int_as_float(0x7f800000));
       btarget[q] = ADJ ? h.g : (int)(slot0 + 1 + nl + S.n_point_lights + k);
       if (ADJ) store_rgb(J.b_dkd, q, dkd);
+      if (bnrm) store_rgb(bnrm, q, n_view);
       brgb[4 * q] = val.x;
       brgb[4 * q + 1] = val.y;
       brgb[4 * q + 2] = val.z;
@@ -318,7 +320,7 @@ __global__ void k_resolve_shadow(const uint8_t *__restrict__ occ, const int *__r
 __global__ void k_resolve_bsdf(SceneDev S, int n_light_samples, const float4 *__restrict__ brays,
                                const int4 *__restrict__ bhits, const int *__restrict__ btarget,
                                const float *__restrict__ brgb, const int *__restrict__ bcount,
-                               float *__restrict__ contrib) {
+                               const float *__restrict__ bnrm, float *__restrict__ contrib) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *bcount) return;
   const int4 hit = bhits[i];
@@ -336,7 +338,7 @@ __global__ void k_resolve_bsdf(SceneDev S, int n_light_samples, const float4 *__
   const float dist = __int_as_float(hit.x) - rb.z;  // ray max_t - min_t
   const float cosl = fabsf(dot(d, ln));
   const float light_pdf = cosl > kEps ? dist * dist / (L.area * cosl) : 0.0f;
-  const float lcp = 1.0f / S.n_area_lights;
+  const float lcp = light_choice_pdf(S, li, v3(ra.x, ra.y, ra.z), load3(bnrm + 3 * (int64_t)i));
   const float bpdf = brgb[4 * i + 3];
   const float w = power_heuristic(n_light_samples, bpdf, n_light_samples, light_pdf * lcp);
   const int64_t t = btarget[i];
@@ -367,7 +369,8 @@ __global__ void k_resolve_shadow_adj(const uint8_t *__restrict__ occ, const int 
 // Adjoint of k_resolve_bsdf (same light density and MIS weight).
 __global__ void k_resolve_bsdf_adj(SceneDev S, int n_light_samples, const float4 *__restrict__ brays,
                                    const int4 *__restrict__ bhits, const int *__restrict__ btri,
-                                   const float *__restrict__ brgb, const int *__restrict__ bcount, AdjointArgs J) {
+                                   const float *__restrict__ brgb, const int *__restrict__ bcount,
+                                   const float *__restrict__ bnrm, AdjointArgs J) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float dem = 0.0f;
   if (i < *bcount) {
@@ -385,7 +388,7 @@ __global__ void k_resolve_bsdf_adj(SceneDev S, int n_light_samples, const float4
         const float dist = __int_as_float(hit.x) - rb.z;
         const float cosl = fabsf(dot(d, ln));
         const float light_pdf = cosl > kEps ? dist * dist / (L.area * cosl) : 0.0f;
-        const float lcp = 1.0f / S.n_area_lights;
+        const float lcp = light_choice_pdf(S, li, v3(ra.x, ra.y, ra.z), load3(bnrm + 3 * (int64_t)i));
         const float w = power_heuristic(n_light_samples, brgb[4 * i + 3], n_light_samples, light_pdf * lcp);
         const V3 le = mul(load3(L.radiance), medium_tr(S.medium, v3(ra.x, ra.y, ra.z), d, rb.z, __int_as_float(hit.x)));
         const V3 dk = mul(load3(J.b_dkd + 3 * (int64_t)i), le) * (S.emission_scale * w);
@@ -627,13 +630,13 @@ cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, i
 cudaError_t launch_shade(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin, int spp,
                          int slots, int n_light_samples, const void *rays, const void *hits, float *contrib,
                          void *srays, int *starget, float *srgb, int *scount, void *brays, int *btarget, float *brgb,
-                         int *bcount, int block, cudaStream_t s) {
+                         int *bcount, float *bnrm, int block, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   if (block != 64) block = 128;
   ShadeArgs A{n, px_begin, spp, slots, n_light_samples, views, n_views, nullptr};
   k_shade<false><<<(unsigned)((n + block - 1) / block), (unsigned)block, 0, s>>>(
       S, A, AdjointArgs{}, (const float4 *)rays, (const int4 *)hits, contrib, (float4 *)srays, starget, srgb, scount,
-      (float4 *)brays, btarget, brgb, bcount);
+      (float4 *)brays, btarget, brgb, bcount, bnrm);
   return cudaGetLastError();
 }
 
@@ -641,40 +644,40 @@ cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_
                                  int n_light_samples, const float *dfilm, float *g_albedo, double *g_emission,
                                  const void *rays, const void *hits, void *srays, int *stri, float *s_dkd,
                                  float *s_dem, int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
-                                 int *bcount, const float *tcam, cudaStream_t s) {
+                                 int *bcount, float *bnrm, const float *tcam, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   ShadeArgs A{n, px_begin, spp, 0, n_light_samples, views, n_views, tcam};
   AdjointArgs J{dfilm, g_albedo, g_emission, s_dkd, s_dem, b_dkd};
   k_shade<true><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, A, J, (const float4 *)rays, (const int4 *)hits,
                                                              nullptr, (float4 *)srays, stri, nullptr, scount,
-                                                             (float4 *)brays, btri, brgb, bcount);
+                                                             (float4 *)brays, btri, brgb, bcount, bnrm);
   return cudaGetLastError();
 }
 
 cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                                    const int *stri, const float *s_dkd, const float *s_dem, const int *scount,
                                    const void *brays, const void *bhits, const int *btri, const float *b_dkd,
-                                   const float *brgb, const int *bcount, float *g_albedo, double *g_emission,
-                                   cudaStream_t s) {
+                                   const float *brgb, const int *bcount, const float *bnrm, float *g_albedo,
+                                   double *g_emission, cudaStream_t s) {
   if (capacity <= 0) return cudaSuccess;
   AdjointArgs J{nullptr, g_albedo, g_emission, const_cast<float *>(s_dkd), const_cast<float *>(s_dem),
                 const_cast<float *>(b_dkd)};
   const unsigned grid = (unsigned)((capacity + 255) / 256);
   k_resolve_shadow_adj<<<grid, 256, 0, s>>>(occ, stri, scount, J);
   k_resolve_bsdf_adj<<<grid, 256, 0, s>>>(S, n_light_samples, (const float4 *)brays, (const int4 *)bhits, btri, brgb,
-                                          bcount, J);
+                                          bcount, bnrm, J);
   return cudaGetLastError();
 }
 
 cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                            const int *starget, const float *srgb, const int *scount, const void *brays,
                            const void *bhits, const int *btarget, const float *brgb, const int *bcount,
-                           float *contrib, cudaStream_t s) {
+                           const float *bnrm, float *contrib, cudaStream_t s) {
   if (capacity <= 0) return cudaSuccess;
   const unsigned grid = (unsigned)((capacity + 255) / 256);
   k_resolve_shadow<<<grid, 256, 0, s>>>(occ, starget, srgb, scount, contrib);
   k_resolve_bsdf<<<grid, 256, 0, s>>>(S, n_light_samples, (const float4 *)brays, (const int4 *)bhits, btarget, brgb,
-                                      bcount, contrib);
+                                      bcount, bnrm, contrib);
   return cudaGetLastError();
 }
 

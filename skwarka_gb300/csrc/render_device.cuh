@@ -463,6 +463,109 @@ __device__ __forceinline__ void store_rgb(float *c, int64_t slot, V3 v) {
 namespace skw {
 namespace {
 
+// ------------------------------------------------------------ light choice --
+// MathRoutines::_SubtendedSolidAngle / SubtendedSolidAngle (Math/
+// MathRoutines.h:321-391): the box's faces that face the point, as two
+// triangles each (Oosterom-Strackee).
+__device__ __forceinline__ float tri_solid_angle(V3 a, V3 b, V3 c) {
+  const float det = dot(a, cross(b, c));
+  const float den = 1.0f + dot(a, b) + dot(a, c) + dot(b, c);
+  if (den > 0.0f) return fabsf(atanf(det / den) * 2.0f);
+  if (den < 0.0f) return 2.0f * (kPi - fabsf(atanf(det / den)));
+  return 2.0f * kPi;
+}
+
+__device__ float box_solid_angle(V3 p, const float lo[3], const float hi[3]) {
+  V3 d[8];
+  for (int i = 0; i < 8; ++i)
+    d[i] = normalized(v3((i & 1) ? hi[0] : lo[0], (i & 2) ? hi[1] : lo[1], (i & 4) ? hi[2] : lo[2]) - p);
+  bool inside = true;
+  float sum = 0.0f;
+  if (p.x < lo[0]) {
+    sum += tri_solid_angle(d[0], d[2], d[6]) + tri_solid_angle(d[0], d[4], d[6]);
+    inside = false;
+  } else if (p.x > hi[0]) {
+    sum += tri_solid_angle(d[1], d[3], d[7]) + tri_solid_angle(d[1], d[5], d[7]);
+    inside = false;
+  }
+  if (p.y < lo[1]) {
+    sum += tri_solid_angle(d[0], d[1], d[5]) + tri_solid_angle(d[0], d[4], d[5]);
+    inside = false;
+  } else if (p.y > hi[1]) {
+    sum += tri_solid_angle(d[2], d[3], d[7]) + tri_solid_angle(d[2], d[6], d[7]);
+    inside = false;
+  }
+  if (p.z < lo[2]) {
+    sum += tri_solid_angle(d[0], d[1], d[3]) + tri_solid_angle(d[0], d[2], d[3]);
+    inside = false;
+  } else if (p.z > hi[2]) {
+    sum += tri_solid_angle(d[4], d[5], d[7]) + tri_solid_angle(d[4], d[6], d[7]);
+    inside = false;
+  }
+  return inside ? 4.0f * kPi : sum;
+}
+
+// IrradianceLightsSamplingStrategy::GetLightsCDF(point, normal) (:57-113)
+// weight of area light `li`: solid angle of its bounds times its intensity
+// times the average (clamped) cosine of the bounds' corners, pi * intensity
+// inside the bounds.
+__device__ float light_weight(const AreaLight &L, V3 p, V3 n) {
+  if (p.x >= L.lo[0] && p.y >= L.lo[1] && p.z >= L.lo[2] && p.x <= L.hi[0] && p.y <= L.hi[1] && p.z <= L.hi[2])
+    return kPi * L.intensity;
+  float avg = 0.0f;
+  for (int j = 0; j < 8; ++j) {
+    const V3 v = v3((j & 1) ? L.lo[0] : L.hi[0], (j & 2) ? L.lo[1] : L.hi[1], (j & 4) ? L.lo[2] : L.hi[2]);
+    avg += fmaxf(0.0f, dot(normalized(v - p), n));
+  }
+  avg *= 0.125f;
+  if (!(avg > 0.0f)) return 0.0f;
+  if (avg < 0.1f) avg = 0.1f;
+  return box_solid_angle(p, L.lo, L.hi) * L.intensity * avg;
+}
+
+// Probability of choosing light `li` at (p, n) among all area lights
+// (_Weights_To_CDF: equal probabilities when every weight is 0).
+__device__ float light_choice_pdf(const SceneDev &S, int li, V3 p, V3 n) {
+  const int nl = S.n_area_lights;
+  if (nl <= 1) return 1.0f;
+  float tot = 0.0f, mine = 0.0f;
+  for (int i = 0; i < nl; ++i) {
+    const float w = light_weight(S.area_lights[i], p, n);
+    tot += w;
+    if (i == li) mine = w;
+  }
+  return tot > 0.0f ? mine / tot : 1.0f / nl;
+}
+
+// Chooses a light with u (BinarySearchCDF over the normalised cumulative
+// weights); returns its index, its probability and the remainder of u
+// rescaled to [0, 1) for the triangle choice.
+__device__ int choose_light(const SceneDev &S, float u, V3 p, V3 n, float &pdf, float &u_rest) {
+  const int nl = S.n_area_lights;
+  if (nl <= 1) {
+    pdf = 1.0f;
+    u_rest = u;
+    return 0;
+  }
+  float tot = 0.0f;
+  for (int i = 0; i < nl; ++i) tot += light_weight(S.area_lights[i], p, n);
+  const bool uniform = !(tot > 0.0f);
+  float cum = 0.0f, prev = 0.0f;
+  int li = nl - 1;
+  for (int i = 0; i < nl; ++i) {
+    const float w = uniform ? 1.0f / nl : light_weight(S.area_lights[i], p, n) / tot;
+    prev = cum;
+    cum += w;
+    if (u < cum || i == nl - 1) {
+      li = i;
+      pdf = w;
+      break;
+    }
+  }
+  u_rest = pdf > 0.0f ? fminf((u - prev) / pdf, 0.99999994f) : 0.0f;
+  return li;
+}
+
 // BBox3D::Intersect (Math/BBox3D.h:150-171) of the ray segment [t0, t1] with
 // the medium's box; false if they miss.
 __device__ __forceinline__ bool medium_segment(const MediumDev &M, V3 o, V3 d, float &t0, float &t1) {

@@ -31,6 +31,12 @@ struct AreaLight {
   int32_t tri_begin;   // range in light_tri / light_cdf
   int32_t tri_count;
   int32_t pad;
+  // IrradianceLightsSamplingStrategy (LightsSamplingStrategies/
+  // IrradianceLightsSamplingStrategy.cpp:19-31): the mesh bounds and
+  // luminance(power) / (pi * bounds area)
+  float lo[3], hi[3];
+  float intensity;
+  float pad2;
 };
 
 struct PointLightDev {

@@ -208,6 +208,27 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
     if (light) {
       L.tri_count = (int32_t)areas.size();
       L.area = (float)area_sum;
+      // mesh bounds (TriangleMesh::GetBounds: over the triangles' vertices)
+      float blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      for (int64_t t = 0; t < m.n_triangles; ++t)
+        for (int k = 0; k < 3; ++k) {
+          const int32_t vi = m.triangles[3 * t + k];
+          if (vi < 0 || (int64_t)vi >= m.n_vertices) continue;
+          for (int c = 0; c < 3; ++c) {
+            blo[c] = std::min(blo[c], m.vertices[3 * vi + c]);
+            bhi[c] = std::max(bhi[c], m.vertices[3 * vi + c]);
+          }
+        }
+      const double bx = std::fabs((double)bhi[0] - blo[0]), by = std::fabs((double)bhi[1] - blo[1]),
+                   bz = std::fabs((double)bhi[2] - blo[2]);
+      const double barea = 2.0 * (bx * by + bx * bz + by * bz);
+      const double lum = 0.05316285 * L.radiance[0] + 0.58515348 * L.radiance[1] + 0.36168367 * L.radiance[2];
+      for (int c = 0; c < 3; ++c) {
+        L.lo[c] = blo[c];
+        L.hi[c] = bhi[c];
+      }
+      // luminance(Power()) / (pi * area) with Power() = pi * A * L
+      L.intensity = barea > 0.0 ? (float)(area_sum * lum / barea) : 0.0f;
       for (double a : areas) light_cdf.push_back(area_sum > 0 ? (float)(a / area_sum) : 1.0f);
       if (L.tri_count > 0 && area_sum > 0) {
         prim_light[(size_t)p] = (int32_t)lights.size();
@@ -335,7 +356,7 @@ struct Plan {
 // Device buffers of one workspace (one pass in flight).
 struct Workspace {
   void *rays = nullptr, *hits = nullptr, *srays = nullptr, *brays = nullptr, *bhits = nullptr;
-  float *contrib = nullptr, *srgb = nullptr, *brgb = nullptr;
+  float *contrib = nullptr, *srgb = nullptr, *brgb = nullptr, *bnrm = nullptr;
   int *starget = nullptr, *btarget = nullptr, *counts = nullptr;
   uint8_t *occ = nullptr;
   // medium
@@ -352,7 +373,8 @@ size_t workspace_bytes(const Plan &P) {
   const int64_t cm = std::max<int64_t>(P.cap_media, 1);
   const size_t media = P.media ? al256(cs * 12) + al256(cm * 32) + al256(cm * 4) + 2 * al256(cm * 12) + al256(cm) : 0;
   return al256(cs * 32) + al256(cs * 16) + al256(cs * P.slots * 12) + al256(sh * 32) + al256(sh * 4) +
-         al256(sh * 12) + al256(sh) + al256(bs * 32) + al256(bs * 4) + al256(bs * 16) + al256(bs * 16) + 256 + media;
+         al256(sh * 12) + al256(sh) + al256(bs * 32) + al256(bs * 4) + al256(bs * 16) + al256(bs * 16) + 256 + media +
+         al256(bs * 12);
 }
 
 void workspace_carve(const Plan &P, char *base, Workspace *W) {
@@ -375,6 +397,7 @@ void workspace_carve(const Plan &P, char *base, Workspace *W) {
   W->brgb = (float *)take(al256(bs * 16));
   W->bhits = take(al256(bs * 16));
   W->counts = (int *)take(256);  // [0] shadow queue length, [1] BSDF queue length, [2] media queue length
+  W->bnrm = (float *)take(al256(bs * 12));
   if (P.media) {
     const int64_t cm = std::max<int64_t>(P.cap_media, 1);
     W->tcam = (float *)take(al256(cs * 12));
@@ -476,8 +499,8 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
     return e;
   if (P.media && (e = record_media(s, P, W, d_views, px0, n, false, nullptr, nullptr, st)) != cudaSuccess) return e;
   if ((e = skw::launch_shade(s->dev, d_views, nv, n, px0, P.spp, P.slots, P.nl, W.rays, W.hits, W.contrib, W.srays,
-                             W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb, W.counts + 1, P.cfg.shade_block,
-                             st)) != cudaSuccess)
+                             W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb, W.counts + 1, W.bnrm,
+                             P.cfg.shade_block, st)) != cudaSuccess)
     return e;
   const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
   if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts, a->scene_abs,
@@ -487,7 +510,7 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
                                             a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas)) != cudaSuccess)
     return e;
   return skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
-                             W.bhits, W.btarget, W.brgb, W.counts + 1, W.contrib, st);
+                             W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st);
 }
 
 // One pass: direct lighting, then the film.
@@ -888,7 +911,7 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
     if (P.media && (e = record_media(s, P, W, d_view, px0, n, true, d_film, g_emission, st)) != cudaSuccess) break;
     if ((e = skw::launch_shade_adjoint(s->dev, d_view, 1, n, px0, P.spp, P.nl, d_film, g_albedo, g_emission, W.rays,
                                        W.hits, W.srays, W.starget, s_dkd, s_dem, W.counts, W.brays, W.btarget, b_dkd,
-                                       W.brgb, W.counts + 1, P.media ? W.tcam : nullptr, st)) != cudaSuccess)
+                                       W.brgb, W.counts + 1, W.bnrm, P.media ? W.tcam : nullptr, st)) != cudaSuccess)
       break;
     const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
     if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts,
@@ -898,7 +921,7 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
                                               a->scene_abs, nullptr, W.bhits, a->d_status, st)) != cudaSuccess)
       break;
     if ((e = skw::launch_resolve_adjoint(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, s_dkd, s_dem,
-                                         W.counts, W.brays, W.bhits, W.btarget, b_dkd, W.brgb, W.counts + 1,
+                                         W.counts, W.brays, W.bhits, W.btarget, b_dkd, W.brgb, W.counts + 1, W.bnrm,
                                          g_albedo, g_emission, st)) != cudaSuccess)
       break;
     launches += 7;

@@ -106,6 +106,14 @@ def measured_golden():
     np.savez_compressed(OUT / "measured_planes.npz", **out)
 
 
+def two_lights_golden():
+    """The reference's render of the box with two area lights, 32 x 32,
+    16x16 spp (its IrradianceLightsSamplingStrategy chooses the light)."""
+    p, m, c = sf.two_light_scene()
+    img, _ = Reference().render_direct(p, m, [], c, 16, 16)
+    np.savez_compressed(OUT / "two_lights_32.npz", ref=img)
+
+
 def medium_golden():
     """The reference's direct-lighting renders with a homogeneous medium
     (scene_fixtures.medium_cases) at 32 x 32, 16x16 spp."""
@@ -136,6 +144,10 @@ def photon_golden():
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "measured":
     measured_golden()
     print("measured golden written")
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "lights":
+    two_lights_golden()
+    print("two-light golden written")
 
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "medium":
     medium_golden()

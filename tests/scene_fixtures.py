@@ -253,3 +253,18 @@ def measured_plane_scenes(measured):
         prims, mats, lights, cam = base[light + "_matte"]
         out[light + "_measured"] = (prims, [m] + mats[1:], lights, cam)
     return out
+
+
+def two_light_scene():
+    """The direct-lighting box with a second, smaller and brighter quad light
+    on the -x wall facing +x: (prims, materials, camera 32 x 32), for the
+    light choice among several area lights."""
+    from skwarka_gb300.accel import TriangleMesh
+    from skwarka_gb300.render import RenderPrimitive
+    prims, mats, cam = scenes.direct_lighting_box()
+    lv = np.array([[-0.98, -0.2, -0.1], [-0.98, 0.2, -0.1], [-0.98, 0.2, 0.1], [-0.98, -0.2, 0.1]], np.float32)
+    lt = np.array([[0, 1, 2], [0, 2, 3]], np.int32)
+    a, b, c = lv[lt[0]]
+    assert np.cross(b - a, c - a)[0] > 0  # emits towards +x
+    prims = prims + [RenderPrimitive(TriangleMesh(lv, lt), 2, emission=(30.0, 20.0, 10.0))]
+    return prims, mats, cam(32, 32)

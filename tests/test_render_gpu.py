@@ -127,10 +127,12 @@ def test_render_is_deterministic(gpu):
 def test_sphere_area_lights_known_answer(gpu):
     """DirectLightingIntegrator.test.h:104-135 analogue: two spherical area
     lights (radiance 10 and 20) seen from a Lambertian point; the GPU estimate
-    at 64x64 samples per pixel agrees with the closed form within 2 %."""
+    at 128x128 samples per pixel agrees with the closed form of ideal spheres
+    within 2 % (the tessellated lights subtend about 1 % less; the estimate's
+    own noise is about 0.5 %)."""
     import scene_fixtures as sf
     prims, mats, cam, want = sf.sphere_area_lights_case()
-    img = RenderScene(prims, mats).render_direct(cam, 64, 64, seed=7).cpu().numpy()
+    img = RenderScene(prims, mats).render_direct(cam, 128, 128, seed=7).cpu().numpy()
     print(f"[sphere lights] gpu {img.mean():.5f} closed form {want:.5f}")
     assert abs(img.mean() / want - 1.0) <= 0.02
 
@@ -160,3 +162,21 @@ def test_measured_brdf_plane_parity(gpu, name):
     m_ref, m_gpu = float((ref @ LUM).mean()), float((img @ LUM).mean())
     print(f"[{name}] mean luminance ref {m_ref:.5f} gpu {m_gpu:.5f}")
     assert abs(m_gpu / m_ref - 1.0) <= 0.02
+
+
+def test_two_area_lights_parity(gpu):
+    """Two area lights of different size and radiance: the light is chosen
+    per shading point by the reference's irradiance strategy (bounds' solid
+    angle x intensity x average cosine); mean luminance within 2 % and 8x8
+    blocks within 5 % of the reference's 16x16-spp render."""
+    import scene_fixtures as sf
+    p, m, c = sf.two_light_scene()
+    ref = np.load(GOLD / "two_lights_32.npz")["ref"]
+    img = RenderScene(p, m).render_direct(c, 32, 32, seed=8).cpu().numpy()
+    m_ref, m_gpu = float((ref @ LUM).mean()), float((img @ LUM).mean())
+    b = lambda im: (im @ LUM).reshape(4, 8, 4, 8).mean(axis=(1, 3))  # noqa: E731
+    rb = b(ref)
+    rel = np.abs(b(img) - rb) / np.maximum(rb, 0.25 * rb.mean())
+    print(f"[two lights] mean luminance ref {m_ref:.5f} gpu {m_gpu:.5f}; worst block {rel.max():.4f}")
+    assert abs(m_gpu / m_ref - 1.0) <= 0.02
+    assert rel.max() <= 0.05
