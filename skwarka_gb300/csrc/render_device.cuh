@@ -551,18 +551,31 @@ __device__ int choose_light(const SceneDev &S, float u, V3 p, V3 n, float &pdf, 
   for (int i = 0; i < nl; ++i) tot += light_weight(S.area_lights[i], p, n);
   const bool uniform = !(tot > 0.0f);
   float cum = 0.0f, prev = 0.0f;
-  int li = nl - 1;
+  int li = -1, last = 0;
+  float last_w = 0.0f, last_prev = 0.0f;
+  pdf = 0.0f;
   for (int i = 0; i < nl; ++i) {
     const float w = uniform ? 1.0f / nl : light_weight(S.area_lights[i], p, n) / tot;
-    prev = cum;
+    const float c0 = cum;
     cum += w;
-    if (u < cum || i == nl - 1) {
-      li = i;
-      pdf = w;
-      break;
+    if (w > 0.0f) {
+      last = i;
+      last_w = w;
+      last_prev = c0;
+      if (u < cum) {
+        li = i;
+        pdf = w;
+        prev = c0;
+        break;
+      }
     }
   }
-  u_rest = pdf > 0.0f ? fminf((u - prev) / pdf, 0.99999994f) : 0.0f;
+  if (li < 0) {  // u beyond the float sum of the weights: the last light that can be chosen
+    li = last;
+    pdf = last_w;
+    prev = last_prev;
+  }
+  u_rest = pdf > 0.0f ? fminf(fmaxf((u - prev) / pdf, 0.0f), 0.99999994f) : 0.0f;
   return li;
 }
 
