@@ -460,7 +460,7 @@ int plan_make(skw_scene *s, const skw_camera *cams, int n_views, const skw_rende
   P->cap_media = P->media ? P->cap_samples * s->dev.medium.max_steps : 0;
   P->cap_shadow = P->cap_samples * (P->nl + P->npl);
   P->cap_bsdf = P->cap_samples * P->nl;
-  if (P->cap_shadow > INT32_MAX || P->cap_samples > INT32_MAX || P->cap_samples * P->slots * 3 > ((int64_t)1 << 40))
+  if (P->cap_shadow > INT32_MAX / 2 || P->cap_samples > INT32_MAX / 2 || P->cap_samples * P->slots * 3 > ((int64_t)1 << 40))
     return fail(ctx, SKW_ERR_ARG, "render pass too large");
   return SKW_OK;
 }
@@ -809,7 +809,8 @@ int skw_render_batch_autotune(skw_render_batch *b, float *scratch, void *stream,
     }
   };
   const int64_t total = b->plan.n_px_total * b->plan.spp;
-  for (int64_t q : {(int64_t)1 << 18, (int64_t)1 << 19, (int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22}) {
+  for (int64_t q : {(int64_t)1 << 18, (int64_t)1 << 19, (int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22,
+                    (int64_t)1 << 23, (int64_t)1 << 24, (int64_t)1 << 25}) {
     if (q == best.samples_per_pass || q > 2 * total) continue;
     PassConfig c = best;
     c.samples_per_pass = q;

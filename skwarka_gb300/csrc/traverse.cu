@@ -48,7 +48,7 @@ constexpr double kDblEps = 2.220446049250313e-16;
 #define SKW_TRAV_BLOCK 128
 #endif
 #ifndef SKW_TRAV_MINB
-#define SKW_TRAV_MINB 7
+#define SKW_TRAV_MINB 8
 #endif
 
 enum : int { kMiss = 0, kHit = 1, kAmbiguous = 2 };
@@ -237,16 +237,64 @@ __device__ __forceinline__ bool node_visit(const float4 na, const float4 nb, con
 // memory as three word arrays indexed [entry][thread] (so lanes never
 // conflict on a bank), deeper entries in local memory.  An entry holds a
 // node's words 6-7 and its widened entry distance.
+#ifndef SKW_TRAV_STACK8
+#define SKW_TRAV_STACK8 0
+#endif
+
 template <int CAP>
 struct Stack {
   static constexpr int SCAP = CAP < SKW_TRAV_SCAP ? CAP : SKW_TRAV_SCAP;
+#if SKW_TRAV_STACK8
+  // Entries are (node index, widened entry distance); a popped node's words
+  // are read back from the tree (a recent, L1-resident line).
+  uint32_t (*sa)[SKW_TRAV_BLOCK];
+  float (*slo)[SKW_TRAV_BLOCK];
+  uint2 ovf[CAP - SCAP > 0 ? CAP - SCAP : 1];
+  const float4 *nodes;
+  int sp;
+
+  __device__ __forceinline__ void push(uint32_t, uint32_t, float lo, uint32_t slot) {
+    if (sp < SCAP) {
+      sa[sp][threadIdx.x] = slot;
+      slo[sp][threadIdx.x] = lo;
+    } else {
+      ovf[sp - SCAP] = make_uint2(slot, __float_as_uint(lo));
+    }
+    ++sp;
+  }
+  __device__ __forceinline__ bool pop(float tcull, uint32_t &a, uint32_t &b) {
+    float lo;
+    return pop(tcull, a, b, lo);
+  }
+  __device__ __forceinline__ bool pop(float tcull, uint32_t &a, uint32_t &b, float &lo) {
+    while (sp > 0) {
+      --sp;
+      uint32_t slot;
+      if (sp < SCAP) {
+        lo = slo[sp][threadIdx.x];
+        slot = sa[sp][threadIdx.x];
+      } else {
+        const uint2 e = ovf[sp - SCAP];
+        slot = e.x;
+        lo = __uint_as_float(e.y);
+      }
+      if (!(lo > tcull)) {
+        const float4 nb = __ldg(nodes + 2 * slot + 1);
+        a = __float_as_uint(nb.z);
+        b = __float_as_uint(nb.w);
+        return true;
+      }
+    }
+    return false;
+  }
+#else
   uint32_t (*sa)[SKW_TRAV_BLOCK];
   uint32_t (*sb)[SKW_TRAV_BLOCK];
   float (*slo)[SKW_TRAV_BLOCK];
   uint4 ovf[CAP - SCAP > 0 ? CAP - SCAP : 1];
   int sp;
 
-  __device__ __forceinline__ void push(uint32_t a, uint32_t b, float lo) {
+  __device__ __forceinline__ void push(uint32_t a, uint32_t b, float lo, uint32_t) {
     if (sp < SCAP) {
       sa[sp][threadIdx.x] = a;
       sb[sp][threadIdx.x] = b;
@@ -279,6 +327,7 @@ struct Stack {
     }
     return false;
   }
+#endif
 };
 
 // Expands internal nodes until (cur_a, cur_b) is a leaf; false when the
@@ -330,8 +379,8 @@ __device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const 
       atomicOr(status, 1u);
       return false;
     }
-    if (pass[2] && first != 2) st.push(wa[2], wb[2], lo[2]);
-    if (pass[1] && first != 1) st.push(wa[1], wb[1], lo[1]);
+    if (pass[2] && first != 2) st.push(wa[2], wb[2], lo[2], slot[2]);
+    if (pass[1] && first != 1) st.push(wa[1], wb[1], lo[1], slot[1]);
     if (first < 0) {
       if (!st.pop(tcull, cur_a, cur_b)) return false;
       continue;
@@ -382,8 +431,8 @@ __device__ __forceinline__ bool step_internal(const float4 *__restrict__ nodes, 
     atomicOr(status, 1u);
     return false;
   }
-  if (pass[2] && first != 2) st.push(wa[2], wb[2], lo[2]);
-  if (pass[1] && first != 1) st.push(wa[1], wb[1], lo[1]);
+  if (pass[2] && first != 2) st.push(wa[2], wb[2], lo[2], slot[2]);
+  if (pass[1] && first != 1) st.push(wa[1], wb[1], lo[1], slot[1]);
   if (first < 0) return st.pop(tcull, cur_a, cur_b, cur_lo);
   cur_a = first == 0 ? wa[0] : (first == 1 ? wa[1] : wa[2]);
   cur_b = first == 0 ? wb[0] : (first == 1 ? wb[1] : wb[2]);
@@ -432,12 +481,16 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
   if (n_dev) n = min(n, *n_dev);  // a queue whose length lives on the device
   constexpr int SCAP = Stack<CAP>::SCAP;
   __shared__ uint32_t s_a[SCAP][SKW_TRAV_BLOCK];
-  __shared__ uint32_t s_b[SCAP][SKW_TRAV_BLOCK];
   __shared__ float s_lo[SCAP][SKW_TRAV_BLOCK];
   Stack<CAP> st;
   st.sa = s_a;
-  st.sb = s_b;
   st.slo = s_lo;
+#if SKW_TRAV_STACK8
+  st.nodes = nodes;
+#else
+  __shared__ uint32_t s_b[SCAP][SKW_TRAV_BLOCK];
+  st.sb = s_b;
+#endif
   st.sp = 0;
 
   const unsigned lane = threadIdx.x & 31u;
