@@ -129,6 +129,24 @@ def log(msg: str) -> None:
     print(f"[bench {time.perf_counter() - _T0:7.1f}s] {msg}", file=sys.stderr, flush=True)
 
 
+def reduce_max(value: float, world: int, device="cpu") -> float:
+    """The maximum of a per-rank scalar over all ranks (the slowest rank's
+    time); the identity with one rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_ray_seed(rank: int) -> int:
+    """Each rank traces its own ray batch (weak scaling: rays are independent
+    units, no data-path collective)."""
+    return 7 + 1000 * rank
+
+
 def load_traffic(kind: str, rays: int):
     """DRAM bytes per launch from the committed ncu summary, scaled to `rays`."""
     p = ROOT / "profiles" / "traffic.json"
@@ -483,7 +501,7 @@ def main():
     log("building the ray-query scene")
     meshes = scenes.ray_query_scene(args.subdiv, args.nrandom, seed=3)
     lo, hi = scenes.scene_bounds(meshes)
-    rays_np = scenes.uniform_rays(args.rays, lo, hi, seed=7 + 1000 * rank)
+    rays_np = scenes.uniform_rays(args.rays, lo, hi, seed=rank_ray_seed(rank))
     ctx = Context(local)
     acc = TriangleAccelerator([Primitive(TriangleMesh(v, t)) for v, t in meshes], ctx)
     rays = torch.from_numpy(rays_np).to(dev)
@@ -518,10 +536,7 @@ def main():
         wall = time.perf_counter() - wall0
     launches = ctx.launch_count() - launches0
     kern_ms = [s.elapsed_time(e) for s, e in evs]
-    total_ms = torch.tensor([sum(kern_ms)], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(total_ms, op=dist.ReduceOp.MAX)
-    total_s = float(total_ms.item()) / 1e3
+    total_s = reduce_max(sum(kern_ms), world, dev) / 1e3
     value = args.rays * args.steps * world / total_s / 1e6
 
     log("closest-hit timed; end-to-end")
@@ -536,10 +551,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         _lib.check(lib.skw_intersect_host(acc.handle, hrays.data_ptr(), args.rays, hhits.data_ptr()), ctx.handle)
-    e2e_s = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(e2e_s, op=dist.ReduceOp.MAX)
-    e2e = args.rays * e2e_steps * world / float(e2e_s.item()) / 1e6
+    e2e_s = reduce_max(time.perf_counter() - t0, world, dev)
+    e2e = args.rays * e2e_steps * world / e2e_s / 1e6
 
     log("any-hit")
     # Any-hit throughput (shadow rays, tmax ~ U[0, 2]) for the record.
