@@ -48,7 +48,7 @@ constexpr double kDblEps = 2.220446049250313e-16;
 #define SKW_TRAV_BLOCK 128
 #endif
 #ifndef SKW_TRAV_MINB
-#define SKW_TRAV_MINB 8
+#define SKW_TRAV_MINB 10
 #endif
 
 enum : int { kMiss = 0, kHit = 1, kAmbiguous = 2 };
@@ -60,6 +60,16 @@ struct RayF {
 // Rays and results stream through once: with SKW_TRAV_STREAMING they are
 // loaded and stored with the evict-first policy so that they do not push the
 // tree out of L2.
+// Measured slower (shared-memory latency on every triangle test outweighs
+// the registers it frees): off by default.
+#ifndef SKW_TRAV_RAYSMEM
+#define SKW_TRAV_RAYSMEM 0
+#endif
+// Preferred shared-memory carveout in percent (cudaFuncAttribute
+// PreferredSharedMemoryCarveout); negative leaves the driver's choice.
+#ifndef SKW_TRAV_CARVEOUT
+#define SKW_TRAV_CARVEOUT -1
+#endif
 #ifndef SKW_TRAV_STREAMING
 #define SKW_TRAV_STREAMING 1
 #endif
@@ -177,12 +187,17 @@ __device__ __forceinline__ void load_tri(const float4 *__restrict__ tris, uint32
 // value for every node of the scene; the reference's double result is within
 // a far smaller distance of the exact one.  The near plane of each axis is
 // selected by the sign of 1/d, which is the reference's "swap if
-// tNear > tFar" for every non-NaN slab.
+// tNear > tFar" for every non-NaN slab.  Together with tmin, tmax and the
+// near-child side of each axis this is all the node walk needs, so the
+// ray's origin and direction can stay out of registers while it runs.
 struct SlabRay {
   float ix, iy, iz;  // 1/d
   float nx, ny, nz;  // near-plane offsets: -o/d - w
   float fx, fy, fz;  // far-plane offsets:  -o/d + w
-  bool sx, sy, sz;   // 1/d < 0: the near plane is the box maximum
+  float tmin, tmax;
+  // bits 0-2: !(d[axis] > 0), the reference pops the right child first;
+  // bits 3-5: 1/d[axis] < 0, the near plane is the box maximum
+  uint32_t bits;
 };
 
 __device__ __forceinline__ SlabRay make_slab_ray(const RayF &r, float scene_abs) {
@@ -201,9 +216,10 @@ __device__ __forceinline__ SlabRay make_slab_ray(const RayF &r, float scene_abs)
   s.fx = ox + wx;
   s.fy = oy + wy;
   s.fz = oz + wz;
-  s.sx = signbit(s.ix);
-  s.sy = signbit(s.iy);
-  s.sz = signbit(s.iz);
+  s.tmin = r.tmin;
+  s.tmax = r.tmax;
+  s.bits = (r.dx > 0.0f ? 0u : 1u) | (r.dy > 0.0f ? 0u : 2u) | (r.dz > 0.0f ? 0u : 4u) |
+           (signbit(s.ix) ? 8u : 0u) | (signbit(s.iy) ? 16u : 0u) | (signbit(s.iz) ? 32u : 0u);
   return s;
 }
 
@@ -212,12 +228,13 @@ __device__ __forceinline__ SlabRay make_slab_ray(const RayF &r, float scene_abs)
 // entry distance max(tnear_x, tnear_y, tnear_z, tmin), all that a later
 // re-test against a smaller tmax needs.  fmaxf/fminf drop NaN operands
 // (0 * inf slabs), as the reference's comparisons are all false on NaN.
-__device__ __forceinline__ bool node_visit(const float4 na, const float4 nb, const SlabRay &s, float tmin,
-                                           float tcull, float &lo) {
-  const float tn0 = fmaf(s.sx ? na.w : na.x, s.ix, s.nx), tf0 = fmaf(s.sx ? na.x : na.w, s.ix, s.fx);
-  const float tn1 = fmaf(s.sy ? nb.x : na.y, s.iy, s.ny), tf1 = fmaf(s.sy ? na.y : nb.x, s.iy, s.fy);
-  const float tn2 = fmaf(s.sz ? nb.y : na.z, s.iz, s.nz), tf2 = fmaf(s.sz ? na.z : nb.y, s.iz, s.fz);
-  lo = fmaxf(fmaxf(tn0, tn1), fmaxf(tn2, tmin));
+__device__ __forceinline__ bool node_visit(const float4 na, const float4 nb, const SlabRay &s, float tcull,
+                                           float &lo) {
+  const bool sx = s.bits & 8u, sy = s.bits & 16u, sz = s.bits & 32u;
+  const float tn0 = fmaf(sx ? na.w : na.x, s.ix, s.nx), tf0 = fmaf(sx ? na.x : na.w, s.ix, s.fx);
+  const float tn1 = fmaf(sy ? nb.x : na.y, s.iy, s.ny), tf1 = fmaf(sy ? na.y : nb.x, s.iy, s.fy);
+  const float tn2 = fmaf(sz ? nb.y : na.z, s.iz, s.nz), tf2 = fmaf(sz ? na.z : nb.y, s.iz, s.fz);
+  lo = fmaxf(fmaxf(tn0, tn1), fmaxf(tn2, s.tmin));
   const float hi = fminf(fminf(tf0, tf1), fminf(tf2, tcull));
   return !(lo > hi);
 }
@@ -226,7 +243,12 @@ __device__ __forceinline__ bool node_visit(const float4 na, const float4 nb, con
 #define SKW_TRAV_SCAP 8
 #endif
 #ifndef SKW_TRAV_REFILL
-#define SKW_TRAV_REFILL 16
+#define SKW_TRAV_REFILL 8
+#endif
+// A walk round ends once at most SKW_TRAV_LAG walking lanes still have no
+// leaf; those keep their place and go on walking in the next round.
+#ifndef SKW_TRAV_LAG
+#define SKW_TRAV_LAG 12
 #endif
 // Postponed leaves (speculative node steps), see k_trace.
 #ifndef SKW_TRAV_POSTPONE
@@ -343,14 +365,13 @@ struct Stack {
 // pop against the tmax of that moment -- the only part of the reference's
 // pop-time test that can change after the push, since tmax only shrinks.
 template <int CAP>
-__device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const RayF &r, const SlabRay &s,
+__device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const SlabRay &s,
                                         float tcull, Stack<CAP> &st, uint32_t &cur_a, uint32_t &cur_b,
                                         unsigned *status) {
   while ((cur_b & 3u) != 0u) {
     const uint32_t type = cur_b & 3u, mask = (cur_b >> 2) & 7u;
     const uint32_t sL = cur_a, sM = cur_a + (mask & 1u), sR = sM + ((mask >> 1) & 1u);
-    const float dax = type == 1u ? r.dx : (type == 2u ? r.dy : r.dz);
-    const bool near_right = !(dax > 0.0f);  // the reference pops left first when d[axis] > 0
+    const bool near_right = (s.bits >> (type - 1u)) & 1u;  // the reference pops left first when d[axis] > 0
     uint32_t slot[3], present[3];
     slot[0] = near_right ? sR : sL;
     present[0] = near_right ? (mask & 4u) : (mask & 1u);
@@ -369,7 +390,7 @@ __device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const 
       if (present[k]) {
         const float4 ca = __ldg(nodes + 2 * slot[k]);
         const float4 cb = __ldg(nodes + 2 * slot[k] + 1);
-        pass[k] = node_visit(ca, cb, s, r.tmin, tcull, lo[k]);
+        pass[k] = node_visit(ca, cb, s, tcull, lo[k]);
         wa[k] = __float_as_uint(cb.z);
         wb[k] = __float_as_uint(cb.w);
       }
@@ -396,13 +417,12 @@ __device__ __forceinline__ bool descend(const float4 *__restrict__ nodes, const 
 // current and pushes the others; pops when none passes.  cur_lo tracks the
 // current node's widened entry distance.  False when the stack runs out.
 template <int CAP>
-__device__ __forceinline__ bool step_internal(const float4 *__restrict__ nodes, const RayF &r, const SlabRay &s,
+__device__ __forceinline__ bool step_internal(const float4 *__restrict__ nodes, const SlabRay &s,
                                               float tcull, Stack<CAP> &st, uint32_t &cur_a, uint32_t &cur_b,
                                               float &cur_lo, unsigned *status) {
   const uint32_t type = cur_b & 3u, mask = (cur_b >> 2) & 7u;
   const uint32_t sL = cur_a, sM = cur_a + (mask & 1u), sR = sM + ((mask >> 1) & 1u);
-  const float dax = type == 1u ? r.dx : (type == 2u ? r.dy : r.dz);
-  const bool near_right = !(dax > 0.0f);
+  const bool near_right = (s.bits >> (type - 1u)) & 1u;
   uint32_t slot[3], present[3];
   slot[0] = near_right ? sR : sL;
   present[0] = near_right ? (mask & 4u) : (mask & 1u);
@@ -421,7 +441,7 @@ __device__ __forceinline__ bool step_internal(const float4 *__restrict__ nodes, 
     if (present[k]) {
       const float4 ca = __ldg(nodes + 2 * slot[k]);
       const float4 cb = __ldg(nodes + 2 * slot[k] + 1);
-      pass[k] = node_visit(ca, cb, s, r.tmin, tcull, lo[k]);
+      pass[k] = node_visit(ca, cb, s, tcull, lo[k]);
       wa[k] = __float_as_uint(cb.z);
       wb[k] = __float_as_uint(cb.w);
     }
@@ -501,7 +521,21 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
   const int end = warp < groups ? ((groups - warp + n_warps - 1) / n_warps) << 5 : 0;
 
   int ray_i = -1;
-  RayF r{};
+  // The ray itself is read only by the triangle tests: with
+  // SKW_TRAV_RAYSMEM it waits in shared memory (one word array per field,
+  // [field][thread], conflict-free) instead of holding eight registers
+  // through the node walk.
+#if SKW_TRAV_RAYSMEM
+  __shared__ float s_ray[8][SKW_TRAV_BLOCK];
+#define SKW_RAY()                                                                                          \
+  RayF {                                                                                                   \
+    s_ray[0][threadIdx.x], s_ray[1][threadIdx.x], s_ray[2][threadIdx.x], s_ray[3][threadIdx.x],            \
+        s_ray[4][threadIdx.x], s_ray[5][threadIdx.x], s_ray[6][threadIdx.x], s_ray[7][threadIdx.x]        \
+  }
+#else
+  RayF r_reg{};
+#define SKW_RAY() r_reg
+#endif
   SlabRay s{};
   uint32_t cur_a = 0, cur_b = 0;
   int best_slot = -1;
@@ -521,17 +555,29 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
       const int idx = ((warp + (mine >> 5) * n_warps) << 5) + (mine & 31);
       if (ray_i < 0 && mine < end && idx < n) {
         ray_i = idx;
-        r = load_ray(rays, ray_i);
-        s = make_slab_ray(r, scene_abs);
+        const RayF rl = load_ray(rays, ray_i);
+#if SKW_TRAV_RAYSMEM
+        s_ray[0][threadIdx.x] = rl.ox;
+        s_ray[1][threadIdx.x] = rl.oy;
+        s_ray[2][threadIdx.x] = rl.oz;
+        s_ray[3][threadIdx.x] = rl.dx;
+        s_ray[4][threadIdx.x] = rl.dy;
+        s_ray[5][threadIdx.x] = rl.dz;
+        s_ray[6][threadIdx.x] = rl.tmin;
+        s_ray[7][threadIdx.x] = rl.tmax;
+#else
+        r_reg = rl;
+#endif
+        s = make_slab_ray(rl, scene_abs);
         best_slot = -1;
-        lo_t = hi_t = r.tmax;
+        lo_t = hi_t = rl.tmax;
         flags = 8u;
         st.sp = 0;
         const float4 na = __ldg(nodes), nb = __ldg(nodes + 1);
         float lo;
         cur_a = __float_as_uint(nb.z);
         cur_b = __float_as_uint(nb.w);
-        if (!node_visit(na, nb, s, r.tmin, r.tmax, lo)) {  // root culled: a miss
+        if (!node_visit(na, nb, s, rl.tmax, lo)) {  // root culled: a miss
           store_result<CLOSEST>(out, out_index, ray_i, make_int4(0x7f800000, -1, -1, 0), false);
           ray_i = -1;
         }
@@ -542,37 +588,61 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
 #endif
       }
     }
-    if (__ballot_sync(0xffffffffu, ray_i >= 0) == 0u) {
+    const unsigned busy = __ballot_sync(0xffffffffu, ray_i >= 0);
+    if (busy == 0u) {
       if (next >= end) break;
       continue;
     }
     if (ray_i < 0) continue;
+    // Independent thread scheduling does not promise that the busy lanes run
+    // the rest of the iteration as one group; without an explicit sync they
+    // were measured to split into 2-3 groups that each walked on their own.
+    __syncwarp(busy);
 
 #if SKW_TRAV_POSTPONE
-    // Node steps continue past a lane's first leaf (postponed) until every
-    // lane of the warp holds one or the lane reaches a second leaf; the
-    // leaves are then tested in the order they were reached, which is the
-    // reference's order.  Nodes stepped through before the postponed leaf
+    // Node steps continue past a lane's first leaf (postponed) until all but
+    // SKW_TRAV_LAG walking lanes hold one, or the lane reaches a second leaf;
+    // the leaves are then tested in the order they were reached, which is
+    // the reference's order.  (Waiting for the last few lanes to find a leaf
+    // left most of the warp idle: with 32 lanes the round length is the
+    // slowest lane's.)  Nodes stepped through before the postponed leaf
     // is tested see a larger tmax than the reference's -- a superset of its
     // visits, whose extra triangles all lie beyond the final tmax.
-    const float tcull = CLOSEST ? hi_t : r.tmax;
-    while (trav) {
-      if ((cur_b & 3u) == 0u) {  // a leaf
-        if (has_post) break;
-        if (!(cur_lo > tcull)) {
-          post_a = cur_a;
-          post_cnt = cur_b >> 8;
-          has_post = true;
+    //
+    // Every busy lane is walking when the round starts (a busy lane whose
+    // walk had ended would have finished its ray).  All of them stay in the
+    // loop -- a lane that is done idles -- and vote on every step over the
+    // busy mask, so they stay one group (a vote over __activemask() would
+    // only cover whatever fragment happens to be running together) and one
+    // vote per step suffices.
+    const float tcull = CLOSEST ? hi_t : s.tmax;
+    bool walking = trav;
+    while (true) {
+      if (walking) {
+        bool stop = false;
+        if ((cur_b & 3u) == 0u) {  // a leaf
+          if (has_post) {
+            stop = true;  // a second leaf: it waits for the next round
+          } else {
+            if (!(cur_lo > tcull)) {
+              post_a = cur_a;
+              post_cnt = cur_b >> 8;
+              has_post = true;
+            }
+            trav = st.pop(tcull, cur_a, cur_b, cur_lo);
+          }
+        } else {
+          trav = step_internal(nodes, s, tcull, st, cur_a, cur_b, cur_lo, status);
         }
-        trav = st.pop(tcull, cur_a, cur_b, cur_lo);
-      } else {
-        trav = step_internal(nodes, r, s, tcull, st, cur_a, cur_b, cur_lo, status);
+        walking = trav && !stop;
       }
-      if (__all_sync(__activemask(), has_post)) break;
+      if (__popc(__ballot_sync(busy, walking && !has_post)) <= SKW_TRAV_LAG) break;
     }
+    __syncwarp(busy);
     bool hit = false;
     if (has_post) {
       has_post = false;
+      const RayF r = SKW_RAY();
       const uint32_t a = post_a, cnt = post_cnt;
       for (uint32_t k = 0; k < cnt; ++k) {
         const int slot = (int)(a + k);
@@ -621,10 +691,11 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     }
     bool done = hit || (!trav && !has_post);
 #else
-    const float tcull = CLOSEST ? hi_t : r.tmax;
-    bool done = !descend(nodes, r, s, tcull, st, cur_a, cur_b, status);
+    const float tcull = CLOSEST ? hi_t : s.tmax;
+    bool done = !descend(nodes, s, tcull, st, cur_a, cur_b, status);
     bool hit = false;
     if (!done) {
+      const RayF r = SKW_RAY();
       // cur is a leaf: test its triangles in order.
       const uint32_t a = cur_a, cnt = cur_b >> 8;
       for (uint32_t k = 0; k < cnt; ++k) {
@@ -671,7 +742,7 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
           }
         }
       }
-      done = hit || !st.pop(CLOSEST ? hi_t : r.tmax, cur_a, cur_b);
+      done = hit || !st.pop(CLOSEST ? hi_t : s.tmax, cur_a, cur_b);
     }
 #endif
     if (done) {
@@ -682,7 +753,7 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
         // A float-decided hit whose bracket is wider than the 1e-5 reporting
         // tolerance (grazing incidence) takes t from the exact test.
         if (!(flags & 8u) && hi_t - lo_t > 1.0e-5f * fabsf(tout)) {
-          tout = (float)exact_t(tris, r, best_slot, tout);
+          tout = (float)exact_t(tris, SKW_RAY(), best_slot, tout);
           flags |= 4u;
         }
         h = make_int4(__float_as_int(tout), __float_as_int(ta.w), __float_as_int(tb.w), (int)(flags & 7u));
@@ -704,8 +775,16 @@ cudaError_t cap_prepare() {
   for (int which = 0; which < 2; ++which) {
     int &occ = cap_occupancy<CAP>(which == 1);
     if (occ != 0) continue;
-    cudaError_t e = which ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<CAP, true>, SKW_TRAV_BLOCK, 0)
-                          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<CAP, false>, SKW_TRAV_BLOCK, 0);
+    cudaError_t e;
+    if (SKW_TRAV_CARVEOUT >= 0) {
+      e = which ? cudaFuncSetAttribute(k_trace<CAP, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       SKW_TRAV_CARVEOUT)
+                : cudaFuncSetAttribute(k_trace<CAP, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       SKW_TRAV_CARVEOUT);
+      if (e != cudaSuccess) return e;
+    }
+    e = which ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<CAP, true>, SKW_TRAV_BLOCK, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<CAP, false>, SKW_TRAV_BLOCK, 0);
     if (e != cudaSuccess) return e;
     if (occ < 1) occ = 1;
   }
