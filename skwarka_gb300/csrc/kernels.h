@@ -32,7 +32,8 @@ int traversal_max_ctas_per_sm(int stack_cap);
 
 
 // Photon kd-tree lookups (knn.cu).  nodes: KdNode[n]; nids: uint16 normal
-// id per node; dirs: 3 doubles per 16-bit direction id; q / qn: 3 doubles
+// id per node; dirs: direction_table_device() (3 doubles per 16-bit
+// direction id, then the same as 3 floats per id); q / qn: 3 doubles
 // per query (qn may be null when cos_t < 0, which disables the filter).
 // Outputs per query: k slots of tree positions and squared distances in the
 // reference's heap order (-1 / 0 when unused) and the found count;

@@ -48,7 +48,11 @@ static __device__ __align__(256) unsigned char g_knn_noalloc_scratch[(size_t)SKW
 namespace skw {
 namespace {
 
-constexpr int kMaxStack = 64;  // > tree depth (ceil(log2(n + 1)) <= 31 for n < 2^31)
+// Walk stack entries per thread: the median-split tree of n < 2^31 points
+// is at most 31 levels deep and the walk holds at most one entry per level.
+constexpr int kStack = 32;
+constexpr int kKnnBlock = 128;  // threads per block of the lookup kernels
+
 
 // A heap entry: the squared distance as its IEEE bit pattern (for the
 // non-negative doubles here, unsigned integer order is the double order, so
@@ -115,6 +119,7 @@ struct Query {
   float eq;     // max |q - qf| over the axes
   bool qle[3];  // q <= qf on the axis (decides q <= split when split == qf)
   float nf[3];  // the normal in float (filter pre-test)
+  float cos_f, sin_f;  // cos_t, sin_t in float (filter pre-test)
 };
 
 // Fills the float copy of the query point used by the pre-tests.
@@ -127,6 +132,8 @@ __device__ __forceinline__ void query_float(Query &Q) {
     Q.nf[k] = (float)Q.n[k];
   }
   Q.eq = e * 1.0001f;
+  Q.cos_f = (float)Q.cos_t;
+  Q.sin_f = (float)Q.sin_t;
 }
 
 // q[axis] <= split for a float split, exactly, without double arithmetic:
@@ -145,17 +152,17 @@ __device__ __forceinline__ bool photon_filter_exact(const Query &Q, const float4
                                                     const double *__restrict__ dirs);
 __device__ __forceinline__ bool photon_filter(const Query &Q, const float4 p, uint16_t nid,
                                               const double *__restrict__ dirs) {
-  const float nx = (float)__ldg(dirs + 3 * nid), ny = (float)__ldg(dirs + 3 * nid + 1),
-              nz = (float)__ldg(dirs + 3 * nid + 2);
+  const float *dirs_f = reinterpret_cast<const float *>(dirs + (3 << 16));  // the table rounded to float
+  const float nx = __ldg(dirs_f + 3 * nid), ny = __ldg(dirs_f + 3 * nid + 1), nz = __ldg(dirs_f + 3 * nid + 2);
   const float cf = nx * Q.nf[0] + ny * Q.nf[1] + nz * Q.nf[2];
-  const float ct = (float)Q.cos_t;
+  const float ct = Q.cos_f;
   if (cf < ct - 2e-6f) return false;
   if (cf > ct + 2e-6f) {
     // |to . n| < sin_t |to|, compared as squares when both sides clearly differ
     const float tx = p.x - Q.qf[0], ty = p.y - Q.qf[1], tz = p.z - Q.qf[2];
     const float dn = tx * Q.nf[0] + ty * Q.nf[1] + tz * Q.nf[2];
     const float l2 = tx * tx + ty * ty + tz * tz;
-    const float st = (float)Q.sin_t;
+    const float st = Q.sin_f;
     const float lhs = dn * dn, rhs = st * st * l2;
     // error: the float query rounding eq on each component plus relative rounding
     const float a = fabsf(tx) + fabsf(ty) + fabsf(tz);
@@ -200,16 +207,21 @@ __device__ __forceinline__ void sq_bound(float d, float eq, float &sq, float &er
 }
 
 // Walks the tree in the reference's order, calling visit(ni, p, d2, maxd2)
-// for every point with d2 < maxd2 (visit may shrink maxd2).  Returns nodes
-// visited (for statistics) or -1 on stack overflow.  Stack entries hold the
-// far child, its parent (to recompute the plane distance exactly when the
-// float pre-test cannot decide) and the float plane distance.
+// for every point with d2 < maxd2; visit returns true when it changed
+// maxd2.  A point whose float distance is certainly inside the radius is
+// visited with d2 = -1 (not computed): the exact double distance is only
+// needed for the heap order, and the caller computes it later, many at a
+// time (the exact distance is a chain of dependent double operations, slow
+// on this GPU's FP64 pipe when done one point after another).  Returns
+// nodes visited (for statistics) or -1 on stack overflow.  The stack lives
+// in shared memory ([entry][thread], so lanes never share a bank) and holds
+// only the parent of each postponed far child: on pop the parent is read
+// again (a recently visited node, usually still in L1) and its split gives
+// both the far child and the plane distance to re-test.
 template <class Visit>
 __device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, const Query &Q, double &maxd2,
-                                    Visit &&visit) {
+                                    uint32_t (*stk)[kKnnBlock], Visit &&visit) {
   if (n <= 0) return 0;
-  uint32_t st_node[kMaxStack], st_parent[kMaxStack];
-  float st_pd[kMaxStack];
   int sp = 0, visited = 0;
   int cur = 0;
   // maxd2 in float, rounded down (a float below it is below maxd2 too)
@@ -226,10 +238,14 @@ __device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, con
       sq_bound(p.z - Q.qf[2], Q.eq, sz, ez);
       const float d2f = (sx + sy) + sz;
       const float E = (ex + ey + ez) * 1.0001f + d2f * 4.0e-7f + 1e-37f;
-      if (!(d2f - E >= mhi)) {  // not certainly outside: decide exactly
+      if (d2f + E < mlo) {  // certainly inside
+        if (visit(cur, p, -1.0, maxd2)) {
+          mlo = lo_f(maxd2);
+          mhi = hi_f(maxd2);
+        }
+      } else if (!(d2f - E >= mhi)) {  // not certainly outside: decide exactly
         const double d2 = point_d2(p, Q);
-        if (d2 < maxd2) {
-          visit(cur, p, d2, maxd2);
+        if (d2 < maxd2 && visit(cur, p, d2, maxd2)) {
           mlo = lo_f(maxd2);
           mhi = hi_f(maxd2);
         }
@@ -242,29 +258,23 @@ __device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, con
       const float split = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
       const uint32_t right = w >> 3;
       const bool has_left = (w & 4u) != 0u, has_right = right < (uint32_t)n;
-      const int left_i = cur + 1;
-      int near_i, far_i;
-      if (q_le_split(Q, axis, split)) {
-        near_i = has_left ? left_i : -1;
-        far_i = has_right ? (int)right : -1;
-      } else {
-        near_i = has_right ? (int)right : -1;
-        far_i = has_left ? left_i : -1;
-      }
-      if (far_i >= 0) {
-        if (sp >= kMaxStack) return -1;
-        st_node[sp] = (uint32_t)far_i;
-        st_parent[sp] = (uint32_t)cur;
-        st_pd[sp] = Q.qf[axis] - split;
+      const bool le = q_le_split(Q, axis, split);
+      next = le ? (has_left ? cur + 1 : -1) : (has_right ? (int)right : -1);
+      if (le ? has_right : has_left) {  // the far child waits on the stack
+        if (sp >= kStack) return -1;
+        stk[sp][threadIdx.x] = (uint32_t)cur;
         ++sp;
       }
-      next = near_i;
     }
     while (next < 0 && sp > 0) {
       --sp;
+      const uint32_t par = stk[sp][threadIdx.x];
+      const float4 pp = __ldg(nodes + par);
+      const uint32_t pw = __float_as_uint(pp.w), ax = pw & 3u;
+      const float split = ax == 0 ? pp.x : (ax == 1 ? pp.y : pp.z);
       // the reference's pop test: (qa - split)^2 < maxd2, in double
       float s2, e2;
-      sq_bound(st_pd[sp], Q.eq, s2, e2);
+      sq_bound(Q.qf[ax] - split, Q.eq, s2, e2);
       const float E = e2 * 1.0001f + s2 * 4.0e-7f + 1e-37f;
       bool take;
       if (s2 + E < mlo) {
@@ -272,29 +282,47 @@ __device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, con
       } else if (s2 - E >= mhi) {
         take = false;
       } else {
-        const float4 pp = __ldg(nodes + st_parent[sp]);
-        const uint32_t ax = __float_as_uint(pp.w) & 3u;
-        const double sp_d = (double)(ax == 0 ? pp.x : (ax == 1 ? pp.y : pp.z));
-        const double pd = __dsub_rn(Q.q[ax], sp_d);
+        const double pd = __dsub_rn(Q.q[ax], (double)split);
         take = __dmul_rn(pd, pd) < maxd2;
       }
-      if (take) next = (int)st_node[sp];
+      if (take) next = q_le_split(Q, ax, split) ? (int)(pw >> 3) : (int)par + 1;
     }
     if (next < 0) return visited;
     cur = next;
   }
 }
 
+// Exact squared distances of entries [0, len) of h, whose idx are set: four
+// independent dependent-chains at a time so that the FP64 pipe overlaps
+// them.
+__device__ __forceinline__ void fill_keys(const float4 *__restrict__ nodes, const Query &Q, Cand *h, int len) {
+  int j = 0;
+  for (; j + 4 <= len; j += 4) {
+    const float4 p0 = __ldg(nodes + h[j].idx), p1 = __ldg(nodes + h[j + 1].idx), p2 = __ldg(nodes + h[j + 2].idx),
+                 p3 = __ldg(nodes + h[j + 3].idx);
+    const double d0 = point_d2(p0, Q), d1 = point_d2(p1, Q), d2 = point_d2(p2, Q), d3 = point_d2(p3, Q);
+    h[j].key = (unsigned long long)__double_as_longlong(d0);
+    h[j + 1].key = (unsigned long long)__double_as_longlong(d1);
+    h[j + 2].key = (unsigned long long)__double_as_longlong(d2);
+    h[j + 3].key = (unsigned long long)__double_as_longlong(d3);
+  }
+  for (; j < len; ++j) h[j].key = (unsigned long long)__double_as_longlong(point_d2(__ldg(nodes + h[j].idx), Q));
+}
+
 // KMAX > 0: heap of KMAX entries in local memory.  KMAX == 0: the heap of
-// query i is scratch[i * k ...].
+// query i is scratch[i * k ...].  Until the heap is full its entries keep
+// only their tree position (the reference's array holds them unordered);
+// their exact distances are computed together when it fills -- or at the
+// end, for a query that finds fewer than k points.
 template <int KMAX>
-__global__ void __launch_bounds__(128) k_knn(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
+__global__ void __launch_bounds__(kKnnBlock) k_knn(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
                                              const double *__restrict__ dirs, int n, const double *__restrict__ q,
                                              const double *__restrict__ qn, int64_t nq, int k, double max_dist,
                                              double cos_t, int32_t *__restrict__ out_idx,
                                              double *__restrict__ out_d2, int32_t *__restrict__ out_count,
                                              int32_t *__restrict__ out_visited, Cand *__restrict__ scratch,
                                              unsigned *__restrict__ status, const int *__restrict__ nq_dev) {
+  __shared__ uint32_t stk[kStack][kKnnBlock];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (nq_dev && *nq_dev < nq) nq = *nq_dev;
   if (i >= nq) return;
@@ -320,25 +348,27 @@ __global__ void __launch_bounds__(128) k_knn(const float4 *__restrict__ nodes, c
   double maxd2 = __dmul_rn(max_dist, max_dist);  // KDTree::Lookup (KDTree.h:475-482)
   int visited = 0;
   if (k > 0) {
-    visited = walk(nodes, n, Q, maxd2, [&](int ni, const float4 p, double d2, double &md2) {
-      if (Q.filter && !photon_filter(Q, p, __ldg(nids + ni), dirs)) return;
+    visited = walk(nodes, n, Q, maxd2, stk, [&](int ni, const float4 p, double d2, double &md2) -> bool {
+      if (Q.filter && !photon_filter(Q, p, __ldg(nids + ni), dirs)) return false;
       if (size < k) {
-        heap[size++] = make_cand(d2, ni);
-        if (size == k) {
-          heap_make(heap, size);
-          md2 = heap[0].d2();
-        }
+        heap[size++].idx = ni;
+        if (size < k) return false;
+        fill_keys(nodes, Q, heap, size);
+        heap_make(heap, size);
       } else {
+        if (d2 < 0.0) d2 = point_d2(p, Q);
         // pop_heap: the top goes to the back; the back's old value is re-placed
         const Cand back = heap[k - 1];
         heap[k - 1] = heap[0];
         heap_adjust(heap, 0, k - 1, back);
         // replace the (popped) back with the new point and push it
         heap_push_up(heap, k - 1, 0, make_cand(d2, ni));
-        md2 = heap[0].d2();
       }
+      md2 = heap[0].d2();
+      return true;
     });
     if (visited < 0) atomicOr(status, 2u);
+    if (size < k) fill_keys(nodes, Q, heap, size);
   }
   out_count[i] = size;
   for (int j = 0; j < k; ++j) {
@@ -350,12 +380,13 @@ __global__ void __launch_bounds__(128) k_knn(const float4 *__restrict__ nodes, c
 
 // GetNearestPoint (KDTree.h:495-503) with NearestPointProc (:293-323):
 // every accepted point becomes the nearest and shrinks the radius.
-__global__ void __launch_bounds__(128) k_nearest(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
+__global__ void __launch_bounds__(kKnnBlock) k_nearest(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
                                                  const double *__restrict__ dirs, int n,
                                                  const double *__restrict__ q, const double *__restrict__ qn,
                                                  int64_t nq, double max_dist, double cos_t,
                                                  int32_t *__restrict__ out_idx, unsigned *__restrict__ status,
                                                  const int *__restrict__ nq_dev) {
+  __shared__ uint32_t stk[kStack][kKnnBlock];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (nq_dev && *nq_dev < nq) nq = *nq_dev;
   if (i >= nq) return;
@@ -377,10 +408,11 @@ __global__ void __launch_bounds__(128) k_nearest(const float4 *__restrict__ node
   query_float(Q);
   double maxd2 = __dmul_rn(max_dist, max_dist);
   int best = -1;
-  const int v = walk(nodes, n, Q, maxd2, [&](int ni, const float4 p, double d2, double &md2) {
-    if (Q.filter && !photon_filter(Q, p, __ldg(nids + ni), dirs)) return;
+  const int v = walk(nodes, n, Q, maxd2, stk, [&](int ni, const float4 p, double d2, double &md2) -> bool {
+    if (Q.filter && !photon_filter(Q, p, __ldg(nids + ni), dirs)) return false;
     best = ni;
-    md2 = d2;
+    md2 = d2 < 0.0 ? point_d2(p, Q) : d2;
+    return true;
   });
   if (v < 0) atomicOr(status, 2u);
   out_idx[i] = best;
@@ -395,7 +427,7 @@ cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *di
                        double *out_d2, int32_t *out_count, int32_t *out_visited, void *scratch, unsigned *status,
                        cudaStream_t stream, const int *nq_dev) {
   if (nq <= 0) return cudaSuccess;
-  const int block = 128;
+  const int block = kKnnBlock;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
   if (k <= 32) {
     k_knn<32><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
@@ -444,7 +476,7 @@ cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const do
   if (e != cudaSuccess) return e;
   // Every heap slot is written before it is read, so the array needs no
   // clearing between calls.
-  const int block = 128;
+  const int block = kKnnBlock;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
   k_knn<0><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
                                         out_idx, out_d2, out_count, nullptr, (Cand *)scratch, status, nullptr);
@@ -455,7 +487,7 @@ cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double
                            const double *qn, int64_t nq, double max_dist, double cos_t, int32_t *out_idx,
                            unsigned *status, cudaStream_t stream, const int *nq_dev) {
   if (nq <= 0) return cudaSuccess;
-  const int block = 128;
+  const int block = kKnnBlock;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
   k_nearest<<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, max_dist, cos_t, out_idx,
                                         status, nq_dev);

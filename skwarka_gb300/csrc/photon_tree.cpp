@@ -111,6 +111,19 @@ const std::vector<double> &direction_table() {
   return table;
 }
 
+const std::vector<double> &direction_table_device() {
+  static std::vector<double> table;
+  static std::once_flag once;
+  std::call_once(once, []() {
+    const std::vector<double> &t = direction_table();
+    table.assign(t.begin(), t.end());
+    table.resize(t.size() + t.size() / 2);
+    float *f = reinterpret_cast<float *>(table.data() + t.size());
+    for (size_t i = 0; i < t.size(); ++i) f[i] = (float)t[i];
+  });
+  return table;
+}
+
 uint16_t compress_direction(double x, double y, double z) {
   unsigned data = 0;
   if (x < 0) {

@@ -31,6 +31,12 @@ void build_photon_tree(const float *pos, int64_t n, int threads, std::vector<KdN
 // of every 16-bit direction id, as 3 doubles per id.
 const std::vector<double> &direction_table();
 
+// The device copy of the table: the 3 << 16 doubles of direction_table()
+// followed by the same values rounded to float (3 floats per id, packed
+// into the vector's last (3 << 16) / 2 doubles).  Kernels that pre-test in
+// float read the float part and never convert a double.
+const std::vector<double> &direction_table_device();
+
 // CompressedDirection(Vector3D) encoder (Math/CompressedDirection.h:107-133).
 uint16_t compress_direction(double x, double y, double z);
 

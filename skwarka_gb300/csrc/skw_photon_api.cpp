@@ -87,7 +87,7 @@ int skw_kdtree_create(skw_ctx *ctx, const float *positions, const uint16_t *norm
   if (normal_ids)
     for (int64_t i = 0; i < n; ++i) nids[(size_t)i] = normal_ids[t->perm[(size_t)i]];
   cudaError_t e = cudaSetDevice(ctx->device);
-  const std::vector<double> &dirs = skw::direction_table();
+  const std::vector<double> &dirs = skw::direction_table_device();
   const size_t nb = (size_t)std::max<int64_t>(n, 1) * sizeof(skw::KdNode);
   if (e == cudaSuccess) e = cudaMalloc(&t->d_nodes, nb);
   if (e == cudaSuccess) e = cudaMalloc(&t->d_nids, nids.size() * sizeof(uint16_t));

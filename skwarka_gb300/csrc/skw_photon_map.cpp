@@ -224,7 +224,7 @@ int build_irradiance(skw_photon_map *pm, cudaStream_t st) {
 int finish_map(skw_photon_map *pm, cudaStream_t st) {
   const auto t0 = std::chrono::steady_clock::now();
   cudaError_t e = cudaSetDevice(pm->ctx->device);
-  const std::vector<double> &dirs = skw::direction_table();
+  const std::vector<double> &dirs = skw::direction_table_device();
   if (e == cudaSuccess) e = upload(dirs, &pm->d_dirs);
   if (e == cudaSuccess) e = cudaMalloc(&pm->d_status, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(pm->d_status, 0, sizeof(unsigned));
