@@ -155,7 +155,7 @@ def load_traffic(kind: str, rays: int):
     d = json.loads(p.read_text()).get(kind)
     if not d:
         return None
-    return d["dram_bytes_per_ray"] * rays
+    return d.get("dram_bytes_per_launch", 0.0) + d["dram_bytes_per_ray"] * rays
 
 
 def cpu_baseline(meshes, rays, sample, rank):
