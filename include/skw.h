@@ -400,15 +400,19 @@ int skw_photon_map_export_irradiance(const skw_photon_map *map, float *pos, floa
  * LTEIntegrators/PhotonLTEIntegrator.h:33-70). */
 typedef struct skw_photon_render_params {
   int32_t gather_samples;   /* final-gather samples per strategy, rounded up to a square as the sampler does */
+  int32_t caustic_lookup;   /* PhotonLTEIntegratorParams::m_caustic_lookup_photons_num (0..4096) */
+  double max_caustic_dist;  /* PhotonLTEIntegratorParams::m_max_caustic_lookup_dist (> 0 when caustics are used) */
 } skw_photon_render_params;
 
 /* Renders (camera, params) with PhotonLTEIntegrator::_SurfaceRadiance
  * (PhotonLTEIntegrator.cpp:320-385): emission + direct lighting (as
- * skw_render_direct) + final gathering (_FinalGather, :387-577: BSDF- and
- * photon-guided gather rays, the nearest irradiance photon and
- * BSDF::TotalScattering at each gather hit).  Maps with caustic photons are
- * rejected (SKW_ERR_UNSUPPORTED): the caustic lookup is not implemented, and
- * no BSDF here is specular, so GPU-shot maps never have caustic photons. */
+ * skw_render_direct) + the caustic-map radiance (_LookupCausticRadiance,
+ * :579-627: the caustic_lookup nearest filtered caustic photons within
+ * max_caustic_dist, Simpson's kernel) + final gathering (_FinalGather,
+ * :387-577: BSDF- and photon-guided gather rays, the nearest irradiance
+ * photon and BSDF::TotalScattering at each gather hit).  No BSDF here is
+ * specular, so maps shot by skw_photon_shoot have no caustic photons; maps
+ * made from photon arrays (skw_photon_map_create) may. */
 int skw_render_photon(skw_scene *scene, const skw_photon_map *map, const skw_camera *camera,
                       const skw_render_params *params, const skw_photon_render_params *photon_params, float *film_rgb,
                       void *stream);

@@ -69,6 +69,9 @@ _REF_SIGS = [
                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, C.c_int,
                                         C.c_double, _P, _P, _P]),
     ("skw_ref_photon_irradiance", C.c_int, [_P, _P, _P, C.c_double, _P, _P, _P, _P, _P, _P]),
+    ("skw_ref_render_photon_maps", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, _P, _P, _P,
+                                             C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                             C.c_double, _P, _P, _P]),
     ("skw_ref_merl_create", _P, [C.c_char_p, _i64]),
     ("skw_ref_merl_destroy", None, [_P]),
     ("skw_ref_merl_export", None, [_P, _P, _P]),
@@ -280,6 +283,38 @@ class Reference:
                                        _ptr(info), _ptr(sec))
         return film, {"shoot_s": float(sec[0]), "render_s": float(sec[1]), "caustic": int(info[0]),
                       "direct": int(info[1]), "indirect": int(info[2]), "irradiance": int(info[3])}
+
+    def render_photon_maps(self, prims, materials, point_lights, camera, spp_x, spp_y, maps, paths, light_samples=1,
+                           gather_samples=16, caustic_lookup=50, max_caustic_dist=0.1):
+        """The reference's photon-mapping render with the given photon maps
+        (structured arrays of PHOTON_DTYPE: caustic, direct, indirect, with
+        their path counts) in place of ShootPhotons: (film, {"render_s",
+        "caustic", "direct", "indirect", "irradiance"})."""
+        from skwarka_gb300.photon import PHOTON_DTYPE
+        from skwarka_gb300.render import c_material, c_prims
+        cm, nm, cp, keep = c_prims(prims)
+        verts = (C.c_void_p * nm)(*[cm[i].vertices for i in range(nm)])
+        tris = (C.c_void_p * nm)(*[cm[i].triangles for i in range(nm)])
+        nv = np.array([cm[i].n_vertices for i in range(nm)], np.int64)
+        nt = np.array([cm[i].n_triangles for i in range(nm)], np.int64)
+        mats = (type(c_material(materials[0])) * len(materials))(
+            *[c_material(m, self._merl(m.measured) if m.measured is not None else None) for m in materials])
+        pl = np.array([list(l.position) + list(l.intensity) for l in point_lights], np.float32).reshape(-1, 6)
+        arrs = [np.ascontiguousarray(m, PHOTON_DTYPE) for m in maps]
+        ptrs = (C.c_void_p * 3)(*[a.ctypes.data for a in arrs])
+        n = np.array([len(a) for a in arrs], np.int64)
+        pth = np.array(paths, np.int64)
+        c2w = np.ascontiguousarray(camera.camera_to_world, np.float64).reshape(-1)
+        film = np.zeros((camera.height, camera.width, 3), np.float32)
+        info = np.zeros(4, np.int64)
+        sec = np.zeros(1)
+        self.lib.skw_ref_render_photon_maps(nm, verts, _ptr(nv), tris, _ptr(nt), len(prims), C.addressof(cp),
+                                            C.addressof(mats), len(point_lights), _ptr(pl) if len(pl) else None, ptrs,
+                                            _ptr(n), _ptr(pth), _ptr(c2w), camera.x_view_angle, camera.width,
+                                            camera.height, spp_x, spp_y, light_samples, gather_samples,
+                                            caustic_lookup, max_caustic_dist, _ptr(film), _ptr(info), _ptr(sec))
+        return film, {"render_s": float(sec[0]), "caustic": int(info[0]), "direct": int(info[1]),
+                      "indirect": int(info[2]), "irradiance": int(info[3])}
 
     def render_direct(self, prims, materials, point_lights, camera, spp_x, spp_y, light_samples=1, medium=None):
         """The reference's own direct-lighting render of a scene described with

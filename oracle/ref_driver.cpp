@@ -604,6 +604,57 @@ int skw_ref_photon_irradiance(const RefPhotonIn *const *photons, const int64_t *
   return 0;
 }
 
+// Photon-mapping render with given photon maps instead of shooting: the
+// maps (28-byte records, each with its number of paths) are added as
+// ShootPhotons' merging filter adds them, the kd-trees and the irradiance
+// map are built as at the end of ShootPhotons (PhotonLTEIntegrator.cpp:
+// 271-277), then the sampler-based render runs.  info_out: the four map
+// sizes; seconds_out: the render time.
+int skw_ref_render_photon_maps(int n_meshes, const float *const *verts, const int64_t *n_verts,
+                               const int32_t *const *tris, const int64_t *n_tris, int n_prims, const RefPrimIn *prims,
+                               const RefMaterialIn *materials, int n_point_lights, const float *point_lights,
+                               const RefPhotonIn *const *photons, const int64_t *n_photons, const int64_t *paths,
+                               const double *camera_to_world, double x_view_angle, int width, int height, int spp_x,
+                               int spp_y, int light_samples, int gather_samples, int caustic_lookup,
+                               double max_caustic_dist, float *film_out, int64_t *info_out, double *seconds_out) {
+  intrusive_ptr<const Scene> scene =
+      make_scene(n_meshes, verts, n_verts, tris, n_tris, n_prims, prims, materials, n_point_lights, point_lights);
+  PhotonLTEIntegratorParams params;
+  params.m_direct_light_samples_num = (size_t)light_samples;
+  params.m_caustic_lookup_photons_num = (size_t)caustic_lookup;
+  params.m_max_caustic_lookup_dist = max_caustic_dist;
+  params.m_gather_samples_num = (size_t)gather_samples;
+  params.m_max_specular_depth = 6;
+  params.m_media_step_size = 0.01;
+  intrusive_ptr<PhotonLTEIntegrator> integrator(new PhotonLTEIntegrator(scene, params));
+  integrator->mp_photon_maps.reset(new PhotonLTEIntegrator::PhotonMaps());
+  for (int m = 0; m < 3; ++m) {
+    std::vector<RefPhoton> ph((size_t)n_photons[m]);
+    for (int64_t i = 0; i < n_photons[m]; ++i) {
+      const RefPhotonIn &r = photons[m][i];
+      ph[(size_t)i] = RefPhoton(Point3D_f(r.p[0], r.p[1], r.p[2]), Spectrum_f(r.w[0], r.w[1], r.w[2]),
+                                CompressedDirection::FromID(r.dir), CompressedDirection::FromID(r.nrm));
+    }
+    if (m == 0) integrator->mp_photon_maps->AddCausticPhotons(ph, (size_t)paths[m]);
+    if (m == 1) integrator->mp_photon_maps->AddDirectPhotons(ph, (size_t)paths[m]);
+    if (m == 2) integrator->mp_photon_maps->AddIndirectPhotons(ph, (size_t)paths[m]);
+  }
+  integrator->mp_photon_maps->GetCausticMap();
+  integrator->mp_photon_maps->GetDirectMap();
+  integrator->mp_photon_maps->GetIndirectMap();
+  integrator->_ConstructIrradiancePhotonMap();
+  if (info_out) {
+    auto &maps = integrator->mp_photon_maps;
+    info_out[0] = maps->GetCausticMap() ? (int64_t)maps->GetCausticMap()->GetNumberOfPoints() : 0;
+    info_out[1] = maps->GetDirectMap() ? (int64_t)maps->GetDirectMap()->GetNumberOfPoints() : 0;
+    info_out[2] = maps->GetIndirectMap() ? (int64_t)maps->GetIndirectMap()->GetNumberOfPoints() : 0;
+    info_out[3] = integrator->mp_irradiance_map ? (int64_t)integrator->mp_irradiance_map->GetNumberOfPoints() : 0;
+  }
+  const double render = render_film(integrator, camera_to_world, x_view_angle, width, height, spp_x, spp_y, film_out);
+  if (seconds_out) seconds_out[0] = render;
+  return 0;
+}
+
 // ------------------------------------------------------------- measured BRDF
 
 // MERLMeasuredData from a file image in the MERL binary format (3 int32

@@ -126,6 +126,15 @@ cudaError_t launch_irradiance_sum(const void *nodes, const float *weight, const 
                                   int64_t nq, int k, double paths, double max_lookup_dist, bool first, float *ext,
                                   float *intr, cudaStream_t st);
 
+// Caustic radiance of a render pass (photon.cu): the filtered k-NN in the
+// caustic map at each camera hit and the Simpson-kernel estimate, written to
+// slot `slot` of contrib.  cws: caustic_bytes(n, k) bytes of workspace.
+struct CausticMap;
+size_t caustic_bytes(int64_t n, int k);
+cudaError_t launch_caustic(const SceneDev &S, const CausticMap &C, const ViewDev *views, int n_views, int n,
+                           int64_t px_begin, int spp, int slots, int slot, const void *rays, const void *hits,
+                           void *cws, float *contrib, unsigned *status, cudaStream_t st);
+
 // Final gather of a render pass (photon.cu): adds each camera hit's gathered
 // indirect radiance to its slots [base_slot, base_slot + 2 gs) of contrib.
 // gws: gather_bytes(n, gs) bytes of workspace.

@@ -745,7 +745,102 @@ __global__ void k_gather_resolve(GatherMaps M, int gs, const int *__restrict__ h
   for (int c = 0; c < 3; ++c) contrib[3 * slot + c] = ts[3 * j + c] * E[c] * gweight[3 * g + c] * s;
 }
 
+// _LookupCausticRadiance (PhotonLTEIntegrator.cpp:579-627) at camera hit j
+// of the pass, from the k-NN output in the reference's heap order: each
+// found photon adds BSDF(photon direction, viewer) * weight * Simpson's
+// kernel 3/pi (1 - d2 / m)^2 (_PhotonKernel, :629-636), where m is the
+// largest squared distance among the photons visited so far -- the
+// reference's running maximum, not the final radius (so the first photon
+// always gets kernel 0).  The sum is divided by the caustic paths times the
+// area term: the lookup radius squared when fewer than k were found (or
+// m == 0), else m * n / (n - 0.5).  Sums in double, as the reference's
+// Spectrum_d; the BSDF in float as everywhere in this renderer.
+__global__ void __launch_bounds__(128) k_caustic_resolve(SceneDev S, GatherArgs G, CausticMap C,
+                                                         const float4 *__restrict__ rays,
+                                                         const int4 *__restrict__ hits, const int *__restrict__ src,
+                                                         const int *__restrict__ src_count,
+                                                         const int32_t *__restrict__ kidx,
+                                                         const double *__restrict__ kd2,
+                                                         const int32_t *__restrict__ kcount, int slot,
+                                                         float *__restrict__ contrib) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= *src_count) return;
+  const int found = kcount[j];
+  if (found <= 0) return;
+  const int i = src[j];
+  const int4 hit = hits[i];
+  const float4 ra = rays[2 * i], rb = rays[2 * i + 1];
+  const V3 dir = v3(ra.w, rb.x, rb.y);
+  const Hit h = make_hit(S, v3(ra.x, ra.y, ra.z), dir, __int_as_float(hit.x), hit.y, hit.z);
+  const Bsdf b = make_bsdf(S, h, hit.y);
+  const V3 wo = v3(-dir.x, -dir.y, -dir.z);
+  double m = 0.0, r0 = 0.0, r1 = 0.0, r2 = 0.0;
+  for (int f = 0; f < found; ++f) {
+    const int64_t e = (int64_t)j * C.k + f;
+    const int t = kidx[e];
+    const double d2 = kd2[e];
+    if (d2 > m) m = d2;
+    const double u = 1.0 - d2 / m;
+    const double kern = 3.0 * 0.31830988618379067154 * u * u;
+    const uint16_t id = C.dirid[t];
+    const V3 wi = v3((float)C.dirs[3 * id], (float)C.dirs[3 * id + 1], (float)C.dirs[3 * id + 2]);
+    const V3 f3 = bsdf_eval(b, wi, wo);
+    r0 += (double)f3.x * (double)C.weight[3 * t] * kern;
+    r1 += (double)f3.y * (double)C.weight[3 * t + 1] * kern;
+    r2 += (double)f3.z * (double)C.weight[3 * t + 2] * kern;
+  }
+  if (found < C.k || m == 0.0)
+    m = C.max_dist * C.max_dist;
+  else
+    m *= (double)found / ((double)found - 0.5);
+  const double sc = 1.0 / (C.paths * m);
+  float *o = contrib + 3 * ((int64_t)i * G.slots + slot);
+  o[0] = (float)(r0 * sc);
+  o[1] = (float)(r1 * sc);
+  o[2] = (float)(r2 * sc);
+}
+
 }  // namespace
+
+size_t caustic_bytes(int64_t n, int k) {
+  auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
+  return 256 + al(n * 4) + 2 * al(n * 24) + al(n * (int64_t)k * 4) + al(n * (int64_t)k * 8) + al(n * 4) +
+         al((int64_t)knn_scratch_bytes(n, k)) + 256;
+}
+
+cudaError_t launch_caustic(const SceneDev &S, const CausticMap &C, const ViewDev *views, int n_views, int n,
+                           int64_t px_begin, int spp, int slots, int slot, const void *rays, const void *hits,
+                           void *cws, float *contrib, unsigned *status, cudaStream_t st) {
+  if (n <= 0 || C.n <= 0 || C.k <= 0) return cudaSuccess;
+  auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
+  char *p = (char *)cws;
+  auto take = [&](size_t b) {
+    char *r = p;
+    p += b;
+    return r;
+  };
+  int *counts = (int *)take(256);
+  int *src = (int *)take(al((int64_t)n * 4));
+  double *q = (double *)take(al((int64_t)n * 24)), *qn = (double *)take(al((int64_t)n * 24));
+  int32_t *kidx = (int32_t *)take(al((int64_t)n * C.k * 4));
+  double *kd2 = (double *)take(al((int64_t)n * C.k * 8));
+  int32_t *kcnt = (int32_t *)take(al((int64_t)n * 4));
+  void *scratch = take(al((int64_t)knn_scratch_bytes(n, C.k)));
+  // GatherArgs: only n, px_begin, spp, slots and the views are used here
+  GatherArgs G{n, px_begin, spp, slots, slot, 0, views, n_views};
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(counts, 0, sizeof(int), st)) != cudaSuccess) return e;
+  k_gather_sources<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S, G, (const float4 *)rays, (const int4 *)hits, src, q,
+                                                                 qn, counts);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // PhotonFilter at the hit's geometric normal, MAX_NORMAL_DEVIATION_COS = 0.87 (:27, :593-594)
+  if ((e = launch_knn(C.nodes, C.nids, C.dirs, C.n, q, qn, n, C.k, C.max_dist, 0.87, kidx, kd2, kcnt, nullptr,
+                      scratch, status, st, counts)) != cudaSuccess)
+    return e;
+  k_caustic_resolve<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S, G, C, (const float4 *)rays, (const int4 *)hits,
+                                                                  src, counts, kidx, kd2, kcnt, slot, contrib);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev *views, int n_views, int n,
                           int64_t px_begin, int spp, int slots, int base_slot, int gs, const void *rays,

@@ -41,6 +41,21 @@ namespace skw {
 
 // What the final-gather stages read: the indirect photon map (tree order) and
 // the irradiance photon map (tree order), plus the direction table.
+// The caustic map of a render (_LookupCausticRadiance,
+// PhotonLTEIntegrator.cpp:579-627): its tree, photons in tree order, number
+// of paths, and the lookup's k and radius.
+struct CausticMap {
+  const void *nodes;
+  const uint16_t *nids;
+  const uint16_t *dirid;
+  const float *weight;
+  int32_t n;
+  double paths;
+  int32_t k;
+  double max_dist;
+  const double *dirs;
+};
+
 struct GatherMaps {
   const void *ind_nodes;
   const uint16_t *ind_nids;

@@ -944,8 +944,10 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   if (!s || !pm || !cam || !params || !pp || !film_rgb) return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "null argument");
   skw_ctx *ctx = s->ctx;
   if (pp->gather_samples < 0 || pp->gather_samples > 1024) return fail(ctx, SKW_ERR_ARG, "gather_samples out of range");
-  if (pm->maps[0].n > 0)
-    return fail(ctx, SKW_ERR_UNSUPPORTED, "caustic photons: the caustic radiance lookup is not implemented");
+  if (pp->caustic_lookup < 0 || pp->caustic_lookup > 4096) return fail(ctx, SKW_ERR_ARG, "caustic_lookup out of range");
+  const bool caustic = pm->maps[0].n > 0 && pp->caustic_lookup > 0;
+  if (caustic && !(pp->max_caustic_dist > 0.0))
+    return fail(ctx, SKW_ERR_ARG, "max_caustic_dist must be positive");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
   // the sampler rounds sequence lengths up to squares (Sampler.cpp:39-57, StratifiedSampler.cpp:33-37)
@@ -957,7 +959,7 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   const bool gather = gs > 0 && pm->n_irr > 0;
   PassConfig cfg;
   cfg.samples_per_pass = (int64_t)1 << 19;
-  cfg.extra_slots = gather ? 2 * gs : 0;
+  cfg.extra_slots = (gather ? 2 * gs : 0) + (caustic ? 1 : 0);
   // PhotonLTEIntegrator has no medium march (_MediaRadianceAndTranmsittance
   // returns transmittance 1, PhotonLTEIntegrator.cpp:638-648); its direct
   // lighting still attenuates light samples through the medium.
@@ -970,14 +972,19 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   cudaMemPool_t pool;
   if ((e = skw::ctx_pool(ctx, &pool)) != cudaSuccess) return cuda_fail(ctx, e, "workspace pool");
   const size_t wbytes = workspace_bytes(P), vbytes = al256(sizeof(skw::ViewDev)),
-               gbytes = gather ? skw::gather_bytes(P.cap_samples, gs) : 0;
+               gbytes = gather ? skw::gather_bytes(P.cap_samples, gs) : 0,
+               cbytes = caustic ? skw::caustic_bytes(P.cap_samples, pp->caustic_lookup) : 0;
   char *w = nullptr;
-  if ((e = cudaMallocFromPoolAsync((void **)&w, wbytes + vbytes + gbytes, pool, st)) != cudaSuccess)
+  if ((e = cudaMallocFromPoolAsync((void **)&w, wbytes + vbytes + gbytes + cbytes, pool, st)) != cudaSuccess)
     return cuda_fail(ctx, e, "photon render workspace");
   Workspace W;
   workspace_carve(P, w, &W);
   skw::ViewDev *d_view = (skw::ViewDev *)(w + wbytes);
   void *gws = w + wbytes + vbytes;
+  void *cws = w + wbytes + vbytes + gbytes;
+  const skw::PhotonMapData &cm = pm->maps[0];
+  skw::CausticMap CM{cm.d_nodes, cm.d_nids, cm.d_dirid, cm.d_weight, (int32_t)cm.n, (double)cm.paths,
+                     pp->caustic_lookup, pp->max_caustic_dist, pm->d_dirs};
   skw::GatherMaps M{};
   const skw::PhotonMapData &im = pm->maps[2];
   M.ind_nodes = im.d_nodes;
@@ -1008,8 +1015,12 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
     if (gather && (e = skw::launch_gather(s->dev, M, d_view, 1, n, px0, P.spp, P.slots, base_slot, gs, W.rays, W.hits,
                                           gws, W.contrib, trace, pm->d_status, st)) != cudaSuccess)
       break;
+    // _LookupCausticRadiance (PhotonLTEIntegrator.cpp:342) into the slot after the gather slots
+    if (caustic && (e = skw::launch_caustic(s->dev, CM, d_view, 1, n, px0, P.spp, P.slots, P.slots - 1, W.rays,
+                                            W.hits, cws, W.contrib, pm->d_status, st)) != cudaSuccess)
+      break;
     if ((e = skw::launch_film(W.contrib, px0, n_px, P.spp, P.slots, film_rgb, st)) != cudaSuccess) break;
-    launches += kLaunchesPerPass + (gather ? 6 : 0);
+    launches += kLaunchesPerPass + (gather ? 6 : 0) + (caustic ? 3 : 0);
   }
   cudaFreeAsync(w, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "photon-map render");

@@ -83,13 +83,17 @@ class PhotonMap:
 
 
 class skw_photon_render_params(C.Structure):
-    _fields_ = [("gather_samples", C.c_int32)]
+    _fields_ = [("gather_samples", C.c_int32), ("caustic_lookup", C.c_int32), ("max_caustic_dist", C.c_double)]
 
 
 def render_photon(scene, photon_map: PhotonMap, camera, spp_x: int = 2, spp_y: int = 2, light_samples: int = 1,
-                  gather_samples: int = 16, seed: int = 0, out=None, stream=None):
-    """Photon-mapping render (emission + direct lighting + final gather) into
-    a CUDA float32 tensor (h, w, 3)."""
+                  gather_samples: int = 16, seed: int = 0, out=None, stream=None, caustic_lookup: int = 50,
+                  max_caustic_dist: float = 0.1):
+    """Photon-mapping render (emission + direct lighting + caustic-map
+    radiance + final gather) into a CUDA float32 tensor (h, w, 3).
+    caustic_lookup / max_caustic_dist: the caustic estimate's photon count
+    and radius (PhotonLTEIntegratorParams); used when the map has caustic
+    photons."""
     import torch
     from .render import c_camera, skw_render_params
     if out is None:
@@ -97,7 +101,7 @@ def render_photon(scene, photon_map: PhotonMap, camera, spp_x: int = 2, spp_y: i
     s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
     cam = c_camera(camera)
     par = skw_render_params(spp_x, spp_y, light_samples, seed)
-    pp = skw_photon_render_params(gather_samples)
+    pp = skw_photon_render_params(gather_samples, caustic_lookup, max_caustic_dist)
     _lib.check(_lib.load().skw_render_photon(scene.handle, photon_map.handle, C.byref(cam), C.byref(par), C.byref(pp),
                                              out.data_ptr(), s), scene.ctx.handle)
     return out

@@ -141,6 +141,27 @@ def photon_golden():
                         counts=np.array([info["caustic"], info["direct"], info["indirect"], info["irradiance"]]))
 
 
+def caustic_golden():
+    """The reference's photon-mapping render (gather and indirect maps
+    empty, so direct lighting + _LookupCausticRadiance) of each
+    scene_fixtures.caustic_cases() case with its seeded caustic map, at 16x16
+    samples per pixel."""
+    out = {}
+    ref = Reference()
+    for name, (prims, mats, lights, cam, maps, paths, k, r) in sf.caustic_cases().items():
+        film, info = ref.render_photon_maps(prims, mats, lights, cam, 16, 16, maps, paths, gather_samples=4,
+                                            caustic_lookup=k, max_caustic_dist=r)
+        assert info["caustic"] == len(maps[0]) and info["irradiance"] == 0, info
+        out[name] = film
+        direct, _ = ref.render_direct(prims, mats, lights, cam, 16, 16)
+        out[name + "_direct"] = direct
+    np.savez_compressed(OUT / "caustic_32.npz", **out)
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "caustic":
+    caustic_golden()
+    print("caustic golden written")
+
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "measured":
     measured_golden()
     print("measured golden written")

@@ -268,3 +268,49 @@ def two_light_scene():
     assert np.cross(b - a, c - a)[0] > 0  # emits towards +x
     prims = prims + [RenderPrimitive(TriangleMesh(lv, lt), 2, emission=(30.0, 20.0, 10.0))]
     return prims, mats, cam(32, 32)
+
+
+def caustic_cases(seed=41):
+    """A 4 x 4 plane (z = 0) under a weak point light, with a seeded caustic
+    photon map and empty direct and indirect maps: 30,000 photons on the
+    plane, 70 % uniform in a disk of radius 0.6 around the origin and 30 %
+    uniform over [-2, 2]^2 (so lookups outside the disk find fewer than k),
+    incident directions from the upper hemisphere, weights
+    U[0.5, 1.5] x (0.8, 0.6, 0.4), 200,000 caustic paths (the caustic term
+    is then about twice the direct lighting).  Cases: matte
+    and plastic planes with (k, radius) = (50, 0.1); the matte plane with
+    (200, 0.05), whose k-NN heaps live in global scratch.  Returns {name:
+    (prims, materials, lights, camera, maps, paths, k, radius)}; a 32 x 32
+    camera looks down at the disk at about 25 degrees from the normal."""
+    from skwarka_gb300.accel import TriangleMesh
+    from skwarka_gb300.kdtree import compress_directions
+    from skwarka_gb300.photon import PHOTON_DTYPE
+    from skwarka_gb300.render import PLASTIC, Camera, Material, PointLight, RenderPrimitive
+    rng = np.random.default_rng(seed)
+    n = 30_000
+    n_disk = int(0.7 * n)
+    r = 0.6 * np.sqrt(rng.uniform(size=n_disk))
+    a = rng.uniform(0.0, 2.0 * np.pi, size=n_disk)
+    pos = np.zeros((n, 3))
+    pos[:n_disk, 0], pos[:n_disk, 1] = r * np.cos(a), r * np.sin(a)
+    pos[n_disk:, :2] = rng.uniform(-2.0, 2.0, size=(n - n_disk, 2))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d[:, 2] = np.abs(d[:, 2])
+    caustic = np.zeros(n, PHOTON_DTYPE)
+    caustic["position"] = pos.astype(np.float32)
+    caustic["weight"] = (rng.uniform(0.5, 1.5, size=(n, 1)) * np.array([0.8, 0.6, 0.4])).astype(np.float32)
+    caustic["incident"] = compress_directions(d)
+    caustic["normal"] = compress_directions(np.tile([0.0, 0.0, 1.0], (n, 1)))
+    empty = np.zeros(0, PHOTON_DTYPE)
+    maps, paths = [caustic, empty, empty], [200_000, 0, 0]
+    s = 2.0
+    plane = TriangleMesh(np.array([[-s, -s, 0], [s, -s, 0], [s, s, 0], [-s, s, 0]], np.float32),
+                         np.array([[0, 1, 2], [0, 2, 3]], np.int32))
+    cam = Camera.look_at((0.0, -0.6, 1.4), (0.0, 0.0, 0.0), (0, 1, 0), np.radians(60.0), 32, 32)
+    lights = [PointLight((0.3, 0.2, 2.0), (0.05, 0.05, 0.05))]
+    matte = Material(kd=(0.7, 0.6, 0.5))
+    plastic = Material(kind=PLASTIC, kd=(0.4, 0.3, 0.2), ks=(0.5, 0.5, 0.5), roughness=0.1)
+    return {"matte_k50": ([RenderPrimitive(plane, 0)], [matte], lights, cam, maps, paths, 50, 0.1),
+            "plastic_k50": ([RenderPrimitive(plane, 0)], [plastic], lights, cam, maps, paths, 50, 0.1),
+            "matte_k200": ([RenderPrimitive(plane, 0)], [matte], lights, cam, maps, paths, 200, 0.05)}
