@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--no-batch", action="store_true", help="skip the batched multi-view render measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     p.add_argument("--no-photon", action="store_true", help="skip the photon-mapping measurement")
+    p.add_argument("--knn-sample", type=int, default=0,
+                   help="time the k-NN on a uniform random sample of this many of the primary hits (0: all)")
     return p.parse_args()
 
 
@@ -396,6 +398,10 @@ def photon_bench(args, dev, ctx, measure_cpu):
         n = torch.linalg.cross(v[tr[:, 1]] - v[tr[:, 0]], v[tr[:, 2]] - v[tr[:, 0]])
         nrm[sel] = n / n.norm(dim=1, keepdim=True)
     qn = nrm.contiguous()
+    if 0 < args.knn_sample < q.shape[0]:
+        keep = torch.from_numpy(np.sort(np.random.default_rng(6).choice(q.shape[0], size=args.knn_sample,
+                                                                         replace=False))).to(dev)
+        q, qn = q[keep].contiguous(), qn[keep].contiguous()
     direct = pm.export("direct")
     kd = PhotonKDTree(direct["position"], direct["normal"], ctx=ctx)
     # warm-up at the full size, so that the timed call reuses its output buffers
@@ -438,6 +444,19 @@ def photon_bench(args, dev, ctx, measure_cpu):
             t0 = time.perf_counter()
             rkd.knn(qs, qns, 100, 0.05, 0.87, threads=os.cpu_count() or 1)
             kdt = time.perf_counter() - t0
+            # the k-NN roofline: algorithmic bytes per query 32 + 36 N_visited + 8 k
+            # (query in; node and photon per visited point; results out), N_visited
+            # from the instrumented oracle walk (the reference's order) on the sample
+            from oracle.api import Oracle
+            ok_ = Oracle().kdtree(direct["position"], direct["normal"])
+            cnt = ok_.knn(qs, qns, 100, 0.05, 0.87, counters=True, threads=os.cpu_count() or 1)
+            n_vis = float(cnt["visited"].mean())
+            bpq = 32 + 36 * n_vis + 8 * 100
+            achieved = bpq * nq / (knn_ms / 1e3) / 1e9
+            peak, peak_kind = peaks()
+            out["knn"]["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                      "frac": achieved / peak, "bytes_per_query": bpq,
+                                      "visited_per_query": n_vis, "peak_source": peak_kind}
             out["cpu_baseline"] = {
                 "kind": "reference", "cores": os.cpu_count() or 1,
                 "shoot_paths_per_s": paths / rinfo["shoot_s"], "shoot_s_incl_maps": rinfo["shoot_s"],
