@@ -96,10 +96,14 @@ def test_query_scene_against_oracle(gpu, oracle):
     assert frac >= MIN_AGREE
 
 
-def test_host_api_equals_device_api(gpu):
+@pytest.mark.parametrize("n", [50_000, 4_500_001])
+def test_host_api_equals_device_api(gpu, n):
+    """The host-buffer entry points (copies in, query, copies out; above
+    2^21 rays in chunks over two streams) equal the device ones bit for
+    bit, including a ragged last chunk."""
     meshes = sf.small_query_scene()
     lo, hi = scenes.scene_bounds(meshes)
-    rays = scenes.uniform_rays(50_000, lo, hi, seed=53)
+    rays = scenes.uniform_rays(n, lo, hi, seed=53)
     acc = _accel(meshes)
     hd = _gpu_hits(acc, rays)
     hh = acc.intersect(rays)  # numpy -> host-buffer entry point
