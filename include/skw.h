@@ -241,6 +241,10 @@ int skw_nearest(skw_kdtree *tree, const double *q, const double *qn, int64_t nq,
 #define SKW_MATERIAL_PLASTIC 1 /* PlasticMaterial: Lambertian(kd) + Blinn microfacet(ks, 1/roughness), dielectric 1.5 */
 #define SKW_MATERIAL_METAL 2   /* MetalMaterial: Blinn microfacet with a conductor Fresnel (eta, k) */
 #define SKW_MATERIAL_MEASURED 3 /* MERLMeasuredMaterial: a tabulated BRDF (skw_merl) */
+/* TransparentMaterial (Raytracer/Materials/TransparentMaterial.cpp:29-55):
+ * SpecularReflection(kd, FresnelDielectric(refractive_index, 1)) +
+ * SpecularTransmission(ks, refractive_index, 1); kd / ks black = component absent. */
+#define SKW_MATERIAL_TRANSPARENT 4
 
 typedef struct skw_merl skw_merl;
 
@@ -252,6 +256,7 @@ typedef struct skw_material {
   float sigma;        /* matte Oren-Nayar sigma (radians); 0 = Lambertian */
   float eta[3], k[3]; /* metal refractive index and absorption */
   const skw_merl *measured; /* SKW_MATERIAL_MEASURED: the tabulated BRDF (must outlive the scene) */
+  float refractive_index;   /* SKW_MATERIAL_TRANSPARENT: index inside (outside 1), > 0 */
 } skw_material;
 
 /* A measured BRDF in the MERL binary layout (MERLMeasuredData(std::istream&),
@@ -341,6 +346,19 @@ typedef struct skw_medium {
 } skw_medium;
 /* Sets (medium != NULL) or removes (NULL) the scene's medium. */
 int skw_scene_set_medium(skw_scene *scene, const skw_medium *medium);
+
+/* DirectLightingLTEIntegratorParams::m_max_specular_depth
+ * (LTEIntegrators/DirectLightingLTEIntegrator.cpp:48-54): camera rays have
+ * depth 0, and a hit on a SKW_MATERIAL_TRANSPARENT surface reached by a ray
+ * of depth d <= max_depth sends a reflected and a transmitted ray of depth
+ * d + 1 (LTEIntegrator::_SpecularReflect / _SpecularTransmit,
+ * Core/LTEIntegrator.cpp:66-126).  Default 10 (the GUI's default); range
+ * [0, 11]: every branch of every sample's tree is given room, so a render
+ * pass holds at most 2^22 >> (max_depth + 1) camera samples.  Scenes with
+ * specular materials cannot have a medium (SKW_ERR_UNSUPPORTED), and the
+ * adjoint and the photon-map render reject them; photon shooting follows
+ * specular bounces (caustic map). */
+int skw_scene_set_max_specular_depth(skw_scene *scene, int32_t max_depth);
 
 /* ---- Photon maps (PhotonLTEIntegrator, LTEIntegrators/PhotonLTEIntegrator/*).
  *

@@ -46,6 +46,7 @@
 #include <Raytracer/Materials/MatteMaterial.h>
 #include <Raytracer/Materials/PlasticMaterial.h>
 #include <Raytracer/Materials/MetalMaterial.h>
+#include <Raytracer/Materials/TransparentMaterial.h>
 #include <Raytracer/LightSources/DiffuseAreaLightSource.h>
 #include <Raytracer/LightSources/PointLight.h>
 #include <Raytracer/Cameras/PerspectiveCamera.h>
@@ -361,6 +362,7 @@ struct RefMaterialIn {
   float roughness, sigma;
   float eta[3], k[3];
   const void *measured;  // kind 3: a MERLMeasuredData (skw_ref_merl_create)
+  float refractive_index;  // kind 4: TransparentMaterial
 };
 struct RefPrimIn {
   int32_t mesh;
@@ -418,6 +420,11 @@ static intrusive_ptr<const Scene> make_scene(int n_meshes, const float *const *v
                                     intrusive_ptr<const Texture<double>>(new ConstantTexture<double>(M.roughness))));
     } else if (M.kind == 3) {
       mat.reset(new MERLMeasuredMaterial(intrusive_ptr<const MERLMeasuredData>((const MERLMeasuredData *)M.measured)));
+    } else if (M.kind == 4) {
+      mat.reset(new TransparentMaterial(
+          intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.kd[0], M.kd[1], M.kd[2]))),
+          intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.ks[0], M.ks[1], M.ks[2]))),
+          (double)M.refractive_index));
     } else {
       mat.reset(new MetalMaterial(
           intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.eta[0], M.eta[1], M.eta[2]))),

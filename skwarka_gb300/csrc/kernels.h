@@ -66,16 +66,40 @@ struct SceneDev;
 struct ViewDev;
 cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, int n_px, int sppx, int sppy,
                           void *rays, cudaStream_t s);
+// Queues of one specular level (render.cu, SpecArgs): the input level's
+// rays / weights / camera samples / tree nodes / count and the next level's.
+struct SpecQueues {
+  const void *in_rays;
+  const float *in_w;
+  const int *in_sample, *in_node, *in_count;
+  void *out_rays;
+  float *out_w;
+  int *out_sample, *out_node, *out_count;
+  int spec_slot;
+};
+// spec (may be null): queue the specular children of the camera hits into
+// spec->out_* (the scene's max_spec_depth >= 0 and some material is
+// specular).
 cudaError_t launch_shade(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin, int spp,
                          int slots, int n_light_samples, const void *rays, const void *hits, float *contrib,
                          void *srays, int *starget, float *srgb, int *scount, void *brays, int *btarget, float *brgb,
-                         int *bcount, float *bnrm, int block, cudaStream_t s);
+                         int *bcount, float *bnrm, int block, cudaStream_t s, const SpecQueues *spec = nullptr);
+// One specular level: shades entries [0, min(*spec.in_count, capacity)) of
+// spec.in_* (hits: their closest hits) at specular depth `depth`, adding
+// weight x (emission + direct lighting) into each entry's sample slot
+// spec.spec_slot through the shadow / BSDF queues, and queues the children.
+cudaError_t launch_shade_specular(const SceneDev &S, const ViewDev *views, int n_views, int64_t capacity,
+                                  int64_t px_begin, int spp, int slots, int n_light_samples, const SpecQueues &spec,
+                                  int depth, const void *hits, float *contrib, void *srays, int *starget, float *srgb,
+                                  int *scount, void *brays, int *btarget, float *brgb, int *bcount, float *bnrm,
+                                  cudaStream_t s);
 // bnrm: per BSDF-queue entry, the shading normal turned to the viewer (the
 // light-choice density of the light a BSDF ray hits depends on it).
+// accumulate: add into the target slots (specular levels) instead of storing.
 cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                            const int *starget, const float *srgb, const int *scount, const void *brays,
                            const void *bhits, const int *btarget, const float *brgb, const int *bcount,
-                           const float *bnrm, float *contrib, cudaStream_t s);
+                           const float *bnrm, float *contrib, cudaStream_t s, bool accumulate = false);
 // tcam (may be null): per-sample transmittance of the camera ray's medium
 // segment; with it, slot media_slot is the medium's radiance and the others
 // are scaled by the transmittance.
@@ -114,11 +138,12 @@ using TraceFn = std::function<cudaError_t(const void *, int64_t, const int *, vo
 // Workspace bytes of one shooting chunk of n_paths paths.
 size_t photon_chunk_bytes(int64_t n_paths, int max_bounces);
 // Shoots paths [path0, path0 + n_paths): writes the chunk's direct photons
-// (at most n_paths) and indirect photons (at most n_paths * (max_bounces - 1))
-// in path order, and their counts to d_totals[0], d_totals[1].
+// (at most n_paths), indirect photons (at most n_paths * (max_bounces - 1))
+// and caustic photons (at most n_paths) in path order, and their counts to
+// d_totals[0], d_totals[1], d_totals[2].
 cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, const TraceFn &trace, int64_t path0,
                                int n_paths, void *ws, PhotonRec *out_direct, PhotonRec *out_indirect,
-                               int *d_totals, cudaStream_t st);
+                               PhotonRec *out_caustic, int *d_totals, cudaStream_t st);
 // Irradiance estimate of nq points from one map's k-NN output (see
 // k_irradiance_sum); first = this is the first map added.
 cudaError_t launch_irradiance_sum(const void *nodes, const float *weight, const uint16_t *dirid, const double *dirs,

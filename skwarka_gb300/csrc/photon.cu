@@ -13,11 +13,14 @@
 //                    radical inverses in bases 2, 3, 5, 7 and 13, in double
 //   k_trace          closest hit of every live path (traverse.cu)
 //   k_photon_bounce  deposit at the hit (the first hit into the direct map,
-//                    later hits into the indirect map; the caustic map needs
-//                    a specular bounce, which no BSDF here has), BSDF sample
+//                    a later hit of a path that has only scattered
+//                    specularly so far into the caustic map, other later
+//                    hits into the indirect map; no direct or caustic
+//                    deposit on a purely specular surface), BSDF sample
 //                    (radical inverses in bases 17, 19, 23 at the first hit,
-//                    the counter-based generator after it), Russian roulette
-//                    with the luminance ratio, next ray
+//                    the counter-based generator after it; between two
+//                    specular components by their luminance), Russian
+//                    roulette with the luminance ratio, next ray
 //   k_scan_* / k_gather_photons  per-path deposits -> maps in path order
 //
 // The deposits of path i land in fixed staging slots (i, bounce), so the maps
@@ -80,9 +83,73 @@ __device__ __forceinline__ float luminance(V3 c) {
 struct Queue {
   float4 *rays;  // 2 per path
   float *w;      // 3 per path
-  int *path;     // path index within the chunk
+  int *path;     // path index within the chunk | kDiffusePath once a bounce was not specular
   int *count;
 };
+
+constexpr int kDiffusePath = 1 << 30;
+
+// BSDF::Sample over all components of a specular-only (transparent) BSDF
+// (Core/BSDF.cpp:72-117, _SampleSpecularOnly): each component's Sample
+// (SpecularReflection: mirror direction, r F; SpecularTransmission:
+// refracted direction, t (1 - F), black on total internal reflection with the
+// mirror direction), then one of them chosen with probability proportional
+// to its luminance (the 0.999 guard as in the reference); pdf = that
+// probability.  A single component is sampled with pdf 1.
+__device__ V3 specular_sample_photon(const Bsdf &b, V3 inc_w, float uc, V3 &dir, float &pdf) {
+  const V3 wi = b.local(inc_w);
+  const float F = fresnel_dielectric_ior(wi.z, b.ior);
+  const bool has_r = !black(b.kd), has_t = !black(b.ks);
+  const V3 dr = b.world(v3(-wi.x, -wi.y, wi.z));
+  const V3 fr = b.kd * F;
+  V3 dt = dr, ft = v3(0, 0, 0);
+  {
+    float zs = -1.0f, ni = b.ior, no = 1.0f;
+    if (wi.z < 0.0f) {
+      zs = 1.0f;
+      ni = 1.0f;
+      no = b.ior;
+    }
+    const float eta = no / ni;
+    const float st2 = eta * eta * (1.0f - wi.z * wi.z);
+    if (st2 < 1.0f) {
+      dt = b.world(v3(-wi.x * eta, -wi.y * eta, sqrtf(1.0f - st2) * zs));
+      ft = b.ks * (1.0f - F);
+    }
+  }
+  pdf = 1.0f;
+  if (has_r && has_t) {
+    const float lr = 0.05316285f * fr.x + 0.58515348f * fr.y + 0.36168367f * fr.z;
+    const float lt = 0.05316285f * ft.x + 0.58515348f * ft.y + 0.36168367f * ft.z;
+    const float sum = lr + lt;
+    float c = uc * sum;
+    if (c * 0.999f < lr) {
+      pdf = lr / sum;
+      dir = dr;
+      return fr;
+    }
+    c -= lr;
+    if (c * 0.999f < lt) {
+      pdf = lt / sum;
+      dir = dt;
+      return ft;
+    }
+    pdf = 0.0f;
+    dir = dr;
+    return v3(0, 0, 0);
+  }
+  if (has_r) {
+    dir = dr;
+    return fr;
+  }
+  if (has_t) {
+    dir = dt;
+    return ft;
+  }
+  pdf = 0.0f;
+  dir = dr;
+  return v3(0, 0, 0);
+}
 
 __device__ __forceinline__ void queue_push(const Queue &Q, int q, V3 o, V3 d, float tmin, V3 w, int path) {
   Q.rays[2 * q] = make_float4(o.x, o.y, o.z, d.x);
@@ -192,16 +259,19 @@ __global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootAr
                                                        PhotonRec *__restrict__ st_direct,
                                                        uint8_t *__restrict__ has_direct,
                                                        PhotonRec *__restrict__ st_indirect,
-                                                       int *__restrict__ n_indirect) {
+                                                       int *__restrict__ n_indirect,
+                                                       PhotonRec *__restrict__ st_caustic,
+                                                       uint8_t *__restrict__ has_caustic) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = min(n_cap, *in.count);
   bool cont = false;
   V3 o = v3(0, 0, 0), dnew = v3(0, 0, 0), wnew = v3(0, 0, 0);
   float tmin = 0.0f;
-  int path = 0;
+  int path = 0, diffuse_path = 0;
   if (i < n) {
     const int4 hit = hits[i];
-    path = in.path[i];
+    path = in.path[i] & ~kDiffusePath;
+    diffuse_path = in.path[i] & kDiffusePath;
     if (hit.y >= 0) {
       const float4 ra = in.rays[2 * i], rb = in.rays[2 * i + 1];
       const V3 ro = v3(ra.x, ra.y, ra.z), d = v3(ra.w, rb.x, rb.y);
@@ -218,14 +288,27 @@ __global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootAr
       rec.w[2] = w.z;
       rec.dir = compress_dir(inc.x, inc.y, inc.z);
       rec.nrm = compress_dir(h.ng.x, h.ng.y, h.ng.z);
+      const bool specular_bsdf = b.kind == kTransparent;  // no non-specular component
       if (bounce == 0) {
-        st_direct[path] = rec;
-        has_direct[path] = 1;
+        if (!specular_bsdf) {
+          st_direct[path] = rec;
+          has_direct[path] = 1;
+        }
+      } else if (!diffuse_path) {
+        // all bounces so far specular: a caustic photon (at most one per
+        // path: the bounce after it is not specular)
+        if (!specular_bsdf) {
+          st_caustic[path] = rec;
+          has_caustic[path] = 1;
+        }
       } else {
-        st_indirect[(int64_t)path * (A.max_bounces - 1) + (bounce - 1)] = rec;
-        n_indirect[path] = bounce;
+        // indirect photons also land on specular surfaces (the reference's
+        // note at PhotonShootingPipeline.cpp:203-210)
+        const int c = n_indirect[path];
+        st_indirect[(int64_t)path * (A.max_bounces - 1) + c] = rec;
+        n_indirect[path] = c + 1;
       }
-      // BSDF::Sample over all components (none is specular here)
+      // BSDF::Sample over all components
       float uc, u0, u1;
       const uint64_t gp = (uint64_t)(path0 + path);
       if (bounce == 0) {
@@ -240,9 +323,11 @@ __global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootAr
       }
       V3 ex;
       float pdf = 0.0f;
-      const V3 f = bsdf_sample(b, inc, uc, u0, u1, ex, pdf);
+      const V3 f = specular_bsdf ? specular_sample_photon(b, inc, uc, ex, pdf) : bsdf_sample(b, inc, uc, u0, u1, ex, pdf);
       if (pdf > 0.0f && bounce + 1 < A.max_bounces) {
-        wnew = mul(w, f) * (fabsf(dot(ex, b.n)) / pdf);
+        // no cosine for specular scattering: the BxDF holds it (:229-231)
+        wnew = specular_bsdf ? mul(w, f) * (1.0f / pdf) : mul(w, f) * (fabsf(dot(ex, b.n)) / pdf);
+        if (!specular_bsdf) diffuse_path = kDiffusePath;
         float p = A.rr_probability;
         if (!(p > 0.0f)) {
           const float lw = luminance(w);
@@ -260,7 +345,7 @@ __global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootAr
     }
   }
   const int q = queue_append(cont, out.count);
-  if (cont) queue_push(out, q, o, dnew, tmin, wnew, path);
+  if (cont) queue_push(out, q, o, dnew, tmin, wnew, path | diffuse_path);
 }
 
 // Exclusive scan of per-path counts, 1024 per block, then block offsets.
@@ -383,13 +468,13 @@ size_t photon_chunk_bytes(int64_t n_paths, int max_bounces) {
   auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
   const int64_t nb = (n_paths + kScanBlock - 1) / kScanBlock;
   return 2 * (al(n_paths * 32) + al(n_paths * 12) + al(n_paths * 4)) + al(n_paths * 16) + 256 +
-         al(n_paths * 28) + al(n_paths) + al(n_paths * B1 * 28) + al(n_paths * 4) + 2 * al(n_paths * 4) +
-         2 * al(nb * 4) + 256;
+         al(n_paths * 28) + al(n_paths) + al(n_paths * B1 * 28) + al(n_paths * 4) + 3 * al(n_paths * 4) +
+         3 * al(nb * 4) + 256 + al(n_paths * 28) + al(n_paths);
 }
 
 cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, const TraceFn &trace, int64_t path0,
                                int n_paths, void *ws, PhotonRec *out_direct, PhotonRec *out_indirect,
-                               int *d_totals, cudaStream_t st) {
+                               PhotonRec *out_caustic, int *d_totals, cudaStream_t st) {
   const int64_t B1 = A.max_bounces > 1 ? A.max_bounces - 1 : 1;
   auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
   char *p = (char *)ws;
@@ -412,12 +497,16 @@ cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, cons
   uint8_t *has_direct = (uint8_t *)take(al(n_paths));
   PhotonRec *st_indirect = (PhotonRec *)take(al((int64_t)n_paths * B1 * 28));
   int *n_indirect = (int *)take(al((int64_t)n_paths * 4));
-  int *excl[2] = {(int *)take(al((int64_t)n_paths * 4)), (int *)take(al((int64_t)n_paths * 4))};
+  int *excl[3] = {(int *)take(al((int64_t)n_paths * 4)), (int *)take(al((int64_t)n_paths * 4)),
+                  (int *)take(al((int64_t)n_paths * 4))};
   const int nb = (n_paths + kScanBlock - 1) / kScanBlock;
-  int *bsum[2] = {(int *)take(al((int64_t)nb * 4)), (int *)take(al((int64_t)nb * 4))};
+  int *bsum[3] = {(int *)take(al((int64_t)nb * 4)), (int *)take(al((int64_t)nb * 4)), (int *)take(al((int64_t)nb * 4))};
+  PhotonRec *st_caustic = (PhotonRec *)take(al((int64_t)n_paths * 28));
+  uint8_t *has_caustic = (uint8_t *)take(al(n_paths));
   cudaError_t e;
   if ((e = cudaMemsetAsync(counts, 0, 2 * sizeof(int), st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(has_direct, 0, (size_t)n_paths, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(has_caustic, 0, (size_t)n_paths, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(n_indirect, 0, (size_t)n_paths * 4, st)) != cudaSuccess) return e;
   const unsigned grid = (unsigned)((n_paths + 127) / 128);
   k_photon_emit<<<grid, 128, 0, st>>>(S, A, path0, n_paths, Q[0]);
@@ -427,7 +516,7 @@ cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, cons
     if ((e = trace(in.rays, n_paths, in.count, hits, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(out.count, 0, sizeof(int), st)) != cudaSuccess) return e;
     k_photon_bounce<<<grid, 128, 0, st>>>(S, A, path0, b, n_paths, in, hits, out, st_direct, has_direct,
-                                          st_indirect, n_indirect);
+                                          st_indirect, n_indirect, st_caustic, has_caustic);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   // direct: one per path; indirect: n_indirect[path] per path
@@ -438,6 +527,10 @@ cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, cons
   k_scan_sums<<<1, kScanBlock, 0, st>>>(bsum[1], nb, d_totals + 1);
   k_gather_photons<<<grid, 128, 0, st>>>(st_indirect, (int)B1, nullptr, n_indirect, n_paths, excl[1], bsum[1],
                                          out_indirect);
+  // caustic: at most one per path
+  k_scan_blocks<uint8_t><<<nb, kScanBlock, 0, st>>>(has_caustic, n_paths, 1, excl[2], bsum[2]);
+  k_scan_sums<<<1, kScanBlock, 0, st>>>(bsum[2], nb, d_totals + 2);
+  k_gather_photons<<<grid, 128, 0, st>>>(st_caustic, 1, has_caustic, nullptr, n_paths, excl[2], bsum[2], out_caustic);
   return cudaGetLastError();
 }
 

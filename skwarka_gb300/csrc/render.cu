@@ -82,6 +82,38 @@ __global__ void k_camera(const ViewDev *__restrict__ views, int n_views, int64_t
   rays[2 * s + 1] = make_float4((float)dy, (float)dz, 0.0f, __int_as_float(0x7f800000));
 }
 
+// The specular tree of a camera sample (LTEIntegrator::_SpecularReflect /
+// _SpecularTransmit, Core/LTEIntegrator.cpp:66-126, called from
+// DirectLightingLTEIntegrator::_SurfaceRadiance while the ray's specular
+// depth <= m_max_specular_depth): a hit on a specular material sends a
+// reflected and a transmitted ray, each weighted by its BxDF value.  The
+// rays of one depth form a queue (ray, RGB weight, camera sample, node); a
+// node numbers the ray in the sample's binary tree (camera ray 1, children
+// 2k and 2k + 1) and selects its random stream.  Shading a queue entry
+// adds weight x (emission + direct lighting) to the sample's specular slot
+// with atomics (so the last bits of that slot depend on the order).
+struct SpecArgs {
+  // input (SPEC): entries [0, min(*in_count, n)) of a level
+  const float *in_w;
+  const int *in_sample;
+  const int *in_node;
+  const int *in_count;
+  // output: the children of the shaded rays (null out_count: none)
+  float4 *out_rays;
+  float *out_w;
+  int *out_sample;
+  int *out_node;
+  int *out_count;
+  int depth;      // specular depth of the rays shaded here (camera rays: 0)
+  int spec_slot;  // slot of a sample that the specular levels add into
+};
+
+__device__ __forceinline__ void atomic_add_rgb(float *c, int64_t slot, V3 v) {
+  if (v.x != 0.0f) atomicAdd(c + 3 * slot, v.x);
+  if (v.y != 0.0f) atomicAdd(c + 3 * slot + 1, v.y);
+  if (v.z != 0.0f) atomicAdd(c + 3 * slot + 2, v.z);
+}
+
 struct ShadeArgs {
   int n;               // samples in this pass
   int64_t px_begin;    // global pixel of the pass's first sample
@@ -118,33 +150,47 @@ __device__ __forceinline__ void add_emission_grad(double *g, float v) {
 // Per camera hit: emission, light samples, point lights and BSDF samples
 // (DirectLightingLTEIntegrator::_SurfaceRadiance with
 // DirectLightingIntegrator::ComputeDirectLighting).
-template <bool ADJ>
-__global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointArgs J, const float4 *__restrict__ rays,
-                                               const int4 *__restrict__ hits, float *__restrict__ contrib,
-                                               float4 *__restrict__ srays, int *__restrict__ starget,
-                                               float *__restrict__ srgb, int *__restrict__ scount,
-                                               float4 *__restrict__ brays, int *__restrict__ btarget,
-                                               float *__restrict__ brgb, int *__restrict__ bcount,
-                                               float *__restrict__ bnrm) {
+// SPEC = false: the camera rays of a pass (entry i = sample i, each term in
+// its own slot); SPEC = true: a specular level (entry i of the level's
+// queue, every term weighted and added into its sample's specular slot).
+// KIDS: queue the specular children of the shaded hits into Q.out_*.
+template <bool ADJ, bool SPEC, bool KIDS>
+__global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointArgs J, SpecArgs Q,
+                                               const float4 *__restrict__ rays, const int4 *__restrict__ hits,
+                                               float *__restrict__ contrib, float4 *__restrict__ srays,
+                                               int *__restrict__ starget, float *__restrict__ srgb,
+                                               int *__restrict__ scount, float4 *__restrict__ brays,
+                                               int *__restrict__ btarget, float *__restrict__ brgb,
+                                               int *__restrict__ bcount, float *__restrict__ bnrm) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < A.n;
+  const bool valid = SPEC ? i < min(*Q.in_count, A.n) : i < A.n;
   int4 hit = make_int4(0x7f800000, -1, -1, 0);
   float4 ra = make_float4(0, 0, 0, 0), rb = make_float4(0, 0, 0, 0);
+  int si = valid ? i : 0;  // camera sample of the entry
+  unsigned node = 1;       // the entry's node in its sample's specular tree
+  V3 wt = v3(1.0f, 1.0f, 1.0f);
   if (valid) {
     hit = hits[i];
     ra = rays[2 * i];
     rb = rays[2 * i + 1];
+    if (SPEC) {
+      si = Q.in_sample[i];
+      node = (unsigned)Q.in_node[i];
+      wt = load3(Q.in_w + 3 * (int64_t)i);
+    }
   }
   const bool surface = valid && hit.y >= 0;
   const int nl = A.n_light_samples;
-  const int64_t slot0 = (int64_t)i * A.slots;
+  const int64_t slot0 = (int64_t)si * A.slots;
+  const int64_t tslot = slot0 + Q.spec_slot;  // SPEC: every term's slot
   uint64_t gid = 0, seed = 0;
   V3 dI = v3(0, 0, 0);  // adjoint: dL/dI of this sample's pixel / spp
   {
-    const int64_t P = A.px_begin + (valid ? i : 0) / A.spp;
+    const int64_t P = A.px_begin + si / A.spp;
     const int v = find_view(A.views, A.n_views, P);
-    gid = (uint64_t)((P - A.views[v].px_begin) * A.spp + (valid ? i : 0) % A.spp);
+    gid = (uint64_t)((P - A.views[v].px_begin) * A.spp + si % A.spp);
     seed = A.views[v].seed;
+    if (SPEC) seed ^= 0xA0761D6478BD642Full * (uint64_t)node;  // a stream per tree node
     if (ADJ && valid) {
       dI = load3(J.dfilm + 3 * P) * (1.0f / A.spp);
       if (A.tcam) dI = mul(dI, load3(A.tcam + 3 * (int64_t)i));
@@ -166,6 +212,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
     if (li >= 0 && dot(wo, h.ng) > 0.0f) {
       const V3 le = load3(S.area_lights[li].radiance);
       if (ADJ) g_em += dot(dI, le);
+      else if (SPEC) atomic_add_rgb(contrib, tslot, mul(le * escale, wt));
       else store_rgb(contrib, slot0, le * escale);
     }
   }
@@ -231,8 +278,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
         store_rgb(J.s_dkd, q, dkd);
         J.s_dem[q] = dem;
       } else {
-        starget[q] = (int)(slot0 + 1 + k);
-        store_rgb(srgb, q, val);
+        starget[q] = (int)(SPEC ? tslot : slot0 + 1 + k);
+        store_rgb(srgb, q, SPEC ? mul(val, wt) : val);
       }
     }
   }
@@ -264,8 +311,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
         store_rgb(J.s_dkd, q, dkd);
         J.s_dem[q] = 0.0f;
       } else {
-        starget[q] = (int)(slot0 + 1 + nl + k);
-        store_rgb(srgb, q, val);
+        starget[q] = (int)(SPEC ? tslot : slot0 + 1 + nl + k);
+        store_rgb(srgb, q, SPEC ? mul(val, wt) : val);
       }
     }
   }
@@ -291,8 +338,9 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
     const int q = queue_append(want, bcount);
     if (want) {
       store_ray(brays, q, h.p, dir, tmin, __int_as_float(0x7f800000));
-      btarget[q] = ADJ ? h.g : (int)(slot0 + 1 + nl + S.n_point_lights + k);
+      btarget[q] = ADJ ? h.g : (int)(SPEC ? tslot : slot0 + 1 + nl + S.n_point_lights + k);
       if (ADJ) store_rgb(J.b_dkd, q, dkd);
+      if (SPEC) val = mul(val, wt);
       if (bnrm) store_rgb(bnrm, q, n_view);
       brgb[4 * q] = val.x;
       brgb[4 * q + 1] = val.y;
@@ -301,14 +349,35 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
     }
   }
   if (ADJ) add_emission_grad(J.g_emission, g_em);
+  // Specular children (reflection, then transmission) while the depth allows.
+  if (!ADJ && KIDS) {
+    const bool deeper = surface && b.kind == kTransparent && Q.depth <= S.max_spec_depth;
+    for (int c = 0; c < 2; ++c) {
+      V3 dir = v3(0, 0, 0), val = v3(0, 0, 0);
+      const bool want = deeper && (c == 0 ? specular_reflect(b, wo, dir, val) : specular_transmit(b, wo, dir, val));
+      const int q = queue_append(want, Q.out_count);
+      if (want) {
+        store_ray(Q.out_rays, q, h.p, dir, next_min_t(h, dir, S.scene_abs), __int_as_float(0x7f800000));
+        store_rgb(Q.out_w, q, mul(wt, val));
+        Q.out_sample[q] = si;
+        Q.out_node[q] = (int)(2u * node + (unsigned)c);
+      }
+    }
+  }
 }
 
+// accumulate: add into the target (the targets of a specular level repeat)
+// instead of storing.
 __global__ void k_resolve_shadow(const uint8_t *__restrict__ occ, const int *__restrict__ starget,
                                  const float *__restrict__ srgb, const int *__restrict__ scount,
-                                 float *__restrict__ contrib) {
+                                 float *__restrict__ contrib, bool accumulate) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *scount || occ[i]) return;
   const int64_t t = starget[i];
+  if (accumulate) {
+    atomic_add_rgb(contrib, t, v3(srgb[3 * i], srgb[3 * i + 1], srgb[3 * i + 2]));
+    return;
+  }
   contrib[3 * t] = srgb[3 * i];
   contrib[3 * t + 1] = srgb[3 * i + 1];
   contrib[3 * t + 2] = srgb[3 * i + 2];
@@ -320,7 +389,7 @@ __global__ void k_resolve_shadow(const uint8_t *__restrict__ occ, const int *__r
 __global__ void k_resolve_bsdf(SceneDev S, int n_light_samples, const float4 *__restrict__ brays,
                                const int4 *__restrict__ bhits, const int *__restrict__ btarget,
                                const float *__restrict__ brgb, const int *__restrict__ bcount,
-                               const float *__restrict__ bnrm, float *__restrict__ contrib) {
+                               const float *__restrict__ bnrm, float *__restrict__ contrib, bool accumulate) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *bcount) return;
   const int4 hit = bhits[i];
@@ -344,6 +413,12 @@ __global__ void k_resolve_bsdf(SceneDev S, int n_light_samples, const float4 *__
   const int64_t t = btarget[i];
   const float sw = S.emission_scale * w;
   const V3 tr = medium_tr(S.medium, v3(ra.x, ra.y, ra.z), d, rb.z, __int_as_float(hit.x));
+  if (accumulate) {
+    atomic_add_rgb(contrib, t,
+                   v3(brgb[4 * i] * L.radiance[0] * tr.x * sw, brgb[4 * i + 1] * L.radiance[1] * tr.y * sw,
+                      brgb[4 * i + 2] * L.radiance[2] * tr.z * sw));
+    return;
+  }
   contrib[3 * t] = brgb[4 * i] * L.radiance[0] * tr.x * sw;
   contrib[3 * t + 1] = brgb[4 * i + 1] * L.radiance[1] * tr.y * sw;
   contrib[3 * t + 2] = brgb[4 * i + 2] * L.radiance[2] * tr.z * sw;
@@ -630,13 +705,49 @@ cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, i
 cudaError_t launch_shade(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin, int spp,
                          int slots, int n_light_samples, const void *rays, const void *hits, float *contrib,
                          void *srays, int *starget, float *srgb, int *scount, void *brays, int *btarget, float *brgb,
-                         int *bcount, float *bnrm, int block, cudaStream_t s) {
+                         int *bcount, float *bnrm, int block, cudaStream_t s, const SpecQueues *spec) {
   if (n <= 0) return cudaSuccess;
   if (block != 64) block = 128;
   ShadeArgs A{n, px_begin, spp, slots, n_light_samples, views, n_views, nullptr};
-  k_shade<false><<<(unsigned)((n + block - 1) / block), (unsigned)block, 0, s>>>(
-      S, A, AdjointArgs{}, (const float4 *)rays, (const int4 *)hits, contrib, (float4 *)srays, starget, srgb, scount,
-      (float4 *)brays, btarget, brgb, bcount, bnrm);
+  SpecArgs Q{};
+  if (spec) {
+    Q.out_rays = (float4 *)spec->out_rays;
+    Q.out_w = spec->out_w;
+    Q.out_sample = spec->out_sample;
+    Q.out_node = spec->out_node;
+    Q.out_count = spec->out_count;
+    Q.depth = 0;
+    Q.spec_slot = spec->spec_slot;
+  }
+  if (spec)
+    k_shade<false, false, true><<<(unsigned)((n + block - 1) / block), (unsigned)block, 0, s>>>(
+        S, A, AdjointArgs{}, Q, (const float4 *)rays, (const int4 *)hits, contrib, (float4 *)srays, starget, srgb,
+        scount, (float4 *)brays, btarget, brgb, bcount, bnrm);
+  else
+    k_shade<false, false, false><<<(unsigned)((n + block - 1) / block), (unsigned)block, 0, s>>>(
+        S, A, AdjointArgs{}, Q, (const float4 *)rays, (const int4 *)hits, contrib, (float4 *)srays, starget, srgb,
+        scount, (float4 *)brays, btarget, brgb, bcount, bnrm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade_specular(const SceneDev &S, const ViewDev *views, int n_views, int64_t capacity,
+                                  int64_t px_begin, int spp, int slots, int n_light_samples, const SpecQueues &spec,
+                                  int depth, const void *hits, float *contrib, void *srays, int *starget, float *srgb,
+                                  int *scount, void *brays, int *btarget, float *brgb, int *bcount, float *bnrm,
+                                  cudaStream_t s) {
+  if (capacity <= 0) return cudaSuccess;
+  ShadeArgs A{(int)capacity, px_begin, spp, slots, n_light_samples, views, n_views, nullptr};
+  SpecArgs Q{spec.in_w,      spec.in_sample, spec.in_node,  spec.in_count, (float4 *)spec.out_rays,
+             spec.out_w,     spec.out_sample, spec.out_node, spec.out_count, depth,
+             spec.spec_slot};
+  if (spec.out_count)
+    k_shade<false, true, true><<<(unsigned)((capacity + 127) / 128), 128, 0, s>>>(
+        S, A, AdjointArgs{}, Q, (const float4 *)spec.in_rays, (const int4 *)hits, contrib, (float4 *)srays, starget,
+        srgb, scount, (float4 *)brays, btarget, brgb, bcount, bnrm);
+  else
+    k_shade<false, true, false><<<(unsigned)((capacity + 127) / 128), 128, 0, s>>>(
+        S, A, AdjointArgs{}, Q, (const float4 *)spec.in_rays, (const int4 *)hits, contrib, (float4 *)srays, starget,
+        srgb, scount, (float4 *)brays, btarget, brgb, bcount, bnrm);
   return cudaGetLastError();
 }
 
@@ -648,9 +759,9 @@ cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_
   if (n <= 0) return cudaSuccess;
   ShadeArgs A{n, px_begin, spp, 0, n_light_samples, views, n_views, tcam};
   AdjointArgs J{dfilm, g_albedo, g_emission, s_dkd, s_dem, b_dkd};
-  k_shade<true><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, A, J, (const float4 *)rays, (const int4 *)hits,
-                                                             nullptr, (float4 *)srays, stri, nullptr, scount,
-                                                             (float4 *)brays, btri, brgb, bcount, bnrm);
+  k_shade<true, false, false><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
+      S, A, J, SpecArgs{}, (const float4 *)rays, (const int4 *)hits, nullptr, (float4 *)srays, stri, nullptr, scount,
+      (float4 *)brays, btri, brgb, bcount, bnrm);
   return cudaGetLastError();
 }
 
@@ -672,12 +783,12 @@ cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_
 cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                            const int *starget, const float *srgb, const int *scount, const void *brays,
                            const void *bhits, const int *btarget, const float *brgb, const int *bcount,
-                           const float *bnrm, float *contrib, cudaStream_t s) {
+                           const float *bnrm, float *contrib, cudaStream_t s, bool accumulate) {
   if (capacity <= 0) return cudaSuccess;
   const unsigned grid = (unsigned)((capacity + 255) / 256);
-  k_resolve_shadow<<<grid, 256, 0, s>>>(occ, starget, srgb, scount, contrib);
+  k_resolve_shadow<<<grid, 256, 0, s>>>(occ, starget, srgb, scount, contrib, accumulate);
   k_resolve_bsdf<<<grid, 256, 0, s>>>(S, n_light_samples, (const float4 *)brays, (const int4 *)bhits, btarget, brgb,
-                                      bcount, bnrm, contrib);
+                                      bcount, bnrm, contrib, accumulate);
   return cudaGetLastError();
 }
 

@@ -101,6 +101,7 @@ struct Bsdf {
   float exponent, on_a, on_b;
   V3 eta, k2;
   MerlDev merl;
+  float ior;  // kTransparent
   __device__ __forceinline__ V3 local(V3 w) const { return v3(dot(w, e1), dot(w, e2), dot(w, n)); }
   __device__ __forceinline__ V3 world(V3 l) const { return e1 * l.x + e2 * l.y + n * l.z; }
   __device__ __forceinline__ int components() const { return kind == kPlastic ? 2 : 1; }
@@ -294,6 +295,7 @@ __device__ V3 merl_sample(const MerlDev &m, V3 wi, float u0, float u1, V3 &wo, f
 // BSDF::Evaluate (Core/BSDF.cpp:22-40): every component is a reflection, so
 // directions on opposite sides of the geometric normal give zero.
 __device__ V3 bsdf_eval(const Bsdf &b, V3 wi_w, V3 wo_w) {
+  if (b.kind == kTransparent) return v3(0, 0, 0);  // specular only: delta components evaluate to 0
   if (!(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f)) return v3(0, 0, 0);
   const V3 wi = b.local(wi_w), wo = b.local(wo_w);
   if (b.kind == kMetal) return microfacet_eval(b, wi, wo);
@@ -306,7 +308,8 @@ __device__ V3 bsdf_eval(const Bsdf &b, V3 wi_w, V3 wo_w) {
 // The derivative of bsdf_eval with respect to kd (per channel): the diffuse
 // component evaluated with kd = 1 (zero for metal, whose BSDF has no kd).
 __device__ V3 bsdf_eval_dkd(const Bsdf &b, V3 wi_w, V3 wo_w) {
-  if (b.kind == kMetal || !(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f)) return v3(0, 0, 0);
+  if (b.kind == kMetal || b.kind == kTransparent || !(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f))
+    return v3(0, 0, 0);
   Bsdf u = b;
   u.kd = v3(1.0f, 1.0f, 1.0f);
   return diffuse_eval(u, b.local(wi_w), b.local(wo_w));
@@ -314,6 +317,7 @@ __device__ V3 bsdf_eval_dkd(const Bsdf &b, V3 wi_w, V3 wo_w) {
 
 // BSDF::PDF (Core/BSDF.cpp:42-58): average of the component densities.
 __device__ float bsdf_pdf(const Bsdf &b, V3 wi_w, V3 wo_w) {
+  if (b.kind == kTransparent) return 0.0f;
   const V3 wi = b.local(wi_w), wo = b.local(wo_w);
   if (b.kind == kMetal) return microfacet_pdf(b, wi, wo);
   if (b.kind == kMeasured) return merl_pdf(b.merl, wi, wo);
@@ -325,6 +329,11 @@ __device__ float bsdf_pdf(const Bsdf &b, V3 wi_w, V3 wo_w) {
 // pick a component uniformly, sample it, average the densities of all
 // components at the sampled direction, evaluate the whole BSDF.
 __device__ V3 bsdf_sample(const Bsdf &b, V3 wi_w, float uc, float u0, float u1, V3 &wo_w, float &pdf) {
+  if (b.kind == kTransparent) {  // no non-specular component to sample
+    pdf = 0.0f;
+    wo_w = wi_w;
+    return v3(0, 0, 0);
+  }
   const V3 wi = b.local(wi_w);
   if (b.kind == kMeasured) {  // the single MERLMeasured component (BSDF.cpp:110-168)
     V3 wo;
@@ -406,7 +415,67 @@ __device__ Bsdf make_bsdf(const SceneDev &S, const Hit &h, int prim) {
   b.eta = load3(m.eta);
   b.k2 = load3(m.k2);
   b.merl = m.merl;
+  b.ior = m.ior;
   return b;
+}
+
+// --------------------------------------------------------------- specular --
+// FresnelDielectric(inner, 1)::operator() (Core/Fresnel.h:96-124).
+__device__ __forceinline__ float fresnel_dielectric_ior(float c, float inner) {
+  c = fminf(1.0f, fmaxf(-1.0f, c));
+  float ni = inner, no = 1.0f;
+  if (c < 0.0f) {
+    ni = 1.0f;
+    no = inner;
+  }
+  const float st = no / ni * sqrtf(fmaxf(0.0f, 1.0f - c * c));
+  if (st >= 1.0f) return 1.0f;
+  const float ct = sqrtf(fmaxf(0.0f, 1.0f - st * st));
+  c = fabsf(c);
+  const float rpar = (ni * c - no * ct) / (ni * c + no * ct);
+  const float rper = (no * c - ni * ct) / (no * c + ni * ct);
+  return (rpar * rpar + rper * rper) * 0.5f;
+}
+
+// LTEIntegrator::_SpecularReflect (Core/LTEIntegrator.cpp:66-92) with
+// SpecularReflection<FresnelDielectric>::Sample (BxDFs/SpecularReflection.h):
+// the mirror direction of wo (towards the viewer) about the shading normal
+// and its weight r * F(cos) -- no cosine and no density, the BxDF accounts
+// for both.  False when the material has no reflection component, the
+// weight is black or the direction grazes the shading plane.
+__device__ __forceinline__ bool specular_reflect(const Bsdf &b, V3 wo_w, V3 &dir, V3 &val) {
+  if (b.kind != kTransparent || black(b.kd)) return false;
+  const V3 wi = b.local(wo_w);
+  dir = b.world(v3(-wi.x, -wi.y, wi.z));
+  val = b.kd * fresnel_dielectric_ior(wi.z, b.ior);
+  return !black(val) && fabsf(dot(dir, b.n)) > kEps;
+}
+
+// LTEIntegrator::_SpecularTransmit (LTEIntegrator.cpp:94-126) with
+// SpecularTransmission::Sample (BxDFs/SpecularTransmission.cpp:33-66): the
+// refracted direction (Snell's law, the indices swapped when wo is inside),
+// its weight t * (1 - F(cos)) * eta^2 (eta = 1/ior entering, ior leaving);
+// false on total internal reflection (black weight), at normal-grazing
+// incidence, or when the material has no transmission component.
+__device__ __forceinline__ bool specular_transmit(const Bsdf &b, V3 wo_w, V3 &dir, V3 &val) {
+  if (b.kind != kTransparent || black(b.ks)) return false;
+  const float cn = dot(wo_w, b.n);
+  if (fabsf(cn) < kEps) return false;
+  const V3 wi = b.local(wo_w);
+  float zs = -1.0f, ni = b.ior, no = 1.0f;
+  if (wi.z < 0.0f) {
+    zs = 1.0f;
+    ni = 1.0f;
+    no = b.ior;
+  }
+  const float eta = no / ni;
+  const float st2 = eta * eta * (1.0f - wi.z * wi.z);
+  if (st2 >= 1.0f) return false;
+  const float ct = sqrtf(1.0f - st2);
+  dir = b.world(v3(-wi.x * eta, -wi.y * eta, ct * zs));
+  const float e = cn > 0.0f ? 1.0f / b.ior : b.ior;
+  val = b.ks * ((1.0f - fresnel_dielectric_ior(wi.z, b.ior)) * (e * e));
+  return !black(val) && fabsf(dot(dir, b.n)) > kEps;
 }
 
 __device__ Hit make_hit(const SceneDev &S, V3 o, V3 d, float t, int prim, int tri) {

@@ -10,10 +10,12 @@
 
 namespace skw {
 
-enum BsdfKind : int32_t { kLambert = 0, kOrenNayar = 1, kPlastic = 2, kMetal = 3, kMeasured = 4 };
+enum BsdfKind : int32_t { kLambert = 0, kOrenNayar = 1, kPlastic = 2, kMetal = 3, kMeasured = 4, kTransparent = 5 };
 
 // Material constants after the reference's clamps (MatteMaterial.cpp:29-50,
-// PlasticMaterial.cpp:33-53, MetalMaterial.cpp:58-101).
+// PlasticMaterial.cpp:33-53, MetalMaterial.cpp:58-101).  kTransparent
+// (TransparentMaterial.cpp:29-55): kd = specular reflectance, ks = specular
+// transmittance (both clamped to [0, 1]), ior = refractive index inside.
 struct DevMaterial {
   int32_t kind;
   float kd[3];
@@ -22,6 +24,7 @@ struct DevMaterial {
   float on_a, on_b;    // Oren-Nayar A, B
   float eta[3], k2[3]; // conductor refractive index and squared absorption
   MerlDev merl;        // kMeasured: the tabulated BRDF
+  float ior;           // kTransparent: refractive index (outside: 1)
 };
 
 struct AreaLight {
@@ -76,6 +79,8 @@ struct SceneDev {
   float scene_abs;                // largest absolute vertex coordinate
   float emission_scale;           // multiplies every area light's radiance
   MediumDev medium;
+  int32_t has_specular;           // some primitive has a kTransparent material
+  int32_t max_spec_depth;         // DirectLightingLTEIntegratorParams::m_max_specular_depth
 };
 
 struct CameraDev {

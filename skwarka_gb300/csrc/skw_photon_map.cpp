@@ -317,38 +317,44 @@ int skw_photon_shoot(skw_scene *s, const skw_photon_params *params, skw_photon_m
   const int64_t chunk = std::min<int64_t>(params->paths, (int64_t)1 << 20);
   const int64_t B1 = std::max(params->max_bounces - 1, 1);
   void *ws = nullptr;
-  PhotonRec *d_dir = nullptr, *d_ind = nullptr;
+  PhotonRec *d_dir = nullptr, *d_ind = nullptr, *d_cau = nullptr;
   int *d_tot = nullptr;
   cudaStream_t st = nullptr;
   e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&ws, skw::photon_chunk_bytes(chunk, params->max_bounces));
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_dir, (size_t)chunk * sizeof(PhotonRec));
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_ind, (size_t)(chunk * B1) * sizeof(PhotonRec));
-  if (e == cudaSuccess) e = cudaMalloc(&d_tot, 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_cau, (size_t)chunk * sizeof(PhotonRec));
+  if (e == cudaSuccess) e = cudaMalloc(&d_tot, 3 * sizeof(int));
   auto *pm = new (std::nothrow) skw_photon_map();
   if (!pm) e = cudaErrorMemoryAllocation;
   int64_t launches = 0;
   for (int64_t p0 = 0; p0 < params->paths && e == cudaSuccess; p0 += chunk) {
     const int n = (int)std::min(chunk, params->paths - p0);
-    e = skw::photon_shoot_chunk(S, A, trace, p0, n, ws, d_dir, d_ind, d_tot, st);
-    int tot[2] = {0, 0};
+    e = skw::photon_shoot_chunk(S, A, trace, p0, n, ws, d_dir, d_ind, d_cau, d_tot, st);
+    int tot[3] = {0, 0, 0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(tot, d_tot, sizeof(tot), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) break;
-    Map &dm = pm->maps[1], &im = pm->maps[2];
-    const size_t od = dm.input.size(), oi = im.input.size();
+    Map &cm = pm->maps[0], &dm = pm->maps[1], &im = pm->maps[2];
+    const size_t oc = cm.input.size(), od = dm.input.size(), oi = im.input.size();
+    cm.input.resize(oc + (size_t)tot[2]);
     dm.input.resize(od + (size_t)tot[0]);
     im.input.resize(oi + (size_t)tot[1]);
     if (tot[0] > 0) e = cudaMemcpy(dm.input.data() + od, d_dir, (size_t)tot[0] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && tot[1] > 0)
       e = cudaMemcpy(im.input.data() + oi, d_ind, (size_t)tot[1] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && tot[2] > 0)
+      e = cudaMemcpy(cm.input.data() + oc, d_cau, (size_t)tot[2] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
+    cm.paths += n;
     dm.paths += n;
     im.paths += n;
-    launches += 1 + 2 * params->max_bounces + 6;
+    launches += 1 + 2 * params->max_bounces + 9;
   }
   cudaFree(ws);
   cudaFree(d_dir);
   cudaFree(d_ind);
+  cudaFree(d_cau);
   cudaFree(d_tot);
   cudaFree(d_lights);
   if (e != cudaSuccess) {
@@ -366,8 +372,8 @@ int skw_photon_shoot(skw_scene *s, const skw_photon_params *params, skw_photon_m
       skw_photon_map_destroy(pm);
       return fail(ctx, SKW_ERR_BUDGET, "a photon map exceeds 40M photons (the reference's MAX_PHOTONS_IN_MAP)");
     }
-  if (pm->maps[1].input.empty()) pm->maps[1].paths = 0;
-  if (pm->maps[2].input.empty()) pm->maps[2].paths = 0;
+  for (int i = 0; i < 3; ++i)
+    if (pm->maps[i].input.empty()) pm->maps[i].paths = 0;
   int rc = finish_map(pm, st);
   cudaStreamDestroy(st);
   if (rc != SKW_OK) {

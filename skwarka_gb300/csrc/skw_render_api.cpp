@@ -272,6 +272,13 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
       }
       d.kind = skw::kMeasured;
       d.merl = skw_merl_device_view(m.measured);
+    } else if (m.kind == SKW_MATERIAL_TRANSPARENT) {
+      if (!(m.refractive_index > 0.0f)) {  // TransparentMaterial.cpp:22-27 asserts a positive index
+        skw_scene_destroy(s);
+        return fail(ctx, SKW_ERR_ARG, "a transparent material needs a positive refractive index");
+      }
+      d.kind = skw::kTransparent;  // kd: reflectance, ks: transmittance (clamped above)
+      d.ior = m.refractive_index;
     } else {
       skw_scene_destroy(s);
       return fail(ctx, SKW_ERR_UNSUPPORTED, "unknown material kind");
@@ -305,6 +312,10 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
   D.n_area_lights = (int32_t)lights.size();
   D.n_point_lights = n_point_lights;
   D.emission_scale = 1.0f;
+  D.has_specular = 0;
+  for (int32_t p = 0; p < n_prims; ++p)
+    if (mats[(size_t)prims[p].material].kind == skw::kTransparent) D.has_specular = 1;
+  D.max_spec_depth = 10;  // the GUI's DirectLightParams / PhotonMapParams default
   s->n_triangles = tri_count;
   D.scene_abs = s->accel->scene_abs;
   *out = s;
@@ -340,7 +351,14 @@ struct PassConfig {
   int overlap = 0;
   int extra_slots = 0;       // contribution slots after the direct-lighting ones (final gather)
   bool media = true;         // march the scene's medium (if any) along the camera rays (one more slot, last)
+  bool specular = true;      // follow specular reflection / transmission (if the scene has such materials)
 };
+
+// Entries of the largest specular level of a pass (the pass is sized so
+// that every branch of every sample's specular tree fits).
+constexpr int64_t kSpecEntries = (int64_t)1 << 22;
+// Deepest specular depth: a sample's tree then holds up to 2^12 - 1 rays.
+constexpr int kMaxSpecDepth = 11;
 
 struct Plan {
   std::vector<skw::ViewDev> views;
@@ -350,6 +368,9 @@ struct Plan {
   bool media = false;
   int media_slot = 0;
   int64_t cap_media = 0;  // media light-sample queue: cap_samples * max_steps
+  int spec_levels = 0;    // specular depths traced after the camera rays (0: none)
+  int spec_slot = 0;
+  int64_t cap_spec = 0;   // entries of a specular level buffer: cap_samples << spec_levels
   PassConfig cfg;
 };
 
@@ -364,6 +385,10 @@ struct Workspace {
   void *mrays = nullptr;
   int *mtarget = nullptr;
   uint8_t *mocc = nullptr;
+  // specular levels: two ping-pong queues and the hits of the level traced
+  void *qrays[2] = {nullptr, nullptr}, *qhits = nullptr;
+  float *qw[2] = {nullptr, nullptr};
+  int *qsample[2] = {nullptr, nullptr}, *qnode[2] = {nullptr, nullptr};
 };
 
 inline size_t al256(int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); }
@@ -372,9 +397,11 @@ size_t workspace_bytes(const Plan &P) {
   const int64_t cs = P.cap_samples, sh = std::max<int64_t>(P.cap_shadow, 1), bs = std::max<int64_t>(P.cap_bsdf, 1);
   const int64_t cm = std::max<int64_t>(P.cap_media, 1);
   const size_t media = P.media ? al256(cs * 12) + al256(cm * 32) + al256(cm * 4) + 2 * al256(cm * 12) + al256(cm) : 0;
+  const int64_t cq = P.cap_spec;
+  const size_t spec = P.spec_levels ? 2 * (al256(cq * 32) + al256(cq * 12) + 2 * al256(cq * 4)) + al256(cq * 16) : 0;
   return al256(cs * 32) + al256(cs * 16) + al256(cs * P.slots * 12) + al256(sh * 32) + al256(sh * 4) +
          al256(sh * 12) + al256(sh) + al256(bs * 32) + al256(bs * 4) + al256(bs * 16) + al256(bs * 16) + 256 + media +
-         al256(bs * 12);
+         al256(bs * 12) + spec;
 }
 
 void workspace_carve(const Plan &P, char *base, Workspace *W) {
@@ -396,7 +423,7 @@ void workspace_carve(const Plan &P, char *base, Workspace *W) {
   W->btarget = (int *)take(al256(bs * 4));
   W->brgb = (float *)take(al256(bs * 16));
   W->bhits = take(al256(bs * 16));
-  W->counts = (int *)take(256);  // [0] shadow queue length, [1] BSDF queue length, [2] media queue length
+  W->counts = (int *)take(256);  // [0] shadow, [1] BSDF, [2] media queue length, [3], [4] specular levels
   W->bnrm = (float *)take(al256(bs * 12));
   if (P.media) {
     const int64_t cm = std::max<int64_t>(P.cap_media, 1);
@@ -406,6 +433,16 @@ void workspace_carve(const Plan &P, char *base, Workspace *W) {
     W->mval = (float *)take(al256(cm * 12));
     W->mdem = (float *)take(al256(cm * 12));
     W->mocc = (uint8_t *)take(al256(cm));
+  }
+  if (P.spec_levels) {
+    const int64_t cq = P.cap_spec;
+    for (int k = 0; k < 2; ++k) {
+      W->qrays[k] = take(al256(cq * 32));
+      W->qw[k] = (float *)take(al256(cq * 12));
+      W->qsample[k] = (int *)take(al256(cq * 4));
+      W->qnode[k] = (int *)take(al256(cq * 4));
+    }
+    W->qhits = take(al256(cq * 16));
   }
 }
 
@@ -447,20 +484,29 @@ int plan_make(skw_scene *s, const skw_camera *cams, int n_views, const skw_rende
   P->nl = params->light_samples;
   P->npl = s->dev.n_point_lights;
   P->media = cfg.media && s->dev.medium.on;
-  P->slots = 1 + 2 * P->nl + P->npl + cfg.extra_slots + (P->media ? 1 : 0);
+  P->spec_levels = cfg.specular && s->dev.has_specular ? s->dev.max_spec_depth + 1 : 0;
+  if (P->media && P->spec_levels)
+    return fail(ctx, SKW_ERR_UNSUPPORTED, "a participating medium together with specular materials");
+  P->slots = 1 + 2 * P->nl + P->npl + cfg.extra_slots + (P->spec_levels ? 1 : 0) + (P->media ? 1 : 0);
   P->media_slot = P->slots - 1;
+  P->spec_slot = P->slots - 1 - (P->media ? 1 : 0);
   P->n_px_total = px;
   P->cfg = cfg;
   if (P->cfg.stack_cap == 0) P->cfg.stack_cap = s->accel->stack_cap;
   int64_t per_pass = cfg.samples_per_pass;
   if (P->media)  // the media queue holds max_steps light samples per camera ray: at most 2^25 per pass
     per_pass = std::min<int64_t>(per_pass, std::max<int64_t>(((int64_t)1 << 25) / s->dev.medium.max_steps, 1));
+  if (P->spec_levels)  // every sample's full specular tree fits the largest level's queue
+    per_pass = std::min<int64_t>(per_pass, std::max<int64_t>(kSpecEntries >> P->spec_levels, 1));
   P->chunk_px = std::max<int64_t>(1, std::min<int64_t>(px, per_pass / P->spp));
   P->cap_samples = P->chunk_px * P->spp;
   P->cap_media = P->media ? P->cap_samples * s->dev.medium.max_steps : 0;
-  P->cap_shadow = P->cap_samples * (P->nl + P->npl);
-  P->cap_bsdf = P->cap_samples * P->nl;
-  if (P->cap_shadow > INT32_MAX / 2 || P->cap_samples > INT32_MAX / 2 || P->cap_samples * P->slots * 3 > ((int64_t)1 << 40))
+  P->cap_spec = P->spec_levels ? P->cap_samples << P->spec_levels : 0;
+  const int64_t shaded = std::max(P->cap_samples, P->cap_spec);  // entries of the largest shade launch
+  P->cap_shadow = shaded * (P->nl + P->npl);
+  P->cap_bsdf = shaded * P->nl;
+  if (P->cap_shadow > INT32_MAX / 2 || P->cap_bsdf > INT32_MAX / 2 || P->cap_samples > INT32_MAX / 2 ||
+      P->cap_samples * P->slots * 3 > ((int64_t)1 << 40))
     return fail(ctx, SKW_ERR_ARG, "render pass too large");
   return SKW_OK;
 }
@@ -484,6 +530,57 @@ cudaError_t record_media(skw_scene *s, const Plan &P, const Workspace &W, const 
   return e;
 }
 
+// The specular levels of a pass (after the camera level queued its
+// children in queue 0): level L (1 .. spec_levels) holds at most n << L
+// rays; each is traced, shaded (emission and direct lighting added into its
+// sample's specular slot) and queues its children while L <= the scene's
+// max_spec_depth.
+cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
+                            int n, cudaStream_t st) {
+  skw_accel *a = s->accel;
+  const int nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
+  cudaError_t e = cudaSuccess;
+  for (int L = 1; L <= P.spec_levels; ++L) {
+    const int qi = (L - 1) & 1, qo = L & 1;
+    const int64_t cl = (int64_t)n << L;
+    skw::SpecQueues q{};
+    q.in_rays = W.qrays[qi];
+    q.in_w = W.qw[qi];
+    q.in_sample = W.qsample[qi];
+    q.in_node = W.qnode[qi];
+    q.in_count = W.counts + 3 + qi;
+    q.spec_slot = P.spec_slot;
+    if (L < P.spec_levels) {  // depth L <= max_spec_depth: children go to the next level
+      q.out_rays = W.qrays[qo];
+      q.out_w = W.qw[qo];
+      q.out_sample = W.qsample[qo];
+      q.out_node = W.qnode[qo];
+      q.out_count = W.counts + 3 + qo;
+      if ((e = cudaMemsetAsync(W.counts + 3 + qo, 0, sizeof(int), st)) != cudaSuccess) return e;
+    }
+    if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) return e;
+    if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.qrays[qi], cl, W.counts + 3 + qi, a->scene_abs,
+                                   nullptr, W.qhits, a->d_status, st, ctas)) != cudaSuccess)
+      return e;
+    if ((e = skw::launch_shade_specular(s->dev, d_views, nv, cl, px0, P.spp, P.slots, P.nl, q, L, W.qhits, W.contrib,
+                                        W.srays, W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb,
+                                        W.counts + 1, W.bnrm, st)) != cudaSuccess)
+      return e;
+    const int64_t csh = cl * (P.nl + P.npl), cbs = cl * P.nl;
+    if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts,
+                                              a->scene_abs, nullptr, W.occ, a->d_status, st, ctas)) != cudaSuccess)
+      return e;
+    if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
+                                              a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas)) != cudaSuccess)
+      return e;
+    if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
+                                 W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st, true)) !=
+        cudaSuccess)
+      return e;
+  }
+  return e;
+}
+
 // The direct-lighting stages of one pass over global pixels
 // [px0, px0 + n_px): every slot of contrib but the extra ones is filled.
 cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
@@ -492,15 +589,24 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
   const int n = n_px * P.spp, nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
   cudaError_t e;
   if ((e = cudaMemsetAsync(W.contrib, 0, (size_t)n * P.slots * 12, st)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(W.counts, 0, 3 * sizeof(int), st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(W.counts, 0, 5 * sizeof(int), st)) != cudaSuccess) return e;
   if ((e = skw::launch_camera(d_views, nv, px0, n_px, P.sppx, P.sppy, W.rays, st)) != cudaSuccess) return e;
   if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr, W.hits,
                                  a->d_status, st, ctas)) != cudaSuccess)
     return e;
   if (P.media && (e = record_media(s, P, W, d_views, px0, n, false, nullptr, nullptr, st)) != cudaSuccess) return e;
+  skw::SpecQueues sq{};
+  if (P.spec_levels) {
+    sq.out_rays = W.qrays[0];
+    sq.out_w = W.qw[0];
+    sq.out_sample = W.qsample[0];
+    sq.out_node = W.qnode[0];
+    sq.out_count = W.counts + 3;
+    sq.spec_slot = P.spec_slot;
+  }
   if ((e = skw::launch_shade(s->dev, d_views, nv, n, px0, P.spp, P.slots, P.nl, W.rays, W.hits, W.contrib, W.srays,
                              W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb, W.counts + 1, W.bnrm,
-                             P.cfg.shade_block, st)) != cudaSuccess)
+                             P.cfg.shade_block, st, P.spec_levels ? &sq : nullptr)) != cudaSuccess)
     return e;
   const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
   if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts, a->scene_abs,
@@ -509,8 +615,10 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
   if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
                                             a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas)) != cudaSuccess)
     return e;
-  return skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
-                             W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st);
+  if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
+                               W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st)) != cudaSuccess)
+    return e;
+  return record_specular(s, P, W, d_views, px0, n, st);
 }
 
 // One pass: direct lighting, then the film.
@@ -522,6 +630,10 @@ cudaError_t record_pass(skw_scene *s, const Plan &P, const Workspace &W, const s
 }
 
 constexpr int kLaunchesPerPass = 8;
+
+// Kernel launches of one pass: the direct-lighting stages, 6 per specular
+// level (traversal, shade, two traversals, two resolves) and 3 for a medium.
+int64_t launches_per_pass(const Plan &P) { return kLaunchesPerPass + 6 * P.spec_levels + (P.media ? 3 : 0); }
 
 int64_t n_passes(const Plan &P) { return (P.n_px_total + P.chunk_px - 1) / P.chunk_px; }
 
@@ -639,7 +751,7 @@ int batch_launch(skw_render_batch *b, float *films, cudaStream_t stream) {
   if ((e = cudaGraphLaunch(b->exec, b->own)) != cudaSuccess) return cuda_fail(ctx, e, "graph launch");
   if ((e = cudaEventRecord(b->ev_out, b->own)) != cudaSuccess) return cuda_fail(ctx, e, "batch run");
   if ((e = cudaStreamWaitEvent(stream, b->ev_out, 0)) != cudaSuccess) return cuda_fail(ctx, e, "batch run");
-  ctx->launches.fetch_add(n_passes(b->plan) * kLaunchesPerPass);
+  ctx->launches.fetch_add(n_passes(b->plan) * launches_per_pass(b->plan));
   return SKW_OK;
 }
 
@@ -693,7 +805,7 @@ int skw_render_direct(skw_scene *s, const skw_camera *cam, const skw_render_para
   if (e == cudaSuccess) e = record_all(s, P, &W, 1, d_view, film_rgb, st, nullptr, nullptr, nullptr);
   cudaFreeAsync(w, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "direct-lighting render");
-  ctx->launches.fetch_add(n_passes(P) * kLaunchesPerPass);
+  ctx->launches.fetch_add(n_passes(P) * launches_per_pass(P));
   return SKW_OK;
 }
 
@@ -879,6 +991,8 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
   if (!s || !cam || !params || !d_film || !g_albedo || !g_emission)
     return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "null argument");
   skw_ctx *ctx = s->ctx;
+  if (s->dev.has_specular)
+    return fail(ctx, SKW_ERR_UNSUPPORTED, "the adjoint covers diffuse / glossy materials, not specular ones");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
   Plan P;
@@ -948,6 +1062,8 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   const bool caustic = pm->maps[0].n > 0 && pp->caustic_lookup > 0;
   if (caustic && !(pp->max_caustic_dist > 0.0))
     return fail(ctx, SKW_ERR_ARG, "max_caustic_dist must be positive");
+  if (s->dev.has_specular)
+    return fail(ctx, SKW_ERR_UNSUPPORTED, "the photon-map render follows no specular paths (shooting does)");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
   // the sampler rounds sequence lengths up to squares (Sampler.cpp:39-57, StratifiedSampler.cpp:33-37)
@@ -1020,7 +1136,7 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
                                             W.hits, cws, W.contrib, pm->d_status, st)) != cudaSuccess)
       break;
     if ((e = skw::launch_film(W.contrib, px0, n_px, P.spp, P.slots, film_rgb, st)) != cudaSuccess) break;
-    launches += kLaunchesPerPass + (gather ? 6 : 0) + (caustic ? 3 : 0);
+    launches += launches_per_pass(P) + (gather ? 6 : 0) + (caustic ? 3 : 0);
   }
   cudaFreeAsync(w, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "photon-map render");
@@ -1031,6 +1147,14 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
 }  // extern "C"
 
 extern "C" {
+
+int skw_scene_set_max_specular_depth(skw_scene *s, int32_t depth) {
+  if (!s) return SKW_ERR_ARG;
+  if (depth < 0 || depth > kMaxSpecDepth)
+    return fail(s->ctx, SKW_ERR_ARG, "max specular depth must be in [0, 11]");
+  s->dev.max_spec_depth = depth;
+  return SKW_OK;
+}
 
 int skw_scene_set_medium(skw_scene *s, const skw_medium *m) {
   if (!s) return SKW_ERR_ARG;

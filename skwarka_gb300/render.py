@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib
 from .accel import Context, TriangleMesh, default_context
 
-MATTE, PLASTIC, METAL, MEASURED = 0, 1, 2, 3
+MATTE, PLASTIC, METAL, MEASURED, TRANSPARENT = 0, 1, 2, 3, 4
 
 
 class MeasuredBRDF:
@@ -79,6 +79,7 @@ class Material:
     eta: tuple = (1.0, 1.0, 1.0)
     k: tuple = (0.0, 0.0, 0.0)
     measured: "MeasuredBRDF | None" = None
+    refractive_index: float = 1.5
 
 
 @dataclass
@@ -134,7 +135,8 @@ class Camera:
 
 class skw_material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("roughness", C.c_float),
-                ("sigma", C.c_float), ("eta", C.c_float * 3), ("k", C.c_float * 3), ("measured", C.c_void_p)]
+                ("sigma", C.c_float), ("eta", C.c_float * 3), ("k", C.c_float * 3), ("measured", C.c_void_p),
+                ("refractive_index", C.c_float)]
 
 
 class skw_render_primitive(C.Structure):
@@ -162,7 +164,7 @@ def c_material(m: Material, measured_handle=None) -> skw_material:
     if h is None and m.measured is not None:
         h = m.measured.handle
     return skw_material(m.kind, (C.c_float * 3)(*m.kd), (C.c_float * 3)(*m.ks), m.roughness, m.sigma,
-                        (C.c_float * 3)(*m.eta), (C.c_float * 3)(*m.k), h)
+                        (C.c_float * 3)(*m.eta), (C.c_float * 3)(*m.k), h, m.refractive_index)
 
 
 def c_camera(cam: Camera) -> skw_camera:
@@ -228,6 +230,10 @@ class RenderScene:
             m = skw_medium((C.c_float * 3)(*medium.lo), (C.c_float * 3)(*medium.hi), (C.c_float * 3)(*medium.sigma_a),
                            (C.c_float * 3)(*medium.sigma_s), (C.c_float * 3)(*medium.emission), medium.g, medium.step)
         _lib.check(_lib.load().skw_scene_set_medium(self.handle, None if m is None else C.byref(m)), self.ctx.handle)
+
+    def set_max_specular_depth(self, depth: int) -> None:
+        """DirectLightingLTEIntegratorParams::m_max_specular_depth (default 10, at most 11)."""
+        _lib.check(_lib.load().skw_scene_set_max_specular_depth(self.handle, int(depth)), self.ctx.handle)
 
     def __del__(self):
         h = getattr(self, "handle", None)

@@ -181,3 +181,25 @@ if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "photon":
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "render":
     render_golden()
     print("render golden written")
+
+
+def specular_golden():
+    """The reference's direct-lighting renders (maximum specular depth 6) of
+    scene_fixtures.specular_cases() at 48 x 32, 16x16 spp, and its photon
+    shooting (ShootPhotons, 200,000 paths, its own bounce and roulette rules)
+    in the clear-glass sphere scene under the point light: the photons of
+    each map."""
+    out = {}
+    ref = Reference()
+    for name, (prims, mats, lights, cam) in sf.specular_cases().items():
+        out[name], _ = ref.render_direct(prims, mats, lights, cam, 16, 16)
+    prims, mats, lights, cam = sf.specular_cases()["glass_point"]
+    from skwarka_gb300.render import Camera
+    _, info = ref.render_photon(prims, mats, lights, Camera(cam.camera_to_world, cam.x_view_angle, 0, 0), 1, 1,
+                                200_000)
+    out["photon_counts"] = np.array([info["caustic"], info["direct"], info["indirect"]], np.int64)
+    np.savez_compressed(OUT / "specular_48x32.npz", **out)
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "specular":
+    specular_golden()

@@ -314,3 +314,53 @@ def caustic_cases(seed=41):
     return {"matte_k50": ([RenderPrimitive(plane, 0)], [matte], lights, cam, maps, paths, 50, 0.1),
             "plastic_k50": ([RenderPrimitive(plane, 0)], [plastic], lights, cam, maps, paths, 50, 0.1),
             "matte_k200": ([RenderPrimitive(plane, 0)], [matte], lights, cam, maps, paths, 200, 0.05)}
+
+
+def specular_scene(material, lights="area", resolution=(48, 32)):
+    """A glass-like sphere (radius 0.4, 4 * 4**4 flat outward-facing
+    triangles) resting above a 10 x 10 matte floor, lit by a 0.6 x 0.6 quad
+    light of radiance 10 at height 2 (lights="area") or a point light of
+    intensity 3 at (0.2, -0.1, 1.6) (lights="point"); `material` is the
+    sphere's skwarka_gb300.render.Material.  Returns (prims, materials,
+    point_lights, camera): the camera looks at the sphere from above and to
+    the side, so the floor is seen directly and through the sphere."""
+    from skwarka_gb300.accel import TriangleMesh
+    from skwarka_gb300.render import Camera, Material, PointLight, RenderPrimitive
+    v, t = scenes.sphere_mesh(4)
+    a, b, c = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
+    outward = (np.cross(b - a, c - a) * (a + b + c)).sum(1) > 0
+    t = np.where(outward[:, None], t, t[:, [0, 2, 1]]).astype(np.int32)
+    sphere = TriangleMesh((v * 0.4 + np.array([0.0, 0.0, 0.45])).astype(np.float32), t)
+    s = 5.0
+    floor = TriangleMesh(np.array([[-s, -s, 0], [s, -s, 0], [s, s, 0], [-s, s, 0]], np.float32),
+                         np.array([[0, 1, 2], [0, 2, 3]], np.int32))
+    prims = [RenderPrimitive(floor, 0), RenderPrimitive(sphere, 1)]
+    mats = [Material(kd=(0.7, 0.6, 0.5)), material]
+    pls = []
+    if lights == "area":
+        q = 0.3
+        lv = np.array([[-q, -q, 2], [q, -q, 2], [q, q, 2], [-q, q, 2]], np.float32)
+        prims.append(RenderPrimitive(TriangleMesh(lv, np.array([[0, 2, 1], [0, 3, 2]], np.int32)), 2,
+                                     emission=(10.0, 10.0, 10.0)))
+        mats.append(Material(kd=(0.0, 0.0, 0.0)))
+    else:
+        pls = [PointLight((0.2, -0.1, 1.6), (3.0, 3.0, 3.0))]
+    w, h = resolution
+    cam = Camera.look_at((1.3, -1.1, 1.2), (0.0, 0.0, 0.35), (0, 0, 1), np.radians(55.0), w, h)
+    return prims, mats, pls, cam
+
+
+def specular_cases():
+    """{name: (prims, materials, point_lights, camera)} of specular_scene:
+    clear glass (r = t = 1, index 1.5) under the area light and under the
+    point light, tinted glass (t = (0.9, 0.6, 0.3), index 1.33), and a
+    reflection-only dielectric of index 8 (a Fresnel mirror, r = (0.9, 0.8,
+    0.7))."""
+    from skwarka_gb300.render import TRANSPARENT, Material
+    glass = Material(kind=TRANSPARENT, kd=(1.0, 1.0, 1.0), ks=(1.0, 1.0, 1.0), refractive_index=1.5)
+    tinted = Material(kind=TRANSPARENT, kd=(1.0, 1.0, 1.0), ks=(0.9, 0.6, 0.3), refractive_index=1.33)
+    mirror = Material(kind=TRANSPARENT, kd=(0.9, 0.8, 0.7), ks=(0.0, 0.0, 0.0), refractive_index=8.0)
+    return {"glass_area": specular_scene(glass, "area"),
+            "glass_point": specular_scene(glass, "point"),
+            "tinted_area": specular_scene(tinted, "area"),
+            "mirror_area": specular_scene(mirror, "area")}
