@@ -69,6 +69,7 @@ _REF_SIGS = [
                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, C.c_int,
                                         C.c_double, _P, _P, _P]),
     ("skw_ref_photon_irradiance", C.c_int, [_P, _P, _P, C.c_double, _P, _P, _P, _P, _P, _P]),
+    ("skw_ref_shoot_photons", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _i64, _P, _P, _P]),
     ("skw_ref_render_photon_maps", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, _P, _P, _P,
                                              C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                              C.c_double, _P, _P, _P]),
@@ -283,6 +284,28 @@ class Reference:
                                        _ptr(info), _ptr(sec))
         return film, {"shoot_s": float(sec[0]), "render_s": float(sec[1]), "caustic": int(info[0]),
                       "direct": int(info[1]), "indirect": int(info[2]), "irradiance": int(info[3])}
+
+    def shoot_photons(self, prims, materials, point_lights, n_paths, cap=4_000_000):
+        """The reference's PhotonLTEIntegrator::ShootPhotons(n_paths): the
+        positions (float32 (n, 3), kd-tree order) of its caustic, direct and
+        indirect photons."""
+        from skwarka_gb300.render import c_material, c_prims
+        cm, nm, cp, keep = c_prims(prims)
+        verts = (C.c_void_p * nm)(*[cm[i].vertices for i in range(nm)])
+        tris = (C.c_void_p * nm)(*[cm[i].triangles for i in range(nm)])
+        nv = np.array([cm[i].n_vertices for i in range(nm)], np.int64)
+        nt = np.array([cm[i].n_triangles for i in range(nm)], np.int64)
+        mats = (type(c_material(materials[0])) * len(materials))(
+            *[c_material(m, self._merl(m.measured) if m.measured is not None else None) for m in materials])
+        pl = np.array([list(l.position) + list(l.intensity) for l in point_lights], np.float32).reshape(-1, 6)
+        bufs = [np.zeros((cap, 3), np.float32) for _ in range(3)]
+        ptrs = (C.c_void_p * 3)(*[b.ctypes.data for b in bufs])
+        caps = np.full(3, cap, np.int64)
+        n = np.zeros(3, np.int64)
+        self.lib.skw_ref_shoot_photons(nm, verts, _ptr(nv), tris, _ptr(nt), len(prims), C.addressof(cp),
+                                       C.addressof(mats), len(point_lights), _ptr(pl) if len(pl) else None,
+                                       int(n_paths), ptrs, _ptr(caps), _ptr(n))
+        return [b[:min(int(k), cap)] for b, k in zip(bufs, n)]
 
     def render_photon_maps(self, prims, materials, point_lights, camera, spp_x, spp_y, maps, paths, light_samples=1,
                            gather_samples=16, caustic_lookup=50, max_caustic_dist=0.1):

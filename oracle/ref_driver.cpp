@@ -546,6 +546,31 @@ int skw_ref_render_photon(int n_meshes, const float *const *verts, const int64_t
   return 0;
 }
 
+// PhotonLTEIntegrator::ShootPhotons(n_paths) alone: the photon positions of
+// the caustic, direct and indirect maps (3 floats each, at most cap[m] per
+// map m, in the maps' kd-tree order) and each map's size in n_out[m].
+int skw_ref_shoot_photons(int n_meshes, const float *const *verts, const int64_t *n_verts, const int32_t *const *tris,
+                          const int64_t *n_tris, int n_prims, const RefPrimIn *prims, const RefMaterialIn *materials,
+                          int n_point_lights, const float *point_lights, int64_t n_paths, float *const *pos_out,
+                          const int64_t *cap, int64_t *n_out) {
+  intrusive_ptr<const Scene> scene =
+      make_scene(n_meshes, verts, n_verts, tris, n_tris, n_prims, prims, materials, n_point_lights, point_lights);
+  PhotonLTEIntegratorParams params;
+  params.m_max_specular_depth = 6;
+  params.m_media_step_size = 0.01;
+  intrusive_ptr<PhotonLTEIntegrator> integrator(new PhotonLTEIntegrator(scene, params));
+  integrator->ShootPhotons((size_t)n_paths, false);
+  auto &maps = integrator->mp_photon_maps;
+  shared_ptr<const KDTree<PhotonLTEIntegrator::Photon>> m[3] = {maps->GetCausticMap(), maps->GetDirectMap(),
+                                                                maps->GetIndirectMap()};
+  for (int k = 0; k < 3; ++k) {
+    n_out[k] = m[k] ? (int64_t)m[k]->GetNumberOfPoints() : 0;
+    for (int64_t i = 0; m[k] && i < std::min(n_out[k], cap[k]); ++i)
+      for (int c = 0; c < 3; ++c) pos_out[k][3 * i + c] = m[k]->m_points[(size_t)i].m_point[c];
+  }
+  return 0;
+}
+
 // _ConstructIrradiancePhotonMap on given photon maps (28-byte records:
 // position, weight, incident id, normal id), each with its number of paths,
 // and the scene's total area: the irradiance photons in the reference's

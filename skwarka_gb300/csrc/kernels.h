@@ -155,10 +155,22 @@ cudaError_t launch_irradiance_sum(const void *nodes, const float *weight, const 
 // caustic map at each camera hit and the Simpson-kernel estimate, written to
 // slot `slot` of contrib.  cws: caustic_bytes(n, k) bytes of workspace.
 struct CausticMap;
+// Entries of a specular level as the shading points of the caustic and
+// gather stages: entry e belongs to camera sample in_sample[e], carries the
+// RGB weight in_w[3e..] and tree node in_node[e] (its random stream), and
+// its weighted terms are added (atomics) into that sample's slot `slot`.
+// Null: the shading points are the pass's camera hits, one per sample.
+struct SpecSource {
+  const int *in_sample = nullptr;
+  const float *in_w = nullptr;
+  const int *in_node = nullptr;
+  int slot = 0;
+};
 size_t caustic_bytes(int64_t n, int k);
 cudaError_t launch_caustic(const SceneDev &S, const CausticMap &C, const ViewDev *views, int n_views, int n,
                            int64_t px_begin, int spp, int slots, int slot, const void *rays, const void *hits,
-                           void *cws, float *contrib, unsigned *status, cudaStream_t st);
+                           void *cws, float *contrib, unsigned *status, cudaStream_t st,
+                           const SpecSource *sp = nullptr);
 
 // Final gather of a render pass (photon.cu): adds each camera hit's gathered
 // indirect radiance to its slots [base_slot, base_slot + 2 gs) of contrib.
@@ -168,6 +180,6 @@ size_t gather_bytes(int64_t n, int gs);
 cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev *views, int n_views, int n,
                           int64_t px_begin, int spp, int slots, int base_slot, int gs, const void *rays,
                           const void *hits, void *gws, float *contrib, const TraceFn &trace, unsigned *status,
-                          cudaStream_t st);
+                          cudaStream_t st, const SpecSource *sp = nullptr);
 
 }  // namespace skw

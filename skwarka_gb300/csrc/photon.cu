@@ -570,7 +570,7 @@ __device__ __forceinline__ float rnd_g(uint64_t seed, uint64_t gid, uint32_t d) 
 }
 
 struct GatherArgs {
-  int n;               // samples in the pass
+  int n;               // shading points: the pass's samples, or a chunk of a specular level
   int64_t px_begin;
   int spp;
   int slots;
@@ -578,7 +578,39 @@ struct GatherArgs {
   int gs;              // gather samples (a square, as the sampler rounds it)
   const ViewDev *views;
   int n_views;
+  SpecSource sp;       // in_sample null: camera hits
 };
+
+// Camera sample, random-stream seed, weight and first target slot of
+// shading point i (a camera hit, or a specular-level entry).
+struct PointRef {
+  int sample;
+  uint64_t gid, seed;
+  V3 w;
+  int64_t slot0;
+};
+__device__ __forceinline__ PointRef point_ref(const GatherArgs &G, int i) {
+  PointRef r;
+  unsigned node = 1;
+  r.sample = i;
+  r.w = v3(1.0f, 1.0f, 1.0f);
+  if (G.sp.in_sample) {
+    r.sample = G.sp.in_sample[i];
+    node = (unsigned)G.sp.in_node[i];
+    r.w = load3(G.sp.in_w + 3 * (int64_t)i);
+  }
+  const int64_t P = G.px_begin + r.sample / G.spp;
+  int lo = 0, hi = G.n_views - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (G.views[mid].px_begin <= P) lo = mid; else hi = mid - 1;
+  }
+  r.gid = (uint64_t)((P - G.views[lo].px_begin) * G.spp + r.sample % G.spp);
+  r.seed = G.views[lo].seed;
+  if (G.sp.in_sample) r.seed ^= 0xA0761D6478BD642Full * (uint64_t)node;  // as k_shade's specular levels
+  r.slot0 = G.sp.in_sample ? (int64_t)r.sample * G.slots + G.sp.slot : (int64_t)r.sample * G.slots + G.base_slot;
+  return r;
+}
 
 __global__ void k_gather_sources(SceneDev S, GatherArgs G, const float4 *__restrict__ rays,
                                  const int4 *__restrict__ hits, int *__restrict__ src, double *__restrict__ q,
@@ -588,7 +620,8 @@ __global__ void k_gather_sources(SceneDev S, GatherArgs G, const float4 *__restr
   Hit h{};
   if (i < G.n) {
     const int4 hit = hits[i];
-    if (hit.y >= 0) {
+    // only surfaces with a non-specular component (PhotonLTEIntegrator.cpp:337-343)
+    if (hit.y >= 0 && S.materials[S.prim_material[hit.y]].kind != kTransparent) {
       const float4 ra = rays[2 * i], rb = rays[2 * i + 1];
       h = make_hit(S, v3(ra.x, ra.y, ra.z), v3(ra.w, rb.x, rb.y), __int_as_float(hit.x), hit.y, hit.z);
       ok = true;
@@ -629,6 +662,8 @@ __global__ void __launch_bounds__(128) k_gather_rays(SceneDev S, GatherArgs G, G
   uint64_t gid = 0, seed = 0;
   int64_t slot0 = 0;
   int found = 0;
+  V3 ew = v3(1.0f, 1.0f, 1.0f);  // specular-level weight of the shading point
+  const bool acc = G.sp.in_sample != nullptr;
   V3 pd[kGatherLookup];
   if (valid) {
     const int i = src[j];
@@ -638,15 +673,11 @@ __global__ void __launch_bounds__(128) k_gather_rays(SceneDev S, GatherArgs G, G
     h = make_hit(S, v3(ra.x, ra.y, ra.z), d, __int_as_float(hit.x), hit.y, hit.z);
     b = make_bsdf(S, h, hit.y);
     wo = d * -1.0f;
-    const int64_t P = G.px_begin + i / G.spp;
-    int lo = 0, hi = G.n_views - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (G.views[mid].px_begin <= P) lo = mid; else hi = mid - 1;
-    }
-    gid = (uint64_t)((P - G.views[lo].px_begin) * G.spp + i % G.spp);
-    seed = G.views[lo].seed;
-    slot0 = (int64_t)i * G.slots + G.base_slot;
+    const PointRef pr = point_ref(G, i);
+    gid = pr.gid;
+    seed = pr.seed;
+    slot0 = pr.slot0;
+    ew = pr.w;
     found = kcount[j];
     for (int k = 0; k < found; ++k) {
       const int did = M.ind_dirid[kidx[(int64_t)j * kGatherLookup + k]];
@@ -675,8 +706,8 @@ __global__ void __launch_bounds__(128) k_gather_rays(SceneDev S, GatherArgs G, G
     const int q = queue_append(want, gcount);
     if (want) {
       store_ray(grays, q, h.p, ex, tmin, __int_as_float(0x7f800000));
-      gtarget[q] = (int)(slot0 + k);
-      store_rgb(gweight, q, wt);
+      gtarget[q] = (int)(acc ? slot0 : slot0 + k);
+      store_rgb(gweight, q, mul(wt, ew));
     }
   }
   // Photon-guided samples (:499-533)
@@ -718,8 +749,8 @@ __global__ void __launch_bounds__(128) k_gather_rays(SceneDev S, GatherArgs G, G
     const int q = queue_append(want, gcount);
     if (want) {
       store_ray(grays, q, h.p, ex, tmin, __int_as_float(0x7f800000));
-      gtarget[q] = (int)(slot0 + gs + k);
-      store_rgb(gweight, q, wt);
+      gtarget[q] = (int)(acc ? slot0 : slot0 + gs + k);
+      store_rgb(gweight, q, mul(wt, ew));
     }
   }
 }
@@ -825,7 +856,7 @@ __global__ void k_gather_hits(SceneDev S, const float4 *__restrict__ grays, cons
 __global__ void k_gather_resolve(GatherMaps M, int gs, const int *__restrict__ hcount, const int *__restrict__ hsrc,
                                  const int32_t *__restrict__ nearest, const float *__restrict__ ts,
                                  const uint8_t *__restrict__ side, const int *__restrict__ gtarget,
-                                 const float *__restrict__ gweight, float *__restrict__ contrib) {
+                                 const float *__restrict__ gweight, float *__restrict__ contrib, bool accumulate) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *hcount) return;
   const int t = nearest[j];
@@ -835,7 +866,14 @@ __global__ void k_gather_resolve(GatherMaps M, int gs, const int *__restrict__ h
   const int g = hsrc[j];
   const int64_t slot = gtarget[g];
   const float s = kInvPi / gs;
-  for (int c = 0; c < 3; ++c) contrib[3 * slot + c] = ts[3 * j + c] * E[c] * gweight[3 * g + c] * s;
+  for (int c = 0; c < 3; ++c) {
+    const float v = ts[3 * j + c] * E[c] * gweight[3 * g + c] * s;
+    if (accumulate) {
+      if (v != 0.0f) atomicAdd(contrib + 3 * slot + c, v);
+    } else {
+      contrib[3 * slot + c] = v;
+    }
+  }
 }
 
 // _LookupCausticRadiance (PhotonLTEIntegrator.cpp:579-627) at camera hit j
@@ -887,6 +925,14 @@ __global__ void __launch_bounds__(128) k_caustic_resolve(SceneDev S, GatherArgs 
   else
     m *= (double)found / ((double)found - 0.5);
   const double sc = 1.0 / (C.paths * m);
+  if (G.sp.in_sample) {  // a specular-level entry: weighted, added into its sample's slot
+    const PointRef pr = point_ref(G, i);
+    float *o = contrib + 3 * pr.slot0;
+    const float v[3] = {(float)(r0 * sc) * pr.w.x, (float)(r1 * sc) * pr.w.y, (float)(r2 * sc) * pr.w.z};
+    for (int c = 0; c < 3; ++c)
+      if (v[c] != 0.0f) atomicAdd(o + c, v[c]);
+    return;
+  }
   float *o = contrib + 3 * ((int64_t)i * G.slots + slot);
   o[0] = (float)(r0 * sc);
   o[1] = (float)(r1 * sc);
@@ -903,7 +949,7 @@ size_t caustic_bytes(int64_t n, int k) {
 
 cudaError_t launch_caustic(const SceneDev &S, const CausticMap &C, const ViewDev *views, int n_views, int n,
                            int64_t px_begin, int spp, int slots, int slot, const void *rays, const void *hits,
-                           void *cws, float *contrib, unsigned *status, cudaStream_t st) {
+                           void *cws, float *contrib, unsigned *status, cudaStream_t st, const SpecSource *sp) {
   if (n <= 0 || C.n <= 0 || C.k <= 0) return cudaSuccess;
   auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
   char *p = (char *)cws;
@@ -920,7 +966,7 @@ cudaError_t launch_caustic(const SceneDev &S, const CausticMap &C, const ViewDev
   int32_t *kcnt = (int32_t *)take(al((int64_t)n * 4));
   void *scratch = take(al((int64_t)knn_scratch_bytes(n, C.k)));
   // GatherArgs: only n, px_begin, spp, slots and the views are used here
-  GatherArgs G{n, px_begin, spp, slots, slot, 0, views, n_views};
+  GatherArgs G{n, px_begin, spp, slots, slot, 0, views, n_views, sp ? *sp : SpecSource{}};
   cudaError_t e;
   if ((e = cudaMemsetAsync(counts, 0, sizeof(int), st)) != cudaSuccess) return e;
   k_gather_sources<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S, G, (const float4 *)rays, (const int4 *)hits, src, q,
@@ -938,7 +984,7 @@ cudaError_t launch_caustic(const SceneDev &S, const CausticMap &C, const ViewDev
 cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev *views, int n_views, int n,
                           int64_t px_begin, int spp, int slots, int base_slot, int gs, const void *rays,
                           const void *hits, void *gws, float *contrib, const TraceFn &trace, unsigned *status,
-                          cudaStream_t st) {
+                          cudaStream_t st, const SpecSource *sp) {
   if (n <= 0 || gs <= 0 || M.n_irr <= 0) return cudaSuccess;
   auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
   const int64_t ng = (int64_t)n * 2 * gs;
@@ -963,7 +1009,7 @@ cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev 
   float *ts = (float *)take(al(ng * 12));
   uint8_t *side = (uint8_t *)take(al(ng));
   int32_t *nearest = (int32_t *)take(al(ng * 4));
-  GatherArgs G{n, px_begin, spp, slots, base_slot, gs, views, n_views};
+  GatherArgs G{n, px_begin, spp, slots, base_slot, gs, views, n_views, sp ? *sp : SpecSource{}};
   cudaError_t e;
   if ((e = cudaMemsetAsync(counts, 0, 3 * sizeof(int), st)) != cudaSuccess) return e;
   k_gather_sources<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S, G, (const float4 *)rays, (const int4 *)hits, src, q,
@@ -985,7 +1031,7 @@ cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev 
                           status, st, counts + 2)) != cudaSuccess)
     return e;
   k_gather_resolve<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(M, gs, counts + 2, hsrc, nearest, ts, side, gtarget,
-                                                                  gweight, contrib);
+                                                                  gweight, contrib, sp != nullptr);
   return cudaGetLastError();
 }
 

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <string>
 #include <vector>
@@ -535,8 +536,20 @@ cudaError_t record_media(skw_scene *s, const Plan &P, const Workspace &W, const 
 // rays; each is traced, shaded (emission and direct lighting added into its
 // sample's specular slot) and queues its children while L <= the scene's
 // max_spec_depth.
+// Extra stages for the entries of a specular level (the photon-map render's
+// caustic and gather terms): called after the level's direct lighting with
+// the level's queue (its rays, their hits, weights, samples, nodes), its
+// device count and its capacity.
+struct SpecLevel {
+  const void *rays, *hits;
+  const float *w;
+  const int *sample, *node, *count;
+  int64_t capacity;
+};
+using SpecHook = std::function<cudaError_t(const SpecLevel &)>;
+
 cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
-                            int n, cudaStream_t st) {
+                            int n, cudaStream_t st, const SpecHook *hook) {
   skw_accel *a = s->accel;
   const int nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
   cudaError_t e = cudaSuccess;
@@ -577,6 +590,9 @@ cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, con
                                  W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st, true)) !=
         cudaSuccess)
       return e;
+    if (hook && (e = (*hook)(SpecLevel{W.qrays[qi], W.qhits, W.qw[qi], W.qsample[qi], W.qnode[qi],
+                                       W.counts + 3 + qi, cl})) != cudaSuccess)
+      return e;
   }
   return e;
 }
@@ -584,7 +600,7 @@ cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, con
 // The direct-lighting stages of one pass over global pixels
 // [px0, px0 + n_px): every slot of contrib but the extra ones is filled.
 cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
-                          int n_px, cudaStream_t st) {
+                          int n_px, cudaStream_t st, const SpecHook *hook = nullptr) {
   skw_accel *a = s->accel;
   const int n = n_px * P.spp, nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
   cudaError_t e;
@@ -618,7 +634,7 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
   if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
                                W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st)) != cudaSuccess)
     return e;
-  return record_specular(s, P, W, d_views, px0, n, st);
+  return record_specular(s, P, W, d_views, px0, n, st, hook);
 }
 
 // One pass: direct lighting, then the film.
@@ -1062,8 +1078,6 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   const bool caustic = pm->maps[0].n > 0 && pp->caustic_lookup > 0;
   if (caustic && !(pp->max_caustic_dist > 0.0))
     return fail(ctx, SKW_ERR_ARG, "max_caustic_dist must be positive");
-  if (s->dev.has_specular)
-    return fail(ctx, SKW_ERR_UNSUPPORTED, "the photon-map render follows no specular paths (shooting does)");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
   // the sampler rounds sequence lengths up to squares (Sampler.cpp:39-57, StratifiedSampler.cpp:33-37)
@@ -1124,21 +1138,60 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   e = cudaMemcpyAsync(d_view, P.views.data(), sizeof(skw::ViewDev), cudaMemcpyHostToDevice, st);
   int64_t launches = 0;
   const int base_slot = 1 + 2 * P.nl + P.npl;
+  // The specular levels' entries get the same caustic and gather terms,
+  // weighted, in their sample's specular slot (PhotonLTEIntegrator::
+  // _SurfaceRadiance at every depth, PhotonLTEIntegrator.cpp:320-385).  A
+  // level's length is read back and its entries run in chunks of the pass's
+  // sample count (the gather and caustic workspaces' capacity).
+  int64_t px_cur = 0;
+  int32_t *h_count = nullptr;
+  if (e == cudaSuccess && P.spec_levels && (gather || caustic)) e = cudaMallocHost((void **)&h_count, sizeof(int32_t));
+  SpecHook hook = [&](const SpecLevel &L) -> cudaError_t {
+    cudaError_t he = cudaMemcpyAsync(h_count, L.count, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (he == cudaSuccess) he = cudaStreamSynchronize(st);
+    if (he != cudaSuccess) return he;
+    const int64_t cnt = std::min<int64_t>(*h_count, L.capacity);
+    for (int64_t off = 0; off < cnt && he == cudaSuccess; off += P.cap_samples) {
+      const int m = (int)std::min<int64_t>(P.cap_samples, cnt - off);
+      skw::SpecSource sp;
+      sp.in_sample = L.sample + off;
+      sp.in_w = L.w + 3 * off;
+      sp.in_node = L.node + off;
+      sp.slot = P.spec_slot;
+      const void *lr = (const char *)L.rays + 32 * off, *lh = (const char *)L.hits + 16 * off;
+      if (gather)
+        he = skw::launch_gather(s->dev, M, d_view, 1, m, px_cur, P.spp, P.slots, base_slot, gs, lr, lh, gws,
+                                W.contrib, trace, pm->d_status, st, &sp);
+      if (he == cudaSuccess && caustic)
+        he = skw::launch_caustic(s->dev, CM, d_view, 1, m, px_cur, P.spp, P.slots, P.spec_slot, lr, lh, cws,
+                                 W.contrib, pm->d_status, st, &sp);
+      launches += (gather ? 6 : 0) + (caustic ? 3 : 0);
+    }
+    return he;
+  };
   for (int64_t px0 = 0; px0 < P.n_px_total && e == cudaSuccess; px0 += P.chunk_px) {
     const int n_px = (int)std::min<int64_t>(P.chunk_px, P.n_px_total - px0);
     const int n = n_px * P.spp;
-    if ((e = record_direct(s, P, W, d_view, px0, n_px, st)) != cudaSuccess) break;
+    px_cur = px0;
+    if ((e = record_direct(s, P, W, d_view, px0, n_px, st, P.spec_levels && (gather || caustic) ? &hook : nullptr)) !=
+        cudaSuccess)
+      break;
     if (gather && (e = skw::launch_gather(s->dev, M, d_view, 1, n, px0, P.spp, P.slots, base_slot, gs, W.rays, W.hits,
                                           gws, W.contrib, trace, pm->d_status, st)) != cudaSuccess)
       break;
     // _LookupCausticRadiance (PhotonLTEIntegrator.cpp:342) into the slot after the gather slots
-    if (caustic && (e = skw::launch_caustic(s->dev, CM, d_view, 1, n, px0, P.spp, P.slots, P.slots - 1, W.rays,
-                                            W.hits, cws, W.contrib, pm->d_status, st)) != cudaSuccess)
+    if (caustic && (e = skw::launch_caustic(s->dev, CM, d_view, 1, n, px0, P.spp, P.slots,
+                                            base_slot + (gather ? 2 * gs : 0), W.rays, W.hits, cws, W.contrib,
+                                            pm->d_status, st)) != cudaSuccess)
       break;
     if ((e = skw::launch_film(W.contrib, px0, n_px, P.spp, P.slots, film_rgb, st)) != cudaSuccess) break;
     launches += launches_per_pass(P) + (gather ? 6 : 0) + (caustic ? 3 : 0);
   }
   cudaFreeAsync(w, st);
+  if (h_count) {
+    cudaStreamSynchronize(st);
+    cudaFreeHost(h_count);
+  }
   if (e != cudaSuccess) return cuda_fail(ctx, e, "photon-map render");
   ctx->launches.fetch_add(launches);
   return SKW_OK;

@@ -186,18 +186,24 @@ if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "render":
 def specular_golden():
     """The reference's direct-lighting renders (maximum specular depth 6) of
     scene_fixtures.specular_cases() at 48 x 32, 16x16 spp, and its photon
-    shooting (ShootPhotons, 200,000 paths, its own bounce and roulette rules)
-    in the clear-glass sphere scene under the point light: the photons of
-    each map."""
+    shooting (ShootPhotons, 2,000,000 paths, its own bounce and roulette rules)
+    in the clear-glass sphere scene under the point light: the sizes of its
+    caustic, direct and indirect maps, the indirect photons on the floor, and
+    the caustic photons' mean (x, y) and RMS distance from the axis; and its
+    photon-mapping renders of the clear-glass scenes."""
     out = {}
     ref = Reference()
     for name, (prims, mats, lights, cam) in sf.specular_cases().items():
         out[name], _ = ref.render_direct(prims, mats, lights, cam, 16, 16)
     prims, mats, lights, cam = sf.specular_cases()["glass_point"]
-    from skwarka_gb300.render import Camera
-    _, info = ref.render_photon(prims, mats, lights, Camera(cam.camera_to_world, cam.x_view_angle, 0, 0), 1, 1,
-                                200_000)
-    out["photon_counts"] = np.array([info["caustic"], info["direct"], info["indirect"]], np.int64)
+    caustic, direct, indirect = ref.shoot_photons(prims, mats, lights, 2_000_000)
+    on_floor = np.abs(indirect[:, 2]) < 1e-4
+    out["photon_counts"] = np.array([len(caustic), len(direct), len(indirect), on_floor.sum()], np.int64)
+    out["caustic_xy"] = np.concatenate([caustic[:, :2].mean(0), [np.sqrt((caustic[:, :2] ** 2).sum(1).mean())]])
+    # photon-mapping renders (1,000,000 paths, 16 gather samples, 8x8 spp)
+    for name in ("glass_point", "glass_area"):
+        prims, mats, lights, cam = sf.specular_cases()[name]
+        out[name + "_photon"], _ = ref.render_photon(prims, mats, lights, cam, 8, 8, 1_000_000, gather_samples=16)
     np.savez_compressed(OUT / "specular_48x32.npz", **out)
 
 

@@ -10,10 +10,13 @@ dielectric Fresnel + SpecularTransmission) on the GPU.
   darker than depth 6 inside the sphere and equal on the floor seen
   directly.
 * Photon shooting deposits caustic photons (a diffuse hit after specular
-  bounces only) and no direct photon on glass; the map sizes agree with the
-  reference's ShootPhotons over the same 200,000 paths.
-* The scenes with a specular material are refused where the GPU path does not
-  follow specular paths (adjoint, photon render, medium).
+  bounces only) and no direct photon on glass; the maps agree with the
+  reference's ShootPhotons over the same 2,000,000 paths.
+* The photon-mapping render follows the same trees, with caustic-map
+  radiance and final gather at their diffuse hits, against the reference's
+  photon renders.
+* Scenes with a specular material are refused where the GPU path does not
+  follow specular paths (adjoint; a medium together with them).
 """
 from pathlib import Path
 
@@ -67,29 +70,76 @@ def test_specular_depth_limits_the_tree(gpu):
 
 
 def test_photon_shooting_through_glass(gpu):
+    """2,000,000 paths from the point light above the glass sphere, against
+    the reference's ShootPhotons over the same paths.  Direct photons (first
+    hits; radical-inverse emission) within 0.5 %; caustic photons (floor hits
+    after specular bounces only) in count within 3 %, centroid within 0.01 and
+    spread within 2 %; indirect photons on the floor within 8 %.  Most
+    indirect photons lie on the glass itself: photons trapped by total
+    internal reflection inside the faceted sphere, whose number of bounces
+    before numerical error lets them out depends on each implementation's
+    arithmetic (double in the reference, float here), compared within 12 %.
+    The GPU ends a path after 64 hits (the reference has no limit); in this
+    scene that ends about 3 % of the paths that would still reach the floor
+    (a double-precision restatement of the walk: 408 floor photons per
+    200,000 paths with the cap, 420 without)."""
     prims, mats, lights, cam = sf.specular_cases()["glass_point"]
     sc = RenderScene(prims, mats, lights)
-    pm = PhotonMap.shoot(sc, 200_000, max_bounces=64, seed=5)
+    pm = PhotonMap.shoot(sc, 2_000_000, max_bounces=64, seed=5)
     info = pm.info()
-    want = np.load(GOLD)["photon_counts"]
-    got = np.array([info["n_caustic"], info["n_direct"], info["n_indirect"]])
-    print(f"[specular photons] caustic / direct / indirect: gpu {got.tolist()} reference {want.tolist()}")
-    assert abs(got[1] / want[1] - 1) <= 0.005  # first hits: radical-inverse emission, no roulette
-    assert abs(got[0] / want[0] - 1) <= 0.06
-    assert abs(got[2] / want[2] - 1) <= 0.05
-    assert info["paths_caustic"] == 200_000
-    c = pm.export("caustic")
-    # caustics land on the floor, inside the region lit through the sphere
-    assert np.allclose(c["position"][:, 2], 0.0, atol=1e-4)
-    assert np.hypot(c["position"][:, 0], c["position"][:, 1]).max() < 2.5
+    g = np.load(GOLD)
+    want = g["photon_counts"]
+    ind = pm.export("indirect")
+    floor = int((np.abs(ind["position"][:, 2]) < 1e-4).sum())
+    got = np.array([info["n_caustic"], info["n_direct"], info["n_indirect"], floor])
+    print(f"[specular photons] caustic / direct / indirect / indirect on the floor: gpu {got.tolist()} "
+          f"reference {want.tolist()}")
+    assert abs(got[1] / want[1] - 1) <= 0.005
+    assert abs(got[0] / want[0] - 1) <= 0.03
+    assert abs(got[3] / want[3] - 1) <= 0.08
+    assert abs(got[2] / want[2] - 1) <= 0.12
+    assert info["paths_caustic"] == 2_000_000
+    c = pm.export("caustic")["position"]
+    assert np.allclose(c[:, 2], 0.0, atol=1e-4)  # caustics land on the floor
+    cxy = np.concatenate([c[:, :2].mean(0), [np.sqrt((c[:, :2] ** 2).sum(1).mean())]])
+    print(f"[specular photons] caustic centroid and spread gpu {cxy.round(4).tolist()} "
+          f"reference {g['caustic_xy'].round(4).tolist()}")
+    assert np.abs(cxy[:2] - g["caustic_xy"][:2]).max() <= 0.01
+    assert abs(cxy[2] / g["caustic_xy"][2] - 1) <= 0.02
     d = pm.export("direct")
     assert (d["position"][:, 2] < 1e-4).all()  # no direct photon on the glass
+
+
+@pytest.mark.parametrize("name", ["glass_point", "glass_area"])
+def test_specular_photon_render_matches_reference(gpu, name):
+    """PhotonLTEIntegrator with the sphere of glass: caustic-map radiance and
+    final gather at every diffuse hit of every sample's specular tree, 1,000,000
+    photon paths, 16 gather samples, 8x8 spp.  The photon-map part (photon
+    render minus direct render) within 6 % in mean luminance and the photon
+    image's 8x8 blocks within 8 % of the reference's (the reference's own
+    photon part moves by 2-3 % in the mean and up to 10 % in the caustic's
+    blocks between 200,000 and 2,000,000 paths)."""
+    from skwarka_gb300.photon import render_photon
+    g = np.load(GOLD)
+    prims, mats, lights, cam = sf.specular_cases()[name]
+    sc = RenderScene(prims, mats, lights)
+    sc.set_max_specular_depth(6)
+    pm = PhotonMap.shoot(sc, 1_000_000, seed=11)
+    img = render_photon(sc, pm, cam, 8, 8, gather_samples=16, seed=13).cpu().numpy()
+    direct = sc.render_direct(cam, 8, 8, seed=13).cpu().numpy()
+    assert np.isfinite(img).all() and (img >= 0).all()
+    ph_gpu, ph_ref = ((img - direct) @ LUM).mean(), ((g[name + "_photon"] - g[name]) @ LUM).mean()
+    rb = _blocks(g[name + "_photon"])
+    rel = np.abs(_blocks(img) - rb) / np.maximum(rb, 0.25 * rb.mean())
+    print(f"[specular photon {name}] photon-map part gpu {ph_gpu:.5f} reference {ph_ref:.5f}; "
+          f"worst block {rel.max():.4f}")
+    assert abs(ph_gpu / ph_ref - 1) <= 0.06
+    assert rel.max() <= 0.08
 
 
 def test_specular_scene_refusals(gpu):
     import torch
     from skwarka_gb300.adjoint import DirectLighting
-    from skwarka_gb300.photon import render_photon
     prims, mats, lights, cam = sf.specular_cases()["glass_point"]
     sc = RenderScene(prims, mats, lights)
     sc.set_medium(Medium())
@@ -100,6 +150,3 @@ def test_specular_scene_refusals(gpu):
     albedo = torch.full((sc.n_triangles, 3), 0.5, device="cuda")
     with pytest.raises(_lib.SkwError, match="specular"):
         dl.adjoint(albedo, 1.0, torch.ones(cam.height, cam.width, 3, device="cuda"))
-    pm = PhotonMap.shoot(sc, 10_000, seed=1)
-    with pytest.raises(_lib.SkwError, match="specular"):
-        render_photon(sc, pm, cam, 1, 1)
