@@ -815,14 +815,33 @@ __device__ V3 total_scattering_reflection(const Bsdf &b, V3 wi) {
   return v3(fminf(1.0f, fmaxf(0.0f, r.x)), fminf(1.0f, fmaxf(0.0f, r.y)), fminf(1.0f, fmaxf(0.0f, r.z)));
 }
 
+// SpecularReflection / SpecularTransmission::TotalScattering (BxDFs/
+// SpecularReflection.h, SpecularTransmission.cpp:75-92) of a transparent
+// BSDF, each clamped as BSDF::TotalScattering does; like the other BxDFs
+// they receive the WORLD incident direction as if it were local, so the
+// Fresnel term and the total-internal-reflection test read its world z.
+__device__ __forceinline__ void total_scattering_transparent(const Bsdf &b, V3 wi, V3 &refl, V3 &trans) {
+  const float F = fresnel_dielectric_ior(wi.z, b.ior);
+  refl = b.kd * F;
+  const float eta = wi.z >= 0.0f ? 1.0f / b.ior : b.ior;
+  const bool tir = eta * eta * (1.0f - wi.z * wi.z) >= 1.0f;
+  trans = tir ? v3(0, 0, 0) : b.ks * (1.0f - F);
+  refl = v3(fminf(1.0f, fmaxf(0.0f, refl.x)), fminf(1.0f, fmaxf(0.0f, refl.y)), fminf(1.0f, fmaxf(0.0f, refl.z)));
+  trans = v3(fminf(1.0f, fmaxf(0.0f, trans.x)), fminf(1.0f, fmaxf(0.0f, trans.y)), fminf(1.0f, fmaxf(0.0f, trans.z)));
+}
+
+// ts: TotalScattering over the reflection components (times the irradiance
+// on the side the gather ray comes from), tt: over the transmission
+// components (times the irradiance on the other side; only a transparent
+// BSDF has one) -- PhotonLTEIntegrator.cpp:556-567.
 __global__ void k_gather_hits(SceneDev S, const float4 *__restrict__ grays, const int4 *__restrict__ ghits,
                               const int *__restrict__ gcount, int *__restrict__ hsrc, double *__restrict__ q,
-                              double *__restrict__ qn, float *__restrict__ ts, uint8_t *__restrict__ side,
-                              int *__restrict__ hcount) {
+                              double *__restrict__ qn, float *__restrict__ ts, float *__restrict__ tt,
+                              uint8_t *__restrict__ side, int *__restrict__ hcount) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool ok = false;
   Hit h{};
-  V3 t = v3(0, 0, 0);
+  V3 t = v3(0, 0, 0), tr = v3(0, 0, 0);
   bool outside = false;
   if (i < *gcount) {
     const int4 hit = ghits[i];
@@ -833,7 +852,10 @@ __global__ void k_gather_hits(SceneDev S, const float4 *__restrict__ grays, cons
       const Bsdf b = make_bsdf(S, h, hit.y);
       const V3 gdir = d * -1.0f;
       outside = dot(gdir, h.ng) > 0.0f;
-      t = total_scattering_reflection(b, gdir);
+      if (b.kind == kTransparent)
+        total_scattering_transparent(b, gdir, t, tr);
+      else
+        t = total_scattering_reflection(b, gdir);
       ok = true;
     }
   }
@@ -849,25 +871,33 @@ __global__ void k_gather_hits(SceneDev S, const float4 *__restrict__ grays, cons
     ts[3 * j] = t.x;
     ts[3 * j + 1] = t.y;
     ts[3 * j + 2] = t.z;
+    tt[3 * j] = tr.x;
+    tt[3 * j + 1] = tr.y;
+    tt[3 * j + 2] = tr.z;
     side[j] = outside ? 1 : 0;
   }
 }
 
 __global__ void k_gather_resolve(GatherMaps M, int gs, const int *__restrict__ hcount, const int *__restrict__ hsrc,
                                  const int32_t *__restrict__ nearest, const float *__restrict__ ts,
-                                 const uint8_t *__restrict__ side, const int *__restrict__ gtarget,
-                                 const float *__restrict__ gweight, float *__restrict__ contrib, bool accumulate) {
+                                 const float *__restrict__ tt, const uint8_t *__restrict__ side,
+                                 const int *__restrict__ gtarget, const float *__restrict__ gweight,
+                                 float *__restrict__ contrib, bool accumulate) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *hcount) return;
   const int t = nearest[j];
   if (t < 0) return;
-  // the side the gather ray arrives from selects external or internal irradiance
+  // the side the gather ray arrives from selects external or internal
+  // irradiance for the reflection part, the other side for transmission
   const float *E = (side[j] ? M.irr_ext : M.irr_int) + 3 * (int64_t)t;
+  const float *Eo = (side[j] ? M.irr_int : M.irr_ext) + 3 * (int64_t)t;
   const int g = hsrc[j];
   const int64_t slot = gtarget[g];
   const float s = kInvPi / gs;
   for (int c = 0; c < 3; ++c) {
-    const float v = ts[3 * j + c] * E[c] * gweight[3 * g + c] * s;
+    float te = ts[3 * j + c] * E[c];
+    if (tt[3 * j + c] != 0.0f) te += tt[3 * j + c] * Eo[c];
+    const float v = te * gweight[3 * g + c] * s;
     if (accumulate) {
       if (v != 0.0f) atomicAdd(contrib + 3 * slot + c, v);
     } else {
@@ -1007,6 +1037,7 @@ cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev 
   int *hsrc = (int *)take(al(ng * 4));
   double *hq = (double *)take(al(ng * 24)), *hqn = (double *)take(al(ng * 24));
   float *ts = (float *)take(al(ng * 12));
+  float *tt = (float *)take(al(ng * 12));
   uint8_t *side = (uint8_t *)take(al(ng));
   int32_t *nearest = (int32_t *)take(al(ng * 4));
   GatherArgs G{n, px_begin, spp, slots, base_slot, gs, views, n_views, sp ? *sp : SpecSource{}};
@@ -1024,14 +1055,14 @@ cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev 
                                                               counts, kidx, kcnt, grays, gtarget, gweight, counts + 1);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if ((e = trace(grays, ng, counts + 1, ghits, st)) != cudaSuccess) return e;
-  k_gather_hits<<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(S, grays, ghits, counts + 1, hsrc, hq, hqn, ts, side,
-                                                               counts + 2);
+  k_gather_hits<<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(S, grays, ghits, counts + 1, hsrc, hq, hqn, ts, tt,
+                                                               side, counts + 2);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if ((e = launch_nearest(M.irr_nodes, M.irr_nids, M.dirs, M.n_irr, hq, hqn, ng, M.max_irr_dist, 0.87, nearest,
                           status, st, counts + 2)) != cudaSuccess)
     return e;
-  k_gather_resolve<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(M, gs, counts + 2, hsrc, nearest, ts, side, gtarget,
-                                                                  gweight, contrib, sp != nullptr);
+  k_gather_resolve<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(M, gs, counts + 2, hsrc, nearest, ts, tt, side,
+                                                                  gtarget, gweight, contrib, sp != nullptr);
   return cudaGetLastError();
 }
 
@@ -1039,8 +1070,8 @@ size_t gather_bytes(int64_t n, int gs) {
   auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
   const int64_t ng = n * 2 * gs;
   return 256 + al(n * 4) + 2 * al(n * 24) + al(n * kGatherLookup * 4) + al(n * kGatherLookup * 8) + al(n * 4) +
-         al(ng * 32) + al(ng * 16) + al(ng * 4) + al(ng * 12) + al(ng * 4) + 2 * al(ng * 24) + al(ng * 12) + al(ng) +
-         al(ng * 4) + 256;
+         al(ng * 32) + al(ng * 16) + al(ng * 4) + al(ng * 12) + al(ng * 4) + 2 * al(ng * 24) + 2 * al(ng * 12) +
+         al(ng) + al(ng * 4) + 256;
 }
 
 }  // namespace skw
