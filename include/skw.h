@@ -314,10 +314,18 @@ typedef struct skw_camera {
   int32_t width, height;
 } skw_camera;
 
+#define SKW_SAMPLER_STRATIFIED 0 /* StratifiedSampler(spp_x, spp_y) (Samplers/StratifiedSampler.cpp:20-103) */
+/* LDSampler(spp_x * spp_y rounded up to a power of two) (Samplers/LDSampler.cpp:20-190):
+ * scrambled (0,2)-sequence image points and light / BSDF sample sequences,
+ * the light-sample count rounded up to a power of two as the reference's
+ * Sampler::AddSamplesSequence* do; the GUI's default sampler. */
+#define SKW_SAMPLER_LD 1
+
 typedef struct skw_render_params {
-  int32_t spp_x, spp_y;        /* stratified pixel samples (StratifiedSampler) */
+  int32_t spp_x, spp_y;        /* pixel samples: spp_x x spp_y strata, or spp_x * spp_y LD samples */
   int32_t light_samples;       /* DirectLightingLTEIntegratorParams::m_direct_light_samples_num */
   uint64_t seed;               /* counter-based random stream seed */
+  int32_t sampler;             /* SKW_SAMPLER_STRATIFIED (0) or SKW_SAMPLER_LD */
 } skw_render_params;
 
 /* Renders the direct-lighting estimate of every pixel into film_rgb

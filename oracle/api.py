@@ -63,7 +63,8 @@ _REF_SIGS = [
     ("skw_ref_compressed_direction_table", None, [_P]),
     ("skw_ref_compress_direction", C.c_uint16, [C.c_double, C.c_double, C.c_double]),
     ("skw_ref_render_direct", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, C.c_int, _P, C.c_int, _P, _P,
-                                        C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
+                                        C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P,
+                                        C.c_int]),
     ("skw_ref_luminance_weights", None, [_P]),
     ("skw_ref_render_photon", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, C.c_double,
                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, C.c_int,
@@ -339,10 +340,12 @@ class Reference:
         return film, {"render_s": float(sec[0]), "caustic": int(info[0]), "direct": int(info[1]),
                       "indirect": int(info[2]), "irradiance": int(info[3])}
 
-    def render_direct(self, prims, materials, point_lights, camera, spp_x, spp_y, light_samples=1, medium=None):
+    def render_direct(self, prims, materials, point_lights, camera, spp_x, spp_y, light_samples=1, medium=None,
+                      ld=False):
         """The reference's own direct-lighting render of a scene described with
         skwarka_gb300.render types: (film (h, w, 3) float32, seconds).
-        medium: skwarka_gb300.render.Medium or None."""
+        medium: skwarka_gb300.render.Medium or None; ld: LDSampler with
+        spp_x * spp_y samples per pixel instead of the StratifiedSampler."""
         from skwarka_gb300.render import c_material, c_prims
         cm, nm, cp, keep = c_prims(prims)
         verts = (C.c_void_p * nm)(*[cm[i].vertices for i in range(nm)])
@@ -362,7 +365,7 @@ class Reference:
         self.lib.skw_ref_render_direct(nm, verts, _ptr(nv), tris, _ptr(nt), len(prims), C.addressof(cp), len(materials),
                                        C.addressof(mats), len(point_lights), _ptr(pl) if len(pl) else None, _ptr(c2w),
                                        camera.x_view_angle, camera.width, camera.height, spp_x, spp_y, light_samples,
-                                       _ptr(film), _ptr(sec), None if med is None else _ptr(med))
+                                       _ptr(film), _ptr(sec), None if med is None else _ptr(med), int(bool(ld)))
         return film, float(sec[0])
 
 

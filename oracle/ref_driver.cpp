@@ -53,6 +53,7 @@
 #include <Raytracer/Films/ImageFilm.h>
 #include <Raytracer/FilmFilters/BoxFilter.h>
 #include <Raytracer/Samplers/StratifiedSampler.h>
+#include <Raytracer/Samplers/LDSampler.h>
 #include <Raytracer/LTEIntegrators/DirectLightingLTEIntegrator.h>
 #include <Raytracer/Renderers/SamplerBasedRenderer.h>
 #include <Raytracer/VolumeRegions/HomogeneousVolumeRegion.h>
@@ -456,16 +457,22 @@ static intrusive_ptr<const Scene> make_scene(int n_meshes, const float *const *v
 }
 
 // Renders `integrator` with the reference's SamplerBasedRenderer,
-// StratifiedSampler, PerspectiveCamera and an ImageFilm with a 0.5-wide
-// BoxFilter into film_out (height x width x 3).
+// StratifiedSampler (ld = 0) or LDSampler with spp_x * spp_y samples per
+// pixel and its default ConsecutiveImagePixelsOrder (ld = 1),
+// PerspectiveCamera and an ImageFilm with a 0.5-wide BoxFilter into film_out
+// (height x width x 3).
 static double render_film(intrusive_ptr<LTEIntegrator> integrator, const double *camera_to_world, double x_view_angle,
-                          int width, int height, int spp_x, int spp_y, float *film_out) {
+                          int width, int height, int spp_x, int spp_y, float *film_out, int ld = 0) {
   intrusive_ptr<FilmFilter> filter(new BoxFilter(0.5, 0.5));
   intrusive_ptr<ImageFilm> film(new ImageFilm((size_t)width, (size_t)height, filter));
   intrusive_ptr<const Camera> camera(new PerspectiveCamera(make_transform(camera_to_world), film, 0.0, 1.0, x_view_angle));
   Point2D_i begin, end;
   film->GetSamplingExtent(begin, end);
-  intrusive_ptr<Sampler> sampler(new StratifiedSampler(begin, end, (size_t)spp_x, (size_t)spp_y));
+  intrusive_ptr<Sampler> sampler;
+  if (ld)
+    sampler.reset(new LDSampler(begin, end, (size_t)spp_x * (size_t)spp_y));
+  else
+    sampler.reset(new StratifiedSampler(begin, end, (size_t)spp_x, (size_t)spp_y));
   SamplerBasedRenderer renderer(integrator, sampler);
   auto t0 = std::chrono::steady_clock::now();
   renderer.Render(camera, false);
@@ -492,7 +499,8 @@ int skw_ref_render_direct(int n_meshes, const float *const *verts, const int64_t
                           const int64_t *n_tris, int n_prims, const RefPrimIn *prims, int n_materials,
                           const RefMaterialIn *materials, int n_point_lights, const float *point_lights,
                           const double *camera_to_world, double x_view_angle, int width, int height, int spp_x,
-                          int spp_y, int light_samples, float *film_out, double *seconds_out, const double *medium) {
+                          int spp_y, int light_samples, float *film_out, double *seconds_out, const double *medium,
+                          int ld) {
   (void)n_materials;
   intrusive_ptr<const Scene> scene = make_scene(n_meshes, verts, n_verts, tris, n_tris, n_prims, prims, materials,
                                                 n_point_lights, point_lights, medium);
@@ -501,7 +509,7 @@ int skw_ref_render_direct(int n_meshes, const float *const *verts, const int64_t
   params.m_max_specular_depth = 6;
   params.m_media_step_size = medium ? medium[16] : 0.01;  // medium[16]: the march step
   intrusive_ptr<LTEIntegrator> integrator(new DirectLightingLTEIntegrator(scene, params));
-  const double sec = render_film(integrator, camera_to_world, x_view_angle, width, height, spp_x, spp_y, film_out);
+  const double sec = render_film(integrator, camera_to_world, x_view_angle, width, height, spp_x, spp_y, film_out, ld);
   if (seconds_out) *seconds_out = sec;
   return 0;
 }

@@ -31,9 +31,9 @@ class DirectLighting:
     both arguments through the CUDA adjoint."""
 
     def __init__(self, scene: RenderScene, camera: Camera, spp_x: int = 4, spp_y: int = 4, light_samples: int = 1,
-                 seed: int = 0):
+                 seed: int = 0, sampler: int = 0):
         self.scene, self.camera = scene, camera
-        self.params = skw_render_params(spp_x, spp_y, light_samples, seed)
+        self.params = skw_render_params(spp_x, spp_y, light_samples, seed, sampler)
         scene.n_triangles = int(_lib.load().skw_scene_n_triangles(scene.handle))
 
     def forward_image(self, albedo, emission_scale):

@@ -64,8 +64,9 @@ cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double
 // concatenated films, every pixel with spp samples.
 struct SceneDev;
 struct ViewDev;
+// ld: LDSampler image points (sppx = samples per pixel, a power of two; sppy = 1)
 cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, int n_px, int sppx, int sppy,
-                          void *rays, cudaStream_t s);
+                          void *rays, cudaStream_t s, int ld = 0);
 // Queues of one specular level (render.cu, SpecArgs): the input level's
 // rays / weights / camera samples / tree nodes / count and the next level's.
 struct SpecQueues {
@@ -83,7 +84,8 @@ struct SpecQueues {
 cudaError_t launch_shade(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin, int spp,
                          int slots, int n_light_samples, const void *rays, const void *hits, float *contrib,
                          void *srays, int *starget, float *srgb, int *scount, void *brays, int *btarget, float *brgb,
-                         int *bcount, float *bnrm, int block, cudaStream_t s, const SpecQueues *spec = nullptr);
+                         int *bcount, float *bnrm, int block, cudaStream_t s, const SpecQueues *spec = nullptr,
+                         int ld = 0);
 // One specular level: shades entries [0, min(*spec.in_count, capacity)) of
 // spec.in_* (hits: their closest hits) at specular depth `depth`, adding
 // weight x (emission + direct lighting) into each entry's sample slot
@@ -123,7 +125,7 @@ cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_
                                  int n_light_samples, const float *dfilm, float *g_albedo, double *g_emission,
                                  const void *rays, const void *hits, void *srays, int *stri, float *s_dkd,
                                  float *s_dem, int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
-                                 int *bcount, float *bnrm, const float *tcam, cudaStream_t s);
+                                 int *bcount, float *bnrm, const float *tcam, cudaStream_t s, int ld = 0);
 cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                                    const int *stri, const float *s_dkd, const float *s_dem, const int *scount,
                                    const void *brays, const void *bhits, const int *btri, const float *b_dkd,

@@ -52,7 +52,7 @@ __device__ __forceinline__ int find_view(const ViewDev *__restrict__ views, int 
 
 // Camera rays for the samples of global pixels [px_begin, px_begin + n_px).
 __global__ void k_camera(const ViewDev *__restrict__ views, int n_views, int64_t px_begin, int n_px, int sppx,
-                         int sppy, float4 *__restrict__ rays) {
+                         int sppy, int ld, float4 *__restrict__ rays) {
   const int spp = sppx * sppy;
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= (int64_t)n_px * spp) return;
@@ -63,9 +63,18 @@ __global__ void k_camera(const ViewDev *__restrict__ views, int n_views, int64_t
   const int64_t px = P - views[v].px_begin;
   const int x = (int)(px % cam.width), y = (int)(px / cam.width);
   const uint64_t gid = (uint64_t)px * spp + j, seed = views[v].seed;
-  // stratified, jittered pixel sample (StratifiedSampling2D)
-  const double ix = x + ((j % sppx) + (double)rnd(seed, gid, 0)) / sppx;
-  const double iy = y + ((j / sppx) + (double)rnd(seed, gid, 1)) / sppy;
+  double ix, iy;
+  if (ld) {
+    // LDSampler image points: one scrambled (0,2)-sequence point per sample
+    float u0, u1;
+    ld_2d(seed, (uint64_t)px, 0, (uint32_t)j, (uint32_t)spp, 0, 1, u0, u1);
+    ix = x + (double)u0;
+    iy = y + (double)u1;
+  } else {
+    // stratified, jittered pixel sample (StratifiedSampling2D)
+    ix = x + ((j % sppx) + (double)rnd(seed, gid, 0)) / sppx;
+    iy = y + ((j / sppx) + (double)rnd(seed, gid, 1)) / sppy;
+  }
   // PerspectiveCamera::GenerateRay (pinhole)
   const double cx = 2.0 * cam.x_tan * (ix - cam.width * 0.5) / cam.width;
   const double cy = 2.0 * cam.y_tan * (iy - cam.height * 0.5) / cam.height;
@@ -123,7 +132,28 @@ struct ShadeArgs {
   const ViewDev *views;
   int n_views;
   const float *tcam;   // per sample: transmittance of the camera ray's medium segment (null: no medium)
+  int ld;              // camera level: light and BSDF samples from the LDSampler's sequences
 };
+
+// The random numbers of light sample k (light choice uc, position u0, u1)
+// or BSDF sample k (component uc, direction u0, u1) of a camera-level
+// entry: the LDSampler's four sequences (light 1D, light 2D, BSDF 1D, BSDF
+// 2D; DirectLightingIntegrator.cpp:41-50) or the counter-based stream.
+__device__ __forceinline__ void direct_sample(const ShadeArgs &A, bool ld, uint64_t seed, uint64_t gid, bool bsdf,
+                                              int k, float &uc, float &u0, float &u1) {
+  const int nl = A.n_light_samples;
+  if (ld) {
+    const uint32_t spp = (uint32_t)A.spp, j = (uint32_t)(gid % spp);
+    const uint64_t px = gid / spp;
+    uc = ld_1d(seed, px, bsdf ? 3 : 1, j, spp, (uint32_t)k, (uint32_t)nl);
+    ld_2d(seed, px, bsdf ? 4 : 2, j, spp, (uint32_t)k, (uint32_t)nl, u0, u1);
+    return;
+  }
+  const uint32_t d = bsdf ? 2 + 3 * nl + 3 * k : 2 + 3 * k;
+  uc = rnd(seed, gid, d);
+  u0 = rnd(seed, gid, d + 1);
+  u1 = rnd(seed, gid, d + 2);
+}
 
 // Adjoint pass (ADJ = true).  The same rays as the forward pass are traced
 // (same random numbers), but instead of radiance each queued ray carries the
@@ -226,8 +256,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
     float dem = 0.0f;
     float tmin = 0.0f, tmax = 0.0f;
     if (surface && S.n_area_lights > 0) {
-      const float uc = rnd(seed, gid, 2 + 3 * k), u0 = rnd(seed, gid, 3 + 3 * k),
-                  u1 = rnd(seed, gid, 4 + 3 * k);
+      float uc, u0, u1;
+      direct_sample(A, !SPEC && A.ld, seed, gid, false, k, uc, u0, u1);
       // the light by IrradianceLightsSamplingStrategy at this point, with
       // the shading normal turned to the viewer (reflection-only BSDFs,
       // DirectLightingIntegrator.cpp:107-111)
@@ -322,8 +352,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
     V3 val = v3(0, 0, 0), dir = v3(0, 0, 0), dkd = v3(0, 0, 0);
     float pdf = 0.0f, tmin = 0.0f;
     if (surface && S.n_area_lights > 0) {
-      const float uc = rnd(seed, gid, 2 + 3 * nl + 3 * k), u0 = rnd(seed, gid, 3 + 3 * nl + 3 * k),
-                  u1 = rnd(seed, gid, 4 + 3 * nl + 3 * k);
+      float uc, u0, u1;
+      direct_sample(A, !SPEC && A.ld, seed, gid, true, k, uc, u0, u1);
       const V3 f = bsdf_sample(b, wo, uc, u0, u1, dir, pdf);
       if (pdf > 0.0f && !black(f)) {
         val = f * (fabsf(dot(dir, shading_n)) / (pdf * nl));
@@ -695,20 +725,21 @@ __global__ void k_film(const float *__restrict__ contrib, int64_t px_begin, int 
 }  // namespace
 
 cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, int n_px, int sppx, int sppy,
-                          void *rays, cudaStream_t s) {
+                          void *rays, cudaStream_t s, int ld) {
   const int64_t n = (int64_t)n_px * sppx * sppy;
   if (n <= 0) return cudaSuccess;
-  k_camera<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(views, n_views, px_begin, n_px, sppx, sppy, (float4 *)rays);
+  k_camera<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(views, n_views, px_begin, n_px, sppx, sppy, ld,
+                                                       (float4 *)rays);
   return cudaGetLastError();
 }
 
 cudaError_t launch_shade(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin, int spp,
                          int slots, int n_light_samples, const void *rays, const void *hits, float *contrib,
                          void *srays, int *starget, float *srgb, int *scount, void *brays, int *btarget, float *brgb,
-                         int *bcount, float *bnrm, int block, cudaStream_t s, const SpecQueues *spec) {
+                         int *bcount, float *bnrm, int block, cudaStream_t s, const SpecQueues *spec, int ld) {
   if (n <= 0) return cudaSuccess;
   if (block != 64) block = 128;
-  ShadeArgs A{n, px_begin, spp, slots, n_light_samples, views, n_views, nullptr};
+  ShadeArgs A{n, px_begin, spp, slots, n_light_samples, views, n_views, nullptr, ld};
   SpecArgs Q{};
   if (spec) {
     Q.out_rays = (float4 *)spec->out_rays;
@@ -736,7 +767,7 @@ cudaError_t launch_shade_specular(const SceneDev &S, const ViewDev *views, int n
                                   int *scount, void *brays, int *btarget, float *brgb, int *bcount, float *bnrm,
                                   cudaStream_t s) {
   if (capacity <= 0) return cudaSuccess;
-  ShadeArgs A{(int)capacity, px_begin, spp, slots, n_light_samples, views, n_views, nullptr};
+  ShadeArgs A{(int)capacity, px_begin, spp, slots, n_light_samples, views, n_views, nullptr, 0};
   SpecArgs Q{spec.in_w,      spec.in_sample, spec.in_node,  spec.in_count, (float4 *)spec.out_rays,
              spec.out_w,     spec.out_sample, spec.out_node, spec.out_count, depth,
              spec.spec_slot};
@@ -755,9 +786,9 @@ cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_
                                  int n_light_samples, const float *dfilm, float *g_albedo, double *g_emission,
                                  const void *rays, const void *hits, void *srays, int *stri, float *s_dkd,
                                  float *s_dem, int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
-                                 int *bcount, float *bnrm, const float *tcam, cudaStream_t s) {
+                                 int *bcount, float *bnrm, const float *tcam, cudaStream_t s, int ld) {
   if (n <= 0) return cudaSuccess;
-  ShadeArgs A{n, px_begin, spp, 0, n_light_samples, views, n_views, tcam};
+  ShadeArgs A{n, px_begin, spp, 0, n_light_samples, views, n_views, tcam, ld};
   AdjointArgs J{dfilm, g_albedo, g_emission, s_dkd, s_dem, b_dkd};
   k_shade<true, false, false><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
       S, A, J, SpecArgs{}, (const float4 *)rays, (const int4 *)hits, nullptr, (float4 *)srays, stri, nullptr, scount,

@@ -28,6 +28,55 @@ __device__ __forceinline__ float rnd(uint64_t seed, uint64_t sample, uint32_t di
   return (float)(z >> 40) * (1.0f / 16777216.0f);  // 24 bits: in [0, 1)
 }
 
+// ------------------------------------------------------ low discrepancy --
+// LDSampler (Samplers/LDSampler.cpp:91-190): per pixel and per requested
+// sequence, spp groups of L points of one scrambled (0,2)-sequence
+// (VanDerCorput x Sobol2, SamplingRoutines.h:468-490), the groups dealt to
+// the pixel's samples in a random order and the points of a group in a
+// random order.  The scrambles and orders come from a hash of (seed, pixel,
+// sequence) instead of the reference's generator; the orders are affine
+// permutations j -> (a j + b) mod m (a odd, m a power of two).
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ uint32_t affine_perm(uint32_t j, uint32_t m, uint64_t h) {
+  return ((uint32_t)(h | 1u) * j + (uint32_t)(h >> 32)) & (m - 1u);
+}
+__device__ __forceinline__ float van_der_corput(uint32_t n, uint32_t scramble) {
+  return (float)((__brev(n) ^ scramble) >> 8) * (1.0f / 16777216.0f);
+}
+__device__ __forceinline__ float sobol2(uint32_t n, uint32_t scramble) {
+  for (uint32_t v = 1u << 31; n != 0; n >>= 1, v ^= v >> 1)
+    if (n & 1u) scramble ^= v;
+  return (float)(scramble >> 8) * (1.0f / 16777216.0f);
+}
+// Point index of element e (of L) of sequence `seq` for sample j (of spp)
+// of pixel px, and the sequence's two scrambles.
+__device__ __forceinline__ uint32_t ld_index(uint64_t seed, uint64_t px, uint32_t seq, uint32_t j, uint32_t spp,
+                                             uint32_t e, uint32_t L, uint32_t &s1, uint32_t &s2) {
+  const uint64_t h = mix64(seed + 0x9E3779B97F4A7C15ull * (px * 16ull + seq + 1ull));
+  const uint64_t hs = mix64(h ^ 0x632BE59BD9B4E019ull);
+  s1 = (uint32_t)hs;
+  s2 = (uint32_t)(hs >> 32);
+  const uint32_t group = affine_perm(j, spp, mix64(h + 1ull));
+  const uint32_t elem = L > 1u ? affine_perm(e, L, mix64(h + 2ull + j)) : 0u;
+  return group * L + elem;
+}
+__device__ __forceinline__ float ld_1d(uint64_t seed, uint64_t px, uint32_t seq, uint32_t j, uint32_t spp, uint32_t e,
+                                       uint32_t L) {
+  uint32_t s1, s2;
+  return van_der_corput(ld_index(seed, px, seq, j, spp, e, L, s1, s2), s1);
+}
+__device__ __forceinline__ void ld_2d(uint64_t seed, uint64_t px, uint32_t seq, uint32_t j, uint32_t spp, uint32_t e,
+                                      uint32_t L, float &u0, float &u1) {
+  uint32_t s1, s2;
+  const uint32_t i = ld_index(seed, px, seq, j, spp, e, L, s1, s2);
+  u0 = van_der_corput(i, s1);
+  u1 = sobol2(i, s2);
+}
+
 // ----------------------------------------------------------------- vectors --
 struct V3 {
   float x, y, z;

@@ -365,6 +365,7 @@ struct Plan {
   std::vector<skw::ViewDev> views;
   std::vector<int64_t> film_offset;  // floats
   int sppx = 1, sppy = 1, spp = 1, nl = 0, npl = 0, slots = 1;
+  int ld = 0;  // LDSampler (sppx = spp, a power of two; sppy = 1)
   int64_t n_px_total = 0, chunk_px = 0, cap_samples = 0, cap_shadow = 0, cap_bsdf = 0;
   bool media = false;
   int media_slot = 0;
@@ -455,7 +456,9 @@ int plan_make(skw_scene *s, const skw_camera *cams, int n_views, const skw_rende
   skw_ctx *ctx = s->ctx;
   if (n_views <= 0 || n_views > (1 << 20)) return fail(ctx, SKW_ERR_ARG, "bad number of views");
   if (params->spp_x <= 0 || params->spp_y <= 0 || params->spp_x > 1024 || params->spp_y > 1024 ||
-      params->light_samples < 0 || params->light_samples > 64)
+      params->light_samples < 0 || params->light_samples > 64 ||
+      (params->sampler != SKW_SAMPLER_STRATIFIED && params->sampler != SKW_SAMPLER_LD) ||
+      (params->sampler == SKW_SAMPLER_LD && (int64_t)params->spp_x * params->spp_y > 4096))
     return fail(ctx, SKW_ERR_ARG, "bad render parameters");
   if (cfg.stack_cap != 0 && (!valid_cap(cfg.stack_cap) || cfg.stack_cap < s->accel->stack_cap))
     return fail(ctx, SKW_ERR_ARG, "stack_cap must be 48, 96, 192 or 416 and cover the tree's depth");
@@ -481,8 +484,17 @@ int plan_make(skw_scene *s, const skw_camera *cams, int n_views, const skw_rende
   }
   P->sppx = params->spp_x;
   P->sppy = params->spp_y;
-  P->spp = P->sppx * P->sppy;
   P->nl = params->light_samples;
+  P->ld = params->sampler == SKW_SAMPLER_LD;
+  if (P->ld) {  // LDSampler / Sampler::AddSamplesSequence*: counts rounded up to powers of two
+    int spp = 1, nl = 1;
+    while (spp < P->sppx * P->sppy) spp <<= 1;
+    while (nl < P->nl) nl <<= 1;
+    P->sppx = spp;
+    P->sppy = 1;
+    if (P->nl > 0) P->nl = nl;
+  }
+  P->spp = P->sppx * P->sppy;
   P->npl = s->dev.n_point_lights;
   P->media = cfg.media && s->dev.medium.on;
   P->spec_levels = cfg.specular && s->dev.has_specular ? s->dev.max_spec_depth + 1 : 0;
@@ -606,7 +618,7 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
   cudaError_t e;
   if ((e = cudaMemsetAsync(W.contrib, 0, (size_t)n * P.slots * 12, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(W.counts, 0, 5 * sizeof(int), st)) != cudaSuccess) return e;
-  if ((e = skw::launch_camera(d_views, nv, px0, n_px, P.sppx, P.sppy, W.rays, st)) != cudaSuccess) return e;
+  if ((e = skw::launch_camera(d_views, nv, px0, n_px, P.sppx, P.sppy, W.rays, st, P.ld)) != cudaSuccess) return e;
   if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr, W.hits,
                                  a->d_status, st, ctas)) != cudaSuccess)
     return e;
@@ -622,7 +634,7 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
   }
   if ((e = skw::launch_shade(s->dev, d_views, nv, n, px0, P.spp, P.slots, P.nl, W.rays, W.hits, W.contrib, W.srays,
                              W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb, W.counts + 1, W.bnrm,
-                             P.cfg.shade_block, st, P.spec_levels ? &sq : nullptr)) != cudaSuccess)
+                             P.cfg.shade_block, st, P.spec_levels ? &sq : nullptr, P.ld)) != cudaSuccess)
     return e;
   const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
   if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts, a->scene_abs,
@@ -1035,14 +1047,15 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
     const int n_px = (int)std::min<int64_t>(P.chunk_px, P.n_px_total - px0);
     const int n = n_px * P.spp, cap = P.cfg.stack_cap;
     if ((e = cudaMemsetAsync(W.counts, 0, 3 * sizeof(int), st)) != cudaSuccess) break;
-    if ((e = skw::launch_camera(d_view, 1, px0, n_px, P.sppx, P.sppy, W.rays, st)) != cudaSuccess) break;
+    if ((e = skw::launch_camera(d_view, 1, px0, n_px, P.sppx, P.sppy, W.rays, st, P.ld)) != cudaSuccess) break;
     if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr,
                                    W.hits, a->d_status, st)) != cudaSuccess)
       break;
     if (P.media && (e = record_media(s, P, W, d_view, px0, n, true, d_film, g_emission, st)) != cudaSuccess) break;
     if ((e = skw::launch_shade_adjoint(s->dev, d_view, 1, n, px0, P.spp, P.nl, d_film, g_albedo, g_emission, W.rays,
                                        W.hits, W.srays, W.starget, s_dkd, s_dem, W.counts, W.brays, W.btarget, b_dkd,
-                                       W.brgb, W.counts + 1, W.bnrm, P.media ? W.tcam : nullptr, st)) != cudaSuccess)
+                                       W.brgb, W.counts + 1, W.bnrm, P.media ? W.tcam : nullptr, st, P.ld)) !=
+        cudaSuccess)
       break;
     const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
     if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts,
@@ -1082,7 +1095,10 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
   // the sampler rounds sequence lengths up to squares (Sampler.cpp:39-57, StratifiedSampler.cpp:33-37)
   int gs = 0;
-  if (pp->gather_samples > 0) {
+  if (pp->gather_samples > 0 && params->sampler == SKW_SAMPLER_LD) {  // LDSampler: powers of two
+    gs = 1;
+    while (gs < pp->gather_samples) gs <<= 1;
+  } else if (pp->gather_samples > 0) {
     const int r = (int)std::ceil(std::sqrt((double)pp->gather_samples));
     gs = r * r;
   }

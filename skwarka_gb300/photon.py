@@ -88,19 +88,19 @@ class skw_photon_render_params(C.Structure):
 
 def render_photon(scene, photon_map: PhotonMap, camera, spp_x: int = 2, spp_y: int = 2, light_samples: int = 1,
                   gather_samples: int = 16, seed: int = 0, out=None, stream=None, caustic_lookup: int = 50,
-                  max_caustic_dist: float = 0.1):
+                  max_caustic_dist: float = 0.1, sampler: int = 0):
     """Photon-mapping render (emission + direct lighting + caustic-map
     radiance + final gather) into a CUDA float32 tensor (h, w, 3).
     caustic_lookup / max_caustic_dist: the caustic estimate's photon count
     and radius (PhotonLTEIntegratorParams); used when the map has caustic
-    photons."""
+    photons.  sampler: render.STRATIFIED or render.LD."""
     import torch
     from .render import c_camera, skw_render_params
     if out is None:
         out = torch.empty((camera.height, camera.width, 3), dtype=torch.float32, device="cuda")
     s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
     cam = c_camera(camera)
-    par = skw_render_params(spp_x, spp_y, light_samples, seed)
+    par = skw_render_params(spp_x, spp_y, light_samples, seed, sampler)
     pp = skw_photon_render_params(gather_samples, caustic_lookup, max_caustic_dist)
     _lib.check(_lib.load().skw_render_photon(scene.handle, photon_map.handle, C.byref(cam), C.byref(par), C.byref(pp),
                                              out.data_ptr(), s), scene.ctx.handle)

@@ -154,7 +154,11 @@ class skw_camera(C.Structure):
 
 
 class skw_render_params(C.Structure):
-    _fields_ = [("spp_x", C.c_int32), ("spp_y", C.c_int32), ("light_samples", C.c_int32), ("seed", C.c_uint64)]
+    _fields_ = [("spp_x", C.c_int32), ("spp_y", C.c_int32), ("light_samples", C.c_int32), ("seed", C.c_uint64),
+                ("sampler", C.c_int32)]
+
+
+STRATIFIED, LD = 0, 1  # SKW_SAMPLER_STRATIFIED (StratifiedSampler), SKW_SAMPLER_LD (LDSampler)
 
 
 def c_material(m: Material, measured_handle=None) -> skw_material:
@@ -242,14 +246,15 @@ class RenderScene:
             self.handle = None
 
     def render_direct(self, camera: Camera, spp_x: int = 2, spp_y: int = 2, light_samples: int = 1, seed: int = 0,
-                      out=None, stream=None):
-        """Renders into a CUDA float32 tensor (height, width, 3) and returns it."""
+                      out=None, stream=None, sampler: int = STRATIFIED):
+        """Renders into a CUDA float32 tensor (height, width, 3) and returns it.
+        sampler=LD: LDSampler with spp_x * spp_y samples per pixel."""
         import torch
         if out is None:
             out = torch.empty((camera.height, camera.width, 3), dtype=torch.float32, device="cuda")
         s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         cam = c_camera(camera)
-        par = skw_render_params(spp_x, spp_y, light_samples, seed)
+        par = skw_render_params(spp_x, spp_y, light_samples, seed, sampler)
         _lib.check(_lib.load().skw_render_direct(self.handle, C.byref(cam), C.byref(par), out.data_ptr(), s),
                    self.ctx.handle)
         return out
@@ -262,12 +267,13 @@ class RenderBatch:
     seed."""
 
     def __init__(self, scene: RenderScene, cameras: list[Camera], spp_x: int = 2, spp_y: int = 2,
-                 light_samples: int = 1, seed: int = 0, seeds=None, config: dict | None = None):
+                 light_samples: int = 1, seed: int = 0, seeds=None, config: dict | None = None,
+                 sampler: int = STRATIFIED):
         import numpy as np
         lib = _lib.load()
         self.scene, self.cameras = scene, list(cameras)
         cams = (skw_camera * len(cameras))(*[c_camera(c) for c in cameras])
-        par = skw_render_params(spp_x, spp_y, light_samples, seed)
+        par = skw_render_params(spp_x, spp_y, light_samples, seed, sampler)
         self._seeds = None if seeds is None else np.ascontiguousarray(seeds, np.uint64)
         cfg = None
         if config is not None:

@@ -209,3 +209,15 @@ def specular_golden():
 
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "specular":
     specular_golden()
+
+
+def ld_golden():
+    """The reference's direct-lighting render of the box (64 x 64) with its
+    LDSampler at 4 samples per pixel (ConsecutiveImagePixelsOrder)."""
+    prims, mats, cam = scenes.direct_lighting_box()
+    img, _ = Reference().render_direct(prims, mats, [], cam(64, 64), 2, 2, ld=True)
+    np.savez_compressed(OUT / "ld_box_64.npz", ref_ld_4=img)
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "ld":
+    ld_golden()
