@@ -385,7 +385,7 @@ typedef struct skw_photon_map skw_photon_map;
 
 typedef struct skw_photon_params {
   int64_t paths;          /* photon paths to shoot (ShootPhotons(i_photons)) */
-  int32_t max_bounces;    /* intersections per path, 1..64 (the reference has no cap) */
+  int32_t max_bounces;    /* intersections per path, 1..1024 (the reference has no cap) */
   float rr_probability;   /* 0: Russian roulette with the reference's luminance ratio
                              (PhotonShootingPipeline.cpp:243-250); > 0: that fixed
                              continue probability */

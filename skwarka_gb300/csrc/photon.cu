@@ -89,6 +89,14 @@ struct Queue {
 
 constexpr int kDiffusePath = 1 << 30;
 
+// The path's random numbers at bounce >= 1: 4 per bounce; bounces 0-15 use
+// numbers 0-63 of the path's counter-based stream, later blocks of 16
+// bounces re-seeded streams (a path's stream holds 64 numbers).
+__device__ __forceinline__ float bounce_rnd(uint64_t seed, uint64_t path, int bounce, int k) {
+  const uint64_t s = bounce < 16 ? seed : seed ^ (0xD6E8FEB86659FD93ull * (uint64_t)(bounce >> 4));
+  return rnd(s, path, (uint32_t)(4 * (bounce & 15) + k));
+}
+
 // BSDF::Sample over all components of a specular-only (transparent) BSDF
 // (Core/BSDF.cpp:72-117, _SampleSpecularOnly): each component's Sample
 // (SpecularReflection: mirror direction, r F; SpecularTransmission:
@@ -317,9 +325,9 @@ __global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootAr
         u1 = (float)radical_inverse(pi, 19);
         uc = (float)radical_inverse(pi, 23);
       } else {
-        u0 = rnd(A.seed, gp, 4 * bounce);
-        u1 = rnd(A.seed, gp, 4 * bounce + 1);
-        uc = rnd(A.seed, gp, 4 * bounce + 2);
+        u0 = bounce_rnd(A.seed, gp, bounce, 0);
+        u1 = bounce_rnd(A.seed, gp, bounce, 1);
+        uc = bounce_rnd(A.seed, gp, bounce, 2);
       }
       V3 ex;
       float pdf = 0.0f;
@@ -333,7 +341,7 @@ __global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootAr
           const float lw = luminance(w);
           p = lw > 0.0f ? fminf(1.0f, luminance(wnew) / lw) : 0.0f;
         }
-        const float r = rnd(A.seed, gp, 4 * bounce + 3);
+        const float r = bounce_rnd(A.seed, gp, bounce, 3);
         if (!(r > p) && p > 0.0f) {
           wnew = wnew * (1.0f / p);
           o = h.p;
@@ -518,6 +526,14 @@ cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, cons
     k_photon_bounce<<<grid, 128, 0, st>>>(S, A, path0, b, n_paths, in, hits, out, st_direct, has_direct,
                                           st_indirect, n_indirect, st_caustic, has_caustic);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (A.max_bounces > 16 && (b & 7) == 7 && b + 1 < A.max_bounces) {
+      // long caps: stop launching once every path of the chunk has ended
+      int left = 0;
+      if ((e = cudaMemcpyAsync(&left, out.count, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+          (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return e;
+      if (left == 0) break;
+    }
   }
   // direct: one per path; indirect: n_indirect[path] per path
   k_scan_blocks<uint8_t><<<nb, kScanBlock, 0, st>>>(has_direct, n_paths, 1, excl[0], bsum[0]);

@@ -272,7 +272,7 @@ int skw_photon_shoot(skw_scene *s, const skw_photon_params *params, skw_photon_m
   skw_ctx *ctx = s->ctx;
   *out = nullptr;
   if (params->paths <= 0 || params->paths > ((int64_t)1 << 31) || params->max_bounces < 1 ||
-      params->max_bounces > 64 || !(params->rr_probability >= 0.0f) || params->rr_probability > 1.0f)
+      params->max_bounces > 1024 || !(params->rr_probability >= 0.0f) || params->rr_probability > 1.0f)
     return fail(ctx, SKW_ERR_ARG, "bad photon parameters");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
@@ -314,7 +314,10 @@ int skw_photon_shoot(skw_scene *s, const skw_photon_params *params, skw_photon_m
     return skw::launch_traversal(true, a->stack_cap, a->d_nodes, a->d_tris, rays, n, n_dev, a->scene_abs, nullptr,
                                  hits, a->d_status, st);
   };
-  const int64_t chunk = std::min<int64_t>(params->paths, (int64_t)1 << 20);
+  // per-path deposit slots for every bounce: 2^20 paths per chunk up to 64
+  // bounces, proportionally fewer above
+  const int64_t chunk = std::min<int64_t>(
+      params->paths, std::max<int64_t>((int64_t)1 << 12, ((int64_t)1 << 26) / std::max(params->max_bounces, 64)));
   const int64_t B1 = std::max(params->max_bounces - 1, 1);
   void *ws = nullptr;
   PhotonRec *d_dir = nullptr, *d_ind = nullptr, *d_cau = nullptr;

@@ -74,18 +74,17 @@ def test_photon_shooting_through_glass(gpu):
     the reference's ShootPhotons over the same paths.  Direct photons (first
     hits; radical-inverse emission) within 0.5 %; caustic photons (floor hits
     after specular bounces only) in count within 3 %, centroid within 0.01 and
-    spread within 2 %; indirect photons on the floor within 8 %.  Most
+    spread within 2 %; indirect photons on the floor within 5 %.  Most
     indirect photons lie on the glass itself: photons trapped by total
     internal reflection inside the faceted sphere, whose number of bounces
     before numerical error lets them out depends on each implementation's
     arithmetic (double in the reference, float here), compared within 12 %.
-    The GPU ends a path after 64 hits (the reference has no limit); in this
-    scene that ends about 3 % of the paths that would still reach the floor
-    (a double-precision restatement of the walk: 408 floor photons per
-    200,000 paths with the cap, 420 without)."""
+    The reference has no bounce limit; the GPU's is set to 1024 here (with
+    the default 64 a double-precision restatement of the walk loses ~3 % of
+    the floor photons and ~8 % of those on the glass)."""
     prims, mats, lights, cam = sf.specular_cases()["glass_point"]
     sc = RenderScene(prims, mats, lights)
-    pm = PhotonMap.shoot(sc, 2_000_000, max_bounces=64, seed=5)
+    pm = PhotonMap.shoot(sc, 2_000_000, max_bounces=1024, seed=5)
     info = pm.info()
     g = np.load(GOLD)
     want = g["photon_counts"]
@@ -96,7 +95,7 @@ def test_photon_shooting_through_glass(gpu):
           f"reference {want.tolist()}")
     assert abs(got[1] / want[1] - 1) <= 0.005
     assert abs(got[0] / want[0] - 1) <= 0.03
-    assert abs(got[3] / want[3] - 1) <= 0.08
+    assert abs(got[3] / want[3] - 1) <= 0.05
     assert abs(got[2] / want[2] - 1) <= 0.12
     assert info["paths_caustic"] == 2_000_000
     c = pm.export("caustic")["position"]
@@ -124,7 +123,7 @@ def test_specular_photon_render_matches_reference(gpu, name):
     prims, mats, lights, cam = sf.specular_cases()[name]
     sc = RenderScene(prims, mats, lights)
     sc.set_max_specular_depth(6)
-    pm = PhotonMap.shoot(sc, 1_000_000, seed=11)
+    pm = PhotonMap.shoot(sc, 1_000_000, max_bounces=1024, seed=11)
     img = render_photon(sc, pm, cam, 8, 8, gather_samples=16, seed=13).cpu().numpy()
     direct = sc.render_direct(cam, 8, 8, seed=13).cpu().numpy()
     assert np.isfinite(img).all() and (img >= 0).all()
