@@ -363,10 +363,12 @@ int skw_scene_set_medium(skw_scene *scene, const skw_medium *medium);
  * Core/LTEIntegrator.cpp:66-126).  Default 10 (the GUI's default); range
  * [0, 11]: every branch of every sample's tree is given room, so a render
  * pass holds at most 2^22 >> (max_depth + 1) camera samples.  Scenes with
- * specular materials cannot have a medium (SKW_ERR_UNSUPPORTED) and the
- * adjoint rejects them; photon shooting follows specular bounces (caustic
- * map) and the photon-map render adds caustic radiance and the final gather
- * at the diffuse hits of every level (PhotonLTEIntegrator.cpp:320-385). */
+ * specular materials cannot have a medium (SKW_ERR_UNSUPPORTED); the
+ * adjoint replays the same trees (a transparent surface's reflectance is
+ * its material's, never a per-triangle albedo); photon shooting follows
+ * specular bounces (caustic map) and the photon-map render adds caustic
+ * radiance and the final gather at the diffuse hits of every level
+ * (PhotonLTEIntegrator.cpp:320-385). */
 int skw_scene_set_max_specular_depth(skw_scene *scene, int32_t max_depth);
 
 /* ---- Photon maps (PhotonLTEIntegrator, LTEIntegrators/PhotonLTEIntegrator/*).

@@ -125,7 +125,15 @@ cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_
                                  int n_light_samples, const float *dfilm, float *g_albedo, double *g_emission,
                                  const void *rays, const void *hits, void *srays, int *stri, float *s_dkd,
                                  float *s_dem, int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
-                                 int *bcount, float *bnrm, const float *tcam, cudaStream_t s, int ld = 0);
+                                 int *bcount, float *bnrm, const float *tcam, cudaStream_t s, int ld = 0,
+                                 const SpecQueues *spec = nullptr);
+// Adjoint of one specular level (the entries' weights multiply dL/dI).
+cudaError_t launch_shade_specular_adjoint(const SceneDev &S, const ViewDev *views, int n_views, int64_t capacity,
+                                          int64_t px_begin, int spp, int n_light_samples, const float *dfilm,
+                                          float *g_albedo, double *g_emission, const SpecQueues &spec, int depth,
+                                          const void *hits, void *srays, int *stri, float *s_dkd, float *s_dem,
+                                          int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
+                                          int *bcount, float *bnrm, cudaStream_t s);
 cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                                    const int *stri, const float *s_dkd, const float *s_dem, const int *scount,
                                    const void *brays, const void *bhits, const int *btri, const float *b_dkd,

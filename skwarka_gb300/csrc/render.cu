@@ -224,6 +224,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
     if (ADJ && valid) {
       dI = load3(J.dfilm + 3 * P) * (1.0f / A.spp);
       if (A.tcam) dI = mul(dI, load3(A.tcam + 3 * (int64_t)i));
+      if (SPEC) dI = mul(dI, wt);  // a specular level's terms carry the entry's weight
     }
   }
   const float escale = S.emission_scale;
@@ -380,7 +381,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
   }
   if (ADJ) add_emission_grad(J.g_emission, g_em);
   // Specular children (reflection, then transmission) while the depth allows.
-  if (!ADJ && KIDS) {
+  if (KIDS) {
     const bool deeper = surface && b.kind == kTransparent && Q.depth <= S.max_spec_depth;
     for (int c = 0; c < 2; ++c) {
       V3 dir = v3(0, 0, 0), val = v3(0, 0, 0);
@@ -786,13 +787,50 @@ cudaError_t launch_shade_adjoint(const SceneDev &S, const ViewDev *views, int n_
                                  int n_light_samples, const float *dfilm, float *g_albedo, double *g_emission,
                                  const void *rays, const void *hits, void *srays, int *stri, float *s_dkd,
                                  float *s_dem, int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
-                                 int *bcount, float *bnrm, const float *tcam, cudaStream_t s, int ld) {
+                                 int *bcount, float *bnrm, const float *tcam, cudaStream_t s, int ld,
+                                 const SpecQueues *spec) {
   if (n <= 0) return cudaSuccess;
   ShadeArgs A{n, px_begin, spp, 0, n_light_samples, views, n_views, tcam, ld};
   AdjointArgs J{dfilm, g_albedo, g_emission, s_dkd, s_dem, b_dkd};
-  k_shade<true, false, false><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
-      S, A, J, SpecArgs{}, (const float4 *)rays, (const int4 *)hits, nullptr, (float4 *)srays, stri, nullptr, scount,
-      (float4 *)brays, btri, brgb, bcount, bnrm);
+  SpecArgs Q{};
+  if (spec) {
+    Q.out_rays = (float4 *)spec->out_rays;
+    Q.out_w = spec->out_w;
+    Q.out_sample = spec->out_sample;
+    Q.out_node = spec->out_node;
+    Q.out_count = spec->out_count;
+  }
+  if (spec)
+    k_shade<true, false, true><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
+        S, A, J, Q, (const float4 *)rays, (const int4 *)hits, nullptr, (float4 *)srays, stri, nullptr, scount,
+        (float4 *)brays, btri, brgb, bcount, bnrm);
+  else
+    k_shade<true, false, false><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
+        S, A, J, Q, (const float4 *)rays, (const int4 *)hits, nullptr, (float4 *)srays, stri, nullptr, scount,
+        (float4 *)brays, btri, brgb, bcount, bnrm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade_specular_adjoint(const SceneDev &S, const ViewDev *views, int n_views, int64_t capacity,
+                                          int64_t px_begin, int spp, int n_light_samples, const float *dfilm,
+                                          float *g_albedo, double *g_emission, const SpecQueues &spec, int depth,
+                                          const void *hits, void *srays, int *stri, float *s_dkd, float *s_dem,
+                                          int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
+                                          int *bcount, float *bnrm, cudaStream_t s) {
+  if (capacity <= 0) return cudaSuccess;
+  ShadeArgs A{(int)capacity, px_begin, spp, 0, n_light_samples, views, n_views, nullptr, 0};
+  AdjointArgs J{dfilm, g_albedo, g_emission, s_dkd, s_dem, b_dkd};
+  SpecArgs Q{spec.in_w,      spec.in_sample, spec.in_node,  spec.in_count, (float4 *)spec.out_rays,
+             spec.out_w,     spec.out_sample, spec.out_node, spec.out_count, depth,
+             0};
+  if (spec.out_count)
+    k_shade<true, true, true><<<(unsigned)((capacity + 127) / 128), 128, 0, s>>>(
+        S, A, J, Q, (const float4 *)spec.in_rays, (const int4 *)hits, nullptr, (float4 *)srays, stri, nullptr, scount,
+        (float4 *)brays, btri, brgb, bcount, bnrm);
+  else
+    k_shade<true, true, false><<<(unsigned)((capacity + 127) / 128), 128, 0, s>>>(
+        S, A, J, Q, (const float4 *)spec.in_rays, (const int4 *)hits, nullptr, (float4 *)srays, stri, nullptr, scount,
+        (float4 *)brays, btri, brgb, bcount, bnrm);
   return cudaGetLastError();
 }
 

@@ -452,7 +452,7 @@ __device__ Bsdf make_bsdf(const SceneDev &S, const Hit &h, int prim) {
   b.e2 = cross(b.n, b.e1);
   b.kind = m.kind;
   b.kd = load3(m.kd);
-  if (S.tri_albedo) {
+  if (S.tri_albedo && m.kind != kTransparent) {  // a transparent surface's reflectance is the material's
     const float *ta = S.tri_albedo + 3 * (int64_t)h.g;
     if (ta[0] == ta[0]) b.kd = v3(fminf(1.0f, fmaxf(0.0f, ta[0])), fminf(1.0f, fmaxf(0.0f, ta[1])),
                                   fminf(1.0f, fmaxf(0.0f, ta[2])));

@@ -1019,8 +1019,6 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
   if (!s || !cam || !params || !d_film || !g_albedo || !g_emission)
     return fail(s ? s->ctx : nullptr, SKW_ERR_ARG, "null argument");
   skw_ctx *ctx = s->ctx;
-  if (s->dev.has_specular)
-    return fail(ctx, SKW_ERR_UNSUPPORTED, "the adjoint covers diffuse / glossy materials, not specular ones");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
   Plan P;
@@ -1042,11 +1040,19 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
   float *s_dkd = W.srgb;  // 3 floats per shadow entry, like the forward pass's radiance
   skw_accel *a = s->accel;
   e = cudaMemcpyAsync(d_view, P.views.data(), sizeof(skw::ViewDev), cudaMemcpyHostToDevice, st);
+  skw::SpecQueues sq0{};  // the camera level's children go to queue 0
+  if (P.spec_levels) {
+    sq0.out_rays = W.qrays[0];
+    sq0.out_w = W.qw[0];
+    sq0.out_sample = W.qsample[0];
+    sq0.out_node = W.qnode[0];
+    sq0.out_count = W.counts + 3;
+  }
   int64_t launches = 0;
   for (int64_t px0 = 0; px0 < P.n_px_total && e == cudaSuccess; px0 += P.chunk_px) {
     const int n_px = (int)std::min<int64_t>(P.chunk_px, P.n_px_total - px0);
     const int n = n_px * P.spp, cap = P.cfg.stack_cap;
-    if ((e = cudaMemsetAsync(W.counts, 0, 3 * sizeof(int), st)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(W.counts, 0, 5 * sizeof(int), st)) != cudaSuccess) break;
     if ((e = skw::launch_camera(d_view, 1, px0, n_px, P.sppx, P.sppy, W.rays, st, P.ld)) != cudaSuccess) break;
     if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr,
                                    W.hits, a->d_status, st)) != cudaSuccess)
@@ -1054,8 +1060,8 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
     if (P.media && (e = record_media(s, P, W, d_view, px0, n, true, d_film, g_emission, st)) != cudaSuccess) break;
     if ((e = skw::launch_shade_adjoint(s->dev, d_view, 1, n, px0, P.spp, P.nl, d_film, g_albedo, g_emission, W.rays,
                                        W.hits, W.srays, W.starget, s_dkd, s_dem, W.counts, W.brays, W.btarget, b_dkd,
-                                       W.brgb, W.counts + 1, W.bnrm, P.media ? W.tcam : nullptr, st, P.ld)) !=
-        cudaSuccess)
+                                       W.brgb, W.counts + 1, W.bnrm, P.media ? W.tcam : nullptr, st, P.ld,
+                                       P.spec_levels ? &sq0 : nullptr)) != cudaSuccess)
       break;
     const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
     if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts,
@@ -1069,6 +1075,47 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
                                          g_albedo, g_emission, st)) != cudaSuccess)
       break;
     launches += 7;
+    // The specular levels, replayed as in record_specular with the adjoint
+    // shading and resolves (the entries' weights scale dL/dI).
+    for (int L = 1; L <= P.spec_levels && e == cudaSuccess; ++L) {
+      const int qi = (L - 1) & 1, qo = L & 1;
+      const int64_t cl = (int64_t)n << L;
+      skw::SpecQueues q{};
+      q.in_rays = W.qrays[qi];
+      q.in_w = W.qw[qi];
+      q.in_sample = W.qsample[qi];
+      q.in_node = W.qnode[qi];
+      q.in_count = W.counts + 3 + qi;
+      if (L < P.spec_levels) {
+        q.out_rays = W.qrays[qo];
+        q.out_w = W.qw[qo];
+        q.out_sample = W.qsample[qo];
+        q.out_node = W.qnode[qo];
+        q.out_count = W.counts + 3 + qo;
+        if ((e = cudaMemsetAsync(W.counts + 3 + qo, 0, sizeof(int), st)) != cudaSuccess) break;
+      }
+      if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) break;
+      if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.qrays[qi], cl, W.counts + 3 + qi,
+                                     a->scene_abs, nullptr, W.qhits, a->d_status, st)) != cudaSuccess)
+        break;
+      if ((e = skw::launch_shade_specular_adjoint(s->dev, d_view, 1, cl, px0, P.spp, P.nl, d_film, g_albedo,
+                                                  g_emission, q, L, W.qhits, W.srays, W.starget, s_dkd, s_dem,
+                                                  W.counts, W.brays, W.btarget, b_dkd, W.brgb, W.counts + 1,
+                                                  W.bnrm, st)) != cudaSuccess)
+        break;
+      const int64_t lsh = cl * (P.nl + P.npl), lbs = cl * P.nl;
+      if (lsh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, lsh, W.counts,
+                                                a->scene_abs, nullptr, W.occ, a->d_status, st)) != cudaSuccess)
+        break;
+      if (lbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, lbs, W.counts + 1,
+                                                a->scene_abs, nullptr, W.bhits, a->d_status, st)) != cudaSuccess)
+        break;
+      if ((e = skw::launch_resolve_adjoint(s->dev, (int)std::max(lsh, lbs), P.nl, W.occ, W.starget, s_dkd, s_dem,
+                                           W.counts, W.brays, W.bhits, W.btarget, b_dkd, W.brgb, W.counts + 1,
+                                           W.bnrm, g_albedo, g_emission, st)) != cudaSuccess)
+        break;
+      launches += 6;
+    }
   }
   cudaFreeAsync(w, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "direct-lighting adjoint");

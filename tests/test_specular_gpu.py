@@ -15,8 +15,8 @@ dielectric Fresnel + SpecularTransmission) on the GPU.
 * The photon-mapping render follows the same trees, with caustic-map
   radiance and final gather at their diffuse hits, against the reference's
   photon renders.
-* Scenes with a specular material are refused where the GPU path does not
-  follow specular paths (adjoint; a medium together with them).
+* The direct-lighting adjoint replays the same trees (finite differences).
+* A medium together with specular materials is refused.
 """
 from pathlib import Path
 
@@ -136,16 +136,47 @@ def test_specular_photon_render_matches_reference(gpu, name):
     assert rel.max() <= 0.08
 
 
-def test_specular_scene_refusals(gpu):
+def test_specular_adjoint_matches_finite_differences(gpu):
+    """The adjoint replays the specular trees too: with the glass fixed (a
+    transparent surface's reflectance is its material's, not a per-triangle
+    albedo) the image is linear in the floor's albedo and in the emission
+    scale, so central differences (eps 1e-3) of a weighted sum of the image
+    match the adjoint within 1e-3 relative; the glass triangles get exactly
+    zero."""
     import torch
     from skwarka_gb300.adjoint import DirectLighting
+    prims, mats, lights, cam = sf.specular_cases()["glass_area"]
+    sc = RenderScene(prims, mats, lights)
+    sc.set_max_specular_depth(6)
+    r = DirectLighting(sc, cam, 4, 4, 1, seed=5)
+    n = sc.n_triangles
+    rng = np.random.default_rng(3)
+    albedo = torch.tensor(rng.uniform(0.2, 0.8, size=(n, 3)), dtype=torch.float32, device="cuda")
+    w = torch.tensor(rng.uniform(0.5, 1.5, size=(cam.height, cam.width, 3)), dtype=torch.float64, device="cuda")
+    g_alb, g_em = r.adjoint(albedo, 1.0, w.float())
+    g = g_alb.double().cpu().numpy()
+    loss = lambda a, sc_: float((r.forward_image(a, sc_).double() * w).sum())  # noqa: E731
+    eps = 1e-3
+    got, want = [], []
+    for t in (0, 1):  # the floor's two triangles (mesh order: the floor is primitive 0)
+        for c in range(3):
+            a_p, a_m = albedo.clone(), albedo.clone()
+            a_p[t, c] += eps
+            a_m[t, c] -= eps
+            want.append((loss(a_p, 1.0) - loss(a_m, 1.0)) / (2 * eps))
+            got.append(g[t, c])
+    fd_em = (loss(albedo, 1.0 + eps) - loss(albedo, 1.0 - eps)) / (2 * eps)
+    got, want = np.array(got), np.array(want)
+    print(f"[specular adjoint] floor albedo: adjoint {got.round(3).tolist()} fd {want.round(3).tolist()}; "
+          f"emission adjoint {float(g_em[0]):.4f} fd {fd_em:.4f}")
+    assert np.linalg.norm(got - want) <= 1e-3 * np.linalg.norm(want)
+    assert abs(float(g_em[0]) - fd_em) <= 1e-3 * abs(fd_em)
+    assert np.all(g[2:2 + 1024] == 0.0)  # the sphere (primitive 1): transparent
+
+
+def test_specular_scene_refusals(gpu):
     prims, mats, lights, cam = sf.specular_cases()["glass_point"]
     sc = RenderScene(prims, mats, lights)
     sc.set_medium(Medium())
     with pytest.raises(_lib.SkwError, match="medium"):
         sc.render_direct(cam, 1, 1, seed=1)
-    sc.set_medium(None)
-    dl = DirectLighting(sc, cam, 1, 1)
-    albedo = torch.full((sc.n_triangles, 3), 0.5, device="cuda")
-    with pytest.raises(_lib.SkwError, match="specular"):
-        dl.adjoint(albedo, 1.0, torch.ones(cam.height, cam.width, 3, device="cuda"))
