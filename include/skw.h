@@ -371,7 +371,7 @@ int skw_scene_set_medium(skw_scene *scene, const skw_medium *medium);
  * (PhotonLTEIntegrator.cpp:320-385). */
 int skw_scene_set_max_specular_depth(skw_scene *scene, int32_t max_depth);
 
-/* ---- Photon maps (PhotonLTEIntegrator, LTEIntegrators/PhotonLTEIntegrator/*).
+/* ---- Photon maps (PhotonLTEIntegrator, LTEIntegrators/PhotonLTEIntegrator/).
  *
  * A photon (PhotonLTEIntegrator::Photon, PhotonInternalTypes.h:35-59):
  * position, weight, and the 16-bit CompressedDirection ids of the incident
