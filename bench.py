@@ -222,11 +222,22 @@ def render_bench(args, dev, ctx, measure_cpu):
         hfilm.copy_(film, non_blocking=True)
         stream.synchronize()
     e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+    # the same frame with the LDSampler (4 samples per pixel)
+    from skwarka_gb300.render import LD
+    for i in range(3):
+        sc.render_direct(cam, 2, 2, seed=i, out=film, sampler=LD)
+    s.record(stream)
+    for i in range(steps):
+        sc.render_direct(cam, 2, 2, seed=300 + i, out=film, sampler=LD)
+    e.record(stream)
+    torch.cuda.synchronize()
+    ld_ms = s.elapsed_time(e) / steps
     out = {"workload": "direct lighting, 256x256, 2x2 spp, 1 light sample, box + 20,480-tri spheres + quad light",
            "unit": "Msamples/s", "value": samples / dev_ms / 1e3, "ms_per_frame": dev_ms,
            "e2e": {"value": samples / e2e_ms / 1e3, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": hfilm.numel() * 4},
-           "gpu_launches_per_frame": launches}
+           "gpu_launches_per_frame": launches,
+           "ld_sampler": {"value": samples / ld_ms / 1e3, "unit": "Msamples/s", "ms_per_frame": ld_ms}}
     if measure_cpu:
         from oracle.api import Reference
         if Reference.available():
@@ -236,6 +247,47 @@ def render_bench(args, dev, ctx, measure_cpu):
             _, sec = ref.render_direct(prims, mats, [], cam, 2, 2)
             out["cpu_baseline"] = {"value": samples / sec / 1e6, "unit": "Msamples/s", "cores": os.cpu_count() or 1,
                                    "kind": "reference", "sample": "one full 256x256 4-spp frame, SamplerBasedRenderer"}
+    return out
+
+
+def specular_bench(args, dev, ctx, measure_cpu):
+    """Direct lighting with specular recursion (maximum depth 6): a glass
+    sphere (1,024 triangles, index 1.5) above a matte floor under a quad
+    light, 256 x 256, 2x2 spp; GPU samples/s beside the reference's
+    SamplerBasedRenderer on the host cores."""
+    import torch
+    from skwarka_gb300 import scenes
+    from skwarka_gb300.render import TRANSPARENT, Material, RenderScene
+    glass = Material(kind=TRANSPARENT, kd=(1.0, 1.0, 1.0), ks=(1.0, 1.0, 1.0), refractive_index=1.5)
+    prims, mats, lights, cam = scenes.glass_sphere_scene(glass, "area", (256, 256))
+    samples = cam.width * cam.height * 4
+    sc = RenderScene(prims, mats, lights, ctx=ctx)
+    sc.set_max_specular_depth(6)
+    film = torch.empty((cam.height, cam.width, 3), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for i in range(3):
+        sc.render_direct(cam, 2, 2, seed=i, out=film)
+    torch.cuda.synchronize()
+    steps = max(5, args.steps)
+    l0 = ctx.launch_count()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for i in range(steps):
+        sc.render_direct(cam, 2, 2, seed=100 + i, out=film)
+    e.record(stream)
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / steps
+    out = {"workload": "direct lighting + specular recursion (depth 6), glass sphere over a floor, 256x256, 2x2 spp",
+           "unit": "Msamples/s", "value": samples / ms / 1e3, "ms_per_frame": ms,
+           "gpu_launches_per_frame": (ctx.launch_count() - l0) / steps}
+    if measure_cpu:
+        from oracle.api import Reference
+        if Reference.available():
+            log("reference specular render")
+            _, sec = Reference().render_direct(prims, mats, lights, cam, 2, 2)
+            out["cpu_baseline"] = {"value": samples / sec / 1e6, "unit": "Msamples/s", "cores": os.cpu_count() or 1,
+                                   "kind": "reference",
+                                   "sample": "one full 256x256 4-spp frame, SamplerBasedRenderer, max specular depth 6"}
     return out
 
 
@@ -611,6 +663,10 @@ def main():
     if not args.no_render:
         log("direct-lighting render")
         render = render_bench(args, dev, ctx, measure_cpu=not args.no_cpu_baseline and world == 1)
+    specular = None
+    if not args.no_render:
+        log("specular render")
+        specular = specular_bench(args, dev, ctx, measure_cpu=not args.no_cpu_baseline and world == 1)
     batch = None
     if not args.no_batch:
         log("batched multi-view render")
@@ -641,7 +697,7 @@ def main():
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": args.rays * 32,
                     "d2h_bytes_per_step": args.rays * 16},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,
-            "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit, "render": render, "batch": batch, "adjoint": adjoint, "photon": photon,
+            "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit, "render": render, "specular": specular, "batch": batch, "adjoint": adjoint, "photon": photon,
             "accel": {k: acc.info[k] for k in ("n_nodes", "max_depth", "build_ms", "device_bytes")}}
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -318,3 +318,37 @@ def merl_table(seed: int = 7, kd=(0.35, 0.25, 0.15), ks=(0.5, 0.5, 0.5), exponen
         f = np.repeat(f[:, :, None], 180, axis=2) * (1.0 + noise * rng.normal(size=(90, 90, 180)))
         out.append((np.maximum(f, 0.0) / scales[c]).astype("<f8").reshape(-1))
     return np.array([90, 90, 180], "<i4").tobytes() + b"".join(o.tobytes() for o in out)
+
+
+def glass_sphere_scene(material, lights="area", resolution=(48, 32)):
+    """A sphere (radius 0.4, 4 * 4**4 flat outward-facing triangles) above a
+    10 x 10 matte floor (albedo (0.7, 0.6, 0.5)), lit by a 0.6 x 0.6 quad
+    light of radiance 10 at height 2 (lights="area") or a point light of
+    intensity 3 at (0.2, -0.1, 1.6) (lights="point"); `material` is the
+    sphere's skwarka_gb300.render.Material.  Returns (prims, materials,
+    point_lights, camera): the camera looks at the sphere from above and to
+    the side, so the floor is seen directly and through the sphere."""
+    from .accel import TriangleMesh
+    from .render import Camera, Material, PointLight, RenderPrimitive
+    v, t = sphere_mesh(4)
+    a, b, c = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
+    outward = (np.cross(b - a, c - a) * (a + b + c)).sum(1) > 0
+    t = np.where(outward[:, None], t, t[:, [0, 2, 1]]).astype(np.int32)
+    sphere = TriangleMesh((v * 0.4 + np.array([0.0, 0.0, 0.45])).astype(np.float32), t)
+    s = 5.0
+    floor = TriangleMesh(np.array([[-s, -s, 0], [s, -s, 0], [s, s, 0], [-s, s, 0]], np.float32),
+                         np.array([[0, 1, 2], [0, 2, 3]], np.int32))
+    prims = [RenderPrimitive(floor, 0), RenderPrimitive(sphere, 1)]
+    mats = [Material(kd=(0.7, 0.6, 0.5)), material]
+    pls = []
+    if lights == "area":
+        q = 0.3
+        lv = np.array([[-q, -q, 2], [q, -q, 2], [q, q, 2], [-q, q, 2]], np.float32)
+        prims.append(RenderPrimitive(TriangleMesh(lv, np.array([[0, 2, 1], [0, 3, 2]], np.int32)), 2,
+                                     emission=(10.0, 10.0, 10.0)))
+        mats.append(Material(kd=(0.0, 0.0, 0.0)))
+    else:
+        pls = [PointLight((0.2, -0.1, 1.6), (3.0, 3.0, 3.0))]
+    w, h = resolution
+    cam = Camera.look_at((1.3, -1.1, 1.2), (0.0, 0.0, 0.35), (0, 0, 1), np.radians(55.0), w, h)
+    return prims, mats, pls, cam

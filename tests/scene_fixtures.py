@@ -317,37 +317,9 @@ def caustic_cases(seed=41):
 
 
 def specular_scene(material, lights="area", resolution=(48, 32)):
-    """A glass-like sphere (radius 0.4, 4 * 4**4 flat outward-facing
-    triangles) resting above a 10 x 10 matte floor, lit by a 0.6 x 0.6 quad
-    light of radiance 10 at height 2 (lights="area") or a point light of
-    intensity 3 at (0.2, -0.1, 1.6) (lights="point"); `material` is the
-    sphere's skwarka_gb300.render.Material.  Returns (prims, materials,
-    point_lights, camera): the camera looks at the sphere from above and to
-    the side, so the floor is seen directly and through the sphere."""
-    from skwarka_gb300.accel import TriangleMesh
-    from skwarka_gb300.render import Camera, Material, PointLight, RenderPrimitive
-    v, t = scenes.sphere_mesh(4)
-    a, b, c = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
-    outward = (np.cross(b - a, c - a) * (a + b + c)).sum(1) > 0
-    t = np.where(outward[:, None], t, t[:, [0, 2, 1]]).astype(np.int32)
-    sphere = TriangleMesh((v * 0.4 + np.array([0.0, 0.0, 0.45])).astype(np.float32), t)
-    s = 5.0
-    floor = TriangleMesh(np.array([[-s, -s, 0], [s, -s, 0], [s, s, 0], [-s, s, 0]], np.float32),
-                         np.array([[0, 1, 2], [0, 2, 3]], np.int32))
-    prims = [RenderPrimitive(floor, 0), RenderPrimitive(sphere, 1)]
-    mats = [Material(kd=(0.7, 0.6, 0.5)), material]
-    pls = []
-    if lights == "area":
-        q = 0.3
-        lv = np.array([[-q, -q, 2], [q, -q, 2], [q, q, 2], [-q, q, 2]], np.float32)
-        prims.append(RenderPrimitive(TriangleMesh(lv, np.array([[0, 2, 1], [0, 3, 2]], np.int32)), 2,
-                                     emission=(10.0, 10.0, 10.0)))
-        mats.append(Material(kd=(0.0, 0.0, 0.0)))
-    else:
-        pls = [PointLight((0.2, -0.1, 1.6), (3.0, 3.0, 3.0))]
-    w, h = resolution
-    cam = Camera.look_at((1.3, -1.1, 1.2), (0.0, 0.0, 0.35), (0, 0, 1), np.radians(55.0), w, h)
-    return prims, mats, pls, cam
+    """skwarka_gb300.scenes.glass_sphere_scene: a sphere of `material` above a
+    matte floor under an area light ("area") or a point light ("point")."""
+    return scenes.glass_sphere_scene(material, lights, resolution)
 
 
 def specular_cases():
