@@ -362,7 +362,7 @@ int skw_scene_set_medium(skw_scene *scene, const skw_medium *medium);
  * d + 1 (LTEIntegrator::_SpecularReflect / _SpecularTransmit,
  * Core/LTEIntegrator.cpp:66-126).  Default 10 (the GUI's default); range
  * [0, 11]: every branch of every sample's tree is given room, so a render
- * pass holds at most 2^22 >> (max_depth + 1) camera samples.  Scenes with
+ * pass holds at most 2^23 >> (max_depth + 1) camera samples.  Scenes with
  * specular materials cannot have a medium (SKW_ERR_UNSUPPORTED); the
  * adjoint replays the same trees (a transparent surface's reflectance is
  * its material's, never a per-triangle albedo); photon shooting follows

@@ -138,7 +138,7 @@ cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_
                                    const int *stri, const float *s_dkd, const float *s_dem, const int *scount,
                                    const void *brays, const void *bhits, const int *btri, const float *b_dkd,
                                    const float *brgb, const int *bcount, const float *bnrm, float *g_albedo,
-                                   double *g_emission, cudaStream_t s);
+                                   double *g_emission, cudaStream_t s, bool capped = false);
 
 // Photon mapping (photon.cu).  trace(rays, n, n_dev, hits, stream) runs the
 // closest-hit traversal of the scene's accelerator.

@@ -30,6 +30,7 @@
 // counter-based hash of seed, sample and dimension replaces the reference's
 // per-thread Mersenne Twister), so parity is statistical.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 
 #include "kernels.h"
@@ -101,6 +102,10 @@ __global__ void k_camera(const ViewDev *__restrict__ views, int n_views, int64_t
 // 2k and 2k + 1) and selects its random stream.  Shading a queue entry
 // adds weight x (emission + direct lighting) to the sample's specular slot
 // with atomics (so the last bits of that slot depend on the order).
+// Grid of the kernels of a specular level (grid-stride loops over the
+// level's queue, whose capacity is far above its usual length).
+constexpr int64_t kStrideBlocks = 2048;
+
 struct SpecArgs {
   // input (SPEC): entries [0, min(*in_count, n)) of a level
   const float *in_w;
@@ -192,8 +197,12 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
                                                int *__restrict__ scount, float4 *__restrict__ brays,
                                                int *__restrict__ btarget, float *__restrict__ brgb,
                                                int *__restrict__ bcount, float *__restrict__ bnrm) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = SPEC ? i < min(*Q.in_count, A.n) : i < A.n;
+  // One entry per thread and iteration; a specular level's grid is capped
+  // and strides over the level (the trip count is uniform in a block).
+  const int n_eff = SPEC ? min(*Q.in_count, A.n) : A.n;
+  for (int i0 = blockIdx.x * blockDim.x; i0 < n_eff; i0 += gridDim.x * blockDim.x) {
+  const int i = i0 + threadIdx.x;
+  const bool valid = i < n_eff;
   int4 hit = make_int4(0x7f800000, -1, -1, 0);
   float4 ra = make_float4(0, 0, 0, 0), rb = make_float4(0, 0, 0, 0);
   int si = valid ? i : 0;  // camera sample of the entry
@@ -395,6 +404,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
       }
     }
   }
+  }  // entries
 }
 
 // accumulate: add into the target (the targets of a specular level repeat)
@@ -402,27 +412,28 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
 __global__ void k_resolve_shadow(const uint8_t *__restrict__ occ, const int *__restrict__ starget,
                                  const float *__restrict__ srgb, const int *__restrict__ scount,
                                  float *__restrict__ contrib, bool accumulate) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= *scount || occ[i]) return;
-  const int64_t t = starget[i];
-  if (accumulate) {
-    atomic_add_rgb(contrib, t, v3(srgb[3 * i], srgb[3 * i + 1], srgb[3 * i + 2]));
-    return;
+  const int n = *scount;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (occ[i]) continue;
+    const int64_t t = starget[i];
+    if (accumulate) {
+      atomic_add_rgb(contrib, t, v3(srgb[3 * i], srgb[3 * i + 1], srgb[3 * i + 2]));
+      continue;
+    }
+    contrib[3 * t] = srgb[3 * i];
+    contrib[3 * t + 1] = srgb[3 * i + 1];
+    contrib[3 * t + 2] = srgb[3 * i + 2];
   }
-  contrib[3 * t] = srgb[3 * i];
-  contrib[3 * t + 1] = srgb[3 * i + 1];
-  contrib[3 * t + 2] = srgb[3 * i + 2];
 }
 
 // A BSDF ray that hits the front of an area light adds its MIS-weighted
 // emission (:300-318); the light density is DiffuseAreaLightSource::
 // LightingPDF (:104-116).
-__global__ void k_resolve_bsdf(SceneDev S, int n_light_samples, const float4 *__restrict__ brays,
-                               const int4 *__restrict__ bhits, const int *__restrict__ btarget,
-                               const float *__restrict__ brgb, const int *__restrict__ bcount,
-                               const float *__restrict__ bnrm, float *__restrict__ contrib, bool accumulate) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= *bcount) return;
+__device__ __forceinline__ void resolve_bsdf_entry(const SceneDev &S, int n_light_samples, int i,
+                                                   const float4 *__restrict__ brays, const int4 *__restrict__ bhits,
+                                                   const int *__restrict__ btarget, const float *__restrict__ brgb,
+                                                   const float *__restrict__ bnrm, float *__restrict__ contrib,
+                                                   bool accumulate) {
   const int4 hit = bhits[i];
   if (hit.y < 0) return;
   const int li = S.prim_light[hit.y];
@@ -455,21 +466,33 @@ __global__ void k_resolve_bsdf(SceneDev S, int n_light_samples, const float4 *__
   contrib[3 * t + 2] = brgb[4 * i + 2] * L.radiance[2] * tr.z * sw;
 }
 
+__global__ void k_resolve_bsdf(SceneDev S, int n_light_samples, const float4 *__restrict__ brays,
+                               const int4 *__restrict__ bhits, const int *__restrict__ btarget,
+                               const float *__restrict__ brgb, const int *__restrict__ bcount,
+                               const float *__restrict__ bnrm, float *__restrict__ contrib, bool accumulate) {
+  const int n = *bcount;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    resolve_bsdf_entry(S, n_light_samples, i, brays, bhits, btarget, brgb, bnrm, contrib, accumulate);
+}
+
 // Adjoint of k_resolve_shadow: an unoccluded shadow ray adds its derivative
 // terms to its triangle's albedo gradient and to the emission gradient.
 __global__ void k_resolve_shadow_adj(const uint8_t *__restrict__ occ, const int *__restrict__ stri,
                                      const int *__restrict__ scount, AdjointArgs J) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  float dem = 0.0f;
-  if (i < *scount && !occ[i]) {
-    const int64_t g = stri[i];
-    const float *d = J.s_dkd + 3 * (int64_t)i;
-    if (d[0] != 0.0f) atomicAdd(J.g_albedo + 3 * g, d[0]);
-    if (d[1] != 0.0f) atomicAdd(J.g_albedo + 3 * g + 1, d[1]);
-    if (d[2] != 0.0f) atomicAdd(J.g_albedo + 3 * g + 2, d[2]);
-    dem = J.s_dem[i];
+  const int n = *scount;
+  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {  // block-uniform trip count
+    const int i = i0 + threadIdx.x;
+    float dem = 0.0f;
+    if (i < n && !occ[i]) {
+      const int64_t g = stri[i];
+      const float *d = J.s_dkd + 3 * (int64_t)i;
+      if (d[0] != 0.0f) atomicAdd(J.g_albedo + 3 * g, d[0]);
+      if (d[1] != 0.0f) atomicAdd(J.g_albedo + 3 * g + 1, d[1]);
+      if (d[2] != 0.0f) atomicAdd(J.g_albedo + 3 * g + 2, d[2]);
+      dem = J.s_dem[i];
+    }
+    add_emission_grad(J.g_emission, dem);
   }
-  add_emission_grad(J.g_emission, dem);
 }
 
 // Adjoint of k_resolve_bsdf (same light density and MIS weight).
@@ -477,9 +500,11 @@ __global__ void k_resolve_bsdf_adj(SceneDev S, int n_light_samples, const float4
                                    const int4 *__restrict__ bhits, const int *__restrict__ btri,
                                    const float *__restrict__ brgb, const int *__restrict__ bcount,
                                    const float *__restrict__ bnrm, AdjointArgs J) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = *bcount;
+  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {  // block-uniform trip count
+  const int i = i0 + threadIdx.x;
   float dem = 0.0f;
-  if (i < *bcount) {
+  if (i < n) {
     const int4 hit = bhits[i];
     const int li = hit.y >= 0 ? S.prim_light[hit.y] : -1;
     if (li >= 0) {
@@ -507,6 +532,7 @@ __global__ void k_resolve_bsdf_adj(SceneDev S, int n_light_samples, const float4
     }
   }
   add_emission_grad(J.g_emission, dem);
+  }
 }
 
 // Single scattering along the camera ray's segment in the medium
@@ -772,12 +798,13 @@ cudaError_t launch_shade_specular(const SceneDev &S, const ViewDev *views, int n
   SpecArgs Q{spec.in_w,      spec.in_sample, spec.in_node,  spec.in_count, (float4 *)spec.out_rays,
              spec.out_w,     spec.out_sample, spec.out_node, spec.out_count, depth,
              spec.spec_slot};
+  const unsigned grid = (unsigned)std::min<int64_t>((capacity + 127) / 128, kStrideBlocks);
   if (spec.out_count)
-    k_shade<false, true, true><<<(unsigned)((capacity + 127) / 128), 128, 0, s>>>(
+    k_shade<false, true, true><<<grid, 128, 0, s>>>(
         S, A, AdjointArgs{}, Q, (const float4 *)spec.in_rays, (const int4 *)hits, contrib, (float4 *)srays, starget,
         srgb, scount, (float4 *)brays, btarget, brgb, bcount, bnrm);
   else
-    k_shade<false, true, false><<<(unsigned)((capacity + 127) / 128), 128, 0, s>>>(
+    k_shade<false, true, false><<<grid, 128, 0, s>>>(
         S, A, AdjointArgs{}, Q, (const float4 *)spec.in_rays, (const int4 *)hits, contrib, (float4 *)srays, starget,
         srgb, scount, (float4 *)brays, btarget, brgb, bcount, bnrm);
   return cudaGetLastError();
@@ -823,12 +850,13 @@ cudaError_t launch_shade_specular_adjoint(const SceneDev &S, const ViewDev *view
   SpecArgs Q{spec.in_w,      spec.in_sample, spec.in_node,  spec.in_count, (float4 *)spec.out_rays,
              spec.out_w,     spec.out_sample, spec.out_node, spec.out_count, depth,
              0};
+  const unsigned grid = (unsigned)std::min<int64_t>((capacity + 127) / 128, kStrideBlocks);
   if (spec.out_count)
-    k_shade<true, true, true><<<(unsigned)((capacity + 127) / 128), 128, 0, s>>>(
+    k_shade<true, true, true><<<grid, 128, 0, s>>>(
         S, A, J, Q, (const float4 *)spec.in_rays, (const int4 *)hits, nullptr, (float4 *)srays, stri, nullptr, scount,
         (float4 *)brays, btri, brgb, bcount, bnrm);
   else
-    k_shade<true, true, false><<<(unsigned)((capacity + 127) / 128), 128, 0, s>>>(
+    k_shade<true, true, false><<<grid, 128, 0, s>>>(
         S, A, J, Q, (const float4 *)spec.in_rays, (const int4 *)hits, nullptr, (float4 *)srays, stri, nullptr, scount,
         (float4 *)brays, btri, brgb, bcount, bnrm);
   return cudaGetLastError();
@@ -838,11 +866,12 @@ cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_
                                    const int *stri, const float *s_dkd, const float *s_dem, const int *scount,
                                    const void *brays, const void *bhits, const int *btri, const float *b_dkd,
                                    const float *brgb, const int *bcount, const float *bnrm, float *g_albedo,
-                                   double *g_emission, cudaStream_t s) {
+                                   double *g_emission, cudaStream_t s, bool capped) {
   if (capacity <= 0) return cudaSuccess;
   AdjointArgs J{nullptr, g_albedo, g_emission, const_cast<float *>(s_dkd), const_cast<float *>(s_dem),
                 const_cast<float *>(b_dkd)};
-  const unsigned grid = (unsigned)((capacity + 255) / 256);
+  const unsigned grid = (unsigned)(capped ? std::min<int64_t>((capacity + 255) / 256, kStrideBlocks)
+                                          : (capacity + 255) / 256);
   k_resolve_shadow_adj<<<grid, 256, 0, s>>>(occ, stri, scount, J);
   k_resolve_bsdf_adj<<<grid, 256, 0, s>>>(S, n_light_samples, (const float4 *)brays, (const int4 *)bhits, btri, brgb,
                                           bcount, bnrm, J);
@@ -854,7 +883,9 @@ cudaError_t launch_resolve(const SceneDev &S, int capacity, int n_light_samples,
                            const void *bhits, const int *btarget, const float *brgb, const int *bcount,
                            const float *bnrm, float *contrib, cudaStream_t s, bool accumulate) {
   if (capacity <= 0) return cudaSuccess;
-  const unsigned grid = (unsigned)((capacity + 255) / 256);
+  // a specular level (accumulate) strides with a capped grid over its queue
+  const unsigned grid = (unsigned)(accumulate ? std::min<int64_t>((capacity + 255) / 256, kStrideBlocks)
+                                              : (capacity + 255) / 256);
   k_resolve_shadow<<<grid, 256, 0, s>>>(occ, starget, srgb, scount, contrib, accumulate);
   k_resolve_bsdf<<<grid, 256, 0, s>>>(S, n_light_samples, (const float4 *)brays, (const int4 *)bhits, btarget, brgb,
                                       bcount, bnrm, contrib, accumulate);

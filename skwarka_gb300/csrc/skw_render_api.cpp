@@ -357,7 +357,7 @@ struct PassConfig {
 
 // Entries of the largest specular level of a pass (the pass is sized so
 // that every branch of every sample's specular tree fits).
-constexpr int64_t kSpecEntries = (int64_t)1 << 22;
+constexpr int64_t kSpecEntries = (int64_t)1 << 23;
 // Deepest specular depth: a sample's tree then holds up to 2^12 - 1 rays.
 constexpr int kMaxSpecDepth = 11;
 
@@ -1112,7 +1112,7 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
         break;
       if ((e = skw::launch_resolve_adjoint(s->dev, (int)std::max(lsh, lbs), P.nl, W.occ, W.starget, s_dkd, s_dem,
                                            W.counts, W.brays, W.bhits, W.btarget, b_dkd, W.brgb, W.counts + 1,
-                                           W.bnrm, g_albedo, g_emission, st)) != cudaSuccess)
+                                           W.bnrm, g_albedo, g_emission, st, true)) != cudaSuccess)
         break;
       launches += 6;
     }
