@@ -24,7 +24,11 @@ int traversal_stack_capacity(int max_depth);
 // kernels ahead of a stream capture.
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
                              int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
-                             unsigned *status, cudaStream_t stream, int ctas_per_sm = 0);
+                             unsigned *status, cudaStream_t stream, int ctas_per_sm = 0, int *work = nullptr);
+// work (may be null): a device int of the caller's, not used by any launch
+// that may run at the same time; it is zeroed on `stream` and the warps
+// then take groups of 32 rays from it as they finish (no idle tail).  Null:
+// each warp traces a fixed share of the rays.
 cudaError_t prepare_traversal(int stack_cap);
 // Resident CTAs per SM of the closest-hit kernel at this capacity.
 int traversal_max_ctas_per_sm(int stack_cap);
@@ -144,7 +148,7 @@ cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_
 // closest-hit traversal of the scene's accelerator.
 struct PhotonRec;
 struct PhotonShootArgs;
-using TraceFn = std::function<cudaError_t(const void *, int64_t, const int *, void *, cudaStream_t)>;
+using TraceFn = std::function<cudaError_t(const void *, int64_t, const int *, void *, cudaStream_t, int *)>;
 // Workspace bytes of one shooting chunk of n_paths paths.
 size_t photon_chunk_bytes(int64_t n_paths, int max_bounces);
 // Shoots paths [path0, path0 + n_paths): writes the chunk's direct photons

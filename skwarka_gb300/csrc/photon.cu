@@ -521,7 +521,7 @@ cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, cons
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   for (int b = 0; b < A.max_bounces; ++b) {
     Queue &in = Q[b & 1], &out = Q[(b + 1) & 1];
-    if ((e = trace(in.rays, n_paths, in.count, hits, st)) != cudaSuccess) return e;
+    if ((e = trace(in.rays, n_paths, in.count, hits, st, counts + 8)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(out.count, 0, sizeof(int), st)) != cudaSuccess) return e;
     k_photon_bounce<<<grid, 128, 0, st>>>(S, A, path0, b, n_paths, in, hits, out, st_direct, has_direct,
                                           st_indirect, n_indirect, st_caustic, has_caustic);
@@ -1070,7 +1070,7 @@ cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev 
   k_gather_rays<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S, G, M, (const float4 *)rays, (const int4 *)hits, src,
                                                               counts, kidx, kcnt, grays, gtarget, gweight, counts + 1);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if ((e = trace(grays, ng, counts + 1, ghits, st)) != cudaSuccess) return e;
+  if ((e = trace(grays, ng, counts + 1, ghits, st, counts + 8)) != cudaSuccess) return e;
   k_gather_hits<<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(S, grays, ghits, counts + 1, hsrc, hq, hqn, ts, tt,
                                                                side, counts + 2);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -235,8 +235,17 @@ static int run_query(skw_accel *a, bool closest, const skw_ray *rays, int64_t n,
   skw_ctx *ctx = a->ctx;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  // the launch's ray-group counter, stream-ordered from the context's pool
+  // (its own for every call, so calls on different streams never share one)
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemPool_t pool;
+  int *work = nullptr;
+  if ((e = skw::ctx_pool(ctx, &pool)) != cudaSuccess ||
+      (e = cudaMallocFromPoolAsync((void **)&work, 256, pool, st)) != cudaSuccess)
+    return cuda_fail(ctx, e, "work counter");
   e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, nullptr, a->scene_abs, nullptr, out,
-                            a->d_status, (cudaStream_t)stream);
+                            a->d_status, st, 0, work);
+  cudaFreeAsync(work, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, closest ? "closest-hit launch" : "any-hit launch");
   ctx->launches.fetch_add(1);
   return SKW_OK;
@@ -281,8 +290,10 @@ static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64
       rc = cuda_fail(a->ctx, e, "stream");
   }
   void *d_rays = nullptr, *d_out = nullptr;
+  int *d_work = nullptr;  // one ray-group counter per stream (256 bytes apart)
   if (rc == SKW_OK && ((e = cudaMallocFromPoolAsync(&d_rays, (size_t)n * sizeof(skw_ray), pool, st[0])) != cudaSuccess ||
-                       (e = cudaMallocFromPoolAsync(&d_out, (size_t)n * out_unit, pool, st[0])) != cudaSuccess))
+                       (e = cudaMallocFromPoolAsync(&d_out, (size_t)n * out_unit, pool, st[0])) != cudaSuccess ||
+                       (e = cudaMallocFromPoolAsync((void **)&d_work, 512, pool, st[0])) != cudaSuccess))
     rc = cuda_fail(a->ctx, e, "cudaMallocAsync");
   // the other streams start after the allocations
   if (rc == SKW_OK && (e = cudaEventRecord(ev[0], st[0])) != cudaSuccess) rc = cuda_fail(a->ctx, e, "event");
@@ -297,7 +308,8 @@ static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64
         cudaSuccess) {
       rc = cuda_fail(a->ctx, e, "copy rays in");
     } else if ((e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, dr, m, nullptr, a->scene_abs,
-                                          nullptr, dout, a->d_status, s, ctas)) != cudaSuccess) {
+                                          nullptr, dout, a->d_status, s, ctas, d_work + 64 * (c % n_streams))) !=
+               cudaSuccess) {
       rc = cuda_fail(a->ctx, e, "launch");
     } else {
       a->ctx->launches.fetch_add(1);
@@ -312,6 +324,7 @@ static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64
   }
   if (d_rays) cudaFreeAsync(d_rays, st[0]);
   if (d_out) cudaFreeAsync(d_out, st[0]);
+  if (d_work) cudaFreeAsync(d_work, st[0]);
   for (int i = 0; i < n_streams; ++i) {
     if (st[i]) {
       e = cudaStreamSynchronize(st[i]);

@@ -536,7 +536,7 @@ cudaError_t record_media(skw_scene *s, const Plan &P, const Workspace &W, const 
   const int64_t cm = (int64_t)n * s->dev.medium.max_steps;
   if (e == cudaSuccess)
     e = skw::launch_traversal(false, P.cfg.stack_cap, a->d_nodes, a->d_tris, W.mrays, cm, W.counts + 2, a->scene_abs,
-                              nullptr, W.mocc, a->d_status, st, P.cfg.trace_ctas_per_sm);
+                              nullptr, W.mocc, a->d_status, st, P.cfg.trace_ctas_per_sm, W.counts + 8);
   if (e == cudaSuccess)
     e = skw::launch_resolve_media(adjoint, cm, W.mocc, W.mtarget, W.mval, W.mdem, W.counts + 2, P.slots, P.media_slot,
                                   W.contrib, g_emission, st);
@@ -585,7 +585,7 @@ cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, con
     }
     if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) return e;
     if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.qrays[qi], cl, W.counts + 3 + qi, a->scene_abs,
-                                   nullptr, W.qhits, a->d_status, st, ctas)) != cudaSuccess)
+                                   nullptr, W.qhits, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
       return e;
     if ((e = skw::launch_shade_specular(s->dev, d_views, nv, cl, px0, P.spp, P.slots, P.nl, q, L, W.qhits, W.contrib,
                                         W.srays, W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb,
@@ -593,10 +593,10 @@ cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, con
       return e;
     const int64_t csh = cl * (P.nl + P.npl), cbs = cl * P.nl;
     if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts,
-                                              a->scene_abs, nullptr, W.occ, a->d_status, st, ctas)) != cudaSuccess)
+                                              a->scene_abs, nullptr, W.occ, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
       return e;
     if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
-                                              a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas)) != cudaSuccess)
+                                              a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
       return e;
     if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
                                  W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st, true)) !=
@@ -620,7 +620,7 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
   if ((e = cudaMemsetAsync(W.counts, 0, 5 * sizeof(int), st)) != cudaSuccess) return e;
   if ((e = skw::launch_camera(d_views, nv, px0, n_px, P.sppx, P.sppy, W.rays, st, P.ld)) != cudaSuccess) return e;
   if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr, W.hits,
-                                 a->d_status, st, ctas)) != cudaSuccess)
+                                 a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
     return e;
   if (P.media && (e = record_media(s, P, W, d_views, px0, n, false, nullptr, nullptr, st)) != cudaSuccess) return e;
   skw::SpecQueues sq{};
@@ -638,10 +638,10 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
     return e;
   const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
   if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts, a->scene_abs,
-                                            nullptr, W.occ, a->d_status, st, ctas)) != cudaSuccess)
+                                            nullptr, W.occ, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
     return e;
   if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
-                                            a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas)) != cudaSuccess)
+                                            a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
     return e;
   if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
                                W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st)) != cudaSuccess)
@@ -1055,7 +1055,7 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
     if ((e = cudaMemsetAsync(W.counts, 0, 5 * sizeof(int), st)) != cudaSuccess) break;
     if ((e = skw::launch_camera(d_view, 1, px0, n_px, P.sppx, P.sppy, W.rays, st, P.ld)) != cudaSuccess) break;
     if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr,
-                                   W.hits, a->d_status, st)) != cudaSuccess)
+                                   W.hits, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
       break;
     if (P.media && (e = record_media(s, P, W, d_view, px0, n, true, d_film, g_emission, st)) != cudaSuccess) break;
     if ((e = skw::launch_shade_adjoint(s->dev, d_view, 1, n, px0, P.spp, P.nl, d_film, g_albedo, g_emission, W.rays,
@@ -1065,10 +1065,10 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
       break;
     const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
     if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts,
-                                              a->scene_abs, nullptr, W.occ, a->d_status, st)) != cudaSuccess)
+                                              a->scene_abs, nullptr, W.occ, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
       break;
     if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
-                                              a->scene_abs, nullptr, W.bhits, a->d_status, st)) != cudaSuccess)
+                                              a->scene_abs, nullptr, W.bhits, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
       break;
     if ((e = skw::launch_resolve_adjoint(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, s_dkd, s_dem,
                                          W.counts, W.brays, W.bhits, W.btarget, b_dkd, W.brgb, W.counts + 1, W.bnrm,
@@ -1096,7 +1096,7 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
       }
       if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) break;
       if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.qrays[qi], cl, W.counts + 3 + qi,
-                                     a->scene_abs, nullptr, W.qhits, a->d_status, st)) != cudaSuccess)
+                                     a->scene_abs, nullptr, W.qhits, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
         break;
       if ((e = skw::launch_shade_specular_adjoint(s->dev, d_view, 1, cl, px0, P.spp, P.nl, d_film, g_albedo,
                                                   g_emission, q, L, W.qhits, W.srays, W.starget, s_dkd, s_dem,
@@ -1105,10 +1105,10 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
         break;
       const int64_t lsh = cl * (P.nl + P.npl), lbs = cl * P.nl;
       if (lsh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, lsh, W.counts,
-                                                a->scene_abs, nullptr, W.occ, a->d_status, st)) != cudaSuccess)
+                                                a->scene_abs, nullptr, W.occ, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
         break;
       if (lbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, lbs, W.counts + 1,
-                                                a->scene_abs, nullptr, W.bhits, a->d_status, st)) != cudaSuccess)
+                                                a->scene_abs, nullptr, W.bhits, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
         break;
       if ((e = skw::launch_resolve_adjoint(s->dev, (int)std::max(lsh, lbs), P.nl, W.occ, W.starget, s_dkd, s_dem,
                                            W.counts, W.brays, W.bhits, W.btarget, b_dkd, W.brgb, W.counts + 1,
@@ -1194,9 +1194,9 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   M.max_irr_dist = pm->max_irr_dist;
   M.dirs = pm->d_dirs;
   skw_accel *a = s->accel;
-  skw::TraceFn trace = [a](const void *rays, int64_t n, const int *n_dev, void *hits, cudaStream_t stq) {
+  skw::TraceFn trace = [a](const void *rays, int64_t n, const int *n_dev, void *hits, cudaStream_t stq, int *work) {
     return skw::launch_traversal(true, a->stack_cap, a->d_nodes, a->d_tris, rays, n, n_dev, a->scene_abs, nullptr,
-                                 hits, a->d_status, stq);
+                                 hits, a->d_status, stq, 0, work);
   };
   e = cudaMemcpyAsync(d_view, P.views.data(), sizeof(skw::ViewDev), cudaMemcpyHostToDevice, st);
   int64_t launches = 0;

@@ -497,7 +497,7 @@ template <int CAP, bool CLOSEST>
 __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, const float4 *__restrict__ rays,
             int n, const int *__restrict__ n_dev, float scene_abs, const int32_t *__restrict__ out_index,
-            void *__restrict__ out, unsigned *__restrict__ status) {
+            void *__restrict__ out, unsigned *__restrict__ status, int *__restrict__ work) {
   if (n_dev) n = min(n, *n_dev);  // a queue whose length lives on the device
   constexpr int SCAP = Stack<CAP>::SCAP;
   __shared__ uint32_t s_a[SCAP][SKW_TRAV_BLOCK];
@@ -517,8 +517,15 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
   const int warp = (int)((blockIdx.x * (unsigned)SKW_TRAV_BLOCK + threadIdx.x) >> 5);
   const int n_warps = (int)(gridDim.x * (unsigned)(SKW_TRAV_BLOCK / 32));
   const int groups = (n + 31) >> 5;
-  int next = 0;  // position in this warp's ray sequence
-  const int end = warp < groups ? ((groups - warp + n_warps - 1) / n_warps) << 5 : 0;
+  // Rays come in groups of 32.  Static (work == null): warp w takes groups
+  // w, w + W, ...; next / end are positions in that sequence.  Dynamic: a
+  // warp whose group is used up takes the launch's next group from the
+  // counter *work (zero at launch), so warps that drew cheap rays take more
+  // and the launch's tail is one group long; next / end are positions in
+  // the current group [gbase, gbase + 32), end = -1 once the rays are gone.
+  int next = 0;
+  int end = work ? 0 : (warp < groups ? ((groups - warp + n_warps - 1) / n_warps) << 5 : 0);
+  int gbase = 0;
 
   int ray_i = -1;
   // The ray itself is read only by the triangle tests: with
@@ -549,10 +556,18 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
 
   while (true) {
     const unsigned idle = __ballot_sync(0xffffffffu, ray_i < 0);
+    if (idle != 0u && (__popc(idle) >= SKW_TRAV_REFILL || idle == 0xffffffffu) && work && end >= 0 && next >= end) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(work, 32);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      gbase = base;
+      next = 0;
+      end = base < n ? min(32, n - base) : -1;
+    }
     if (idle != 0u && next < end && (__popc(idle) >= SKW_TRAV_REFILL || idle == 0xffffffffu)) {
       const int mine = next + __popc(idle & ((1u << lane) - 1u));
       next += __popc(idle);
-      const int idx = ((warp + (mine >> 5) * n_warps) << 5) + (mine & 31);
+      const int idx = work ? gbase + mine : ((warp + (mine >> 5) * n_warps) << 5) + (mine & 31);
       if (ray_i < 0 && mine < end && idx < n) {
         ray_i = idx;
         const RayF rl = load_ray(rays, ray_i);
@@ -590,7 +605,7 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     }
     const unsigned busy = __ballot_sync(0xffffffffu, ray_i >= 0);
     if (busy == 0u) {
-      if (next >= end) break;
+      if (next >= end && (!work || end < 0)) break;
       continue;
     }
     if (ray_i < 0) continue;
@@ -804,7 +819,7 @@ int device_sms() {
 template <int CAP>
 cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const void *rays, int64_t n,
                        const int *n_dev, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
-                       cudaStream_t stream, int ctas_per_sm) {
+                       cudaStream_t stream, int ctas_per_sm, int *work) {
   cudaError_t e = cap_prepare<CAP>();
   if (e != cudaSuccess) return e;
   int per_sm = cap_occupancy<CAP>(closest);
@@ -813,12 +828,15 @@ cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const 
   int64_t blocks = (int64_t)per_sm * device_sms();
   const int64_t needed = (n + 32 * warps_per_block - 1) / (32 * warps_per_block);
   if (blocks > needed) blocks = needed;
+  if (work && (e = cudaMemsetAsync(work, 0, sizeof(int), stream)) != cudaSuccess) return e;
   if (closest) {
     k_trace<CAP, true><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
-        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, n_dev, scene_abs, out_index, out, status);
+        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, n_dev, scene_abs, out_index, out, status,
+        work);
   } else {
     k_trace<CAP, false><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
-        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, n_dev, scene_abs, out_index, out, status);
+        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, n_dev, scene_abs, out_index, out, status,
+        work);
   }
   return cudaGetLastError();
 }
@@ -855,17 +873,17 @@ int traversal_stack_capacity(int max_depth) {
 
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
                              int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
-                             unsigned *status, cudaStream_t stream, int ctas_per_sm) {
+                             unsigned *status, cudaStream_t stream, int ctas_per_sm, int *work) {
   if (n <= 0) return cudaSuccess;
   switch (stack_cap) {
     case 48:
-      return launch_cap<48>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm);
+      return launch_cap<48>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm, work);
     case 96:
-      return launch_cap<96>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm);
+      return launch_cap<96>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm, work);
     case 192:
-      return launch_cap<192>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm);
+      return launch_cap<192>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm, work);
     default:
-      return launch_cap<416>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm);
+      return launch_cap<416>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm, work);
   }
 }
 
