@@ -828,6 +828,8 @@ cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const 
   int64_t blocks = (int64_t)per_sm * device_sms();
   const int64_t needed = (n + 32 * warps_per_block - 1) / (32 * warps_per_block);
   if (blocks > needed) blocks = needed;
+  // every warp draws at most one group past the end: keep the counter in int range
+  if (n > (int64_t)INT32_MAX - 32 * warps_per_block * blocks) work = nullptr;
   if (work && (e = cudaMemsetAsync(work, 0, sizeof(int), stream)) != cudaSuccess) return e;
   if (closest) {
     k_trace<CAP, true><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
