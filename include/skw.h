@@ -355,6 +355,24 @@ typedef struct skw_medium {
 /* Sets (medium != NULL) or removes (NULL) the scene's medium. */
 int skw_scene_set_medium(skw_scene *scene, const skw_medium *medium);
 
+/* The differential geometry of closest hits, as TriangleAccelerator::Intersect
+ * completes its Intersection with TriangleMesh::ComputeDifferentialGeometry
+ * (Raytracer/Core/TriangleAccelerator.cpp:303-347, TriangleMesh.cpp:414-484):
+ * the point o + d t, the geometric normal, the shading normal (interpolated
+ * vertex normals, or the geometric normal) and the barycentrics b1, b2 and t
+ * of the double Moller-Trumbore test, in double with the reference's
+ * operation order, on the scene's world-space triangle.  NaN for a miss.
+ * hits: as skw_intersect returns them for the scene's accelerator (prim, tri
+ * index the scene's primitives).  Device buffers. */
+typedef struct skw_hit_geometry {
+  double point[3];
+  double geometric_normal[3];
+  double shading_normal[3];
+  double b1, b2, t;
+} skw_hit_geometry;
+int skw_scene_hit_geometry(skw_scene *scene, const skw_ray *rays, const skw_hit *hits, int64_t n,
+                           skw_hit_geometry *out, void *stream);
+
 /* DirectLightingLTEIntegratorParams::m_max_specular_depth
  * (LTEIntegrators/DirectLightingLTEIntegrator.cpp:48-54): camera rays have
  * depth 0, and a hit on a SKW_MATERIAL_TRANSPARENT surface reached by a ray

@@ -223,6 +223,14 @@ class Scene {
   void RenderDirect(const skw_camera &camera, const skw_render_params &params, float *d_film, void *stream) {
     check(skw_render_direct(h_.get(), &camera, &params, d_film, stream), ctx_, "skw_render_direct");
   }
+  // The scene's accelerator (owned by the scene) and the differential
+  // geometry of its closest hits (TriangleMesh::ComputeDifferentialGeometry);
+  // device buffers.
+  skw_accel *Accelerator() const { return skw_scene_accel(h_.get()); }
+  void HitGeometry(const skw_ray *d_rays, const skw_hit *d_hits, int64_t n, skw_hit_geometry *d_out,
+                   void *stream) const {
+    check(skw_scene_hit_geometry(h_.get(), d_rays, d_hits, n, d_out, stream), ctx_, "skw_scene_hit_geometry");
+  }
   skw_scene *get() const { return h_.get(); }
   skw_ctx *context() const { return ctx_; }
 

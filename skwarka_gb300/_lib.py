@@ -92,6 +92,7 @@ SIGNATURES = [
     ("skw_merl_sample_host", C.c_int, [_P, _P, _P, C.c_int64, _P, _P, _P]),
     ("skw_scene_set_medium", C.c_int, [_P, C.c_void_p]),
     ("skw_scene_set_max_specular_depth", C.c_int, [_P, C.c_int32]),
+    ("skw_scene_hit_geometry", C.c_int, [_P, _P, _P, C.c_int64, _P, _P]),
     ("skw_render_photon", C.c_int, [_P, _P, C.c_void_p, C.c_void_p, C.c_void_p, _P, _P]),
     ("skw_scene_n_triangles", C.c_int64, [_P]),
     ("skw_scene_set_triangle_albedo", C.c_int, [_P, _P, _P]),

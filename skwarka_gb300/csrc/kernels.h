@@ -68,6 +68,9 @@ cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double
 // concatenated films, every pixel with spp samples.
 struct SceneDev;
 struct ViewDev;
+// Point, normals, barycentrics and t of closest hits (12 doubles each).
+cudaError_t launch_hit_geometry(const SceneDev &S, const void *rays, const void *hits, int64_t n, double *out,
+                                cudaStream_t s);
 // ld: LDSampler image points (sppx = samples per pixel, a power of two; sppy = 1)
 cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, int n_px, int sppx, int sppy,
                           void *rays, cudaStream_t s, int ld = 0);

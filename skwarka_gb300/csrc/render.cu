@@ -749,7 +749,80 @@ __global__ void k_film(const float *__restrict__ contrib, int64_t px_begin, int 
   film[o + 2] = bb * inv;
 }
 
+// TriangleMesh::ComputeDifferentialGeometry's point, barycentrics and
+// normals (Core/TriangleMesh.cpp:414-484) for closest hits of a render
+// scene, in double with the reference's operation order (no contraction):
+// Moller-Trumbore against the world triangle (_ComputeIntersectionPoint),
+// the point o + d t, the geometric normal (v1 - v0) x (v2 - v0) normalised
+// as Vector3D::Normalize does (times 1 / sqrt of the squared length), and the
+// shading normal b0 n0 + b1 n1 + b2 n2 normalised (the geometric normal
+// without vertex normals).  Out per hit: point, geometric normal, shading
+// normal, b1, b2, t (12 doubles); NaN for a miss.
+struct D3 {
+  double x, y, z;
+};
+__device__ __forceinline__ D3 d3sub(D3 a, D3 b) { return D3{__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y), __dsub_rn(a.z, b.z)}; }
+__device__ __forceinline__ D3 d3cross(D3 a, D3 b) {
+  return D3{__dsub_rn(__dmul_rn(a.y, b.z), __dmul_rn(a.z, b.y)), __dsub_rn(__dmul_rn(a.z, b.x), __dmul_rn(a.x, b.z)),
+            __dsub_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x))};
+}
+__device__ __forceinline__ double d3dot(D3 a, D3 b) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ D3 d3scale(D3 a, double s) { return D3{__dmul_rn(a.x, s), __dmul_rn(a.y, s), __dmul_rn(a.z, s)}; }
+__device__ __forceinline__ D3 d3normalized(D3 a) {
+  const double l2 = d3dot(a, a);
+  return l2 > 0.0 ? d3scale(a, __ddiv_rn(1.0, __dsqrt_rn(l2))) : a;
+}
+__device__ __forceinline__ D3 d3load(const float *p) { return D3{(double)p[0], (double)p[1], (double)p[2]}; }
+
+__global__ void k_hit_geometry(SceneDev S, const float4 *__restrict__ rays, const int4 *__restrict__ hits, int n,
+                               double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double *o = out + 12 * (int64_t)i;
+  const int4 hit = hits[i];
+  if (hit.y < 0) {
+    for (int k = 0; k < 12; ++k) o[k] = __longlong_as_double(0x7ff8000000000000ll);
+    return;
+  }
+  const int g = S.prim_tri_offset[hit.y] + hit.z;
+  const int j0 = S.tri_vidx[3 * g], j1 = S.tri_vidx[3 * g + 1], j2 = S.tri_vidx[3 * g + 2];
+  const D3 v0 = d3load(S.vpos + 3 * j0), v1 = d3load(S.vpos + 3 * j1), v2 = d3load(S.vpos + 3 * j2);
+  const float4 ra = rays[2 * i], rb = rays[2 * i + 1];
+  const D3 org{(double)ra.x, (double)ra.y, (double)ra.z}, dir{(double)ra.w, (double)rb.x, (double)rb.y};
+  const D3 e1 = d3sub(v1, v0), e2 = d3sub(v2, v0);
+  const D3 s1 = d3cross(dir, e2);
+  const double inv = __ddiv_rn(1.0, d3dot(s1, e1));
+  const D3 dd = d3sub(org, v0);
+  const double b1 = __dmul_rn(d3dot(dd, s1), inv);
+  const D3 s2 = d3cross(dd, e1);
+  const double b2 = __dmul_rn(d3dot(dir, s2), inv);
+  const double t = __dmul_rn(d3dot(e2, s2), inv);
+  const D3 p{__dadd_rn(org.x, __dmul_rn(dir.x, t)), __dadd_rn(org.y, __dmul_rn(dir.y, t)),
+             __dadd_rn(org.z, __dmul_rn(dir.z, t))};
+  const D3 ng = d3normalized(d3cross(e1, e2));
+  D3 ns = ng;
+  if (S.prim_has_normals[hit.y]) {
+    const double b0 = __dsub_rn(__dsub_rn(1.0, b1), b2);
+    const D3 n0 = d3load(S.vnrm + 3 * j0), n1 = d3load(S.vnrm + 3 * j1), n2 = d3load(S.vnrm + 3 * j2);
+    const D3 a = d3scale(n0, b0), b = d3scale(n1, b1), c = d3scale(n2, b2);
+    ns = d3normalized(D3{__dadd_rn(__dadd_rn(a.x, b.x), c.x), __dadd_rn(__dadd_rn(a.y, b.y), c.y),
+                         __dadd_rn(__dadd_rn(a.z, b.z), c.z)});
+  }
+  const double v[12] = {p.x, p.y, p.z, ng.x, ng.y, ng.z, ns.x, ns.y, ns.z, b1, b2, t};
+  for (int k = 0; k < 12; ++k) o[k] = v[k];
+}
+
 }  // namespace
+
+cudaError_t launch_hit_geometry(const SceneDev &S, const void *rays, const void *hits, int64_t n, double *out,
+                                cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_hit_geometry<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, (const float4 *)rays, (const int4 *)hits, (int)n,
+                                                              out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, int n_px, int sppx, int sppy,
                           void *rays, cudaStream_t s, int ld) {

@@ -1264,6 +1264,19 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
 
 extern "C" {
 
+int skw_scene_hit_geometry(skw_scene *s, const skw_ray *rays, const skw_hit *hits, int64_t n,
+                           skw_hit_geometry *out, void *stream) {
+  if (!s) return SKW_ERR_ARG;
+  if (n < 0 || n > (int64_t)INT32_MAX || (n > 0 && (!rays || !hits || !out)))
+    return fail(s->ctx, SKW_ERR_ARG, "bad hit-geometry buffers");
+  static_assert(sizeof(skw_hit_geometry) == 12 * sizeof(double), "skw_hit_geometry layout");
+  cudaError_t e = cudaSetDevice(s->ctx->device);
+  if (e == cudaSuccess) e = skw::launch_hit_geometry(s->dev, rays, hits, n, (double *)out, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(s->ctx, e, "hit geometry");
+  s->ctx->launches.fetch_add(n > 0 ? 1 : 0);
+  return SKW_OK;
+}
+
 int skw_scene_set_max_specular_depth(skw_scene *s, int32_t depth) {
   if (!s) return SKW_ERR_ARG;
   if (depth < 0 || depth > kMaxSpecDepth)

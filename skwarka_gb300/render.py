@@ -235,6 +235,18 @@ class RenderScene:
                            (C.c_float * 3)(*medium.sigma_s), (C.c_float * 3)(*medium.emission), medium.g, medium.step)
         _lib.check(_lib.load().skw_scene_set_medium(self.handle, None if m is None else C.byref(m)), self.ctx.handle)
 
+    def hit_geometry(self, rays, hits, stream=None):
+        """(n, 12) float64 CUDA tensor: point, geometric normal, shading
+        normal, b1, b2, t of closest hits (rays (n, 8) float32 and hits (n, 4)
+        int32 as skw_intersect returns them for this scene's accelerator)."""
+        import torch
+        n = rays.shape[0]
+        out = torch.empty((n, 12), dtype=torch.float64, device=rays.device)
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _lib.check(_lib.load().skw_scene_hit_geometry(self.handle, rays.data_ptr(), hits.data_ptr(), n,
+                                                      out.data_ptr(), s), self.ctx.handle)
+        return out
+
     def set_max_specular_depth(self, depth: int) -> None:
         """DirectLightingLTEIntegratorParams::m_max_specular_depth (default 10, at most 11)."""
         _lib.check(_lib.load().skw_scene_set_max_specular_depth(self.handle, int(depth)), self.ctx.handle)
