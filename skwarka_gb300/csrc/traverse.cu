@@ -482,12 +482,13 @@ __device__ __forceinline__ void store_result(void *__restrict__ out, const int32
   }
 }
 
-// Persistent traversal.  The rays form groups of 32 consecutive rays; warp w
-// of W owns groups w, w + W, w + 2W, ... (interleaved, so that every warp
-// gets a representative mix of cheap and expensive rays).  A
-// lane whose ray is finished takes the next ray of the warp's sequence when
-// at least SKW_TRAV_REFILL lanes are idle (or all are), so lanes rarely idle
-// while long rays finish.  No global atomics, no cross-warp waits.
+// Persistent traversal.  The rays form groups of 32 consecutive rays; a warp
+// takes the launch's next group from the launch's counter (`work`, one
+// atomicAdd per group) when its current group is used up, or, without a
+// counter, warp w of W owns groups w, w + W, w + 2W, ...  A lane whose ray
+// is finished takes the next ray of the warp's group when at least
+// SKW_TRAV_REFILL lanes are idle (or all are), so lanes rarely idle while
+// long rays finish.  No cross-warp waits.
 //
 // Closest-hit state is kept small: the slot of the current best hit and a
 // float interval [lo_t, hi_t] that contains the reference's current tmax
