@@ -122,6 +122,15 @@ cudaError_t launch_media(bool adjoint, const SceneDev &S, const ViewDev *views, 
                          int spp, int slots, int media_slot, const float *dfilm, const void *rays, const void *hits,
                          float *contrib, float *tcam, void *mrays, int *mtarget, float *mval, float *mdem,
                          int *mcount, unsigned *status, cudaStream_t s);
+// The medium along n entries of a specular level (rays, hits, in_sample,
+// in_w, in_node point at the first): in_w is multiplied by each segment's
+// transmittance, emission and queued light samples target the entry's
+// sample's slot spec_slot (mtarget holds full slot indices: resolve with
+// slots = 1, media_slot = 0).
+cudaError_t launch_media_specular(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin,
+                                  int spp, int slots, int spec_slot, const void *rays, const void *hits,
+                                  const int *in_sample, float *in_w, const int *in_node, float *contrib, void *mrays,
+                                  int *mtarget, float *mval, int *mcount, unsigned *status, cudaStream_t s);
 cudaError_t launch_resolve_media(bool adjoint, int64_t capacity, const uint8_t *occ, const int *mtarget,
                                  const float *mval, const float *mdem, const int *mcount, int slots, int media_slot,
                                  float *contrib, double *g_emission, cudaStream_t s);

@@ -552,6 +552,14 @@ struct MediaArgs {
   int media_slot;
   const ViewDev *views;
   int n_views;
+  // A specular level's entries instead of camera rays (in_sample non-null):
+  // entry i's sample, weight (multiplied by the segment's transmittance in
+  // place) and tree node; its emission and in-scattering go, weighted, into
+  // its sample's slot spec_slot.
+  const int *in_sample;
+  float *in_w;
+  const int *in_node;
+  int spec_slot;
 };
 
 __device__ __forceinline__ double radical_inverse_r(unsigned n, unsigned base) {
@@ -575,6 +583,9 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
                                                unsigned *__restrict__ status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.n) return;
+  const bool spec = A.in_sample != nullptr;  // a specular level's entry (forward only)
+  const int si = spec ? A.in_sample[i] : i;
+  const V3 wt = spec ? load3(A.in_w + 3 * (int64_t)i) : v3(1.0f, 1.0f, 1.0f);
   const MediumDev &M = S.medium;
   const float4 ra = rays[2 * i], rb = rays[2 * i + 1];
   const V3 o = v3(ra.x, ra.y, ra.z), d = v3(ra.w, rb.x, rb.y);
@@ -582,16 +593,18 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
   float t0 = 0.0f, t1 = hit.y >= 0 ? __int_as_float(hit.x) : __int_as_float(0x7f800000);
   V3 T = v3(1.0f, 1.0f, 1.0f);
   if (!medium_segment(M, o, d, t0, t1) || fabsf(t0 - t1) < kEps) {
-    store_rgb(tcam, i, T);
+    if (!spec) store_rgb(tcam, i, T);
     return;
   }
-  const int64_t P = A.px_begin + i / A.spp;
+  const int64_t P = A.px_begin + si / A.spp;
   int lo = 0, hi = A.n_views - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
     if (A.views[mid].px_begin <= P) lo = mid; else hi = mid - 1;
   }
-  const uint64_t gid = (uint64_t)((P - A.views[lo].px_begin) * A.spp + i % A.spp), seed = A.views[lo].seed;
+  const uint64_t gid = (uint64_t)((P - A.views[lo].px_begin) * A.spp + si % A.spp);
+  uint64_t seed = A.views[lo].seed;
+  if (spec) seed ^= 0xA0761D6478BD642Full * (uint64_t)A.in_node[i];  // the entry's stream, as in k_shade
   V3 dI = v3(0, 0, 0);
   if (ADJ) dI = load3(J.dfilm + 3 * P) * (1.0f / A.spp);
   const double offset1 = rnd(seed, gid, 62);
@@ -666,7 +679,8 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
       const int q = queue_append(want, mcount);
       if (want) {
         store_ray(mrays, q, point, ldir, 0.0f, dist);
-        mtarget[q] = i;
+        mtarget[q] = spec ? (int)((int64_t)si * A.slots + A.spec_slot) : i;
+        if (spec) val = mul(val, wt);
         if (ADJ) {
           mdem[q] = area && S.emission_scale > 0.0f ? dot(dI, val) / S.emission_scale : 0.0f;
         } else {
@@ -677,6 +691,13 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
     const float lum = 0.05316285f * T.x + 0.58515348f * T.y + 0.36168367f * T.z;
     if (lum < kEps) break;
     step = M.step / lum;
+  }
+  if (spec) {
+    // LTEIntegrator::Radiance of the specular ray: its surface radiance
+    // (shaded next, with the weight) times T, plus the medium's radiance
+    atomic_add_rgb(contrib, (int64_t)si * A.slots + A.spec_slot, mul(rad, wt));
+    store_rgb(A.in_w, i, mul(wt, T));
+    return;
   }
   store_rgb(tcam, i, T);
   if (!ADJ) store_rgb(contrib, (int64_t)i * A.slots + A.media_slot, rad);
@@ -977,7 +998,7 @@ cudaError_t launch_media(bool adjoint, const SceneDev &S, const ViewDev *views, 
                          float *contrib, float *tcam, void *mrays, int *mtarget, float *mval, float *mdem,
                          int *mcount, unsigned *status, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  MediaArgs A{n, px_begin, spp, slots, media_slot, views, n_views};
+  MediaArgs A{n, px_begin, spp, slots, media_slot, views, n_views, nullptr, nullptr, nullptr, 0};
   AdjointArgs J{dfilm, nullptr, nullptr, nullptr, nullptr, nullptr};
   const unsigned grid = (unsigned)((n + 127) / 128);
   if (adjoint)
@@ -986,6 +1007,18 @@ cudaError_t launch_media(bool adjoint, const SceneDev &S, const ViewDev *views, 
   else
     k_media<false><<<grid, 128, 0, s>>>(S, A, J, (const float4 *)rays, (const int4 *)hits, contrib, tcam,
                                         (float4 *)mrays, mtarget, mval, mdem, mcount, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_media_specular(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin,
+                                  int spp, int slots, int spec_slot, const void *rays, const void *hits,
+                                  const int *in_sample, float *in_w, const int *in_node, float *contrib, void *mrays,
+                                  int *mtarget, float *mval, int *mcount, unsigned *status, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  MediaArgs A{n, px_begin, spp, slots, 0, views, n_views, in_sample, in_w, in_node, spec_slot};
+  k_media<false><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, A, AdjointArgs{}, (const float4 *)rays,
+                                                              (const int4 *)hits, contrib, nullptr, (float4 *)mrays,
+                                                              mtarget, mval, nullptr, mcount, status);
   return cudaGetLastError();
 }
 

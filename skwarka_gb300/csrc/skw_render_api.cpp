@@ -353,6 +353,7 @@ struct PassConfig {
   int extra_slots = 0;       // contribution slots after the direct-lighting ones (final gather)
   bool media = true;         // march the scene's medium (if any) along the camera rays (one more slot, last)
   bool specular = true;      // follow specular reflection / transmission (if the scene has such materials)
+  bool media_specular = false;  // a medium along specular rays too (host round trips: not in graphs)
 };
 
 // Entries of the largest specular level of a pass (the pass is sized so
@@ -498,8 +499,9 @@ int plan_make(skw_scene *s, const skw_camera *cams, int n_views, const skw_rende
   P->npl = s->dev.n_point_lights;
   P->media = cfg.media && s->dev.medium.on;
   P->spec_levels = cfg.specular && s->dev.has_specular ? s->dev.max_spec_depth + 1 : 0;
-  if (P->media && P->spec_levels)
-    return fail(ctx, SKW_ERR_UNSUPPORTED, "a participating medium together with specular materials");
+  if (P->media && P->spec_levels && !cfg.media_specular)
+    return fail(ctx, SKW_ERR_UNSUPPORTED,
+                "a participating medium together with specular materials (single-camera render only)");
   P->slots = 1 + 2 * P->nl + P->npl + cfg.extra_slots + (P->spec_levels ? 1 : 0) + (P->media ? 1 : 0);
   P->media_slot = P->slots - 1;
   P->spec_slot = P->slots - 1 - (P->media ? 1 : 0);
@@ -587,6 +589,33 @@ cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, con
     if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.qrays[qi], cl, W.counts + 3 + qi, a->scene_abs,
                                    nullptr, W.qhits, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
       return e;
+    if (P.media) {
+      // The medium along the level's rays (LTEIntegrator::Radiance of each
+      // specular ray): the level's length is read back and its entries
+      // marched in chunks that the media queue holds.
+      int cnt = 0;
+      if ((e = cudaMemcpyAsync(&cnt, W.counts + 3 + qi, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+          (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return e;
+      cnt = (int)std::min<int64_t>(cnt, cl);
+      for (int off = 0; off < cnt; off += (int)P.cap_samples) {
+        const int m = (int)std::min<int64_t>(P.cap_samples, cnt - off);
+        if ((e = cudaMemsetAsync(W.counts + 2, 0, sizeof(int), st)) != cudaSuccess) return e;
+        if ((e = skw::launch_media_specular(s->dev, d_views, nv, m, px0, P.spp, P.slots, P.spec_slot,
+                                            (const char *)W.qrays[qi] + 32 * (int64_t)off,
+                                            (const char *)W.qhits + 16 * (int64_t)off, W.qsample[qi] + off,
+                                            W.qw[qi] + 3 * (int64_t)off, W.qnode[qi] + off, W.contrib, W.mrays,
+                                            W.mtarget, W.mval, W.counts + 2, a->d_status, st)) != cudaSuccess)
+          return e;
+        const int64_t cm = (int64_t)m * s->dev.medium.max_steps;
+        if ((e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.mrays, cm, W.counts + 2, a->scene_abs,
+                                       nullptr, W.mocc, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
+          return e;
+        if ((e = skw::launch_resolve_media(false, cm, W.mocc, W.mtarget, W.mval, W.mdem, W.counts + 2, 1, 0,
+                                           W.contrib, nullptr, st)) != cudaSuccess)
+          return e;
+      }
+    }
     if ((e = skw::launch_shade_specular(s->dev, d_views, nv, cl, px0, P.spp, P.slots, P.nl, q, L, W.qhits, W.contrib,
                                         W.srays, W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb,
                                         W.counts + 1, W.bnrm, st)) != cudaSuccess)
@@ -817,7 +846,9 @@ int skw_render_direct(skw_scene *s, const skw_camera *cam, const skw_render_para
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
   Plan P;
   const uint64_t seed = params->seed;
-  int rc = plan_make(s, cam, 1, params, &seed, PassConfig{}, &P);
+  PassConfig cfg;
+  cfg.media_specular = true;  // no graph here: the specular levels' media may read their lengths back
+  int rc = plan_make(s, cam, 1, params, &seed, cfg, &P);
   if (rc != SKW_OK) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   cudaMemPool_t pool;

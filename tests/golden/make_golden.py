@@ -200,6 +200,11 @@ def specular_golden():
     on_floor = np.abs(indirect[:, 2]) < 1e-4
     out["photon_counts"] = np.array([len(caustic), len(direct), len(indirect), on_floor.sum()], np.int64)
     out["caustic_xy"] = np.concatenate([caustic[:, :2].mean(0), [np.sqrt((caustic[:, :2] ** 2).sum(1).mean())]])
+    # the clear-glass sphere under the point light inside a scattering medium
+    from skwarka_gb300.render import Medium
+    prims, mats, lights, cam = sf.specular_cases()["glass_point"]
+    out["glass_point_medium"], _ = ref.render_direct(prims, mats, lights, cam, 16, 16, 1,
+                                                     medium=sf.specular_medium())
     # photon-mapping renders (1,000,000 paths, 16 gather samples, 8x8 spp)
     for name in ("glass_point", "glass_area"):
         prims, mats, lights, cam = sf.specular_cases()[name]

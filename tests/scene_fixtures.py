@@ -336,3 +336,12 @@ def specular_cases():
             "glass_point": specular_scene(glass, "point"),
             "tinted_area": specular_scene(tinted, "area"),
             "mirror_area": specular_scene(mirror, "area")}
+
+
+def specular_medium():
+    """A scattering, absorbing medium around the glass sphere and the lit
+    floor (box [-1.5, 1.5]^2 x [0, 1.3], sigma_a 0.1, sigma_s 0.3, HG g 0.3,
+    march step 0.05)."""
+    from skwarka_gb300.render import Medium
+    return Medium(lo=(-1.5, -1.5, 0.0), hi=(1.5, 1.5, 1.3), sigma_a=(0.1, 0.1, 0.1), sigma_s=(0.3, 0.3, 0.3),
+                  g=0.3, step=0.05)
