@@ -215,3 +215,20 @@ def test_ld_sampler_parity_with_reference(gpu):
     again = sc.render_direct(c, 2, 2, seed=21, sampler=LD).cpu().numpy()
     other = sc.render_direct(c, 2, 2, seed=23, sampler=LD).cpu().numpy()
     assert np.array_equal(again, gpu_ld) and not np.array_equal(other, gpu_ld)
+
+
+def test_ld_sampler_rounds_counts_to_powers_of_two(gpu):
+    """LDSampler(n) takes the next power of two samples per pixel, and the
+    light-sample count is rounded the same way (Sampler::AddSamplesSequence*):
+    3 x 1, 4 x 1 and 2 x 2 are all 4 samples; 3 light samples are 4."""
+    from skwarka_gb300.render import LD
+    prims, mats, cam = scenes.direct_lighting_box()
+    sc = RenderScene(prims, mats)
+    c = cam(16, 16)
+    a = sc.render_direct(c, 3, 1, seed=5, sampler=LD).cpu().numpy()
+    b = sc.render_direct(c, 4, 1, seed=5, sampler=LD).cpu().numpy()
+    d = sc.render_direct(c, 2, 2, seed=5, sampler=LD).cpu().numpy()
+    assert np.array_equal(a, b) and np.array_equal(a, d)
+    l3 = sc.render_direct(c, 2, 2, light_samples=3, seed=5, sampler=LD).cpu().numpy()
+    l4 = sc.render_direct(c, 2, 2, light_samples=4, seed=5, sampler=LD).cpu().numpy()
+    assert np.array_equal(l3, l4)

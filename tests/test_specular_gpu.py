@@ -204,3 +204,26 @@ def test_specular_scene_refusals(gpu):
     sc = RenderScene(prims, mats, lights, medium=sf.specular_medium())
     with pytest.raises(_lib.SkwError, match="medium"):
         RenderBatch(sc, [cam], 1, 1)
+
+
+def test_specular_edge_cases(gpu):
+    """Depth 11 (the deepest: 4,095 rays per sample) renders; depths outside
+    [0, 11] and a non-positive refractive index are refused; a transparent
+    material with neither reflection nor transmission scatters nothing (the
+    sphere goes dark where it is seen directly)."""
+    from skwarka_gb300.render import TRANSPARENT, Material
+    prims, mats, lights, cam = sf.specular_cases()["glass_area"]
+    sc = RenderScene(prims, mats, lights)
+    sc.set_max_specular_depth(11)
+    deep = sc.render_direct(cam, 1, 1, seed=2).cpu().numpy()
+    assert np.isfinite(deep).all() and (deep >= 0).all() and deep.mean() > 0
+    for bad in (-1, 12):
+        with pytest.raises(_lib.SkwError):
+            sc.set_max_specular_depth(bad)
+    with pytest.raises(_lib.SkwError, match="refractive index"):
+        RenderScene(prims, [mats[0], Material(kind=TRANSPARENT, refractive_index=0.0), mats[2]], lights)
+    dark = RenderScene(prims, [mats[0], Material(kind=TRANSPARENT, kd=(0, 0, 0), ks=(0, 0, 0)), mats[2]], lights)
+    img = dark.render_direct(cam, 2, 2, seed=2).cpu().numpy() @ LUM
+    glass = sc.render_direct(cam, 2, 2, seed=2).cpu().numpy() @ LUM
+    center = (slice(cam.height // 2 - 2, cam.height // 2 + 2), slice(cam.width // 2 - 2, cam.width // 2 + 2))
+    assert np.all(img[center] == 0.0) and glass[center].mean() > 0.0
