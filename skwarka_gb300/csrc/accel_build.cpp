@@ -104,6 +104,7 @@ struct Builder {
   std::vector<int32_t> tidx;  // mesh triangle index per triangle
   std::vector<BoxF> tbox;     // per-triangle AABB
   std::atomic<int> threads_left{0};
+  int threads = 1;  // the build's thread budget
   std::atomic<int32_t> max_depth{0};
   std::atomic<int64_t> n_leaves{0};
 
@@ -114,37 +115,67 @@ struct Builder {
     std::swap(tbox[a], tbox[b]);
   }
 
+  // One axis's buckets of _DetermineBestSplit over triangles [ib, ie):
+  // left / middle / right boxes and counts per candidate plane.  Box unions
+  // (min / max) and counts do not depend on the order the triangles come
+  // in, so partial buckets over slices of the range merge exactly.
+  struct Buckets {
+    BoxD L[kMaxSplitTries], M[kMaxSplitTries], R[kMaxSplitTries];
+    size_t Ln[kMaxSplitTries] = {0}, Mn[kMaxSplitTries] = {0}, Rn[kMaxSplitTries] = {0};
+    void merge(const Buckets &o, size_t tries) {
+      for (size_t i = 0; i < tries; ++i) {
+        L[i].unite(o.L[i]);
+        M[i].unite(o.M[i]);
+        R[i].unite(o.R[i]);
+        Ln[i] += o.Ln[i];
+        Mn[i] += o.Mn[i];
+        Rn[i] += o.Rn[i];
+      }
+    }
+  };
+  void fill_buckets(const BoxF &nb, int axis, size_t ib, size_t ie, size_t tries, double coef, Buckets &k) const {
+    for (size_t i = ib; i < ie; ++i) {
+      const BoxF &b = tbox[i];
+      const float dmax = b.hi[axis] - nb.lo[axis];
+      const float dmin = b.lo[axis] - nb.lo[axis];
+      const size_t lefts_begin = std::min(tries, cast_size((double)dmax * coef + 1.0));
+      const size_t rights_end = std::min(tries, cast_size((double)dmin * coef + 1.0));
+      if (rights_end > 0) {
+        k.R[rights_end - 1].unite(b);
+        k.Rn[rights_end - 1] += 1;
+      }
+      if (lefts_begin < tries) {
+        k.L[lefts_begin].unite(b);
+        k.Ln[lefts_begin] += 1;
+      }
+      for (size_t j = rights_end; j < lefts_begin; ++j) {
+        k.M[j].unite(b);
+        k.Mn[j] += 1;
+      }
+    }
+  }
+
   // _DetermineBestSplit (TriangleAccelerator.cpp:505-617), triangles only.
+  // Nodes of at least kParallelSplit triangles (the top of the tree, where
+  // few subtrees run side by side) fill their buckets on several threads,
+  // one slice of the triangles and one axis each.
+  static constexpr size_t kParallelSplit = (size_t)1 << 17;
   void best_split(const BoxF &nb, size_t tb, size_t te, unsigned mask, int &axis_out, double &pos_out) const {
     const size_t n = te - tb;
     double best_pos[3] = {0, 0, 0}, best_cost[3] = {kInfD, kInfD, kInfD};
+    const size_t tries = std::min(kMaxSplitTries, 2 * n);
+    double coefs[3] = {0, 0, 0};
     for (int axis = 0; axis < 3; ++axis) {
-      if (mask & (1u << axis)) continue;
-      BoxD L[kMaxSplitTries], M[kMaxSplitTries], R[kMaxSplitTries];
-      size_t Ln[kMaxSplitTries] = {0}, Mn[kMaxSplitTries] = {0}, Rn[kMaxSplitTries] = {0};
-      const size_t tries = std::min(kMaxSplitTries, 2 * n);
       const float ext = nb.hi[axis] - nb.lo[axis];
       // size_t / float converts the count to float: float division.
-      const double coef = (double)((float)tries / ext);
-      for (size_t i = 0; i < n; ++i) {
-        const BoxF &b = tbox[tb + i];
-        const float dmax = b.hi[axis] - nb.lo[axis];
-        const float dmin = b.lo[axis] - nb.lo[axis];
-        const size_t lefts_begin = std::min(tries, cast_size((double)dmax * coef + 1.0));
-        const size_t rights_end = std::min(tries, cast_size((double)dmin * coef + 1.0));
-        if (rights_end > 0) {
-          R[rights_end - 1].unite(b);
-          Rn[rights_end - 1] += 1;
-        }
-        if (lefts_begin < tries) {
-          L[lefts_begin].unite(b);
-          Ln[lefts_begin] += 1;
-        }
-        for (size_t j = rights_end; j < lefts_begin; ++j) {
-          M[j].unite(b);
-          Mn[j] += 1;
-        }
-      }
+      coefs[axis] = (double)((float)tries / ext);
+    }
+    // The reference's cost of every candidate plane of one axis (prefix
+    // unions of the left boxes, suffix unions of the right ones).
+    auto score = [&](int axis, Buckets &k) {
+      const float ext = nb.hi[axis] - nb.lo[axis];
+      BoxD *L = k.L, *M = k.M, *R = k.R;
+      size_t *Ln = k.Ln, *Mn = k.Mn, *Rn = k.Rn;
       for (size_t i = 1; i < tries; ++i) {
         L[i].unite(L[i - 1]);
         Ln[i] += Ln[i - 1];
@@ -165,6 +196,34 @@ struct Builder {
           // min + i*(max-min)/tries, evaluated in float.
           best_pos[axis] = (double)(nb.lo[axis] + ((float)i * ext) / (float)tries);
         }
+      }
+    };
+    const size_t slices = n >= kParallelSplit && threads > 1 ? std::min<size_t>(std::max(1, threads / 3), 16) : 1;
+    if (slices > 1) {
+      std::vector<Buckets> part(3 * slices);
+      std::vector<std::thread> pool;
+      for (int axis = 0; axis < 3; ++axis) {
+        if (mask & (1u << axis)) continue;
+        for (size_t c = 0; c < slices; ++c) {
+          const size_t ib = tb + n * c / slices, ie = tb + n * (c + 1) / slices;
+          pool.emplace_back([this, &nb, &part, axis, ib, ie, tries, c, slices, coef = coefs[axis]]() {
+            fill_buckets(nb, axis, ib, ie, tries, coef, part[(size_t)axis * slices + c]);
+          });
+        }
+      }
+      for (std::thread &t : pool) t.join();
+      for (int axis = 0; axis < 3; ++axis) {
+        if (mask & (1u << axis)) continue;
+        Buckets &k = part[(size_t)axis * slices];
+        for (size_t c = 1; c < slices; ++c) k.merge(part[(size_t)axis * slices + c], tries);
+        score(axis, k);
+      }
+    } else {
+      for (int axis = 0; axis < 3; ++axis) {
+        if (mask & (1u << axis)) continue;
+        Buckets k;
+        fill_buckets(nb, axis, tb, te, tries, coefs[axis], k);
+        score(axis, k);
       }
     }
     if (best_cost[0] <= best_cost[1] && best_cost[0] <= best_cost[2]) {
@@ -306,7 +365,8 @@ std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *pr
   const size_t n = B.prim.size();
   if (n > (size_t)INT32_MAX) return "too many triangles";
   unsigned hw = std::thread::hardware_concurrency();
-  B.threads_left = (threads > 0 ? threads : (int)(hw ? hw : 1)) - 1;
+  B.threads = threads > 0 ? threads : (int)(hw ? hw : 1);
+  B.threads_left = B.threads - 1;
 
   out.nodes.clear();
   out.tris.clear();
