@@ -39,6 +39,9 @@ def test_version_and_null_args(built):
     assert lib.skw_ctx_create(0, None) == 1  # SKW_ERR_ARG
     assert lib.skw_accel_get_info(None, None) == 1
     assert lib.skw_flat_tree_build(None, 0, None, 0, 0, None, None, 0) == 1
+    assert lib.skw_scene_set_max_specular_depth(None, 3) == 1
+    assert lib.skw_scene_hit_geometry(None, None, None, 0, None, None) == 1
+    assert lib.skw_scene_set_medium(None, None) == 1
 
 
 def test_ctx_without_gpu_reports_no_device(built):
