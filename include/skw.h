@@ -149,7 +149,10 @@ int skw_accel_export(const skw_accel *accel, uint32_t *nodes, int32_t *tri_prim,
 /* Closest hit for n rays, device buffers.  Stands in for
  * TriangleAccelerator::Intersect / Scene::Intersect
  * (Raytracer/Core/TriangleAccelerator.cpp:295-352, Scene.h:77-85) without the
- * differential-geometry step. */
+ * differential-geometry step (skw_scene_hit_geometry does that part).  Each
+ * call takes a 256-byte work counter from the context's stream-ordered
+ * pool (allocated and freed on `stream`), so calls on different streams
+ * may run at the same time. */
 int skw_intersect(skw_accel *accel, const skw_ray *rays, int64_t n, skw_hit *hits, void *stream);
 
 /* Any hit in [tmin, tmax] for n rays, device buffers; occluded[i] = 0 or 1.
