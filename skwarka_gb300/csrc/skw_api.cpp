@@ -76,6 +76,10 @@ int skw_ctx_create(int device, skw_ctx **out) {
 
 void skw_ctx_destroy(skw_ctx *ctx) {
   if (!ctx) return;
+  for (int i = 0; i < 2; ++i) {
+    if (ctx->host_st[i]) cudaStreamDestroy(ctx->host_st[i]);
+    if (ctx->host_ev[i]) cudaEventDestroy(ctx->host_ev[i]);
+  }
   if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   delete ctx;
 }
@@ -285,9 +289,12 @@ static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64
   cudaEvent_t ev[2] = {nullptr, nullptr};
   int rc = SKW_OK;
   for (int i = 0; i < n_streams && rc == SKW_OK; ++i) {
-    if ((e = cudaStreamCreateWithFlags(&st[i], cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming)) != cudaSuccess)
-      rc = cuda_fail(a->ctx, e, "stream");
+    skw_ctx *c = a->ctx;
+    if ((!c->host_st[i] && (e = cudaStreamCreateWithFlags(&c->host_st[i], cudaStreamNonBlocking)) != cudaSuccess) ||
+        (!c->host_ev[i] && (e = cudaEventCreateWithFlags(&c->host_ev[i], cudaEventDisableTiming)) != cudaSuccess))
+      rc = cuda_fail(c, e, "stream");
+    st[i] = c->host_st[i];
+    ev[i] = c->host_ev[i];
   }
   void *d_rays = nullptr, *d_out = nullptr;
   int *d_work = nullptr;  // one ray-group counter per stream (256 bytes apart)
@@ -329,9 +336,7 @@ static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64
     if (st[i]) {
       e = cudaStreamSynchronize(st[i]);
       if (rc == SKW_OK && e != cudaSuccess) rc = cuda_fail(a->ctx, e, "query execution");
-      cudaStreamDestroy(st[i]);
     }
-    if (ev[i]) cudaEventDestroy(ev[i]);
   }
   if (rc == SKW_OK) {
     unsigned sv = 0;

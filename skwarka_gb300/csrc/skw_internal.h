@@ -20,6 +20,10 @@ struct skw_ctx {
   // Stream-ordered pool for per-call workspaces; it keeps freed memory
   // (release threshold = max) so repeated calls do not remap.
   cudaMemPool_t pool = nullptr;
+  // The host-buffer queries' two streams and events, made on first use and
+  // kept (creating and destroying them per call cost ~0.1 ms).
+  cudaStream_t host_st[2] = {nullptr, nullptr};
+  cudaEvent_t host_ev[2] = {nullptr, nullptr};
 };
 
 // A device-resident accelerator (skw_accel_create / _from_flat).
