@@ -160,9 +160,48 @@ def load_traffic(kind: str, rays: int):
     return d.get("dram_bytes_per_launch", 0.0) + d["dram_bytes_per_ray"] * rays
 
 
-def cpu_baseline(meshes, rays, sample, rank):
+def hit_parity(gpu_hits: np.ndarray, ref: dict) -> dict:
+    """Agreement of the GPU's closest hits (int32 (n, 4): t bits, prim, tri,
+    flags) with the reference's on the same rays: hit-id agreement over
+    (primitive, mesh triangle), the largest relative t difference on agreeing
+    hits, and how many GPU hits were decided or refined in double precision
+    or flagged as near ties."""
+    g = np.asarray(gpu_hits)
+    prim, tri, flags = g[:, 1], g[:, 2], g[:, 3].astype(np.uint32)
+    t = g[:, 0].copy().view(np.float32).astype(np.float64)
+    same = (prim == ref["prim"]) & (tri == ref["tri"])
+    hit = same & (ref["prim"] >= 0)
+    rel = np.abs(t[hit] - ref["t"][hit]) / np.maximum(np.abs(ref["t"][hit]), 1e-300)
+    diff = np.nonzero(~same)[0]
+    return {"rays": int(len(g)), "hit_id_agree": float(same.mean()), "mismatches": int(len(diff)),
+            "mismatch_near_tie": int(((flags[diff] & 2) != 0).sum()),
+            "max_t_rel": float(rel.max()) if len(rel) else 0.0,
+            "fp64_decided": int(((flags & 1) != 0).sum()), "near_ties": int(((flags & 2) != 0).sum()),
+            "t_refined": int(((flags & 4) != 0).sum()), "hits": int((ref["prim"] >= 0).sum())}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (from /proc/cpuinfo or lscpu)."""
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            k = line.split(":")[0].strip().lower()
+            if k in ("model name", "cpu model", "hardware"):
+                return line.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def cpu_baseline(meshes, rays, sample, rank, gpu_hits=None):
     """The reference's own Intersect over `sample` rays on all host cores, plus
-    the instrumented oracle's node / triangle counts on the same rays."""
+    the instrumented oracle's node / triangle counts on the same rays.  With
+    the GPU's hits for those rays, the reference's answers are kept and
+    compared with them (parity on the timed workload)."""
     from oracle.api import Oracle, Reference
     cores = os.cpu_count() or 1
     sub = rays[:sample]
@@ -173,17 +212,35 @@ def cpu_baseline(meshes, rays, sample, rank):
         ra = Reference().accel(meshes)
         ra.intersect(sub[:10_000])
         t0 = time.perf_counter()
-        ra.intersect(sub, threads=cores)
+        res = ra.intersect(sub, threads=cores)
         dt = time.perf_counter() - t0
         kind = "reference"
     else:
         t0 = time.perf_counter()
-        oa.intersect(sub, threads=cores)
+        res = oa.intersect(sub, threads=cores)
         dt = time.perf_counter() - t0
         kind = "port"
-    return {"value": sample / dt / 1e6, "unit": UNIT, "cores": cores, "kind": kind,
-            "sample": f"{sample} of the step's rays, TriangleAccelerator::Intersect incl. differential geometry"
-            if kind == "reference" else f"{sample} of the step's rays, oracle restatement"}, (n_nodes, n_tris)
+    out = {"value": sample / dt / 1e6, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": kind,
+           "sample": f"{sample} of the step's rays, TriangleAccelerator::Intersect incl. differential geometry"
+           if kind == "reference" else f"{sample} of the step's rays, oracle restatement"}
+    parity = hit_parity(gpu_hits[:sample], res) if gpu_hits is not None else None
+    return out, (n_nodes, n_tris), parity
+
+
+def knn_parity(gpu: dict, gpu_perm: np.ndarray, ref: dict, ref_perm: np.ndarray) -> dict:
+    """Agreement of the GPU's k-NN answers with the reference's on the same
+    queries and photons: found counts, index sets, heap order and squared
+    distances (indices mapped through each tree's permutation to input
+    order, so that the comparison does not rest on the two trees' orders)."""
+    def ids(idx, perm):
+        out = np.where(idx >= 0, perm[np.maximum(idx, 0)], -1)
+        return out
+    gi, ri = ids(gpu["idx"], gpu_perm), ids(ref["idx"], ref_perm)
+    sets = np.array_equal(np.sort(gi, axis=1), np.sort(ri, axis=1))
+    return {"queries": int(len(gi)), "counts_equal": bool(np.array_equal(gpu["count"], ref["count"])),
+            "sets_equal": bool(sets), "order_equal": bool(np.array_equal(gi, ri)),
+            "d2_equal": bool(np.array_equal(gpu["d2"].view(np.uint64), ref["d2"].view(np.uint64))),
+            "rows_differing": int((gi != ri).any(axis=1).sum())}
 
 
 def render_bench(args, dev, ctx, measure_cpu):
@@ -245,7 +302,7 @@ def render_bench(args, dev, ctx, measure_cpu):
             ref = Reference()
             ref.render_direct(prims, mats, [], camf(64, 64), 2, 2)
             _, sec = ref.render_direct(prims, mats, [], cam, 2, 2)
-            out["cpu_baseline"] = {"value": samples / sec / 1e6, "unit": "Msamples/s", "cores": os.cpu_count() or 1,
+            out["cpu_baseline"] = {"value": samples / sec / 1e6, "unit": "Msamples/s", "cores": os.cpu_count() or 1, "cpu": cpu_model(),
                                    "kind": "reference", "sample": "one full 256x256 4-spp frame, SamplerBasedRenderer"}
     return out
 
@@ -285,7 +342,7 @@ def specular_bench(args, dev, ctx, measure_cpu):
         if Reference.available():
             log("reference specular render")
             _, sec = Reference().render_direct(prims, mats, lights, cam, 2, 2)
-            out["cpu_baseline"] = {"value": samples / sec / 1e6, "unit": "Msamples/s", "cores": os.cpu_count() or 1,
+            out["cpu_baseline"] = {"value": samples / sec / 1e6, "unit": "Msamples/s", "cores": os.cpu_count() or 1, "cpu": cpu_model(),
                                    "kind": "reference",
                                    "sample": "one full 256x256 4-spp frame, SamplerBasedRenderer, max specular depth 6"}
     return out
@@ -429,6 +486,18 @@ def photon_bench(args, dev, ctx, measure_cpu):
            "paths": paths, "shoot_paths_per_s": paths / (info["shoot_ms"] / 1e3), "shoot_ms": info["shoot_ms"],
            "maps_build_ms": info["build_ms"], "shoot_and_build_wall_s": wall,
            "photons": {k: info["n_" + k] for k in ("caustic", "direct", "indirect", "irradiance")}}
+    # the same shoot with the reference's own rules (luminance Russian
+    # roulette, no bounce cap within the 1,024 the GPU allows): the figure to
+    # set beside the reference's ShootPhotons
+    PhotonMap.shoot(sc, 100_000, max_bounces=1024, rr_probability=0.0, seed=1)
+    torch.cuda.synchronize()
+    pm_ref_rules = PhotonMap.shoot(sc, paths, max_bounces=1024, rr_probability=0.0, seed=2)
+    ir = pm_ref_rules.info()
+    out["shoot_reference_rules"] = {
+        "rules": "luminance Russian roulette (the reference's), bounce cap 1024", "paths_per_s":
+        paths / (ir["shoot_ms"] / 1e3), "shoot_ms": ir["shoot_ms"], "maps_build_ms": ir["build_ms"],
+        "photons": {k: ir["n_" + k] for k in ("caustic", "direct", "indirect", "irradiance")}}
+    del pm_ref_rules
     # k-NN at the primary hits
     cam = camf(512, 512)
     rays = torch.from_numpy(scenes.camera_rays(cam, 4, 4, seed=3)).to(dev)
@@ -494,8 +563,10 @@ def photon_bench(args, dev, ctx, measure_cpu):
             qs, qns = q.cpu().numpy()[pick], qn.cpu().numpy()[pick]
             ns = len(pick)
             t0 = time.perf_counter()
-            rkd.knn(qs, qns, 100, 0.05, 0.87, threads=os.cpu_count() or 1)
+            rres = rkd.knn(qs, qns, 100, 0.05, 0.87, threads=os.cpu_count() or 1)
             kdt = time.perf_counter() - t0
+            out["knn"]["parity"] = knn_parity({k: v.cpu().numpy()[pick] for k, v in res.items()}, kd.perm, rres,
+                                              rkd.perm)
             # the k-NN roofline: algorithmic bytes per query 32 + 36 N_visited + 8 k
             # (query in; node and photon per visited point; results out), N_visited
             # from the instrumented oracle walk (the reference's order) on the sample
@@ -510,7 +581,7 @@ def photon_bench(args, dev, ctx, measure_cpu):
                                       "frac": achieved / peak, "bytes_per_query": bpq,
                                       "visited_per_query": n_vis, "peak_source": peak_kind}
             out["cpu_baseline"] = {
-                "kind": "reference", "cores": os.cpu_count() or 1,
+                "kind": "reference", "cores": os.cpu_count() or 1, "cpu": cpu_model(),
                 "shoot_paths_per_s": paths / rinfo["shoot_s"], "shoot_s_incl_maps": rinfo["shoot_s"],
                 "photons": {k: rinfo[k] for k in ("caustic", "direct", "indirect", "irradiance")},
                 "knn_queries_per_s": ns / kdt,
@@ -530,29 +601,31 @@ def run_reference(args):
     from oracle.api import Oracle, Reference
     meshes = scenes.ray_query_scene(args.subdiv, args.nrandom, seed=3)
     lo, hi = scenes.scene_bounds(meshes)
-    rays = scenes.uniform_rays(args.cpu_sample, lo, hi, seed=7)
+    # the same rays as rank 0 of the GPU arm traces, all of them every step
+    rays = scenes.uniform_rays(args.rays, lo, hi, seed=rank_ray_seed(0))
     cores = os.cpu_count() or 1
     if Reference.available():
         acc, kind = Reference().accel(meshes), "reference"
     else:
         acc, kind = Oracle().accel(meshes), "port"
     for _ in range(args.warmup):
-        acc.intersect(rays[:100_000], threads=cores)
+        acc.intersect(rays[:100_000], threads=cores)  # warm-up on a slice of the rays
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         acc.intersect(rays, threads=cores)
         times.append(time.perf_counter() - t0)
     total = sum(times)
-    value = args.cpu_sample * args.steps / total / 1e6
+    value = args.rays * args.steps / total / 1e6
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {**config(args, world), "rays_per_step_per_gpu": args.cpu_sample,
-                       "note": "each step traces a bounded sample of the workload's rays"},
+            "config": config(args, world),
+            "note": "host CPU (no L2 flush); TriangleAccelerator::Intersect includes the differential geometry "
+                    "of each hit",
             "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
-                             "sample": f"{args.cpu_sample} rays per step"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": kind,
+                             "sample": f"all {args.rays} rays of the step, every step"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -655,10 +728,12 @@ def main():
         return 0
 
     cpu = None
+    parity = None
     n_nodes, n_tris = None, None
     if not args.no_cpu_baseline and world == 1:
         log("CPU baseline (reference Intersect)")
-        cpu, (n_nodes, n_tris) = cpu_baseline(meshes, rays_np, min(args.cpu_sample, args.rays), rank)
+        cpu, (n_nodes, n_tris), parity = cpu_baseline(meshes, rays_np, min(args.cpu_sample, args.rays), rank,
+                                                      gpu_hits=hits.cpu().numpy())
     render = None
     if not args.no_render:
         log("direct-lighting render")
@@ -696,7 +771,7 @@ def main():
             "config": config(args, world),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": args.rays * 32,
                     "d2h_bytes_per_step": args.rays * 16},
-            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,
+            "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "clocks": clk.summary(), "gpu_launches": launches,
             "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit, "render": render, "specular": specular, "batch": batch, "adjoint": adjoint, "photon": photon,
             "accel": {k: acc.info[k] for k in ("n_nodes", "max_depth", "build_ms", "device_bytes")}}
     print(json.dumps(line), flush=True)

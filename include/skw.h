@@ -220,6 +220,9 @@ int skw_knn(skw_kdtree *tree, const double *q, const double *qn, int64_t nq, int
  * that.  Results are identical to skw_knn.  The first call on a device looks
  * the array's device address up (cudaGetSymbolAddress), which can load the
  * library's device code; make that first call before any stream capture.
+ * The address is looked up again when the device's current context has
+ * changed since (a cudaDeviceReset destroys the array's module; every
+ * handle made before a reset is invalid anyway).
  * All calls share the array, and it keeps the previous call's contents:
  * every heap slot is written before it is read, so nothing needs clearing,
  * but calls that overlap on the GPU (different streams or contexts) race on

@@ -29,7 +29,9 @@ What it does:
    ray-query / light-transport path), plus ``oracle/ref_driver.cpp`` (our
    C-ABI shim over the reference classes), into one shared library.
 
-Usage: ``python oracle/build_ref.py`` (idempotent; rebuilds changed files).
+Usage: ``python oracle/build_ref.py [SKWARKA_SOURCE_ROOT]`` (idempotent;
+rebuilds changed files).  The source root defaults to $SKW_REFERENCE_ROOT,
+then to a checkout named ``reference`` beside this repository.
 """
 from __future__ import annotations
 
@@ -48,7 +50,17 @@ SRC = OUT / "src"
 SHIMS = OUT / "shims"
 OBJ = OUT / "obj"
 LIB = OUT / "libskw_ref.so"
-REFERENCE = Path(os.environ.get("SKW_REFERENCE_ROOT", "/root/reference"))
+def reference_root(arg: str | None = None) -> Path:
+    """The Skwarka source tree: the given path, else $SKW_REFERENCE_ROOT,
+    else a checkout named ``reference`` beside this repository."""
+    if arg:
+        return Path(arg)
+    if os.environ.get("SKW_REFERENCE_ROOT"):
+        return Path(os.environ["SKW_REFERENCE_ROOT"])
+    return HERE.parent.parent / "reference"
+
+
+REFERENCE: Path | None = None
 SUBDIRS = ("Common", "Math", "Raytracer", "Shapes")
 EXCLUDE = {"ImageEnvironmentalLight.cpp", "RGBImageSource.cpp", "TranslucentMaterial.cpp", "dllmain.cpp"}
 # -ffp-contract=off: no fused multiply-add, so that an aarch64 build rounds
@@ -73,7 +85,7 @@ def _rewrite(path: Path) -> None:
 
 def stage() -> None:
     """Copy + patch the reference sources (only where the reference exists)."""
-    root = REFERENCE / "Source" / "RayLibs"
+    root = (REFERENCE or reference_root()) / "Source" / "RayLibs"
     if not root.is_dir():
         return
     stamp = SRC / ".staged"
@@ -170,6 +182,8 @@ def build(verbose: bool = False) -> Path | None:
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 1:
+        REFERENCE = reference_root(sys.argv[1])
     p = build(verbose=True)
     if p is None:
         print("reference sources not available; nothing built", file=sys.stderr)

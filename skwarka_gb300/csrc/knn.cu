@@ -30,7 +30,9 @@
 // For k <= 128 the heap and the stack live in local memory, which the L1
 // caches; larger k use a heap in a caller-provided global scratch buffer of
 // k 16-byte entries per query.
+#include <cuda.h>
 #include <cuda_runtime.h>
+
 #include <cstdint>
 #include <mutex>
 
@@ -444,22 +446,47 @@ cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *di
 
 int64_t knn_noalloc_capacity() { return SKW_KNN_NOALLOC_ENTRIES; }
 
+// The calling thread's current CUDA context (the driver's cuCtxGetCurrent,
+// reached through the runtime so that the library needs no link against the
+// driver library); null where the driver does not offer it.
+static void *current_context() {
+  using Fn = CUresult (*)(CUcontext *);
+  static const Fn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return (Fn)p;
+  }();
+  CUcontext c = nullptr;
+  if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+  return (void *)c;
+}
+
 // Device address of the static scratch for the current device, looked up
 // once per device (cudaGetSymbolAddress with that device current; the first
-// lookup may load this module on the device).
+// lookup may load this module on the device) and again whenever the
+// device's current context has changed since (a device reset destroys the
+// context and the module with it; the next context loads the module anew).
 static cudaError_t knn_noalloc_scratch(void **out) {
   static std::mutex mu;
   static void *addr[64] = {nullptr};
+  static void *owner[64] = {nullptr};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  // make the device's primary context current (a no-op when it already is)
+  if ((e = cudaFree(nullptr)) != cudaSuccess) return e;
+  void *ctx = current_context();
   std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
+  if (!addr[dev] || owner[dev] != ctx) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_knn_noalloc_scratch);
     if (e != cudaSuccess) return e;
     addr[dev] = p;
+    owner[dev] = ctx;
   }
   *out = addr[dev];
   return cudaSuccess;

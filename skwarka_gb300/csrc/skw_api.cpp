@@ -296,26 +296,33 @@ static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64
     st[i] = c->host_st[i];
     ev[i] = c->host_ev[i];
   }
+  // One chunk of rays and results per stream: chunks c, c + 2, ... reuse
+  // their stream's buffers in stream order, so device memory stays at two
+  // chunks however many rays the call has.
+  const int64_t chunk_rays = std::min(n, kHostChunk);
   void *d_rays = nullptr, *d_out = nullptr;
   int *d_work = nullptr;  // one ray-group counter per stream (256 bytes apart)
-  if (rc == SKW_OK && ((e = cudaMallocFromPoolAsync(&d_rays, (size_t)n * sizeof(skw_ray), pool, st[0])) != cudaSuccess ||
-                       (e = cudaMallocFromPoolAsync(&d_out, (size_t)n * out_unit, pool, st[0])) != cudaSuccess ||
-                       (e = cudaMallocFromPoolAsync((void **)&d_work, 512, pool, st[0])) != cudaSuccess))
+  if (rc == SKW_OK &&
+      ((e = cudaMallocFromPoolAsync(&d_rays, (size_t)(n_streams * chunk_rays) * sizeof(skw_ray), pool, st[0])) !=
+           cudaSuccess ||
+       (e = cudaMallocFromPoolAsync(&d_out, (size_t)(n_streams * chunk_rays) * out_unit, pool, st[0])) != cudaSuccess ||
+       (e = cudaMallocFromPoolAsync((void **)&d_work, 512, pool, st[0])) != cudaSuccess))
     rc = cuda_fail(a->ctx, e, "cudaMallocAsync");
   // the other streams start after the allocations
   if (rc == SKW_OK && (e = cudaEventRecord(ev[0], st[0])) != cudaSuccess) rc = cuda_fail(a->ctx, e, "event");
   for (int i = 1; i < n_streams && rc == SKW_OK; ++i)
     if ((e = cudaStreamWaitEvent(st[i], ev[0], 0)) != cudaSuccess) rc = cuda_fail(a->ctx, e, "event");
   for (int64_t c = 0; c < n_chunks && rc == SKW_OK; ++c) {
-    cudaStream_t s = st[c % n_streams];
+    const int si = (int)(c % n_streams);
+    cudaStream_t s = st[si];
     const int64_t r0 = c * kHostChunk, m = std::min(kHostChunk, n - r0);
-    const skw_ray *dr = (const skw_ray *)d_rays + r0;
-    char *dout = (char *)d_out + (size_t)r0 * out_unit;
+    const skw_ray *dr = (const skw_ray *)d_rays + si * chunk_rays;
+    char *dout = (char *)d_out + (size_t)(si * chunk_rays) * out_unit;
     if ((e = cudaMemcpyAsync((void *)dr, rays + r0, (size_t)m * sizeof(skw_ray), cudaMemcpyHostToDevice, s)) !=
         cudaSuccess) {
       rc = cuda_fail(a->ctx, e, "copy rays in");
     } else if ((e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, dr, m, nullptr, a->scene_abs,
-                                          nullptr, dout, a->d_status, s, ctas, d_work + 64 * (c % n_streams))) !=
+                                          nullptr, dout, a->d_status, s, ctas, d_work + 64 * si)) !=
                cudaSuccess) {
       rc = cuda_fail(a->ctx, e, "launch");
     } else {

@@ -11,21 +11,30 @@
 //     equal t the last tested triangle wins) and becomes the new tmax.
 //
 // The reference does all of this in double precision over float data.  Here
-// the node tests run in float with the slab interval widened by 8 ulp, so a
-// node is culled only if the reference culls it too.  The triangle test runs
-// in float with a forward error bound on every quantity; only when a decision
+// the node tests run in float: a plane distance is fma(coordinate, 1/d,
+// -o/d -+ w) with the per-ray absolute widening w = 6u (B + |o|) |1/d|
+// (u = 2^-24, B = the scene's largest absolute coordinate; see SlabRay),
+// which bounds the float error for every node, so a node is culled only if
+// the reference culls it too.  The triangle test runs in float with a
+// forward error bound on every quantity; only when a decision
 // (inside/outside an edge, t inside [tmin, tmax], which of two hits is
 // nearer) falls inside that bound is the triangle re-tested with the
-// reference's exact double-precision arithmetic (round-to-nearest intrinsics,
-// no fused multiply-add).  Such hits are flagged SKW_HIT_FP64_DECIDED.
+// reference's exact double-precision arithmetic (round-to-nearest
+// intrinsics, no fused multiply-add).  Such hits are flagged
+// SKW_HIT_FP64_DECIDED.
 //
 // Layout: nodes are 32-byte DevNode records read as two 16-byte loads; each
 // triangle slot is 3 x float4 (v0|prim, v1|tri, v2|slot); rays are 2 x float4.
-// The per-thread stack (16-byte entries) lives in local memory (L1-resident);
-// its capacity CAP is chosen on the host as >= 2 * tree depth + 1, which
-// bounds its use (at most two entries are pushed per level).
+// The traversal stack holds 12-byte entries (node words 6-7 and the widened
+// entry distance): the first SKW_TRAV_SCAP (8) of each thread in shared
+// memory, deeper ones in local memory.  Its capacity CAP is chosen on the
+// host as >= 2 * tree depth + 1, which bounds its use (at most two entries
+// are pushed per level).
 #include <cuda_runtime.h>
+
+#include <atomic>
 #include <cstdint>
+#include <mutex>
 
 #include "kernels.h"
 
@@ -780,17 +789,37 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
   }
 }
 
+// Per-device launch facts, computed once per device on first use and read
+// without a lock afterwards (launches may come from several host threads).
+constexpr int kMaxDevices = 64;
+
+std::mutex &prepare_mutex() {
+  static std::mutex m;
+  return m;
+}
+
+cudaError_t current_device(int &dev) {
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  return dev < 0 || dev >= kMaxDevices ? cudaErrorInvalidDevice : cudaSuccess;
+}
+
+// Resident CTAs per SM of k_trace<CAP, closest> on each device (0 = not yet known).
 template <int CAP>
-int &cap_occupancy(bool closest) {
-  static int blocks_per_sm[2] = {0, 0};
-  return blocks_per_sm[closest ? 1 : 0];
+std::atomic<int> &cap_occupancy(int dev, bool closest) {
+  static std::atomic<int> blocks_per_sm[kMaxDevices][2];
+  return blocks_per_sm[dev][closest ? 1 : 0];
 }
 
 template <int CAP>
-cudaError_t cap_prepare() {
+cudaError_t cap_prepare(int dev) {
+  if (cap_occupancy<CAP>(dev, true).load(std::memory_order_acquire) != 0 &&
+      cap_occupancy<CAP>(dev, false).load(std::memory_order_acquire) != 0)
+    return cudaSuccess;
+  std::lock_guard<std::mutex> lock(prepare_mutex());
   for (int which = 0; which < 2; ++which) {
-    int &occ = cap_occupancy<CAP>(which == 1);
-    if (occ != 0) continue;
+    std::atomic<int> &slot = cap_occupancy<CAP>(dev, which == 1);
+    if (slot.load(std::memory_order_relaxed) != 0) continue;
     cudaError_t e;
     if (SKW_TRAV_CARVEOUT >= 0) {
       e = which ? cudaFuncSetAttribute(k_trace<CAP, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -799,34 +828,38 @@ cudaError_t cap_prepare() {
                                        SKW_TRAV_CARVEOUT);
       if (e != cudaSuccess) return e;
     }
+    int occ = 0;
     e = which ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<CAP, true>, SKW_TRAV_BLOCK, 0)
               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<CAP, false>, SKW_TRAV_BLOCK, 0);
     if (e != cudaSuccess) return e;
-    if (occ < 1) occ = 1;
+    slot.store(occ < 1 ? 1 : occ, std::memory_order_release);
   }
   return cudaSuccess;
 }
 
-int device_sms() {
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  }
-  return sms;
+// SM count of each device (0 = not yet known).
+cudaError_t device_sms(int dev, int &sms) {
+  static std::atomic<int> cache[kMaxDevices];
+  sms = cache[dev].load(std::memory_order_acquire);
+  if (sms != 0) return cudaSuccess;
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  cache[dev].store(sms, std::memory_order_release);
+  return cudaSuccess;
 }
 
 template <int CAP>
 cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const void *rays, int64_t n,
                        const int *n_dev, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
                        cudaStream_t stream, int ctas_per_sm, int *work) {
-  cudaError_t e = cap_prepare<CAP>();
-  if (e != cudaSuccess) return e;
-  int per_sm = cap_occupancy<CAP>(closest);
+  int dev = 0, sms = 0;
+  cudaError_t e = current_device(dev);
+  if (e != cudaSuccess || (e = cap_prepare<CAP>(dev)) != cudaSuccess || (e = device_sms(dev, sms)) != cudaSuccess)
+    return e;
+  int per_sm = cap_occupancy<CAP>(dev, closest).load(std::memory_order_acquire);
   if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
   const int64_t warps_per_block = SKW_TRAV_BLOCK / 32;
-  int64_t blocks = (int64_t)per_sm * device_sms();
+  int64_t blocks = (int64_t)per_sm * sms;
   const int64_t needed = (n + 32 * warps_per_block - 1) / (32 * warps_per_block);
   if (blocks > needed) blocks = needed;
   // every warp draws at most one group past the end: keep the counter in int range
@@ -847,22 +880,25 @@ cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const 
 }  // namespace
 
 cudaError_t prepare_traversal(int stack_cap) {
-  device_sms();
+  int dev = 0, sms = 0;
+  cudaError_t e = current_device(dev);
+  if (e != cudaSuccess || (e = device_sms(dev, sms)) != cudaSuccess) return e;
   switch (stack_cap) {
-    case 48: return cap_prepare<48>();
-    case 96: return cap_prepare<96>();
-    case 192: return cap_prepare<192>();
-    default: return cap_prepare<416>();
+    case 48: return cap_prepare<48>(dev);
+    case 96: return cap_prepare<96>(dev);
+    case 192: return cap_prepare<192>(dev);
+    default: return cap_prepare<416>(dev);
   }
 }
 
 int traversal_max_ctas_per_sm(int stack_cap) {
-  if (prepare_traversal(stack_cap) != cudaSuccess) return 1;
+  int dev = 0;
+  if (current_device(dev) != cudaSuccess || prepare_traversal(stack_cap) != cudaSuccess) return 1;
   switch (stack_cap) {
-    case 48: return cap_occupancy<48>(true);
-    case 96: return cap_occupancy<96>(true);
-    case 192: return cap_occupancy<192>(true);
-    default: return cap_occupancy<416>(true);
+    case 48: return cap_occupancy<48>(dev, true).load();
+    case 96: return cap_occupancy<96>(dev, true).load();
+    case 192: return cap_occupancy<192>(dev, true).load();
+    default: return cap_occupancy<416>(dev, true).load();
   }
 }
 

@@ -96,11 +96,12 @@ def test_query_scene_against_oracle(gpu, oracle):
     assert frac >= MIN_AGREE
 
 
-@pytest.mark.parametrize("n", [50_000, 4_500_001])
+@pytest.mark.parametrize("n", [50_000, 4_500_001, 9_437_185])
 def test_host_api_equals_device_api(gpu, n):
     """The host-buffer entry points (copies in, query, copies out; above
-    2^21 rays in chunks over two streams) equal the device ones bit for
-    bit, including a ragged last chunk."""
+    2^21 rays in chunks over two streams that reuse one chunk buffer each)
+    equal the device ones bit for bit, including a ragged last chunk and
+    more than four chunks."""
     meshes = sf.small_query_scene()
     lo, hi = scenes.scene_bounds(meshes)
     rays = scenes.uniform_rays(n, lo, hi, seed=53)

@@ -5,10 +5,12 @@ skw_knn_noalloc serves callers that cannot allocate device memory while
 they query -- a renderer running inside a device-memory budget reserved up
 front, or a host callback that must not block on cudaMalloc / cudaFree -- by
 keeping its heaps in a static device array.  The test calls both entry
-points through the C ABI on the same tree and queries, twice in a row with
-different sizes (the second call must not be disturbed by what the first
-left in the shared array), and compares counts, indices and squared
-distances exactly (the tolerance of every k-NN test here: bit-exact).  It
+points through the C ABI on the same tree and queries, several times in a
+row with different sizes (a call must not be disturbed by what the previous
+one left in the shared array), for k in {0, 1, 32, 100, 150, 200} (each of
+skw_knn's kernels), and compares counts, indices and squared distances
+exactly (the tolerance of every k-NN test here: bit-exact); the k = 100 call
+is also compared with the oracle.  It
 also checks that a batch larger than the array is refused with an error.
 This file is named to run last.
 """
@@ -38,8 +40,8 @@ def test_knn_noalloc_matches_knn_twice(gpu):
 
     def run(entry, q, qn, k, r, cos_t):
         nq = q.shape[0]
-        idx = torch.full((nq, k), -7, dtype=torch.int32, device="cuda")
-        d2 = torch.full((nq, k), -7.0, dtype=torch.float64, device="cuda")
+        idx = torch.full((nq, max(k, 1)), -7, dtype=torch.int32, device="cuda")[:, :k]
+        d2 = torch.full((nq, max(k, 1)), -7.0, dtype=torch.float64, device="cuda")[:, :k]
         cnt = torch.full((nq,), -7, dtype=torch.int32, device="cuda")
         rc = entry(tree.handle, q.data_ptr(), qn.data_ptr(), nq, k, r, cos_t, idx.data_ptr(), d2.data_ptr(),
                    cnt.data_ptr(), s)
@@ -47,15 +49,30 @@ def test_knn_noalloc_matches_knn_twice(gpu):
         torch.cuda.synchronize()
         return idx.cpu().numpy(), d2.cpu().numpy(), cnt.cpu().numpy()
 
-    for call, (nq, k, r, cos_t) in enumerate([(4000, 200, 0.08, 0.5), (2500, 150, 0.05, -1.0)]):
-        q = torch.from_numpy(rng.uniform(0, 1, size=(nq, 3))).cuda()
+    # skw_knn serves k <= 32 and k <= 128 with per-thread heaps and skips the
+    # heap for k = 0; the allocation-free entry point always uses the scratch
+    # heaps, so every branch of skw_knn is compared, plus the oracle once.
+    cases = [(4000, 200, 0.08, 0.5), (2500, 150, 0.05, -1.0), (3000, 1, 0.1, 0.5), (3000, 32, 0.05, 0.87),
+             (3000, 100, 0.06, 0.5), (3000, 0, 0.05, 0.5)]
+    for call, (nq, k, r, cos_t) in enumerate(cases):
+        q_np = rng.uniform(0, 1, size=(nq, 3))
         qn_np = rng.normal(size=(nq, 3))
-        qn = torch.from_numpy(qn_np / np.linalg.norm(qn_np, axis=1, keepdims=True)).cuda()
+        qn_np /= np.linalg.norm(qn_np, axis=1, keepdims=True)
+        q, qn = torch.from_numpy(q_np).cuda(), torch.from_numpy(qn_np).cuda()
         a = run(lib.skw_knn, q, qn, k, r, cos_t)
         b = run(lib.skw_knn_noalloc, q, qn, k, r, cos_t)
         for x, y in zip(a, b):
-            assert np.array_equal(x, y), f"call {call}: no-allocation results differ"
-        assert a[2].max() > 0
+            assert np.array_equal(x, y), f"call {call} (k={k}): no-allocation results differ"
+        if k > 0:
+            assert a[2].max() > 0
+        else:
+            assert (b[2] == 0).all()
+        if k == 100:
+            from oracle.api import Oracle
+            want = Oracle().kdtree(pos, compress_directions(nrm)).knn(q_np, qn_np, k, r, cos_t)
+            assert np.array_equal(b[2], want["count"])
+            assert np.array_equal(b[0], want["idx"])
+            assert np.array_equal(b[1].view(np.uint64), want["d2"].view(np.uint64))
 
     # A batch beyond the static array is refused, not truncated.
     nq, k = 10_000, 200
