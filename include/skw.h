@@ -165,6 +165,37 @@ int skw_intersect_test(skw_accel *accel, const skw_ray *rays, int64_t n, uint8_t
 int skw_intersect_host(skw_accel *accel, const skw_ray *rays, int64_t n, skw_hit *hits);
 int skw_intersect_test_host(skw_accel *accel, const skw_ray *rays, int64_t n, uint8_t *occluded);
 
+/* A ray in double precision, the reference's Ray (Math/Ray.h:57-59): origin,
+ * direction (normalised), [tmin, tmax].  64 bytes. */
+typedef struct skw_ray_d {
+  double ox, oy, oz;
+  double dx, dy, dz;
+  double tmin, tmax;
+} skw_ray_d;
+
+/* Closest hit of a double ray: t is the reference's exact double t (the
+ * o_t of TriangleAccelerator::Intersect); t = +inf and prim = tri = -1 on a
+ * miss.  16 bytes. */
+typedef struct skw_hit_d {
+  double t;
+  int32_t prim;
+  int32_t tri;
+} skw_hit_d;
+
+/* Closest / any hit of double rays, device buffers: Scene::Intersect /
+ * IntersectTest on the reference's own ray type (TriangleAccelerator.cpp:
+ * 154-352, 354-468).  Nodes are culled in float with bounds that cover the
+ * rounding of the ray to float, so a node is skipped only if the reference
+ * skips it; every triangle of a reached leaf is tested with the reference's
+ * double Moller-Trumbore on the double ray, so the hit ids and t are the
+ * reference's, bit for bit.  Slower than the float entry points (every
+ * triangle test runs in double). */
+int skw_intersect_d(skw_accel *accel, const skw_ray_d *rays, int64_t n, skw_hit_d *hits, void *stream);
+int skw_intersect_test_d(skw_accel *accel, const skw_ray_d *rays, int64_t n, uint8_t *occluded, void *stream);
+/* The same with host buffers; waits for completion. */
+int skw_intersect_d_host(skw_accel *accel, const skw_ray_d *rays, int64_t n, skw_hit_d *hits);
+int skw_intersect_test_d_host(skw_accel *accel, const skw_ray_d *rays, int64_t n, uint8_t *occluded);
+
 /* Kernel launches made by this library since the context was created. */
 int64_t skw_launch_count(const skw_ctx *ctx);
 
@@ -378,6 +409,63 @@ typedef struct skw_hit_geometry {
 } skw_hit_geometry;
 int skw_scene_hit_geometry(skw_scene *scene, const skw_ray *rays, const skw_hit *hits, int64_t n,
                            skw_hit_geometry *out, void *stream);
+
+/* A RayDifferential (Math/Ray.h:68-111): the base ray in double plus,
+ * when has_differentials is nonzero, the rays of the next pixel in x and y.
+ * 168 bytes. */
+typedef struct skw_ray_differential {
+  skw_ray_d ray;
+  double origin_dx[3], direction_dx[3];
+  double origin_dy[3], direction_dy[3];
+  int32_t has_differentials;
+  int32_t reserved;
+} skw_ray_differential;
+
+/* The Intersection that TriangleAccelerator::Intersect fills
+ * (Raytracer/Core/Intersection.h:26-54, DifferentialGeometry.h:25-90):
+ * the DifferentialGeometry's point, normals, uv, the next-pixel points and
+ * normals, uv derivatives and tangent, the m_cross / m_dot that
+ * CoreUtils::GetNextMinT reads, the hit's t, primitive and mesh triangle.
+ * 288 bytes. */
+typedef struct skw_intersection {
+  double point[3];
+  double geometric_normal[3];
+  double shading_normal[3];
+  double uv[2];
+  double point_dx[3], point_dy[3];
+  double normal_dx[3], normal_dy[3];
+  double duv_dx[2], duv_dy[2];
+  double tangent[3];
+  double cross[3];  /* m_cross */
+  double dot;       /* m_dot */
+  double t;
+  int32_t prim, tri;
+} skw_intersection;
+
+/* Completes closest hits into Intersections: TriangleMesh::
+ * ComputeDifferentialGeometry (Raytracer/Core/TriangleMesh.cpp:414-561) and
+ * the rest of TriangleAccelerator::Intersect (TriangleAccelerator.cpp:
+ * 303-347) on the GPU, in double with the reference's operation order.
+ * rays / hits: as given to and returned by skw_intersect_d on the scene's
+ * accelerator (skw_scene_accel).  Bit-identical to the reference for
+ * primitives without a mesh-to-world matrix; a transformed primitive is
+ * evaluated on its world-space triangle (the same quantities, rounded
+ * differently).  The meshes carry no uv coordinates (the reference's
+ * default of zero) and no tangents.  NaN fields and prim = tri = -1 for a
+ * miss.  Device buffers. */
+int skw_scene_intersection(skw_scene *scene, const skw_ray_differential *rays, const skw_hit_d *hits, int64_t n,
+                           skw_intersection *out, void *stream);
+/* CoreUtils::GetNextMinT (Raytracer/Core/CoreUtils.h:139-149) of an
+ * Intersection for a normalised world direction of a primitive without a
+ * mesh-to-world matrix: max(0, dot / (direction . cross) + 1e-14).  Host. */
+double skw_next_min_t(const skw_intersection *isect, const double *direction);
+/* The outgoing rays the renders make at closest hits (float rays and
+ * skw_hit from skw_intersect on the scene's accelerator): origin = the float
+ * hit point o + d t, direction = directions[3 i ..] (normalised), tmin =
+ * GetNextMinT evaluated in double for that origin and rounded up to float,
+ * tmax = +inf; NaN rays for misses.  Device buffers. */
+int skw_scene_next_rays(skw_scene *scene, const skw_ray *rays, const skw_hit *hits, const float *directions,
+                        int64_t n, skw_ray *out, void *stream);
 
 /* DirectLightingLTEIntegratorParams::m_max_specular_depth
  * (LTEIntegrators/DirectLightingLTEIntegrator.cpp:48-54): camera rays have

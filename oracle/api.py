@@ -40,6 +40,8 @@ _ORACLE_SIGS = [
     ("oracle_accel_export", None, [_P, _P, _P, _P, _P]),
     ("oracle_intersect", None, [_P, _P, _i64, _P, _P, _P, _P, _P, C.c_int]),
     ("oracle_intersect_test", None, [_P, _P, _i64, _P, _P, _P, C.c_int]),
+    ("oracle_intersect_d", None, [_P, _P, _i64, _P, _P, _P, C.c_int]),
+    ("oracle_intersect_test_d", None, [_P, _P, _i64, _P, C.c_int]),
     ("oracle_brute_force", None, [_P, _P, _P, _i64, _P, _i64, _P, _P, _P, C.c_int]),
     ("oracle_kdtree_create", _P, [_P, _P, _i64, _P, _P]),
     ("oracle_kdtree_destroy", None, [_P]),
@@ -53,6 +55,10 @@ _REF_SIGS = [
     ("skw_ref_accel_destroy", None, [_P]),
     ("skw_ref_intersect", None, [_P, _P, _i64, _P, _P, _P, C.c_int]),
     ("skw_ref_intersect_test", None, [_P, _P, _i64, _P, C.c_int]),
+    ("skw_ref_accel_create_normals", _P, [C.c_int, _P, C.c_int, _P, _P, _P, _P, _P, _P]),
+    ("skw_ref_intersect_d", None, [_P, _P, _i64, _P, _P, _P, C.c_int]),
+    ("skw_ref_intersect_test_d", None, [_P, _P, _i64, _P, C.c_int]),
+    ("skw_ref_intersection", None, [_P, _P, _P, _i64, _P, _P, _P, C.c_int]),
     ("skw_ref_accel_num_nodes", _i64, [_P]),
     ("skw_ref_accel_num_triangles", _i64, [_P]),
     ("skw_ref_accel_export", None, [_P, _P, _P, _P, _P, _P]),
@@ -158,6 +164,20 @@ class OracleAccel:
             out.update(nodes=nv, tris=nt)
         return out
 
+    def intersect_d(self, rays, threads=0):
+        """Closest hits of double rays ((n, 8) float64)."""
+        rays = np.ascontiguousarray(rays, np.float64)
+        n = rays.shape[0]
+        p, t, th = np.empty(n, np.int32), np.empty(n, np.int32), np.empty(n, np.float64)
+        self.lib.oracle_intersect_d(self.h, _ptr(rays), n, _ptr(p), _ptr(t), _ptr(th), threads)
+        return {"prim": p, "tri": t, "t": th}
+
+    def intersect_test_d(self, rays, threads=0):
+        rays = np.ascontiguousarray(rays, np.float64)
+        occ = np.empty(rays.shape[0], np.uint8)
+        self.lib.oracle_intersect_test_d(self.h, _ptr(rays), rays.shape[0], _ptr(occ), threads)
+        return occ
+
     def intersect_test(self, rays, counters=False, threads=0):
         rays = np.ascontiguousarray(rays, np.float32)
         n = rays.shape[0]
@@ -218,8 +238,8 @@ class Reference:
     def available() -> bool:
         return REF_LIB.exists()
 
-    def accel(self, meshes):
-        return RefAccel(self.lib, meshes)
+    def accel(self, meshes, normals=None, mesh_of=None, xforms=None):
+        return RefAccel(self.lib, meshes, normals, mesh_of, xforms)
 
     def kdtree(self, pos, normal_ids=None, dir_ids=None):
         return RefKD(self.lib, pos, normal_ids, dir_ids)
@@ -370,7 +390,11 @@ class Reference:
 
 
 class RefAccel:
-    def __init__(self, lib, meshes):
+    def __init__(self, lib, meshes, normals=None, mesh_of=None, xforms=None):
+        """meshes: [(vertices, triangles)]; normals: optional per-mesh vertex
+        normals (or None entries); mesh_of: the mesh of each primitive
+        (default one primitive per mesh); xforms: optional (n_prims, 4, 4)
+        mesh-to-world matrices."""
         self.lib = lib
         self._v = [np.ascontiguousarray(v, np.float32) for v, _ in meshes]
         self._t = [np.ascontiguousarray(t, np.int32) for _, t in meshes]
@@ -379,9 +403,44 @@ class RefAccel:
         tp = (C.c_void_p * nm)(*[t.ctypes.data for t in self._t])
         nv = np.array([v.shape[0] for v in self._v], np.int64)
         nt = np.array([t.shape[0] for t in self._t], np.int64)
-        mesh_of = np.arange(nm, dtype=np.int32)
-        self.h = lib.skw_ref_accel_create(nm, _ptr(mesh_of), nm, vp, _ptr(nv), tp, _ptr(nt), None)
+        self._mesh_of = np.arange(nm, dtype=np.int32) if mesh_of is None else np.ascontiguousarray(mesh_of, np.int32)
+        npr = len(self._mesh_of)
+        self._x = None if xforms is None else np.ascontiguousarray(xforms, np.float64).reshape(npr, 16)
+        if normals is None:
+            self.h = lib.skw_ref_accel_create(npr, _ptr(self._mesh_of), nm, vp, _ptr(nv), tp, _ptr(nt),
+                                              _ptr(self._x))
+        else:
+            self._n = [None if n is None else np.ascontiguousarray(n, np.float32) for n in normals]
+            np_ = (C.c_void_p * nm)(*[None if n is None else n.ctypes.data for n in self._n])
+            self.h = lib.skw_ref_accel_create_normals(npr, _ptr(self._mesh_of), nm, vp, _ptr(nv), tp, _ptr(nt), np_,
+                                                      _ptr(self._x))
         self.n_tris = lib.skw_ref_accel_num_triangles(self.h)
+
+    def intersect_d(self, rays, threads=0):
+        """TriangleAccelerator::Intersect of double rays ((n, 8) float64)."""
+        rays = np.ascontiguousarray(rays, np.float64)
+        n = rays.shape[0]
+        p, t, th = np.empty(n, np.int32), np.empty(n, np.int32), np.empty(n, np.float64)
+        self.lib.skw_ref_intersect_d(self.h, _ptr(rays), n, _ptr(p), _ptr(t), _ptr(th), threads)
+        return {"prim": p, "tri": t, "t": th}
+
+    def intersect_test_d(self, rays, threads=0):
+        rays = np.ascontiguousarray(rays, np.float64)
+        occ = np.empty(rays.shape[0], np.uint8)
+        self.lib.skw_ref_intersect_test_d(self.h, _ptr(rays), rays.shape[0], _ptr(occ), threads)
+        return occ
+
+    def intersection(self, rays, diffs=None, next_dirs=None, threads=0):
+        """The whole Intersection of each double ray ((n, 40) float64, see
+        skw_ref_intersection) and, with next_dirs, GetNextMinT per hit."""
+        rays = np.ascontiguousarray(rays, np.float64)
+        n = rays.shape[0]
+        d = None if diffs is None else np.ascontiguousarray(diffs, np.float64)
+        nd = None if next_dirs is None else np.ascontiguousarray(next_dirs, np.float64)
+        out = np.empty((n, 40), np.float64)
+        nt = np.empty(n, np.float64) if nd is not None else None
+        self.lib.skw_ref_intersection(self.h, _ptr(rays), _ptr(d), n, _ptr(out), _ptr(nd), _ptr(nt), threads)
+        return (out, nt) if nd is not None else out
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -61,6 +61,7 @@
 #include <Raytracer/BxDFs/MERLMeasured.h>
 #include <Raytracer/Materials/MERLMeasuredMaterial.h>
 #include <Raytracer/Core/Color.h>
+#include <Raytracer/Core/CoreUtils.h>
 #undef private
 #undef protected
 #include <chrono>
@@ -132,6 +133,138 @@ void *skw_ref_accel_create(int n_prims, const int32_t *mesh_of_prim, int n_meshe
 }
 
 void skw_ref_accel_destroy(void *a) { delete (RefAccel *)a; }
+
+// skw_ref_accel_create with optional per-mesh shading normals (float xyz per
+// vertex; null = none): a mesh with normals uses them for shading
+// (TriangleMesh(vertices, triangles, normals, tangents, true, false)), one
+// without has use_shading_normals = false, as the render scenes build them.
+void *skw_ref_accel_create_normals(int n_prims, const int32_t *mesh_of_prim, int n_meshes, const float *const *verts,
+                                   const int64_t *n_verts, const int32_t *const *tris, const int64_t *n_tris,
+                                   const float *const *normals, const double *xforms) {
+  auto *ra = new RefAccel();
+  std::vector<intrusive_ptr<const TriangleMesh>> meshes;
+  for (int m = 0; m < n_meshes; ++m) {
+    std::vector<Point3D_f> v((size_t)n_verts[m]);
+    for (int64_t i = 0; i < n_verts[m]; ++i)
+      v[(size_t)i] = Point3D_f(verts[m][3 * i], verts[m][3 * i + 1], verts[m][3 * i + 2]);
+    std::vector<MeshTriangle> t((size_t)n_tris[m]);
+    for (int64_t i = 0; i < n_tris[m]; ++i)
+      t[(size_t)i] = MeshTriangle(tris[m][3 * i], tris[m][3 * i + 1], tris[m][3 * i + 2]);
+    if (normals && normals[m]) {
+      std::vector<Vector3D_f> nv((size_t)n_verts[m]);
+      for (int64_t i = 0; i < n_verts[m]; ++i)
+        nv[(size_t)i] = Vector3D_f(normals[m][3 * i], normals[m][3 * i + 1], normals[m][3 * i + 2]);
+      meshes.push_back(intrusive_ptr<const TriangleMesh>(
+          new TriangleMesh(v, t, nv, std::vector<Vector3D_f>(), true, false)));
+    } else {
+      meshes.push_back(intrusive_ptr<const TriangleMesh>(new TriangleMesh(v, t, false, false)));
+    }
+  }
+  for (int p = 0; p < n_prims; ++p) {
+    Transform tr = make_transform(xforms ? xforms + 16 * p : nullptr);
+    ra->prims.push_back(intrusive_ptr<const Primitive>(
+        new Primitive(meshes[(size_t)mesh_of_prim[p]], tr, intrusive_ptr<const Material>(), NULL, NULL)));
+  }
+  ra->accel.reset(new TriangleAccelerator(ra->prims));
+  return ra;
+}
+
+// Double rays (8 doubles: ox oy oz dx dy dz tmin tmax) through
+// TriangleAccelerator::Intersect: (primitive, mesh triangle, t); -1, -1,
+// +inf on a miss.
+void skw_ref_intersect_d(void *a, const double *rays, int64_t n, int32_t *prim, int32_t *tri, double *t,
+                         int threads) {
+  const RefAccel *ra = (const RefAccel *)a;
+  parallel_ranges(n, threads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      const double *r = rays + 8 * i;
+      Ray ray(Point3D_d(r[0], r[1], r[2]), Vector3D_d(r[3], r[4], r[5]), r[6], r[7]);
+      Intersection isect;
+      double th;
+      if (ra->accel->Intersect(RayDifferential(ray), isect, &th)) {
+        size_t pi = 0;
+        for (; pi < ra->prims.size(); ++pi)
+          if (ra->prims[pi].get() == isect.mp_primitive) break;
+        prim[i] = (int32_t)pi;
+        tri[i] = (int32_t)isect.m_triangle_index;
+        t[i] = th;
+      } else {
+        prim[i] = -1;
+        tri[i] = -1;
+        t[i] = std::numeric_limits<double>::infinity();
+      }
+    }
+  });
+}
+
+void skw_ref_intersect_test_d(void *a, const double *rays, int64_t n, uint8_t *occluded, int threads) {
+  const RefAccel *ra = (const RefAccel *)a;
+  parallel_ranges(n, threads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      const double *r = rays + 8 * i;
+      occluded[i] = ra->accel->IntersectTest(Ray(Point3D_d(r[0], r[1], r[2]), Vector3D_d(r[3], r[4], r[5]), r[6], r[7]))
+                        ? 1
+                        : 0;
+    }
+  });
+}
+
+// The whole Intersection of TriangleAccelerator::Intersect for ray
+// differentials: rays 8 doubles as above; diffs (may be null = no
+// differentials) 12 doubles per ray: origin_dx, direction_dx, origin_dy,
+// direction_dy.  out: 40 doubles per ray -- point, geometric normal, shading
+// normal (3 each), uv (2), point_dx, point_dy, normal_dx, normal_dy (3 each),
+// duv_dx, duv_dy (2 each), tangent (3), m_cross (3), m_dot, t, primitive,
+// mesh triangle (as doubles), 3 unused; NaN and primitive -1 on a miss.
+// Also GetNextMinT (CoreUtils.h:139-149) of each hit for the direction
+// next_dirs[3 i ...] (may be null) into next_tmin[i].
+void skw_ref_intersection(void *a, const double *rays, const double *diffs, int64_t n, double *out,
+                          const double *next_dirs, double *next_tmin, int threads) {
+  const RefAccel *ra = (const RefAccel *)a;
+  parallel_ranges(n, threads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      const double *r = rays + 8 * i;
+      RayDifferential rd(Ray(Point3D_d(r[0], r[1], r[2]), Vector3D_d(r[3], r[4], r[5]), r[6], r[7]));
+      if (diffs) {
+        const double *d = diffs + 12 * i;
+        rd.m_has_differentials = true;
+        rd.m_origin_dx = Point3D_d(d[0], d[1], d[2]);
+        rd.m_direction_dx = Vector3D_d(d[3], d[4], d[5]);
+        rd.m_origin_dy = Point3D_d(d[6], d[7], d[8]);
+        rd.m_direction_dy = Vector3D_d(d[9], d[10], d[11]);
+      }
+      double *o = out + 40 * i;
+      Intersection is;
+      double th;
+      if (!ra->accel->Intersect(rd, is, &th)) {
+        for (int k = 0; k < 40; ++k) o[k] = std::numeric_limits<double>::quiet_NaN();
+        o[35] = o[36] = -1.0;
+        if (next_tmin) next_tmin[i] = std::numeric_limits<double>::quiet_NaN();
+        continue;
+      }
+      const DifferentialGeometry &g = is.m_dg;
+      const double v[35] = {g.m_point[0], g.m_point[1], g.m_point[2], g.m_geometric_normal[0],
+                            g.m_geometric_normal[1], g.m_geometric_normal[2], g.m_shading_normal[0],
+                            g.m_shading_normal[1], g.m_shading_normal[2], g.m_uv[0], g.m_uv[1], g.m_point_dx[0],
+                            g.m_point_dx[1], g.m_point_dx[2], g.m_point_dy[0], g.m_point_dy[1], g.m_point_dy[2],
+                            g.m_normal_dx[0], g.m_normal_dx[1], g.m_normal_dx[2], g.m_normal_dy[0], g.m_normal_dy[1],
+                            g.m_normal_dy[2], g.m_duv_dx[0], g.m_duv_dx[1], g.m_duv_dy[0], g.m_duv_dy[1],
+                            g.m_tangent[0], g.m_tangent[1], g.m_tangent[2], is.m_cross[0], is.m_cross[1],
+                            is.m_cross[2], is.m_dot, th};
+      for (int k = 0; k < 35; ++k) o[k] = v[k];
+      size_t pi = 0;
+      for (; pi < ra->prims.size(); ++pi)
+        if (ra->prims[pi].get() == is.mp_primitive) break;
+      o[35] = (double)pi;
+      o[36] = (double)is.m_triangle_index;
+      o[37] = o[38] = o[39] = 0.0;
+      if (next_dirs && next_tmin) {
+        const double *nd = next_dirs + 3 * i;
+        next_tmin[i] = CoreUtils::GetNextMinT(is, Vector3D_d(nd[0], nd[1], nd[2]));
+      }
+    }
+  });
+}
 
 // rays: 8 floats per ray (ox oy oz dx dy dz tmin tmax), widened exactly to
 // double.  Outputs the reference's (primitive index, mesh triangle index, t);

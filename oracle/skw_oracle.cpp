@@ -207,6 +207,17 @@ RayD ray_from(const float *r) {
   return ray;
 }
 
+RayD ray_from_d(const double *r) {
+  RayD ray;
+  for (int k = 0; k < 3; ++k) {
+    ray.o[k] = r[k];
+    ray.d[k] = r[3 + k];
+  }
+  ray.tmin = r[6];
+  ray.tmax = r[7];
+  return ray;
+}
+
 // Slab test of _NodeIntersect (TriangleAccelerator.cpp:176-192); true = culled.
 bool culled(const BoxF &b, const RayD &ray, const double inv[3], double tmin, double tmax) {
   double tn[3], tf[3];
@@ -458,13 +469,14 @@ void oracle_accel_export(void *ap, float *node_bbox, int32_t *node_info, int32_t
 
 // Closest hit: _NodeIntersect (TriangleAccelerator.cpp:154-293).
 // counters (optional): per ray nodes popped, triangles tested.
-void oracle_intersect(void *ap, const float *rays, int64_t n, int32_t *prim, int32_t *tri, double *t_out,
-                      int32_t *nodes_visited, int32_t *tris_tested, int threads) {
+// rays_d (if rays is null): 8 doubles per ray, the reference's own Ray.
+static void intersect_impl(void *ap, const float *rays, const double *rays_d, int64_t n, int32_t *prim, int32_t *tri,
+                           double *t_out, int32_t *nodes_visited, int32_t *tris_tested, int threads) {
   const Accel &a = *(Accel *)ap;
   for_ranges(n, threads, [&](int64_t b, int64_t e) {
     std::vector<int> todo(401);
     for (int64_t i = b; i < e; ++i) {
-      RayD ray = ray_from(rays + 8 * i);
+      RayD ray = rays ? ray_from(rays + 8 * i) : ray_from_d(rays_d + 8 * i);
       double inv[3] = {1.0 / ray.d[0], 1.0 / ray.d[1], 1.0 / ray.d[2]};
       int sp = 0, nv = 0, nt = 0;
       if (a.root >= 0) todo[(size_t)sp++] = a.root;
@@ -502,14 +514,24 @@ void oracle_intersect(void *ap, const float *rays, int64_t n, int32_t *prim, int
   });
 }
 
+void oracle_intersect(void *ap, const float *rays, int64_t n, int32_t *prim, int32_t *tri, double *t_out,
+                      int32_t *nodes_visited, int32_t *tris_tested, int threads) {
+  intersect_impl(ap, rays, nullptr, n, prim, tri, t_out, nodes_visited, tris_tested, threads);
+}
+
+void oracle_intersect_d(void *ap, const double *rays, int64_t n, int32_t *prim, int32_t *tri, double *t_out,
+                        int threads) {
+  intersect_impl(ap, nullptr, rays, n, prim, tri, t_out, nullptr, nullptr, threads);
+}
+
 // Any hit: _NodeIntersectTest (TriangleAccelerator.cpp:354-462).
-void oracle_intersect_test(void *ap, const float *rays, int64_t n, uint8_t *occluded, int32_t *nodes_visited,
-                           int32_t *tris_tested, int threads) {
+static void intersect_test_impl(void *ap, const float *rays, const double *rays_d, int64_t n, uint8_t *occluded,
+                                int32_t *nodes_visited, int32_t *tris_tested, int threads) {
   const Accel &a = *(Accel *)ap;
   for_ranges(n, threads, [&](int64_t b, int64_t e) {
     std::vector<int> todo(401);
     for (int64_t i = b; i < e; ++i) {
-      RayD ray = ray_from(rays + 8 * i);
+      RayD ray = rays ? ray_from(rays + 8 * i) : ray_from_d(rays_d + 8 * i);
       double inv[3] = {1.0 / ray.d[0], 1.0 / ray.d[1], 1.0 / ray.d[2]};
       int sp = 0, nv = 0, nt = 0;
       if (a.root >= 0) todo[(size_t)sp++] = a.root;
@@ -540,6 +562,15 @@ void oracle_intersect_test(void *ap, const float *rays, int64_t n, uint8_t *occl
       if (tris_tested) tris_tested[i] = nt;
     }
   });
+}
+
+void oracle_intersect_test(void *ap, const float *rays, int64_t n, uint8_t *occluded, int32_t *nodes_visited,
+                           int32_t *tris_tested, int threads) {
+  intersect_test_impl(ap, rays, nullptr, n, occluded, nodes_visited, tris_tested, threads);
+}
+
+void oracle_intersect_test_d(void *ap, const double *rays, int64_t n, uint8_t *occluded, int threads) {
+  intersect_test_impl(ap, nullptr, rays, n, occluded, nullptr, nullptr, threads);
 }
 
 // Brute force over all triangles in input order, the unit test's check

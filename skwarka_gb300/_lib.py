@@ -63,6 +63,10 @@ SIGNATURES = [
     ("skw_intersect_test", C.c_int, [_P, _P, C.c_int64, _P, _P]),
     ("skw_intersect_host", C.c_int, [_P, _P, C.c_int64, _P]),
     ("skw_intersect_test_host", C.c_int, [_P, _P, C.c_int64, _P]),
+    ("skw_intersect_d", C.c_int, [_P, _P, C.c_int64, _P, _P]),
+    ("skw_intersect_test_d", C.c_int, [_P, _P, C.c_int64, _P, _P]),
+    ("skw_intersect_d_host", C.c_int, [_P, _P, C.c_int64, _P]),
+    ("skw_intersect_test_d_host", C.c_int, [_P, _P, C.c_int64, _P]),
     ("skw_compress_direction", C.c_uint16, [C.c_double, C.c_double, C.c_double]),
     ("skw_direction_table", C.c_int, [_P]),
     ("skw_kdtree_build_host", C.c_int, [_P, C.c_int64, C.c_int, _P, _P]),
@@ -93,6 +97,9 @@ SIGNATURES = [
     ("skw_scene_set_medium", C.c_int, [_P, C.c_void_p]),
     ("skw_scene_set_max_specular_depth", C.c_int, [_P, C.c_int32]),
     ("skw_scene_hit_geometry", C.c_int, [_P, _P, _P, C.c_int64, _P, _P]),
+    ("skw_scene_intersection", C.c_int, [_P, _P, _P, C.c_int64, _P, _P]),
+    ("skw_next_min_t", C.c_double, [_P, _P]),
+    ("skw_scene_next_rays", C.c_int, [_P, _P, _P, _P, C.c_int64, _P, _P]),
     ("skw_render_photon", C.c_int, [_P, _P, C.c_void_p, C.c_void_p, C.c_void_p, _P, _P]),
     ("skw_scene_n_triangles", C.c_int64, [_P]),
     ("skw_scene_set_triangle_albedo", C.c_int, [_P, _P, _P]),

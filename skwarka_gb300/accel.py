@@ -111,9 +111,9 @@ class TriangleAccelerator:
 
     def __del__(self):
         h = getattr(self, "handle", None)
-        if h:
+        if h and not getattr(self, "_borrowed", False):
             _lib.load().skw_accel_destroy(h)
-            self.handle = None
+        self.handle = None
 
     def export(self):
         """(nodes uint32 (n_nodes, 8), tri_prim int32, tri_index int32) of the flattened tree."""
@@ -142,6 +142,43 @@ class TriangleAccelerator:
         s = stream if stream is not None else torch.cuda.current_stream(rays.device).cuda_stream
         _lib.check(_lib.load().skw_intersect(self.handle, rays.data_ptr(), n, hits.data_ptr(), s), self.ctx.handle)
         return hits
+
+    def intersect_d(self, rays, stream=None):
+        """Closest hits of double rays (skw_ray_d: (n, 8) float64 ox oy oz dx dy
+        dz tmin tmax), the reference's exact t.  numpy in -> dict of numpy
+        (prim, tri, t); CUDA tensor in -> (n, 2) float64 CUDA tensor of
+        skw_hit_d records (t, then prim and tri as the bits of the second
+        double; unpack_hits_d reads them)."""
+        lib = _lib.load()
+        if isinstance(rays, np.ndarray):
+            r = np.ascontiguousarray(rays, dtype=np.float64).reshape(-1, 8)
+            hits = np.zeros((r.shape[0], 2), np.float64)
+            _lib.check(lib.skw_intersect_d_host(self.handle, r.ctypes.data, r.shape[0], hits.ctypes.data),
+                       self.ctx.handle)
+            return unpack_hits_d(hits)
+        import torch
+        assert rays.is_cuda and rays.dtype == torch.float64 and rays.is_contiguous() and rays.shape[-1] == 8
+        n = rays.numel() // 8
+        hits = torch.empty((n, 2), dtype=torch.float64, device=rays.device)
+        s = stream if stream is not None else torch.cuda.current_stream(rays.device).cuda_stream
+        _lib.check(lib.skw_intersect_d(self.handle, rays.data_ptr(), n, hits.data_ptr(), s), self.ctx.handle)
+        return hits
+
+    def intersect_test_d(self, rays, stream=None):
+        """Any hit of double rays: uint8 0/1 per ray (numpy in -> numpy out)."""
+        lib = _lib.load()
+        if isinstance(rays, np.ndarray):
+            r = np.ascontiguousarray(rays, dtype=np.float64).reshape(-1, 8)
+            occ = np.zeros(r.shape[0], np.uint8)
+            _lib.check(lib.skw_intersect_test_d_host(self.handle, r.ctypes.data, r.shape[0], occ.ctypes.data),
+                       self.ctx.handle)
+            return occ
+        import torch
+        n = rays.numel() // 8
+        occ = torch.empty((n,), dtype=torch.uint8, device=rays.device)
+        s = stream if stream is not None else torch.cuda.current_stream(rays.device).cuda_stream
+        _lib.check(lib.skw_intersect_test_d(self.handle, rays.data_ptr(), n, occ.data_ptr(), s), self.ctx.handle)
+        return occ
 
     def intersect_test(self, rays, stream=None):
         """Any hit in [tmin, tmax]: uint8 0/1 per ray (numpy in -> numpy out)."""
@@ -205,3 +242,12 @@ def build_flat_tree(primitives: list[Primitive], threads: int = 0) -> dict:
         lib.skw_flat_tree_destroy(h)
     n = nt.value
     return {"nodes": nodes, "tris": tris[:n], "tri_prim": tp[:n], "tri_index": ti[:n], "max_depth": md.value}
+
+
+def unpack_hits_d(hits) -> dict:
+    """skw_hit_d records ((n, 2) float64, numpy or CUDA) -> dict of numpy
+    arrays: prim, tri (int32) and t (float64)."""
+    h = hits.cpu().numpy() if hasattr(hits, "cpu") else np.asarray(hits)
+    h = np.ascontiguousarray(h, np.float64).reshape(-1, 2)
+    ids = h[:, 1].copy().view(np.int32).reshape(-1, 2)
+    return {"prim": ids[:, 0].copy(), "tri": ids[:, 1].copy(), "t": h[:, 0].copy()}

@@ -32,6 +32,11 @@ cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, con
 cudaError_t prepare_traversal(int stack_cap);
 // Resident CTAs per SM of the closest-hit kernel at this capacity.
 int traversal_max_ctas_per_sm(int stack_cap);
+// Double rays (skw_ray_d, 64 bytes each): closest = true writes skw_hit_d
+// (double t, prim, tri; t = +inf, ids -1 on a miss), false uint8_t per ray.
+cudaError_t launch_traversal_d(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
+                               int64_t n, float scene_abs, void *out, unsigned *status, cudaStream_t stream,
+                               int *work);
 
 
 
@@ -71,6 +76,14 @@ struct ViewDev;
 // Point, normals, barycentrics and t of closest hits (12 doubles each).
 cudaError_t launch_hit_geometry(const SceneDev &S, const void *rays, const void *hits, int64_t n, double *out,
                                 cudaStream_t s);
+// The whole Intersection (36 doubles each, skw_intersection) of double ray
+// differentials (21 doubles each, skw_ray_differential) and their
+// skw_hit_d hits.
+cudaError_t launch_intersection(const SceneDev &S, const void *rays, const void *hits, int64_t n, double *out,
+                                cudaStream_t s);
+// Outgoing rays of closest hits (float rays, skw_hit) in directions dirs.
+cudaError_t launch_next_rays(const SceneDev &S, const void *rays, const void *hits, const float *dirs, int64_t n,
+                             void *out, cudaStream_t s);
 // ld: LDSampler image points (sppx = samples per pixel, a power of two; sppy = 1)
 cudaError_t launch_camera(const ViewDev *views, int n_views, int64_t px_begin, int n_px, int sppx, int sppy,
                           void *rays, cudaStream_t s, int ld = 0);

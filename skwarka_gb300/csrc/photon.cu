@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootAr
           wnew = wnew * (1.0f / p);
           o = h.p;
           dnew = ex;
-          tmin = next_min_t(h, ex, S.scene_abs);
+          tmin = next_min_t(S, h, ex);
           cont = true;
         }
       }
@@ -715,7 +715,7 @@ __global__ void __launch_bounds__(128) k_gather_rays(SceneDev S, GatherArgs G, G
         const float ppdf = photon_pdf_of(pd, found, ex);
         const float w = power_heuristic(gs, pdf, gs, ppdf);
         wt = f * (w * fabsf(dot(ex, ns)) / pdf);
-        tmin = next_min_t(h, ex, S.scene_abs);
+        tmin = next_min_t(S, h, ex);
         want = true;
       }
     }
@@ -757,7 +757,7 @@ __global__ void __launch_bounds__(128) k_gather_rays(SceneDev S, GatherArgs G, G
         if (ppdf > 0.0f) {
           const float w = power_heuristic(gs, ppdf, gs, bpdf);
           wt = f * (w * fabsf(dot(ex, ns)) / ppdf);
-          tmin = next_min_t(h, ex, S.scene_abs);
+          tmin = next_min_t(S, h, ex);
           want = true;
         }
       }

@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
           const float bpdf = bsdf_pdf(b, wo, dir);
           const float w = power_heuristic(nl, light_pdf * lcp, nl, bpdf) * fabsf(dot(dir, shading_n)) /
                           (light_pdf * lcp);
-          tmin = next_min_t(h, dir, S.scene_abs);
+          tmin = next_min_t(S, h, dir);
           tmax = dist - 1e-4f;  // to avoid hitting the light itself (:237)
           const V3 le = mul(load3(L.radiance), medium_tr(S.medium, h.p, dir, tmin, tmax));
           val = mul(f, le) * (escale * w / nl);
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
       dir = lv * inv;
       const V3 f = bsdf_eval(b, dir, wo);
       if (!black(f)) {
-        tmin = next_min_t(h, dir, S.scene_abs);
+        tmin = next_min_t(S, h, dir);
         tmax = dist;
         const V3 li = mul(load3(P.intensity), medium_tr(S.medium, h.p, dir, tmin, tmax));
         val = mul(f, li) * (inv * inv * fabsf(dot(dir, shading_n)));
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
           dkd = mul(dI, bsdf_eval_dkd(b, wo, dir)) * (fabsf(dot(dir, shading_n)) / (pdf * nl));
           val = mul(dI, val);
         }
-        tmin = next_min_t(h, dir, S.scene_abs);
+        tmin = next_min_t(S, h, dir);
         want = true;
       }
     }
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
       const bool want = deeper && (c == 0 ? specular_reflect(b, wo, dir, val) : specular_transmit(b, wo, dir, val));
       const int q = queue_append(want, Q.out_count);
       if (want) {
-        store_ray(Q.out_rays, q, h.p, dir, next_min_t(h, dir, S.scene_abs), __int_as_float(0x7f800000));
+        store_ray(Q.out_rays, q, h.p, dir, next_min_t(S, h, dir), __int_as_float(0x7f800000));
         store_rgb(Q.out_w, q, mul(wt, val));
         Q.out_sample[q] = si;
         Q.out_node[q] = (int)(2u * node + (unsigned)c);
@@ -535,6 +535,112 @@ __global__ void k_resolve_bsdf_adj(SceneDev S, int n_light_samples, const float4
   }
 }
 
+// Double-precision vectors with every product and sum rounded separately
+// (no contraction), as the reference's x86-64 build computes them.
+struct D3 {
+  double x, y, z;
+};
+__device__ __forceinline__ D3 d3sub(D3 a, D3 b) { return D3{__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y), __dsub_rn(a.z, b.z)}; }
+__device__ __forceinline__ D3 d3cross(D3 a, D3 b) {
+  return D3{__dsub_rn(__dmul_rn(a.y, b.z), __dmul_rn(a.z, b.y)), __dsub_rn(__dmul_rn(a.z, b.x), __dmul_rn(a.x, b.z)),
+            __dsub_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x))};
+}
+__device__ __forceinline__ double d3dot(D3 a, D3 b) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ D3 d3scale(D3 a, double s) { return D3{__dmul_rn(a.x, s), __dmul_rn(a.y, s), __dmul_rn(a.z, s)}; }
+__device__ __forceinline__ D3 d3normalized(D3 a) {
+  const double l2 = d3dot(a, a);
+  return l2 > 0.0 ? d3scale(a, __ddiv_rn(1.0, __dsqrt_rn(l2))) : a;
+}
+__device__ __forceinline__ D3 d3load(const float *p) { return D3{(double)p[0], (double)p[1], (double)p[2]}; }
+
+// The reference's medium march samples an area light with the lighting ray
+// of DiffuseAreaLightSource::SampleLighting (DiffuseAreaLightSource.cpp:
+// 77-98, _SampleArea :149-175): the sampled point p = b1 v0 + b2 v1 +
+// (1 - b1 - b2) v2 with b1 = 1 - sqrt(u0), b2 = u1 sqrt(u0)
+// (SamplingRoutines::UniformTriangleSampling), the ray (x, (p - x) / |p - x|,
+// 0, |p - x|), and tests it as is (DirectLightingLTEIntegrator.cpp:149-156,
+// without the surface path's 1e-4 pull-back).  The ray ends exactly on the
+// light, so whether the light's own triangle occludes it is decided by the
+// double rounding of the ray, of the slab test and of the Moller-Trumbore t
+// (TriangleAccelerator.cpp:354-462).  This restates that decision on the
+// same double arithmetic: the reference reaches the leaf holding the light
+// triangle exactly when the leaf's own slab test passes (every ancestor's
+// box contains the leaf's, and (b - o) * (1/d) is monotone in b, so an
+// ancestor's slab interval contains the leaf's), and then tests the leaf's
+// triangles.  Only triangles whose box contains p are tested here: the ray
+// reaches any other triangle of the leaf before p, and the float shadow ray
+// (whose tmax stops short of the light) decides those.  Returns true when
+// the light's leaf occludes the ray; p_out, len_out give the sampled point
+// and the ray length.
+__device__ bool own_light_leaf_occludes(const SceneDev &S, int j, D3 x, double u0, double u1, D3 &p_out,
+                                        double &len_out) {
+  const int g = S.light_tri[j];
+  const int j0 = S.tri_vidx[3 * g], j1 = S.tri_vidx[3 * g + 1], j2 = S.tri_vidx[3 * g + 2];
+  const D3 v0 = d3load(S.vpos + 3 * j0), v1 = d3load(S.vpos + 3 * j1), v2 = d3load(S.vpos + 3 * j2);
+  const double sq = __dsqrt_rn(u0);
+  const double b1 = __dsub_rn(1.0, sq), b2 = __dmul_rn(u1, sq);
+  const double b0 = __dsub_rn(__dsub_rn(1.0, b1), b2);
+  const D3 a = d3scale(v0, b1), b = d3scale(v1, b2), c = d3scale(v2, b0);
+  const D3 p{__dadd_rn(__dadd_rn(a.x, b.x), c.x), __dadd_rn(__dadd_rn(a.y, b.y), c.y),
+             __dadd_rn(__dadd_rn(a.z, b.z), c.z)};
+  const D3 lv = d3sub(p, x);
+  const double len = __dsqrt_rn(d3dot(lv, lv));
+  const D3 dir = d3scale(lv, __ddiv_rn(1.0, len));
+  p_out = p;
+  len_out = len;
+  const float *lb = S.light_leaf + 8 * (int64_t)j;
+  // the leaf's slab test (TriangleAccelerator.cpp:373-390)
+  const double inv[3] = {__ddiv_rn(1.0, dir.x), __ddiv_rn(1.0, dir.y), __ddiv_rn(1.0, dir.z)};
+  const double org[3] = {x.x, x.y, x.z};
+  double tn[3], tf[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    tn[k] = __dmul_rn(__dsub_rn((double)lb[k], org[k]), inv[k]);
+    tf[k] = __dmul_rn(__dsub_rn((double)lb[3 + k], org[k]), inv[k]);
+    if (tn[k] > tf[k]) {
+      const double tmp = tn[k];
+      tn[k] = tf[k];
+      tf[k] = tmp;
+    }
+  }
+  const double tmin = 0.0, tmax = len;
+  if (tmin > tf[0] || tn[0] > tf[1] || tn[1] > tf[0] || tn[2] > tf[0] || tmin > tf[1] || tn[0] > tf[2] ||
+      tn[1] > tf[2] || tn[2] > tf[1] || tmin > tf[2] || tn[0] > tmax || tn[1] > tmax || tn[2] > tmax)
+    return false;
+  const int first = __float_as_int(lb[6]), count = __float_as_int(lb[7]);
+  const float pf[3] = {(float)p.x, (float)p.y, (float)p.z};
+  for (int k = 0; k < count; ++k) {
+    const float4 ta = S.accel_tris[3 * (first + k)], tb = S.accel_tris[3 * (first + k) + 1],
+                 tc = S.accel_tris[3 * (first + k) + 2];
+    // the triangle's box, widened by a few float ulps of the point, must hold p
+    bool near = true;
+    const float va[3] = {ta.x, ta.y, ta.z}, vb[3] = {tb.x, tb.y, tb.z}, vc[3] = {tc.x, tc.y, tc.z};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const float w = 4.0f * 1.1920929e-7f * (fabsf(pf[q]) + 1e-30f);
+      near = near && pf[q] >= fminf(fminf(va[q], vb[q]), vc[q]) - w && pf[q] <= fmaxf(fmaxf(va[q], vb[q]), vc[q]) + w;
+    }
+    if (!near) continue;
+    // Moller-Trumbore in double (TriangleAccelerator.cpp:419-452)
+    const D3 w0{(double)ta.x, (double)ta.y, (double)ta.z};
+    const D3 e1 = d3sub(D3{(double)tb.x, (double)tb.y, (double)tb.z}, w0);
+    const D3 e2 = d3sub(D3{(double)tc.x, (double)tc.y, (double)tc.z}, w0);
+    const D3 s1 = d3cross(dir, e2);
+    const double idv = __ddiv_rn(1.0, d3dot(s1, e1));
+    const D3 dd = d3sub(x, w0);
+    const double c1 = __dmul_rn(d3dot(dd, s1), idv);
+    if (!(c1 > -2.220446049250313e-16 && c1 < 1.0 + 2.220446049250313e-16)) continue;
+    const D3 s2 = d3cross(dd, e1);
+    const double c2 = __dmul_rn(d3dot(dir, s2), idv);
+    if (!(c2 > -2.220446049250313e-16 && __dadd_rn(c1, c2) < 1.0 + 2.220446049250313e-16)) continue;
+    const double t = __dmul_rn(d3dot(e2, s2), idv);
+    if (t >= tmin && t <= tmax) return true;
+  }
+  return false;
+}
+
 // Single scattering along the camera ray's segment in the medium
 // (DirectLightingLTEIntegrator::_MediaRadianceAndTranmsittance,
 // LTEIntegrators/DirectLightingLTEIntegrator.cpp:62-175): march with step
@@ -625,9 +731,10 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
     ++steps;
     step = fmin(step, te - tb);
     const double s1 = radical_inverse_r(k + 1, 2);
-    const float s2a = (float)radical_inverse_r(k + 1, 3), s2b = (float)radical_inverse_r(k + 1, 5);
+    const double s2ad = radical_inverse_r(k + 1, 3), s2bd = radical_inverse_r(k + 1, 5);
     const V3 prev = point;
-    point = o + d * (float)(tb + offset1 * step);
+    const double tp = tb + offset1 * step;
+    point = o + d * (float)tp;
     tb += step;
     const float seg = len(point - prev);
     T = v3(T.x * expf(-st.x * seg), T.y * expf(-st.y * seg), T.z * expf(-st.z * seg));
@@ -636,7 +743,7 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
       const int li = min((int)(s1 * nlights), nlights - 1);
       V3 lv = v3(0, 0, 0), ldir = v3(0, 0, 0);
       float dist = 0.0f, pdf = 1.0f;
-      bool area = false;
+      bool area = false, self_occ = false;
       if (li < S.n_point_lights) {
         const PointLightDev PL = S.point_lights[li];
         const V3 to = load3(PL.position) - point;
@@ -656,8 +763,15 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
         const int j0 = S.tri_vidx[3 * g], j1 = S.tri_vidx[3 * g + 1], j2 = S.tri_vidx[3 * g + 2];
         const V3 q0 = load3(S.vpos + 3 * j0), q1 = load3(S.vpos + 3 * j1), q2 = load3(S.vpos + 3 * j2);
         const V3 ln = normalized(cross(q1 - q0, q2 - q0));
-        const float sq = sqrtf(s2a), b1 = 1.0f - sq, b2 = s2b * sq;
-        const V3 sp = q0 * b1 + q1 * b2 + q2 * (1.0f - b1 - b2);
+        D3 spd;
+        double lend;
+        // the march point in double, o + d t as the reference's Ray::operator()
+        // computes it from its double ray (a float point would round the
+        // light ray differently from the reference's double one)
+        const D3 xd{__dadd_rn((double)o.x, __dmul_rn((double)d.x, tp)), __dadd_rn((double)o.y, __dmul_rn((double)d.y, tp)),
+                    __dadd_rn((double)o.z, __dmul_rn((double)d.z, tp))};
+        self_occ = own_light_leaf_occludes(S, L.tri_begin + a, xd, s2ad, s2bd, spd, lend);
+        const V3 sp = v3((float)spd.x, (float)spd.y, (float)spd.z);
         const V3 to = sp - point;
         dist = len(to);
         ldir = to * (1.0f / dist);
@@ -666,7 +780,7 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
         if (dot(ln, ldir) < 0.0f) lv = load3(L.radiance) * S.emission_scale;
         area = true;
       }
-      const bool want = !black(lv) && pdf > 0.0f;
+      const bool want = !black(lv) && pdf > 0.0f && !self_occ;
       V3 val = v3(0, 0, 0);
       if (want) {
         // HGPhaseFunction::ScatteringPDF(incoming = -light direction, outgoing = -ray direction)
@@ -678,7 +792,9 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
       }
       const int q = queue_append(want, mcount);
       if (want) {
-        store_ray(mrays, q, point, ldir, 0.0f, dist);
+        // An area light's own leaf was decided above; the float ray stops
+        // short of the light so that it tests everything in front of it.
+        store_ray(mrays, q, point, ldir, 0.0f, area ? dist * (1.0f - 1e-4f) : dist);
         mtarget[q] = spec ? (int)((int64_t)si * A.slots + A.spec_slot) : i;
         if (spec) val = mul(val, wt);
         if (ADJ) {
@@ -779,24 +895,6 @@ __global__ void k_film(const float *__restrict__ contrib, int64_t px_begin, int 
 // shading normal b0 n0 + b1 n1 + b2 n2 normalised (the geometric normal
 // without vertex normals).  Out per hit: point, geometric normal, shading
 // normal, b1, b2, t (12 doubles); NaN for a miss.
-struct D3 {
-  double x, y, z;
-};
-__device__ __forceinline__ D3 d3sub(D3 a, D3 b) { return D3{__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y), __dsub_rn(a.z, b.z)}; }
-__device__ __forceinline__ D3 d3cross(D3 a, D3 b) {
-  return D3{__dsub_rn(__dmul_rn(a.y, b.z), __dmul_rn(a.z, b.y)), __dsub_rn(__dmul_rn(a.z, b.x), __dmul_rn(a.x, b.z)),
-            __dsub_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x))};
-}
-__device__ __forceinline__ double d3dot(D3 a, D3 b) {
-  return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
-}
-__device__ __forceinline__ D3 d3scale(D3 a, double s) { return D3{__dmul_rn(a.x, s), __dmul_rn(a.y, s), __dmul_rn(a.z, s)}; }
-__device__ __forceinline__ D3 d3normalized(D3 a) {
-  const double l2 = d3dot(a, a);
-  return l2 > 0.0 ? d3scale(a, __ddiv_rn(1.0, __dsqrt_rn(l2))) : a;
-}
-__device__ __forceinline__ D3 d3load(const float *p) { return D3{(double)p[0], (double)p[1], (double)p[2]}; }
-
 __global__ void k_hit_geometry(SceneDev S, const float4 *__restrict__ rays, const int4 *__restrict__ hits, int n,
                                double *__restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -835,6 +933,175 @@ __global__ void k_hit_geometry(SceneDev S, const float4 *__restrict__ rays, cons
   for (int k = 0; k < 12; ++k) o[k] = v[k];
 }
 
+// ---------------------------------------------- the whole Intersection --
+// TriangleAccelerator::Intersect's Intersection for ray differentials
+// (TriangleAccelerator.cpp:295-347 with TriangleMesh::
+// ComputeDifferentialGeometry, TriangleMesh.cpp:414-561), in double with
+// every operation rounded separately as the reference's x86-64 build does.
+// Identity-transform primitives reproduce the reference bit for bit,
+// including the identity Transform's own arithmetic on the way into and out
+// of mesh space (1 x + 0 y + 0 z + 0 turns a -0 into +0; TransformNormal
+// normalises again).  A transformed primitive is evaluated on its
+// world-space triangle (same formulas, not the reference's rounding).
+// The meshes here carry no uv coordinates (the reference's default: all
+// zero) and no tangents, so the tangent comes from CoordinateSystem around
+// the shading normal, as the reference's zero-determinant branch does.
+
+__device__ __forceinline__ D3 d3add(D3 a, D3 b) { return D3{__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y), __dadd_rn(a.z, b.z)}; }
+
+// Transform::operator() of the identity matrix on a point / vector and
+// TransformNormal (Math/Transform.h:223-292).
+__device__ __forceinline__ double id_row(double a, double b, double c, int r) {
+  const double m0 = r == 0 ? 1.0 : 0.0, m1 = r == 1 ? 1.0 : 0.0, m2 = r == 2 ? 1.0 : 0.0;
+  return __dadd_rn(__dadd_rn(__dmul_rn(m0, a), __dmul_rn(m1, b)), __dmul_rn(m2, c));
+}
+__device__ __forceinline__ D3 id_point(D3 p) {
+  return D3{__dadd_rn(id_row(p.x, p.y, p.z, 0), 0.0), __dadd_rn(id_row(p.x, p.y, p.z, 1), 0.0),
+            __dadd_rn(id_row(p.x, p.y, p.z, 2), 0.0)};
+}
+__device__ __forceinline__ D3 id_vector(D3 v) { return D3{id_row(v.x, v.y, v.z, 0), id_row(v.x, v.y, v.z, 1), id_row(v.x, v.y, v.z, 2)}; }
+
+// TriangleMesh::_ComputeIntersectionPoint (TriangleMesh.cpp:414-437).
+__device__ __forceinline__ bool plane_point(D3 v0, D3 v1, D3 v2, D3 o, D3 d, double &b1, double &b2, double &t) {
+  const D3 e1 = d3sub(v1, v0), e2 = d3sub(v2, v0);
+  const D3 s1 = d3cross(d, e2);
+  const double div = d3dot(s1, e1);
+  if (div == 0.0) return false;
+  const double inv = __ddiv_rn(1.0, div);
+  const D3 dd = d3sub(o, v0);
+  b1 = __dmul_rn(d3dot(dd, s1), inv);
+  const D3 s2 = d3cross(dd, e1);
+  b2 = __dmul_rn(d3dot(d, s2), inv);
+  t = __dmul_rn(d3dot(e2, s2), inv);
+  return true;
+}
+
+// MathRoutines::CoordinateSystem (Math/MathRoutines.h:298-313): e2.
+__device__ __forceinline__ D3 coordinate_e2(D3 e1) {
+  if (fabs(e1.x) > fabs(e1.y)) {
+    const double il = __ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(__dmul_rn(e1.x, e1.x), __dmul_rn(e1.z, e1.z))));
+    return D3{__dmul_rn(-e1.z, il), 0.0, __dmul_rn(e1.x, il)};
+  }
+  const double il = __ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(__dmul_rn(e1.y, e1.y), __dmul_rn(e1.z, e1.z))));
+  return D3{0.0, __dmul_rn(e1.z, il), __dmul_rn(-e1.y, il)};
+}
+
+// b0 a + b1 b + b2 c (uv interpolation with the all-zero uv of the meshes:
+// the sign of each zero product is kept, as the reference computes it).
+__device__ __forceinline__ double lerp0(double b0, double b1, double b2) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(b0, 0.0), __dmul_rn(b1, 0.0)), __dmul_rn(b2, 0.0));
+}
+
+__global__ void k_intersection(SceneDev S, const double *__restrict__ rays, const int4 *__restrict__ hits, int n,
+                               double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double *o = out + 36 * (int64_t)i;
+  const int4 hit = hits[i];
+  const int prim = hit.z, tri = hit.w;
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  if (prim < 0) {
+    for (int k = 0; k < 35; ++k) o[k] = nan;
+    ((int *)(o + 35))[0] = -1;
+    ((int *)(o + 35))[1] = -1;
+    return;
+  }
+  const double *r = rays + 21 * (int64_t)i;
+  const bool ident = S.prim_xform == nullptr || S.prim_xform[prim] == 0;
+  const int g = S.prim_tri_offset[prim] + tri;
+  const int j0 = S.tri_vidx[3 * g], j1 = S.tri_vidx[3 * g + 1], j2 = S.tri_vidx[3 * g + 2];
+  const D3 v0 = d3load(S.vpos + 3 * j0), v1 = d3load(S.vpos + 3 * j1), v2 = d3load(S.vpos + 3 * j2);
+  // world_to_mesh of the base ray and of the differentials
+  auto pt = [&](D3 p) { return ident ? id_point(p) : p; };
+  auto vc = [&](D3 v) { return ident ? id_vector(v) : v; };
+  const D3 org = pt(D3{r[0], r[1], r[2]}), dir = vc(D3{r[3], r[4], r[5]});
+  const bool has_diff = __double_as_longlong(r[20]) & 1;
+  double b1 = nan, b2 = nan, t = nan;
+  plane_point(v0, v1, v2, org, dir, b1, b2, t);
+  const D3 point = d3add(org, d3scale(dir, t));  // Ray::operator()(t)
+  const double b0 = __dsub_rn(__dsub_rn(1.0, b1), b2);
+  const double uv[2] = {lerp0(b0, b1, b2), lerp0(b0, b1, b2)};
+  const bool use_sn = S.prim_has_normals[prim] != 0;
+  D3 n0{0, 0, 0}, n1{0, 0, 0}, n2{0, 0, 0};
+  if (use_sn) {
+    n0 = d3load(S.vnrm + 3 * j0);
+    n1 = d3load(S.vnrm + 3 * j1);
+    n2 = d3load(S.vnrm + 3 * j2);
+  }
+  const D3 gn = d3normalized(d3cross(d3sub(v1, v0), d3sub(v2, v0)));
+  const D3 sn = use_sn ? d3normalized(d3add(d3add(d3scale(n0, b0), d3scale(n1, b1)), d3scale(n2, b2))) : gn;
+  // tangent: zero uv determinant -> CoordinateSystem(shading normal)
+  D3 tangent = coordinate_e2(sn);
+  const D3 t2 = d3cross(sn, tangent);
+  if (d3dot(t2, t2) > 2.220446049250313e-16) {
+    const D3 tt = d3cross(t2, sn);
+    const double l2 = d3dot(tt, tt);
+    tangent = l2 > 0.0 ? d3scale(tt, __ddiv_rn(1.0, __dsqrt_rn(l2))) : tt;
+  }
+  // screen-space differentials
+  D3 pdx = point, pdy = point, ndx = sn, ndy = sn;
+  double duv[4] = {0.0, 0.0, 0.0, 0.0};
+  double b1x, b2x, tx, b1y, b2y, ty;
+  if (has_diff && plane_point(v0, v1, v2, pt(D3{r[8], r[9], r[10]}), vc(D3{r[11], r[12], r[13]}), b1x, b2x, tx) &&
+      plane_point(v0, v1, v2, pt(D3{r[14], r[15], r[16]}), vc(D3{r[17], r[18], r[19]}), b1y, b2y, ty)) {
+    const double b0x = __dsub_rn(__dsub_rn(1.0, b1x), b2x), b0y = __dsub_rn(__dsub_rn(1.0, b1y), b2y);
+    pdx = d3add(pt(D3{r[8], r[9], r[10]}), d3scale(vc(D3{r[11], r[12], r[13]}), tx));
+    pdy = d3add(pt(D3{r[14], r[15], r[16]}), d3scale(vc(D3{r[17], r[18], r[19]}), ty));
+    duv[0] = __dsub_rn(lerp0(b0x, b1x, b2x), uv[0]);
+    duv[1] = __dsub_rn(lerp0(b0x, b1x, b2x), uv[1]);
+    duv[2] = __dsub_rn(lerp0(b0y, b1y, b2y), uv[0]);
+    duv[3] = __dsub_rn(lerp0(b0y, b1y, b2y), uv[1]);
+    if (use_sn) {
+      ndx = d3normalized(d3add(d3add(d3scale(n0, b0x), d3scale(n1, b1x)), d3scale(n2, b2x)));
+      ndy = d3normalized(d3add(d3add(d3scale(n0, b0y), d3scale(n1, b1y)), d3scale(n2, b2y)));
+    } else {
+      ndx = ndy = gn;
+    }
+  }
+  // back to world space (identity: the Transform's own arithmetic)
+  auto nrm = [&](D3 v) { return ident ? d3normalized(id_vector(v)) : v; };
+  const D3 wp = pt(point);
+  const D3 out3[9] = {wp, nrm(gn), nrm(sn), pt(pdx), pt(pdy), nrm(ndx), nrm(ndy), vc(tangent),
+                      d3cross(d3sub(v1, v0), d3sub(v2, v0))};
+  // m_dot uses world_to_mesh of the world point (TriangleAccelerator.cpp:345)
+  const double mdot = d3dot(d3cross(d3sub(v0, pt(wp)), d3sub(v1, v0)), d3sub(v2, v0));
+  // layout: point, geometric normal, shading normal, uv, point_dx, point_dy,
+  // normal_dx, normal_dy, duv_dx, duv_dy, tangent, cross, dot, t
+  const int at[9] = {0, 3, 6, 11, 14, 17, 20, 27, 30};
+  for (int k = 0; k < 9; ++k) {
+    o[at[k]] = out3[k].x;
+    o[at[k] + 1] = out3[k].y;
+    o[at[k] + 2] = out3[k].z;
+  }
+  o[9] = uv[0];
+  o[10] = uv[1];
+  for (int k = 0; k < 4; ++k) o[23 + k] = duv[k];
+  o[33] = mdot;
+  o[34] = __hiloint2double(hit.y, hit.x);
+  ((int *)(o + 35))[0] = prim;
+  ((int *)(o + 35))[1] = tri;
+}
+
+// Outgoing rays as the renders make them: from the float hit point of each
+// closest hit in direction dirs[i], tmin = GetNextMinT (next_min_t), tmax =
+// +inf; NaN rays for misses.
+__global__ void k_next_rays(SceneDev S, const float4 *__restrict__ rays, const int4 *__restrict__ hits,
+                            const float *__restrict__ dirs, int n, float4 *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 hit = hits[i];
+  const V3 w = load3(dirs + 3 * (int64_t)i);
+  if (hit.y < 0) {
+    const float nanf_ = __int_as_float(0x7fc00000);
+    out[2 * i] = make_float4(nanf_, nanf_, nanf_, nanf_);
+    out[2 * i + 1] = make_float4(nanf_, nanf_, nanf_, nanf_);
+    return;
+  }
+  const float4 ra = rays[2 * i], rb = rays[2 * i + 1];
+  const Hit h = make_hit(S, v3(ra.x, ra.y, ra.z), v3(ra.w, rb.x, rb.y), __int_as_float(hit.x), hit.y, hit.z);
+  store_ray(out, i, h.p, w, next_min_t(S, h, w), __int_as_float(0x7f800000));
+}
+
 }  // namespace
 
 cudaError_t launch_hit_geometry(const SceneDev &S, const void *rays, const void *hits, int64_t n, double *out,
@@ -842,6 +1109,22 @@ cudaError_t launch_hit_geometry(const SceneDev &S, const void *rays, const void 
   if (n <= 0) return cudaSuccess;
   k_hit_geometry<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, (const float4 *)rays, (const int4 *)hits, (int)n,
                                                               out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_intersection(const SceneDev &S, const void *rays, const void *hits, int64_t n, double *out,
+                                cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_intersection<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, (const double *)rays, (const int4 *)hits, (int)n,
+                                                              out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_next_rays(const SceneDev &S, const void *rays, const void *hits, const float *dirs, int64_t n,
+                             void *out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_next_rays<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, (const float4 *)rays, (const int4 *)hits, dirs, (int)n,
+                                                          (float4 *)out);
   return cudaGetLastError();
 }
 

@@ -427,18 +427,68 @@ __device__ V3 bsdf_sample(const Bsdf &b, V3 wi_w, float uc, float u0, float u1, 
 // ------------------------------------------------------------------ shading --
 struct Hit {
   V3 p, ng, ns;
-  V3 v0, cr;  // triangle vertex 0 and (v1 - v0) x (v2 - v0), for the next ray's tmin
   int g;      // global triangle
 };
 
-// Ray start offset for leaving a surface: past the point where the ray
-// crosses the triangle's plane (CoreUtils::GetNextMinT, CoreUtils.h:139-149),
-// plus a margin for the float hit point.
-__device__ __forceinline__ float next_min_t(const Hit &h, V3 w, float scene_abs) {
-  const float den = dot(w, h.cr);
-  float t = 0.0f;
-  if (den != 0.0f) t = fmaxf(0.0f, dot(h.v0 - h.p, h.cr) / den);
-  return t + 2.0e-6f * (1.0f + scene_abs);
+// CoreUtils::GetNextMinT (CoreUtils.h:139-149) for a ray leaving the hit
+// point p in direction w: max(0, m_dot / (w . m_cross) + 1e-14), with the
+// Intersection's m_cross = (v1 - v0) x (v2 - v0) and m_dot = ((v0 - p) x
+// (v1 - v0)) . (v2 - v0) = (v0 - p) . m_cross (TriangleAccelerator.cpp:
+// 341-345): the ray's own crossing of the triangle's plane plus 1e-14.
+//
+// next_min_t_exact evaluates that in double with every operation rounded
+// separately, as the reference does, for the float point p the ray actually
+// starts from, rounded up to float.  On GB300 a double operation costs
+// about 64 float ones, so the renders use next_min_t: the same quantity in
+// float with a rigorous bound on its error, E; the returned tmin is an upper
+// bound of the reference's value that exceeds it by at most 2E (a few float
+// roundings of the hit point's distance to the plane, the precision of a
+// float ray anyway), so the outgoing ray never re-hits its own triangle and
+// skips no geometry farther than that from its plane.  Where the direction
+// is nearly parallel to the plane (the bound on the denominator covers zero)
+// the double evaluation decides.  World-space triangle: for a transformed
+// primitive the reference evaluates the same quantity in mesh space (t is
+// the same parameter in both spaces).
+__device__ __noinline__ float next_min_t_exact(const SceneDev &S, const Hit &h, V3 w) {
+  const int i0 = S.tri_vidx[3 * h.g], i1 = S.tri_vidx[3 * h.g + 1], i2 = S.tri_vidx[3 * h.g + 2];
+  const double ax = S.vpos[3 * i0], ay = S.vpos[3 * i0 + 1], az = S.vpos[3 * i0 + 2];
+  const double e1x = __dsub_rn(S.vpos[3 * i1], ax), e1y = __dsub_rn(S.vpos[3 * i1 + 1], ay),
+               e1z = __dsub_rn(S.vpos[3 * i1 + 2], az);
+  const double e2x = __dsub_rn(S.vpos[3 * i2], ax), e2y = __dsub_rn(S.vpos[3 * i2 + 1], ay),
+               e2z = __dsub_rn(S.vpos[3 * i2 + 2], az);
+  const double cx = __dsub_rn(__dmul_rn(e1y, e2z), __dmul_rn(e1z, e2y));
+  const double cy = __dsub_rn(__dmul_rn(e1z, e2x), __dmul_rn(e1x, e2z));
+  const double cz = __dsub_rn(__dmul_rn(e1x, e2y), __dmul_rn(e1y, e2x));
+  const double qx = __dsub_rn(ax, (double)h.p.x), qy = __dsub_rn(ay, (double)h.p.y), qz = __dsub_rn(az, (double)h.p.z);
+  const double sx = __dsub_rn(__dmul_rn(qy, e1z), __dmul_rn(qz, e1y));
+  const double sy = __dsub_rn(__dmul_rn(qz, e1x), __dmul_rn(qx, e1z));
+  const double sz = __dsub_rn(__dmul_rn(qx, e1y), __dmul_rn(qy, e1x));
+  const double mdot = __dadd_rn(__dadd_rn(__dmul_rn(sx, e2x), __dmul_rn(sy, e2y)), __dmul_rn(sz, e2z));
+  const double div = __dadd_rn(__dadd_rn(__dmul_rn((double)w.x, cx), __dmul_rn((double)w.y, cy)),
+                               __dmul_rn((double)w.z, cz));
+  if (div == 0.0) return 0.0f;
+  const double t = fmax(0.0, __dadd_rn(__dmul_rn(mdot, __ddiv_rn(1.0, div)), 1e-14));
+  return __double2float_ru(t);
+}
+
+__device__ __forceinline__ float next_min_t(const SceneDev &S, const Hit &h, V3 w) {
+  const int i0 = S.tri_vidx[3 * h.g], i1 = S.tri_vidx[3 * h.g + 1], i2 = S.tri_vidx[3 * h.g + 2];
+  const V3 p0 = load3(S.vpos + 3 * i0), p1 = load3(S.vpos + 3 * i1), p2 = load3(S.vpos + 3 * i2);
+  const V3 e1 = p1 - p0, e2 = p2 - p0, n = cross(e1, e2), q = p0 - h.p;
+  // componentwise magnitude of the cross product, bounding its terms
+  const V3 a1 = v3(fabsf(e1.x), fabsf(e1.y), fabsf(e1.z)), a2 = v3(fabsf(e2.x), fabsf(e2.y), fabsf(e2.z));
+  const V3 A = v3(a1.y * a2.z + a1.z * a2.y, a1.z * a2.x + a1.x * a2.z, a1.x * a2.y + a1.y * a2.x);
+  const float num = dot(q, n), den = dot(w, n);
+  // u = 2^-24: the edges carry <= u relative error, the cross product
+  // <= 4u A, q <= u |q|; the dot products add 3u of their magnitude sums
+  const float u = 5.9604645e-8f;
+  const float en = 9.0f * u * (fabsf(q.x) * A.x + fabsf(q.y) * A.y + fabsf(q.z) * A.z) + 1e-35f;
+  const float ed = 8.0f * u * (fabsf(w.x) * A.x + fabsf(w.y) * A.y + fabsf(w.z) * A.z) + 1e-35f;
+  const float ad = fabsf(den);
+  if (!(ad > 4.0f * ed)) return next_min_t_exact(S, h, w);
+  const float t = num / den;
+  const float et = 1.01f * (en + fabsf(t) * ed) / (ad - ed) + 4.0f * u * fabsf(t);
+  return fmaxf(0.0f, __fadd_ru(__fadd_ru(t, et), 1e-14f));
 }
 
 __device__ Bsdf make_bsdf(const SceneDev &S, const Hit &h, int prim) {
@@ -533,9 +583,7 @@ __device__ Hit make_hit(const SceneDev &S, V3 o, V3 d, float t, int prim, int tr
   const int i0 = S.tri_vidx[3 * h.g], i1 = S.tri_vidx[3 * h.g + 1], i2 = S.tri_vidx[3 * h.g + 2];
   const V3 p0 = load3(S.vpos + 3 * i0), p1 = load3(S.vpos + 3 * i1), p2 = load3(S.vpos + 3 * i2);
   h.p = o + d * t;
-  h.v0 = p0;
-  h.cr = cross(p1 - p0, p2 - p0);
-  h.ng = normalized(h.cr);
+  h.ng = normalized(cross(p1 - p0, p2 - p0));
   h.ns = h.ng;
   if (S.prim_has_normals[prim]) {
     // barycentrics of the hit point (Moller-Trumbore), then the

@@ -4,6 +4,8 @@
 // g = prim_tri_offset[prim] + mesh triangle index.
 #pragma once
 
+#include <vector_types.h>
+
 #include <cstdint>
 
 #include "merl.h"
@@ -69,11 +71,19 @@ struct SceneDev {
   const int32_t *prim_material;
   const int32_t *prim_light;      // area light index or -1
   const int32_t *prim_has_normals;
+  const int32_t *prim_xform;      // 1 where the primitive has a mesh-to-world matrix
   const DevMaterial *materials;
   const AreaLight *area_lights;
   int32_t n_area_lights;
   const int32_t *light_tri;       // global triangle ids of all light triangles
   const float *light_cdf;         // normalised cumulative area per light range
+  // Per light triangle (light_tri order), the accelerator leaf that holds
+  // it: 8 words -- the leaf's float box (min xyz, max xyz), its first
+  // triangle slot and slot count (int bits) -- for the reference-exact test
+  // of medium light samples that end on the light (render.cu,
+  // own_light_leaf_occludes); accel_tris: the accelerator's triangle slots.
+  const float *light_leaf;
+  const float4 *accel_tris;
   const PointLightDev *point_lights;
   int32_t n_point_lights;
   float scene_abs;                // largest absolute vertex coordinate

@@ -231,7 +231,7 @@ int skw_accel_export(const skw_accel *a, uint32_t *nodes, int32_t *tri_prim, int
   return SKW_OK;
 }
 
-static int run_query(skw_accel *a, bool closest, const skw_ray *rays, int64_t n, void *out, void *stream) {
+static int run_query(skw_accel *a, bool closest, bool dray, const void *rays, int64_t n, void *out, void *stream) {
   if (!a) return SKW_ERR_ARG;
   if (n < 0 || (n > 0 && (!rays || !out))) return fail(a->ctx, SKW_ERR_ARG, "bad ray buffer");
   if (n > (int64_t)INT32_MAX) return fail(a->ctx, SKW_ERR_ARG, "too many rays for one call (max 2^31-1)");
@@ -247,8 +247,10 @@ static int run_query(skw_accel *a, bool closest, const skw_ray *rays, int64_t n,
   if ((e = skw::ctx_pool(ctx, &pool)) != cudaSuccess ||
       (e = cudaMallocFromPoolAsync((void **)&work, 256, pool, st)) != cudaSuccess)
     return cuda_fail(ctx, e, "work counter");
-  e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, nullptr, a->scene_abs, nullptr, out,
-                            a->d_status, st, 0, work);
+  e = dray ? skw::launch_traversal_d(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, a->scene_abs, out,
+                                     a->d_status, st, work)
+           : skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rays, n, nullptr, a->scene_abs,
+                                   nullptr, out, a->d_status, st, 0, work);
   cudaFreeAsync(work, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, closest ? "closest-hit launch" : "any-hit launch");
   ctx->launches.fetch_add(1);
@@ -256,11 +258,19 @@ static int run_query(skw_accel *a, bool closest, const skw_ray *rays, int64_t n,
 }
 
 int skw_intersect(skw_accel *a, const skw_ray *rays, int64_t n, skw_hit *hits, void *stream) {
-  return run_query(a, true, rays, n, hits, stream);
+  return run_query(a, true, false, rays, n, hits, stream);
 }
 
 int skw_intersect_test(skw_accel *a, const skw_ray *rays, int64_t n, uint8_t *occluded, void *stream) {
-  return run_query(a, false, rays, n, occluded, stream);
+  return run_query(a, false, false, rays, n, occluded, stream);
+}
+
+int skw_intersect_d(skw_accel *a, const skw_ray_d *rays, int64_t n, skw_hit_d *hits, void *stream) {
+  return run_query(a, true, true, rays, n, hits, stream);
+}
+
+int skw_intersect_test_d(skw_accel *a, const skw_ray_d *rays, int64_t n, uint8_t *occluded, void *stream) {
+  return run_query(a, false, true, rays, n, occluded, stream);
 }
 
 // Host-buffer queries.  Above kHostChunk rays the rays go in and the results
@@ -273,13 +283,14 @@ int skw_intersect_test(skw_accel *a, const skw_ray *rays, int64_t n, uint8_t *oc
 // end against 787 for one copy-in, query, copy-out sequence.
 static constexpr int64_t kHostChunk = (int64_t)1 << 21;
 
-static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64_t n, void *out) {
+static int run_query_host(skw_accel *a, bool closest, bool dray, const void *rays, int64_t n, void *out) {
   if (!a) return SKW_ERR_ARG;
   if (n < 0 || (n > 0 && (!rays || !out))) return fail(a->ctx, SKW_ERR_ARG, "bad ray buffer");
   if (n == 0) return SKW_OK;
   cudaError_t e = cudaSetDevice(a->ctx->device);
   if (e != cudaSuccess) return cuda_fail(a->ctx, e, "cudaSetDevice");
-  const size_t out_unit = closest ? sizeof(skw_hit) : 1;
+  const size_t out_unit = closest ? (dray ? sizeof(skw_hit_d) : sizeof(skw_hit)) : 1;
+  const size_t ray_unit = dray ? sizeof(skw_ray_d) : sizeof(skw_ray);
   const int64_t n_chunks = (n + kHostChunk - 1) / kHostChunk;
   const int n_streams = (int)std::min<int64_t>(n_chunks, 2);
   const int ctas = n_chunks > 1 ? std::max(1, skw::traversal_max_ctas_per_sm(a->stack_cap) / 2) : 0;
@@ -303,7 +314,7 @@ static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64
   void *d_rays = nullptr, *d_out = nullptr;
   int *d_work = nullptr;  // one ray-group counter per stream (256 bytes apart)
   if (rc == SKW_OK &&
-      ((e = cudaMallocFromPoolAsync(&d_rays, (size_t)(n_streams * chunk_rays) * sizeof(skw_ray), pool, st[0])) !=
+      ((e = cudaMallocFromPoolAsync(&d_rays, (size_t)(n_streams * chunk_rays) * ray_unit, pool, st[0])) !=
            cudaSuccess ||
        (e = cudaMallocFromPoolAsync(&d_out, (size_t)(n_streams * chunk_rays) * out_unit, pool, st[0])) != cudaSuccess ||
        (e = cudaMallocFromPoolAsync((void **)&d_work, 512, pool, st[0])) != cudaSuccess))
@@ -316,14 +327,16 @@ static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64
     const int si = (int)(c % n_streams);
     cudaStream_t s = st[si];
     const int64_t r0 = c * kHostChunk, m = std::min(kHostChunk, n - r0);
-    const skw_ray *dr = (const skw_ray *)d_rays + si * chunk_rays;
+    char *dr = (char *)d_rays + (size_t)(si * chunk_rays) * ray_unit;
     char *dout = (char *)d_out + (size_t)(si * chunk_rays) * out_unit;
-    if ((e = cudaMemcpyAsync((void *)dr, rays + r0, (size_t)m * sizeof(skw_ray), cudaMemcpyHostToDevice, s)) !=
-        cudaSuccess) {
+    if ((e = cudaMemcpyAsync(dr, (const char *)rays + (size_t)r0 * ray_unit, (size_t)m * ray_unit,
+                             cudaMemcpyHostToDevice, s)) != cudaSuccess) {
       rc = cuda_fail(a->ctx, e, "copy rays in");
-    } else if ((e = skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, dr, m, nullptr, a->scene_abs,
-                                          nullptr, dout, a->d_status, s, ctas, d_work + 64 * si)) !=
-               cudaSuccess) {
+    } else if ((e = dray ? skw::launch_traversal_d(closest, a->stack_cap, a->d_nodes, a->d_tris, dr, m, a->scene_abs,
+                                                   dout, a->d_status, s, d_work + 64 * si)
+                         : skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, dr, m, nullptr,
+                                                 a->scene_abs, nullptr, dout, a->d_status, s, ctas,
+                                                 d_work + 64 * si)) != cudaSuccess) {
       rc = cuda_fail(a->ctx, e, "launch");
     } else {
       a->ctx->launches.fetch_add(1);
@@ -358,11 +371,19 @@ static int run_query_host(skw_accel *a, bool closest, const skw_ray *rays, int64
 }
 
 int skw_intersect_host(skw_accel *a, const skw_ray *rays, int64_t n, skw_hit *hits) {
-  return run_query_host(a, true, rays, n, hits);
+  return run_query_host(a, true, false, rays, n, hits);
 }
 
 int skw_intersect_test_host(skw_accel *a, const skw_ray *rays, int64_t n, uint8_t *occluded) {
-  return run_query_host(a, false, rays, n, occluded);
+  return run_query_host(a, false, false, rays, n, occluded);
+}
+
+int skw_intersect_d_host(skw_accel *a, const skw_ray_d *rays, int64_t n, skw_hit_d *hits) {
+  return run_query_host(a, true, true, rays, n, hits);
+}
+
+int skw_intersect_test_d_host(skw_accel *a, const skw_ray_d *rays, int64_t n, uint8_t *occluded) {
+  return run_query_host(a, false, true, rays, n, occluded);
 }
 
 }  // extern "C"

@@ -78,6 +78,22 @@ void xform_normal(const double *inv, const float *n, float *out) {
   for (int k = 0; k < 3; ++k) out[k] = (float)(l > 0 ? v[k] / l : v[k]);
 }
 
+// Vector3D<float>::Normalized (Math/Vector3D.h:259-276), as TriangleMesh
+// stores its shading normals (TriangleMesh.cpp:208-213): the squared length
+// and its square root in float, the reciprocal in double, each coordinate
+// times it rounded to float.
+void ref_normalize_f(const float *n, float *out) {
+  const float l2 = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+  if (!(l2 > 0.0f)) {
+    out[0] = n[0];
+    out[1] = n[1];
+    out[2] = n[2];
+    return;
+  }
+  const double inv = 1.0 / (double)std::sqrt(l2);
+  for (int k = 0; k < 3; ++k) out[k] = (float)((double)n[k] * inv);
+}
+
 bool inverse3(const double *m4, double *inv) {
   const double a = m4[0], b = m4[1], c = m4[2], d = m4[4], e = m4[5], f = m4[6], g = m4[8], h = m4[9], i = m4[10];
   const double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
@@ -129,7 +145,8 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
   // Mesh-order geometry.
   std::vector<float> vpos, vnrm, albedo;
   std::vector<int32_t> tri_vidx, prim_tri_offset((size_t)std::max(n_prims, 1)), prim_material((size_t)std::max(n_prims, 1)),
-      prim_light((size_t)std::max(n_prims, 1), -1), prim_has_normals((size_t)std::max(n_prims, 1), 0);
+      prim_light((size_t)std::max(n_prims, 1), -1), prim_has_normals((size_t)std::max(n_prims, 1), 0),
+      prim_xform((size_t)std::max(n_prims, 1), 0);
   // Per-triangle albedo is always present (NaN = the material's kd) so that
   // skw_scene_set_triangle_albedo can replace it.
   bool any_albedo = true, any_normals = false;
@@ -144,6 +161,7 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
     prim_tri_offset[(size_t)p] = tri_count;
     prim_material[(size_t)p] = prims[p].material;
     prim_has_normals[(size_t)p] = prims[p].vertex_normals ? 1 : 0;
+    prim_xform[(size_t)p] = prims[p].mesh_to_world ? 1 : 0;
     double inv[9];
     const bool has_inv = prims[p].mesh_to_world && inverse3(prims[p].mesh_to_world, inv);
     for (int64_t v = 0; v < m.n_vertices; ++v) {
@@ -152,7 +170,13 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
       vpos.insert(vpos.end(), w, w + 3);
       if (any_normals) {
         float nn[3] = {0, 0, 1};
-        if (prims[p].vertex_normals) xform_normal(has_inv ? inv : nullptr, prims[p].vertex_normals + 3 * v, nn);
+        if (prims[p].vertex_normals) {
+          ref_normalize_f(prims[p].vertex_normals + 3 * v, nn);  // the mesh's stored normal
+          if (has_inv) {
+            const float mn[3] = {nn[0], nn[1], nn[2]};
+            xform_normal(inv, mn, nn);
+          }
+        }
         vnrm.insert(vnrm.end(), nn, nn + 3);
       }
     }
@@ -291,8 +315,40 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
       pls[(size_t)i].position[k] = point_lights[i].position[k];
       pls[(size_t)i].intensity[k] = point_lights[i].intensity[k];
     }
+  // The accelerator leaf of every light triangle (its box and slot range).
+  std::vector<float> light_leaf(8 * std::max<size_t>(light_tri.size(), 1), 0.0f);
+  {
+    const std::vector<skw::DevNode> &nodes = s->accel->h_nodes;
+    const std::vector<skw::DevTri> &slots = s->accel->h_tris;
+    std::vector<int32_t> leaf_of_slot(slots.size(), -1), slot_of_tri((size_t)std::max(tri_count, 1), -1);
+    for (size_t n = 0; n < nodes.size(); ++n)
+      if ((nodes[n].b & 3u) == 0u)
+        for (uint32_t k = 0; k < (nodes[n].b >> 8); ++k) leaf_of_slot[nodes[n].a + k] = (int32_t)n;
+    for (size_t k = 0; k < slots.size(); ++k)
+      slot_of_tri[(size_t)(prim_tri_offset[(size_t)slots[k].prim] + slots[k].tri)] = (int32_t)k;
+    for (size_t j = 0; j < light_tri.size(); ++j) {
+      const int32_t slot = slot_of_tri[(size_t)light_tri[j]];
+      const int32_t leaf = slot >= 0 ? leaf_of_slot[(size_t)slot] : -1;
+      float *o = light_leaf.data() + 8 * j;
+      if (leaf < 0) {  // cannot happen for a triangle the tree holds; an empty range tests nothing
+        o[0] = o[1] = o[2] = INFINITY;
+        o[3] = o[4] = o[5] = -INFINITY;
+        continue;
+      }
+      const skw::DevNode &L = nodes[(size_t)leaf];
+      for (int c = 0; c < 3; ++c) {
+        o[c] = L.lo[c];
+        o[3 + c] = L.hi[c];
+      }
+      const int32_t first = (int32_t)L.a, count = (int32_t)(L.b >> 8);
+      std::memcpy(o + 6, &first, 4);
+      std::memcpy(o + 7, &count, 4);
+    }
+  }
   cudaError_t e = cudaSetDevice(ctx->device);
   skw::SceneDev &D = s->dev;
+  D.accel_tris = (const float4 *)s->accel->d_tris;
+  if (e == cudaSuccess) e = upload(s, light_leaf, &D.light_leaf);
   if (e == cudaSuccess) e = upload(s, vpos, &D.vpos);
   if (e == cudaSuccess) e = upload(s, vnrm, &D.vnrm);
   if (e == cudaSuccess) e = upload(s, tri_vidx, &D.tri_vidx);
@@ -301,6 +357,7 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
   if (e == cudaSuccess) e = upload(s, prim_material, &D.prim_material);
   if (e == cudaSuccess) e = upload(s, prim_light, &D.prim_light);
   if (e == cudaSuccess) e = upload(s, prim_has_normals, &D.prim_has_normals);
+  if (e == cudaSuccess) e = upload(s, prim_xform, &D.prim_xform);
   if (e == cudaSuccess) e = upload(s, mats, &D.materials);
   if (e == cudaSuccess) e = upload(s, lights, &D.area_lights);
   if (e == cudaSuccess) e = upload(s, light_tri, &D.light_tri);
@@ -1304,6 +1361,40 @@ int skw_scene_hit_geometry(skw_scene *s, const skw_ray *rays, const skw_hit *hit
   cudaError_t e = cudaSetDevice(s->ctx->device);
   if (e == cudaSuccess) e = skw::launch_hit_geometry(s->dev, rays, hits, n, (double *)out, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "hit geometry");
+  s->ctx->launches.fetch_add(n > 0 ? 1 : 0);
+  return SKW_OK;
+}
+
+int skw_scene_intersection(skw_scene *s, const skw_ray_differential *rays, const skw_hit_d *hits, int64_t n,
+                           skw_intersection *out, void *stream) {
+  if (!s) return SKW_ERR_ARG;
+  if (n < 0 || n > (int64_t)INT32_MAX || (n > 0 && (!rays || !hits || !out)))
+    return fail(s->ctx, SKW_ERR_ARG, "bad intersection buffers");
+  static_assert(sizeof(skw_ray_differential) == 21 * sizeof(double), "skw_ray_differential layout");
+  static_assert(sizeof(skw_intersection) == 36 * sizeof(double), "skw_intersection layout");
+  static_assert(sizeof(skw_hit_d) == 16, "skw_hit_d layout");
+  cudaError_t e = cudaSetDevice(s->ctx->device);
+  if (e == cudaSuccess) e = skw::launch_intersection(s->dev, rays, hits, n, (double *)out, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(s->ctx, e, "intersection");
+  s->ctx->launches.fetch_add(n > 0 ? 1 : 0);
+  return SKW_OK;
+}
+
+double skw_next_min_t(const skw_intersection *isect, const double *direction) {
+  if (!isect || !direction) return 0.0;
+  const double div = direction[0] * isect->cross[0] + direction[1] * isect->cross[1] + direction[2] * isect->cross[2];
+  if (div == 0.0) return 0.0;
+  return std::max(0.0, isect->dot * (1.0 / div) + 1e-14);
+}
+
+int skw_scene_next_rays(skw_scene *s, const skw_ray *rays, const skw_hit *hits, const float *directions, int64_t n,
+                        skw_ray *out, void *stream) {
+  if (!s) return SKW_ERR_ARG;
+  if (n < 0 || n > (int64_t)INT32_MAX || (n > 0 && (!rays || !hits || !directions || !out)))
+    return fail(s->ctx, SKW_ERR_ARG, "bad outgoing-ray buffers");
+  cudaError_t e = cudaSetDevice(s->ctx->device);
+  if (e == cudaSuccess) e = skw::launch_next_rays(s->dev, rays, hits, directions, n, out, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(s->ctx, e, "outgoing rays");
   s->ctx->launches.fetch_add(n > 0 ? 1 : 0);
   return SKW_OK;
 }

@@ -140,12 +140,23 @@ __device__ __forceinline__ int tri_test32(const RayF &r, float3 v0, float3 v1, f
   return kAmbiguous;
 }
 
+// A ray given in double (skw_ray_d): origin, direction, tmin, tmax.
+struct RayD {
+  double ox, oy, oz, dx, dy, dz, tmin, tmax;
+};
+
+__device__ __forceinline__ RayD load_ray_d(const float4 *__restrict__ rays, int64_t i) {
+  const double2 *p = reinterpret_cast<const double2 *>(rays) + 4 * i;
+  const double2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3);
+  return RayD{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y};
+}
+
 // The reference's double-precision Moller-Trumbore test, operation by
 // operation (TriangleAccelerator.cpp:240-273).  Intrinsics keep every
 // product and sum separately rounded, as in the x86-64 SSE2 build.
-__device__ __forceinline__ bool tri_test64(const RayF &r, float3 v0f, float3 v1f, float3 v2f, double tmin, double tmax,
-                                        double &t_out) {
-  const double ox = r.ox, oy = r.oy, oz = r.oz, dx = r.dx, dy = r.dy, dz = r.dz;
+__device__ __forceinline__ bool tri_test64v(double ox, double oy, double oz, double dx, double dy, double dz,
+                                            float3 v0f, float3 v1f, float3 v2f, double tmin, double tmax,
+                                            double &t_out) {
   const double v0x = v0f.x, v0y = v0f.y, v0z = v0f.z;
   const double e1x = __dsub_rn((double)v1f.x, v0x), e1y = __dsub_rn((double)v1f.y, v0y),
                e1z = __dsub_rn((double)v1f.z, v0z);
@@ -175,6 +186,12 @@ __device__ __forceinline__ bool tri_test64(const RayF &r, float3 v0f, float3 v1f
     }
   }
   return false;
+}
+
+// The same test for a float ray widened exactly to double.
+__device__ __forceinline__ bool tri_test64(const RayF &r, float3 v0f, float3 v1f, float3 v2f, double tmin, double tmax,
+                                        double &t_out) {
+  return tri_test64v(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, v0f, v1f, v2f, tmin, tmax, t_out);
 }
 
 __device__ __forceinline__ void load_tri(const float4 *__restrict__ tris, uint32_t slot, float3 &v0, float3 &v1,
@@ -209,12 +226,15 @@ struct SlabRay {
   uint32_t bits;
 };
 
-__device__ __forceinline__ SlabRay make_slab_ray(const RayF &r, float scene_abs) {
+// widen_u: the widening in units of u -- 6 for a float ray; 9 for a double
+// ray rounded to float, whose rounding moves a plane distance by at most
+// u |o| |1/d| (origin) + u |b - o| |1/d| (direction) more.
+__device__ __forceinline__ SlabRay make_slab_ray(const RayF &r, float scene_abs, float widen_u = 6.0f) {
   SlabRay s;
   s.ix = 1.0f / r.dx;
   s.iy = 1.0f / r.dy;
   s.iz = 1.0f / r.dz;
-  const float c = 6.0f * 5.9604645e-8f;
+  const float c = widen_u * 5.9604645e-8f;
   const float wx = c * (scene_abs + fabsf(r.ox)) * fabsf(s.ix);
   const float wy = c * (scene_abs + fabsf(r.oy)) * fabsf(s.iy);
   const float wz = c * (scene_abs + fabsf(r.oz)) * fabsf(s.iz);
@@ -503,11 +523,21 @@ __device__ __forceinline__ void store_result(void *__restrict__ out, const int32
 // float interval [lo_t, hi_t] that contains the reference's current tmax
 // (the best hit's double t).  Where a decision needs that tmax exactly, it is
 // recomputed from the slot with the exact test.
-template <int CAP, bool CLOSEST>
+//
+// DRAY: the rays are skw_ray_d (double).  The walk runs on the ray rounded
+// to float (origin and direction to nearest, tmin down, tmax up) with the
+// slab widening of make_slab_ray for rounded rays, so a node is still
+// culled only if the reference culls it; every triangle of a reached leaf
+// is tested with the reference's double arithmetic on the double ray
+// (reloaded from memory for the leaf), and the current tmax is kept as the
+// exact double t of the best hit.  Closest-hit results are skw_hit_d
+// (double t, prim, tri).
+template <int CAP, bool CLOSEST, bool DRAY>
 __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, const float4 *__restrict__ rays,
             int n, const int *__restrict__ n_dev, float scene_abs, const int32_t *__restrict__ out_index,
             void *__restrict__ out, unsigned *__restrict__ status, int *__restrict__ work) {
+  static_assert(!DRAY || SKW_TRAV_POSTPONE, "double rays use the postponed-leaf walk");
   if (n_dev) n = min(n, *n_dev);  // a queue whose length lives on the device
   constexpr int SCAP = Stack<CAP>::SCAP;
   __shared__ uint32_t s_a[SCAP][SKW_TRAV_BLOCK];
@@ -556,6 +586,7 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
   SlabRay s{};
   uint32_t cur_a = 0, cur_b = 0;
   int best_slot = -1;
+  double best_t = 0.0;             // DRAY: the exact t of the best hit
   float lo_t = 0.0f, hi_t = 0.0f;  // bracket of the reference's current tmax
   uint32_t flags = 0;              // SKW_HIT_* bits; bit 3: [lo_t, hi_t] brackets an exact double
 #if SKW_TRAV_POSTPONE
@@ -580,7 +611,14 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
       const int idx = work ? gbase + mine : ((warp + (mine >> 5) * n_warps) << 5) + (mine & 31);
       if (ray_i < 0 && mine < end && idx < n) {
         ray_i = idx;
-        const RayF rl = load_ray(rays, ray_i);
+        RayF rl;
+        if (DRAY) {
+          const RayD rd = load_ray_d(rays, ray_i);
+          rl = RayF{(float)rd.ox, (float)rd.oy, (float)rd.oz, (float)rd.dx, (float)rd.dy, (float)rd.dz,
+                    __double2float_rd(rd.tmin), __double2float_ru(rd.tmax)};
+        } else {
+          rl = load_ray(rays, ray_i);
+        }
 #if SKW_TRAV_RAYSMEM
         s_ray[0][threadIdx.x] = rl.ox;
         s_ray[1][threadIdx.x] = rl.oy;
@@ -593,7 +631,7 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
 #else
         r_reg = rl;
 #endif
-        s = make_slab_ray(rl, scene_abs);
+        s = make_slab_ray(rl, scene_abs, DRAY ? 9.0f : 6.0f);
         best_slot = -1;
         lo_t = hi_t = rl.tmax;
         flags = 8u;
@@ -603,7 +641,11 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
         cur_a = __float_as_uint(nb.z);
         cur_b = __float_as_uint(nb.w);
         if (!node_visit(na, nb, s, rl.tmax, lo)) {  // root culled: a miss
-          store_result<CLOSEST>(out, out_index, ray_i, make_int4(0x7f800000, -1, -1, 0), false);
+          if (DRAY && CLOSEST) {
+            ((int4 *)out)[out_index ? out_index[ray_i] : ray_i] = make_int4(0, 0x7ff00000, -1, -1);
+          } else {
+            store_result<CLOSEST>(out, out_index, ray_i, make_int4(0x7f800000, -1, -1, 0), false);
+          }
           ray_i = -1;
         }
 #if SKW_TRAV_POSTPONE
@@ -665,7 +707,31 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     }
     __syncwarp(busy);
     bool hit = false;
-    if (has_post) {
+    if (DRAY && has_post) {
+      // every triangle of the leaf in the reference's double arithmetic
+      has_post = false;
+      const RayD rd = load_ray_d(rays, ray_i);
+      for (uint32_t k = 0; k < post_cnt; ++k) {
+        const int slot = (int)(post_a + k);
+        float3 v0, v1, v2;
+        int prim, tri;
+        load_tri(tris, (uint32_t)slot, v0, v1, v2, prim, tri);
+        double t64;
+        if (tri_test64v(rd.ox, rd.oy, rd.oz, rd.dx, rd.dy, rd.dz, v0, v1, v2, rd.tmin,
+                        CLOSEST && best_slot >= 0 ? best_t : rd.tmax, t64)) {
+          if (!CLOSEST) {
+            hit = true;
+            break;
+          }
+          if (best_slot >= 0 && fabs(t64 - best_t) <= 1e-12 * fabs(t64)) flags |= 2u;
+          best_slot = slot;
+          best_t = t64;
+          lo_t = __double2float_rd(t64);
+          hi_t = __double2float_ru(t64);
+        }
+      }
+    }
+    if (!DRAY && has_post) {
       has_post = false;
       const RayF r = SKW_RAY();
       const uint32_t a = post_a, cnt = post_cnt;
@@ -770,7 +836,20 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
       done = hit || !st.pop(CLOSEST ? hi_t : s.tmax, cur_a, cur_b);
     }
 #endif
-    if (done) {
+    if (DRAY && done) {
+      if (CLOSEST) {
+        int4 h = make_int4(0, 0x7ff00000, -1, -1);  // t = +inf, a miss
+        if (best_slot >= 0) {
+          const float4 ta = __ldg(tris + 3 * best_slot), tb = __ldg(tris + 3 * best_slot + 1);
+          const long long tb64 = __double_as_longlong(best_t);
+          h = make_int4((int)(tb64 & 0xffffffffll), (int)(tb64 >> 32), __float_as_int(ta.w), __float_as_int(tb.w));
+        }
+        ((int4 *)out)[out_index ? out_index[ray_i] : ray_i] = h;
+      } else {
+        store_result<CLOSEST>(out, out_index, ray_i, int4{}, hit);
+      }
+      ray_i = -1;
+    } else if (done) {
       int4 h = make_int4(0x7f800000, -1, -1, (int)(flags & 7u));
       if (CLOSEST && best_slot >= 0) {
         const float4 ta = __ldg(tris + 3 * best_slot), tb = __ldg(tris + 3 * best_slot + 1);
@@ -804,33 +883,41 @@ cudaError_t current_device(int &dev) {
   return dev < 0 || dev >= kMaxDevices ? cudaErrorInvalidDevice : cudaSuccess;
 }
 
-// Resident CTAs per SM of k_trace<CAP, closest> on each device (0 = not yet known).
+// The kernel of a variant: bit 0 closest hit, bit 1 double rays.
 template <int CAP>
-std::atomic<int> &cap_occupancy(int dev, bool closest) {
-  static std::atomic<int> blocks_per_sm[kMaxDevices][2];
-  return blocks_per_sm[dev][closest ? 1 : 0];
+const void *trace_kernel(int variant) {
+  switch (variant) {
+    case 0: return (const void *)k_trace<CAP, false, false>;
+    case 1: return (const void *)k_trace<CAP, true, false>;
+    case 2: return (const void *)k_trace<CAP, false, true>;
+    default: return (const void *)k_trace<CAP, true, true>;
+  }
+}
+
+// Resident CTAs per SM of each variant on each device (0 = not yet known).
+template <int CAP>
+std::atomic<int> &cap_occupancy(int dev, int variant) {
+  static std::atomic<int> blocks_per_sm[kMaxDevices][4];
+  return blocks_per_sm[dev][variant];
 }
 
 template <int CAP>
 cudaError_t cap_prepare(int dev) {
-  if (cap_occupancy<CAP>(dev, true).load(std::memory_order_acquire) != 0 &&
-      cap_occupancy<CAP>(dev, false).load(std::memory_order_acquire) != 0)
-    return cudaSuccess;
+  bool known = true;
+  for (int v = 0; v < 4; ++v) known = known && cap_occupancy<CAP>(dev, v).load(std::memory_order_acquire) != 0;
+  if (known) return cudaSuccess;
   std::lock_guard<std::mutex> lock(prepare_mutex());
-  for (int which = 0; which < 2; ++which) {
-    std::atomic<int> &slot = cap_occupancy<CAP>(dev, which == 1);
+  for (int v = 0; v < 4; ++v) {
+    std::atomic<int> &slot = cap_occupancy<CAP>(dev, v);
     if (slot.load(std::memory_order_relaxed) != 0) continue;
     cudaError_t e;
     if (SKW_TRAV_CARVEOUT >= 0) {
-      e = which ? cudaFuncSetAttribute(k_trace<CAP, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                       SKW_TRAV_CARVEOUT)
-                : cudaFuncSetAttribute(k_trace<CAP, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                       SKW_TRAV_CARVEOUT);
+      e = cudaFuncSetAttribute(trace_kernel<CAP>(v), cudaFuncAttributePreferredSharedMemoryCarveout,
+                               SKW_TRAV_CARVEOUT);
       if (e != cudaSuccess) return e;
     }
     int occ = 0;
-    e = which ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<CAP, true>, SKW_TRAV_BLOCK, 0)
-              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<CAP, false>, SKW_TRAV_BLOCK, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trace_kernel<CAP>(v), SKW_TRAV_BLOCK, 0);
     if (e != cudaSuccess) return e;
     slot.store(occ < 1 ? 1 : occ, std::memory_order_release);
   }
@@ -849,14 +936,14 @@ cudaError_t device_sms(int dev, int &sms) {
 }
 
 template <int CAP>
-cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const void *rays, int64_t n,
+cudaError_t launch_cap(int variant, const void *nodes, const void *tris, const void *rays, int64_t n,
                        const int *n_dev, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
                        cudaStream_t stream, int ctas_per_sm, int *work) {
   int dev = 0, sms = 0;
   cudaError_t e = current_device(dev);
   if (e != cudaSuccess || (e = cap_prepare<CAP>(dev)) != cudaSuccess || (e = device_sms(dev, sms)) != cudaSuccess)
     return e;
-  int per_sm = cap_occupancy<CAP>(dev, closest).load(std::memory_order_acquire);
+  int per_sm = cap_occupancy<CAP>(dev, variant).load(std::memory_order_acquire);
   if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
   const int64_t warps_per_block = SKW_TRAV_BLOCK / 32;
   int64_t blocks = (int64_t)per_sm * sms;
@@ -865,16 +952,46 @@ cudaError_t launch_cap(bool closest, const void *nodes, const void *tris, const 
   // every warp draws at most one group past the end: keep the counter in int range
   if (n > (int64_t)INT32_MAX - 32 * warps_per_block * blocks) work = nullptr;
   if (work && (e = cudaMemsetAsync(work, 0, sizeof(int), stream)) != cudaSuccess) return e;
-  if (closest) {
-    k_trace<CAP, true><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
-        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, n_dev, scene_abs, out_index, out, status,
-        work);
-  } else {
-    k_trace<CAP, false><<<(unsigned)blocks, SKW_TRAV_BLOCK, 0, stream>>>(
-        (const float4 *)nodes, (const float4 *)tris, (const float4 *)rays, (int)n, n_dev, scene_abs, out_index, out, status,
-        work);
+  const float4 *nd = (const float4 *)nodes, *tr = (const float4 *)tris, *ry = (const float4 *)rays;
+  const dim3 grid((unsigned)blocks), block(SKW_TRAV_BLOCK);
+  switch (variant) {
+    case 0:
+      k_trace<CAP, false, false><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
+                                                             status, work);
+      break;
+    case 1:
+      k_trace<CAP, true, false><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
+                                                            status, work);
+      break;
+    case 2:
+      k_trace<CAP, false, true><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
+                                                            status, work);
+      break;
+    default:
+      k_trace<CAP, true, true><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
+                                                           status, work);
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_variant(int variant, int stack_cap, const void *nodes, const void *tris, const void *rays,
+                           int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
+                           unsigned *status, cudaStream_t stream, int ctas_per_sm, int *work) {
+  if (n <= 0) return cudaSuccess;
+  switch (stack_cap) {
+    case 48:
+      return launch_cap<48>(variant, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream,
+                            ctas_per_sm, work);
+    case 96:
+      return launch_cap<96>(variant, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream,
+                            ctas_per_sm, work);
+    case 192:
+      return launch_cap<192>(variant, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream,
+                             ctas_per_sm, work);
+    default:
+      return launch_cap<416>(variant, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream,
+                             ctas_per_sm, work);
+  }
 }
 
 }  // namespace
@@ -895,10 +1012,10 @@ int traversal_max_ctas_per_sm(int stack_cap) {
   int dev = 0;
   if (current_device(dev) != cudaSuccess || prepare_traversal(stack_cap) != cudaSuccess) return 1;
   switch (stack_cap) {
-    case 48: return cap_occupancy<48>(dev, true).load();
-    case 96: return cap_occupancy<96>(dev, true).load();
-    case 192: return cap_occupancy<192>(dev, true).load();
-    default: return cap_occupancy<416>(dev, true).load();
+    case 48: return cap_occupancy<48>(dev, 1).load();
+    case 96: return cap_occupancy<96>(dev, 1).load();
+    case 192: return cap_occupancy<192>(dev, 1).load();
+    default: return cap_occupancy<416>(dev, 1).load();
   }
 }
 
@@ -913,17 +1030,15 @@ int traversal_stack_capacity(int max_depth) {
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
                              int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
                              unsigned *status, cudaStream_t stream, int ctas_per_sm, int *work) {
-  if (n <= 0) return cudaSuccess;
-  switch (stack_cap) {
-    case 48:
-      return launch_cap<48>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm, work);
-    case 96:
-      return launch_cap<96>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm, work);
-    case 192:
-      return launch_cap<192>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm, work);
-    default:
-      return launch_cap<416>(closest, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream, ctas_per_sm, work);
-  }
+  return launch_variant(closest ? 1 : 0, stack_cap, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status,
+                        stream, ctas_per_sm, work);
+}
+
+cudaError_t launch_traversal_d(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
+                               int64_t n, float scene_abs, void *out, unsigned *status, cudaStream_t stream,
+                               int *work) {
+  return launch_variant(closest ? 3 : 2, stack_cap, nodes, tris, rays, n, nullptr, scene_abs, nullptr, out, status,
+                        stream, 0, work);
 }
 
 }  // namespace skw

@@ -247,6 +247,52 @@ class RenderScene:
                                                       out.data_ptr(), s), self.ctx.handle)
         return out
 
+    def accelerator(self):
+        """The scene's own accelerator (skw_scene_accel; owned by the scene)
+        for ray queries on the scene's primitives."""
+        from .accel import TriangleAccelerator
+        a = TriangleAccelerator.__new__(TriangleAccelerator)
+        a.ctx, a.primitives, a._owner = self.ctx, self.prims, self
+        a.handle = C.c_void_p(_lib.load().skw_scene_accel(self.handle))
+        a._borrowed = True
+        return a
+
+    def intersection(self, rays_d, hits_d, diffs=None, stream=None):
+        """The whole Intersection of closest hits (skw_scene_intersection):
+        rays_d (n, 8) float64 CUDA tensor of double rays, hits_d the (n, 2)
+        float64 skw_hit_d records skw_intersect_d returned for them on this
+        scene's accelerator, diffs (optional) (n, 12) float64: origin_dx,
+        direction_dx, origin_dy, direction_dy.  Returns an (n, 36) float64
+        CUDA tensor in skw_intersection layout: point, geometric normal,
+        shading normal, uv, point_dx, point_dy, normal_dx, normal_dy, duv_dx,
+        duv_dy, tangent, cross, dot, t, then prim and tri as int32 bits."""
+        import torch
+        n = rays_d.shape[0]
+        rd = torch.zeros((n, 21), dtype=torch.float64, device=rays_d.device)
+        rd[:, :8] = rays_d
+        if diffs is not None:
+            rd[:, 8:20] = diffs
+            rd[:, 20] = torch.tensor([1], dtype=torch.int64).view(torch.float64).item()
+        out = torch.empty((n, 36), dtype=torch.float64, device=rays_d.device)
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _lib.check(_lib.load().skw_scene_intersection(self.handle, rd.data_ptr(), hits_d.data_ptr(), n,
+                                                      out.data_ptr(), s), self.ctx.handle)
+        return out
+
+    def next_rays(self, rays, hits, directions, stream=None):
+        """Outgoing rays as the renders make them (skw_scene_next_rays): from
+        the float hit points of closest hits (rays (n, 8) float32, hits (n, 4)
+        int32 from skw_intersect on this scene's accelerator) in the given
+        (n, 3) float32 directions, tmin = GetNextMinT.  (n, 8) float32."""
+        import torch
+        n = rays.shape[0]
+        out = torch.empty((n, 8), dtype=torch.float32, device=rays.device)
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        d = directions.contiguous()
+        _lib.check(_lib.load().skw_scene_next_rays(self.handle, rays.data_ptr(), hits.data_ptr(), d.data_ptr(), n,
+                                                   out.data_ptr(), s), self.ctx.handle)
+        return out
+
     def set_max_specular_depth(self, depth: int) -> None:
         """DirectLightingLTEIntegratorParams::m_max_specular_depth (default 10, at most 11)."""
         _lib.check(_lib.load().skw_scene_set_max_specular_depth(self.handle, int(depth)), self.ctx.handle)

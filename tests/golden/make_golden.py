@@ -226,3 +226,29 @@ def ld_golden():
 
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "ld":
     ld_golden()
+
+
+def c1_golden():
+    """The plain direct-lighting configuration at its own size: the box at
+    256 x 256 rendered by the reference's SamplerBasedRenderer with 2x2
+    stratified samples (the configuration's 4 spp) and with 16x16 (the
+    comparison image, stored as float16).  The 2x2 image itself is not
+    stored, only its mean relative error against the 16x16 image, its mean
+    luminance and its 8x8-block mean luminances."""
+    from skwarka_gb300 import scenes
+    prims, mats, cam = scenes.direct_lighting_box()
+    c = cam(256, 256)
+    ref = Reference()
+    lo, t_lo = ref.render_direct(prims, mats, [], c, 2, 2)
+    hi, t_hi = ref.render_direct(prims, mats, [], c, 16, 16)
+    lum = np.array([0.05316285, 0.58515348, 0.36168367])
+    lh, ll = hi @ lum, lo @ lum
+    mre = float(np.mean(np.abs(ll - lh) / np.maximum(lh, 1e-3 * lh.mean())))
+    blocks = ll.reshape(32, 8, 32, 8).mean(axis=(1, 3)).astype(np.float32)
+    np.savez_compressed(OUT / "direct_box_256.npz", ref_16x16=hi.astype(np.float16), ref_2x2_mre=mre,
+                        ref_2x2_mean=float(ll.mean()), ref_2x2_blocks=blocks, seconds=np.array([t_lo, t_hi]))
+    print(f"c1: reference 2x2 MRE {mre:.4f}; render seconds {t_lo:.2f} / {t_hi:.2f}")
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "c1":
+    c1_golden()

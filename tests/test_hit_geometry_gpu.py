@@ -52,11 +52,13 @@ def _expected(prims, rays, hits):
         ng = normalized(np.cross(e1, e2))
         ns = ng
         if prims[h[1]].vertex_normals is not None:
-            # the scene stores each vertex normal normalised in double, then
-            # rounded to float (Transform::TransformNormal)
-            n = prims[h[1]].vertex_normals.astype(np.float64)
-            n = (n / np.sqrt((n[:, 0] * n[:, 0] + n[:, 1] * n[:, 1]) + n[:, 2] * n[:, 2])[:, None])
-            n = n.astype(np.float32).astype(np.float64)
+            # the mesh stores each vertex normal as Vector3D<float>::Normalized
+            # makes it: squared length and root in float, the double
+            # reciprocal, each coordinate times it rounded to float
+            n = prims[h[1]].vertex_normals.astype(np.float32)
+            l2 = (n[:, 0] * n[:, 0] + n[:, 1] * n[:, 1]) + n[:, 2] * n[:, 2]
+            inv = 1.0 / np.sqrt(l2).astype(np.float64)
+            n = (n.astype(np.float64) * inv[:, None]).astype(np.float32).astype(np.float64)
             b0 = (1.0 - b1) - b2
             ns = normalized((n[tri[0]] * b0 + n[tri[1]] * b1) + n[tri[2]] * b2)
         out[i] = np.concatenate([p, ng, ns, [b1, b2, t]])

@@ -1,20 +1,19 @@
 """Homogeneous participating medium (HomogeneousVolumeRegion + HG phase,
 DirectLightingLTEIntegrator's single-scattering march) on the GPU against
 the reference's renders (tests/golden/medium_32.npz, 16x16 spp): mean
-luminance within 2 % and 8x8 blocks within 5 %; a zero-density medium
-renders exactly like no medium; and the adjoint with a medium against finite
-differences.
+luminance within 2 % and 8x8 blocks within 5 % for every case, including
+in-scattering from an area light; a zero-density medium renders exactly like
+no medium; and the adjoint with a medium against finite differences.
 
-In-scattering from AREA lights is the one known difference: the reference's
-march samples the light with a shadow ray that ends exactly on the light
-(DiffuseAreaLightSource::SampleLighting, DiffuseAreaLightSource.cpp:87-90,
-tested as is in DirectLightingLTEIntegrator.cpp:149, without the 1e-4
-pull-back of the surface path), so the light's own triangle occludes it
-whenever double rounding puts the hit at t <= length -- about a third of the
-samples in the box scene.  This build's float ray decides that boundary by
-its own rounding and rarely occludes, so its area-light in-scattering is
-larger; the test below bounds the difference by the reference's own
-in-scattering and checks the attenuated surface part exactly as above."""
+In-scattering from AREA lights depends on a double-rounding outcome: the
+reference's march samples the light with a shadow ray that ends exactly on
+the light (DiffuseAreaLightSource::SampleLighting, DiffuseAreaLightSource.cpp:
+87-90, tested as is in DirectLightingLTEIntegrator.cpp:149, without the
+1e-4 pull-back of the surface path), so the light's own triangle occludes
+the sample whenever the double slab test and Moller-Trumbore t put the hit
+inside [0, length] -- about a third of the samples in the box scene.  The
+GPU march restates that decision in double for the light's own leaf, so
+the box-with-area-light case is held to the same bounds as the others."""
 from pathlib import Path
 
 import numpy as np
@@ -28,7 +27,7 @@ GOLD = Path(__file__).resolve().parent / "golden" / "medium_32.npz"
 LUM = np.array([0.05316285, 0.58515348, 0.36168367])
 
 
-@pytest.mark.parametrize("name", ["point_scatter", "point_emit", "box_absorb"])
+@pytest.mark.parametrize("name", ["point_scatter", "point_emit", "box_absorb", "box_area"])
 def test_medium_matches_reference(gpu, name):
     prims, mats, lights, cam, med = sf.medium_cases()[name]
     ref = np.load(GOLD)[name]
@@ -42,15 +41,19 @@ def test_medium_matches_reference(gpu, name):
     assert rel.max() <= 0.05
 
 
-def test_area_light_inscattering_bounded(gpu):
+def test_area_light_inscattering_matches_reference(gpu):
+    """The in-scattered part alone (the area-light render minus the absorbing
+    render, same medium without scattering) within 3 % of the reference's:
+    the term the light's self-occlusion decides."""
     prims, mats, lights, cam, med = sf.medium_cases()["box_area"]
     g = np.load(GOLD)
-    ref_full, ref_absorb = float((g["box_area"] @ LUM).mean()), float((g["box_absorb"] @ LUM).mean())
-    img = RenderScene(prims, mats, lights, medium=med).render_direct(cam, 32, 32, seed=4).cpu().numpy()
-    m = float((img @ LUM).mean())
-    ref_in = ref_full - ref_absorb
-    print(f"[medium box_area] gpu {m:.5f} reference {ref_full:.5f} (its in-scattering {ref_in:.5f})")
-    assert ref_full * 0.99 <= m <= ref_full + ref_in
+    ref_in = float((g["box_area"] @ LUM).mean()) - float((g["box_absorb"] @ LUM).mean())
+    _, _, _, cam_a, med_a = sf.medium_cases()["box_absorb"]
+    full = RenderScene(prims, mats, lights, medium=med).render_direct(cam, 32, 32, seed=4).cpu().numpy()
+    absorb = RenderScene(prims, mats, lights, medium=med_a).render_direct(cam_a, 32, 32, seed=4).cpu().numpy()
+    gpu_in = float((full @ LUM).mean()) - float((absorb @ LUM).mean())
+    print(f"[medium box_area] in-scattering gpu {gpu_in:.5f} reference {ref_in:.5f}")
+    assert abs(gpu_in / ref_in - 1) <= 0.03
 
 
 def test_empty_medium_is_no_medium(gpu):

@@ -134,3 +134,24 @@ def test_oracle_nearest_equals_reference(oracle, reference):
     q = rng.uniform(-0.1, 1.1, size=(2000, 3))
     for r in (0.01, 0.05, np.inf):
         assert np.array_equal(ko.nearest(q, None, r), kr.nearest(q, r))
+
+
+def test_oracle_double_rays_match_reference(oracle, reference):
+    """The oracle's traversal of double rays (the reference's own Ray type)
+    equals the reference's Intersect / IntersectTest bit for bit."""
+    import scene_fixtures as sf
+    from skwarka_gb300 import scenes
+    meshes = sf.unit_test_spheres()
+    lo, hi = scenes.scene_bounds(meshes)
+    rng = np.random.default_rng(36)
+    n = 5000
+    rays = np.zeros((n, 8))
+    rays[:, :3] = rng.uniform(lo, hi, size=(n, 3))
+    d = rng.uniform(0, 1, size=(n, 3))
+    rays[:, 3:6] = d / np.sqrt((d * d).sum(1))[:, None]
+    rays[:, 6] = rng.uniform(-10, 10, n)
+    rays[:, 7] = rng.uniform(100, 10000, n)
+    got, want = oracle.accel(meshes).intersect_d(rays), reference.accel(meshes).intersect_d(rays)
+    assert np.array_equal(got["prim"], want["prim"]) and np.array_equal(got["tri"], want["tri"])
+    assert np.array_equal(got["t"].view(np.uint64), want["t"].view(np.uint64))
+    assert np.array_equal(oracle.accel(meshes).intersect_test_d(rays), reference.accel(meshes).intersect_test_d(rays))
