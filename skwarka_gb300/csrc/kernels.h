@@ -22,9 +22,14 @@ int traversal_stack_capacity(int max_depth);
 // ctas_per_sm > 0 caps the persistent grid at that many CTAs per SM (0: as
 // many as fit).  prepare_traversal computes the occupancy of a capacity's
 // kernels ahead of a stream capture.
+// surface: the rays leave surfaces with tmin from next_min_t (an upper bound
+// of the reference's GetNextMinT); a triangle whose t cannot be told apart
+// from tmin in float is then skipped (it lies on the ray's own plane
+// crossing) instead of being decided in double.
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
                              int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
-                             unsigned *status, cudaStream_t stream, int ctas_per_sm = 0, int *work = nullptr);
+                             unsigned *status, cudaStream_t stream, int ctas_per_sm = 0, int *work = nullptr,
+                             bool surface = false);
 // work (may be null): a device int of the caller's, not used by any launch
 // that may run at the same time; it is zeroed on `stream` and the warps
 // then take groups of 32 rays from it as they finish (no idle tail).  Null:

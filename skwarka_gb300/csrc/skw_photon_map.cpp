@@ -312,7 +312,7 @@ int skw_photon_shoot(skw_scene *s, const skw_photon_params *params, skw_photon_m
   skw_accel *a = s->accel;
   skw::TraceFn trace = [a](const void *rays, int64_t n, const int *n_dev, void *hits, cudaStream_t st, int *work) {
     return skw::launch_traversal(true, a->stack_cap, a->d_nodes, a->d_tris, rays, n, n_dev, a->scene_abs, nullptr,
-                                 hits, a->d_status, st, 0, work);
+                                 hits, a->d_status, st, 0, work, true);
   };
   // per-path deposit slots for every bounce: 2^20 paths per chunk up to 64
   // bounces, proportionally fewer above

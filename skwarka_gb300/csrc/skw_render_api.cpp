@@ -644,7 +644,7 @@ cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, con
     }
     if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) return e;
     if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.qrays[qi], cl, W.counts + 3 + qi, a->scene_abs,
-                                   nullptr, W.qhits, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
+                                   nullptr, W.qhits, a->d_status, st, ctas, W.counts + 8, true)) != cudaSuccess)
       return e;
     if (P.media) {
       // The medium along the level's rays (LTEIntegrator::Radiance of each
@@ -679,10 +679,10 @@ cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, con
       return e;
     const int64_t csh = cl * (P.nl + P.npl), cbs = cl * P.nl;
     if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts,
-                                              a->scene_abs, nullptr, W.occ, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
+                                              a->scene_abs, nullptr, W.occ, a->d_status, st, ctas, W.counts + 8, true)) != cudaSuccess)
       return e;
     if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
-                                              a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
+                                              a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas, W.counts + 8, true)) != cudaSuccess)
       return e;
     if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
                                  W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st, true)) !=
@@ -724,10 +724,10 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
     return e;
   const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
   if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts, a->scene_abs,
-                                            nullptr, W.occ, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
+                                            nullptr, W.occ, a->d_status, st, ctas, W.counts + 8, true)) != cudaSuccess)
     return e;
   if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
-                                            a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
+                                            a->scene_abs, nullptr, W.bhits, a->d_status, st, ctas, W.counts + 8, true)) != cudaSuccess)
     return e;
   if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
                                W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st)) != cudaSuccess)
@@ -1153,10 +1153,10 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
       break;
     const int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
     if (csh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts,
-                                              a->scene_abs, nullptr, W.occ, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
+                                              a->scene_abs, nullptr, W.occ, a->d_status, st, 0, W.counts + 8, true)) != cudaSuccess)
       break;
     if (cbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1,
-                                              a->scene_abs, nullptr, W.bhits, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
+                                              a->scene_abs, nullptr, W.bhits, a->d_status, st, 0, W.counts + 8, true)) != cudaSuccess)
       break;
     if ((e = skw::launch_resolve_adjoint(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, s_dkd, s_dem,
                                          W.counts, W.brays, W.bhits, W.btarget, b_dkd, W.brgb, W.counts + 1, W.bnrm,
@@ -1184,7 +1184,7 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
       }
       if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) break;
       if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.qrays[qi], cl, W.counts + 3 + qi,
-                                     a->scene_abs, nullptr, W.qhits, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
+                                     a->scene_abs, nullptr, W.qhits, a->d_status, st, 0, W.counts + 8, true)) != cudaSuccess)
         break;
       if ((e = skw::launch_shade_specular_adjoint(s->dev, d_view, 1, cl, px0, P.spp, P.nl, d_film, g_albedo,
                                                   g_emission, q, L, W.qhits, W.srays, W.starget, s_dkd, s_dem,
@@ -1193,10 +1193,10 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
         break;
       const int64_t lsh = cl * (P.nl + P.npl), lbs = cl * P.nl;
       if (lsh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, lsh, W.counts,
-                                                a->scene_abs, nullptr, W.occ, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
+                                                a->scene_abs, nullptr, W.occ, a->d_status, st, 0, W.counts + 8, true)) != cudaSuccess)
         break;
       if (lbs > 0 && (e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, lbs, W.counts + 1,
-                                                a->scene_abs, nullptr, W.bhits, a->d_status, st, 0, W.counts + 8)) != cudaSuccess)
+                                                a->scene_abs, nullptr, W.bhits, a->d_status, st, 0, W.counts + 8, true)) != cudaSuccess)
         break;
       if ((e = skw::launch_resolve_adjoint(s->dev, (int)std::max(lsh, lbs), P.nl, W.occ, W.starget, s_dkd, s_dem,
                                            W.counts, W.brays, W.bhits, W.btarget, b_dkd, W.brgb, W.counts + 1,
@@ -1284,7 +1284,7 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   skw_accel *a = s->accel;
   skw::TraceFn trace = [a](const void *rays, int64_t n, const int *n_dev, void *hits, cudaStream_t stq, int *work) {
     return skw::launch_traversal(true, a->stack_cap, a->d_nodes, a->d_tris, rays, n, n_dev, a->scene_abs, nullptr,
-                                 hits, a->d_status, stq, 0, work);
+                                 hits, a->d_status, stq, 0, work, true);
   };
   e = cudaMemcpyAsync(d_view, P.views.data(), sizeof(skw::ViewDev), cudaMemcpyHostToDevice, st);
   int64_t launches = 0;

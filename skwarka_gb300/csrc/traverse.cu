@@ -101,6 +101,8 @@ __device__ __forceinline__ RayF load_ray(const float4 *__restrict__ rays, int64_
 // kHit when its barycentric tests and t >= tmin certainly pass (t and a bound
 // et on |t - t_exact| are returned), else kAmbiguous.
 __device__ __forceinline__ int tri_test32(const RayF &r, float3 v0, float3 v1, float3 v2, float &t, float &et) {
+  t = __int_as_float(0x7fffffff);  // NaN until computed
+  et = 0.0f;
   const float e1x = v1.x - v0.x, e1y = v1.y - v0.y, e1z = v1.z - v0.z;
   const float e2x = v2.x - v0.x, e2y = v2.y - v0.y, e2z = v2.z - v0.z;
   const float s1x = r.dy * e2z - r.dz * e2y;
@@ -524,6 +526,9 @@ __device__ __forceinline__ void store_result(void *__restrict__ out, const int32
 // (the best hit's double t).  Where a decision needs that tmax exactly, it is
 // recomputed from the slot with the exact test.
 //
+// surf: the rays leave surfaces with tmin from next_min_t (the renders'
+// shadow, BSDF, specular and gather rays, photon bounces).
+//
 // DRAY: the rays are skw_ray_d (double).  The walk runs on the ray rounded
 // to float (origin and direction to nearest, tmin down, tmax up) with the
 // slab widening of make_slab_ray for rounded rays, so a node is still
@@ -536,7 +541,7 @@ template <int CAP, bool CLOSEST, bool DRAY>
 __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, const float4 *__restrict__ rays,
             int n, const int *__restrict__ n_dev, float scene_abs, const int32_t *__restrict__ out_index,
-            void *__restrict__ out, unsigned *__restrict__ status, int *__restrict__ work) {
+            void *__restrict__ out, unsigned *__restrict__ status, int *__restrict__ work, int surf) {
   static_assert(!DRAY || SKW_TRAV_POSTPONE, "double rays use the postponed-leaf walk");
   if (n_dev) n = min(n, *n_dev);  // a queue whose length lives on the device
   constexpr int SCAP = Stack<CAP>::SCAP;
@@ -743,6 +748,12 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
         float t, et;
         int res = tri_test32(r, v0, v1, v2, t, et);
         if (res == kMiss) continue;
+        // A ray leaving a surface (surf) starts at an upper bound of the
+        // reference's GetNextMinT: a triangle whose t cannot be told apart
+        // from that tmin in float lies on the ray's own plane crossing --
+        // the triangle it leaves, or geometry touching it there -- and is
+        // skipped, as the reference's tmin skips the triangle it leaves.
+        if (surf && res == kAmbiguous && t - et < r.tmin) continue;
         if (CLOSEST) {
           if (res == kHit) {
             if (__fsub_rd(t, et) > hi_t) continue;  // certainly beyond the current tmax
@@ -797,6 +808,12 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
         float t, et;
         int res = tri_test32(r, v0, v1, v2, t, et);
         if (res == kMiss) continue;
+        // A ray leaving a surface (surf) starts at an upper bound of the
+        // reference's GetNextMinT: a triangle whose t cannot be told apart
+        // from that tmin in float lies on the ray's own plane crossing --
+        // the triangle it leaves, or geometry touching it there -- and is
+        // skipped, as the reference's tmin skips the triangle it leaves.
+        if (surf && res == kAmbiguous && t - et < r.tmin) continue;
         if (CLOSEST) {
           if (res == kHit) {
             if (__fsub_rd(t, et) > hi_t) continue;  // certainly beyond the current tmax
@@ -938,7 +955,7 @@ cudaError_t device_sms(int dev, int &sms) {
 template <int CAP>
 cudaError_t launch_cap(int variant, const void *nodes, const void *tris, const void *rays, int64_t n,
                        const int *n_dev, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
-                       cudaStream_t stream, int ctas_per_sm, int *work) {
+                       cudaStream_t stream, int ctas_per_sm, int *work, int surf) {
   int dev = 0, sms = 0;
   cudaError_t e = current_device(dev);
   if (e != cudaSuccess || (e = cap_prepare<CAP>(dev)) != cudaSuccess || (e = device_sms(dev, sms)) != cudaSuccess)
@@ -957,40 +974,40 @@ cudaError_t launch_cap(int variant, const void *nodes, const void *tris, const v
   switch (variant) {
     case 0:
       k_trace<CAP, false, false><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
-                                                             status, work);
+                                                             status, work, surf);
       break;
     case 1:
       k_trace<CAP, true, false><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
-                                                            status, work);
+                                                            status, work, surf);
       break;
     case 2:
       k_trace<CAP, false, true><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
-                                                            status, work);
+                                                            status, work, surf);
       break;
     default:
       k_trace<CAP, true, true><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
-                                                           status, work);
+                                                           status, work, surf);
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_variant(int variant, int stack_cap, const void *nodes, const void *tris, const void *rays,
                            int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
-                           unsigned *status, cudaStream_t stream, int ctas_per_sm, int *work) {
+                           unsigned *status, cudaStream_t stream, int ctas_per_sm, int *work, int surf) {
   if (n <= 0) return cudaSuccess;
   switch (stack_cap) {
     case 48:
       return launch_cap<48>(variant, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream,
-                            ctas_per_sm, work);
+                            ctas_per_sm, work, surf);
     case 96:
       return launch_cap<96>(variant, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream,
-                            ctas_per_sm, work);
+                            ctas_per_sm, work, surf);
     case 192:
       return launch_cap<192>(variant, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream,
-                             ctas_per_sm, work);
+                             ctas_per_sm, work, surf);
     default:
       return launch_cap<416>(variant, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status, stream,
-                             ctas_per_sm, work);
+                             ctas_per_sm, work, surf);
   }
 }
 
@@ -1029,16 +1046,16 @@ int traversal_stack_capacity(int max_depth) {
 
 cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
                              int64_t n, const int *n_dev, float scene_abs, const int32_t *out_index, void *out,
-                             unsigned *status, cudaStream_t stream, int ctas_per_sm, int *work) {
+                             unsigned *status, cudaStream_t stream, int ctas_per_sm, int *work, bool surface) {
   return launch_variant(closest ? 1 : 0, stack_cap, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status,
-                        stream, ctas_per_sm, work);
+                        stream, ctas_per_sm, work, surface ? 1 : 0);
 }
 
 cudaError_t launch_traversal_d(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,
                                int64_t n, float scene_abs, void *out, unsigned *status, cudaStream_t stream,
                                int *work) {
   return launch_variant(closest ? 3 : 2, stack_cap, nodes, tris, rays, n, nullptr, scene_abs, nullptr, out, status,
-                        stream, 0, work);
+                        stream, 0, work, 0);
 }
 
 }  // namespace skw
