@@ -115,7 +115,12 @@ typedef struct skw_accel_info {
  * splits, partitions and leaf rule as TriangleAccelerator::TriangleAccelerator,
  * Raytracer/Core/TriangleAccelerator.cpp:22-147, 505-729), flattened into the
  * device layout.  Needs no GPU.  threads <= 0 uses all hardware threads.
- * Meshes shared by several primitives (instancing) are SKW_ERR_UNSUPPORTED.
+ * A mesh used by several primitives is instanced as the reference does it
+ * (TriangleAccelerator.cpp:54-102): one subtree over its mesh-space
+ * triangles, and per primitive an instance (its world box, its primitive's
+ * world-to-mesh matrix) placed in the tree like a triangle; queries on such
+ * an accelerator run an exact double-precision traversal that takes rays
+ * into each instance's mesh space (TriangleAccelerator.cpp:213-233).
  * On failure a message is written to err (if errlen > 0). */
 typedef struct skw_flat_tree skw_flat_tree;
 int skw_flat_tree_build(const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims, int32_t n_prims,
@@ -128,6 +133,19 @@ int skw_flat_tree_sizes(const skw_flat_tree *tree, int64_t *n_nodes, int64_t *n_
  * triangle) ids.  Any pointer may be NULL. */
 int skw_flat_tree_export(const skw_flat_tree *tree, uint32_t *nodes, float *tris, int32_t *tri_prim,
                          int32_t *tri_index);
+
+/* Instances of a flat tree, in the tree's final order: per instance its
+ * primitive, the node index of its mesh's subtree root and its
+ * world-to-mesh matrix (16 doubles, row-major: the inverse of the
+ * primitive's mesh-to-world matrix as Matrix4x4::Inverted computes it,
+ * Math/Matrix4x4.h:240-316); and the subtree roots (one per shared mesh, in
+ * mesh order; the tree's own root is node 0).  Any output may be NULL.
+ * A leaf holding instances has bit 7 set in its word 7, and its word 6
+ * indexes a table read by skw_flat_tree_leaf_ranges: its triangle-slot
+ * range (first, count) and instance range (first, count). */
+int skw_flat_tree_instances(const skw_flat_tree *tree, int64_t *n_instances, int32_t *prim, uint32_t *subtree_root,
+                            double *world_to_mesh, int64_t *n_subtrees, uint32_t *subtree_roots);
+int skw_flat_tree_leaf_ranges(const skw_flat_tree *tree, uint32_t leaf_word6, uint32_t *out4);
 
 /* Uploads a flat tree to the context's device (the tree stays owned by the
  * caller).  Together with skw_flat_tree_build this is

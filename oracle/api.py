@@ -56,6 +56,10 @@ _REF_SIGS = [
     ("skw_ref_intersect", None, [_P, _P, _i64, _P, _P, _P, C.c_int]),
     ("skw_ref_intersect_test", None, [_P, _P, _i64, _P, C.c_int]),
     ("skw_ref_accel_create_normals", _P, [C.c_int, _P, C.c_int, _P, _P, _P, _P, _P, _P]),
+    ("skw_ref_accel_num_instances", _i64, [_P]),
+    ("skw_ref_accel_export_instances", None, [_P, _P, _P, _P]),
+    ("skw_ref_accel_meshes_ascending", C.c_int, [_P]),
+    ("skw_ref_accel_mesh_rank", None, [_P, _P]),
     ("skw_ref_intersect_d", None, [_P, _P, _i64, _P, _P, _P, C.c_int]),
     ("skw_ref_intersect_test_d", None, [_P, _P, _i64, _P, C.c_int]),
     ("skw_ref_intersection", None, [_P, _P, _P, _i64, _P, _P, _P, C.c_int]),
@@ -415,6 +419,27 @@ class RefAccel:
             self.h = lib.skw_ref_accel_create_normals(npr, _ptr(self._mesh_of), nm, vp, _ptr(nv), tp, _ptr(nt), np_,
                                                       _ptr(self._x))
         self.n_tris = lib.skw_ref_accel_num_triangles(self.h)
+
+    def instances(self):
+        """(primitive int32 (n,), world_to_mesh float64 (n, 4, 4), subtree
+        triangles int32 (n,)) in the accelerator's final instance order."""
+        n = self.lib.skw_ref_accel_num_instances(self.h)
+        p, m, c = np.zeros(n, np.int32), np.zeros((n, 4, 4)), np.zeros(n, np.int32)
+        if n:
+            self.lib.skw_ref_accel_export_instances(self.h, _ptr(p), _ptr(m), _ptr(c))
+        return p, m, c
+
+    def mesh_rank(self, n_meshes):
+        """Rank of each mesh (numbered in order of first use) in the
+        reference's address order of meshes."""
+        r = np.zeros(n_meshes, np.int32)
+        self.lib.skw_ref_accel_mesh_rank(self.h, _ptr(r))
+        return r
+
+    def meshes_ascending(self) -> bool:
+        """The meshes' addresses ascend in creation order (the reference
+        orders shared meshes by address)."""
+        return bool(self.lib.skw_ref_accel_meshes_ascending(self.h))
 
     def intersect_d(self, rays, threads=0):
         """TriangleAccelerator::Intersect of double rays ((n, 8) float64)."""

@@ -370,6 +370,53 @@ void skw_ref_accel_export(void *a, float *node_bbox, int32_t *node_info, int32_t
   }
 }
 
+// Instances of the accelerator in its final (partitioned) order: primitive
+// index, the world-to-mesh matrix the traversal applies to rays (the
+// instance Transform's inverse matrix, row-major) and the triangle count of
+// the instanced subtree; plus whether the meshes' addresses ascend with
+// their creation order (the reference orders shared meshes by address).
+int64_t skw_ref_accel_num_instances(void *a) { return (int64_t)((RefAccel *)a)->accel->m_instance_nodes.size(); }
+
+void skw_ref_accel_export_instances(void *a, int32_t *prim, double *world_to_mesh, int32_t *sub_tris) {
+  const TriangleAccelerator &acc = *((RefAccel *)a)->accel;
+  for (size_t i = 0; i < acc.m_instance_nodes.size(); ++i) {
+    prim[i] = (int32_t)acc.m_instance_primitive_indices[i];
+    const Matrix4x4_d &m = acc.m_instance_to_world_transformations[i].m_inverted_matrix;
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) world_to_mesh[16 * i + 4 * r + c] = m.m_values[r][c];
+    sub_tris[i] = (int32_t)(acc.m_instance_nodes[i]->m_triangles_end - acc.m_instance_nodes[i]->m_triangles_begin);
+  }
+}
+
+// rank[m] = position of mesh m (meshes numbered in order of first use by
+// the primitives) in the reference's address order of meshes.
+void skw_ref_accel_mesh_rank(void *a, int32_t *rank) {
+  const RefAccel *ra = (const RefAccel *)a;
+  std::vector<const TriangleMesh *> seen;
+  for (const auto &p : ra->prims) {
+    const TriangleMesh *m = p->GetTriangleMesh_RawPtr();
+    if (std::find(seen.begin(), seen.end(), m) == seen.end()) seen.push_back(m);
+  }
+  std::vector<const TriangleMesh *> sorted = seen;
+  std::sort(sorted.begin(), sorted.end());
+  for (size_t i = 0; i < seen.size(); ++i)
+    rank[i] = (int32_t)(std::find(sorted.begin(), sorted.end(), seen[i]) - sorted.begin());
+}
+
+int skw_ref_accel_meshes_ascending(void *a) {
+  const RefAccel *ra = (const RefAccel *)a;
+  const TriangleMesh *prev = nullptr;
+  std::vector<const TriangleMesh *> seen;
+  for (const auto &p : ra->prims) {
+    const TriangleMesh *m = p->GetTriangleMesh_RawPtr();
+    if (std::find(seen.begin(), seen.end(), m) != seen.end()) continue;
+    if (prev && m < prev) return 0;
+    seen.push_back(m);
+    prev = m;
+  }
+  return 1;
+}
+
 // ---------------------------------------------------------------- photons --
 
 typedef PhotonLTEIntegrator::Photon RefPhoton;

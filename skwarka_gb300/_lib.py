@@ -53,6 +53,8 @@ SIGNATURES = [
     ("skw_flat_tree_destroy", None, [_P]),
     ("skw_flat_tree_sizes", C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     ("skw_flat_tree_export", C.c_int, [_P, _P, _P, _P, _P]),
+    ("skw_flat_tree_instances", C.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    ("skw_flat_tree_leaf_ranges", C.c_int, [_P, C.c_uint32, _P]),
     ("skw_accel_create_from_flat", C.c_int, [_P, _P, C.POINTER(_P)]),
     ("skw_accel_create", C.c_int, [_P, C.POINTER(skw_mesh), C.c_int32, C.POINTER(skw_primitive), C.c_int32,
                                    C.POINTER(_P)]),

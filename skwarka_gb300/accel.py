@@ -238,10 +238,25 @@ def build_flat_tree(primitives: list[Primitive], threads: int = 0) -> dict:
         tp = np.zeros(max(nt.value, 1), np.int32)
         ti = np.zeros(max(nt.value, 1), np.int32)
         _lib.check(lib.skw_flat_tree_export(h, nodes.ctypes.data, tris.ctypes.data, tp.ctypes.data, ti.ctypes.data))
+        ni, ns = C.c_int64(), C.c_int64()
+        _lib.check(lib.skw_flat_tree_instances(h, C.byref(ni), None, None, None, C.byref(ns), None))
+        ip = np.zeros(max(ni.value, 1), np.int32)
+        ir = np.zeros(max(ni.value, 1), np.uint32)
+        im = np.zeros((max(ni.value, 1), 4, 4), np.float64)
+        sr = np.zeros(max(ns.value, 1), np.uint32)
+        _lib.check(lib.skw_flat_tree_instances(h, None, ip.ctypes.data, ir.ctypes.data, im.ctypes.data, None,
+                                               sr.ctypes.data))
+        ext = {}
+        for i in np.nonzero((nodes[:, 7] & 3 == 0) & (nodes[:, 7] & 0x80 != 0))[0]:
+            r = np.zeros(4, np.uint32)
+            _lib.check(lib.skw_flat_tree_leaf_ranges(h, int(nodes[i, 6]), r.ctypes.data))
+            ext[int(i)] = tuple(int(x) for x in r)
     finally:
         lib.skw_flat_tree_destroy(h)
     n = nt.value
-    return {"nodes": nodes, "tris": tris[:n], "tri_prim": tp[:n], "tri_index": ti[:n], "max_depth": md.value}
+    return {"nodes": nodes, "tris": tris[:n], "tri_prim": tp[:n], "tri_index": ti[:n], "max_depth": md.value,
+            "inst_prim": ip[:ni.value], "inst_root": ir[:ni.value], "inst_world_to_mesh": im[:ni.value],
+            "subtree_roots": sr[:ns.value], "leaf_ranges": ext}
 
 
 def unpack_hits_d(hits) -> dict:

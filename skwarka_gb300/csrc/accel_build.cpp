@@ -1,5 +1,10 @@
 // Host construction of the ternary bbox kd-tree, restating the reference
 // TriangleAccelerator build (Raytracer/Core/TriangleAccelerator.cpp):
+//   * meshes shared by several primitives (instancing, ctor step 2,
+//     :54-102): one subtree over the mesh-space triangles per mesh, and per
+//     primitive an instance with the world box of the subtree box's
+//     transformed corners, weighted by the subtree's triangle count in the
+//     split search and partitioned like triangles;
 //   * world-space float triangles per primitive, in primitive order
 //     (ctor steps 3-4, :104-139; the transform is Transform::operator()
 //     on Point3D_f, Math/Transform.h:219-230);
@@ -94,6 +99,7 @@ inline size_t cast_size(double v) {
 struct BNode {
   BoxF box;
   uint32_t tb = 0, te = 0;  // triangle range
+  uint32_t ib = 0, ie = 0;  // instance range
   uint8_t flags = 0;        // 0 leaf, 1..3 axis + 1
   std::unique_ptr<BNode> child[3];
 };
@@ -103,6 +109,13 @@ struct Builder {
   std::vector<int32_t> prim;  // primitive index per triangle
   std::vector<int32_t> tidx;  // mesh triangle index per triangle
   std::vector<BoxF> tbox;     // per-triangle AABB
+  // Instances of shared meshes (TriangleAccelerator.cpp:54-102): world box
+  // of the instance, triangles of its mesh's subtree (the split search's
+  // weight), its primitive and the subtree it instances.
+  std::vector<BoxF> ibox;
+  std::vector<size_t> icount;
+  std::vector<int32_t> iprim;
+  std::vector<int32_t> isub;
   std::atomic<int> threads_left{0};
   int threads = 1;  // the build's thread budget
   std::atomic<int32_t> max_depth{0};
@@ -113,6 +126,13 @@ struct Builder {
     std::swap(prim[a], prim[b]);
     std::swap(tidx[a], tidx[b]);
     std::swap(tbox[a], tbox[b]);
+  }
+  // _SwapInstances (TriangleAccelerator.cpp:495-503)
+  void swap_inst(size_t a, size_t b) {
+    std::swap(ibox[a], ibox[b]);
+    std::swap(icount[a], icount[b]);
+    std::swap(iprim[a], iprim[b]);
+    std::swap(isub[a], isub[b]);
   }
 
   // One axis's buckets of _DetermineBestSplit over triangles [ib, ie):
@@ -133,37 +153,44 @@ struct Builder {
       }
     }
   };
-  void fill_buckets(const BoxF &nb, int axis, size_t ib, size_t ie, size_t tries, double coef, Buckets &k) const {
-    for (size_t i = ib; i < ie; ++i) {
-      const BoxF &b = tbox[i];
-      const float dmax = b.hi[axis] - nb.lo[axis];
-      const float dmin = b.lo[axis] - nb.lo[axis];
-      const size_t lefts_begin = std::min(tries, cast_size((double)dmax * coef + 1.0));
-      const size_t rights_end = std::min(tries, cast_size((double)dmin * coef + 1.0));
-      if (rights_end > 0) {
-        k.R[rights_end - 1].unite(b);
-        k.Rn[rights_end - 1] += 1;
-      }
-      if (lefts_begin < tries) {
-        k.L[lefts_begin].unite(b);
-        k.Ln[lefts_begin] += 1;
-      }
-      for (size_t j = rights_end; j < lefts_begin; ++j) {
-        k.M[j].unite(b);
-        k.Mn[j] += 1;
-      }
+  static void add_bucket(const BoxF &nb, int axis, const BoxF &b, size_t count, size_t tries, double coef,
+                         Buckets &k) {
+    const float dmax = b.hi[axis] - nb.lo[axis];
+    const float dmin = b.lo[axis] - nb.lo[axis];
+    const size_t lefts_begin = std::min(tries, cast_size((double)dmax * coef + 1.0));
+    const size_t rights_end = std::min(tries, cast_size((double)dmin * coef + 1.0));
+    if (rights_end > 0) {
+      k.R[rights_end - 1].unite(b);
+      k.Rn[rights_end - 1] += count;
+    }
+    if (lefts_begin < tries) {
+      k.L[lefts_begin].unite(b);
+      k.Ln[lefts_begin] += count;
+    }
+    for (size_t j = rights_end; j < lefts_begin; ++j) {
+      k.M[j].unite(b);
+      k.Mn[j] += count;
     }
   }
+  void fill_buckets(const BoxF &nb, int axis, size_t ib, size_t ie, size_t tries, double coef, Buckets &k) const {
+    for (size_t i = ib; i < ie; ++i) add_bucket(nb, axis, tbox[i], 1, tries, coef, k);
+  }
+  // An instance counts as its subtree's triangles (TriangleAccelerator.cpp:553).
+  void fill_inst_buckets(const BoxF &nb, int axis, size_t ib, size_t ie, size_t tries, double coef,
+                         Buckets &k) const {
+    for (size_t i = ib; i < ie; ++i) add_bucket(nb, axis, ibox[i], icount[i], tries, coef, k);
+  }
 
-  // _DetermineBestSplit (TriangleAccelerator.cpp:505-617), triangles only.
+  // _DetermineBestSplit (TriangleAccelerator.cpp:505-617).
   // Nodes of at least kParallelSplit triangles (the top of the tree, where
   // few subtrees run side by side) fill their buckets on several threads,
   // one slice of the triangles and one axis each.
   static constexpr size_t kParallelSplit = (size_t)1 << 17;
-  void best_split(const BoxF &nb, size_t tb, size_t te, unsigned mask, int &axis_out, double &pos_out) const {
+  void best_split(const BoxF &nb, size_t tb, size_t te, size_t ib, size_t ie, unsigned mask, int &axis_out,
+                  double &pos_out) const {
     const size_t n = te - tb;
     double best_pos[3] = {0, 0, 0}, best_cost[3] = {kInfD, kInfD, kInfD};
-    const size_t tries = std::min(kMaxSplitTries, 2 * n);
+    const size_t tries = std::min(kMaxSplitTries, 2 * n + 2 * (ie - ib));
     double coefs[3] = {0, 0, 0};
     for (int axis = 0; axis < 3; ++axis) {
       const float ext = nb.hi[axis] - nb.lo[axis];
@@ -216,6 +243,7 @@ struct Builder {
         if (mask & (1u << axis)) continue;
         Buckets &k = part[(size_t)axis * slices];
         for (size_t c = 1; c < slices; ++c) k.merge(part[(size_t)axis * slices + c], tries);
+        fill_inst_buckets(nb, axis, ib, ie, tries, coefs[axis], k);
         score(axis, k);
       }
     } else {
@@ -223,6 +251,7 @@ struct Builder {
         if (mask & (1u << axis)) continue;
         Buckets k;
         fill_buckets(nb, axis, tb, te, tries, coefs[axis], k);
+        fill_inst_buckets(nb, axis, ib, ie, tries, coefs[axis], k);
         score(axis, k);
       }
     }
@@ -236,24 +265,28 @@ struct Builder {
     pos_out = best_pos[axis_out];
   }
 
-  // Node::Node (TriangleAccelerator.cpp:621-729), triangles only.
-  std::unique_ptr<BNode> build(size_t tb, size_t te, unsigned mask, size_t depth) {
+  // Node::Node (TriangleAccelerator.cpp:621-729): triangles [tb, te) and
+  // instances [ib, ie).
+  std::unique_ptr<BNode> build(size_t tb, size_t te, size_t ib, size_t ie, unsigned mask, size_t depth) {
     auto node = std::make_unique<BNode>();
     node->tb = (uint32_t)tb;
     node->te = (uint32_t)te;
+    node->ib = (uint32_t)ib;
+    node->ie = (uint32_t)ie;
     for (size_t i = tb; i < te; ++i) node->box.unite(tbox[i]);
+    for (size_t i = ib; i < ie; ++i) node->box.unite(ibox[i]);
     int32_t d = (int32_t)depth;
     int32_t cur = max_depth.load();
     while (d > cur && !max_depth.compare_exchange_weak(cur, d)) {
     }
-    if (te - tb <= kMaxTrianglesInLeaf || mask == 7u || depth >= kMaxTreeDepth) {
+    if ((te - tb) + (ie - ib) <= kMaxTrianglesInLeaf || mask == 7u || depth >= kMaxTreeDepth) {
       node->flags = 0;
       n_leaves.fetch_add(1);
       return node;
     }
     int axis;
     double split;
-    best_split(node->box, tb, te, mask, axis, split);
+    best_split(node->box, tb, te, ib, ie, mask, axis, split);
     node->flags = (uint8_t)(axis + 1);
 
     size_t mid_begin = tb, right_begin = te, i = tb;
@@ -270,22 +303,40 @@ struct Builder {
         ++i;
       }
     }
+    // the instances, partitioned the same way (TriangleAccelerator.cpp:677-700)
+    size_t imid = ib, iright = ie;
+    i = ib;
+    while (i < iright) {
+      const BoxF &b = ibox[i];
+      if ((double)b.hi[axis] < split) {
+        swap_inst(imid, i);
+        ++imid;
+        ++i;
+      } else if ((double)b.lo[axis] > split) {
+        --iright;
+        swap_inst(i, iright);
+      } else {
+        ++i;
+      }
+    }
     struct Range {
-      size_t b, e;
+      size_t b, e, ib, ie;
       unsigned m;
-    } ranges[3] = {{tb, mid_begin, mask}, {mid_begin, right_begin, mask | (1u << axis)}, {right_begin, te, mask}};
+    } ranges[3] = {{tb, mid_begin, ib, imid, mask},
+                   {mid_begin, right_begin, imid, iright, mask | (1u << axis)},
+                   {right_begin, te, iright, ie, mask}};
     // Large subtrees run on their own thread while the budget lasts.
     std::thread workers[3];
     bool spawned[3] = {false, false, false};
     for (int c = 0; c < 3; ++c) {
-      if (ranges[c].b >= ranges[c].e) continue;
+      if (ranges[c].b >= ranges[c].e && ranges[c].ib >= ranges[c].ie) continue;
       if (ranges[c].e - ranges[c].b > 20000 && threads_left.fetch_sub(1) > 0) {
         spawned[c] = true;
         workers[c] = std::thread([this, node_ptr = node.get(), c, r = ranges[c], depth]() {
-          node_ptr->child[c] = build(r.b, r.e, r.m, depth + 1);
+          node_ptr->child[c] = build(r.b, r.e, r.ib, r.ie, r.m, depth + 1);
         });
       } else {
-        node->child[c] = build(ranges[c].b, ranges[c].e, ranges[c].m, depth + 1);
+        node->child[c] = build(ranges[c].b, ranges[c].e, ranges[c].ib, ranges[c].ie, ranges[c].m, depth + 1);
       }
     }
     for (int c = 0; c < 3; ++c)
@@ -316,81 +367,100 @@ inline void transform_point(const double *m, const float *p, float *out) {
 
 }  // namespace
 
-std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *prims, int32_t n_prims, int threads,
-                        FlatTree &out) {
-  if (n_prims < 0 || n_meshes < 0) return "negative primitive or mesh count";
-  std::vector<int> uses((size_t)n_meshes, 0);
-  for (int32_t p = 0; p < n_prims; ++p) {
-    if (prims[p].mesh < 0 || prims[p].mesh >= n_meshes) return "primitive references a mesh index out of range";
-    if (++uses[(size_t)prims[p].mesh] > 1)
-      return "a mesh shared by several primitives (instancing) is not supported by this build";
-  }
-  Builder B;
-  // TriangleMesh drops triangles with an out-of-range or repeated vertex
-  // index (TriangleMesh.cpp:176-182); mesh triangle indices count kept ones.
-  for (int32_t p = 0; p < n_prims; ++p) {
-    const MeshIn &m = meshes[prims[p].mesh];
-    if (m.n_triangles > 0 && (!m.triangles || !m.vertices)) return "mesh has triangles but null arrays";
-    int32_t kept = 0;
-    for (int64_t t = 0; t < m.n_triangles; ++t) {
-      const int32_t *ix = m.triangles + 3 * t;
-      bool bad = false;
-      for (int k = 0; k < 3; ++k)
-        if (ix[k] < 0 || (int64_t)ix[k] >= m.n_vertices) bad = true;
-      if (bad || ix[0] == ix[1] || ix[0] == ix[2] || ix[1] == ix[2]) continue;
-      float v[9];
-      for (int k = 0; k < 3; ++k) {
-        const float *src = m.vertices + 3 * (int64_t)ix[k];
-        if (prims[p].mesh_to_world) {
-          transform_point(prims[p].mesh_to_world, src, v + 3 * k);
-        } else {
-          v[3 * k] = src[0];
-          v[3 * k + 1] = src[1];
-          v[3 * k + 2] = src[2];
+bool invert4(const double *m, double *out) {
+  int indxc[4], indxr[4];
+  int ipiv[4] = {0, 0, 0, 0};
+  double minv[4][4];
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) minv[r][c] = m[4 * r + c];
+  bool singular = false;
+  for (int i = 0; i < 4; ++i) {
+    int irow = -1, icol = -1;
+    double big = 0.0;
+    for (int j = 0; j < 4; ++j) {
+      if (ipiv[j] == 1) continue;
+      for (int k = 0; k < 4; ++k) {
+        if (ipiv[k] == 0) {
+          if (std::fabs(minv[j][k]) >= big) {
+            big = std::fabs(minv[j][k]);
+            irow = j;
+            icol = k;
+          }
+        } else if (ipiv[k] > 1) {
+          singular = true;
         }
       }
-      BoxF b;
-      for (int k = 0; k < 3; ++k) {
-        for (int c = 0; c < 3; ++c) {
-          b.lo[c] = std::min(b.lo[c], v[3 * k + c]);
-          b.hi[c] = std::max(b.hi[c], v[3 * k + c]);
-        }
-      }
-      B.tv.insert(B.tv.end(), v, v + 9);
-      B.prim.push_back(p);
-      B.tidx.push_back(kept++);
-      B.tbox.push_back(b);
+    }
+    if (irow < 0 || icol < 0) return false;  // NaN entries
+    ++ipiv[icol];
+    if (irow != icol)
+      for (int k = 0; k < 4; ++k) std::swap(minv[irow][k], minv[icol][k]);
+    indxr[i] = irow;
+    indxc[i] = icol;
+    if (minv[icol][icol] == 0.0) singular = true;
+    const double pivinv = 1.0 / minv[icol][icol];
+    minv[icol][icol] = 1.0;
+    for (int j = 0; j < 4; ++j) minv[icol][j] *= pivinv;
+    for (int j = 0; j < 4; ++j) {
+      if (j == icol) continue;
+      const double save = minv[j][icol];
+      minv[j][icol] = 0;
+      for (int k = 0; k < 4; ++k) minv[j][k] -= minv[icol][k] * save;
     }
   }
-  const size_t n = B.prim.size();
-  if (n > (size_t)INT32_MAX) return "too many triangles";
-  unsigned hw = std::thread::hardware_concurrency();
-  B.threads = threads > 0 ? threads : (int)(hw ? hw : 1);
-  B.threads_left = B.threads - 1;
+  for (int j = 3; j >= 0; --j)
+    if (indxr[j] != indxc[j])
+      for (int k = 0; k < 4; ++k) std::swap(minv[k][indxr[j]], minv[k][indxc[j]]);
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) out[4 * r + c] = minv[r][c];
+  return !singular;
+}
 
-  out.nodes.clear();
-  out.tris.clear();
-  if (n == 0) {
-    // An empty accelerator: a single empty leaf whose box culls every ray.
-    DevNode leaf{};
+namespace {
+
+// A mesh's triangles, dropping those TriangleMesh drops (an out-of-range or
+// repeated vertex index, TriangleMesh.cpp:176-182; mesh triangle indices
+// count the kept ones), in mesh space or through `m` (Transform on
+// Point3D_f), appended to the builder with primitive id `prim`.
+void add_mesh_triangles(Builder &B, const MeshIn &m, const double *xf, int32_t prim) {
+  int32_t kept = 0;
+  for (int64_t t = 0; t < m.n_triangles; ++t) {
+    const int32_t *ix = m.triangles + 3 * t;
+    bool bad = false;
+    for (int k = 0; k < 3; ++k)
+      if (ix[k] < 0 || (int64_t)ix[k] >= m.n_vertices) bad = true;
+    if (bad || ix[0] == ix[1] || ix[0] == ix[2] || ix[1] == ix[2]) continue;
+    float v[9];
     for (int k = 0; k < 3; ++k) {
-      leaf.lo[k] = kInfF;
-      leaf.hi[k] = -kInfF;
+      const float *src = m.vertices + 3 * (int64_t)ix[k];
+      if (xf) {
+        transform_point(xf, src, v + 3 * k);
+      } else {
+        v[3 * k] = src[0];
+        v[3 * k + 1] = src[1];
+        v[3 * k + 2] = src[2];
+      }
     }
-    leaf.a = 0;
-    leaf.b = 0;
-    out.nodes.push_back(leaf);
-    out.max_depth = 0;
-    out.n_leaves = 1;
-    for (int k = 0; k < 6; ++k) out.bounds[k] = 0.f;
-    return "";
+    BoxF b;
+    for (int k = 0; k < 3; ++k) {
+      for (int c = 0; c < 3; ++c) {
+        b.lo[c] = std::min(b.lo[c], v[3 * k + c]);
+        b.hi[c] = std::max(b.hi[c], v[3 * k + c]);
+      }
+    }
+    B.tv.insert(B.tv.end(), v, v + 9);
+    B.prim.push_back(prim);
+    B.tidx.push_back(kept++);
+    B.tbox.push_back(b);
   }
-  std::unique_ptr<BNode> root = B.build(0, n, 0u, 0);
+}
 
-  // Flatten: pre-order; a node's present children occupy consecutive slots.
-  out.nodes.reserve(n);
+// Pre-order flattening of one tree into out.nodes; a node's present
+// children occupy consecutive slots.  Returns the root's index.
+uint32_t flatten(const BNode *root, FlatTree &out) {
+  const uint32_t root_idx = (uint32_t)out.nodes.size();
   out.nodes.emplace_back();
-  std::vector<std::pair<const BNode *, uint32_t>> stack{{root.get(), 0u}};
+  std::vector<std::pair<const BNode *, uint32_t>> stack{{root, root_idx}};
   while (!stack.empty()) {
     auto [bn, idx] = stack.back();
     stack.pop_back();
@@ -400,8 +470,14 @@ std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *pr
       dn.hi[k] = bn->box.hi[k];
     }
     if (bn->flags == 0) {
-      dn.a = bn->tb;
-      dn.b = (uint32_t)(bn->te - bn->tb) << 8;
+      if (bn->ie > bn->ib) {
+        dn.a = (uint32_t)out.leaf_ext.size();
+        dn.b = kLeafExt;
+        out.leaf_ext.push_back(LeafExt{bn->tb, bn->te - bn->tb, bn->ib, bn->ie - bn->ib});
+      } else {
+        dn.a = bn->tb;
+        dn.b = (uint32_t)(bn->te - bn->tb) << 8;
+      }
     } else {
       uint32_t first = (uint32_t)out.nodes.size(), mask = 0, slot = first;
       std::pair<const BNode *, uint32_t> kids[3];
@@ -418,6 +494,93 @@ std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *pr
     }
     out.nodes[idx] = dn;
   }
+  return root_idx;
+}
+
+const double kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+
+}  // namespace
+
+std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *prims, int32_t n_prims, int threads,
+                        FlatTree &out) {
+  if (n_prims < 0 || n_meshes < 0) return "negative primitive or mesh count";
+  std::vector<int> uses((size_t)n_meshes, 0);
+  for (int32_t p = 0; p < n_prims; ++p) {
+    if (prims[p].mesh < 0 || prims[p].mesh >= n_meshes) return "primitive references a mesh index out of range";
+    ++uses[(size_t)prims[p].mesh];
+    const MeshIn &m = meshes[prims[p].mesh];
+    if (m.n_triangles > 0 && (!m.triangles || !m.vertices)) return "mesh has triangles but null arrays";
+  }
+  Builder B;
+  unsigned hw = std::thread::hardware_concurrency();
+  B.threads = threads > 0 ? threads : (int)(hw ? hw : 1);
+  B.threads_left = B.threads - 1;
+  out = FlatTree();
+
+  // Step 2 of the reference's constructor: every mesh used by more than one
+  // primitive gets a subtree over its mesh-space triangles, and each of its
+  // primitives an instance whose world box is the union of the subtree
+  // box's eight corners transformed to world space.  Meshes in index order
+  // (the reference orders them by address, which follows creation order).
+  std::vector<std::unique_ptr<BNode>> subtrees;
+  std::vector<std::vector<double>> inverses((size_t)n_prims);
+  for (int32_t mi = 0; mi < n_meshes; ++mi) {
+    if (uses[(size_t)mi] < 2) continue;
+    const size_t tb = B.prim.size();
+    add_mesh_triangles(B, meshes[mi], nullptr, -1);
+    const size_t te = B.prim.size();
+    subtrees.push_back(B.build(tb, te, 0, 0, 0u, 0));
+    const BNode *sub = subtrees.back().get();
+    for (int32_t p = 0; p < n_prims; ++p) {
+      if (prims[p].mesh != mi) continue;
+      const double *xf = prims[p].mesh_to_world ? prims[p].mesh_to_world : kIdentity;
+      BoxF ib;
+      for (int j = 0; j < 8; ++j) {
+        const float corner[3] = {(j & 1) ? sub->box.lo[0] : sub->box.hi[0], (j & 2) ? sub->box.lo[1] : sub->box.hi[1],
+                                 (j & 4) ? sub->box.lo[2] : sub->box.hi[2]};
+        float w[3];
+        transform_point(xf, corner, w);
+        for (int c = 0; c < 3; ++c) {
+          ib.lo[c] = std::min(ib.lo[c], w[c]);
+          ib.hi[c] = std::max(ib.hi[c], w[c]);
+        }
+      }
+      std::vector<double> inv(16);
+      if (!invert4(xf, inv.data())) return "a primitive's mesh-to-world matrix is singular";
+      inverses[(size_t)p] = inv;
+      B.ibox.push_back(ib);
+      B.icount.push_back(te - tb);
+      B.iprim.push_back(p);
+      B.isub.push_back((int32_t)subtrees.size() - 1);
+    }
+  }
+  // Step 3: the primitives that own their mesh, in world space.
+  const size_t shared_end = B.prim.size();
+  for (int32_t p = 0; p < n_prims; ++p)
+    if (uses[(size_t)prims[p].mesh] < 2) add_mesh_triangles(B, meshes[prims[p].mesh], prims[p].mesh_to_world, p);
+  const size_t n = B.prim.size(), n_inst = B.ibox.size();
+  if (n > (size_t)INT32_MAX) return "too many triangles";
+
+  if (n == shared_end && n_inst == 0) {
+    // An empty accelerator: a single empty leaf whose box culls every ray.
+    DevNode leaf{};
+    for (int k = 0; k < 3; ++k) {
+      leaf.lo[k] = kInfF;
+      leaf.hi[k] = -kInfF;
+    }
+    leaf.a = 0;
+    leaf.b = 0;
+    out.nodes.push_back(leaf);
+    out.max_depth = 0;
+    out.n_leaves = 1;
+    for (int k = 0; k < 6; ++k) out.bounds[k] = 0.f;
+    return "";
+  }
+  // Step 4: the tree over the world triangles and the instances.
+  std::unique_ptr<BNode> root = B.build(shared_end, n, 0, n_inst, 0u, 0);
+  out.nodes.reserve(n + 1);
+  flatten(root.get(), out);
+  for (const auto &sub : subtrees) out.subtree_roots.push_back(flatten(sub.get(), out));
   out.tris.resize(n);
   for (size_t i = 0; i < n; ++i) {
     DevTri &t = out.tris[i];
@@ -427,6 +590,14 @@ std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *pr
     t.prim = B.prim[i];
     t.tri = B.tidx[i];
     t.slot = (int32_t)i;
+  }
+  out.inst.resize(n_inst);
+  for (size_t i = 0; i < n_inst; ++i) {
+    DevInst &d = out.inst[i];
+    std::memcpy(d.world_to_mesh, inverses[(size_t)B.iprim[i]].data(), sizeof(d.world_to_mesh));
+    d.root = out.subtree_roots[(size_t)B.isub[i]];
+    d.prim = B.iprim[i];
+    d.pad[0] = d.pad[1] = 0;
   }
   out.max_depth = B.max_depth.load();
   out.n_leaves = B.n_leaves.load();

@@ -50,16 +50,46 @@ struct PrimIn {
   const double *mesh_to_world;  // row-major 4x4 or null
 };
 
+// An instance of a mesh shared by several primitives (the reference's
+// m_instance_nodes / m_instance_to_world_transformations /
+// m_instance_primitive_indices, TriangleAccelerator.cpp:54-102): the
+// world-to-mesh matrix of its primitive (row-major; the inverse that
+// Matrix4x4::Inverted computes, which the traversal applies to rays), the
+// node index of its mesh's subtree and its primitive.  144 bytes.
+struct alignas(16) DevInst {
+  double world_to_mesh[16];
+  uint32_t root;
+  int32_t prim;
+  uint32_t pad[2];
+};
+static_assert(sizeof(DevInst) == 144, "DevInst must be 144 bytes");
+
+// A leaf holding instances: DevNode.b has kLeafExt set and DevNode.a indexes
+// the tree's leaf_ext table (its triangle and instance ranges).
+constexpr uint32_t kLeafExt = 1u << 7;
+struct LeafExt {
+  uint32_t tri_first, tri_count, inst_first, inst_count;
+};
+
 struct FlatTree {
-  std::vector<DevNode> nodes;
-  std::vector<DevTri> tris;
-  int32_t max_depth = 0;
+  std::vector<DevNode> nodes;    // the tree (root 0), then every shared mesh's subtree
+  std::vector<DevTri> tris;      // shared meshes' triangles (mesh space, prim -1) first
+  std::vector<DevInst> inst;     // in the final (partitioned) order
+  std::vector<LeafExt> leaf_ext;
+  std::vector<uint32_t> subtree_roots;  // one per shared mesh, in mesh order
+  int32_t max_depth = 0;         // over the tree and the subtrees
   int64_t n_leaves = 0;
   float bounds[6] = {0, 0, 0, 0, 0, 0};
 };
 
+// Matrix4x4<double>::Inverted (Math/Matrix4x4.h:240-316): Gauss-Jordan
+// elimination with full pivoting, row-major 4x4; false if singular.
+bool invert4(const double *m, double *out);
+
 // Builds the tree (same split search, partition order and leaf rule as the
-// reference TriangleAccelerator) and flattens it.  `threads` <= 0 uses all
+// reference TriangleAccelerator, instancing included: a mesh used by several
+// primitives gets one subtree in mesh space and each of its primitives an
+// instance) and flattens it.  `threads` <= 0 uses all
 // hardware threads.  Returns an empty string on success, else an error.
 std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *prims, int32_t n_prims,
                         int threads, FlatTree &out);

@@ -37,6 +37,11 @@ cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, con
 cudaError_t prepare_traversal(int stack_cap);
 // Resident CTAs per SM of the closest-hit kernel at this capacity.
 int traversal_max_ctas_per_sm(int stack_cap);
+// An accelerator with instances registers its device tables (DevInst[],
+// LeafExt[]) under its node array; traversal launches on that node array
+// then run the exact instance-aware kernel.
+void register_instances(const void *nodes, const void *inst, const void *ext);
+void unregister_instances(const void *nodes);
 // Double rays (skw_ray_d, 64 bytes each): closest = true writes skw_hit_d
 // (double t, prim, tri; t = +inf, ids -1 on a miss), false uint8_t per ray.
 cudaError_t launch_traversal_d(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,

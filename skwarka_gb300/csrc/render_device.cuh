@@ -428,6 +428,7 @@ __device__ V3 bsdf_sample(const Bsdf &b, V3 wi_w, float uc, float u0, float u1, 
 struct Hit {
   V3 p, ng, ns;
   int g;      // global triangle
+  int prim;   // primitive
 };
 
 // CoreUtils::GetNextMinT (CoreUtils.h:139-149) for a ray leaving the hit
@@ -471,7 +472,44 @@ __device__ __noinline__ float next_min_t_exact(const SceneDev &S, const Hit &h, 
   return __double2float_ru(t);
 }
 
+// A primitive whose mesh is shared is traced in mesh space (the ray taken
+// there by its world-to-mesh matrix in double), so its outgoing rays get
+// GetNextMinT exactly as the reference computes it: in mesh space, for the
+// ray's origin and direction transformed with the same double operations
+// as the traversal uses, rounded up to float.
+__device__ __noinline__ float next_min_t_instance(const SceneDev &S, const Hit &h, V3 w) {
+  const double *m = S.prim_w2m + 16 * h.prim;
+  auto row = [&](int r, double x, double y, double z) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(m[4 * r], x), __dmul_rn(m[4 * r + 1], y)), __dmul_rn(m[4 * r + 2], z));
+  };
+  double o[3] = {__dadd_rn(row(0, h.p.x, h.p.y, h.p.z), m[3]), __dadd_rn(row(1, h.p.x, h.p.y, h.p.z), m[7]),
+                 __dadd_rn(row(2, h.p.x, h.p.y, h.p.z), m[11])};
+  const double wq = __dadd_rn(row(3, h.p.x, h.p.y, h.p.z), m[15]);
+  if (wq != 1.0) {
+    const double inv = __ddiv_rn(1.0, wq);
+    for (int k = 0; k < 3; ++k) o[k] = __dmul_rn(o[k], inv);
+  }
+  const double d[3] = {row(0, w.x, w.y, w.z), row(1, w.x, w.y, w.z), row(2, w.x, w.y, w.z)};
+  const int i0 = S.tri_vidx[3 * h.g], i1 = S.tri_vidx[3 * h.g + 1], i2 = S.tri_vidx[3 * h.g + 2];
+  const float *vm = S.vpos_mesh;
+  const double ax = vm[3 * i0], ay = vm[3 * i0 + 1], az = vm[3 * i0 + 2];
+  const double e1x = __dsub_rn(vm[3 * i1], ax), e1y = __dsub_rn(vm[3 * i1 + 1], ay), e1z = __dsub_rn(vm[3 * i1 + 2], az);
+  const double e2x = __dsub_rn(vm[3 * i2], ax), e2y = __dsub_rn(vm[3 * i2 + 1], ay), e2z = __dsub_rn(vm[3 * i2 + 2], az);
+  const double cx = __dsub_rn(__dmul_rn(e1y, e2z), __dmul_rn(e1z, e2y));
+  const double cy = __dsub_rn(__dmul_rn(e1z, e2x), __dmul_rn(e1x, e2z));
+  const double cz = __dsub_rn(__dmul_rn(e1x, e2y), __dmul_rn(e1y, e2x));
+  const double qx = __dsub_rn(ax, o[0]), qy = __dsub_rn(ay, o[1]), qz = __dsub_rn(az, o[2]);
+  const double sx = __dsub_rn(__dmul_rn(qy, e1z), __dmul_rn(qz, e1y));
+  const double sy = __dsub_rn(__dmul_rn(qz, e1x), __dmul_rn(qx, e1z));
+  const double sz = __dsub_rn(__dmul_rn(qx, e1y), __dmul_rn(qy, e1x));
+  const double mdot = __dadd_rn(__dadd_rn(__dmul_rn(sx, e2x), __dmul_rn(sy, e2y)), __dmul_rn(sz, e2z));
+  const double div = __dadd_rn(__dadd_rn(__dmul_rn(d[0], cx), __dmul_rn(d[1], cy)), __dmul_rn(d[2], cz));
+  if (div == 0.0) return 0.0f;
+  return __double2float_ru(fmax(0.0, __dadd_rn(__dmul_rn(mdot, __ddiv_rn(1.0, div)), 1e-14)));
+}
+
 __device__ __forceinline__ float next_min_t(const SceneDev &S, const Hit &h, V3 w) {
+  if (S.prim_inst && S.prim_inst[h.prim]) return next_min_t_instance(S, h, w);
   const int i0 = S.tri_vidx[3 * h.g], i1 = S.tri_vidx[3 * h.g + 1], i2 = S.tri_vidx[3 * h.g + 2];
   const V3 p0 = load3(S.vpos + 3 * i0), p1 = load3(S.vpos + 3 * i1), p2 = load3(S.vpos + 3 * i2);
   const V3 e1 = p1 - p0, e2 = p2 - p0, n = cross(e1, e2), q = p0 - h.p;
@@ -579,6 +617,7 @@ __device__ __forceinline__ bool specular_transmit(const Bsdf &b, V3 wo_w, V3 &di
 
 __device__ Hit make_hit(const SceneDev &S, V3 o, V3 d, float t, int prim, int tri) {
   Hit h;
+  h.prim = prim;
   h.g = S.prim_tri_offset[prim] + tri;
   const int i0 = S.tri_vidx[3 * h.g], i1 = S.tri_vidx[3 * h.g + 1], i2 = S.tri_vidx[3 * h.g + 2];
   const V3 p0 = load3(S.vpos + 3 * i0), p1 = load3(S.vpos + 3 * i1), p2 = load3(S.vpos + 3 * i2);

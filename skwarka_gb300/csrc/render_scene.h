@@ -72,6 +72,14 @@ struct SceneDev {
   const int32_t *prim_light;      // area light index or -1
   const int32_t *prim_has_normals;
   const int32_t *prim_xform;      // 1 where the primitive has a mesh-to-world matrix
+  // Primitives whose mesh is shared (the accelerator traces them in mesh
+  // space through their world-to-mesh matrix): prim_inst[p] = 1, their
+  // world-to-mesh matrices (16 doubles per primitive, row-major, the
+  // accelerator's) and the mesh-space vertex positions (3 floats per global
+  // vertex).  All null when no mesh is shared.
+  const int32_t *prim_inst;
+  const double *prim_w2m;
+  const float *vpos_mesh;
   const DevMaterial *materials;
   const AreaLight *area_lights;
   int32_t n_area_lights;

@@ -119,7 +119,7 @@ int skw_flat_tree_build(const skw_mesh *meshes, int32_t n_meshes, const skw_prim
   if (!e.empty()) {
     delete t;
     set_err(e);
-    return e.find("instancing") != std::string::npos ? SKW_ERR_UNSUPPORTED : SKW_ERR_ARG;
+    return SKW_ERR_ARG;
   }
   *out = t;
   return SKW_OK;
@@ -151,6 +151,31 @@ int skw_flat_tree_export(const skw_flat_tree *t, uint32_t *nodes, float *tris, i
   return SKW_OK;
 }
 
+int skw_flat_tree_instances(const skw_flat_tree *t, int64_t *n_instances, int32_t *prim, uint32_t *subtree_root,
+                            double *world_to_mesh, int64_t *n_subtrees, uint32_t *subtree_roots) {
+  if (!t) return SKW_ERR_ARG;
+  if (n_instances) *n_instances = (int64_t)t->ft.inst.size();
+  if (n_subtrees) *n_subtrees = (int64_t)t->ft.subtree_roots.size();
+  for (size_t i = 0; i < t->ft.inst.size(); ++i) {
+    if (prim) prim[i] = t->ft.inst[i].prim;
+    if (subtree_root) subtree_root[i] = t->ft.inst[i].root;
+    if (world_to_mesh) std::memcpy(world_to_mesh + 16 * i, t->ft.inst[i].world_to_mesh, 16 * sizeof(double));
+  }
+  if (subtree_roots)
+    for (size_t i = 0; i < t->ft.subtree_roots.size(); ++i) subtree_roots[i] = t->ft.subtree_roots[i];
+  return SKW_OK;
+}
+
+int skw_flat_tree_leaf_ranges(const skw_flat_tree *t, uint32_t leaf_word_a, uint32_t *out4) {
+  if (!t || !out4 || leaf_word_a >= t->ft.leaf_ext.size()) return SKW_ERR_ARG;
+  const skw::LeafExt &e = t->ft.leaf_ext[leaf_word_a];
+  out4[0] = e.tri_first;
+  out4[1] = e.tri_count;
+  out4[2] = e.inst_first;
+  out4[3] = e.inst_count;
+  return SKW_OK;
+}
+
 int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_accel **out) {
   if (!ctx || !tree || !out) return fail(ctx, SKW_ERR_ARG, "null argument");
   *out = nullptr;
@@ -168,6 +193,15 @@ int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_acce
       (e = cudaMalloc(&a->d_status, sizeof(unsigned))) != cudaSuccess) {
     skw_accel_destroy(a);
     return cuda_fail(ctx, e, "cudaMalloc (accelerator)");
+  }
+  const size_t ib = ft.inst.size() * sizeof(skw::DevInst), eb = ft.leaf_ext.size() * sizeof(skw::LeafExt);
+  if (!ft.inst.empty() && ((e = cudaMalloc(&a->d_inst, ib)) != cudaSuccess ||
+                           (e = cudaMalloc(&a->d_leaf_ext, std::max<size_t>(eb, 16))) != cudaSuccess ||
+                           (e = cudaMemcpy(a->d_inst, ft.inst.data(), ib, cudaMemcpyHostToDevice)) != cudaSuccess ||
+                           (eb > 0 && (e = cudaMemcpy(a->d_leaf_ext, ft.leaf_ext.data(), eb, cudaMemcpyHostToDevice)) !=
+                                          cudaSuccess))) {
+    skw_accel_destroy(a);
+    return cuda_fail(ctx, e, "instance tables");
   }
   if ((e = cudaMemcpy(a->d_nodes, ft.nodes.data(), nb, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (!ft.tris.empty() &&
@@ -188,9 +222,14 @@ int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_acce
   info.stack_need = 2 * ft.max_depth + 1;
   std::memcpy(info.bounds, ft.bounds, sizeof(info.bounds));
   info.build_ms = tree->build_ms;
-  info.device_bytes = (int64_t)(nb + tb);
+  info.device_bytes = (int64_t)(nb + tb + ib + eb);
   a->h_nodes = ft.nodes;
   a->h_tris = ft.tris;
+  a->h_inst = ft.inst;
+  a->h_leaf_ext = ft.leaf_ext;
+  a->h_subtree_roots = ft.subtree_roots;
+  // instances need the stack of the top tree and of the deepest subtree at once
+  if (a->d_inst) skw::register_instances(a->d_nodes, a->d_inst, a->d_leaf_ext);
   *out = a;
   return SKW_OK;
 }
@@ -209,6 +248,9 @@ int skw_accel_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
 
 void skw_accel_destroy(skw_accel *a) {
   if (!a) return;
+  if (a->d_inst) skw::unregister_instances(a->d_nodes);
+  cudaFree(a->d_inst);
+  cudaFree(a->d_leaf_ext);
   cudaFree(a->d_nodes);
   cudaFree(a->d_tris);
   cudaFree(a->d_status);

@@ -31,12 +31,17 @@ struct skw_accel {
   skw_ctx *ctx = nullptr;
   skw::DevNode *d_nodes = nullptr;
   skw::DevTri *d_tris = nullptr;
+  skw::DevInst *d_inst = nullptr;     // instances (null: none)
+  skw::LeafExt *d_leaf_ext = nullptr; // leaves holding instances
   unsigned *d_status = nullptr;
   int stack_cap = 0;
   float scene_abs = 0.0f;  // largest absolute vertex coordinate
   skw_accel_info info{};
   std::vector<skw::DevNode> h_nodes;
   std::vector<skw::DevTri> h_tris;
+  std::vector<skw::DevInst> h_inst;
+  std::vector<skw::LeafExt> h_leaf_ext;
+  std::vector<uint32_t> h_subtree_roots;
 };
 
 // A render scene (skw_scene_create): its accelerator plus the shading data.

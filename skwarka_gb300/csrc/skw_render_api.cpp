@@ -143,7 +143,25 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
     return rc;
   }
   // Mesh-order geometry.
-  std::vector<float> vpos, vnrm, albedo;
+  std::vector<float> vpos, vnrm, albedo, vpos_mesh;
+  std::vector<double> prim_w2m;
+  std::vector<int32_t> prim_inst((size_t)std::max(n_prims, 1), 0);
+  {
+    std::vector<int> uses((size_t)std::max(n_meshes, 1), 0);
+    for (int32_t p = 0; p < n_prims; ++p) ++uses[(size_t)prims[p].mesh];
+    bool any = false;
+    for (int32_t p = 0; p < n_prims; ++p) any |= (prim_inst[(size_t)p] = uses[(size_t)prims[p].mesh] > 1 ? 1 : 0) != 0;
+    if (any) {
+      // the accelerator's world-to-mesh matrices (identity for unshared meshes)
+      const double id[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+      prim_w2m.assign(16 * (size_t)n_prims, 0.0);
+      for (int32_t p = 0; p < n_prims; ++p) {
+        double *o = prim_w2m.data() + 16 * (size_t)p;
+        if (!skw::invert4(prims[p].mesh_to_world ? prims[p].mesh_to_world : id, o)) std::memcpy(o, id, sizeof(id));
+      }
+    }
+  }
+  const bool instanced = !prim_w2m.empty();
   std::vector<int32_t> tri_vidx, prim_tri_offset((size_t)std::max(n_prims, 1)), prim_material((size_t)std::max(n_prims, 1)),
       prim_light((size_t)std::max(n_prims, 1), -1), prim_has_normals((size_t)std::max(n_prims, 1), 0),
       prim_xform((size_t)std::max(n_prims, 1), 0);
@@ -168,6 +186,7 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
       float w[3];
       xform_point(prims[p].mesh_to_world, m.vertices + 3 * v, w);
       vpos.insert(vpos.end(), w, w + 3);
+      if (instanced) vpos_mesh.insert(vpos_mesh.end(), m.vertices + 3 * v, m.vertices + 3 * v + 3);
       if (any_normals) {
         float nn[3] = {0, 0, 1};
         if (prims[p].vertex_normals) {
@@ -321,16 +340,30 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
     const std::vector<skw::DevNode> &nodes = s->accel->h_nodes;
     const std::vector<skw::DevTri> &slots = s->accel->h_tris;
     std::vector<int32_t> leaf_of_slot(slots.size(), -1), slot_of_tri((size_t)std::max(tri_count, 1), -1);
+    // a leaf's triangle-slot range (leaves holding instances keep it in the ext table)
+    auto leaf_range = [&](const skw::DevNode &nd, uint32_t &first, uint32_t &count) {
+      if (nd.b & skw::kLeafExt) {
+        first = s->accel->h_leaf_ext[nd.a].tri_first;
+        count = s->accel->h_leaf_ext[nd.a].tri_count;
+      } else {
+        first = nd.a;
+        count = nd.b >> 8;
+      }
+    };
     for (size_t n = 0; n < nodes.size(); ++n)
-      if ((nodes[n].b & 3u) == 0u)
-        for (uint32_t k = 0; k < (nodes[n].b >> 8); ++k) leaf_of_slot[nodes[n].a + k] = (int32_t)n;
-    for (size_t k = 0; k < slots.size(); ++k)
-      slot_of_tri[(size_t)(prim_tri_offset[(size_t)slots[k].prim] + slots[k].tri)] = (int32_t)k;
+      if ((nodes[n].b & 3u) == 0u) {
+        uint32_t first, count;
+        leaf_range(nodes[n], first, count);
+        for (uint32_t k = 0; k < count; ++k) leaf_of_slot[first + k] = (int32_t)n;
+      }
+    for (size_t k = 0; k < slots.size(); ++k)  // (a shared mesh's slots, prim -1, belong to no one primitive)
+      if (slots[k].prim >= 0)
+        slot_of_tri[(size_t)(prim_tri_offset[(size_t)slots[k].prim] + slots[k].tri)] = (int32_t)k;
     for (size_t j = 0; j < light_tri.size(); ++j) {
       const int32_t slot = slot_of_tri[(size_t)light_tri[j]];
       const int32_t leaf = slot >= 0 ? leaf_of_slot[(size_t)slot] : -1;
       float *o = light_leaf.data() + 8 * j;
-      if (leaf < 0) {  // cannot happen for a triangle the tree holds; an empty range tests nothing
+      if (leaf < 0) {  // an instanced light mesh: an empty range tests nothing
         o[0] = o[1] = o[2] = INFINITY;
         o[3] = o[4] = o[5] = -INFINITY;
         continue;
@@ -340,7 +373,9 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
         o[c] = L.lo[c];
         o[3 + c] = L.hi[c];
       }
-      const int32_t first = (int32_t)L.a, count = (int32_t)(L.b >> 8);
+      uint32_t ufirst, ucount;
+      leaf_range(L, ufirst, ucount);
+      const int32_t first = (int32_t)ufirst, count = (int32_t)ucount;
       std::memcpy(o + 6, &first, 4);
       std::memcpy(o + 7, &count, 4);
     }
@@ -358,6 +393,11 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
   if (e == cudaSuccess) e = upload(s, prim_light, &D.prim_light);
   if (e == cudaSuccess) e = upload(s, prim_has_normals, &D.prim_has_normals);
   if (e == cudaSuccess) e = upload(s, prim_xform, &D.prim_xform);
+  if (instanced) {
+    if (e == cudaSuccess) e = upload(s, prim_inst, &D.prim_inst);
+    if (e == cudaSuccess) e = upload(s, prim_w2m, &D.prim_w2m);
+    if (e == cudaSuccess) e = upload(s, vpos_mesh, &D.vpos_mesh);
+  }
   if (e == cudaSuccess) e = upload(s, mats, &D.materials);
   if (e == cudaSuccess) e = upload(s, lights, &D.area_lights);
   if (e == cudaSuccess) e = upload(s, light_tri, &D.light_tri);

@@ -35,7 +35,9 @@
 #include <atomic>
 #include <cstdint>
 #include <mutex>
+#include <unordered_map>
 
+#include "accel_build.h"
 #include "kernels.h"
 
 namespace skw {
@@ -885,6 +887,182 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
   }
 }
 
+// --------------------------------------------------------------------------
+// Accelerators with instances (meshes shared by several primitives) are
+// traversed by k_trace_inst: one ray per thread, the reference's
+// _NodeIntersect / _NodeIntersectTest restated in double throughout
+// (TriangleAccelerator.cpp:154-293, 354-462) -- the slab test of every
+// node, the children pushed in the reference's order, at a leaf first its
+// instances (the ray taken to mesh space by the instance's world-to-mesh
+// Transform, TriangleAccelerator.cpp:213-233, and the instance's subtree
+// traversed with it) and then its triangles, all with the reference's
+// double Moller-Trumbore.  Exact but slow: instanced scenes are rare and
+// the float walk of k_trace does not apply to rays in mesh space.
+
+struct InstDev {
+  double m[16];  // world to mesh, row-major
+  uint32_t root;
+  int32_t prim;
+  uint32_t pad[2];
+};
+
+// Transform::operator() on a point (with the w division) and a vector
+// (Math/Transform.h:239-269), every sum and product rounded separately.
+__device__ __forceinline__ void xf_point(const double *m, double x, double y, double z, double *o) {
+  const double xp = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(m[0], x), __dmul_rn(m[1], y)), __dmul_rn(m[2], z)), m[3]);
+  const double yp = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(m[4], x), __dmul_rn(m[5], y)), __dmul_rn(m[6], z)), m[7]);
+  const double zp = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(m[8], x), __dmul_rn(m[9], y)), __dmul_rn(m[10], z)), m[11]);
+  const double w = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(m[12], x), __dmul_rn(m[13], y)), __dmul_rn(m[14], z)), m[15]);
+  o[0] = xp;
+  o[1] = yp;
+  o[2] = zp;
+  if (w != 1.0) {
+    const double inv = __ddiv_rn(1.0, w);
+    o[0] = __dmul_rn(xp, inv);
+    o[1] = __dmul_rn(yp, inv);
+    o[2] = __dmul_rn(zp, inv);
+  }
+}
+__device__ __forceinline__ void xf_vector(const double *m, double x, double y, double z, double *o) {
+  o[0] = __dadd_rn(__dadd_rn(__dmul_rn(m[0], x), __dmul_rn(m[1], y)), __dmul_rn(m[2], z));
+  o[1] = __dadd_rn(__dadd_rn(__dmul_rn(m[4], x), __dmul_rn(m[5], y)), __dmul_rn(m[6], z));
+  o[2] = __dadd_rn(__dadd_rn(__dmul_rn(m[8], x), __dmul_rn(m[9], y)), __dmul_rn(m[10], z));
+}
+
+// The reference's slab test (TriangleAccelerator.cpp:176-192): true when
+// the node is culled.
+__device__ __forceinline__ bool slab_culled(float4 na, float4 nb, const double *o, const double *inv, double tmin,
+                                            double tmax) {
+  const double lo[3] = {na.x, na.y, na.z}, hi[3] = {na.w, nb.x, nb.y};
+  double tn[3], tf[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    tn[k] = __dmul_rn(__dsub_rn(lo[k], o[k]), inv[k]);
+    tf[k] = __dmul_rn(__dsub_rn(hi[k], o[k]), inv[k]);
+    if (tn[k] > tf[k]) {
+      const double t = tn[k];
+      tn[k] = tf[k];
+      tf[k] = t;
+    }
+  }
+  return tmin > tf[0] || tn[0] > tf[1] || tn[1] > tf[0] || tn[2] > tf[0] || tmin > tf[1] || tn[0] > tf[2] ||
+         tn[1] > tf[2] || tn[2] > tf[1] || tmin > tf[2] || tn[0] > tmax || tn[1] > tmax || tn[2] > tmax;
+}
+
+// One (sub)tree walk from `root` for the ray (o, d, tmin, tmax): closest hit
+// updates tmax and the hit's slot (best_slot; the instance's primitive in
+// best_prim when inside an instance), any hit returns on the first.  Leaves
+// of the top tree may hold instances (INNER = false); a subtree's do not.
+// Returns false on stack overflow.
+template <int CAP, bool CLOSEST, bool INNER>
+__device__ bool walk_exact(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
+                           const InstDev *__restrict__ inst, const uint4 *__restrict__ ext, uint32_t root,
+                           const double *o, const double *d, double tmin, double &tmax, int &best_slot,
+                           int &best_prim, bool &hit, uint32_t *stk) {
+  const double inv[3] = {__ddiv_rn(1.0, d[0]), __ddiv_rn(1.0, d[1]), __ddiv_rn(1.0, d[2])};
+  int sp = 0;
+  stk[sp++] = root;
+  while (sp > 0) {
+    const uint32_t ni = stk[--sp];
+    const float4 na = __ldg(nodes + 2 * ni), nb = __ldg(nodes + 2 * ni + 1);
+    if (slab_culled(na, nb, o, inv, tmin, tmax)) continue;
+    const uint32_t a = __float_as_uint(nb.z), b = __float_as_uint(nb.w);
+    if (b & 3u) {
+      const uint32_t axis = (b & 3u) - 1u, mask = (b >> 2) & 7u;
+      const uint32_t sL = a, sM = a + (mask & 1u), sR = sM + ((mask >> 1) & 1u);
+      if (sp + 3 > CAP) return false;
+      if (d[axis] > 0.0) {  // children pushed in reverse so that the left one pops first
+        if (mask & 4u) stk[sp++] = sR;
+        if (mask & 2u) stk[sp++] = sM;
+        if (mask & 1u) stk[sp++] = sL;
+      } else {
+        if (mask & 1u) stk[sp++] = sL;
+        if (mask & 2u) stk[sp++] = sM;
+        if (mask & 4u) stk[sp++] = sR;
+      }
+      continue;
+    }
+    uint32_t tf = a, tc = b >> 8, i0 = 0, ic = 0;
+    if (!INNER && (b & kLeafExt)) {
+      const uint4 e = __ldg(ext + a);
+      tf = e.x;
+      tc = e.y;
+      i0 = e.z;
+      ic = e.w;
+    }
+    for (uint32_t k = 0; k < ic && !INNER; ++k) {
+      const InstDev *I = inst + i0 + k;
+      double mo[3], md[3];
+      xf_point(I->m, o[0], o[1], o[2], mo);
+      xf_vector(I->m, d[0], d[1], d[2], md);
+      int slot = -1, pr = -1;
+      bool h2 = false;
+      if (!walk_exact<CAP, CLOSEST, true>(nodes, tris, inst, ext, I->root, mo, md, tmin, tmax, slot, pr, h2,
+                                          stk + sp))
+        return false;
+      if (h2) {
+        hit = true;
+        if (!CLOSEST) return true;
+        best_slot = slot;
+        best_prim = I->prim;
+      }
+    }
+    for (uint32_t k = 0; k < tc; ++k) {
+      const int slot = (int)(tf + k);
+      float3 v0, v1, v2;
+      int prim, tri;
+      load_tri(tris, (uint32_t)slot, v0, v1, v2, prim, tri);
+      double t64;
+      if (tri_test64v(o[0], o[1], o[2], d[0], d[1], d[2], v0, v1, v2, tmin, tmax, t64)) {
+        hit = true;
+        if (!CLOSEST) return true;
+        tmax = t64;
+        best_slot = slot;
+        best_prim = prim;
+      }
+    }
+  }
+  return true;
+}
+
+template <int CAP, bool CLOSEST, bool DRAY>
+__global__ void __launch_bounds__(128)
+    k_trace_inst(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, const InstDev *__restrict__ inst,
+                 const uint4 *__restrict__ ext, const float4 *__restrict__ rays, int n, const int *__restrict__ n_dev,
+                 const int32_t *__restrict__ out_index, void *__restrict__ out, unsigned *__restrict__ status) {
+  if (n_dev) n = min(n, *n_dev);
+  uint32_t stk[2 * CAP];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double o[3], d[3], tmin, tmax;
+    if (DRAY) {
+      const RayD r = load_ray_d(rays, i);
+      o[0] = r.ox, o[1] = r.oy, o[2] = r.oz, d[0] = r.dx, d[1] = r.dy, d[2] = r.dz, tmin = r.tmin, tmax = r.tmax;
+    } else {
+      const RayF r = load_ray(rays, i);
+      o[0] = r.ox, o[1] = r.oy, o[2] = r.oz, d[0] = r.dx, d[1] = r.dy, d[2] = r.dz, tmin = r.tmin, tmax = r.tmax;
+    }
+    int slot = -1, prim = -1;
+    bool hit = false;
+    if (!walk_exact<CAP, CLOSEST, false>(nodes, tris, inst, ext, 0u, o, d, tmin, tmax, slot, prim, hit, stk))
+      atomicOr(status, 1u);
+    const int oi = out_index ? out_index[i] : i;
+    if (!CLOSEST) {
+      ((uint8_t *)out)[oi] = hit ? 1 : 0;
+    } else if (DRAY) {
+      int4 h = make_int4(0, 0x7ff00000, -1, -1);
+      if (hit) {
+        const long long tb = __double_as_longlong(tmax);
+        h = make_int4((int)(tb & 0xffffffffll), (int)(tb >> 32), prim, __float_as_int(__ldg(tris + 3 * slot + 1).w));
+      }
+      ((int4 *)out)[oi] = h;
+    } else {
+      int4 h = make_int4(0x7f800000, -1, -1, 0);
+      if (hit) h = make_int4(__float_as_int((float)tmax), prim, __float_as_int(__ldg(tris + 3 * slot + 1).w), 1);
+      ((int4 *)out)[oi] = h;
+    }
+  }
+}
+
 // Per-device launch facts, computed once per device on first use and read
 // without a lock afterwards (launches may come from several host threads).
 constexpr int kMaxDevices = 64;
@@ -952,6 +1130,55 @@ cudaError_t device_sms(int dev, int &sms) {
   return cudaSuccess;
 }
 
+// Device tables of the accelerators that have instances, by their node
+// array (the traversal launches receive the node pointer).
+struct InstTables {
+  const void *inst;
+  const void *ext;
+};
+std::mutex &inst_mutex() {
+  static std::mutex m;
+  return m;
+}
+std::unordered_map<const void *, InstTables> &inst_registry() {
+  static std::unordered_map<const void *, InstTables> r;
+  return r;
+}
+bool find_instances(const void *nodes, InstTables &t) {
+  std::lock_guard<std::mutex> lock(inst_mutex());
+  auto &r = inst_registry();
+  if (r.empty()) return false;
+  auto it = r.find(nodes);
+  if (it == r.end()) return false;
+  t = it->second;
+  return true;
+}
+
+template <int CAP>
+cudaError_t launch_inst(int variant, const void *nodes, const void *tris, const InstTables &T, const void *rays,
+                        int64_t n, const int *n_dev, const int32_t *out_index, void *out, unsigned *status,
+                        cudaStream_t stream, int sms) {
+  const int64_t want = (n + 127) / 128, cap = (int64_t)sms * 16;
+  const dim3 grid((unsigned)(want < cap ? want : cap)), block(128);
+  const float4 *nd = (const float4 *)nodes, *tr = (const float4 *)tris, *ry = (const float4 *)rays;
+  const InstDev *in = (const InstDev *)T.inst;
+  const uint4 *ex = (const uint4 *)T.ext;
+  switch (variant) {
+    case 0:
+      k_trace_inst<CAP, false, false><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status);
+      break;
+    case 1:
+      k_trace_inst<CAP, true, false><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status);
+      break;
+    case 2:
+      k_trace_inst<CAP, false, true><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status);
+      break;
+    default:
+      k_trace_inst<CAP, true, true><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status);
+  }
+  return cudaGetLastError();
+}
+
 template <int CAP>
 cudaError_t launch_cap(int variant, const void *nodes, const void *tris, const void *rays, int64_t n,
                        const int *n_dev, float scene_abs, const int32_t *out_index, void *out, unsigned *status,
@@ -960,6 +1187,9 @@ cudaError_t launch_cap(int variant, const void *nodes, const void *tris, const v
   cudaError_t e = current_device(dev);
   if (e != cudaSuccess || (e = cap_prepare<CAP>(dev)) != cudaSuccess || (e = device_sms(dev, sms)) != cudaSuccess)
     return e;
+  InstTables T;
+  if (find_instances(nodes, T))
+    return launch_inst<CAP>(variant, nodes, tris, T, rays, n, n_dev, out_index, out, status, stream, sms);
   int per_sm = cap_occupancy<CAP>(dev, variant).load(std::memory_order_acquire);
   if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
   const int64_t warps_per_block = SKW_TRAV_BLOCK / 32;
@@ -1049,6 +1279,16 @@ cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, con
                              unsigned *status, cudaStream_t stream, int ctas_per_sm, int *work, bool surface) {
   return launch_variant(closest ? 1 : 0, stack_cap, nodes, tris, rays, n, n_dev, scene_abs, out_index, out, status,
                         stream, ctas_per_sm, work, surface ? 1 : 0);
+}
+
+void register_instances(const void *nodes, const void *inst, const void *ext) {
+  std::lock_guard<std::mutex> lock(inst_mutex());
+  inst_registry()[nodes] = InstTables{inst, ext};
+}
+
+void unregister_instances(const void *nodes) {
+  std::lock_guard<std::mutex> lock(inst_mutex());
+  inst_registry().erase(nodes);
 }
 
 cudaError_t launch_traversal_d(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,

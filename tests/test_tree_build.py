@@ -114,14 +114,6 @@ def test_builder_transform_matches_point_transform():
     assert np.array_equal(got, want[t[order]])
 
 
-def test_builder_rejects_instancing():
-    v, t = scenes.sphere_mesh(1)
-    mesh = TriangleMesh(v.astype(np.float32), t)
-    with pytest.raises(_lib.SkwError) as e:
-        build_flat_tree([Primitive(mesh), Primitive(mesh)])
-    assert e.value.code == 6  # SKW_ERR_UNSUPPORTED
-
-
 def test_builder_parallel_split_search_matches_oracle(oracle):
     """Nodes of 2^17 triangles or more fill their split buckets on several
     threads (slices of the triangles per axis, merged); the tree stays the
