@@ -15,10 +15,15 @@ What it does:
    * ``Texture()`` in the constructors of the texture class templates becomes
      ``Texture<T>()`` (``Raytracer/Textures/{Constant,Mix,Scale,Windy,Wrinkled}Texture.h``);
    * a ``MAth`` -> ``Math`` alias for a case typo
-     (``PhotonInternalTypes.h:23``).
+     (``PhotonInternalTypes.h:23``);
+   * the unit tests' ``VolumeRegionMock`` constructor takes its spectra by
+     const reference (``UnitTests/Mocks/VolumeRegionMock.h:30``; the tests
+     pass temporaries).
 
-   The staged copy is git-ignored; it exists so that the same build can be
-   repeated on a machine without the reference tree.
+   The staged copy (plus the reference's unit tests and its vendored CxxTest
+   4.4, which the drop-in tests compile against the GPU accelerator) is
+   git-ignored; it exists so that the same build can be repeated on a
+   machine without the reference tree.
 2. Shim headers (``oracle/ref_shims``) stand in for Windows, the MSVC debug
    CRT, Boost (``mt19937``, ``intrusive_ptr``) and TBB (a real thread pool).
    The MSVC-style ``<a\\b.h>`` includes are satisfied by files whose names
@@ -61,7 +66,9 @@ def reference_root(arg: str | None = None) -> Path:
 
 
 REFERENCE: Path | None = None
-SUBDIRS = ("Common", "Math", "Raytracer", "Shapes")
+SUBDIRS = ("Common", "Math", "Raytracer", "Shapes", "UnitTests")
+CXXTEST = OUT / "cxxtest"  # the reference's vendored CxxTest 4.4 (its unit-test framework)
+STAGE_VERSION = "staged 3: RayLibs sources, unit tests, CxxTest\n"
 EXCLUDE = {"ImageEnvironmentalLight.cpp", "RGBImageSource.cpp", "TranslucentMaterial.cpp", "dllmain.cpp"}
 # -ffp-contract=off: no fused multiply-add, so that an aarch64 build rounds
 # exactly like the x86-64 (SSE2) build the reference targets.
@@ -79,6 +86,10 @@ def _rewrite(path: Path) -> None:
     text = re.sub(r"(\w+)\.swap\((std::vector<\w+>)\(\)\)", r"\2().swap(\1)", text)
     if path.parent.name == "Textures" and path.suffix == ".h":
         text = re.sub(r"^Texture\(\),", "Texture<T>(),", text, flags=re.M)
+    if path.name == "VolumeRegionMock.h":
+        # the unit tests pass temporaries to non-const reference parameters
+        # (an MSVC extension): take them by const reference
+        text = re.sub(r"(\w+) &i_(emission|absorption|scattering)", r"const \1 &i_\2", text)
     if text != orig:
         path.write_text(text, encoding="latin-1")
 
@@ -89,17 +100,22 @@ def stage() -> None:
     if not root.is_dir():
         return
     stamp = SRC / ".staged"
-    if stamp.exists():
+    if stamp.exists() and stamp.read_text() == STAGE_VERSION:
         return
     if SRC.exists():
         shutil.rmtree(SRC)
+    if CXXTEST.exists():
+        shutil.rmtree(CXXTEST)
     for sub in SUBDIRS:
         shutil.copytree(root / sub, SRC / sub)
+    cxx = (REFERENCE or reference_root()) / "ThirdParty" / "cxxtest" / "4.4"
+    if cxx.is_dir():
+        shutil.copytree(cxx, CXXTEST)
     for p in SRC.rglob("*"):
         if p.suffix in (".h", ".cpp") and p.is_file():
             _rewrite(p)
     (SRC / "MAth").symlink_to("Math")
-    stamp.write_text("staged\n")
+    stamp.write_text(STAGE_VERSION)
 
 
 def make_shims() -> None:
@@ -151,6 +167,8 @@ def build(verbose: bool = False) -> Path | None:
     stage()
     if not (SRC / ".staged").exists():
         return None
+    if (SRC / ".staged").read_text() != STAGE_VERSION:
+        raise RuntimeError("the staged reference sources are from an older recipe and the reference tree is absent")
     make_shims()
     # The objects depend on the flags and on every shim header: a change to
     # either rebuilds everything.
