@@ -27,9 +27,9 @@
 //
 // Layout: 16-byte nodes (x, y, z, word) read with one vector load; the
 // photon normal ids (uint16) are read only for points inside the radius.
-// For k <= 128 the heap and the stack live in local memory, which the L1
-// caches; larger k use a heap in a caller-provided global scratch buffer of
-// k 16-byte entries per query.
+// The walk stack lives in shared memory; for k <= 128 the heap (8-byte
+// entries: float key, tree position) lives in local memory, larger k use a
+// heap in a caller-provided global scratch buffer of k entries per query.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -55,62 +55,6 @@ namespace {
 constexpr int kStack = 32;
 constexpr int kKnnBlock = 128;  // threads per block of the lookup kernels
 
-
-// A heap entry: the squared distance as its IEEE bit pattern (for the
-// non-negative doubles here, unsigned integer order is the double order, so
-// the heap compares on the integer pipe) and the tree position.
-struct Cand {
-  unsigned long long key;
-  int32_t idx;
-  __device__ __forceinline__ double d2() const { return __longlong_as_double((long long)key); }
-};
-
-__device__ __forceinline__ Cand make_cand(double d2, int32_t idx) {
-  return Cand{(unsigned long long)__double_as_longlong(d2), idx};
-}
-
-// (d2, idx) lexicographic, as the reference's NearestPoint comparison.
-__device__ __forceinline__ bool cand_less(const Cand &a, const Cand &b) {
-  return a.key == b.key ? a.idx < b.idx : a.key < b.key;
-}
-
-// Sift `value` up from `hole` towards `top`.
-__device__ __forceinline__ void heap_push_up(Cand *h, int hole, int top, Cand value) {
-  int parent = (hole - 1) / 2;
-  while (hole > top && cand_less(h[parent], value)) {
-    h[hole] = h[parent];
-    hole = parent;
-    parent = (hole - 1) / 2;
-  }
-  h[hole] = value;
-}
-
-// Move the hole at `hole` down to a leaf along larger children, then place
-// `value` by sifting it up.
-__device__ __forceinline__ void heap_adjust(Cand *h, int hole, int len, Cand value) {
-  const int top = hole;
-  int second = hole;
-  while (second < (len - 1) / 2) {
-    second = 2 * (second + 1);
-    if (cand_less(h[second], h[second - 1])) second--;
-    h[hole] = h[second];
-    hole = second;
-  }
-  if ((len & 1) == 0 && second == (len - 2) / 2) {
-    second = 2 * (second + 1);
-    h[hole] = h[second - 1];
-    hole = second - 1;
-  }
-  heap_push_up(h, hole, top, value);
-}
-
-__device__ __forceinline__ void heap_make(Cand *h, int len) {
-  if (len < 2) return;
-  for (int parent = (len - 2) / 2;; --parent) {
-    heap_adjust(h, parent, len, h[parent]);
-    if (parent == 0) return;
-  }
-}
 
 struct Query {
   double q[3];
@@ -138,12 +82,21 @@ __device__ __forceinline__ void query_float(Query &Q) {
   Q.sin_f = (float)Q.sin_t;
 }
 
+// Coordinates of the query by a run-time axis, selected without indexing so
+// that the query stays in registers.
+__device__ __forceinline__ float qf_at(const Query &Q, uint32_t a) {
+  return a == 0 ? Q.qf[0] : (a == 1 ? Q.qf[1] : Q.qf[2]);
+}
+__device__ __forceinline__ double q_at(const Query &Q, uint32_t a) {
+  return a == 0 ? Q.q[0] : (a == 1 ? Q.q[1] : Q.q[2]);
+}
+
 // q[axis] <= split for a float split, exactly, without double arithmetic:
 // qf is the float nearest to q, so qf < split implies q < split and
 // qf > split implies q > split.
 __device__ __forceinline__ bool q_le_split(const Query &Q, uint32_t axis, float split) {
-  const float qf = Q.qf[axis];
-  return qf < split || (qf == split && Q.qle[axis]);
+  const float qf = qf_at(Q, axis);
+  return qf < split || (qf == split && (axis == 0 ? Q.qle[0] : (axis == 1 ? Q.qle[1] : Q.qle[2])));
 }
 
 // PhotonFilter::operator() (PhotonInternalTypes.h:127-133), with float
@@ -276,7 +229,7 @@ __device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, con
       const float split = ax == 0 ? pp.x : (ax == 1 ? pp.y : pp.z);
       // the reference's pop test: (qa - split)^2 < maxd2, in double
       float s2, e2;
-      sq_bound(Q.qf[ax] - split, Q.eq, s2, e2);
+      sq_bound(qf_at(Q, ax) - split, Q.eq, s2, e2);
       const float E = e2 * 1.0001f + s2 * 4.0e-7f + 1e-37f;
       bool take;
       if (s2 + E < mlo) {
@@ -284,7 +237,7 @@ __device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, con
       } else if (s2 - E >= mhi) {
         take = false;
       } else {
-        const double pd = __dsub_rn(Q.q[ax], (double)split);
+        const double pd = __dsub_rn(q_at(Q, ax), (double)split);
         take = __dmul_rn(pd, pd) < maxd2;
       }
       if (take) next = q_le_split(Q, ax, split) ? (int)(pw >> 3) : (int)par + 1;
@@ -294,35 +247,92 @@ __device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, con
   }
 }
 
-// Exact squared distances of entries [0, len) of h, whose idx are set: four
-// independent dependent-chains at a time so that the FP64 pipe overlaps
-// them.
-__device__ __forceinline__ void fill_keys(const float4 *__restrict__ nodes, const Query &Q, Cand *h, int len) {
-  int j = 0;
-  for (; j + 4 <= len; j += 4) {
-    const float4 p0 = __ldg(nodes + h[j].idx), p1 = __ldg(nodes + h[j + 1].idx), p2 = __ldg(nodes + h[j + 2].idx),
-                 p3 = __ldg(nodes + h[j + 3].idx);
-    const double d0 = point_d2(p0, Q), d1 = point_d2(p1, Q), d2 = point_d2(p2, Q), d3 = point_d2(p3, Q);
-    h[j].key = (unsigned long long)__double_as_longlong(d0);
-    h[j + 1].key = (unsigned long long)__double_as_longlong(d1);
-    h[j + 2].key = (unsigned long long)__double_as_longlong(d2);
-    h[j + 3].key = (unsigned long long)__double_as_longlong(d3);
+// ------------------------------------------------------------ k_knn --
+// The heap holds float squared distances: an entry's key is the float
+// distance of its point, within key_err of the reference's double value.
+// Heap comparisons are decided on the keys and their bounds, and only when
+// two keys' intervals overlap are the exact doubles of both points computed
+// (GB300 runs a double operation at ~1/64 of the float rate, and divergent
+// double work in the former exact-keyed heap kept its FP64 pipe half busy);
+// ties of exact distances go to the lower tree position, as the reference's
+// NearestPoint comparison (KDTree.h:331-387) decides them.  So the heap
+// takes the same branches as the reference's and its order is the
+// reference's.  The search radius is max_dist^2 until the heap is full and
+// then the top's exact distance, represented by a float bracket [rlo, rhi]
+// and computed exactly on demand.  The exact distances of the output are
+// computed at the end, four independent chains at a time.
+
+// A heap entry: float squared distance and tree position.
+struct FCand {
+  float key;
+  int32_t idx;
+};
+
+// Bound on |key - d2| for a point whose float squared distance is key: the
+// float query's rounding eq on each axis, the float differences and squares
+// (the terms of sq_bound summed: 2u d2 + 2 eq sum|d| + 3 eq^2 with
+// sum|d| <= sqrt(3 d2)), the float sum and the double result's rounding.
+__device__ __forceinline__ float key_err(float eq, float key) {
+  return 1.001f * (2.0f * eq * sqrtf(3.0f * key) + 9.0f * eq * eq) + 6.0e-7f * key + 1e-37f;
+}
+
+// (d2, idx) lexicographic on the exact distances, decided on the keys when
+// their bounds do not overlap.
+__device__ __forceinline__ bool fcand_less(const float4 *__restrict__ nodes, const Query &Q, const FCand &a,
+                                           const FCand &b) {
+  const float ea = key_err(Q.eq, a.key), eb = key_err(Q.eq, b.key);
+  if (a.key + ea < b.key - eb) return true;
+  if (b.key + eb < a.key - ea) return false;
+  const double da = point_d2(__ldg(nodes + a.idx), Q), db = point_d2(__ldg(nodes + b.idx), Q);
+  return da == db ? a.idx < b.idx : da < db;
+}
+
+__device__ __forceinline__ void fheap_push_up(const float4 *__restrict__ nodes, const Query &Q, FCand *h, int hole, int top, FCand value) {
+  int parent = (hole - 1) / 2;
+  while (hole > top && fcand_less(nodes, Q, h[parent], value)) {
+    h[hole] = h[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
   }
-  for (; j < len; ++j) h[j].key = (unsigned long long)__double_as_longlong(point_d2(__ldg(nodes + h[j].idx), Q));
+  h[hole] = value;
+}
+
+__device__ __forceinline__ void fheap_adjust(const float4 *__restrict__ nodes, const Query &Q, FCand *h, int hole, int len, FCand value) {
+  const int top = hole;
+  int second = hole;
+  while (second < (len - 1) / 2) {
+    second = 2 * (second + 1);
+    if (fcand_less(nodes, Q, h[second], h[second - 1])) second--;
+    h[hole] = h[second];
+    hole = second;
+  }
+  if ((len & 1) == 0 && second == (len - 2) / 2) {
+    second = 2 * (second + 1);
+    h[hole] = h[second - 1];
+    hole = second - 1;
+  }
+  fheap_push_up(nodes, Q, h, hole, top, value);
+}
+
+__device__ __forceinline__ void fheap_make(const float4 *__restrict__ nodes, const Query &Q, FCand *h, int len) {
+  if (len < 2) return;
+  for (int parent = (len - 2) / 2;; --parent) {
+    fheap_adjust(nodes, Q, h, parent, len, h[parent]);
+    if (parent == 0) return;
+  }
 }
 
 // KMAX > 0: heap of KMAX entries in local memory.  KMAX == 0: the heap of
-// query i is scratch[i * k ...].  Until the heap is full its entries keep
-// only their tree position (the reference's array holds them unordered);
-// their exact distances are computed together when it fills -- or at the
-// end, for a query that finds fewer than k points.
+// query i is scratch[i * k ...].  Until the heap is full its entries are
+// the accepted points in visit order (the reference's array holds them
+// unordered); at k entries it becomes a heap.
 template <int KMAX>
 __global__ void __launch_bounds__(kKnnBlock) k_knn(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
                                              const double *__restrict__ dirs, int n, const double *__restrict__ q,
                                              const double *__restrict__ qn, int64_t nq, int k, double max_dist,
                                              double cos_t, int32_t *__restrict__ out_idx,
                                              double *__restrict__ out_d2, int32_t *__restrict__ out_count,
-                                             int32_t *__restrict__ out_visited, Cand *__restrict__ scratch,
+                                             int32_t *__restrict__ out_visited, FCand *__restrict__ scratch,
                                              unsigned *__restrict__ status, const int *__restrict__ nq_dev) {
   __shared__ uint32_t stk[kStack][kKnnBlock];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -344,38 +354,134 @@ __global__ void __launch_bounds__(kKnnBlock) k_knn(const float4 *__restrict__ no
     Q.cos_t = Q.sin_t = 0.0;
   }
   query_float(Q);
-  Cand local_heap[KMAX > 0 ? KMAX : 1];
-  Cand *heap = KMAX > 0 ? local_heap : scratch + i * (int64_t)k;
-  int size = 0;
-  double maxd2 = __dmul_rn(max_dist, max_dist);  // KDTree::Lookup (KDTree.h:475-482)
-  int visited = 0;
-  if (k > 0) {
-    visited = walk(nodes, n, Q, maxd2, stk, [&](int ni, const float4 p, double d2, double &md2) -> bool {
-      if (Q.filter && !photon_filter(Q, p, __ldg(nids + ni), dirs)) return false;
-      if (size < k) {
-        heap[size++].idx = ni;
-        if (size < k) return false;
-        fill_keys(nodes, Q, heap, size);
-        heap_make(heap, size);
-      } else {
-        if (d2 < 0.0) d2 = point_d2(p, Q);
-        // pop_heap: the top goes to the back; the back's old value is re-placed
-        const Cand back = heap[k - 1];
-        heap[k - 1] = heap[0];
-        heap_adjust(heap, 0, k - 1, back);
-        // replace the (popped) back with the new point and push it
-        heap_push_up(heap, k - 1, 0, make_cand(d2, ni));
+  FCand local_heap[KMAX > 0 ? KMAX : 1];
+  FCand *heap = KMAX > 0 ? local_heap : scratch + i * (int64_t)k;
+  int size = 0, visited = 0;
+  if (k > 0 && n > 0) {
+    // the search radius: max_dist^2 (KDTree::Lookup, KDTree.h:475-482)
+    // until the heap is full, then the top's exact squared distance
+    double rex = __dmul_rn(max_dist, max_dist);
+    bool rex_ok = true;
+    float rlo = __double2float_rd(rex), rhi = __double2float_ru(rex);
+    auto radius = [&]() -> double {
+      if (!rex_ok) {
+        rex = point_d2(__ldg(nodes + heap[0].idx), Q);
+        rex_ok = true;
       }
-      md2 = heap[0].d2();
-      return true;
-    });
-    if (visited < 0) atomicOr(status, 2u);
-    if (size < k) fill_keys(nodes, Q, heap, size);
+      return rex;
+    };
+    auto new_top = [&]() {
+      const float t = heap[0].key, e = key_err(Q.eq, t);
+      rlo = __fsub_rd(t, e);
+      rhi = __fadd_ru(t, e);
+      rex_ok = false;
+    };
+    int sp = 0, cur = 0;
+    bool overflow = false;
+    for (;;) {
+      const float4 p = __ldg(nodes + cur);
+      ++visited;
+      {
+        float sx, ex, sy, ey, sz, ez;
+        sq_bound(p.x - Q.qf[0], Q.eq, sx, ex);
+        sq_bound(p.y - Q.qf[1], Q.eq, sy, ey);
+        sq_bound(p.z - Q.qf[2], Q.eq, sz, ez);
+        const float d2f = (sx + sy) + sz;
+        const float E = (ex + ey + ez) * 1.0001f + d2f * 4.0e-7f + 1e-37f;
+        bool inside;
+        if (d2f + E < rlo) {
+          inside = true;
+        } else if (d2f - E >= rhi) {
+          inside = false;
+        } else {
+          inside = point_d2(p, Q) < radius();
+        }
+        if (inside && (!Q.filter || photon_filter(Q, p, __ldg(nids + cur), dirs))) {
+          const FCand c{d2f, cur};
+          if (size < k) {
+            heap[size++] = c;
+            if (size == k) {
+              fheap_make(nodes, Q, heap, k);
+              new_top();
+            }
+          } else {
+            // pop_heap: the top goes to the back; the back's old value is re-placed
+            const FCand back = heap[k - 1];
+            heap[k - 1] = heap[0];
+            fheap_adjust(nodes, Q, heap, 0, k - 1, back);
+            // the popped back slot takes the new point, pushed up
+            fheap_push_up(nodes, Q, heap, k - 1, 0, c);
+            new_top();
+          }
+        }
+      }
+      const uint32_t w = __float_as_uint(p.w);
+      int next = -1;
+      if ((w & 3u) != 3u) {
+        const uint32_t axis = w & 3u;
+        const float split = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
+        const uint32_t right = w >> 3;
+        const bool has_left = (w & 4u) != 0u, has_right = right < (uint32_t)n;
+        const bool le = q_le_split(Q, axis, split);
+        next = le ? (has_left ? cur + 1 : -1) : (has_right ? (int)right : -1);
+        if (le ? has_right : has_left) {  // the far child waits on the stack
+          if (sp >= kStack) {
+            overflow = true;
+            break;
+          }
+          stk[sp][threadIdx.x] = (uint32_t)cur;
+          ++sp;
+        }
+      }
+      while (next < 0 && sp > 0) {
+        --sp;
+        const uint32_t par = stk[sp][threadIdx.x];
+        const float4 pp = __ldg(nodes + par);
+        const uint32_t pw = __float_as_uint(pp.w), ax = pw & 3u;
+        const float split = ax == 0 ? pp.x : (ax == 1 ? pp.y : pp.z);
+        // the reference's pop test: (qa - split)^2 < radius, in double
+        float s2, e2;
+        sq_bound(qf_at(Q, ax) - split, Q.eq, s2, e2);
+        const float E = e2 * 1.0001f + s2 * 4.0e-7f + 1e-37f;
+        bool take;
+        if (s2 + E < rlo) {
+          take = true;
+        } else if (s2 - E >= rhi) {
+          take = false;
+        } else {
+          const double pd = __dsub_rn(q_at(Q, ax), (double)split);
+          take = __dmul_rn(pd, pd) < radius();
+        }
+        if (take) next = q_le_split(Q, ax, split) ? (int)(pw >> 3) : (int)par + 1;
+      }
+      if (next < 0) break;
+      cur = next;
+    }
+    if (overflow) atomicOr(status, 2u);
   }
   out_count[i] = size;
-  for (int j = 0; j < k; ++j) {
-    out_idx[i * k + j] = j < size ? heap[j].idx : -1;
-    out_d2[i * k + j] = j < size ? heap[j].d2() : 0.0;
+  // the exact squared distances of the output, four chains at a time
+  int j = 0;
+  for (; j + 4 <= size; j += 4) {
+    const int32_t a0 = heap[j].idx, a1 = heap[j + 1].idx, a2 = heap[j + 2].idx, a3 = heap[j + 3].idx;
+    const double d0 = point_d2(__ldg(nodes + a0), Q), d1 = point_d2(__ldg(nodes + a1), Q),
+                 d2 = point_d2(__ldg(nodes + a2), Q), d3 = point_d2(__ldg(nodes + a3), Q);
+    out_idx[i * k + j] = a0;
+    out_idx[i * k + j + 1] = a1;
+    out_idx[i * k + j + 2] = a2;
+    out_idx[i * k + j + 3] = a3;
+    out_d2[i * k + j] = d0;
+    out_d2[i * k + j + 1] = d1;
+    out_d2[i * k + j + 2] = d2;
+    out_d2[i * k + j + 3] = d3;
+  }
+  for (; j < size; ++j) {
+    out_idx[i * k + j] = heap[j].idx;
+    out_d2[i * k + j] = point_d2(__ldg(nodes + heap[j].idx), Q);
+  }
+  for (; j < k; ++j) {
+    out_idx[i * k + j] = -1;
+    out_d2[i * k + j] = 0.0;
   }
   if (out_visited) out_visited[i] = visited;
 }
@@ -422,7 +528,7 @@ __global__ void __launch_bounds__(kKnnBlock) k_nearest(const float4 *__restrict_
 
 }  // namespace
 
-size_t knn_scratch_bytes(int64_t nq, int k) { return k > 128 ? (size_t)nq * (size_t)k * sizeof(Cand) : 0; }
+size_t knn_scratch_bytes(int64_t nq, int k) { return k > 128 ? (size_t)nq * (size_t)k * sizeof(FCand) : 0; }
 
 cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                        const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,
@@ -439,7 +545,7 @@ cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *di
                                             out_idx, out_d2, out_count, out_visited, nullptr, status, nq_dev);
   } else {
     k_knn<0><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
-                                          out_idx, out_d2, out_count, out_visited, (Cand *)scratch, status, nq_dev);
+                                          out_idx, out_d2, out_count, out_visited, (FCand *)scratch, status, nq_dev);
   }
   return cudaGetLastError();
 }
@@ -506,7 +612,7 @@ cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const do
   const int block = kKnnBlock;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
   k_knn<0><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
-                                        out_idx, out_d2, out_count, nullptr, (Cand *)scratch, status, nullptr);
+                                        out_idx, out_d2, out_count, nullptr, (FCand *)scratch, status, nullptr);
   return cudaGetLastError();
 }
 
