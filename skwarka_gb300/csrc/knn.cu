@@ -54,6 +54,12 @@ namespace {
 // is at most 31 levels deep and the walk holds at most one entry per level.
 constexpr int kStack = 32;
 constexpr int kKnnBlock = 128;  // threads per block of the lookup kernels
+// minimum resident blocks per SM of k_knn (bounds its registers at 64;
+// measured on the k = 100 photon lookups: 1 (72 registers) 57 ms, 8 50.5 ms,
+// 10 (48 registers) 58.5 ms, 12 61 ms)
+#ifndef SKW_KNN_MINB
+#define SKW_KNN_MINB 8
+#endif
 
 
 struct Query {
@@ -66,6 +72,7 @@ struct Query {
   bool qle[3];  // q <= qf on the axis (decides q <= split when split == qf)
   float nf[3];  // the normal in float (filter pre-test)
   float cos_f, sin_f;  // cos_t, sin_t in float (filter pre-test)
+  float ke0, ke1;      // error bound of a float squared distance k: ke0 + ke1 k (key_err)
 };
 
 // Fills the float copy of the query point used by the pre-tests.
@@ -78,6 +85,8 @@ __device__ __forceinline__ void query_float(Query &Q) {
     Q.nf[k] = (float)Q.n[k];
   }
   Q.eq = e * 1.0001f;
+  Q.ke0 = 1.001f * (Q.eq + 9.0f * Q.eq * Q.eq) + 1e-37f;
+  Q.ke1 = 3.003f * Q.eq + 6.0e-7f;
   Q.cos_f = (float)Q.cos_t;
   Q.sin_f = (float)Q.sin_t;
 }
@@ -271,18 +280,18 @@ struct FCand {
 // Bound on |key - d2| for a point whose float squared distance is key: the
 // float query's rounding eq on each axis, the float differences and squares
 // (the terms of sq_bound summed: 2u d2 + 2 eq sum|d| + 3 eq^2 with
-// sum|d| <= sqrt(3 d2)), the float sum and the double result's rounding.
-__device__ __forceinline__ float key_err(float eq, float key) {
-  return 1.001f * (2.0f * eq * sqrtf(3.0f * key) + 9.0f * eq * eq) + 6.0e-7f * key + 1e-37f;
-}
+// sum|d| <= sqrt(3 d2) and 2 sqrt(3 d2) <= 1 + 3 d2), the float sum and the
+// double result's rounding: ke0 + ke1 key (Query::ke0, ke1).
+__device__ __forceinline__ float key_err(const Query &Q, float key) { return fmaf(Q.ke1, key, Q.ke0); }
 
 // (d2, idx) lexicographic on the exact distances, decided on the keys when
 // their bounds do not overlap.
 __device__ __forceinline__ bool fcand_less(const float4 *__restrict__ nodes, const Query &Q, const FCand &a,
                                            const FCand &b) {
-  const float ea = key_err(Q.eq, a.key), eb = key_err(Q.eq, b.key);
-  if (a.key + ea < b.key - eb) return true;
-  if (b.key + eb < a.key - ea) return false;
+  // decided when |a - b| exceeds both bounds (with a margin for this float arithmetic)
+  const float d = a.key - b.key, tol = 1.0001f * fmaf(Q.ke1, a.key + b.key, 2.0f * Q.ke0);
+  if (d < -tol) return true;
+  if (d > tol) return false;
   const double da = point_d2(__ldg(nodes + a.idx), Q), db = point_d2(__ldg(nodes + b.idx), Q);
   return da == db ? a.idx < b.idx : da < db;
 }
@@ -327,7 +336,7 @@ __device__ __forceinline__ void fheap_make(const float4 *__restrict__ nodes, con
 // the accepted points in visit order (the reference's array holds them
 // unordered); at k entries it becomes a heap.
 template <int KMAX>
-__global__ void __launch_bounds__(kKnnBlock) k_knn(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
+__global__ void __launch_bounds__(kKnnBlock, SKW_KNN_MINB) k_knn(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
                                              const double *__restrict__ dirs, int n, const double *__restrict__ q,
                                              const double *__restrict__ qn, int64_t nq, int k, double max_dist,
                                              double cos_t, int32_t *__restrict__ out_idx,
@@ -371,7 +380,7 @@ __global__ void __launch_bounds__(kKnnBlock) k_knn(const float4 *__restrict__ no
       return rex;
     };
     auto new_top = [&]() {
-      const float t = heap[0].key, e = key_err(Q.eq, t);
+      const float t = heap[0].key, e = key_err(Q, t);
       rlo = __fsub_rd(t, e);
       rhi = __fadd_ru(t, e);
       rex_ok = false;
