@@ -51,45 +51,48 @@ __device__ __forceinline__ int find_view(const ViewDev *__restrict__ views, int 
   return lo;
 }
 
-// Camera rays for the samples of global pixels [px_begin, px_begin + n_px).
+// Camera rays for the samples of global pixels [px_begin, px_begin + n_px):
+// PerspectiveCamera::GenerateRay (PerspectiveCamera.cpp:36-65; pinhole) in
+// float -- the rays are stored as floats, so double arithmetic would only
+// round differently, and GB300 runs it at ~1/64 of the float rate -- with
+// 32-bit index arithmetic (a pass holds fewer than 2^31 samples).
 __global__ void k_camera(const ViewDev *__restrict__ views, int n_views, int64_t px_begin, int n_px, int sppx,
                          int sppy, int ld, float4 *__restrict__ rays) {
-  const int spp = sppx * sppy;
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= (int64_t)n_px * spp) return;
-  const int64_t P = px_begin + s / spp;
-  const int j = (int)(s % spp);
+  const uint32_t spp = (uint32_t)(sppx * sppy);
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= (uint32_t)n_px * spp) return;
+  const uint32_t pl = s / spp, j = s - pl * spp;
+  const int64_t P = px_begin + pl;
   const int v = find_view(views, n_views, P);
   const CameraDev &cam = views[v].cam;
-  const int64_t px = P - views[v].px_begin;
-  const int x = (int)(px % cam.width), y = (int)(px / cam.width);
+  const uint32_t px = (uint32_t)(P - views[v].px_begin), w = (uint32_t)cam.width;
+  const uint32_t y = px / w, x = px - y * w;
   const uint64_t gid = (uint64_t)px * spp + j, seed = views[v].seed;
-  double ix, iy;
+  float ix, iy;
   if (ld) {
     // LDSampler image points: one scrambled (0,2)-sequence point per sample
     float u0, u1;
-    ld_2d(seed, (uint64_t)px, 0, (uint32_t)j, (uint32_t)spp, 0, 1, u0, u1);
-    ix = x + (double)u0;
-    iy = y + (double)u1;
+    ld_2d(seed, (uint64_t)px, 0, j, spp, 0, 1, u0, u1);
+    ix = (float)x + u0;
+    iy = (float)y + u1;
   } else {
     // stratified, jittered pixel sample (StratifiedSampling2D)
-    ix = x + ((j % sppx) + (double)rnd(seed, gid, 0)) / sppx;
-    iy = y + ((j / sppx) + (double)rnd(seed, gid, 1)) / sppy;
+    const uint32_t jy = j / (uint32_t)sppx, jx = j - jy * (uint32_t)sppx;
+    ix = (float)x + ((float)jx + rnd(seed, gid, 0)) / (float)sppx;
+    iy = (float)y + ((float)jy + rnd(seed, gid, 1)) / (float)sppy;
   }
-  // PerspectiveCamera::GenerateRay (pinhole)
-  const double cx = 2.0 * cam.x_tan * (ix - cam.width * 0.5) / cam.width;
-  const double cy = 2.0 * cam.y_tan * (iy - cam.height * 0.5) / cam.height;
-  const double *m = cam.c2w;
-  const double ox = m[3], oy = m[7], oz = m[11];
-  double dx = m[0] * cx + m[1] * cy + m[2];
-  double dy = m[4] * cx + m[5] * cy + m[6];
-  double dz = m[8] * cx + m[9] * cy + m[10];
-  const double il = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+  const float cx = cam.sx * (ix - 0.5f * (float)cam.width);
+  const float cy = cam.sy * (iy - 0.5f * (float)cam.height);
+  const float *m = cam.m;
+  float dx = m[0] * cx + m[1] * cy + m[2];
+  float dy = m[4] * cx + m[5] * cy + m[6];
+  float dz = m[8] * cx + m[9] * cy + m[10];
+  const float il = 1.0f / sqrtf(dx * dx + dy * dy + dz * dz);
   dx *= il;
   dy *= il;
   dz *= il;
-  rays[2 * s] = make_float4((float)ox, (float)oy, (float)oz, (float)dx);
-  rays[2 * s + 1] = make_float4((float)dy, (float)dz, 0.0f, __int_as_float(0x7f800000));
+  rays[2 * (uint64_t)s] = make_float4(m[3], m[7], m[11], dx);
+  rays[2 * (uint64_t)s + 1] = make_float4(dy, dz, 0.0f, __int_as_float(0x7f800000));
 }
 
 // The specular tree of a camera sample (LTEIntegrator::_SpecularReflect /

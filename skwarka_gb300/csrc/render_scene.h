@@ -105,6 +105,10 @@ struct CameraDev {
   double c2w[16];
   double x_tan, y_tan;
   int32_t width, height;
+  // float copies for the ray generation: the 3x4 camera-to-world rows and
+  // 2 tan / size per axis
+  float m[12];
+  float sx, sy;
 };
 
 // One view of a render: its camera, the index of its first pixel in the
