@@ -227,6 +227,101 @@ def cpu_baseline(meshes, rays, sample, rank, gpu_hits=None):
     return out, (n_nodes, n_tris), parity
 
 
+def ray_bytes(prims, cams, spp_x, spp_y, light_quads, sample=20_000, seed=11):
+    """Algorithmic bytes per ray query of a direct-lighting sample in this
+    scene: 32 (ray in) + 16 (hit out) + 32 N_nodes + 36 N_tris, with N the
+    mean nodes visited and triangles tested by the instrumented oracle walk
+    (the reference's traversal) on a sample of the frame's camera rays, of
+    shadow rays from their hits to a uniform point of a quad light (or to a
+    point light: light_quads of shape (n, 3)), and of
+    cosine-hemisphere BSDF rays from the hits.  Returns the per-kind figures,
+    the camera hit fraction and the mean over the rays of one sample (one
+    camera ray, one shadow and one BSDF ray per camera hit)."""
+    from oracle.api import Oracle
+    rng = np.random.default_rng(seed)
+    meshes = [(np.asarray(p.mesh.vertices, np.float32), np.asarray(p.mesh.triangles, np.int32)) for p in prims]
+    cam_rays = np.concatenate([scenes_camera_rays(c, spp_x, spp_y, seed) for c in cams])
+    cam_rays = cam_rays[rng.choice(len(cam_rays), size=min(sample, len(cam_rays)), replace=False)]
+    oa = Oracle().accel(meshes)
+    ch = oa.intersect(cam_rays, counters=True)
+    hit = ch["prim"] >= 0
+    p = cam_rays[hit, :3].astype(np.float64) + ch["t"][hit, None] * cam_rays[hit, 3:6].astype(np.float64)
+    if light_quads.ndim == 2:  # point lights
+        lp = light_quads[rng.integers(len(light_quads), size=len(p))]
+    else:
+        quad = light_quads[rng.integers(len(light_quads), size=len(p))]
+        u, v = rng.uniform(size=(2, len(p), 1))
+        lp = quad[:, 0] + u * (quad[:, 1] - quad[:, 0]) + v * (quad[:, 3] - quad[:, 0])
+    to = lp - p
+    dist = np.linalg.norm(to, axis=1)
+    sray = np.zeros((len(p), 8), np.float32)
+    sray[:, :3], sray[:, 3:6] = p, to / dist[:, None]
+    sray[:, 6], sray[:, 7] = 1e-4, dist - 1e-4
+    _, sn, st = oa.intersect_test(sray, counters=True)
+    d = rng.normal(size=(len(p), 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d *= np.sign((d * -cam_rays[hit, 3:6]).sum(1))[:, None]  # the hemisphere facing the camera
+    bray = np.zeros((len(p), 8), np.float32)
+    bray[:, :3], bray[:, 3:6], bray[:, 6], bray[:, 7] = p, d, 1e-4, np.inf
+    bh = oa.intersect(bray, counters=True)
+
+    def b(nodes, tris):
+        return 48.0 + 32.0 * float(np.mean(nodes)) + 36.0 * float(np.mean(tris))
+    f = float(hit.mean())
+    cb, sb, bb = b(ch["nodes"], ch["tris"]), b(sn, st), b(bh["nodes"], bh["tris"])
+    return {"camera_ray_bytes": cb, "shadow_ray_bytes": sb, "bsdf_ray_bytes": bb, "camera_hit_fraction": f,
+            "mean_ray_bytes": (cb + f * (sb + bb)) / (1.0 + 2.0 * f)}
+
+
+def scenes_camera_rays(cam, spp_x, spp_y, seed):
+    from skwarka_gb300 import scenes
+    return scenes.camera_rays(cam, spp_x, spp_y, seed=seed)
+
+
+def render_roofline(msamples_per_s, rays_per_sample, rb, what, extra_per_ray=0.0):
+    """HBM roofline of a render line: bytes per sample = rays traced per
+    sample (counted on the device over the timed frames) x the mean
+    algorithmic bytes per ray (+ extra_per_ray) + 24 bytes of film + 68 bytes
+    of shading reads (triangle attributes and material) per camera hit."""
+    peak, kind = peaks()
+    bps = rays_per_sample * (rb["mean_ray_bytes"] + extra_per_ray) + 24.0 + 68.0 * rb["camera_hit_fraction"]
+    achieved = msamples_per_s * 1e6 * bps / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "bytes_per_sample": bps, "rays_per_sample": rays_per_sample, "peak_source": kind, "what": what, **rb}
+
+
+def photon_ray_bytes(prims, light_pos, sample=20_000, seed=12):
+    """Algorithmic bytes per ray query of photon shooting on this scene
+    (32 + 16 + 32 N_nodes + 36 N_tris, N from the instrumented oracle walk):
+    rays leaving the point light in uniform directions, and cosine bounce
+    rays from their hits.  Returns (emitted, bounce) bytes per ray."""
+    from oracle.api import Oracle
+    rng = np.random.default_rng(seed)
+    meshes = [(np.asarray(p.mesh.vertices, np.float32), np.asarray(p.mesh.triangles, np.int32)) for p in prims]
+    oa = Oracle().accel(meshes)
+    d = rng.normal(size=(sample, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    er = np.zeros((sample, 8), np.float32)
+    er[:, :3], er[:, 3:6], er[:, 6], er[:, 7] = np.asarray(light_pos), d, 0.0, np.inf
+    eh = oa.intersect(er, counters=True)
+    hit = eh["prim"] >= 0
+    p = er[hit, :3].astype(np.float64) + eh["t"][hit, None] * er[hit, 3:6].astype(np.float64)
+    bd = rng.normal(size=(len(p), 3))
+    bd /= np.linalg.norm(bd, axis=1, keepdims=True)
+    bd *= np.sign((bd * -er[hit, 3:6]).sum(1))[:, None]
+    br = np.zeros((len(p), 8), np.float32)
+    br[:, :3], br[:, 3:6], br[:, 6], br[:, 7] = p, bd, 1e-4, np.inf
+    bh = oa.intersect(br, counters=True)
+
+    def b(h):
+        return 48.0 + 32.0 * float(np.mean(h["nodes"])) + 36.0 * float(np.mean(h["tris"]))
+    return b(eh), b(bh)
+
+
+def light_quads(prims):
+    return np.stack([np.asarray(p.mesh.vertices, np.float64)[:4] for p in prims if any(p.emission)])
+
+
 def knn_parity(gpu: dict, gpu_perm: np.ndarray, ref: dict, ref_perm: np.ndarray) -> dict:
     """Agreement of the GPU's k-NN answers with the reference's on the same
     queries and photons: found counts, index sets, heap order and squared
@@ -265,6 +360,7 @@ def render_bench(args, dev, ctx, measure_cpu):
     torch.cuda.synchronize()
     steps = max(5, args.steps)
     l0 = ctx.launch_count()
+    r0 = sc.accelerator().rays_traced()
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s.record(stream)
     for i in range(steps):
@@ -273,6 +369,7 @@ def render_bench(args, dev, ctx, measure_cpu):
     torch.cuda.synchronize()
     dev_ms = s.elapsed_time(e) / steps
     launches = (ctx.launch_count() - l0) / steps
+    rays_per_sample = (sc.accelerator().rays_traced() - r0) / (steps * samples)
     t0 = time.perf_counter()
     for i in range(steps):
         sc.render_direct(cam, 2, 2, seed=200 + i, out=film)
@@ -295,6 +392,9 @@ def render_bench(args, dev, ctx, measure_cpu):
                    "d2h_bytes_per_step": hfilm.numel() * 4},
            "gpu_launches_per_frame": launches,
            "ld_sampler": {"value": samples / ld_ms / 1e3, "unit": "Msamples/s", "ms_per_frame": ld_ms}}
+    out["roofline"] = render_roofline(out["value"], rays_per_sample, ray_bytes(prims, [cam], 2, 2, light_quads(prims)),
+                                      "rays traced per sample x algorithmic bytes per ray (the oracle's visit "
+                                      "counts on the frame's camera, shadow and BSDF rays) + film + shading reads")
     if measure_cpu:
         from oracle.api import Reference
         if Reference.available():
@@ -327,6 +427,7 @@ def specular_bench(args, dev, ctx, measure_cpu):
     torch.cuda.synchronize()
     steps = max(5, args.steps)
     l0 = ctx.launch_count()
+    r0 = sc.accelerator().rays_traced()
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s.record(stream)
     for i in range(steps):
@@ -334,9 +435,15 @@ def specular_bench(args, dev, ctx, measure_cpu):
     e.record(stream)
     torch.cuda.synchronize()
     ms = s.elapsed_time(e) / steps
+    rays_per_sample = (sc.accelerator().rays_traced() - r0) / (steps * samples)
     out = {"workload": "direct lighting + specular recursion (depth 6), glass sphere over a floor, 256x256, 2x2 spp",
            "unit": "Msamples/s", "value": samples / ms / 1e3, "ms_per_frame": ms,
-           "gpu_launches_per_frame": (ctx.launch_count() - l0) / steps}
+           "gpu_launches_per_frame": (ctx.launch_count() - l0) / steps,
+           "mrays_per_s": samples * rays_per_sample / ms / 1e3}
+    out["roofline"] = render_roofline(out["value"], rays_per_sample, ray_bytes(prims, [cam], 2, 2, light_quads(prims)),
+                                      "rays traced per sample (the specular trees included) x algorithmic bytes per "
+                                      "ray (the oracle's visit counts on the frame's camera, shadow and BSDF rays) + "
+                                      "film + shading reads")
     if measure_cpu:
         from oracle.api import Reference
         if Reference.available():
@@ -392,10 +499,17 @@ def batch_bench(args, dev, ctx):
     tune_s = time.perf_counter() - t0
     b.run(films)
     l0 = ctx.launch_count()
+    r0 = sc.accelerator().rays_traced()
     batch_ms = timed(lambda: b.run(films), reps)
     launches = (ctx.launch_count() - l0) / reps
+    rays_per_sample = (sc.accelerator().rays_traced() - r0) / (reps * samples)
     identical = bool(torch.equal(films, ref_img))
+    roof = render_roofline(samples / batch_ms / 1e3, rays_per_sample,
+                           ray_bytes(prims, cams[::8], 4, 2, light_quads(prims)),
+                           "batched run: rays traced per sample x algorithmic bytes per ray (the oracle's visit "
+                           "counts on camera, shadow and BSDF rays of 8 of the views) + film + shading reads")
     return {"workload": "64 views of the 201,742-tri scene, films 64^2..1024^2 log-uniform, 8 spp, 1 light sample",
+            "roofline": roof,
             "samples_per_run": samples, "unit": "Msamples/s",
             "plain_value": samples / plain_ms / 1e3, "batched_value": samples / batch_ms / 1e3,
             "speedup": plain_ms / batch_ms, "plain_ms": plain_ms, "batched_ms": batch_ms,
@@ -437,12 +551,19 @@ def adjoint_bench(args, dev, ctx):
         torch.cuda.synchronize()
         return s.elapsed_time(e) / reps
 
+    acc = sc.accelerator()
     fwd_ms = timed(lambda: r.forward_image(albedo, 1.0))
+    r0 = acc.rays_traced()
     adj_ms = timed(lambda: r.adjoint(albedo, 1.0, d_img))
     samples = 512 * 512 * 16
+    rays_per_sample = (acc.rays_traced() - r0) / (6 * samples)  # timed() runs the adjoint 1 + 5 times
     out = {"workload": "adjoint of direct lighting, 201,742-tri scene, 512x512, 16 spp, per-triangle albedo + "
                        "emission scale", "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
            "forward_msamples_s": samples / fwd_ms / 1e3, "adjoint_msamples_s": samples / adj_ms / 1e3}
+    out["roofline"] = render_roofline(samples / adj_ms / 1e3, rays_per_sample,
+                                      ray_bytes(prims, [cam], 4, 4, light_quads(prims)),
+                                      "adjoint: rays traced per sample x (algorithmic bytes per ray + 12 bytes of "
+                                      "gradient atomics per ray) + film + shading reads", extra_per_ray=12.0)
     # the same with the configuration's homogeneous medium in the box
     from skwarka_gb300.render import Medium
     sc.set_medium(Medium(sigma_a=(0.05,) * 3, sigma_s=(0.2,) * 3, g=0.3, step=0.05))
@@ -477,15 +598,31 @@ def photon_bench(args, dev, ctx, measure_cpu):
     paths = 2_000_000
     PhotonMap.shoot(sc, 100_000, max_bounces=8, rr_probability=0.7, seed=1)  # warm-up
     torch.cuda.synchronize()
+    sacc = sc.accelerator()
+    r0 = sacc.rays_traced()
     t0 = time.perf_counter()
     pm = PhotonMap.shoot(sc, paths, max_bounces=8, rr_probability=0.7, seed=2)
     wall = time.perf_counter() - t0
+    shoot_rays = sacc.rays_traced() - r0
     info = pm.info()
     out = {"workload": "2M photon paths (<= 8 bounces, RR p=0.7) on the 1,098,576-tri scene, matte 0.6, "
                        "point light I=50; k=100 r=0.05 lookups at 512x512x16 primary hits; render 512x512x4 spp",
            "paths": paths, "shoot_paths_per_s": paths / (info["shoot_ms"] / 1e3), "shoot_ms": info["shoot_ms"],
            "maps_build_ms": info["build_ms"], "shoot_and_build_wall_s": wall,
            "photons": {k: info["n_" + k] for k in ("caustic", "direct", "indirect", "irradiance")}}
+    # shooting roofline: rays traced (emitted + bounces, counted on the device)
+    # at the oracle's bytes per emitted / bounce ray, plus 28 bytes per stored
+    # photon (position, normal and direction ids, weight)
+    eb, bb = photon_ray_bytes(prims, lights[0].position)
+    stored = sum(info["n_" + k] for k in ("caustic", "direct", "indirect"))
+    shoot_bytes = paths * eb + max(shoot_rays - paths, 0) * bb + 28.0 * stored
+    peak, peak_kind = peaks()
+    ach = shoot_bytes / (info["shoot_ms"] / 1e3) / 1e9
+    out["shoot_roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                             "rays_per_path": shoot_rays / paths, "emitted_ray_bytes": eb, "bounce_ray_bytes": bb,
+                             "peak_source": peak_kind,
+                             "what": "rays traced (device count) x the oracle's bytes per emitted / bounce ray + 28 B "
+                                     "per stored photon, over the shooting time"}
     # the same shoot with the reference's own rules (luminance Russian
     # roulette, no bounce cap within the 1,024 the GPU allows): the figure to
     # set beside the reference's ShootPhotons
@@ -541,12 +678,22 @@ def photon_bench(args, dev, ctx, measure_cpu):
     cam4 = camf(512, 512)
     render_photon(sc, pm, camf(64, 64), 2, 2, gather_samples=16)
     torch.cuda.synchronize()
+    r0 = sacc.rays_traced()
     s.record()
     render_photon(sc, pm, cam4, 2, 2, gather_samples=16, seed=4)
     e.record()
     torch.cuda.synchronize()
     rms = s.elapsed_time(e)
-    out["render"] = {"samples": 512 * 512 * 4, "ms": rms, "msamples_per_s": 512 * 512 * 4 / rms / 1e3}
+    rsamples = 512 * 512 * 4
+    rrays = (sacc.rays_traced() - r0) / rsamples
+    out["render"] = {"samples": rsamples, "ms": rms, "msamples_per_s": rsamples / rms / 1e3,
+                     "roofline": render_roofline(rsamples / rms / 1e3, rrays,
+                                                 ray_bytes(prims, [cam4], 2, 2,
+                                                           np.asarray([l.position for l in lights], np.float64)),
+                                                 "rays traced per sample (camera, shadow and gather rays) x "
+                                                 "algorithmic bytes per ray (the oracle's visit counts on the frame's "
+                                                 "camera, shadow and cosine rays) + film + shading reads; the "
+                                                 "irradiance-photon lookups of the gather hits are not counted")}
     if measure_cpu:
         from oracle.api import Reference
         if Reference.available():

@@ -157,6 +157,10 @@ int skw_accel_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
                      int32_t n_prims, skw_accel **out);
 void skw_accel_destroy(skw_accel *accel);
 int skw_accel_get_info(const skw_accel *accel, skw_accel_info *info);
+/* Rays traced so far by every query, render and photon launch on this
+ * accelerator (queue lengths as the device saw them); waits for the device.
+ * A statistic of this library: the reference keeps none. */
+int skw_accel_rays_traced(const skw_accel *accel, uint64_t *out);
 
 /* Copies out the flattened tree for inspection: nodes as 8 x 32-bit words
  * (min xyz, max xyz as float bits; word 6: first child / first triangle;

@@ -60,6 +60,7 @@ SIGNATURES = [
                                    C.POINTER(_P)]),
     ("skw_accel_destroy", None, [_P]),
     ("skw_accel_get_info", C.c_int, [_P, C.POINTER(skw_accel_info)]),
+    ("skw_accel_rays_traced", C.c_int, [_P, C.POINTER(C.c_uint64)]),
     ("skw_accel_export", C.c_int, [_P, _P, _P, _P]),
     ("skw_intersect", C.c_int, [_P, _P, C.c_int64, _P, _P]),
     ("skw_intersect_test", C.c_int, [_P, _P, C.c_int64, _P, _P]),

@@ -115,6 +115,12 @@ class TriangleAccelerator:
             _lib.load().skw_accel_destroy(h)
         self.handle = None
 
+    def rays_traced(self) -> int:
+        """Rays traced so far by every launch on this accelerator (waits for the device)."""
+        v = C.c_uint64()
+        _lib.check(_lib.load().skw_accel_rays_traced(self.handle, C.byref(v)), self.ctx.handle)
+        return int(v.value)
+
     def export(self):
         """(nodes uint32 (n_nodes, 8), tri_prim int32, tri_index int32) of the flattened tree."""
         nn, nt = self.info["n_nodes"], self.info["n_triangles"]

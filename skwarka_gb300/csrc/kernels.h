@@ -42,6 +42,9 @@ int traversal_max_ctas_per_sm(int stack_cap);
 // then run the exact instance-aware kernel.
 void register_instances(const void *nodes, const void *inst, const void *ext);
 void unregister_instances(const void *nodes);
+// Every traversal launch on the accelerator whose device node array is
+// `nodes` adds its ray count to *traced (a device counter).
+void register_ray_counter(const void *nodes, unsigned long long *traced);
 // Double rays (skw_ray_d, 64 bytes each): closest = true writes skw_hit_d
 // (double t, prim, tri; t = +inf, ids -1 on a miss), false uint8_t per ray.
 cudaError_t launch_traversal_d(bool closest, int stack_cap, const void *nodes, const void *tris, const void *rays,

@@ -190,7 +190,8 @@ int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_acce
   }
   const size_t nb = ft.nodes.size() * sizeof(DevNode), tb = std::max<size_t>(ft.tris.size(), 1) * sizeof(DevTri);
   if ((e = cudaMalloc(&a->d_nodes, nb)) != cudaSuccess || (e = cudaMalloc(&a->d_tris, tb)) != cudaSuccess ||
-      (e = cudaMalloc(&a->d_status, sizeof(unsigned))) != cudaSuccess) {
+      (e = cudaMalloc(&a->d_status, sizeof(unsigned))) != cudaSuccess ||
+      (e = cudaMalloc(&a->d_traced, sizeof(unsigned long long))) != cudaSuccess) {
     skw_accel_destroy(a);
     return cuda_fail(ctx, e, "cudaMalloc (accelerator)");
   }
@@ -207,7 +208,8 @@ int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_acce
       (!ft.tris.empty() &&
        (e = cudaMemcpy(a->d_tris, ft.tris.data(), ft.tris.size() * sizeof(DevTri), cudaMemcpyHostToDevice)) !=
            cudaSuccess) ||
-      (e = cudaMemset(a->d_status, 0, sizeof(unsigned))) != cudaSuccess) {
+      (e = cudaMemset(a->d_status, 0, sizeof(unsigned))) != cudaSuccess ||
+      (e = cudaMemset(a->d_traced, 0, sizeof(unsigned long long))) != cudaSuccess) {
     skw_accel_destroy(a);
     return cuda_fail(ctx, e, "upload (accelerator)");
   }
@@ -230,6 +232,7 @@ int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_acce
   a->h_subtree_roots = ft.subtree_roots;
   // instances need the stack of the top tree and of the deepest subtree at once
   if (a->d_inst) skw::register_instances(a->d_nodes, a->d_inst, a->d_leaf_ext);
+  skw::register_ray_counter(a->d_nodes, a->d_traced);
   *out = a;
   return SKW_OK;
 }
@@ -248,13 +251,25 @@ int skw_accel_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
 
 void skw_accel_destroy(skw_accel *a) {
   if (!a) return;
-  if (a->d_inst) skw::unregister_instances(a->d_nodes);
+  if (a->d_nodes) skw::unregister_instances(a->d_nodes);
+  cudaFree(a->d_traced);
   cudaFree(a->d_inst);
   cudaFree(a->d_leaf_ext);
   cudaFree(a->d_nodes);
   cudaFree(a->d_tris);
   cudaFree(a->d_status);
   delete a;
+}
+
+int skw_accel_rays_traced(const skw_accel *a, uint64_t *out) {
+  if (!a || !out) return fail(a ? a->ctx : nullptr, SKW_ERR_ARG, "null argument");
+  cudaError_t e = cudaSetDevice(a->ctx->device);
+  unsigned long long v = 0;
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&v, a->d_traced, sizeof(v), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(a->ctx, e, "rays traced");
+  *out = (uint64_t)v;
+  return SKW_OK;
 }
 
 int skw_accel_get_info(const skw_accel *a, skw_accel_info *info) {

@@ -34,6 +34,7 @@ struct skw_accel {
   skw::DevInst *d_inst = nullptr;     // instances (null: none)
   skw::LeafExt *d_leaf_ext = nullptr; // leaves holding instances
   unsigned *d_status = nullptr;
+  unsigned long long *d_traced = nullptr;  // rays traced by all launches on this accelerator
   int stack_cap = 0;
   float scene_abs = 0.0f;  // largest absolute vertex coordinate
   skw_accel_info info{};

@@ -295,6 +295,13 @@ __device__ __forceinline__ bool node_visit(const float4 na, const float4 nb, con
 #ifndef SKW_TRAV_STACK8
 #define SKW_TRAV_STACK8 0
 #endif
+// With SKW_TRAV_SLAB_ROUND the slab data (12 words) is recomputed from the
+// ray at the start of every walk round instead of being held through the
+// triangle tests, which shortens the register-resident state that the
+// walk and the triangle tests would otherwise both carry.
+#ifndef SKW_TRAV_SLAB_ROUND
+#define SKW_TRAV_SLAB_ROUND 0
+#endif
 
 template <int CAP>
 struct Stack {
@@ -543,9 +550,11 @@ template <int CAP, bool CLOSEST, bool DRAY>
 __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, const float4 *__restrict__ rays,
             int n, const int *__restrict__ n_dev, float scene_abs, const int32_t *__restrict__ out_index,
-            void *__restrict__ out, unsigned *__restrict__ status, int *__restrict__ work, int surf) {
+            void *__restrict__ out, unsigned *__restrict__ status, int *__restrict__ work, int surf,
+            unsigned long long *__restrict__ traced) {
   static_assert(!DRAY || SKW_TRAV_POSTPONE, "double rays use the postponed-leaf walk");
   if (n_dev) n = min(n, *n_dev);  // a queue whose length lives on the device
+  if (traced && blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(traced, (unsigned long long)n);
   constexpr int SCAP = Stack<CAP>::SCAP;
   __shared__ uint32_t s_a[SCAP][SKW_TRAV_BLOCK];
   __shared__ float s_lo[SCAP][SKW_TRAV_BLOCK];
@@ -590,7 +599,9 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
   RayF r_reg{};
 #define SKW_RAY() r_reg
 #endif
+#if !SKW_TRAV_SLAB_ROUND
   SlabRay s{};
+#endif
   uint32_t cur_a = 0, cur_b = 0;
   int best_slot = -1;
   double best_t = 0.0;             // DRAY: the exact t of the best hit
@@ -638,7 +649,11 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
 #else
         r_reg = rl;
 #endif
+#if SKW_TRAV_SLAB_ROUND
+        const SlabRay s = make_slab_ray(rl, scene_abs, DRAY ? 9.0f : 6.0f);
+#else
         s = make_slab_ray(rl, scene_abs, DRAY ? 9.0f : 6.0f);
+#endif
         best_slot = -1;
         lo_t = hi_t = rl.tmax;
         flags = 8u;
@@ -672,6 +687,9 @@ __global__ void __launch_bounds__(SKW_TRAV_BLOCK, SKW_TRAV_MINB)
     // the rest of the iteration as one group; without an explicit sync they
     // were measured to split into 2-3 groups that each walked on their own.
     __syncwarp(busy);
+#if SKW_TRAV_SLAB_ROUND
+    const SlabRay s = make_slab_ray(SKW_RAY(), scene_abs, DRAY ? 9.0f : 6.0f);
+#endif
 
 #if SKW_TRAV_POSTPONE
     // Node steps continue past a lane's first leaf (postponed) until all but
@@ -1029,8 +1047,10 @@ template <int CAP, bool CLOSEST, bool DRAY>
 __global__ void __launch_bounds__(128)
     k_trace_inst(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, const InstDev *__restrict__ inst,
                  const uint4 *__restrict__ ext, const float4 *__restrict__ rays, int n, const int *__restrict__ n_dev,
-                 const int32_t *__restrict__ out_index, void *__restrict__ out, unsigned *__restrict__ status) {
+                 const int32_t *__restrict__ out_index, void *__restrict__ out, unsigned *__restrict__ status,
+                 unsigned long long *__restrict__ traced) {
   if (n_dev) n = min(n, *n_dev);
+  if (traced && blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(traced, (unsigned long long)n);
   uint32_t stk[2 * CAP];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double o[3], d[3], tmin, tmax;
@@ -1132,9 +1152,13 @@ cudaError_t device_sms(int dev, int &sms) {
 
 // Device tables of the accelerators that have instances, by their node
 // array (the traversal launches receive the node pointer).
+// Per-accelerator launch tables, keyed by the device node array: the
+// instance tables (null: no instances) and the accelerator's traced-ray
+// counter (null: none).
 struct InstTables {
-  const void *inst;
-  const void *ext;
+  const void *inst = nullptr;
+  const void *ext = nullptr;
+  unsigned long long *traced = nullptr;
 };
 std::mutex &inst_mutex() {
   static std::mutex m;
@@ -1165,16 +1189,16 @@ cudaError_t launch_inst(int variant, const void *nodes, const void *tris, const 
   const uint4 *ex = (const uint4 *)T.ext;
   switch (variant) {
     case 0:
-      k_trace_inst<CAP, false, false><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status);
+      k_trace_inst<CAP, false, false><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status, T.traced);
       break;
     case 1:
-      k_trace_inst<CAP, true, false><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status);
+      k_trace_inst<CAP, true, false><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status, T.traced);
       break;
     case 2:
-      k_trace_inst<CAP, false, true><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status);
+      k_trace_inst<CAP, false, true><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status, T.traced);
       break;
     default:
-      k_trace_inst<CAP, true, true><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status);
+      k_trace_inst<CAP, true, true><<<grid, block, 0, stream>>>(nd, tr, in, ex, ry, (int)n, n_dev, out_index, out, status, T.traced);
   }
   return cudaGetLastError();
 }
@@ -1188,7 +1212,7 @@ cudaError_t launch_cap(int variant, const void *nodes, const void *tris, const v
   if (e != cudaSuccess || (e = cap_prepare<CAP>(dev)) != cudaSuccess || (e = device_sms(dev, sms)) != cudaSuccess)
     return e;
   InstTables T;
-  if (find_instances(nodes, T))
+  if (find_instances(nodes, T) && T.inst)
     return launch_inst<CAP>(variant, nodes, tris, T, rays, n, n_dev, out_index, out, status, stream, sms);
   int per_sm = cap_occupancy<CAP>(dev, variant).load(std::memory_order_acquire);
   if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
@@ -1204,19 +1228,19 @@ cudaError_t launch_cap(int variant, const void *nodes, const void *tris, const v
   switch (variant) {
     case 0:
       k_trace<CAP, false, false><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
-                                                             status, work, surf);
+                                                             status, work, surf, T.traced);
       break;
     case 1:
       k_trace<CAP, true, false><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
-                                                            status, work, surf);
+                                                            status, work, surf, T.traced);
       break;
     case 2:
       k_trace<CAP, false, true><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
-                                                            status, work, surf);
+                                                            status, work, surf, T.traced);
       break;
     default:
       k_trace<CAP, true, true><<<grid, block, 0, stream>>>(nd, tr, ry, (int)n, n_dev, scene_abs, out_index, out,
-                                                           status, work, surf);
+                                                           status, work, surf, T.traced);
   }
   return cudaGetLastError();
 }
@@ -1283,7 +1307,14 @@ cudaError_t launch_traversal(bool closest, int stack_cap, const void *nodes, con
 
 void register_instances(const void *nodes, const void *inst, const void *ext) {
   std::lock_guard<std::mutex> lock(inst_mutex());
-  inst_registry()[nodes] = InstTables{inst, ext};
+  InstTables &t = inst_registry()[nodes];
+  t.inst = inst;
+  t.ext = ext;
+}
+
+void register_ray_counter(const void *nodes, unsigned long long *traced) {
+  std::lock_guard<std::mutex> lock(inst_mutex());
+  inst_registry()[nodes].traced = traced;
 }
 
 void unregister_instances(const void *nodes) {
