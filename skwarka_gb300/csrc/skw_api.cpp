@@ -79,6 +79,7 @@ void skw_ctx_destroy(skw_ctx *ctx) {
   for (int i = 0; i < 2; ++i) {
     if (ctx->host_st[i]) cudaStreamDestroy(ctx->host_st[i]);
     if (ctx->host_ev[i]) cudaEventDestroy(ctx->host_ev[i]);
+    if (ctx->aux_st[i]) cudaStreamDestroy(ctx->aux_st[i]);
   }
   if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   delete ctx;

@@ -5,6 +5,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -24,6 +25,10 @@ struct skw_ctx {
   // kept (creating and destroying them per call cost ~0.1 ms).
   cudaStream_t host_st[2] = {nullptr, nullptr};
   cudaEvent_t host_ev[2] = {nullptr, nullptr};
+  // The renders' side streams (a level's shadow and BSDF traversals), made
+  // on first use under aux_mu and kept.
+  std::mutex aux_mu;
+  cudaStream_t aux_st[2] = {nullptr, nullptr};
 };
 
 // A device-resident accelerator (skw_accel_create / _from_flat).

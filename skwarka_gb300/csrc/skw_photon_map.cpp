@@ -79,23 +79,63 @@ cudaError_t build_map(Map &m) {
 
 const PhotonRec &tree_photon(const Map &m, int64_t t) { return m.input[(size_t)m.perm[(size_t)t]]; }
 
-// _ConstructIrradiancePhotonMap: every 10th indirect photon (in tree order)
-// becomes an irradiance photon whose irradiance is estimated from the three
-// maps; then the 0.1 % percentile of the distance from every 11th indirect
-// photon to its nearest irradiance photon bounds the irradiance lookups.
-int build_irradiance(skw_photon_map *pm, cudaStream_t st) {
+// Device buffers of the irradiance construction, freed on every path.
+struct IrrBuffers {
+  double *q = nullptr, *qn = nullptr, *sq = nullptr, *sqn = nullptr;
+  int32_t *idx[3] = {nullptr, nullptr, nullptr}, *cnt[3] = {nullptr, nullptr, nullptr};
+  double *d2[3] = {nullptr, nullptr, nullptr};
+  float *ext = nullptr, *intr = nullptr;
+  int32_t *near = nullptr;
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+  ~IrrBuffers() {
+    for (void *p : {(void *)q, (void *)qn, (void *)sq, (void *)sqn, (void *)ext, (void *)intr, (void *)near}) cudaFree(p);
+    for (int i = 0; i < 3; ++i) {
+      cudaFree(idx[i]);
+      cudaFree(cnt[i]);
+      cudaFree(d2[i]);
+    }
+    for (int i = 0; i < 2; ++i) {
+      if (side[i]) cudaStreamDestroy(side[i]);
+      if (join[i]) cudaEventDestroy(join[i]);
+    }
+    if (fork) cudaEventDestroy(fork);
+  }
+};
+
+// The maps' kd-trees and _ConstructIrradiancePhotonMap: every 10th indirect
+// photon (in tree order) becomes an irradiance photon whose irradiance is
+// estimated from the three maps; then the 0.1 % percentile of the distance
+// from every 11th indirect photon to its nearest irradiance photon bounds
+// the irradiance lookups.
+//
+// The work is one pipeline.  The indirect map's tree is built first (the
+// irradiance photons are its photons); its lookups start on a side stream
+// while the host builds the direct and caustic trees, whose lookups start
+// on a second side stream as each is uploaded; the irradiance photons' own
+// tree (built from their positions alone) and the lookup-distance queries
+// run on the caller's stream meanwhile.  The three maps' estimates are then
+// added on the caller's stream in map order (caustic, direct, indirect), so
+// every float sum is the one the sequential construction makes.
+int build_maps(skw_photon_map *pm, cudaStream_t st) {
   skw_ctx *ctx = pm->ctx;
-  const Map &dm = pm->maps[1], &im = pm->maps[2];
+  Map &im = pm->maps[2];
+  cudaError_t e = build_map(im);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "photon map upload");
+  if (im.n == 0) {  // no indirect map: no irradiance photons
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = build_map(pm->maps[i]);
+    return e == cudaSuccess ? SKW_OK : cuda_fail(ctx, e, "photon map upload");
+  }
   const std::vector<double> &dirs = skw::direction_table();
-  if (im.n == 0) return SKW_OK;  // no indirect map: nothing to do
   for (int64_t i = 0; i < im.n; i += 10) {
     const PhotonRec &r = tree_photon(im, i);
     pm->irr_pos.insert(pm->irr_pos.end(), r.p, r.p + 3);
     pm->irr_nrm.push_back(r.nrm);
   }
   const int64_t nq = (int64_t)pm->irr_nrm.size();
-  const double da = dm.n == 0 ? 0.0 : pm->scene_area / dm.n;
-  const double ia = im.n == 0 ? 0.0 : pm->scene_area / im.n;
+  const int64_t nd = (int64_t)pm->maps[1].input.size(), nc = (int64_t)pm->maps[0].input.size();
+  const double da = nd == 0 ? 0.0 : pm->scene_area / nd;
+  const double ia = pm->scene_area / im.n;
   pm->lookup_dist[1] = std::sqrt(da * kLookupIrradiance * kInvPi);
   pm->lookup_dist[2] = std::sqrt(ia * kLookupIrradiance * kInvPi);
   pm->lookup_dist[0] = std::max(pm->lookup_dist[1], pm->lookup_dist[2]);
@@ -105,59 +145,101 @@ int build_irradiance(skw_photon_map *pm, cudaStream_t st) {
       q[(size_t)(3 * i + k)] = (double)pm->irr_pos[(size_t)(3 * i + k)];
       qn[(size_t)(3 * i + k)] = dirs[3 * (size_t)pm->irr_nrm[(size_t)i] + k];
     }
-  // Lookups in chunks of queries (k-NN output is 12 bytes per neighbour).
-  const int64_t chunk = std::min<int64_t>(nq, (int64_t)1 << 20);
-  double *d_q = nullptr, *d_qn = nullptr;
-  int32_t *d_idx = nullptr, *d_cnt = nullptr;
-  double *d_d2 = nullptr;
-  float *d_ext = nullptr, *d_int = nullptr;
-  cudaError_t e = cudaMalloc(&d_q, (size_t)nq * 24);
-  if (e == cudaSuccess) e = cudaMalloc(&d_qn, (size_t)nq * 24);
-  if (e == cudaSuccess) e = cudaMalloc(&d_idx, (size_t)chunk * kLookupIrradiance * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&d_d2, (size_t)chunk * kLookupIrradiance * 8);
-  if (e == cudaSuccess) e = cudaMalloc(&d_cnt, (size_t)chunk * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&d_ext, (size_t)nq * 12);
-  if (e == cudaSuccess) e = cudaMalloc(&d_int, (size_t)nq * 12);
-  if (e == cudaSuccess) e = cudaMemcpy(d_q, q.data(), (size_t)nq * 24, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(d_qn, qn.data(), (size_t)nq * 24, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_ext, 0, (size_t)nq * 12, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_int, 0, (size_t)nq * 12, st);
-  bool first = true;
-  for (int mi = 0; mi < 3 && e == cudaSuccess; ++mi) {
-    const Map &m = pm->maps[mi];
-    if (m.n == 0) continue;  // a null map adds nothing
-    for (int64_t q0 = 0; q0 < nq && e == cudaSuccess; q0 += chunk) {
-      const int64_t c = std::min(chunk, nq - q0);
-      e = skw::launch_knn(m.d_nodes, m.d_nids, pm->d_dirs, (int)m.n, d_q + 3 * q0, d_qn + 3 * q0, c,
-                          kLookupIrradiance, pm->lookup_dist[mi], kMaxNormalDeviationCos, d_idx, d_d2, d_cnt, nullptr,
-                          nullptr, pm->d_status, st);
-      if (e == cudaSuccess)
-        e = skw::launch_irradiance_sum(m.d_nodes, m.d_weight, m.d_dirid, pm->d_dirs, d_q + 3 * q0, d_qn + 3 * q0,
-                                       d_idx, d_cnt, c, kLookupIrradiance, (double)m.paths, pm->lookup_dist[mi], first,
-                                       d_ext + 3 * q0, d_int + 3 * q0, st);
+  // queries of the lookup-distance percentile: every 11th indirect photon
+  const int64_t step = 11, ns = (im.n + step - 1) / step;
+  std::vector<double> sq((size_t)ns * 3), sqn((size_t)ns * 3);
+  for (int64_t i = 0; i < ns; ++i) {
+    const PhotonRec &r = tree_photon(im, i * step);
+    for (int k = 0; k < 3; ++k) {
+      sq[(size_t)(3 * i + k)] = (double)r.p[k];
+      sqn[(size_t)(3 * i + k)] = dirs[3 * (size_t)r.nrm + k];
     }
-    first = false;
   }
+  // Lookups in chunks of queries (k-NN output is 12 bytes per neighbour),
+  // each map's into its own buffers.
+  const int64_t chunk = std::min<int64_t>(nq, (int64_t)1 << 20);
+  const bool has[3] = {nc > 0, nd > 0, true};
+  IrrBuffers B;
+  e = cudaMalloc(&B.q, (size_t)nq * 24);
+  if (e == cudaSuccess) e = cudaMalloc(&B.qn, (size_t)nq * 24);
+  for (int mi = 0; mi < 3 && e == cudaSuccess; ++mi) {
+    if (!has[mi]) continue;
+    if ((e = cudaMalloc(&B.idx[mi], (size_t)chunk * kLookupIrradiance * 4)) == cudaSuccess &&
+        (e = cudaMalloc(&B.d2[mi], (size_t)chunk * kLookupIrradiance * 8)) == cudaSuccess)
+      e = cudaMalloc(&B.cnt[mi], (size_t)chunk * 4);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&B.ext, (size_t)nq * 12);
+  if (e == cudaSuccess) e = cudaMalloc(&B.intr, (size_t)nq * 12);
+  if (e == cudaSuccess) e = cudaMalloc(&B.sq, (size_t)ns * 24);
+  if (e == cudaSuccess) e = cudaMalloc(&B.sqn, (size_t)ns * 24);
+  if (e == cudaSuccess) e = cudaMalloc(&B.near, (size_t)ns * 4);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+    if ((e = cudaStreamCreateWithFlags(&B.side[i], cudaStreamNonBlocking)) == cudaSuccess)
+      e = cudaEventCreateWithFlags(&B.join[i], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMemcpy(B.q, q.data(), (size_t)nq * 24, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(B.qn, qn.data(), (size_t)nq * 24, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(B.sq, sq.data(), (size_t)ns * 24, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(B.sqn, sqn.data(), (size_t)ns * 24, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "irradiance photon buffers");
   std::vector<float> ext((size_t)nq * 3), intr((size_t)nq * 3);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(ext.data(), d_ext, (size_t)nq * 12, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(intr.data(), d_int, (size_t)nq * 12, cudaMemcpyDeviceToHost, st);
+  std::vector<int32_t> nearest((size_t)ns);
+  std::vector<int32_t> irr_perm;
+  // side stream of each map's lookups: the indirect map's alone, the
+  // caustic and direct maps' together
+  const int side_of[3] = {1, 1, 0};
+  for (int64_t q0 = 0; q0 < nq && e == cudaSuccess; q0 += chunk) {
+    const int64_t c = std::min(chunk, nq - q0);
+    if ((e = cudaEventRecord(B.fork, st)) != cudaSuccess) break;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(B.side[i], B.fork, 0);
+    for (int mi : {2, 1, 0}) {  // the indirect map's tree exists; the others are built as they are needed
+      if (e != cudaSuccess) break;
+      Map &m = pm->maps[mi];
+      if (q0 == 0 && mi != 2 && (e = build_map(m)) != cudaSuccess) break;
+      if (!has[mi]) continue;
+      e = skw::launch_knn(m.d_nodes, m.d_nids, pm->d_dirs, (int)m.n, B.q + 3 * q0, B.qn + 3 * q0, c,
+                          kLookupIrradiance, pm->lookup_dist[mi], kMaxNormalDeviationCos, B.idx[mi], B.d2[mi],
+                          B.cnt[mi], nullptr, nullptr, pm->d_status, B.side[side_of[mi]]);
+    }
+    if (e == cudaSuccess && q0 == 0) {
+      // KDTree<IrradiancePhoton>(irradiance_photons) on the positions, and
+      // the lookup-distance queries against it, on the caller's stream
+      std::vector<skw::KdNode> nodes;
+      skw::build_photon_tree(pm->irr_pos.data(), nq, 0, nodes, irr_perm);
+      std::vector<uint16_t> nrm_t((size_t)nq);
+      for (int64_t t = 0; t < nq; ++t) nrm_t[(size_t)t] = pm->irr_nrm[(size_t)irr_perm[(size_t)t]];
+      skw::KdNode *dn = nullptr;
+      e = upload(nodes, &dn);
+      pm->d_irr_nodes = dn;
+      if (e == cudaSuccess) e = upload(nrm_t, &pm->d_irr_nids);
+      if (e == cudaSuccess)
+        e = skw::launch_nearest(pm->d_irr_nodes, pm->d_irr_nids, pm->d_dirs, (int)nq, B.sq, B.sqn, ns,
+                                std::numeric_limits<double>::infinity(), kMaxNormalDeviationCos, B.near,
+                                pm->d_status, st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(nearest.data(), B.near, (size_t)ns * 4, cudaMemcpyDeviceToHost, st);
+    }
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+      if ((e = cudaEventRecord(B.join[i], B.side[i])) == cudaSuccess) e = cudaStreamWaitEvent(st, B.join[i], 0);
+    bool first = true;
+    for (int mi = 0; mi < 3 && e == cudaSuccess; ++mi) {
+      if (!has[mi]) continue;  // a null map adds nothing
+      const Map &m = pm->maps[mi];
+      e = skw::launch_irradiance_sum(m.d_nodes, m.d_weight, m.d_dirid, pm->d_dirs, B.q + 3 * q0, B.qn + 3 * q0,
+                                     B.idx[mi], B.cnt[mi], c, kLookupIrradiance, (double)m.paths,
+                                     pm->lookup_dist[mi], first, B.ext + 3 * q0, B.intr + 3 * q0, st);
+      first = false;
+    }
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ext.data(), B.ext, (size_t)nq * 12, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(intr.data(), B.intr, (size_t)nq * 12, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  cudaFree(d_q);
-  cudaFree(d_qn);
-  cudaFree(d_idx);
-  cudaFree(d_d2);
-  cudaFree(d_cnt);
-  cudaFree(d_ext);
-  cudaFree(d_int);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "irradiance photon estimates");
-  // KDTree<IrradiancePhoton>(irradiance_photons)
-  std::vector<skw::KdNode> nodes;
-  std::vector<int32_t> perm;
-  skw::build_photon_tree(pm->irr_pos.data(), nq, 0, nodes, perm);
+  // the irradiance photons in their tree's order
   std::vector<float> pos_t((size_t)nq * 3), ext_t((size_t)nq * 3), int_t((size_t)nq * 3);
   std::vector<uint16_t> nrm_t((size_t)nq);
   for (int64_t t = 0; t < nq; ++t) {
-    const int32_t s = perm[(size_t)t];
+    const int32_t s = irr_perm[(size_t)t];
     for (int k = 0; k < 3; ++k) {
       pos_t[(size_t)(3 * t + k)] = pm->irr_pos[(size_t)(3 * s + k)];
       ext_t[(size_t)(3 * t + k)] = ext[(size_t)(3 * s + k)];
@@ -170,40 +252,9 @@ int build_irradiance(skw_photon_map *pm, cudaStream_t st) {
   pm->irr_ext.swap(ext_t);
   pm->irr_int.swap(int_t);
   pm->n_irr = nq;
-  skw::KdNode *dn = nullptr;
-  e = upload(nodes, &dn);
-  pm->d_irr_nodes = dn;
-  if (e == cudaSuccess) e = upload(pm->irr_nrm, &pm->d_irr_nids);
-  if (e == cudaSuccess) e = upload(pm->irr_ext, &pm->d_irr_ext);
+  e = upload(pm->irr_ext, &pm->d_irr_ext);
   if (e == cudaSuccess) e = upload(pm->irr_int, &pm->d_irr_int);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "irradiance map upload");
-  // max irradiance lookup distance from every 11th indirect photon
-  const int64_t step = 11, ns = (im.n + step - 1) / step;
-  std::vector<double> sq((size_t)ns * 3), sqn((size_t)ns * 3);
-  for (int64_t i = 0; i < ns; ++i) {
-    const PhotonRec &r = tree_photon(im, i * step);
-    for (int k = 0; k < 3; ++k) {
-      sq[(size_t)(3 * i + k)] = (double)r.p[k];
-      sqn[(size_t)(3 * i + k)] = dirs[3 * (size_t)r.nrm + k];
-    }
-  }
-  std::vector<int32_t> nearest((size_t)ns);
-  double *d_sq = nullptr, *d_sqn = nullptr;
-  int32_t *d_near = nullptr;
-  e = cudaMalloc(&d_sq, (size_t)ns * 24);
-  if (e == cudaSuccess) e = cudaMalloc(&d_sqn, (size_t)ns * 24);
-  if (e == cudaSuccess) e = cudaMalloc(&d_near, (size_t)ns * 4);
-  if (e == cudaSuccess) e = cudaMemcpy(d_sq, sq.data(), (size_t)ns * 24, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(d_sqn, sqn.data(), (size_t)ns * 24, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = skw::launch_nearest(pm->d_irr_nodes, pm->d_irr_nids, pm->d_dirs, (int)nq, d_sq, d_sqn, ns,
-                            std::numeric_limits<double>::infinity(), kMaxNormalDeviationCos, d_near, pm->d_status, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(nearest.data(), d_near, (size_t)ns * 4, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  cudaFree(d_sq);
-  cudaFree(d_sqn);
-  cudaFree(d_near);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "irradiance lookup distance");
   std::vector<double> d2((size_t)ns, 0.0);
   for (int64_t i = 0; i < ns; ++i) {
     const int32_t t = nearest[(size_t)i];
@@ -228,9 +279,8 @@ int finish_map(skw_photon_map *pm, cudaStream_t st) {
   if (e == cudaSuccess) e = upload(dirs, &pm->d_dirs);
   if (e == cudaSuccess) e = cudaMalloc(&pm->d_status, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(pm->d_status, 0, sizeof(unsigned));
-  for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = build_map(pm->maps[i]);
   if (e != cudaSuccess) return cuda_fail(pm->ctx, e, "photon map upload");
-  int rc = build_irradiance(pm, st);
+  int rc = build_maps(pm, st);
   pm->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return rc;
 }

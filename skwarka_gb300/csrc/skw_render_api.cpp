@@ -785,10 +785,147 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
   return record_specular(s, P, W, d_views, px0, n, st, hook);
 }
 
+// Side streams and events of one pass workspace: a level's shadow and BSDF
+// traversals run on aux[0] and aux[1] while the pass's own stream traces the
+// next specular level.
+struct Lanes {
+  cudaStream_t aux[2] = {nullptr, nullptr};
+  cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+  bool ready() const { return aux[0] && aux[1] && fork && join[0] && join[1]; }
+};
+
+cudaError_t lanes_events(Lanes &L) {
+  cudaError_t e = cudaEventCreateWithFlags(&L.fork, cudaEventDisableTiming);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&L.join[i], cudaEventDisableTiming);
+  return e;
+}
+
+void lanes_release_events(Lanes &L) {
+  for (cudaEvent_t ev : {L.fork, L.join[0], L.join[1]})
+    if (ev) cudaEventDestroy(ev);
+  L.fork = L.join[0] = L.join[1] = nullptr;
+}
+
+// Lanes of a single-camera render: the context's side streams (shared by the
+// context's callers; each call orders its own work on them with its own
+// events) and this call's events.  On failure the lanes stay incomplete and
+// the pass runs its stages in turn.
+void render_lanes(skw_ctx *ctx, Lanes &L) {
+  {
+    std::lock_guard<std::mutex> lock(ctx->aux_mu);
+    for (int i = 0; i < 2; ++i)
+      if (!ctx->aux_st[i] && cudaStreamCreateWithFlags(&ctx->aux_st[i], cudaStreamNonBlocking) != cudaSuccess) {
+        ctx->aux_st[i] = nullptr;
+        cudaGetLastError();
+      }
+    L.aux[0] = ctx->aux_st[0];
+    L.aux[1] = ctx->aux_st[1];
+  }
+  if (lanes_events(L) != cudaSuccess) {
+    lanes_release_events(L);
+    cudaGetLastError();
+  }
+}
+
+// The direct-lighting stages of one pass with the levels overlapped (no
+// medium, no per-level hook).  The order of dependent work is the one of
+// record_direct; what changes is what runs at the same time:
+//   main:   camera, trace, shade(0) | trace(1)  | resolve(0), shade(1) | trace(2) ...
+//   aux[0]:                          shadow(0) |                      | shadow(1) ...
+//   aux[1]:                          BSDF(0)   |                      | BSDF(1) ...
+// A level's shadow and BSDF traversals and the next level's traversal read
+// different queues and write different outputs (each launch with its own
+// ray-group counter, counts[8..10]); the main stream waits for both side
+// streams before the level's resolve, which precedes the next shade that
+// refills the shadow and BSDF queues.  Small levels (a few tens of
+// thousands of rays each) no longer leave the GPU mostly idle in turn.
+cudaError_t record_direct_pipelined(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views,
+                                    int64_t px0, int n_px, cudaStream_t st, const Lanes &ln) {
+  skw_accel *a = s->accel;
+  const int n = n_px * P.spp, nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(W.contrib, 0, (size_t)n * P.slots * 12, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(W.counts, 0, 5 * sizeof(int), st)) != cudaSuccess) return e;
+  if ((e = skw::launch_camera(d_views, nv, px0, n_px, P.sppx, P.sppy, W.rays, st, P.ld)) != cudaSuccess) return e;
+  if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.rays, n, nullptr, a->scene_abs, nullptr, W.hits,
+                                 a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
+    return e;
+  skw::SpecQueues sq{};
+  if (P.spec_levels) {
+    sq.out_rays = W.qrays[0];
+    sq.out_w = W.qw[0];
+    sq.out_sample = W.qsample[0];
+    sq.out_node = W.qnode[0];
+    sq.out_count = W.counts + 3;
+    sq.spec_slot = P.spec_slot;
+  }
+  if ((e = skw::launch_shade(s->dev, d_views, nv, n, px0, P.spp, P.slots, P.nl, W.rays, W.hits, W.contrib, W.srays,
+                             W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb, W.counts + 1, W.bnrm,
+                             P.cfg.shade_block, st, P.spec_levels ? &sq : nullptr, P.ld)) != cudaSuccess)
+    return e;
+  // the shadow and BSDF traversals of a level, on the side streams
+  auto side = [&](int64_t csh, int64_t cbs) -> cudaError_t {
+    cudaError_t r = cudaEventRecord(ln.fork, st);
+    for (int i = 0; i < 2 && r == cudaSuccess; ++i) r = cudaStreamWaitEvent(ln.aux[i], ln.fork, 0);
+    if (r == cudaSuccess && csh > 0)
+      r = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, csh, W.counts, a->scene_abs, nullptr,
+                                W.occ, a->d_status, ln.aux[0], ctas, W.counts + 9, true);
+    if (r == cudaSuccess && cbs > 0)
+      r = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.brays, cbs, W.counts + 1, a->scene_abs, nullptr,
+                                W.bhits, a->d_status, ln.aux[1], ctas, W.counts + 10, true);
+    for (int i = 0; i < 2 && r == cudaSuccess; ++i) r = cudaEventRecord(ln.join[i], ln.aux[i]);
+    return r;
+  };
+  // ... and their resolve, on the pass's stream once both are done
+  auto resolve = [&](int64_t csh, int64_t cbs, bool accumulate) -> cudaError_t {
+    cudaError_t r = cudaSuccess;
+    for (int i = 0; i < 2 && r == cudaSuccess; ++i) r = cudaStreamWaitEvent(st, ln.join[i], 0);
+    if (r == cudaSuccess)
+      r = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
+                              W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st, accumulate);
+    return r;
+  };
+  int64_t csh = (int64_t)n * (P.nl + P.npl), cbs = (int64_t)n * P.nl;
+  if ((e = side(csh, cbs)) != cudaSuccess) return e;
+  for (int L = 1; L <= P.spec_levels; ++L) {
+    const int qi = (L - 1) & 1, qo = L & 1;
+    const int64_t cl = (int64_t)n << L;
+    if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.qrays[qi], cl, W.counts + 3 + qi, a->scene_abs,
+                                   nullptr, W.qhits, a->d_status, st, ctas, W.counts + 8, true)) != cudaSuccess)
+      return e;
+    if ((e = resolve(csh, cbs, L > 1)) != cudaSuccess) return e;
+    skw::SpecQueues q{};
+    q.in_rays = W.qrays[qi];
+    q.in_w = W.qw[qi];
+    q.in_sample = W.qsample[qi];
+    q.in_node = W.qnode[qi];
+    q.in_count = W.counts + 3 + qi;
+    q.spec_slot = P.spec_slot;
+    if (L < P.spec_levels) {  // depth L <= max_spec_depth: children go to the next level
+      q.out_rays = W.qrays[qo];
+      q.out_w = W.qw[qo];
+      q.out_sample = W.qsample[qo];
+      q.out_node = W.qnode[qo];
+      q.out_count = W.counts + 3 + qo;
+      if ((e = cudaMemsetAsync(W.counts + 3 + qo, 0, sizeof(int), st)) != cudaSuccess) return e;
+    }
+    if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) return e;
+    if ((e = skw::launch_shade_specular(s->dev, d_views, nv, cl, px0, P.spp, P.slots, P.nl, q, L, W.qhits, W.contrib,
+                                        W.srays, W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb,
+                                        W.counts + 1, W.bnrm, st)) != cudaSuccess)
+      return e;
+    csh = cl * (P.nl + P.npl);
+    cbs = cl * P.nl;
+    if ((e = side(csh, cbs)) != cudaSuccess) return e;
+  }
+  return resolve(csh, cbs, P.spec_levels > 0);
+}
+
 // One pass: direct lighting, then the film.
 cudaError_t record_pass(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
-                        int n_px, float *films, cudaStream_t st) {
-  cudaError_t e = record_direct(s, P, W, d_views, px0, n_px, st);
+                        int n_px, float *films, cudaStream_t st, const Lanes *ln) {
+  cudaError_t e = ln && ln->ready() && !P.media ? record_direct_pipelined(s, P, W, d_views, px0, n_px, st, *ln)
+                                                 : record_direct(s, P, W, d_views, px0, n_px, st);
   if (e != cudaSuccess) return e;
   return skw::launch_film(W.contrib, px0, n_px, P.spp, P.slots, films, st, P.media ? W.tcam : nullptr, P.media_slot);
 }
@@ -804,7 +941,8 @@ int64_t n_passes(const Plan &P) { return (P.n_px_total + P.chunk_px - 1) / P.chu
 // All passes.  With two workspaces, passes alternate between them on two
 // streams (st and side), joined back into st at the end.
 cudaError_t record_all(skw_scene *s, const Plan &P, const Workspace *W, int n_ws, const skw::ViewDev *d_views,
-                       float *films, cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+                       float *films, cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                       const Lanes *lanes) {
   cudaError_t e = cudaSuccess;
   if (n_ws > 1) {
     if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
@@ -814,7 +952,9 @@ cudaError_t record_all(skw_scene *s, const Plan &P, const Workspace *W, int n_ws
   for (int64_t px0 = 0; px0 < P.n_px_total; px0 += P.chunk_px, ++k) {
     const int n_px = (int)std::min<int64_t>(P.chunk_px, P.n_px_total - px0);
     const int w = n_ws > 1 ? (int)(k & 1) : 0;
-    if ((e = record_pass(s, P, W[w], d_views, px0, n_px, films, w ? side : st)) != cudaSuccess) return e;
+    if ((e = record_pass(s, P, W[w], d_views, px0, n_px, films, w ? side : st, lanes ? &lanes[w] : nullptr)) !=
+        cudaSuccess)
+      return e;
   }
   if (n_ws > 1) {
     if ((e = cudaEventRecord(join, side)) != cudaSuccess) return e;
@@ -838,6 +978,7 @@ struct skw_render_batch {
   cudaEvent_t ev_in = nullptr, ev_out = nullptr, fork = nullptr, join = nullptr;
   cudaGraphExec_t exec = nullptr;
   float *graph_films = nullptr;
+  Lanes lanes[2];  // side streams of the two workspaces' levels
 };
 
 namespace {
@@ -884,7 +1025,7 @@ int batch_capture(skw_render_batch *b, float *films) {
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamBeginCapture(b->own, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
-  cudaError_t er = record_all(b->scene, P, W, n_ws, b->d_views, films, b->own, b->side, b->fork, b->join);
+  cudaError_t er = record_all(b->scene, P, W, n_ws, b->d_views, films, b->own, b->side, b->fork, b->join, b->lanes);
   e = cudaStreamEndCapture(b->own, &g);
   if (er != cudaSuccess || e != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
@@ -968,7 +1109,10 @@ int skw_render_direct(skw_scene *s, const skw_camera *cam, const skw_render_para
   workspace_carve(P, w, &W);
   skw::ViewDev *d_view = (skw::ViewDev *)(w + wbytes);
   e = cudaMemcpyAsync(d_view, P.views.data(), sizeof(skw::ViewDev), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = record_all(s, P, &W, 1, d_view, film_rgb, st, nullptr, nullptr, nullptr);
+  Lanes ln;
+  if (e == cudaSuccess && !P.media) render_lanes(ctx, ln);  // without side streams the stages run in turn
+  if (e == cudaSuccess) e = record_all(s, P, &W, 1, d_view, film_rgb, st, nullptr, nullptr, nullptr, &ln);
+  lanes_release_events(ln);
   cudaFreeAsync(w, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "direct-lighting render");
   ctx->launches.fetch_add(n_passes(P) * launches_per_pass(P));
@@ -1002,6 +1146,11 @@ int skw_render_batch_create(skw_scene *s, const skw_camera *cams, int32_t n_view
         (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming)) != cudaSuccess)
       rc = cuda_fail(ctx, e, "batch resources");
+    for (int w = 0; w < 2 && rc == SKW_OK; ++w)
+      for (int i = 0; i < 2 && rc == SKW_OK; ++i)
+        if ((e = cudaStreamCreateWithFlags(&b->lanes[w].aux[i], cudaStreamNonBlocking)) != cudaSuccess ||
+            (i == 0 && (e = lanes_events(b->lanes[w])) != cudaSuccess))
+          rc = cuda_fail(ctx, e, "batch resources");
   }
   if (rc != SKW_OK) {
     skw_render_batch_destroy(b);
@@ -1020,6 +1169,11 @@ void skw_render_batch_destroy(skw_render_batch *b) {
   if (b->d_views) cudaFree(b->d_views);
   if (b->own) cudaStreamDestroy(b->own);
   if (b->side) cudaStreamDestroy(b->side);
+  for (Lanes &L : b->lanes) {
+    for (cudaStream_t &a : L.aux)
+      if (a) cudaStreamDestroy(a);
+    lanes_release_events(L);
+  }
   for (cudaEvent_t ev : {b->ev_in, b->ev_out, b->fork, b->join})
     if (ev) cudaEventDestroy(ev);
   delete b;
