@@ -160,6 +160,23 @@ def load_traffic(kind: str, rays: int):
     return d.get("dram_bytes_per_launch", 0.0) + d["dram_bytes_per_ray"] * rays
 
 
+def load_l2(kind: str, rays: int, seconds: float):
+    """The L2 side of the roofline: L2 bytes per ray (lts__t_sectors of the
+    committed ncu capture) at this run's rays per second, against the L2
+    peak of the same capture (its bytes over its duration over its
+    lts__throughput fraction)."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text()).get(kind) or {}
+    if "l2_bytes_per_ray" not in d:
+        return None
+    achieved = d["l2_bytes_per_ray"] * rays / seconds / 1e9
+    return {"achieved": achieved, "peak": d["l2_peak_gbs"], "unit": "GB/s", "frac": achieved / d["l2_peak_gbs"],
+            "bytes_per_ray": d["l2_bytes_per_ray"],
+            "source": "lts__t_sectors per ray and the L2 peak from the committed ncu capture, at this run's rays/s"}
+
+
 def hit_parity(gpu_hits: np.ndarray, ref: dict) -> dict:
     """Agreement of the GPU's closest hits (int32 (n, 4): t bits, prim, tri,
     flags) with the reference's on the same rays: hit-id agreement over
@@ -911,7 +928,8 @@ def main():
                     "frac": achieved / peak, "traffic": load_traffic("closest", args.rays),
                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                     else "fallback 6.8 TB/s",
-                    "bytes_per_ray": bytes_per_ray, "nodes_per_ray": n_nodes, "tris_per_ray": n_tris}
+                    "bytes_per_ray": bytes_per_ray, "nodes_per_ray": n_nodes, "tris_per_ray": n_tris,
+                    "l2": load_l2("closest", args.rays, per_launch_s)}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": sum(kern_ms) / len(kern_ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",

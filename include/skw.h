@@ -496,10 +496,9 @@ int skw_scene_next_rays(skw_scene *scene, const skw_ray *rays, const skw_hit *hi
  * d + 1 (LTEIntegrator::_SpecularReflect / _SpecularTransmit,
  * Core/LTEIntegrator.cpp:66-126).  Default 10 (the GUI's default); range
  * [0, 11]: every branch of every sample's tree is given room, so a render
- * pass holds at most 2^23 >> (max_depth + 1) camera samples.  Scenes with
- * a medium and specular materials together work in skw_render_direct (the
- * specular rays are marched too), not in the batch or the adjoint
- * (SKW_ERR_UNSUPPORTED); the adjoint replays the same trees (a transparent surface's reflectance is
+ * pass holds at most 2^25 >> (max_depth + 1) camera samples.  With a
+ * medium the specular rays are marched through it too, in the single-camera
+ * render, the batch and the adjoint; the adjoint replays the same trees (a transparent surface's reflectance is
  * its material's, never a per-triangle albedo); photon shooting follows
  * specular bounces (caustic map) and the photon-map render adds caustic
  * radiance and the final gather at the diffuse hits of every level

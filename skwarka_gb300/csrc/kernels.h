@@ -148,15 +148,32 @@ cudaError_t launch_media(bool adjoint, const SceneDev &S, const ViewDev *views, 
                          int spp, int slots, int media_slot, const float *dfilm, const void *rays, const void *hits,
                          float *contrib, float *tcam, void *mrays, int *mtarget, float *mval, float *mdem,
                          int *mcount, unsigned *status, cudaStream_t s);
+// A chunk of a specular level counted on the device: entries
+// [*off_dev, *off_dev + n) of the level, clipped to min(*count_dev,
+// capacity).  All null / 0: the n entries the pointers start at.
+struct MediaChunk {
+  const int *off_dev = nullptr;
+  const int *count_dev = nullptr;
+  int64_t capacity = 0;
+};
 // The medium along n entries of a specular level (rays, hits, in_sample,
-// in_w, in_node point at the first): in_w is multiplied by each segment's
+// in_w, in_node point at the first, or at the level's start for a
+// device-counted chunk): in_w is multiplied by each segment's
 // transmittance, emission and queued light samples target the entry's
 // sample's slot spec_slot (mtarget holds full slot indices: resolve with
-// slots = 1, media_slot = 0).
-cudaError_t launch_media_specular(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin,
-                                  int spp, int slots, int spec_slot, const void *rays, const void *hits,
-                                  const int *in_sample, float *in_w, const int *in_node, float *contrib, void *mrays,
-                                  int *mtarget, float *mval, int *mcount, unsigned *status, cudaStream_t s);
+// slots = 1, media_slot = 0).  adjoint: mdem receives each queued light
+// sample's emission-scale derivative (dfilm = dL/dI) and nothing is added
+// to contrib.
+cudaError_t launch_media_specular(bool adjoint, const SceneDev &S, const ViewDev *views, int n_views, int n,
+                                  int64_t px_begin, int spp, int slots, int spec_slot, const void *rays,
+                                  const void *hits, const int *in_sample, float *in_w, const int *in_node,
+                                  const MediaChunk &chunk, const float *dfilm, float *contrib, void *mrays,
+                                  int *mtarget, float *mval, float *mdem, int *mcount, unsigned *status,
+                                  cudaStream_t s);
+// Ends one iteration of a graph's device-counted chunk loop: *off += chunk,
+// and the loop's conditional set to whether *off < min(*count, capacity).
+cudaError_t launch_media_advance(cudaGraphConditionalHandle h, int *off, const int *count, int chunk,
+                                 int64_t capacity, cudaStream_t s);
 cudaError_t launch_resolve_media(bool adjoint, int64_t capacity, const uint8_t *occ, const int *mtarget,
                                  const float *mval, const float *mdem, const int *mcount, int slots, int media_slot,
                                  float *contrib, double *g_emission, cudaStream_t s);

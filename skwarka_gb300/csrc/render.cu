@@ -664,11 +664,18 @@ struct MediaArgs {
   // A specular level's entries instead of camera rays (in_sample non-null):
   // entry i's sample, weight (multiplied by the segment's transmittance in
   // place) and tree node; its emission and in-scattering go, weighted, into
-  // its sample's slot spec_slot.
+  // its sample's slot spec_slot (adjoint: only the weight and the
+  // in-scattering's emission-scale derivative).
   const int *in_sample;
   float *in_w;
   const int *in_node;
   int spec_slot;
+  // Device-counted chunk of a level (off_dev non-null): entries
+  // [*off_dev, *off_dev + n) of the level, clipped to min(*count_dev,
+  // capacity); the arrays are the level's own, indexed by entry.
+  const int *off_dev;
+  const int *count_dev;
+  int64_t capacity;
 };
 
 __device__ __forceinline__ double radical_inverse_r(unsigned n, unsigned base) {
@@ -690,9 +697,14 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
                                                int *__restrict__ mtarget, float *__restrict__ mval,
                                                float *__restrict__ mdem, int *__restrict__ mcount,
                                                unsigned *__restrict__ status) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.n) return;
-  const bool spec = A.in_sample != nullptr;  // a specular level's entry (forward only)
+  if (A.off_dev) {  // a device-counted chunk of a specular level
+    const int64_t e = (int64_t)*A.off_dev + i;
+    if (e >= min((int64_t)*A.count_dev, A.capacity)) return;
+    i = (int)e;
+  }
+  const bool spec = A.in_sample != nullptr;  // a specular level's entry
   const int si = spec ? A.in_sample[i] : i;
   const V3 wt = spec ? load3(A.in_w + 3 * (int64_t)i) : v3(1.0f, 1.0f, 1.0f);
   const MediumDev &M = S.medium;
@@ -814,7 +826,8 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
   if (spec) {
     // LTEIntegrator::Radiance of the specular ray: its surface radiance
     // (shaded next, with the weight) times T, plus the medium's radiance
-    atomic_add_rgb(contrib, (int64_t)si * A.slots + A.spec_slot, mul(rad, wt));
+    // (the medium's own emission is no parameter of the adjoint)
+    if (!ADJ) atomic_add_rgb(contrib, (int64_t)si * A.slots + A.spec_slot, mul(rad, wt));
     store_rgb(A.in_w, i, mul(wt, T));
     return;
   }
@@ -1284,7 +1297,7 @@ cudaError_t launch_media(bool adjoint, const SceneDev &S, const ViewDev *views, 
                          float *contrib, float *tcam, void *mrays, int *mtarget, float *mval, float *mdem,
                          int *mcount, unsigned *status, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  MediaArgs A{n, px_begin, spp, slots, media_slot, views, n_views, nullptr, nullptr, nullptr, 0};
+  MediaArgs A{n, px_begin, spp, slots, media_slot, views, n_views, nullptr, nullptr, nullptr, 0, nullptr, nullptr, 0};
   AdjointArgs J{dfilm, nullptr, nullptr, nullptr, nullptr, nullptr};
   const unsigned grid = (unsigned)((n + 127) / 128);
   if (adjoint)
@@ -1296,15 +1309,38 @@ cudaError_t launch_media(bool adjoint, const SceneDev &S, const ViewDev *views, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_media_specular(const SceneDev &S, const ViewDev *views, int n_views, int n, int64_t px_begin,
-                                  int spp, int slots, int spec_slot, const void *rays, const void *hits,
-                                  const int *in_sample, float *in_w, const int *in_node, float *contrib, void *mrays,
-                                  int *mtarget, float *mval, int *mcount, unsigned *status, cudaStream_t s) {
+cudaError_t launch_media_specular(bool adjoint, const SceneDev &S, const ViewDev *views, int n_views, int n,
+                                  int64_t px_begin, int spp, int slots, int spec_slot, const void *rays,
+                                  const void *hits, const int *in_sample, float *in_w, const int *in_node,
+                                  const MediaChunk &chunk, const float *dfilm, float *contrib, void *mrays,
+                                  int *mtarget, float *mval, float *mdem, int *mcount, unsigned *status,
+                                  cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  MediaArgs A{n, px_begin, spp, slots, 0, views, n_views, in_sample, in_w, in_node, spec_slot};
-  k_media<false><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(S, A, AdjointArgs{}, (const float4 *)rays,
-                                                              (const int4 *)hits, contrib, nullptr, (float4 *)mrays,
-                                                              mtarget, mval, nullptr, mcount, status);
+  MediaArgs A{n,         px_begin, spp,    slots,         0,          views,       n_views,
+              in_sample, in_w,     in_node, spec_slot, chunk.off_dev, chunk.count_dev, chunk.capacity};
+  AdjointArgs J{dfilm, nullptr, nullptr, nullptr, nullptr, nullptr};
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  if (adjoint)
+    k_media<true><<<grid, 128, 0, s>>>(S, A, J, (const float4 *)rays, (const int4 *)hits, contrib, nullptr,
+                                       (float4 *)mrays, mtarget, mval, mdem, mcount, status);
+  else
+    k_media<false><<<grid, 128, 0, s>>>(S, A, J, (const float4 *)rays, (const int4 *)hits, contrib, nullptr,
+                                        (float4 *)mrays, mtarget, mval, mdem, mcount, status);
+  return cudaGetLastError();
+}
+
+// The end of a device-counted chunk loop: the next chunk's offset, and the
+// loop's condition (another chunk remains).
+__global__ void k_media_advance(cudaGraphConditionalHandle h, int *off, const int *count, int chunk, int64_t capacity) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int64_t o = (int64_t)*off + chunk;
+  *off = (int)min(o, (int64_t)INT32_MAX);
+  cudaGraphSetConditional(h, o < min((int64_t)*count, capacity) ? 1u : 0u);
+}
+
+cudaError_t launch_media_advance(cudaGraphConditionalHandle h, int *off, const int *count, int chunk,
+                                 int64_t capacity, cudaStream_t s) {
+  k_media_advance<<<1, 32, 0, s>>>(h, off, count, chunk, capacity);
   return cudaGetLastError();
 }
 

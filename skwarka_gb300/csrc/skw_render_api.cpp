@@ -450,7 +450,6 @@ struct PassConfig {
   int extra_slots = 0;       // contribution slots after the direct-lighting ones (final gather)
   bool media = true;         // march the scene's medium (if any) along the camera rays (one more slot, last)
   bool specular = true;      // follow specular reflection / transmission (if the scene has such materials)
-  bool media_specular = false;  // a medium along specular rays too (host round trips: not in graphs)
 };
 
 // Entries of the largest specular level of a pass (the pass is sized so
@@ -606,9 +605,6 @@ int plan_make(skw_scene *s, const skw_camera *cams, int n_views, const skw_rende
   P->npl = s->dev.n_point_lights;
   P->media = cfg.media && s->dev.medium.on;
   P->spec_levels = cfg.specular && s->dev.has_specular ? s->dev.max_spec_depth + 1 : 0;
-  if (P->media && P->spec_levels && !cfg.media_specular)
-    return fail(ctx, SKW_ERR_UNSUPPORTED,
-                "a participating medium together with specular materials (single-camera render only)");
   P->slots = 1 + 2 * P->nl + P->npl + cfg.extra_slots + (P->spec_levels ? 1 : 0) + (P->media ? 1 : 0);
   P->media_slot = P->slots - 1;
   P->spec_slot = P->slots - 1 - (P->media ? 1 : 0);
@@ -669,8 +665,85 @@ struct SpecLevel {
 };
 using SpecHook = std::function<cudaError_t(const SpecLevel &)>;
 
+// The medium along specular level L's rays (LTEIntegrator::Radiance of each
+// specular ray), queue qi holding at most cl entries, marched in chunks of
+// the pass's sample count (the media queue's capacity).  On a stream the
+// level's length is read back and the chunks launched for it; in a graph
+// capture the chunks run in a conditional while-node whose body advances a
+// device offset (counts[11]) until it passes the level's device length, so
+// the graph needs no host round trip.  body: a stream not otherwise in use
+// by the capture, on which the loop's body is captured.  adjoint: the
+// entries' weights and the in-scattering's emission-scale derivative only.
+cudaError_t record_media_level(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views,
+                               int64_t px0, int qi, int64_t cl, bool adjoint, const float *dfilm, double *g_emission,
+                               cudaStream_t st, cudaStream_t body) {
+  skw_accel *a = s->accel;
+  const int nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
+  const int chunk = (int)P.cap_samples;
+  const int64_t cm = (int64_t)chunk * s->dev.medium.max_steps;
+  int *count = W.counts + 3 + qi, *off = W.counts + 11;
+  // one chunk: the march, the light samples' occlusion, their resolve
+  auto run = [&](const void *rays, const void *hits, const int *sample, float *w, const int *node, int m,
+                 const skw::MediaChunk &c, cudaStream_t sq) -> cudaError_t {
+    cudaError_t r = cudaMemsetAsync(W.counts + 2, 0, sizeof(int), sq);
+    if (r == cudaSuccess)
+      r = skw::launch_media_specular(adjoint, s->dev, d_views, nv, m, px0, P.spp, P.slots, P.spec_slot, rays, hits,
+                                     sample, w, node, c, dfilm, W.contrib, W.mrays, W.mtarget, W.mval, W.mdem,
+                                     W.counts + 2, a->d_status, sq);
+    if (r == cudaSuccess)
+      r = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.mrays, (int64_t)m * s->dev.medium.max_steps,
+                                W.counts + 2, a->scene_abs, nullptr, W.mocc, a->d_status, sq, ctas, W.counts + 8);
+    if (r == cudaSuccess)
+      r = skw::launch_resolve_media(adjoint, cm, W.mocc, W.mtarget, W.mval, W.mdem, W.counts + 2, 1, 0, W.contrib,
+                                    g_emission, sq);
+    return r;
+  };
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cs);
+  if (e != cudaSuccess) return e;
+  if (cs != cudaStreamCaptureStatusActive) {
+    int cnt = 0;
+    if ((e = cudaMemcpyAsync(&cnt, count, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+      return e;
+    cnt = (int)std::min<int64_t>(cnt, cl);
+    for (int o = 0; o < cnt && e == cudaSuccess; o += chunk) {
+      const int m = std::min(chunk, cnt - o);
+      e = run((const char *)W.qrays[qi] + 32 * (int64_t)o, (const char *)W.qhits + 16 * (int64_t)o,
+              W.qsample[qi] + o, W.qw[qi] + 3 * (int64_t)o, W.qnode[qi] + o, m, skw::MediaChunk{}, st);
+    }
+    return e;
+  }
+  if (!body) return cudaErrorNotSupported;
+  if ((e = cudaMemsetAsync(off, 0, sizeof(int), st)) != cudaSuccess) return e;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd)) != cudaSuccess) return e;
+  cudaGraphConditionalHandle h;
+  if ((e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  if ((e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &np)) != cudaSuccess) return e;
+  cudaGraph_t bg = np.conditional.phGraph_out[0];
+  if ((e = cudaStreamBeginCaptureToGraph(body, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+      cudaSuccess)
+    return e;
+  cudaError_t eb = run(W.qrays[qi], W.qhits, W.qsample[qi], W.qw[qi], W.qnode[qi], chunk,
+                       skw::MediaChunk{off, count, cl}, body);
+  if (eb == cudaSuccess) eb = skw::launch_media_advance(h, off, count, chunk, cl, body);
+  e = cudaStreamEndCapture(body, &bg);
+  if (eb != cudaSuccess) return eb;
+  if (e != cudaSuccess) return e;
+  return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
 cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
-                            int n, cudaStream_t st, const SpecHook *hook) {
+                            int n, cudaStream_t st, const SpecHook *hook, cudaStream_t body) {
   skw_accel *a = s->accel;
   const int nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
   cudaError_t e = cudaSuccess;
@@ -696,33 +769,9 @@ cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, con
     if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.qrays[qi], cl, W.counts + 3 + qi, a->scene_abs,
                                    nullptr, W.qhits, a->d_status, st, ctas, W.counts + 8, true)) != cudaSuccess)
       return e;
-    if (P.media) {
-      // The medium along the level's rays (LTEIntegrator::Radiance of each
-      // specular ray): the level's length is read back and its entries
-      // marched in chunks that the media queue holds.
-      int cnt = 0;
-      if ((e = cudaMemcpyAsync(&cnt, W.counts + 3 + qi, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-          (e = cudaStreamSynchronize(st)) != cudaSuccess)
-        return e;
-      cnt = (int)std::min<int64_t>(cnt, cl);
-      for (int off = 0; off < cnt; off += (int)P.cap_samples) {
-        const int m = (int)std::min<int64_t>(P.cap_samples, cnt - off);
-        if ((e = cudaMemsetAsync(W.counts + 2, 0, sizeof(int), st)) != cudaSuccess) return e;
-        if ((e = skw::launch_media_specular(s->dev, d_views, nv, m, px0, P.spp, P.slots, P.spec_slot,
-                                            (const char *)W.qrays[qi] + 32 * (int64_t)off,
-                                            (const char *)W.qhits + 16 * (int64_t)off, W.qsample[qi] + off,
-                                            W.qw[qi] + 3 * (int64_t)off, W.qnode[qi] + off, W.contrib, W.mrays,
-                                            W.mtarget, W.mval, W.counts + 2, a->d_status, st)) != cudaSuccess)
-          return e;
-        const int64_t cm = (int64_t)m * s->dev.medium.max_steps;
-        if ((e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.mrays, cm, W.counts + 2, a->scene_abs,
-                                       nullptr, W.mocc, a->d_status, st, ctas, W.counts + 8)) != cudaSuccess)
-          return e;
-        if ((e = skw::launch_resolve_media(false, cm, W.mocc, W.mtarget, W.mval, W.mdem, W.counts + 2, 1, 0,
-                                           W.contrib, nullptr, st)) != cudaSuccess)
-          return e;
-      }
-    }
+    if (P.media && (e = record_media_level(s, P, W, d_views, px0, qi, cl, false, nullptr, nullptr, st, body)) !=
+                       cudaSuccess)
+      return e;
     if ((e = skw::launch_shade_specular(s->dev, d_views, nv, cl, px0, P.spp, P.slots, P.nl, q, L, W.qhits, W.contrib,
                                         W.srays, W.starget, W.srgb, W.counts, W.brays, W.btarget, W.brgb,
                                         W.counts + 1, W.bnrm, st)) != cudaSuccess)
@@ -748,7 +797,7 @@ cudaError_t record_specular(skw_scene *s, const Plan &P, const Workspace &W, con
 // The direct-lighting stages of one pass over global pixels
 // [px0, px0 + n_px): every slot of contrib but the extra ones is filled.
 cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
-                          int n_px, cudaStream_t st, const SpecHook *hook = nullptr) {
+                          int n_px, cudaStream_t st, const SpecHook *hook = nullptr, cudaStream_t body = nullptr) {
   skw_accel *a = s->accel;
   const int n = n_px * P.spp, nv = (int)P.views.size(), cap = P.cfg.stack_cap, ctas = P.cfg.trace_ctas_per_sm;
   cudaError_t e;
@@ -782,7 +831,7 @@ cudaError_t record_direct(skw_scene *s, const Plan &P, const Workspace &W, const
   if ((e = skw::launch_resolve(s->dev, (int)std::max(csh, cbs), P.nl, W.occ, W.starget, W.srgb, W.counts, W.brays,
                                W.bhits, W.btarget, W.brgb, W.counts + 1, W.bnrm, W.contrib, st)) != cudaSuccess)
     return e;
-  return record_specular(s, P, W, d_views, px0, n, st, hook);
+  return record_specular(s, P, W, d_views, px0, n, st, hook, body);
 }
 
 // Side streams and events of one pass workspace: a level's shadow and BSDF
@@ -925,7 +974,7 @@ cudaError_t record_direct_pipelined(skw_scene *s, const Plan &P, const Workspace
 cudaError_t record_pass(skw_scene *s, const Plan &P, const Workspace &W, const skw::ViewDev *d_views, int64_t px0,
                         int n_px, float *films, cudaStream_t st, const Lanes *ln) {
   cudaError_t e = ln && ln->ready() && !P.media ? record_direct_pipelined(s, P, W, d_views, px0, n_px, st, *ln)
-                                                 : record_direct(s, P, W, d_views, px0, n_px, st);
+                                                 : record_direct(s, P, W, d_views, px0, n_px, st, nullptr, ln ? ln->aux[0] : nullptr);
   if (e != cudaSuccess) return e;
   return skw::launch_film(W.contrib, px0, n_px, P.spp, P.slots, films, st, P.media ? W.tcam : nullptr, P.media_slot);
 }
@@ -1095,7 +1144,6 @@ int skw_render_direct(skw_scene *s, const skw_camera *cam, const skw_render_para
   Plan P;
   const uint64_t seed = params->seed;
   PassConfig cfg;
-  cfg.media_specular = true;  // no graph here: the specular levels' media may read their lengths back
   int rc = plan_make(s, cam, 1, params, &seed, cfg, &P);
   if (rc != SKW_OK) return rc;
   cudaStream_t st = (cudaStream_t)stream;
@@ -1389,6 +1437,11 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
       if ((e = cudaMemsetAsync(W.counts, 0, 2 * sizeof(int), st)) != cudaSuccess) break;
       if ((e = skw::launch_traversal(true, cap, a->d_nodes, a->d_tris, W.qrays[qi], cl, W.counts + 3 + qi,
                                      a->scene_abs, nullptr, W.qhits, a->d_status, st, 0, W.counts + 8, true)) != cudaSuccess)
+        break;
+      // the medium along the level's rays: the entries' weights take the
+      // segments' transmittance, the in-scattering its emission derivative
+      if (P.media &&
+          (e = record_media_level(s, P, W, d_view, px0, qi, cl, true, d_film, g_emission, st, nullptr)) != cudaSuccess)
         break;
       if ((e = skw::launch_shade_specular_adjoint(s->dev, d_view, 1, cl, px0, P.spp, P.nl, d_film, g_albedo,
                                                   g_emission, q, L, W.qhits, W.srays, W.starget, s_dkd, s_dem,
