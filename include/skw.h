@@ -304,6 +304,23 @@ int skw_nearest(skw_kdtree *tree, const double *q, const double *qn, int64_t nq,
  * SpecularReflection(kd, FresnelDielectric(refractive_index, 1)) +
  * SpecularTransmission(ks, refractive_index, 1); kd / ks black = component absent. */
 #define SKW_MATERIAL_TRANSPARENT 4
+/* SubstrateMaterial (Raytracer/Materials/SubstrateMaterial.cpp:42-72, the
+ * isotropic form): FresnelBlend<BlinnDistribution>(kd, ks) with exponent
+ * 1 / clamp(roughness, 0.001, 1); kd, ks clamped to [0, 1]. */
+#define SKW_MATERIAL_SUBSTRATE 5
+/* UberMaterial (Raytracer/Materials/UberMaterial.cpp:39-85): with op =
+ * clamp(opacity, 0, 1): SpecularTransmission(1 - op, refractive_index) when
+ * some channel of op is outside [0.99, 1.01], Lambertian(clamp(op kd)),
+ * Microfacet(clamp(op ks), FresnelDielectric(refractive_index, 1),
+ * Blinn(1 / roughness)), SpecularReflection(clamp(kr), the same Fresnel);
+ * black weights leave their component out.  opacity (1, 1, 1) is opaque. */
+#define SKW_MATERIAL_UBER 6
+/* MixMaterial (Raytracer/Materials/MixMaterial.cpp:29-57): the components of
+ * materials mix[0] and mix[1] (indices into the same array; mix[1] = -1:
+ * none) scaled by clamp(mix_scale, 0, 1) and 1 - that.  Neither may itself
+ * be a mix, and at most one of them may have specular components
+ * (SKW_ERR_UNSUPPORTED otherwise). */
+#define SKW_MATERIAL_MIX 7
 
 typedef struct skw_merl skw_merl;
 
@@ -315,7 +332,11 @@ typedef struct skw_material {
   float sigma;        /* matte Oren-Nayar sigma (radians); 0 = Lambertian */
   float eta[3], k[3]; /* metal refractive index and absorption */
   const skw_merl *measured; /* SKW_MATERIAL_MEASURED: the tabulated BRDF (must outlive the scene) */
-  float refractive_index;   /* SKW_MATERIAL_TRANSPARENT: index inside (outside 1), > 0 */
+  float refractive_index;   /* SKW_MATERIAL_TRANSPARENT, _UBER: index inside (outside 1), > 0 */
+  float kr[3];              /* SKW_MATERIAL_UBER: specular reflectance */
+  float opacity[3];         /* SKW_MATERIAL_UBER: opacity (1: opaque) */
+  int32_t mix[2];           /* SKW_MATERIAL_MIX: the two materials */
+  float mix_scale[3];       /* SKW_MATERIAL_MIX: the first material's scale */
 } skw_material;
 
 /* A measured BRDF in the MERL binary layout (MERLMeasuredData(std::istream&),

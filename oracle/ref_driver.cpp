@@ -47,6 +47,9 @@
 #include <Raytracer/Materials/PlasticMaterial.h>
 #include <Raytracer/Materials/MetalMaterial.h>
 #include <Raytracer/Materials/TransparentMaterial.h>
+#include <Raytracer/Materials/SubstrateMaterial.h>
+#include <Raytracer/Materials/UberMaterial.h>
+#include <Raytracer/Materials/MixMaterial.h>
 #include <Raytracer/LightSources/DiffuseAreaLightSource.h>
 #include <Raytracer/LightSources/PointLight.h>
 #include <Raytracer/Cameras/PerspectiveCamera.h>
@@ -543,7 +546,11 @@ struct RefMaterialIn {
   float roughness, sigma;
   float eta[3], k[3];
   const void *measured;  // kind 3: a MERLMeasuredData (skw_ref_merl_create)
-  float refractive_index;  // kind 4: TransparentMaterial
+  float refractive_index;  // kinds 4, 6: TransparentMaterial, UberMaterial
+  float kr[3];             // kind 6: UberMaterial
+  float opacity[3];        // kind 6: UberMaterial
+  int32_t mix[2];          // kind 7: MixMaterial
+  float mix_scale[3];      // kind 7: MixMaterial
 };
 struct RefPrimIn {
   int32_t mesh;
@@ -553,6 +560,44 @@ struct RefPrimIn {
   const float *triangle_albedo;
   float emission[3];
 };
+
+static intrusive_ptr<const Texture<SpectrumCoef_d>> const_rgb(const float *v) {
+  return intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(v[0], v[1], v[2])));
+}
+static intrusive_ptr<const Texture<double>> const_d(double v) {
+  return intrusive_ptr<const Texture<double>>(new ConstantTexture<double>(v));
+}
+
+// The reference material for materials[i]; kd: its diffuse texture (the
+// per-triangle albedo where the primitive has one).
+static intrusive_ptr<const Material> make_material(const RefMaterialIn *materials, int i,
+                                                   intrusive_ptr<const Texture<SpectrumCoef_d>> kd) {
+  const RefMaterialIn &M = materials[i];
+  intrusive_ptr<const Material> mat;
+  if (M.kind == 0) {
+    mat.reset(new MatteMaterial(kd, const_d(M.sigma)));
+  } else if (M.kind == 1) {
+    mat.reset(new PlasticMaterial(kd, const_rgb(M.ks), const_d(M.roughness)));
+  } else if (M.kind == 3) {
+    mat.reset(new MERLMeasuredMaterial(intrusive_ptr<const MERLMeasuredData>((const MERLMeasuredData *)M.measured)));
+  } else if (M.kind == 4) {
+    mat.reset(new TransparentMaterial(const_rgb(M.kd), const_rgb(M.ks), (double)M.refractive_index));
+  } else if (M.kind == 5) {
+    mat.reset(new SubstrateMaterial(kd, const_rgb(M.ks), const_d(M.roughness)));
+  } else if (M.kind == 6) {
+    mat.reset(new UberMaterial(kd, const_rgb(M.ks), const_rgb(M.kr), const_d(M.roughness), const_rgb(M.opacity),
+                               (double)M.refractive_index));
+  } else if (M.kind == 7) {
+    auto sub = [&](int j) {
+      return make_material(materials, j, const_rgb(materials[j].kd));
+    };
+    mat.reset(new MixMaterial(sub(M.mix[0]), M.mix[1] >= 0 ? sub(M.mix[1]) : intrusive_ptr<const Material>(),
+                              const_rgb(M.mix_scale)));
+  } else {
+    mat.reset(new MetalMaterial(const_rgb(M.eta), const_rgb(M.k), const_d(M.roughness)));
+  }
+  return mat;
+}
 
 // The reference Scene for the product's scene description (meshes,
 // primitives with materials / emission / shading normals / per-triangle
@@ -592,26 +637,7 @@ static intrusive_ptr<const Scene> make_scene(int n_meshes, const float *const *v
     } else {
       kd.reset(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.kd[0], M.kd[1], M.kd[2])));
     }
-    intrusive_ptr<const Material> mat;
-    if (M.kind == 0) {
-      mat.reset(new MatteMaterial(kd, intrusive_ptr<const Texture<double>>(new ConstantTexture<double>(M.sigma))));
-    } else if (M.kind == 1) {
-      mat.reset(new PlasticMaterial(kd, intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(
-                                            SpectrumCoef_d(M.ks[0], M.ks[1], M.ks[2]))),
-                                    intrusive_ptr<const Texture<double>>(new ConstantTexture<double>(M.roughness))));
-    } else if (M.kind == 3) {
-      mat.reset(new MERLMeasuredMaterial(intrusive_ptr<const MERLMeasuredData>((const MERLMeasuredData *)M.measured)));
-    } else if (M.kind == 4) {
-      mat.reset(new TransparentMaterial(
-          intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.kd[0], M.kd[1], M.kd[2]))),
-          intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.ks[0], M.ks[1], M.ks[2]))),
-          (double)M.refractive_index));
-    } else {
-      mat.reset(new MetalMaterial(
-          intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.eta[0], M.eta[1], M.eta[2]))),
-          intrusive_ptr<const Texture<SpectrumCoef_d>>(new ConstantTexture<SpectrumCoef_d>(SpectrumCoef_d(M.k[0], M.k[1], M.k[2]))),
-          intrusive_ptr<const Texture<double>>(new ConstantTexture<double>(M.roughness))));
-    }
+    intrusive_ptr<const Material> mat = make_material(materials, P.material, kd);
     intrusive_ptr<const AreaLightSource> light;
     if (P.emission[0] > 0 || P.emission[1] > 0 || P.emission[2] > 0) {
       light.reset(new DiffuseAreaLightSource(Spectrum_d(P.emission[0], P.emission[1], P.emission[2]), mesh));

@@ -77,9 +77,13 @@ cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const do
 // Nearest accepted point per query (-1 if none within max_dist).
 // nq_dev (launch_knn, launch_nearest; may be null): device int holding the
 // number of queries to run (at most nq), for queues filled on the device.
+// order (may be null): thread t answers query order[t] (a permutation of
+// the queries that groups nearby ones into warps); results stay indexed by
+// query.
 cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                            const double *qn, int64_t nq, double max_dist, double cos_t, int32_t *out_idx,
-                           unsigned *status, cudaStream_t stream, const int *nq_dev = nullptr);
+                           unsigned *status, cudaStream_t stream, const int *nq_dev = nullptr,
+                           const int32_t *order = nullptr);
 
 // Direct-lighting render stages (render.cu); see render_scene.h.
 // A pass covers global pixels [px_begin, px_begin + n_px) of the views'
@@ -162,14 +166,14 @@ struct MediaChunk {
 // transmittance, emission and queued light samples target the entry's
 // sample's slot spec_slot (mtarget holds full slot indices: resolve with
 // slots = 1, media_slot = 0).  adjoint: mdem receives each queued light
-// sample's emission-scale derivative (dfilm = dL/dI) and nothing is added
-// to contrib.
+// sample's emission-scale derivative (dfilm = dL/dI, scaled by the sample's
+// camera-segment transmittance tcam) and nothing is added to contrib.
 cudaError_t launch_media_specular(bool adjoint, const SceneDev &S, const ViewDev *views, int n_views, int n,
                                   int64_t px_begin, int spp, int slots, int spec_slot, const void *rays,
                                   const void *hits, const int *in_sample, float *in_w, const int *in_node,
-                                  const MediaChunk &chunk, const float *dfilm, float *contrib, void *mrays,
-                                  int *mtarget, float *mval, float *mdem, int *mcount, unsigned *status,
-                                  cudaStream_t s);
+                                  const MediaChunk &chunk, const float *dfilm, const float *tcam, float *contrib,
+                                  void *mrays, int *mtarget, float *mval, float *mdem, int *mcount,
+                                  unsigned *status, cudaStream_t s);
 // Ends one iteration of a graph's device-counted chunk loop: *off += chunk,
 // and the loop's conditional set to whether *off < min(*count, capacity).
 cudaError_t launch_media_advance(cudaGraphConditionalHandle h, int *off, const int *count, int chunk,
@@ -192,7 +196,8 @@ cudaError_t launch_shade_specular_adjoint(const SceneDev &S, const ViewDev *view
                                           float *g_albedo, double *g_emission, const SpecQueues &spec, int depth,
                                           const void *hits, void *srays, int *stri, float *s_dkd, float *s_dem,
                                           int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
-                                          int *bcount, float *bnrm, cudaStream_t s);
+                                          int *bcount, float *bnrm, cudaStream_t s,
+                                          const float *tcam = nullptr);
 cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_samples, const uint8_t *occ,
                                    const int *stri, const float *s_dkd, const float *s_dem, const int *scount,
                                    const void *brays, const void *bhits, const int *btri, const float *b_dkd,

@@ -502,11 +502,12 @@ __global__ void __launch_bounds__(kKnnBlock) k_nearest(const float4 *__restrict_
                                                  const double *__restrict__ q, const double *__restrict__ qn,
                                                  int64_t nq, double max_dist, double cos_t,
                                                  int32_t *__restrict__ out_idx, unsigned *__restrict__ status,
-                                                 const int *__restrict__ nq_dev) {
+                                                 const int *__restrict__ nq_dev, const int32_t *__restrict__ order) {
   __shared__ uint32_t stk[kStack][kKnnBlock];
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (nq_dev && *nq_dev < nq) nq = *nq_dev;
   if (i >= nq) return;
+  if (order) i = order[i];
   Query Q;
   Q.q[0] = q[3 * i];
   Q.q[1] = q[3 * i + 1];
@@ -627,12 +628,12 @@ cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const do
 
 cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                            const double *qn, int64_t nq, double max_dist, double cos_t, int32_t *out_idx,
-                           unsigned *status, cudaStream_t stream, const int *nq_dev) {
+                           unsigned *status, cudaStream_t stream, const int *nq_dev, const int32_t *order) {
   if (nq <= 0) return cudaSuccess;
   const int block = kKnnBlock;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
   k_nearest<<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, max_dist, cos_t, out_idx,
-                                        status, nq_dev);
+                                        status, nq_dev, order);
   return cudaGetLastError();
 }
 

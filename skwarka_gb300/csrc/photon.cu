@@ -97,34 +97,52 @@ __device__ __forceinline__ float bounce_rnd(uint64_t seed, uint64_t path, int bo
   return rnd(s, path, (uint32_t)(4 * (bounce & 15) + k));
 }
 
-// BSDF::Sample over all components of a specular-only (transparent) BSDF
-// (Core/BSDF.cpp:72-117, _SampleSpecularOnly): each component's Sample
-// (SpecularReflection: mirror direction, r F; SpecularTransmission:
-// refracted direction, t (1 - F), black on total internal reflection with the
-// mirror direction), then one of them chosen with probability proportional
-// to its luminance (the 0.999 guard as in the reference); pdf = that
-// probability.  A single component is sampled with pdf 1.
-__device__ V3 specular_sample_photon(const Bsdf &b, V3 inc_w, float uc, V3 &dir, float &pdf) {
-  const V3 wi = b.local(inc_w);
-  const float F = fresnel_dielectric_ior(wi.z, b.ior);
-  const bool has_r = !black(b.kd), has_t = !black(b.ks);
-  const V3 dr = b.world(v3(-wi.x, -wi.y, wi.z));
-  const V3 fr = b.kd * F;
-  V3 dt = dr, ft = v3(0, 0, 0);
-  {
-    float zs = -1.0f, ni = b.ior, no = 1.0f;
+// The specular components of a BSDF as the photon pipeline samples them
+// (SpecularReflection / SpecularTransmission::Sample): the mirror
+// direction with scale r F, and the refracted direction with scale t (1 - F)
+// (black on total internal reflection, with the mirror direction).  The
+// host admits at most one layer with specular components.
+__device__ bool specular_parts(const Bsdf &b, V3 inc_w, V3 &dr, V3 &fr, V3 &dt, V3 &ft) {
+  for (int i = 0; i < b.nl; ++i) {
+    const Layer l = i == 0 ? b.L0 : layer1(b);
+    const V3 r = layer_spec_r(l), t = layer_spec_t(l);
+    if (black(r) && black(t)) continue;
+    const V3 wi = b.local(inc_w);
+    const float F = fresnel_dielectric_ior(wi.z, l.ior);
+    dr = b.world(v3(-wi.x, -wi.y, wi.z));
+    fr = mul(l.scale, r) * F;
+    dt = dr;
+    ft = v3(0, 0, 0);
+    float zs = -1.0f, ni = l.ior, no = 1.0f;
     if (wi.z < 0.0f) {
       zs = 1.0f;
       ni = 1.0f;
-      no = b.ior;
+      no = l.ior;
     }
     const float eta = no / ni;
     const float st2 = eta * eta * (1.0f - wi.z * wi.z);
     if (st2 < 1.0f) {
       dt = b.world(v3(-wi.x * eta, -wi.y * eta, sqrtf(1.0f - st2) * zs));
-      ft = b.ks * (1.0f - F);
+      if (!black(t)) ft = mul(l.scale, t) * (1.0f - F);
     }
+    if (black(r)) fr = v3(0, 0, 0);
+    return true;
   }
+  return false;
+}
+
+// BSDF::Sample over all components of a specular-only BSDF (Core/BSDF.cpp:
+// 72-117, _SampleSpecularOnly): each component's Sample, then one of them
+// chosen with probability proportional to its luminance (the 0.999 guard as
+// in the reference); pdf = that probability.  A single component is sampled
+// with pdf 1.
+__device__ V3 specular_sample_photon(const Bsdf &b, V3 inc_w, float uc, V3 &dir, float &pdf) {
+  V3 dr, fr, dt, ft;
+  pdf = 0.0f;
+  dir = inc_w;
+  if (!specular_parts(b, inc_w, dr, fr, dt, ft)) return v3(0, 0, 0);
+  const bool has_r = !black(layer_spec_r(b.L0)) || (b.nl == 2 && !black(layer_spec_r(layer1(b))));
+  const bool has_t = !black(layer_spec_t(b.L0)) || (b.nl == 2 && !black(layer_spec_t(layer1(b))));
   pdf = 1.0f;
   if (has_r && has_t) {
     const float lr = 0.05316285f * fr.x + 0.58515348f * fr.y + 0.36168367f * fr.z;
@@ -157,6 +175,32 @@ __device__ V3 specular_sample_photon(const Bsdf &b, V3 inc_w, float uc, V3 &dir,
   pdf = 0.0f;
   dir = dr;
   return v3(0, 0, 0);
+}
+
+// BSDF::Sample over every component of a BSDF with both kinds (Core/
+// BSDF.cpp:119-168): one component chosen uniformly among all; a specular
+// one gives its direction and value with pdf 1 / count (`specular` set), a
+// non-specular one its direction, the whole BSDF's value there and the sum
+// of the non-specular densities over the count.
+__device__ V3 bsdf_sample_all(const Bsdf &b, V3 inc_w, float uc, float u0, float u1, V3 &dir, float &pdf,
+                              bool &specular) {
+  const int nn = bsdf_ncomp(b), ns = bsdf_nspec(b), n = nn + ns;
+  specular = false;
+  if (ns == 0) return bsdf_sample(b, inc_w, uc, u0, u1, dir, pdf);
+  if (nn == 0) {
+    specular = true;
+    return specular_sample_photon(b, inc_w, uc, dir, pdf);
+  }
+  const int c = min((int)(uc * n), n - 1);
+  if (c < nn) return bsdf_sample_c(b, c, inc_w, u0, u1, dir, pdf, n);
+  specular = true;
+  V3 dr, fr, dt, ft;
+  specular_parts(b, inc_w, dr, fr, dt, ft);
+  const bool has_r = !black(layer_spec_r(b.L0)) || (b.nl == 2 && !black(layer_spec_r(layer1(b))));
+  const bool refl = has_r && c == nn;  // the reflection comes first when both are present
+  dir = refl ? dr : dt;
+  pdf = 1.0f / n;
+  return refl ? fr : ft;
 }
 
 __device__ __forceinline__ void queue_push(const Queue &Q, int q, V3 o, V3 d, float tmin, V3 w, int path) {
@@ -296,7 +340,7 @@ __global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootAr
       rec.w[2] = w.z;
       rec.dir = compress_dir(inc.x, inc.y, inc.z);
       rec.nrm = compress_dir(h.ng.x, h.ng.y, h.ng.z);
-      const bool specular_bsdf = b.kind == kTransparent;  // no non-specular component
+      const bool specular_bsdf = bsdf_ncomp(b) == 0;  // no non-specular component: no photon stored
       if (bounce == 0) {
         if (!specular_bsdf) {
           st_direct[path] = rec;
@@ -331,11 +375,12 @@ __global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootAr
       }
       V3 ex;
       float pdf = 0.0f;
-      const V3 f = specular_bsdf ? specular_sample_photon(b, inc, uc, ex, pdf) : bsdf_sample(b, inc, uc, u0, u1, ex, pdf);
+      bool spec_sampled = false;
+      const V3 f = bsdf_sample_all(b, inc, uc, u0, u1, ex, pdf, spec_sampled);
       if (pdf > 0.0f && bounce + 1 < A.max_bounces) {
         // no cosine for specular scattering: the BxDF holds it (:229-231)
-        wnew = specular_bsdf ? mul(w, f) * (1.0f / pdf) : mul(w, f) * (fabsf(dot(ex, b.n)) / pdf);
-        if (!specular_bsdf) diffuse_path = kDiffusePath;
+        wnew = spec_sampled ? mul(w, f) * (1.0f / pdf) : mul(w, f) * (fabsf(dot(ex, b.n)) / pdf);
+        if (!spec_sampled) diffuse_path = kDiffusePath;
         float p = A.rr_probability;
         if (!(p > 0.0f)) {
           const float lw = luminance(w);
@@ -637,10 +682,10 @@ __global__ void k_gather_sources(SceneDev S, GatherArgs G, const float4 *__restr
   if (i < G.n) {
     const int4 hit = hits[i];
     // only surfaces with a non-specular component (PhotonLTEIntegrator.cpp:337-343)
-    if (hit.y >= 0 && S.materials[S.prim_material[hit.y]].kind != kTransparent) {
+    if (hit.y >= 0) {
       const float4 ra = rays[2 * i], rb = rays[2 * i + 1];
       h = make_hit(S, v3(ra.x, ra.y, ra.z), v3(ra.w, rb.x, rb.y), __int_as_float(hit.x), hit.y, hit.z);
-      ok = true;
+      ok = bsdf_ncomp(make_bsdf(S, h, hit.y)) > 0;
     }
   }
   const int j = queue_append(ok, count);
@@ -775,7 +820,8 @@ __global__ void __launch_bounds__(128) k_gather_rays(SceneDev S, GatherArgs G, G
 // with the 5x5 grid of BSDF::TotalScattering's caller.  The reference hands
 // the BxDF the WORLD incident direction (BSDF.cpp:213-219 passes i_incident,
 // not its local form), which the BxDF then treats as local; this keeps that.
-__device__ V3 total_scattering_bxdf(const Bsdf &b, bool glossy, V3 wi) {
+// what: 0 Oren-Nayar, 1 the Blinn microfacet, 2 FresnelBlend.
+__device__ V3 total_scattering_bxdf(const Layer &b, int what, V3 wi) {
   V3 ret = v3(0, 0, 0);
   for (int y = 0; y < 5; ++y)
     for (int x = 0; x < 5; ++x) {
@@ -783,17 +829,16 @@ __device__ V3 total_scattering_bxdf(const Bsdf &b, bool glossy, V3 wi) {
       V3 wo;
       float pdf;
       V3 f;
-      if (glossy) {
+      if (what == 1) {
         // Microfacet::Sample (BxDFs/Microfacet.h:112-129) with BlinnDistribution::Sample
-        const float ct = powf(u0, 1.0f / (b.exponent + 1.0f));
-        const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
-        const float phi = u1 * 2.0f * kPi;
-        V3 hh = v3(st * cosf(phi), st * sinf(phi), ct);
-        if (wi.z * hh.z < 0.0f) hh.z = -hh.z;
-        wo = hh * (2.0f * dot(wi, hh)) - wi;
+        if (!blinn_sample(b.exponent, wi, u0, u1, wo)) continue;
         pdf = microfacet_pdf(b, wi, wo);
-        if (wi.z * wo.z < 0.0f) continue;
         f = microfacet_eval(b, wi, wo);
+      } else if (what == 2) {
+        // FresnelBlend::Sample: the lobe mixture, Evaluate at the sampled direction
+        if (!fb_sample(b, wi, u0, u1, wo)) continue;
+        pdf = fb_pdf(b, wi, wo);
+        f = fb_eval(b, wi, wo);
       } else {
         wo = cosine_hemisphere(u0, u1);
         if (wi.z < 0.0f) wo.z = -wo.z;
@@ -808,7 +853,7 @@ __device__ V3 total_scattering_bxdf(const Bsdf &b, bool glossy, V3 wi) {
 
 // BxDF::TotalScattering of the measured BRDF: MERLMeasured::Sample over the
 // same grid, again with the world incident direction taken as local.
-__device__ V3 total_scattering_measured(const Bsdf &b, V3 wi) {
+__device__ V3 total_scattering_measured(const Layer &b, V3 wi) {
   V3 ret = v3(0, 0, 0);
   for (int y = 0; y < 5; ++y)
     for (int x = 0; x < 5; ++x) {
@@ -821,29 +866,49 @@ __device__ V3 total_scattering_measured(const Bsdf &b, V3 wi) {
   return v3(fminf(1.0f, fmaxf(0.0f, ret.x)), fminf(1.0f, fmaxf(0.0f, ret.y)), fminf(1.0f, fmaxf(0.0f, ret.z)));
 }
 
-// BSDF::TotalScattering over the reflection components (BSDF.cpp:209-224).
-__device__ V3 total_scattering_reflection(const Bsdf &b, V3 wi) {
-  V3 r = v3(0, 0, 0);
-  if (b.kind == kMeasured) r = total_scattering_measured(b, wi);
-  if (b.kind == kLambert || b.kind == kPlastic) r = b.kd;  // Lambertian::TotalScattering returns kd
-  if (b.kind == kOrenNayar) r = total_scattering_bxdf(b, false, wi);
-  if (b.kind == kPlastic || b.kind == kMetal) r = r + total_scattering_bxdf(b, true, wi);
+__device__ __forceinline__ V3 clamp01(V3 r) {
   return v3(fminf(1.0f, fmaxf(0.0f, r.x)), fminf(1.0f, fmaxf(0.0f, r.y)), fminf(1.0f, fmaxf(0.0f, r.z)));
 }
 
-// SpecularReflection / SpecularTransmission::TotalScattering (BxDFs/
-// SpecularReflection.h, SpecularTransmission.cpp:75-92) of a transparent
-// BSDF, each clamped as BSDF::TotalScattering does; like the other BxDFs
-// they receive the WORLD incident direction as if it were local, so the
-// Fresnel term and the total-internal-reflection test read its world z.
-__device__ __forceinline__ void total_scattering_transparent(const Bsdf &b, V3 wi, V3 &refl, V3 &trans) {
-  const float F = fresnel_dielectric_ior(wi.z, b.ior);
-  refl = b.kd * F;
-  const float eta = wi.z >= 0.0f ? 1.0f / b.ior : b.ior;
-  const bool tir = eta * eta * (1.0f - wi.z * wi.z) >= 1.0f;
-  trans = tir ? v3(0, 0, 0) : b.ks * (1.0f - F);
-  refl = v3(fminf(1.0f, fmaxf(0.0f, refl.x)), fminf(1.0f, fmaxf(0.0f, refl.y)), fminf(1.0f, fmaxf(0.0f, refl.z)));
-  trans = v3(fminf(1.0f, fmaxf(0.0f, trans.x)), fminf(1.0f, fmaxf(0.0f, trans.y)), fminf(1.0f, fmaxf(0.0f, trans.z)));
+// BSDF::TotalScattering (BSDF.cpp:209-224) over the reflection components
+// (refl: the non-specular ones and a specular reflection) and over the
+// transmission components (trans: a specular transmission), each sum
+// clamped; every layer's components scaled by the layer's scale
+// (ScaledBxDF::TotalScattering).  SpecularReflection / SpecularTransmission::
+// TotalScattering (BxDFs/SpecularReflection.h, SpecularTransmission.cpp:
+// 75-92) receive the WORLD incident direction as if it were local too, so
+// the Fresnel term and the total-internal-reflection test read its world z.
+__device__ void total_scattering(const Bsdf &bs, V3 wi, V3 &refl, V3 &trans) {
+  refl = trans = v3(0, 0, 0);
+  for (int i = 0; i < bs.nl; ++i) {
+    const Layer b = i == 0 ? bs.L0 : layer1(bs);
+    V3 r = v3(0, 0, 0), t = v3(0, 0, 0);
+    switch (b.kind) {
+      case kMeasured: r = total_scattering_measured(b, wi); break;
+      case kLambert: r = b.kd; break;  // Lambertian::TotalScattering returns kd
+      case kOrenNayar: r = total_scattering_bxdf(b, 0, wi); break;
+      case kPlastic: r = b.kd + total_scattering_bxdf(b, 1, wi); break;
+      case kMetal: r = total_scattering_bxdf(b, 1, wi); break;
+      case kSubstrate: r = total_scattering_bxdf(b, 2, wi); break;
+      case kUber:
+        if (!black(b.kd)) r = b.kd;
+        if (!black(b.ks)) r = r + total_scattering_bxdf(b, 1, wi);
+        break;
+      default: break;
+    }
+    const V3 sr = layer_spec_r(b), st = layer_spec_t(b);
+    if (!black(sr) || !black(st)) {
+      const float F = fresnel_dielectric_ior(wi.z, b.ior);
+      if (!black(sr)) r = r + clamp01(sr * F);
+      const float eta = wi.z >= 0.0f ? 1.0f / b.ior : b.ior;
+      const bool tir = eta * eta * (1.0f - wi.z * wi.z) >= 1.0f;
+      if (!black(st) && !tir) t = clamp01(st * (1.0f - F));
+    }
+    refl = refl + mul(b.scale, r);
+    trans = trans + mul(b.scale, t);
+  }
+  refl = clamp01(refl);
+  trans = clamp01(trans);
 }
 
 // ts: TotalScattering over the reflection components (times the irradiance
@@ -868,10 +933,7 @@ __global__ void k_gather_hits(SceneDev S, const float4 *__restrict__ grays, cons
       const Bsdf b = make_bsdf(S, h, hit.y);
       const V3 gdir = d * -1.0f;
       outside = dot(gdir, h.ng) > 0.0f;
-      if (b.kind == kTransparent)
-        total_scattering_transparent(b, gdir, t, tr);
-      else
-        t = total_scattering_reflection(b, gdir);
+      total_scattering(b, gdir, t, tr);
       ok = true;
     }
   }
@@ -1027,6 +1089,66 @@ cudaError_t launch_caustic(const SceneDev &S, const CausticMap &C, const ViewDev
   return cudaGetLastError();
 }
 
+// Spatial bins of the gather hits' irradiance queries: the scene's box cut
+// into 64^3 cells, each query's cell as an 18-bit Morton code; a counting
+// sort by cell (count, one exclusive scan, scatter) gives the order in which
+// k_nearest takes the queries, so that a warp's walks start near each other.
+// The order inside a cell follows the atomics; every query's answer is the
+// same whichever thread computes it.
+constexpr int kBinBits = 6, kBins = 1 << (3 * kBinBits);
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // bit b of v to bit 3b
+  uint32_t r = 0;
+#pragma unroll
+  for (int b = 0; b < kBinBits; ++b) r |= ((v >> b) & 1u) << (3 * b);
+  return r;
+}
+
+__global__ void k_bin_keys(const double *__restrict__ q, const int *__restrict__ count, float3 lo, float3 scale,
+                           uint32_t *__restrict__ key, int *__restrict__ bins) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *count) return;
+  const float c[3] = {((float)q[3 * i] - lo.x) * scale.x, ((float)q[3 * i + 1] - lo.y) * scale.y,
+                      ((float)q[3 * i + 2] - lo.z) * scale.z};
+  uint32_t k = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float f = fminf(fmaxf(c[a], 0.0f), (float)((1 << kBinBits) - 1));  // NaN -> 0
+    k |= spread3((uint32_t)f) << a;
+  }
+  key[i] = k;
+  atomicAdd(bins + k, 1);
+}
+
+// Exclusive scan of the kBins counts in place, one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_bin_scan(int *__restrict__ bins) {
+  constexpr int per = kBins / 1024;
+  __shared__ int part[1024];
+  int local[per];
+  int sum = 0;
+  for (int j = 0; j < per; ++j) {
+    local[j] = sum;
+    sum += bins[threadIdx.x * per + j];
+  }
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan of the parts
+    const int v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  const int base = part[threadIdx.x] - sum;
+  for (int j = 0; j < per; ++j) bins[threadIdx.x * per + j] = base + local[j];
+}
+
+__global__ void k_bin_scatter(const uint32_t *__restrict__ key, const int *__restrict__ count, int *__restrict__ bins,
+                              int32_t *__restrict__ order) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *count) return;
+  order[atomicAdd(bins + key[i], 1)] = i;
+}
+
 cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev *views, int n_views, int n,
                           int64_t px_begin, int spp, int slots, int base_slot, int gs, const void *rays,
                           const void *hits, void *gws, float *contrib, const TraceFn &trace, unsigned *status,
@@ -1056,6 +1178,9 @@ cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev 
   float *tt = (float *)take(al(ng * 12));
   uint8_t *side = (uint8_t *)take(al(ng));
   int32_t *nearest = (int32_t *)take(al(ng * 4));
+  uint32_t *bkey = (uint32_t *)take(al(ng * 4));
+  int32_t *border = (int32_t *)take(al(ng * 4));
+  int *bins = (int *)take(al((int64_t)kBins * 4));
   GatherArgs G{n, px_begin, spp, slots, base_slot, gs, views, n_views, sp ? *sp : SpecSource{}};
   cudaError_t e;
   if ((e = cudaMemsetAsync(counts, 0, 3 * sizeof(int), st)) != cudaSuccess) return e;
@@ -1074,8 +1199,22 @@ cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev 
   k_gather_hits<<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(S, grays, ghits, counts + 1, hsrc, hq, hqn, ts, tt,
                                                                side, counts + 2);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  {
+    const float3 lo = make_float3(M.lo[0], M.lo[1], M.lo[2]);
+    float sc[3];
+    for (int a = 0; a < 3; ++a) {
+      const float ext = M.hi[a] - M.lo[a];
+      sc[a] = ext > 0.0f && ext < INFINITY ? (float)(1 << kBinBits) / ext : 0.0f;
+    }
+    const unsigned grid = (unsigned)((ng + 255) / 256);
+    if ((e = cudaMemsetAsync(bins, 0, (size_t)kBins * 4, st)) != cudaSuccess) return e;
+    k_bin_keys<<<grid, 256, 0, st>>>(hq, counts + 2, lo, make_float3(sc[0], sc[1], sc[2]), bkey, bins);
+    k_bin_scan<<<1, 1024, 0, st>>>(bins);
+    k_bin_scatter<<<grid, 256, 0, st>>>(bkey, counts + 2, bins, border);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
   if ((e = launch_nearest(M.irr_nodes, M.irr_nids, M.dirs, M.n_irr, hq, hqn, ng, M.max_irr_dist, 0.87, nearest,
-                          status, st, counts + 2)) != cudaSuccess)
+                          status, st, counts + 2, border)) != cudaSuccess)
     return e;
   k_gather_resolve<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(M, gs, counts + 2, hsrc, nearest, ts, tt, side,
                                                                   gtarget, gweight, contrib, sp != nullptr);
@@ -1087,7 +1226,7 @@ size_t gather_bytes(int64_t n, int gs) {
   const int64_t ng = n * 2 * gs;
   return 256 + al(n * 4) + 2 * al(n * 24) + al(n * kGatherLookup * 4) + al(n * kGatherLookup * 8) + al(n * 4) +
          al(ng * 32) + al(ng * 16) + al(ng * 4) + al(ng * 12) + al(ng * 4) + 2 * al(ng * 24) + 2 * al(ng * 12) +
-         al(ng) + al(ng * 4) + 256;
+         al(ng) + al(ng * 4) + 2 * al(ng * 4) + al((int64_t)kBins * 4) + 256;
 }
 
 }  // namespace skw

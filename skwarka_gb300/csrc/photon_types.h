@@ -68,6 +68,7 @@ struct GatherMaps {
   int32_t n_irr;
   double max_irr_dist;
   const double *dirs;
+  float lo[3], hi[3];  // the scene's bounds (the gather hits' spatial bins)
 };
 
 }  // namespace skw

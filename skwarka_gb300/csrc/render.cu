@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
     if (SPEC) seed ^= 0xA0761D6478BD642Full * (uint64_t)node;  // a stream per tree node
     if (ADJ && valid) {
       dI = load3(J.dfilm + 3 * P) * (1.0f / A.spp);
-      if (A.tcam) dI = mul(dI, load3(A.tcam + 3 * (int64_t)i));
+      if (A.tcam) dI = mul(dI, load3(A.tcam + 3 * (int64_t)si));  // the camera ray's medium segment
       if (SPEC) dI = mul(dI, wt);  // a specular level's terms carry the entry's weight
     }
   }
@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev S, ShadeArgs A, AdjointA
   if (ADJ) add_emission_grad(J.g_emission, g_em);
   // Specular children (reflection, then transmission) while the depth allows.
   if (KIDS) {
-    const bool deeper = surface && b.kind == kTransparent && Q.depth <= S.max_spec_depth;
+    const bool deeper = surface && bsdf_nspec(b) > 0 && Q.depth <= S.max_spec_depth;
     for (int c = 0; c < 2; ++c) {
       V3 dir = v3(0, 0, 0), val = v3(0, 0, 0);
       const bool want = deeper && (c == 0 ? specular_reflect(b, wo, dir, val) : specular_transmit(b, wo, dir, val));
@@ -676,6 +676,9 @@ struct MediaArgs {
   const int *off_dev;
   const int *count_dev;
   int64_t capacity;
+  // Adjoint of a specular level: the samples' camera-segment transmittance
+  // (it scales the whole specular slot in the film, so dL/dI too).
+  const float *tcam_in;
 };
 
 __device__ __forceinline__ double radical_inverse_r(unsigned n, unsigned base) {
@@ -727,7 +730,10 @@ __global__ void __launch_bounds__(128) k_media(SceneDev S, MediaArgs A, AdjointA
   uint64_t seed = A.views[lo].seed;
   if (spec) seed ^= 0xA0761D6478BD642Full * (uint64_t)A.in_node[i];  // the entry's stream, as in k_shade
   V3 dI = v3(0, 0, 0);
-  if (ADJ) dI = load3(J.dfilm + 3 * P) * (1.0f / A.spp);
+  if (ADJ) {
+    dI = load3(J.dfilm + 3 * P) * (1.0f / A.spp);
+    if (spec && A.tcam_in) dI = mul(dI, load3(A.tcam_in + 3 * (int64_t)si));
+  }
   const double offset1 = rnd(seed, gid, 62);
   const V3 ss = load3(M.sigma_s), st = load3(M.sigma_t), em = load3(M.emission);
   const bool scatters = !black(ss);
@@ -1236,9 +1242,9 @@ cudaError_t launch_shade_specular_adjoint(const SceneDev &S, const ViewDev *view
                                           float *g_albedo, double *g_emission, const SpecQueues &spec, int depth,
                                           const void *hits, void *srays, int *stri, float *s_dkd, float *s_dem,
                                           int *scount, void *brays, int *btri, float *b_dkd, float *brgb,
-                                          int *bcount, float *bnrm, cudaStream_t s) {
+                                          int *bcount, float *bnrm, cudaStream_t s, const float *tcam) {
   if (capacity <= 0) return cudaSuccess;
-  ShadeArgs A{(int)capacity, px_begin, spp, 0, n_light_samples, views, n_views, nullptr, 0};
+  ShadeArgs A{(int)capacity, px_begin, spp, 0, n_light_samples, views, n_views, tcam, 0};
   AdjointArgs J{dfilm, g_albedo, g_emission, s_dkd, s_dem, b_dkd};
   SpecArgs Q{spec.in_w,      spec.in_sample, spec.in_node,  spec.in_count, (float4 *)spec.out_rays,
              spec.out_w,     spec.out_sample, spec.out_node, spec.out_count, depth,
@@ -1297,7 +1303,8 @@ cudaError_t launch_media(bool adjoint, const SceneDev &S, const ViewDev *views, 
                          float *contrib, float *tcam, void *mrays, int *mtarget, float *mval, float *mdem,
                          int *mcount, unsigned *status, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  MediaArgs A{n, px_begin, spp, slots, media_slot, views, n_views, nullptr, nullptr, nullptr, 0, nullptr, nullptr, 0};
+  MediaArgs A{n, px_begin, spp, slots, media_slot, views, n_views, nullptr, nullptr, nullptr, 0, nullptr, nullptr, 0,
+              nullptr};
   AdjointArgs J{dfilm, nullptr, nullptr, nullptr, nullptr, nullptr};
   const unsigned grid = (unsigned)((n + 127) / 128);
   if (adjoint)
@@ -1312,12 +1319,12 @@ cudaError_t launch_media(bool adjoint, const SceneDev &S, const ViewDev *views, 
 cudaError_t launch_media_specular(bool adjoint, const SceneDev &S, const ViewDev *views, int n_views, int n,
                                   int64_t px_begin, int spp, int slots, int spec_slot, const void *rays,
                                   const void *hits, const int *in_sample, float *in_w, const int *in_node,
-                                  const MediaChunk &chunk, const float *dfilm, float *contrib, void *mrays,
-                                  int *mtarget, float *mval, float *mdem, int *mcount, unsigned *status,
-                                  cudaStream_t s) {
+                                  const MediaChunk &chunk, const float *dfilm, const float *tcam, float *contrib,
+                                  void *mrays, int *mtarget, float *mval, float *mdem, int *mcount,
+                                  unsigned *status, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   MediaArgs A{n,         px_begin, spp,    slots,         0,          views,       n_views,
-              in_sample, in_w,     in_node, spec_slot, chunk.off_dev, chunk.count_dev, chunk.capacity};
+              in_sample, in_w,     in_node, spec_slot, chunk.off_dev, chunk.count_dev, chunk.capacity, tcam};
   AdjointArgs J{dfilm, nullptr, nullptr, nullptr, nullptr, nullptr};
   const unsigned grid = (unsigned)((n + 127) / 128);
   if (adjoint)

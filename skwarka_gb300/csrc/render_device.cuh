@@ -143,26 +143,50 @@ __device__ __forceinline__ float power_heuristic(int n1, float p1, int n2, float
 }
 
 // ------------------------------------------------------------------- BSDF --
-struct Bsdf {
-  V3 n, e1, e2, ng;  // shading frame and geometric normal
+// A BSDF is one or two layers (two for MixMaterial: each layer one of the
+// other materials' BxDF sets, scaled -- ScaledBxDF, BxDFs/ScaledBxDF.cpp).
+// A layer's non-specular components, in the order its material adds them:
+//   kLambert, kOrenNayar: the diffuse BxDF          (1)
+//   kPlastic: Lambertian(kd), Microfacet(ks, dielectric 1.5, Blinn)  (2)
+//   kMetal: Microfacet(conductor, Blinn)            (1)
+//   kMeasured: MERLMeasured                         (1)
+//   kSubstrate: FresnelBlend<Blinn>(kd, ks)         (1)
+//   kUber: Lambertian(kd) if kd is not black, Microfacet(ks, dielectric ior,
+//          Blinn) if ks is not black                (0-2)
+//   kTransparent: none
+// and its specular ones: kTransparent SpecularReflection(kd) and
+// SpecularTransmission(ks); kUber SpecularReflection(kr) and
+// SpecularTransmission(kt) -- each only when its weight is not black.
+struct Layer {
   int kind;
-  V3 kd, ks;
+  V3 kd, ks, kr, kt;
   float exponent, on_a, on_b;
+  float ior;    // dielectric Fresnel (inside index; outside 1)
+  float pdiff;  // kSubstrate: probability of sampling the diffuse lobe
   V3 eta, k2;
   MerlDev merl;
-  float ior;  // kTransparent
+  V3 scale;
+};
+// The second layer of a mix is kept as its material (read again where it
+// is needed, an L1-resident line) so that the common one-layer BSDF stays
+// in registers.
+struct Bsdf {
+  V3 n, e1, e2, ng;  // shading frame and geometric normal
+  int nl;            // layers (1, or 2 for a mix)
+  Layer L0;
+  const DevMaterial *m1;  // nl == 2: the second layer's material
+  V3 s1;                  // nl == 2: its scale
   __device__ __forceinline__ V3 local(V3 w) const { return v3(dot(w, e1), dot(w, e2), dot(w, n)); }
   __device__ __forceinline__ V3 world(V3 l) const { return e1 * l.x + e2 * l.y + n * l.z; }
-  __device__ __forceinline__ int components() const { return kind == kPlastic ? 2 : 1; }
 };
 
-// FresnelDielectric (Core/Fresnel.h:96-124), inner 1.5, outer 1.0.
-__device__ __forceinline__ float fresnel_dielectric(float c) {
+// FresnelDielectric(inner, 1)::operator() (Core/Fresnel.h:96-124).
+__device__ __forceinline__ float fresnel_dielectric_ior(float c, float inner) {
   c = fminf(1.0f, fmaxf(-1.0f, c));
-  float ni = 1.5f, no = 1.0f;
+  float ni = inner, no = 1.0f;
   if (c < 0.0f) {
     ni = 1.0f;
-    no = 1.5f;
+    no = inner;
   }
   const float st = no / ni * sqrtf(fmaxf(0.0f, 1.0f - c * c));
   if (st >= 1.0f) return 1.0f;
@@ -182,35 +206,54 @@ __device__ __forceinline__ float fresnel_conductor1(float c, float eta, float k2
   return (rpar + rper) * 0.5f;
 }
 
-// Microfacet<Fresnel, Blinn>::Evaluate (BxDFs/Microfacet.h:86-104) for the
-// glossy component of plastic (ks, dielectric) or metal (1, conductor).
-__device__ V3 microfacet_eval(const Bsdf &b, V3 wi, V3 wo) {
+// BlinnDistribution::Evaluate (MicrofacetDistributions/BlinnDistribution.h).
+__device__ __forceinline__ float blinn_d(float exponent, V3 h) {
+  return (exponent + 2.0f) * (0.5f * kInvPi) * powf(fabsf(h.z), exponent);
+}
+
+// Microfacet<Fresnel, Blinn>::Evaluate (BxDFs/Microfacet.h:86-104): the
+// glossy component of plastic and uber (ks, dielectric) or metal
+// (conductor).
+__device__ V3 microfacet_eval(const Layer &b, V3 wi, V3 wo) {
   const float ci = fabsf(wi.z), co = fabsf(wo.z);
   if (ci < kEps || co < kEps) return v3(0, 0, 0);
   V3 h = wi + wo;
   if (fabsf(h.x) < kEps && fabsf(h.y) < kEps && fabsf(h.z) < kEps) return v3(0, 0, 0);
   h = normalized(h);
   const float ch = dot(wo, h);
-  const float d = (b.exponent + 2.0f) * (0.5f * kInvPi) * powf(fabsf(h.z), b.exponent);
+  const float d = blinn_d(b.exponent, h);
   const float tmp = 2.0f * fabsf(h.z) / fabsf(dot(wi, h));
   const float g = fminf(1.0f, fminf(ci * tmp, co * tmp));
   const float s = d * g / (4.0f * ci * co);
-  if (b.kind == kPlastic) return b.ks * (fresnel_dielectric(ch) * s);
+  if (b.kind != kMetal) return b.ks * (fresnel_dielectric_ior(ch, b.ior) * s);
   return v3(fresnel_conductor1(ch, b.eta.x, b.k2.x) * s, fresnel_conductor1(ch, b.eta.y, b.k2.y) * s,
             fresnel_conductor1(ch, b.eta.z, b.k2.z) * s);
 }
 
 // BlinnDistribution::PDF (MicrofacetDistributions/BlinnDistribution.h:104-111)
 // inside Microfacet::PDF (Microfacet.h:125-134).
-__device__ float microfacet_pdf(const Bsdf &b, V3 wi, V3 wo) {
+__device__ float microfacet_pdf(const Layer &b, V3 wi, V3 wo) {
   if (wi.z * wo.z < 0.0f) return 0.0f;
   const V3 h = normalized(wi + wo);
   return ((b.exponent + 1.0f) * powf(fabsf(h.z), b.exponent)) / (2.0f * kPi * 4.0f * fabsf(dot(wi, h)));
 }
 
+// BlinnDistribution::Sample (BlinnDistribution.h:86-101): the mirror of wi
+// about a sampled half vector on wi's side; false (pdf 0) when wo falls in
+// the other hemisphere, which Microfacet::Sample rejects.
+__device__ __forceinline__ bool blinn_sample(float exponent, V3 wi, float u0, float u1, V3 &wo) {
+  const float ct = powf(u0, 1.0f / (exponent + 1.0f));
+  const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+  const float phi = u1 * 2.0f * kPi;
+  V3 h = v3(st * cosf(phi), st * sinf(phi), ct);
+  if (wi.z * h.z < 0.0f) h.z = -h.z;
+  wo = h * (2.0f * dot(wi, h)) - wi;
+  return !(wi.z * wo.z < 0.0f);
+}
+
 // Diffuse component: Lambertian (BxDFs/Lambertian.cpp:18-30) or the
 // reference's Oren-Nayar (BxDFs/OrenNayar.cpp:19-42).
-__device__ __forceinline__ V3 diffuse_eval(const Bsdf &b, V3 wi, V3 wo) {
+__device__ __forceinline__ V3 diffuse_eval(const Layer &b, V3 wi, V3 wo) {
   if (b.kind != kOrenNayar) return b.kd * kInvPi;
   const float dcos = fmaxf(0.0f, wi.x * wo.x + wi.y * wo.y);
   const float denom = fmaxf(fabsf(wi.z), fabsf(wo.z));
@@ -218,6 +261,40 @@ __device__ __forceinline__ V3 diffuse_eval(const Bsdf &b, V3 wi, V3 wo) {
 }
 __device__ __forceinline__ float diffuse_pdf(V3 wi, V3 wo) {  // BxDF::PDF (Core/BxDF.cpp:33-37)
   return wi.z * wo.z > 0.0f ? fabsf(wo.z) * kInvPi : 0.0f;
+}
+
+// FresnelBlend<BlinnDistribution> (BxDFs/FresnelBlend.h): Ashikhmin and
+// Shirley's diffuse substrate under a glossy coat.  Evaluate: the diffuse
+// term (28 / 23 pi) kd (1 - ks) (1 - (1 - |cos o| / 2)^5)
+// (1 - (1 - |cos i| / 2)^5) plus the Schlick-Fresnel-weighted Blinn term
+// D(h) / (4 |o.h| max(|cos o|, |cos i|)).  The lobe is sampled as a mixture:
+// the cosine lobe with probability pdiff (on wi's side), the Blinn half
+// vector otherwise; the density is the mixture's (0 across hemispheres).
+__device__ V3 fb_eval(const Layer &b, V3 wi, V3 wo) {
+  const float ci = fabsf(wi.z), co = fabsf(wo.z);
+  const V3 h = normalized(wi + wo);
+  const float ch = dot(wo, h);
+  const float t1 = 1.0f - 0.5f * co, t2 = 1.0f - 0.5f * ci;
+  const float p1 = t1 * t1 * t1 * t1 * t1, p2 = t2 * t2 * t2 * t2 * t2;
+  const V3 one = v3(1.0f, 1.0f, 1.0f);
+  const V3 diffuse = mul(b.kd, one - b.ks) * ((28.0f / (23.0f * kPi)) * (1.0f - p1) * (1.0f - p2));
+  const float m = 1.0f - fminf(1.0f, fabsf(ch)), m5 = m * m * m * m * m;
+  const V3 schlick = b.ks + (one - b.ks) * m5;
+  const float denom = 4.0f * fabsf(ch) * fmaxf(co, ci);
+  const V3 specular = denom > 0.0f ? schlick * (blinn_d(b.exponent, h) / denom) : v3(0, 0, 0);
+  return diffuse + specular;
+}
+__device__ float fb_pdf(const Layer &b, V3 wi, V3 wo) {
+  if (wi.z * wo.z < 0.0f) return 0.0f;
+  return b.pdiff * fabsf(wo.z) * kInvPi + (1.0f - b.pdiff) * microfacet_pdf(b, wi, wo);
+}
+__device__ bool fb_sample(const Layer &b, V3 wi, float u0, float u1, V3 &wo) {
+  if (u0 < b.pdiff) {
+    wo = cosine_hemisphere(fminf(u0 / b.pdiff, 0.99999994f), u1);
+    if (wi.z < 0.0f) wo.z = -wo.z;
+    return true;
+  }
+  return blinn_sample(b.exponent, wi, fminf((u0 - b.pdiff) / (1.0f - b.pdiff), 0.99999994f), u1, wo);
 }
 
 // ------------------------------------------------------- measured BRDF --
@@ -341,87 +418,202 @@ __device__ V3 merl_sample(const MerlDev &m, V3 wi, float u0, float u1, V3 &wo, f
   return f;
 }
 
-// BSDF::Evaluate (Core/BSDF.cpp:22-40): every component is a reflection, so
-// directions on opposite sides of the geometric normal give zero.
-__device__ V3 bsdf_eval(const Bsdf &b, V3 wi_w, V3 wo_w) {
-  if (b.kind == kTransparent) return v3(0, 0, 0);  // specular only: delta components evaluate to 0
-  if (!(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f)) return v3(0, 0, 0);
-  const V3 wi = b.local(wi_w), wo = b.local(wo_w);
-  if (b.kind == kMetal) return microfacet_eval(b, wi, wo);
-  if (b.kind == kMeasured) return merl_eval(b.merl, wi, wo);
-  V3 f = diffuse_eval(b, wi, wo);
-  if (b.kind == kPlastic) f = f + microfacet_eval(b, wi, wo);
-  return f;
+// ------------------------------------------------------------ layers --
+// Non-specular component count of a layer, and of the whole BSDF.
+__device__ __forceinline__ int layer_ncomp(const Layer &b) {
+  switch (b.kind) {
+    case kTransparent: return 0;
+    case kPlastic: return 2;
+    case kUber: return (black(b.kd) ? 0 : 1) + (black(b.ks) ? 0 : 1);
+    default: return 1;
+  }
+}
+// Specular component count (reflection + transmission).
+__device__ __forceinline__ int layer_nspec(const Layer &b) {
+  if (b.kind == kTransparent) return (black(b.kd) ? 0 : 1) + (black(b.ks) ? 0 : 1);
+  if (b.kind == kUber) return (black(b.kr) ? 0 : 1) + (black(b.kt) ? 0 : 1);
+  return 0;
+}
+// A material's BxDF set as one layer (scale 1).
+__device__ Layer make_layer(const DevMaterial &m) {
+  Layer l;
+  l.kind = m.kind;
+  l.kd = load3(m.kd);
+  l.ks = load3(m.ks);
+  l.kr = load3(m.kr);
+  l.kt = load3(m.kt);
+  l.exponent = m.exponent;
+  l.on_a = m.on_a;
+  l.on_b = m.on_b;
+  l.ior = m.ior;
+  l.pdiff = m.pdiff;
+  l.eta = load3(m.eta);
+  l.k2 = load3(m.k2);
+  l.merl = m.merl;
+  l.scale = v3(1.0f, 1.0f, 1.0f);
+  return l;
+}
+// The second layer of a mix (nl == 2).
+__device__ __forceinline__ Layer layer1(const Bsdf &b) {
+  Layer l = make_layer(*b.m1);
+  l.scale = b.s1;
+  return l;
+}
+__device__ __forceinline__ int bsdf_ncomp(const Bsdf &b) {
+  return layer_ncomp(b.L0) + (b.nl == 2 ? layer_ncomp(layer1(b)) : 0);
+}
+__device__ __forceinline__ int bsdf_nspec(const Bsdf &b) {
+  return layer_nspec(b.L0) + (b.nl == 2 ? layer_nspec(layer1(b)) : 0);
 }
 
-// The derivative of bsdf_eval with respect to kd (per channel): the diffuse
-// component evaluated with kd = 1 (zero for metal, whose BSDF has no kd).
-__device__ V3 bsdf_eval_dkd(const Bsdf &b, V3 wi_w, V3 wo_w) {
-  if (b.kind == kMetal || b.kind == kTransparent || !(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f))
-    return v3(0, 0, 0);
-  Bsdf u = b;
-  u.kd = v3(1.0f, 1.0f, 1.0f);
-  return diffuse_eval(u, b.local(wi_w), b.local(wo_w));
+// A layer's non-specular components summed (local frame, unscaled).
+__device__ V3 layer_eval(const Layer &b, V3 wi, V3 wo) {
+  switch (b.kind) {
+    case kTransparent: return v3(0, 0, 0);
+    case kMetal: return microfacet_eval(b, wi, wo);
+    case kMeasured: return merl_eval(b.merl, wi, wo);
+    case kSubstrate: return fb_eval(b, wi, wo);
+    case kPlastic: return diffuse_eval(b, wi, wo) + microfacet_eval(b, wi, wo);
+    case kUber: {
+      V3 f = v3(0, 0, 0);
+      if (!black(b.kd)) f = f + b.kd * kInvPi;
+      if (!black(b.ks)) f = f + microfacet_eval(b, wi, wo);
+      return f;
+    }
+    default: return diffuse_eval(b, wi, wo);
+  }
 }
-
-// BSDF::PDF (Core/BSDF.cpp:42-58): average of the component densities.
-__device__ float bsdf_pdf(const Bsdf &b, V3 wi_w, V3 wo_w) {
-  if (b.kind == kTransparent) return 0.0f;
-  const V3 wi = b.local(wi_w), wo = b.local(wo_w);
-  if (b.kind == kMetal) return microfacet_pdf(b, wi, wo);
-  if (b.kind == kMeasured) return merl_pdf(b.merl, wi, wo);
-  if (b.kind == kPlastic) return 0.5f * (diffuse_pdf(wi, wo) + microfacet_pdf(b, wi, wo));
+// The sum of a layer's non-specular component densities.
+__device__ float layer_pdf_sum(const Layer &b, V3 wi, V3 wo) {
+  switch (b.kind) {
+    case kTransparent: return 0.0f;
+    case kMetal: return microfacet_pdf(b, wi, wo);
+    case kMeasured: return merl_pdf(b.merl, wi, wo);
+    case kSubstrate: return fb_pdf(b, wi, wo);
+    case kPlastic: return diffuse_pdf(wi, wo) + microfacet_pdf(b, wi, wo);
+    case kUber: {
+      float p = 0.0f;
+      if (!black(b.kd)) p += diffuse_pdf(wi, wo);
+      if (!black(b.ks)) p += microfacet_pdf(b, wi, wo);
+      return p;
+    }
+    default: return diffuse_pdf(wi, wo);
+  }
+}
+// Samples non-specular component c of a layer: the exitant direction and
+// that component's own density (0: the sample is rejected).
+__device__ float layer_sample(const Layer &b, int c, V3 wi, float u0, float u1, V3 &wo) {
+  bool glossy = false;
+  switch (b.kind) {
+    case kMeasured: {  // MERLMeasured::Sample (MERLMeasured.cpp:302-369)
+      float pdf = 0.0f;
+      merl_sample(b.merl, wi, u0, u1, wo, pdf);
+      return pdf;
+    }
+    case kSubstrate:
+      if (!fb_sample(b, wi, u0, u1, wo)) return 0.0f;
+      return fb_pdf(b, wi, wo);
+    case kMetal: glossy = true; break;
+    case kPlastic: glossy = c == 1; break;
+    case kUber: glossy = black(b.kd) || c == 1; break;
+    default: break;
+  }
+  if (glossy) {
+    if (!blinn_sample(b.exponent, wi, u0, u1, wo)) return 0.0f;
+    return microfacet_pdf(b, wi, wo);
+  }
+  // BxDF::Sample (Core/BxDF.cpp:20-31): cosine hemisphere on the incident side
+  wo = cosine_hemisphere(u0, u1);
+  if (wi.z < 0.0f) wo.z = -wo.z;
   return diffuse_pdf(wi, wo);
 }
 
+// BSDF::Evaluate (Core/BSDF.cpp:22-40): every non-specular component is a
+// reflection, so directions on opposite sides of the geometric normal give
+// zero; the layers' components are summed, each layer scaled.
+__device__ V3 bsdf_eval(const Bsdf &b, V3 wi_w, V3 wo_w) {
+  if (!(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f)) return v3(0, 0, 0);
+  const V3 wi = b.local(wi_w), wo = b.local(wo_w);
+  const V3 f = mul(b.L0.scale, layer_eval(b.L0, wi, wo));
+  if (b.nl == 1) return f;
+  const Layer l = layer1(b);
+  return f + mul(l.scale, layer_eval(l, wi, wo));
+}
+
+// The derivative of bsdf_eval with respect to the per-triangle albedo kd of
+// a single-layer matte, plastic or substrate surface (the diffuse term with
+// kd = 1); zero for the others, whose reflectance the albedo does not set.
+__device__ V3 bsdf_eval_dkd(const Bsdf &b, V3 wi_w, V3 wo_w) {
+  const Layer &l = b.L0;
+  const bool albedo = b.nl == 1 && (l.kind == kLambert || l.kind == kOrenNayar || l.kind == kPlastic ||
+                                    l.kind == kSubstrate);
+  if (!albedo || !(dot(wi_w, b.ng) * dot(wo_w, b.ng) > 0.0f)) return v3(0, 0, 0);
+  const V3 wi = b.local(wi_w), wo = b.local(wo_w);
+  if (l.kind == kSubstrate) {
+    const float t1 = 1.0f - 0.5f * fabsf(wo.z), t2 = 1.0f - 0.5f * fabsf(wi.z);
+    const float p1 = t1 * t1 * t1 * t1 * t1, p2 = t2 * t2 * t2 * t2 * t2;
+    return (v3(1.0f, 1.0f, 1.0f) - l.ks) * ((28.0f / (23.0f * kPi)) * (1.0f - p1) * (1.0f - p2));
+  }
+  Layer u = l;
+  u.kd = v3(1.0f, 1.0f, 1.0f);
+  return diffuse_eval(u, wi, wo);
+}
+
+// BSDF::PDF (Core/BSDF.cpp:42-58): the average of the non-specular
+// component densities.
+__device__ float bsdf_pdf(const Bsdf &b, V3 wi_w, V3 wo_w) {
+  const int n = bsdf_ncomp(b);
+  if (n == 0) return 0.0f;
+  const V3 wi = b.local(wi_w), wo = b.local(wo_w);
+  float p = layer_pdf_sum(b.L0, wi, wo);
+  if (b.nl == 2) p += layer_pdf_sum(layer1(b), wi, wo);
+  return n == 1 ? p : p / n;
+}
+
 // BSDF::Sample (Core/BSDF.cpp:110-168) over the non-specular components:
-// pick a component uniformly, sample it, average the densities of all
-// components at the sampled direction, evaluate the whole BSDF.
-__device__ V3 bsdf_sample(const Bsdf &b, V3 wi_w, float uc, float u0, float u1, V3 &wo_w, float &pdf) {
-  if (b.kind == kTransparent) {  // no non-specular component to sample
-    pdf = 0.0f;
-    wo_w = wi_w;
-    return v3(0, 0, 0);
-  }
+// sample component comp (0 .. bsdf_ncomp - 1; the caller picks it
+// uniformly), add the other components' densities at the sampled direction
+// and average over n_all (the non-specular count for direct lighting;
+// every component, specular ones included, when the caller samples
+// BSDF_ALL), evaluate the whole BSDF.
+__device__ V3 bsdf_sample_c(const Bsdf &b, int comp, V3 wi_w, float u0, float u1, V3 &wo_w, float &pdf, int n_all) {
+  const int n = bsdf_ncomp(b);
+  pdf = 0.0f;
+  wo_w = wi_w;
+  if (n == 0) return v3(0, 0, 0);
   const V3 wi = b.local(wi_w);
-  if (b.kind == kMeasured) {  // the single MERLMeasured component (BSDF.cpp:110-168)
-    V3 wo;
-    merl_sample(b.merl, wi, u0, u1, wo, pdf);
-    wo_w = b.world(wo);
-    if (!(pdf > 0.0f)) return v3(0, 0, 0);
-    return bsdf_eval(b, wi_w, wo_w);
-  }
-  const int nc = b.components();
-  const int comp = min((int)(uc * nc), nc - 1);
   V3 wo;
-  const bool glossy = b.kind == kMetal || (b.kind == kPlastic && comp == 1);
-  if (glossy) {
-    // BlinnDistribution::Sample (BlinnDistribution.h:86-101)
-    const float ct = powf(u0, 1.0f / (b.exponent + 1.0f));
-    const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
-    const float phi = u1 * 2.0f * kPi;
-    V3 h = v3(st * cosf(phi), st * sinf(phi), ct);
-    if (wi.z * h.z < 0.0f) h.z = -h.z;
-    wo = h * (2.0f * dot(wi, h)) - wi;
-    if (wi.z * wo.z < 0.0f) {  // Microfacet::Sample rejects the wrong hemisphere
-      pdf = 0.0f;
-      wo_w = b.world(wo);
-      return v3(0, 0, 0);
-    }
+  float pc;
+  int kind;
+  MerlDev merl;
+  const int n0 = layer_ncomp(b.L0);
+  if (comp < n0 || b.nl == 1) {
+    pc = layer_sample(b.L0, comp, wi, u0, u1, wo);
+    kind = b.L0.kind;
+    merl = b.L0.merl;
   } else {
-    // BxDF::Sample (Core/BxDF.cpp:20-31): cosine hemisphere on the incident side
-    wo = cosine_hemisphere(u0, u1);
-    if (wi.z < 0.0f) wo.z = -wo.z;
+    const Layer l = layer1(b);
+    pc = layer_sample(l, comp - n0, wi, u0, u1, wo);
+    kind = l.kind;
+    merl = l.merl;
   }
   wo_w = b.world(wo);
-  if (b.kind == kMetal) {
-    pdf = microfacet_pdf(b, wi, wo);
-  } else if (b.kind == kPlastic) {
-    pdf = 0.5f * (diffuse_pdf(wi, wo) + microfacet_pdf(b, wi, wo));
+  if (!(pc > 0.0f)) return v3(0, 0, 0);
+  if (n == 1 && n_all == 1) {
+    pdf = pc;
   } else {
-    pdf = diffuse_pdf(wi, wo);
+    // the sampled component's own density, plus the others' at wo
+    float p = layer_pdf_sum(b.L0, wi, wo) + (b.nl == 2 ? layer_pdf_sum(layer1(b), wi, wo) : 0.0f);
+    if (kind == kMeasured) p += pc - merl_pdf(merl, wi, wo);  // MERL's sample density as it returned it
+    pdf = p / n_all;
   }
   return bsdf_eval(b, wi_w, wo_w);
+}
+// The direct-lighting form: a non-specular component picked uniformly with uc.
+__device__ __forceinline__ V3 bsdf_sample(const Bsdf &b, V3 wi_w, float uc, float u0, float u1, V3 &wo_w,
+                                          float &pdf) {
+  const int n = bsdf_ncomp(b);
+  return bsdf_sample_c(b, min((int)(uc * n), max(n - 1, 0)), wi_w, u0, u1, wo_w, pdf, n);
 }
 
 // ------------------------------------------------------------------ shading --
@@ -529,8 +721,13 @@ __device__ __forceinline__ float next_min_t(const SceneDev &S, const Hit &h, V3 
   return fmaxf(0.0f, __fadd_ru(__fadd_ru(t, et), 1e-14f));
 }
 
+// The material's BSDF at a hit (Material::GetBSDF).  MixMaterial
+// (Materials/MixMaterial.cpp:29-57): the first material's components scaled
+// by the mix's scale s and the second's by 1 - s, a side whose scale is
+// black left out.  A per-triangle albedo replaces the diffuse reflectance
+// of a single-layer surface other than transparent and uber ones.
 __device__ Bsdf make_bsdf(const SceneDev &S, const Hit &h, int prim) {
-  const DevMaterial m = S.materials[S.prim_material[prim]];
+  const DevMaterial &m = S.materials[S.prim_material[prim]];
   Bsdf b;
   b.ng = h.ng;
   b.n = h.ns;
@@ -538,81 +735,99 @@ __device__ Bsdf make_bsdf(const SceneDev &S, const Hit &h, int prim) {
   const V3 a = fabsf(b.n.x) > 0.9f ? v3(0, 1, 0) : v3(1, 0, 0);
   b.e1 = normalized(cross(a, b.n));
   b.e2 = cross(b.n, b.e1);
-  b.kind = m.kind;
-  b.kd = load3(m.kd);
-  if (S.tri_albedo && m.kind != kTransparent) {  // a transparent surface's reflectance is the material's
-    const float *ta = S.tri_albedo + 3 * (int64_t)h.g;
-    if (ta[0] == ta[0]) b.kd = v3(fminf(1.0f, fmaxf(0.0f, ta[0])), fminf(1.0f, fmaxf(0.0f, ta[1])),
-                                  fminf(1.0f, fmaxf(0.0f, ta[2])));
+  b.m1 = nullptr;
+  b.s1 = v3(0, 0, 0);
+  if (m.kind == kMix) {
+    const V3 s0 = load3(m.mix_scale), s1 = v3(1.0f - s0.x, 1.0f - s0.y, 1.0f - s0.z);
+    const bool has0 = !black(s0), has1 = !black(s1) && m.mix[1] >= 0;
+    b.nl = has0 && has1 ? 2 : 1;
+    if (has0) {
+      b.L0 = make_layer(S.materials[m.mix[0]]);
+      b.L0.scale = s0;
+      if (has1) {
+        b.m1 = S.materials + m.mix[1];
+        b.s1 = s1;
+      }
+    } else if (has1) {
+      b.L0 = make_layer(S.materials[m.mix[1]]);
+      b.L0.scale = s1;
+    } else {  // nothing scatters
+      b.L0 = make_layer(m);
+      b.L0.kind = kTransparent;
+      b.L0.kd = b.L0.ks = v3(0, 0, 0);
+    }
+    return b;
   }
-  b.ks = load3(m.ks);
-  b.exponent = m.exponent;
-  b.on_a = m.on_a;
-  b.on_b = m.on_b;
-  b.eta = load3(m.eta);
-  b.k2 = load3(m.k2);
-  b.merl = m.merl;
-  b.ior = m.ior;
+  b.nl = 1;
+  b.L0 = make_layer(m);
+  if (S.tri_albedo && m.kind != kTransparent && m.kind != kUber) {
+    const float *ta = S.tri_albedo + 3 * (int64_t)h.g;
+    if (ta[0] == ta[0]) b.L0.kd = v3(fminf(1.0f, fmaxf(0.0f, ta[0])), fminf(1.0f, fmaxf(0.0f, ta[1])),
+                                     fminf(1.0f, fmaxf(0.0f, ta[2])));
+  }
   return b;
 }
 
 // --------------------------------------------------------------- specular --
-// FresnelDielectric(inner, 1)::operator() (Core/Fresnel.h:96-124).
-__device__ __forceinline__ float fresnel_dielectric_ior(float c, float inner) {
-  c = fminf(1.0f, fmaxf(-1.0f, c));
-  float ni = inner, no = 1.0f;
-  if (c < 0.0f) {
-    ni = 1.0f;
-    no = inner;
-  }
-  const float st = no / ni * sqrtf(fmaxf(0.0f, 1.0f - c * c));
-  if (st >= 1.0f) return 1.0f;
-  const float ct = sqrtf(fmaxf(0.0f, 1.0f - st * st));
-  c = fabsf(c);
-  const float rpar = (ni * c - no * ct) / (ni * c + no * ct);
-  const float rper = (no * c - ni * ct) / (no * c + ni * ct);
-  return (rpar * rpar + rper * rper) * 0.5f;
+// The specular reflection and transmission weights of a layer
+// (TransparentMaterial: kd, ks; UberMaterial: kr, 1 - opacity).
+__device__ __forceinline__ V3 layer_spec_r(const Layer &l) {
+  return l.kind == kTransparent ? l.kd : (l.kind == kUber ? l.kr : v3(0, 0, 0));
+}
+__device__ __forceinline__ V3 layer_spec_t(const Layer &l) {
+  return l.kind == kTransparent ? l.ks : (l.kind == kUber ? l.kt : v3(0, 0, 0));
 }
 
 // LTEIntegrator::_SpecularReflect (Core/LTEIntegrator.cpp:66-92) with
 // SpecularReflection<FresnelDielectric>::Sample (BxDFs/SpecularReflection.h):
 // the mirror direction of wo (towards the viewer) about the shading normal
-// and its weight r * F(cos) -- no cosine and no density, the BxDF accounts
-// for both.  False when the material has no reflection component, the
-// weight is black or the direction grazes the shading plane.
+// and its weight scale * r * F(cos) -- no cosine and no density, the BxDF
+// accounts for both.  False when the BSDF has no reflection component, the
+// weight is black or the direction grazes the shading plane.  (A BSDF has
+// at most one specular reflection: the host refuses mixes of two.)
 __device__ __forceinline__ bool specular_reflect(const Bsdf &b, V3 wo_w, V3 &dir, V3 &val) {
-  if (b.kind != kTransparent || black(b.kd)) return false;
-  const V3 wi = b.local(wo_w);
-  dir = b.world(v3(-wi.x, -wi.y, wi.z));
-  val = b.kd * fresnel_dielectric_ior(wi.z, b.ior);
-  return !black(val) && fabsf(dot(dir, b.n)) > kEps;
+  for (int i = 0; i < b.nl; ++i) {
+    const Layer l = i == 0 ? b.L0 : layer1(b);
+    const V3 r = layer_spec_r(l);
+    if (black(r)) continue;
+    const V3 wi = b.local(wo_w);
+    dir = b.world(v3(-wi.x, -wi.y, wi.z));
+    val = mul(l.scale, r) * fresnel_dielectric_ior(wi.z, l.ior);
+    return !black(val) && fabsf(dot(dir, b.n)) > kEps;
+  }
+  return false;
 }
 
 // LTEIntegrator::_SpecularTransmit (LTEIntegrator.cpp:94-126) with
 // SpecularTransmission::Sample (BxDFs/SpecularTransmission.cpp:33-66): the
 // refracted direction (Snell's law, the indices swapped when wo is inside),
-// its weight t * (1 - F(cos)) * eta^2 (eta = 1/ior entering, ior leaving);
-// false on total internal reflection (black weight), at normal-grazing
-// incidence, or when the material has no transmission component.
+// its weight scale * t * (1 - F(cos)) * eta^2 (eta = 1/ior entering, ior
+// leaving); false on total internal reflection (black weight), at
+// normal-grazing incidence, or when the BSDF has no transmission component.
 __device__ __forceinline__ bool specular_transmit(const Bsdf &b, V3 wo_w, V3 &dir, V3 &val) {
-  if (b.kind != kTransparent || black(b.ks)) return false;
-  const float cn = dot(wo_w, b.n);
-  if (fabsf(cn) < kEps) return false;
-  const V3 wi = b.local(wo_w);
-  float zs = -1.0f, ni = b.ior, no = 1.0f;
-  if (wi.z < 0.0f) {
-    zs = 1.0f;
-    ni = 1.0f;
-    no = b.ior;
+  for (int i = 0; i < b.nl; ++i) {
+    const Layer l = i == 0 ? b.L0 : layer1(b);
+    const V3 t = layer_spec_t(l);
+    if (black(t)) continue;
+    const float cn = dot(wo_w, b.n);
+    if (fabsf(cn) < kEps) return false;
+    const V3 wi = b.local(wo_w);
+    float zs = -1.0f, ni = l.ior, no = 1.0f;
+    if (wi.z < 0.0f) {
+      zs = 1.0f;
+      ni = 1.0f;
+      no = l.ior;
+    }
+    const float eta = no / ni;
+    const float st2 = eta * eta * (1.0f - wi.z * wi.z);
+    if (st2 >= 1.0f) return false;
+    const float ct = sqrtf(1.0f - st2);
+    dir = b.world(v3(-wi.x * eta, -wi.y * eta, ct * zs));
+    const float e = cn > 0.0f ? 1.0f / l.ior : l.ior;
+    val = mul(l.scale, t) * ((1.0f - fresnel_dielectric_ior(wi.z, l.ior)) * (e * e));
+    return !black(val) && fabsf(dot(dir, b.n)) > kEps;
   }
-  const float eta = no / ni;
-  const float st2 = eta * eta * (1.0f - wi.z * wi.z);
-  if (st2 >= 1.0f) return false;
-  const float ct = sqrtf(1.0f - st2);
-  dir = b.world(v3(-wi.x * eta, -wi.y * eta, ct * zs));
-  const float e = cn > 0.0f ? 1.0f / b.ior : b.ior;
-  val = b.ks * ((1.0f - fresnel_dielectric_ior(wi.z, b.ior)) * (e * e));
-  return !black(val) && fabsf(dot(dir, b.n)) > kEps;
+  return false;
 }
 
 __device__ Hit make_hit(const SceneDev &S, V3 o, V3 d, float t, int prim, int tri) {

@@ -12,7 +12,17 @@
 
 namespace skw {
 
-enum BsdfKind : int32_t { kLambert = 0, kOrenNayar = 1, kPlastic = 2, kMetal = 3, kMeasured = 4, kTransparent = 5 };
+enum BsdfKind : int32_t {
+  kLambert = 0,
+  kOrenNayar = 1,
+  kPlastic = 2,
+  kMetal = 3,
+  kMeasured = 4,
+  kTransparent = 5,
+  kSubstrate = 6,
+  kUber = 7,
+  kMix = 8
+};
 
 // Material constants after the reference's clamps (MatteMaterial.cpp:29-50,
 // PlasticMaterial.cpp:33-53, MetalMaterial.cpp:58-101).  kTransparent
@@ -26,7 +36,12 @@ struct DevMaterial {
   float on_a, on_b;    // Oren-Nayar A, B
   float eta[3], k2[3]; // conductor refractive index and squared absorption
   MerlDev merl;        // kMeasured: the tabulated BRDF
-  float ior;           // kTransparent: refractive index (outside: 1)
+  float ior;           // kTransparent, kUber: refractive index (outside: 1); kPlastic 1.5
+  float kr[3];         // kUber: specular reflectance
+  float kt[3];         // kUber: specular transmittance (1 - opacity; 0 for an opaque surface)
+  float pdiff;         // kSubstrate: probability of sampling the diffuse lobe
+  int32_t mix[2];      // kMix: the two materials (indices; mix[1] may be -1)
+  float mix_scale[3];  // kMix: the first material's scale (the second's is 1 - scale)
 };
 
 struct AreaLight {

@@ -38,6 +38,8 @@ cudaError_t upload(skw_scene *s, const std::vector<T> &v, const T **out) {
 }
 
 inline float clamp01(float v) { return std::min(1.0f, std::max(0.0f, v)); }
+// The reference's luminance of an RGB coefficient (SpectrumRoutines::Luminance).
+inline float lum(float r, float g, float b) { return 0.05316285f * r + 0.58515348f * g + 0.36168367f * b; }
 
 // Transform::operator()(Point3D<float>) (Math/Transform.h:219-230), like the
 // accelerator builder, so shading points agree with the traced triangles.
@@ -307,6 +309,50 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
       }
     } else if (m.kind == SKW_MATERIAL_PLASTIC) {
       d.kind = skw::kPlastic;
+      d.ior = 1.5f;  // PlasticMaterial.cpp:43: FresnelDielectric(1.5, 1)
+    } else if (m.kind == SKW_MATERIAL_SUBSTRATE) {
+      d.kind = skw::kSubstrate;
+      // The lobe-sampling probability only shapes the variance (the
+      // estimator divides by the mixture density it samples): the share of
+      // the diffuse term's luminance in the two terms' luminances, kept in
+      // [0.1, 0.9] so that neither lobe goes unsampled.
+      const float ld = lum(d.kd[0] * (1 - d.ks[0]), d.kd[1] * (1 - d.ks[1]), d.kd[2] * (1 - d.ks[2]));
+      const float ls = lum(d.ks[0], d.ks[1], d.ks[2]);
+      d.pdiff = ld + ls > 0.0f ? std::min(0.9f, std::max(0.1f, ld / (ld + ls))) : 0.5f;
+    } else if (m.kind == SKW_MATERIAL_UBER) {
+      if (!(m.refractive_index > 0.0f)) {
+        skw_scene_destroy(s);
+        return fail(ctx, SKW_ERR_ARG, "an uber material needs a positive refractive index");
+      }
+      d.kind = skw::kUber;
+      d.ior = m.refractive_index;
+      bool opaque = true;
+      for (int k = 0; k < 3; ++k) {
+        const float op = clamp01(m.opacity[k]);
+        opaque = opaque && op >= 1.0f - 1e-2f && op <= 1.0f + 1e-2f;
+        d.kd[k] = clamp01(op * m.kd[k]);
+        d.ks[k] = clamp01(op * m.ks[k]);
+        d.kr[k] = clamp01(m.kr[k]);
+      }
+      for (int k = 0; k < 3; ++k) d.kt[k] = opaque ? 0.0f : 1.0f - clamp01(m.opacity[k]);
+      // BlinnDistribution(1 / roughness), clamped to [0, 1000] by the distribution
+      const float inv = m.roughness > 0.0f ? 1.0f / m.roughness : 1000.0f;
+      d.exponent = std::min(1000.0f, std::max(0.0f, inv));
+    } else if (m.kind == SKW_MATERIAL_MIX) {
+      d.kind = skw::kMix;
+      for (int k = 0; k < 2; ++k) {
+        const int32_t j = m.mix[k];
+        if (j < -1 || j >= n_materials || (k == 0 && j < 0)) {
+          skw_scene_destroy(s);
+          return fail(ctx, SKW_ERR_ARG, "a mix material's materials must be indices into the material array");
+        }
+        if (j >= 0 && materials[j].kind == SKW_MATERIAL_MIX) {
+          skw_scene_destroy(s);
+          return fail(ctx, SKW_ERR_UNSUPPORTED, "a mix of mix materials");
+        }
+        d.mix[k] = j;
+      }
+      for (int k = 0; k < 3; ++k) d.mix_scale[k] = clamp01(m.mix_scale[k]);
     } else if (m.kind == SKW_MATERIAL_METAL) {
       d.kind = skw::kMetal;
     } else if (m.kind == SKW_MATERIAL_MEASURED) {
@@ -410,9 +456,29 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
   D.n_area_lights = (int32_t)lights.size();
   D.n_point_lights = n_point_lights;
   D.emission_scale = 1.0f;
+  // Specular components of a material: a transparent one's, an uber one's
+  // reflection (kr) and transmission (kt); a mix's from its two materials,
+  // of which at most one may have any (one specular reflection and one
+  // transmission per BSDF, as the specular stages follow them).
+  auto has_spec = [&](const skw::DevMaterial &d) {
+    auto nb = [](const float *v) { return v[0] != 0.0f || v[1] != 0.0f || v[2] != 0.0f; };
+    return d.kind == skw::kTransparent || (d.kind == skw::kUber && (nb(d.kr) || nb(d.kt)));
+  };
+  for (int32_t i = 0; i < n_materials; ++i) {
+    const skw::DevMaterial &d = mats[(size_t)i];
+    if (d.kind == skw::kMix && d.mix[1] >= 0 && has_spec(mats[(size_t)d.mix[0]]) &&
+        has_spec(mats[(size_t)d.mix[1]])) {
+      skw_scene_destroy(s);
+      return fail(ctx, SKW_ERR_UNSUPPORTED, "a mix of two materials that both have specular components");
+    }
+  }
   D.has_specular = 0;
-  for (int32_t p = 0; p < n_prims; ++p)
-    if (mats[(size_t)prims[p].material].kind == skw::kTransparent) D.has_specular = 1;
+  for (int32_t p = 0; p < n_prims; ++p) {
+    const skw::DevMaterial &d = mats[(size_t)prims[p].material];
+    if (has_spec(d) || (d.kind == skw::kMix && (has_spec(mats[(size_t)d.mix[0]]) ||
+                                                (d.mix[1] >= 0 && has_spec(mats[(size_t)d.mix[1]])))))
+      D.has_specular = 1;
+  }
   D.max_spec_depth = 10;  // the GUI's DirectLightParams / PhotonMapParams default
   s->n_triangles = tri_count;
   D.scene_abs = s->accel->scene_abs;
@@ -688,8 +754,8 @@ cudaError_t record_media_level(skw_scene *s, const Plan &P, const Workspace &W, 
     cudaError_t r = cudaMemsetAsync(W.counts + 2, 0, sizeof(int), sq);
     if (r == cudaSuccess)
       r = skw::launch_media_specular(adjoint, s->dev, d_views, nv, m, px0, P.spp, P.slots, P.spec_slot, rays, hits,
-                                     sample, w, node, c, dfilm, W.contrib, W.mrays, W.mtarget, W.mval, W.mdem,
-                                     W.counts + 2, a->d_status, sq);
+                                     sample, w, node, c, dfilm, adjoint ? W.tcam : nullptr, W.contrib, W.mrays,
+                                     W.mtarget, W.mval, W.mdem, W.counts + 2, a->d_status, sq);
     if (r == cudaSuccess)
       r = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.mrays, (int64_t)m * s->dev.medium.max_steps,
                                 W.counts + 2, a->scene_abs, nullptr, W.mocc, a->d_status, sq, ctas, W.counts + 8);
@@ -1446,7 +1512,7 @@ int skw_render_direct_adjoint(skw_scene *s, const skw_camera *cam, const skw_ren
       if ((e = skw::launch_shade_specular_adjoint(s->dev, d_view, 1, cl, px0, P.spp, P.nl, d_film, g_albedo,
                                                   g_emission, q, L, W.qhits, W.srays, W.starget, s_dkd, s_dem,
                                                   W.counts, W.brays, W.btarget, b_dkd, W.brgb, W.counts + 1,
-                                                  W.bnrm, st)) != cudaSuccess)
+                                                  W.bnrm, st, P.media ? W.tcam : nullptr)) != cudaSuccess)
         break;
       const int64_t lsh = cl * (P.nl + P.npl), lbs = cl * P.nl;
       if (lsh > 0 && (e = skw::launch_traversal(false, cap, a->d_nodes, a->d_tris, W.srays, lsh, W.counts,
@@ -1538,6 +1604,10 @@ int skw_render_photon(skw_scene *s, const skw_photon_map *pm, const skw_camera *
   M.n_irr = (int32_t)pm->n_irr;
   M.max_irr_dist = pm->max_irr_dist;
   M.dirs = pm->d_dirs;
+  for (int k = 0; k < 3; ++k) {
+    M.lo[k] = s->accel->info.bounds[k];
+    M.hi[k] = s->accel->info.bounds[3 + k];
+  }
   skw_accel *a = s->accel;
   skw::TraceFn trace = [a](const void *rays, int64_t n, const int *n_dev, void *hits, cudaStream_t stq, int *work) {
     return skw::launch_traversal(true, a->stack_cap, a->d_nodes, a->d_tris, rays, n, n_dev, a->scene_abs, nullptr,

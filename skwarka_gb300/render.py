@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib
 from .accel import Context, TriangleMesh, default_context
 
-MATTE, PLASTIC, METAL, MEASURED, TRANSPARENT = 0, 1, 2, 3, 4
+MATTE, PLASTIC, METAL, MEASURED, TRANSPARENT, SUBSTRATE, UBER, MIX = 0, 1, 2, 3, 4, 5, 6, 7
 
 
 class MeasuredBRDF:
@@ -80,6 +80,10 @@ class Material:
     k: tuple = (0.0, 0.0, 0.0)
     measured: "MeasuredBRDF | None" = None
     refractive_index: float = 1.5
+    kr: tuple = (0.0, 0.0, 0.0)         # UBER: specular reflectance
+    opacity: tuple = (1.0, 1.0, 1.0)    # UBER: opacity (1: opaque)
+    mix: tuple = (-1, -1)               # MIX: indices of the two mixed materials
+    mix_scale: tuple = (0.5, 0.5, 0.5)  # MIX: the first material's scale
 
 
 @dataclass
@@ -136,7 +140,8 @@ class Camera:
 class skw_material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("roughness", C.c_float),
                 ("sigma", C.c_float), ("eta", C.c_float * 3), ("k", C.c_float * 3), ("measured", C.c_void_p),
-                ("refractive_index", C.c_float)]
+                ("refractive_index", C.c_float), ("kr", C.c_float * 3), ("opacity", C.c_float * 3),
+                ("mix", C.c_int32 * 2), ("mix_scale", C.c_float * 3)]
 
 
 class skw_render_primitive(C.Structure):
@@ -168,7 +173,9 @@ def c_material(m: Material, measured_handle=None) -> skw_material:
     if h is None and m.measured is not None:
         h = m.measured.handle
     return skw_material(m.kind, (C.c_float * 3)(*m.kd), (C.c_float * 3)(*m.ks), m.roughness, m.sigma,
-                        (C.c_float * 3)(*m.eta), (C.c_float * 3)(*m.k), h, m.refractive_index)
+                        (C.c_float * 3)(*m.eta), (C.c_float * 3)(*m.k), h, m.refractive_index,
+                        (C.c_float * 3)(*m.kr), (C.c_float * 3)(*m.opacity), (C.c_int32 * 2)(*m.mix),
+                        (C.c_float * 3)(*m.mix_scale))
 
 
 def c_camera(cam: Camera) -> skw_camera:

@@ -252,3 +252,21 @@ def c1_golden():
 
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "c1":
     c1_golden()
+
+
+def materials_golden():
+    """The reference's direct-lighting renders (16x16 spp, maximum specular
+    depth 6) of scene_fixtures.material_cases(): SubstrateMaterial,
+    UberMaterial and MixMaterial planes under an area light and spheres over
+    the floor."""
+    ref = Reference()
+    out = {}
+    for name, (prims, mats, lights, cam) in sf.material_cases().items():
+        out[name], _ = ref.render_direct(prims, mats, lights, cam, 16, 16)
+        print(f"materials: {name} mean {out[name].mean():.5f}")
+    np.savez_compressed(OUT / "materials.npz", **out)
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "materials":
+    materials_golden()
+

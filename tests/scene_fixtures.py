@@ -345,3 +345,41 @@ def specular_medium():
     from skwarka_gb300.render import Medium
     return Medium(lo=(-1.5, -1.5, 0.0), hi=(1.5, 1.5, 1.3), sigma_a=(0.1, 0.1, 0.1), sigma_s=(0.3, 0.3, 0.3),
                   g=0.3, step=0.05)
+
+
+def material_cases():
+    """{name: (prims, materials, point_lights, camera)} for SubstrateMaterial,
+    UberMaterial and MixMaterial: the plane of material_plane_scenes() under
+    its area light with a substrate (smooth and rough), an opaque uber with a
+    specular reflection (the light's mirror image in the plane), and a mix of
+    matte and plastic; and the sphere of specular_scene() as a half-opaque
+    uber (its specular transmission, reflection, diffuse and glossy parts)
+    and as a mix of clear glass and matte."""
+    from skwarka_gb300.render import MATTE, MIX, PLASTIC, SUBSTRATE, TRANSPARENT, UBER, Material
+    planes = material_plane_scenes()
+    prims, mats, pls, cam = planes["area_matte"]
+    out = {}
+    plane_mats = {
+        "substrate": [Material(kind=SUBSTRATE, kd=(0.6, 0.45, 0.3), ks=(0.25, 0.25, 0.25), roughness=0.1)],
+        "substrate_rough": [Material(kind=SUBSTRATE, kd=(0.6, 0.45, 0.3), ks=(0.25, 0.25, 0.25), roughness=0.5)],
+        "uber_opaque": [Material(kind=UBER, kd=(0.4, 0.3, 0.2), ks=(0.3, 0.3, 0.3), kr=(0.2, 0.2, 0.2),
+                                 roughness=0.1, refractive_index=1.5)],
+        "mix_matte_plastic": [Material(kind=MIX, mix=(1, 2), mix_scale=(0.3, 0.5, 0.7)),
+                              Material(kind=MATTE, kd=(0.8, 0.6, 0.4)),
+                              Material(kind=PLASTIC, kd=(0.2, 0.3, 0.5), ks=(0.5, 0.5, 0.5), roughness=0.1)],
+    }
+    for name, ms in plane_mats.items():
+        # the plane takes material 0; the light's black matte goes last
+        out["plane_" + name] = ([prims[0].__class__(prims[0].mesh, 0), prims[1].__class__(
+            prims[1].mesh, len(ms), emission=prims[1].emission)], ms + [Material(kd=(0.0, 0.0, 0.0))], pls, cam)
+    uber = Material(kind=UBER, kd=(0.3, 0.3, 0.3), ks=(0.2, 0.2, 0.2), kr=(0.3, 0.3, 0.3), roughness=0.2,
+                    opacity=(0.5, 0.6, 0.7), refractive_index=1.5)
+    out["sphere_uber"] = specular_scene(uber, "area")
+    glass = Material(kind=TRANSPARENT, kd=(1.0, 1.0, 1.0), ks=(1.0, 1.0, 1.0), refractive_index=1.5)
+    sp, sm, sl, sc = specular_scene(glass, "area")
+    # the sphere (material 1) becomes a mix of glass (appended) and a matte
+    n = len(sm)
+    mix = Material(kind=MIX, mix=(n, n + 1), mix_scale=(0.6, 0.6, 0.6))
+    out["sphere_mix_glass_matte"] = (sp, [sm[0], mix] + list(sm[2:]) + [glass, Material(kd=(0.7, 0.2, 0.2))], sl, sc)
+    return out
+
