@@ -626,6 +626,8 @@ def photon_bench(args, dev, ctx, measure_cpu):
                        "point light I=50; k=100 r=0.05 lookups at 512x512x16 primary hits; render 512x512x4 spp",
            "paths": paths, "shoot_paths_per_s": paths / (info["shoot_ms"] / 1e3), "shoot_ms": info["shoot_ms"],
            "maps_build_ms": info["build_ms"], "shoot_and_build_wall_s": wall,
+           "trees_on_gpu": {k: bool(info["trees_on_gpu"] & (1 << i)) for i, k in
+                            enumerate(("caustic", "direct", "indirect"))},
            "photons": {k: info["n_" + k] for k in ("caustic", "direct", "indirect", "irradiance")}}
     # shooting roofline: rays traced (emitted + bounces, counted on the device)
     # at the oracle's bytes per emitted / bounce ray, plus 28 bytes per stored

@@ -236,8 +236,17 @@ int skw_direction_table(double *out);
  * (split coordinate as float bits, right-child/flags word).  Needs no GPU.
  * Either output may be NULL. */
 int skw_kdtree_build_host(const float *positions, int64_t n, int threads, int32_t *perm, uint32_t *node_words);
+/* The same tree built on the GPU (level by level over per-axis sorted
+ * lists), same outputs; *median_tie = 1 when some node's median ties on its
+ * split axis (there the reference's tree is std::nth_element's choice among
+ * the equal points and the host build is the one to use), else 0 and the
+ * outputs equal skw_kdtree_build_host's.  Host buffers. */
+int skw_kdtree_build_device(skw_ctx *ctx, const float *positions, int64_t n, int32_t *perm, uint32_t *node_words,
+                            int32_t *median_tie);
 
-/* Builds the tree on the host and uploads it.  positions: float xyz per
+/* Builds the tree -- on the GPU for 16,384 or more photons when no node's
+ * median ties on its split axis, else on the host; the same tree either way
+ * -- and keeps it on the device.  positions: float xyz per
  * photon; normal_ids: the photons' 16-bit surface-normal ids (NULL = all 0),
  * used by the filtered lookups.  Lookup results index the TREE order
  * (skw_kdtree_permutation maps them back to input order), as the
@@ -555,12 +564,14 @@ typedef struct skw_photon_map_info {
   double max_irradiance_lookup_dist;  /* m_max_irradiance_lookup_dist (inf if unbounded) */
   double scene_area;                  /* sum of the primitives' mesh areas */
   double shoot_ms, build_ms;          /* host wall time: GPU shooting; trees + irradiance map */
+  int32_t trees_on_gpu;               /* bit i: map i's tree (caustic, direct, indirect) built on the GPU */
 } skw_photon_map_info;
 
 /* Photon maps from given photon arrays (caustic, direct, indirect; any may
  * be empty except that an indirect map needs a direct one) and the paths each
  * map's photons came from: builds the three kd-trees (the reference's median
- * builder, KDTree.h:428-473, on the host) and the irradiance photon map
+ * builder, KDTree.h:428-473: on the GPU where no node's median ties on its
+ * split axis, else on the host, the same tree either way) and the irradiance photon map
  * (_ConstructIrradiancePhotonMap, PhotonLTEIntegrator.cpp:171-245: every 10th
  * indirect photon in tree order, k = 100 filtered lookups in each map on the
  * GPU, its kd-tree, and the 0.1 % percentile lookup radius).  scene_area is

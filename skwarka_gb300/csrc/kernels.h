@@ -209,10 +209,11 @@ cudaError_t launch_resolve_adjoint(const SceneDev &S, int capacity, int n_light_
 struct PhotonRec;
 struct PhotonShootArgs;
 using TraceFn = std::function<cudaError_t(const void *, int64_t, const int *, void *, cudaStream_t, int *)>;
-// Workspace bytes of one shooting chunk of n_paths paths.
-size_t photon_chunk_bytes(int64_t n_paths, int max_bounces);
+// Workspace bytes of one shooting chunk of n_paths paths with `slots`
+// indirect-photon slots per path.
+size_t photon_chunk_bytes(int64_t n_paths, int slots);
 // Shoots paths [path0, path0 + n_paths): writes the chunk's direct photons
-// (at most n_paths), indirect photons (at most n_paths * (max_bounces - 1))
+// (at most n_paths), indirect photons (at most n_paths * A.slots)
 // and caustic photons (at most n_paths) in path order, and their counts to
 // d_totals[0], d_totals[1], d_totals[2].
 cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, const TraceFn &trace, int64_t path0,

@@ -357,8 +357,12 @@ __global__ void __launch_bounds__(128) k_photon_bounce(SceneDev S, PhotonShootAr
         // indirect photons also land on specular surfaces (the reference's
         // note at PhotonShootingPipeline.cpp:203-210)
         const int c = n_indirect[path];
-        st_indirect[(int64_t)path * (A.max_bounces - 1) + c] = rec;
-        n_indirect[path] = c + 1;
+        if (c < A.slots) {
+          st_indirect[(int64_t)path * A.slots + c] = rec;
+          n_indirect[path] = c + 1;
+        } else {
+          atomicOr(A.overflow, 1);
+        }
       }
       // BSDF::Sample over all components
       float uc, u0, u1;
@@ -516,8 +520,8 @@ __global__ void k_irradiance_sum(const float4 *__restrict__ nodes, const float *
 
 }  // namespace
 
-size_t photon_chunk_bytes(int64_t n_paths, int max_bounces) {
-  const int64_t B1 = max_bounces > 1 ? max_bounces - 1 : 1;
+size_t photon_chunk_bytes(int64_t n_paths, int slots) {
+  const int64_t B1 = slots > 1 ? slots : 1;
   auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
   const int64_t nb = (n_paths + kScanBlock - 1) / kScanBlock;
   return 2 * (al(n_paths * 32) + al(n_paths * 12) + al(n_paths * 4)) + al(n_paths * 16) + 256 +
@@ -528,7 +532,7 @@ size_t photon_chunk_bytes(int64_t n_paths, int max_bounces) {
 cudaError_t photon_shoot_chunk(const SceneDev &S, const PhotonShootArgs &A, const TraceFn &trace, int64_t path0,
                                int n_paths, void *ws, PhotonRec *out_direct, PhotonRec *out_indirect,
                                PhotonRec *out_caustic, int *d_totals, cudaStream_t st) {
-  const int64_t B1 = A.max_bounces > 1 ? A.max_bounces - 1 : 1;
+  const int64_t B1 = A.slots > 1 ? A.slots : 1;
   auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
   char *p = (char *)ws;
   auto take = [&](size_t b) {

@@ -22,6 +22,7 @@ struct PhotonMapData {
   void *d_nodes = nullptr;
   uint16_t *d_nids = nullptr, *d_dirid = nullptr;
   float *d_weight = nullptr;
+  bool built_on_gpu = false;     // the tree came from the GPU builder
 };
 
 }  // namespace skw

@@ -2,6 +2,8 @@
 // split on the longest axis) and the 16-bit direction codec table.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
 #include <vector>
 
@@ -26,6 +28,28 @@ static_assert(sizeof(KdNode) == 16, "KdNode must be 16 bytes");
 // built on several threads (`threads` <= 0: all hardware threads).
 void build_photon_tree(const float *pos, int64_t n, int threads, std::vector<KdNode> &nodes,
                        std::vector<int32_t> &perm);
+
+// The same tree built on the GPU (photon_tree_gpu.cu) from device positions
+// (n x 3 floats): nodes and perm in device memory, *tie (device int) set
+// when some node's median ties on its split axis -- there the reference's
+// tree depends on std::nth_element's choice among equal points, and the
+// host build is the one to use.  Otherwise the tree equals
+// build_photon_tree's node for node.  scratch: photon_tree_gpu_scratch(n)
+// bytes.
+size_t photon_tree_gpu_scratch(int64_t n);
+int photon_tree_levels(int64_t n);
+cudaError_t build_photon_tree_gpu(const float *pos, int64_t n, KdNode *nodes, int32_t *perm, int *tie,
+                                  void *scratch, cudaStream_t st);
+// Gathers per-photon attributes into tree order: out[t] = in[perm[t]]
+// (normal ids, direction ids and 3-float weights; any may be null).
+cudaError_t gather_tree_order(const int32_t *perm, int64_t n, const uint16_t *nrm_in, const uint16_t *dir_in,
+                              const float *w_in, uint16_t *nrm_out, uint16_t *dir_out, float *w_out,
+                              cudaStream_t st);
+// Builds on the GPU where that gives the reference's tree, else on the host:
+// the device nodes (allocated here, freed by the caller with cudaFree), the
+// permutation on the host, and *on_gpu.  pos: host positions.
+cudaError_t build_photon_tree_device(const float *pos, int64_t n, cudaStream_t st, KdNode **d_nodes,
+                                     std::vector<int32_t> &perm, int32_t **d_perm, bool *on_gpu);
 
 // CompressedDirection table (Math/CompressedDirection.cpp:21-41): unit vector
 // of every 16-bit direction id, as 3 doubles per id.

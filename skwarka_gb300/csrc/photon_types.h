@@ -33,6 +33,11 @@ struct PhotonShootArgs {
   int32_t max_bounces;      // intersections per path
   float rr_probability;     // > 0: fixed Russian-roulette continue probability; 0: the reference's luminance rule
   uint64_t seed;
+  // Indirect-photon slots per path in a chunk's staging (<= max_bounces - 1);
+  // a path that would deposit more raises *overflow and the chunk is shot
+  // again with every slot (its photons then depend on nothing but the path).
+  int32_t slots;
+  int *overflow;
 };
 
 }  // namespace skw

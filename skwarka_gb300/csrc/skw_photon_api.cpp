@@ -52,11 +52,10 @@ int skw_direction_table(double *out) {
   return SKW_OK;
 }
 
-int skw_kdtree_build_host(const float *positions, int64_t n, int threads, int32_t *perm, uint32_t *node_words) {
-  if (n < 0 || (n > 0 && !positions) || n >= ((int64_t)1 << 29)) return SKW_ERR_ARG;
-  std::vector<skw::KdNode> nodes;
-  std::vector<int32_t> p;
-  skw::build_photon_tree(positions, n, threads, nodes, p);
+namespace {
+// perm and the (split, word) node pairs of a built tree.
+void export_tree(const std::vector<skw::KdNode> &nodes, const std::vector<int32_t> &p, int64_t n, int32_t *perm,
+                 uint32_t *node_words) {
   for (int64_t i = 0; i < n; ++i) {
     if (perm) perm[i] = p[(size_t)i];
     if (node_words) {
@@ -68,6 +67,47 @@ int skw_kdtree_build_host(const float *positions, int64_t n, int threads, int32_
       node_words[2 * i + 1] = nd.word;
     }
   }
+}
+}  // namespace
+
+int skw_kdtree_build_host(const float *positions, int64_t n, int threads, int32_t *perm, uint32_t *node_words) {
+  if (n < 0 || (n > 0 && !positions) || n >= ((int64_t)1 << 29)) return SKW_ERR_ARG;
+  std::vector<skw::KdNode> nodes;
+  std::vector<int32_t> p;
+  skw::build_photon_tree(positions, n, threads, nodes, p);
+  export_tree(nodes, p, n, perm, node_words);
+  return SKW_OK;
+}
+
+int skw_kdtree_build_device(skw_ctx *ctx, const float *positions, int64_t n, int32_t *perm, uint32_t *node_words,
+                            int32_t *median_tie) {
+  if (!ctx || !median_tie) return fail(ctx, SKW_ERR_ARG, "null argument");
+  if (n < 0 || (n > 0 && !positions) || n >= ((int64_t)1 << 29)) return fail(ctx, SKW_ERR_ARG, "bad photon buffer");
+  *median_tie = 0;
+  if (n == 0) return SKW_OK;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  float *d_pos = nullptr;
+  int32_t *d_perm = nullptr;
+  int *d_tie = nullptr;
+  skw::KdNode *d_nodes = nullptr;
+  void *scratch = nullptr;
+  int tie = 0;
+  std::vector<skw::KdNode> nodes((size_t)n);
+  std::vector<int32_t> p((size_t)n);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_pos, (size_t)n * 12);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_perm, (size_t)n * 4);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_tie, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_nodes, (size_t)n * sizeof(skw::KdNode));
+  if (e == cudaSuccess) e = cudaMalloc(&scratch, skw::photon_tree_gpu_scratch(n));
+  if (e == cudaSuccess) e = cudaMemcpy(d_pos, positions, (size_t)n * 12, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = skw::build_photon_tree_gpu(d_pos, n, d_nodes, d_perm, d_tie, scratch, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(&tie, d_tie, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(nodes.data(), d_nodes, (size_t)n * sizeof(skw::KdNode), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(p.data(), d_perm, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  for (void *q : {(void *)d_pos, (void *)d_perm, (void *)d_tie, (void *)d_nodes, scratch}) cudaFree(q);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "photon tree build");
+  export_tree(nodes, p, n, perm, node_words);
+  *median_tie = tie;
   return SKW_OK;
 }
 
@@ -77,23 +117,26 @@ int skw_kdtree_create(skw_ctx *ctx, const float *positions, const uint16_t *norm
   *out = nullptr;
   if (n < 0 || (n > 0 && !positions)) return fail(ctx, SKW_ERR_ARG, "bad photon buffer");
   if (n >= ((int64_t)1 << 29)) return fail(ctx, SKW_ERR_ARG, "too many photons (the node format holds < 2^29)");
-  std::vector<skw::KdNode> nodes;
   auto *t = new (std::nothrow) skw_kdtree();
   if (!t) return fail(ctx, SKW_ERR_OOM, "host allocation failed");
   t->ctx = ctx;
   t->n = n;
-  skw::build_photon_tree(positions, n, 0, nodes, t->perm);
-  std::vector<uint16_t> nids((size_t)std::max<int64_t>(n, 1), 0);
-  if (normal_ids)
-    for (int64_t i = 0; i < n; ++i) nids[(size_t)i] = normal_ids[t->perm[(size_t)i]];
   cudaError_t e = cudaSetDevice(ctx->device);
+  // the tree on the GPU where that gives the reference's (no median ties),
+  // else on the host
+  skw::KdNode *dn = nullptr;
+  int32_t *d_perm = nullptr;
+  bool on_gpu = false;
+  if (e == cudaSuccess) e = skw::build_photon_tree_device(positions, n, nullptr, &dn, t->perm, &d_perm, &on_gpu);
+  cudaFree(d_perm);
+  t->d_nodes = dn;
+  std::vector<uint16_t> nids((size_t)std::max<int64_t>(n, 1), 0);
+  if (normal_ids && e == cudaSuccess)
+    for (int64_t i = 0; i < n; ++i) nids[(size_t)i] = normal_ids[t->perm[(size_t)i]];
   const std::vector<double> &dirs = skw::direction_table_device();
-  const size_t nb = (size_t)std::max<int64_t>(n, 1) * sizeof(skw::KdNode);
-  if (e == cudaSuccess) e = cudaMalloc(&t->d_nodes, nb);
   if (e == cudaSuccess) e = cudaMalloc(&t->d_nids, nids.size() * sizeof(uint16_t));
   if (e == cudaSuccess) e = cudaMalloc(&t->d_dirs, dirs.size() * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&t->d_status, sizeof(unsigned));
-  if (e == cudaSuccess && n > 0) e = cudaMemcpy(t->d_nodes, nodes.data(), (size_t)n * sizeof(skw::KdNode), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(t->d_nids, nids.data(), nids.size() * sizeof(uint16_t), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(t->d_dirs, dirs.data(), dirs.size() * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(t->d_status, 0, sizeof(unsigned));

@@ -52,28 +52,58 @@ void free_map(Map &m) {
   m.d_weight = nullptr;
 }
 
-// KDTree<Photon>(photons) (Core/KDTree.h:428-473) on the host, then upload.
-cudaError_t build_map(Map &m) {
+// KDTree<Photon>(photons) (Core/KDTree.h:428-473): on the GPU where that
+// gives the reference's tree (no median ties; build_photon_tree_device),
+// else on the host; the photons' attributes in tree order.
+cudaError_t build_map(Map &m, cudaStream_t st) {
   m.n = (int64_t)m.input.size();
-  std::vector<float> pos((size_t)m.n * 3);
-  for (int64_t i = 0; i < m.n; ++i)
-    for (int k = 0; k < 3; ++k) pos[(size_t)(3 * i + k)] = m.input[(size_t)i].p[k];
-  std::vector<skw::KdNode> nodes;
-  skw::build_photon_tree(pos.data(), m.n, 0, nodes, m.perm);
-  std::vector<uint16_t> nids((size_t)m.n), dirid((size_t)m.n);
-  std::vector<float> w((size_t)m.n * 3);
-  for (int64_t t = 0; t < m.n; ++t) {
-    const PhotonRec &r = m.input[(size_t)m.perm[(size_t)t]];
-    nids[(size_t)t] = r.nrm;
-    dirid[(size_t)t] = r.dir;
-    for (int k = 0; k < 3; ++k) w[(size_t)(3 * t + k)] = r.w[k];
+  const size_t n = (size_t)m.n;
+  std::vector<float> pos(n * 3), w(n * 3);
+  std::vector<uint16_t> nids(n), dirid(n);
+  for (size_t i = 0; i < n; ++i) {
+    const PhotonRec &r = m.input[i];
+    for (int k = 0; k < 3; ++k) {
+      pos[3 * i + k] = r.p[k];
+      w[3 * i + k] = r.w[k];
+    }
+    nids[i] = r.nrm;
+    dirid[i] = r.dir;
   }
   skw::KdNode *dn = nullptr;
-  cudaError_t e = upload(nodes, &dn);
+  int32_t *d_perm = nullptr;
+  bool on_gpu = false;
+  cudaError_t e = skw::build_photon_tree_device(pos.data(), m.n, st, &dn, m.perm, &d_perm, &on_gpu);
   m.d_nodes = dn;
-  if (e == cudaSuccess) e = upload(nids, &m.d_nids);
-  if (e == cudaSuccess) e = upload(dirid, &m.d_dirid);
-  if (e == cudaSuccess) e = upload(w, &m.d_weight);
+  m.built_on_gpu = on_gpu;
+  if (e == cudaSuccess && on_gpu) {
+    // the attributes uploaded in photon order and gathered into tree order
+    uint16_t *nin = nullptr, *din = nullptr;
+    float *win = nullptr;
+    if ((e = upload(nids, &nin)) == cudaSuccess && (e = upload(dirid, &din)) == cudaSuccess &&
+        (e = upload(w, &win)) == cudaSuccess && (e = cudaMalloc(&m.d_nids, n * 2)) == cudaSuccess &&
+        (e = cudaMalloc(&m.d_dirid, n * 2)) == cudaSuccess && (e = cudaMalloc(&m.d_weight, n * 12)) == cudaSuccess &&
+        (e = skw::gather_tree_order(d_perm, m.n, nin, din, win, m.d_nids, m.d_dirid, m.d_weight, st)) ==
+            cudaSuccess)
+      e = cudaStreamSynchronize(st);
+    cudaFree(nin);
+    cudaFree(din);
+    cudaFree(win);
+    cudaFree(d_perm);
+    return e;
+  }
+  cudaFree(d_perm);
+  if (e != cudaSuccess) return e;
+  std::vector<uint16_t> nt(n), dt(n);
+  std::vector<float> wt(n * 3);
+  for (size_t t = 0; t < n; ++t) {
+    const size_t i = (size_t)m.perm[t];
+    nt[t] = nids[i];
+    dt[t] = dirid[i];
+    for (int k = 0; k < 3; ++k) wt[3 * t + k] = w[3 * i + k];
+  }
+  if (e == cudaSuccess) e = upload(nt, &m.d_nids);
+  if (e == cudaSuccess) e = upload(dt, &m.d_dirid);
+  if (e == cudaSuccess) e = upload(wt, &m.d_weight);
   return e;
 }
 
@@ -120,10 +150,10 @@ struct IrrBuffers {
 int build_maps(skw_photon_map *pm, cudaStream_t st) {
   skw_ctx *ctx = pm->ctx;
   Map &im = pm->maps[2];
-  cudaError_t e = build_map(im);
+  cudaError_t e = build_map(im, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "photon map upload");
   if (im.n == 0) {  // no indirect map: no irradiance photons
-    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = build_map(pm->maps[i]);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = build_map(pm->maps[i], st);
     return e == cudaSuccess ? SKW_OK : cuda_fail(ctx, e, "photon map upload");
   }
   const std::vector<double> &dirs = skw::direction_table();
@@ -195,7 +225,7 @@ int build_maps(skw_photon_map *pm, cudaStream_t st) {
     for (int mi : {2, 1, 0}) {  // the indirect map's tree exists; the others are built as they are needed
       if (e != cudaSuccess) break;
       Map &m = pm->maps[mi];
-      if (q0 == 0 && mi != 2 && (e = build_map(m)) != cudaSuccess) break;
+      if (q0 == 0 && mi != 2 && (e = build_map(m, st)) != cudaSuccess) break;
       if (!has[mi]) continue;
       e = skw::launch_knn(m.d_nodes, m.d_nids, pm->d_dirs, (int)m.n, B.q + 3 * q0, B.qn + 3 * q0, c,
                           kLookupIrradiance, pm->lookup_dist[mi], kMaxNormalDeviationCos, B.idx[mi], B.d2[mi],
@@ -358,51 +388,80 @@ int skw_photon_shoot(skw_scene *s, const skw_photon_params *params, skw_photon_m
   if (!(total > 2.220446049250313e-16)) lights.back().cdf = 1.0;
   skw::PhotonLight *d_lights = nullptr;
   if ((e = upload(lights, &d_lights)) != cudaSuccess) return cuda_fail(ctx, e, "light table");
-  skw::PhotonShootArgs A{d_lights, (int32_t)lights.size(), params->max_bounces, params->rr_probability, params->seed};
+  // Indirect photons are staged in per-path slots, so that the chunk's
+  // photons come out in path order; 63 slots cover every path of a scene
+  // whose paths end by Russian roulette (a path of 64 bounces survives with
+  // probability ~p^63).  A chunk where a path needs more is shot again in
+  // sub-chunks with a slot for every bounce.
+  const int full_slots = std::max(params->max_bounces - 1, 1);
+  const int slots = std::min(full_slots, 63);
+  skw::PhotonShootArgs A{d_lights, (int32_t)lights.size(), params->max_bounces, params->rr_probability, params->seed,
+                         slots, nullptr};
   skw_accel *a = s->accel;
   skw::TraceFn trace = [a](const void *rays, int64_t n, const int *n_dev, void *hits, cudaStream_t st, int *work) {
     return skw::launch_traversal(true, a->stack_cap, a->d_nodes, a->d_tris, rays, n, n_dev, a->scene_abs, nullptr,
                                  hits, a->d_status, st, 0, work, true);
   };
-  // per-path deposit slots for every bounce: 2^20 paths per chunk up to 64
-  // bounces, proportionally fewer above
+  // 2^20 paths per chunk with 63 indirect slots each; a re-shot chunk (every
+  // slot) runs in sub-chunks of the same workspace size
   const int64_t chunk = std::min<int64_t>(
-      params->paths, std::max<int64_t>((int64_t)1 << 12, ((int64_t)1 << 26) / std::max(params->max_bounces, 64)));
-  const int64_t B1 = std::max(params->max_bounces - 1, 1);
+      params->paths, std::max<int64_t>((int64_t)1 << 12, ((int64_t)1 << 26) / std::max(slots + 1, 64)));
+  const int64_t sub = std::max<int64_t>((int64_t)1 << 12, ((int64_t)1 << 26) / std::max(full_slots + 1, 64));
+  const int64_t B1 = std::max<int64_t>(std::max((int64_t)chunk * slots, std::min(chunk, sub) * full_slots), 1);
   void *ws = nullptr;
   PhotonRec *d_dir = nullptr, *d_ind = nullptr, *d_cau = nullptr;
   int *d_tot = nullptr;
   cudaStream_t st = nullptr;
   e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&ws, skw::photon_chunk_bytes(chunk, params->max_bounces));
+  const size_t wsb = std::max(skw::photon_chunk_bytes(chunk, slots), skw::photon_chunk_bytes(std::min(chunk, sub), full_slots));
+  if (e == cudaSuccess) e = cudaMalloc(&ws, wsb);
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_dir, (size_t)chunk * sizeof(PhotonRec));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&d_ind, (size_t)(chunk * B1) * sizeof(PhotonRec));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_ind, (size_t)B1 * sizeof(PhotonRec));
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_cau, (size_t)chunk * sizeof(PhotonRec));
-  if (e == cudaSuccess) e = cudaMalloc(&d_tot, 3 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&d_tot, 4 * sizeof(int));
+  A.overflow = d_tot + 3;
   auto *pm = new (std::nothrow) skw_photon_map();
   if (!pm) e = cudaErrorMemoryAllocation;
   int64_t launches = 0;
-  for (int64_t p0 = 0; p0 < params->paths && e == cudaSuccess; p0 += chunk) {
-    const int n = (int)std::min(chunk, params->paths - p0);
-    e = skw::photon_shoot_chunk(S, A, trace, p0, n, ws, d_dir, d_ind, d_cau, d_tot, st);
-    int tot[3] = {0, 0, 0};
-    if (e == cudaSuccess) e = cudaMemcpyAsync(tot, d_tot, sizeof(tot), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) break;
+  // One chunk [p0, p0 + n) with the given slots; its photons appended to the
+  // maps unless a path overflowed its slots (*overflowed set, nothing kept).
+  auto shoot = [&](int64_t p0, int n, int sl, bool *overflowed) -> cudaError_t {
+    skw::PhotonShootArgs a = A;
+    a.slots = sl;
+    cudaError_t r = cudaMemsetAsync(d_tot + 3, 0, sizeof(int), st);
+    if (r == cudaSuccess) r = skw::photon_shoot_chunk(S, a, trace, p0, n, ws, d_dir, d_ind, d_cau, d_tot, st);
+    int tot[4] = {0, 0, 0, 0};
+    if (r == cudaSuccess) r = cudaMemcpyAsync(tot, d_tot, sizeof(tot), cudaMemcpyDeviceToHost, st);
+    if (r == cudaSuccess) r = cudaStreamSynchronize(st);
+    if (r != cudaSuccess) return r;
+    launches += 1 + 2 * params->max_bounces + 9;
+    *overflowed = tot[3] != 0;
+    if (*overflowed) return cudaSuccess;
     Map &cm = pm->maps[0], &dm = pm->maps[1], &im = pm->maps[2];
     const size_t oc = cm.input.size(), od = dm.input.size(), oi = im.input.size();
     cm.input.resize(oc + (size_t)tot[2]);
     dm.input.resize(od + (size_t)tot[0]);
     im.input.resize(oi + (size_t)tot[1]);
-    if (tot[0] > 0) e = cudaMemcpy(dm.input.data() + od, d_dir, (size_t)tot[0] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && tot[1] > 0)
-      e = cudaMemcpy(im.input.data() + oi, d_ind, (size_t)tot[1] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && tot[2] > 0)
-      e = cudaMemcpy(cm.input.data() + oc, d_cau, (size_t)tot[2] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
+    if (tot[0] > 0) r = cudaMemcpy(dm.input.data() + od, d_dir, (size_t)tot[0] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
+    if (r == cudaSuccess && tot[1] > 0)
+      r = cudaMemcpy(im.input.data() + oi, d_ind, (size_t)tot[1] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
+    if (r == cudaSuccess && tot[2] > 0)
+      r = cudaMemcpy(cm.input.data() + oc, d_cau, (size_t)tot[2] * sizeof(PhotonRec), cudaMemcpyDeviceToHost);
     cm.paths += n;
     dm.paths += n;
     im.paths += n;
-    launches += 1 + 2 * params->max_bounces + 9;
+    return r;
+  };
+  for (int64_t p0 = 0; p0 < params->paths && e == cudaSuccess; p0 += chunk) {
+    const int n = (int)std::min(chunk, params->paths - p0);
+    bool over = false;
+    e = shoot(p0, n, slots, &over);
+    // a path deposited more than `slots` indirect photons: the chunk again,
+    // in sub-chunks with a slot for every bounce
+    for (int64_t q0 = p0; over && e == cudaSuccess && q0 < p0 + n; q0 += sub) {
+      bool again = false;
+      e = shoot(q0, (int)std::min<int64_t>(sub, p0 + n - q0), full_slots, &again);
+    }
   }
   cudaFree(ws);
   cudaFree(d_dir);
@@ -463,6 +522,9 @@ int skw_photon_map_get_info(const skw_photon_map *pm, skw_photon_map_info *out) 
   out->scene_area = pm->scene_area;
   out->shoot_ms = pm->shoot_ms;
   out->build_ms = pm->build_ms;
+  out->trees_on_gpu = 0;
+  for (int i = 0; i < 3; ++i)
+    if (pm->maps[i].built_on_gpu) out->trees_on_gpu |= 1 << i;
   return SKW_OK;
 }
 

@@ -45,6 +45,20 @@ def build_host(positions: np.ndarray, threads: int = 0):
     return perm, nodes
 
 
+def build_device(positions: np.ndarray, ctx: Context | None = None):
+    """The GPU build: (perm int32 (n,), node_words uint32 (n, 2), median_tie
+    bool); equal to build_host's outputs unless median_tie."""
+    ctx = ctx or default_context()
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    perm = np.empty(n, np.int32)
+    nodes = np.empty((n, 2), np.uint32)
+    tie = C.c_int32()
+    _lib.check(_lib.load().skw_kdtree_build_device(ctx.handle, pos.ctypes.data, n, perm.ctypes.data,
+                                                    nodes.ctypes.data, C.byref(tie)), ctx.handle)
+    return perm, nodes, bool(tie.value)
+
+
 class PhotonKDTree:
     def __init__(self, positions: np.ndarray, normal_ids: np.ndarray | None = None, ctx: Context | None = None):
         self.ctx = ctx or default_context()

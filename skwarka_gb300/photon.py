@@ -26,7 +26,7 @@ class skw_photon_map_info(C.Structure):
     _fields_ = [("n_caustic", C.c_int64), ("n_direct", C.c_int64), ("n_indirect", C.c_int64),
                 ("n_irradiance", C.c_int64), ("paths_caustic", C.c_int64), ("paths_direct", C.c_int64),
                 ("paths_indirect", C.c_int64), ("max_irradiance_lookup_dist", C.c_double), ("scene_area", C.c_double),
-                ("shoot_ms", C.c_double), ("build_ms", C.c_double)]
+                ("shoot_ms", C.c_double), ("build_ms", C.c_double), ("trees_on_gpu", C.c_int32)]
 
 
 class PhotonMap:
