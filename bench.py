@@ -10,8 +10,10 @@ inputs with the shapes of the ray-query microbenchmark configuration.
                256 MiB write) before every timed step, CUDA events on the
                launching stream.
 * e2e        : the same metric through the C ABI host-buffer entry point
-               (skw_intersect_host): pinned host rays in, hits out, copies
-               inside the timed region.
+               (skw_intersect_host): pinned host rays in, hits out, the
+               transfers inside the timed region (on a coherent CPU-GPU
+               link the traversal reads the rays from and writes the hits
+               to the pinned host buffers itself).
 * roofline   : algorithmic bytes per launch (32 + 16 + 32*N_nodes +
                36*N_tris per ray, N from the instrumented oracle on a sample
                of the same rays) / kernel time, against the measured HBM
@@ -158,6 +160,15 @@ def load_traffic(kind: str, rays: int):
     if not d:
         return None
     return d.get("dram_bytes_per_launch", 0.0) + d["dram_bytes_per_ray"] * rays
+
+
+def host_transfer_mode(ctx) -> str:
+    """How skw_intersect_host moves pinned host buffers on this device."""
+    from skwarka_gb300 import _lib
+    if _lib.load().skw_ctx_host_buffers_in_place(ctx.handle) == 1:
+        return ("in place: the traversal reads the rays from and writes the hits to the pinned host buffers over "
+                "the coherent CPU-GPU link")
+    return "staged: 2M-ray chunks copied in and out on two streams, overlapped with the traversals"
 
 
 def load_l2(kind: str, rays: int, seconds: float):
@@ -936,7 +947,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": sum(kern_ms) / len(kern_ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config(args, world),
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": args.rays * 32,
+            "e2e": {"value": e2e, "unit": UNIT, "transfer": host_transfer_mode(ctx),
+                    "h2d_bytes_per_step": args.rays * 32,
                     "d2h_bytes_per_step": args.rays * 16},
             "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "clocks": clk.summary(), "gpu_launches": launches,
             "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit, "render": render, "specular": specular, "batch": batch, "adjoint": adjoint, "photon": photon,

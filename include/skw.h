@@ -182,8 +182,12 @@ int skw_intersect(skw_accel *accel, const skw_ray *rays, int64_t n, skw_hit *hit
  * (Raytracer/Core/TriangleAccelerator.cpp:354-468, Scene.h:140-148). */
 int skw_intersect_test(skw_accel *accel, const skw_ray *rays, int64_t n, uint8_t *occluded, void *stream);
 
-/* Same as above with host buffers (pinned or pageable): copies rays in,
- * runs, copies results out, and waits for completion. */
+/* Same as above with host buffers (pinned or pageable), waiting for
+ * completion.  Page-locked buffers (cudaHostAlloc, cudaHostRegister) on a
+ * device with a coherent link to the host (NVLink-C2C:
+ * skw_ctx_host_buffers_in_place) are read and written in place by the
+ * traversal; otherwise the rays are copied in and the results out in 2M-ray
+ * chunks on two streams, overlapped with the traversals. */
 int skw_intersect_host(skw_accel *accel, const skw_ray *rays, int64_t n, skw_hit *hits);
 int skw_intersect_test_host(skw_accel *accel, const skw_ray *rays, int64_t n, uint8_t *occluded);
 
@@ -220,6 +224,10 @@ int skw_intersect_test_d_host(skw_accel *accel, const skw_ray_d *rays, int64_t n
 
 /* Kernel launches made by this library since the context was created. */
 int64_t skw_launch_count(const skw_ctx *ctx);
+/* 1 when the context's device reaches host memory over a coherent link
+ * (native atomics across it, as NVLink-C2C on a Grace system): the
+ * host-buffer queries then work on page-locked buffers in place; else 0. */
+int skw_ctx_host_buffers_in_place(const skw_ctx *ctx);
 
 /* ---------------------------------------------------- photon kd-tree -- */
 

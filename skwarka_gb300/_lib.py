@@ -48,6 +48,7 @@ SIGNATURES = [
     ("skw_ctx_destroy", None, [_P]),
     ("skw_last_error", C.c_char_p, [_P]),
     ("skw_launch_count", C.c_int64, [_P]),
+    ("skw_ctx_host_buffers_in_place", C.c_int, [_P]),
     ("skw_flat_tree_build", C.c_int, [C.POINTER(skw_mesh), C.c_int32, C.POINTER(skw_primitive), C.c_int32, C.c_int,
                                       C.POINTER(_P), C.c_char_p, C.c_size_t]),
     ("skw_flat_tree_destroy", None, [_P]),

@@ -89,6 +89,9 @@ const char *skw_last_error(const skw_ctx *ctx) { return ctx ? ctx->err.c_str() :
 
 int64_t skw_launch_count(const skw_ctx *ctx) { return ctx ? ctx->launches.load() : 0; }
 
+static bool coherent_host_link(int dev);
+int skw_ctx_host_buffers_in_place(const skw_ctx *ctx) { return ctx && coherent_host_link(ctx->device) ? 1 : 0; }
+
 struct skw_flat_tree {
   skw::FlatTree ft;
   double build_ms = 0.0;
@@ -341,12 +344,87 @@ int skw_intersect_test_d(skw_accel *a, const skw_ray_d *rays, int64_t n, uint8_t
 // end against 787 for one copy-in, query, copy-out sequence.
 static constexpr int64_t kHostChunk = (int64_t)1 << 21;
 
+// Whether the device reaches host memory over a coherent link (NVLink-C2C on
+// a Grace system: native atomics across the link), once per device.
+static bool coherent_host_link(int dev) {
+  static std::mutex mu;
+  static int known[64] = {0};  // 0 unknown, 1 no, 2 yes
+  if (dev < 0 || dev >= 64) return false;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!known[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrHostNativeAtomicSupported, dev) != cudaSuccess) {
+      cudaGetLastError();
+      v = 0;
+    }
+    known[dev] = v ? 2 : 1;
+  }
+  return known[dev] == 2;
+}
+
+// The device address of a page-locked host buffer (cudaHostAlloc /
+// cudaHostRegister), or null when the buffer is not one.
+static void *mapped_host(const void *p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+// Status check after a host-buffer query.
+static int query_status(skw_accel *a) {
+  unsigned sv = 0;
+  cudaError_t e = cudaMemcpy(&sv, a->d_status, sizeof(sv), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(a->ctx, e, "status read");
+  if (sv & 1u) {
+    cudaMemset(a->d_status, 0, sizeof(unsigned));
+    return fail(a->ctx, SKW_ERR_STACK_OVERFLOW, "traversal stack overflow");
+  }
+  return SKW_OK;
+}
+
 static int run_query_host(skw_accel *a, bool closest, bool dray, const void *rays, int64_t n, void *out) {
   if (!a) return SKW_ERR_ARG;
   if (n < 0 || (n > 0 && (!rays || !out))) return fail(a->ctx, SKW_ERR_ARG, "bad ray buffer");
   if (n == 0) return SKW_OK;
   cudaError_t e = cudaSetDevice(a->ctx->device);
   if (e != cudaSuccess) return cuda_fail(a->ctx, e, "cudaSetDevice");
+  // Page-locked host buffers on a coherent CPU-GPU link: the traversal reads
+  // the rays from host memory and writes the results there itself, so the
+  // transfers run inside the kernel, overlapped with its work, with no
+  // staging buffers and no separate copies.
+  void *hr = nullptr, *ho = nullptr;
+  if (coherent_host_link(a->ctx->device) && (hr = mapped_host(rays)) != nullptr && (ho = mapped_host(out)) != nullptr) {
+    skw_ctx *c = a->ctx;
+    if (!c->host_st[0] && (e = cudaStreamCreateWithFlags(&c->host_st[0], cudaStreamNonBlocking)) != cudaSuccess)
+      return cuda_fail(c, e, "stream");
+    cudaStream_t s = c->host_st[0];
+    cudaMemPool_t pool;
+    if ((e = skw::ctx_pool(c, &pool)) != cudaSuccess) return cuda_fail(c, e, "workspace pool");
+    int *d_work = nullptr;
+    if ((e = cudaMallocFromPoolAsync((void **)&d_work, 256, pool, s)) != cudaSuccess)
+      return cuda_fail(c, e, "cudaMallocAsync");
+    const size_t ru = dray ? sizeof(skw_ray_d) : sizeof(skw_ray);
+    const size_t ou = closest ? (dray ? sizeof(skw_hit_d) : sizeof(skw_hit)) : 1;
+    const int64_t per = (int64_t)1 << 30;  // rays per launch (the kernels index rays with 32-bit ints)
+    for (int64_t r0 = 0; r0 < n && e == cudaSuccess; r0 += per) {
+      const int64_t m = std::min(per, n - r0);
+      const char *rr = (const char *)hr + (size_t)r0 * ru;
+      char *oo = (char *)ho + (size_t)r0 * ou;
+      e = dray ? skw::launch_traversal_d(closest, a->stack_cap, a->d_nodes, a->d_tris, rr, m, a->scene_abs, oo,
+                                         a->d_status, s, d_work)
+               : skw::launch_traversal(closest, a->stack_cap, a->d_nodes, a->d_tris, rr, m, nullptr, a->scene_abs,
+                                       nullptr, oo, a->d_status, s, 0, d_work);
+    }
+    cudaFreeAsync(d_work, s);
+    cudaError_t es = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "launch");
+    if (es != cudaSuccess) return cuda_fail(c, es, "query execution");
+    c->launches.fetch_add(1);
+    return query_status(a);
+  }
   const size_t out_unit = closest ? (dray ? sizeof(skw_hit_d) : sizeof(skw_hit)) : 1;
   const size_t ray_unit = dray ? sizeof(skw_ray_d) : sizeof(skw_ray);
   const int64_t n_chunks = (n + kHostChunk - 1) / kHostChunk;
@@ -416,15 +494,7 @@ static int run_query_host(skw_accel *a, bool closest, bool dray, const void *ray
       if (rc == SKW_OK && e != cudaSuccess) rc = cuda_fail(a->ctx, e, "query execution");
     }
   }
-  if (rc == SKW_OK) {
-    unsigned sv = 0;
-    if ((e = cudaMemcpy(&sv, a->d_status, sizeof(sv), cudaMemcpyDeviceToHost)) != cudaSuccess)
-      return cuda_fail(a->ctx, e, "status read");
-    if (sv & 1u) {
-      cudaMemset(a->d_status, 0, sizeof(unsigned));
-      return fail(a->ctx, SKW_ERR_STACK_OVERFLOW, "traversal stack overflow");
-    }
-  }
+  if (rc == SKW_OK) return query_status(a);
   return rc;
 }
 
