@@ -27,6 +27,9 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include"), "-I", str(CSRC)]
+# Extra device-compiler flags, e.g. the kernels' tuning macros
+# (SKW_KNN_BLOCK, SKW_TRAV_SCAP, ...) for a sweep; a change rebuilds every unit.
+NVCC_FLAGS += os.environ.get("SKW_NVCC_EXTRA", "").split()
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-Wall", "-Wno-unused-function",
              "-I", str(ROOT / "include"), "-I", str(CSRC), "-I", str(CUDA_HOME / "include")]
 

@@ -108,7 +108,8 @@ struct Builder {
   std::vector<float> tv;      // 9 floats per triangle (world space)
   std::vector<int32_t> prim;  // primitive index per triangle
   std::vector<int32_t> tidx;  // mesh triangle index per triangle
-  std::vector<BoxF> tbox;     // per-triangle AABB
+  std::vector<BoxF> tbox;     // per-triangle AABB, in the build's current order
+  std::vector<uint32_t> order;  // the triangle (index into tv, prim, tidx) in each slot
   // Instances of shared meshes (TriangleAccelerator.cpp:54-102): world box
   // of the instance, triangles of its mesh's subtree (the split search's
   // weight), its primitive and the subtree it instances.
@@ -121,10 +122,11 @@ struct Builder {
   std::atomic<int32_t> max_depth{0};
   std::atomic<int64_t> n_leaves{0};
 
+  // The partition's swaps move the box the split search reads and the
+  // slot's triangle index; the triangles themselves are gathered in the
+  // final order once, when the tree is flattened.
   void swap_tris(size_t a, size_t b) {
-    for (int k = 0; k < 9; ++k) std::swap(tv[9 * a + k], tv[9 * b + k]);
-    std::swap(prim[a], prim[b]);
-    std::swap(tidx[a], tidx[b]);
+    std::swap(order[a], order[b]);
     std::swap(tbox[a], tbox[b]);
   }
   // _SwapInstances (TriangleAccelerator.cpp:495-503)
@@ -142,6 +144,13 @@ struct Builder {
   struct Buckets {
     BoxD L[kMaxSplitTries], M[kMaxSplitTries], R[kMaxSplitTries];
     size_t Ln[kMaxSplitTries] = {0}, Mn[kMaxSplitTries] = {0}, Rn[kMaxSplitTries] = {0};
+    // Empties the first `tries` candidates (the only ones a node uses).
+    void reset(size_t tries) {
+      for (size_t i = 0; i < tries; ++i) {
+        L[i] = M[i] = R[i] = BoxD();
+        Ln[i] = Mn[i] = Rn[i] = 0;
+      }
+    }
     void merge(const Buckets &o, size_t tries) {
       for (size_t i = 0; i < tries; ++i) {
         L[i].unite(o.L[i]);
@@ -247,9 +256,11 @@ struct Builder {
         score(axis, k);
       }
     } else {
+      // one bucket set per thread, emptied over the node's own candidates
+      static thread_local Buckets k;
       for (int axis = 0; axis < 3; ++axis) {
         if (mask & (1u << axis)) continue;
-        Buckets k;
+        k.reset(tries);
         fill_buckets(nb, axis, tb, te, tries, coefs[axis], k);
         fill_inst_buckets(nb, axis, ib, ie, tries, coefs[axis], k);
         score(axis, k);
@@ -330,10 +341,16 @@ struct Builder {
     bool spawned[3] = {false, false, false};
     for (int c = 0; c < 3; ++c) {
       if (ranges[c].b >= ranges[c].e && ranges[c].ib >= ranges[c].ie) continue;
-      if (ranges[c].e - ranges[c].b > 20000 && threads_left.fetch_sub(1) > 0) {
+      bool spawn = false;
+      if (ranges[c].e - ranges[c].b > 20000) {
+        spawn = threads_left.fetch_sub(1) > 0;
+        if (!spawn) threads_left.fetch_add(1);
+      }
+      if (spawn) {
         spawned[c] = true;
         workers[c] = std::thread([this, node_ptr = node.get(), c, r = ranges[c], depth]() {
           node_ptr->child[c] = build(r.b, r.e, r.ib, r.ie, r.m, depth + 1);
+          threads_left.fetch_add(1);  // the thread goes back to the budget
         });
       } else {
         node->child[c] = build(ranges[c].b, ranges[c].e, ranges[c].ib, ranges[c].ie, ranges[c].m, depth + 1);
@@ -452,6 +469,7 @@ void add_mesh_triangles(Builder &B, const MeshIn &m, const double *xf, int32_t p
     B.prim.push_back(prim);
     B.tidx.push_back(kept++);
     B.tbox.push_back(b);
+    B.order.push_back((uint32_t)B.order.size());
   }
 }
 
@@ -584,11 +602,12 @@ std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *pr
   out.tris.resize(n);
   for (size_t i = 0; i < n; ++i) {
     DevTri &t = out.tris[i];
-    std::memcpy(t.v0, &B.tv[9 * i], 12);
-    std::memcpy(t.v1, &B.tv[9 * i + 3], 12);
-    std::memcpy(t.v2, &B.tv[9 * i + 6], 12);
-    t.prim = B.prim[i];
-    t.tri = B.tidx[i];
+    const size_t o = B.order[i];
+    std::memcpy(t.v0, &B.tv[9 * o], 12);
+    std::memcpy(t.v1, &B.tv[9 * o + 3], 12);
+    std::memcpy(t.v2, &B.tv[9 * o + 6], 12);
+    t.prim = B.prim[o];
+    t.tri = B.tidx[o];
     t.slot = (int32_t)i;
   }
   out.inst.resize(n_inst);
