@@ -59,8 +59,8 @@ cudaError_t launch_traversal_d(bool closest, int stack_cap, const void *nodes, c
 // per query (qn may be null when cos_t < 0, which disables the filter).
 // Outputs per query: k slots of tree positions and squared distances in the
 // reference's heap order (-1 / 0 when unused) and the found count;
-// out_visited (optional) counts visited nodes.  k > 128 needs a scratch
-// buffer of knn_scratch_bytes(nq, k) bytes.  status bit 1: stack overflow.
+// out_visited (optional) counts visited nodes.  A non-zero knn_scratch_bytes(nq, k) (k > 128) means a scratch buffer of that
+// many bytes is required.  status bit 1: stack overflow.
 size_t knn_scratch_bytes(int64_t nq, int k);
 cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                        const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,

@@ -50,15 +50,28 @@ static __device__ __align__(256) unsigned char g_knn_noalloc_scratch[(size_t)SKW
 namespace skw {
 namespace {
 
-// Walk stack entries per thread: the median-split tree of n < 2^31 points
-// is at most 31 levels deep and the walk holds at most one entry per level.
-constexpr int kStack = 32;
-constexpr int kKnnBlock = 128;  // threads per block of the lookup kernels
-// minimum resident blocks per SM of k_knn (bounds its registers at 64;
-// measured on the k = 100 photon lookups: 1 (72 registers) 57 ms, 8 50.5 ms,
-// 10 (48 registers) 58.5 ms, 12 61 ms)
+// One warp per block: a block's slot frees as soon as its warp's slowest
+// query ends (queries differ widely in cost), and small blocks let the
+// walk stack's shared memory be sized to fit, leaving the rest of the SM's
+// storage to L1 (measured on the k = 100 photon lookups, 2,971,920 queries:
+// 128 threads 34.3 ms, 32 threads 32.7 ms).
+#ifndef SKW_KNN_BLOCK
+#define SKW_KNN_BLOCK 32
+#endif
+constexpr int kKnnBlock = SKW_KNN_BLOCK;  // threads per block of the lookup kernels
+// Load the near child's node as soon as the node word is read, so that the
+// load overlaps the node's own distance, filter and heap work (off: at one
+// warp per block it measured slower, 42.4 against 32.7 ms, at 128 threads
+// the same).
+#ifndef SKW_KNN_EARLY
+#define SKW_KNN_EARLY 0
+#endif
+constexpr bool kEarlyLoad = SKW_KNN_EARLY != 0;
+// minimum resident blocks per SM of k_knn: 32 one-warp blocks bound its
+// registers at 64 (with 128-thread blocks, measured on the k = 100 photon
+// lookups: 72 registers 57 ms, 64 50.5 ms, 48 58.5 ms)
 #ifndef SKW_KNN_MINB
-#define SKW_KNN_MINB 8
+#define SKW_KNN_MINB (1024 / SKW_KNN_BLOCK)
 #endif
 
 
@@ -158,16 +171,57 @@ __device__ __forceinline__ double point_d2(const float4 p, const Query &Q) {
 }
 
 // Float pre-tests.  A point's squared distance and a splitting plane's
-// squared distance are first computed in float with a bound E on their
-// distance from the reference's double values (the float query rounding eq,
-// the rounding of each float difference and square, and the double
-// result's own rounding); only when the float value lies within E of the
-// current radius is the exact double value computed.  u = 2^-24.
-__device__ __forceinline__ void sq_bound(float d, float eq, float &sq, float &err) {
-  const float a = fabsf(d);
-  const float ex = a * 5.9604645e-8f + eq;  // |exact difference - d|
-  sq = d * d;
-  err = (2.0f * a + ex) * ex;
+// squared distance are first computed in float and compared with two
+// thresholds derived from the current radius and a bound on the float
+// value's distance from the reference's double value; only a value between
+// the thresholds is decided in double.
+// The float squared distance of a point from the float query, and a bound
+// E(F) on its distance from the reference's double value, as a function of
+// the float value F: with u = 2^-24, each float difference d within u|d| +
+// eq of the exact one, its square, the fused sum's three roundings and the
+// double result's own rounding give
+//   |F - d2| <= 5u D + 2 eq sum|d| + 3 eq^2 (+ 2^-52 D),  D = sum d^2 <= F (1 + 3u),
+// and sum|d| <= sqrt(3 D):  E(F) = 3.0e-7 F + 3.47 eq sqrt(F) + 3.01 eq^2,
+// plus 1e-37 for roundings in the subnormal range.  A plane's squared
+// distance (one axis, one rounding fewer) is within the same bound.
+__device__ __forceinline__ float dist2f(const float4 p, const Query &Q) {
+  const float dx = p.x - Q.qf[0], dy = p.y - Q.qf[1], dz = p.z - Q.qf[2];
+  return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+}
+__device__ __forceinline__ float d2_err(const Query &Q, float x) {
+  // 1.0001: the roundings of this float evaluation (about 6u)
+  return (3.0e-7f * x + 3.47f * Q.eq * __fsqrt_ru(x) + 3.01f * Q.eq * Q.eq + 1e-37f) * 1.0001f;
+}
+// Thresholds on a float squared distance F against a radius known to lie
+// in [rlo, rhi]: F < tin => inside, F >= tout => outside (else decide in
+// double).  tin = rlo - E(rlo): for F < tin, F + E(F) < rlo because E grows
+// with F.  tout = rhi + E(2 rhi): for F in [tout, 2 rhi], F - E(F) >= rhi;
+// above 2 rhi, E(F) <= F / 2 <= F - rhi once sqrt(rhi) >= 8 eq; below that
+// (or for an infinite radius) nothing is decided outside in float.
+__device__ __forceinline__ void radius_thresholds(const Query &Q, float rlo, float rhi, float &tin, float &tout) {
+  tin = isinf(rlo) ? rlo : (rlo > 0.0f ? __fsub_rd(rlo, d2_err(Q, rlo)) : -1.0f);
+  const float two = 2.0f * rhi;
+  tout = (!isinf(two) && rhi >= fmaxf(64.0f * Q.eq * Q.eq, 1e-36f)) ? __fadd_ru(rhi, d2_err(Q, two)) : INFINITY;
+}
+
+// A node's children in the reference's visit order: near = the child on the
+// query's side of the split (visited next), far = the other (postponed and
+// visited only if its plane is within the radius when it is popped); -1
+// where a child is absent or the node is a leaf.
+__device__ __forceinline__ void node_children(const float4 p, int cur, int n, const Query &Q, int &near, int &far,
+                                              uint32_t &axis, float &split) {
+  const uint32_t w = __float_as_uint(p.w);
+  near = far = -1;
+  axis = w & 3u;
+  split = 0.0f;
+  if (axis == 3u) return;
+  split = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
+  const uint32_t right = w >> 3;
+  const bool has_left = (w & 4u) != 0u, has_right = right < (uint32_t)n;
+  const bool le = q_le_split(Q, axis, split);
+  const int l = has_left ? cur + 1 : -1, r = has_right ? (int)right : -1;
+  near = le ? l : r;
+  far = le ? r : l;
 }
 
 // Walks the tree in the reference's order, calling visit(ni, p, d2, maxd2)
@@ -177,82 +231,85 @@ __device__ __forceinline__ void sq_bound(float d, float eq, float &sq, float &er
 // needed for the heap order, and the caller computes it later, many at a
 // time (the exact distance is a chain of dependent double operations, slow
 // on this GPU's FP64 pipe when done one point after another).  Returns
-// nodes visited (for statistics) or -1 on stack overflow.  The stack lives
-// in shared memory ([entry][thread], so lanes never share a bank) and holds
-// only the parent of each postponed far child: on pop the parent is read
-// again (a recently visited node, usually still in L1) and its split gives
-// both the far child and the plane distance to re-test.
-template <class Visit>
+// nodes visited (for statistics) or -1 on stack overflow.
+//
+// The stack lives in shared memory ([entry][thread], so lanes never share a
+// bank) and holds only the parent of each postponed far child: on pop the
+// parent is read again (a recently visited node, usually still in L1) and
+// its split gives both the far child and the plane distance to re-test.
+// Shared memory and L1 share the SM's storage, and the walk's node and heap
+// reads want the L1, so the stack is sized by the tree's depth: the
+// median-split tree of n points is floor(log2 n) + 1 levels deep and the
+// walk holds at most one entry per level, so S = 20 serves n < 2^20 and
+// S = 32 any n < 2^31.
+template <int S, class Visit>
 __device__ __forceinline__ int walk(const float4 *__restrict__ nodes, int n, const Query &Q, double &maxd2,
                                     uint32_t (*stk)[kKnnBlock], Visit &&visit) {
   if (n <= 0) return 0;
   int sp = 0, visited = 0;
   int cur = 0;
-  // maxd2 in float, rounded down (a float below it is below maxd2 too)
+  // maxd2 in float, rounded down / up (a float below the lower one is below
+  // maxd2, one at or above the upper one is not)
   auto lo_f = [](double m) { return __double2float_rd(m); };
   auto hi_f = [](double m) { return __double2float_ru(m); };
-  float mlo = lo_f(maxd2), mhi = hi_f(maxd2);
+  float tin, tout;
+  radius_thresholds(Q, lo_f(maxd2), hi_f(maxd2), tin, tout);
+  float4 p = __ldg(nodes);
   for (;;) {
-    const float4 p = __ldg(nodes + cur);
     ++visited;
+    int near, far;
+    uint32_t axis;
+    float split;
+    node_children(p, cur, n, Q, near, far, axis, split);
+    float4 pn = p;
+    if (kEarlyLoad && near >= 0) pn = __ldg(nodes + near);  // overlaps this node's work
     {
-      float sx, ex, sy, ey, sz, ez;
-      sq_bound(p.x - Q.qf[0], Q.eq, sx, ex);
-      sq_bound(p.y - Q.qf[1], Q.eq, sy, ey);
-      sq_bound(p.z - Q.qf[2], Q.eq, sz, ez);
-      const float d2f = (sx + sy) + sz;
-      const float E = (ex + ey + ez) * 1.0001f + d2f * 4.0e-7f + 1e-37f;
-      if (d2f + E < mlo) {  // certainly inside
-        if (visit(cur, p, -1.0, maxd2)) {
-          mlo = lo_f(maxd2);
-          mhi = hi_f(maxd2);
-        }
-      } else if (!(d2f - E >= mhi)) {  // not certainly outside: decide exactly
+      const float d2f = dist2f(p, Q);
+      if (d2f < tin) {  // certainly inside
+        if (visit(cur, p, -1.0, maxd2)) radius_thresholds(Q, lo_f(maxd2), hi_f(maxd2), tin, tout);
+      } else if (!(d2f >= tout)) {  // not certainly outside: decide exactly
         const double d2 = point_d2(p, Q);
-        if (d2 < maxd2 && visit(cur, p, d2, maxd2)) {
-          mlo = lo_f(maxd2);
-          mhi = hi_f(maxd2);
-        }
+        if (d2 < maxd2 && visit(cur, p, d2, maxd2)) radius_thresholds(Q, lo_f(maxd2), hi_f(maxd2), tin, tout);
       }
     }
-    const uint32_t w = __float_as_uint(p.w);
+    if (far >= 0) {  // the far child waits on the stack
+      if (sp >= S) return -1;
+      stk[sp][threadIdx.x] = (uint32_t)cur;
+      ++sp;
+    }
+    if (near >= 0) {
+      cur = near;
+      p = kEarlyLoad ? pn : __ldg(nodes + near);
+      continue;
+    }
     int next = -1;
-    if ((w & 3u) != 3u) {
-      const uint32_t axis = w & 3u;
-      const float split = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
-      const uint32_t right = w >> 3;
-      const bool has_left = (w & 4u) != 0u, has_right = right < (uint32_t)n;
-      const bool le = q_le_split(Q, axis, split);
-      next = le ? (has_left ? cur + 1 : -1) : (has_right ? (int)right : -1);
-      if (le ? has_right : has_left) {  // the far child waits on the stack
-        if (sp >= kStack) return -1;
-        stk[sp][threadIdx.x] = (uint32_t)cur;
-        ++sp;
-      }
-    }
-    while (next < 0 && sp > 0) {
+    while (sp > 0) {
       --sp;
-      const uint32_t par = stk[sp][threadIdx.x];
-      const float4 pp = __ldg(nodes + par);
-      const uint32_t pw = __float_as_uint(pp.w), ax = pw & 3u;
-      const float split = ax == 0 ? pp.x : (ax == 1 ? pp.y : pp.z);
       // the reference's pop test: (qa - split)^2 < maxd2, in double
-      float s2, e2;
-      sq_bound(qf_at(Q, ax) - split, Q.eq, s2, e2);
-      const float E = e2 * 1.0001f + s2 * 4.0e-7f + 1e-37f;
+      const uint32_t par = stk[sp][threadIdx.x];
+      int pnear, pfar;
+      uint32_t ax;
+      float ps;
+      const float4 pp = __ldg(nodes + par);
+      node_children(pp, (int)par, n, Q, pnear, pfar, ax, ps);
+      const float sd = qf_at(Q, ax) - ps, s2 = sd * sd;
       bool take;
-      if (s2 + E < mlo) {
+      if (s2 < tin) {
         take = true;
-      } else if (s2 - E >= mhi) {
+      } else if (s2 >= tout) {
         take = false;
       } else {
-        const double pd = __dsub_rn(q_at(Q, ax), (double)split);
+        const double pd = __dsub_rn(q_at(Q, ax), (double)ps);
         take = __dmul_rn(pd, pd) < maxd2;
       }
-      if (take) next = q_le_split(Q, ax, split) ? (int)(pw >> 3) : (int)par + 1;
+      if (take) {
+        next = pfar;
+        break;
+      }
     }
     if (next < 0) return visited;
     cur = next;
+    p = __ldg(nodes + cur);
   }
 }
 
@@ -277,11 +334,13 @@ struct FCand {
   int32_t idx;
 };
 
-// Bound on |key - d2| for a point whose float squared distance is key: the
-// float query's rounding eq on each axis, the float differences and squares
-// (the terms of sq_bound summed: 2u d2 + 2 eq sum|d| + 3 eq^2 with
-// sum|d| <= sqrt(3 d2) and 2 sqrt(3 d2) <= 1 + 3 d2), the float sum and the
-// double result's rounding: ke0 + ke1 key (Query::ke0, ke1).
+// Entries per query of a global heap: k + 1 rounded up to even.
+__host__ __device__ __forceinline__ int64_t knn_heap_stride(int k) { return ((int64_t)k + 2) & ~(int64_t)1; }
+
+// Bound on |key - d2| for a point whose float squared distance is key
+// (dist2f): ke0 + ke1 key (Query::ke0, ke1) bounds the error derived
+// above, 5u D + 2 sqrt(3) eq sqrt(D) + 3 eq^2, the square-root term by
+// 2 sqrt(3) eq sqrt(key) <= 2 sqrt(1.001 eq * 3.003 eq key) <= 1.001 eq + 3.003 eq key.
 __device__ __forceinline__ float key_err(const Query &Q, float key) { return fmaf(Q.ke1, key, Q.ke0); }
 
 // (d2, idx) lexicographic on the exact distances, decided on the keys when
@@ -306,13 +365,24 @@ __device__ __forceinline__ void fheap_push_up(const float4 *__restrict__ nodes, 
   h[hole] = value;
 }
 
+// PAIR: h[1] is 16-byte aligned, so that the children 2j+1, 2j+2 of every
+// entry j share one 16-byte load.
+template <bool PAIR = false>
 __device__ __forceinline__ void fheap_adjust(const float4 *__restrict__ nodes, const Query &Q, FCand *h, int hole, int len, FCand value) {
   const int top = hole;
   int second = hole;
   while (second < (len - 1) / 2) {
     second = 2 * (second + 1);
-    if (fcand_less(nodes, Q, h[second], h[second - 1])) second--;
-    h[hole] = h[second];
+    if (PAIR) {
+      const uint4 two = *reinterpret_cast<const uint4 *>(h + second - 1);
+      const FCand a{__uint_as_float(two.x), (int32_t)two.y}, b{__uint_as_float(two.z), (int32_t)two.w};
+      const bool left = fcand_less(nodes, Q, b, a);
+      second -= left ? 1 : 0;
+      h[hole] = left ? a : b;
+    } else {
+      if (fcand_less(nodes, Q, h[second], h[second - 1])) second--;
+      h[hole] = h[second];
+    }
     hole = second;
   }
   if ((len & 1) == 0 && second == (len - 2) / 2) {
@@ -335,7 +405,7 @@ __device__ __forceinline__ void fheap_make(const float4 *__restrict__ nodes, con
 // query i is scratch[i * k ...].  Until the heap is full its entries are
 // the accepted points in visit order (the reference's array holds them
 // unordered); at k entries it becomes a heap.
-template <int KMAX>
+template <int KMAX, int S>
 __global__ void __launch_bounds__(kKnnBlock, SKW_KNN_MINB) k_knn(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
                                              const double *__restrict__ dirs, int n, const double *__restrict__ q,
                                              const double *__restrict__ qn, int64_t nq, int k, double max_dist,
@@ -343,7 +413,7 @@ __global__ void __launch_bounds__(kKnnBlock, SKW_KNN_MINB) k_knn(const float4 *_
                                              double *__restrict__ out_d2, int32_t *__restrict__ out_count,
                                              int32_t *__restrict__ out_visited, FCand *__restrict__ scratch,
                                              unsigned *__restrict__ status, const int *__restrict__ nq_dev) {
-  __shared__ uint32_t stk[kStack][kKnnBlock];
+  __shared__ uint32_t stk[S][kKnnBlock];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (nq_dev && *nq_dev < nq) nq = *nq_dev;
   if (i >= nq) return;
@@ -364,14 +434,17 @@ __global__ void __launch_bounds__(kKnnBlock, SKW_KNN_MINB) k_knn(const float4 *_
   }
   query_float(Q);
   FCand local_heap[KMAX > 0 ? KMAX : 1];
-  FCand *heap = KMAX > 0 ? local_heap : scratch + i * (int64_t)k;
+  // global heaps: query i's entries from scratch[i * stride + 1], stride even
+  // (16-byte aligned sibling pairs, fheap_adjust<true>)
+  FCand *heap = KMAX > 0 ? local_heap : scratch + i * (int64_t)knn_heap_stride(k) + 1;
   int size = 0, visited = 0;
   if (k > 0 && n > 0) {
     // the search radius: max_dist^2 (KDTree::Lookup, KDTree.h:475-482)
     // until the heap is full, then the top's exact squared distance
     double rex = __dmul_rn(max_dist, max_dist);
     bool rex_ok = true;
-    float rlo = __double2float_rd(rex), rhi = __double2float_ru(rex);
+    float rlo = __double2float_rd(rex), rhi = __double2float_ru(rex), tin, tout;
+    radius_thresholds(Q, rlo, rhi, tin, tout);
     auto radius = [&]() -> double {
       if (!rex_ok) {
         rex = point_d2(__ldg(nodes + heap[0].idx), Q);
@@ -384,23 +457,27 @@ __global__ void __launch_bounds__(kKnnBlock, SKW_KNN_MINB) k_knn(const float4 *_
       rlo = __fsub_rd(t, e);
       rhi = __fadd_ru(t, e);
       rex_ok = false;
+      radius_thresholds(Q, rlo, rhi, tin, tout);
     };
     int sp = 0, cur = 0;
     bool overflow = false;
+    float4 p = __ldg(nodes);
     for (;;) {
-      const float4 p = __ldg(nodes + cur);
       ++visited;
+      int near, far;
+      uint32_t axis;
+      float split;
+      node_children(p, cur, n, Q, near, far, axis, split);
+      // the near child is visited next: its node is loaded now, so that the
+      // load overlaps this node's work
+      float4 pn = p;
+      if (kEarlyLoad && near >= 0) pn = __ldg(nodes + near);
       {
-        float sx, ex, sy, ey, sz, ez;
-        sq_bound(p.x - Q.qf[0], Q.eq, sx, ex);
-        sq_bound(p.y - Q.qf[1], Q.eq, sy, ey);
-        sq_bound(p.z - Q.qf[2], Q.eq, sz, ez);
-        const float d2f = (sx + sy) + sz;
-        const float E = (ex + ey + ez) * 1.0001f + d2f * 4.0e-7f + 1e-37f;
+        const float d2f = dist2f(p, Q);
         bool inside;
-        if (d2f + E < rlo) {
+        if (d2f < tin) {
           inside = true;
-        } else if (d2f - E >= rhi) {
+        } else if (d2f >= tout) {
           inside = false;
         } else {
           inside = point_d2(p, Q) < radius();
@@ -417,54 +494,54 @@ __global__ void __launch_bounds__(kKnnBlock, SKW_KNN_MINB) k_knn(const float4 *_
             // pop_heap: the top goes to the back; the back's old value is re-placed
             const FCand back = heap[k - 1];
             heap[k - 1] = heap[0];
-            fheap_adjust(nodes, Q, heap, 0, k - 1, back);
+            fheap_adjust<KMAX == 0>(nodes, Q, heap, 0, k - 1, back);
             // the popped back slot takes the new point, pushed up
             fheap_push_up(nodes, Q, heap, k - 1, 0, c);
             new_top();
           }
         }
       }
-      const uint32_t w = __float_as_uint(p.w);
-      int next = -1;
-      if ((w & 3u) != 3u) {
-        const uint32_t axis = w & 3u;
-        const float split = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
-        const uint32_t right = w >> 3;
-        const bool has_left = (w & 4u) != 0u, has_right = right < (uint32_t)n;
-        const bool le = q_le_split(Q, axis, split);
-        next = le ? (has_left ? cur + 1 : -1) : (has_right ? (int)right : -1);
-        if (le ? has_right : has_left) {  // the far child waits on the stack
-          if (sp >= kStack) {
-            overflow = true;
-            break;
-          }
-          stk[sp][threadIdx.x] = (uint32_t)cur;
-          ++sp;
+      if (far >= 0) {  // the far child waits on the stack
+        if (sp >= S) {
+          overflow = true;
+          break;
         }
+        stk[sp][threadIdx.x] = (uint32_t)cur;
+        ++sp;
       }
-      while (next < 0 && sp > 0) {
+      if (near >= 0) {
+        cur = near;
+        p = kEarlyLoad ? pn : __ldg(nodes + near);
+        continue;
+      }
+      int next = -1;
+      while (sp > 0) {
         --sp;
-        const uint32_t par = stk[sp][threadIdx.x];
-        const float4 pp = __ldg(nodes + par);
-        const uint32_t pw = __float_as_uint(pp.w), ax = pw & 3u;
-        const float split = ax == 0 ? pp.x : (ax == 1 ? pp.y : pp.z);
         // the reference's pop test: (qa - split)^2 < radius, in double
-        float s2, e2;
-        sq_bound(qf_at(Q, ax) - split, Q.eq, s2, e2);
-        const float E = e2 * 1.0001f + s2 * 4.0e-7f + 1e-37f;
+        const uint32_t par = stk[sp][threadIdx.x];
+        int pnear, pfar;
+        uint32_t ax;
+        float ps;
+        const float4 pp = __ldg(nodes + par);
+        node_children(pp, (int)par, n, Q, pnear, pfar, ax, ps);
+        const float sd = qf_at(Q, ax) - ps, s2 = sd * sd;
         bool take;
-        if (s2 + E < rlo) {
+        if (s2 < tin) {
           take = true;
-        } else if (s2 - E >= rhi) {
+        } else if (s2 >= tout) {
           take = false;
         } else {
-          const double pd = __dsub_rn(q_at(Q, ax), (double)split);
+          const double pd = __dsub_rn(q_at(Q, ax), (double)ps);
           take = __dmul_rn(pd, pd) < radius();
         }
-        if (take) next = q_le_split(Q, ax, split) ? (int)(pw >> 3) : (int)par + 1;
+        if (take) {
+          next = pfar;
+          break;
+        }
       }
       if (next < 0) break;
       cur = next;
+      p = __ldg(nodes + cur);
     }
     if (overflow) atomicOr(status, 2u);
   }
@@ -497,13 +574,14 @@ __global__ void __launch_bounds__(kKnnBlock, SKW_KNN_MINB) k_knn(const float4 *_
 
 // GetNearestPoint (KDTree.h:495-503) with NearestPointProc (:293-323):
 // every accepted point becomes the nearest and shrinks the radius.
-__global__ void __launch_bounds__(kKnnBlock) k_nearest(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
+template <int S>
+__global__ void __launch_bounds__(kKnnBlock, SKW_KNN_MINB) k_nearest(const float4 *__restrict__ nodes, const uint16_t *__restrict__ nids,
                                                  const double *__restrict__ dirs, int n,
                                                  const double *__restrict__ q, const double *__restrict__ qn,
                                                  int64_t nq, double max_dist, double cos_t,
                                                  int32_t *__restrict__ out_idx, unsigned *__restrict__ status,
                                                  const int *__restrict__ nq_dev, const int32_t *__restrict__ order) {
-  __shared__ uint32_t stk[kStack][kKnnBlock];
+  __shared__ uint32_t stk[S][kKnnBlock];
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (nq_dev && *nq_dev < nq) nq = *nq_dev;
   if (i >= nq) return;
@@ -526,7 +604,7 @@ __global__ void __launch_bounds__(kKnnBlock) k_nearest(const float4 *__restrict_
   query_float(Q);
   double maxd2 = __dmul_rn(max_dist, max_dist);
   int best = -1;
-  const int v = walk(nodes, n, Q, maxd2, stk, [&](int ni, const float4 p, double d2, double &md2) -> bool {
+  const int v = walk<S>(nodes, n, Q, maxd2, stk, [&](int ni, const float4 p, double d2, double &md2) -> bool {
     if (Q.filter && !photon_filter(Q, p, __ldg(nids + ni), dirs)) return false;
     best = ni;
     md2 = d2 < 0.0 ? point_d2(p, Q) : d2;
@@ -536,9 +614,33 @@ __global__ void __launch_bounds__(kKnnBlock) k_nearest(const float4 *__restrict_
   out_idx[i] = best;
 }
 
+// Walk stack entries for a tree of n points (see walk).
+constexpr int kShallowStack = 20;
+inline bool shallow_tree(int n) { return n < (1 << kShallowStack); }
+
+// k_knn<KMAX, S> with S chosen by the tree's depth.
+template <int KMAX>
+void knn_kernel(unsigned grid, cudaStream_t stream, const float4 *nodes, const uint16_t *nids, const double *dirs,
+                int n, const double *q, const double *qn, int64_t nq, int k, double max_dist, double cos_t,
+                int32_t *out_idx, double *out_d2, int32_t *out_count, int32_t *out_visited, FCand *scratch,
+                unsigned *status, const int *nq_dev) {
+  if (shallow_tree(n))
+    k_knn<KMAX, kShallowStack><<<grid, kKnnBlock, 0, stream>>>(nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
+                                                               out_idx, out_d2, out_count, out_visited, scratch,
+                                                               status, nq_dev);
+  else
+    k_knn<KMAX, 32><<<grid, kKnnBlock, 0, stream>>>(nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx,
+                                                    out_d2, out_count, out_visited, scratch, status, nq_dev);
+}
+
 }  // namespace
 
-size_t knn_scratch_bytes(int64_t nq, int k) { return k > 128 ? (size_t)nq * (size_t)k * sizeof(FCand) : 0; }
+#ifndef SKW_KNN_GHEAP
+#define SKW_KNN_GHEAP 129  // smallest k whose heaps live in global scratch
+#endif
+size_t knn_scratch_bytes(int64_t nq, int k) {
+  return k >= SKW_KNN_GHEAP ? (size_t)nq * (size_t)knn_heap_stride(k) * sizeof(FCand) : 0;
+}
 
 cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                        const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,
@@ -547,15 +649,20 @@ cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *di
   if (nq <= 0) return cudaSuccess;
   const int block = kKnnBlock;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
-  if (k <= 32) {
-    k_knn<32><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
-                                           out_idx, out_d2, out_count, out_visited, nullptr, status, nq_dev);
+  const float4 *nd = (const float4 *)nodes;
+  if (scratch && k >= SKW_KNN_GHEAP) {
+    knn_kernel<0>(grid, stream, nd, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx, out_d2, out_count,
+                  out_visited, (FCand *)scratch, status, nq_dev);
+  } else if (k <= 32) {
+    knn_kernel<32>(grid, stream, nd, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx, out_d2, out_count,
+                   out_visited, nullptr, status, nq_dev);
   } else if (k <= 128) {
-    k_knn<128><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
-                                            out_idx, out_d2, out_count, out_visited, nullptr, status, nq_dev);
+    knn_kernel<128>(grid, stream, nd, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx, out_d2, out_count,
+                    out_visited, nullptr, status, nq_dev);
   } else {
-    k_knn<0><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
-                                          out_idx, out_d2, out_count, out_visited, (FCand *)scratch, status, nq_dev);
+    if (!scratch) return cudaErrorInvalidValue;
+    knn_kernel<0>(grid, stream, nd, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx, out_d2, out_count,
+                  out_visited, (FCand *)scratch, status, nq_dev);
   }
   return cudaGetLastError();
 }
@@ -621,8 +728,8 @@ cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const do
   // clearing between calls.
   const int block = kKnnBlock;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
-  k_knn<0><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
-                                        out_idx, out_d2, out_count, nullptr, (FCand *)scratch, status, nullptr);
+  knn_kernel<0>(grid, stream, (const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx, out_d2,
+                out_count, nullptr, (FCand *)scratch, status, nullptr);
   return cudaGetLastError();
 }
 
@@ -632,8 +739,12 @@ cudaError_t launch_nearest(const void *nodes, const uint16_t *nids, const double
   if (nq <= 0) return cudaSuccess;
   const int block = kKnnBlock;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
-  k_nearest<<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, max_dist, cos_t, out_idx,
-                                        status, nq_dev, order);
+  if (shallow_tree(n))
+    k_nearest<kShallowStack><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, max_dist,
+                                                         cos_t, out_idx, status, nq_dev, order);
+  else
+    k_nearest<32><<<grid, block, 0, stream>>>((const float4 *)nodes, nids, dirs, n, q, qn, nq, max_dist, cos_t,
+                                              out_idx, status, nq_dev, order);
   return cudaGetLastError();
 }
 
