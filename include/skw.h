@@ -107,8 +107,9 @@ typedef struct skw_accel_info {
   int32_t max_depth;   /* deepest node (root = 0) */
   int32_t stack_need;  /* traversal stack entries that suffice: 2*max_depth+1 */
   float bounds[6];     /* world bounds: min xyz, max xyz (GetWorldBounds) */
-  double build_ms;     /* host build time */
+  double build_ms;     /* build time (wall clock) */
   int64_t device_bytes;
+  int32_t built_on_device; /* 1: the tree was built on the GPU */
 } skw_accel_info;
 
 /* Host-only build of the ternary bbox kd-tree over all primitives (the same
@@ -126,6 +127,15 @@ typedef struct skw_flat_tree skw_flat_tree;
 int skw_flat_tree_build(const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims, int32_t n_prims,
                         int threads, skw_flat_tree **out, char *err, size_t errlen);
 void skw_flat_tree_destroy(skw_flat_tree *tree);
+/* skw_flat_tree_build with the tree built on the context's GPU: node for
+ * node the same tree (the split search's float and double arithmetic and
+ * the partition's element order reproduced exactly).  Accelerators with
+ * instancing, or of fewer than min_device_triangles triangles, are built on
+ * the host; *on_device (optional) is 1 when the GPU built it.  Errors are
+ * the context's (skw_last_error). */
+int skw_flat_tree_build_device(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims,
+                               int32_t n_prims, int64_t min_device_triangles, skw_flat_tree **out,
+                               int32_t *on_device);
 /* n_nodes, n_triangles, max_depth (root = 0) of a flat tree. */
 int skw_flat_tree_sizes(const skw_flat_tree *tree, int64_t *n_nodes, int64_t *n_triangles, int32_t *max_depth);
 /* Copies out nodes (8 x 32-bit words each, see skw_accel_export), triangle
@@ -152,7 +162,8 @@ int skw_flat_tree_leaf_ranges(const skw_flat_tree *tree, uint32_t leaf_word6, ui
  * TriangleAccelerator::TriangleAccelerator. */
 int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_accel **out);
 
-/* skw_flat_tree_build + skw_accel_create_from_flat. */
+/* skw_flat_tree_build_device (trees of 16,384 triangles or more on the GPU)
+ * + skw_accel_create_from_flat. */
 int skw_accel_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims,
                      int32_t n_prims, skw_accel **out);
 void skw_accel_destroy(skw_accel *accel);

@@ -37,7 +37,7 @@ class skw_primitive(C.Structure):
 class skw_accel_info(C.Structure):
     _fields_ = [("n_triangles", C.c_int64), ("n_nodes", C.c_int64), ("n_leaves", C.c_int64),
                 ("max_depth", C.c_int32), ("stack_need", C.c_int32), ("bounds", C.c_float * 6),
-                ("build_ms", C.c_double), ("device_bytes", C.c_int64)]
+                ("build_ms", C.c_double), ("device_bytes", C.c_int64), ("built_on_device", C.c_int32)]
 
 
 # (name, restype, argtypes) for every symbol include/skw.h declares.
@@ -51,6 +51,8 @@ SIGNATURES = [
     ("skw_ctx_host_buffers_in_place", C.c_int, [_P]),
     ("skw_flat_tree_build", C.c_int, [C.POINTER(skw_mesh), C.c_int32, C.POINTER(skw_primitive), C.c_int32, C.c_int,
                                       C.POINTER(_P), C.c_char_p, C.c_size_t]),
+    ("skw_flat_tree_build_device", C.c_int, [_P, C.POINTER(skw_mesh), C.c_int32, C.POINTER(skw_primitive), C.c_int32,
+                                             C.c_int64, C.POINTER(_P), C.POINTER(C.c_int32)]),
     ("skw_flat_tree_destroy", None, [_P]),
     ("skw_flat_tree_sizes", C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     ("skw_flat_tree_export", C.c_int, [_P, _P, _P, _P, _P]),

@@ -107,6 +107,7 @@ class TriangleAccelerator:
             "n_triangles": info.n_triangles, "n_nodes": info.n_nodes, "n_leaves": info.n_leaves,
             "max_depth": info.max_depth, "stack_need": info.stack_need, "bounds": list(info.bounds),
             "build_ms": info.build_ms, "device_bytes": info.device_bytes,
+            "built_on_device": bool(info.built_on_device),
         }
 
     def __del__(self):
@@ -213,10 +214,14 @@ def unpack_hits(hits) -> dict:
             "flags": hits[:, 3].view(np.uint32).copy()}
 
 
-def build_flat_tree(primitives: list[Primitive], threads: int = 0) -> dict:
-    """Host-only tree build (no GPU needed): the flattened device layout as
-    numpy arrays -- nodes uint32 (n, 8), tris float32 (n, 9), tri_prim,
-    tri_index -- plus max_depth."""
+def build_flat_tree(primitives: list[Primitive], threads: int = 0, device: Context | None = None,
+                    min_device_triangles: int = 0) -> dict:
+    """Tree build, flattened into the device layout as numpy arrays -- nodes
+    uint32 (n, 8), tris float32 (n, 9), tri_prim, tri_index -- plus
+    max_depth.  On the host (no GPU needed), or with ``device`` given on that
+    context's GPU (``on_device`` in the result tells whether the GPU built it:
+    instancing, or fewer than ``min_device_triangles`` triangles, builds on
+    the host)."""
     lib = _lib.load()
     meshes, mesh_ids = [], {}
     for p in primitives:
@@ -232,10 +237,15 @@ def build_flat_tree(primitives: list[Primitive], threads: int = 0) -> dict:
         xf = p.mesh_to_world.ctypes.data if p.mesh_to_world is not None else None
         cp[i] = _lib.skw_primitive(mesh_ids[id(p.mesh)], xf)
     h = C.c_void_p()
-    err = C.create_string_buffer(256)
-    rc = lib.skw_flat_tree_build(cm, len(meshes), cp, len(primitives), threads, C.byref(h), err, 256)
-    if rc != _lib.SKW_OK:
-        raise _lib.SkwError(rc, err.value.decode())
+    on_dev = C.c_int32(0)
+    if device is not None:
+        _lib.check(lib.skw_flat_tree_build_device(device.handle, cm, len(meshes), cp, len(primitives),
+                                                  min_device_triangles, C.byref(h), C.byref(on_dev)), device.handle)
+    else:
+        err = C.create_string_buffer(256)
+        rc = lib.skw_flat_tree_build(cm, len(meshes), cp, len(primitives), threads, C.byref(h), err, 256)
+        if rc != _lib.SKW_OK:
+            raise _lib.SkwError(rc, err.value.decode())
     try:
         nn, nt, md = C.c_int64(), C.c_int64(), C.c_int32()
         _lib.check(lib.skw_flat_tree_sizes(h, C.byref(nn), C.byref(nt), C.byref(md)))
@@ -262,7 +272,7 @@ def build_flat_tree(primitives: list[Primitive], threads: int = 0) -> dict:
     n = nt.value
     return {"nodes": nodes, "tris": tris[:n], "tri_prim": tp[:n], "tri_index": ti[:n], "max_depth": md.value,
             "inst_prim": ip[:ni.value], "inst_root": ir[:ni.value], "inst_world_to_mesh": im[:ni.value],
-            "subtree_roots": sr[:ns.value], "leaf_ranges": ext}
+            "subtree_roots": sr[:ns.value], "leaf_ranges": ext, "on_device": bool(on_dev.value)}
 
 
 def unpack_hits_d(hits) -> dict:

@@ -515,9 +515,98 @@ uint32_t flatten(const BNode *root, FlatTree &out) {
   return root_idx;
 }
 
+// The same pre-order flattening over the GPU build's node records.
+uint32_t flatten_records(const AccelTreeGpu &g, FlatTree &out) {
+  const uint32_t root_idx = (uint32_t)out.nodes.size();
+  out.nodes.emplace_back();
+  std::vector<std::pair<int64_t, uint32_t>> stack{{0, root_idx}};
+  while (!stack.empty()) {
+    auto [id, idx] = stack.back();
+    stack.pop_back();
+    DevNode dn{};
+    for (int k = 0; k < 3; ++k) {
+      dn.lo[k] = g.box[(size_t)id * 6 + k];
+      dn.hi[k] = g.box[(size_t)id * 6 + 3 + k];
+    }
+    if (g.flags[(size_t)id] == 0) {
+      dn.a = g.tb[(size_t)id];
+      dn.b = (g.te[(size_t)id] - g.tb[(size_t)id]) << 8;
+    } else {
+      uint32_t first = (uint32_t)out.nodes.size(), mask = 0, slot = first;
+      std::pair<int64_t, uint32_t> kids[3];
+      int nk = 0;
+      for (int c = 0; c < 3; ++c) {
+        const int32_t ch = g.child[(size_t)id * 3 + c];
+        if (ch >= 0) {
+          mask |= 1u << c;
+          kids[nk++] = {ch, slot++};
+          out.nodes.emplace_back();
+        }
+      }
+      dn.a = first;
+      dn.b = (uint32_t)g.flags[(size_t)id] | (mask << 2);
+      for (int k = nk - 1; k >= 0; --k) stack.push_back(kids[k]);
+    }
+    out.nodes[idx] = dn;
+  }
+  return root_idx;
+}
+
 const double kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
 
 }  // namespace
+
+std::string build_accel_device(const MeshIn *meshes, int32_t n_meshes, const PrimIn *prims, int32_t n_prims,
+                               int threads, cudaStream_t st, int64_t min_gpu, FlatTree &out, bool *on_gpu) {
+  if (on_gpu) *on_gpu = false;
+  if (n_prims < 0 || n_meshes < 0) return "negative primitive or mesh count";
+  std::vector<int> uses((size_t)n_meshes, 0);
+  int64_t n_tris = 0;
+  for (int32_t p = 0; p < n_prims; ++p) {
+    if (prims[p].mesh < 0 || prims[p].mesh >= n_meshes) return "primitive references a mesh index out of range";
+    ++uses[(size_t)prims[p].mesh];
+    n_tris += meshes[prims[p].mesh].n_triangles;
+  }
+  bool shared = false;
+  for (int u : uses) shared = shared || u > 1;
+  if (shared || n_tris < std::max<int64_t>(min_gpu, 1))
+    return build_accel(meshes, n_meshes, prims, n_prims, threads, out);
+  for (int32_t p = 0; p < n_prims; ++p) {
+    const MeshIn &m = meshes[prims[p].mesh];
+    if (m.n_triangles > 0 && (!m.triangles || !m.vertices)) return "mesh has triangles but null arrays";
+  }
+  // Steps 3-4 of the reference's constructor: the primitives' triangles in
+  // world space, then the tree over them (on the GPU).
+  Builder B;
+  for (int32_t p = 0; p < n_prims; ++p) add_mesh_triangles(B, meshes[prims[p].mesh], prims[p].mesh_to_world, p);
+  const size_t n = B.prim.size();
+  if (n > (size_t)INT32_MAX / 2) return "too many triangles";
+  if (n < (size_t)std::max<int64_t>(min_gpu, 1)) return build_accel(meshes, n_meshes, prims, n_prims, threads, out);
+  static_assert(sizeof(BoxF) == 24, "BoxF is 6 floats");
+  AccelTreeGpu g;
+  cudaError_t e = build_accel_tree_gpu(reinterpret_cast<const float *>(B.tbox.data()), (int64_t)n, st, g);
+  if (e != cudaSuccess) return std::string("GPU tree build: ") + cudaGetErrorString(e);
+  if (g.inconsistent) return build_accel(meshes, n_meshes, prims, n_prims, threads, out);
+  out = FlatTree();
+  out.nodes.reserve((size_t)g.n_nodes);
+  flatten_records(g, out);
+  out.tris.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    DevTri &t = out.tris[i];
+    const size_t o = g.perm[i];
+    std::memcpy(t.v0, &B.tv[9 * o], 12);
+    std::memcpy(t.v1, &B.tv[9 * o + 3], 12);
+    std::memcpy(t.v2, &B.tv[9 * o + 6], 12);
+    t.prim = B.prim[o];
+    t.tri = B.tidx[o];
+    t.slot = (int32_t)i;
+  }
+  out.max_depth = g.max_depth;
+  out.n_leaves = g.n_leaves;
+  for (int k = 0; k < 6; ++k) out.bounds[k] = g.box[(size_t)k];
+  if (on_gpu) *on_gpu = true;
+  return "";
+}
 
 std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *prims, int32_t n_prims, int threads,
                         FlatTree &out) {

@@ -2,6 +2,8 @@
 // the device layout used by the traversal kernels.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -85,6 +87,31 @@ struct FlatTree {
 // Matrix4x4<double>::Inverted (Math/Matrix4x4.h:240-316): Gauss-Jordan
 // elimination with full pivoting, row-major 4x4; false if singular.
 bool invert4(const double *m, double *out);
+
+// The tree built on the GPU over triangle boxes (build_accel_tree_gpu):
+// node records by node id (level by level from the root), and the final
+// slot order.
+struct AccelTreeGpu {
+  std::vector<float> box;       // 6 floats per node: lo xyz, hi xyz
+  std::vector<uint32_t> tb, te; // triangle-slot range per node
+  std::vector<uint8_t> flags;   // 0 leaf, 1..3 split axis + 1
+  std::vector<int32_t> child;   // 3 per node (left, middle, right), -1 if absent
+  std::vector<uint32_t> perm;   // triangle (input order) of each final slot
+  int64_t n_nodes = 0, n_leaves = 0;
+  int32_t max_depth = 0;
+  bool inconsistent = false;    // the partition's step map was not a permutation
+};
+
+// Builds the tree of the host build over n triangle boxes (6 floats each:
+// lo xyz, hi xyz, host memory, in the order the host build starts from) on
+// the current device, on stream st (waits for it).
+cudaError_t build_accel_tree_gpu(const float *tbox, int64_t n, cudaStream_t st, AccelTreeGpu &out);
+
+// build_accel for accelerators without instancing, the tree built on the
+// GPU (the same tree; meshes shared by several primitives, or fewer than
+// min_gpu triangles, build on the host).  *on_gpu tells which.
+std::string build_accel_device(const MeshIn *meshes, int32_t n_meshes, const PrimIn *prims, int32_t n_prims,
+                               int threads, cudaStream_t st, int64_t min_gpu, FlatTree &out, bool *on_gpu);
 
 // Builds the tree (same split search, partition order and leaf rule as the
 // reference TriangleAccelerator, instancing included: a mesh used by several

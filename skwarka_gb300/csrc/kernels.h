@@ -62,6 +62,9 @@ cudaError_t launch_traversal_d(bool closest, int stack_cap, const void *nodes, c
 // out_visited (optional) counts visited nodes.  A non-zero knn_scratch_bytes(nq, k) (k > 128) means a scratch buffer of that
 // many bytes is required.  status bit 1: stack overflow.
 size_t knn_scratch_bytes(int64_t nq, int k);
+// Exclusive scan of n 64-bit values in place (three launches); sums holds
+// ceil(n / 256) values of scratch.
+cudaError_t scan64(uint64_t *v, int64_t n, uint64_t *sums, cudaStream_t st);
 cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                        const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,
                        double *out_d2, int32_t *out_count, int32_t *out_visited, void *scratch, unsigned *status,

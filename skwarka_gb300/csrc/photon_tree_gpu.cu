@@ -96,6 +96,8 @@ __global__ void k_scan64_add(uint64_t *__restrict__ v, int64_t n, const uint64_t
   if (i < n) v[i] += sums[blockIdx.x];
 }
 
+}  // namespace
+
 cudaError_t scan64(uint64_t *v, int64_t n, uint64_t *sums, cudaStream_t st) {
   const int nb = (int)((n + kBlock - 1) / kBlock);
   k_scan64_blocks<<<nb, kBlock, 0, st>>>(v, n, sums);
@@ -103,6 +105,8 @@ cudaError_t scan64(uint64_t *v, int64_t n, uint64_t *sums, cudaStream_t st) {
   k_scan64_add<<<nb, kBlock, 0, st>>>(v, n, sums);
   return cudaGetLastError();
 }
+
+namespace {
 
 // ------------------------------------------------------------ sort --
 // The three lists (axis a at [a n, a n + n)): key and point index.

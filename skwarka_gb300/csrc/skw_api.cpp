@@ -95,6 +95,7 @@ int skw_ctx_host_buffers_in_place(const skw_ctx *ctx) { return ctx && coherent_h
 struct skw_flat_tree {
   skw::FlatTree ft;
   double build_ms = 0.0;
+  bool on_device = false;
 };
 
 int skw_flat_tree_build(const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims, int32_t n_prims,
@@ -125,6 +126,42 @@ int skw_flat_tree_build(const skw_mesh *meshes, int32_t n_meshes, const skw_prim
     set_err(e);
     return SKW_ERR_ARG;
   }
+  *out = t;
+  return SKW_OK;
+}
+
+int skw_flat_tree_build_device(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims,
+                               int32_t n_prims, int64_t min_device_triangles, skw_flat_tree **out, int32_t *on_device) {
+  if (!ctx || !out || (n_meshes > 0 && !meshes) || (n_prims > 0 && !prims))
+    return fail(ctx, SKW_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (on_device) *on_device = 0;
+  cudaError_t ce = cudaSetDevice(ctx->device);
+  if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaSetDevice");
+  std::vector<skw::MeshIn> m((size_t)std::max(n_meshes, 0));
+  for (int32_t i = 0; i < n_meshes; ++i)
+    m[(size_t)i] = skw::MeshIn{meshes[i].vertices, meshes[i].n_vertices, meshes[i].triangles, meshes[i].n_triangles};
+  std::vector<skw::PrimIn> p((size_t)std::max(n_prims, 0));
+  for (int32_t i = 0; i < n_prims; ++i) p[(size_t)i] = skw::PrimIn{prims[i].mesh, prims[i].mesh_to_world};
+  auto *t = new (std::nothrow) skw_flat_tree();
+  if (!t) return fail(ctx, SKW_ERR_OOM, "out of host memory");
+  cudaStream_t st = nullptr;
+  if ((ce = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) {
+    delete t;
+    return cuda_fail(ctx, ce, "cudaStreamCreate");
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  bool on_gpu = false;
+  std::string e = skw::build_accel_device(m.data(), n_meshes, p.data(), n_prims, 0, st, min_device_triangles,
+                                          t->ft, &on_gpu);
+  t->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  cudaStreamDestroy(st);
+  if (!e.empty()) {
+    delete t;
+    return fail(ctx, e.rfind("GPU tree build", 0) == 0 ? SKW_ERR_CUDA : SKW_ERR_ARG, e);
+  }
+  t->on_device = on_gpu;
+  if (on_device) *on_device = on_gpu ? 1 : 0;
   *out = t;
   return SKW_OK;
 }
@@ -228,6 +265,7 @@ int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_acce
   info.stack_need = 2 * ft.max_depth + 1;
   std::memcpy(info.bounds, ft.bounds, sizeof(info.bounds));
   info.build_ms = tree->build_ms;
+  info.built_on_device = tree->on_device ? 1 : 0;
   info.device_bytes = (int64_t)(nb + tb + ib + eb);
   a->h_nodes = ft.nodes;
   a->h_tris = ft.tris;
@@ -241,13 +279,16 @@ int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_acce
   return SKW_OK;
 }
 
+// Accelerators of at least this many triangles (and no instancing) build
+// their tree on the GPU; below it the host build is as fast.
+constexpr int64_t kDeviceBuildMin = 16384;
+
 int skw_accel_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, const skw_primitive *prims,
                      int32_t n_prims, skw_accel **out) {
   if (!ctx || !out) return fail(ctx, SKW_ERR_ARG, "null argument");
   skw_flat_tree *t = nullptr;
-  char err[256] = {0};
-  int rc = skw_flat_tree_build(meshes, n_meshes, prims, n_prims, 0, &t, err, sizeof(err));
-  if (rc != SKW_OK) return fail(ctx, rc, err);
+  int rc = skw_flat_tree_build_device(ctx, meshes, n_meshes, prims, n_prims, kDeviceBuildMin, &t, nullptr);
+  if (rc != SKW_OK) return rc;
   rc = skw_accel_create_from_flat(ctx, t, out);
   skw_flat_tree_destroy(t);
   return rc;
