@@ -439,38 +439,113 @@ namespace {
 // repeated vertex index, TriangleMesh.cpp:176-182; mesh triangle indices
 // count the kept ones), in mesh space or through `m` (Transform on
 // Point3D_f), appended to the builder with primitive id `prim`.
-void add_mesh_triangles(Builder &B, const MeshIn &m, const double *xf, int32_t prim) {
-  int32_t kept = 0;
-  for (int64_t t = 0; t < m.n_triangles; ++t) {
-    const int32_t *ix = m.triangles + 3 * t;
-    bool bad = false;
-    for (int k = 0; k < 3; ++k)
-      if (ix[k] < 0 || (int64_t)ix[k] >= m.n_vertices) bad = true;
-    if (bad || ix[0] == ix[1] || ix[0] == ix[2] || ix[1] == ix[2]) continue;
-    float v[9];
-    for (int k = 0; k < 3; ++k) {
-      const float *src = m.vertices + 3 * (int64_t)ix[k];
-      if (xf) {
-        transform_point(xf, src, v + 3 * k);
-      } else {
-        v[3 * k] = src[0];
-        v[3 * k + 1] = src[1];
-        v[3 * k + 2] = src[2];
-      }
-    }
-    BoxF b;
-    for (int k = 0; k < 3; ++k) {
-      for (int c = 0; c < 3; ++c) {
-        b.lo[c] = std::min(b.lo[c], v[3 * k + c]);
-        b.hi[c] = std::max(b.hi[c], v[3 * k + c]);
-      }
-    }
-    B.tv.insert(B.tv.end(), v, v + 9);
-    B.prim.push_back(prim);
-    B.tidx.push_back(kept++);
-    B.tbox.push_back(b);
-    B.order.push_back((uint32_t)B.order.size());
+struct MeshJob {
+  const MeshIn *m;
+  const double *xf;
+  int32_t prim;
+};
+
+inline bool dropped(const MeshIn &m, int64_t t) {
+  const int32_t *ix = m.triangles + 3 * t;
+  for (int k = 0; k < 3; ++k)
+    if (ix[k] < 0 || (int64_t)ix[k] >= m.n_vertices) return true;
+  return ix[0] == ix[1] || ix[0] == ix[2] || ix[1] == ix[2];
+}
+
+// Runs f(c) for c in [0, n) on up to `threads` threads.
+template <class F>
+void parallel_for(size_t n, int threads, F &&f) {
+  const size_t nt = std::min<size_t>(n, (size_t)std::max(threads, 1));
+  if (nt <= 1) {
+    for (size_t c = 0; c < n; ++c) f(c);
+    return;
   }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (size_t w = 0; w < nt; ++w)
+    pool.emplace_back([&]() {
+      for (size_t c; (c = next.fetch_add(1)) < n;) f(c);
+    });
+  for (std::thread &t : pool) t.join();
+}
+
+// The meshes' triangles, dropping those TriangleMesh drops (an
+// out-of-range or repeated vertex index, TriangleMesh.cpp:176-182; mesh
+// triangle indices count the kept ones), in mesh space or through each
+// job's matrix (Transform on Point3D_f), appended to the builder in job
+// order with the job's primitive id.  Chunks of triangles are counted,
+// then filled, on several threads; the result is the sequential one.
+void add_meshes(Builder &B, const std::vector<MeshJob> &jobs, int threads) {
+  constexpr int64_t kChunk = 1 << 15;
+  struct Chunk {
+    size_t job;
+    int64_t t0, t1;
+    size_t out = 0;
+    int32_t kept_before = 0;  // kept triangles of the job before the chunk
+    int64_t kept = 0;
+  };
+  std::vector<Chunk> chunks;
+  for (size_t j = 0; j < jobs.size(); ++j)
+    for (int64_t t0 = 0; t0 < jobs[j].m->n_triangles; t0 += kChunk)
+      chunks.push_back(Chunk{j, t0, std::min(jobs[j].m->n_triangles, t0 + kChunk)});
+  parallel_for(chunks.size(), threads, [&](size_t c) {
+    Chunk &k = chunks[c];
+    int64_t kept = 0;
+    for (int64_t t = k.t0; t < k.t1; ++t) kept += dropped(*jobs[k.job].m, t) ? 0 : 1;
+    k.kept = kept;
+  });
+  size_t total = B.prim.size();
+  for (size_t c = 0; c < chunks.size(); ++c) {
+    chunks[c].out = total;
+    chunks[c].kept_before = (c > 0 && chunks[c - 1].job == chunks[c].job)
+                                ? chunks[c - 1].kept_before + (int32_t)chunks[c - 1].kept
+                                : 0;
+    total += (size_t)chunks[c].kept;
+  }
+  const size_t base = B.prim.size();
+  B.tv.resize(9 * total);
+  B.prim.resize(total);
+  B.tidx.resize(total);
+  B.tbox.resize(total);
+  B.order.resize(total);
+  for (size_t i = base; i < total; ++i) B.order[i] = (uint32_t)i;
+  parallel_for(chunks.size(), threads, [&](size_t c) {
+    const Chunk &k = chunks[c];
+    const MeshJob &jb = jobs[k.job];
+    const MeshIn &m = *jb.m;
+    size_t o = k.out;
+    int32_t kept = k.kept_before;
+    for (int64_t t = k.t0; t < k.t1; ++t) {
+      if (dropped(m, t)) continue;
+      const int32_t *ix = m.triangles + 3 * t;
+      float *v = &B.tv[9 * o];
+      for (int q = 0; q < 3; ++q) {
+        const float *src = m.vertices + 3 * (int64_t)ix[q];
+        if (jb.xf) {
+          transform_point(jb.xf, src, v + 3 * q);
+        } else {
+          v[3 * q] = src[0];
+          v[3 * q + 1] = src[1];
+          v[3 * q + 2] = src[2];
+        }
+      }
+      BoxF b;
+      for (int q = 0; q < 3; ++q) {
+        for (int a = 0; a < 3; ++a) {
+          b.lo[a] = std::min(b.lo[a], v[3 * q + a]);
+          b.hi[a] = std::max(b.hi[a], v[3 * q + a]);
+        }
+      }
+      B.prim[o] = jb.prim;
+      B.tidx[o] = kept++;
+      B.tbox[o] = b;
+      ++o;
+    }
+  });
+}
+
+void add_mesh_triangles(Builder &B, const MeshIn &m, const double *xf, int32_t prim) {
+  add_meshes(B, {MeshJob{&m, xf, prim}}, B.threads);
 }
 
 // Pre-order flattening of one tree into out.nodes; a node's present
@@ -578,7 +653,13 @@ std::string build_accel_device(const MeshIn *meshes, int32_t n_meshes, const Pri
   // Steps 3-4 of the reference's constructor: the primitives' triangles in
   // world space, then the tree over them (on the GPU).
   Builder B;
-  for (int32_t p = 0; p < n_prims; ++p) add_mesh_triangles(B, meshes[prims[p].mesh], prims[p].mesh_to_world, p);
+  unsigned hw = std::thread::hardware_concurrency();
+  B.threads = threads > 0 ? threads : (int)(hw ? hw : 1);
+  {
+    std::vector<MeshJob> jobs;
+    for (int32_t p = 0; p < n_prims; ++p) jobs.push_back(MeshJob{&meshes[prims[p].mesh], prims[p].mesh_to_world, p});
+    add_meshes(B, jobs, B.threads);
+  }
   const size_t n = B.prim.size();
   if (n > (size_t)INT32_MAX / 2) return "too many triangles";
   if (n < (size_t)std::max<int64_t>(min_gpu, 1)) return build_accel(meshes, n_meshes, prims, n_prims, threads, out);
@@ -591,16 +672,19 @@ std::string build_accel_device(const MeshIn *meshes, int32_t n_meshes, const Pri
   out.nodes.reserve((size_t)g.n_nodes);
   flatten_records(g, out);
   out.tris.resize(n);
-  for (size_t i = 0; i < n; ++i) {
-    DevTri &t = out.tris[i];
-    const size_t o = g.perm[i];
-    std::memcpy(t.v0, &B.tv[9 * o], 12);
-    std::memcpy(t.v1, &B.tv[9 * o + 3], 12);
-    std::memcpy(t.v2, &B.tv[9 * o + 6], 12);
-    t.prim = B.prim[o];
-    t.tri = B.tidx[o];
-    t.slot = (int32_t)i;
-  }
+  const size_t gchunks = (n + 65535) / 65536;
+  parallel_for(gchunks, B.threads, [&](size_t c) {
+    for (size_t i = c * 65536; i < std::min(n, (c + 1) * 65536); ++i) {
+      DevTri &t = out.tris[i];
+      const size_t o = g.perm[i];
+      std::memcpy(t.v0, &B.tv[9 * o], 12);
+      std::memcpy(t.v1, &B.tv[9 * o + 3], 12);
+      std::memcpy(t.v2, &B.tv[9 * o + 6], 12);
+      t.prim = B.prim[o];
+      t.tri = B.tidx[o];
+      t.slot = (int32_t)i;
+    }
+  });
   out.max_depth = g.max_depth;
   out.n_leaves = g.n_leaves;
   for (int k = 0; k < 6; ++k) out.bounds[k] = g.box[(size_t)k];
@@ -663,8 +747,12 @@ std::string build_accel(const MeshIn *meshes, int32_t n_meshes, const PrimIn *pr
   }
   // Step 3: the primitives that own their mesh, in world space.
   const size_t shared_end = B.prim.size();
-  for (int32_t p = 0; p < n_prims; ++p)
-    if (uses[(size_t)prims[p].mesh] < 2) add_mesh_triangles(B, meshes[prims[p].mesh], prims[p].mesh_to_world, p);
+  {
+    std::vector<MeshJob> jobs;
+    for (int32_t p = 0; p < n_prims; ++p)
+      if (uses[(size_t)prims[p].mesh] < 2) jobs.push_back(MeshJob{&meshes[prims[p].mesh], prims[p].mesh_to_world, p});
+    add_meshes(B, jobs, B.threads);
+  }
   const size_t n = B.prim.size(), n_inst = B.ibox.size();
   if (n > (size_t)INT32_MAX) return "too many triangles";
 

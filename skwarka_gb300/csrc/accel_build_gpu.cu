@@ -102,6 +102,7 @@ struct Dev {
   double *hsplit;
   // (a node's bucket base is cnt2[b] between the bucket scan and the split search)
   int32_t *hid, *htries, *haxis;
+  uint32_t *heads;            // the level's nodes' first slots, by rank
   uint32_t *hnl, *hnr;
   uint8_t *hleaf;
   double *bcost, *bpos;       // 3 per node
@@ -111,6 +112,7 @@ struct Dev {
   uint64_t *cnt, *cnt2, *cnt3, *sums;  // n + 1 each (sums: block totals)
   uint32_t *tarr, *jarr, *ord, *iarr, *f0, *f1, *lmb, *dest;
   int *err;
+  int *maxseg;                // the level's largest node (triangles)
   unsigned long long *n_leaves;
   // node records, by node id
   float *rbox;
@@ -139,6 +141,7 @@ __global__ void k_heads(Dev D) {
   uint64_t h = 0;
   if (s < D.n && D.seg[s].x == (int)s) {
     h = 1;
+    atomicMax(D.maxseg, D.seg[s].y - (int)s);
     for (int c = 0; c < 3; ++c) {
       D.hkeys[s * 6 + c] = ~0ull;
       D.hkeys[s * 6 + 3 + c] = 0ull;
@@ -202,6 +205,7 @@ __global__ void k_head_setup(Dev D, int64_t level_base, int depth) {
     const int2 r = D.seg[s];
     const int64_t id = level_base + (int64_t)D.cnt[s];
     D.hid[s] = (int32_t)id;
+    D.heads[D.cnt[s]] = (uint32_t)s;
     float lo[3], hi[3];
     for (int c = 0; c < 3; ++c) {
       const unsigned long long kl = D.hkeys[s * 6 + c], kh = D.hkeys[s * 6 + 3 + c];
@@ -247,12 +251,25 @@ __global__ void k_bucket_init(Dev D) {
   }
 }
 
-__device__ __forceinline__ void bucket_add(uint32_t *r, const float *lo, const float *hi) {
+// Adds a box to bucket idx (-1: none) for the lanes that reach this call
+// together: lanes adding to the same bucket are merged first, one atomic
+// per bucket and key (NaN coordinates take no part, as in the reference's
+// min / max).
+__device__ __forceinline__ void bucket_add_grouped(uint32_t *buckets, int64_t idx, const float *lo, const float *hi) {
+  const unsigned grp = __match_any_sync(__activemask(), idx);
+  if (idx < 0) return;
+  uint32_t kl[3], kh[3];
   for (int c = 0; c < 3; ++c) {
-    if (!isnan(lo[c])) atomicMin(r + c, okey(lo[c]));
-    if (!isnan(hi[c])) atomicMax(r + 3 + c, okey(hi[c]));
+    kl[c] = __reduce_min_sync(grp, isnan(lo[c]) ? 0xFFFFFFFFu : okey(lo[c]));
+    kh[c] = __reduce_max_sync(grp, isnan(hi[c]) ? 0u : okey(hi[c]));
   }
-  atomicAdd(r + 6, 1u);
+  if ((threadIdx.x & 31) != __ffs(grp) - 1) return;
+  uint32_t *r = buckets + idx * 7;
+  for (int c = 0; c < 3; ++c) {
+    if (kl[c] != 0xFFFFFFFFu) atomicMin(r + c, kl[c]);
+    if (kh[c] != 0u) atomicMax(r + 3 + c, kh[c]);
+  }
+  atomicAdd(r + 6, (uint32_t)__popc(grp));
 }
 
 // The buckets of every internal node (_DetermineBestSplit, :531-565): per
@@ -279,82 +296,185 @@ __global__ void k_bucket_fill(Dev D) {
     const float dmax = __fsub_rn(hi[a], nlo), dmin = __fsub_rn(lo[a], nlo);
     const uint64_t lefts_begin = min(tries, cast_size(__dadd_rn(__dmul_rn((double)dmax, coef), 1.0)));
     const uint64_t rights_end = min(tries, cast_size(__dadd_rn(__dmul_rn((double)dmin, coef), 1.0)));
-    uint32_t *L = D.buckets + (base + (int64_t)(a * 3) * (int64_t)tries) * 7;
-    uint32_t *M = L + tries * 7, *R = M + tries * 7;
-    if (rights_end > 0) bucket_add(R + (rights_end - 1) * 7, lo, hi);
-    if (lefts_begin < tries) bucket_add(L + lefts_begin * 7, lo, hi);
-    for (uint64_t j = rights_end; j < lefts_begin; ++j) bucket_add(M + j * 7, lo, hi);
+    const int64_t lb = base + (int64_t)(a * 3) * (int64_t)tries;  // bucket index of L[0]
+    bucket_add_grouped(D.buckets, rights_end > 0 ? lb + 2 * (int64_t)tries + (int64_t)(rights_end - 1) : -1, lo, hi);
+    bucket_add_grouped(D.buckets, lefts_begin < tries ? lb + (int64_t)lefts_begin : -1, lo, hi);
+    // the middle buckets: the lanes of one node walk the union of their
+    // ranges together, one merged add per bucket
+    uint32_t *M = D.buckets + (lb + (int64_t)tries) * 7;
+    const unsigned grp = __match_any_sync(__activemask(), b);
+    const bool any = rights_end < lefts_begin;
+    const uint32_t jlo = __reduce_min_sync(grp, any ? (uint32_t)rights_end : 0xFFFFFFFFu);
+    const uint32_t jhi = __reduce_max_sync(grp, any ? (uint32_t)lefts_begin : 0u);
+    uint32_t kl[3], kh[3];
+    for (int c = 0; c < 3; ++c) {
+      kl[c] = isnan(lo[c]) ? 0xFFFFFFFFu : okey(lo[c]);
+      kh[c] = isnan(hi[c]) ? 0u : okey(hi[c]);
+    }
+    const bool leader = (threadIdx.x & 31) == __ffs(grp) - 1;
+    for (uint32_t j = jlo; j < jhi; ++j) {
+      const bool in = rights_end <= j && j < lefts_begin;
+      const unsigned who = __ballot_sync(grp, in);
+      if (who == 0u) continue;
+      uint32_t ml[3], mh[3];
+      for (int c = 0; c < 3; ++c) {
+        ml[c] = __reduce_min_sync(grp, in ? kl[c] : 0xFFFFFFFFu);
+        mh[c] = __reduce_max_sync(grp, in ? kh[c] : 0u);
+      }
+      if (leader) {
+        uint32_t *r = M + (int64_t)j * 7;
+        for (int c = 0; c < 3; ++c) {
+          if (ml[c] != 0xFFFFFFFFu) atomicMin(r + c, ml[c]);
+          if (mh[c] != 0u) atomicMax(r + 3 + c, mh[c]);
+        }
+        atomicAdd(r + 6, (uint32_t)__popc(who));
+      }
+    }
   }
 }
 
-// One axis of one node's split search (_DetermineBestSplit, :566-608):
-// suffix unions of the right buckets, then per candidate plane, in order,
-// the cost sum(n_child * area_child / area_node) in double with the 0.8
-// bonus for an empty side; the first strict minimum wins.
-__global__ void k_score(Dev D) {
-  const int64_t t = (int64_t)blockIdx.x * kB + threadIdx.x;
-  if (t >= 3 * D.n) return;
-  const int64_t s = t / 3;
-  const int a = (int)(t - 3 * s);
-  if (D.seg[s].x != (int)s || D.hleaf[s]) return;
+// Union of two bucket boxes with counts (the order of unions does not
+// change a union of float boxes).
+struct BoxN {
+  float lo[3], hi[3];
+  uint32_t n;
+};
+__device__ __forceinline__ BoxN box_empty() {
+  BoxN b;
+  for (int c = 0; c < 3; ++c) {
+    b.lo[c] = INFINITY;
+    b.hi[c] = -INFINITY;
+  }
+  b.n = 0;
+  return b;
+}
+__device__ __forceinline__ void box_unite(BoxN &a, const BoxN &b) {
+  for (int c = 0; c < 3; ++c) {
+    a.lo[c] = fminf(a.lo[c], b.lo[c]);
+    a.hi[c] = fmaxf(a.hi[c], b.hi[c]);
+  }
+  a.n += b.n;
+}
+__device__ __forceinline__ BoxN box_keys(const uint32_t *r) {  // a bucket as filled (keys)
+  BoxN b;
+  for (int c = 0; c < 3; ++c) {
+    b.lo[c] = lo_of(r[c]);
+    b.hi[c] = hi_of(r[3 + c]);
+  }
+  b.n = r[6];
+  return b;
+}
+__device__ __forceinline__ BoxN box_shfl_up(const BoxN &a, int o) {
+  BoxN b;
+  for (int c = 0; c < 3; ++c) {
+    b.lo[c] = __shfl_up_sync(0xffffffffu, a.lo[c], o);
+    b.hi[c] = __shfl_up_sync(0xffffffffu, a.hi[c], o);
+  }
+  b.n = __shfl_up_sync(0xffffffffu, a.n, o);
+  return b;
+}
+__device__ __forceinline__ BoxN box_shfl_down(const BoxN &a, int o) {
+  BoxN b;
+  for (int c = 0; c < 3; ++c) {
+    b.lo[c] = __shfl_down_sync(0xffffffffu, a.lo[c], o);
+    b.hi[c] = __shfl_down_sync(0xffffffffu, a.hi[c], o);
+  }
+  b.n = __shfl_down_sync(0xffffffffu, a.n, o);
+  return b;
+}
+
+// One axis of one node's split search (_DetermineBestSplit, :566-608),
+// one warp: lane l takes a contiguous slice of the candidate planes.  The
+// right buckets' suffix unions and the left buckets' prefix unions come
+// from warp scans of the slices' unions; each lane then walks its slice
+// (the right suffixes stored back in place), computing the cost
+// sum(n_child * area_child / area_node) in the reference's double
+// arithmetic with the 0.8 bonus for an empty side; the first strict
+// minimum over all planes is the smallest (cost, plane) pair.
+__global__ void k_score(Dev D, int64_t level_nodes) {
+  const int64_t w = ((int64_t)blockIdx.x * kB + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= 3 * level_nodes) return;  // whole warps
+  const int64_t node = w / 3;
+  const int a = (int)(w - 3 * node);
+  const int64_t s = D.heads[node];
+  if (D.hleaf[s]) return;
   if (D.smask[s] & (1u << a)) {
-    D.bcost[t] = INFINITY;
-    D.bpos[t] = 0.0;
+    if (lane == 0) {
+      D.bcost[3 * s + a] = INFINITY;
+      D.bpos[3 * s + a] = 0.0;
+    }
     return;
   }
   const int tries = D.htries[s];
   uint32_t *L = D.buckets + ((int64_t)D.cnt2[s] + (int64_t)(a * 3) * tries) * 7;
   uint32_t *M = L + (int64_t)tries * 7, *R = M + (int64_t)tries * 7;
-  // suffix unions of the right buckets, stored back decoded
-  float rl[3] = {INFINITY, INFINITY, INFINITY}, rh[3] = {-INFINITY, -INFINITY, -INFINITY};
-  uint32_t rn = 0;
-  for (int i = tries - 1; i >= 0; --i) {
+  const int per = (tries + 31) / 32, i0 = min(tries, lane * per), i1 = min(tries, i0 + per);
+  BoxN ls = box_empty(), rs = box_empty();
+  for (int i = i0; i < i1; ++i) {
+    box_unite(ls, box_keys(L + (int64_t)i * 7));
+    box_unite(rs, box_keys(R + (int64_t)i * 7));
+  }
+  // inclusive prefix of the left slices, inclusive suffix of the right ones
+  for (int o = 1; o < 32; o <<= 1) {
+    const BoxN u = box_shfl_up(ls, o), d = box_shfl_down(rs, o);
+    if (lane >= o) box_unite(ls, u);
+    if (lane + o < 32) box_unite(rs, d);
+  }
+  BoxN lp = box_shfl_up(ls, 1), rp = box_shfl_down(rs, 1);  // exclusive
+  if (lane == 0) lp = box_empty();
+  if (lane == 31) rp = box_empty();
+  // the right suffixes of the slice, stored back decoded
+  for (int i = i1 - 1; i >= i0; --i) {
     uint32_t *r = R + (int64_t)i * 7;
+    box_unite(rp, box_keys(r));
     for (int c = 0; c < 3; ++c) {
-      rl[c] = fminf(rl[c], lo_of(r[c]));
-      rh[c] = fmaxf(rh[c], hi_of(r[3 + c]));
-      r[c] = __float_as_uint(rl[c]);
-      r[3 + c] = __float_as_uint(rh[c]);
+      r[c] = __float_as_uint(rp.lo[c]);
+      r[3 + c] = __float_as_uint(rp.hi[c]);
     }
-    rn += r[6];
-    r[6] = rn;
+    r[6] = rp.n;
   }
   const float *nlo = D.hbox + s * 6, *nhi = nlo + 3;
   const double inv_area = __ddiv_rn(1.0, (double)area_f(nlo, nhi));
-  float ll[3] = {INFINITY, INFINITY, INFINITY}, lh[3] = {-INFINITY, -INFINITY, -INFINITY};
-  uint32_t ln = 0;
   double best = INFINITY;
-  int bi = -1;
-  for (int i = 0; i < tries; ++i) {
-    const uint32_t *l = L + (int64_t)i * 7, *m = M + (int64_t)i * 7, *r = R + (int64_t)i * 7;
-    float ml[3], mh[3], sl[3], sh[3];
+  int bi = 0x7FFFFFFF;
+  for (int i = i0; i < i1; ++i) {
+    box_unite(lp, box_keys(L + (int64_t)i * 7));
+    const BoxN m = box_keys(M + (int64_t)i * 7);
+    const uint32_t *r = R + (int64_t)i * 7;
+    float sl[3], sh[3];
     for (int c = 0; c < 3; ++c) {
-      ll[c] = fminf(ll[c], lo_of(l[c]));
-      lh[c] = fmaxf(lh[c], hi_of(l[3 + c]));
-      ml[c] = lo_of(m[c]);
-      mh[c] = hi_of(m[3 + c]);
       sl[c] = __uint_as_float(r[c]);
       sh[c] = __uint_as_float(r[3 + c]);
     }
-    ln += l[6];
-    const uint32_t mn = m[6], sn = r[6];
-    const double p1 = min1(__dmul_rn(area_d(ll, lh), inv_area));
-    const double p2 = min1(__dmul_rn(area_d(ml, mh), inv_area));
+    const uint32_t sn = r[6];
+    const double p1 = min1(__dmul_rn(area_d(lp.lo, lp.hi), inv_area));
+    const double p2 = min1(__dmul_rn(area_d(m.lo, m.hi), inv_area));
     const double p3 = min1(__dmul_rn(area_d(sl, sh), inv_area));
-    double cost = __dadd_rn(__dadd_rn(__dmul_rn((double)ln, p1), __dmul_rn((double)mn, p2)), __dmul_rn((double)sn, p3));
-    if (ln == 0 || sn == 0) cost = __dmul_rn(cost, 0.8);
+    double cost = __dadd_rn(__dadd_rn(__dmul_rn((double)lp.n, p1), __dmul_rn((double)m.n, p2)), __dmul_rn((double)sn, p3));
+    if (lp.n == 0 || sn == 0) cost = __dmul_rn(cost, 0.8);
     if (cost < best) {
       best = cost;
       bi = i;
     }
   }
-  D.bcost[t] = best;
-  if (bi >= 0) {
-    // min + i * (max - min) / tries, evaluated in float
-    const float ext = __fsub_rn(nhi[a], nlo[a]);
-    D.bpos[t] = (double)__fadd_rn(nlo[a], __fdiv_rn(__fmul_rn((float)bi, ext), (float)tries));
-  } else {
-    D.bpos[t] = 0.0;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double oc = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (oc < best || (oc == best && oi < bi)) {
+      best = oc;
+      bi = oi;
+    }
+  }
+  if (lane == 0) {
+    D.bcost[3 * s + a] = best;
+    if (bi < tries) {
+      // min + i * (max - min) / tries, evaluated in float
+      const float ext = __fsub_rn(nhi[a], nlo[a]);
+      D.bpos[3 * s + a] = (double)__fadd_rn(nlo[a], __fdiv_rn(__fmul_rn((float)bi, ext), (float)tries));
+    } else {
+      D.bpos[3 * s + a] = 0.0;
+    }
   }
 }
 
@@ -626,6 +746,7 @@ cudaError_t build_accel_tree_gpu(const float *tbox, int64_t n, cudaStream_t st, 
   want(&D.hcoef, nn * 24);
   want(&D.hsplit, nn * 8);
   want(&D.hid, nn * 4);
+  want(&D.heads, nn * 4);
   want(&D.htries, nn * 4);
   want(&D.haxis, nn * 4);
   want(&D.hnl, nn * 4);
@@ -649,6 +770,7 @@ cudaError_t build_accel_tree_gpu(const float *tbox, int64_t n, cudaStream_t st, 
   want(&D.lmb, nn * 4);
   want(&D.dest, nn * 4);
   want(&D.err, 256);
+  want(&D.maxseg, 256);
   want(&D.n_leaves, 256);
   char *arena = nullptr;
   cudaError_t e = cudaMalloc(&arena, total);
@@ -716,8 +838,6 @@ cudaError_t build_accel_tree_gpu(const float *tbox, int64_t n, cudaStream_t st, 
     release();
     return e;
   }
-  int rounds = 1;
-  while (((int64_t)1 << rounds) < n) ++rounds;
   const unsigned gn = grid_of(n), gn1 = grid_of((int64_t)n1);
   e = cudaMemcpyAsync(d_tbox, tbox, nn * 24, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(D.err, 0, 4, st);
@@ -729,13 +849,19 @@ cudaError_t build_accel_tree_gpu(const float *tbox, int64_t n, cudaStream_t st, 
   }
   int depth = 0;
   for (; e == cudaSuccess; ++depth) {
+    if ((e = cudaMemsetAsync(D.maxseg, 0, 4, st)) != cudaSuccess) break;
     k_heads<<<gn1, kB, 0, st>>>(D);
     if ((e = scan64(D.cnt, (int64_t)n1, D.sums, st)) != cudaSuccess) break;
     if ((e = cudaMemcpyAsync(h_count, D.cnt + n, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
     if ((e = cudaMemcpyAsync(h_count + 1, D.err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync((char *)(h_count + 1) + 4, D.maxseg, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
     const int64_t level_nodes = (int64_t)h_count[0];
     if (level_nodes == 0 || (uint32_t)h_count[1] != 0) break;
+    // a middle element's chain stays inside its node: 2^rounds >= its size
+    const int64_t maxseg = (int64_t)(h_count[1] >> 32);
+    int rounds = 1;
+    while (((int64_t)1 << rounds) < maxseg) ++rounds;
     if ((e = grow(n_nodes + level_nodes)) != cudaSuccess) break;
     k_node_box<<<gn, kB, 0, st>>>(D);
     k_head_setup<<<gn1, kB, 0, st>>>(D, n_nodes, depth);
@@ -743,7 +869,7 @@ cudaError_t build_accel_tree_gpu(const float *tbox, int64_t n, cudaStream_t st, 
     if ((e = scan64(D.cnt2, (int64_t)n1, D.sums, st)) != cudaSuccess) break;
     k_bucket_init<<<4096, kB, 0, st>>>(D);
     k_bucket_fill<<<gn, kB, 0, st>>>(D);
-    k_score<<<grid_of(3 * n), kB, 0, st>>>(D);
+    k_score<<<grid_of(3 * 32 * level_nodes), kB, 0, st>>>(D, level_nodes);
     k_choose<<<gn, kB, 0, st>>>(D);
     k_classify<<<gn1, kB, 0, st>>>(D);
     if ((e = scan64(D.cnt, (int64_t)n1, D.sums, st)) != cudaSuccess) break;

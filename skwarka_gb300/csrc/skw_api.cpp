@@ -217,7 +217,15 @@ int skw_flat_tree_leaf_ranges(const skw_flat_tree *t, uint32_t leaf_word_a, uint
   return SKW_OK;
 }
 
+// take: the tree's host arrays move into the accelerator (the caller
+// destroys the tree next) instead of being copied.
+static int accel_from_flat(skw_ctx *ctx, skw_flat_tree *tree, bool take, skw_accel **out);
+
 int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_accel **out) {
+  return accel_from_flat(ctx, const_cast<skw_flat_tree *>(tree), false, out);
+}
+
+static int accel_from_flat(skw_ctx *ctx, skw_flat_tree *tree, bool take, skw_accel **out) {
   if (!ctx || !tree || !out) return fail(ctx, SKW_ERR_ARG, "null argument");
   *out = nullptr;
   const skw::FlatTree &ft = tree->ft;
@@ -267,11 +275,20 @@ int skw_accel_create_from_flat(skw_ctx *ctx, const skw_flat_tree *tree, skw_acce
   info.build_ms = tree->build_ms;
   info.built_on_device = tree->on_device ? 1 : 0;
   info.device_bytes = (int64_t)(nb + tb + ib + eb);
-  a->h_nodes = ft.nodes;
-  a->h_tris = ft.tris;
-  a->h_inst = ft.inst;
-  a->h_leaf_ext = ft.leaf_ext;
-  a->h_subtree_roots = ft.subtree_roots;
+  if (take) {
+    skw::FlatTree &mft = tree->ft;
+    a->h_nodes = std::move(mft.nodes);
+    a->h_tris = std::move(mft.tris);
+    a->h_inst = std::move(mft.inst);
+    a->h_leaf_ext = std::move(mft.leaf_ext);
+    a->h_subtree_roots = std::move(mft.subtree_roots);
+  } else {
+    a->h_nodes = ft.nodes;
+    a->h_tris = ft.tris;
+    a->h_inst = ft.inst;
+    a->h_leaf_ext = ft.leaf_ext;
+    a->h_subtree_roots = ft.subtree_roots;
+  }
   // instances need the stack of the top tree and of the deepest subtree at once
   if (a->d_inst) skw::register_instances(a->d_nodes, a->d_inst, a->d_leaf_ext);
   skw::register_ray_counter(a->d_nodes, a->d_traced);
@@ -289,7 +306,7 @@ int skw_accel_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
   skw_flat_tree *t = nullptr;
   int rc = skw_flat_tree_build_device(ctx, meshes, n_meshes, prims, n_prims, kDeviceBuildMin, &t, nullptr);
   if (rc != SKW_OK) return rc;
-  rc = skw_accel_create_from_flat(ctx, t, out);
+  rc = accel_from_flat(ctx, t, true, out);
   skw_flat_tree_destroy(t);
   return rc;
 }
