@@ -952,7 +952,7 @@ def main():
                     "d2h_bytes_per_step": args.rays * 16},
             "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "clocks": clk.summary(), "gpu_launches": launches,
             "wall_s_timed_region": wall, "anyhit_mrays_s": anyhit, "render": render, "specular": specular, "batch": batch, "adjoint": adjoint, "photon": photon,
-            "accel": {k: acc.info[k] for k in ("n_nodes", "max_depth", "build_ms", "device_bytes")}}
+            "accel": {k: acc.info[k] for k in ("n_nodes", "max_depth", "build_ms", "built_on_device", "device_bytes")}}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()
