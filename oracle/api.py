@@ -76,6 +76,7 @@ _REF_SIGS = [
                                         C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P,
                                         C.c_int]),
     ("skw_ref_luminance_weights", None, [_P]),
+    ("skw_ref_pbrt_rgb", None, [C.c_int, _P, _i64, _P]),
     ("skw_ref_render_photon", C.c_int, [C.c_int, _P, _P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, C.c_double,
                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, C.c_int,
                                         C.c_double, _P, _P, _P]),
@@ -244,6 +245,14 @@ class Reference:
 
     def accel(self, meshes, normals=None, mesh_of=None, xforms=None):
         return RefAccel(self.lib, meshes, normals, mesh_of, xforms)
+
+    def pbrt_rgb(self, kind: int, rgb) -> np.ndarray:
+        """The PBRT importer's colour conversion of float RGB triples (kind 0
+        a reflectance, 1 an emission): (n, 3) float64."""
+        x = np.ascontiguousarray(np.asarray(rgb, np.float32).reshape(-1, 3))
+        out = np.zeros(x.shape, np.float64)
+        self.lib.skw_ref_pbrt_rgb(kind, x.ctypes.data, x.shape[0], out.ctypes.data)
+        return out
 
     def kdtree(self, pos, normal_ids=None, dir_ids=None):
         return RefKD(self.lib, pos, normal_ids, dir_ids)

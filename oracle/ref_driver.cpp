@@ -989,6 +989,30 @@ void skw_ref_color_stage(int stage, const double *in, int64_t n, double *out) {
   }
 }
 
+// The PBRT importer's colour parameters (PbrtImport::ParamSet,
+// CADImport/SceneImporters/PbrtSceneImporter/PbrtParamSet.cpp:99-129) for n
+// float RGB triples: kind 0 a reflectance (AddRGBSpectrumCoef: a grey
+// triple as is, else sRGB with the E white point, then XYZ ->
+// coefficients), kind 1 an emission (AddRGBSpectrum: sRGB with the D65
+// white point, then XYZ -> spectrum); kind 2 that emission's XYZ.
+void skw_ref_pbrt_rgb(int kind, const float *rgb, int64_t n, double *out) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float r = rgb[3 * i], g = rgb[3 * i + 1], b = rgb[3 * i + 2];
+    if (kind == 0) {
+      SpectrumCoef_d s = (r == g && r == b)
+                             ? SpectrumCoef_d(r)
+                             : SpectrumRoutines::XYZToSpectrumCoef(global_sRGB_E_ColorSystem.RGB_To_XYZ(RGBColor_d(r, g, b)));
+      for (int k = 0; k < 3; ++k) out[3 * i + k] = s[k];
+    } else if (kind == 1) {
+      Spectrum_d s = SpectrumRoutines::XYZToSpectrum(global_sRGB_D65_ColorSystem.RGB_To_XYZ(RGBColor_d(r, g, b)));
+      for (int k = 0; k < 3; ++k) out[3 * i + k] = s[k];
+    } else {  // kind 2: the first stage of kind 1 alone (RGB -> XYZ, D65)
+      XYZColor_d x = global_sRGB_D65_ColorSystem.RGB_To_XYZ(RGBColor_d(r, g, b));
+      for (int k = 0; k < 3; ++k) out[3 * i + k] = x[k];
+    }
+  }
+}
+
 // Row Y of the reference's spectrum-to-XYZ matrix (its luminance weights).
 void skw_ref_luminance_weights(double *out) {
   for (int k = 0; k < 3; ++k) {
