@@ -6,8 +6,9 @@ transform semantics, parameter types and defaults, and the same mapping of
 PBRT's shapes, materials, lights, camera, film and volumes onto the
 renderer's types, for the part of PBRT that the renderer here implements:
 
-* shapes: ``trianglemesh`` (P, indices, N) and ``sphere`` (the reference's
-  sphere mesh at 5 subdivisions, ShapeFactory.h:62-78) -- meshes in world
+* shapes: ``trianglemesh`` (P, indices, N), ``sphere`` (the reference's
+  sphere mesh at 5 subdivisions, ShapeFactory.h:62-78), ``disk`` and
+  ``cylinder`` (the reference's 360-step meshes) -- meshes in world
   space as the reference builds them (Convert<float>(Transform(P)) in
   double); ``ReverseOrientation`` and orientation-inverting transforms flip
   a mesh's winding (the reference's TriangleMesh orientation flag);
@@ -157,6 +158,60 @@ def apply_normal(m: np.ndarray, n: np.ndarray) -> np.ndarray:
     x, y, z = n[:, 0], n[:, 1], n[:, 2]
     out = np.stack([(inv[0, i] * x + inv[1, i] * y) + inv[2, i] * z for i in range(3)], 1)
     return out / np.sqrt((out * out).sum(1))[:, None]
+
+
+# ------------------------------------------------------------------ shapes --
+def disk_mesh(m: np.ndarray, max_phi: float, inner: float, subdivisions: int = 360):
+    """Disk::BuildMesh (Shapes/Disk.cpp:57-171) through transform m: the
+    unit disk (or the ring from `inner` to 1) in the z = 0 plane, its phi
+    stepped by accumulation; flat (no shading normals).  Returns float32
+    vertices, int32 triangles."""
+    d_phi = max_phi / subdivisions
+    ring, phi = [], 0.0
+    for _ in range(subdivisions + 1):
+        ring.append((math.cos(phi), math.sin(phi)))
+        phi += d_phi
+    c = np.array(ring, np.float64)
+    i = np.arange(subdivisions)
+    if inner == 0.0:
+        pts = np.concatenate([[[0.0, 0.0, 0.0]], np.stack([c[:, 0], c[:, 1], np.zeros(len(c))], 1)])
+        tris = np.stack([np.zeros(subdivisions, np.int64), i + 1, i + 2], 1)
+    else:
+        pts = np.empty((2 * len(c), 3))
+        pts[0::2] = np.stack([inner * c[:, 0], inner * c[:, 1], np.zeros(len(c))], 1)
+        pts[1::2] = np.stack([c[:, 0], c[:, 1], np.zeros(len(c))], 1)
+        tris = np.concatenate([np.stack([2 * i, 2 * i + 1, 2 * i + 3], 1),
+                               np.stack([2 * i + 3, 2 * i + 2, 2 * i], 1)], 1).reshape(-1, 3)
+    return apply_point(m, pts).astype(np.float32), tris.astype(np.int32)
+
+
+def cylinder_mesh(m: np.ndarray, max_phi: float, subdivisions: int = 360):
+    """Cylinder::BuildMesh (Shapes/Cylinder.cpp:48-103) through transform m:
+    the unit cylinder from z = 0 to 1, smooth.  Returns float32 vertices,
+    int32 triangles and float32 shading normals (negated for a mirroring m,
+    as the reference does)."""
+    d_phi = max_phi / subdivisions
+    ang, phi = [], 0.0
+    for _ in range(subdivisions + 1):
+        ang.append((math.cos(phi), math.sin(phi)))
+        phi += d_phi
+    c = np.array(ang, np.float64)
+    pts = np.empty((2 * len(c), 3))
+    pts[0::2] = np.stack([c[:, 0], c[:, 1], np.zeros(len(c))], 1)
+    pts[1::2] = np.stack([c[:, 0], c[:, 1], np.ones(len(c))], 1)
+    sign = -1.0 if inverts_orientation(m) else 1.0
+    nrm = sign * apply_normal(m, np.stack([c[:, 0], c[:, 1], np.zeros(len(c))], 1))
+    i = np.arange(subdivisions)
+    tris = np.concatenate([np.stack([2 * i + 1, 2 * i, 2 * i + 2], 1),
+                           np.stack([2 * i + 2, 2 * i + 3, 2 * i + 1], 1)], 1).reshape(-1, 3)
+    return (apply_point(m, pts).astype(np.float32), tris.astype(np.int32),
+            np.repeat(nrm, 2, axis=0).astype(np.float32))
+
+
+def _max_phi(phimax_deg: float) -> float:
+    """The factories pass phimax * INV_PI (ShapeFactory.h:86, :100), which the
+    shapes clamp to [0, 2 pi]; kept as the reference computes it."""
+    return max(0.0, min(2.0 * math.pi, phimax_deg * (1.0 / math.pi)))
 
 
 # ------------------------------------------------------------- the parser --
@@ -514,6 +569,17 @@ class _Importer:
             sign = -1.0 if inverts_orientation(sm) else 1.0
             normals = (sign * apply_normal(sm, sv)).astype(np.float32)
             flip = self.gs.reverse != inverts_orientation(sm)
+        elif name == "disk":
+            height, radius = p.float1("height", 0.0), p.float1("radius", 1.0)
+            inner = p.float1("innerradius", 0.0)
+            dm = m @ translate((0.0, 0.0, height)) @ scale((radius, radius, 1.0))
+            v, t = disk_mesh(dm, _max_phi(p.float1("phimax", 360.0)), inner / radius)
+            flip = self.gs.reverse != inverts_orientation(dm)
+        elif name == "cylinder":
+            radius, zmin, zmax = p.float1("radius", 1.0), p.float1("zmin", -1.0), p.float1("zmax", 1.0)
+            cm = m @ translate((0.0, 0.0, zmin)) @ scale((radius, radius, zmax - zmin))
+            v, t, normals = cylinder_mesh(cm, _max_phi(p.float1("phimax", 360.0)))
+            flip = self.gs.reverse != inverts_orientation(cm)
         else:
             self.warn(f"shape \"{name}\" is not supported")
             return

@@ -1,7 +1,7 @@
 """PBRT scene import (skwarka_gb300.pbrt), on the CPU: colour conversions
 pinned to the reference's own code, the directives' transform semantics,
 the camera and film, materials and their PBRT defaults, lights, volumes,
-object instancing, orientation, Include, and the reported unsupported
+object instancing, orientation, the disk and cylinder meshes, Include, and the reported unsupported
 features."""
 import math
 import os
@@ -214,3 +214,28 @@ def test_include_and_errors(tmp_path):
         pbrt.loads('WorldBegin\nShape "sphere"\nWorldEnd')  # no lights
     s = pbrt.loads(HEADER + 'Shape "cone"\nLightSource "spot"\nShape "sphere"\nWorldEnd')
     assert any('shape "cone"' in w for w in s.warnings) and any('light "spot"' in w for w in s.warnings)
+
+
+def test_disk_and_cylinder_are_the_reference_meshes():
+    s = pbrt.loads(HEADER + '''
+Shape "disk" "float radius" 2 "float height" 1
+Shape "disk" "float innerradius" 0.5 "float phimax" 180
+Shape "cylinder" "float radius" 0.5 "float zmin" 0 "float zmax" 2
+WorldEnd''')
+    full, ring, cyl = s.prims
+    # 360 segments; the factories pass phimax / pi (clamped to 2 pi): a full turn at 180 degrees too
+    assert full.mesh.triangles.shape == (360, 3) and ring.mesh.triangles.shape == (720, 3)
+    assert np.allclose(full.mesh.vertices[0], (0, 0, 1)) and np.allclose(np.abs(full.mesh.vertices[1:, :2]).max(), 2)
+    r = np.linalg.norm(ring.mesh.vertices[:, :2], axis=1)
+    assert np.allclose(r[0::2], 0.5, atol=1e-6) and np.allclose(r[1::2], 1.0, atol=1e-6)
+    assert np.allclose(ring.mesh.vertices[-1], ring.mesh.vertices[1], atol=1e-6)  # the last step closes the ring
+    for p in (full, ring):  # flat disks face +z and carry no shading normals
+        v, t = p.mesh.vertices.astype(np.float64), p.mesh.triangles
+        n = np.cross(v[t[:, 1]] - v[t[:, 0]], v[t[:, 2]] - v[t[:, 0]])
+        assert (n[:, 2] > 0).all() and p.vertex_normals is None
+    v, t = cyl.mesh.vertices.astype(np.float64), cyl.mesh.triangles
+    assert np.allclose([v[:, 2].min(), v[:, 2].max()], [0, 2]) and np.allclose(np.linalg.norm(v[:, :2], axis=1), 0.5)
+    n = np.cross(v[t[:, 1]] - v[t[:, 0]], v[t[:, 2]] - v[t[:, 0]])
+    c = v[t].mean(1)
+    assert (np.einsum("ij,ij->i", n[:, :2], c[:, :2]) > 0).all()  # outward
+    assert np.allclose(cyl.vertex_normals[:, :2] * 0.5, v[:, :2], atol=1e-6)
