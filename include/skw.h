@@ -332,9 +332,12 @@ int skw_nearest(skw_kdtree *tree, const double *q, const double *qn, int64_t nq,
  * SpecularReflection(kd, FresnelDielectric(refractive_index, 1)) +
  * SpecularTransmission(ks, refractive_index, 1); kd / ks black = component absent. */
 #define SKW_MATERIAL_TRANSPARENT 4
-/* SubstrateMaterial (Raytracer/Materials/SubstrateMaterial.cpp:42-72, the
- * isotropic form): FresnelBlend<BlinnDistribution>(kd, ks) with exponent
- * 1 / clamp(roughness, 0.001, 1); kd, ks clamped to [0, 1]. */
+/* SubstrateMaterial (Raytracer/Materials/SubstrateMaterial.cpp:42-72):
+ * with v_roughness <= 0 the one-roughness form, FresnelBlend<BlinnDistribution>
+ * (kd, ks) with exponent 1 / clamp(roughness, 0.001, 1); with v_roughness > 0
+ * the two-roughness form, FresnelBlend<AnisotropicDistribution> (Ashikhmin
+ * and Shirley) with exponents 1 / clamp(roughness) along the shading tangent
+ * and 1 / clamp(v_roughness) across it; kd, ks clamped to [0, 1]. */
 #define SKW_MATERIAL_SUBSTRATE 5
 /* UberMaterial (Raytracer/Materials/UberMaterial.cpp:39-85): with op =
  * clamp(opacity, 0, 1): SpecularTransmission(1 - op, refractive_index) when
@@ -365,6 +368,7 @@ typedef struct skw_material {
   float opacity[3];         /* SKW_MATERIAL_UBER: opacity (1: opaque) */
   int32_t mix[2];           /* SKW_MATERIAL_MIX: the two materials */
   float mix_scale[3];       /* SKW_MATERIAL_MIX: the first material's scale */
+  float v_roughness;        /* SKW_MATERIAL_SUBSTRATE: > 0 selects the two-roughness form */
 } skw_material;
 
 /* A measured BRDF in the MERL binary layout (MERLMeasuredData(std::istream&),
@@ -396,6 +400,15 @@ typedef struct skw_render_primitive {
                                     then the geometric normal shades (use_shading_normals = false) */
   const float *triangle_albedo;  /* optional per-triangle RGB replacing the material's kd */
   float emission[3];             /* DiffuseAreaLightSource radiance; all 0 = not a light */
+  /* The shading tangent (the BSDF frame's first axis, which anisotropic
+   * BxDFs read; TriangleMesh::ComputeDifferentialGeometry,
+   * TriangleMesh.cpp:490-528): interpolated per-vertex tangents (mesh
+   * space) if given, else the direction of increasing u of per-triangle uvs
+   * (6 floats: u0 v0 u1 v1 u2 v2) if given, else -- and where the uvs are
+   * degenerate -- CoordinateSystem of the shading normal; made
+   * perpendicular to the shading normal. */
+  const float *vertex_tangents;
+  const float *triangle_uvs;
 } skw_render_primitive;
 
 typedef struct skw_point_light {

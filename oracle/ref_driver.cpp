@@ -551,6 +551,7 @@ struct RefMaterialIn {
   float opacity[3];        // kind 6: UberMaterial
   int32_t mix[2];          // kind 7: MixMaterial
   float mix_scale[3];      // kind 7: MixMaterial
+  float v_roughness;       // kind 5: > 0 the two-roughness SubstrateMaterial
 };
 struct RefPrimIn {
   int32_t mesh;
@@ -559,6 +560,8 @@ struct RefPrimIn {
   const float *vertex_normals;
   const float *triangle_albedo;
   float emission[3];
+  const float *vertex_tangents;  // TriangleMesh tangents (mesh space) or NULL
+  const float *triangle_uvs;     // 6 floats per triangle (MeshTriangle::m_uvs) or NULL
 };
 
 static intrusive_ptr<const Texture<SpectrumCoef_d>> const_rgb(const float *v) {
@@ -583,7 +586,10 @@ static intrusive_ptr<const Material> make_material(const RefMaterialIn *material
   } else if (M.kind == 4) {
     mat.reset(new TransparentMaterial(const_rgb(M.kd), const_rgb(M.ks), (double)M.refractive_index));
   } else if (M.kind == 5) {
-    mat.reset(new SubstrateMaterial(kd, const_rgb(M.ks), const_d(M.roughness)));
+    if (M.v_roughness > 0.0f)
+      mat.reset(new SubstrateMaterial(kd, const_rgb(M.ks), const_d(M.roughness), const_d(M.v_roughness)));
+    else
+      mat.reset(new SubstrateMaterial(kd, const_rgb(M.ks), const_d(M.roughness)));
   } else if (M.kind == 6) {
     mat.reset(new UberMaterial(kd, const_rgb(M.ks), const_rgb(M.kr), const_d(M.roughness), const_rgb(M.opacity),
                                (double)M.refractive_index));
@@ -617,13 +623,26 @@ static intrusive_ptr<const Scene> make_scene(int n_meshes, const float *const *v
     for (int64_t i = 0; i < n_verts[m]; ++i)
       v[(size_t)i] = Point3D_f(verts[m][3 * i], verts[m][3 * i + 1], verts[m][3 * i + 2]);
     std::vector<MeshTriangle> t((size_t)n_tris[m]);
-    for (int64_t i = 0; i < n_tris[m]; ++i) t[(size_t)i] = MeshTriangle(tris[m][3 * i], tris[m][3 * i + 1], tris[m][3 * i + 2]);
+    for (int64_t i = 0; i < n_tris[m]; ++i) {
+      t[(size_t)i] = MeshTriangle(tris[m][3 * i], tris[m][3 * i + 1], tris[m][3 * i + 2]);
+      if (P.triangle_uvs)
+        for (int k = 0; k < 3; ++k)
+          t[(size_t)i].m_uvs[k] = Point2D_f(P.triangle_uvs[6 * i + 2 * k], P.triangle_uvs[6 * i + 2 * k + 1]);
+    }
     intrusive_ptr<TriangleMesh> mesh;
+    std::vector<Vector3D_f> tan;
+    if (P.vertex_tangents) {
+      tan.resize((size_t)n_verts[m]);
+      for (int64_t i = 0; i < n_verts[m]; ++i)
+        tan[(size_t)i] = Vector3D_f(P.vertex_tangents[3 * i], P.vertex_tangents[3 * i + 1], P.vertex_tangents[3 * i + 2]);
+    }
     if (P.vertex_normals) {
       std::vector<Vector3D_f> nrm((size_t)n_verts[m]);
       for (int64_t i = 0; i < n_verts[m]; ++i)
         nrm[(size_t)i] = Vector3D_f(P.vertex_normals[3 * i], P.vertex_normals[3 * i + 1], P.vertex_normals[3 * i + 2]);
-      mesh.reset(new TriangleMesh(v, t, nrm, std::vector<Vector3D_f>(), true, false));
+      mesh.reset(new TriangleMesh(v, t, nrm, tan, true, false));
+    } else if (!tan.empty()) {
+      mesh.reset(new TriangleMesh(v, t, std::vector<Vector3D_f>(), tan, false, false));
     } else {
       mesh.reset(new TriangleMesh(v, t, false, false));
     }

@@ -163,6 +163,7 @@ struct Layer {
   float exponent, on_a, on_b;
   float ior;    // dielectric Fresnel (inside index; outside 1)
   float pdiff;  // kSubstrate: probability of sampling the diffuse lobe
+  float ev;     // kSubstrate: < 0 Blinn(exponent), else Ashikhmin-Shirley(exponent, ev)
   V3 eta, k2;
   MerlDev merl;
   V3 scale;
@@ -270,6 +271,56 @@ __device__ __forceinline__ float diffuse_pdf(V3 wi, V3 wo) {  // BxDF::PDF (Core
 // D(h) / (4 |o.h| max(|cos o|, |cos i|)).  The lobe is sampled as a mixture:
 // the cosine lobe with probability pdiff (on wi's side), the Blinn half
 // vector otherwise; the density is the mixture's (0 across hemispheres).
+// AnisotropicDistribution (MicrofacetDistributions/AnisotropicDistribution.h):
+// Ashikhmin and Shirley's half-vector distribution with exponents eu along
+// the shading tangent (x) and ev across it (y).  Evaluate: sqrt((eu + 2)
+// (ev + 2)) / 2 pi cos^e, e = (eu hx^2 + ev hy^2) / (1 - cos^2), 0 at the
+// pole; PDF: sqrt((eu + 1)(ev + 1)) cos^e / (8 pi |wi.h|); Sample: the
+// first quadrant's phi = atan(sqrt((eu + 1) / (ev + 1)) tan(pi u / 2)) (pi u
+// / 2 when eu == ev) mirrored into the quadrant u0 selects, cos theta =
+// u1^(1 / (eu cos^2 phi + ev sin^2 phi + 1)), the half vector on wi's side.
+__device__ __forceinline__ float aniso_d(float eu, float ev, V3 h) {
+  const float ct = fabsf(h.z), d = 1.0f - ct * ct;
+  if (!(d > 0.0f)) return 0.0f;
+  const float e = (eu * h.x * h.x + ev * h.y * h.y) / d;
+  return sqrtf((eu + 2.0f) * (ev + 2.0f)) * (0.5f * kInvPi) * powf(ct, e);
+}
+__device__ __forceinline__ float aniso_pdf(float eu, float ev, V3 wi, V3 wo) {
+  const V3 h = normalized(wi + wo);
+  const float ct = fabsf(h.z), ds = 1.0f - ct * ct;
+  if (!(ds > 0.0f)) return 0.0f;
+  const float e = (eu * h.x * h.x + ev * h.y * h.y) / ds;
+  return sqrtf((eu + 1.0f) * (ev + 1.0f)) * powf(ct, e) / (2.0f * kPi * 4.0f * fabsf(dot(wi, h)));
+}
+__device__ __forceinline__ bool aniso_sample(float eu, float ev, V3 wi, float u0, float u1, V3 &wo) {
+  float s0;
+  int q;
+  if (u0 < 0.25f) {
+    s0 = 4.0f * u0;
+    q = 0;
+  } else if (u0 < 0.5f) {
+    s0 = 4.0f * (0.5f - u0);
+    q = 1;
+  } else if (u0 < 0.75f) {
+    s0 = 4.0f * (u0 - 0.5f);
+    q = 2;
+  } else {
+    s0 = 4.0f * (1.0f - u0);
+    q = 3;
+  }
+  float phi = eu == ev ? kPi * s0 * 0.5f : atanf(sqrtf((eu + 1.0f) / (ev + 1.0f)) * tanf(kPi * s0 * 0.5f));
+  const float cp = cosf(phi), sp = sinf(phi);
+  const float ct = powf(u1, 1.0f / (eu * cp * cp + ev * sp * sp + 1.0f));
+  if (q == 1) phi = kPi - phi;
+  else if (q == 2) phi += kPi;
+  else if (q == 3) phi = 2.0f * kPi - phi;
+  const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+  V3 h = v3(st * cosf(phi), st * sinf(phi), ct);
+  if (wi.z * h.z < 0.0f) h.z = -h.z;
+  wo = h * (2.0f * dot(wi, h)) - wi;
+  return !(wi.z * wo.z < 0.0f);
+}
+
 __device__ V3 fb_eval(const Layer &b, V3 wi, V3 wo) {
   const float ci = fabsf(wi.z), co = fabsf(wo.z);
   const V3 h = normalized(wi + wo);
@@ -281,12 +332,14 @@ __device__ V3 fb_eval(const Layer &b, V3 wi, V3 wo) {
   const float m = 1.0f - fminf(1.0f, fabsf(ch)), m5 = m * m * m * m * m;
   const V3 schlick = b.ks + (one - b.ks) * m5;
   const float denom = 4.0f * fabsf(ch) * fmaxf(co, ci);
-  const V3 specular = denom > 0.0f ? schlick * (blinn_d(b.exponent, h) / denom) : v3(0, 0, 0);
+  const float dh = b.ev < 0.0f ? blinn_d(b.exponent, h) : aniso_d(b.exponent, b.ev, h);
+  const V3 specular = denom > 0.0f ? schlick * (dh / denom) : v3(0, 0, 0);
   return diffuse + specular;
 }
 __device__ float fb_pdf(const Layer &b, V3 wi, V3 wo) {
   if (wi.z * wo.z < 0.0f) return 0.0f;
-  return b.pdiff * fabsf(wo.z) * kInvPi + (1.0f - b.pdiff) * microfacet_pdf(b, wi, wo);
+  const float pm = b.ev < 0.0f ? microfacet_pdf(b, wi, wo) : aniso_pdf(b.exponent, b.ev, wi, wo);
+  return b.pdiff * fabsf(wo.z) * kInvPi + (1.0f - b.pdiff) * pm;
 }
 __device__ bool fb_sample(const Layer &b, V3 wi, float u0, float u1, V3 &wo) {
   if (u0 < b.pdiff) {
@@ -294,7 +347,8 @@ __device__ bool fb_sample(const Layer &b, V3 wi, float u0, float u1, V3 &wo) {
     if (wi.z < 0.0f) wo.z = -wo.z;
     return true;
   }
-  return blinn_sample(b.exponent, wi, fminf((u0 - b.pdiff) / (1.0f - b.pdiff), 0.99999994f), u1, wo);
+  const float us = fminf((u0 - b.pdiff) / (1.0f - b.pdiff), 0.99999994f);
+  return b.ev < 0.0f ? blinn_sample(b.exponent, wi, us, u1, wo) : aniso_sample(b.exponent, b.ev, wi, us, u1, wo);
 }
 
 // ------------------------------------------------------- measured BRDF --
@@ -447,6 +501,7 @@ __device__ Layer make_layer(const DevMaterial &m) {
   l.on_b = m.on_b;
   l.ior = m.ior;
   l.pdiff = m.pdiff;
+  l.ev = m.ev;
   l.eta = load3(m.eta);
   l.k2 = load3(m.k2);
   l.merl = m.merl;
@@ -621,6 +676,7 @@ struct Hit {
   V3 p, ng, ns;
   int g;      // global triangle
   int prim;   // primitive
+  float b1, b2;  // barycentrics of vertices 1 and 2 (where the primitive interpolates vertex data)
 };
 
 // CoreUtils::GetNextMinT (CoreUtils.h:139-149) for a ray leaving the hit
@@ -721,6 +777,49 @@ __device__ __forceinline__ float next_min_t(const SceneDev &S, const Hit &h, V3 
   return fmaxf(0.0f, __fadd_ru(__fadd_ru(t, et), 1e-14f));
 }
 
+// MathRoutines::CoordinateSystem (Math/MathRoutines.h:298-313): the first
+// tangent of the frame it builds around a unit vector.
+__device__ __forceinline__ V3 coordinate_tangent(V3 n) {
+  if (fabsf(n.x) > fabsf(n.y)) {
+    const float il = 1.0f / sqrtf(n.x * n.x + n.z * n.z);
+    return v3(-n.z * il, 0.0f, n.x * il);
+  }
+  const float il = 1.0f / sqrtf(n.y * n.y + n.z * n.z);
+  return v3(0.0f, n.z * il, -n.y * il);
+}
+
+// The differential geometry's tangent (TriangleMesh::
+// ComputeDifferentialGeometry, TriangleMesh.cpp:490-528): interpolated
+// vertex tangents; else the direction of increasing u from the triangle's
+// uvs; else (no uvs, or degenerate ones) CoordinateSystem of the shading
+// normal; then made perpendicular to the shading normal, (n x t) x n.
+__device__ V3 shading_tangent(const SceneDev &S, const Hit &h) {
+  const V3 n = h.ns;
+  const int mode = S.prim_frame ? S.prim_frame[h.prim] : 0;
+  V3 t;
+  if (mode == 1) {
+    const int i0 = S.tri_vidx[3 * h.g], i1 = S.tri_vidx[3 * h.g + 1], i2 = S.tri_vidx[3 * h.g + 2];
+    t = load3(S.vtan + 3 * i0) * (1.0f - h.b1 - h.b2) + load3(S.vtan + 3 * i1) * h.b1 +
+        load3(S.vtan + 3 * i2) * h.b2;
+  } else if (mode == 2) {
+    const float *uv = S.tri_uv + 6 * h.g;
+    const float du1 = uv[0] - uv[4], du2 = uv[2] - uv[4], dv1 = uv[1] - uv[5], dv2 = uv[3] - uv[5];
+    const float det = du1 * dv2 - dv1 * du2;
+    if (fabsf(det) < 1e-12f) {
+      t = coordinate_tangent(n);
+    } else {
+      const int i0 = S.tri_vidx[3 * h.g], i1 = S.tri_vidx[3 * h.g + 1], i2 = S.tri_vidx[3 * h.g + 2];
+      const V3 p0 = load3(S.vpos + 3 * i0), p1 = load3(S.vpos + 3 * i1), p2 = load3(S.vpos + 3 * i2);
+      t = ((p0 - p2) * dv2 - (p1 - p2) * dv1) * (1.0f / det);
+    }
+  } else {
+    t = coordinate_tangent(n);
+  }
+  const V3 t2 = cross(n, t);
+  if (dot(t2, t2) > 1e-20f) return normalized(cross(t2, n));
+  return coordinate_tangent(n);
+}
+
 // The material's BSDF at a hit (Material::GetBSDF).  MixMaterial
 // (Materials/MixMaterial.cpp:29-57): the first material's components scaled
 // by the mix's scale s and the second's by 1 - s, a side whose scale is
@@ -731,10 +830,8 @@ __device__ Bsdf make_bsdf(const SceneDev &S, const Hit &h, int prim) {
   Bsdf b;
   b.ng = h.ng;
   b.n = h.ns;
-  // Any frame around the shading normal: all the BxDFs here are isotropic.
-  const V3 a = fabsf(b.n.x) > 0.9f ? v3(0, 1, 0) : v3(1, 0, 0);
-  b.e1 = normalized(cross(a, b.n));
-  b.e2 = cross(b.n, b.e1);
+  b.e1 = shading_tangent(S, h);
+  b.e2 = cross(b.n, b.e1);  // BSDF::BSDF (Core/BSDF.h:182-192): e2 = n x tangent
   b.m1 = nullptr;
   b.s1 = v3(0, 0, 0);
   if (m.kind == kMix) {
@@ -839,16 +936,20 @@ __device__ Hit make_hit(const SceneDev &S, V3 o, V3 d, float t, int prim, int tr
   h.p = o + d * t;
   h.ng = normalized(cross(p1 - p0, p2 - p0));
   h.ns = h.ng;
-  if (S.prim_has_normals[prim]) {
-    // barycentrics of the hit point (Moller-Trumbore), then the
-    // interpolated vertex normal (TriangleMesh.cpp:478-484)
+  h.b1 = h.b2 = 0.0f;
+  const bool normals = S.prim_has_normals[prim] != 0;
+  if (normals || (S.prim_frame && S.prim_frame[prim] == 1)) {
+    // barycentrics of the hit point (Moller-Trumbore)
     const V3 e1 = p1 - p0, e2 = p2 - p0, s1 = cross(d, e2);
     const float inv = 1.0f / dot(s1, e1);
     const V3 dd = o - p0;
-    const float b1 = dot(dd, s1) * inv;
-    const float b2 = dot(d, cross(dd, e1)) * inv;
-    const float b0 = 1.0f - b1 - b2;
-    const V3 n = load3(S.vnrm + 3 * i0) * b0 + load3(S.vnrm + 3 * i1) * b1 + load3(S.vnrm + 3 * i2) * b2;
+    h.b1 = dot(dd, s1) * inv;
+    h.b2 = dot(d, cross(dd, e1)) * inv;
+  }
+  if (normals) {
+    // the interpolated vertex normal (TriangleMesh.cpp:478-484)
+    const float b0 = 1.0f - h.b1 - h.b2;
+    const V3 n = load3(S.vnrm + 3 * i0) * b0 + load3(S.vnrm + 3 * i1) * h.b1 + load3(S.vnrm + 3 * i2) * h.b2;
     h.ns = normalized(n);
   }
   return h;

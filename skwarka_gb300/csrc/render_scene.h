@@ -42,6 +42,7 @@ struct DevMaterial {
   float pdiff;         // kSubstrate: probability of sampling the diffuse lobe
   int32_t mix[2];      // kMix: the two materials (indices; mix[1] may be -1)
   float mix_scale[3];  // kMix: the first material's scale (the second's is 1 - scale)
+  float ev;            // kSubstrate: < 0 Blinn (exponent); else Ashikhmin-Shirley with exponents (exponent, ev)
 };
 
 struct AreaLight {
@@ -87,6 +88,13 @@ struct SceneDev {
   const int32_t *prim_light;      // area light index or -1
   const int32_t *prim_has_normals;
   const int32_t *prim_xform;      // 1 where the primitive has a mesh-to-world matrix
+  // The shading tangent's source per primitive (0: CoordinateSystem of the
+  // shading normal, 1: vertex tangents, 2: triangle uvs), the vertex
+  // tangents (3 floats per global vertex, world; null if no primitive has
+  // them) and the triangle uvs (6 floats per global triangle; null if none).
+  const int32_t *prim_frame;
+  const float *vtan;
+  const float *tri_uv;
   // Primitives whose mesh is shared (the accelerator traces them in mesh
   // space through their world-to-mesh matrix): prim_inst[p] = 1, their
   // world-to-mesh matrices (16 doubles per primitive, row-major, the

@@ -80,6 +80,19 @@ void xform_normal(const double *inv, const float *n, float *out) {
   for (int k = 0; k < 3; ++k) out[k] = (float)(l > 0 ? v[k] / l : v[k]);
 }
 
+// Transform::operator()(Vector3D) on a mesh tangent, normalised (the
+// world-space tangent of a transformed primitive's differential geometry).
+void xform_tangent(const double *m, const float *t, float *out) {
+  double v[3] = {t[0], t[1], t[2]};
+  if (m) {
+    v[0] = m[0] * t[0] + m[1] * t[1] + m[2] * t[2];
+    v[1] = m[4] * t[0] + m[5] * t[1] + m[6] * t[2];
+    v[2] = m[8] * t[0] + m[9] * t[1] + m[10] * t[2];
+  }
+  const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  for (int k = 0; k < 3; ++k) out[k] = (float)(l > 0 ? v[k] / l : v[k]);
+}
+
 // Vector3D<float>::Normalized (Math/Vector3D.h:259-276), as TriangleMesh
 // stores its shading normals (TriangleMesh.cpp:208-213): the squared length
 // and its square root in float, the reciprocal in double, each coordinate
@@ -145,7 +158,7 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
     return rc;
   }
   // Mesh-order geometry.
-  std::vector<float> vpos, vnrm, albedo, vpos_mesh;
+  std::vector<float> vpos, vnrm, vtan, tri_uv, albedo, vpos_mesh;
   std::vector<double> prim_w2m;
   std::vector<int32_t> prim_inst((size_t)std::max(n_prims, 1), 0);
   {
@@ -166,11 +179,16 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
   const bool instanced = !prim_w2m.empty();
   std::vector<int32_t> tri_vidx, prim_tri_offset((size_t)std::max(n_prims, 1)), prim_material((size_t)std::max(n_prims, 1)),
       prim_light((size_t)std::max(n_prims, 1), -1), prim_has_normals((size_t)std::max(n_prims, 1), 0),
-      prim_xform((size_t)std::max(n_prims, 1), 0);
+      prim_xform((size_t)std::max(n_prims, 1), 0), prim_frame((size_t)std::max(n_prims, 1), 0);
   // Per-triangle albedo is always present (NaN = the material's kd) so that
   // skw_scene_set_triangle_albedo can replace it.
   bool any_albedo = true, any_normals = false;
-  for (int32_t p = 0; p < n_prims; ++p) any_normals |= prims[p].vertex_normals != nullptr;
+  bool any_tangents = false, any_uvs = false;
+  for (int32_t p = 0; p < n_prims; ++p) {
+    any_normals |= prims[p].vertex_normals != nullptr;
+    any_tangents |= prims[p].vertex_tangents != nullptr;
+    any_uvs |= prims[p].vertex_tangents == nullptr && prims[p].triangle_uvs != nullptr;
+  }
   std::vector<skw::AreaLight> lights;
   std::vector<int32_t> light_tri;
   std::vector<float> light_cdf;
@@ -182,6 +200,7 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
     prim_material[(size_t)p] = prims[p].material;
     prim_has_normals[(size_t)p] = prims[p].vertex_normals ? 1 : 0;
     prim_xform[(size_t)p] = prims[p].mesh_to_world ? 1 : 0;
+    prim_frame[(size_t)p] = prims[p].vertex_tangents ? 1 : (prims[p].triangle_uvs ? 2 : 0);
     double inv[9];
     const bool has_inv = prims[p].mesh_to_world && inverse3(prims[p].mesh_to_world, inv);
     for (int64_t v = 0; v < m.n_vertices; ++v) {
@@ -199,6 +218,15 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
           }
         }
         vnrm.insert(vnrm.end(), nn, nn + 3);
+      }
+      if (any_tangents) {
+        float tt[3] = {1, 0, 0};
+        if (prims[p].vertex_tangents) {
+          ref_normalize_f(prims[p].vertex_tangents + 3 * v, tt);  // the mesh's stored tangent
+          const float mt[3] = {tt[0], tt[1], tt[2]};
+          xform_tangent(prims[p].mesh_to_world, mt, tt);
+        }
+        vtan.insert(vtan.end(), tt, tt + 3);
       }
     }
     const bool light = prims[p].emission[0] > 0 || prims[p].emission[1] > 0 || prims[p].emission[2] > 0;
@@ -221,6 +249,13 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
         if (ix[k] < 0 || (int64_t)ix[k] >= m.n_vertices) bad = true;
       if (bad || ix[0] == ix[1] || ix[0] == ix[2] || ix[1] == ix[2]) continue;  // TriangleMesh.cpp:176-182
       for (int k = 0; k < 3; ++k) tri_vidx.push_back(voff + ix[k]);
+      if (any_uvs) {
+        if (prim_frame[(size_t)p] == 2) {
+          tri_uv.insert(tri_uv.end(), prims[p].triangle_uvs + 6 * t, prims[p].triangle_uvs + 6 * t + 6);
+        } else {
+          tri_uv.insert(tri_uv.end(), {0, 0, 0, 0, 0, 0});
+        }
+      }
       if (any_albedo) {
         const float nanv = std::nanf("");
         if (prims[p].triangle_albedo) {
@@ -297,6 +332,7 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
     }
     const float rough = std::min(1.0f, std::max(0.001f, m.roughness));
     d.exponent = std::min(1000.0f, std::max(0.0f, 1.0f / rough));  // BlinnDistribution clamps to [0, 1000]
+    d.ev = -1.0f;
     if (m.kind == SKW_MATERIAL_MATTE) {
       const float sig = clamp01(m.sigma);
       if (sig < 2.220446e-16f) {
@@ -312,6 +348,12 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
       d.ior = 1.5f;  // PlasticMaterial.cpp:43: FresnelDielectric(1.5, 1)
     } else if (m.kind == SKW_MATERIAL_SUBSTRATE) {
       d.kind = skw::kSubstrate;
+      if (m.v_roughness > 0.0f) {
+        // AnisotropicDistribution(1 / clamp(u), 1 / clamp(v)), each exponent
+        // clamped to [0, 1000] (AnisotropicDistribution.h: constructor)
+        const float rv = std::min(1.0f, std::max(0.001f, m.v_roughness));
+        d.ev = std::min(1000.0f, std::max(0.0f, 1.0f / rv));
+      }
       // The lobe-sampling probability only shapes the variance (the
       // estimator divides by the mixture density it samples): the share of
       // the diffuse term's luminance in the two terms' luminances, kept in
@@ -439,6 +481,9 @@ int skw_scene_create(skw_ctx *ctx, const skw_mesh *meshes, int32_t n_meshes, con
   if (e == cudaSuccess) e = upload(s, prim_light, &D.prim_light);
   if (e == cudaSuccess) e = upload(s, prim_has_normals, &D.prim_has_normals);
   if (e == cudaSuccess) e = upload(s, prim_xform, &D.prim_xform);
+  if (e == cudaSuccess) e = upload(s, prim_frame, &D.prim_frame);
+  if (e == cudaSuccess) e = upload(s, vtan, &D.vtan);
+  if (e == cudaSuccess) e = upload(s, tri_uv, &D.tri_uv);
   if (instanced) {
     if (e == cudaSuccess) e = upload(s, prim_inst, &D.prim_inst);
     if (e == cudaSuccess) e = upload(s, prim_w2m, &D.prim_w2m);

@@ -152,6 +152,14 @@ def apply_point(m: np.ndarray, p: np.ndarray) -> np.ndarray:
     return out
 
 
+def apply_vector(m: np.ndarray, v: np.ndarray) -> np.ndarray:
+    """Transform::operator()(Vector3D_d), normalised (the shapes' tangents)."""
+    x, y, z = v[:, 0], v[:, 1], v[:, 2]
+    out = np.stack([(m[i, 0] * x + m[i, 1] * y) + m[i, 2] * z for i in range(3)], 1)
+    ln = np.sqrt((out * out).sum(1))
+    return np.where(ln[:, None] > 0, out / np.where(ln > 0, ln, 1.0)[:, None], out)
+
+
 def apply_normal(m: np.ndarray, n: np.ndarray) -> np.ndarray:
     """Transform::TransformNormal: the inverse transpose, normalised."""
     inv = np.linalg.inv(m)
@@ -165,31 +173,35 @@ def disk_mesh(m: np.ndarray, max_phi: float, inner: float, subdivisions: int = 3
     """Disk::BuildMesh (Shapes/Disk.cpp:57-171) through transform m: the
     unit disk (or the ring from `inner` to 1) in the z = 0 plane, its phi
     stepped by accumulation; flat (no shading normals).  Returns float32
-    vertices, int32 triangles."""
+    vertices, int32 triangles and float32 vertex tangents (T(-sin, cos, 0)
+    normalised; the centre's is 0)."""
     d_phi = max_phi / subdivisions
     ring, phi = [], 0.0
     for _ in range(subdivisions + 1):
         ring.append((math.cos(phi), math.sin(phi)))
         phi += d_phi
     c = np.array(ring, np.float64)
+    tang = apply_vector(m, np.stack([-c[:, 1], c[:, 0], np.zeros(len(c))], 1))
     i = np.arange(subdivisions)
     if inner == 0.0:
         pts = np.concatenate([[[0.0, 0.0, 0.0]], np.stack([c[:, 0], c[:, 1], np.zeros(len(c))], 1)])
+        tan = np.concatenate([[[0.0, 0.0, 0.0]], tang])
         tris = np.stack([np.zeros(subdivisions, np.int64), i + 1, i + 2], 1)
     else:
         pts = np.empty((2 * len(c), 3))
         pts[0::2] = np.stack([inner * c[:, 0], inner * c[:, 1], np.zeros(len(c))], 1)
         pts[1::2] = np.stack([c[:, 0], c[:, 1], np.zeros(len(c))], 1)
+        tan = np.repeat(tang, 2, axis=0)
         tris = np.concatenate([np.stack([2 * i, 2 * i + 1, 2 * i + 3], 1),
                                np.stack([2 * i + 3, 2 * i + 2, 2 * i], 1)], 1).reshape(-1, 3)
-    return apply_point(m, pts).astype(np.float32), tris.astype(np.int32)
+    return apply_point(m, pts).astype(np.float32), tris.astype(np.int32), tan.astype(np.float32)
 
 
 def cylinder_mesh(m: np.ndarray, max_phi: float, subdivisions: int = 360):
     """Cylinder::BuildMesh (Shapes/Cylinder.cpp:48-103) through transform m:
     the unit cylinder from z = 0 to 1, smooth.  Returns float32 vertices,
-    int32 triangles and float32 shading normals (negated for a mirroring m,
-    as the reference does)."""
+    int32 triangles, float32 shading normals (negated for a mirroring m, as
+    the reference does) and tangents (T(-sin, cos, 0) normalised)."""
     d_phi = max_phi / subdivisions
     ang, phi = [], 0.0
     for _ in range(subdivisions + 1):
@@ -201,11 +213,12 @@ def cylinder_mesh(m: np.ndarray, max_phi: float, subdivisions: int = 360):
     pts[1::2] = np.stack([c[:, 0], c[:, 1], np.ones(len(c))], 1)
     sign = -1.0 if inverts_orientation(m) else 1.0
     nrm = sign * apply_normal(m, np.stack([c[:, 0], c[:, 1], np.zeros(len(c))], 1))
+    tan = apply_vector(m, np.stack([-c[:, 1], c[:, 0], np.zeros(len(c))], 1))
     i = np.arange(subdivisions)
     tris = np.concatenate([np.stack([2 * i + 1, 2 * i, 2 * i + 2], 1),
                            np.stack([2 * i + 2, 2 * i + 3, 2 * i + 1], 1)], 1).reshape(-1, 3)
     return (apply_point(m, pts).astype(np.float32), tris.astype(np.int32),
-            np.repeat(nrm, 2, axis=0).astype(np.float32))
+            np.repeat(nrm, 2, axis=0).astype(np.float32), np.repeat(tan, 2, axis=0).astype(np.float32))
 
 
 def _max_phi(phimax_deg: float) -> float:
@@ -491,11 +504,11 @@ class _Importer:
                 return Material(METAL, eta=p.coef("eta", _COPPER_ETA, ct), k=p.coef("k", _COPPER_K, ct),
                                 roughness=p.scalar("roughness", 0.1, ft))
             if name == "substrate":
+                # the factory takes the two-roughness constructor
+                # (AnisotropicDistribution), whatever the two values
                 u, v = p.scalar("uroughness", 0.1, ft), p.scalar("vroughness", 0.1, ft)
-                if u != v:
-                    raise _Unsupported("anisotropic substrate (uroughness != vroughness)")
                 return Material(SUBSTRATE, kd=p.coef("Kd", (0.5,) * 3, ct), ks=p.coef("Ks", (0.5,) * 3, ct),
-                                roughness=u)
+                                roughness=u, v_roughness=max(v, 1e-30))
             if name == "uber":
                 return Material(UBER, kd=p.coef("Kd", (0.25,) * 3, ct), ks=p.coef("Ks", (0.25,) * 3, ct),
                                 kr=p.coef("Kr", (0.0,) * 3, ct), roughness=p.scalar("roughness", 0.1, ft),
@@ -537,7 +550,7 @@ class _Importer:
     # ---- shapes (ShapeFactory.h)
     def _shape(self, name: str, p: _Params):
         m = self.ctm
-        normals = None
+        normals = tangents = uvs = None
         if name == "trianglemesh":
             P, idx = p.points("P"), p.ints("indices")
             if P is None or idx is None:
@@ -556,6 +569,17 @@ class _Importer:
                 else:
                     N = N / np.sqrt((N * N).sum(1))[:, None]
                     normals = apply_normal(m, N).astype(np.float32)
+            # per-triangle uvs: the "uv" (or "st") of the vertices, else
+            # (0, 0), (1, 0), (1, 1) as the factory sets them (ShapeFactory.h)
+            uv = p.floats("uv") or p.floats("st")
+            if uv is not None and len(uv) < 2 * len(P):
+                self.warn("trianglemesh: not enough uvs; discarded")
+                uv = None
+            if uv is not None:
+                uvv = np.asarray(uv[: 2 * len(P)], np.float32).reshape(-1, 2)
+                uvs = uvv[t].reshape(-1, 6)
+            else:
+                uvs = np.tile(np.array([0, 0, 1, 0, 1, 1], np.float32), (len(t), 1))
             flip = self.gs.reverse
         elif name == "sphere":
             radius = p.float1("radius", 1.0)
@@ -568,23 +592,30 @@ class _Importer:
             t = st.astype(np.int32)
             sign = -1.0 if inverts_orientation(sm) else 1.0
             normals = (sign * apply_normal(sm, sv)).astype(np.float32)
+            # tangents (0, 0, 1) x v, or (1, 0, 0) at the poles, through the transform
+            tv = np.cross(np.array([0.0, 0.0, 1.0]), sv)
+            ln = np.sqrt((tv * tv).sum(1))
+            tv = np.where(ln[:, None] > 0, tv / np.where(ln > 0, ln, 1.0)[:, None], [1.0, 0.0, 0.0])
+            tangents = apply_vector(sm, tv).astype(np.float32)
             flip = self.gs.reverse != inverts_orientation(sm)
         elif name == "disk":
             height, radius = p.float1("height", 0.0), p.float1("radius", 1.0)
             inner = p.float1("innerradius", 0.0)
             dm = m @ translate((0.0, 0.0, height)) @ scale((radius, radius, 1.0))
-            v, t = disk_mesh(dm, _max_phi(p.float1("phimax", 360.0)), inner / radius)
+            v, t, tangents = disk_mesh(dm, _max_phi(p.float1("phimax", 360.0)), inner / radius)
             flip = self.gs.reverse != inverts_orientation(dm)
         elif name == "cylinder":
             radius, zmin, zmax = p.float1("radius", 1.0), p.float1("zmin", -1.0), p.float1("zmax", 1.0)
             cm = m @ translate((0.0, 0.0, zmin)) @ scale((radius, radius, zmax - zmin))
-            v, t, normals = cylinder_mesh(cm, _max_phi(p.float1("phimax", 360.0)))
+            v, t, normals, tangents = cylinder_mesh(cm, _max_phi(p.float1("phimax", 360.0)))
             flip = self.gs.reverse != inverts_orientation(cm)
         else:
             self.warn(f"shape \"{name}\" is not supported")
             return
         if flip:
             t = t[:, [0, 2, 1]].copy()
+            if uvs is not None:
+                uvs = uvs[:, [0, 1, 4, 5, 2, 3]].copy()
         mat = self._current_material(p)
         emission = (0.0, 0.0, 0.0)
         if self.gs.area_light is not None:
@@ -595,7 +626,8 @@ class _Importer:
                 emission = tuple(float(a * b) for a, b in zip(L, sc))
             else:
                 self.warn(f"area light \"{lname}\" is not supported")
-        prim = RenderPrimitive(TriangleMesh(v, t), mat, None, normals, None, emission)
+        prim = RenderPrimitive(TriangleMesh(v, t), mat, None, normals, None, emission, tangents,
+                               uvs if tangents is None else None)
         if self.current_instance is not None:
             if any(emission):
                 self.warn("area lights in object instances are not supported")
@@ -800,7 +832,8 @@ class _Importer:
             for prim in self.instances[nm]:
                 # the shared mesh (built in its definition's space) with this instance's transform
                 self.out.prims.append(RenderPrimitive(prim.mesh, prim.material, self.ctm.copy(),
-                                                      prim.vertex_normals, None, prim.emission))
+                                                      prim.vertex_normals, None, prim.emission,
+                                                      prim.vertex_tangents, prim.triangle_uvs))
 
 
 def loads(text: str, base_dir: str = ".", ctx=None, device: bool = True) -> PbrtScene:

@@ -84,6 +84,7 @@ class Material:
     opacity: tuple = (1.0, 1.0, 1.0)    # UBER: opacity (1: opaque)
     mix: tuple = (-1, -1)               # MIX: indices of the two mixed materials
     mix_scale: tuple = (0.5, 0.5, 0.5)  # MIX: the first material's scale
+    v_roughness: float = 0.0            # SUBSTRATE: > 0 the two-roughness (anisotropic) form
 
 
 @dataclass
@@ -94,6 +95,8 @@ class RenderPrimitive:
     vertex_normals: np.ndarray | None = None
     triangle_albedo: np.ndarray | None = None
     emission: tuple = (0.0, 0.0, 0.0)
+    vertex_tangents: np.ndarray | None = None  # (nv, 3) mesh-space tangents (the BSDF frame's first axis)
+    triangle_uvs: np.ndarray | None = None     # (nt, 6) per-triangle uvs, when no vertex tangents
 
 
 @dataclass
@@ -141,12 +144,13 @@ class skw_material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("roughness", C.c_float),
                 ("sigma", C.c_float), ("eta", C.c_float * 3), ("k", C.c_float * 3), ("measured", C.c_void_p),
                 ("refractive_index", C.c_float), ("kr", C.c_float * 3), ("opacity", C.c_float * 3),
-                ("mix", C.c_int32 * 2), ("mix_scale", C.c_float * 3)]
+                ("mix", C.c_int32 * 2), ("mix_scale", C.c_float * 3), ("v_roughness", C.c_float)]
 
 
 class skw_render_primitive(C.Structure):
     _fields_ = [("mesh", C.c_int32), ("mesh_to_world", C.c_void_p), ("material", C.c_int32),
-                ("vertex_normals", C.c_void_p), ("triangle_albedo", C.c_void_p), ("emission", C.c_float * 3)]
+                ("vertex_normals", C.c_void_p), ("triangle_albedo", C.c_void_p), ("emission", C.c_float * 3),
+                ("vertex_tangents", C.c_void_p), ("triangle_uvs", C.c_void_p)]
 
 
 class skw_point_light(C.Structure):
@@ -175,7 +179,7 @@ def c_material(m: Material, measured_handle=None) -> skw_material:
     return skw_material(m.kind, (C.c_float * 3)(*m.kd), (C.c_float * 3)(*m.ks), m.roughness, m.sigma,
                         (C.c_float * 3)(*m.eta), (C.c_float * 3)(*m.k), h, m.refractive_index,
                         (C.c_float * 3)(*m.kr), (C.c_float * 3)(*m.opacity), (C.c_int32 * 2)(*m.mix),
-                        (C.c_float * 3)(*m.mix_scale))
+                        (C.c_float * 3)(*m.mix_scale), m.v_roughness)
 
 
 def c_camera(cam: Camera) -> skw_camera:
@@ -198,10 +202,13 @@ def c_prims(prims: list[RenderPrimitive]):
         xf = None if p.mesh_to_world is None else np.ascontiguousarray(p.mesh_to_world, np.float64).reshape(4, 4)
         vn = None if p.vertex_normals is None else np.ascontiguousarray(p.vertex_normals, np.float32).reshape(-1, 3)
         ta = None if p.triangle_albedo is None else np.ascontiguousarray(p.triangle_albedo, np.float32).reshape(-1, 3)
-        keep += [xf, vn, ta]
+        vt = None if p.vertex_tangents is None else np.ascontiguousarray(p.vertex_tangents, np.float32).reshape(-1, 3)
+        uv = None if p.triangle_uvs is None else np.ascontiguousarray(p.triangle_uvs, np.float32).reshape(-1, 6)
+        keep += [xf, vn, ta, vt, uv]
         cp[i] = skw_render_primitive(mesh_ids[id(p.mesh)], None if xf is None else xf.ctypes.data, p.material,
                                      None if vn is None else vn.ctypes.data, None if ta is None else ta.ctypes.data,
-                                     (C.c_float * 3)(*p.emission))
+                                     (C.c_float * 3)(*p.emission), None if vt is None else vt.ctypes.data,
+                                     None if uv is None else uv.ctypes.data)
     return cm, len(meshes), cp, keep
 
 

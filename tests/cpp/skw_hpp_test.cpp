@@ -83,8 +83,8 @@ int main() {
 
     // Direct lighting: a matte floor under a quad light, 8 x 8, 2 x 2 spp.
     std::vector<skw::Mesh> rm = {square(0.0f, 5.0f, true), square(1.0f, 0.3f, false)};
-    skw_render_primitive floor_p{0, nullptr, 0, nullptr, nullptr, {0, 0, 0}};
-    skw_render_primitive light_p{1, nullptr, 1, nullptr, nullptr, {10, 10, 10}};
+    skw_render_primitive floor_p{0, nullptr, 0, nullptr, nullptr, {0, 0, 0}, nullptr, nullptr};
+    skw_render_primitive light_p{1, nullptr, 1, nullptr, nullptr, {10, 10, 10}, nullptr, nullptr};
     skw_material matte{};
     matte.kind = SKW_MATERIAL_MATTE;
     matte.kd[0] = matte.kd[1] = matte.kd[2] = 0.5f;

@@ -354,7 +354,8 @@ def material_cases():
     specular reflection (the light's mirror image in the plane), and a mix of
     matte and plastic; and the sphere of specular_scene() as a half-opaque
     uber (its specular transmission, reflection, diffuse and glossy parts)
-    and as a mix of clear glass and matte."""
+    and as a mix of clear glass and matte; and the two-roughness substrate
+    on the plane (no uvs, and uvs) and on the sphere (vertex tangents)."""
     from skwarka_gb300.render import MATTE, MIX, PLASTIC, SUBSTRATE, TRANSPARENT, UBER, Material
     planes = material_plane_scenes()
     prims, mats, pls, cam = planes["area_matte"]
@@ -381,5 +382,22 @@ def material_cases():
     n = len(sm)
     mix = Material(kind=MIX, mix=(n, n + 1), mix_scale=(0.6, 0.6, 0.6))
     out["sphere_mix_glass_matte"] = (sp, [sm[0], mix] + list(sm[2:]) + [glass, Material(kd=(0.7, 0.2, 0.2))], sl, sc)
+    # the two-roughness substrate (AnisotropicDistribution) under each source
+    # of the shading tangent: CoordinateSystem of the normal (the plane
+    # without uvs), triangle uvs (the plane, u along a diagonal), and vertex
+    # tangents (the sphere, Sphere::BuildMesh's (0, 0, 1) x v)
+    aniso = Material(kind=SUBSTRATE, kd=(0.5, 0.4, 0.3), ks=(0.3, 0.3, 0.3), roughness=0.04, v_roughness=0.6)
+    out["plane_substrate_aniso"] = ([prims[0].__class__(prims[0].mesh, 0), prims[1].__class__(
+        prims[1].mesh, 1, emission=prims[1].emission)], [aniso, Material(kd=(0.0, 0.0, 0.0))], pls, cam)
+    uv = np.array([[0.0, 0.0, 0.7, 0.7, 0.0, 1.0]] * len(prims[0].mesh.triangles), np.float32)
+    out["plane_substrate_aniso_uv"] = ([prims[0].__class__(prims[0].mesh, 0, triangle_uvs=uv), prims[1].__class__(
+        prims[1].mesh, 1, emission=prims[1].emission)], [aniso, Material(kd=(0.0, 0.0, 0.0))], pls, cam)
+    ap, am, al, ac = specular_scene(aniso, "area")
+    sv = (ap[1].mesh.vertices.astype(np.float64) - [0.0, 0.0, 0.45]) / 0.4
+    tan = np.cross(np.array([0.0, 0.0, 1.0]), sv)
+    ln = np.linalg.norm(tan, axis=1)
+    tan = np.where(ln[:, None] > 0, tan / np.maximum(ln, 1e-300)[:, None], [1.0, 0.0, 0.0])
+    ap = [ap[0], ap[1].__class__(ap[1].mesh, 1, vertex_tangents=tan.astype(np.float32))] + list(ap[2:])
+    out["sphere_substrate_aniso"] = (ap, am, al, ac)
     return out
 

@@ -1,5 +1,7 @@
-"""SubstrateMaterial, UberMaterial and MixMaterial on the GPU against the
-reference's own renders of the same scenes (tests/golden/materials.npz,
+"""SubstrateMaterial (one- and two-roughness: Blinn and Ashikhmin-Shirley,
+the latter under each source of the shading tangent), UberMaterial and
+MixMaterial on the GPU against the reference's own renders of the same
+scenes (tests/golden/materials.npz,
 from tests/golden/make_golden.py materials: SamplerBasedRenderer with
 DirectLightingLTEIntegrator, 16x16 spp, maximum specular depth 6).
 
@@ -23,7 +25,8 @@ LUM = np.array([0.05316285, 0.58515348, 0.36168367])
 
 
 @pytest.mark.parametrize("name", ["plane_substrate", "plane_substrate_rough", "plane_uber_opaque",
-                                  "plane_mix_matte_plastic", "sphere_uber", "sphere_mix_glass_matte"])
+                                  "plane_mix_matte_plastic", "sphere_uber", "sphere_mix_glass_matte",
+                                  "plane_substrate_aniso", "plane_substrate_aniso_uv", "sphere_substrate_aniso"])
 def test_material_render_matches_reference(gpu, name):
     prims, mats, lights, cam = sf.material_cases()[name]
     ref = np.load(GOLD)[name]
@@ -36,6 +39,13 @@ def test_material_render_matches_reference(gpu, name):
     if name.startswith("sphere"):
         rb = (ref @ LUM).reshape(4, 8, 6, 8).mean(axis=(1, 3))
         gb = (img @ LUM).reshape(4, 8, 6, 8).mean(axis=(1, 3))
+        rel = np.abs(gb - rb) / np.maximum(rb, 0.25 * rb.mean())
+        msg += f"; worst block {rel.max():.4f}"
+        assert rel.max() <= 0.06, msg
+    elif "aniso" in name:
+        # the highlight's shape follows the shading tangent: 4x4-pixel blocks
+        rb = (ref @ LUM).reshape(4, 4, 6, 4).mean(axis=(1, 3))
+        gb = (img @ LUM).reshape(4, 4, 6, 4).mean(axis=(1, 3))
         rel = np.abs(gb - rb) / np.maximum(rb, 0.25 * rb.mean())
         msg += f"; worst block {rel.max():.4f}"
         assert rel.max() <= 0.06, msg

@@ -38,7 +38,8 @@ def test_imported_scene_renders_like_the_same_scene_built_directly(gpu):
     img = s.render_scene().render_direct(s.camera, 2, 2, seed=5).cpu().numpy()
     # the same scene through the API, from the importer's own arrays
     prims = [RenderPrimitive(TriangleMesh(p.mesh.vertices.copy(), p.mesh.triangles.copy()), p.material,
-                             p.mesh_to_world, p.vertex_normals, None, p.emission) for p in s.prims]
+                             p.mesh_to_world, p.vertex_normals, None, p.emission, p.vertex_tangents,
+                             p.triangle_uvs) for p in s.prims]
     mats = [Material(**m.__dict__) for m in s.materials]
     lights = [PointLight(l.position, l.intensity) for l in s.point_lights]
     cam = Camera(s.camera.camera_to_world.copy(), s.camera.x_view_angle, s.camera.width, s.camera.height)

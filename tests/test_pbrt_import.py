@@ -123,13 +123,15 @@ WorldEnd''')
     assert m[2].refractive_index == float(np.float32(1.33))
     assert m[3].kind == TRANSPARENT and m[3].ks == (0.0,) * 3 and m[3].refractive_index == 1e10
     assert m[4].kind == METAL and m[4].eta == (1.165312, 0.950375, 0.35125) and m[4].roughness == 0.1
+    # the factory's two-roughness constructor (AnisotropicDistribution) even for u == v
     assert m[5].kind == SUBSTRATE and m[5].kd == (0.5,) * 3 and m[5].roughness == float(np.float32(0.2))
+    assert m[5].v_roughness == float(np.float32(0.2))
     assert m[6].kind == UBER and m[6].opacity == (0.5,) * 3 and m[6].kr == (0.0,) * 3
     assert m[7].kind == MIX and m[7].mix_scale == (0.25,) * 3
     a, b = (s.materials[i] for i in m[7].mix)
     assert a.kind == MATTE and a.kd == (float(np.float32(0.9)),) * 3 and b.kind == PLASTIC
-    assert m[8].kind == MATTE  # anisotropic substrate: reported, matte used
-    assert any("anisotropic substrate" in w for w in s.warnings)
+    assert m[8].kind == SUBSTRATE and m[8].roughness == float(np.float32(0.1))
+    assert m[8].v_roughness == float(np.float32(0.3)) and not s.warnings
 
 
 def test_area_light_volume_and_constant_textures():
@@ -239,3 +241,28 @@ WorldEnd''')
     c = v[t].mean(1)
     assert (np.einsum("ij,ij->i", n[:, :2], c[:, :2]) > 0).all()  # outward
     assert np.allclose(cyl.vertex_normals[:, :2] * 0.5, v[:, :2], atol=1e-6)
+
+
+def test_shading_tangent_sources():
+    s = pbrt.loads(HEADER + '''
+Shape "trianglemesh" "point P" [0 0 0 1 0 0 0 1 0] "integer indices" [0 1 2]
+Shape "trianglemesh" "point P" [0 0 0 1 0 0 0 1 0] "integer indices" [0 1 2] "float uv" [0 0 0 1 1 0]
+Shape "sphere"
+Shape "cylinder"
+Shape "disk"
+WorldEnd''')
+    a, b, sph, cyl, dsk = s.prims
+    # PBRT's default uvs (0, 0), (1, 0), (1, 1): u increases along the first edge
+    assert a.triangle_uvs.tolist() == [[0, 0, 1, 0, 1, 1]] and a.vertex_tangents is None
+    assert b.triangle_uvs.tolist() == [[0, 0, 0, 1, 1, 0]]
+    # the shapes' tangents: (0, 0, 1) x v for the sphere, (-sin, cos, 0) around the cylinder and disk
+    v = sph.mesh.vertices.astype(np.float64)
+    want = np.cross([0.0, 0.0, 1.0], v)
+    ln = np.linalg.norm(want, axis=1)
+    ok = ln > 1e-6
+    assert np.allclose(sph.vertex_tangents[ok], want[ok] / ln[ok, None], atol=1e-6)
+    assert np.allclose(sph.vertex_tangents[~ok], [1, 0, 0])
+    c = cyl.mesh.vertices[:, :2].astype(np.float64)
+    assert np.allclose(cyl.vertex_tangents[:, :2], np.stack([-c[:, 1], c[:, 0]], 1), atol=1e-6)
+    assert np.allclose(dsk.vertex_tangents[0], 0) and np.allclose(np.abs(dsk.vertex_tangents[1:, 2]), 0)
+    assert cyl.triangle_uvs is None and sph.triangle_uvs is None
