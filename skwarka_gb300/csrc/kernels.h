@@ -68,7 +68,20 @@ cudaError_t scan64(uint64_t *v, int64_t n, uint64_t *sums, cudaStream_t st);
 cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                        const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,
                        double *out_d2, int32_t *out_count, int32_t *out_visited, void *scratch, unsigned *status,
-                       cudaStream_t stream, const int *nq_dev = nullptr);
+                       cudaStream_t stream, const int *nq_dev = nullptr, const int32_t *order = nullptr);
+// Spatial-bin order of n queries (3 doubles each; count_dev, if not null,
+// caps n on the device) in the box [lo, hi]: order[t] = the query the t-th
+// lookup thread takes (launch_knn / launch_nearest order), grouped by 64^3
+// Morton cells.  keys: n uint32; bins: bin_order_bins() ints.
+int64_t bin_order_bins();
+cudaError_t launch_bin_order(const double *q, int64_t n, const int *count_dev, const float lo[3], const float hi[3],
+                             uint32_t *keys, int *bins, int32_t *order, cudaStream_t st);
+// The same cells as launch_bin_order, sorted stably (a radix sort of the
+// cell keys): the queries of a cell keep their order.  scratch:
+// sort_order_bytes(n).
+size_t sort_order_bytes(int64_t n);
+cudaError_t launch_sort_order(const double *q, int64_t n, const float lo[3], const float hi[3], void *scratch,
+                              int32_t *order, cudaStream_t st);
 // k-NN with its heaps in the library's static device scratch (no
 // allocation): nq * k must be <= knn_noalloc_capacity() entries, else
 // cudaErrorInvalidValue.  Overlapping calls race on that scratch.

@@ -412,11 +412,13 @@ __global__ void __launch_bounds__(kKnnBlock, SKW_KNN_MINB) k_knn(const float4 *_
                                              double cos_t, int32_t *__restrict__ out_idx,
                                              double *__restrict__ out_d2, int32_t *__restrict__ out_count,
                                              int32_t *__restrict__ out_visited, FCand *__restrict__ scratch,
-                                             unsigned *__restrict__ status, const int *__restrict__ nq_dev) {
+                                             unsigned *__restrict__ status, const int *__restrict__ nq_dev,
+                                             const int32_t *__restrict__ order) {
   __shared__ uint32_t stk[S][kKnnBlock];
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (nq_dev && *nq_dev < nq) nq = *nq_dev;
   if (i >= nq) return;
+  if (order) i = order[i];
   Query Q;
   Q.q[0] = q[3 * i];
   Q.q[1] = q[3 * i + 1];
@@ -623,17 +625,198 @@ template <int KMAX>
 void knn_kernel(unsigned grid, cudaStream_t stream, const float4 *nodes, const uint16_t *nids, const double *dirs,
                 int n, const double *q, const double *qn, int64_t nq, int k, double max_dist, double cos_t,
                 int32_t *out_idx, double *out_d2, int32_t *out_count, int32_t *out_visited, FCand *scratch,
-                unsigned *status, const int *nq_dev) {
+                unsigned *status, const int *nq_dev, const int32_t *order) {
   if (shallow_tree(n))
     k_knn<KMAX, kShallowStack><<<grid, kKnnBlock, 0, stream>>>(nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t,
                                                                out_idx, out_d2, out_count, out_visited, scratch,
-                                                               status, nq_dev);
+                                                               status, nq_dev, order);
   else
     k_knn<KMAX, 32><<<grid, kKnnBlock, 0, stream>>>(nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx,
-                                                    out_d2, out_count, out_visited, scratch, status, nq_dev);
+                                                    out_d2, out_count, out_visited, scratch, status, nq_dev, order);
+}
+
+// Spatial bins of queries: a box cut into 64^3 cells, each query's cell as
+// an 18-bit Morton code; a counting sort by cell (count, one exclusive scan,
+// scatter) gives the order in which the lookup kernels take the queries, so
+// that a warp's walks start near each other.  The order inside a cell
+// follows the atomics; every query's answer is the same whichever thread
+// computes it, and it is written at the query's own index.
+constexpr int kBinBits = 6, kBins = 1 << (3 * kBinBits);
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // bit b of v to bit 3b
+  uint32_t r = 0;
+#pragma unroll
+  for (int b = 0; b < kBinBits; ++b) r |= ((v >> b) & 1u) << (3 * b);
+  return r;
+}
+
+__global__ void k_bin_keys(const double *__restrict__ q, int64_t n, const int *__restrict__ count, float3 lo,
+                           float3 scale, uint32_t *__restrict__ key, int *__restrict__ bins) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || (count && i >= *count)) return;
+  const float c[3] = {((float)q[3 * i] - lo.x) * scale.x, ((float)q[3 * i + 1] - lo.y) * scale.y,
+                      ((float)q[3 * i + 2] - lo.z) * scale.z};
+  uint32_t k = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float f = fminf(fmaxf(c[a], 0.0f), (float)((1 << kBinBits) - 1));  // NaN -> 0
+    k |= spread3((uint32_t)f) << a;
+  }
+  key[i] = k;
+  if (bins) atomicAdd(bins + k, 1);
+}
+
+// Exclusive scan of the kBins counts in place, one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_bin_scan(int *__restrict__ bins) {
+  constexpr int per = kBins / 1024;
+  __shared__ int part[1024];
+  int local[per];
+  int sum = 0;
+  for (int j = 0; j < per; ++j) {
+    local[j] = sum;
+    sum += bins[threadIdx.x * per + j];
+  }
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan of the parts
+    const int v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  const int base = part[threadIdx.x] - sum;
+  for (int j = 0; j < per; ++j) bins[threadIdx.x * per + j] = base + local[j];
+}
+
+__global__ void k_bin_scatter(const uint32_t *__restrict__ key, int64_t n, const int *__restrict__ count,
+                              int *__restrict__ bins, int32_t *__restrict__ order) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || (count && i >= *count)) return;
+  // the lanes of one cell take consecutive slots in lane order (one atomic
+  // per cell and warp), so runs of neighbouring queries stay in order
+  const uint32_t k = key[i];
+  const unsigned grp = __match_any_sync(__activemask(), k);
+  const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(bins + k, __popc(grp));
+  base = __shfl_sync(grp, base, leader);
+  order[base + __popc(grp & ((1u << lane) - 1u))] = (int32_t)i;
+}
+
+// A stable LSD radix sort of the 18-bit cell keys (three passes of 6-bit
+// digits) carrying the query indices: per block of 256 keys, each digit's
+// count (lanes of a warp grouped by digit with __match_any_sync), one
+// exclusive scan of the counts digit-major (all blocks of digit 0, then
+// digit 1, ...), and a scatter that ranks a key after the block's earlier
+// warps and the warp's earlier lanes with the same digit.  Stable, so the
+// queries of a cell keep their image order.
+constexpr int kSortBlock = 256, kDigitBits = 6, kDigits = 1 << kDigitBits;
+
+__device__ __forceinline__ void digit_counts(uint32_t d, bool valid, unsigned &grp, int (*wcnt)[kDigits]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  grp = __match_any_sync(0xffffffffu, valid ? d : 0xFFFFFFFFu);
+  if (valid && lane == __ffs(grp) - 1) wcnt[w][d] = __popc(grp);
+}
+
+__global__ void __launch_bounds__(kSortBlock) k_sort_hist(const uint32_t *__restrict__ key, int64_t n, int shift,
+                                                          uint64_t *__restrict__ hist, int64_t nblocks) {
+  __shared__ int wcnt[kSortBlock / 32][kDigits];
+  for (int j = threadIdx.x; j < (kSortBlock / 32) * kDigits; j += kSortBlock) (&wcnt[0][0])[j] = 0;
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * kSortBlock + threadIdx.x;
+  const bool valid = i < n;
+  const uint32_t d = valid ? (key[i] >> shift) & (kDigits - 1) : 0u;
+  unsigned grp;
+  digit_counts(d, valid, grp, wcnt);
+  __syncthreads();
+  if (threadIdx.x < kDigits) {
+    int c = 0;
+    for (int w = 0; w < kSortBlock / 32; ++w) c += wcnt[w][threadIdx.x];
+    hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = (uint64_t)c;
+  }
+}
+
+__global__ void __launch_bounds__(kSortBlock) k_sort_scatter(const uint32_t *__restrict__ key,
+                                                             const int32_t *__restrict__ val, int64_t n, int shift,
+                                                             const uint64_t *__restrict__ offs, int64_t nblocks,
+                                                             uint32_t *__restrict__ key2, int32_t *__restrict__ val2) {
+  __shared__ int wcnt[kSortBlock / 32][kDigits];
+  for (int j = threadIdx.x; j < (kSortBlock / 32) * kDigits; j += kSortBlock) (&wcnt[0][0])[j] = 0;
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * kSortBlock + threadIdx.x;
+  const bool valid = i < n;
+  const uint32_t k = valid ? key[i] : 0u, d = (k >> shift) & (kDigits - 1);
+  unsigned grp;
+  digit_counts(d, valid, grp, wcnt);
+  __syncthreads();
+  if (!valid) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int before = 0;
+  for (int v = 0; v < w; ++v) before += wcnt[v][d];
+  const int64_t dst = (int64_t)offs[(int64_t)d * nblocks + blockIdx.x] + before + __popc(grp & ((1u << lane) - 1u));
+  key2[dst] = k;
+  val2[dst] = val ? val[i] : (int32_t)i;
 }
 
 }  // namespace
+
+int64_t bin_order_bins() { return kBins; }
+
+size_t sort_order_bytes(int64_t n) {
+  const int64_t nb = (n + kSortBlock - 1) / kSortBlock, m = nb * kDigits;
+  auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
+  return 3 * al(n * 4) + al(m * 8) + al(((m + 255) / 256) * 8);
+}
+
+cudaError_t launch_sort_order(const double *q, int64_t n, const float lo[3], const float hi[3], void *scratch,
+                              int32_t *order, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t nb = (n + kSortBlock - 1) / kSortBlock, m = nb * kDigits;
+  auto al = [](int64_t x) { return (size_t)((x + 255) & ~(int64_t)255); };
+  char *w = (char *)scratch;
+  uint32_t *ka = (uint32_t *)w, *kb = (uint32_t *)(w + al(n * 4));
+  int32_t *va = (int32_t *)(w + 2 * al(n * 4)), *vb = order;
+  uint64_t *hist = (uint64_t *)(w + 3 * al(n * 4));
+  uint64_t *sums = (uint64_t *)((char *)hist + al(m * 8));
+  float sc[3];
+  for (int a = 0; a < 3; ++a) {
+    const float ext = hi[a] - lo[a];
+    sc[a] = ext > 0.0f && ext < INFINITY ? (float)(1 << kBinBits) / ext : 0.0f;
+  }
+  k_bin_keys<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(q, n, nullptr, make_float3(lo[0], lo[1], lo[2]),
+                                                          make_float3(sc[0], sc[1], sc[2]), ka, nullptr);
+  // three passes: ka/va -> kb/vb -> ka/va -> kb/vb, so the last lands in order (vb)
+  const int32_t *vin = nullptr;
+  for (int pass = 0; pass < 3; ++pass) {
+    const int shift = pass * kDigitBits;
+    uint32_t *kin = pass == 1 ? kb : ka, *kout = pass == 1 ? ka : kb;
+    int32_t *vout = pass == 1 ? va : vb;
+    k_sort_hist<<<(unsigned)nb, kSortBlock, 0, st>>>(kin, n, shift, hist, nb);
+    cudaError_t e = scan64(hist, m, sums, st);
+    if (e != cudaSuccess) return e;
+    k_sort_scatter<<<(unsigned)nb, kSortBlock, 0, st>>>(kin, vin, n, shift, hist, nb, kout, vout);
+    vin = vout;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bin_order(const double *q, int64_t n, const int *count_dev, const float lo[3], const float hi[3],
+                             uint32_t *keys, int *bins, int32_t *order, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  float sc[3];
+  for (int a = 0; a < 3; ++a) {
+    const float ext = hi[a] - lo[a];
+    sc[a] = ext > 0.0f && ext < INFINITY ? (float)(1 << kBinBits) / ext : 0.0f;
+  }
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)kBins * 4, st);
+  if (e != cudaSuccess) return e;
+  k_bin_keys<<<grid, 256, 0, st>>>(q, n, count_dev, make_float3(lo[0], lo[1], lo[2]),
+                                   make_float3(sc[0], sc[1], sc[2]), keys, bins);
+  k_bin_scan<<<1, 1024, 0, st>>>(bins);
+  k_bin_scatter<<<grid, 256, 0, st>>>(keys, n, count_dev, bins, order);
+  return cudaGetLastError();
+}
 
 #ifndef SKW_KNN_GHEAP
 #define SKW_KNN_GHEAP 129  // smallest k whose heaps live in global scratch
@@ -645,24 +828,24 @@ size_t knn_scratch_bytes(int64_t nq, int k) {
 cudaError_t launch_knn(const void *nodes, const uint16_t *nids, const double *dirs, int n, const double *q,
                        const double *qn, int64_t nq, int k, double max_dist, double cos_t, int32_t *out_idx,
                        double *out_d2, int32_t *out_count, int32_t *out_visited, void *scratch, unsigned *status,
-                       cudaStream_t stream, const int *nq_dev) {
+                       cudaStream_t stream, const int *nq_dev, const int32_t *order) {
   if (nq <= 0) return cudaSuccess;
   const int block = kKnnBlock;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
   const float4 *nd = (const float4 *)nodes;
   if (scratch && k >= SKW_KNN_GHEAP) {
     knn_kernel<0>(grid, stream, nd, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx, out_d2, out_count,
-                  out_visited, (FCand *)scratch, status, nq_dev);
+                  out_visited, (FCand *)scratch, status, nq_dev, order);
   } else if (k <= 32) {
     knn_kernel<32>(grid, stream, nd, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx, out_d2, out_count,
-                   out_visited, nullptr, status, nq_dev);
+                   out_visited, nullptr, status, nq_dev, order);
   } else if (k <= 128) {
     knn_kernel<128>(grid, stream, nd, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx, out_d2, out_count,
-                    out_visited, nullptr, status, nq_dev);
+                    out_visited, nullptr, status, nq_dev, order);
   } else {
     if (!scratch) return cudaErrorInvalidValue;
     knn_kernel<0>(grid, stream, nd, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx, out_d2, out_count,
-                  out_visited, (FCand *)scratch, status, nq_dev);
+                  out_visited, (FCand *)scratch, status, nq_dev, order);
   }
   return cudaGetLastError();
 }
@@ -729,7 +912,7 @@ cudaError_t launch_knn_noalloc(const void *nodes, const uint16_t *nids, const do
   const int block = kKnnBlock;
   const unsigned grid = (unsigned)((nq + block - 1) / block);
   knn_kernel<0>(grid, stream, (const float4 *)nodes, nids, dirs, n, q, qn, nq, k, max_dist, cos_t, out_idx, out_d2,
-                out_count, nullptr, (FCand *)scratch, status, nullptr);
+                out_count, nullptr, (FCand *)scratch, status, nullptr, nullptr);
   return cudaGetLastError();
 }
 

@@ -1093,66 +1093,6 @@ cudaError_t launch_caustic(const SceneDev &S, const CausticMap &C, const ViewDev
   return cudaGetLastError();
 }
 
-// Spatial bins of the gather hits' irradiance queries: the scene's box cut
-// into 64^3 cells, each query's cell as an 18-bit Morton code; a counting
-// sort by cell (count, one exclusive scan, scatter) gives the order in which
-// k_nearest takes the queries, so that a warp's walks start near each other.
-// The order inside a cell follows the atomics; every query's answer is the
-// same whichever thread computes it.
-constexpr int kBinBits = 6, kBins = 1 << (3 * kBinBits);
-
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // bit b of v to bit 3b
-  uint32_t r = 0;
-#pragma unroll
-  for (int b = 0; b < kBinBits; ++b) r |= ((v >> b) & 1u) << (3 * b);
-  return r;
-}
-
-__global__ void k_bin_keys(const double *__restrict__ q, const int *__restrict__ count, float3 lo, float3 scale,
-                           uint32_t *__restrict__ key, int *__restrict__ bins) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= *count) return;
-  const float c[3] = {((float)q[3 * i] - lo.x) * scale.x, ((float)q[3 * i + 1] - lo.y) * scale.y,
-                      ((float)q[3 * i + 2] - lo.z) * scale.z};
-  uint32_t k = 0;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const float f = fminf(fmaxf(c[a], 0.0f), (float)((1 << kBinBits) - 1));  // NaN -> 0
-    k |= spread3((uint32_t)f) << a;
-  }
-  key[i] = k;
-  atomicAdd(bins + k, 1);
-}
-
-// Exclusive scan of the kBins counts in place, one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_bin_scan(int *__restrict__ bins) {
-  constexpr int per = kBins / 1024;
-  __shared__ int part[1024];
-  int local[per];
-  int sum = 0;
-  for (int j = 0; j < per; ++j) {
-    local[j] = sum;
-    sum += bins[threadIdx.x * per + j];
-  }
-  part[threadIdx.x] = sum;
-  __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan of the parts
-    const int v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
-    __syncthreads();
-    part[threadIdx.x] += v;
-    __syncthreads();
-  }
-  const int base = part[threadIdx.x] - sum;
-  for (int j = 0; j < per; ++j) bins[threadIdx.x * per + j] = base + local[j];
-}
-
-__global__ void k_bin_scatter(const uint32_t *__restrict__ key, const int *__restrict__ count, int *__restrict__ bins,
-                              int32_t *__restrict__ order) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= *count) return;
-  order[atomicAdd(bins + key[i], 1)] = i;
-}
-
 cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev *views, int n_views, int n,
                           int64_t px_begin, int spp, int slots, int base_slot, int gs, const void *rays,
                           const void *hits, void *gws, float *contrib, const TraceFn &trace, unsigned *status,
@@ -1184,7 +1124,7 @@ cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev 
   int32_t *nearest = (int32_t *)take(al(ng * 4));
   uint32_t *bkey = (uint32_t *)take(al(ng * 4));
   int32_t *border = (int32_t *)take(al(ng * 4));
-  int *bins = (int *)take(al((int64_t)kBins * 4));
+  int *bins = (int *)take(al((int64_t)bin_order_bins() * 4));
   GatherArgs G{n, px_begin, spp, slots, base_slot, gs, views, n_views, sp ? *sp : SpecSource{}};
   cudaError_t e;
   if ((e = cudaMemsetAsync(counts, 0, 3 * sizeof(int), st)) != cudaSuccess) return e;
@@ -1203,20 +1143,8 @@ cudaError_t launch_gather(const SceneDev &S, const GatherMaps &M, const ViewDev 
   k_gather_hits<<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(S, grays, ghits, counts + 1, hsrc, hq, hqn, ts, tt,
                                                                side, counts + 2);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  {
-    const float3 lo = make_float3(M.lo[0], M.lo[1], M.lo[2]);
-    float sc[3];
-    for (int a = 0; a < 3; ++a) {
-      const float ext = M.hi[a] - M.lo[a];
-      sc[a] = ext > 0.0f && ext < INFINITY ? (float)(1 << kBinBits) / ext : 0.0f;
-    }
-    const unsigned grid = (unsigned)((ng + 255) / 256);
-    if ((e = cudaMemsetAsync(bins, 0, (size_t)kBins * 4, st)) != cudaSuccess) return e;
-    k_bin_keys<<<grid, 256, 0, st>>>(hq, counts + 2, lo, make_float3(sc[0], sc[1], sc[2]), bkey, bins);
-    k_bin_scan<<<1, 1024, 0, st>>>(bins);
-    k_bin_scatter<<<grid, 256, 0, st>>>(bkey, counts + 2, bins, border);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
+  // the gather hits' nearest-photon queries in spatial-bin order
+  if ((e = launch_bin_order(hq, ng, counts + 2, M.lo, M.hi, bkey, bins, border, st)) != cudaSuccess) return e;
   if ((e = launch_nearest(M.irr_nodes, M.irr_nids, M.dirs, M.n_irr, hq, hqn, ng, M.max_irr_dist, 0.87, nearest,
                           status, st, counts + 2, border)) != cudaSuccess)
     return e;
@@ -1230,7 +1158,7 @@ size_t gather_bytes(int64_t n, int gs) {
   const int64_t ng = n * 2 * gs;
   return 256 + al(n * 4) + 2 * al(n * 24) + al(n * kGatherLookup * 4) + al(n * kGatherLookup * 8) + al(n * 4) +
          al(ng * 32) + al(ng * 16) + al(ng * 4) + al(ng * 12) + al(ng * 4) + 2 * al(ng * 24) + 2 * al(ng * 12) +
-         al(ng) + al(ng * 4) + 2 * al(ng * 4) + al((int64_t)kBins * 4) + 256;
+         al(ng) + al(ng * 4) + 2 * al(ng * 4) + al((int64_t)bin_order_bins() * 4) + 256;
 }
 
 }  // namespace skw

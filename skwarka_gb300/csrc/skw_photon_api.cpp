@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <string>
@@ -20,6 +22,7 @@ struct skw_kdtree {
   double *d_dirs = nullptr;      // 3 << 16 doubles
   unsigned *d_status = nullptr;
   std::vector<int32_t> perm;
+  float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // the points' bounds (the queries' spatial bins)
 };
 
 using skw::cuda_fail;
@@ -27,6 +30,7 @@ using skw::fail;
 
 namespace {
 constexpr int kMaxK = 4096;
+constexpr int64_t kBinMin = 65536;  // batches from this size are looked up in spatial-bin order
 
 int check_query_args(skw_kdtree *t, const double *q, const double *qn, int64_t nq, int32_t k, double max_dist,
                      double cos_threshold, bool need_k) {
@@ -121,6 +125,15 @@ int skw_kdtree_create(skw_ctx *ctx, const float *positions, const uint16_t *norm
   if (!t) return fail(ctx, SKW_ERR_OOM, "host allocation failed");
   t->ctx = ctx;
   t->n = n;
+  for (int a = 0; a < 3; ++a) {
+    t->lo[a] = INFINITY;
+    t->hi[a] = -INFINITY;
+  }
+  for (int64_t i = 0; i < n; ++i)
+    for (int a = 0; a < 3; ++a) {
+      t->lo[a] = std::min(t->lo[a], positions[3 * i + a]);
+      t->hi[a] = std::max(t->hi[a], positions[3 * i + a]);
+    }
   cudaError_t e = cudaSetDevice(ctx->device);
   // the tree on the GPU where that gives the reference's (no median ties),
   // else on the host
@@ -181,14 +194,31 @@ int skw_knn(skw_kdtree *t, const double *q, const double *qn, int64_t nq, int32_
   cudaStream_t s = (cudaStream_t)stream;
   void *scratch = nullptr;
   const size_t sb = skw::knn_scratch_bytes(nq, k);
-  if (sb > 0) {
-    cudaMemPool_t pool;
-    if ((e = skw::ctx_pool(t->ctx, &pool)) != cudaSuccess) return cuda_fail(t->ctx, e, "workspace pool");
-    if ((e = cudaMallocFromPoolAsync(&scratch, sb, pool, s)) != cudaSuccess)
-      return cuda_fail(t->ctx, e, "k-NN heap workspace");
+  cudaMemPool_t pool;
+  if ((e = skw::ctx_pool(t->ctx, &pool)) != cudaSuccess) return cuda_fail(t->ctx, e, "workspace pool");
+  if (sb > 0 && (e = cudaMallocFromPoolAsync(&scratch, sb, pool, s)) != cudaSuccess)
+    return cuda_fail(t->ctx, e, "k-NN heap workspace");
+  // Large batches are looked up in spatial-bin order of the queries (64^3
+  // cells over the points' bounds, sorted stably so that each cell's
+  // queries keep their order): a warp's walks then start near each other.
+  int32_t *order = nullptr;
+  void *bin_ws = nullptr;
+  if (nq >= kBinMin && t->n > 0) {
+    const size_t ob = ((size_t)nq * 4 + 255) & ~(size_t)255;
+    if ((e = cudaMallocFromPoolAsync(&bin_ws, ob + skw::sort_order_bytes(nq), pool, s)) == cudaSuccess) {
+      char *w = (char *)bin_ws;
+      order = (int32_t *)w;
+      e = skw::launch_sort_order(q, nq, t->lo, t->hi, w + ob, order, s);
+    }
+    if (e != cudaSuccess) {
+      if (bin_ws) cudaFreeAsync(bin_ws, s);
+      if (scratch) cudaFreeAsync(scratch, s);
+      return cuda_fail(t->ctx, e, "k-NN query bins");
+    }
   }
   e = skw::launch_knn(t->d_nodes, t->d_nids, t->d_dirs, (int)t->n, q, qn, nq, k, max_dist, cos_threshold, out_idx,
-                      out_d2, out_count, nullptr, scratch, t->d_status, s);
+                      out_d2, out_count, nullptr, scratch, t->d_status, s, nullptr, order);
+  if (bin_ws) cudaFreeAsync(bin_ws, s);
   if (scratch) cudaFreeAsync(scratch, s);
   if (e != cudaSuccess) return cuda_fail(t->ctx, e, "k-NN launch");
   t->ctx->launches.fetch_add(1);
