@@ -642,14 +642,20 @@ void knn_kernel(unsigned grid, cudaStream_t stream, const float4 *nodes, const u
 // follows the atomics; every query's answer is the same whichever thread
 // computes it, and it is written at the query's own index.
 constexpr int kBinBits = 6, kBins = 1 << (3 * kBinBits);
+#ifndef SKW_KNN_SORT_BITS
+#define SKW_KNN_SORT_BITS 6  // cell bits per axis of the sorted order (1..10)
+#endif
+constexpr int kSortCellBits = SKW_KNN_SORT_BITS;
+static_assert(kSortCellBits >= 1 && kSortCellBits <= 10, "sorted cells: 1 to 10 bits per axis");
 
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // bit b of v to bit 3b
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // bit b of v (v < 2^10) to bit 3b
   uint32_t r = 0;
 #pragma unroll
-  for (int b = 0; b < kBinBits; ++b) r |= ((v >> b) & 1u) << (3 * b);
+  for (int b = 0; b < 10; ++b) r |= ((v >> b) & 1u) << (3 * b);
   return r;
 }
 
+template <int BITS>
 __global__ void k_bin_keys(const double *__restrict__ q, int64_t n, const int *__restrict__ count, float3 lo,
                            float3 scale, uint32_t *__restrict__ key, int *__restrict__ bins) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -659,7 +665,7 @@ __global__ void k_bin_keys(const double *__restrict__ q, int64_t n, const int *_
   uint32_t k = 0;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const float f = fminf(fmaxf(c[a], 0.0f), (float)((1 << kBinBits) - 1));  // NaN -> 0
+    const float f = fminf(fmaxf(c[a], 0.0f), (float)((1 << BITS) - 1));  // NaN -> 0
     k |= spread3((uint32_t)f) << a;
   }
   key[i] = k;
@@ -703,8 +709,8 @@ __global__ void k_bin_scatter(const uint32_t *__restrict__ key, int64_t n, const
   order[base + __popc(grp & ((1u << lane) - 1u))] = (int32_t)i;
 }
 
-// A stable LSD radix sort of the 18-bit cell keys (three passes of 6-bit
-// digits) carrying the query indices: per block of 256 keys, each digit's
+// A stable LSD radix sort of the cell keys (3 × SKW_KNN_SORT_BITS bits, 6-bit
+// digits, one pass per digit) carrying the query indices: per block of 256 keys, each digit's
 // count (lanes of a warp grouped by digit with __match_any_sync), one
 // exclusive scan of the counts digit-major (all blocks of digit 0, then
 // digit 1, ...), and a scatter that ranks a key after the block's earlier
@@ -781,16 +787,18 @@ cudaError_t launch_sort_order(const double *q, int64_t n, const float lo[3], con
   float sc[3];
   for (int a = 0; a < 3; ++a) {
     const float ext = hi[a] - lo[a];
-    sc[a] = ext > 0.0f && ext < INFINITY ? (float)(1 << kBinBits) / ext : 0.0f;
+    sc[a] = ext > 0.0f && ext < INFINITY ? (float)(1 << kSortCellBits) / ext : 0.0f;
   }
-  k_bin_keys<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(q, n, nullptr, make_float3(lo[0], lo[1], lo[2]),
-                                                          make_float3(sc[0], sc[1], sc[2]), ka, nullptr);
-  // three passes: ka/va -> kb/vb -> ka/va -> kb/vb, so the last lands in order (vb)
+  k_bin_keys<kSortCellBits><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+      q, n, nullptr, make_float3(lo[0], lo[1], lo[2]), make_float3(sc[0], sc[1], sc[2]), ka, nullptr);
+  // passes alternate ka/kb for the keys and va/vb for the indices, the
+  // indices' parity chosen so that the last pass lands in order (vb)
+  constexpr int passes = (3 * kSortCellBits + kDigitBits - 1) / kDigitBits;
   const int32_t *vin = nullptr;
-  for (int pass = 0; pass < 3; ++pass) {
+  for (int pass = 0; pass < passes; ++pass) {
     const int shift = pass * kDigitBits;
-    uint32_t *kin = pass == 1 ? kb : ka, *kout = pass == 1 ? ka : kb;
-    int32_t *vout = pass == 1 ? va : vb;
+    uint32_t *kin = pass % 2 ? kb : ka, *kout = pass % 2 ? ka : kb;
+    int32_t *vout = (passes - 1 - pass) % 2 ? va : vb;
     k_sort_hist<<<(unsigned)nb, kSortBlock, 0, st>>>(kin, n, shift, hist, nb);
     cudaError_t e = scan64(hist, m, sums, st);
     if (e != cudaSuccess) return e;
@@ -811,7 +819,7 @@ cudaError_t launch_bin_order(const double *q, int64_t n, const int *count_dev, c
   const unsigned grid = (unsigned)((n + 255) / 256);
   cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)kBins * 4, st);
   if (e != cudaSuccess) return e;
-  k_bin_keys<<<grid, 256, 0, st>>>(q, n, count_dev, make_float3(lo[0], lo[1], lo[2]),
+  k_bin_keys<kBinBits><<<grid, 256, 0, st>>>(q, n, count_dev, make_float3(lo[0], lo[1], lo[2]),
                                    make_float3(sc[0], sc[1], sc[2]), keys, bins);
   k_bin_scan<<<1, 1024, 0, st>>>(bins);
   k_bin_scatter<<<grid, 256, 0, st>>>(keys, n, count_dev, bins, order);
