@@ -283,9 +283,13 @@ int skw_kdtree_permutation(const skw_kdtree *tree, int32_t *perm);
  * when cos_threshold < 0 (qn may be NULL).  q, qn: 3 doubles per query.
  * Per query: out_count = points found (<= k); out_idx / out_d2: k slots in
  * the reference's heap order, -1 / 0 past out_count.  The index sets and
- * their order equal the reference's bit for bit.  k <= 128 needs no
- * workspace; larger k (up to 4096) allocates one from the context's
- * stream-ordered pool. */
+ * their order equal the reference's bit for bit.  Batches of 65,536 or
+ * more queries are walked in spatial order (the queries sorted by a 64^3
+ * cell of the tree's bounding box, stably, so a cell keeps the caller's
+ * order): each result still lands in its own query's slots, the same as in
+ * any order.  Workspace from the context's stream-ordered pool: the sort's
+ * (18 bytes per query) for such batches, and the heaps' for k > 128
+ * (up to 4096). */
 int skw_knn(skw_kdtree *tree, const double *q, const double *qn, int64_t nq, int32_t k, double max_dist,
             double cos_threshold, int32_t *out_idx, double *out_d2, int32_t *out_count, void *stream);
 /* skw_knn without any allocation, for callers that cannot allocate device
