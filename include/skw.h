@@ -256,10 +256,19 @@ int skw_direction_table(double *out);
  * Either output may be NULL. */
 int skw_kdtree_build_host(const float *positions, int64_t n, int threads, int32_t *perm, uint32_t *node_words);
 /* The same tree built on the GPU (level by level over per-axis sorted
- * lists), same outputs; *median_tie = 1 when some node's median ties on its
- * split axis (there the reference's tree is std::nth_element's choice among
- * the equal points and the host build is the one to use), else 0 and the
- * outputs equal skw_kdtree_build_host's.  Host buffers. */
+ * lists), same outputs as skw_kdtree_build_host.  *median_tie = the number
+ * of nodes whose median ties on its split axis: below such a node the
+ * reference's tree is std::nth_element's choice among the equal points, so
+ * those subtrees and the paths to them are remade on the host from the
+ * input order (skw_kdtree_repair_host); above 256 of them the whole tree is
+ * built on the host.  Host buffers. */
+/* The host half of skw_kdtree_build_device: perm / node_words (in/out) hold
+ * a tree equal to the reference's except below the tie nodes at tree
+ * positions ties[0..n_ties) (all of them); remakes the paths from the root
+ * to those nodes and their subtrees as KDTree::_Build makes them, leaving
+ * every other subtree as it is.  Needs no GPU. */
+int skw_kdtree_repair_host(const float *positions, int64_t n, const int32_t *ties, int64_t n_ties, int32_t *perm,
+                           uint32_t *node_words);
 int skw_kdtree_build_device(skw_ctx *ctx, const float *positions, int64_t n, int32_t *perm, uint32_t *node_words,
                             int32_t *median_tie);
 

@@ -76,6 +76,7 @@ SIGNATURES = [
     ("skw_compress_direction", C.c_uint16, [C.c_double, C.c_double, C.c_double]),
     ("skw_direction_table", C.c_int, [_P]),
     ("skw_kdtree_build_host", C.c_int, [_P, C.c_int64, C.c_int, _P, _P]),
+    ("skw_kdtree_repair_host", C.c_int, [_P, C.c_int64, _P, C.c_int64, _P, _P]),
     ("skw_kdtree_build_device", C.c_int, [_P, _P, C.c_int64, _P, _P, C.POINTER(C.c_int32)]),
     ("skw_kdtree_create", C.c_int, [_P, _P, _P, C.c_int64, C.POINTER(_P)]),
     ("skw_kdtree_destroy", None, [_P]),

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <mutex>
 #include <thread>
+#include <utility>
 
 namespace skw {
 namespace {
@@ -20,46 +21,95 @@ struct Build {
   std::vector<uint32_t> word;
   std::atomic<int> threads_left{0};
 
+  // One inner node of KDTree::_Build (KDTree.h:436-470) over pts[b, e),
+  // e - b >= 2: the median of the longest axis (`known_axis` when the
+  // caller knows it, else from the points' box) moved to b, its node word
+  // (split axis, left child, right child) set; returns the split position.
+  size_t node(size_t b, size_t e, int known_axis = -1) {
+    int axis = known_axis;
+    if (axis < 0 || axis > 2) {
+      double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      for (size_t i = b; i < e; ++i)
+        for (int k = 0; k < 3; ++k) {
+          lo[k] = std::min(lo[k], (double)pts[i].p[k]);
+          hi[k] = std::max(hi[k], (double)pts[i].p[k]);
+        }
+      axis = 0;
+      if (hi[1] - lo[1] > hi[axis] - lo[axis]) axis = 1;
+      if (hi[2] - lo[2] > hi[axis] - lo[axis]) axis = 2;
+    }
+    const size_t split = (b + e) / 2;
+    std::nth_element(pts.begin() + (long)b, pts.begin() + (long)split, pts.begin() + (long)e,
+                     [axis](const Pt &u, const Pt &v) { return u.p[axis] < v.p[axis]; });
+    std::swap(pts[b], pts[split]);
+    word[b] = (word[b] & ~3u) + (uint32_t)axis;  // SetSplitAxis
+    if (b < split)
+      word[b] = (word[b] & ~4u) + 4u;  // SetHasLeftChild(true)
+    else
+      word[b] = word[b] & ~4u;
+    if (split + 1 < e)
+      word[b] = ((uint32_t)(split + 1) << 3) + (word[b] & 7u);  // SetRightChild
+    else
+      word[b] = (((1u << 29) - 1u) << 3) + (word[b] & 7u);
+    return split;
+  }
+
   // KDTree::_Build (KDTree.h:428-473).
   void build(size_t b, size_t e) {
     if (b + 1 == e) {
       word[b] = (word[b] & ~3u) + 3u;  // SetLeaf
       return;
     }
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (size_t i = b; i < e; ++i)
-      for (int k = 0; k < 3; ++k) {
-        lo[k] = std::min(lo[k], (double)pts[i].p[k]);
-        hi[k] = std::max(hi[k], (double)pts[i].p[k]);
-      }
-    int axis = 0;
-    if (hi[1] - lo[1] > hi[axis] - lo[axis]) axis = 1;
-    if (hi[2] - lo[2] > hi[axis] - lo[axis]) axis = 2;
-    const size_t split = (b + e) / 2;
-    std::nth_element(pts.begin() + (long)b, pts.begin() + (long)split, pts.begin() + (long)e,
-                     [axis](const Pt &u, const Pt &v) { return u.p[axis] < v.p[axis]; });
-    std::swap(pts[b], pts[split]);
-    word[b] = (word[b] & ~3u) + (uint32_t)axis;  // SetSplitAxis
+    const size_t split = node(b, e);
     std::thread left_worker;
     bool spawned = false;
     if (b < split) {
-      word[b] = (word[b] & ~4u) + 4u;  // SetHasLeftChild(true)
       if (split - b > 50000 && threads_left.fetch_sub(1) > 0) {
         spawned = true;
         left_worker = std::thread([this, b, split]() { build(b + 1, split + 1); });
       } else {
         build(b + 1, split + 1);
       }
-    } else {
-      word[b] = word[b] & ~4u;
     }
-    if (split + 1 < e) {
-      word[b] = ((uint32_t)(split + 1) << 3) + (word[b] & 7u);  // SetRightChild
-      build(split + 1, e);
-    } else {
-      word[b] = (((1u << 29) - 1u) << 3) + (word[b] & 7u);
-    }
+    if (split + 1 < e) build(split + 1, e);
     if (spawned) left_worker.join();
+  }
+
+  // The repair of a tree built on the GPU (repair_photon_tree): pts[b, e)
+  // holds the range as _Build sees it.  A range without a tie node is the
+  // GPU's; a tie node's subtree is built whole; any other node is made here
+  // (its split axis is the GPU's: the node's point set is the reference's)
+  // and its children repaired.  `done` collects the ranges made here.
+  bool has_tie(size_t b, size_t e, const std::vector<int32_t> &ties) const {
+    const auto it = std::lower_bound(ties.begin(), ties.end(), (int32_t)b);
+    return it != ties.end() && (size_t)*it < e;
+  }
+  void repair(size_t b, size_t e, const std::vector<int32_t> &ties, const std::vector<KdNode> &gpu,
+              std::vector<std::pair<size_t, size_t>> &done) {
+    if (!has_tie(b, e, ties)) return;
+    if (std::binary_search(ties.begin(), ties.end(), (int32_t)b)) {
+      build(b, e);
+      done.emplace_back(b, e);
+      return;
+    }
+    const size_t split = node(b, e, (int)(gpu[b].word & 3u));
+    done.emplace_back(b, b + 1);
+    std::vector<std::pair<size_t, size_t>> left_done;
+    std::thread left_worker;
+    bool spawned = false;
+    if (has_tie(b + 1, split + 1, ties)) {
+      if (split - b > 50000 && has_tie(split + 1, e, ties) && threads_left.fetch_sub(1) > 0) {
+        spawned = true;
+        left_worker = std::thread([&, b, split]() { repair(b + 1, split + 1, ties, gpu, left_done); });
+      } else {
+        repair(b + 1, split + 1, ties, gpu, done);
+      }
+    }
+    if (split + 1 < e) repair(split + 1, e, ties, gpu, done);
+    if (spawned) {
+      left_worker.join();
+      done.insert(done.end(), left_done.begin(), left_done.end());
+    }
   }
 };
 
@@ -83,6 +133,28 @@ void build_photon_tree(const float *pos, int64_t n, int threads, std::vector<KdN
     nodes[i] = KdNode{B.pts[i].p[0], B.pts[i].p[1], B.pts[i].p[2], B.word[i]};
     perm[i] = B.pts[i].orig;
   }
+}
+
+void repair_photon_tree(const float *pos, int64_t n, std::vector<int32_t> ties, std::vector<KdNode> &nodes,
+                        std::vector<int32_t> &perm) {
+  if (n <= 0 || ties.empty()) return;
+  std::sort(ties.begin(), ties.end());
+  Build B;
+  B.pts.resize((size_t)n);
+  for (int64_t i = 0; i < n; ++i) {
+    for (int k = 0; k < 3; ++k) B.pts[(size_t)i].p[k] = pos[3 * i + k];
+    B.pts[(size_t)i].orig = (int32_t)i;
+  }
+  B.word.assign((size_t)n, 0u);
+  unsigned hw = std::thread::hardware_concurrency();
+  B.threads_left = (int)(hw ? hw : 1) - 1;
+  std::vector<std::pair<size_t, size_t>> done;
+  B.repair(0, (size_t)n, ties, nodes, done);
+  for (const auto &r : done)
+    for (size_t i = r.first; i < r.second; ++i) {
+      nodes[i] = KdNode{B.pts[i].p[0], B.pts[i].p[1], B.pts[i].p[2], B.word[i]};
+      perm[i] = B.pts[i].orig;
+    }
 }
 
 const std::vector<double> &direction_table() {

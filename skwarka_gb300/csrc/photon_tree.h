@@ -30,24 +30,35 @@ void build_photon_tree(const float *pos, int64_t n, int threads, std::vector<KdN
                        std::vector<int32_t> &perm);
 
 // The same tree built on the GPU (photon_tree_gpu.cu) from device positions
-// (n x 3 floats): nodes and perm in device memory, *tie (device int) set
-// when some node's median ties on its split axis -- there the reference's
-// tree depends on std::nth_element's choice among equal points, and the
-// host build is the one to use.  Otherwise the tree equals
-// build_photon_tree's node for node.  scratch: photon_tree_gpu_scratch(n)
-// bytes.
+// (n x 3 floats): nodes and perm in device memory, and the tie record
+// (device, 1 + kTieCap ints): [0] = the number of nodes whose median ties
+// on its split axis, then the tree positions of the first kTieCap of them.
+// Below a tie node the reference's tree depends on std::nth_element's
+// choice among the equal points (repair_photon_tree rebuilds those parts);
+// elsewhere the tree equals build_photon_tree's node for node.  scratch:
+// photon_tree_gpu_scratch(n) bytes.
+constexpr int kTieCap = 256;
 size_t photon_tree_gpu_scratch(int64_t n);
 int photon_tree_levels(int64_t n);
 cudaError_t build_photon_tree_gpu(const float *pos, int64_t n, KdNode *nodes, int32_t *perm, int *tie,
                                   void *scratch, cudaStream_t st);
+// Makes a GPU-built tree (nodes, perm: host copies, overwritten in place)
+// equal to build_photon_tree's, given the tree positions of all its tie
+// nodes: the nodes on the paths from the root to the tie nodes, and the tie
+// nodes' whole subtrees, are made on the host from the input order, as
+// _Build makes them; every other subtree holds the same points as the
+// reference's (no tie above it), so it is already the reference's.
+void repair_photon_tree(const float *pos, int64_t n, std::vector<int32_t> ties, std::vector<KdNode> &nodes,
+                        std::vector<int32_t> &perm);
 // Gathers per-photon attributes into tree order: out[t] = in[perm[t]]
 // (normal ids, direction ids and 3-float weights; any may be null).
 cudaError_t gather_tree_order(const int32_t *perm, int64_t n, const uint16_t *nrm_in, const uint16_t *dir_in,
                               const float *w_in, uint16_t *nrm_out, uint16_t *dir_out, float *w_out,
                               cudaStream_t st);
-// Builds on the GPU where that gives the reference's tree, else on the host:
-// the device nodes (allocated here, freed by the caller with cudaFree), the
-// permutation on the host, and *on_gpu.  pos: host positions.
+// Builds the reference's tree on the GPU (repaired on the host where medians
+// tie, up to kTieCap tie nodes), else on the host: the device nodes
+// (allocated here, freed by the caller with cudaFree), the permutation on
+// the host, and *on_gpu.  pos: host positions.
 cudaError_t build_photon_tree_device(const float *pos, int64_t n, cudaStream_t st, KdNode **d_nodes,
                                      std::vector<int32_t> &perm, int32_t **d_perm, bool *on_gpu);
 

@@ -9,7 +9,8 @@
 // [b + 1, b + m + 1), its right subtree the larger ones at [b + m + 1, e).
 // (With ties at the median, which of the equal points std::nth_element puts
 // at the median and how it splits the others is the standard library's own
-// choice; the builder reports the tie and the caller builds on the host.)
+// choice; the builder reports the tie nodes, and the host remakes their
+// subtrees and the paths to them from the input order, repair_photon_tree.)
 //
 // GPU form: the points are sorted once per axis (a stable radix sort of
 // order-preserving 32-bit keys, one bit per pass), then the tree is built
@@ -23,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "kernels.h"
 #include "photon_tree.h"
@@ -149,7 +151,8 @@ __global__ void k_sort_scatter(const uint32_t *__restrict__ key, const int32_t *
 // ------------------------------------------------------------ levels --
 // Segment of every position: seg[p] = (b, e), b = -1 once p's node is made.
 // Heads (p == b) make their node: a leaf for a one-point segment, else the
-// median of the longest axis (the flag is raised on a tie at the median).
+// median of the longest axis (a tie at the median is counted in tie[0] and
+// the first kTieCap tie nodes' positions kept in tie[1..]).
 __global__ void k_level_nodes(const float *__restrict__ pos, int64_t n, const int2 *__restrict__ seg,
                               const int32_t *__restrict__ id, KdNode *__restrict__ nodes,
                               int32_t *__restrict__ perm, int *__restrict__ seg_axis, int *__restrict__ tie) {
@@ -175,8 +178,10 @@ __global__ void k_level_nodes(const float *__restrict__ pos, int64_t n, const in
   const int32_t *L = id + (int64_t)axis * n;
   const int32_t med = L[split];
   const float mk = pos[3 * med + axis];
-  if ((m > 0 && pos[3 * L[split - 1] + axis] == mk) || (split + 1 < e && pos[3 * L[split + 1] + axis] == mk))
-    atomicOr(tie, 1);
+  if ((m > 0 && pos[3 * L[split - 1] + axis] == mk) || (split + 1 < e && pos[3 * L[split + 1] + axis] == mk)) {
+    const int slot = atomicAdd(tie, 1);
+    if (slot < kTieCap) tie[1 + slot] = b;
+  }
   const uint32_t right = split + 1 < e ? (uint32_t)(split + 1) : kNoRight;
   nodes[b] = KdNode{pos[3 * med], pos[3 * med + 1], pos[3 * med + 2], (right << 3) | 4u | (uint32_t)axis};
   perm[b] = med;
@@ -370,18 +375,33 @@ cudaError_t build_photon_tree_device(const float *pos, int64_t n, cudaStream_t s
     float *d_pos = nullptr;
     void *scratch = nullptr;
     int *d_tie = nullptr;
-    int tie = 1;
+    std::vector<int> tie(1 + kTieCap, 0);
+    tie[0] = kTieCap + 1;
     if ((e = cudaMalloc((void **)&d_pos, (size_t)n * 12)) == cudaSuccess &&
         (e = cudaMalloc((void **)d_perm, (size_t)n * 4)) == cudaSuccess &&
         (e = cudaMalloc(&scratch, photon_tree_gpu_scratch(n))) == cudaSuccess &&
-        (e = cudaMalloc((void **)&d_tie, sizeof(int))) == cudaSuccess &&
+        (e = cudaMalloc((void **)&d_tie, tie.size() * sizeof(int))) == cudaSuccess &&
         (e = cudaMemcpyAsync(d_pos, pos, (size_t)n * 12, cudaMemcpyHostToDevice, st)) == cudaSuccess &&
         (e = build_photon_tree_gpu(d_pos, n, *d_nodes, *d_perm, d_tie, scratch, st)) == cudaSuccess &&
-        (e = cudaMemcpyAsync(&tie, d_tie, sizeof(int), cudaMemcpyDeviceToHost, st)) == cudaSuccess)
+        (e = cudaMemcpyAsync(tie.data(), d_tie, tie.size() * sizeof(int), cudaMemcpyDeviceToHost, st)) ==
+            cudaSuccess)
       e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess && !tie) {
+    if (e == cudaSuccess && tie[0] <= kTieCap) {
       perm.resize((size_t)n);
       e = cudaMemcpyAsync(perm.data(), *d_perm, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+      if (tie[0] > 0) {
+        // the few subtrees below tied medians, and the paths to them, on the host
+        std::vector<KdNode> nodes((size_t)n);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(nodes.data(), *d_nodes, (size_t)n * sizeof(KdNode), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) {
+          repair_photon_tree(pos, n, std::vector<int32_t>(tie.begin() + 1, tie.begin() + 1 + tie[0]), nodes, perm);
+          if ((e = cudaMemcpyAsync(*d_nodes, nodes.data(), (size_t)n * sizeof(KdNode), cudaMemcpyHostToDevice,
+                                   st)) == cudaSuccess)
+            e = cudaMemcpyAsync(*d_perm, perm.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st);
+        }
+      }
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);
       *on_gpu = e == cudaSuccess;
     }
@@ -392,7 +412,7 @@ cudaError_t build_photon_tree_device(const float *pos, int64_t n, cudaStream_t s
     cudaFree(*d_perm);
     *d_perm = nullptr;
   }
-  // the host build: small trees, and trees with a tie at some median
+  // the host build: small trees, and trees with more than kTieCap tied medians
   std::vector<KdNode> nodes;
   build_photon_tree(pos, n, 0, nodes, perm);
   if (n > 0) e = cudaMemcpyAsync(*d_nodes, nodes.data(), (size_t)n * sizeof(KdNode), cudaMemcpyHostToDevice, st);

@@ -83,6 +83,25 @@ int skw_kdtree_build_host(const float *positions, int64_t n, int threads, int32_
   return SKW_OK;
 }
 
+int skw_kdtree_repair_host(const float *positions, int64_t n, const int32_t *ties, int64_t n_ties, int32_t *perm,
+                           uint32_t *node_words) {
+  if (n < 0 || (n > 0 && (!positions || !perm || !node_words)) || n >= ((int64_t)1 << 29) || n_ties < 0 ||
+      (n_ties > 0 && !ties))
+    return SKW_ERR_ARG;
+  std::vector<skw::KdNode> nodes((size_t)n);
+  std::vector<int32_t> p(perm, perm + n);
+  for (int64_t i = 0; i < n; ++i) {
+    const int32_t s = p[(size_t)i];
+    if (s < 0 || s >= n) return SKW_ERR_ARG;
+    nodes[(size_t)i] = skw::KdNode{positions[3 * s], positions[3 * s + 1], positions[3 * s + 2], node_words[2 * i + 1]};
+  }
+  for (int64_t i = 0; i < n_ties; ++i)
+    if (ties[i] < 0 || ties[i] >= n) return SKW_ERR_ARG;
+  skw::repair_photon_tree(positions, n, std::vector<int32_t>(ties, ties + n_ties), nodes, p);
+  export_tree(nodes, p, n, perm, node_words);
+  return SKW_OK;
+}
+
 int skw_kdtree_build_device(skw_ctx *ctx, const float *positions, int64_t n, int32_t *perm, uint32_t *node_words,
                             int32_t *median_tie) {
   if (!ctx || !median_tie) return fail(ctx, SKW_ERR_ARG, "null argument");
@@ -95,23 +114,27 @@ int skw_kdtree_build_device(skw_ctx *ctx, const float *positions, int64_t n, int
   int *d_tie = nullptr;
   skw::KdNode *d_nodes = nullptr;
   void *scratch = nullptr;
-  int tie = 0;
+  std::vector<int> tie(1 + skw::kTieCap, 0);
   std::vector<skw::KdNode> nodes((size_t)n);
   std::vector<int32_t> p((size_t)n);
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_pos, (size_t)n * 12);
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_perm, (size_t)n * 4);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&d_tie, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_tie, tie.size() * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_nodes, (size_t)n * sizeof(skw::KdNode));
   if (e == cudaSuccess) e = cudaMalloc(&scratch, skw::photon_tree_gpu_scratch(n));
   if (e == cudaSuccess) e = cudaMemcpy(d_pos, positions, (size_t)n * 12, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = skw::build_photon_tree_gpu(d_pos, n, d_nodes, d_perm, d_tie, scratch, nullptr);
-  if (e == cudaSuccess) e = cudaMemcpy(&tie, d_tie, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(tie.data(), d_tie, tie.size() * sizeof(int), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(nodes.data(), d_nodes, (size_t)n * sizeof(skw::KdNode), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(p.data(), d_perm, (size_t)n * 4, cudaMemcpyDeviceToHost);
   for (void *q : {(void *)d_pos, (void *)d_perm, (void *)d_tie, (void *)d_nodes, scratch}) cudaFree(q);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "photon tree build");
+  if (tie[0] > skw::kTieCap)  // too many tied medians to repair: the host build
+    skw::build_photon_tree(positions, n, 0, nodes, p);
+  else if (tie[0] > 0)
+    skw::repair_photon_tree(positions, n, std::vector<int32_t>(tie.begin() + 1, tie.begin() + 1 + tie[0]), nodes, p);
   export_tree(nodes, p, n, perm, node_words);
-  *median_tie = tie;
+  *median_tie = tie[0];
   return SKW_OK;
 }
 

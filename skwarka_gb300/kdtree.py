@@ -45,9 +45,25 @@ def build_host(positions: np.ndarray, threads: int = 0):
     return perm, nodes
 
 
+def repair_host(positions: np.ndarray, ties, perm: np.ndarray, nodes: np.ndarray):
+    """The host half of the GPU build: (perm, node_words) of a tree equal to
+    the reference's except below the tie nodes at tree positions `ties`,
+    remade there (the paths from the root to them and their subtrees) as the
+    host build makes them.  Returns new arrays."""
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    t = np.ascontiguousarray(ties, np.int32)
+    p = np.array(perm, np.int32, copy=True)
+    w = np.array(nodes, np.uint32, copy=True).reshape(n, 2)
+    _lib.check(_lib.load().skw_kdtree_repair_host(pos.ctypes.data, n, t.ctypes.data if len(t) else None, len(t),
+                                                   p.ctypes.data, w.ctypes.data))
+    return p, w
+
+
 def build_device(positions: np.ndarray, ctx: Context | None = None):
     """The GPU build: (perm int32 (n,), node_words uint32 (n, 2), median_tie
-    bool); equal to build_host's outputs unless median_tie."""
+    int), equal to build_host's outputs; median_tie counts the nodes whose
+    median ties on its split axis (their subtrees are remade on the host)."""
     ctx = ctx or default_context()
     pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
     n = pos.shape[0]
@@ -56,7 +72,7 @@ def build_device(positions: np.ndarray, ctx: Context | None = None):
     tie = C.c_int32()
     _lib.check(_lib.load().skw_kdtree_build_device(ctx.handle, pos.ctypes.data, n, perm.ctypes.data,
                                                     nodes.ctypes.data, C.byref(tie)), ctx.handle)
-    return perm, nodes, bool(tie.value)
+    return perm, nodes, int(tie.value)
 
 
 class PhotonKDTree:
