@@ -696,13 +696,19 @@ def photon_bench(args, dev, ctx, measure_cpu):
     kd.get_nearest_points(q, qn, 100, 0.05, 0.87)
     torch.cuda.synchronize()
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s.record()
-    res = kd.get_nearest_points(q, qn, 100, 0.05, 0.87)
-    e.record()
-    torch.cuda.synchronize()
-    knn_ms = s.elapsed_time(e)
+    # three timed lookups, the median reported (each writes 12 bytes per
+    # neighbour slot, 3.6 GB at full size: far past L2 between them)
+    runs = []
+    for _ in range(3):
+        res = None  # its buffers back to the cache: the next call reuses them, no allocation inside the timing
+        s.record()
+        res = kd.get_nearest_points(q, qn, 100, 0.05, 0.87)
+        e.record()
+        torch.cuda.synchronize()
+        runs.append(s.elapsed_time(e))
+    knn_ms = float(np.median(runs))
     nq = q.shape[0]
-    out["knn"] = {"queries": nq, "ms": knn_ms, "queries_per_s": nq / (knn_ms / 1e3),
+    out["knn"] = {"queries": nq, "ms": knn_ms, "queries_per_s": nq / (knn_ms / 1e3), "ms_runs": runs,
                   "mean_found": float(res["count"].float().mean())}
     # photon-mapping render
     cam4 = camf(512, 512)
