@@ -13,6 +13,7 @@
 #include <functional>
 #include <limits>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "kernels.h"
@@ -109,6 +110,34 @@ cudaError_t build_map(Map &m, cudaStream_t st) {
 
 const PhotonRec &tree_photon(const Map &m, int64_t t) { return m.input[(size_t)m.perm[(size_t)t]]; }
 
+// One map's build_map on a host thread and stream of its own, joined (and
+// its stream destroyed) on every path out of the caller.
+struct SideBuild {
+  std::thread worker;
+  cudaStream_t s = nullptr;
+  cudaError_t e = cudaSuccess;
+  bool started = false;
+  void start(Map &m, int device) {
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+      s = nullptr;  // the caller builds the map in line
+      return;
+    }
+    started = true;
+    worker = std::thread([this, &m, device]() {
+      e = cudaSetDevice(device);
+      if (e == cudaSuccess) e = build_map(m, s);
+    });
+  }
+  cudaError_t finish() {
+    if (worker.joinable()) worker.join();
+    return e;
+  }
+  ~SideBuild() {
+    if (worker.joinable()) worker.join();
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
 // Device buffers of the irradiance construction, freed on every path.
 struct IrrBuffers {
   double *q = nullptr, *qn = nullptr, *sq = nullptr, *sqn = nullptr;
@@ -150,6 +179,11 @@ struct IrrBuffers {
 int build_maps(skw_photon_map *pm, cudaStream_t st) {
   skw_ctx *ctx = pm->ctx;
   Map &im = pm->maps[2];
+  // the direct map's tree (the largest; a host repair where its medians
+  // tie) on a thread of its own while the indirect map's is built and its
+  // irradiance photons set up
+  SideBuild direct;
+  if (!im.input.empty() && !pm->maps[1].input.empty()) direct.start(pm->maps[1], ctx->device);
   cudaError_t e = build_map(im, st);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "photon map upload");
   if (im.n == 0) {  // no indirect map: no irradiance photons
@@ -225,7 +259,8 @@ int build_maps(skw_photon_map *pm, cudaStream_t st) {
     for (int mi : {2, 1, 0}) {  // the indirect map's tree exists; the others are built as they are needed
       if (e != cudaSuccess) break;
       Map &m = pm->maps[mi];
-      if (q0 == 0 && mi != 2 && (e = build_map(m, st)) != cudaSuccess) break;
+      if (q0 == 0 && mi != 2 && (e = mi == 1 && direct.started ? direct.finish() : build_map(m, st)) != cudaSuccess)
+        break;
       if (!has[mi]) continue;
       e = skw::launch_knn(m.d_nodes, m.d_nids, pm->d_dirs, (int)m.n, B.q + 3 * q0, B.qn + 3 * q0, c,
                           kLookupIrradiance, pm->lookup_dist[mi], kMaxNormalDeviationCos, B.idx[mi], B.d2[mi],
